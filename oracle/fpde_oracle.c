@@ -1,0 +1,361 @@
+/* fpde_oracle -- CPU restatement of FPDE_HPC's hot path (test infrastructure only; see
+ * fpde_oracle.h). Every function follows the reference's operation order so that the
+ * golden vectors produced by the reference's own FP64 code are met to rounding level.
+ * Compiled with -ffp-contract=off, like the reference build (x86-64 baseline, no FMA). */
+#define _DEFAULT_SOURCE
+#include "fpde_oracle.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+/* ---------------------------------------------------------------- weights */
+
+/* int_{s0}^{s1} (T - s)^{-alpha} ds with a = T - s1 >= 0, d = s1 - s0 > 0, in the
+ * cancellation-free form a^{1-alpha} expm1((1-alpha) log1p(d/a)) / (1-alpha). This is the
+ * closed form of kb (fpde_hpc_1d.cpp:2167-2301) for g(t) = t, which the reference
+ * evaluates by truncated series (_kb_row :1933, _kb_row2 :2000). */
+static double l1_interval_weight(double alpha, double a, double d)
+{
+    double e = 1.0 - alpha;
+    if (a <= 0.0) return pow(d, e) / e;
+    return pow(a, e) * expm1(e * log1p(d / a)) / e;
+}
+
+void fo_l1_weights(double alpha, const double *time, int n, double *kb, double *kkk0)
+{
+    double T1 = time[n + 1];
+    if (alpha == 1.0) {                      /* kb :2169-2175 */
+        for (int t = 0; t < n; t++) kb[t] = 0.0;
+        if (kkk0) *kkk0 = 1.0;
+        return;
+    }
+    for (int t = 0; t < n; t++)
+        kb[t] = l1_interval_weight(alpha, T1 - time[t + 1], time[t + 1] - time[t]);
+    if (kkk0) *kkk0 = l1_interval_weight(alpha, 0.0, T1 - time[n]);
+}
+
+/* ------------------------------------------------------------ history sum */
+
+void fo_l1_sum(const double *D, int64_t P, int n, const double *kb, const double *tau,
+               int64_t i0, int64_t i1, double *S)
+{
+#pragma omp parallel for schedule(static)
+    for (int64_t i = i0; i < i1; i++) {
+        double s = 0.0;
+        for (int t = n - 1; t >= 0; t--)          /* time_summing :4111, newest first */
+            s += kb[t] * D[(int64_t)t * P + i] / tau[t];
+        S[i] = s;
+    }
+}
+
+void fo_l1_sum_snapshots(const double *old, int64_t OS, int nold, const double *kb,
+                         const double *tau, int64_t nodes, double *S)
+{
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < nodes; i++) {
+        double s = 0.0;
+        for (int t = nold - 2; t >= 0; t--) {
+            double diff = old[(int64_t)(t + 1) * OS + i] - old[(int64_t)t * OS + i];
+            s += kb[t] * diff / tau[t];
+        }
+        S[i] = s;
+    }
+}
+
+/* ------------------------------------------------------------------ Thomas */
+
+static void thomas_core(int N, const double *A, const double *B, const double *R,
+                        const double *Om, int ltype, double g0, int rtype, double gN,
+                        double dLN, double *U, double *Al, double *Bt)
+{
+    Al[1] = ltype ? 1.0 : 0.0;                                /* al1 :4004-4025 */
+    for (int i = 1; i < N; i++) Al[i + 1] = B[i] / (R[i] - A[i] * Al[i]);
+    Bt[1] = g0;                                               /* bt1 :4587-4589 */
+    for (int i = 1; i < N; i++) Bt[i + 1] = (Al[i + 1] / B[i]) * (A[i] * Bt[i] - Om[i]);
+    if (rtype == 0) {
+        U[N] = gN;                                            /* U1 :4685-4686 */
+    } else {                                                  /* U1 :4689-4718 */
+        if (fabs(Bt[N]) > 1e-15) {
+            if (fabs(1.0 - Al[N]) > 1e-15) U[N] = (Bt[N] + gN * dLN) / (1.0 - Al[N]);
+            else U[N] = U[N - 1];
+        } else {
+            if (fabs(1.0 - Al[N]) > 1e-15) U[N] = 0.0;
+            else U[N] = U[N - 1];
+        }
+    }
+    for (int i = N - 1; i >= 0; i--) U[i] = Al[i + 1] * U[i + 1] + Bt[i + 1];   /* :4723 */
+}
+
+void fo_thomas_line(int N, const double *A, const double *B, const double *R, const double *Om,
+                    int ltype, double g0, int rtype, double gN, double dLN, double *U)
+{
+    double *Al = (double *)malloc(sizeof(double) * (size_t)(N + 2));
+    double *Bt = (double *)malloc(sizeof(double) * (size_t)(N + 2));
+    thomas_core(N, A, B, R, Om, ltype, g0, rtype, gN, dLN, U, Al, Bt);
+    free(Al);
+    free(Bt);
+}
+
+void fo_line_coefs(int N, const double *k, const double *iw, const double *dL,
+                   double *A, double *B, double *Rlap)
+{
+    for (int i = 1; i < N; i++) {             /* A_ / B / R :3095-3122, Dg = kb = 1 */
+        A[i] = k[i - 1] * iw[i] / (dL[i] * dL[i - 1]);
+        B[i] = k[i] * iw[i] / (dL[i] * dL[i]);
+        Rlap[i] = iw[i] * ((k[i] / (dL[i] * dL[i])) + (k[i - 1] / (dL[i] * dL[i - 1])));
+    }
+}
+
+/* ------------------------------------------------------------- line steps */
+
+int fo_line_step(int N, double *U, double *hist, int64_t P, int n,
+                 const double *kb, const double *tau, double Da, double kkk0,
+                 const double *A, const double *B, const double *Rlap, const double *src,
+                 int ltype, double g0, int rtype, double gN, double dLN, double *S_out)
+{
+    double tn = tau[n];
+    double lam = Da * (kkk0 / tn);            /* Om1 :4191 */
+    double lamR = Da * kkk0 / tn;             /* R :3120 */
+    double *S = (double *)calloc((size_t)N + 1, sizeof(double));
+    double *Om = (double *)calloc((size_t)N + 1, sizeof(double));
+    double *R = (double *)calloc((size_t)N + 1, sizeof(double));
+    double *Uold = (double *)malloc(sizeof(double) * (size_t)(N + 1));
+    double *Al = (double *)malloc(sizeof(double) * (size_t)(N + 2));
+    double *Bt = (double *)malloc(sizeof(double) * (size_t)(N + 2));
+    memcpy(Uold, U, sizeof(double) * (size_t)(N + 1));
+    if (n > 0) fo_l1_sum(hist, P, n, kb, tau, 1, N, S);
+    for (int i = 1; i < N; i++) {
+        Om[i] = -(lam * U[i]) + (src ? src[i] : 0.0);
+        Om[i] += Da * S[i];                    /* Om1 :4267 (mult = 1) */
+        R[i] = Rlap[i] + lamR;
+    }
+    thomas_core(N, A, B, R, Om, ltype, g0, rtype, gN, dLN, U, Al, Bt);
+    double *row = hist + (int64_t)n * P;
+    for (int64_t i = 0; i < P; i++) row[i] = (i <= N) ? U[i] - Uold[i] : 0.0;
+    if (S_out) memcpy(S_out, S, sizeof(double) * (size_t)(N + 1));
+    free(S); free(Om); free(R); free(Uold); free(Al); free(Bt);
+    return 0;
+}
+
+int fo_line_run(int N, double *U, double *hist, int64_t P, int steps, double tau, double alpha,
+                double Da, const double *A, const double *B, const double *Rlap,
+                int ltype, double g0, int rtype, double gN, double dLN)
+{
+    double *time = (double *)malloc(sizeof(double) * (size_t)(steps + 2));
+    double *taus = (double *)malloc(sizeof(double) * (size_t)(steps + 1));
+    double *kb = (double *)malloc(sizeof(double) * (size_t)(steps + 1));
+    time[0] = 0.0;                            /* Time.push_back(0) :3571 */
+    for (int n = 0; n <= steps; n++) { taus[n] = tau; time[n + 1] = time[n] + tau; }
+    for (int n = 0; n < steps; n++) {
+        double kkk0;
+        fo_l1_weights(alpha, time, n, kb, &kkk0);
+        fo_line_step(N, U, hist, P, n, kb, taus, Da, kkk0, A, B, Rlap, NULL,
+                     ltype, g0, rtype, gN, dLN, NULL);
+    }
+    free(time); free(taus); free(kb);
+    return 0;
+}
+
+/* ---------------------------------------------------------------- 3D LOD */
+
+int fo_lod_step_dirichlet(int sN, int M, int K, double *U, double *hist, int n,
+                          const double *kb, const double *tau, double Da, double kkk0,
+                          const double *coefA, const double *coefB, const double *coefRlap,
+                          const double *rp, const double *bc, double *S_out)
+{
+    const double lam = Da * (kkk0 / tau[n]);      /* Om1 :4191 */
+    const double lamR = Da * kkk0 / tau[n];       /* R :3120 */
+    const int64_t sx = 1, sy = sN + 2, sz = (int64_t)(sN + 2) * (M + 2);
+    const int64_t G = sz * (K + 2);
+    int L = sN; if (M > L) L = M; if (K > L) L = K;
+    double *Uold = (double *)malloc(sizeof(double) * (size_t)G);
+    double *S = (double *)calloc((size_t)G, sizeof(double));
+    double *la = (double *)malloc(sizeof(double) * (size_t)(L + 2));
+    double *lb = (double *)malloc(sizeof(double) * (size_t)(L + 2));
+    double *lr = (double *)malloc(sizeof(double) * (size_t)(L + 2));
+    double *lo = (double *)malloc(sizeof(double) * (size_t)(L + 2));
+    double *lu = (double *)malloc(sizeof(double) * (size_t)(L + 2));
+    double *Al = (double *)malloc(sizeof(double) * (size_t)(L + 2));
+    double *Bt = (double *)malloc(sizeof(double) * (size_t)(L + 2));
+    memcpy(Uold, U, sizeof(double) * (size_t)G);
+    /* history sum on the K-pass nodes (time_summing is evaluated for k = 1..K) */
+    if (n > 0)
+        for (int i = 1; i < sN; i++)
+            for (int j = 1; j < M; j++)
+                for (int k = 1; k <= K; k++) {
+                    int64_t id = i * sx + j * sy + k * sz;
+                    double s = 0.0;
+                    for (int t = n - 1; t >= 0; t--) s += kb[t] * hist[(int64_t)t * G + id] / tau[t];
+                    S[id] = s;
+                }
+    /* passes in the order of calc_step: K (c=2), _M (c=1), sN (c=0) */
+    for (int pass = 2; pass >= 0; pass--) {
+        int Nl = pass == 2 ? K : (pass == 1 ? M : sN);
+        int64_t st = pass == 2 ? sz : (pass == 1 ? sy : sx);
+        const double *cA = coefA + (int64_t)pass * G, *cB = coefB + (int64_t)pass * G;
+        const double *cR = coefRlap + (int64_t)pass * G;
+        int na = pass == 2 ? sN : (pass == 1 ? sN : M);     /* first line index range */
+        int nb = pass == 2 ? M : K;                          /* second line index range */
+        for (int a = 1; a < na; a++)
+            for (int b = 1; b < nb; b++) {
+                int64_t base;
+                if (pass == 2) base = a * sx + b * sy;               /* line (i, j) */
+                else if (pass == 1) base = a * sx + b * sz;          /* line (i, k) */
+                else base = a * sy + b * sz;                         /* line (j, k) */
+                for (int p = 0; p <= Nl + 1; p++) lu[p] = U[base + p * st];
+                for (int p = 1; p < Nl; p++) {
+                    int64_t id = base + p * st;
+                    la[p] = cA[id]; lb[p] = cB[id]; lr[p] = cR[id] + lamR;
+                    lo[p] = -(lam * lu[p]) + (pass == 2 ? rp[id] : 0.0);
+                    if (pass == 2) lo[p] += Da * S[id];
+                }
+                thomas_core(Nl, la, lb, lr, lo, 0, bc[base], 0, bc[base + Nl * st], 0.0, lu, Al, Bt);
+                lu[Nl + 1] = lu[Nl];                                 /* U1 :4792 */
+                for (int p = 0; p <= Nl + 1; p++) U[base + p * st] = lu[p];
+            }
+    }
+    double *row = hist + (int64_t)n * G;
+    for (int64_t q = 0; q < G; q++) row[q] = U[q] - Uold[q];
+    if (S_out) memcpy(S_out, S, sizeof(double) * (size_t)G);
+    free(Uold); free(S); free(la); free(lb); free(lr); free(lo); free(lu); free(Al); free(Bt);
+    return 0;
+}
+
+/* ------------------------------------------------------ distributed order */
+
+static double bk_pow(double d1, double d2, double beta)   /* fr_do.cpp:129-134 */
+{
+    if (d1 == 0.0) return pow(d2, 1.0 - beta);
+    if (d2 == 0.0) return pow(d1, 1.0 - beta);
+    return pow(d1, 1.0 - beta) - pow(d2, 1.0 - beta);
+}
+
+void fo_caputo_derivative(int ntau, double tau, double a, double g2a, const double *F, double *DF)
+{
+    double *bkk = (double *)malloc(sizeof(double) * (size_t)ntau);
+    for (int i = 0; i < ntau; i++) bkk[i] = bk_pow((i + 1) * tau, i * tau, a);  /* :67 */
+    DF[0] = 0.0;
+    for (int t = 1; t < ntau; t++) {                                           /* :77-85 */
+        double sum = 0.0;
+        for (int i = 0; i < t; i++) sum += ((F[i + 1] - F[i]) / tau) * bkk[t - i - 1];
+        DF[t] = sum / g2a;
+    }
+    free(bkk);
+}
+
+void fo_do_derivative(int ntau, double tau, int na, const double *WA, const double *gs,
+                      const double *F, int maxt, int t0, int j0, double *DF)
+{
+    double *bkk = (double *)malloc(sizeof(double) * (size_t)ntau * na);
+    double *CD = (double *)malloc(sizeof(double) * (size_t)na);
+    for (int i = 0; i < ntau; i++)                                   /* fill_arrays :67-68 */
+        for (int j = 0; j < na; j++)
+            bkk[(int64_t)i * na + j] = bk_pow((i + 1) * tau, i * tau, (na == 1) ? 0.0 : (1.0 * j) / (double)(na - 1));
+    for (int t = t0; t < ntau; t++) {                                /* DO_Cder :93-112 */
+        double sum = 0.0;
+        int jend = (maxt == -1) ? t : ((t > maxt) ? maxt : t);
+        for (int i = 0; i < na; i++) {
+            double s2 = 0.0;
+            for (int j = j0; j < jend; j++)
+                if (j >= 0) s2 += ((F[j + 1] - F[j]) / tau) * bkk[(int64_t)(t - j - 1) * na + i];
+            s2 /= gs[i];
+            CD[i] = s2;
+        }
+        for (int i = 0; i < na - 1; i++) sum += 0.5 * (WA[i] * CD[i] + WA[i + 1] * CD[i + 1]);
+        DF[t] = sum;
+    }
+    free(bkk);
+    free(CD);
+}
+
+void fo_do_fused_weights(int nq, const double *aq, const double *Wq, const double *gq,
+                         double tau, int nl, double *c)
+{
+    for (int l = 0; l < nl; l++) {
+        double s = 0.0;
+        for (int q = 0; q < nq; q++) {
+            double e = 1.0 - aq[q];
+            /* ((l+1) tau)^e - (l tau)^e = tau^e * b_l(e), b_0 = 1 */
+            double b = (l == 0) ? 1.0 : pow((double)l, e) * expm1(e * log1p(1.0 / l));
+            s += Wq[q] * pow(tau, e) * b / gq[q];
+        }
+        c[l] = s;
+    }
+}
+
+/* source of fr_do eq_ex 0 (fr_do.cpp:464-470) */
+static double do_eq_f(int ex, double t, double x)
+{
+    if (ex == 0)
+        return sin(2 * M_PI * x) * (800 * M_PI * M_PI * t * t * t * t + (2400 * (t * t * t * t - t * t * t) / log(t)));
+    return 0.0;
+}
+
+int fo_do_eq_solve(int ex, int Nx, int Nt, int tblock, int na, double h, double tau, double D,
+                   const double *WA, const double *gs, double *C, double *b0_out)
+{
+    double Aa = 0.5 * D / (h * h), Bb = 0.5 * D / (h * h);           /* eq_init :674-675 */
+    double *bkk = (double *)malloc(sizeof(double) * (size_t)Nt * na);
+    double *eA = (double *)calloc((size_t)Nx + 1, sizeof(double));
+    double *eB = (double *)calloc((size_t)Nx + 1, sizeof(double));
+    double *eDF = (double *)calloc((size_t)Nx * tblock, sizeof(double));
+    double *DF = (double *)calloc((size_t)Nt + tblock + 2, sizeof(double));
+    double *CD = (double *)malloc(sizeof(double) * (size_t)na);
+    for (int i = 0; i < Nt; i++)
+        for (int j = 0; j < na; j++)
+            bkk[(int64_t)i * na + j] = bk_pow((i + 1) * tau, i * tau, (1.0 * j) / (double)(na - 1));
+    double b0 = 0.0;                                                  /* :688-690 */
+    for (int a = 0; a < na - 1; a++)
+        b0 += 0.5 * (WA[a] * bkk[a] / gs[a] + WA[a + 1] * bkk[a + 1] / gs[a + 1]);
+    double Ss = (D / (h * h)) + (b0 / tau);
+    eA[1] = 0.0;                                                      /* :692-694 */
+    for (int i = 1; i < Nx - 1; i++) eA[i + 1] = Bb / (Ss - Aa * eA[i]);
+    /* DO_Cder restricted to one node's series, summing j in [j0, min(t,maxt)) */
+    #define DO_NODE(Fp, ntau, maxt, t0, j0)                                               \
+        for (int t = (t0); t < (ntau); t++) {                                             \
+            double sum = 0.0;                                                             \
+            int jend = ((maxt) == -1) ? t : ((t > (maxt)) ? (maxt) : t);                  \
+            for (int q = 0; q < na; q++) {                                                \
+                double s2 = 0.0;                                                          \
+                for (int j = (j0); j < jend; j++)                                         \
+                    if (j >= 0) s2 += (((Fp)[j + 1] - (Fp)[j]) / tau) * bkk[(int64_t)(t - j - 1) * na + q]; \
+                s2 /= gs[q];                                                              \
+                CD[q] = s2;                                                               \
+            }                                                                             \
+            for (int q = 0; q < na - 1; q++) sum += 0.5 * (WA[q] * CD[q] + WA[q + 1] * CD[q + 1]); \
+            DF[t] = sum;                                                                  \
+        }
+    for (int i = 0; i < Nt; i += tblock) {                            /* eq_solve :737-771 */
+        for (int j = 0; j < Nx; j++) {
+            const double *Fp = C + (int64_t)j * Nt;
+            DO_NODE(Fp, i + tblock, ((i == 0) ? i : i - 1), i, 0);
+            for (int k = 0; k < tblock; k++) eDF[(int64_t)j * tblock + k] = DF[i + k];
+        }
+        for (int j = ((i == 0) ? 1 : 0); j < tblock; j++) {
+            int s = i + j;                                            /* eq_one_step :724-732 */
+            eB[1] = 0.0;
+            for (int x = 1; x < Nx - 1; x++) {
+                int jj = s - 1;
+                double rp = -0.5 * (D / (h * h)) * (C[(int64_t)(x - 1) * Nt + jj] - 2.0 * C[(int64_t)x * Nt + jj] + C[(int64_t)(x + 1) * Nt + jj]);
+                double lp = -(b0 * C[(int64_t)x * Nt + jj] / tau) - 0.5 * (do_eq_f(ex, jj * tau, x * h) + do_eq_f(ex, (jj + 1) * tau, x * h));
+                double nlp = eDF[(int64_t)x * tblock + ((jj + 1) % tblock)];
+                if (!isfinite(lp)) lp = -(b0 * C[(int64_t)x * Nt + jj] / tau) - do_eq_f(ex, (jj + 1) * tau, x * h);
+                double Ff = rp + lp + nlp;                            /* eq_Ff :656-665 */
+                eB[x + 1] = (eA[x + 1] / Bb) * (Aa * eB[x] - Ff);
+            }
+            C[s + (int64_t)Nt * (Nx - 1)] = 0.0;
+            for (int x = Nx - 2; x >= 0; x--) C[s + (int64_t)Nt * x] = eA[x + 1] * C[s + (int64_t)Nt * (x + 1)] + eB[x + 1];
+            if (j != tblock - 1)
+                for (int jj = 0; jj < Nx; jj++) {
+                    const double *Fp = C + (int64_t)jj * Nt;
+                    DO_NODE(Fp, i + j + 2, i + j, i + j + 1, i - 1);
+                    eDF[(int64_t)jj * tblock + j + 1] += DF[i + j + 1];
+                }
+        }
+    }
+    #undef DO_NODE
+    if (b0_out) *b0_out = b0;
+    free(bkk); free(eA); free(eB); free(eDF); free(DF); free(CD);
+    return 0;
+}

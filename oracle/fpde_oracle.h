@@ -1,0 +1,121 @@
+/* fpde_oracle -- CPU restatement of FPDE_HPC's L1 history sum and tridiagonal line
+ * solves, used ONLY as the checker (tests, the smoke check, and the CPU-baseline leg of
+ * the benchmark). It is never linked into, called by or shipped with the GPU library.
+ *
+ * Parity status: pinned. tests/golden/*.fgv.gz hold outputs of the reference's own FP64
+ * code (built from its sources by oracle/Makefile + oracle/ref_pin), and the CPU test
+ * suite checks this restatement against them.
+ *
+ * Conventions (following fpde_hpc_1d.cpp):
+ *  - a line has N intervals and nodes 0..N; the unknowns are 1..N-1, nodes 0 and N carry
+ *    the boundary conditions (set_xyz_steps :2381-2388);
+ *  - the L1 weight of history interval t at step n (producing u^{n+1}) is
+ *    kb_t = int_{T_t}^{T_{t+1}} (T_{n+1}-s)^{-alpha} ds  (kb :2167, precalc_kb_3 :4069);
+ *  - history increments D_t = u^{t+1} - u^t, stored time-major, one row of P doubles
+ *    per interval.
+ */
+#ifndef FPDE_ORACLE_H
+#define FPDE_ORACLE_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Closed-form L1 weights for step n: kb[t], t = 0..n-1, from the time points
+ * time[0..n+1]. Cancellation-free: (a+d)^{1-a} - a^{1-a} = a^{1-a} expm1((1-a) log1p(d/a)).
+ * Also returns the local weight kkk0 = kb(alpha, n, n+1, n+1) (init_time_step :3947).
+ * alpha == 1 gives kb = 0 and kkk0 = 1 (kb :2169-2175). */
+void fo_l1_weights(double alpha, const double *time, int n, double *kb, double *kkk0);
+
+/* History sum of one step in the reference's order (time_summing :4110-4136, t descending):
+ * S[i] = sum_t (kb[t] * D[t][i]) / tau[t], for i in [i0, i1). D is n rows of P doubles. */
+void fo_l1_sum(const double *D, int64_t P, int n, const double *kb, const double *tau,
+               int64_t i0, int64_t i1, double *S);
+
+/* Same sum over stored snapshots old[t][i] (t = 0..nold-1), the argument form of the
+ * reference's GPU Sum kernel (fpde_hpc_1d.cpp:1407-1478, sum_alg 0): the increment is
+ * formed as old[t+1]-old[t] on the fly. */
+void fo_l1_sum_snapshots(const double *old, int64_t OS, int nold, const double *kb,
+                         const double *tau, int64_t nodes, double *S);
+
+/* Thomas solve of one line (al1 :4002-4027, bt1 :4585-4590, back-substitution in U1
+ * :4678-4725): A[i] U[i-1] - R[i] U[i] + B[i] U[i+1] = Om[i], i = 1..N-1.
+ * Left boundary: ltype 0 -> U[0] = g0 (Al[1] = 0, Bt[1] = g0); ltype 1 -> flux form
+ * (Al[1] = 1, Bt[1] = g0). Right boundary: rtype 0 -> U[N] = gN; rtype 1 -> the
+ * zero-/given-flux closure of U1 :4687-4719 with dLN = dL[N-1], including its 1e-15
+ * thresholds (which may read the previous U[N-1]). U holds N+1 values in and out.
+ * Arrays A, B, R, Om are indexed 0..N (entries 0 and N unused). */
+void fo_thomas_line(int N, const double *A, const double *B, const double *R, const double *Om,
+                    int ltype, double g0, int rtype, double gN, double dLN, double *U);
+
+/* Tridiagonal coefficients of the H equation with gamma = 1 on one line
+ * (A_ / B / R :3095-3142 with Dg = 1, kb(1,..) = 1): from the node conductivities k[i],
+ * the inverse capacity iw[i] and the steps dL[i] = x[i+1]-x[i]:
+ *   A[i] = k[i-1] iw[i] / (dL[i] dL[i-1]),  B[i] = k[i] iw[i] / dL[i]^2,
+ *   Rlap[i] = iw[i] (k[i]/dL[i]^2 + k[i-1]/(dL[i] dL[i-1])).
+ * The full diagonal is R[i] = Rlap[i] + Da*kkk0/tau. */
+void fo_line_coefs(int N, const double *k, const double *iw, const double *dL,
+                   double *A, double *B, double *Rlap);
+
+/* One time step of a single line (the 1D form of the K pass, Om1 :4165-4267 + U1):
+ *   Om[i] = -lam U[i] + src[i] + Da S[i],   R[i] = Rlap[i] + lamR
+ * with lam = Da*(kkk0/tau_n), lamR = Da*kkk0/tau_n, S from the stored history.
+ * hist holds n increment rows of P >= N+1 doubles; the new increment is written to row n.
+ * src may be NULL (no source). Returns 0. */
+int fo_line_step(int N, double *U, double *hist, int64_t P, int n,
+                 const double *kb, const double *tau, double Da, double kkk0,
+                 const double *A, const double *B, const double *Rlap, const double *src,
+                 int ltype, double g0, int rtype, double gN, double dLN, double *S_out);
+
+/* Full run of the 1D Caputo line problem with uniform tau and constant boundary data:
+ * steps time steps from U (N+1 values, overwritten with the final state).
+ * hist must hold steps rows of P doubles. Weights are the closed form above; Da is the
+ * caller's 1/Gamma(1-alpha). Returns 0. OpenMP parallel over nodes for the history sum. */
+int fo_line_run(int N, double *U, double *hist, int64_t P, int steps, double tau, double alpha,
+                double Da, const double *A, const double *B, const double *Rlap,
+                int ltype, double g0, int rtype, double gN, double dLN);
+
+/* One step of the reference's 3D LOD scheme (calc_step mode 3 :5144-5779, implicit3d 0,
+ * split3d 0): K pass (lines along k, with source Rp and the history sum), then the _M
+ * pass (lines along j), then the sN pass (lines along i). The grid has (sN+2)(M+2)(K+2)
+ * points indexed i + j (sN+2) + k (sN+2)(M+2) (idx :1181). coefA/B/Rlap are three grids
+ * (pass 2 = K, 1 = _M, 0 = sN) of the line coefficients at each node; the diagonal is
+ * R = Rlap + Da*kkk0/tau_n and the RHS local term Da*(kkk0/tau_n) U. bc is a grid of
+ * Dirichlet values on the line ends, rp the K-pass source. hist holds n increment
+ * grids; the new one is written as row n.
+ * S_out (grid, may be NULL) receives the history sums. Left/right boundaries Dirichlet
+ * (the analytic-test configuration). */
+int fo_lod_step_dirichlet(int sN, int M, int K, double *U, double *hist, int n,
+                          const double *kb, const double *tau, double Da, double kkk0,
+                          const double *coefA, const double *coefB, const double *coefRlap,
+                          const double *rp, const double *bc, double *S_out);
+
+/* ---- distributed order (fr_do.cpp) ---- */
+
+/* Caputo derivative of sampled F (Cder :74-86 with an F array): DF[t] for t = 1..ntau-1,
+ * bk weights ((i+1)tau)^{1-a} - (i tau)^{1-a}, divided by Gamma(2-a) = g2a. */
+void fo_caputo_derivative(int ntau, double tau, double a, double g2a, const double *F, double *DF);
+
+/* DO derivative (DO_Cder :89-113): na orders a_i = i/(na-1) on [0,1], weights WA[i],
+ * Gamma(2-a_i) = gs[i], trapezoid in a, samples F[0..ntau-1] (uniform tau). Terms j in
+ * [j0, min(t, maxt)) (maxt = -1: no limit) for t in [t0, ntau). Writes DF[t]. */
+void fo_do_derivative(int ntau, double tau, int na, const double *WA, const double *gs,
+                      const double *F, int maxt, int t0, int j0, double *DF);
+
+/* Fused DO weights: c[l] = sum_q Wq[q] ((l+1)tau)^{1-a_q} - (l tau)^{1-a_q}) / Gamma(2-a_q)
+ * for l = 0..nl-1 (cancellation-free), with Wq the effective quadrature weights. */
+void fo_do_fused_weights(int nq, const double *aq, const double *Wq, const double *gq,
+                         double tau, int nl, double *c);
+
+/* DO diffusion solve of fr_do.cpp eq_solve (:733-775): Crank-Nicolson in x, blocked
+ * far/near DO history, Thomas sweeps with fixed alphas (eq_init :666-695,
+ * eq_one_step :724-732). ex selects the source (0: eq_ex 0, 1: zero). C is Nx*Nt,
+ * node-major, with C[i*Nt] the initial state. Returns 0. */
+int fo_do_eq_solve(int ex, int Nx, int Nt, int tblock, int na, double h, double tau, double D,
+                   const double *WA, const double *gs, double *C, double *b0_out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,175 @@
+"""ctypes binding of the CPU oracle (oracle/fpde_oracle.c).
+
+Test infrastructure: imported only by tests/, the smoke check and the CPU-baseline leg
+of bench.py, as the checker. The GPU library never loads it. ``load()`` builds the
+shared object with ``make -C oracle`` on first use (a second or two with gcc).
+"""
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB_PATH = os.path.join(HERE, "_build", "libfpde_oracle.so")
+_lib = None
+
+_dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
+
+
+def build():
+    subprocess.check_call(["make", "-s", "-C", HERE], stdout=subprocess.DEVNULL)
+    return _LIB_PATH
+
+
+def load():
+    global _lib
+    if _lib is not None:
+        return _lib
+    src = os.path.join(HERE, "fpde_oracle.c")
+    if (not os.path.exists(_LIB_PATH)) or os.path.getmtime(_LIB_PATH) < os.path.getmtime(src):
+        build()
+    lib = C.CDLL(_LIB_PATH)
+    i64, i32, d = C.c_int64, C.c_int, C.c_double
+    vp = C.c_void_p
+    lib.fo_l1_weights.argtypes = [d, _dp, i32, _dp, C.POINTER(d)]
+    lib.fo_l1_sum.argtypes = [_dp, i64, i32, _dp, _dp, i64, i64, _dp]
+    lib.fo_l1_sum_snapshots.argtypes = [_dp, i64, i32, _dp, _dp, i64, _dp]
+    lib.fo_thomas_line.argtypes = [i32, _dp, _dp, _dp, _dp, i32, d, i32, d, d, _dp]
+    lib.fo_line_coefs.argtypes = [i32, _dp, _dp, _dp, _dp, _dp, _dp]
+    lib.fo_line_step.argtypes = [i32, _dp, _dp, i64, i32, _dp, _dp, d, d, _dp, _dp, _dp, vp,
+                                 i32, d, i32, d, d, vp]
+    lib.fo_line_step.restype = i32
+    lib.fo_line_run.argtypes = [i32, _dp, _dp, i64, i32, d, d, d, _dp, _dp, _dp, i32, d, i32, d, d]
+    lib.fo_line_run.restype = i32
+    lib.fo_lod_step_dirichlet.argtypes = [i32, i32, i32, _dp, _dp, i32, _dp, _dp, d, d,
+                                          _dp, _dp, _dp, _dp, _dp, vp]
+    lib.fo_lod_step_dirichlet.restype = i32
+    lib.fo_caputo_derivative.argtypes = [i32, d, d, d, _dp, _dp]
+    lib.fo_do_derivative.argtypes = [i32, d, i32, _dp, _dp, _dp, i32, i32, i32, _dp]
+    lib.fo_do_fused_weights.argtypes = [i32, _dp, _dp, _dp, d, i32, _dp]
+    lib.fo_do_eq_solve.argtypes = [i32, i32, i32, i32, i32, d, d, d, _dp, _dp, _dp, C.POINTER(d)]
+    lib.fo_do_eq_solve.restype = i32
+    _lib = lib
+    return lib
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def time_points(taus):
+    """Time[0] = 0, Time[k+1] = Time[k] + tau[k] (the reference accumulates the same way)."""
+    t = np.zeros(len(taus) + 1)
+    for k, v in enumerate(taus):
+        t[k + 1] = t[k] + v
+    return t
+
+
+def l1_weights(alpha, time, n):
+    lib = load()
+    kb = np.zeros(max(n, 1))
+    k0 = C.c_double()
+    lib.fo_l1_weights(alpha, np.ascontiguousarray(time, dtype=np.float64), n, kb, C.byref(k0))
+    return kb[:n], k0.value
+
+
+def l1_sum(D, n, kb, tau, i0=0, i1=None):
+    lib = load()
+    D = np.ascontiguousarray(D, dtype=np.float64)
+    P = D.shape[-1]
+    i1 = P if i1 is None else i1
+    S = np.zeros(P)
+    lib.fo_l1_sum(D.reshape(-1), P, n, np.ascontiguousarray(kb, dtype=np.float64),
+                  np.ascontiguousarray(tau, dtype=np.float64), i0, i1, S)
+    return S
+
+
+def l1_sum_snapshots(old, kb, tau):
+    lib = load()
+    old = np.ascontiguousarray(old, dtype=np.float64)
+    nold, OS = old.shape
+    S = np.zeros(OS)
+    lib.fo_l1_sum_snapshots(old.reshape(-1), OS, nold, np.ascontiguousarray(kb, dtype=np.float64),
+                            np.ascontiguousarray(tau, dtype=np.float64), OS, S)
+    return S
+
+
+def thomas_line(A, B, R, Om, ltype, g0, rtype, gN, dLN, U):
+    lib = load()
+    U = np.array(U, dtype=np.float64)
+    N = len(U) - 1
+    lib.fo_thomas_line(N, *(np.ascontiguousarray(x, dtype=np.float64) for x in (A, B, R, Om)),
+                       ltype, g0, rtype, gN, dLN, U)
+    return U
+
+
+def line_coefs(k, iw, dL):
+    lib = load()
+    N = len(k) - 1
+    A, B, Rl = np.zeros(N + 1), np.zeros(N + 1), np.zeros(N + 1)
+    lib.fo_line_coefs(N, *(np.ascontiguousarray(x, dtype=np.float64) for x in (k, iw, dL)), A, B, Rl)
+    return A, B, Rl
+
+
+def line_run(U0, steps, tau, alpha, Da, A, B, Rl, ltype=0, g0=0.0, rtype=0, gN=0.0, dLN=0.0,
+             P=None):
+    """Full run of the 1D line problem; returns the final state and the increment history."""
+    lib = load()
+    U = np.array(U0, dtype=np.float64)
+    N = len(U) - 1
+    P = P or (N + 1)
+    hist = np.zeros((steps, P))
+    lib.fo_line_run(N, U, hist.reshape(-1), P, steps, tau, alpha, Da,
+                    *(np.ascontiguousarray(x, dtype=np.float64) for x in (A, B, Rl)),
+                    ltype, g0, rtype, gN, dLN)
+    return U, hist
+
+
+def lod_step_dirichlet(dims, U, hist, n, kb, tau, Da, kkk0, coefA, coefB, coefRlap, rp, bc, want_S=False):
+    lib = load()
+    sN, M, K = dims
+    S = np.zeros_like(U) if want_S else None
+    lib.fo_lod_step_dirichlet(sN, M, K, U.reshape(-1), hist.reshape(-1), n,
+                              np.ascontiguousarray(kb, dtype=np.float64),
+                              np.ascontiguousarray(tau, dtype=np.float64), Da, kkk0,
+                              coefA.reshape(-1), coefB.reshape(-1), coefRlap.reshape(-1),
+                              rp.reshape(-1), bc.reshape(-1), _ptr(S))
+    return S
+
+
+def caputo_derivative(F, tau, a, g2a):
+    lib = load()
+    F = np.ascontiguousarray(F, dtype=np.float64)
+    DF = np.zeros(len(F))
+    lib.fo_caputo_derivative(len(F), tau, a, g2a, F, DF)
+    return DF
+
+
+def do_derivative(F, tau, WA, gs, maxt=-1, t0=1, j0=0):
+    lib = load()
+    F = np.ascontiguousarray(F, dtype=np.float64)
+    DF = np.zeros(len(F))
+    lib.fo_do_derivative(len(F), tau, len(WA), np.ascontiguousarray(WA, dtype=np.float64),
+                         np.ascontiguousarray(gs, dtype=np.float64), F, maxt, t0, j0, DF)
+    return DF
+
+
+def do_fused_weights(aq, Wq, gq, tau, nl):
+    lib = load()
+    c = np.zeros(nl)
+    lib.fo_do_fused_weights(len(aq), *(np.ascontiguousarray(x, dtype=np.float64) for x in (aq, Wq, gq)),
+                            tau, nl, c)
+    return c
+
+
+def do_eq_solve(ex, C0, Nt, tblock, h, tau, D, WA, gs):
+    lib = load()
+    Nx = len(C0)
+    Cm = np.zeros((Nx, Nt))
+    Cm[:, 0] = C0
+    b0 = C.c_double()
+    lib.fo_do_eq_solve(ex, Nx, Nt, tblock, len(WA), h, tau, D,
+                       np.ascontiguousarray(WA, dtype=np.float64),
+                       np.ascontiguousarray(gs, dtype=np.float64), Cm.reshape(-1), C.byref(b0))
+    return Cm, b0.value

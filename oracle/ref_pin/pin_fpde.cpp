@@ -1,0 +1,241 @@
+/* Pin harness for the FP64 Caputo path of fpde_hpc_1d.cpp (test infrastructure).
+ *
+ * Built by oracle/Makefile from the reference source where it lies (the file is
+ * #included with its main renamed), never from a copy. It runs the reference's own
+ * H_solver in its 3D LOD mode -- the only mode in which the reference applies the FP64
+ * L1 history sum (fpde_hpc_1d.cpp:4258-4263, :4108) -- and records, step by step:
+ *   - the L1 weights kb_3_cache and the local weight kkk0 (precalc_kb_3 :4069-4085,
+ *     init_time_step :3942-3949);
+ *   - the history sum b_Utimesum computed by time_summing (:4086-4164);
+ *   - the grid after each step (calc_step :5100-5779);
+ *   - everything a replay of the step needs that the reference computes from its
+ *     hard-coded analytic problems: the tridiagonal coefficients A_/B/R of every line of
+ *     every pass (:3095-3142), the source Rp of the K pass (:2724) and the Dirichlet
+ *     boundary values bc0/bcN of every line (:4491-4583).
+ * The oracle and the GPU path replay the same steps from those inputs and must match the
+ * recorded grids to 1e-12. Scenarios are listed in main().
+ */
+#define main fpde_reference_main
+#include "fpde_hpc_1d.cpp"
+#undef main
+#include "fgv_write.h"
+
+struct PassState {
+    int m3d_x, m3d_y, m3d_c, N_, NB_;
+    double *dL_, *Z_;
+};
+
+static PassState save_state(H_solver *s)
+{
+    PassState p = {s->m3d_x, s->m3d_y, s->m3d_c, N, NB, s->dL, s->Z};
+    return p;
+}
+static void restore_state(H_solver *s, const PassState &p)
+{
+    s->m3d_x = p.m3d_x; s->m3d_y = p.m3d_y; s->m3d_c = p.m3d_c;
+    N = p.N_; NB = p.NB_; s->dL = p.dL_; s->Z = p.Z_;
+}
+/* Put the solver in the state calc_step gives it for one line of one pass
+ * (K pass :5258-5268, _M pass :5409-5419, sN pass :5559-5569). */
+static void enter_line(H_solver *s, int pass, int a, int b)
+{
+    s->equation = 0;
+    s->m3d_x = a; s->m3d_y = b; s->m3d_c = pass;
+    s->U.set(s->b_U, a, b, pass);
+    if (pass == 2) { s->dL = s->dLy; s->Z = s->Y; N = K; NB = KB; }
+    if (pass == 1) { s->dL = s->dLx; s->Z = s->X; N = _M; NB = MB; }
+    if (pass == 0) { s->dL = s->sdL; s->Z = s->sZ; N = sN; NB = sNB; }
+}
+static inline size_t gidx(int i, int j, int k) { return (size_t)idx(i, j, k); }
+
+/* Record the coefficient grids of the three passes: for pass c the value at the grid
+ * node of line position i is the reference's A_(i), B(i) and the Laplacian part a1 of
+ * R(i) (:3117-3123). a1 is read by evaluating R with Da = 0, so that a2 = Da*kkk0/tau
+ * vanishes exactly; a replay adds a2 of each step (kkk0 varies in its last bits from
+ * step to step because Time is accumulated). */
+static void record_coefs(H_solver *s, FgvWriter &w)
+{
+    size_t G = (size_t)(sN + 2) * (_M + 2) * (K + 2);
+    PassState st = save_state(s);
+    double Da_saved = s->Da;
+    s->Da = 0.0;
+    for (int pass = 0; pass < 3; pass++) {
+        std::vector<double> A(G, 0.0), B(G, 0.0), R(G, 0.0);
+        if (pass == 2)
+            for (int i = 1; i < sN; i++) for (int j = 1; j < _M; j++) {
+                enter_line(s, 2, i, j);
+                for (int k = 1; k < K; k++) { A[gidx(i, j, k)] = s->A_(k); B[gidx(i, j, k)] = s->B(k); R[gidx(i, j, k)] = s->R(k); }
+            }
+        if (pass == 1)
+            for (int k = 1; k < K; k++) for (int i = 1; i < sN; i++) {
+                enter_line(s, 1, i, k);
+                for (int j = 1; j < _M; j++) { A[gidx(i, j, k)] = s->A_(j); B[gidx(i, j, k)] = s->B(j); R[gidx(i, j, k)] = s->R(j); }
+            }
+        if (pass == 0)
+            for (int j = 1; j < _M; j++) for (int k = 1; k < K; k++) {
+                enter_line(s, 0, j, k);
+                for (int i = 1; i < sN; i++) { A[gidx(i, j, k)] = s->A_(i); B[gidx(i, j, k)] = s->B(i); R[gidx(i, j, k)] = s->R(i); }
+            }
+        char nm[32];
+        std::vector<uint64_t> dims = {(uint64_t)(K + 2), (uint64_t)(_M + 2), (uint64_t)(sN + 2)};
+        snprintf(nm, sizeof nm, "coefA_pass%d", pass); w.put(nm, dims, A.data());
+        snprintf(nm, sizeof nm, "coefB_pass%d", pass); w.put(nm, dims, B.data());
+        snprintf(nm, sizeof nm, "coefRlap_pass%d", pass); w.put(nm, dims, R.data());
+    }
+    s->Da = Da_saved;
+    restore_state(s, st);
+}
+
+/* Source of the K pass and Dirichlet values of every line, as used by the step that
+ * has just been taken (Rp and bc0/bcN read Time/tstep of that step). */
+static void record_step_inputs(H_solver *s, std::vector<double> &rp, std::vector<double> &bc)
+{
+    size_t G = (size_t)(sN + 2) * (_M + 2) * (K + 2);
+    size_t o = rp.size();
+    rp.resize(o + G, 0.0);
+    bc.resize(o + G, 0.0);
+    double *RP = &rp[o], *BC = &bc[o];
+    PassState st = save_state(s);
+    for (int i = 1; i < sN; i++) for (int j = 1; j < _M; j++) {
+        enter_line(s, 2, i, j);
+        for (int k = 1; k < K; k++) RP[gidx(i, j, k)] = s->Rp(k);
+        BC[gidx(i, j, 0)] = s->bc0();
+        BC[gidx(i, j, K)] = s->bcN();
+    }
+    for (int k = 1; k < K; k++) for (int i = 1; i < sN; i++) {
+        enter_line(s, 1, i, k);
+        BC[gidx(i, 0, k)] = s->bc0();
+        BC[gidx(i, _M, k)] = s->bcN();
+    }
+    for (int j = 1; j < _M; j++) for (int k = 1; k < K; k++) {
+        enter_line(s, 0, j, k);
+        BC[gidx(0, j, k)] = s->bc0();
+        BC[gidx(sN, j, k)] = s->bcN();
+    }
+    restore_state(s, st);
+}
+
+static void set_dims(int bs, int nb, int mb, int kb)
+{
+    BS = bs; NB = nb; MB = mb; KB = kb;
+    sN = N = BS * NB; sNB = NB;
+    _M = BS * MB; K = BS * KB;
+    delete[] F; delete[] BVK;
+    F = new double[N + _M + K + 2];
+    BVK = new double[BS];
+}
+
+/* One LOD run (mode 3, implicit 0, impl3d 0, split3d 0, sum_alg 0, EPS 1e-15). */
+static void run_lod(const char *path, int analytic, int bs, int nb, int mb, int kb,
+                    double alpha, const std::vector<double> &taus, int record_inputs)
+{
+    set_dims(bs, nb, mb, kb);
+    varT = 0; varZ = 0; varXY = 0;
+    implicit = 0; implicit3d = 0; rp_split_3d = 0; sum_alg = 0;
+    global_eps = 1e-15; global_eps2 = 1e-15;
+    FILE *lg = fopen("/dev/null", "w");
+    H_solver *s = new H_solver(analytic, 1, 5, 0, 1, alpha, 1.0, 0, 0, 0, 3, lg, 2);
+    size_t G = (size_t)(sN + 2) * (_M + 2) * (K + 2);
+    FgvWriter w(path);
+    w.scalar("sN", sN); w.scalar("M", _M); w.scalar("K", K);
+    w.scalar("alpha", alpha); w.scalar("Da", s->Da); w.scalar("analytic", analytic);
+    std::vector<uint64_t> gdims = {(uint64_t)(K + 2), (uint64_t)(_M + 2), (uint64_t)(sN + 2)};
+    w.put("U0", gdims, s->b_U);
+    std::vector<double> kb_all, kb_off, kkk0, tauv, S_all, U_all, rp, bc;
+    for (size_t n = 0; n < taus.size(); n++) {
+        s->calc_step(taus[n]);
+        kb_off.push_back((double)kb_all.size());
+        kb_all.insert(kb_all.end(), s->kb_3_cache.begin(), s->kb_3_cache.end());
+        kkk0.push_back(s->kkk0);
+        tauv.push_back(s->tau[s->tstep]);
+        if (n == 0 && record_inputs) record_coefs(s, w);
+        if (record_inputs) {
+            S_all.insert(S_all.end(), s->b_Utimesum, s->b_Utimesum + G);
+            U_all.insert(U_all.end(), s->b_U, s->b_U + G);
+            record_step_inputs(s, rp, bc);
+        }
+    }
+    kb_off.push_back((double)kb_all.size());
+    uint64_t ns = taus.size();
+    w.put("tau", tauv); w.put("kkk0", kkk0);
+    w.put("kb_flat", kb_all); w.put("kb_off", kb_off);
+    if (record_inputs) {
+        w.put("S", {ns, (uint64_t)(K + 2), (uint64_t)(_M + 2), (uint64_t)(sN + 2)}, S_all.data());
+        w.put("U", {ns, (uint64_t)(K + 2), (uint64_t)(_M + 2), (uint64_t)(sN + 2)}, U_all.data());
+        w.put("Rp", {ns, (uint64_t)(K + 2), (uint64_t)(_M + 2), (uint64_t)(sN + 2)}, rp.data());
+        w.put("BC", {ns, (uint64_t)(K + 2), (uint64_t)(_M + 2), (uint64_t)(sN + 2)}, bc.data());
+    }
+    double err = s->analytic_compare(NULL);
+    w.scalar("analytic_sq_err", err);
+    delete s;
+    fclose(lg);
+    printf("wrote %s (%zu steps, grid %dx%dx%d)\n", path, taus.size(), sN, _M, K);
+}
+
+/* Wall-clock timing of the reference's column run, for the CPU baseline
+ * (mode 3 BS 1 NB 3 M 3 K <n>, analytic 2, sum_alg 0, EPS 1e-15). */
+static void time_column(int kcells, double alpha, double tau, int steps)
+{
+    set_dims(1, 3, 3, kcells);
+    varT = 0; varZ = 0; varXY = 0;
+    implicit = 0; implicit3d = 0; rp_split_3d = 0; sum_alg = 0;
+    global_eps = 1e-15; global_eps2 = 1e-15;
+    FILE *lg = fopen("/dev/null", "w");
+    H_solver *s = new H_solver(2, 1, 5, 0, 1, alpha, 1.0, 0, 0, 0, 3, lg, 2);
+    struct timespec a, b;
+    clock_gettime(CLOCK_MONOTONIC, &a);
+    for (int n = 0; n < steps; n++) s->calc_step(tau);
+    clock_gettime(CLOCK_MONOTONIC, &b);
+    double sec = (b.tv_sec - a.tv_sec) + 1e-9 * (b.tv_nsec - a.tv_nsec);
+    double node_steps = 4.0 * (kcells - 1) * steps;
+    printf("{\"K\": %d, \"steps\": %d, \"seconds\": %.6f, \"node_steps_per_s\": %.6g}\n",
+           kcells, steps, sec, node_steps / sec);
+    delete s;
+    fclose(lg);
+}
+
+int main(int argc, char **argv)
+{
+    if (argc >= 2 && strcmp(argv[1], "time") == 0) {
+        int kc = argc > 2 ? atoi(argv[2]) : 1000;
+        int st = argc > 3 ? atoi(argv[3]) : 200;
+        double a = argc > 4 ? atof(argv[4]) : 0.8;
+        time_column(kc, a, 1e-3, st);
+        return 0;
+    }
+    const char *dir = argc >= 2 ? argv[1] : ".";
+    char p[4096];
+    /* 1D column form (4 identical columns), analytic problem 2, alpha 0.8. */
+    {
+        std::vector<double> taus(40, 0.0025);
+        snprintf(p, sizeof p, "%s/fpde_column_a2.fgv", dir);
+        run_lod(p, 2, 1, 3, 3, 32, 0.8, taus, 1);
+    }
+    /* Same column with analytic problem 5 (the gpu_test.sh problem) and alpha 0.5.
+     * (Analytic problem 1 is not used: with gamma = 1 its source evaluates to NaN.) */
+    {
+        std::vector<double> taus(30, 0.002);
+        snprintf(p, sizeof p, "%s/fpde_column_a5.fgv", dir);
+        run_lod(p, 5, 1, 3, 3, 24, 0.5, taus, 1);
+    }
+    /* True 3D LOD (6 x 4 x 8 cells), analytic problem 2, alpha 0.85. */
+    {
+        std::vector<double> taus(16, 0.0025);
+        snprintf(p, sizeof p, "%s/fpde_lod3d_a2.fgv", dir);
+        run_lod(p, 2, 2, 3, 2, 4, 0.85, taus, 1);
+    }
+    /* Weights only: variable time steps, alpha 0.7 (kb() with non-uniform Time). */
+    {
+        std::vector<double> taus;
+        for (int n = 0; n < 48; n++) taus.push_back(1e-3 * (1.0 + 0.5 * sin(0.7 * n)));
+        snprintf(p, sizeof p, "%s/fpde_weights_vartau.fgv", dir);
+        run_lod(p, 2, 1, 3, 3, 4, 0.7, taus, 0);
+    }
+    /* Weights only: long uniform run, alpha 0.3 (deep history, j up to 255). */
+    {
+        std::vector<double> taus(256, 1e-3);
+        snprintf(p, sizeof p, "%s/fpde_weights_long.fgv", dir);
+        run_lod(p, 2, 1, 3, 3, 4, 0.3, taus, 0);
+    }
+    return 0;
+}

@@ -1,0 +1,131 @@
+"""Pins the CPU oracle to the reference's own FP64 code.
+
+The fixtures in tests/golden were produced by running the reference (fpde_hpc_1d.cpp,
+fr_do.cpp) through the harnesses in oracle/ref_pin (regenerate with
+tests/golden/make_golden.py). Tolerances: 1e-12 relative wherever the oracle is given
+the reference's own weights (identical arithmetic up to operation order), and 1e-12 for
+the closed-form weights against the reference's series at EPS 1e-15.
+"""
+import numpy as np
+import pytest
+
+import fgv
+import oracle
+from conftest import golden_path
+
+RTOL = 1e-12
+
+
+def _relmax(a, b):
+    a, b = np.asarray(a), np.asarray(b)
+    scale = max(np.max(np.abs(b)), 1e-300)
+    return float(np.max(np.abs(a - b)) / scale)
+
+
+def _weights_of(g, n):
+    off = g["kb_off"].astype(int)
+    return g["kb_flat"][off[n]:off[n + 1]]
+
+
+@pytest.mark.parametrize("name", ["fpde_weights_long", "fpde_weights_vartau", "fpde_column_a2",
+                                  "fpde_column_a5", "fpde_lod3d_a2"])
+def test_l1_weights_closed_form_matches_reference_series(name):
+    g = fgv.load(golden_path(name))
+    alpha = g["alpha"]
+    time = oracle.time_points(g["tau"])
+    nsteps = len(g["tau"])
+    worst = 0.0
+    for n in range(nsteps):
+        kb_ref = _weights_of(g, n)
+        assert len(kb_ref) == n
+        kb, k0 = oracle.l1_weights(alpha, time, n)
+        if n:
+            worst = max(worst, float(np.max(np.abs(kb - kb_ref) / np.abs(kb_ref))))
+        worst = max(worst, abs(k0 - g["kkk0"][n]) / g["kkk0"][n])
+    assert worst <= RTOL, worst
+
+
+def _grids(g):
+    G = g["U0"].shape
+    cA = np.stack([g["coefA_pass%d" % p] for p in range(3)])
+    cB = np.stack([g["coefB_pass%d" % p] for p in range(3)])
+    cR = np.stack([g["coefRlap_pass%d" % p] for p in range(3)])
+    return G, cA, cB, cR
+
+
+@pytest.mark.parametrize("name", ["fpde_column_a2", "fpde_column_a5", "fpde_lod3d_a2"])
+@pytest.mark.parametrize("weights", ["reference", "closed_form"])
+def test_lod_replay_matches_reference_run(name, weights):
+    """Replays the reference's mode-3 LOD steps (history sum + three Thomas passes)."""
+    g = fgv.load(golden_path(name))
+    dims = (int(g["sN"]), int(g["M"]), int(g["K"]))
+    G, cA, cB, cR = _grids(g)
+    taus = g["tau"]
+    time = oracle.time_points(taus)
+    Da = g["Da"]
+    U = g["U0"].copy()
+    nsteps = len(taus)
+    hist = np.zeros((nsteps,) + G)
+    sN, M, K = dims
+    for n in range(nsteps):
+        if weights == "reference":
+            kb, k0 = _weights_of(g, n), g["kkk0"][n]
+        else:
+            kb, k0 = oracle.l1_weights(g["alpha"], time, n)
+        S = oracle.lod_step_dirichlet(dims, U, hist, n, kb if n else np.zeros(1), taus, Da, k0,
+                                      cA, cB, cR, g["Rp"][n], g["BC"][n], want_S=True)
+        # history sums on the K-pass nodes
+        sl = (slice(1, K + 1), slice(1, M), slice(1, sN))
+        if n:
+            # S is an intermediate with cancellation (a weighted sum of increments of
+            # O(1) values): closed-form weights, which differ from the reference's series
+            # by ~1e-13, move it by up to a few 1e-12 of its maximum.
+            tol_s = RTOL if weights == "reference" else 1e-11
+            assert _relmax(S[sl], g["S"][n][sl]) <= tol_s, (n, _relmax(S[sl], g["S"][n][sl]))
+        assert _relmax(U, g["U"][n]) <= RTOL, (n, _relmax(U, g["U"][n]))
+
+
+def test_l1_sum_snapshot_form_equals_increment_form():
+    g = fgv.load(golden_path("fpde_column_a2"))
+    U = g["U"]
+    n = U.shape[0] - 1
+    old = np.concatenate([g["U0"][None], U[:n]]).reshape(n + 1, -1)
+    kb = _weights_of(g, n)
+    S1 = oracle.l1_sum_snapshots(old, kb, g["tau"])
+    D = np.diff(old, axis=0)
+    S2 = oracle.l1_sum(D, n, kb, g["tau"])
+    np.testing.assert_array_equal(S1, S2)
+    Sref = g["S"][n].reshape(-1)
+    sN, M, K = int(g["sN"]), int(g["M"]), int(g["K"])
+    grid = np.zeros(g["U0"].shape, dtype=bool)
+    grid[1:K + 1, 1:M, 1:sN] = True
+    assert _relmax(S1[grid.reshape(-1)], Sref[grid.reshape(-1)]) <= RTOL
+
+
+def test_do_derivative_matches_fr_do():
+    g = fgv.load(golden_path("frdo_derivative"))
+    n, tau = int(g["N"]), g["tau"]
+    x = np.arange(n) * tau
+    F = x * x
+    DF = oracle.do_derivative(F, tau, g["WA"], g["gs"])
+    assert _relmax(DF[1:], g["DF_do"][1:]) <= RTOL
+    from math import gamma
+    DC = oracle.caputo_derivative(F, tau, 0.5, gamma(1.5))
+    assert _relmax(DC[1:], g["DF_caputo05"][1:]) <= RTOL
+
+
+@pytest.mark.parametrize("name", ["frdo_eq_ex0", "frdo_eq_ex1"])
+def test_do_equation_matches_fr_do(name):
+    g = fgv.load(golden_path(name))
+    ex, Nx, Nt = int(g["ex"]), int(g["Nx"]), int(g["Nt"])
+    h = g["h"]
+    x = np.arange(Nx) * h
+    C0 = np.zeros(Nx) if ex == 0 else x * (1.0 - x)
+    from math import gamma
+    Na = int(g["Na"])
+    gs = np.array([gamma(2.0 - (i / (Na - 1))) for i in range(Na)])
+    Cm, b0 = oracle.do_eq_solve(ex, C0, Nt, int(g["tblock"]), h, g["tau"], g["D"], g["WA"], gs)
+    assert abs(b0 - g["b0"]) <= RTOL * abs(g["b0"])
+    assert _relmax(Cm, g["C"]) <= RTOL, _relmax(Cm, g["C"])
+    err = np.sqrt(np.mean((Cm[:, -1] - g["analytic_last"]) ** 2))
+    assert abs(err - g["err"]) <= 1e-9 * max(g["err"], 1e-300) + 1e-15
