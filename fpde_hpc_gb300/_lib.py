@@ -1,0 +1,90 @@
+"""ctypes binding of libfpde_gb300.so (declared in include/fpde_gb300.h).
+
+Loading fails loudly when the library is missing: there is no CPU fallback.
+"""
+import ctypes as C
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libfpde_gb300.so")
+
+c_int, c_i64, c_dbl, c_vp = C.c_int, C.c_int64, C.c_double, C.c_void_p
+P_dbl = C.POINTER(C.c_double)
+
+
+class FpdeError(RuntimeError):
+    def __init__(self, code, where, msg):
+        super().__init__(f"{where} failed with status {code}: {msg}")
+        self.code = code
+
+
+class LineDesc(C.Structure):
+    _fields_ = [("N", c_i64), ("alpha", c_dbl), ("tau", c_dbl), ("Da", c_dbl),
+                ("left_kind", c_int), ("left_value", c_dbl), ("right_kind", c_int),
+                ("right_value", c_dbl), ("dLN", c_dbl), ("precision", c_int), ("block", c_int),
+                ("max_steps", c_int)]
+
+
+# name -> (restype, argtypes)
+_SIGS = {
+    "fpde_ctx_create": (c_int, [c_int, C.POINTER(c_vp)]),
+    "fpde_ctx_destroy": (c_int, [c_vp]),
+    "fpde_ctx_set_stream": (c_int, [c_vp, c_vp]),
+    "fpde_ctx_synchronize": (c_int, [c_vp]),
+    "fpde_ctx_sm_count": (c_int, [c_vp, C.POINTER(c_int)]),
+    "fpde_last_error_string": (C.c_char_p, []),
+    "fpde_kernel_launch_count": (c_i64, []),
+    "fpde_weights_l1": (c_int, [c_dbl, c_vp, c_int, c_vp, P_dbl]),
+    "fpde_weights_l1_lags": (c_int, [c_dbl, c_int, c_vp]),
+    "fpde_gamma": (c_int, [c_dbl, P_dbl]),
+    "fpde_history_create": (c_int, [c_vp, c_i64, c_i64, c_int, C.POINTER(c_vp)]),
+    "fpde_history_destroy": (c_int, [c_vp]),
+    "fpde_history_reset": (c_int, [c_vp]),
+    "fpde_history_length": (c_int, [c_vp, C.POINTER(c_i64)]),
+    "fpde_history_append": (c_int, [c_vp, c_vp, c_int]),
+    "fpde_l1_sum": (c_int, [c_vp, c_vp, c_vp, c_dbl, c_vp, c_int]),
+    "fpde_sum_snapshots": (c_int, [c_vp, c_vp, c_vp, c_int, c_i64, c_i64, c_vp, c_vp, c_int]),
+    "fpde_tridiag_solve": (c_int, [c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_i64, c_i64, c_i64, c_i64,
+                                   c_int, c_vp, c_int, c_vp, c_dbl, c_int]),
+    "fpde_line_create": (c_int, [c_vp, C.POINTER(LineDesc), c_vp, c_vp, c_vp, c_vp, C.POINTER(c_vp)]),
+    "fpde_line_destroy": (c_int, [c_vp]),
+    "fpde_line_reset": (c_int, [c_vp, c_vp, c_int]),
+    "fpde_line_run": (c_int, [c_vp, c_int]),
+    "fpde_line_get_state": (c_int, [c_vp, c_vp, c_int]),
+    "fpde_line_state_ptr": (c_int, [c_vp, C.POINTER(c_vp)]),
+    "fpde_line_solve_host": (c_int, [c_vp, c_vp, c_int, c_vp]),
+    "fpde_line_steps_done": (c_int, [c_vp, C.POINTER(c_i64)]),
+    "fpde_line_coefs": (c_int, [c_i64, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]),
+    "fpde_line_set_probe": (c_int, [c_vp, c_int]),
+    "fpde_line_probe_stats": (c_int, [c_vp, P_dbl, P_dbl, P_dbl, C.POINTER(c_int)]),
+}
+
+_lib = None
+
+
+def exported_symbols():
+    return list(_SIGS)
+
+
+def load(path=None):
+    """Load the shared library (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = path or LIB_PATH
+    if not os.path.exists(path):
+        raise ImportError(f"{path} not found: build it with fpde_hpc_gb300.build.build() "
+                          "(nvcc, sm_103a); there is no CPU fallback")
+    lib = C.CDLL(path)
+    for name, (res, args) in _SIGS.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def check(rc, where):
+    if rc != 0:
+        msg = load().fpde_last_error_string().decode(errors="replace")
+        raise FpdeError(rc, where, msg)

@@ -1,0 +1,205 @@
+"""Pythonic wrappers over the C ABI (host numpy arrays or CUDA torch tensors)."""
+import ctypes as C
+
+import numpy as np
+
+from ._lib import LineDesc, check, load
+
+FP64, SPLIT_BF16, SPLIT_F16 = 0, 1, 2
+
+
+def _is_dev(x):
+    return hasattr(x, "is_cuda") and x.is_cuda
+
+
+def _ptr(x):
+    if x is None:
+        return None
+    if hasattr(x, "data_ptr"):
+        if x.dtype.__str__() != "torch.float64" or not x.is_contiguous():
+            raise TypeError("device buffers must be contiguous float64 tensors")
+        return C.c_void_p(x.data_ptr())
+    if not (isinstance(x, np.ndarray) and x.dtype == np.float64 and x.flags["C_CONTIGUOUS"]):
+        raise TypeError("host buffers must be C-contiguous float64 numpy arrays")
+    return x.ctypes.data_as(C.c_void_p)
+
+
+def _f64(x):
+    return x if _is_dev(x) else np.ascontiguousarray(x, dtype=np.float64)
+
+
+def weights_l1(alpha, time, n):
+    t = np.ascontiguousarray(time, dtype=np.float64)
+    kb = np.zeros(max(n, 1))
+    k0 = C.c_double()
+    check(load().fpde_weights_l1(alpha, _ptr(t), n, _ptr(kb), C.byref(k0)), "fpde_weights_l1")
+    return kb[:n], k0.value
+
+
+def weights_l1_lags(alpha, n):
+    b = np.zeros(max(n, 1))
+    check(load().fpde_weights_l1_lags(alpha, n, _ptr(b)), "fpde_weights_l1_lags")
+    return b[:n]
+
+
+def gamma(x):
+    out = C.c_double()
+    check(load().fpde_gamma(x, C.byref(out)), "fpde_gamma")
+    return out.value
+
+
+def line_coefs(k, dL, iw=None):
+    k = np.ascontiguousarray(k, dtype=np.float64)
+    N = len(k) - 1
+    dL = np.ascontiguousarray(dL, dtype=np.float64)
+    A, B, R = np.zeros(N + 1), np.zeros(N + 1), np.zeros(N + 1)
+    iwp = None if iw is None else _ptr(np.ascontiguousarray(iw, dtype=np.float64))
+    check(load().fpde_line_coefs(N, _ptr(k), iwp, _ptr(dL), _ptr(A), _ptr(B), _ptr(R)), "fpde_line_coefs")
+    return A, B, R
+
+
+class Context:
+    def __init__(self, device=0):
+        self.lib = load()
+        self.h = C.c_void_p()
+        check(self.lib.fpde_ctx_create(device, C.byref(self.h)), "fpde_ctx_create")
+
+    def close(self):
+        if self.h:
+            self.lib.fpde_ctx_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def synchronize(self):
+        check(self.lib.fpde_ctx_synchronize(self.h), "fpde_ctx_synchronize")
+
+    def set_stream(self, stream_handle):
+        check(self.lib.fpde_ctx_set_stream(self.h, C.c_void_p(stream_handle)), "fpde_ctx_set_stream")
+
+    @property
+    def sm_count(self):
+        v = C.c_int()
+        check(self.lib.fpde_ctx_sm_count(self.h, C.byref(v)), "fpde_ctx_sm_count")
+        return v.value
+
+    def sum_snapshots(self, old, kb, tau, nodes=None):
+        """The reference Sum kernel contract: old is (old_size, OS) time-major snapshots."""
+        dev = _is_dev(old)
+        old = _f64(old)
+        nold, OS = old.shape
+        nodes = OS if nodes is None else nodes
+        if dev:
+            import torch
+            S = torch.zeros(nodes, dtype=torch.float64, device=old.device)
+        else:
+            S = np.zeros(nodes)
+        kb = _f64(kb) if nold >= 2 else None
+        tau = _f64(tau) if nold >= 2 else None
+        check(self.lib.fpde_sum_snapshots(self.h, _ptr(S), _ptr(old), nold, OS, nodes, _ptr(tau), _ptr(kb),
+                                          1 if dev else 0), "fpde_sum_snapshots")
+        return S
+
+    def tridiag_solve(self, a, b, r, om, u, n_lines, N, stride_elem, stride_line, left_kind=0,
+                      left_val=None, right_kind=0, right_val=None, dLN=0.0):
+        dev = _is_dev(u)
+        args = [_f64(x) for x in (a, b, r, om)]
+        lv = None if left_val is None else _f64(left_val)
+        rv = None if right_val is None else _f64(right_val)
+        check(self.lib.fpde_tridiag_solve(self.h, *(_ptr(x) for x in args), _ptr(u), n_lines, N, stride_elem,
+                                          stride_line, left_kind, _ptr(lv), right_kind, _ptr(rv), dLN,
+                                          1 if dev else 0), "fpde_tridiag_solve")
+        return u
+
+
+class History:
+    def __init__(self, ctx, nodes, max_steps, precision=FP64):
+        self.ctx, self.nodes = ctx, nodes
+        self.h = C.c_void_p()
+        check(ctx.lib.fpde_history_create(ctx.h, nodes, max_steps, precision, C.byref(self.h)),
+              "fpde_history_create")
+
+    def close(self):
+        if self.h:
+            self.ctx.lib.fpde_history_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def append(self, u):
+        u = _f64(u)
+        check(self.ctx.lib.fpde_history_append(self.h, _ptr(u), 1 if _is_dev(u) else 0), "fpde_history_append")
+
+    def __len__(self):
+        n = C.c_int64()
+        check(self.ctx.lib.fpde_history_length(self.h, C.byref(n)), "fpde_history_length")
+        return n.value
+
+    def l1_sum(self, kb, tau=None, scale=1.0, out=None):
+        kb = np.ascontiguousarray(kb, dtype=np.float64)
+        tp = None if tau is None else np.ascontiguousarray(tau, dtype=np.float64)
+        if out is None:
+            out = np.zeros(self.nodes)
+        check(self.ctx.lib.fpde_l1_sum(self.h, _ptr(kb), _ptr(tp), scale, _ptr(out), 1 if _is_dev(out) else 0),
+              "fpde_l1_sum")
+        return out
+
+
+class Line:
+    """A 1D Caputo line problem advanced on the GPU (fpde_line_*)."""
+
+    def __init__(self, ctx, N, alpha, tau, Da, A, B, Rlap, u0, max_steps, left=(0, 0.0), right=(0, 0.0),
+                 dLN=0.0, precision=FP64, block=0):
+        self.ctx, self.N = ctx, N
+        d = LineDesc(N=N, alpha=alpha, tau=tau, Da=Da, left_kind=left[0], left_value=left[1],
+                     right_kind=right[0], right_value=right[1], dLN=dLN, precision=precision, block=block,
+                     max_steps=max_steps)
+        self.desc = d
+        arrs = [np.ascontiguousarray(x, dtype=np.float64) for x in (A, B, Rlap, u0)]
+        self.h = C.c_void_p()
+        check(ctx.lib.fpde_line_create(ctx.h, C.byref(d), *(_ptr(x) for x in arrs), C.byref(self.h)),
+              "fpde_line_create")
+
+    def close(self):
+        if self.h:
+            self.ctx.lib.fpde_line_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def reset(self, u0):
+        u0 = _f64(u0)
+        check(self.ctx.lib.fpde_line_reset(self.h, _ptr(u0), 1 if _is_dev(u0) else 0), "fpde_line_reset")
+
+    def run(self, steps):
+        check(self.ctx.lib.fpde_line_run(self.h, steps), "fpde_line_run")
+
+    def state(self, out=None):
+        if out is None:
+            out = np.zeros(self.N + 1)
+        check(self.ctx.lib.fpde_line_get_state(self.h, _ptr(out), 1 if _is_dev(out) else 0), "fpde_line_get_state")
+        return out
+
+    def state_ptr(self):
+        p = C.c_void_p()
+        check(self.ctx.lib.fpde_line_state_ptr(self.h, C.byref(p)), "fpde_line_state_ptr")
+        return p.value
+
+    def solve_host(self, u0, steps, out):
+        check(self.ctx.lib.fpde_line_solve_host(self.h, _ptr(u0), steps, _ptr(out)), "fpde_line_solve_host")
+        return out
+
+    def set_probe(self, every):
+        check(self.ctx.lib.fpde_line_set_probe(self.h, every), "fpde_line_set_probe")
+
+    def probe_stats(self):
+        hm, hb, sm, n = C.c_double(), C.c_double(), C.c_double(), C.c_int()
+        check(self.ctx.lib.fpde_line_probe_stats(self.h, C.byref(hm), C.byref(hb), C.byref(sm), C.byref(n)),
+              "fpde_line_probe_stats")
+        return {"hist_ms": hm.value, "hist_bytes": hb.value, "solve_ms": sm.value, "probes": n.value}
+
+    @property
+    def steps_done(self):
+        n = C.c_int64()
+        check(self.ctx.lib.fpde_line_steps_done(self.h, C.byref(n)), "fpde_line_steps_done")
+        return n.value

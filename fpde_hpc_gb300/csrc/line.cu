@@ -1,0 +1,586 @@
+// 1D line problem (fpde_line_*): the plain FP64 path.
+//
+// Per time step n (fpde_hpc_1d.cpp calc_step / U1 with the history applied every step):
+//   1. k_l1_partial : part[ks][i] = sum_t w[n-t] D_t[i]        (HBM-bound FP64 GEMV)
+//   2. k_line_solve : S = sum_ks part, Om = -lam U + src + S, Thomas solve, U <- U^{n+1},
+//                     D_n = U^{n+1} - U^n                       (one cooperative launch)
+// The whole run is captured once into a CUDA graph and replayed.
+//
+// The Thomas solve of a long line runs on all SMs. The alpha recurrence
+// Al[i+1] = B/(R - A Al[i]) is time-invariant (uniform tau) and is done once on the host;
+// per step only the two first-order recurrences remain,
+//   forward   Bt[i+1] = g_i (A_i Bt[i] - Om_i),      g_i = Al[i+1]/B_i
+//   backward  U_i     = Al[i+1] U_{i+1} + Bt[i+1],
+// each an affine scan x_i = p_i x_{i-1} + r_i. Every thread runs its segment of <= 8 nodes
+// sequentially from zero, segments are combined by warp-shuffle scans of (P, X) pairs, then
+// across warps through shared memory, then across CTAs through a bounded grid barrier;
+// finally each node adds (prefix product) x (carry), with the within-segment prefix products
+// of p and Al precomputed once (cf, cb).
+#include <map>
+#include <vector>
+#include <cmath>
+#include <cstring>
+
+#include "common.cuh"
+#include "kernels.cuh"
+
+namespace fpde {
+
+constexpr int LT = 128;      // threads per CTA of the line solve
+constexpr int LSEG = 8;      // max nodes per thread
+constexpr unsigned FULL = 0xffffffffu;
+
+struct LineSolveArgs {
+    const double *A, *g, *al, *cf, *cb;   // time-invariant, indexed by node 0..N-1
+    const double *src;                    // optional source (N+1), may be null
+    double *U;                            // state (N+1)
+    double *Drow;                         // increment row of this step (P)
+    const double *part;                   // partial history sums [KS][P]
+    double *aggf, *aggb;                  // [G][2] CTA aggregates
+    double *UN;                           // right boundary value slot
+    unsigned *barrier, *flags;
+    int64_t P;
+    double lam, g0, gN, dLN, AlN;
+    int KS, N, s, G, rkind;
+};
+
+__device__ __forceinline__ void warp_scan_up(double &P, double &X, int lane)
+{
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+        double Pp = __shfl_up_sync(FULL, P, off), Xp = __shfl_up_sync(FULL, X, off);
+        if (lane >= off) { X = fma(P, Xp, X); P = P * Pp; }
+    }
+}
+__device__ __forceinline__ void warp_scan_down(double &P, double &X, int lane)
+{
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+        double Pn = __shfl_down_sync(FULL, P, off), Xn = __shfl_down_sync(FULL, X, off);
+        if (lane + off < 32) { X = fma(P, Xn, X); P = P * Pn; }
+    }
+}
+
+// Carry into CTA c from the aggregates of the CTAs before it (forward, from carry 0)
+// or after it (backward, from carry `init`). Executed by warp 0; returns the carry.
+__device__ __forceinline__ double grid_carry(const double *agg, int G, int c, bool forward, double init, int lane)
+{
+    int lo = forward ? 0 : c + 1, hi = forward ? c : G;          // CTAs [lo, hi)
+    int cnt = hi - lo;
+    int m = (cnt + 31) / 32;
+    double P = 1.0, X = 0.0;
+    if (forward) {
+        for (int k = 0; k < m; ++k) {                             // lane's range in order
+            int cc = lo + lane * m + k;
+            if (cc < hi) { double Pc = __ldcg(agg + 2 * cc), Xc = __ldcg(agg + 2 * cc + 1); X = fma(Pc, X, Xc); P *= Pc; }
+        }
+        warp_scan_up(P, X, lane);
+        double Pt = __shfl_sync(FULL, P, 31), Xt = __shfl_sync(FULL, X, 31);
+        return fma(Pt, init, Xt);
+    } else {
+        for (int k = m - 1; k >= 0; --k) {                        // descending
+            int cc = lo + lane * m + k;
+            if (cc < hi) { double Pc = __ldcg(agg + 2 * cc), Xc = __ldcg(agg + 2 * cc + 1); X = fma(Pc, X, Xc); P *= Pc; }
+        }
+        warp_scan_down(P, X, lane);
+        double Pt = __shfl_sync(FULL, P, 0), Xt = __shfl_sync(FULL, X, 0);
+        return fma(Pt, init, Xt);
+    }
+}
+
+__global__ void __launch_bounds__(LT) k_line_solve(LineSolveArgs p)
+{
+    __shared__ double wP[LT / 32], wX[LT / 32], wPe[LT / 32], wXe[LT / 32];
+    __shared__ double s_carry, s_UN;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int c = blockIdx.x;
+    const int i0 = (c * LT + tid) * p.s;
+    const int i1 = min(i0 + p.s, p.N);
+    const int cnt = max(0, i1 - i0);
+
+    double uo[LSEG], y[LSEG];
+    // ---- forward: local sweep from zero
+    double yl = 0.0;
+#pragma unroll
+    for (int k = 0; k < LSEG; ++k) {
+        if (k < cnt) {
+            const int i = i0 + k;
+            const double u_old = p.U[i];
+            uo[k] = u_old;
+            if (i == 0) {
+                yl = p.g0;                                        // Bt[1]
+            } else {
+                double S = 0.0;
+                for (int q = 0; q < p.KS; ++q) S += p.part[(int64_t)q * p.P + i];
+                const double Om = (-(p.lam * u_old) + (p.src ? p.src[i] : 0.0)) + S;
+                yl = p.g[i] * (p.A[i] * yl - Om);
+            }
+            y[k] = yl;
+        }
+    }
+    double P = cnt > 0 ? p.cf[i1 - 1] : 1.0, X = cnt > 0 ? yl : 0.0;
+    warp_scan_up(P, X, lane);
+    double Pe = __shfl_up_sync(FULL, P, 1), Xe = __shfl_up_sync(FULL, X, 1);
+    if (lane == 0) { Pe = 1.0; Xe = 0.0; }
+    if (lane == 31) { wP[warp] = P; wX[warp] = X; }
+    __syncthreads();
+    if (warp == 0) {
+        double Pw = lane < LT / 32 ? wP[lane] : 1.0, Xw = lane < LT / 32 ? wX[lane] : 0.0;
+        warp_scan_up(Pw, Xw, lane);
+        double Pwe = __shfl_up_sync(FULL, Pw, 1), Xwe = __shfl_up_sync(FULL, Xw, 1);
+        if (lane == 0) { Pwe = 1.0; Xwe = 0.0; }
+        if (lane < LT / 32) { wPe[lane] = Pwe; wXe[lane] = Xwe; }
+        if (lane == LT / 32 - 1 && p.G > 1) { p.aggf[2 * c] = Pw; p.aggf[2 * c + 1] = Xw; __threadfence(); }
+    }
+    if (p.G > 1) {
+        if (!grid_barrier(p.barrier, p.G, p.flags)) return;
+        if (warp == 0) {
+            double cc = grid_carry(p.aggf, p.G, c, true, 0.0, lane);
+            if (lane == 0) s_carry = cc;
+        }
+    } else if (tid == 0) {
+        s_carry = 0.0;
+    }
+    __syncthreads();
+    {
+        const double carry_w = fma(wPe[warp], s_carry, wXe[warp]);
+        const double carry = fma(Pe, carry_w, Xe);
+#pragma unroll
+        for (int k = 0; k < LSEG; ++k)
+            if (k < cnt) y[k] = fma(p.cf[i0 + k], carry, y[k]);
+    }
+    // ---- right boundary value (owner of node N-1)
+    if (cnt > 0 && i1 == p.N) {
+        const double BtN = y[cnt - 1], uNm1 = uo[cnt - 1];
+        double UN;
+        if (p.rkind == FPDE_BC_DIRICHLET) {
+            UN = p.gN;
+        } else if (fabs(BtN) > 1e-15) {
+            UN = (fabs(1.0 - p.AlN) > 1e-15) ? (BtN + p.gN * p.dLN) / (1.0 - p.AlN) : uNm1;
+        } else {
+            UN = (fabs(1.0 - p.AlN) > 1e-15) ? 0.0 : uNm1;
+        }
+        if (p.G > 1) { *p.UN = UN; __threadfence(); }
+        s_UN = UN;
+        const double uNold = p.U[p.N];
+        p.U[p.N] = UN;
+        p.Drow[p.N] = UN - uNold;
+    }
+    // ---- backward: local sweep from zero, descending
+    double ub[LSEG];
+    double ul = 0.0;
+#pragma unroll
+    for (int k = LSEG - 1; k >= 0; --k) {
+        if (k < cnt) {
+            ul = fma(p.al[i0 + k], ul, y[k]);
+            ub[k] = ul;
+        }
+    }
+    P = cnt > 0 ? p.cb[i0] : 1.0;
+    X = cnt > 0 ? ul : 0.0;
+    warp_scan_down(P, X, lane);
+    Pe = __shfl_down_sync(FULL, P, 1);
+    Xe = __shfl_down_sync(FULL, X, 1);
+    if (lane == 31) { Pe = 1.0; Xe = 0.0; }
+    __syncthreads();                                    // wP/wX reuse
+    if (lane == 0) { wP[warp] = P; wX[warp] = X; }
+    __syncthreads();
+    if (warp == 0) {
+        constexpr int NW = LT / 32;
+        double Pw = lane < NW ? wP[lane] : 1.0, Xw = lane < NW ? wX[lane] : 0.0;
+        // suffix scan over warps 0..NW-1 (later warps first)
+        warp_scan_down(Pw, Xw, lane);
+        double Pwe = __shfl_down_sync(FULL, Pw, 1), Xwe = __shfl_down_sync(FULL, Xw, 1);
+        if (lane >= NW - 1) { Pwe = 1.0; Xwe = 0.0; }
+        if (lane < NW) { wPe[lane] = Pwe; wXe[lane] = Xwe; }
+        if (lane == 0 && p.G > 1) { p.aggb[2 * c] = Pw; p.aggb[2 * c + 1] = Xw; __threadfence(); }
+    }
+    if (p.G > 1) {
+        if (!grid_barrier(p.barrier, p.G, p.flags)) return;
+        if (warp == 0) {
+            const double UN = __ldcg(p.UN);
+            double cc = grid_carry(p.aggb, p.G, c, false, UN, lane);
+            if (lane == 0) s_carry = cc;
+        }
+    } else {
+        __syncthreads();
+        if (tid == 0) s_carry = s_UN;
+    }
+    __syncthreads();
+    {
+        const double carry_w = fma(wPe[warp], s_carry, wXe[warp]);
+        const double carry = fma(Pe, carry_w, Xe);
+#pragma unroll
+        for (int k = 0; k < LSEG; ++k) {
+            if (k < cnt) {
+                const int i = i0 + k;
+                const double un = fma(p.cb[i], carry, ub[k]);
+                p.U[i] = un;
+                p.Drow[i] = un - uo[k];
+            }
+        }
+    }
+}
+
+}  // namespace fpde
+
+using namespace fpde;
+
+struct fpde_line {
+    fpde_ctx *ctx = nullptr;
+    fpde_line_desc d{};
+    int64_t N = 0, P = 0;
+    int G = 1, s = 1, max_steps = 0;
+    double lam = 0, lamR = 0, kkk0 = 0, AlN = 0;
+    double *A = nullptr, *g = nullptr, *al = nullptr, *cf = nullptr, *cb = nullptr;
+    double *U = nullptr, *D = nullptr, *part = nullptr, *wrev = nullptr;
+    double *aggf = nullptr, *aggb = nullptr, *UN = nullptr;
+    unsigned *barrier = nullptr;
+    double *pinned = nullptr;
+    int64_t n_done = 0;
+    std::map<std::pair<int64_t, int>, cudaGraphExec_t> graphs;
+    std::map<std::pair<int64_t, int>, int64_t> graph_launches;
+    int probe_every = 0;
+    std::vector<cudaEvent_t> probe_ev;          // 3 per probed step
+    std::vector<int64_t> probe_steps;           // steps probed by the last enqueue
+    std::map<std::pair<int64_t, int>, std::vector<int64_t>> graph_probe_steps;
+    std::vector<int64_t> last_probe_steps;
+};
+
+namespace fpde {
+
+static int line_launch_solve(fpde_line *L, cudaStream_t st, int64_t n, int KS)
+{
+    LineSolveArgs a;
+    a.A = L->A; a.g = L->g; a.al = L->al; a.cf = L->cf; a.cb = L->cb; a.src = nullptr;
+    a.U = L->U; a.Drow = L->D + n * L->P; a.part = L->part;
+    a.aggf = L->aggf; a.aggb = L->aggb; a.UN = L->UN;
+    a.barrier = L->barrier; a.flags = L->ctx->d_flags;
+    a.P = L->P; a.lam = L->lam; a.g0 = L->d.left_value; a.gN = L->d.right_value; a.dLN = L->d.dLN;
+    a.AlN = L->AlN; a.KS = KS; a.N = (int)L->N; a.s = L->s; a.G = L->G; a.rkind = L->d.right_kind;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(L->G);
+    cfg.blockDim = dim3(LT);
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = L->G > 1 ? 1 : 0;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    FPDE_CUDA(cudaLaunchKernelEx(&cfg, k_line_solve, a));
+    count_launches(1);
+    return FPDE_OK;
+}
+
+// Enqueue steps [n0, n0+steps) on st; returns the number of kernels enqueued via *nk.
+static int line_enqueue(fpde_line *L, cudaStream_t st, int64_t n0, int steps, int64_t *nk)
+{
+    int64_t k = 0;
+    L->probe_steps.clear();
+    for (int64_t n = n0; n < n0 + steps; ++n) {
+        int KS = 0;
+        cudaEvent_t *ev = nullptr;
+        if (L->probe_every > 0 && n >= 1 && (n % L->probe_every) == L->probe_every - 1 &&
+            (L->probe_steps.size() + 1) * 3 <= L->probe_ev.size()) {
+            ev = &L->probe_ev[3 * L->probe_steps.size()];
+            L->probe_steps.push_back(n);
+        }
+        if (n >= 1) {
+            KS = choose_splits((int)n, L->P);
+            const double *wt = L->wrev + (L->max_steps - n);   // wt[t] = w[n - t]
+            if (ev) FPDE_CUDA(cudaEventRecordWithFlags(ev[0], st, cudaEventRecordExternal));
+            int rc = launch_l1_partial(st, L->D, L->P, (int)n, wt, L->part, KS);
+            if (rc) return rc;
+            if (ev) FPDE_CUDA(cudaEventRecordWithFlags(ev[1], st, cudaEventRecordExternal));
+            ++k;
+        }
+        int rc = line_launch_solve(L, st, n, KS);
+        if (rc) return rc;
+        if (ev) FPDE_CUDA(cudaEventRecordWithFlags(ev[2], st, cudaEventRecordExternal));
+        ++k;
+    }
+    if (nk) *nk = k;
+    return FPDE_OK;
+}
+
+}  // namespace fpde
+
+extern "C" {
+
+int fpde_line_coefs(int64_t N, const double *k, const double *iw, const double *dL, double *A, double *B,
+                    double *Rlap)
+{
+    FPDE_CHECK_ARG(N >= 2 && k && dL && A && B && Rlap, "bad arguments");
+    for (int64_t i = 1; i < N; ++i) {
+        const double w = iw ? iw[i] : 1.0;
+        A[i] = k[i - 1] * w / (dL[i] * dL[i - 1]);
+        B[i] = k[i] * w / (dL[i] * dL[i]);
+        Rlap[i] = w * ((k[i] / (dL[i] * dL[i])) + (k[i - 1] / (dL[i] * dL[i - 1])));
+    }
+    return FPDE_OK;
+}
+
+int fpde_line_destroy(fpde_line *L)
+{
+    if (!L) return FPDE_OK;
+    if (L->ctx) {
+        cudaSetDevice(L->ctx->device);
+        cudaStreamSynchronize(L->ctx->stream);
+        L->ctx->lines.erase(L);
+    }
+    for (auto &kv : L->graphs) cudaGraphExecDestroy(kv.second);
+    for (cudaEvent_t e : L->probe_ev) cudaEventDestroy(e);
+    for (double *p : {L->A, L->g, L->al, L->cf, L->cb, L->U, L->D, L->part, L->wrev, L->aggf, L->aggb, L->UN})
+        dev_free(p);
+    dev_free(L->barrier);
+    if (L->pinned) cudaFreeHost(L->pinned);
+    delete L;
+    return FPDE_OK;
+}
+
+int fpde_line_create(fpde_ctx *ctx, const fpde_line_desc *desc, const double *A, const double *B,
+                     const double *Rlap, const double *u0, fpde_line **out)
+{
+    clear_error();
+    FPDE_CHECK_ARG(out && desc && A && B && Rlap && u0, "null argument");
+    *out = nullptr;
+    int rc = ctx_enter(ctx);
+    if (rc) return rc;
+    const fpde_line_desc &d = *desc;
+    FPDE_CHECK_ARG(d.N >= 2, "N must be >= 2");
+    FPDE_CHECK_ARG(d.alpha > 0.0 && d.alpha < 1.0, "alpha must be in (0, 1)");
+    FPDE_CHECK_ARG(d.tau > 0.0, "tau must be positive");
+    FPDE_CHECK_ARG(d.max_steps > 0, "max_steps must be positive");
+    FPDE_CHECK_ARG(d.left_kind == 0 || d.left_kind == 1, "bad left boundary kind");
+    FPDE_CHECK_ARG(d.right_kind == 0 || d.right_kind == 1, "bad right boundary kind");
+    FPDE_CHECK_ARG(d.precision == FPDE_PREC_FP64 || d.precision == FPDE_PREC_SPLIT_BF16 ||
+                   d.precision == FPDE_PREC_SPLIT_F16, "bad precision mode");
+    const int64_t N = d.N;
+    // partition of nodes 0..N-1 over G CTAs x LT threads x s nodes
+    int G = (int)((N + (int64_t)LT * 4 - 1) / ((int64_t)LT * 4));
+    if (G > ctx->sm_count) G = ctx->sm_count;
+    if (G < 1) G = 1;
+    int64_t s = (N + (int64_t)G * LT - 1) / ((int64_t)G * LT);
+    if (s > LSEG)
+        return set_error(FPDE_ERR_UNSUPPORTED, "line of %lld intervals exceeds %lld (SMs x %d x %d)", (long long)N,
+                         (long long)ctx->sm_count * LT * LSEG, LT, LSEG);
+    int per_sm = 0;
+    FPDE_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_line_solve, LT, 0));
+    if (G > 1 && G > per_sm * ctx->sm_count)
+        return set_error(FPDE_ERR_UNSUPPORTED, "line solve grid of %d CTAs cannot be co-resident", G);
+
+    fpde_line *L = new fpde_line();
+    L->ctx = ctx;
+    L->d = d;
+    L->N = N;
+    L->P = (N + 1 + 511) / 512 * 512;
+    L->G = G;
+    L->s = (int)s;
+    L->max_steps = d.max_steps;
+    // local weight kkk0 = tau^{1-alpha}/(1-alpha); lam as in Om1 (:4191), lamR as in R (:3120)
+    L->kkk0 = l1_interval_weight(d.alpha, 0.0, d.tau);
+    L->lam = d.Da * (L->kkk0 / d.tau);
+    L->lamR = d.Da * L->kkk0 / d.tau;
+
+    // time-invariant Thomas data (host, FP64)
+    std::vector<double> Al(N + 2, 0.0), hA(N, 0.0), hg(N, 0.0), hal(N, 0.0), hp(N, 0.0), hcf(N), hcb(N);
+    Al[1] = d.left_kind == FPDE_BC_FLUX ? 1.0 : 0.0;
+    for (int64_t i = 1; i < N; ++i) Al[i + 1] = B[i] / ((Rlap[i] + L->lamR) - A[i] * Al[i]);
+    L->AlN = Al[N];
+    for (int64_t i = 0; i < N; ++i) {
+        hal[i] = Al[i + 1];
+        if (i >= 1) {
+            hA[i] = A[i];
+            hg[i] = Al[i + 1] / B[i];
+            hp[i] = hg[i] * A[i];
+        }
+    }
+    for (int64_t t0 = 0; t0 < N; t0 += s) {                      // per-thread segments
+        int64_t t1 = t0 + s < N ? t0 + s : N;
+        double pr = 1.0;
+        for (int64_t i = t0; i < t1; ++i) { pr *= hp[i]; hcf[i] = pr; }
+        pr = 1.0;
+        for (int64_t i = t1 - 1; i >= t0; --i) { pr *= hal[i]; hcb[i] = pr; }
+    }
+    // lag weights, reversed: wrev[m] = Da * kb(lag L-m) / tau, kb(lag j) = kkk0 * b_j
+    std::vector<double> wrev(L->max_steps + 1, 0.0);
+    for (int64_t m = 0; m < L->max_steps; ++m) {
+        int64_t j = L->max_steps - m;
+        wrev[m] = d.Da * (L->kkk0 * l1_lag(d.alpha, j)) / d.tau;
+    }
+    const size_t nb = N * sizeof(double);
+    if (dev_alloc((void **)&L->A, nb) || dev_alloc((void **)&L->g, nb) || dev_alloc((void **)&L->al, nb) ||
+        dev_alloc((void **)&L->cf, nb) || dev_alloc((void **)&L->cb, nb) ||
+        dev_alloc((void **)&L->U, L->P * sizeof(double)) ||
+        dev_alloc((void **)&L->D, (size_t)L->max_steps * L->P * sizeof(double)) ||
+        dev_alloc((void **)&L->part, (size_t)KS_MAX * L->P * sizeof(double)) ||
+        dev_alloc((void **)&L->wrev, wrev.size() * sizeof(double)) ||
+        dev_alloc((void **)&L->aggf, 2 * G * sizeof(double)) || dev_alloc((void **)&L->aggb, 2 * G * sizeof(double)) ||
+        dev_alloc((void **)&L->UN, sizeof(double)) || dev_alloc((void **)&L->barrier, 2 * sizeof(unsigned))) {
+        std::string keep = fpde_last_error_string();
+        fpde_line_destroy(L);
+        return set_error(FPDE_ERR_NOMEM, "%s", keep.c_str());
+    }
+    cudaStream_t st = ctx->stream;
+    cudaMemcpyAsync(L->A, hA.data(), nb, cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(L->g, hg.data(), nb, cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(L->al, hal.data(), nb, cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(L->cf, hcf.data(), nb, cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(L->cb, hcb.data(), nb, cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(L->wrev, wrev.data(), wrev.size() * sizeof(double), cudaMemcpyHostToDevice, st);
+    cudaMemsetAsync(L->U, 0, L->P * sizeof(double), st);
+    cudaMemcpyAsync(L->U, u0, (N + 1) * sizeof(double), cudaMemcpyHostToDevice, st);
+    cudaMemsetAsync(L->D, 0, (size_t)L->max_steps * L->P * sizeof(double), st);
+    cudaMemsetAsync(L->barrier, 0, 2 * sizeof(unsigned), st);
+    cudaError_t e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) {
+        fpde_line_destroy(L);
+        return set_error(FPDE_ERR_CUDA, "line setup: %s", cudaGetErrorString(e));
+    }
+    ctx->lines.insert(L);
+    *out = L;
+    return FPDE_OK;
+}
+
+int fpde_line_reset(fpde_line *L, const double *u0, int on_device)
+{
+    clear_error();
+    FPDE_CHECK_ARG(L && u0, "null argument");
+    int rc = ctx_enter(L->ctx);
+    if (rc) return rc;
+    FPDE_CUDA(cudaMemcpyAsync(L->U, u0, (L->N + 1) * sizeof(double),
+                              on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, L->ctx->stream));
+    if (!on_device) FPDE_CUDA(cudaStreamSynchronize(L->ctx->stream));
+    L->n_done = 0;
+    return FPDE_OK;
+}
+
+int fpde_line_run(fpde_line *L, int steps)
+{
+    clear_error();
+    FPDE_CHECK_ARG(L && steps >= 0, "bad arguments");
+    int rc = ctx_enter(L->ctx);
+    if (rc) return rc;
+    if (steps == 0) return FPDE_OK;
+    if (L->n_done + steps > L->max_steps)
+        return set_error(FPDE_ERR_CAPACITY, "run of %d steps exceeds the history capacity %d", steps, L->max_steps);
+    cudaStream_t st = L->ctx->stream;
+    auto key = std::make_pair(L->n_done, steps);
+    auto it = L->graphs.find(key);
+    if (it == L->graphs.end()) {
+        cudaStream_t cs;
+        FPDE_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+        cudaGraph_t graph;
+        FPDE_CUDA(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
+        int64_t nk = 0;
+        int64_t before = fpde_kernel_launch_count();
+        rc = line_enqueue(L, cs, L->n_done, steps, &nk);
+        cudaError_t e = cudaStreamEndCapture(cs, &graph);
+        fpde::count_launches(-(fpde_kernel_launch_count() - before));   // counted at replay
+        cudaStreamDestroy(cs);
+        if (rc) return rc;
+        if (e != cudaSuccess) return set_error(FPDE_ERR_CUDA, "graph capture: %s", cudaGetErrorString(e));
+        cudaGraphExec_t exec;
+        e = cudaGraphInstantiate(&exec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (e != cudaSuccess) return set_error(FPDE_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(e));
+        it = L->graphs.emplace(key, exec).first;
+        L->graph_launches[key] = nk;
+        L->graph_probe_steps[key] = L->probe_steps;
+    }
+    L->last_probe_steps = L->graph_probe_steps[key];
+    FPDE_CUDA(cudaGraphLaunch(it->second, st));
+    count_launches(L->graph_launches[key]);
+    L->n_done += steps;
+    return FPDE_OK;
+}
+
+int fpde_line_get_state(fpde_line *L, double *u, int on_device)
+{
+    clear_error();
+    FPDE_CHECK_ARG(L && u, "null argument");
+    int rc = ctx_enter(L->ctx);
+    if (rc) return rc;
+    FPDE_CUDA(cudaMemcpyAsync(u, L->U, (L->N + 1) * sizeof(double),
+                              on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, L->ctx->stream));
+    FPDE_CUDA(cudaStreamSynchronize(L->ctx->stream));
+    return ctx_check_flags(L->ctx, "line");
+}
+
+int fpde_line_state_ptr(fpde_line *L, double **u_dev)
+{
+    FPDE_CHECK_ARG(L && u_dev, "null argument");
+    *u_dev = L->U;
+    return FPDE_OK;
+}
+
+int fpde_line_solve_host(fpde_line *L, const double *u0_host, int steps, double *u_out_host)
+{
+    clear_error();
+    FPDE_CHECK_ARG(L && u0_host && u_out_host, "null argument");
+    int rc = ctx_enter(L->ctx);
+    if (rc) return rc;
+    cudaStream_t st = L->ctx->stream;
+    FPDE_CUDA(cudaMemcpyAsync(L->U, u0_host, (L->N + 1) * sizeof(double), cudaMemcpyHostToDevice, st));
+    L->n_done = 0;
+    if ((rc = fpde_line_run(L, steps))) return rc;
+    FPDE_CUDA(cudaMemcpyAsync(u_out_host, L->U, (L->N + 1) * sizeof(double), cudaMemcpyDeviceToHost, st));
+    FPDE_CUDA(cudaStreamSynchronize(st));
+    return ctx_check_flags(L->ctx, "line");
+}
+
+int fpde_line_set_probe(fpde_line *L, int every)
+{
+    clear_error();
+    FPDE_CHECK_ARG(L && every >= 0, "bad arguments");
+    int rc = ctx_enter(L->ctx);
+    if (rc) return rc;
+    FPDE_CUDA(cudaStreamSynchronize(L->ctx->stream));
+    for (auto &kv : L->graphs) cudaGraphExecDestroy(kv.second);
+    L->graphs.clear();
+    L->graph_launches.clear();
+    L->graph_probe_steps.clear();
+    L->last_probe_steps.clear();
+    for (cudaEvent_t e : L->probe_ev) cudaEventDestroy(e);
+    L->probe_ev.clear();
+    L->probe_every = every;
+    if (every > 0) {
+        int64_t n = L->max_steps / every + 1;
+        if (n > 4096) n = 4096;
+        L->probe_ev.resize(3 * n);
+        for (auto &e : L->probe_ev) FPDE_CUDA(cudaEventCreate(&e));
+    }
+    return FPDE_OK;
+}
+
+int fpde_line_probe_stats(fpde_line *L, double *hist_ms, double *hist_bytes, double *solve_ms, int *probes)
+{
+    clear_error();
+    FPDE_CHECK_ARG(L && hist_ms && hist_bytes && solve_ms && probes, "null argument");
+    int rc = ctx_enter(L->ctx);
+    if (rc) return rc;
+    FPDE_CUDA(cudaStreamSynchronize(L->ctx->stream));
+    double hm = 0, hb = 0, sm = 0;
+    for (size_t q = 0; q < L->last_probe_steps.size(); ++q) {
+        float a = 0, b = 0;
+        FPDE_CUDA(cudaEventElapsedTime(&a, L->probe_ev[3 * q], L->probe_ev[3 * q + 1]));
+        FPDE_CUDA(cudaEventElapsedTime(&b, L->probe_ev[3 * q + 1], L->probe_ev[3 * q + 2]));
+        hm += a;
+        sm += b;
+        hb += 8.0 * (double)L->last_probe_steps[q] * (double)(L->N + 1);
+    }
+    *hist_ms = hm;
+    *hist_bytes = hb;
+    *solve_ms = sm;
+    *probes = (int)L->last_probe_steps.size();
+    return FPDE_OK;
+}
+
+int fpde_line_steps_done(const fpde_line *L, int64_t *n)
+{
+    FPDE_CHECK_ARG(L && n, "null argument");
+    *n = L->n_done;
+    return FPDE_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,94 @@
+"""Seeded synthetic inputs of the benchmark configurations (host side, numpy).
+
+The reference ships no data; its problems are hard-coded analytic tests. These generators
+give the line problems of the benchmark their coefficient fields and initial states:
+  - lognormal conductivity: white noise N(0,1) on the grid, convolved with a Gaussian of
+    correlation length ell (periodic FFT convolution), rescaled to unit variance,
+    k = exp(mu + sigma g);
+  - initial head: a sum of 8 Gaussians with centres U[0.1,0.9], widths U[0.01,0.1] and
+    amplitudes U[0.5,1.0], times a taper that is zero at both ends (Dirichlet 0).
+"""
+import math
+from dataclasses import dataclass
+
+import numpy as np
+
+
+def lognormal_field(n_nodes, mu, sigma, ell, seed, h):
+    rng = np.random.default_rng(seed)
+    w = rng.standard_normal(n_nodes)
+    freqs = np.fft.rfftfreq(n_nodes, d=h)
+    kern = np.exp(-0.5 * (2 * np.pi * freqs * ell) ** 2)       # Gaussian filter, length ell
+    g = np.fft.irfft(np.fft.rfft(w) * kern, n=n_nodes)
+    g = (g - g.mean()) / g.std()
+    return np.exp(mu + sigma * g)
+
+
+def gaussian_mixture(x, seed, n=8):
+    rng = np.random.default_rng(seed)
+    c = rng.uniform(0.1, 0.9, n)
+    w = rng.uniform(0.01, 0.1, n)
+    a = rng.uniform(0.5, 1.0, n)
+    u = np.zeros_like(x)
+    for ci, wi, ai in zip(c, w, a):
+        u += ai * np.exp(-0.5 * ((x - ci) / wi) ** 2)
+    return u * np.sin(np.pi * x)          # zero at x = 0 and x = 1
+
+
+@dataclass
+class LineProblem:
+    name: str
+    N: int            # intervals (nodes 0..N)
+    alpha: float
+    tau: float
+    steps: int
+    k: np.ndarray     # N+1 node conductivities
+    u0: np.ndarray    # N+1 initial values
+    left: tuple = (0, 0.0)
+    right: tuple = (0, 0.0)
+
+    @property
+    def x(self):
+        return np.arange(self.N + 1) / self.N
+
+    @property
+    def dL(self):
+        return np.full(self.N + 1, 1.0 / self.N)
+
+    @property
+    def Da(self):
+        return 1.0 / math.gamma(1.0 - self.alpha)
+
+    def coefs(self):
+        """A, B, Rlap of fpde_hpc_1d.cpp A_/B/R with gamma = 1, iw = 1 (numpy restatement of
+        fpde_line_coefs; the library function gives identical values)."""
+        N, k, dL = self.N, self.k, self.dL
+        A, B, R = np.zeros(N + 1), np.zeros(N + 1), np.zeros(N + 1)
+        i = np.arange(1, N)
+        A[i] = k[i - 1] * 1.0 / (dL[i] * dL[i - 1])
+        B[i] = k[i] * 1.0 / (dL[i] * dL[i])
+        R[i] = 1.0 * ((k[i] / (dL[i] * dL[i])) + (k[i - 1] / (dL[i] * dL[i - 1])))
+        return A, B, R
+
+    @property
+    def node_steps(self):
+        return (self.N - 1) * self.steps
+
+
+def config1(steps=1000):
+    """1D, N=1000, alpha 0.8, tau 1e-3, k = 1 + 0.5 sin(2 pi x), H0 = exp(-50 (x-0.5)^2), Dirichlet 0."""
+    N = 1000
+    x = np.arange(N + 1) / N
+    u0 = np.exp(-50.0 * (x - 0.5) ** 2)
+    u0[0] = u0[-1] = 0.0
+    return LineProblem("config1_N1000", N, 0.8, 1e-3, steps, 1.0 + 0.5 * np.sin(2 * np.pi * x), u0)
+
+
+def config2(N=65536, steps=8192, tau=1e-4):
+    """1D, N=65536, 8192 steps, alpha 0.7, lognormal k (mu 0, sigma 0.5, ell 0.01, seed 1),
+    8-Gaussian H0 (seed 2), Dirichlet 0; tau = 1e-4 (T = 0.8192)."""
+    x = np.arange(N + 1) / N
+    k = lognormal_field(N + 1, 0.0, 0.5, 0.01, 1, 1.0 / N)
+    u0 = gaussian_mixture(x, 2)
+    u0[0] = u0[-1] = 0.0
+    return LineProblem(f"config2_N{N}", N, 0.7, tau, steps, k, u0)

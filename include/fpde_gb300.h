@@ -1,0 +1,206 @@
+/* fpde_gb300.h -- C ABI of the GB300 (sm_103a) implementation of FPDE_HPC's hot path:
+ * the Caputo / distributed-order L1 history sum and the per-step implicit tridiagonal
+ * (Thomas / LOD) line solves.
+ *
+ * This header replaces the reference's OpenCL/CUDA backend seam (the OpenCL_* classes of
+ * opencl_cuda_class.h:4-67 and the run-time-compiled kernels driven through them by
+ * fpde_hpc_1d.cpp and fr_do.cpp). Every entry point names the reference interface it
+ * stands in for. Conventions:
+ *   - every function returns FPDE_OK (0) or an FPDE_ERR_* code; nothing exits the
+ *     process (the reference calls exit(0) on any backend error, opencl_cuda_base.cpp:14-17);
+ *     fpde_last_error_string() describes the last failure of the calling thread;
+ *   - pointers are plain C pointers; an `on_device` flag says whether a buffer is in device
+ *     memory (of the context's GPU) or in host memory. Host buffers are copied in/out by the
+ *     call; device buffers are used in place;
+ *   - a context owns every device allocation made through it; one context per host thread;
+ *   - lines have N intervals and nodes 0..N; unknowns are 1..N-1 and nodes 0 and N carry
+ *     the boundary conditions (fpde_hpc_1d.cpp:2381-2388);
+ *   - the tridiagonal systems use the reference's sign convention
+ *         A[i] U[i-1] - R[i] U[i] + B[i] U[i+1] = Om[i]        (fpde_hpc_1d.cpp:3094)
+ */
+#ifndef FPDE_GB300_H
+#define FPDE_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FPDE_ABI_VERSION 1
+
+enum fpde_status {
+    FPDE_OK = 0,
+    FPDE_ERR_ARG = 1,          /* invalid argument (null pointer, size, mode) */
+    FPDE_ERR_CUDA = 2,         /* a CUDA runtime call failed */
+    FPDE_ERR_NOMEM = 3,        /* device or host allocation failed */
+    FPDE_ERR_CAPACITY = 4,     /* history full / size above a fixed maximum */
+    FPDE_ERR_TIMEOUT = 5,      /* a bounded device-side wait gave up (error flag set) */
+    FPDE_ERR_UNSUPPORTED = 6,  /* feature not available on this device / build */
+    FPDE_ERR_NUMERIC = 7       /* non-finite value detected where one is not allowed */
+};
+
+/* History storage / arithmetic of the L1 sum. */
+enum fpde_precision {
+    FPDE_PREC_FP64 = 0,        /* FP64 increments, FP64 FMA sum (the plain method) */
+    FPDE_PREC_SPLIT_BF16 = 1,  /* far history as bf16 hi+lo on tensor cores, FP64 fold */
+    FPDE_PREC_SPLIT_F16 = 2    /* same with fp16 hi+lo (per-node power-of-two scaling) */
+};
+
+/* Boundary condition kinds of a line end (al1 :4002-4027, bt1 :4585, U1 :4683-4719). */
+enum fpde_bc_kind {
+    FPDE_BC_DIRICHLET = 0,     /* U = value */
+    FPDE_BC_FLUX = 1           /* left: Al[1] = 1, Bt[1] = value; right: flux closure */
+};
+
+typedef struct fpde_ctx fpde_ctx;
+typedef struct fpde_hist fpde_hist;
+typedef struct fpde_line fpde_line;
+
+/* ---------------------------------------------------------------- context */
+
+/* Create a context on CUDA device `device` with its own stream.
+ * Replaces OpenCL_program(int gpu) + create_queue (opencl_cuda_class.h:57-60;
+ * CUDA impl opencl_cuda_base.cpp:759-785), which always used device 0. */
+int fpde_ctx_create(int device, fpde_ctx **out);
+/* Destroy a context and everything allocated through it (~OpenCL_program,
+ * opencl_cuda_base.cpp:786-801). */
+int fpde_ctx_destroy(fpde_ctx *ctx);
+/* Use a caller-provided cudaStream_t (passed as void*) for all work of this context;
+ * NULL restores the context's own stream. No counterpart: the reference is synchronous. */
+int fpde_ctx_set_stream(fpde_ctx *ctx, void *cuda_stream);
+/* Wait for all work of the context (OpenCL_commandqueue::Finish, opencl_cuda_class.h:45). */
+int fpde_ctx_synchronize(fpde_ctx *ctx);
+/* Number of streaming multiprocessors of the context's device. */
+int fpde_ctx_sm_count(const fpde_ctx *ctx, int *out);
+/* Description of the last error on this host thread ("" if none). Replaces the
+ * reference's printf-and-exit error reporting (SERROR, opencl_cuda_base.cpp:14-17). */
+const char *fpde_last_error_string(void);
+/* Number of kernels this library has launched on the calling host thread (a counter for
+ * benchmarks). */
+int64_t fpde_kernel_launch_count(void);
+
+/* ------------------------------------------------------------ L1 weights */
+
+/* FP64 closed-form L1 weights of step n from the time points time[0..n+1]:
+ *   kb[t] = int_{time[t]}^{time[t+1]} (time[n+1]-s)^{-alpha} ds,  t = 0..n-1,
+ *   kkk0  = int_{time[n]}^{time[n+1]} (time[n+1]-s)^{-alpha} ds
+ * evaluated cancellation-free. Replaces kb() / precalc_kb_3() / init_time_step()
+ * (fpde_hpc_1d.cpp:2167-2301, :4069-4085, :3942-3949), which approximate the same
+ * integrals by truncated series. Host function; kb may be NULL when n == 0. */
+int fpde_weights_l1(double alpha, const double *time, int n, double *kb, double *kkk0);
+
+/* Lag form for uniform steps: b[j] = (j+1)^{1-alpha} - j^{1-alpha}, j = 0..n-1,
+ * cancellation-free (so kb[t] of step n = tau^{1-alpha}/(1-alpha) * b[n-t]). Host. */
+int fpde_weights_l1_lags(double alpha, int n, double *b);
+
+/* Gamma function (FP64, host). Used for Da = 1/Gamma(1-alpha) (fpde_hpc_1d.cpp:3598-3605)
+ * and the distributed-order normalisers Gamma(2-alpha) (fr_do.cpp:337-341). */
+int fpde_gamma(double x, double *out);
+
+/* ---------------------------------------------------------- L1 history sum */
+
+/* Create a history of `nodes` values per snapshot with room for `max_steps` increments.
+ * Replaces the reference's snapshot buffer boldU and its doubling resize
+ * (init_opencl / fr_ocl_check_and_resize, fpde_hpc_1d.cpp:1715-1818): increments are
+ * stored instead of snapshots and capacity is fixed up front. precision: fpde_precision
+ * (FPDE_PREC_FP64 for this interface). */
+int fpde_history_create(fpde_ctx *ctx, int64_t nodes, int64_t max_steps, int precision,
+                        fpde_hist **out);
+int fpde_history_destroy(fpde_hist *h);
+/* Forget all snapshots (length 0). */
+int fpde_history_reset(fpde_hist *h);
+/* Number of stored increments. */
+int fpde_history_length(const fpde_hist *h, int64_t *n);
+/* Push a snapshot (the reference's oldH.push_back, calc_step :5104-5132 / :5729-5745).
+ * The first push stores the base state; each later push stores the increment
+ * u - previous snapshot. u has `nodes` values. */
+int fpde_history_append(fpde_hist *h, const double *u, int on_device);
+/* One step's history sum (time_summing :4086-4164 / the GPU Sum kernel :1407-1478, sum_alg 0):
+ *   S[i] = scale * sum_{t<n} (kb[t] * D_t[i]) / tau[t]
+ * over the n stored increments. kb and tau are host arrays of n values (tau may be NULL,
+ * meaning all 1); S has `nodes` values (host or device per out_on_device). */
+int fpde_l1_sum(fpde_hist *h, const double *kb, const double *tau, double scale,
+                double *S, int out_on_device);
+
+/* The reference's Sum kernel contract taken literally (fpde_hpc_1d.cpp:1407, sum_alg 0,
+ * args :1851-1868): S[id] = sum_{t=0}^{old_size-2} kb_3_cache[t]*(old[(t+1)*OS+id]-old[t*OS+id])/tau[t]
+ * for id < nodes, from time-major snapshots. All pointers per on_device. */
+int fpde_sum_snapshots(fpde_ctx *ctx, double *S, const double *old, int old_size, int64_t OS,
+                       int64_t nodes, const double *tau, const double *kb_3_cache, int on_device);
+
+/* ----------------------------------------------------- tridiagonal solves */
+
+/* Batched Thomas solves of n_lines independent lines (al1 / bt1 / back-substitution,
+ * fpde_hpc_1d.cpp:4002-4027, :4585-4590, :4678-4725), FP64. Line l, node i (0..N) lives at
+ * element offset l*stride_line + i*stride_elem of every array (a, b, r, om, u). a, b, r, om
+ * are read at i = 1..N-1. Boundary kinds/values per line end; left/right values are arrays
+ * of n_lines (NULL = 0). dLN is the last step (flux closure only). u is read (old U[N-1] for
+ * the degenerate flux case) and written at nodes 0..N. */
+int fpde_tridiag_solve(fpde_ctx *ctx, const double *a, const double *b, const double *r,
+                       const double *om, double *u, int64_t n_lines, int64_t N,
+                       int64_t stride_elem, int64_t stride_line,
+                       int left_kind, const double *left_val, int right_kind,
+                       const double *right_val, double dLN, int on_device);
+
+/* ------------------------------------------------------- 1D line problem */
+
+/* A time-fractional diffusion line  D_t^alpha U = d/dx(k dU/dx) (+ source)  discretised as in
+ * fpde_hpc_1d.cpp (L1 Caputo in time, implicit 3-point FD in space, Thomas per step):
+ *   Om[i] = -Da*(kkk0/tau) U[i] + src[i] + Da*S[i],  R[i] = Rlap[i] + Da*kkk0/tau.
+ * The time step tau is uniform; weights are the closed form. */
+typedef struct fpde_line_desc {
+    int64_t N;            /* intervals; nodes 0..N */
+    double alpha;         /* time order, 0 < alpha < 1 */
+    double tau;           /* time step */
+    double Da;            /* 1/Gamma(1-alpha) (caller's value; fpde_gamma gives one) */
+    int left_kind;        /* fpde_bc_kind */
+    double left_value;
+    int right_kind;
+    double right_value;
+    double dLN;           /* last space step (flux closure) */
+    int precision;        /* fpde_precision */
+    int block;            /* split paths: steps per far-history block (0 = auto) */
+    int max_steps;        /* history capacity */
+} fpde_line_desc;
+
+/* Set up a line: A, B, Rlap (N+1 host values, entries 1..N-1 used; see fpde_line_coefs)
+ * and the initial state u0 (N+1 host values). Replaces constructing H_solver + init_opencl
+ * for one column (fpde_hpc_1d.cpp:3457-3606, :1715). */
+int fpde_line_create(fpde_ctx *ctx, const fpde_line_desc *desc, const double *A, const double *B,
+                     const double *Rlap, const double *u0, fpde_line **out);
+int fpde_line_destroy(fpde_line *line);
+/* Reset to the state u0 (N+1 values, host or device) and an empty history. */
+int fpde_line_reset(fpde_line *line, const double *u0, int on_device);
+/* Advance `steps` time steps (calc_step / U1 per step, fpde_hpc_1d.cpp:5100-5135, with the
+ * history applied every step). The whole loop is one CUDA graph. */
+int fpde_line_run(fpde_line *line, int steps);
+/* Copy the state (N+1 values) out. */
+int fpde_line_get_state(fpde_line *line, double *u, int on_device);
+/* Device pointer of the state (N+1 doubles, valid until the line is destroyed). */
+int fpde_line_state_ptr(fpde_line *line, double **u_dev);
+/* End-to-end call: upload u0 from host, run `steps`, download the final state to host. */
+int fpde_line_solve_host(fpde_line *line, const double *u0_host, int steps, double *u_out_host);
+/* Current step count. */
+int fpde_line_steps_done(const fpde_line *line, int64_t *n);
+/* Kernel timing probes (no counterpart in the reference, which times whole calls with
+ * clock_gettime, opencl_cuda_base.cpp:708-716): with every > 0, later runs record CUDA
+ * events around the history-sum and solve kernels of every `every`-th step, inside the
+ * captured graph. fpde_line_probe_stats returns, for the last run, the summed event times
+ * (ms) of the probed history-sum launches and of the probed solve launches, the summed
+ * algorithmic bytes of the probed history-sum launches (8 * rows * (N+1) FP64 reads) and
+ * the number of probed steps. */
+int fpde_line_set_probe(fpde_line *line, int every);
+int fpde_line_probe_stats(fpde_line *line, double *hist_ms, double *hist_bytes, double *solve_ms,
+                          int *probes);
+
+/* Line coefficients of the H equation with gamma = 1 (A_ / B / R, fpde_hpc_1d.cpp:3095-3142):
+ * A[i] = k[i-1] iw[i]/(dL[i] dL[i-1]), B[i] = k[i] iw[i]/dL[i]^2,
+ * Rlap[i] = iw[i] (k[i]/dL[i]^2 + k[i-1]/(dL[i] dL[i-1])), i = 1..N-1. Host. iw may be NULL (1). */
+int fpde_line_coefs(int64_t N, const double *k, const double *iw, const double *dL,
+                    double *A, double *B, double *Rlap);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
