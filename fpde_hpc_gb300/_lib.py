@@ -43,6 +43,7 @@ _SIGS = {
     "fpde_history_length": (c_int, [c_vp, C.POINTER(c_i64)]),
     "fpde_history_append": (c_int, [c_vp, c_vp, c_int]),
     "fpde_l1_sum": (c_int, [c_vp, c_vp, c_vp, c_dbl, c_vp, c_int]),
+    "fpde_l1_sum_noalloc": (c_int, [c_vp, c_int, c_i64, c_i64, c_vp, c_vp, c_vp]),
     "fpde_sum_snapshots": (c_int, [c_vp, c_vp, c_vp, c_int, c_i64, c_i64, c_vp, c_vp, c_int]),
     "fpde_tridiag_solve": (c_int, [c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_i64, c_i64, c_i64, c_i64,
                                    c_int, c_vp, c_int, c_vp, c_dbl, c_int]),

@@ -129,6 +129,21 @@ int fpde_l1_sum(fpde_hist *h, const double *kb, const double *tau, double scale,
 int fpde_sum_snapshots(fpde_ctx *ctx, double *S, const double *old, int old_size, int64_t OS,
                        int64_t nodes, const double *tau, const double *kb_3_cache, int on_device);
 
+/* The history sum of fpde_l1_sum from caller-owned device buffers, allocating nothing.
+ * No counterpart in the reference. For callers that cannot call cudaMalloc while they run
+ * (a host framework that owns all device memory, a fixed device-memory budget, a step loop
+ * that must avoid the device synchronisation of cudaMalloc/cudaFree):
+ *   S[i] = sum_{t<n} w[t] * D[t*P + i],  i < nodes
+ * with D (n rows, row pitch P even, 16-byte aligned), w (n) and S (nodes) in device memory
+ * of the current device, launched on `stream` (a cudaStream_t, NULL = default stream); the
+ * call does not synchronise. Its split-K partials live in a fixed 8 MiB array inside the
+ * library (2^20 doubles), so P may be at most 1,048,576; larger pitches return
+ * FPDE_ERR_CAPACITY. The first call on each device looks up that array's device address;
+ * make that first call before any stream capture. All calls share the array: calls whose
+ * work overlaps on the GPU race and must be serialised by the caller. */
+int fpde_l1_sum_noalloc(const double *D, int n, int64_t P, int64_t nodes, const double *w,
+                        double *S, void *stream);
+
 /* ----------------------------------------------------- tridiagonal solves */
 
 /* Batched Thomas solves of n_lines independent lines (al1 / bt1 / back-substitution,

@@ -1,0 +1,63 @@
+"""fpde_l1_sum_noalloc: the history sum for callers that cannot allocate device memory.
+
+Such callers (a host framework that owns every device allocation, a fixed device-memory
+budget, a time-step loop that must not trigger the device synchronisation of
+cudaMalloc/cudaFree) pass their own device buffers; the library keeps its split-K partials
+in a fixed array compiled into it. This file is named so that pytest collects it last.
+The check: through the C ABI, two calls in a row (different history lengths and weights,
+so the second call runs over the first call's leftover partials) must equal the allocating
+entry point fpde_l1_sum within the FP64 tolerance of the other parity tests (1e-12).
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+RTOL = 1e-12
+
+
+def relmax(a, b):
+    return float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
+
+
+def test_noalloc_sum_equals_allocating_entry_point_twice():
+    import torch
+    import fpde_hpc_gb300 as fp
+    lib = fp.load()
+    rng = np.random.default_rng(11)
+    nodes, steps = 70001, 300
+    snaps = np.cumsum(rng.standard_normal((steps + 1, nodes)) * 1e-2, axis=0) + 1.0
+    D = np.diff(snaps, axis=0)
+    P = (nodes + 511) // 512 * 512
+    Dpad = np.zeros((steps, P))
+    Dpad[:, :nodes] = D
+    Ddev = torch.from_numpy(Dpad).cuda()          # caller-owned device buffers
+    Sdev = torch.zeros(nodes, dtype=torch.float64, device="cuda")
+    torch.cuda.synchronize()
+    with fp.Context(0) as ctx:
+        for n, (seed, scale) in enumerate([(1, 0.37), (2, 1.9)]):
+            r = np.random.default_rng(seed)
+            nrows = steps if n == 0 else steps // 3 + 7
+            kb = r.random(nrows) + 0.1
+            tau = r.random(nrows) * 1e-3 + 1e-4
+            h2 = fp.History(ctx, nodes, nrows)
+            for s in snaps[:nrows + 1]:
+                h2.append(s)
+            Sref = h2.l1_sum(kb, tau, scale=scale)     # allocating entry point
+            h2.close()
+            w = torch.from_numpy(scale * (kb / tau)).cuda()
+            torch.cuda.synchronize()
+            rc = lib.fpde_l1_sum_noalloc(C.c_void_p(Ddev.data_ptr()), nrows, P, nodes,
+                                         C.c_void_p(w.data_ptr()), C.c_void_p(Sdev.data_ptr()), None)
+            fp.check(rc, "fpde_l1_sum_noalloc")
+            torch.cuda.synchronize()
+            assert relmax(Sdev.cpu().numpy(), Sref) <= RTOL, n
+
+
+def test_noalloc_rejects_pitch_beyond_scratch():
+    import fpde_hpc_gb300 as fp
+    lib = fp.load()
+    rc = lib.fpde_l1_sum_noalloc(None, 0, (1 << 20) + 2, 1 << 20, None, C.c_void_p(16), None)
+    assert rc == 4
+    assert b"scratch" in lib.fpde_last_error_string()
