@@ -37,7 +37,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--precision", default="auto", choices=["auto", "fp64", "bf16", "f16"])
+    ap.add_argument("--precision", default="auto", choices=["auto", "fp64", "bf16", "f16", "bf16x3"])
     ap.add_argument("--time-steps", type=int, default=8192)
     ap.add_argument("--nodes", type=int, default=65536)
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -161,6 +161,39 @@ def run_reference(args):
     print(json.dumps(out), flush=True)
 
 
+def _timed_runs(line, u0_dev, steps, reps, stream):
+    """reps full solves, each from reset; CUDA events on the library's stream."""
+    import torch
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    totals = {k: {"ms": 0.0, "bytes": 0.0, "flops": 0.0, "count": 0} for k in (0, 1, 2)}
+    e0.record(stream)
+    for _ in range(reps):
+        line.reset(u0_dev)
+        line.run(steps)
+        for k in totals:
+            ps = line.probe_stats(k)
+            for f in ps:
+                totals[k][f] += ps[f]
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / reps, totals
+
+
+def _roofline(totals, kind, peak_gbs, peak_kind, name, extra=None):
+    t = totals[kind]
+    if t["ms"] <= 0:
+        return None
+    gbs = t["bytes"] / (t["ms"] / 1e3) / 1e9
+    r = {"kernel": name, "bound": "hbm", "achieved": gbs, "peak": peak_gbs, "unit": "GB/s",
+         "frac": gbs / peak_gbs, "peak_source": peak_kind, "traffic": None, "probed_launches": t["count"],
+         "ms_per_launch": t["ms"] / t["count"]}
+    if t["flops"]:
+        r["achieved_tflops"] = t["flops"] / (t["ms"] / 1e3) / 1e12
+    if extra:
+        r.update(extra)
+    return r
+
+
 def run_ours(args):
     import torch
     rank, world, local = dist_info()
@@ -177,20 +210,17 @@ def run_ours(args):
     stream = torch.cuda.current_stream()
     ctx.set_stream(stream.cuda_stream)
     lib = ctx.lib
-
-    prec = {"auto": fp.FPDE_PREC_FP64, "fp64": fp.FPDE_PREC_FP64, "bf16": fp.FPDE_PREC_SPLIT_BF16,
-            "f16": fp.FPDE_PREC_SPLIT_F16}[args.precision]
-    line = fp.Line(ctx, prob.N, prob.alpha, prob.tau, prob.Da, A, B, R, prob.u0, prob.steps, precision=prec)
-    probe_every = max(1, prob.steps // 32)
-    line.set_probe(probe_every)
+    prec = {"auto": fp.FPDE_PREC_SPLIT_BF16X3, "fp64": fp.FPDE_PREC_FP64, "bf16": fp.FPDE_PREC_SPLIT_BF16,
+            "f16": fp.FPDE_PREC_SPLIT_F16, "bf16x3": fp.FPDE_PREC_SPLIT_BF16X3}[args.precision]
+    pname = {0: "fp64", 1: "split-bf16", 2: "split-fp16", 3: "split-bf16x3"}[prec]
     u0_dev = torch.from_numpy(prob.u0).cuda()
+    probe_every = max(1, prob.steps // 32)
 
-    def one_step():
+    line = fp.Line(ctx, prob.N, prob.alpha, prob.tau, prob.Da, A, B, R, prob.u0, prob.steps, precision=prec)
+    line.set_probe(probe_every)
+    for _ in range(args.warmup):
         line.reset(u0_dev)
         line.run(prob.steps)
-
-    for _ in range(args.warmup):
-        one_step()
     torch.cuda.synchronize()
 
     def barrier():
@@ -204,28 +234,19 @@ def run_ours(args):
     barrier()
     torch.cuda.synchronize()
     launches0 = lib.fpde_kernel_launch_count()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    probe = {"hist_ms": 0.0, "hist_bytes": 0.0, "solve_ms": 0.0, "probes": 0}
-    for _ in range(args.steps):
-        one_step()
-        ps = line.probe_stats()
-        for k in probe:
-            probe[k] += ps[k]
-    e1.record(stream)
-    torch.cuda.synchronize()
+    ms, totals = _timed_runs(line, u0_dev, prob.steps, args.steps, stream)
     barrier()
     launches = lib.fpde_kernel_launch_count() - launches0
     clk = clocks.stop()
-    ms = e0.elapsed_time(e1) / args.steps
     if world > 1:
         import torch.distributed as dist
         t = torch.tensor([ms], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms = float(t.item())
     value = prob.node_steps * world / (ms / 1e3)
+    u_main = line.state()
 
-    # end to end through the C ABI with host buffers
+    # end to end through the C ABI with host buffers (pinned)
     u0_h = torch.from_numpy(prob.u0.copy()).pin_memory()
     out_h = torch.empty(prob.N + 1, dtype=torch.float64).pin_memory()
     u0_np, out_np = u0_h.numpy(), out_h.numpy()
@@ -244,34 +265,59 @@ def run_ours(args):
     e2e = {"value": prob.node_steps * world / e2e_s, "unit": "node-steps/s",
            "h2d_bytes_per_step": 8 * (prob.N + 1), "d2h_bytes_per_step": 8 * (prob.N + 1),
            "ms_per_step": e2e_s * 1e3}
+    line.close()
 
     peak, peak_kind = measured_peaks()
-    achieved = probe["hist_bytes"] / (probe["hist_ms"] / 1e3) / 1e9 if probe["hist_ms"] > 0 else None
-    roofline = {"kernel": "k_l1_partial (FP64 history GEMV)", "bound": "hbm", "achieved": achieved,
-                "peak": peak, "unit": "GB/s", "frac": (achieved / peak) if achieved else None,
-                "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs, copy)" if peak_kind == "measured"
-                else "fallback 6.8 TB/s",
-                "traffic": None,
-                "fp64_fma_ceiling_gbs": 4800.0,
-                "probed_launches": probe["probes"], "solve_ms_per_probed_step": (
-                    probe["solve_ms"] / probe["probes"]) if probe["probes"] else None}
+    peak_src = "of measured (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else "of fallback 6.8 TB/s"
+    kernels = {}
+    if prec == 0:
+        kernels["hist_gemv"] = _roofline(totals, 0, peak, peak_src, "k_l1_partial (FP64 history GEMV)",
+                                         {"fp64_fma_ceiling_gbs": 4800.0})
+    else:
+        kernels["far_tc"] = _roofline(totals, 1, peak, peak_src, "k_far_tc (tcgen05 split contraction)")
+    solve = totals[2]
+    kernels["solve"] = {"kernel": "k_line_solve", "probed_launches": solve["count"],
+                        "ms_per_launch": solve["ms"] / solve["count"] if solve["count"] else None}
+    # dominant kernel by measured time share (probes sample 1/probe_every of the solves)
+    far_ms = totals[1]["ms"] + totals[0]["ms"] * probe_every
+    solve_ms_est = (solve["ms"] / max(solve["count"], 1)) * prob.steps * args.steps
+    main_kernel = kernels.get("far_tc") or kernels.get("hist_gemv")
+    roofline = dict(main_kernel) if main_kernel else {}
+    roofline["time_share_of_step"] = (totals[1]["ms"] if prec else totals[0]["ms"] * probe_every) / (ms * args.steps)
+    roofline["solve_time_share_of_step"] = solve_ms_est / (ms * args.steps)
 
     out = {"metric": METRIC, "value": value, "unit": "node-steps/s", "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-           "vs_baseline": None, "dtype": "f64" if prec == 0 else "bf16-split+f32+f64",
+           "vs_baseline": None, "dtype": "f64" if prec == 0 else f"{pname}(tensor)+f64",
            "data": "synthetic (seeded lognormal k, 8-Gaussian H0)",
            "config": {"workload": f"1D Caputo line N={prob.N}, {prob.steps} steps, alpha 0.7, tau 1e-4, "
                                   "lognormal k (sigma 0.5, ell 0.01), 8-Gaussian H0 (config 2)",
-                      "nodes": prob.N, "time_steps": prob.steps, "path": "fp64" if prec == 0 else "split",
-                      "l2": "inputs larger than L2 (history 4.3 GB rows streamed every step)",
+                      "nodes": prob.N, "time_steps": prob.steps, "path": pname, "block": 64,
+                      "l2": "inputs larger than L2 (history 2.1-4.3 GB streamed)",
                       "parallelism": f"replicas x{world}"},
-           "e2e": e2e, "gpu_launches": int(launches // max(args.steps, 1) * args.steps),
-           "roofline": roofline, "clocks": clk}
+           "e2e": e2e, "gpu_launches": int(launches), "roofline": roofline, "kernels": kernels, "clocks": clk}
+
+    if prec != 0 and not args.no_fp64_arm:
+        # the plain FP64 kernel on the same workload: speed-up and accuracy of the split path
+        l64 = fp.Line(ctx, prob.N, prob.alpha, prob.tau, prob.Da, A, B, R, prob.u0, prob.steps,
+                      precision=fp.FPDE_PREC_FP64)
+        l64.set_probe(probe_every)
+        l64.reset(u0_dev)
+        l64.run(prob.steps)
+        ms64, tot64 = _timed_runs(l64, u0_dev, prob.steps, 1, stream)
+        u64 = l64.state()
+        l64.close()
+        err = float(np.max(np.abs(u_main - u64)) / np.max(np.abs(u64)))
+        rms = float(np.sqrt(np.mean((u_main - u64) ** 2)) / np.sqrt(np.mean(u64 ** 2)))
+        out["fp64_kernel"] = {"value": prob.node_steps / (ms64 / 1e3), "ms_per_step": ms64,
+                              "roofline": _roofline(tot64, 0, peak, peak_src, "k_l1_partial (FP64 history GEMV)",
+                                                    {"fp64_fma_ceiling_gbs": 4800.0})}
+        out["split_vs_fp64"] = {"speedup": ms64 / ms, "max_rel_err": err, "rms_rel_err": rms,
+                                "bound": 1e-7}
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cb = cpu_port_rate(prob, os.cpu_count() or 1)
         out["cpu_baseline"] = {"value": cb["value"], "unit": "node-steps/s", "cores": os.cpu_count() or 1,
                                "kind": "port", "sample": cb["sample"]}
-    line.close()
     ctx.close()
     if rank == 0:
         print(json.dumps(out), flush=True)

@@ -11,5 +11,6 @@ from .api import Context, History, Line, weights_l1, weights_l1_lags, gamma, lin
 FPDE_PREC_FP64 = 0
 FPDE_PREC_SPLIT_BF16 = 1
 FPDE_PREC_SPLIT_F16 = 2
+FPDE_PREC_SPLIT_BF16X3 = 3
 FPDE_BC_DIRICHLET = 0
 FPDE_BC_FLUX = 1

@@ -44,6 +44,10 @@ _SIGS = {
     "fpde_history_append": (c_int, [c_vp, c_vp, c_int]),
     "fpde_l1_sum": (c_int, [c_vp, c_vp, c_vp, c_dbl, c_vp, c_int]),
     "fpde_l1_sum_noalloc": (c_int, [c_vp, c_int, c_i64, c_i64, c_vp, c_vp, c_vp]),
+    "fpde_far_contract": (c_int, [c_vp, c_vp, c_vp, c_i64, c_i64, c_vp, c_vp, c_i64, c_int, c_int, c_dbl,
+                                  c_vp, c_int]),
+    "fpde_far_contract3": (c_int, [c_vp, C.POINTER(c_vp), c_i64, c_i64, C.POINTER(c_vp), c_i64, c_int, c_vp, c_vp,
+                                   c_i64, c_vp, c_int]),
     "fpde_sum_snapshots": (c_int, [c_vp, c_vp, c_vp, c_int, c_i64, c_i64, c_vp, c_vp, c_int]),
     "fpde_tridiag_solve": (c_int, [c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_i64, c_i64, c_i64, c_i64,
                                    c_int, c_vp, c_int, c_vp, c_dbl, c_int]),
@@ -57,7 +61,7 @@ _SIGS = {
     "fpde_line_steps_done": (c_int, [c_vp, C.POINTER(c_i64)]),
     "fpde_line_coefs": (c_int, [c_i64, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]),
     "fpde_line_set_probe": (c_int, [c_vp, c_int]),
-    "fpde_line_probe_stats": (c_int, [c_vp, P_dbl, P_dbl, P_dbl, C.POINTER(c_int)]),
+    "fpde_line_probe_stats": (c_int, [c_vp, c_int, P_dbl, P_dbl, P_dbl, C.POINTER(c_int)]),
 }
 
 _lib = None

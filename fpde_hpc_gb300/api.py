@@ -192,11 +192,13 @@ class Line:
     def set_probe(self, every):
         check(self.ctx.lib.fpde_line_set_probe(self.h, every), "fpde_line_set_probe")
 
-    def probe_stats(self):
-        hm, hb, sm, n = C.c_double(), C.c_double(), C.c_double(), C.c_int()
-        check(self.ctx.lib.fpde_line_probe_stats(self.h, C.byref(hm), C.byref(hb), C.byref(sm), C.byref(n)),
+    PROBE_HIST, PROBE_FAR, PROBE_SOLVE = 0, 1, 2
+
+    def probe_stats(self, kind):
+        ms, b, f, n = C.c_double(), C.c_double(), C.c_double(), C.c_int()
+        check(self.ctx.lib.fpde_line_probe_stats(self.h, kind, C.byref(ms), C.byref(b), C.byref(f), C.byref(n)),
               "fpde_line_probe_stats")
-        return {"hist_ms": hm.value, "hist_bytes": hb.value, "solve_ms": sm.value, "probes": n.value}
+        return {"ms": ms.value, "bytes": b.value, "flops": f.value, "count": n.value}
 
     @property
     def steps_done(self):

@@ -16,3 +16,38 @@ int launch_l1_partial(cudaStream_t st, const double *D, int64_t P, int n, const 
 int choose_splits(int n, int64_t P);
 
 }  // namespace fpde
+
+namespace fpde {
+
+// Buffers of the split-precision path touched by the per-block preparation (split.cu).
+struct SplitPrep {
+    const double *ring = nullptr;        // [64][P] FP64 increments of the finished block
+    int64_t P = 0, nvalid = 0;           // row pitch of the ring, nodes with history
+    unsigned long long *slots = nullptr; // per block: max |increment| (double bits)
+    int *exps = nullptr;                 // per block: scale exponent sexp
+    uint16_t *hist_hi = nullptr, *hist_lo = nullptr;   // [rows][ld] node-major history
+    uint16_t *w_hi = nullptr, *w_lo = nullptr;         // [64][ld] weight tile
+    int64_t ld = 0;
+    const double *wlag = nullptr;        // w[lag], lag = 0 .. max_steps + 64
+    double *out_scale = nullptr;         // 2^-kexp for the contraction
+    int bf16 = 0;
+};
+// Convert the block ending at n0 (n0 % 64 == 0, n0 >= 64) and build the weights of the
+// next contraction (K = n0).
+int launch_block_prep(cudaStream_t st, const SplitPrep &p, int64_t n0);
+
+// Exact three-slice form: history slices and per-(node, block) exponents, weight slices and
+// per-(step, k-tile) exponents.
+struct SplitPrep3 {
+    const double *ring = nullptr;
+    int64_t P = 0, nvalid = 0;
+    uint16_t *hist[3] = {nullptr, nullptr, nullptr};
+    uint16_t *w[3] = {nullptr, nullptr, nullptr};
+    int64_t ld = 0;
+    int8_t *pA = nullptr, *pW = nullptr;
+    int64_t ldp = 0;
+    const double *wlag = nullptr;
+};
+int launch_block_prep3(cudaStream_t st, const SplitPrep3 &p, int64_t n0);
+
+}  // namespace fpde

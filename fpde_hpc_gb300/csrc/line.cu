@@ -1,9 +1,17 @@
-// 1D line problem (fpde_line_*): the plain FP64 path.
+// 1D line problem (fpde_line_*): the plain FP64 path and the split-precision path.
 //
 // Per time step n (fpde_hpc_1d.cpp calc_step / U1 with the history applied every step):
-//   1. k_l1_partial : part[ks][i] = sum_t w[n-t] D_t[i]        (HBM-bound FP64 GEMV)
-//   2. k_line_solve : S = sum_ks part, Om = -lam U + src + S, Thomas solve, U <- U^{n+1},
-//                     D_n = U^{n+1} - U^n                       (one cooperative launch)
+//   FP64 path
+//     1. k_l1_partial : part[ks][i] = sum_t w[n-t] D_t[i]        (FP64 history GEMV)
+//     2. k_line_solve : S = sum_ks part, Om = -lam U + src + S, Thomas solve, U <- U^{n+1},
+//                       D_n = U^{n+1} - U^n                       (one cooperative launch)
+//   split path (blocks of 64 steps starting at n0)
+//     at n0:  convert the finished block's FP64 increments into 16-bit hi/lo history,
+//             build the Toeplitz weight tile and run the tensor-core contraction for the
+//             far history t < n0 (tc_far.cu) -> FP64 partials C[split][j][i]
+//     each step j = n - n0:
+//             S = sum_split C[split][j][i] + sum_{n0 <= t < n} w[n-t] D_t[i]   (near: FP64)
+//             then the same solve; D_n goes to a 64-row FP64 ring.
 // The whole run is captured once into a CUDA graph and replayed.
 //
 // The Thomas solve of a long line runs on all SMs. The alpha recurrence
@@ -11,11 +19,12 @@
 // per step only the two first-order recurrences remain,
 //   forward   Bt[i+1] = g_i (A_i Bt[i] - Om_i),      g_i = Al[i+1]/B_i
 //   backward  U_i     = Al[i+1] U_{i+1} + Bt[i+1],
-// each an affine scan x_i = p_i x_{i-1} + r_i. Every thread runs its segment of <= 8 nodes
+// each an affine scan x_i = p_i x_{i-1} + r_i. Every thread runs its segment of SP nodes
 // sequentially from zero, segments are combined by warp-shuffle scans of (P, X) pairs, then
 // across warps through shared memory, then across CTAs through a bounded grid barrier;
 // finally each node adds (prefix product) x (carry), with the within-segment prefix products
-// of p and Al precomputed once (cf, cb).
+// of p and Al precomputed once (cf, cb). The history sums and the state are read in a
+// coalesced pattern first and handed to the segment layout through shared memory.
 #include <map>
 #include <vector>
 #include <cmath>
@@ -23,11 +32,13 @@
 
 #include "common.cuh"
 #include "kernels.cuh"
+#include "tc_far.cuh"
 
 namespace fpde {
 
 constexpr int LT = 128;      // threads per CTA of the line solve
 constexpr int LSEG = 8;      // max nodes per thread
+constexpr int BLK = 64;      // steps per block of the split path (= tensor-core N)
 constexpr unsigned FULL = 0xffffffffu;
 
 struct LineSolveArgs {
@@ -35,13 +46,16 @@ struct LineSolveArgs {
     const double *src;                    // optional source (N+1), may be null
     double *U;                            // state (N+1)
     double *Drow;                         // increment row of this step (P)
-    const double *part;                   // partial history sums [KS][P]
+    const double *part;                   // S += sum_{q<KS} part[q*pstride + i]
+    int64_t pstride;
+    const double *ring;                   // S += sum_{r<nr} wn[r] * ring[r*P + i]
+    const double *wn;
     double *aggf, *aggb;                  // [G][2] CTA aggregates
     double *UN;                           // right boundary value slot
     unsigned *barrier, *flags;
     int64_t P;
     double lam, g0, gN, dLN, AlN;
-    int KS, N, s, G, rkind;
+    int KS, nr, N, G, rkind;
 };
 
 __device__ __forceinline__ void warp_scan_up(double &P, double &X, int lane)
@@ -88,33 +102,77 @@ __device__ __forceinline__ double grid_carry(const double *agg, int G, int c, bo
     }
 }
 
+template <int SP>
 __global__ void __launch_bounds__(LT) k_line_solve(LineSolveArgs p)
 {
+    __shared__ double sh_om[LT * SP], sh_u[LT * SP];
     __shared__ double wP[LT / 32], wX[LT / 32], wPe[LT / 32], wXe[LT / 32];
     __shared__ double s_carry, s_UN;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int c = blockIdx.x;
-    const int i0 = (c * LT + tid) * p.s;
-    const int i1 = min(i0 + p.s, p.N);
-    const int cnt = max(0, i1 - i0);
+    const int base = c * LT * SP;
 
-    double uo[LSEG], y[LSEG];
-    // ---- forward: local sweep from zero
-    double yl = 0.0;
+    // ---- phase 0 (coalesced): history sum, right-hand side, state -> shared memory
+    {
+        double acc[SP], acc2[SP], uu[SP];
 #pragma unroll
-    for (int k = 0; k < LSEG; ++k) {
+        for (int k = 0; k < SP; ++k) { acc[k] = 0.0; acc2[k] = 0.0; uu[k] = 0.0; }
+#pragma unroll
+        for (int k = 0; k < SP; ++k) {
+            const int i = base + k * LT + tid;
+            if (i < p.N) uu[k] = p.U[i];
+        }
+        for (int q = 0; q < p.KS; ++q) {
+#pragma unroll
+            for (int k = 0; k < SP; ++k) {
+                const int i = base + k * LT + tid;
+                if (i < p.N) acc[k] += __ldcg(p.part + (int64_t)q * p.pstride + i);
+            }
+        }
+        int r = 0;
+        for (; r + 2 <= p.nr; r += 2) {
+            const double w0 = __ldg(p.wn + r), w1 = __ldg(p.wn + r + 1);
+#pragma unroll
+            for (int k = 0; k < SP; ++k) {
+                const int i = base + k * LT + tid;
+                if (i < p.N) {
+                    acc[k] = fma(w0, __ldcg(p.ring + (int64_t)r * p.P + i), acc[k]);
+                    acc2[k] = fma(w1, __ldcg(p.ring + (int64_t)(r + 1) * p.P + i), acc2[k]);
+                }
+            }
+        }
+        if (r < p.nr) {
+            const double w0 = __ldg(p.wn + r);
+#pragma unroll
+            for (int k = 0; k < SP; ++k) {
+                const int i = base + k * LT + tid;
+                if (i < p.N) acc[k] = fma(w0, __ldcg(p.ring + (int64_t)r * p.P + i), acc[k]);
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < SP; ++k) {
+            const int i = base + k * LT + tid;
+            const double S = acc[k] + acc2[k];
+            sh_u[k * LT + tid] = uu[k];
+            sh_om[k * LT + tid] = (-(p.lam * uu[k]) + (p.src && i < p.N ? p.src[i] : 0.0)) + S;
+        }
+    }
+    __syncthreads();
+
+    const int i0 = base + tid * SP;
+    const int i1 = min(i0 + SP, p.N);
+    const int cnt = max(0, i1 - i0);
+    double uo[SP], y[SP];
+    // ---- forward: local sweep from zero
+    double yl = 0.0, ulast = 0.0;
+#pragma unroll
+    for (int k = 0; k < SP; ++k) {
         if (k < cnt) {
             const int i = i0 + k;
-            const double u_old = p.U[i];
-            uo[k] = u_old;
-            if (i == 0) {
-                yl = p.g0;                                        // Bt[1]
-            } else {
-                double S = 0.0;
-                for (int q = 0; q < p.KS; ++q) S += p.part[(int64_t)q * p.P + i];
-                const double Om = (-(p.lam * u_old) + (p.src ? p.src[i] : 0.0)) + S;
-                yl = p.g[i] * (p.A[i] * yl - Om);
-            }
+            uo[k] = sh_u[tid * SP + k];
+            ulast = uo[k];
+            if (i == 0) yl = p.g0;                                 // Bt[1]
+            else yl = p.g[i] * (p.A[i] * yl - sh_om[tid * SP + k]);
             y[k] = yl;
         }
     }
@@ -146,12 +204,12 @@ __global__ void __launch_bounds__(LT) k_line_solve(LineSolveArgs p)
         const double carry_w = fma(wPe[warp], s_carry, wXe[warp]);
         const double carry = fma(Pe, carry_w, Xe);
 #pragma unroll
-        for (int k = 0; k < LSEG; ++k)
-            if (k < cnt) y[k] = fma(p.cf[i0 + k], carry, y[k]);
+        for (int k = 0; k < SP; ++k)
+            if (k < cnt) { y[k] = fma(p.cf[i0 + k], carry, y[k]); yl = y[k]; }
     }
     // ---- right boundary value (owner of node N-1)
     if (cnt > 0 && i1 == p.N) {
-        const double BtN = y[cnt - 1], uNm1 = uo[cnt - 1];
+        const double BtN = yl, uNm1 = ulast;
         double UN;
         if (p.rkind == FPDE_BC_DIRICHLET) {
             UN = p.gN;
@@ -167,10 +225,10 @@ __global__ void __launch_bounds__(LT) k_line_solve(LineSolveArgs p)
         p.Drow[p.N] = UN - uNold;
     }
     // ---- backward: local sweep from zero, descending
-    double ub[LSEG];
+    double ub[SP];
     double ul = 0.0;
 #pragma unroll
-    for (int k = LSEG - 1; k >= 0; --k) {
+    for (int k = SP - 1; k >= 0; --k) {
         if (k < cnt) {
             ul = fma(p.al[i0 + k], ul, y[k]);
             ub[k] = ul;
@@ -188,8 +246,7 @@ __global__ void __launch_bounds__(LT) k_line_solve(LineSolveArgs p)
     if (warp == 0) {
         constexpr int NW = LT / 32;
         double Pw = lane < NW ? wP[lane] : 1.0, Xw = lane < NW ? wX[lane] : 0.0;
-        // suffix scan over warps 0..NW-1 (later warps first)
-        warp_scan_down(Pw, Xw, lane);
+        warp_scan_down(Pw, Xw, lane);                   // suffix scan over warps
         double Pwe = __shfl_down_sync(FULL, Pw, 1), Xwe = __shfl_down_sync(FULL, Xw, 1);
         if (lane >= NW - 1) { Pwe = 1.0; Xwe = 0.0; }
         if (lane < NW) { wPe[lane] = Pwe; wXe[lane] = Xwe; }
@@ -211,7 +268,7 @@ __global__ void __launch_bounds__(LT) k_line_solve(LineSolveArgs p)
         const double carry_w = fma(wPe[warp], s_carry, wXe[warp]);
         const double carry = fma(Pe, carry_w, Xe);
 #pragma unroll
-        for (int k = 0; k < LSEG; ++k) {
+        for (int k = 0; k < SP; ++k) {
             if (k < cnt) {
                 const int i = i0 + k;
                 const double un = fma(p.cb[i], carry, ub[k]);
@@ -231,33 +288,55 @@ struct fpde_line {
     fpde_line_desc d{};
     int64_t N = 0, P = 0;
     int G = 1, s = 1, max_steps = 0;
+    bool split = false;
     double lam = 0, lamR = 0, kkk0 = 0, AlN = 0;
     double *A = nullptr, *g = nullptr, *al = nullptr, *cf = nullptr, *cb = nullptr;
     double *U = nullptr, *D = nullptr, *part = nullptr, *wrev = nullptr;
     double *aggf = nullptr, *aggb = nullptr, *UN = nullptr;
     unsigned *barrier = nullptr;
-    double *pinned = nullptr;
+    // split path
+    int64_t rows16 = 0, ld16 = 0;
+    uint16_t *h_hi = nullptr, *h_lo = nullptr, *w_hi = nullptr, *w_lo = nullptr;
+    double *ring = nullptr, *cfar = nullptr, *wlag = nullptr, *out_scale = nullptr;
+    unsigned long long *slots = nullptr;
+    int *exps = nullptr;
+    FarPlan plan;
+    // exact three-slice form
+    bool x3 = false;
+    uint16_t *h3[3] = {nullptr, nullptr, nullptr}, *w3[3] = {nullptr, nullptr, nullptr};
+    int8_t *pA = nullptr, *pW = nullptr;
+    int64_t ldp = 0;
+    FarPlan3 plan3;
     int64_t n_done = 0;
     std::map<std::pair<int64_t, int>, cudaGraphExec_t> graphs;
     std::map<std::pair<int64_t, int>, int64_t> graph_launches;
+    // probes: CUDA events around kernels inside the captured graph
+    struct Probe { int kind; int64_t n; double bytes, flops; int ev; };
     int probe_every = 0;
-    std::vector<cudaEvent_t> probe_ev;          // 3 per probed step
-    std::vector<int64_t> probe_steps;           // steps probed by the last enqueue
-    std::map<std::pair<int64_t, int>, std::vector<int64_t>> graph_probe_steps;
-    std::vector<int64_t> last_probe_steps;
+    std::vector<cudaEvent_t> probe_ev;
+    std::vector<Probe> probes;                            // recorded by the last enqueue
+    std::map<std::pair<int64_t, int>, std::vector<Probe>> graph_probes;
+    std::vector<Probe> last_probes;
 };
 
 namespace fpde {
 
-static int line_launch_solve(fpde_line *L, cudaStream_t st, int64_t n, int KS)
+template <int SP>
+static cudaError_t launch_solve_sp(const cudaLaunchConfig_t &cfg, const LineSolveArgs &a)
+{
+    return cudaLaunchKernelEx(&cfg, k_line_solve<SP>, a);
+}
+
+static int line_launch_solve(fpde_line *L, cudaStream_t st, const double *part, int KS, int64_t pstride,
+                             const double *ring, const double *wn, int nr, double *Drow)
 {
     LineSolveArgs a;
     a.A = L->A; a.g = L->g; a.al = L->al; a.cf = L->cf; a.cb = L->cb; a.src = nullptr;
-    a.U = L->U; a.Drow = L->D + n * L->P; a.part = L->part;
+    a.U = L->U; a.Drow = Drow; a.part = part; a.pstride = pstride; a.ring = ring; a.wn = wn;
     a.aggf = L->aggf; a.aggb = L->aggb; a.UN = L->UN;
     a.barrier = L->barrier; a.flags = L->ctx->d_flags;
     a.P = L->P; a.lam = L->lam; a.g0 = L->d.left_value; a.gN = L->d.right_value; a.dLN = L->d.dLN;
-    a.AlN = L->AlN; a.KS = KS; a.N = (int)L->N; a.s = L->s; a.G = L->G; a.rkind = L->d.right_kind;
+    a.AlN = L->AlN; a.KS = KS; a.nr = nr; a.N = (int)L->N; a.G = L->G; a.rkind = L->d.right_kind;
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(L->G);
     cfg.blockDim = dim3(LT);
@@ -267,37 +346,103 @@ static int line_launch_solve(fpde_line *L, cudaStream_t st, int64_t n, int KS)
     attr[0].val.cooperative = L->G > 1 ? 1 : 0;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    FPDE_CUDA(cudaLaunchKernelEx(&cfg, k_line_solve, a));
+    cudaError_t e;
+    switch (L->s) {
+    case 1: e = launch_solve_sp<1>(cfg, a); break;
+    case 2: e = launch_solve_sp<2>(cfg, a); break;
+    case 4: e = launch_solve_sp<4>(cfg, a); break;
+    default: e = launch_solve_sp<8>(cfg, a); break;
+    }
+    if (e != cudaSuccess) return set_error(FPDE_ERR_CUDA, "line solve launch: %s", cudaGetErrorString(e));
     count_launches(1);
     return FPDE_OK;
 }
+
+static cudaEvent_t *probe_begin(fpde_line *L, int kind, int64_t n, double bytes, double flops)
+{
+    const size_t k = L->probes.size();
+    if (2 * (k + 1) > L->probe_ev.size()) return nullptr;
+    L->probes.push_back({kind, n, bytes, flops, (int)(2 * k)});
+    return &L->probe_ev[2 * k];
+}
+
+#define PROBE_REC(ev, i) \
+    do { if (ev) FPDE_CUDA(cudaEventRecordWithFlags((ev)[i], st, cudaEventRecordExternal)); } while (0)
 
 // Enqueue steps [n0, n0+steps) on st; returns the number of kernels enqueued via *nk.
 static int line_enqueue(fpde_line *L, cudaStream_t st, int64_t n0, int steps, int64_t *nk)
 {
     int64_t k = 0;
-    L->probe_steps.clear();
+    int rc;
+    L->probes.clear();
+    const int64_t nodes_hist = L->N + 1;
     for (int64_t n = n0; n < n0 + steps; ++n) {
-        int KS = 0;
-        cudaEvent_t *ev = nullptr;
-        if (L->probe_every > 0 && n >= 1 && (n % L->probe_every) == L->probe_every - 1 &&
-            (L->probe_steps.size() + 1) * 3 <= L->probe_ev.size()) {
-            ev = &L->probe_ev[3 * L->probe_steps.size()];
-            L->probe_steps.push_back(n);
-        }
-        if (n >= 1) {
-            KS = choose_splits((int)n, L->P);
-            const double *wt = L->wrev + (L->max_steps - n);   // wt[t] = w[n - t]
-            if (ev) FPDE_CUDA(cudaEventRecordWithFlags(ev[0], st, cudaEventRecordExternal));
-            int rc = launch_l1_partial(st, L->D, L->P, (int)n, wt, L->part, KS);
-            if (rc) return rc;
-            if (ev) FPDE_CUDA(cudaEventRecordWithFlags(ev[1], st, cudaEventRecordExternal));
+        const bool probe_step = L->probe_every > 0 && n >= 1 && (n % L->probe_every) == L->probe_every - 1;
+        cudaEvent_t *ev;
+        if (!L->split) {
+            int KS = 0;
+            if (n >= 1) {
+                KS = choose_splits((int)n, L->P);
+                const double *wt = L->wrev + (L->max_steps - n);   // wt[t] = w[n - t]
+                ev = probe_step ? probe_begin(L, 0, n, 8.0 * (double)n * nodes_hist, 2.0 * n * nodes_hist) : nullptr;
+                PROBE_REC(ev, 0);
+                if ((rc = launch_l1_partial(st, L->D, L->P, (int)n, wt, L->part, KS))) return rc;
+                PROBE_REC(ev, 1);
+                ++k;
+            }
+            ev = probe_step ? probe_begin(L, 2, n, 0.0, 0.0) : nullptr;
+            PROBE_REC(ev, 0);
+            if ((rc = line_launch_solve(L, st, L->part, KS, L->P, nullptr, nullptr, 0, L->D + n * L->P))) return rc;
+            PROBE_REC(ev, 1);
+            ++k;
+        } else {
+            const int64_t nb0 = n - n % BLK;                     // block start
+            const int j = (int)(n - nb0);
+            int splits = 0;
+            if (nb0 > 0) splits = far_splits((int)(nb0 / 64), L->rows16);
+            if (j == 0 && nb0 > 0 && L->x3) {
+                SplitPrep3 sp;
+                sp.ring = L->ring; sp.P = L->P; sp.nvalid = nodes_hist; sp.ld = L->ld16; sp.wlag = L->wlag;
+                for (int q = 0; q < 3; ++q) { sp.hist[q] = L->h3[q]; sp.w[q] = L->w3[q]; }
+                sp.pA = L->pA; sp.pW = L->pW; sp.ldp = L->ldp;
+                if ((rc = launch_block_prep3(st, sp, nb0))) return rc;
+                k += 2;
+                ev = L->probe_every > 0 ? probe_begin(L, 1, nb0, 6.0 * (double)nb0 * nodes_hist,
+                                                      6.0 * 2.0 * (double)nodes_hist * nb0 * BLK)
+                                        : nullptr;
+                PROBE_REC(ev, 0);
+                if ((rc = far3_launch(st, &L->plan3, (int)nb0, L->cfar, (int64_t)BLK * L->P, L->P, splits, L->pA,
+                                      L->pW, L->ldp, L->ctx->d_flags)))
+                    return rc;
+                PROBE_REC(ev, 1);
+                ++k;
+            } else if (j == 0 && nb0 > 0) {
+                SplitPrep sp;
+                sp.ring = L->ring; sp.P = L->P; sp.nvalid = nodes_hist; sp.slots = L->slots; sp.exps = L->exps;
+                sp.hist_hi = L->h_hi; sp.hist_lo = L->h_lo; sp.w_hi = L->w_hi; sp.w_lo = L->w_lo; sp.ld = L->ld16;
+                sp.wlag = L->wlag; sp.out_scale = L->out_scale;
+                sp.bf16 = L->d.precision == FPDE_PREC_SPLIT_BF16 ? 1 : 0;
+                if ((rc = launch_block_prep(st, sp, nb0))) return rc;
+                k += sp.bf16 ? 2 : 3;
+                ev = L->probe_every > 0 ? probe_begin(L, 1, nb0, 4.0 * (double)nb0 * nodes_hist,
+                                                      3.0 * 2.0 * (double)nodes_hist * nb0 * BLK)
+                                        : nullptr;
+                PROBE_REC(ev, 0);
+                if ((rc = far_launch(st, &L->plan, (int)nb0, L->cfar, (int64_t)BLK * L->P, L->P, splits, 1.0,
+                                     L->out_scale, L->ctx->d_flags)))
+                    return rc;
+                PROBE_REC(ev, 1);
+                ++k;
+            }
+            const double *wn = L->wrev + (L->max_steps - j);       // wn[r] = w[j - r]
+            ev = probe_step ? probe_begin(L, 2, n, 0.0, 0.0) : nullptr;
+            PROBE_REC(ev, 0);
+            if ((rc = line_launch_solve(L, st, L->cfar + (int64_t)j * L->P, splits, (int64_t)BLK * L->P, L->ring, wn,
+                                        j, L->ring + (int64_t)j * L->P)))
+                return rc;
+            PROBE_REC(ev, 1);
             ++k;
         }
-        int rc = line_launch_solve(L, st, n, KS);
-        if (rc) return rc;
-        if (ev) FPDE_CUDA(cudaEventRecordWithFlags(ev[2], st, cudaEventRecordExternal));
-        ++k;
     }
     if (nk) *nk = k;
     return FPDE_OK;
@@ -330,10 +475,17 @@ int fpde_line_destroy(fpde_line *L)
     }
     for (auto &kv : L->graphs) cudaGraphExecDestroy(kv.second);
     for (cudaEvent_t e : L->probe_ev) cudaEventDestroy(e);
-    for (double *p : {L->A, L->g, L->al, L->cf, L->cb, L->U, L->D, L->part, L->wrev, L->aggf, L->aggb, L->UN})
+    for (double *p : {L->A, L->g, L->al, L->cf, L->cb, L->U, L->D, L->part, L->wrev, L->aggf, L->aggb, L->UN,
+                      L->ring, L->cfar, L->wlag, L->out_scale})
         dev_free(p);
+    for (uint16_t *p : {L->h_hi, L->h_lo, L->w_hi, L->w_lo, L->h3[0], L->h3[1], L->h3[2], L->w3[0], L->w3[1],
+                        L->w3[2]})
+        dev_free(p);
+    dev_free(L->pA);
+    dev_free(L->pW);
+    dev_free(L->slots);
+    dev_free(L->exps);
     dev_free(L->barrier);
-    if (L->pinned) cudaFreeHost(L->pinned);
     delete L;
     return FPDE_OK;
 }
@@ -354,9 +506,12 @@ int fpde_line_create(fpde_ctx *ctx, const fpde_line_desc *desc, const double *A,
     FPDE_CHECK_ARG(d.left_kind == 0 || d.left_kind == 1, "bad left boundary kind");
     FPDE_CHECK_ARG(d.right_kind == 0 || d.right_kind == 1, "bad right boundary kind");
     FPDE_CHECK_ARG(d.precision == FPDE_PREC_FP64 || d.precision == FPDE_PREC_SPLIT_BF16 ||
-                   d.precision == FPDE_PREC_SPLIT_F16, "bad precision mode");
+                   d.precision == FPDE_PREC_SPLIT_F16 || d.precision == FPDE_PREC_SPLIT_BF16X3,
+                   "bad precision mode");
+    FPDE_CHECK_ARG(d.precision == FPDE_PREC_FP64 || d.block == 0 || d.block == BLK,
+                   "split path: block must be 0 (auto) or 64");
     const int64_t N = d.N;
-    // partition of nodes 0..N-1 over G CTAs x LT threads x s nodes
+    // partition of nodes 0..N-1 over G CTAs x LT threads x s nodes (s a power of two)
     int G = (int)((N + (int64_t)LT * 4 - 1) / ((int64_t)LT * 4));
     if (G > ctx->sm_count) G = ctx->sm_count;
     if (G < 1) G = 1;
@@ -364,8 +519,11 @@ int fpde_line_create(fpde_ctx *ctx, const fpde_line_desc *desc, const double *A,
     if (s > LSEG)
         return set_error(FPDE_ERR_UNSUPPORTED, "line of %lld intervals exceeds %lld (SMs x %d x %d)", (long long)N,
                          (long long)ctx->sm_count * LT * LSEG, LT, LSEG);
+    int sp = 1;
+    while (sp < s) sp <<= 1;
+    G = (int)((N + (int64_t)LT * sp - 1) / ((int64_t)LT * sp));
     int per_sm = 0;
-    FPDE_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_line_solve, LT, 0));
+    FPDE_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_line_solve<LSEG>, LT, 0));
     if (G > 1 && G > per_sm * ctx->sm_count)
         return set_error(FPDE_ERR_UNSUPPORTED, "line solve grid of %d CTAs cannot be co-resident", G);
 
@@ -375,8 +533,10 @@ int fpde_line_create(fpde_ctx *ctx, const fpde_line_desc *desc, const double *A,
     L->N = N;
     L->P = (N + 1 + 511) / 512 * 512;
     L->G = G;
-    L->s = (int)s;
+    L->s = sp;
     L->max_steps = d.max_steps;
+    L->split = d.precision != FPDE_PREC_FP64;
+    L->x3 = d.precision == FPDE_PREC_SPLIT_BF16X3;
     // local weight kkk0 = tau^{1-alpha}/(1-alpha); lam as in Om1 (:4191), lamR as in R (:3120)
     L->kkk0 = l1_interval_weight(d.alpha, 0.0, d.tau);
     L->lam = d.Da * (L->kkk0 / d.tau);
@@ -395,28 +555,77 @@ int fpde_line_create(fpde_ctx *ctx, const fpde_line_desc *desc, const double *A,
             hp[i] = hg[i] * A[i];
         }
     }
-    for (int64_t t0 = 0; t0 < N; t0 += s) {                      // per-thread segments
-        int64_t t1 = t0 + s < N ? t0 + s : N;
+    for (int64_t t0 = 0; t0 < N; t0 += sp) {                     // per-thread segments
+        int64_t t1 = t0 + sp < N ? t0 + sp : N;
         double pr = 1.0;
         for (int64_t i = t0; i < t1; ++i) { pr *= hp[i]; hcf[i] = pr; }
         pr = 1.0;
         for (int64_t i = t1 - 1; i >= t0; --i) { pr *= hal[i]; hcb[i] = pr; }
     }
-    // lag weights, reversed: wrev[m] = Da * kb(lag L-m) / tau, kb(lag j) = kkk0 * b_j
+    // lag weights w[j] = Da * kb(lag j) / tau with kb(lag j) = kkk0 * b_j; wrev[m] = w[L - m]
+    const int64_t LW = L->max_steps + BLK + 1;
+    std::vector<double> wlag(LW, 0.0);
+    for (int64_t j = 1; j < LW; ++j) wlag[j] = d.Da * (L->kkk0 * l1_lag(d.alpha, j)) / d.tau;
     std::vector<double> wrev(L->max_steps + 1, 0.0);
-    for (int64_t m = 0; m < L->max_steps; ++m) {
-        int64_t j = L->max_steps - m;
-        wrev[m] = d.Da * (L->kkk0 * l1_lag(d.alpha, j)) / d.tau;
-    }
+    for (int64_t m = 0; m < L->max_steps; ++m) wrev[m] = wlag[L->max_steps - m];
     const size_t nb = N * sizeof(double);
-    if (dev_alloc((void **)&L->A, nb) || dev_alloc((void **)&L->g, nb) || dev_alloc((void **)&L->al, nb) ||
-        dev_alloc((void **)&L->cf, nb) || dev_alloc((void **)&L->cb, nb) ||
-        dev_alloc((void **)&L->U, L->P * sizeof(double)) ||
-        dev_alloc((void **)&L->D, (size_t)L->max_steps * L->P * sizeof(double)) ||
-        dev_alloc((void **)&L->part, (size_t)KS_MAX * L->P * sizeof(double)) ||
-        dev_alloc((void **)&L->wrev, wrev.size() * sizeof(double)) ||
-        dev_alloc((void **)&L->aggf, 2 * G * sizeof(double)) || dev_alloc((void **)&L->aggb, 2 * G * sizeof(double)) ||
-        dev_alloc((void **)&L->UN, sizeof(double)) || dev_alloc((void **)&L->barrier, 2 * sizeof(unsigned))) {
+    bool fail = dev_alloc((void **)&L->A, nb) || dev_alloc((void **)&L->g, nb) || dev_alloc((void **)&L->al, nb) ||
+                dev_alloc((void **)&L->cf, nb) || dev_alloc((void **)&L->cb, nb) ||
+                dev_alloc((void **)&L->U, L->P * sizeof(double)) ||
+                dev_alloc((void **)&L->wrev, wrev.size() * sizeof(double)) ||
+                dev_alloc((void **)&L->aggf, 2 * G * sizeof(double)) ||
+                dev_alloc((void **)&L->aggb, 2 * G * sizeof(double)) || dev_alloc((void **)&L->UN, sizeof(double)) ||
+                dev_alloc((void **)&L->barrier, 2 * sizeof(unsigned));
+    if (!fail && !L->split) {
+        fail = dev_alloc((void **)&L->D, (size_t)L->max_steps * L->P * sizeof(double)) ||
+               dev_alloc((void **)&L->part, (size_t)KS_MAX * L->P * sizeof(double));
+    }
+    if (!fail && L->x3) {
+        L->rows16 = (N + 1 + 127) / 128 * 128;
+        L->ld16 = ((int64_t)L->max_steps + 63) / 64 * 64;
+        L->ldp = L->ld16 / 64;
+        for (int q = 0; q < 3 && !fail; ++q)
+            fail = dev_alloc((void **)&L->h3[q], (size_t)L->rows16 * L->ld16 * 2) ||
+                   dev_alloc((void **)&L->w3[q], (size_t)BLK * L->ld16 * 2);
+        fail = fail || dev_alloc((void **)&L->pA, (size_t)L->rows16 * L->ldp) ||
+               dev_alloc((void **)&L->pW, (size_t)BLK * L->ldp) ||
+               dev_alloc((void **)&L->ring, (size_t)BLK * L->P * sizeof(double)) ||
+               dev_alloc((void **)&L->cfar, (size_t)FAR_MAX_SPLITS * BLK * L->P * sizeof(double)) ||
+               dev_alloc((void **)&L->wlag, LW * sizeof(double));
+        if (!fail) {
+            const void *a[3] = {L->h3[0], L->h3[1], L->h3[2]}, *w[3] = {L->w3[0], L->w3[1], L->w3[2]};
+            int rcp = far_plan3_init(&L->plan3, a, L->rows16, L->ld16, w, L->ld16);
+            if (rcp) {
+                std::string keep = fpde_last_error_string();
+                fpde_line_destroy(L);
+                return set_error(rcp, "%s", keep.c_str());
+            }
+        }
+    } else if (!fail && L->split) {
+        L->rows16 = (N + 1 + 127) / 128 * 128;
+        L->ld16 = ((int64_t)L->max_steps + 63) / 64 * 64;
+        const int64_t nblk = L->ld16 / 64 + 1;
+        fail = dev_alloc((void **)&L->h_hi, (size_t)L->rows16 * L->ld16 * 2) ||
+               dev_alloc((void **)&L->h_lo, (size_t)L->rows16 * L->ld16 * 2) ||
+               dev_alloc((void **)&L->w_hi, (size_t)BLK * L->ld16 * 2) ||
+               dev_alloc((void **)&L->w_lo, (size_t)BLK * L->ld16 * 2) ||
+               dev_alloc((void **)&L->ring, (size_t)BLK * L->P * sizeof(double)) ||
+               dev_alloc((void **)&L->cfar, (size_t)FAR_MAX_SPLITS * BLK * L->P * sizeof(double)) ||
+               dev_alloc((void **)&L->wlag, LW * sizeof(double)) ||
+               dev_alloc((void **)&L->out_scale, sizeof(double)) ||
+               dev_alloc((void **)&L->slots, nblk * sizeof(unsigned long long)) ||
+               dev_alloc((void **)&L->exps, nblk * sizeof(int));
+        if (!fail) {
+            int rcp = far_plan_init(&L->plan, L->h_hi, L->h_lo, L->rows16, L->ld16, L->w_hi, L->w_lo, L->ld16,
+                                    d.precision == FPDE_PREC_SPLIT_BF16 ? 1 : 0);
+            if (rcp) {
+                std::string keep = fpde_last_error_string();
+                fpde_line_destroy(L);
+                return set_error(rcp, "%s", keep.c_str());
+            }
+        }
+    }
+    if (fail) {
         std::string keep = fpde_last_error_string();
         fpde_line_destroy(L);
         return set_error(FPDE_ERR_NOMEM, "%s", keep.c_str());
@@ -430,8 +639,28 @@ int fpde_line_create(fpde_ctx *ctx, const fpde_line_desc *desc, const double *A,
     cudaMemcpyAsync(L->wrev, wrev.data(), wrev.size() * sizeof(double), cudaMemcpyHostToDevice, st);
     cudaMemsetAsync(L->U, 0, L->P * sizeof(double), st);
     cudaMemcpyAsync(L->U, u0, (N + 1) * sizeof(double), cudaMemcpyHostToDevice, st);
-    cudaMemsetAsync(L->D, 0, (size_t)L->max_steps * L->P * sizeof(double), st);
     cudaMemsetAsync(L->barrier, 0, 2 * sizeof(unsigned), st);
+    if (!L->split) {
+        cudaMemsetAsync(L->D, 0, (size_t)L->max_steps * L->P * sizeof(double), st);
+    } else if (L->x3) {
+        for (int q = 0; q < 3; ++q) {
+            cudaMemsetAsync(L->h3[q], 0, (size_t)L->rows16 * L->ld16 * 2, st);
+            cudaMemsetAsync(L->w3[q], 0, (size_t)BLK * L->ld16 * 2, st);
+        }
+        cudaMemsetAsync(L->pA, 0, (size_t)L->rows16 * L->ldp, st);
+        cudaMemsetAsync(L->pW, 0, (size_t)BLK * L->ldp, st);
+        cudaMemsetAsync(L->ring, 0, (size_t)BLK * L->P * sizeof(double), st);
+        cudaMemsetAsync(L->cfar, 0, (size_t)FAR_MAX_SPLITS * BLK * L->P * sizeof(double), st);
+        cudaMemcpyAsync(L->wlag, wlag.data(), LW * sizeof(double), cudaMemcpyHostToDevice, st);
+    } else {
+        cudaMemsetAsync(L->h_hi, 0, (size_t)L->rows16 * L->ld16 * 2, st);
+        cudaMemsetAsync(L->h_lo, 0, (size_t)L->rows16 * L->ld16 * 2, st);
+        cudaMemsetAsync(L->w_hi, 0, (size_t)BLK * L->ld16 * 2, st);
+        cudaMemsetAsync(L->w_lo, 0, (size_t)BLK * L->ld16 * 2, st);
+        cudaMemsetAsync(L->ring, 0, (size_t)BLK * L->P * sizeof(double), st);
+        cudaMemsetAsync(L->cfar, 0, (size_t)FAR_MAX_SPLITS * BLK * L->P * sizeof(double), st);
+        cudaMemcpyAsync(L->wlag, wlag.data(), LW * sizeof(double), cudaMemcpyHostToDevice, st);
+    }
     cudaError_t e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) {
         fpde_line_destroy(L);
@@ -486,9 +715,9 @@ int fpde_line_run(fpde_line *L, int steps)
         if (e != cudaSuccess) return set_error(FPDE_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(e));
         it = L->graphs.emplace(key, exec).first;
         L->graph_launches[key] = nk;
-        L->graph_probe_steps[key] = L->probe_steps;
+        L->graph_probes[key] = L->probes;
     }
-    L->last_probe_steps = L->graph_probe_steps[key];
+    L->last_probes = L->graph_probes[key];
     FPDE_CUDA(cudaGraphLaunch(it->second, st));
     count_launches(L->graph_launches[key]);
     L->n_done += steps;
@@ -539,40 +768,42 @@ int fpde_line_set_probe(fpde_line *L, int every)
     for (auto &kv : L->graphs) cudaGraphExecDestroy(kv.second);
     L->graphs.clear();
     L->graph_launches.clear();
-    L->graph_probe_steps.clear();
-    L->last_probe_steps.clear();
+    L->graph_probes.clear();
+    L->last_probes.clear();
     for (cudaEvent_t e : L->probe_ev) cudaEventDestroy(e);
     L->probe_ev.clear();
     L->probe_every = every;
     if (every > 0) {
-        int64_t n = L->max_steps / every + 1;
-        if (n > 4096) n = 4096;
-        L->probe_ev.resize(3 * n);
+        int64_t n = L->max_steps / every + L->max_steps / BLK + 2;
+        if (n > 8192) n = 8192;
+        L->probe_ev.resize(2 * n);
         for (auto &e : L->probe_ev) FPDE_CUDA(cudaEventCreate(&e));
     }
     return FPDE_OK;
 }
 
-int fpde_line_probe_stats(fpde_line *L, double *hist_ms, double *hist_bytes, double *solve_ms, int *probes)
+int fpde_line_probe_stats(fpde_line *L, int kind, double *ms, double *bytes, double *flops, int *count)
 {
     clear_error();
-    FPDE_CHECK_ARG(L && hist_ms && hist_bytes && solve_ms && probes, "null argument");
+    FPDE_CHECK_ARG(L && ms && bytes && flops && count, "null argument");
     int rc = ctx_enter(L->ctx);
     if (rc) return rc;
     FPDE_CUDA(cudaStreamSynchronize(L->ctx->stream));
-    double hm = 0, hb = 0, sm = 0;
-    for (size_t q = 0; q < L->last_probe_steps.size(); ++q) {
-        float a = 0, b = 0;
-        FPDE_CUDA(cudaEventElapsedTime(&a, L->probe_ev[3 * q], L->probe_ev[3 * q + 1]));
-        FPDE_CUDA(cudaEventElapsedTime(&b, L->probe_ev[3 * q + 1], L->probe_ev[3 * q + 2]));
-        hm += a;
-        sm += b;
-        hb += 8.0 * (double)L->last_probe_steps[q] * (double)(L->N + 1);
+    double m = 0, b = 0, f = 0;
+    int c = 0;
+    for (const auto &p : L->last_probes) {
+        if (p.kind != kind) continue;
+        float t = 0;
+        FPDE_CUDA(cudaEventElapsedTime(&t, L->probe_ev[p.ev], L->probe_ev[p.ev + 1]));
+        m += t;
+        b += p.bytes;
+        f += p.flops;
+        ++c;
     }
-    *hist_ms = hm;
-    *hist_bytes = hb;
-    *solve_ms = sm;
-    *probes = (int)L->last_probe_steps.size();
+    *ms = m;
+    *bytes = b;
+    *flops = f;
+    *count = c;
     return FPDE_OK;
 }
 

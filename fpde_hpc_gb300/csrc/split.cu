@@ -1,0 +1,229 @@
+// Block preparation of the split-precision path (per block of 64 steps):
+//   k_absmax  : largest |increment| of the finished block (for the fp16 scale)
+//   k_convert : FP64 increments (time-major ring, 64 rows) -> 16-bit hi/lo pairs in the
+//               node-major history used as the K-major A operand, scaled by 2^sexp
+//   k_wgen    : Toeplitz weight tile W[j][t] = w[n0+j-t] * 2^(kexp - sexp(t)), split hi/lo,
+//               and the output scale 2^-kexp of the contraction
+// The power-of-two scales keep fp16 operands inside its normal range; they are exact, and
+// A*W keeps its value up to the single global factor 2^kexp undone in the epilogue.
+// bf16 has float's exponent range and runs unscaled (sexp = kexp = 0).
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+
+#include "common.cuh"
+#include "kernels.cuh"
+
+namespace fpde {
+
+__global__ void k_absmax(const double *__restrict__ x, int64_t n, unsigned long long *slot)
+{
+    double m = 0.0;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        m = fmax(m, fabs(x[i]));
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+    __shared__ double red[32];
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        m = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.0;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+        if (threadIdx.x == 0 && m > 0.0) atomicMax(slot, (unsigned long long)__double_as_longlong(m));
+    }
+}
+
+__device__ __forceinline__ int scale_exp_from_max(unsigned long long bits)
+{
+    const double m = __longlong_as_double((long long)bits);
+    if (!(m > 0.0)) return 0;
+    const int e = ilogb(m) + 1;           // m < 2^e
+    return 14 - e;                        // scaled max < 2^14
+}
+
+__device__ __forceinline__ void split16(double v, int bf16, uint16_t &h, uint16_t &l)
+{
+    if (bf16) {
+        __nv_bfloat16 hb = __double2bfloat16(v);
+        __nv_bfloat16 lb = __double2bfloat16(v - (double)__bfloat162float(hb));
+        h = __bfloat16_as_ushort(hb);
+        l = __bfloat16_as_ushort(lb);
+    } else {
+        __half hh = __double2half(v);
+        __half lh = __double2half(v - (double)__half2float(hh));
+        h = __half_as_ushort(hh);
+        l = __half_as_ushort(lh);
+    }
+}
+
+// One CTA per 64 nodes: transpose a 64 (rows of the ring) x 64 (nodes) FP64 tile through
+// shared memory and write each node's 64 new history columns as 16-byte vectors.
+__global__ void __launch_bounds__(256) k_convert(const double *__restrict__ ring, int64_t P, int64_t nvalid,
+                                                 const unsigned long long *__restrict__ slot, int *__restrict__ exps,
+                                                 int blk, uint16_t *__restrict__ hi, uint16_t *__restrict__ lo,
+                                                 int64_t ld, int64_t col0, int bf16)
+{
+    __shared__ double tile[64][65];
+    const int64_t node0 = (int64_t)blockIdx.x * 64;
+    const int sexp = bf16 ? 0 : scale_exp_from_max(*slot);
+    const double sc = ldexp(1.0, sexp);
+    if (blockIdx.x == 0 && threadIdx.x == 0) exps[blk] = sexp;
+    for (int e = threadIdx.x; e < 64 * 64; e += 256) {
+        const int r = e >> 6, c = e & 63;
+        const int64_t node = node0 + c;
+        tile[c][r] = node < nvalid ? ring[(int64_t)r * P + node] * sc : 0.0;
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < 64 * 8; e += 256) {
+        const int c = e >> 3, g = e & 7;                 // node c, columns 8g..8g+7
+        const int64_t node = node0 + c;
+        if (node >= nvalid) continue;
+        uint16_t h[8], l[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) split16(tile[c][8 * g + k], bf16, h[k], l[k]);
+        uint4 vh, vl;
+        vh.x = h[0] | ((uint32_t)h[1] << 16); vh.y = h[2] | ((uint32_t)h[3] << 16);
+        vh.z = h[4] | ((uint32_t)h[5] << 16); vh.w = h[6] | ((uint32_t)h[7] << 16);
+        vl.x = l[0] | ((uint32_t)l[1] << 16); vl.y = l[2] | ((uint32_t)l[3] << 16);
+        vl.z = l[4] | ((uint32_t)l[5] << 16); vl.w = l[6] | ((uint32_t)l[7] << 16);
+        *(uint4 *)(hi + node * ld + col0 + 8 * g) = vh;
+        *(uint4 *)(lo + node * ld + col0 + 8 * g) = vl;
+    }
+}
+
+// grid = (ceil(n0/256), 64): row j of the weight tile, columns t < n0.
+__global__ void __launch_bounds__(256) k_wgen(const double *__restrict__ wlag, int n0, const int *__restrict__ exps,
+                                              uint16_t *__restrict__ whi, uint16_t *__restrict__ wlo, int64_t ldw,
+                                              int bf16, double *__restrict__ out_scale)
+{
+    __shared__ int s_kexp;
+    if (threadIdx.x < 32) {
+        int kmax = -100000;
+        if (!bf16) {
+            for (int b = threadIdx.x; b < n0 / 64; b += 32) {
+                const double wm = wlag[n0 - 64 * b - 63];            // largest weight of block b
+                const int ew = (wm > 0.0) ? ilogb(wm) + 1 : -100000; // wm < 2^ew
+                kmax = max(kmax, ew - exps[b]);
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) kmax = max(kmax, __shfl_xor_sync(0xffffffffu, kmax, o));
+        }
+        if (threadIdx.x == 0) s_kexp = bf16 ? 0 : (kmax > -100000 ? 14 - kmax : 0);
+    }
+    __syncthreads();
+    const int kexp = s_kexp;
+    const int j = blockIdx.y;
+    const int t = blockIdx.x * 256 + threadIdx.x;
+    if (blockIdx.x == 0 && j == 0 && threadIdx.x == 0) *out_scale = ldexp(1.0, -kexp);
+    if (t >= n0) return;
+    const double v = wlag[n0 + j - t] * ldexp(1.0, kexp - (bf16 ? 0 : exps[t >> 6]));
+    uint16_t h, l;
+    split16(v, bf16, h, l);
+    whi[(int64_t)j * ldw + t] = h;
+    wlo[(int64_t)j * ldw + t] = l;
+}
+
+// ---- exact three-slice form (bf16): x * 2^(8-e) = a0 + a1 2^-8 + a2 2^-16 + O(2^-17),
+// |x| < 2^e, with integer a0, a1, a2 of at most 8 bits; the exponent p = e - 8 is stored
+// per (node, 64-column block) for the history and per (step j, k-tile) for the weights.
+__device__ __forceinline__ int slice_exp(double m)
+{
+    if (!(m > 0.0)) return 0;
+    int p = ilogb(m) + 1 - 8;                 // m < 2^(p+8)
+    return p < -127 ? -127 : (p > 127 ? 127 : p);
+}
+__device__ __forceinline__ void slice3(double x, uint16_t &s0, uint16_t &s1, uint16_t &s2)
+{
+    const double a0 = rint(x);
+    const double r1 = (x - a0) * 256.0;
+    const double a1 = rint(r1);
+    const double a2 = rint((r1 - a1) * 256.0);
+    s0 = __bfloat16_as_ushort(__double2bfloat16(a0));
+    s1 = __bfloat16_as_ushort(__double2bfloat16(a1 * (1.0 / 256.0)));
+    s2 = __bfloat16_as_ushort(__double2bfloat16(a2 * (1.0 / 65536.0)));
+}
+
+// One thread per node: the node's 64 increments of the finished block.
+__global__ void __launch_bounds__(128) k_convert3(const double *__restrict__ ring, int64_t P, int64_t nvalid,
+                                                  uint16_t *__restrict__ h0, uint16_t *__restrict__ h1,
+                                                  uint16_t *__restrict__ h2, int64_t ld, int64_t col0,
+                                                  int8_t *__restrict__ pA, int64_t ldp, int blk)
+{
+    const int64_t node = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (node >= nvalid) return;
+    double m = 0.0;
+    for (int r = 0; r < 64; ++r) m = fmax(m, fabs(ring[(int64_t)r * P + node]));
+    const int pe = slice_exp(m);
+    pA[node * ldp + blk] = (int8_t)pe;
+    const double sc = ldexp(1.0, -pe);
+    for (int g = 0; g < 8; ++g) {
+        uint16_t a[8], b[8], c[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) slice3(ring[(int64_t)(8 * g + k) * P + node] * sc, a[k], b[k], c[k]);
+        uint4 va, vb, vc;
+        va.x = a[0] | ((uint32_t)a[1] << 16); va.y = a[2] | ((uint32_t)a[3] << 16);
+        va.z = a[4] | ((uint32_t)a[5] << 16); va.w = a[6] | ((uint32_t)a[7] << 16);
+        vb.x = b[0] | ((uint32_t)b[1] << 16); vb.y = b[2] | ((uint32_t)b[3] << 16);
+        vb.z = b[4] | ((uint32_t)b[5] << 16); vb.w = b[6] | ((uint32_t)b[7] << 16);
+        vc.x = c[0] | ((uint32_t)c[1] << 16); vc.y = c[2] | ((uint32_t)c[3] << 16);
+        vc.z = c[4] | ((uint32_t)c[5] << 16); vc.w = c[6] | ((uint32_t)c[7] << 16);
+        *(uint4 *)(h0 + node * ld + col0 + 8 * g) = va;
+        *(uint4 *)(h1 + node * ld + col0 + 8 * g) = vb;
+        *(uint4 *)(h2 + node * ld + col0 + 8 * g) = vc;
+    }
+}
+
+// grid = (n0/64 k-tiles, 64 steps j), 64 threads: W[j][t] = w[n0 + j - t] for the k-tile.
+__global__ void __launch_bounds__(64) k_wgen3(const double *__restrict__ wlag, int n0, uint16_t *__restrict__ w0,
+                                              uint16_t *__restrict__ w1, uint16_t *__restrict__ w2, int64_t ld,
+                                              int8_t *__restrict__ pW, int64_t ldp)
+{
+    __shared__ double red[2];
+    const int kt = blockIdx.x, j = blockIdx.y;
+    const int t = kt * 64 + threadIdx.x;
+    const double v = wlag[n0 + j - t];
+    double m = fabs(v);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+    __syncthreads();
+    m = fmax(red[0], red[1]);
+    const int pe = slice_exp(m);
+    if (threadIdx.x == 0) pW[(int64_t)j * ldp + kt] = (int8_t)pe;
+    uint16_t a, b, c;
+    slice3(v * ldexp(1.0, -pe), a, b, c);
+    w0[(int64_t)j * ld + t] = a;
+    w1[(int64_t)j * ld + t] = b;
+    w2[(int64_t)j * ld + t] = c;
+}
+
+int launch_block_prep3(cudaStream_t st, const SplitPrep3 &p, int64_t n0)
+{
+    const int blk = (int)(n0 / 64) - 1;
+    k_convert3<<<(unsigned)((p.nvalid + 127) / 128), 128, 0, st>>>(p.ring, p.P, p.nvalid, p.hist[0], p.hist[1],
+                                                                   p.hist[2], p.ld, n0 - 64, p.pA, p.ldp, blk);
+    FPDE_LAUNCHED(1);
+    dim3 g((unsigned)(n0 / 64), 64);
+    k_wgen3<<<g, 64, 0, st>>>(p.wlag, (int)n0, p.w[0], p.w[1], p.w[2], p.ld, p.pW, p.ldp);
+    FPDE_LAUNCHED(1);
+    return FPDE_OK;
+}
+
+int launch_block_prep(cudaStream_t st, const SplitPrep &p, int64_t n0)
+{
+    const int blk = (int)(n0 / 64) - 1;          // the block that has just finished
+    if (!p.bf16) {
+        FPDE_CUDA(cudaMemsetAsync(p.slots + blk, 0, sizeof(unsigned long long), st));
+        k_absmax<<<512, 256, 0, st>>>(p.ring, 64 * p.P, p.slots + blk);
+        FPDE_LAUNCHED(1);
+    }
+    k_convert<<<(unsigned)((p.nvalid + 63) / 64), 256, 0, st>>>(p.ring, p.P, p.nvalid, p.slots + blk, p.exps, blk,
+                                                                p.hist_hi, p.hist_lo, p.ld, n0 - 64, p.bf16);
+    FPDE_LAUNCHED(1);
+    dim3 g((unsigned)((n0 + 255) / 256), 64);
+    k_wgen<<<g, 256, 0, st>>>(p.wlag, (int)n0, p.exps, p.w_hi, p.w_lo, p.ld, p.bf16, p.out_scale);
+    FPDE_LAUNCHED(1);
+    return FPDE_OK;
+}
+
+}  // namespace fpde

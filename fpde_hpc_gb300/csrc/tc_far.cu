@@ -1,0 +1,640 @@
+// Far-history contraction on the 5th-generation tensor cores (tcgen05), split precision.
+//
+// For a block of BN upcoming steps starting at n0, the history older than the block enters
+// every step of the block through a dense product
+//     C[i][j] = sum_{t < n0} A[i][t] * W[t][j],   A[i][t] = D_t[i] (node i, increment t),
+//                                                  W[t][j] = w[n0 + j - t] (Toeplitz weights),
+// M = nodes, N = BN = 64 steps, K = n0. This is the reference's mode-1 far-history tile
+// product (fr_do.cpp:173-235, wmma 16x16x16 half/float), rebuilt for sm_103a:
+//   * A and W are stored as 16-bit hi/lo pairs (fp16 with power-of-two scaling, or bf16);
+//     three products A_hi W_hi + A_hi W_lo + A_lo W_hi run as kind::f16 MMAs
+//     (M=128, N=64, K=16) accumulating in FP32 in TMEM;
+//   * every 256 history columns the TMEM accumulator is folded into float-float (hi, lo)
+//     registers by the epilogue warps while the MMA warp fills the other TMEM buffer; the
+//     CTA's result is written as FP64 partial sums C[split][j][row];
+//   * operands arrive by TMA (cp.async.bulk.tensor, 128-byte swizzle) into a 4-stage ring
+//     guarded by mbarriers; no multicast.
+// Warp roles (192 threads): warp 0 TMA producer, warp 1 TMEM allocator + MMA issuer,
+// warps 2-5 epilogue (TMEM lane quadrant = warp % 4).
+// Every wait is bounded (2 s of %globaltimer); on timeout the kernel raises
+// DEVERR_MBAR_TIMEOUT, stops issuing, drains its own copies (bounded) and frees its TMEM.
+#include <cuda.h>
+#include <cuda_runtime.h>
+
+#include "common.cuh"
+#include "kernels.cuh"
+#include "tc_far.cuh"
+
+namespace fpde {
+namespace tc {
+
+constexpr int BM = 128, BN = 64, BK = 64;
+constexpr int STAGES = 4;
+constexpr int CHUNK_KT = 4;                          // k-tiles per TMEM accumulation chunk
+constexpr int A_BYTES = BM * BK * 2;                 // 16 KB
+constexpr int W_BYTES = BN * BK * 2;                 // 8 KB
+constexpr int STAGE_BYTES = 2 * A_BYTES + 2 * W_BYTES;
+constexpr int TMEM_COLS = 128;                       // two 64-column fp32 accumulators
+constexpr int THREADS = 192;
+constexpr int SMEM_BYTES = 1024 + STAGES * STAGE_BYTES + 256;
+constexpr unsigned long long WAIT_NS = 2000000000ull;
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ unsigned long long gtimer()
+{
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar)
+{
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity)
+{
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}\n"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// Bounded wait on the phase with the given parity.
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, unsigned *flags, volatile int *abort_s)
+{
+    if (mbar_try_wait(bar, parity)) return true;
+    const unsigned long long t0 = gtimer();
+    while (true) {
+        if (mbar_try_wait(bar, parity)) return true;
+        if (*abort_s) return false;
+        if (gtimer() - t0 > WAIT_NS) {
+            atomicOr(flags, DEVERR_MBAR_TIMEOUT);
+            *abort_s = 1;
+            return false;
+        }
+    }
+}
+
+__device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *tm, int x, int y, uint64_t *bar)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];"
+        ::"r"(smem_u32(dst)), "l"((uint64_t)tm), "r"(x), "r"(y), "r"(smem_u32(bar))
+        : "memory");
+}
+
+// K-major operand tile, 128-byte swizzle: rows of 128 B, 8-row atoms of 1024 B (SBO).
+__device__ __forceinline__ uint64_t sdesc_sw128(uint32_t saddr)
+{
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);        // start address
+    d |= (uint64_t)1 << 16;                          // leading byte offset (unused for SW128 K-major)
+    d |= (uint64_t)(1024 >> 4) << 32;                // stride byte offset: 8 rows x 128 B
+    d |= (uint64_t)1 << 46;                          // descriptor version (tcgen05)
+    d |= (uint64_t)2 << 61;                          // SWIZZLE_128B
+    return d;
+}
+
+// Instruction descriptor, kind::f16: D f32, A/B fp16 (0) or bf16 (1), both K-major.
+__host__ __device__ constexpr uint32_t idesc_f16(int bf16, int M, int N)
+{
+    return (1u << 4) | ((uint32_t)bf16 << 7) | ((uint32_t)bf16 << 10) | ((uint32_t)(N >> 3) << 17) |
+           ((uint32_t)(M >> 4) << 24);
+}
+
+__device__ __forceinline__ void umma(uint32_t dtm, uint64_t ad, uint64_t bd, uint32_t idesc, uint32_t acc)
+{
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n"
+        ::"r"(dtm), "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
+}
+__device__ __forceinline__ void umma_commit(uint64_t *bar)
+{
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+                 : "memory");
+}
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float *v)
+{
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+#pragma unroll
+    for (int k = 0; k < 16; ++k) v[k] = __uint_as_float(r[k]);
+}
+__device__ __forceinline__ void tmem_ld_wait() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+
+struct __align__(64) FarMaps {
+    CUtensorMap a_hi, a_lo, w_hi, w_lo;
+};
+
+// grid = (row tiles, K splits); split y covers k-tiles [y*kt_per, min((y+1)*kt_per, kt_total)).
+__global__ void __launch_bounds__(THREADS, 1)
+    k_far_tc(const __grid_constant__ FarMaps maps, double *__restrict__ C, int64_t ldc_split, int64_t ldc_col,
+             int64_t rows, int kt_total, int kt_per, uint32_t idesc, double out_scale,
+             const double *__restrict__ out_scale_ptr, unsigned *flags)
+{
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    uint8_t *stage_base = smem;
+    uint64_t *bars = (uint64_t *)(smem + STAGES * STAGE_BYTES);
+    uint64_t *full = bars, *empty = bars + STAGES, *tfull = bars + 2 * STAGES, *tempty = bars + 2 * STAGES + 2;
+    uint64_t *mma_done = bars + 2 * STAGES + 4;
+    volatile uint32_t *tmem_slot = (volatile uint32_t *)(bars + 2 * STAGES + 5);
+    volatile int *abort_s = (volatile int *)(bars + 2 * STAGES + 6);
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int mt = blockIdx.x, split = blockIdx.y;
+    const int kt0 = split * kt_per;
+    const int kt1 = min(kt0 + kt_per, kt_total);
+    const int nkt = max(0, kt1 - kt0);
+    const int nchunks = (nkt + CHUNK_KT - 1) / CHUNK_KT;
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < STAGES; ++s) { mbar_init(&full[s], 1); mbar_init(&empty[s], 1); }
+        for (int b = 0; b < 2; ++b) { mbar_init(&tfull[b], 1); mbar_init(&tempty[b], 128); }
+        mbar_init(mma_done, 1);
+        *abort_s = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 1) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                         smem_u32((const void *)tmem_slot)),
+                     "r"(TMEM_COLS));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tmem_slot;
+
+    if (warp == 0) {
+        // ------------------------------------------------ TMA producer
+        if (lane == 0) {
+            int issued = 0;
+            for (int it = 0; it < nkt; ++it) {
+                const int s = it % STAGES;
+                const uint32_t ph = (uint32_t)(it / STAGES) & 1u;
+                if (!mbar_wait(&empty[s], ph ^ 1u, flags, abort_s)) break;
+                uint8_t *st = stage_base + s * STAGE_BYTES;
+                mbar_expect_tx(&full[s], STAGE_BYTES);
+                const int x = (kt0 + it) * BK, y = mt * BM;
+                tma_load_2d(st, &maps.a_hi, x, y, &full[s]);
+                tma_load_2d(st + A_BYTES, &maps.a_lo, x, y, &full[s]);
+                tma_load_2d(st + 2 * A_BYTES, &maps.w_hi, x, 0, &full[s]);
+                tma_load_2d(st + 2 * A_BYTES + W_BYTES, &maps.w_lo, x, 0, &full[s]);
+                ++issued;
+            }
+            // Drain: every issued stage's copy must land before the CTA exits.
+            for (int it = (issued > STAGES ? issued - STAGES : 0); it < issued; ++it) {
+                const int s = it % STAGES;
+                const uint32_t ph = (uint32_t)(it / STAGES) & 1u;
+                unsigned long long t0 = gtimer();
+                while (!mbar_try_wait(&full[s], ph) && gtimer() - t0 < WAIT_NS) {}
+            }
+        }
+    } else if (warp == 1) {
+        // ------------------------------------------------ MMA issuer
+        if (lane == 0) {
+            int it = 0;
+            for (int c = 0; c < nchunks && !*abort_s; ++c) {
+                const int buf = c & 1;
+                const uint32_t use = (uint32_t)(c >> 1);
+                if (!mbar_wait(&tempty[buf], (use & 1u) ^ 1u, flags, abort_s)) break;
+                tc_fence_after();
+                const uint32_t dtm = tmem + (uint32_t)(buf * BN);
+                const int kend = min(nkt, (c + 1) * CHUNK_KT);
+                bool ok = true;
+                for (int first = 1; it < kend; ++it, first = 0) {
+                    const int s = it % STAGES;
+                    const uint32_t ph = (uint32_t)(it / STAGES) & 1u;
+                    if (!mbar_wait(&full[s], ph, flags, abort_s)) { ok = false; break; }
+                    tc_fence_after();
+                    const uint32_t st = smem_u32(stage_base + s * STAGE_BYTES);
+                    const uint32_t a_hi = st, a_lo = st + A_BYTES, w_hi = st + 2 * A_BYTES,
+                                   w_lo = st + 2 * A_BYTES + W_BYTES;
+#pragma unroll
+                    for (int k = 0; k < BK / 16; ++k) {
+                        const uint32_t off = (uint32_t)(k * 32);     // 16 elements x 2 B along K
+                        const uint32_t acc = (first && k == 0) ? 0u : 1u;
+                        umma(dtm, sdesc_sw128(a_hi + off), sdesc_sw128(w_hi + off), idesc, acc);
+                        umma(dtm, sdesc_sw128(a_hi + off), sdesc_sw128(w_lo + off), idesc, 1u);
+                        umma(dtm, sdesc_sw128(a_lo + off), sdesc_sw128(w_hi + off), idesc, 1u);
+                    }
+                    umma_commit(&empty[s]);                 // frees the stage when these MMAs finish
+                }
+                if (!ok) break;
+                umma_commit(&tfull[buf]);                   // chunk accumulator ready
+            }
+            // Every MMA of this CTA must have finished before its TMEM is released.
+            umma_commit(mma_done);
+            const unsigned long long t0 = gtimer();
+            while (!mbar_try_wait(mma_done, 0) && gtimer() - t0 < WAIT_NS) {}
+        }
+    } else {
+        // ------------------------------------------------ epilogue (warps 2..5)
+        const int q = warp & 3;                            // TMEM lane quadrant of this warp
+        const int64_t row = (int64_t)mt * BM + q * 32 + lane;
+        float hi[BN], lo[BN];
+#pragma unroll
+        for (int j = 0; j < BN; ++j) { hi[j] = 0.f; lo[j] = 0.f; }
+        bool ok = true;
+        for (int c = 0; c < nchunks; ++c) {
+            const int buf = c & 1;
+            const uint32_t use = (uint32_t)(c >> 1);
+            if (!mbar_wait(&tfull[buf], use & 1u, flags, abort_s)) { ok = false; break; }
+            tc_fence_after();
+            const uint32_t taddr = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(buf * BN);
+            float v[BN];
+            tmem_ld16(taddr + 0, v);
+            tmem_ld16(taddr + 16, v + 16);
+            tmem_ld16(taddr + 32, v + 32);
+            tmem_ld16(taddr + 48, v + 48);
+            tmem_ld_wait();
+            tc_fence_before();
+            mbar_arrive(&tempty[buf]);
+#pragma unroll
+            for (int j = 0; j < BN; ++j) {                 // float-float accumulation (TwoSum)
+                const float s = hi[j] + v[j];
+                const float bb = s - hi[j];
+                const float e = (hi[j] - (s - bb)) + (v[j] - bb);
+                hi[j] = s;
+                lo[j] += e;
+            }
+        }
+        if (ok && row < rows && nchunks > 0) {
+            if (out_scale_ptr) out_scale *= *out_scale_ptr;
+            double *out = C + (int64_t)split * ldc_split + row;
+#pragma unroll
+            for (int j = 0; j < BN; ++j) out[(int64_t)j * ldc_col] = ((double)hi[j] + (double)lo[j]) * out_scale;
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 1) {
+        tc_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS));
+    }
+}
+
+// ------------------------------------------------------------------------------------
+// Exact-slice variant (three bf16 slices per operand).
+// A[i][t] = (a0 + a1' + a2') * 2^pA[i][kt], W[j][t] = (w0 + w1' + w2') * 2^pW[j][kt] with
+// a0, w0 integers of at most 8 bits and a1' = a1 2^-8, a2' = a2 2^-16 (a1, a2 integers of
+// at most 8 bits), per node (or step) and 64-column k-tile. Per k-tile the products
+//   X0  = sum a0 w0                                  (integers < 2^16, 64 of them < 2^22:
+//                                                    exact in the FP32 accumulator)
+//   X12 = sum a0 w1' + a1' w0 + a0 w2' + a1' w1' + a2' w0     (2^-8 below X0)
+// go to two TMEM accumulators; the epilogue scales both by 2^(pA+pW) and folds them into
+// float-float every k-tile. The leading product is therefore free of accumulation error,
+// whatever the rounding of the tensor core's FP32 adder.
+constexpr int STAGES3 = 3;
+constexpr int STAGE3_BYTES = 3 * A_BYTES + 3 * W_BYTES;      // 72 KB
+constexpr int TMEM3_COLS = 256;                               // 2 buffers x (X0, X12)
+constexpr int SMEM3_BYTES = 1024 + STAGES3 * STAGE3_BYTES + 256;
+
+struct __align__(64) FarMaps3 {
+    CUtensorMap a[3], w[3];
+};
+
+__global__ void __launch_bounds__(THREADS, 1)
+    k_far_tc3(const __grid_constant__ FarMaps3 maps, double *__restrict__ C, int64_t ldc_split, int64_t ldc_col,
+              int64_t rows, int kt_total, int kt_per, uint32_t idesc, const int8_t *__restrict__ pA,
+              const int8_t *__restrict__ pW, int64_t ldp, unsigned *flags)
+{
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    uint8_t *stage_base = smem;
+    uint64_t *bars = (uint64_t *)(smem + STAGES3 * STAGE3_BYTES);
+    uint64_t *full = bars, *empty = bars + STAGES3, *tfull = bars + 2 * STAGES3, *tempty = bars + 2 * STAGES3 + 2;
+    uint64_t *mma_done = bars + 2 * STAGES3 + 4;
+    volatile uint32_t *tmem_slot = (volatile uint32_t *)(bars + 2 * STAGES3 + 5);
+    volatile int *abort_s = (volatile int *)(bars + 2 * STAGES3 + 6);
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int mt = blockIdx.x, split = blockIdx.y;
+    const int kt0 = split * kt_per;
+    const int kt1 = min(kt0 + kt_per, kt_total);
+    const int nkt = max(0, kt1 - kt0);
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < STAGES3; ++s) { mbar_init(&full[s], 1); mbar_init(&empty[s], 1); }
+        for (int b = 0; b < 2; ++b) { mbar_init(&tfull[b], 1); mbar_init(&tempty[b], 128); }
+        mbar_init(mma_done, 1);
+        *abort_s = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 1) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                         smem_u32((const void *)tmem_slot)),
+                     "r"(TMEM3_COLS));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *tmem_slot;
+
+    if (warp == 0) {
+        if (lane == 0) {                                   // TMA producer
+            int issued = 0;
+            for (int it = 0; it < nkt; ++it) {
+                const int s = it % STAGES3;
+                const uint32_t ph = (uint32_t)(it / STAGES3) & 1u;
+                if (!mbar_wait(&empty[s], ph ^ 1u, flags, abort_s)) break;
+                uint8_t *st = stage_base + s * STAGE3_BYTES;
+                mbar_expect_tx(&full[s], STAGE3_BYTES);
+                const int x = (kt0 + it) * BK, y = mt * BM;
+#pragma unroll
+                for (int q = 0; q < 3; ++q) tma_load_2d(st + q * A_BYTES, &maps.a[q], x, y, &full[s]);
+#pragma unroll
+                for (int q = 0; q < 3; ++q) tma_load_2d(st + 3 * A_BYTES + q * W_BYTES, &maps.w[q], x, 0, &full[s]);
+                ++issued;
+            }
+            for (int it = (issued > STAGES3 ? issued - STAGES3 : 0); it < issued; ++it) {
+                const int s = it % STAGES3;
+                const uint32_t ph = (uint32_t)(it / STAGES3) & 1u;
+                unsigned long long t0 = gtimer();
+                while (!mbar_try_wait(&full[s], ph) && gtimer() - t0 < WAIT_NS) {}
+            }
+        }
+    } else if (warp == 1) {
+        if (lane == 0) {                                   // MMA issuer: one k-tile per chunk
+            for (int it = 0; it < nkt && !*abort_s; ++it) {
+                const int buf = it & 1;
+                const uint32_t use = (uint32_t)(it >> 1);
+                if (!mbar_wait(&tempty[buf], (use & 1u) ^ 1u, flags, abort_s)) break;
+                tc_fence_after();
+                const int s = it % STAGES3;
+                const uint32_t ph = (uint32_t)(it / STAGES3) & 1u;
+                if (!mbar_wait(&full[s], ph, flags, abort_s)) break;
+                tc_fence_after();
+                const uint32_t x0 = tmem + (uint32_t)(buf * 2 * BN), x12 = x0 + BN;
+                const uint32_t st = smem_u32(stage_base + s * STAGE3_BYTES);
+                const uint32_t a0 = st, a1 = st + A_BYTES, a2 = st + 2 * A_BYTES;
+                const uint32_t w0 = st + 3 * A_BYTES, w1 = w0 + W_BYTES, w2 = w0 + 2 * W_BYTES;
+#pragma unroll
+                for (int k = 0; k < BK / 16; ++k) {
+                    const uint32_t off = (uint32_t)(k * 32);
+                    const uint32_t acc = k ? 1u : 0u;
+                    umma(x0, sdesc_sw128(a0 + off), sdesc_sw128(w0 + off), idesc, acc);
+                    umma(x12, sdesc_sw128(a0 + off), sdesc_sw128(w1 + off), idesc, acc);
+                    umma(x12, sdesc_sw128(a1 + off), sdesc_sw128(w0 + off), idesc, 1u);
+                    umma(x12, sdesc_sw128(a0 + off), sdesc_sw128(w2 + off), idesc, 1u);
+                    umma(x12, sdesc_sw128(a1 + off), sdesc_sw128(w1 + off), idesc, 1u);
+                    umma(x12, sdesc_sw128(a2 + off), sdesc_sw128(w0 + off), idesc, 1u);
+                }
+                umma_commit(&empty[s]);
+                umma_commit(&tfull[buf]);
+            }
+            umma_commit(mma_done);
+            const unsigned long long t0 = gtimer();
+            while (!mbar_try_wait(mma_done, 0) && gtimer() - t0 < WAIT_NS) {}
+        }
+    } else {
+        const int q = warp & 3;                            // TMEM lane quadrant
+        const int64_t row = (int64_t)mt * BM + q * 32 + lane;
+        const int64_t row_c = row < rows ? row : rows - 1;
+        float hi[BN], lo[BN];
+#pragma unroll
+        for (int j = 0; j < BN; ++j) { hi[j] = 0.f; lo[j] = 0.f; }
+        bool ok = true;
+        for (int it = 0; it < nkt; ++it) {
+            const int buf = it & 1;
+            const uint32_t use = (uint32_t)(it >> 1);
+            if (!mbar_wait(&tfull[buf], use & 1u, flags, abort_s)) { ok = false; break; }
+            tc_fence_after();
+            const int kt = kt0 + it;
+            const int ea = (int)pA[row_c * ldp + kt];
+            const uint32_t tb = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(buf * 2 * BN);
+#pragma unroll
+            for (int h = 0; h < BN / 16; ++h) {
+                float v0[16], v1[16];
+                tmem_ld16(tb + 16 * h, v0);
+                tmem_ld16(tb + BN + 16 * h, v1);
+                tmem_ld_wait();
+#pragma unroll
+                for (int jj = 0; jj < 16; ++jj) {
+                    const int j = 16 * h + jj;
+                    const float sc = ldexpf(1.0f, ea + (int)__ldg(pW + (int64_t)j * ldp + kt));
+                    float x = v0[jj] * sc;                     // exact (power-of-two scaling)
+                    float s = hi[j] + x, bb = s - hi[j];
+                    float e = (hi[j] - (s - bb)) + (x - bb);
+                    hi[j] = s;
+                    lo[j] += e;
+                    x = v1[jj] * sc;
+                    s = hi[j] + x;
+                    bb = s - hi[j];
+                    e = (hi[j] - (s - bb)) + (x - bb);
+                    hi[j] = s;
+                    lo[j] += e;
+                }
+            }
+            tc_fence_before();
+            mbar_arrive(&tempty[buf]);
+        }
+        if (ok && row < rows && nkt > 0) {
+            double *out = C + (int64_t)split * ldc_split + row;
+#pragma unroll
+            for (int j = 0; j < BN; ++j) out[(int64_t)j * ldc_col] = (double)hi[j] + (double)lo[j];
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 1) {
+        tc_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM3_COLS));
+    }
+}
+
+// ---------------------------------------------------------------- host side
+
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                  const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static EncodeTiledFn encode_fn()
+{
+    static EncodeTiledFn fn = nullptr;
+    if (!fn) {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = (EncodeTiledFn)p;
+    }
+    return fn;
+}
+
+// 2D tensor map over a row-major [rows][cols] array of 16-bit values, box 64 cols x box_rows.
+static int make_map(CUtensorMap *tm, const void *base, int64_t rows, int64_t cols, int box_rows)
+{
+    EncodeTiledFn enc = encode_fn();
+    if (!enc) return set_error(FPDE_ERR_UNSUPPORTED, "cuTensorMapEncodeTiled is not available");
+    if ((cols * 2) % 16 != 0 || ((uintptr_t)base % 16) != 0)
+        return set_error(FPDE_ERR_ARG, "tensor map: row pitch and base must be 16-byte aligned");
+    cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
+    cuuint64_t strides[1] = {(cuuint64_t)(cols * 2)};
+    cuuint32_t box[2] = {(cuuint32_t)BK, (cuuint32_t)box_rows};
+    cuuint32_t es[2] = {1, 1};
+    CUresult r = enc(tm, CU_TENSOR_MAP_DATA_TYPE_UINT16, 2, const_cast<void *>(base), dims, strides, box, es,
+                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return set_error(FPDE_ERR_ARG, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+    return FPDE_OK;
+}
+
+}  // namespace tc
+
+int far_plan_init(FarPlan *p, const void *a_hi, const void *a_lo, int64_t rows, int64_t lda, const void *w_hi,
+                  const void *w_lo, int64_t ldw, int bf16)
+{
+    if (rows % tc::BM != 0 || lda % tc::BK != 0 || ldw % tc::BK != 0)
+        return set_error(FPDE_ERR_ARG, "far contraction: rows must be a multiple of 128, pitches of 64");
+    static_assert(sizeof(tc::FarMaps) <= sizeof(p->maps), "map storage");
+    tc::FarMaps *m = (tc::FarMaps *)p->maps;
+    int rc;
+    if ((rc = tc::make_map(&m->a_hi, a_hi, rows, lda, tc::BM)) || (rc = tc::make_map(&m->a_lo, a_lo, rows, lda, tc::BM)) ||
+        (rc = tc::make_map(&m->w_hi, w_hi, tc::BN, ldw, tc::BN)) || (rc = tc::make_map(&m->w_lo, w_lo, tc::BN, ldw, tc::BN)))
+        return rc;
+    p->rows = rows;
+    p->idesc = tc::idesc_f16(bf16 ? 1 : 0, tc::BM, tc::BN);
+    static bool attr_set = false;
+    if (!attr_set) {
+        cudaError_t e = cudaFuncSetAttribute(tc::k_far_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, tc::SMEM_BYTES);
+        if (e != cudaSuccess) return set_error(FPDE_ERR_CUDA, "far kernel smem attribute: %s", cudaGetErrorString(e));
+        attr_set = true;
+    }
+    return FPDE_OK;
+}
+
+int far_plan3_init(FarPlan3 *p, const void *const a[3], int64_t rows, int64_t lda, const void *const w[3],
+                   int64_t ldw)
+{
+    if (rows % tc::BM != 0 || lda % tc::BK != 0 || ldw % tc::BK != 0)
+        return set_error(FPDE_ERR_ARG, "far contraction: rows must be a multiple of 128, pitches of 64");
+    static_assert(sizeof(tc::FarMaps3) <= sizeof(p->maps), "map storage");
+    tc::FarMaps3 *m = (tc::FarMaps3 *)p->maps;
+    int rc;
+    for (int q = 0; q < 3; ++q) {
+        if ((rc = tc::make_map(&m->a[q], a[q], rows, lda, tc::BM))) return rc;
+        if ((rc = tc::make_map(&m->w[q], w[q], tc::BN, ldw, tc::BN))) return rc;
+    }
+    p->rows = rows;
+    p->idesc = tc::idesc_f16(1, tc::BM, tc::BN);
+    static bool attr_set = false;
+    if (!attr_set) {
+        cudaError_t e = cudaFuncSetAttribute(tc::k_far_tc3, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             tc::SMEM3_BYTES);
+        if (e != cudaSuccess) return set_error(FPDE_ERR_CUDA, "far kernel smem attribute: %s", cudaGetErrorString(e));
+        attr_set = true;
+    }
+    return FPDE_OK;
+}
+
+int far3_launch(cudaStream_t st, const FarPlan3 *p, int k_cols, double *C, int64_t ldc_split, int64_t ldc_col,
+                int splits, const int8_t *pA, const int8_t *pW, int64_t ldp, unsigned *flags)
+{
+    if (k_cols % tc::BK != 0) return set_error(FPDE_ERR_ARG, "far contraction: K must be a multiple of 64");
+    if (k_cols == 0) return FPDE_OK;
+    const int kt_total = k_cols / tc::BK;
+    if (splits < 1) splits = 1;
+    if (splits > FAR_MAX_SPLITS) splits = FAR_MAX_SPLITS;
+    const int kt_per = (kt_total + splits - 1) / splits;
+    splits = (kt_total + kt_per - 1) / kt_per;
+    dim3 grid((unsigned)(p->rows / tc::BM), (unsigned)splits);
+    const tc::FarMaps3 *m = (const tc::FarMaps3 *)p->maps;
+    tc::k_far_tc3<<<grid, tc::THREADS, tc::SMEM3_BYTES, st>>>(*m, C, ldc_split, ldc_col, p->rows, kt_total, kt_per,
+                                                             p->idesc, pA, pW, ldp, flags);
+    FPDE_LAUNCHED(1);
+    return FPDE_OK;
+}
+
+int far_splits(int kt_total, int64_t rows)
+{
+    int64_t tiles = rows / tc::BM;
+    int s = 1;
+    while (s < FAR_MAX_SPLITS && tiles * s < 152 * 6 && kt_total / (s + 1) >= 8) ++s;
+    return s;
+}
+
+int far_launch(cudaStream_t st, const FarPlan *p, int k_cols, double *C, int64_t ldc_split, int64_t ldc_col,
+               int splits, double out_scale, const double *out_scale_ptr, unsigned *flags)
+{
+    if (k_cols % tc::BK != 0) return set_error(FPDE_ERR_ARG, "far contraction: K must be a multiple of 64");
+    if (k_cols == 0) return FPDE_OK;
+    const int kt_total = k_cols / tc::BK;
+    if (splits < 1) splits = 1;
+    if (splits > FAR_MAX_SPLITS) splits = FAR_MAX_SPLITS;
+    const int kt_per = (kt_total + splits - 1) / splits;
+    splits = (kt_total + kt_per - 1) / kt_per;
+    dim3 grid((unsigned)(p->rows / tc::BM), (unsigned)splits);
+    const tc::FarMaps *m = (const tc::FarMaps *)p->maps;
+    tc::k_far_tc<<<grid, tc::THREADS, tc::SMEM_BYTES, st>>>(*m, C, ldc_split, ldc_col, p->rows, kt_total, kt_per,
+                                                           p->idesc, out_scale, out_scale_ptr, flags);
+    FPDE_LAUNCHED(1);
+    return FPDE_OK;
+}
+
+}  // namespace fpde
+
+using namespace fpde;
+
+extern "C" int fpde_far_contract(fpde_ctx *ctx, const void *a_hi, const void *a_lo, int64_t rows, int64_t lda,
+                                 const void *w_hi, const void *w_lo, int64_t ldw, int k_cols, int bf16,
+                                 double out_scale, double *C, int splits)
+{
+    clear_error();
+    int rc = ctx_enter(ctx);
+    if (rc) return rc;
+    FPDE_CHECK_ARG(a_hi && a_lo && w_hi && w_lo && C && rows > 0 && k_cols >= 0, "bad arguments");
+    FPDE_CHECK_ARG(k_cols <= lda && k_cols <= ldw, "K beyond the operand pitch");
+    FarPlan plan;
+    if ((rc = far_plan_init(&plan, a_hi, a_lo, rows, lda, w_hi, w_lo, ldw, bf16))) return rc;
+    const int kt_total = k_cols / 64;
+    if (splits <= 0) splits = far_splits(kt_total, rows);
+    if ((rc = far_launch(ctx->stream, &plan, k_cols, C, rows * 64, rows, splits, out_scale, nullptr, ctx->d_flags)))
+        return rc;
+    FPDE_CUDA(cudaStreamSynchronize(ctx->stream));
+    return ctx_check_flags(ctx, "far contraction");
+}
+
+extern "C" int fpde_far_contract3(fpde_ctx *ctx, const void *const a[3], int64_t rows, int64_t lda,
+                                  const void *const w[3], int64_t ldw, int k_cols, const int8_t *pA,
+                                  const int8_t *pW, int64_t ldp, double *C, int splits)
+{
+    clear_error();
+    int rc = ctx_enter(ctx);
+    if (rc) return rc;
+    FPDE_CHECK_ARG(a && w && a[0] && a[1] && a[2] && w[0] && w[1] && w[2] && pA && pW && C, "null argument");
+    FPDE_CHECK_ARG(rows > 0 && k_cols >= 0 && k_cols <= lda && k_cols <= ldw && ldp * 64 >= k_cols, "bad shape");
+    FarPlan3 plan;
+    if ((rc = far_plan3_init(&plan, a, rows, lda, w, ldw))) return rc;
+    if (splits <= 0) splits = far_splits(k_cols / 64, rows);
+    if ((rc = far3_launch(ctx->stream, &plan, k_cols, C, rows * 64, rows, splits, pA, pW, ldp, ctx->d_flags)))
+        return rc;
+    FPDE_CUDA(cudaStreamSynchronize(ctx->stream));
+    return ctx_check_flags(ctx, "far contraction (three slices)");
+}

@@ -44,7 +44,10 @@ enum fpde_status {
 enum fpde_precision {
     FPDE_PREC_FP64 = 0,        /* FP64 increments, FP64 FMA sum (the plain method) */
     FPDE_PREC_SPLIT_BF16 = 1,  /* far history as bf16 hi+lo on tensor cores, FP64 fold */
-    FPDE_PREC_SPLIT_F16 = 2    /* same with fp16 hi+lo (per-node power-of-two scaling) */
+    FPDE_PREC_SPLIT_F16 = 2,   /* same with fp16 hi+lo (per-block power-of-two scaling) */
+    FPDE_PREC_SPLIT_BF16X3 = 3 /* far history as three exact bf16 slices (8-bit integers with
+                                  per-node/per-block exponents), six products per k-step, leading
+                                  product summed exactly; FP64 fold */
 };
 
 /* Boundary condition kinds of a line end (al1 :4002-4027, bt1 :4585, U1 :4683-4719). */
@@ -144,6 +147,29 @@ int fpde_sum_snapshots(fpde_ctx *ctx, double *S, const double *old, int old_size
 int fpde_l1_sum_noalloc(const double *D, int n, int64_t P, int64_t nodes, const double *w,
                         double *S, void *stream);
 
+/* Far-history contraction of the split-precision path, on the tensor cores:
+ *   C[s][j][i] = out_scale * sum_{t in split s} (Ah[i][t] Wh[j][t] + Ah[i][t] Wl[j][t] + Al[i][t] Wh[j][t])
+ * for j < 64, with FP32 accumulation folded into float-float every 256 columns and FP64
+ * partial sums per K split s (C is splits x 64 x rows doubles, device). Ah/Al are
+ * [rows][lda] and Wh/Wl [64][ldw] 16-bit arrays in device memory (fp16, or bf16 when
+ * bf16 != 0); rows % 128 == 0, lda and ldw % 64 == 0, k_cols % 64 == 0 and <= both pitches.
+ * splits <= 0 picks a split count (at most 4). This replaces the reference's mode-1
+ * far-history tile product (DOC kernel, fr_do.cpp:173-235, wmma 16x16x16 half/float). */
+int fpde_far_contract(fpde_ctx *ctx, const void *a_hi, const void *a_lo, int64_t rows, int64_t lda,
+                      const void *w_hi, const void *w_lo, int64_t ldw, int k_cols, int bf16,
+                      double out_scale, double *C, int splits);
+
+/* Exact-slice form of the far contraction: operands as three bf16 slices each
+ * (A[i][t] = (a0 + a1 + a2)[i][t] * 2^pA[i][t/64], W[j][t] = (w0 + w1 + w2)[j][t] * 2^pW[j][t/64],
+ * a0/w0 integers |.| <= 256, a1/w1 multiples of 2^-8 and a2/w2 of 2^-16 with at most 8
+ * significant bits), int8 exponents pA [rows][ldp] and pW [64][ldp];
+ *   C[s][j][i] = sum_{t in split s} A[i][t] W[j][t]   (partials, FP64, device)
+ * with the leading products a0*w0 summed exactly per 64 columns and everything folded in
+ * float-float. Same shape rules as fpde_far_contract. Replaces the same reference code. */
+int fpde_far_contract3(fpde_ctx *ctx, const void *const a[3], int64_t rows, int64_t lda,
+                       const void *const w[3], int64_t ldw, int k_cols, const int8_t *pA,
+                       const int8_t *pW, int64_t ldp, double *C, int splits);
+
 /* ----------------------------------------------------- tridiagonal solves */
 
 /* Batched Thomas solves of n_lines independent lines (al1 / bt1 / back-substitution,
@@ -200,14 +226,15 @@ int fpde_line_solve_host(fpde_line *line, const double *u0_host, int steps, doub
 int fpde_line_steps_done(const fpde_line *line, int64_t *n);
 /* Kernel timing probes (no counterpart in the reference, which times whole calls with
  * clock_gettime, opencl_cuda_base.cpp:708-716): with every > 0, later runs record CUDA
- * events around the history-sum and solve kernels of every `every`-th step, inside the
- * captured graph. fpde_line_probe_stats returns, for the last run, the summed event times
- * (ms) of the probed history-sum launches and of the probed solve launches, the summed
- * algorithmic bytes of the probed history-sum launches (8 * rows * (N+1) FP64 reads) and
- * the number of probed steps. */
+ * events inside the captured graph around the history-sum and solve kernels of every
+ * `every`-th step and around every far-history contraction. fpde_line_probe_stats returns,
+ * for the last run and one kind of kernel (0 FP64 history GEMV, 1 tensor-core far
+ * contraction, 2 line solve), the summed event time (ms), the summed algorithmic bytes
+ * (GEMV: 8 * rows * (N+1); contraction: 4 * rows * (N+1) of hi/lo history), the summed
+ * algorithmic flops and the number of probed launches. */
 int fpde_line_set_probe(fpde_line *line, int every);
-int fpde_line_probe_stats(fpde_line *line, double *hist_ms, double *hist_bytes, double *solve_ms,
-                          int *probes);
+int fpde_line_probe_stats(fpde_line *line, int kind, double *ms, double *bytes, double *flops,
+                          int *count);
 
 /* Line coefficients of the H equation with gamma = 1 (A_ / B / R, fpde_hpc_1d.cpp:3095-3142):
  * A[i] = k[i-1] iw[i]/(dL[i] dL[i-1]), B[i] = k[i] iw[i]/dL[i]^2,
