@@ -17,18 +17,20 @@
 // The Thomas solve of a long line runs on all SMs. The alpha recurrence
 // Al[i+1] = B/(R - A Al[i]) is time-invariant (uniform tau) and is done once on the host;
 // per step only the two first-order recurrences remain,
-//   forward   Bt[i+1] = g_i (A_i Bt[i] - Om_i),      g_i = Al[i+1]/B_i
-//   backward  U_i     = Al[i+1] U_{i+1} + Bt[i+1],
-// each an affine scan x_i = p_i x_{i-1} + r_i. Every thread runs its segment of SP nodes
-// sequentially from zero, segments are combined by warp-shuffle scans of (P, X) pairs, then
-// across warps through shared memory, then across CTAs through a bounded grid barrier;
-// finally each node adds (prefix product) x (carry), with the within-segment prefix products
-// of p and Al precomputed once (cf, cb). The history sums and the state are read in a
-// coalesced pattern first and handed to the segment layout through shared memory.
+//   forward   y_i = Bt[i+1] = g_i (A_i y_{i-1} - Om_i),   g_i = Al[i+1]/B_i
+//   backward  U_i = Al[i+1] U_{i+1} + y_i.
+// Each CTA owns a chunk of nodes and solves both recurrences inside it from zero carries:
+// threads sweep segments of SP nodes sequentially, segments are joined by warp-shuffle
+// scans of (product, value) pairs and across warps through shared memory. Because the
+// recurrences are linear, the true solution is U = U^cta + c_in GG + u_b CB, with GG and CB
+// time-invariant per node. After one bounded grid barrier, warp 0 of every CTA solves the
+// two short chunk-level recurrences for all carries (c_in forward, u_b backward) from the
+// chunks' published end values, and every node takes two FMAs to finish.
 #include <map>
 #include <vector>
 #include <cmath>
 #include <cstring>
+#include <algorithm>
 
 #include "common.cuh"
 #include "kernels.cuh"
@@ -36,24 +38,27 @@
 
 namespace fpde {
 
-constexpr int LT = 128;      // threads per CTA of the line solve
+constexpr int LT = 256;      // threads per CTA of the line solve
 constexpr int LSEG = 8;      // max nodes per thread
 constexpr int BLK = 64;      // steps per block of the split path (= tensor-core N)
 constexpr unsigned FULL = 0xffffffffu;
 
 struct LineSolveArgs {
-    const double *A, *g, *al, *cf, *cb;   // time-invariant, indexed by node 0..N-1
+    const double *A, *g, *al, *cf, *cb;   // per node: coefficients, thread-segment products
+    const double *CF, *CB, *GG;           // per node: chunk-level forward/backward data
     const double *src;                    // optional source (N+1), may be null
     double *U;                            // state (N+1)
-    double *Drow;                         // increment row of this step (P)
+    double *Drow;                         // increment of node i goes to Drow[i * dstride]
+    int64_t dstride;
     const double *part;                   // S += sum_{q<KS} part[q*pstride + i]
     int64_t pstride;
-    const double *ring;                   // S += sum_{r<nr} wn[r] * ring[r*P + i]
+    const double *ring;                   // S += sum_{r<nr} wn[r] * ring[i*64 + r]   (node-major)
     const double *wn;
-    double *aggf, *aggb;                  // [G][2] CTA aggregates
-    double *UN;                           // right boundary value slot
+    double *agg;                          // [G][2] (chunk's last y, chunk's first u), agg[2G] = old U[N-1]
+    unsigned long long *cflag;            // per chunk: launch sequence number of its published values
+    unsigned long long *seq;              // launch sequence counter (read at start, advanced by CTA 0)
+    const double *Lf, *Mb, *Kb, *mb;      // chunk-carry rows: c_in = Lf Y, u_b = Mb U0 + Kb Y + mb U_N
     unsigned *barrier, *flags;
-    int64_t P;
     double lam, g0, gN, dLN, AlN;
     int KS, nr, N, G, rkind;
 };
@@ -75,208 +80,277 @@ __device__ __forceinline__ void warp_scan_down(double &P, double &X, int lane)
     }
 }
 
-// Carry into CTA c from the aggregates of the CTAs before it (forward, from carry 0)
-// or after it (backward, from carry `init`). Executed by warp 0; returns the carry.
-__device__ __forceinline__ double grid_carry(const double *agg, int G, int c, bool forward, double init, int lane)
+__device__ __forceinline__ unsigned long long gtimer_ns()
 {
-    int lo = forward ? 0 : c + 1, hi = forward ? c : G;          // CTAs [lo, hi)
-    int cnt = hi - lo;
-    int m = (cnt + 31) / 32;
-    double P = 1.0, X = 0.0;
-    if (forward) {
-        for (int k = 0; k < m; ++k) {                             // lane's range in order
-            int cc = lo + lane * m + k;
-            if (cc < hi) { double Pc = __ldcg(agg + 2 * cc), Xc = __ldcg(agg + 2 * cc + 1); X = fma(Pc, X, Xc); P *= Pc; }
-        }
-        warp_scan_up(P, X, lane);
-        double Pt = __shfl_sync(FULL, P, 31), Xt = __shfl_sync(FULL, X, 31);
-        return fma(Pt, init, Xt);
-    } else {
-        for (int k = m - 1; k >= 0; --k) {                        // descending
-            int cc = lo + lane * m + k;
-            if (cc < hi) { double Pc = __ldcg(agg + 2 * cc), Xc = __ldcg(agg + 2 * cc + 1); X = fma(Pc, X, Xc); P *= Pc; }
-        }
-        warp_scan_down(P, X, lane);
-        double Pt = __shfl_sync(FULL, P, 0), Xt = __shfl_sync(FULL, X, 0);
-        return fma(Pt, init, Xt);
-    }
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
 }
 
 template <int SP>
+__device__ __forceinline__ double right_value(const LineSolveArgs &p, double BtN, double uNm1)
+{
+    if (p.rkind == FPDE_BC_DIRICHLET) return p.gN;
+    if (fabs(BtN) > 1e-15) return (fabs(1.0 - p.AlN) > 1e-15) ? (BtN + p.gN * p.dLN) / (1.0 - p.AlN) : uNm1;
+    return (fabs(1.0 - p.AlN) > 1e-15) ? 0.0 : uNm1;
+}
+
+// One time step of a line: history sum -> right-hand side -> Thomas solve -> U, increment.
+// Each CTA owns a chunk [a, b) of nodes and solves it with zero carries in both sweeps
+// (y^cta, u^cta). The true solution is u = u^cta + c_in * GG + u_b * CB with the chunk's
+// forward carry c_in and backward carry u_b; after one grid barrier, warp 0 of every CTA
+// resolves all chunk carries from two published numbers per chunk.
+template <int SP>
 __global__ void __launch_bounds__(LT) k_line_solve(LineSolveArgs p)
 {
-    __shared__ double sh_om[LT * SP], sh_u[LT * SP];
-    __shared__ double wP[LT / 32], wX[LT / 32], wPe[LT / 32], wXe[LT / 32];
-    __shared__ double s_carry, s_UN;
+    constexpr int NW = LT / 32;
+    __shared__ double wP[NW], wX[NW], wPe[NW], wXe[NW];
+    __shared__ double s_cin, s_ub, s_UN;
+    __shared__ unsigned long long s_seq;
+    __shared__ int s_abort;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int c = blockIdx.x;
-    const int base = c * LT * SP;
+    if (tid == 0) s_seq = *((volatile unsigned long long *)p.seq) + 1;
+    const int a = c * LT * SP;
+    const int b = min(a + LT * SP, p.N);
+    const int i0 = a + tid * SP;
+    const int i1 = min(i0 + SP, p.N);
+    const int cnt = max(0, i1 - i0);
 
-    // ---- phase 0 (coalesced): history sum, right-hand side, state -> shared memory
-    {
-        double acc[SP], acc2[SP], uu[SP];
+    // ---- warp 0: the time-invariant chunk-carry rows of this chunk (used after the gather)
+    double lf[5], lfN[5], mbv[5], kbv[5], mbc = 0.0;
+    if (warp == 0) {
+        const int G = p.G;
 #pragma unroll
-        for (int k = 0; k < SP; ++k) { acc[k] = 0.0; acc2[k] = 0.0; uu[k] = 0.0; }
-#pragma unroll
-        for (int k = 0; k < SP; ++k) {
-            const int i = base + k * LT + tid;
-            if (i < p.N) uu[k] = p.U[i];
+        for (int t = 0; t < 5; ++t) {
+            const int q = lane + 32 * t;
+            const bool in = q < G;
+            lf[t] = in ? __ldg(p.Lf + (int64_t)c * G + q) : 0.0;
+            lfN[t] = in ? __ldg(p.Lf + (int64_t)G * G + q) : 0.0;
+            mbv[t] = in ? __ldg(p.Mb + (int64_t)c * G + q) : 0.0;
+            kbv[t] = in ? __ldg(p.Kb + (int64_t)c * G + q) : 0.0;
         }
-        for (int q = 0; q < p.KS; ++q) {
+        mbc = __ldg(p.mb + c);
+    }
+    // ---- every per-node input of the step in one round of loads
+    double uo[SP], om[SP], kA[SP], kg[SP], kal[SP], kcf[SP], kcb[SP], kCB[SP], kGG[SP];
+#pragma unroll
+    for (int k = 0; k < SP; ++k) {
+        const bool in = k < cnt;
+        const int i = in ? i0 + k : 0;
+        uo[k] = in ? p.U[i] : 0.0;
+        kA[k] = in ? __ldg(p.A + i) : 0.0;
+        kg[k] = in ? __ldg(p.g + i) : 0.0;
+        kal[k] = in ? __ldg(p.al + i) : 0.0;
+        kcf[k] = in ? __ldg(p.cf + i) : 1.0;
+        kcb[k] = in ? __ldg(p.cb + i) : 1.0;
+        kCB[k] = in ? __ldg(p.CB + i) : 0.0;
+        kGG[k] = in ? __ldg(p.GG + i) : 0.0;
+        om[k] = 0.0;
+    }
+    if (p.KS > 0) {                                                  // FP64 partials, 4-way ILP
+        double a0[SP], a1[SP], a2[SP], a3[SP];
+#pragma unroll
+        for (int k = 0; k < SP; ++k) { a0[k] = 0.0; a1[k] = 0.0; a2[k] = 0.0; a3[k] = 0.0; }
+        int q = 0;
+        for (; q + 4 <= p.KS; q += 4) {
 #pragma unroll
             for (int k = 0; k < SP; ++k) {
-                const int i = base + k * LT + tid;
-                if (i < p.N) acc[k] += __ldcg(p.part + (int64_t)q * p.pstride + i);
-            }
-        }
-        int r = 0;
-        for (; r + 2 <= p.nr; r += 2) {
-            const double w0 = __ldg(p.wn + r), w1 = __ldg(p.wn + r + 1);
-#pragma unroll
-            for (int k = 0; k < SP; ++k) {
-                const int i = base + k * LT + tid;
-                if (i < p.N) {
-                    acc[k] = fma(w0, __ldcg(p.ring + (int64_t)r * p.P + i), acc[k]);
-                    acc2[k] = fma(w1, __ldcg(p.ring + (int64_t)(r + 1) * p.P + i), acc2[k]);
+                if (k < cnt) {
+                    const double *pp = p.part + (int64_t)q * p.pstride + i0 + k;
+                    a0[k] += __ldcg(pp);
+                    a1[k] += __ldcg(pp + p.pstride);
+                    a2[k] += __ldcg(pp + 2 * p.pstride);
+                    a3[k] += __ldcg(pp + 3 * p.pstride);
                 }
             }
         }
-        if (r < p.nr) {
-            const double w0 = __ldg(p.wn + r);
+        for (; q < p.KS; ++q) {
+#pragma unroll
+            for (int k = 0; k < SP; ++k)
+                if (k < cnt) a0[k] += __ldcg(p.part + (int64_t)q * p.pstride + i0 + k);
+        }
+#pragma unroll
+        for (int k = 0; k < SP; ++k) om[k] = (a0[k] + a1[k]) + (a2[k] + a3[k]);
+    }
+    if (p.nr > 0) {                                                  // FP64 near history, 4-way ILP
+        double a0[SP], a1[SP], a2[SP], a3[SP];
+#pragma unroll
+        for (int k = 0; k < SP; ++k) { a0[k] = 0.0; a1[k] = 0.0; a2[k] = 0.0; a3[k] = 0.0; }
+        int r = 0;
+        for (; r + 4 <= p.nr; r += 4) {
+            const double w0 = __ldg(p.wn + r), w1 = __ldg(p.wn + r + 1), w2 = __ldg(p.wn + r + 2),
+                         w3 = __ldg(p.wn + r + 3);
 #pragma unroll
             for (int k = 0; k < SP; ++k) {
-                const int i = base + k * LT + tid;
-                if (i < p.N) acc[k] = fma(w0, __ldcg(p.ring + (int64_t)r * p.P + i), acc[k]);
+                if (k < cnt) {
+                    const double2 *rp = (const double2 *)(p.ring + (int64_t)(i0 + k) * 64 + r);
+                    const double2 v = __ldg(rp), v2 = __ldg(rp + 1);
+                    a0[k] = fma(w0, v.x, a0[k]);
+                    a1[k] = fma(w1, v.y, a1[k]);
+                    a2[k] = fma(w2, v2.x, a2[k]);
+                    a3[k] = fma(w3, v2.y, a3[k]);
+                }
             }
         }
+        for (; r < p.nr; ++r) {
+            const double w0 = __ldg(p.wn + r);
 #pragma unroll
-        for (int k = 0; k < SP; ++k) {
-            const int i = base + k * LT + tid;
-            const double S = acc[k] + acc2[k];
-            sh_u[k * LT + tid] = uu[k];
-            sh_om[k * LT + tid] = (-(p.lam * uu[k]) + (p.src && i < p.N ? p.src[i] : 0.0)) + S;
+            for (int k = 0; k < SP; ++k)
+                if (k < cnt) a0[k] = fma(w0, __ldg(p.ring + (int64_t)(i0 + k) * 64 + r), a0[k]);
         }
+#pragma unroll
+        for (int k = 0; k < SP; ++k) om[k] += (a0[k] + a1[k]) + (a2[k] + a3[k]);
     }
-    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < SP; ++k)
+        om[k] = (-(p.lam * uo[k]) + (p.src && k < cnt ? p.src[i0 + k] : 0.0)) + om[k];
 
-    const int i0 = base + tid * SP;
-    const int i1 = min(i0 + SP, p.N);
-    const int cnt = max(0, i1 - i0);
-    double uo[SP], y[SP];
-    // ---- forward: local sweep from zero
-    double yl = 0.0, ulast = 0.0;
+    // ---- forward sweep of the chunk from zero carry
+    double y[SP];
+    double yl = 0.0;
 #pragma unroll
     for (int k = 0; k < SP; ++k) {
         if (k < cnt) {
             const int i = i0 + k;
-            uo[k] = sh_u[tid * SP + k];
-            ulast = uo[k];
-            if (i == 0) yl = p.g0;                                 // Bt[1]
-            else yl = p.g[i] * (p.A[i] * yl - sh_om[tid * SP + k]);
+            if (i == 0) yl = p.g0;                                  // Bt[1]
+            else yl = kg[k] * (kA[k] * yl - om[k]);
             y[k] = yl;
         }
     }
-    double P = cnt > 0 ? p.cf[i1 - 1] : 1.0, X = cnt > 0 ? yl : 0.0;
+    double P = 1.0, X = cnt > 0 ? yl : 0.0;
+#pragma unroll
+    for (int k = 0; k < SP; ++k)
+        if (k < cnt) P = kcf[k];
     warp_scan_up(P, X, lane);
     double Pe = __shfl_up_sync(FULL, P, 1), Xe = __shfl_up_sync(FULL, X, 1);
     if (lane == 0) { Pe = 1.0; Xe = 0.0; }
     if (lane == 31) { wP[warp] = P; wX[warp] = X; }
     __syncthreads();
     if (warp == 0) {
-        double Pw = lane < LT / 32 ? wP[lane] : 1.0, Xw = lane < LT / 32 ? wX[lane] : 0.0;
+        double Pw = lane < NW ? wP[lane] : 1.0, Xw = lane < NW ? wX[lane] : 0.0;
         warp_scan_up(Pw, Xw, lane);
         double Pwe = __shfl_up_sync(FULL, Pw, 1), Xwe = __shfl_up_sync(FULL, Xw, 1);
         if (lane == 0) { Pwe = 1.0; Xwe = 0.0; }
-        if (lane < LT / 32) { wPe[lane] = Pwe; wXe[lane] = Xwe; }
-        if (lane == LT / 32 - 1 && p.G > 1) { p.aggf[2 * c] = Pw; p.aggf[2 * c + 1] = Xw; __threadfence(); }
-    }
-    if (p.G > 1) {
-        if (!grid_barrier(p.barrier, p.G, p.flags)) return;
-        if (warp == 0) {
-            double cc = grid_carry(p.aggf, p.G, c, true, 0.0, lane);
-            if (lane == 0) s_carry = cc;
-        }
-    } else if (tid == 0) {
-        s_carry = 0.0;
+        if (lane < NW) { wPe[lane] = Pwe; wXe[lane] = Xwe; }
     }
     __syncthreads();
     {
-        const double carry_w = fma(wPe[warp], s_carry, wXe[warp]);
-        const double carry = fma(Pe, carry_w, Xe);
+        const double carry = fma(Pe, wXe[warp], Xe);               // chunk carry-in taken as 0
 #pragma unroll
         for (int k = 0; k < SP; ++k)
-            if (k < cnt) { y[k] = fma(p.cf[i0 + k], carry, y[k]); yl = y[k]; }
+            if (k < cnt) y[k] = fma(kcf[k], carry, y[k]);
     }
-    // ---- right boundary value (owner of node N-1)
-    if (cnt > 0 && i1 == p.N) {
-        const double BtN = yl, uNm1 = ulast;
-        double UN;
-        if (p.rkind == FPDE_BC_DIRICHLET) {
-            UN = p.gN;
-        } else if (fabs(BtN) > 1e-15) {
-            UN = (fabs(1.0 - p.AlN) > 1e-15) ? (BtN + p.gN * p.dLN) / (1.0 - p.AlN) : uNm1;
-        } else {
-            UN = (fabs(1.0 - p.AlN) > 1e-15) ? 0.0 : uNm1;
-        }
-        if (p.G > 1) { *p.UN = UN; __threadfence(); }
-        s_UN = UN;
-        const double uNold = p.U[p.N];
-        p.U[p.N] = UN;
-        p.Drow[p.N] = UN - uNold;
-    }
-    // ---- backward: local sweep from zero, descending
+    // ---- backward sweep of the chunk from zero carry
     double ub[SP];
     double ul = 0.0;
 #pragma unroll
     for (int k = SP - 1; k >= 0; --k) {
         if (k < cnt) {
-            ul = fma(p.al[i0 + k], ul, y[k]);
+            ul = fma(kal[k], ul, y[k]);
             ub[k] = ul;
         }
     }
-    P = cnt > 0 ? p.cb[i0] : 1.0;
+    P = cnt > 0 ? kcb[0] : 1.0;
     X = cnt > 0 ? ul : 0.0;
     warp_scan_down(P, X, lane);
     Pe = __shfl_down_sync(FULL, P, 1);
     Xe = __shfl_down_sync(FULL, X, 1);
     if (lane == 31) { Pe = 1.0; Xe = 0.0; }
-    __syncthreads();                                    // wP/wX reuse
+    __syncthreads();                                                // wP/wX reuse
     if (lane == 0) { wP[warp] = P; wX[warp] = X; }
     __syncthreads();
     if (warp == 0) {
-        constexpr int NW = LT / 32;
         double Pw = lane < NW ? wP[lane] : 1.0, Xw = lane < NW ? wX[lane] : 0.0;
-        warp_scan_down(Pw, Xw, lane);                   // suffix scan over warps
+        warp_scan_down(Pw, Xw, lane);
         double Pwe = __shfl_down_sync(FULL, Pw, 1), Xwe = __shfl_down_sync(FULL, Xw, 1);
         if (lane >= NW - 1) { Pwe = 1.0; Xwe = 0.0; }
         if (lane < NW) { wPe[lane] = Pwe; wXe[lane] = Xwe; }
-        if (lane == 0 && p.G > 1) { p.aggb[2 * c] = Pw; p.aggb[2 * c + 1] = Xw; __threadfence(); }
-    }
-    if (p.G > 1) {
-        if (!grid_barrier(p.barrier, p.G, p.flags)) return;
-        if (warp == 0) {
-            const double UN = __ldcg(p.UN);
-            double cc = grid_carry(p.aggb, p.G, c, false, UN, lane);
-            if (lane == 0) s_carry = cc;
-        }
-    } else {
-        __syncthreads();
-        if (tid == 0) s_carry = s_UN;
     }
     __syncthreads();
     {
-        const double carry_w = fma(wPe[warp], s_carry, wXe[warp]);
-        const double carry = fma(Pe, carry_w, Xe);
+        const double carry = fma(Pe, wXe[warp], Xe);
 #pragma unroll
-        for (int k = 0; k < SP; ++k) {
-            if (k < cnt) {
-                const int i = i0 + k;
-                const double un = fma(p.cb[i], carry, ub[k]);
-                p.U[i] = un;
-                p.Drow[i] = un - uo[k];
+        for (int k = 0; k < SP; ++k)
+            if (k < cnt) ub[k] = fma(kcb[k], carry, ub[k]);
+    }
+    // ---- publish the chunk's last y and first u (and the old U[N-1])
+    if (cnt > 0 && i1 == b) {
+        double ylast = 0.0, ulast = 0.0;
+#pragma unroll
+        for (int k = 0; k < SP; ++k)
+            if (k < cnt) { ylast = y[k]; ulast = uo[k]; }
+        p.agg[2 * c] = ylast;
+        if (b == p.N) p.agg[2 * p.G] = ulast;
+    }
+    if (cnt > 0 && i0 == a) p.agg[2 * c + 1] = ub[0];
+    __syncthreads();
+    if (tid == 0 && p.G > 1) {
+        __threadfence();
+        asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p.cflag + c), "l"(s_seq) : "memory");
+    }
+    // ---- warp 0: wait for every chunk, then this chunk's carries by three dot products
+    if (warp == 0) {
+        const int G = p.G;
+        bool ok = true;
+        if (G > 1) {
+            const unsigned long long t0 = gtimer_ns();
+#pragma unroll
+            for (int t = 0; t < 5; ++t) {
+                const int q = lane + 32 * t;
+                if (q < G && ok) {
+                    unsigned long long f;
+                    while (true) {
+                        asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(f) : "l"(p.cflag + q) : "memory");
+                        if (f >= s_seq) break;
+                        if (gtimer_ns() - t0 > 1000000000ull) { ok = false; break; }
+                    }
+                }
             }
         }
+        ok = __all_sync(FULL, ok);
+        if (!ok) {
+            if (lane == 0) { atomicOr(p.flags, DEVERR_BARRIER_TIMEOUT); s_abort = 1; }
+        } else {
+            double sc = 0.0, syN = 0.0, sub = 0.0;
+#pragma unroll
+            for (int t = 0; t < 5; ++t) {
+                const int q = lane + 32 * t;
+                if (q < G) {
+                    const double ye = __ldcg(p.agg + 2 * q), u0 = __ldcg(p.agg + 2 * q + 1);
+                    sc = fma(lf[t], ye, sc);
+                    syN = fma(lfN[t], ye, syN);
+                    sub = fma(mbv[t], u0, fma(kbv[t], ye, sub));
+                }
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                sc += __shfl_xor_sync(FULL, sc, o);
+                syN += __shfl_xor_sync(FULL, syN, o);
+                sub += __shfl_xor_sync(FULL, sub, o);
+            }
+            const double UN = right_value<SP>(p, syN, __ldcg(p.agg + 2 * G));
+            if (lane == 0) { s_cin = sc; s_ub = fma(mbc, UN, sub); s_UN = UN; s_abort = 0; }
+        }
     }
+    __syncthreads();
+    if (s_abort) return;
+    const double cin = s_cin, ubv = s_ub;
+#pragma unroll
+    for (int k = 0; k < SP; ++k) {
+        if (k < cnt) {
+            const int i = i0 + k;
+            const double un = fma(kCB[k], ubv, fma(kGG[k], cin, ub[k]));
+            p.U[i] = un;
+            p.Drow[(int64_t)i * p.dstride] = un - uo[k];
+        }
+    }
+    if (cnt > 0 && i1 == p.N) {
+        const double UN = s_UN, uNold = p.U[p.N];
+        p.U[p.N] = UN;
+        p.Drow[(int64_t)p.N * p.dstride] = UN - uNold;
+    }
+    if (c == 0 && tid == 0) *((volatile unsigned long long *)p.seq) = s_seq;   // all CTAs have read it
 }
 
 }  // namespace fpde
@@ -291,8 +365,11 @@ struct fpde_line {
     bool split = false;
     double lam = 0, lamR = 0, kkk0 = 0, AlN = 0;
     double *A = nullptr, *g = nullptr, *al = nullptr, *cf = nullptr, *cb = nullptr;
+    double *CF = nullptr, *CB = nullptr, *GG = nullptr;
+    double *Lf = nullptr, *Mb = nullptr, *Kb = nullptr, *mb = nullptr;
+    unsigned long long *cflag = nullptr, *seq = nullptr;
     double *U = nullptr, *D = nullptr, *part = nullptr, *wrev = nullptr;
-    double *aggf = nullptr, *aggb = nullptr, *UN = nullptr;
+    double *agg = nullptr;
     unsigned *barrier = nullptr;
     // split path
     int64_t rows16 = 0, ld16 = 0;
@@ -328,14 +405,16 @@ static cudaError_t launch_solve_sp(const cudaLaunchConfig_t &cfg, const LineSolv
 }
 
 static int line_launch_solve(fpde_line *L, cudaStream_t st, const double *part, int KS, int64_t pstride,
-                             const double *ring, const double *wn, int nr, double *Drow)
+                             const double *ring, const double *wn, int nr, double *Drow, int64_t dstride)
 {
     LineSolveArgs a;
     a.A = L->A; a.g = L->g; a.al = L->al; a.cf = L->cf; a.cb = L->cb; a.src = nullptr;
-    a.U = L->U; a.Drow = Drow; a.part = part; a.pstride = pstride; a.ring = ring; a.wn = wn;
-    a.aggf = L->aggf; a.aggb = L->aggb; a.UN = L->UN;
+    a.CF = L->CF; a.CB = L->CB; a.GG = L->GG;
+    a.Lf = L->Lf; a.Mb = L->Mb; a.Kb = L->Kb; a.mb = L->mb; a.cflag = L->cflag; a.seq = L->seq;
+    a.U = L->U; a.Drow = Drow; a.dstride = dstride; a.part = part; a.pstride = pstride; a.ring = ring; a.wn = wn;
+    a.agg = L->agg;
     a.barrier = L->barrier; a.flags = L->ctx->d_flags;
-    a.P = L->P; a.lam = L->lam; a.g0 = L->d.left_value; a.gN = L->d.right_value; a.dLN = L->d.dLN;
+    a.lam = L->lam; a.g0 = L->d.left_value; a.gN = L->d.right_value; a.dLN = L->d.dLN;
     a.AlN = L->AlN; a.KS = KS; a.nr = nr; a.N = (int)L->N; a.G = L->G; a.rkind = L->d.right_kind;
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(L->G);
@@ -392,7 +471,7 @@ static int line_enqueue(fpde_line *L, cudaStream_t st, int64_t n0, int steps, in
             }
             ev = probe_step ? probe_begin(L, 2, n, 0.0, 0.0) : nullptr;
             PROBE_REC(ev, 0);
-            if ((rc = line_launch_solve(L, st, L->part, KS, L->P, nullptr, nullptr, 0, L->D + n * L->P))) return rc;
+            if ((rc = line_launch_solve(L, st, L->part, KS, L->P, nullptr, nullptr, 0, L->D + n * L->P, 1))) return rc;
             PROBE_REC(ev, 1);
             ++k;
         } else {
@@ -438,7 +517,7 @@ static int line_enqueue(fpde_line *L, cudaStream_t st, int64_t n0, int steps, in
             ev = probe_step ? probe_begin(L, 2, n, 0.0, 0.0) : nullptr;
             PROBE_REC(ev, 0);
             if ((rc = line_launch_solve(L, st, L->cfar + (int64_t)j * L->P, splits, (int64_t)BLK * L->P, L->ring, wn,
-                                        j, L->ring + (int64_t)j * L->P)))
+                                        j, L->ring + j, BLK)))
                 return rc;
             PROBE_REC(ev, 1);
             ++k;
@@ -475,8 +554,10 @@ int fpde_line_destroy(fpde_line *L)
     }
     for (auto &kv : L->graphs) cudaGraphExecDestroy(kv.second);
     for (cudaEvent_t e : L->probe_ev) cudaEventDestroy(e);
-    for (double *p : {L->A, L->g, L->al, L->cf, L->cb, L->U, L->D, L->part, L->wrev, L->aggf, L->aggb, L->UN,
-                      L->ring, L->cfar, L->wlag, L->out_scale})
+    dev_free(L->cflag);
+    dev_free(L->seq);
+    for (double *p : {L->A, L->g, L->al, L->cf, L->cb, L->CF, L->CB, L->GG, L->Lf, L->Mb, L->Kb, L->mb, L->U, L->D,
+                      L->part, L->wrev, L->agg, L->ring, L->cfar, L->wlag, L->out_scale})
         dev_free(p);
     for (uint16_t *p : {L->h_hi, L->h_lo, L->w_hi, L->w_lo, L->h3[0], L->h3[1], L->h3[2], L->w3[0], L->w3[1],
                         L->w3[2]})
@@ -511,17 +592,20 @@ int fpde_line_create(fpde_ctx *ctx, const fpde_line_desc *desc, const double *A,
     FPDE_CHECK_ARG(d.precision == FPDE_PREC_FP64 || d.block == 0 || d.block == BLK,
                    "split path: block must be 0 (auto) or 64");
     const int64_t N = d.N;
-    // partition of nodes 0..N-1 over G CTAs x LT threads x s nodes (s a power of two)
-    int G = (int)((N + (int64_t)LT * 4 - 1) / ((int64_t)LT * 4));
-    if (G > ctx->sm_count) G = ctx->sm_count;
-    if (G < 1) G = 1;
-    int64_t s = (N + (int64_t)G * LT - 1) / ((int64_t)G * LT);
-    if (s > LSEG)
-        return set_error(FPDE_ERR_UNSUPPORTED, "line of %lld intervals exceeds %lld (SMs x %d x %d)", (long long)N,
-                         (long long)ctx->sm_count * LT * LSEG, LT, LSEG);
-    int sp = 1;
-    while (sp < s) sp <<= 1;
-    G = (int)((N + (int64_t)LT * sp - 1) / ((int64_t)LT * sp));
+    // partition of nodes 0..N-1 into G chunks (CTAs) of LT threads x sp nodes (sp a power of
+    // two): one CTA when the line fits in 8 nodes per thread, otherwise the smallest sp that
+    // keeps G within the SM count
+    int sp = 1, G = 1;
+    if (N <= (int64_t)LT * LSEG) {
+        while ((int64_t)LT * sp < N) sp <<= 1;
+    } else {
+        while (sp <= LSEG && (N + (int64_t)LT * sp - 1) / ((int64_t)LT * sp) > ctx->sm_count) sp <<= 1;
+        if (sp > LSEG)
+            return set_error(FPDE_ERR_UNSUPPORTED, "line of %lld intervals exceeds %lld (SMs x %d x %d)",
+                             (long long)N, (long long)ctx->sm_count * LT * LSEG, LT, LSEG);
+        G = (int)((N + (int64_t)LT * sp - 1) / ((int64_t)LT * sp));
+    }
+    if (G > 160) return set_error(FPDE_ERR_UNSUPPORTED, "line solve: at most 160 chunks");
     int per_sm = 0;
     FPDE_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_line_solve<LSEG>, LT, 0));
     if (G > 1 && G > per_sm * ctx->sm_count)
@@ -562,6 +646,41 @@ int fpde_line_create(fpde_ctx *ctx, const fpde_line_desc *desc, const double *A,
         pr = 1.0;
         for (int64_t i = t1 - 1; i >= t0; --i) { pr *= hal[i]; hcb[i] = pr; }
     }
+    // per chunk (CTA): forward prefix products CF, backward suffix products CB and the
+    // backward sweep GG of CF, so that u = u^cta + c_in GG + u_b CB
+    std::vector<double> hCF(N), hCB(N), hGG(N), hPend(G), hG0(G), hB0(G);
+    for (int cc = 0; cc < G; ++cc) {
+        const int64_t a0 = (int64_t)cc * LT * sp, b0 = std::min<int64_t>(a0 + (int64_t)LT * sp, N);
+        double pr = 1.0;
+        for (int64_t i = a0; i < b0; ++i) { pr *= hp[i]; hCF[i] = pr; }
+        double cbv = 1.0, gg = 0.0;
+        for (int64_t i = b0 - 1; i >= a0; --i) {
+            cbv *= hal[i];
+            hCB[i] = cbv;
+            gg = hal[i] * gg + hCF[i];
+            hGG[i] = gg;
+        }
+        hPend[cc] = hCF[b0 - 1];
+        hG0[cc] = hGG[a0];
+        hB0[cc] = hCB[a0];
+    }
+    // chunk-level carries as dot products with the chunks' published values Y (last y) and
+    // U0 (first u):  c_in(c) = sum_r Lf[c][r] Y[r]        (c_in(G) = y at node N-1)
+    //                u_b(c)  = sum_q Mb[c][q] U0[q] + sum_r Kb[c][r] Y[r] + mb[c] U_N
+    std::vector<double> hLf((size_t)(G + 1) * G, 0.0), hMb((size_t)G * G, 0.0), hKb((size_t)G * G, 0.0), hmb(G);
+    for (int q = 1; q <= G; ++q) {
+        double pr = 1.0;
+        for (int r = q - 1; r >= 0; --r) { hLf[(size_t)q * G + r] = pr; pr *= hPend[r]; }
+    }
+    for (int cc = 0; cc < G; ++cc) {
+        double pr = 1.0;
+        for (int q = cc + 1; q < G; ++q) { hMb[(size_t)cc * G + q] = pr; pr *= hB0[q]; }
+        hmb[cc] = pr;
+        for (int q = cc + 1; q < G; ++q) {
+            const double f = hMb[(size_t)cc * G + q] * hG0[q];
+            for (int r = 0; r < q; ++r) hKb[(size_t)cc * G + r] += f * hLf[(size_t)q * G + r];
+        }
+    }
     // lag weights w[j] = Da * kb(lag j) / tau with kb(lag j) = kkk0 * b_j; wrev[m] = w[L - m]
     const int64_t LW = L->max_steps + BLK + 1;
     std::vector<double> wlag(LW, 0.0);
@@ -569,12 +688,17 @@ int fpde_line_create(fpde_ctx *ctx, const fpde_line_desc *desc, const double *A,
     std::vector<double> wrev(L->max_steps + 1, 0.0);
     for (int64_t m = 0; m < L->max_steps; ++m) wrev[m] = wlag[L->max_steps - m];
     const size_t nb = N * sizeof(double);
+    const size_t gb = (size_t)G * sizeof(double);
     bool fail = dev_alloc((void **)&L->A, nb) || dev_alloc((void **)&L->g, nb) || dev_alloc((void **)&L->al, nb) ||
                 dev_alloc((void **)&L->cf, nb) || dev_alloc((void **)&L->cb, nb) ||
+                dev_alloc((void **)&L->CF, nb) || dev_alloc((void **)&L->CB, nb) || dev_alloc((void **)&L->GG, nb) ||
+                dev_alloc((void **)&L->Lf, (size_t)(G + 1) * gb) || dev_alloc((void **)&L->Mb, (size_t)G * gb) ||
+                dev_alloc((void **)&L->Kb, (size_t)G * gb) || dev_alloc((void **)&L->mb, gb) ||
+                dev_alloc((void **)&L->cflag, (size_t)G * sizeof(unsigned long long)) ||
+                dev_alloc((void **)&L->seq, sizeof(unsigned long long)) ||
                 dev_alloc((void **)&L->U, L->P * sizeof(double)) ||
                 dev_alloc((void **)&L->wrev, wrev.size() * sizeof(double)) ||
-                dev_alloc((void **)&L->aggf, 2 * G * sizeof(double)) ||
-                dev_alloc((void **)&L->aggb, 2 * G * sizeof(double)) || dev_alloc((void **)&L->UN, sizeof(double)) ||
+                dev_alloc((void **)&L->agg, (2 * G + 2) * sizeof(double)) ||
                 dev_alloc((void **)&L->barrier, 2 * sizeof(unsigned));
     if (!fail && !L->split) {
         fail = dev_alloc((void **)&L->D, (size_t)L->max_steps * L->P * sizeof(double)) ||
@@ -636,6 +760,15 @@ int fpde_line_create(fpde_ctx *ctx, const fpde_line_desc *desc, const double *A,
     cudaMemcpyAsync(L->al, hal.data(), nb, cudaMemcpyHostToDevice, st);
     cudaMemcpyAsync(L->cf, hcf.data(), nb, cudaMemcpyHostToDevice, st);
     cudaMemcpyAsync(L->cb, hcb.data(), nb, cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(L->CF, hCF.data(), nb, cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(L->CB, hCB.data(), nb, cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(L->GG, hGG.data(), nb, cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(L->Lf, hLf.data(), hLf.size() * sizeof(double), cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(L->Mb, hMb.data(), hMb.size() * sizeof(double), cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(L->Kb, hKb.data(), hKb.size() * sizeof(double), cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(L->mb, hmb.data(), gb, cudaMemcpyHostToDevice, st);
+    cudaMemsetAsync(L->cflag, 0, (size_t)G * sizeof(unsigned long long), st);
+    cudaMemsetAsync(L->seq, 0, sizeof(unsigned long long), st);
     cudaMemcpyAsync(L->wrev, wrev.data(), wrev.size() * sizeof(double), cudaMemcpyHostToDevice, st);
     cudaMemsetAsync(L->U, 0, L->P * sizeof(double), st);
     cudaMemcpyAsync(L->U, u0, (N + 1) * sizeof(double), cudaMemcpyHostToDevice, st);

@@ -1,6 +1,6 @@
 // Block preparation of the split-precision path (per block of 64 steps):
 //   k_absmax  : largest |increment| of the finished block (for the fp16 scale)
-//   k_convert : FP64 increments (time-major ring, 64 rows) -> 16-bit hi/lo pairs in the
+//   k_convert : FP64 increments (node-major ring, 64 per node) -> 16-bit hi/lo pairs in the
 //               node-major history used as the K-major A operand, scaled by 2^sexp
 //   k_wgen    : Toeplitz weight tile W[j][t] = w[n0+j-t] * 2^(kexp - sexp(t)), split hi/lo,
 //               and the output scale 2^-kexp of the contraction
@@ -71,7 +71,7 @@ __global__ void __launch_bounds__(256) k_convert(const double *__restrict__ ring
     for (int e = threadIdx.x; e < 64 * 64; e += 256) {
         const int r = e >> 6, c = e & 63;
         const int64_t node = node0 + c;
-        tile[c][r] = node < nvalid ? ring[(int64_t)r * P + node] * sc : 0.0;
+        tile[c][r] = node < nvalid ? ring[node * 64 + r] * sc : 0.0;
     }
     __syncthreads();
     for (int e = threadIdx.x; e < 64 * 8; e += 256) {
@@ -123,27 +123,55 @@ __global__ void __launch_bounds__(256) k_wgen(const double *__restrict__ wlag, i
     wlo[(int64_t)j * ldw + t] = l;
 }
 
-// ---- exact three-slice form (bf16): x * 2^(8-e) = a0 + a1 2^-8 + a2 2^-16 + O(2^-17),
-// |x| < 2^e, with integer a0, a1, a2 of at most 8 bits; the exponent p = e - 8 is stored
-// per (node, 64-column block) for the history and per (step j, k-tile) for the weights.
-__device__ __forceinline__ int slice_exp(double m)
+// ---- exact three-slice form (bf16): x 2^-pe = a0 + a1 2^-8 + a2 2^-16 (+ rounding at 2^-16),
+// |x| < 2^(pe+8), with integer a0 (|a0| <= 256) and a1, a2 (|.| <= 128); the exponent pe is
+// stored per (node, 64-column block) for the history and per (step j, k-tile) for the
+// weights.
+// Integer form of the slicing (no FP64 arithmetic; GB300's FP64 pipe is narrow):
+// v = rint(x * 2^(16 - pe)) from the double's bits, |v| <= 2^24, then balanced base-256
+// digits v = a0 2^16 + a1 2^8 + a2 with |a0| <= 256, |a1|, |a2| <= 128.
+__device__ __forceinline__ long long fixed16(double x, int pe)
 {
-    if (!(m > 0.0)) return 0;
-    int p = ilogb(m) + 1 - 8;                 // m < 2^(p+8)
+    const unsigned long long bits = (unsigned long long)__double_as_longlong(x);
+    const int ex = (int)((bits >> 52) & 0x7FF);
+    if (ex == 0) return 0;                               // zero / subnormal: below the 2^-16 grid
+    const long long mant = (long long)((bits & 0xFFFFFFFFFFFFFull) | (1ull << 52));
+    const int sh = (ex - 1075) + 16 - pe;                // value * 2^(16-pe) = mant * 2^sh
+    long long v;
+    if (sh >= 0) {
+        v = sh > 10 ? (1ll << 62) : (mant << sh);        // out of range: caller's exponent prevents it
+    } else if (sh < -62) {
+        v = 0;
+    } else {
+        const int r = -sh;
+        const long long q = mant >> r;
+        const long long rem = mant & ((1ll << r) - 1);
+        const long long half = 1ll << (r - 1);
+        v = q + ((rem > half || (rem == half && (q & 1))) ? 1 : 0);   // round half to even
+    }
+    return (bits >> 63) ? -v : v;
+}
+__device__ __forceinline__ void digits3(long long v, uint16_t &s0, uint16_t &s1, uint16_t &s2)
+{
+    const int iv = (int)v;                               // |v| <= 2^24
+    const int a0 = (iv + 32768) >> 16;
+    const int r1 = iv - a0 * 65536;                      // [-32768, 32767]
+    const int a1 = (r1 + 128) >> 8;
+    const int a2 = r1 - a1 * 256;                        // [-128, 127]
+    s0 = __bfloat16_as_ushort(__float2bfloat16((float)a0));
+    s1 = __bfloat16_as_ushort(__float2bfloat16((float)a1 * (1.0f / 256.0f)));
+    s2 = __bfloat16_as_ushort(__float2bfloat16((float)a2 * (1.0f / 65536.0f)));
+}
+// Block exponent from the largest magnitude: |x| < 2^(pe + 8).
+__device__ __forceinline__ int exp_of_maxbits(unsigned long long mbits)
+{
+    const int ex = (int)((mbits >> 52) & 0x7FF);
+    if (ex == 0) return 0;
+    const int p = (ex - 1023) + 1 - 8;
     return p < -127 ? -127 : (p > 127 ? 127 : p);
 }
-__device__ __forceinline__ void slice3(double x, uint16_t &s0, uint16_t &s1, uint16_t &s2)
-{
-    const double a0 = rint(x);
-    const double r1 = (x - a0) * 256.0;
-    const double a1 = rint(r1);
-    const double a2 = rint((r1 - a1) * 256.0);
-    s0 = __bfloat16_as_ushort(__double2bfloat16(a0));
-    s1 = __bfloat16_as_ushort(__double2bfloat16(a1 * (1.0 / 256.0)));
-    s2 = __bfloat16_as_ushort(__double2bfloat16(a2 * (1.0 / 65536.0)));
-}
 
-// One thread per node: the node's 64 increments of the finished block.
+// One thread per node: the node's 64 increments of the finished block (node-major ring).
 __global__ void __launch_bounds__(128) k_convert3(const double *__restrict__ ring, int64_t P, int64_t nvalid,
                                                   uint16_t *__restrict__ h0, uint16_t *__restrict__ h1,
                                                   uint16_t *__restrict__ h2, int64_t ld, int64_t col0,
@@ -151,15 +179,25 @@ __global__ void __launch_bounds__(128) k_convert3(const double *__restrict__ rin
 {
     const int64_t node = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (node >= nvalid) return;
-    double m = 0.0;
-    for (int r = 0; r < 64; ++r) m = fmax(m, fabs(ring[(int64_t)r * P + node]));
-    const int pe = slice_exp(m);
+    const ulonglong2 *src = (const ulonglong2 *)(ring + node * 64);
+    unsigned long long mb = 0;
+#pragma unroll 8
+    for (int r = 0; r < 32; ++r) {
+        const ulonglong2 v = __ldg(src + r);
+        const unsigned long long m0 = v.x & 0x7FFFFFFFFFFFFFFFull, m1 = v.y & 0x7FFFFFFFFFFFFFFFull;
+        mb = m0 > mb ? m0 : mb;
+        mb = m1 > mb ? m1 : mb;
+    }
+    const int pe = exp_of_maxbits(mb);
     pA[node * ldp + blk] = (int8_t)pe;
-    const double sc = ldexp(1.0, -pe);
     for (int g = 0; g < 8; ++g) {
         uint16_t a[8], b[8], c[8];
 #pragma unroll
-        for (int k = 0; k < 8; ++k) slice3(ring[(int64_t)(8 * g + k) * P + node] * sc, a[k], b[k], c[k]);
+        for (int k = 0; k < 8; k += 2) {
+            const ulonglong2 v = __ldg(src + 4 * g + k / 2);
+            digits3(fixed16(__longlong_as_double((long long)v.x), pe), a[k], b[k], c[k]);
+            digits3(fixed16(__longlong_as_double((long long)v.y), pe), a[k + 1], b[k + 1], c[k + 1]);
+        }
         uint4 va, vb, vc;
         va.x = a[0] | ((uint32_t)a[1] << 16); va.y = a[2] | ((uint32_t)a[3] << 16);
         va.z = a[4] | ((uint32_t)a[5] << 16); va.w = a[6] | ((uint32_t)a[7] << 16);
@@ -188,10 +226,10 @@ __global__ void __launch_bounds__(64) k_wgen3(const double *__restrict__ wlag, i
     if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
     __syncthreads();
     m = fmax(red[0], red[1]);
-    const int pe = slice_exp(m);
+    const int pe = exp_of_maxbits((unsigned long long)__double_as_longlong(m));
     if (threadIdx.x == 0) pW[(int64_t)j * ldp + kt] = (int8_t)pe;
     uint16_t a, b, c;
-    slice3(v * ldexp(1.0, -pe), a, b, c);
+    digits3(fixed16(v, pe), a, b, c);
     w0[(int64_t)j * ld + t] = a;
     w1[(int64_t)j * ld + t] = b;
     w2[(int64_t)j * ld + t] = c;
