@@ -22,7 +22,8 @@ class LineDesc(C.Structure):
     _fields_ = [("N", c_i64), ("alpha", c_dbl), ("tau", c_dbl), ("Da", c_dbl),
                 ("left_kind", c_int), ("left_value", c_dbl), ("right_kind", c_int),
                 ("right_value", c_dbl), ("dLN", c_dbl), ("precision", c_int), ("block", c_int),
-                ("max_steps", c_int)]
+                ("max_steps", c_int), ("lag_weights", c_vp), ("theta", c_dbl), ("source", c_vp),
+                ("source_rows", c_int)]
 
 
 # name -> (restype, argtypes)
@@ -37,6 +38,9 @@ _SIGS = {
     "fpde_weights_l1": (c_int, [c_dbl, c_vp, c_int, c_vp, P_dbl]),
     "fpde_weights_l1_lags": (c_int, [c_dbl, c_int, c_vp]),
     "fpde_gamma": (c_int, [c_dbl, P_dbl]),
+    "fpde_do_weights": (c_int, [c_int, c_vp, c_vp, c_vp, c_dbl, c_int, c_vp]),
+    "fpde_do_derivative": (c_int, [c_vp, c_vp, c_i64, c_i64, c_int, c_dbl, c_vp, c_int, c_int, c_int, c_vp, c_i64,
+                                   c_int]),
     "fpde_history_create": (c_int, [c_vp, c_i64, c_i64, c_int, C.POINTER(c_vp)]),
     "fpde_history_destroy": (c_int, [c_vp]),
     "fpde_history_reset": (c_int, [c_vp]),

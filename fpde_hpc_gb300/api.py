@@ -48,6 +48,17 @@ def gamma(x):
     return out.value
 
 
+def do_weights(orders, qw, tau, n, gnorm=None):
+    """Fused distributed-order lag weights c[0..n-1] (fpde_do_weights)."""
+    a = np.ascontiguousarray(orders, dtype=np.float64)
+    q = np.ascontiguousarray(qw, dtype=np.float64)
+    g = None if gnorm is None else np.ascontiguousarray(gnorm, dtype=np.float64)
+    c = np.zeros(n)
+    check(load().fpde_do_weights(len(a), _ptr(a), _ptr(q), None if g is None else _ptr(g), tau, n, _ptr(c)),
+          "fpde_do_weights")
+    return c
+
+
 def line_coefs(k, dL, iw=None):
     k = np.ascontiguousarray(k, dtype=np.float64)
     N = len(k) - 1
@@ -151,11 +162,28 @@ class Line:
     """A 1D Caputo line problem advanced on the GPU (fpde_line_*)."""
 
     def __init__(self, ctx, N, alpha, tau, Da, A, B, Rlap, u0, max_steps, left=(0, 0.0), right=(0, 0.0),
-                 dLN=0.0, precision=FP64, block=0):
+                 dLN=0.0, precision=FP64, block=0, lag_weights=None, theta=0.0, source=None):
+        """lag_weights (max_steps+1 values, w[0] local) replace the Caputo L1 weights (the
+        distributed-order equation passes fused weights / tau); theta is the explicit fraction
+        of the space operator; source is one row or a (rows, N+1) array of per-step rows."""
         self.ctx, self.N = ctx, N
         d = LineDesc(N=N, alpha=alpha, tau=tau, Da=Da, left_kind=left[0], left_value=left[1],
                      right_kind=right[0], right_value=right[1], dLN=dLN, precision=precision, block=block,
-                     max_steps=max_steps)
+                     max_steps=max_steps, theta=theta)
+        self._keep = []
+        if lag_weights is not None:
+            w = np.ascontiguousarray(lag_weights, dtype=np.float64)
+            if len(w) < max_steps + 1:
+                raise ValueError("lag_weights needs max_steps + 1 values")
+            self._keep.append(w)
+            d.lag_weights = w.ctypes.data
+        if source is not None:
+            src = np.ascontiguousarray(np.atleast_2d(source), dtype=np.float64)
+            if src.shape[1] != N + 1:
+                raise ValueError("source rows need N + 1 values")
+            self._keep.append(src)
+            d.source = src.ctypes.data
+            d.source_rows = src.shape[0]
         self.desc = d
         arrs = [np.ascontiguousarray(x, dtype=np.float64) for x in (A, B, Rlap, u0)]
         self.h = C.c_void_p()

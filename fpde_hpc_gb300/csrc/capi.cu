@@ -8,6 +8,7 @@
 #include <cmath>
 #include <cstring>
 #include <mutex>
+#include <vector>
 #include <string>
 
 #include "common.cuh"
@@ -320,6 +321,28 @@ int fpde_gamma(double x, double *out)
     FPDE_CHECK_ARG(out, "null output");
     FPDE_CHECK_ARG(x > 0.0, "Gamma argument must be positive");
     *out = std::tgamma(x);
+    return FPDE_OK;
+}
+
+int fpde_do_weights(int n_orders, const double *a, const double *qw, const double *gnorm, double tau, int n,
+                    double *c)
+{
+    clear_error();
+    FPDE_CHECK_ARG(n_orders > 0 && a && qw && c && n >= 0, "bad arguments");
+    FPDE_CHECK_ARG(tau > 0.0, "tau must be positive");
+    for (int q = 0; q < n_orders; ++q) {
+        FPDE_CHECK_ARG(a[q] >= 0.0 && a[q] <= 1.0, "orders must lie in [0, 1]");
+        FPDE_CHECK_ARG(!gnorm || gnorm[q] != 0.0, "zero normaliser");
+    }
+    // per order: qw * tau^{1-a} / Gamma(2-a), then the lag factors b_l(a) summed over orders
+    std::vector<double> f(n_orders);
+    for (int q = 0; q < n_orders; ++q)
+        f[q] = qw[q] * std::pow(tau, 1.0 - a[q]) / (gnorm ? gnorm[q] : std::tgamma(2.0 - a[q]));
+    for (int l = 0; l < n; ++l) {
+        double s = 0.0;
+        for (int q = 0; q < n_orders; ++q) s += f[q] * l1_lag(a[q], l);
+        c[l] = s;
+    }
     return FPDE_OK;
 }
 

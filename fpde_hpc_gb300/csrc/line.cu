@@ -46,7 +46,9 @@ constexpr unsigned FULL = 0xffffffffu;
 struct LineSolveArgs {
     const double *A, *g, *al, *cf, *cb;   // per node: coefficients, thread-segment products
     const double *CF, *CB, *GG;           // per node: chunk-level forward/backward data
-    const double *src;                    // optional source (N+1), may be null
+    const double *src;                    // optional source (N+1) of this step, may be null
+    const double *lamv;                   // optional per-node local weight (replaces lam)
+    const double *eA, *eB;                // optional explicit neighbour weights (theta A, theta B)
     double *U;                            // state (N+1)
     double *Drow;                         // increment of node i goes to Drow[i * dstride]
     int64_t dstride;
@@ -203,8 +205,22 @@ __global__ void __launch_bounds__(LT) k_line_solve(LineSolveArgs p)
         for (int k = 0; k < SP; ++k) om[k] += (a0[k] + a1[k]) + (a2[k] + a3[k]);
     }
 #pragma unroll
-    for (int k = 0; k < SP; ++k)
-        om[k] = (-(p.lam * uo[k]) + (p.src && k < cnt ? p.src[i0 + k] : 0.0)) + om[k];
+    for (int k = 0; k < SP; ++k) {
+        const double lam = (p.lamv && k < cnt) ? __ldg(p.lamv + i0 + k) : p.lam;
+        om[k] = (-(lam * uo[k]) + (p.src && k < cnt ? __ldg(p.src + i0 + k) : 0.0)) + om[k];
+    }
+    if (p.eA && cnt > 0) {                                           // explicit part on the old state
+        double ul = i0 > 0 ? p.U[i0 - 1] : 0.0;
+        const double ur = p.U[i0 + cnt];                              // i0 + cnt <= N
+#pragma unroll
+        for (int k = 0; k < SP; ++k) {
+            if (k < cnt) {
+                const double un = k + 1 < cnt ? uo[k + 1] : ur;
+                om[k] -= fma(__ldg(p.eA + i0 + k), ul, __ldg(p.eB + i0 + k) * un);
+                ul = uo[k];
+            }
+        }
+    }
 
     // ---- forward sweep of the chunk from zero carry
     double y[SP];
@@ -371,6 +387,9 @@ struct fpde_line {
     double *U = nullptr, *D = nullptr, *part = nullptr, *wrev = nullptr;
     double *agg = nullptr;
     unsigned *barrier = nullptr;
+    // optional: per-step source rows, explicit space part, per-node local weight
+    double *srcd = nullptr, *lamv = nullptr, *eA = nullptr, *eB = nullptr;
+    int src_rows = 0;
     // split path
     int64_t rows16 = 0, ld16 = 0;
     uint16_t *h_hi = nullptr, *h_lo = nullptr, *w_hi = nullptr, *w_lo = nullptr;
@@ -404,11 +423,13 @@ static cudaError_t launch_solve_sp(const cudaLaunchConfig_t &cfg, const LineSolv
     return cudaLaunchKernelEx(&cfg, k_line_solve<SP>, a);
 }
 
-static int line_launch_solve(fpde_line *L, cudaStream_t st, const double *part, int KS, int64_t pstride,
+static int line_launch_solve(fpde_line *L, cudaStream_t st, int64_t n, const double *part, int KS, int64_t pstride,
                              const double *ring, const double *wn, int nr, double *Drow, int64_t dstride)
 {
     LineSolveArgs a;
-    a.A = L->A; a.g = L->g; a.al = L->al; a.cf = L->cf; a.cb = L->cb; a.src = nullptr;
+    a.A = L->A; a.g = L->g; a.al = L->al; a.cf = L->cf; a.cb = L->cb;
+    a.src = L->srcd ? L->srcd + (n < L->src_rows ? n : L->src_rows - 1) * (L->N + 1) : nullptr;
+    a.lamv = L->lamv; a.eA = L->eA; a.eB = L->eB;
     a.CF = L->CF; a.CB = L->CB; a.GG = L->GG;
     a.Lf = L->Lf; a.Mb = L->Mb; a.Kb = L->Kb; a.mb = L->mb; a.cflag = L->cflag; a.seq = L->seq;
     a.U = L->U; a.Drow = Drow; a.dstride = dstride; a.part = part; a.pstride = pstride; a.ring = ring; a.wn = wn;
@@ -471,7 +492,7 @@ static int line_enqueue(fpde_line *L, cudaStream_t st, int64_t n0, int steps, in
             }
             ev = probe_step ? probe_begin(L, 2, n, 0.0, 0.0) : nullptr;
             PROBE_REC(ev, 0);
-            if ((rc = line_launch_solve(L, st, L->part, KS, L->P, nullptr, nullptr, 0, L->D + n * L->P, 1))) return rc;
+            if ((rc = line_launch_solve(L, st, n, L->part, KS, L->P, nullptr, nullptr, 0, L->D + n * L->P, 1))) return rc;
             PROBE_REC(ev, 1);
             ++k;
         } else {
@@ -516,7 +537,7 @@ static int line_enqueue(fpde_line *L, cudaStream_t st, int64_t n0, int steps, in
             const double *wn = L->wrev + (L->max_steps - j);       // wn[r] = w[j - r]
             ev = probe_step ? probe_begin(L, 2, n, 0.0, 0.0) : nullptr;
             PROBE_REC(ev, 0);
-            if ((rc = line_launch_solve(L, st, L->cfar + (int64_t)j * L->P, splits, (int64_t)BLK * L->P, L->ring, wn,
+            if ((rc = line_launch_solve(L, st, n, L->cfar + (int64_t)j * L->P, splits, (int64_t)BLK * L->P, L->ring, wn,
                                         j, L->ring + j, BLK)))
                 return rc;
             PROBE_REC(ev, 1);
@@ -557,7 +578,8 @@ int fpde_line_destroy(fpde_line *L)
     dev_free(L->cflag);
     dev_free(L->seq);
     for (double *p : {L->A, L->g, L->al, L->cf, L->cb, L->CF, L->CB, L->GG, L->Lf, L->Mb, L->Kb, L->mb, L->U, L->D,
-                      L->part, L->wrev, L->agg, L->ring, L->cfar, L->wlag, L->out_scale})
+                      L->part, L->wrev, L->agg, L->ring, L->cfar, L->wlag, L->out_scale, L->srcd, L->lamv, L->eA,
+                      L->eB})
         dev_free(p);
     for (uint16_t *p : {L->h_hi, L->h_lo, L->w_hi, L->w_lo, L->h3[0], L->h3[1], L->h3[2], L->w3[0], L->w3[1],
                         L->w3[2]})
@@ -581,7 +603,9 @@ int fpde_line_create(fpde_ctx *ctx, const fpde_line_desc *desc, const double *A,
     if (rc) return rc;
     const fpde_line_desc &d = *desc;
     FPDE_CHECK_ARG(d.N >= 2, "N must be >= 2");
-    FPDE_CHECK_ARG(d.alpha > 0.0 && d.alpha < 1.0, "alpha must be in (0, 1)");
+    FPDE_CHECK_ARG(d.lag_weights || (d.alpha > 0.0 && d.alpha < 1.0), "alpha must be in (0, 1)");
+    FPDE_CHECK_ARG(!d.source || d.source_rows >= 1, "source needs source_rows >= 1");
+    FPDE_CHECK_ARG(std::isfinite(d.theta), "theta must be finite");
     FPDE_CHECK_ARG(d.tau > 0.0, "tau must be positive");
     FPDE_CHECK_ARG(d.max_steps > 0, "max_steps must be positive");
     FPDE_CHECK_ARG(d.left_kind == 0 || d.left_kind == 1, "bad left boundary kind");
@@ -621,10 +645,16 @@ int fpde_line_create(fpde_ctx *ctx, const fpde_line_desc *desc, const double *A,
     L->max_steps = d.max_steps;
     L->split = d.precision != FPDE_PREC_FP64;
     L->x3 = d.precision == FPDE_PREC_SPLIT_BF16X3;
-    // local weight kkk0 = tau^{1-alpha}/(1-alpha); lam as in Om1 (:4191), lamR as in R (:3120)
-    L->kkk0 = l1_interval_weight(d.alpha, 0.0, d.tau);
-    L->lam = d.Da * (L->kkk0 / d.tau);
-    L->lamR = d.Da * L->kkk0 / d.tau;
+    // local weight kkk0 = tau^{1-alpha}/(1-alpha); lam as in Om1 (:4191), lamR as in R (:3120);
+    // or the caller's lag weights (distributed order: w[0] = b0/tau of eq_init, fr_do.cpp:688-694)
+    if (d.lag_weights) {
+        L->kkk0 = 0.0;
+        L->lam = L->lamR = d.lag_weights[0];
+    } else {
+        L->kkk0 = l1_interval_weight(d.alpha, 0.0, d.tau);
+        L->lam = d.Da * (L->kkk0 / d.tau);
+        L->lamR = d.Da * L->kkk0 / d.tau;
+    }
 
     // time-invariant Thomas data (host, FP64)
     std::vector<double> Al(N + 2, 0.0), hA(N, 0.0), hg(N, 0.0), hal(N, 0.0), hp(N, 0.0), hcf(N), hcb(N);
@@ -684,7 +714,9 @@ int fpde_line_create(fpde_ctx *ctx, const fpde_line_desc *desc, const double *A,
     // lag weights w[j] = Da * kb(lag j) / tau with kb(lag j) = kkk0 * b_j; wrev[m] = w[L - m]
     const int64_t LW = L->max_steps + BLK + 1;
     std::vector<double> wlag(LW, 0.0);
-    for (int64_t j = 1; j < LW; ++j) wlag[j] = d.Da * (L->kkk0 * l1_lag(d.alpha, j)) / d.tau;
+    for (int64_t j = 1; j < LW; ++j)
+        wlag[j] = d.lag_weights ? (j <= L->max_steps ? d.lag_weights[j] : 0.0)
+                                : d.Da * (L->kkk0 * l1_lag(d.alpha, j)) / d.tau;
     std::vector<double> wrev(L->max_steps + 1, 0.0);
     for (int64_t m = 0; m < L->max_steps; ++m) wrev[m] = wlag[L->max_steps - m];
     const size_t nb = N * sizeof(double);
@@ -749,12 +781,34 @@ int fpde_line_create(fpde_ctx *ctx, const fpde_line_desc *desc, const double *A,
             }
         }
     }
+    if (!fail && d.source) {
+        L->src_rows = std::min(d.source_rows, d.max_steps);
+        fail = dev_alloc((void **)&L->srcd, (size_t)L->src_rows * (N + 1) * sizeof(double));
+    }
+    if (!fail && d.theta != 0.0)
+        fail = dev_alloc((void **)&L->lamv, nb) || dev_alloc((void **)&L->eA, nb) || dev_alloc((void **)&L->eB, nb);
     if (fail) {
         std::string keep = fpde_last_error_string();
         fpde_line_destroy(L);
         return set_error(FPDE_ERR_NOMEM, "%s", keep.c_str());
     }
     cudaStream_t st = ctx->stream;
+    std::vector<double> hlamv, heA, heB;
+    if (d.theta != 0.0) {                          // Om -= theta (A U[i-1] - Rlap U[i] + B U[i+1])
+        hlamv.assign(N, L->lam);
+        heA.assign(N, 0.0);
+        heB.assign(N, 0.0);
+        for (int64_t i = 1; i < N; ++i) {
+            hlamv[i] = L->lam - d.theta * Rlap[i];
+            heA[i] = d.theta * A[i];
+            heB[i] = d.theta * B[i];
+        }
+        cudaMemcpyAsync(L->lamv, hlamv.data(), nb, cudaMemcpyHostToDevice, st);
+        cudaMemcpyAsync(L->eA, heA.data(), nb, cudaMemcpyHostToDevice, st);
+        cudaMemcpyAsync(L->eB, heB.data(), nb, cudaMemcpyHostToDevice, st);
+    }
+    if (L->srcd)
+        cudaMemcpyAsync(L->srcd, d.source, (size_t)L->src_rows * (N + 1) * sizeof(double), cudaMemcpyHostToDevice, st);
     cudaMemcpyAsync(L->A, hA.data(), nb, cudaMemcpyHostToDevice, st);
     cudaMemcpyAsync(L->g, hg.data(), nb, cudaMemcpyHostToDevice, st);
     cudaMemcpyAsync(L->al, hal.data(), nb, cudaMemcpyHostToDevice, st);

@@ -92,3 +92,53 @@ def config2(N=65536, steps=8192, tau=1e-4):
     u0 = gaussian_mixture(x, 2)
     u0[0] = u0[-1] = 0.0
     return LineProblem(f"config2_N{N}", N, 0.7, tau, steps, k, u0)
+
+
+@dataclass
+class DOProblem:
+    """Distributed-order line problem in fr_do's Crank-Nicolson form (eq_solve, fr_do.cpp:733-775)
+    with variable conductivity: int_0^1 w(a) D^a u da = d/dx(k du/dx), half the space operator
+    implicit and half explicit (theta = 1 on the halved coefficients), Dirichlet 0 ends.
+    The a-integral is a quadrature (orders, qw = quadrature weights x w(a)); the library fuses
+    it into one lag-weight vector (fpde_do_weights)."""
+    name: str
+    N: int
+    tau: float
+    steps: int
+    k: np.ndarray
+    u0: np.ndarray
+    orders: np.ndarray
+    qw: np.ndarray
+
+    @property
+    def x(self):
+        return np.arange(self.N + 1) / self.N
+
+    def coefs(self):
+        """Halved A, B, Rlap of the k-Laplacian (implicit half; theta = 1 adds the explicit half)."""
+        A, B, R = LineProblem("", self.N, 0.5, self.tau, self.steps, self.k, self.u0).coefs()
+        return 0.5 * A, 0.5 * B, 0.5 * R
+
+    @property
+    def gnorm(self):
+        return np.array([math.gamma(2.0 - a) for a in self.orders])
+
+    @property
+    def node_steps(self):
+        return (self.N - 1) * self.steps
+
+
+def gauss_legendre_01(n):
+    x, w = np.polynomial.legendre.leggauss(n)
+    return 0.5 * (x + 1.0), 0.5 * w
+
+
+def config3(N=16384, steps=4096, tau=1e-4):
+    """DO, N=16384, 4096 steps, w(a) = 6a(1-a), 16-node Gauss-Legendre on [0,1]; lognormal k
+    (mu 0, sigma 0.5, ell 0.01, seed 3), 8-Gaussian initial state (seed 4), Dirichlet 0."""
+    x = np.arange(N + 1) / N
+    k = lognormal_field(N + 1, 0.0, 0.5, 0.01, 3, 1.0 / N)
+    u0 = gaussian_mixture(x, 4)
+    u0[0] = u0[-1] = 0.0
+    a, w = gauss_legendre_01(16)
+    return DOProblem(f"config3_DO_N{N}", N, tau, steps, k, u0, a, w * 6.0 * a * (1.0 - a))

@@ -101,6 +101,29 @@ int fpde_weights_l1_lags(double alpha, int n, double *b);
  * and the distributed-order normalisers Gamma(2-alpha) (fr_do.cpp:337-341). */
 int fpde_gamma(double x, double *out);
 
+/* Fused distributed-order weights (host, FP64). The DO derivative of fr_do.cpp
+ * (DO_Cder :89-113, GPU Fill/DOC/Sum :136-252) evaluates, per order a_q, the L1 Caputo sum
+ * with bk((l+1)tau, l tau, a_q) = ((l+1)tau)^{1-a_q} - (l tau)^{1-a_q} divided by
+ * Gamma(2-a_q), and then integrates over a with weights. All of that is linear in the
+ * history, so the orders fuse into one lag-weight vector:
+ *   c[l] = sum_q qw[q] * tau^{1-a_q} * b_l(a_q) / gnorm[q],   l = 0..n-1,
+ * b_l(a) = (l+1)^{1-a} - l^{1-a} in cancellation-free form. qw holds the quadrature weights
+ * of the a-integral times the weight function (fr_do: trapezoid x WA, :108-110), gnorm
+ * Gamma(2 - a_q) (NULL: computed). The DO derivative of samples F at time t is then
+ * sum_j (F[j+1]-F[j])/tau * c[t-j-1], and c[0] is the local weight b0 of eq_init (:688-690).
+ * Replaces the per-order bkk table (Fill) and the order loop of DOC and Sum. */
+int fpde_do_weights(int n_orders, const double *a, const double *qw, const double *gnorm, double tau, int n,
+                    double *c);
+
+/* DO derivative of sampled series on the device (replaces DO_Cder_CUDA, fr_do.cpp:361-430,
+ * with its kernels Fill/DOC/Sum :136-252, for use_f > 0 arrays):
+ *   DF[pt*ldd + t] (+)= sum_{j in [max(j0,0), min(t, maxt))} (F[pt*ldf+j+1] - F[pt*ldf+j])/tau * c[t-j-1]
+ * for t in [t0, ntau) and every node pt < nodes; maxt = -1 sums up to t (the reference's
+ * convention), append != 0 adds to DF (Sum's append). F, c (>= ntau fused weights of
+ * fpde_do_weights) and DF are device pointers; runs on the context's stream. */
+int fpde_do_derivative(fpde_ctx *ctx, const double *F, int64_t nodes, int64_t ldf, int ntau, double tau,
+                       const double *c, int t0, int j0, int maxt, double *DF, int64_t ldd, int append);
+
 /* ---------------------------------------------------------- L1 history sum */
 
 /* Create a history of `nodes` values per snapshot with room for `max_steps` increments.
@@ -203,6 +226,16 @@ typedef struct fpde_line_desc {
     int precision;        /* fpde_precision */
     int block;            /* split paths: steps per far-history block (0 = auto) */
     int max_steps;        /* history capacity */
+    /* Optional; all-zero keeps the Caputo L1 scheme above. */
+    const double *lag_weights; /* host, max_steps+1 values: w[0] replaces Da*kkk0/tau (in Om and
+                                  R), w[l] the history weight of lag l (Da*kkk0*b_l/tau): the
+                                  distributed-order equation uses c[l]/tau of fpde_do_weights */
+    double theta;         /* explicit fraction of the space operator on the old state,
+                             Om[i] -= theta*(A[i] U[i-1] - Rlap[i] U[i] + B[i] U[i+1])
+                             (fr_do eq_Ff :656-665: theta 1 with A = B = D/(2h^2)) */
+    const double *source; /* host, source_rows x (N+1): step n adds row min(n, source_rows-1)
+                             to Om (fr_do's -(f(t_n,x)+f(t_{n+1},x))/2; Rp of Om1) */
+    int source_rows;
 } fpde_line_desc;
 
 /* Set up a line: A, B, Rlap (N+1 host values, entries 1..N-1 used; see fpde_line_coefs)

@@ -157,6 +157,43 @@ int fo_line_run(int N, double *U, double *hist, int64_t P, int steps, double tau
     return 0;
 }
 
+int fo_line_run_general(int N, double *U, double *hist, int64_t P, int steps, const double *w, double theta,
+                        const double *A, const double *B, const double *Rlap, const double *src, int src_rows,
+                        int ltype, double g0, int rtype, double gN, double dLN)
+{
+    double *S = (double *)calloc((size_t)N + 1, sizeof(double));
+    double *Om = (double *)calloc((size_t)N + 1, sizeof(double));
+    double *R = (double *)calloc((size_t)N + 1, sizeof(double));
+    double *Uold = (double *)malloc(sizeof(double) * (size_t)(N + 1));
+    double *Al = (double *)malloc(sizeof(double) * (size_t)(N + 2));
+    double *Bt = (double *)malloc(sizeof(double) * (size_t)(N + 2));
+    double *wl = (double *)malloc(sizeof(double) * (size_t)(steps + 1));
+    for (int n = 0; n < steps; n++) {
+        memcpy(Uold, U, sizeof(double) * (size_t)(N + 1));
+        /* history: S[i] = sum_{t<n} w[n-t] D_t[i] (lag weights, eq_DF of fr_do.cpp :737-771) */
+        for (int t = 0; t < n; t++) wl[t] = w[n - t];
+#pragma omp parallel for schedule(static)
+        for (int i = 1; i < N; i++) {
+            double s = 0.0;
+            for (int t = n - 1; t >= 0; t--) s += wl[t] * hist[(int64_t)t * P + i];
+            S[i] = s;
+        }
+        const double *sr = src ? src + (int64_t)(n < src_rows ? n : src_rows - 1) * (N + 1) : NULL;
+        for (int i = 1; i < N; i++) {
+            /* explicit part of the space operator (rp of eq_Ff :656-665) */
+            double ex = theta != 0.0 ? -(theta * ((A[i] * Uold[i - 1] - Rlap[i] * Uold[i]) + B[i] * Uold[i + 1])) : 0.0;
+            Om[i] = ex + (-(w[0] * Uold[i]) + (sr ? sr[i] : 0.0));
+            Om[i] += S[i];
+            R[i] = Rlap[i] + w[0];
+        }
+        thomas_core(N, A, B, R, Om, ltype, g0, rtype, gN, dLN, U, Al, Bt);
+        double *row = hist + (int64_t)n * P;
+        for (int64_t i = 0; i < P; i++) row[i] = (i <= N) ? U[i] - Uold[i] : 0.0;
+    }
+    free(S); free(Om); free(R); free(Uold); free(Al); free(Bt); free(wl);
+    return 0;
+}
+
 /* ---------------------------------------------------------------- 3D LOD */
 
 int fo_lod_step_dirichlet(int sN, int M, int K, double *U, double *hist, int n,

@@ -76,6 +76,19 @@ int fo_line_run(int N, double *U, double *hist, int64_t P, int steps, double tau
                 double Da, const double *A, const double *B, const double *Rlap,
                 int ltype, double g0, int rtype, double gN, double dLN);
 
+/* General line run (uniform tau), used for the distributed-order equation of fr_do.cpp
+ * (eq_solve :733-775, eq_Ff :656-665, eq_one_step :724-732) and any other lag weights:
+ *   S[i]  = sum_{t<n} w[n-t] D_t[i]                            (history, lag weights w[1..])
+ *   Om[i] = -theta (A[i] U[i-1] - Rlap[i] U[i] + B[i] U[i+1])  (explicit part, old U)
+ *           - w[0] U[i] + src[i] + S[i],       R[i] = Rlap[i] + w[0].
+ * w holds steps+1 values (w[0] the local weight). src (may be NULL) holds src_rows rows of
+ * N+1 values; step n uses row min(n, src_rows-1). fr_do's scheme is w[l] = c_l / tau with
+ * the fused DO weights c (fo_do_fused_weights), theta = 1, A = B = D/(2h^2), Rlap = D/h^2,
+ * src = -(f(t_n) + f(t_{n+1}))/2. hist must hold steps rows of P doubles. Returns 0. */
+int fo_line_run_general(int N, double *U, double *hist, int64_t P, int steps, const double *w, double theta,
+                        const double *A, const double *B, const double *Rlap, const double *src, int src_rows,
+                        int ltype, double g0, int rtype, double gN, double dLN);
+
 /* One step of the reference's 3D LOD scheme (calc_step mode 3 :5144-5779, implicit3d 0,
  * split3d 0): K pass (lines along k, with source Rp and the history sum), then the _M
  * pass (lines along j), then the sN pass (lines along i). The grid has (sN+2)(M+2)(K+2)

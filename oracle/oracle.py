@@ -42,6 +42,8 @@ def load():
     lib.fo_line_step.restype = i32
     lib.fo_line_run.argtypes = [i32, _dp, _dp, i64, i32, d, d, d, _dp, _dp, _dp, i32, d, i32, d, d]
     lib.fo_line_run.restype = i32
+    lib.fo_line_run_general.argtypes = [i32, _dp, _dp, i64, i32, _dp, d, _dp, _dp, _dp, vp, i32, i32, d, i32, d, d]
+    lib.fo_line_run_general.restype = i32
     lib.fo_lod_step_dirichlet.argtypes = [i32, i32, i32, _dp, _dp, i32, _dp, _dp, d, d,
                                           _dp, _dp, _dp, _dp, _dp, vp]
     lib.fo_lod_step_dirichlet.restype = i32
@@ -123,6 +125,28 @@ def line_run(U0, steps, tau, alpha, Da, A, B, Rl, ltype=0, g0=0.0, rtype=0, gN=0
     lib.fo_line_run(N, U, hist.reshape(-1), P, steps, tau, alpha, Da,
                     *(np.ascontiguousarray(x, dtype=np.float64) for x in (A, B, Rl)),
                     ltype, g0, rtype, gN, dLN)
+    return U, hist
+
+
+def line_run_general(U0, steps, w, theta, A, B, Rl, src=None, ltype=0, g0=0.0, rtype=0, gN=0.0, dLN=0.0):
+    """Line run with explicit lag weights w (w[0] local), explicit fraction theta and an
+    optional source (rows x (N+1); step n uses row min(n, rows-1)). Returns (U, hist)."""
+    lib = load()
+    U = np.array(U0, dtype=np.float64)
+    N = len(U) - 1
+    hist = np.zeros((steps, N + 1))
+    w = np.ascontiguousarray(w, dtype=np.float64)
+    assert len(w) >= steps + 1
+    rows = 0
+    sp = None
+    if src is not None:
+        src = np.ascontiguousarray(np.atleast_2d(src), dtype=np.float64)
+        assert src.shape[1] == N + 1
+        rows = src.shape[0]
+        sp = src.ctypes.data_as(C.c_void_p)
+    lib.fo_line_run_general(N, U, hist.reshape(-1), N + 1, steps, w, theta,
+                            *(np.ascontiguousarray(x, dtype=np.float64) for x in (A, B, Rl)),
+                            sp, rows, ltype, g0, rtype, gN, dLN)
     return U, hist
 
 

@@ -82,3 +82,27 @@ def test_errors_are_codes_not_exits(lib_path):
     assert b"alpha" in lib.fpde_last_error_string() or b"bad" in lib.fpde_last_error_string()
     out = C.c_double()
     assert lib.fpde_gamma(-1.0, C.byref(out)) == 1
+
+
+def test_do_weights_match_oracle(lib_path):
+    """fpde_do_weights (host) fuses the per-order L1 weights like the oracle, and its c[0]
+    is the local weight b0 of fr_do's eq_init for the reference's own orders and weights."""
+    import numpy as np
+    import fgv
+    import oracle
+    import do_cases
+    import fpde_hpc_gb300 as fp
+    from conftest import golden_path
+    g = fgv.load(golden_path("frdo_eq_ex0"))
+    Na = len(g["WA"])
+    aq, qw, gq = do_cases.orders(Na), do_cases.quad_weights(g["WA"]), do_cases.gammas(Na)
+    for tau, n in ((g["tau"], 64), (1e-4, 5000)):
+        c = fp.do_weights(aq, qw, tau, n, gq)
+        c_or = oracle.do_fused_weights(aq, qw, gq, tau, n)
+        assert np.max(np.abs(c - c_or) / np.abs(c_or)) <= 1e-14
+    c = fp.do_weights(aq, qw, g["tau"], 4, gq)
+    assert abs(c[0] - g["b0"]) <= 1e-13 * g["b0"]
+    c2 = fp.do_weights(aq, qw, g["tau"], 4)          # normalisers computed by the library
+    assert np.allclose(c2, c, rtol=1e-14, atol=0)
+    with pytest.raises(fp.FpdeError):
+        fp.do_weights([1.5], [1.0], 0.1, 3)

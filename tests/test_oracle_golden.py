@@ -129,3 +129,18 @@ def test_do_equation_matches_fr_do(name):
     assert _relmax(Cm, g["C"]) <= RTOL, _relmax(Cm, g["C"])
     err = np.sqrt(np.mean((Cm[:, -1] - g["analytic_last"]) ** 2))
     assert abs(err - g["err"]) <= 1e-9 * max(g["err"], 1e-300) + 1e-15
+
+
+@pytest.mark.parametrize("name", ["frdo_eq_ex0", "frdo_eq_ex1"])
+def test_do_equation_as_general_line_run(name):
+    """fr_do's eq_solve, restated as a line run with fused DO lag weights, theta = 1 and a
+    per-step source (the form the GPU line path runs), meets the reference's own output."""
+    import do_cases
+    g = fgv.load(golden_path(name))
+    u0, A, B, Rl, w, theta, src, steps = do_cases.line_problem(g, oracle.do_fused_weights)
+    assert abs(w[0] * g["tau"] - g["b0"]) <= 1e-12 * g["b0"]
+    Cref = g["C"]
+    U = u0.copy()
+    for n in range(1, steps + 1):            # compare every time level
+        U, _ = oracle.line_run_general(u0, n, w, theta, A, B, Rl, src)
+        assert _relmax(U, Cref[:, n]) <= RTOL, (n, _relmax(U, Cref[:, n]))
