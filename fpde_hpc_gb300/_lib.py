@@ -26,6 +26,13 @@ class LineDesc(C.Structure):
                 ("source_rows", c_int)]
 
 
+class Lod3dDesc(C.Structure):
+    _fields_ = [("sN", c_int), ("M", c_int), ("K", c_int), ("alpha", c_dbl), ("tau", c_dbl), ("Da", c_dbl),
+                ("left_kind", c_int * 3), ("right_kind", c_int * 3), ("dLN", c_dbl * 3), ("precision", c_int),
+                ("max_steps", c_int), ("lag_weights", c_vp), ("source", c_vp), ("source_rows", c_int),
+                ("bc", c_vp), ("bc_rows", c_int)]
+
+
 # name -> (restype, argtypes)
 _SIGS = {
     "fpde_ctx_create": (c_int, [c_int, C.POINTER(c_vp)]),
@@ -39,6 +46,13 @@ _SIGS = {
     "fpde_weights_l1_lags": (c_int, [c_dbl, c_int, c_vp]),
     "fpde_gamma": (c_int, [c_dbl, P_dbl]),
     "fpde_do_weights": (c_int, [c_int, c_vp, c_vp, c_vp, c_dbl, c_int, c_vp]),
+    "fpde_lod3d_create": (c_int, [c_vp, C.POINTER(Lod3dDesc), c_vp, c_vp, c_vp, c_vp, C.POINTER(c_vp)]),
+    "fpde_lod3d_destroy": (c_int, [c_vp]),
+    "fpde_lod3d_run": (c_int, [c_vp, c_int]),
+    "fpde_lod3d_get_state": (c_int, [c_vp, c_vp, c_int]),
+    "fpde_lod3d_reset": (c_int, [c_vp, c_vp, c_int]),
+    "fpde_lod3d_solve_host": (c_int, [c_vp, c_vp, c_int, c_vp]),
+    "fpde_lod3d_steps_done": (c_int, [c_vp, C.POINTER(c_i64)]),
     "fpde_do_derivative": (c_int, [c_vp, c_vp, c_i64, c_i64, c_int, c_dbl, c_vp, c_int, c_int, c_int, c_vp, c_i64,
                                    c_int]),
     "fpde_history_create": (c_int, [c_vp, c_i64, c_i64, c_int, C.POINTER(c_vp)]),

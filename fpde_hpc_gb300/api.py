@@ -3,7 +3,7 @@ import ctypes as C
 
 import numpy as np
 
-from ._lib import LineDesc, check, load
+from ._lib import LineDesc, Lod3dDesc, check, load
 
 FP64, SPLIT_BF16, SPLIT_F16 = 0, 1, 2
 
@@ -233,3 +233,71 @@ class Line:
         n = C.c_int64()
         check(self.ctx.lib.fpde_line_steps_done(self.h, C.byref(n)), "fpde_line_steps_done")
         return n.value
+
+
+class Lod3D:
+    """The 3D LOD step of the reference (fpde_lod3d_*): grids are numpy arrays of shape
+    (K+2, M+2, sN+2) (idx = i + j (sN+2) + k (sN+2)(M+2)); coefA/B/Rlap have a leading axis of 3
+    passes (0 = sN along i, 1 = _M along j, 2 = K along k)."""
+
+    def __init__(self, ctx, dims, alpha, tau, Da, coefA, coefB, coefRlap, u0, max_steps, left_kind=(0, 0, 0),
+                 right_kind=(0, 0, 0), dLN=(0.0, 0.0, 0.0), source=None, bc=None, lag_weights=None,
+                 precision=FP64):
+        sN, M, K = dims
+        self.ctx, self.dims = ctx, dims
+        self.shape = (K + 2, M + 2, sN + 2)
+        d = Lod3dDesc(sN=sN, M=M, K=K, alpha=alpha, tau=tau, Da=Da, precision=precision, max_steps=max_steps)
+        for q in range(3):
+            d.left_kind[q], d.right_kind[q], d.dLN[q] = left_kind[q], right_kind[q], dLN[q]
+        keep = []
+
+        def rows(x):
+            a = np.ascontiguousarray(x, dtype=np.float64)
+            if a.shape == self.shape:
+                a = a[None]
+            if a.shape[1:] != self.shape:
+                raise ValueError("grid inputs need shape (rows, K+2, M+2, sN+2)")
+            keep.append(a)
+            return a.ctypes.data, a.shape[0]
+
+        if source is not None:
+            d.source, d.source_rows = rows(source)
+        if bc is not None:
+            d.bc, d.bc_rows = rows(bc)
+        if lag_weights is not None:
+            w = np.ascontiguousarray(lag_weights, dtype=np.float64)
+            if len(w) < max_steps + 1:
+                raise ValueError("lag_weights needs max_steps + 1 values")
+            keep.append(w)
+            d.lag_weights = w.ctypes.data
+        cs = [np.ascontiguousarray(x, dtype=np.float64) for x in (coefA, coefB, coefRlap)]
+        for c in cs:
+            if c.shape != (3,) + self.shape:
+                raise ValueError("coefficient grids need shape (3, K+2, M+2, sN+2)")
+        u0 = np.ascontiguousarray(u0, dtype=np.float64)
+        self.h = C.c_void_p()
+        check(ctx.lib.fpde_lod3d_create(ctx.h, C.byref(d), *(_ptr(x) for x in cs), _ptr(u0), C.byref(self.h)),
+              "fpde_lod3d_create")
+
+    def close(self):
+        if self.h:
+            self.ctx.lib.fpde_lod3d_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def run(self, steps):
+        check(self.ctx.lib.fpde_lod3d_run(self.h, steps), "fpde_lod3d_run")
+
+    def state(self, out=None):
+        if out is None:
+            out = np.zeros(self.shape)
+        check(self.ctx.lib.fpde_lod3d_get_state(self.h, _ptr(out), 1 if _is_dev(out) else 0),
+              "fpde_lod3d_get_state")
+        return out
+
+    def reset(self, u0):
+        u0 = _f64(u0)
+        check(self.ctx.lib.fpde_lod3d_reset(self.h, _ptr(u0), 1 if _is_dev(u0) else 0), "fpde_lod3d_reset")
+
+    def solve_host(self, u0, steps, out):
+        check(self.ctx.lib.fpde_lod3d_solve_host(self.h, _ptr(u0), steps, _ptr(out)), "fpde_lod3d_solve_host")
+        return out

@@ -17,7 +17,10 @@ OBJ = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libfpde_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC = os.environ.get("NVCC", "nvcc")
+# Host code keeps the reference's evaluation order: no FMA contraction (the Arm host
+# compiler contracts by default, the x86 one has no FMA without -mfma).
 FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
+                "-Xcompiler", "-ffp-contract=off",
                 "-I", os.path.join(ROOT, "include"), "-I", CSRC, "--expt-relaxed-constexpr"]
 
 

@@ -182,6 +182,13 @@ int launch_l1_partial(cudaStream_t st, const double *D, int64_t P, int n, const 
     return FPDE_OK;
 }
 
+int launch_append(cudaStream_t st, const double *u, double *last, double *row, int64_t nodes, int64_t P)
+{
+    k_append<<<(unsigned)((P + 255) / 256), 256, 0, st>>>(u, last, row, nodes, P);
+    FPDE_LAUNCHED(1);
+    return FPDE_OK;
+}
+
 int choose_splits(int n, int64_t P)
 {
     // Split the rows so that ~32 CTAs per SM are in flight (the stream needs many loads

@@ -14,6 +14,8 @@ double l1_lag(double alpha, int64_t j);
 int launch_l1_partial(cudaStream_t st, const double *D, int64_t P, int n, const double *wt,
                       double *part, int KS);
 int choose_splits(int n, int64_t P);
+// row[i] = u[i] - last[i], last[i] = u[i] for i < nodes; row[i] = 0 up to P.
+int launch_append(cudaStream_t st, const double *u, double *last, double *row, int64_t nodes, int64_t P);
 
 }  // namespace fpde
 

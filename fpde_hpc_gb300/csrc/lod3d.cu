@@ -1,0 +1,395 @@
+// 3D LOD time stepping (fpde_lod3d_*): the reference's mode-3 calc_step
+// (fpde_hpc_1d.cpp:5144-5779, implicit3d 0, split3d 0) on the GPU.
+//
+// Per time step n:
+//   1. k_l1_partial  : part[ks][q] = sum_t w[n-t] D_t[q] over the whole grid (FP64 history)
+//   2. K pass        : lines along k for every (i, j); Om = -lam U + Rp + S (time_summing
+//                      is added only in this pass, Om1 :4165-4268 with m3d_c == 2)
+//   3. _M pass       : lines along j for every (i, k); Om = -lam U
+//   4. sN pass       : lines along i for every (j, k); Om = -lam U
+//   5. append        : D_n = U - U_old over the grid (the snapshot of the step, :5733-5745)
+// Each pass is a Thomas solve per line with R = Rlap + lam (A_/B/R :3095-3142). For a
+// uniform step the alpha recurrence Al[p+1] = B/(R - A Al[p]) is time-invariant, so it is
+// evaluated once on the host in the reference's order; a pass then needs two first-order
+// recurrences per line (y forward into U in place, U backward).
+//
+// HBM layout: the state and every grid input keep the reference's index
+// idx = i + j (sN+2) + k (sN+2)(M+2) (:1181). The per-pass line coefficients (A, g =
+// Al[p+1]/B, al = Al[p+1]) are stored pass-line-major, c[p * lines + line], so the threads of
+// a warp (consecutive lines) read consecutive addresses in every pass. K and _M lines are
+// numbered with i fastest, so their state accesses are coalesced too; the sN pass walks
+// along the contiguous axis and relies on L1 for reuse of each line's cache lines.
+// The whole run is captured once into a CUDA graph and replayed.
+#include <map>
+#include <vector>
+#include <cmath>
+#include <string>
+
+#include "common.cuh"
+#include "kernels.cuh"
+
+namespace fpde {
+
+struct LodPassArgs {
+    double *U;
+    const double *A, *g, *al;        // (Nl+1) x lines, pass-line-major
+    const double *part;              // history partials [KS][pstride] (K pass), or KS = 0
+    int KS;
+    int64_t pstride;
+    const double *rp;                // K-pass source grid of this step, may be null
+    const double *bc;                // boundary grid of this step (line ends), may be null (0)
+    double lam;
+    int Nl, lines, n1;               // line = a + n1 * b
+    int64_t s1, s2, st;              // base = (1+a) s1 + (1+b) s2, node stride st
+    int lkind, rkind;
+    double dLN;
+};
+
+__global__ void __launch_bounds__(128) k_lod_pass(LodPassArgs p)
+{
+    const int line = blockIdx.x * blockDim.x + threadIdx.x;
+    if (line >= p.lines) return;
+    const int a = line % p.n1, b = line / p.n1;
+    const int64_t base = (int64_t)(1 + a) * p.s1 + (int64_t)(1 + b) * p.s2;
+    const int Nl = p.Nl, L = p.lines;
+    const double g0 = p.bc ? p.bc[base] : 0.0;
+    // forward: y_q = Bt[q+1] = g_q (A_q y_{q-1} - Om_q), y_0 = Bt[1] = g0; y_q overwrites U_q
+    double y = g0, uold_last = 0.0;
+    for (int q = 1; q < Nl; ++q) {
+        const int64_t id = base + (int64_t)q * p.st;
+        const double u = p.U[id];
+        if (q == Nl - 1) uold_last = u;
+        double om = -(p.lam * u) + (p.rp ? p.rp[id] : 0.0);
+        if (p.KS > 0) {
+            double s = 0.0;
+            for (int k = 0; k < p.KS; ++k) s += __ldcg(p.part + (int64_t)k * p.pstride + id);
+            om += s;
+        }
+        y = __ldg(p.g + (int64_t)q * L + line) * (__ldg(p.A + (int64_t)q * L + line) * y - om);
+        p.U[id] = y;
+    }
+    // right end: Dirichlet value or the flux closure of U1 (:4687-4719) with the old U[Nl-1]
+    const double gN = p.bc ? p.bc[base + (int64_t)Nl * p.st] : 0.0;
+    double uN;
+    if (p.rkind == FPDE_BC_DIRICHLET) {
+        uN = gN;
+    } else {
+        const double AlN = __ldg(p.al + (int64_t)(Nl - 1) * L + line);
+        if (fabs(y) > 1e-15) uN = (fabs(1.0 - AlN) > 1e-15) ? (y + gN * p.dLN) / (1.0 - AlN) : uold_last;
+        else uN = (fabs(1.0 - AlN) > 1e-15) ? 0.0 : uold_last;
+    }
+    p.U[base + (int64_t)Nl * p.st] = uN;
+    p.U[base + (int64_t)(Nl + 1) * p.st] = uN;                  // ghost copy (U1 :4792)
+    double u = uN;
+    for (int q = Nl - 1; q >= 1; --q) {
+        const int64_t id = base + (int64_t)q * p.st;
+        u = fma(__ldg(p.al + (int64_t)q * L + line), u, p.U[id]);
+        p.U[id] = u;
+    }
+    p.U[base] = fma(__ldg(p.al + line), u, g0);                   // Al[1] U[1] + Bt[1]
+}
+
+}  // namespace fpde
+
+using namespace fpde;
+
+struct fpde_lod3d {
+    fpde_ctx *ctx = nullptr;
+    fpde_lod3d_desc d{};
+    int dims[3] = {0, 0, 0};                 // sN, M, K
+    int64_t G = 0, P = 0;
+    int max_steps = 0;
+    double lam = 0.0, lamR = 0.0;
+    double *U = nullptr, *last = nullptr, *D = nullptr, *part = nullptr, *wrev = nullptr;
+    double *rp = nullptr, *bc = nullptr;
+    int rp_rows = 0, bc_rows = 0;
+    double *cA[3] = {nullptr, nullptr, nullptr}, *cg[3] = {nullptr, nullptr, nullptr},
+           *cal[3] = {nullptr, nullptr, nullptr};
+    int lines[3] = {0, 0, 0};
+    int64_t n_done = 0;
+    std::map<std::pair<int64_t, int>, cudaGraphExec_t> graphs;
+    std::map<std::pair<int64_t, int>, int64_t> graph_launches;
+};
+
+namespace fpde {
+
+// Pass geometry (pass 0 = sN along i, 1 = _M along j, 2 = K along k): line count, the two
+// line-index ranges (first fastest) with their strides, the node stride and Nl.
+static void pass_geometry(const fpde_lod3d *L, int pass, int *Nl, int *n1, int *n2, int64_t *s1, int64_t *s2,
+                          int64_t *st)
+{
+    const int sN = L->dims[0], M = L->dims[1], K = L->dims[2];
+    const int64_t sx = 1, sy = sN + 2, sz = (int64_t)(sN + 2) * (M + 2);
+    if (pass == 2) { *Nl = K; *n1 = sN - 1; *n2 = M - 1; *s1 = sx; *s2 = sy; *st = sz; }
+    else if (pass == 1) { *Nl = M; *n1 = sN - 1; *n2 = K - 1; *s1 = sx; *s2 = sz; *st = sy; }
+    else { *Nl = sN; *n1 = M - 1; *n2 = K - 1; *s1 = sy; *s2 = sz; *st = sx; }
+}
+
+static int lod_launch_pass(fpde_lod3d *L, cudaStream_t st, int pass, int64_t n, int KS)
+{
+    LodPassArgs a;
+    int n2;
+    pass_geometry(L, pass, &a.Nl, &a.n1, &n2, &a.s1, &a.s2, &a.st);
+    a.lines = L->lines[pass];
+    a.U = L->U;
+    a.A = L->cA[pass]; a.g = L->cg[pass]; a.al = L->cal[pass];
+    a.part = pass == 2 ? L->part : nullptr;
+    a.KS = pass == 2 ? KS : 0;
+    a.pstride = L->P;
+    a.rp = (pass == 2 && L->rp) ? L->rp + (n < L->rp_rows ? n : L->rp_rows - 1) * L->G : nullptr;
+    a.bc = L->bc ? L->bc + (n < L->bc_rows ? n : L->bc_rows - 1) * L->G : nullptr;
+    a.lam = L->lam;
+    a.lkind = L->d.left_kind[pass];
+    a.rkind = L->d.right_kind[pass];
+    a.dLN = L->d.dLN[pass];
+    if (a.lines <= 0) return FPDE_OK;
+    k_lod_pass<<<(unsigned)((a.lines + 127) / 128), 128, 0, st>>>(a);
+    FPDE_LAUNCHED(1);
+    return FPDE_OK;
+}
+
+static int lod_enqueue(fpde_lod3d *L, cudaStream_t st, int64_t n0, int steps, int64_t *nk)
+{
+    int64_t k = 0;
+    int rc;
+    for (int64_t n = n0; n < n0 + steps; ++n) {
+        int KS = 0;
+        if (n >= 1) {
+            KS = choose_splits((int)n, L->P);
+            const double *wt = L->wrev + (L->max_steps - n);         // wt[t] = w[n - t]
+            if ((rc = launch_l1_partial(st, L->D, L->P, (int)n, wt, L->part, KS))) return rc;
+            ++k;
+        }
+        for (int pass = 2; pass >= 0; --pass) {                      // K, _M, sN (calc_step order)
+            if ((rc = lod_launch_pass(L, st, pass, n, KS))) return rc;
+            ++k;
+        }
+        if ((rc = launch_append(st, L->U, L->last, L->D + n * L->P, L->G, L->P))) return rc;
+        ++k;
+    }
+    *nk = k;
+    return FPDE_OK;
+}
+
+}  // namespace fpde
+
+extern "C" {
+
+int fpde_lod3d_destroy(fpde_lod3d *L)
+{
+    if (!L) return FPDE_OK;
+    if (L->ctx) {
+        cudaSetDevice(L->ctx->device);
+        cudaStreamSynchronize(L->ctx->stream);
+    }
+    for (auto &kv : L->graphs) cudaGraphExecDestroy(kv.second);
+    for (double *p : {L->U, L->last, L->D, L->part, L->wrev, L->rp, L->bc}) dev_free(p);
+    for (int q = 0; q < 3; ++q) {
+        dev_free(L->cA[q]);
+        dev_free(L->cg[q]);
+        dev_free(L->cal[q]);
+    }
+    delete L;
+    return FPDE_OK;
+}
+
+int fpde_lod3d_create(fpde_ctx *ctx, const fpde_lod3d_desc *desc, const double *coefA, const double *coefB,
+                      const double *coefRlap, const double *u0, fpde_lod3d **out)
+{
+    clear_error();
+    FPDE_CHECK_ARG(out && desc && coefA && coefB && coefRlap && u0, "null argument");
+    *out = nullptr;
+    int rc = ctx_enter(ctx);
+    if (rc) return rc;
+    const fpde_lod3d_desc &d = *desc;
+    FPDE_CHECK_ARG(d.sN >= 2 && d.M >= 2 && d.K >= 2, "every axis needs at least 2 intervals");
+    FPDE_CHECK_ARG(d.lag_weights || (d.alpha > 0.0 && d.alpha < 1.0), "alpha must be in (0, 1)");
+    FPDE_CHECK_ARG(d.tau > 0.0 && d.max_steps > 0, "tau and max_steps must be positive");
+    FPDE_CHECK_ARG(d.precision == FPDE_PREC_FP64, "the 3D LOD path computes in FP64");
+    FPDE_CHECK_ARG(!d.source || d.source_rows >= 1, "source needs source_rows >= 1");
+    FPDE_CHECK_ARG(!d.bc || d.bc_rows >= 1, "bc needs bc_rows >= 1");
+    for (int q = 0; q < 3; ++q)
+        FPDE_CHECK_ARG((d.left_kind[q] == 0 || d.left_kind[q] == 1) && (d.right_kind[q] == 0 || d.right_kind[q] == 1),
+                       "bad boundary kind");
+
+    fpde_lod3d *L = new fpde_lod3d();
+    L->ctx = ctx;
+    L->d = d;
+    L->dims[0] = d.sN; L->dims[1] = d.M; L->dims[2] = d.K;
+    L->G = (int64_t)(d.sN + 2) * (d.M + 2) * (d.K + 2);
+    L->P = (L->G + 511) / 512 * 512;
+    L->max_steps = d.max_steps;
+    if (d.lag_weights) {
+        L->lam = L->lamR = d.lag_weights[0];
+    } else {                                   // lam as in Om1 (:4191), lamR as in R (:3120)
+        const double kkk0 = l1_interval_weight(d.alpha, 0.0, d.tau);
+        L->lam = d.Da * (kkk0 / d.tau);
+        L->lamR = d.Da * kkk0 / d.tau;
+    }
+    const double kkk0 = d.lag_weights ? 0.0 : l1_interval_weight(d.alpha, 0.0, d.tau);
+    std::vector<double> wrev(L->max_steps + 1, 0.0);               // wrev[m] = w[max_steps - m]
+    for (int64_t m = 0; m < L->max_steps; ++m) {
+        const int64_t j = L->max_steps - m;
+        wrev[m] = d.lag_weights ? d.lag_weights[j] : d.Da * (kkk0 * l1_lag(d.alpha, j)) / d.tau;
+    }
+    const size_t gbytes = (size_t)L->G * sizeof(double), pbytes = (size_t)L->P * sizeof(double);
+    bool fail = dev_alloc((void **)&L->U, pbytes) || dev_alloc((void **)&L->last, pbytes) ||
+                dev_alloc((void **)&L->D, (size_t)L->max_steps * pbytes) ||
+                dev_alloc((void **)&L->part, (size_t)KS_MAX * pbytes) ||
+                dev_alloc((void **)&L->wrev, wrev.size() * sizeof(double));
+    if (!fail && d.source) {
+        L->rp_rows = std::min(d.source_rows, d.max_steps);
+        fail = dev_alloc((void **)&L->rp, (size_t)L->rp_rows * gbytes);
+    }
+    if (!fail && d.bc) {
+        L->bc_rows = std::min(d.bc_rows, d.max_steps);
+        fail = dev_alloc((void **)&L->bc, (size_t)L->bc_rows * gbytes);
+    }
+    // per-pass line coefficients, evaluated in the reference's order (al1 :4002-4027)
+    std::vector<double> hA, hg, hal;
+    cudaStream_t st = ctx->stream;
+    for (int pass = 0; pass < 3 && !fail; ++pass) {
+        int Nl, n1, n2;
+        int64_t s1, s2, stp;
+        pass_geometry(L, pass, &Nl, &n1, &n2, &s1, &s2, &stp);
+        const int lines = n1 * n2;
+        L->lines[pass] = lines;
+        const size_t cnt = (size_t)(Nl + 1) * lines;
+        hA.assign(cnt, 0.0);
+        hg.assign(cnt, 0.0);
+        hal.assign(cnt, 0.0);
+        const double *cA = coefA + (int64_t)pass * L->G, *cB = coefB + (int64_t)pass * L->G,
+                     *cR = coefRlap + (int64_t)pass * L->G;
+        for (int line = 0; line < lines; ++line) {
+            const int a = line % n1, b = line / n1;
+            const int64_t base = (int64_t)(1 + a) * s1 + (int64_t)(1 + b) * s2;
+            double Al = d.left_kind[pass] == FPDE_BC_FLUX ? 1.0 : 0.0;            // Al[1]
+            hal[line] = Al;
+            for (int q = 1; q < Nl; ++q) {
+                const int64_t id = base + (int64_t)q * stp;
+                const double R = cR[id] + L->lamR;
+                const double Aq = cA[id], Bq = cB[id];
+                Al = Bq / (R - Aq * Al);                                           // Al[q+1]
+                hal[(size_t)q * lines + line] = Al;
+                hg[(size_t)q * lines + line] = Al / Bq;
+                hA[(size_t)q * lines + line] = Aq;
+            }
+        }
+        fail = dev_alloc((void **)&L->cA[pass], cnt * sizeof(double)) ||
+               dev_alloc((void **)&L->cg[pass], cnt * sizeof(double)) ||
+               dev_alloc((void **)&L->cal[pass], cnt * sizeof(double));
+        if (!fail) {                                                  // synchronous: host vectors are reused
+            fail = cudaMemcpy(L->cA[pass], hA.data(), cnt * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess ||
+                   cudaMemcpy(L->cg[pass], hg.data(), cnt * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess ||
+                   cudaMemcpy(L->cal[pass], hal.data(), cnt * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess;
+            if (fail) set_error(FPDE_ERR_CUDA, "lod3d: coefficient upload failed");
+        }
+    }
+    if (fail) {
+        std::string keep = fpde_last_error_string();
+        fpde_lod3d_destroy(L);
+        return set_error(FPDE_ERR_NOMEM, "%s", keep.c_str());
+    }
+    cudaMemsetAsync(L->U, 0, pbytes, st);
+    cudaMemcpyAsync(L->U, u0, gbytes, cudaMemcpyHostToDevice, st);
+    cudaMemsetAsync(L->last, 0, pbytes, st);
+    cudaMemcpyAsync(L->last, u0, gbytes, cudaMemcpyHostToDevice, st);
+    cudaMemsetAsync(L->D, 0, (size_t)L->max_steps * pbytes, st);
+    cudaMemcpyAsync(L->wrev, wrev.data(), wrev.size() * sizeof(double), cudaMemcpyHostToDevice, st);
+    if (L->rp) cudaMemcpyAsync(L->rp, d.source, (size_t)L->rp_rows * gbytes, cudaMemcpyHostToDevice, st);
+    if (L->bc) cudaMemcpyAsync(L->bc, d.bc, (size_t)L->bc_rows * gbytes, cudaMemcpyHostToDevice, st);
+    cudaError_t e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) {
+        fpde_lod3d_destroy(L);
+        return set_error(FPDE_ERR_CUDA, "lod3d setup: %s", cudaGetErrorString(e));
+    }
+    L->d.lag_weights = nullptr;                 // host pointers are not kept
+    L->d.source = nullptr;
+    L->d.bc = nullptr;
+    *out = L;
+    return FPDE_OK;
+}
+
+int fpde_lod3d_run(fpde_lod3d *L, int steps)
+{
+    clear_error();
+    FPDE_CHECK_ARG(L && steps >= 0, "bad arguments");
+    int rc = ctx_enter(L->ctx);
+    if (rc) return rc;
+    if (steps == 0) return FPDE_OK;
+    if (L->n_done + steps > L->max_steps)
+        return set_error(FPDE_ERR_CAPACITY, "run of %d steps exceeds the history capacity %d", steps, L->max_steps);
+    auto key = std::make_pair(L->n_done, steps);
+    auto it = L->graphs.find(key);
+    if (it == L->graphs.end()) {
+        cudaStream_t cs;
+        FPDE_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+        cudaGraph_t graph;
+        FPDE_CUDA(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
+        int64_t nk = 0;
+        const int64_t before = fpde_kernel_launch_count();
+        rc = lod_enqueue(L, cs, L->n_done, steps, &nk);
+        cudaError_t e = cudaStreamEndCapture(cs, &graph);
+        count_launches(-(fpde_kernel_launch_count() - before));         // counted at replay
+        cudaStreamDestroy(cs);
+        if (rc) return rc;
+        if (e != cudaSuccess) return set_error(FPDE_ERR_CUDA, "graph capture: %s", cudaGetErrorString(e));
+        cudaGraphExec_t exec;
+        e = cudaGraphInstantiate(&exec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (e != cudaSuccess) return set_error(FPDE_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(e));
+        it = L->graphs.emplace(key, exec).first;
+        L->graph_launches[key] = nk;
+    }
+    FPDE_CUDA(cudaGraphLaunch(it->second, L->ctx->stream));
+    count_launches(L->graph_launches[key]);
+    L->n_done += steps;
+    return FPDE_OK;
+}
+
+int fpde_lod3d_get_state(fpde_lod3d *L, double *u, int on_device)
+{
+    clear_error();
+    FPDE_CHECK_ARG(L && u, "null argument");
+    int rc = ctx_enter(L->ctx);
+    if (rc) return rc;
+    FPDE_CUDA(cudaMemcpyAsync(u, L->U, L->G * sizeof(double),
+                              on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, L->ctx->stream));
+    FPDE_CUDA(cudaStreamSynchronize(L->ctx->stream));
+    return ctx_check_flags(L->ctx, "lod3d");
+}
+
+int fpde_lod3d_reset(fpde_lod3d *L, const double *u0, int on_device)
+{
+    clear_error();
+    FPDE_CHECK_ARG(L && u0, "null argument");
+    int rc = ctx_enter(L->ctx);
+    if (rc) return rc;
+    const cudaMemcpyKind kind = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+    FPDE_CUDA(cudaMemcpyAsync(L->U, u0, L->G * sizeof(double), kind, L->ctx->stream));
+    FPDE_CUDA(cudaMemcpyAsync(L->last, u0, L->G * sizeof(double), kind, L->ctx->stream));
+    if (!on_device) FPDE_CUDA(cudaStreamSynchronize(L->ctx->stream));
+    L->n_done = 0;
+    return FPDE_OK;
+}
+
+int fpde_lod3d_solve_host(fpde_lod3d *L, const double *u0_host, int steps, double *u_out_host)
+{
+    clear_error();
+    FPDE_CHECK_ARG(L && u0_host && u_out_host, "null argument");
+    int rc = fpde_lod3d_reset(L, u0_host, 0);
+    if (rc) return rc;
+    if ((rc = fpde_lod3d_run(L, steps))) return rc;
+    FPDE_CUDA(cudaMemcpyAsync(u_out_host, L->U, L->G * sizeof(double), cudaMemcpyDeviceToHost, L->ctx->stream));
+    FPDE_CUDA(cudaStreamSynchronize(L->ctx->stream));
+    return ctx_check_flags(L->ctx, "lod3d");
+}
+
+int fpde_lod3d_steps_done(const fpde_lod3d *L, int64_t *n)
+{
+    FPDE_CHECK_ARG(L && n, "null argument");
+    *n = L->n_done;
+    return FPDE_OK;
+}
+
+}  // extern "C"

@@ -142,3 +142,73 @@ def config3(N=16384, steps=4096, tau=1e-4):
     u0[0] = u0[-1] = 0.0
     a, w = gauss_legendre_01(16)
     return DOProblem(f"config3_DO_N{N}", N, tau, steps, k, u0, a, w * 6.0 * a * (1.0 - a))
+
+
+def lognormal_field_3d(shape, mu, sigma, ell, seed, h):
+    """3D version of lognormal_field on a (nz, ny, nx) grid with uniform spacing h."""
+    rng = np.random.default_rng(seed)
+    w = rng.standard_normal(shape)
+    fz = np.fft.fftfreq(shape[0], d=h)[:, None, None]
+    fy = np.fft.fftfreq(shape[1], d=h)[None, :, None]
+    fx = np.fft.rfftfreq(shape[2], d=h)[None, None, :]
+    kern = np.exp(-0.5 * (2 * np.pi * ell) ** 2 * (fz ** 2 + fy ** 2 + fx ** 2))
+    g = np.fft.irfftn(np.fft.rfftn(w) * kern, s=shape, axes=(0, 1, 2))
+    g = (g - g.mean()) / g.std()
+    return np.exp(mu + sigma * g)
+
+
+@dataclass
+class LodProblem:
+    """3D LOD problem on (sN+2)(M+2)(K+2) grid points, grids shaped (K+2, M+2, sN+2)."""
+    name: str
+    dims: tuple         # (sN, M, K) intervals
+    alpha: float
+    tau: float
+    steps: int
+    k: np.ndarray       # conductivity at every grid point
+    u0: np.ndarray
+    left_kind: tuple = (0, 0, 0)
+    right_kind: tuple = (0, 0, 0)
+
+    @property
+    def h(self):
+        return tuple(1.0 / n for n in self.dims)
+
+    @property
+    def dLN(self):
+        return self.h
+
+    @property
+    def Da(self):
+        return 1.0 / math.gamma(1.0 - self.alpha)
+
+    def coefs(self):
+        """Per-pass A, B, Rlap grids (pass 0 along i, 1 along j, 2 along k) from node-sampled k
+        at p and p-1 along the pass axis (A_/B/R of fpde_hpc_1d.cpp with gamma = 1, iw = 1)."""
+        shape = self.u0.shape
+        cA, cB, cR = (np.zeros((3,) + shape) for _ in range(3))
+        for pss, axis in ((0, 2), (1, 1), (2, 0)):
+            hh = self.h[pss]
+            km = np.roll(self.k, 1, axis=axis)          # k at p-1 (wraps only at p = 0, unused)
+            cA[pss] = km / (hh * hh)
+            cB[pss] = self.k / (hh * hh)
+            cR[pss] = (self.k / (hh * hh)) + (km / (hh * hh))
+        return cA, cB, cR
+
+    @property
+    def node_steps(self):
+        sN, M, K = self.dims
+        return (sN - 1) * (M - 1) * (K - 1) * self.steps
+
+
+def config4(n=128, steps=1024, tau=1e-3):
+    """3D n^3 (default 128^3), alpha 0.85, LOD x/y/z, lognormal k (mu 0, sigma 0.4, ell 0.05,
+    seed 5), Gaussian blob initial state (centre (0.5, 0.5, 0.6), width 0.1), zero-flux sides
+    (i and j passes), Dirichlet 0 top and bottom (k pass)."""
+    shape = (n + 2, n + 2, n + 2)
+    k = lognormal_field_3d(shape, 0.0, 0.4, 0.05, 5, 1.0 / n)
+    z, y, x = np.meshgrid(*(np.arange(n + 2) / n for _ in range(3)), indexing="ij")
+    u0 = np.exp(-((x - 0.5) ** 2 + (y - 0.5) ** 2 + (z - 0.6) ** 2) / (2 * 0.1 ** 2))
+    u0[0] = 0.0
+    u0[n:] = 0.0
+    return LodProblem(f"config4_{n}^3", (n, n, n), 0.85, tau, steps, k, u0, (1, 1, 0), (1, 1, 0))

@@ -59,6 +59,7 @@ enum fpde_bc_kind {
 typedef struct fpde_ctx fpde_ctx;
 typedef struct fpde_hist fpde_hist;
 typedef struct fpde_line fpde_line;
+typedef struct fpde_lod3d fpde_lod3d;
 
 /* ---------------------------------------------------------------- context */
 
@@ -274,6 +275,46 @@ int fpde_line_probe_stats(fpde_line *line, int kind, double *ms, double *bytes, 
  * Rlap[i] = iw[i] (k[i]/dL[i]^2 + k[i-1]/(dL[i] dL[i-1])), i = 1..N-1. Host. iw may be NULL (1). */
 int fpde_line_coefs(int64_t N, const double *k, const double *iw, const double *dL,
                     double *A, double *B, double *Rlap);
+
+/* ------------------------------------------------------------------ 3D LOD */
+
+/* The 3D locally-one-dimensional step of the reference (calc_step, mode 3 with implicit3d 0
+ * and split3d 0, fpde_hpc_1d.cpp:5144-5779): per time step the history sum, then Thomas
+ * passes along k (K, with the history and the source Rp, Om1 :4165-4268 for m3d_c == 2),
+ * along j (_M) and along i (sN), each with R = Rlap + Da*kkk0/tau and Om = -Da*(kkk0/tau) U
+ * (+ Rp + Da S in the K pass), and a ghost copy at the far end of every line (U1 :4792).
+ * The grid has (sN+2)(M+2)(K+2) points with idx = i + j (sN+2) + k (sN+2)(M+2) (:1181). */
+typedef struct fpde_lod3d_desc {
+    int sN, M, K;           /* intervals along i, j, k */
+    double alpha, tau, Da;  /* as for lines; tau uniform */
+    int left_kind[3];       /* per pass (0 = sN, 1 = _M, 2 = K): fpde_bc_kind at the line start */
+    int right_kind[3];      /* and at the line end (flux: the U1 closure with dLN[pass]) */
+    double dLN[3];
+    int precision;          /* FPDE_PREC_FP64 */
+    int max_steps;          /* history capacity */
+    const double *lag_weights; /* optional, as in fpde_line_desc */
+    const double *source;   /* optional host grids Rp of the K pass, source_rows x grid; step n uses
+                               row min(n, source_rows-1) */
+    int source_rows;
+    const double *bc;       /* optional host grids of boundary data (Dirichlet values / fluxes at the
+                               line ends), bc_rows x grid; NULL = 0 */
+    int bc_rows;
+} fpde_lod3d_desc;
+
+/* coefA/B/Rlap: three host grids each (pass 0 = sN, 1 = _M, 2 = K) of the line coefficients at
+ * every node (A_/B/R of the pass's axis, :3095-3142); u0: the initial grid. Replaces the
+ * H_solver set-up of a 3D run plus init_opencl (:1715-1883). */
+int fpde_lod3d_create(fpde_ctx *ctx, const fpde_lod3d_desc *desc, const double *coefA, const double *coefB,
+                      const double *coefRlap, const double *u0, fpde_lod3d **out);
+int fpde_lod3d_destroy(fpde_lod3d *lod);
+/* Advance `steps` steps (one CUDA graph per (start, steps)). */
+int fpde_lod3d_run(fpde_lod3d *lod, int steps);
+int fpde_lod3d_get_state(fpde_lod3d *lod, double *u, int on_device);
+/* New initial grid and an empty history. */
+int fpde_lod3d_reset(fpde_lod3d *lod, const double *u0, int on_device);
+/* End-to-end call: upload u0 from host, run `steps`, download the grid to host. */
+int fpde_lod3d_solve_host(fpde_lod3d *lod, const double *u0_host, int steps, double *u_out_host);
+int fpde_lod3d_steps_done(const fpde_lod3d *lod, int64_t *n);
 
 #ifdef __cplusplus
 }

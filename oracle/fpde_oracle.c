@@ -201,6 +201,18 @@ int fo_lod_step_dirichlet(int sN, int M, int K, double *U, double *hist, int n,
                           const double *coefA, const double *coefB, const double *coefRlap,
                           const double *rp, const double *bc, double *S_out)
 {
+    const int kinds[3] = {0, 0, 0};
+    const double dLN[3] = {0.0, 0.0, 0.0};
+    return fo_lod_step(sN, M, K, U, hist, n, kb, tau, Da, kkk0, coefA, coefB, coefRlap, rp, bc, kinds, kinds, dLN,
+                       S_out);
+}
+
+int fo_lod_step(int sN, int M, int K, double *U, double *hist, int n,
+                const double *kb, const double *tau, double Da, double kkk0,
+                const double *coefA, const double *coefB, const double *coefRlap,
+                const double *rp, const double *bc, const int *lkind, const int *rkind, const double *dLN,
+                double *S_out)
+{
     const double lam = Da * (kkk0 / tau[n]);      /* Om1 :4191 */
     const double lamR = Da * kkk0 / tau[n];       /* R :3120 */
     const int64_t sx = 1, sy = sN + 2, sz = (int64_t)(sN + 2) * (M + 2);
@@ -244,10 +256,11 @@ int fo_lod_step_dirichlet(int sN, int M, int K, double *U, double *hist, int n,
                 for (int p = 1; p < Nl; p++) {
                     int64_t id = base + p * st;
                     la[p] = cA[id]; lb[p] = cB[id]; lr[p] = cR[id] + lamR;
-                    lo[p] = -(lam * lu[p]) + (pass == 2 ? rp[id] : 0.0);
+                    lo[p] = -(lam * lu[p]) + ((pass == 2 && rp) ? rp[id] : 0.0);
                     if (pass == 2) lo[p] += Da * S[id];
                 }
-                thomas_core(Nl, la, lb, lr, lo, 0, bc[base], 0, bc[base + Nl * st], 0.0, lu, Al, Bt);
+                thomas_core(Nl, la, lb, lr, lo, lkind[pass], bc[base], rkind[pass], bc[base + Nl * st], dLN[pass],
+                            lu, Al, Bt);
                 lu[Nl + 1] = lu[Nl];                                 /* U1 :4792 */
                 for (int p = 0; p <= Nl + 1; p++) U[base + p * st] = lu[p];
             }

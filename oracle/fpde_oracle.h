@@ -104,6 +104,15 @@ int fo_lod_step_dirichlet(int sN, int M, int K, double *U, double *hist, int n,
                           const double *coefA, const double *coefB, const double *coefRlap,
                           const double *rp, const double *bc, double *S_out);
 
+/* The same step with boundary kinds per pass (index = pass: 0 sN, 1 _M, 2 K): lkind/rkind 0
+ * Dirichlet with the value from bc at the line end, 1 the flux form of al1 (Al[1] = 1,
+ * Bt[1] = bc) and the flux closure of U1 (:4687-4719) with the pass's last step dLN. */
+int fo_lod_step(int sN, int M, int K, double *U, double *hist, int n,
+                const double *kb, const double *tau, double Da, double kkk0,
+                const double *coefA, const double *coefB, const double *coefRlap,
+                const double *rp, const double *bc, const int *lkind, const int *rkind, const double *dLN,
+                double *S_out);
+
 /* ---- distributed order (fr_do.cpp) ---- */
 
 /* Caputo derivative of sampled F (Cder :74-86 with an F array): DF[t] for t = 1..ntau-1,

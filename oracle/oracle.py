@@ -15,6 +15,7 @@ _LIB_PATH = os.path.join(HERE, "_build", "libfpde_oracle.so")
 _lib = None
 
 _dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
+_ip = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
 
 
 def build():
@@ -47,6 +48,9 @@ def load():
     lib.fo_lod_step_dirichlet.argtypes = [i32, i32, i32, _dp, _dp, i32, _dp, _dp, d, d,
                                           _dp, _dp, _dp, _dp, _dp, vp]
     lib.fo_lod_step_dirichlet.restype = i32
+    lib.fo_lod_step.argtypes = [i32, i32, i32, _dp, _dp, i32, _dp, _dp, d, d, _dp, _dp, _dp, vp, _dp,
+                                _ip, _ip, _dp, vp]
+    lib.fo_lod_step.restype = i32
     lib.fo_caputo_derivative.argtypes = [i32, d, d, d, _dp, _dp]
     lib.fo_do_derivative.argtypes = [i32, d, i32, _dp, _dp, _dp, i32, i32, i32, _dp]
     lib.fo_do_fused_weights.argtypes = [i32, _dp, _dp, _dp, d, i32, _dp]
@@ -160,6 +164,40 @@ def lod_step_dirichlet(dims, U, hist, n, kb, tau, Da, kkk0, coefA, coefB, coefRl
                               coefA.reshape(-1), coefB.reshape(-1), coefRlap.reshape(-1),
                               rp.reshape(-1), bc.reshape(-1), _ptr(S))
     return S
+
+
+def lod_step(dims, U, hist, n, kb, tau, Da, kkk0, coefA, coefB, coefRlap, rp, bc, lkind=(0, 0, 0),
+             rkind=(0, 0, 0), dLN=(0.0, 0.0, 0.0), want_S=False):
+    """fo_lod_step: one LOD step with boundary kinds per pass (0 sN, 1 _M, 2 K); rp may be None."""
+    lib = load()
+    sN, M, K = dims
+    S = np.zeros_like(U) if want_S else None
+    rpp = None if rp is None else np.ascontiguousarray(rp, dtype=np.float64).reshape(-1)
+    lib.fo_lod_step(sN, M, K, U.reshape(-1), hist.reshape(-1), n,
+                    np.ascontiguousarray(kb, dtype=np.float64), np.ascontiguousarray(tau, dtype=np.float64),
+                    Da, kkk0, coefA.reshape(-1), coefB.reshape(-1), coefRlap.reshape(-1),
+                    None if rpp is None else rpp.ctypes.data_as(C.c_void_p),
+                    np.ascontiguousarray(bc, dtype=np.float64).reshape(-1),
+                    np.array(lkind, dtype=np.int32), np.array(rkind, dtype=np.int32),
+                    np.array(dLN, dtype=np.float64), _ptr(S))
+    return S
+
+
+def lod_run(dims, U0, steps, tau, alpha, Da, coefA, coefB, coefRlap, rp=None, bc=None, lkind=(0, 0, 0),
+            rkind=(0, 0, 0), dLN=(0.0, 0.0, 0.0)):
+    """Uniform-tau LOD run with the closed-form weights; returns the final grid."""
+    sN, M, K = dims
+    U = np.array(U0, dtype=np.float64)
+    G = U.shape
+    hist = np.zeros((steps,) + G)
+    taus = np.full(steps + 1, tau)
+    time = time_points(taus)
+    bc = np.zeros(G) if bc is None else bc
+    for n in range(steps):
+        kb, k0 = l1_weights(alpha, time, n)
+        lod_step(dims, U, hist, n, kb if n else np.zeros(1), taus, Da, k0, coefA, coefB, coefRlap, rp, bc,
+                 lkind, rkind, dLN)
+    return U
 
 
 def caputo_derivative(F, tau, a, g2a):

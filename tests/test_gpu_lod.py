@@ -1,0 +1,97 @@
+"""3D LOD path (fpde_lod3d_*) on the GPU against the reference's own run and the oracle.
+
+  * replay of the reference's mode-3 run (fixture fpde_lod3d_a2: 6 x 4 x 8 intervals,
+    alpha 0.85, 16 steps, the analytic test's Rp and boundary grids per step): every step's
+    grid equals the reference's to 1e-12;
+  * the benchmark form (lognormal k, zero-flux sides, Dirichlet top and bottom) on cubic and
+    non-cubic grids against the oracle's LOD restatement: 1e-12 or 4x the oracle's one-ulp
+    rounding envelope.
+"""
+import numpy as np
+import pytest
+
+import fgv
+import oracle
+from conftest import golden_path
+
+pytestmark = pytest.mark.gpu
+
+
+def relmax(a, b):
+    return float(np.max(np.abs(a - b)) / np.max(np.abs(b)))
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    import fpde_hpc_gb300 as fp
+    c = fp.Context(0)
+    yield c
+    c.close()
+
+
+def test_lod_replays_reference_run(ctx):
+    import fpde_hpc_gb300 as fp
+    g = fgv.load(golden_path("fpde_lod3d_a2"))
+    dims = (int(g["sN"]), int(g["M"]), int(g["K"]))
+    cA = np.stack([g["coefA_pass%d" % p] for p in range(3)])
+    cB = np.stack([g["coefB_pass%d" % p] for p in range(3)])
+    cR = np.stack([g["coefRlap_pass%d" % p] for p in range(3)])
+    taus = g["tau"]
+    assert np.all(taus == taus[0])
+    steps = len(taus)
+    lod = fp.Lod3D(ctx, dims, g["alpha"], taus[0], g["Da"], cA, cB, cR, g["U0"], steps,
+                   source=g["Rp"], bc=g["BC"])
+    worst = 0.0
+    for n in range(steps):
+        lod.run(1)
+        worst = max(worst, relmax(lod.state(), g["U"][n]))
+    lod.close()
+    print(f"LOD replay 6x4x8, {steps} steps: max rel {worst:.2e}")
+    assert worst <= 1e-12
+
+
+def _envelope(p, cA, cB, cR):
+    rng = np.random.default_rng(0)
+    pert = lambda x: x * (1 + 2.2e-16 * rng.choice([-1, 1], size=x.shape))
+    args = (None, None, p.left_kind, p.right_kind, p.dLN)
+    u1 = oracle.lod_run(p.dims, p.u0, p.steps, p.tau, p.alpha, p.Da, cA, cB, cR, *args)
+    u2 = oracle.lod_run(p.dims, p.u0, p.steps, p.tau, p.alpha, p.Da, pert(cA), pert(cB), pert(cR), *args)
+    return u1, relmax(u2, u1)
+
+
+@pytest.mark.parametrize("dims,steps", [((20, 20, 20), 40), ((24, 12, 18), 33)])
+def test_lod_benchmark_form_vs_oracle(ctx, dims, steps):
+    import fpde_hpc_gb300 as fp
+    from fpde_hpc_gb300 import problems
+    base = problems.config4(n=max(dims), steps=steps)
+    sN, M, K = dims
+    p = problems.LodProblem("lod", dims, base.alpha, base.tau, steps, base.k[:K + 2, :M + 2, :sN + 2].copy(),
+                            base.u0[:K + 2, :M + 2, :sN + 2].copy(), base.left_kind, base.right_kind)
+    p.u0[K:] = 0.0
+    cA, cB, cR = p.coefs()
+    lod = fp.Lod3D(ctx, dims, p.alpha, p.tau, p.Da, cA, cB, cR, p.u0, steps, left_kind=p.left_kind,
+                   right_kind=p.right_kind, dLN=p.dLN)
+    lod.run(steps)
+    u = lod.state()
+    lod.close()
+    uref, env = _envelope(p, cA, cB, cR)
+    err = relmax(u, uref)
+    print(f"LOD {dims} {steps} steps vs oracle: {err:.2e} (one-ulp envelope {env:.2e})")
+    assert err <= max(1e-12, 4 * env)
+
+
+def test_lod_runs_in_pieces_and_solve_host(ctx):
+    """Two runs of 10 steps equal one of 20; the host end-to-end call equals both."""
+    import fpde_hpc_gb300 as fp
+    from fpde_hpc_gb300 import problems
+    p = problems.config4(n=16, steps=20)
+    cA, cB, cR = p.coefs()
+    kw = dict(left_kind=p.left_kind, right_kind=p.right_kind, dLN=p.dLN)
+    lod = fp.Lod3D(ctx, p.dims, p.alpha, p.tau, p.Da, cA, cB, cR, p.u0, 20, **kw)
+    lod.run(10)
+    lod.run(10)
+    u_two = lod.state()
+    out = np.zeros_like(p.u0)
+    lod.solve_host(p.u0, 20, out)
+    lod.close()
+    assert np.array_equal(u_two, out)
