@@ -33,6 +33,12 @@ class Lod3dDesc(C.Structure):
                 ("bc", c_vp), ("bc_rows", c_int)]
 
 
+class ColumnDesc(C.Structure):
+    _fields_ = [("N", c_i64), ("alpha", c_dbl), ("tau", c_dbl), ("Da", c_dbl), ("left_kind", c_int),
+                ("left_value", c_dbl), ("right_kind", c_int), ("right_value", c_dbl), ("dLN", c_dbl),
+                ("A", c_vp), ("B", c_vp), ("Rlap", c_vp), ("u0", c_vp), ("lag_weights", c_vp)]
+
+
 # name -> (restype, argtypes)
 _SIGS = {
     "fpde_ctx_create": (c_int, [c_int, C.POINTER(c_vp)]),
@@ -46,6 +52,13 @@ _SIGS = {
     "fpde_weights_l1_lags": (c_int, [c_dbl, c_int, c_vp]),
     "fpde_gamma": (c_int, [c_dbl, P_dbl]),
     "fpde_do_weights": (c_int, [c_int, c_vp, c_vp, c_vp, c_dbl, c_int, c_vp]),
+    "fpde_batch_create": (c_int, [c_vp, C.POINTER(ColumnDesc), c_int, c_int, c_int, C.POINTER(c_vp)]),
+    "fpde_batch_destroy": (c_int, [c_vp]),
+    "fpde_batch_run": (c_int, [c_vp, c_int]),
+    "fpde_batch_get_state": (c_int, [c_vp, c_int, c_vp, c_int]),
+    "fpde_batch_layout": (c_int, [c_vp, c_int, C.POINTER(c_i64), C.POINTER(c_i64), C.POINTER(c_i64)]),
+    "fpde_batch_reset": (c_int, [c_vp, c_vp, c_int]),
+    "fpde_batch_solve_host": (c_int, [c_vp, c_vp, c_int, c_vp]),
     "fpde_lod3d_create": (c_int, [c_vp, C.POINTER(Lod3dDesc), c_vp, c_vp, c_vp, c_vp, C.POINTER(c_vp)]),
     "fpde_lod3d_destroy": (c_int, [c_vp]),
     "fpde_lod3d_run": (c_int, [c_vp, c_int]),

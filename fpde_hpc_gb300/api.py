@@ -3,7 +3,7 @@ import ctypes as C
 
 import numpy as np
 
-from ._lib import LineDesc, Lod3dDesc, check, load
+from ._lib import ColumnDesc, LineDesc, Lod3dDesc, check, load
 
 FP64, SPLIT_BF16, SPLIT_F16 = 0, 1, 2
 
@@ -301,3 +301,68 @@ class Lod3D:
     def solve_host(self, u0, steps, out):
         check(self.ctx.lib.fpde_lod3d_solve_host(self.h, _ptr(u0), steps, _ptr(out)), "fpde_lod3d_solve_host")
         return out
+
+
+class Batch:
+    """An ensemble of independent 1D Caputo columns (fpde_batch_*). columns: list of dicts with
+    N, alpha, tau, Da, A, B, Rlap, u0 and optional left/right (kind, value), dLN, lag_weights."""
+
+    def __init__(self, ctx, columns, max_steps, precision=FP64):
+        self.ctx = ctx
+        descs = (ColumnDesc * len(columns))()
+        keep = []
+        for d, c in zip(descs, columns):
+            arrs = [np.ascontiguousarray(c[k], dtype=np.float64) for k in ("A", "B", "Rlap", "u0")]
+            keep += arrs
+            left, right = c.get("left", (0, 0.0)), c.get("right", (0, 0.0))
+            d.N, d.alpha, d.tau, d.Da = c["N"], c.get("alpha", 0.5), c["tau"], c.get("Da", 1.0)
+            d.left_kind, d.left_value, d.right_kind, d.right_value = left[0], left[1], right[0], right[1]
+            d.dLN = c.get("dLN", 0.0)
+            d.A, d.B, d.Rlap, d.u0 = (a.ctypes.data for a in arrs)
+            if c.get("lag_weights") is not None:
+                w = np.ascontiguousarray(c["lag_weights"], dtype=np.float64)
+                keep.append(w)
+                d.lag_weights = w.ctypes.data
+        self.n_cols = len(columns)
+        self.h = C.c_void_p()
+        check(ctx.lib.fpde_batch_create(ctx.h, descs, len(columns), max_steps, precision, C.byref(self.h)),
+              "fpde_batch_create")
+        self.layout = []
+        for c in range(self.n_cols):
+            off, n, tot = C.c_int64(), C.c_int64(), C.c_int64()
+            check(ctx.lib.fpde_batch_layout(self.h, c, C.byref(off), C.byref(n), C.byref(tot)), "fpde_batch_layout")
+            self.layout.append((off.value, n.value))
+            self.total = tot.value
+
+    def close(self):
+        if self.h:
+            self.ctx.lib.fpde_batch_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def run(self, steps):
+        check(self.ctx.lib.fpde_batch_run(self.h, steps), "fpde_batch_run")
+
+    def state(self, col):
+        out = np.zeros(self.layout[col][1] + 1)
+        check(self.ctx.lib.fpde_batch_get_state(self.h, col, _ptr(out), 0), "fpde_batch_get_state")
+        return out
+
+    def pack(self, states):
+        """Padded device-layout vector from a list of per-column states."""
+        v = np.zeros(self.total)
+        for (off, n), u in zip(self.layout, states):
+            v[off:off + n + 1] = u
+        return v
+
+    def unpack(self, v):
+        return [v[off:off + n + 1].copy() for off, n in self.layout]
+
+    def reset(self, u_padded=None):
+        p = None if u_padded is None else _ptr(_f64(u_padded))
+        check(self.ctx.lib.fpde_batch_reset(self.h, p, 1 if (u_padded is not None and _is_dev(u_padded)) else 0),
+              "fpde_batch_reset")
+
+    def solve_host(self, u0_padded, steps, out_padded):
+        check(self.ctx.lib.fpde_batch_solve_host(self.h, _ptr(u0_padded), steps, _ptr(out_padded)),
+              "fpde_batch_solve_host")
+        return out_padded

@@ -1,0 +1,452 @@
+// Ensemble of independent 1D Caputo columns (fpde_batch_*): many lines of different length,
+// order and coefficients advanced together, two kernels per time step for the whole ensemble.
+//
+// Layout in HBM: the columns' nodes are concatenated, column c occupying
+// [off_c, off_c + P_c) with P_c = N_c + 1 rounded up to 512, so that every CTA of the
+// history sum (256 threads x 2 nodes) lies inside one column. The increments are one
+// time-major table D[t][sum_c P_c]; padding nodes stay zero.
+//
+// Per time step n:
+//   1. k_batch_partial : part[ks][q] = sum_t w_c[n-t] D_t[q], the column's lag weights picked
+//                        per CTA (one flat grid over all nodes: balanced by construction)
+//   2. k_batch_solve   : one CTA per column, launched largest first; Thomas per column
+//                        (fpde_hpc_1d.cpp al1/bt1/U1 :4002-4027, :4585-4590, :4683-4724) as
+//                        segment sweeps joined by a CTA scan, then U and D_n written.
+// The alpha recurrence is time-invariant and precomputed on the host per column.
+#include <algorithm>
+#include <cmath>
+#include <map>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "common.cuh"
+#include "kernels.cuh"
+#include "scan.cuh"
+
+namespace fpde {
+
+constexpr int BT = 256;       // threads per column CTA
+constexpr int BW = BT / 32;
+
+struct ColInfo {
+    int64_t off;              // first node of the column in the concatenated node space
+    int N;                    // intervals (nodes 0..N)
+    int seg;                  // nodes per thread segment (nodes 0..N-1 are swept)
+    double lam, g0, gN, dLN, AlN;
+    int rkind;
+    int pad;
+};
+
+__global__ void __launch_bounds__(256) k_batch_partial(const double2 *__restrict__ D, int64_t P2, int n,
+                                                       const double *__restrict__ wall, int64_t wstride,
+                                                       int64_t woff, const int *__restrict__ cta_col,
+                                                       double2 *__restrict__ part)
+{
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int ks = blockIdx.y, KS = gridDim.y;
+    const int t0 = (int)((int64_t)n * ks / KS), t1 = (int)((int64_t)n * (ks + 1) / KS);
+    if (i >= P2) return;
+    const double *wt = wall + (int64_t)cta_col[blockIdx.x] * wstride + woff;   // wt[t] = w_c[n - t]
+    double ax = 0.0, ay = 0.0;
+    int t = t0;
+    for (; t + 8 <= t1; t += 8) {
+        double2 v[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) v[u] = __ldcs(D + (int64_t)(t + u) * P2 + i);
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            const double w = __ldg(wt + t + u);
+            ax = fma(w, v[u].x, ax);
+            ay = fma(w, v[u].y, ay);
+        }
+    }
+    for (; t < t1; ++t) {
+        const double2 v = __ldcs(D + (int64_t)t * P2 + i);
+        const double w = __ldg(wt + t);
+        ax = fma(w, v.x, ax);
+        ay = fma(w, v.y, ay);
+    }
+    part[(int64_t)ks * P2 + i] = make_double2(ax, ay);
+}
+
+// Exclusive CTA scan of (P, X) pairs in thread order (up) or reverse order (down).
+template <bool UP>
+__device__ __forceinline__ void cta_scan_excl(double &P, double &X, double *wP, double *wX, int lane, int warp)
+{
+    if (UP) warp_scan_up(P, X, lane);
+    else warp_scan_down(P, X, lane);
+    double Pe = UP ? __shfl_up_sync(FULL, P, 1) : __shfl_down_sync(FULL, P, 1);
+    double Xe = UP ? __shfl_up_sync(FULL, X, 1) : __shfl_down_sync(FULL, X, 1);
+    if (lane == (UP ? 0 : 31)) { Pe = 1.0; Xe = 0.0; }
+    if (lane == (UP ? 31 : 0)) { wP[warp] = P; wX[warp] = X; }
+    __syncthreads();
+    if (warp == 0) {
+        double Pw = lane < BW ? wP[lane] : 1.0, Xw = lane < BW ? wX[lane] : 0.0;
+        if (UP) warp_scan_up(Pw, Xw, lane);
+        else warp_scan_down(Pw, Xw, lane);
+        double Pwe = UP ? __shfl_up_sync(FULL, Pw, 1) : __shfl_down_sync(FULL, Pw, 1);
+        double Xwe = UP ? __shfl_up_sync(FULL, Xw, 1) : __shfl_down_sync(FULL, Xw, 1);
+        if (UP ? lane == 0 : lane >= BW - 1) { Pwe = 1.0; Xwe = 0.0; }
+        __syncwarp();
+        if (lane < BW) { wP[lane] = Pwe; wX[lane] = Xwe; }
+    }
+    __syncthreads();
+    // compose: the warps before this one (wP, wX of this warp), then this warp's earlier lanes
+    X = fma(Pe, wX[warp], Xe);
+    P = Pe * wP[warp];
+    __syncthreads();                                                // wP/wX reused by the caller
+}
+
+__global__ void __launch_bounds__(BT) k_batch_solve(const ColInfo *__restrict__ cols, const int *__restrict__ order,
+                                                    const double *__restrict__ A, const double *__restrict__ g,
+                                                    const double *__restrict__ al, const double *__restrict__ segP,
+                                                    const double *__restrict__ segQ, const double *__restrict__ part,
+                                                    int KS, int64_t pstride, double *__restrict__ U,
+                                                    double *__restrict__ Y, double *__restrict__ Drow)
+{
+    __shared__ double wP[BW], wX[BW];
+    __shared__ double s_y, s_uN;
+    const int col = order[blockIdx.x];
+    const ColInfo c = cols[col];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int64_t o = c.off;
+    const int i0 = min(tid * c.seg, c.N), i1 = min(i0 + c.seg, c.N);
+    // forward, pass 1: Om into Y and the segment's sweep from a zero carry
+    double yl = 0.0;
+    for (int i = i0; i < i1; ++i) {
+        const int64_t q = o + i;
+        double om = 0.0;
+        if (i == 0) {
+            yl = c.g0;                                                  // Bt[1]
+        } else {
+            double s = 0.0;
+            for (int k = 0; k < KS; ++k) s += __ldcg(part + (int64_t)k * pstride + q);
+            om = -(c.lam * U[q]) + s;
+            yl = __ldg(g + q) * (__ldg(A + q) * yl - om);
+        }
+        Y[q] = om;
+    }
+    double P = i1 > i0 ? __ldg(segP + (int64_t)col * BT + tid) : 1.0;
+    double X = i1 > i0 ? yl : 0.0;
+    cta_scan_excl<true>(P, X, wP, wX, lane, warp);
+    // forward, pass 2: the exact sweep from the true carry y_{i0-1} = X
+    double y = X;
+    for (int i = i0; i < i1; ++i) {
+        const int64_t q = o + i;
+        y = (i == 0) ? c.g0 : __ldg(g + q) * (__ldg(A + q) * y - Y[q]);
+        Y[q] = y;
+    }
+    if (i1 == c.N && i1 > i0) s_y = y;                                  // Bt[N]
+    __syncthreads();
+    if (tid == 0) {
+        double uN;
+        const double uNm1 = U[o + c.N - 1];
+        if (c.rkind == FPDE_BC_DIRICHLET) uN = c.gN;
+        else if (fabs(s_y) > 1e-15) uN = (fabs(1.0 - c.AlN) > 1e-15) ? (s_y + c.gN * c.dLN) / (1.0 - c.AlN) : uNm1;
+        else uN = (fabs(1.0 - c.AlN) > 1e-15) ? 0.0 : uNm1;
+        s_uN = uN;
+    }
+    __syncthreads();
+    const double uN = s_uN;
+    // backward, pass 1: the segment's sweep from a zero carry
+    double ul = 0.0;
+    for (int i = i1 - 1; i >= i0; --i) {
+        const int64_t q = o + i;
+        ul = fma(__ldg(al + q), ul, Y[q]);
+    }
+    P = i1 > i0 ? __ldg(segQ + (int64_t)col * BT + tid) : 1.0;
+    X = i1 > i0 ? ul : 0.0;
+    cta_scan_excl<false>(P, X, wP, wX, lane, warp);
+    // backward, pass 2: U_{i1} = P uN + X, exact sweep, write U and the increment
+    double u = fma(P, uN, X);
+    for (int i = i1 - 1; i >= i0; --i) {
+        const int64_t q = o + i;
+        u = fma(__ldg(al + q), u, Y[q]);
+        const double uo = U[q];
+        U[q] = u;
+        Drow[q] = u - uo;
+    }
+    if (tid == 0) {
+        const double uo = U[o + c.N];
+        U[o + c.N] = uN;
+        Drow[o + c.N] = uN - uo;
+    }
+}
+
+}  // namespace fpde
+
+using namespace fpde;
+
+struct fpde_batch {
+    fpde_ctx *ctx = nullptr;
+    int n_cols = 0, max_steps = 0;
+    int64_t Ptot = 0;
+    std::vector<int64_t> off;
+    std::vector<int> N;
+    double *A = nullptr, *g = nullptr, *al = nullptr, *segP = nullptr, *segQ = nullptr;
+    double *U = nullptr, *U0 = nullptr, *Y = nullptr, *D = nullptr, *part = nullptr, *wall = nullptr;
+    ColInfo *cols = nullptr;
+    int *order = nullptr, *cta_col = nullptr;
+    int64_t n_done = 0;
+    std::map<std::pair<int64_t, int>, cudaGraphExec_t> graphs;
+    std::map<std::pair<int64_t, int>, int64_t> graph_launches;
+};
+
+namespace fpde {
+
+static int batch_enqueue(fpde_batch *b, cudaStream_t st, int64_t n0, int steps, int64_t *nk)
+{
+    int64_t k = 0;
+    for (int64_t n = n0; n < n0 + steps; ++n) {
+        int KS = 0;
+        if (n >= 1) {
+            KS = choose_splits((int)n, b->Ptot);
+            dim3 grid((unsigned)(b->Ptot / 512), (unsigned)KS);
+            k_batch_partial<<<grid, 256, 0, st>>>((const double2 *)b->D, b->Ptot / 2, (int)n, b->wall,
+                                                  b->max_steps + 1, b->max_steps - n, b->cta_col,
+                                                  (double2 *)b->part);
+            FPDE_LAUNCHED(1);
+            ++k;
+        }
+        k_batch_solve<<<b->n_cols, BT, 0, st>>>(b->cols, b->order, b->A, b->g, b->al, b->segP, b->segQ, b->part, KS,
+                                                b->Ptot, b->U, b->Y, b->D + n * b->Ptot);
+        FPDE_LAUNCHED(1);
+        ++k;
+    }
+    *nk = k;
+    return FPDE_OK;
+}
+
+}  // namespace fpde
+
+extern "C" {
+
+int fpde_batch_destroy(fpde_batch *b)
+{
+    if (!b) return FPDE_OK;
+    if (b->ctx) {
+        cudaSetDevice(b->ctx->device);
+        cudaStreamSynchronize(b->ctx->stream);
+    }
+    for (auto &kv : b->graphs) cudaGraphExecDestroy(kv.second);
+    for (double *p : {b->A, b->g, b->al, b->segP, b->segQ, b->U, b->U0, b->Y, b->D, b->part, b->wall}) dev_free(p);
+    dev_free(b->cols);
+    dev_free(b->order);
+    dev_free(b->cta_col);
+    delete b;
+    return FPDE_OK;
+}
+
+int fpde_batch_create(fpde_ctx *ctx, const fpde_column_desc *cols, int n_cols, int max_steps, int precision,
+                      fpde_batch **out)
+{
+    clear_error();
+    FPDE_CHECK_ARG(out && cols && n_cols > 0, "bad arguments");
+    *out = nullptr;
+    int rc = ctx_enter(ctx);
+    if (rc) return rc;
+    FPDE_CHECK_ARG(max_steps > 0, "max_steps must be positive");
+    FPDE_CHECK_ARG(precision == FPDE_PREC_FP64, "the ensemble computes in FP64");
+    for (int c = 0; c < n_cols; ++c) {
+        const fpde_column_desc &d = cols[c];
+        FPDE_CHECK_ARG(d.N >= 2 && d.N <= (1 << 24), "column N out of range");
+        FPDE_CHECK_ARG(d.A && d.B && d.Rlap && d.u0, "column arrays missing");
+        FPDE_CHECK_ARG(d.lag_weights || (d.alpha > 0.0 && d.alpha < 1.0), "alpha must be in (0, 1)");
+        FPDE_CHECK_ARG(d.tau > 0.0, "tau must be positive");
+        FPDE_CHECK_ARG((d.left_kind == 0 || d.left_kind == 1) && (d.right_kind == 0 || d.right_kind == 1),
+                       "bad boundary kind");
+    }
+    fpde_batch *b = new fpde_batch();
+    b->ctx = ctx;
+    b->n_cols = n_cols;
+    b->max_steps = max_steps;
+    b->off.resize(n_cols);
+    b->N.resize(n_cols);
+    int64_t tot = 0;
+    for (int c = 0; c < n_cols; ++c) {
+        b->off[c] = tot;
+        b->N[c] = (int)cols[c].N;
+        tot += (cols[c].N + 1 + 511) / 512 * 512;
+    }
+    b->Ptot = tot;
+    std::vector<double> hA(tot, 0.0), hg(tot, 0.0), hal(tot, 0.0), hU(tot, 0.0);
+    std::vector<double> hP((size_t)n_cols * BT, 1.0), hQ((size_t)n_cols * BT, 1.0);
+    std::vector<double> hw((size_t)n_cols * (max_steps + 1), 0.0);
+    std::vector<ColInfo> hc(n_cols);
+    std::vector<int> cta_col(tot / 512);
+    for (int c = 0; c < n_cols; ++c) {
+        const fpde_column_desc &d = cols[c];
+        const int64_t N = d.N, o = b->off[c];
+        double lam, lamR, kkk0 = 0.0;
+        if (d.lag_weights) {
+            lam = lamR = d.lag_weights[0];
+        } else {                                                   // Om1 :4191, R :3120
+            kkk0 = l1_interval_weight(d.alpha, 0.0, d.tau);
+            lam = d.Da * (kkk0 / d.tau);
+            lamR = d.Da * kkk0 / d.tau;
+        }
+        double Al = d.left_kind == FPDE_BC_FLUX ? 1.0 : 0.0;         // Al[1]
+        hal[o] = Al;
+        for (int64_t i = 1; i < N; ++i) {
+            Al = d.B[i] / ((d.Rlap[i] + lamR) - d.A[i] * Al);        // Al[i+1]
+            hal[o + i] = Al;
+            hg[o + i] = Al / d.B[i];
+            hA[o + i] = d.A[i];
+        }
+        for (int64_t i = 0; i <= N; ++i) hU[o + i] = d.u0[i];
+        ColInfo &ci = hc[c];
+        ci.off = o;
+        ci.N = (int)N;
+        ci.seg = (int)((N + BT - 1) / BT);
+        ci.lam = lam;
+        ci.g0 = d.left_value;
+        ci.gN = d.right_value;
+        ci.dLN = d.dLN;
+        ci.AlN = Al;
+        ci.rkind = d.right_kind;
+        ci.pad = 0;
+        for (int t = 0; t < BT; ++t) {                              // segment products (time-invariant)
+            const int64_t i0 = std::min<int64_t>((int64_t)t * ci.seg, N), i1 = std::min<int64_t>(i0 + ci.seg, N);
+            double pf = 1.0, pb = 1.0;
+            for (int64_t i = i0; i < i1; ++i) {
+                pf *= hg[o + i] * hA[o + i];
+                pb *= hal[o + i];
+            }
+            hP[(size_t)c * BT + t] = pf;
+            hQ[(size_t)c * BT + t] = pb;
+        }
+        double *w = hw.data() + (size_t)c * (max_steps + 1);          // w[m] = w_c[max_steps - m]
+        for (int64_t m = 0; m < max_steps; ++m) {
+            const int64_t j = max_steps - m;
+            w[m] = d.lag_weights ? d.lag_weights[j] : d.Da * (kkk0 * l1_lag(d.alpha, j)) / d.tau;
+        }
+        for (int64_t q = o / 512; q < (o + (N + 1 + 511) / 512 * 512) / 512; ++q) cta_col[q] = c;
+    }
+    std::vector<int> order(n_cols);                                    // largest columns first
+    std::iota(order.begin(), order.end(), 0);
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return b->N[x] > b->N[y]; });
+    const size_t tb = (size_t)tot * sizeof(double);
+    bool fail = dev_alloc((void **)&b->A, tb) || dev_alloc((void **)&b->g, tb) || dev_alloc((void **)&b->al, tb) ||
+                dev_alloc((void **)&b->segP, hP.size() * sizeof(double)) ||
+                dev_alloc((void **)&b->segQ, hQ.size() * sizeof(double)) || dev_alloc((void **)&b->U, tb) ||
+                dev_alloc((void **)&b->U0, tb) || dev_alloc((void **)&b->Y, tb) ||
+                dev_alloc((void **)&b->D, (size_t)max_steps * tb) || dev_alloc((void **)&b->part, (size_t)KS_MAX * tb) ||
+                dev_alloc((void **)&b->wall, hw.size() * sizeof(double)) ||
+                dev_alloc((void **)&b->cols, hc.size() * sizeof(ColInfo)) ||
+                dev_alloc((void **)&b->order, order.size() * sizeof(int)) ||
+                dev_alloc((void **)&b->cta_col, cta_col.size() * sizeof(int));
+    if (fail) {
+        std::string keep = fpde_last_error_string();
+        fpde_batch_destroy(b);
+        return set_error(FPDE_ERR_NOMEM, "%s", keep.c_str());
+    }
+    cudaStream_t st = ctx->stream;
+    cudaMemcpyAsync(b->A, hA.data(), tb, cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(b->g, hg.data(), tb, cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(b->al, hal.data(), tb, cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(b->segP, hP.data(), hP.size() * sizeof(double), cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(b->segQ, hQ.data(), hQ.size() * sizeof(double), cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(b->U, hU.data(), tb, cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(b->U0, hU.data(), tb, cudaMemcpyHostToDevice, st);
+    cudaMemsetAsync(b->Y, 0, tb, st);
+    cudaMemsetAsync(b->D, 0, (size_t)max_steps * tb, st);
+    cudaMemcpyAsync(b->wall, hw.data(), hw.size() * sizeof(double), cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(b->cols, hc.data(), hc.size() * sizeof(ColInfo), cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(b->order, order.data(), order.size() * sizeof(int), cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(b->cta_col, cta_col.data(), cta_col.size() * sizeof(int), cudaMemcpyHostToDevice, st);
+    cudaError_t e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) {
+        fpde_batch_destroy(b);
+        return set_error(FPDE_ERR_CUDA, "batch setup: %s", cudaGetErrorString(e));
+    }
+    *out = b;
+    return FPDE_OK;
+}
+
+int fpde_batch_run(fpde_batch *b, int steps)
+{
+    clear_error();
+    FPDE_CHECK_ARG(b && steps >= 0, "bad arguments");
+    int rc = ctx_enter(b->ctx);
+    if (rc) return rc;
+    if (steps == 0) return FPDE_OK;
+    if (b->n_done + steps > b->max_steps)
+        return set_error(FPDE_ERR_CAPACITY, "run of %d steps exceeds the history capacity %d", steps, b->max_steps);
+    auto key = std::make_pair(b->n_done, steps);
+    auto it = b->graphs.find(key);
+    if (it == b->graphs.end()) {
+        cudaStream_t cs;
+        FPDE_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+        cudaGraph_t graph;
+        FPDE_CUDA(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
+        int64_t nk = 0;
+        const int64_t before = fpde_kernel_launch_count();
+        rc = batch_enqueue(b, cs, b->n_done, steps, &nk);
+        cudaError_t e = cudaStreamEndCapture(cs, &graph);
+        count_launches(-(fpde_kernel_launch_count() - before));           // counted at replay
+        cudaStreamDestroy(cs);
+        if (rc) return rc;
+        if (e != cudaSuccess) return set_error(FPDE_ERR_CUDA, "graph capture: %s", cudaGetErrorString(e));
+        cudaGraphExec_t exec;
+        e = cudaGraphInstantiate(&exec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (e != cudaSuccess) return set_error(FPDE_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(e));
+        it = b->graphs.emplace(key, exec).first;
+        b->graph_launches[key] = nk;
+    }
+    FPDE_CUDA(cudaGraphLaunch(it->second, b->ctx->stream));
+    count_launches(b->graph_launches[key]);
+    b->n_done += steps;
+    return FPDE_OK;
+}
+
+int fpde_batch_get_state(fpde_batch *b, int col, double *u, int on_device)
+{
+    clear_error();
+    FPDE_CHECK_ARG(b && u && col >= 0 && col < b->n_cols, "bad arguments");
+    int rc = ctx_enter(b->ctx);
+    if (rc) return rc;
+    FPDE_CUDA(cudaMemcpyAsync(u, b->U + b->off[col], (b->N[col] + 1) * sizeof(double),
+                              on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, b->ctx->stream));
+    FPDE_CUDA(cudaStreamSynchronize(b->ctx->stream));
+    return FPDE_OK;
+}
+
+int fpde_batch_layout(const fpde_batch *b, int col, int64_t *offset, int64_t *N, int64_t *total)
+{
+    FPDE_CHECK_ARG(b && col >= 0 && col < b->n_cols, "bad arguments");
+    if (offset) *offset = b->off[col];
+    if (N) *N = b->N[col];
+    if (total) *total = b->Ptot;
+    return FPDE_OK;
+}
+
+int fpde_batch_reset(fpde_batch *b, const double *u_padded, int on_device)
+{
+    clear_error();
+    FPDE_CHECK_ARG(b, "null argument");
+    int rc = ctx_enter(b->ctx);
+    if (rc) return rc;
+    const double *src = u_padded ? u_padded : b->U0;
+    const cudaMemcpyKind kind = (!u_padded || on_device) ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+    FPDE_CUDA(cudaMemcpyAsync(b->U, src, b->Ptot * sizeof(double), kind, b->ctx->stream));
+    if (u_padded && !on_device) FPDE_CUDA(cudaStreamSynchronize(b->ctx->stream));
+    b->n_done = 0;
+    return FPDE_OK;
+}
+
+int fpde_batch_solve_host(fpde_batch *b, const double *u0_padded_host, int steps, double *u_out_padded_host)
+{
+    clear_error();
+    FPDE_CHECK_ARG(b && u0_padded_host && u_out_padded_host, "null argument");
+    int rc = fpde_batch_reset(b, u0_padded_host, 0);
+    if (rc) return rc;
+    if ((rc = fpde_batch_run(b, steps))) return rc;
+    FPDE_CUDA(cudaMemcpyAsync(u_out_padded_host, b->U, b->Ptot * sizeof(double), cudaMemcpyDeviceToHost,
+                              b->ctx->stream));
+    FPDE_CUDA(cudaStreamSynchronize(b->ctx->stream));
+    return ctx_check_flags(b->ctx, "batch");
+}
+
+}  // extern "C"

@@ -35,13 +35,13 @@
 #include "common.cuh"
 #include "kernels.cuh"
 #include "tc_far.cuh"
+#include "scan.cuh"
 
 namespace fpde {
 
 constexpr int LT = 256;      // threads per CTA of the line solve
 constexpr int LSEG = 8;      // max nodes per thread
 constexpr int BLK = 64;      // steps per block of the split path (= tensor-core N)
-constexpr unsigned FULL = 0xffffffffu;
 
 struct LineSolveArgs {
     const double *A, *g, *al, *cf, *cb;   // per node: coefficients, thread-segment products
@@ -65,29 +65,6 @@ struct LineSolveArgs {
     int KS, nr, N, G, rkind;
 };
 
-__device__ __forceinline__ void warp_scan_up(double &P, double &X, int lane)
-{
-#pragma unroll
-    for (int off = 1; off < 32; off <<= 1) {
-        double Pp = __shfl_up_sync(FULL, P, off), Xp = __shfl_up_sync(FULL, X, off);
-        if (lane >= off) { X = fma(P, Xp, X); P = P * Pp; }
-    }
-}
-__device__ __forceinline__ void warp_scan_down(double &P, double &X, int lane)
-{
-#pragma unroll
-    for (int off = 1; off < 32; off <<= 1) {
-        double Pn = __shfl_down_sync(FULL, P, off), Xn = __shfl_down_sync(FULL, X, off);
-        if (lane + off < 32) { X = fma(P, Xn, X); P = P * Pn; }
-    }
-}
-
-__device__ __forceinline__ unsigned long long gtimer_ns()
-{
-    unsigned long long t;
-    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-    return t;
-}
 
 template <int SP>
 __device__ __forceinline__ double right_value(const LineSolveArgs &p, double BtN, double uNm1)

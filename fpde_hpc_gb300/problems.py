@@ -212,3 +212,21 @@ def config4(n=128, steps=1024, tau=1e-3):
     u0[0] = 0.0
     u0[n:] = 0.0
     return LodProblem(f"config4_{n}^3", (n, n, n), 0.85, tau, steps, k, u0, (1, 1, 0), (1, 1, 0))
+
+
+def config5(n_cols=512, steps=2048, tau=1e-3, n_min=256, n_max=16384, seed=6):
+    """Ensemble of n_cols 1D columns: N log-uniform in [n_min, n_max] (E[N] ~ 3878 for the
+    defaults), alpha ~ U[0.5, 0.95] (both drawn with seed 6); column c has a lognormal k
+    (mu 0, sigma 0.5, ell 0.01) and an 8-Gaussian initial state, both seeded seed + c;
+    Dirichlet 0 ends, tau 1e-3."""
+    rng = np.random.default_rng(seed)
+    Ns = np.rint(np.exp(rng.uniform(math.log(n_min), math.log(n_max), n_cols))).astype(int)
+    alphas = rng.uniform(0.5, 0.95, n_cols)
+    cols = []
+    for c, (N, a) in enumerate(zip(Ns, alphas)):
+        x = np.arange(N + 1) / N
+        k = lognormal_field(N + 1, 0.0, 0.5, 0.01, seed + c, 1.0 / N)
+        u0 = gaussian_mixture(x, seed + c)
+        u0[0] = u0[-1] = 0.0
+        cols.append(LineProblem(f"col{c}", int(N), float(a), tau, steps, k, u0))
+    return cols

@@ -60,6 +60,7 @@ typedef struct fpde_ctx fpde_ctx;
 typedef struct fpde_hist fpde_hist;
 typedef struct fpde_line fpde_line;
 typedef struct fpde_lod3d fpde_lod3d;
+typedef struct fpde_batch fpde_batch;
 
 /* ---------------------------------------------------------------- context */
 
@@ -315,6 +316,41 @@ int fpde_lod3d_reset(fpde_lod3d *lod, const double *u0, int on_device);
 /* End-to-end call: upload u0 from host, run `steps`, download the grid to host. */
 int fpde_lod3d_solve_host(fpde_lod3d *lod, const double *u0_host, int steps, double *u_out_host);
 int fpde_lod3d_steps_done(const fpde_lod3d *lod, int64_t *n);
+
+/* --------------------------------------------------------------- ensembles */
+
+/* One column of an ensemble: an independent 1D Caputo line (the reference runs one column
+ * per process, mode 3 with BS 1, or the 1D mode; fpde_hpc_1d.cpp:3457-3606). Arrays are
+ * host pointers read at fpde_batch_create. */
+typedef struct fpde_column_desc {
+    int64_t N;               /* intervals; nodes 0..N */
+    double alpha, tau, Da;
+    int left_kind;
+    double left_value;
+    int right_kind;
+    double right_value;
+    double dLN;
+    const double *A, *B, *Rlap, *u0;   /* N+1 values each (as for fpde_line_create) */
+    const double *lag_weights;         /* optional, max_steps+1 values (fpde_line_desc) */
+} fpde_column_desc;
+
+/* An ensemble of columns of any lengths and orders advanced together: per step one history
+ * sum over all columns' nodes and one solve kernel with a CTA per column, largest columns
+ * first. No counterpart in the reference, which runs such ensembles as separate processes
+ * (fpde_hpc_1d.cpp main); stands in for a loop of H_solver runs. Node layout on the device:
+ * column c at offset off_c (fpde_batch_layout) of a padded vector of `total` values. */
+int fpde_batch_create(fpde_ctx *ctx, const fpde_column_desc *cols, int n_cols, int max_steps, int precision,
+                      fpde_batch **out);
+int fpde_batch_destroy(fpde_batch *batch);
+int fpde_batch_run(fpde_batch *batch, int steps);
+/* Column `col`'s state (N+1 values) out. */
+int fpde_batch_get_state(fpde_batch *batch, int col, double *u, int on_device);
+/* Offset and N of column `col` in the padded node vector, and the vector's length. */
+int fpde_batch_layout(const fpde_batch *batch, int col, int64_t *offset, int64_t *N, int64_t *total);
+/* Reset to a padded state vector (NULL: the columns' u0) and an empty history. */
+int fpde_batch_reset(fpde_batch *batch, const double *u_padded, int on_device);
+/* End-to-end call: padded initial vector from host, run `steps`, padded final vector to host. */
+int fpde_batch_solve_host(fpde_batch *batch, const double *u0_padded_host, int steps, double *u_out_padded_host);
 
 #ifdef __cplusplus
 }
