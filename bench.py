@@ -1,18 +1,25 @@
-"""Benchmark of the hot path on the 65,536-node 1D Caputo configuration.
+"""Benchmark of the hot path: implicit fractional time stepping with the full L1 history.
 
-One bench step = one full solve of the line problem: 8,192 implicit time steps of a
-65,536-interval line (alpha 0.7, tau 1e-4, seeded lognormal k and 8-Gaussian H0), i.e.
-65,535 x 8,192 = 5.37e8 node-steps, each with the full L1 history sum and a Thomas solve.
-Inputs (coefficients, history, state) are resident in HBM for `value`; `e2e` goes through
-the C ABI with host buffers (fpde_line_solve_host: upload H0, solve, download the state).
+Default workload (the headline, config 2): one bench step = one full solve of a
+65,536-interval 1D Caputo line, 8,192 implicit time steps (alpha 0.7, tau 1e-4, seeded
+lognormal k and 8-Gaussian H0), i.e. 65,535 x 8,192 = 5.37e8 node-steps, each with the full
+L1 history sum and a Thomas solve. Other workloads of the same operator:
+  config3  distributed-order line, N=16,384, 4,096 steps, 16-node Gauss-Legendre orders
+  config4  3D LOD 128^3, 1,024 steps, alpha 0.85 (history in the K pass, three Thomas passes)
+  config5  ensemble of 512 columns, N log-uniform [256, 16384], alpha U[0.5, 0.95], 2,048 steps
+`value` is measured with inputs resident in HBM (CUDA events on the library's stream, the
+run replayed from a captured CUDA graph, no probes); `e2e` goes through the C ABI with host
+buffers (the *_solve_host calls: upload the initial state, solve, download the state).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--workload config2|config3|config4|config5] [--precision auto|fp64|bf16|f16|bf16x3]
 
---impl reference times the reference algorithm on the host cores: the CPU restatement of
-the reference's FP64 path (oracle/), on all host threads, on a bounded sample of the same
-workload, extrapolated with t(S) = a S + b S^2 (the history term makes the cost quadratic
-in the step count).
-Multi-GPU: the line does not shard, so N GPUs run N independent replicas (weak scaling).
+--impl reference times the reference algorithm on the host cores: the CPU restatement of the
+reference's FP64 path (oracle/), on all host threads, on a bounded sample of the same workload
+(the first S1 and S2 time steps at full size), extrapolated with t(S) = a S + b S^2 (the history
+term makes the cost quadratic in the step count).
+Multi-GPU: nothing here shards (a line couples all its nodes; the ensemble could shard by column
+but runs on one GPU), so N GPUs run N independent replicas (weak scaling).
 """
 import argparse
 import json
@@ -28,8 +35,6 @@ sys.path.insert(0, ROOT)
 
 import numpy as np  # noqa: E402
 
-METRIC = "node-steps/s (1D Caputo L1 history sum + Thomas, N=65536, 8192 steps)"
-
 
 def parse():
     ap = argparse.ArgumentParser()
@@ -37,9 +42,10 @@ def parse():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="config2", choices=["config2", "config3", "config4", "config5"])
     ap.add_argument("--precision", default="auto", choices=["auto", "fp64", "bf16", "f16", "bf16x3"])
-    ap.add_argument("--time-steps", type=int, default=8192)
-    ap.add_argument("--nodes", type=int, default=65536)
+    ap.add_argument("--time-steps", type=int, default=None, help="override the workload's step count")
+    ap.add_argument("--nodes", type=int, default=None, help="override the workload's size")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64-arm", action="store_true")
     return ap.parse_args()
@@ -55,8 +61,8 @@ def measured_peaks():
     if os.path.exists(p):
         with open(p) as f:
             d = json.load(f)
-        return d.get("hbm_gbs", 6800.0), "measured"
-    return 6800.0, "fallback"
+        return d.get("hbm_gbs", 6800.0), "of measured (MEASURED_PEAKS.json hbm_gbs)"
+    return 6800.0, "of fallback 6.8 TB/s"
 
 
 class ClockSampler:
@@ -111,87 +117,279 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def cpu_port_rate(prob, threads, s1=48, s2=144):
-    """Time the CPU restatement of the reference FP64 path (all host threads) on the first
-    s1 and s2 steps of the workload, fit t(S) = a S + b S^2 and extrapolate to the full run."""
-    os.environ["OMP_NUM_THREADS"] = str(threads)
+# ------------------------------------------------------------------ workloads
+
+def _fit_quadratic(ts, ss, S):
+    (t1, t2), (s1, s2) = ts, ss
+    b = (t2 / s2 - t1 / s1) / (s2 - s1)
+    a = t1 / s1 - b * s1
+    if b <= 0:          # timing noise: linear model through the longer sample
+        a, b = t2 / s2, 0.0
+    return a * S + b * S * S
+
+
+def _oracle():
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle
     oracle.load()
-    A, B, R = prob.coefs()
-    ts = []
-    for s in (s1, s2):
-        t0 = time.perf_counter()
-        oracle.line_run(prob.u0, s, prob.tau, prob.alpha, prob.Da, A, B, R)
-        ts.append(time.perf_counter() - t0)
-    (t1, t2) = ts
-    b = (t2 / s2 - t1 / s1) / (s2 - s1)
-    a = t1 / s1 - b * s1
-    if b <= 0:          # timing noise: fall back to a linear model through the longer sample
-        a, b = t2 / s2, 0.0
-    S = prob.steps
-    T = a * S + b * S * S
-    return {"value": prob.node_steps / T, "seconds_full_extrapolated": T, "sample_seconds": sum(ts),
-            "sample": f"first {s1} and {s2} steps of the {prob.N}-node line (full history), "
-                      f"fit t(S)=aS+bS^2, extrapolated to {S} steps"}
+    return oracle
 
+
+class LineWorkload:
+    """1D lines: config2 (Caputo) and config3 (distributed order)."""
+
+    def __init__(self, name, args):
+        from fpde_hpc_gb300 import problems
+        self.name = name
+        if name == "config2":
+            kw = {}
+            if args.nodes:
+                kw["N"] = args.nodes
+            if args.time_steps:
+                kw["steps"] = args.time_steps
+            self.p = problems.config2(**kw)
+            self.do = False
+            self.metric = f"node-steps/s (1D Caputo L1 history sum + Thomas, N={self.p.N}, {self.p.steps} steps)"
+            self.desc = (f"1D Caputo line N={self.p.N}, {self.p.steps} steps, alpha 0.7, tau 1e-4, lognormal k "
+                         "(sigma 0.5, ell 0.01), 8-Gaussian H0 (config 2)")
+        else:
+            kw = {}
+            if args.nodes:
+                kw["N"] = args.nodes
+            if args.time_steps:
+                kw["steps"] = args.time_steps
+            self.p = problems.config3(**kw)
+            self.do = True
+            self.metric = (f"node-steps/s (1D distributed-order L1 history sum + Crank-Nicolson Thomas, "
+                           f"N={self.p.N}, {self.p.steps} steps)")
+            self.desc = (f"distributed-order line N={self.p.N}, {self.p.steps} steps, w(a)=6a(1-a), 16-node "
+                         "Gauss-Legendre, tau 1e-4, lognormal k (seed 3), 8-Gaussian H0 (seed 4) (config 3)")
+        self.node_steps = self.p.node_steps
+        self.paths = ["fp64", "split-bf16", "split-fp16", "split-bf16x3"]
+
+    def weights(self, n):
+        import fpde_hpc_gb300 as fp
+        return fp.do_weights(self.p.orders, self.p.qw, self.p.tau, n, self.p.gnorm) / self.p.tau
+
+    def build(self, ctx, prec):
+        import fpde_hpc_gb300 as fp
+        p = self.p
+        A, B, R = p.coefs()
+        if self.do:
+            return fp.Line(ctx, p.N, 0.5, p.tau, 1.0, A, B, R, p.u0, p.steps, precision=prec,
+                           lag_weights=self.weights(p.steps + 1), theta=1.0)
+        return fp.Line(ctx, p.N, p.alpha, p.tau, p.Da, A, B, R, p.u0, p.steps, precision=prec)
+
+    @property
+    def u0(self):
+        return self.p.u0
+
+    @property
+    def steps(self):
+        return self.p.steps
+
+    def cpu_rate(self, threads, s1=48, s2=144):
+        os.environ["OMP_NUM_THREADS"] = str(threads)
+        oracle = _oracle()
+        p = self.p
+        A, B, R = p.coefs()
+        ts = []
+        w = self.weights_host(s2 + 1) if self.do else None
+        for s in (s1, s2):
+            t0 = time.perf_counter()
+            if self.do:
+                oracle.line_run_general(p.u0, s, w, 1.0, A, B, R)
+            else:
+                oracle.line_run(p.u0, s, p.tau, p.alpha, p.Da, A, B, R)
+            ts.append(time.perf_counter() - t0)
+        T = _fit_quadratic(ts, (s1, s2), p.steps)
+        return {"value": self.node_steps / T, "sample_seconds": sum(ts),
+                "sample": f"first {s1} and {s2} steps of the {p.N}-node line (full history), fit t(S)=aS+bS^2, "
+                          f"extrapolated to {p.steps} steps"}
+
+    def weights_host(self, n):
+        oracle = _oracle()
+        return oracle.do_fused_weights(self.p.orders, self.p.qw, self.p.gnorm, self.p.tau, n) / self.p.tau
+
+    def bytes_io(self):
+        return 8 * (self.p.N + 1), 8 * (self.p.N + 1)
+
+
+class LodWorkload:
+    def __init__(self, args):
+        from fpde_hpc_gb300 import problems
+        n = args.nodes or 128
+        self.p = problems.config4(n=n, steps=args.time_steps or 1024)
+        self.name = "config4"
+        self.node_steps = self.p.node_steps
+        self.metric = (f"node-steps/s (3D LOD: L1 history sum + three Thomas passes, {n}^3, "
+                       f"{self.p.steps} steps)")
+        self.desc = (f"3D LOD {n}^3, {self.p.steps} steps, alpha 0.85, tau 1e-3, lognormal k (sigma 0.4, seed 5), "
+                     "Gaussian blob, zero-flux sides, Dirichlet top/bottom (config 4)")
+        self.paths = ["fp64"]
+
+    def build(self, ctx, prec):
+        import fpde_hpc_gb300 as fp
+        p = self.p
+        cA, cB, cR = p.coefs()
+        return fp.Lod3D(ctx, p.dims, p.alpha, p.tau, p.Da, cA, cB, cR, p.u0, p.steps, left_kind=p.left_kind,
+                        right_kind=p.right_kind, dLN=p.dLN, precision=prec)
+
+    @property
+    def u0(self):
+        return self.p.u0
+
+    @property
+    def steps(self):
+        return self.p.steps
+
+    def cpu_rate(self, threads, s1=8, s2=32):
+        os.environ["OMP_NUM_THREADS"] = str(threads)
+        oracle = _oracle()
+        p = self.p
+        cA, cB, cR = p.coefs()
+        ts = []
+        for s in (s1, s2):
+            t0 = time.perf_counter()
+            oracle.lod_run(p.dims, p.u0, s, p.tau, p.alpha, p.Da, cA, cB, cR, None, None, p.left_kind,
+                           p.right_kind, p.dLN)
+            ts.append(time.perf_counter() - t0)
+        T = _fit_quadratic(ts, (s1, s2), p.steps)
+        return {"value": self.node_steps / T, "sample_seconds": sum(ts),
+                "sample": f"first {s1} and {s2} steps of the {p.dims[0]}^3 grid, fit t(S)=aS+bS^2, "
+                          f"extrapolated to {p.steps} steps"}
+
+    def bytes_io(self):
+        return 8 * self.p.u0.size, 8 * self.p.u0.size
+
+
+class BatchWorkload:
+    def __init__(self, args):
+        from fpde_hpc_gb300 import problems
+        self.cols = problems.config5(n_cols=args.nodes or 512, steps=args.time_steps or 2048)
+        self.name = "config5"
+        self._steps = self.cols[0].steps
+        self.node_steps = sum(c.node_steps for c in self.cols)
+        self.metric = (f"node-steps/s (ensemble of {len(self.cols)} 1D Caputo columns, N log-uniform "
+                       f"[256,16384], {self._steps} steps)")
+        self.desc = (f"ensemble of {len(self.cols)} columns, N log-uniform [256, 16384] "
+                     f"(sum N = {sum(c.N for c in self.cols)}), alpha U[0.5, 0.95], tau 1e-3, {self._steps} steps, "
+                     "seeds 6.. (config 5)")
+        self.paths = ["fp64"]
+        self._b = None
+
+    def build(self, ctx, prec):
+        import fpde_hpc_gb300 as fp
+        cols = []
+        for c in self.cols:
+            A, B, R = c.coefs()
+            cols.append(dict(N=c.N, alpha=c.alpha, tau=c.tau, Da=c.Da, A=A, B=B, Rlap=R, u0=c.u0))
+        self._b = fp.Batch(ctx, cols, self._steps, precision=prec)
+        return self._b
+
+    @property
+    def u0(self):
+        return self._b.pack([c.u0 for c in self.cols])
+
+    @property
+    def steps(self):
+        return self._steps
+
+    def cpu_rate(self, threads, s1=48, s2=144, sample=16):
+        os.environ["OMP_NUM_THREADS"] = str(threads)
+        oracle = _oracle()
+        idx = np.linspace(0, len(self.cols) - 1, sample).astype(int)
+        ts = []
+        for s in (s1, s2):
+            t0 = time.perf_counter()
+            for i in idx:
+                c = self.cols[i]
+                A, B, R = c.coefs()
+                oracle.line_run(c.u0, s, c.tau, c.alpha, c.Da, A, B, R)
+            ts.append(time.perf_counter() - t0)
+        T = _fit_quadratic(ts, (s1, s2), self._steps)
+        scale = sum(c.N for c in self.cols) / sum(self.cols[i].N for i in idx)
+        T *= scale
+        return {"value": self.node_steps / T, "sample_seconds": sum(ts),
+                "sample": f"{sample} of the {len(self.cols)} columns, first {s1} and {s2} steps, fit t(S)=aS+bS^2, "
+                          f"extrapolated to {self._steps} steps and scaled by total nodes"}
+
+    def bytes_io(self):
+        n = 8 * sum(c.N + 1 for c in self.cols)
+        return n, n
+
+
+def make_workload(args):
+    if args.workload in ("config2", "config3"):
+        return LineWorkload(args.workload, args)
+    if args.workload == "config4":
+        return LodWorkload(args)
+    return BatchWorkload(args)
+
+
+# ------------------------------------------------------------------ reference arm
 
 def run_reference(args):
     rank, world, _ = dist_info()
     if rank != 0:
         return
-    from fpde_hpc_gb300 import problems
-    prob = problems.config2(N=args.nodes, steps=args.time_steps)
+    wl = make_workload(args)
     threads = os.cpu_count() or 1
     vals = []
     for it in range(args.warmup + args.steps):
-        r = cpu_port_rate(prob, threads)
+        r = wl.cpu_rate(threads)
         if it >= args.warmup:
             vals.append(r)
     v = float(np.median([r["value"] for r in vals]))
-    out = {"impl": "reference", "metric": METRIC, "value": v, "unit": "node-steps/s", "n_gpus": args.gpus,
-           "steps": args.steps, "warmup": args.warmup, "ms_per_step": prob.node_steps / v * 1e3,
+    out = {"impl": "reference", "metric": wl.metric, "value": v, "unit": "node-steps/s", "n_gpus": args.gpus,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": wl.node_steps / v * 1e3,
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-           "config": {"workload": f"1D Caputo line N={prob.N}, {prob.steps} steps, alpha 0.7, tau 1e-4, "
-                                  "lognormal k, 8-Gaussian H0 (config 2)", "nodes": prob.N,
-                      "time_steps": prob.steps},
+           "config": {"workload": wl.desc},
            "cpu_baseline": {"value": v, "unit": "node-steps/s", "cores": threads, "kind": "port",
                             "sample": vals[0]["sample"]},
            "e2e": {"value": v, "unit": "node-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out), flush=True)
 
 
-def _timed_runs(line, u0_dev, steps, reps, stream):
-    """reps full solves, each from reset; CUDA events on the library's stream."""
+# ------------------------------------------------------------------ our arm
+
+def _timed(obj, u0_dev, steps, reps, stream):
+    """reps full solves from reset, CUDA events on the library's stream; ms per solve."""
     import torch
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    totals = {k: {"ms": 0.0, "bytes": 0.0, "flops": 0.0, "count": 0} for k in (0, 1, 2)}
     e0.record(stream)
     for _ in range(reps):
-        line.reset(u0_dev)
-        line.run(steps)
-        for k in totals:
-            ps = line.probe_stats(k)
-            for f in ps:
-                totals[k][f] += ps[f]
+        obj.reset(u0_dev)
+        obj.run(steps)
     e1.record(stream)
     torch.cuda.synchronize()
-    return e0.elapsed_time(e1) / reps, totals
+    return e0.elapsed_time(e1) / reps
 
 
-def _roofline(totals, kind, peak_gbs, peak_kind, name, extra=None):
-    t = totals[kind]
-    if t["ms"] <= 0:
+def _probe(line, u0_dev, steps, every):
+    """One probed solve: per-kind event sums (0 FP64 GEMV, 1 tensor-core far contraction, 2 solve)."""
+    import torch
+    line.set_probe(every)
+    line.reset(u0_dev)
+    line.run(steps)           # builds the probed graph
+    line.reset(u0_dev)
+    line.run(steps)
+    torch.cuda.synchronize()
+    tot = {k: line.probe_stats(k) for k in (0, 1, 2)}
+    line.set_probe(0)
+    return tot
+
+
+def _kernel_entry(t, name, peak, peak_src, scale=1.0):
+    if t["count"] <= 0 or t["ms"] <= 0:
         return None
     gbs = t["bytes"] / (t["ms"] / 1e3) / 1e9
-    r = {"kernel": name, "bound": "hbm", "achieved": gbs, "peak": peak_gbs, "unit": "GB/s",
-         "frac": gbs / peak_gbs, "peak_source": peak_kind, "traffic": None, "probed_launches": t["count"],
-         "ms_per_launch": t["ms"] / t["count"]}
+    e = {"kernel": name, "bound": "hbm", "achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak,
+         "peak_source": peak_src, "traffic": None, "probed_launches": t["count"],
+         "ms_per_launch": t["ms"] / t["count"], "est_ms_per_solve": t["ms"] * scale}
     if t["flops"]:
-        r["achieved_tflops"] = t["flops"] / (t["ms"] / 1e3) / 1e12
-    if extra:
-        r.update(extra)
-    return r
+        e["achieved_tflops"] = t["flops"] / (t["ms"] / 1e3) / 1e12
+    return e
 
 
 def run_ours(args):
@@ -202,25 +400,29 @@ def run_ours(args):
         dist.init_process_group("nccl", init_method="env://")
     torch.cuda.set_device(local)
     import fpde_hpc_gb300 as fp
-    from fpde_hpc_gb300 import problems
 
-    prob = problems.config2(N=args.nodes, steps=args.time_steps)
-    A, B, R = prob.coefs()
+    wl = make_workload(args)
     ctx = fp.Context(local)
-    stream = torch.cuda.current_stream()
+    # one explicit stream for the library and the timing events (a null handle would select
+    # the library's own stream, which torch's events do not order against)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
     ctx.set_stream(stream.cuda_stream)
     lib = ctx.lib
-    prec = {"auto": fp.FPDE_PREC_SPLIT_BF16X3, "fp64": fp.FPDE_PREC_FP64, "bf16": fp.FPDE_PREC_SPLIT_BF16,
-            "f16": fp.FPDE_PREC_SPLIT_F16, "bf16x3": fp.FPDE_PREC_SPLIT_BF16X3}[args.precision]
+    is_line = isinstance(wl, LineWorkload)
+    prec = {"auto": fp.FPDE_PREC_SPLIT_BF16X3 if is_line else fp.FPDE_PREC_FP64, "fp64": fp.FPDE_PREC_FP64,
+            "bf16": fp.FPDE_PREC_SPLIT_BF16, "f16": fp.FPDE_PREC_SPLIT_F16,
+            "bf16x3": fp.FPDE_PREC_SPLIT_BF16X3}[args.precision]
+    if not is_line and prec != fp.FPDE_PREC_FP64:
+        raise SystemExit(f"{wl.name} runs in FP64 only")
     pname = {0: "fp64", 1: "split-bf16", 2: "split-fp16", 3: "split-bf16x3"}[prec]
-    u0_dev = torch.from_numpy(prob.u0).cuda()
-    probe_every = max(1, prob.steps // 32)
 
-    line = fp.Line(ctx, prob.N, prob.alpha, prob.tau, prob.Da, A, B, R, prob.u0, prob.steps, precision=prec)
-    line.set_probe(probe_every)
+    obj = wl.build(ctx, prec)
+    u0_dev = torch.from_numpy(np.ascontiguousarray(wl.u0)).cuda()
+    steps = wl.steps
     for _ in range(args.warmup):
-        line.reset(u0_dev)
-        line.run(prob.steps)
+        obj.reset(u0_dev)
+        obj.run(steps)
     torch.cuda.synchronize()
 
     def barrier():
@@ -234,7 +436,7 @@ def run_ours(args):
     barrier()
     torch.cuda.synchronize()
     launches0 = lib.fpde_kernel_launch_count()
-    ms, totals = _timed_runs(line, u0_dev, prob.steps, args.steps, stream)
+    ms = _timed(obj, u0_dev, steps, args.steps, stream)
     barrier()
     launches = lib.fpde_kernel_launch_count() - launches0
     clk = clocks.stop()
@@ -243,79 +445,88 @@ def run_ours(args):
         t = torch.tensor([ms], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms = float(t.item())
-    value = prob.node_steps * world / (ms / 1e3)
-    u_main = line.state()
+    value = wl.node_steps * world / (ms / 1e3)
+    u_main = obj.state() if is_line else None
 
     # end to end through the C ABI with host buffers (pinned)
-    u0_h = torch.from_numpy(prob.u0.copy()).pin_memory()
-    out_h = torch.empty(prob.N + 1, dtype=torch.float64).pin_memory()
+    u0_h = torch.from_numpy(np.ascontiguousarray(wl.u0).copy()).pin_memory()
+    out_h = torch.empty_like(u0_h).pin_memory()
     u0_np, out_np = u0_h.numpy(), out_h.numpy()
-    line.solve_host(u0_np, prob.steps, out_np)
+    obj.solve_host(u0_np, steps, out_np)
     barrier()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        line.solve_host(u0_np, prob.steps, out_np)
+        obj.solve_host(u0_np, steps, out_np)
     e2e_s = (time.perf_counter() - t0) / args.steps
     if world > 1:
         import torch.distributed as dist
         t = torch.tensor([e2e_s], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         e2e_s = float(t.item())
-    e2e = {"value": prob.node_steps * world / e2e_s, "unit": "node-steps/s",
-           "h2d_bytes_per_step": 8 * (prob.N + 1), "d2h_bytes_per_step": 8 * (prob.N + 1),
-           "ms_per_step": e2e_s * 1e3}
-    line.close()
+    bi, bo = wl.bytes_io()
+    e2e = {"value": wl.node_steps * world / e2e_s, "unit": "node-steps/s", "h2d_bytes_per_step": bi,
+           "d2h_bytes_per_step": bo, "ms_per_step": e2e_s * 1e3}
 
-    peak, peak_kind = measured_peaks()
-    peak_src = "of measured (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else "of fallback 6.8 TB/s"
-    kernels = {}
-    if prec == 0:
-        kernels["hist_gemv"] = _roofline(totals, 0, peak, peak_src, "k_l1_partial (FP64 history GEMV)",
-                                         {"fp64_fma_ceiling_gbs": 4800.0})
-    else:
-        kernels["far_tc"] = _roofline(totals, 1, peak, peak_src, "k_far_tc (tcgen05 split contraction)")
-    solve = totals[2]
-    kernels["solve"] = {"kernel": "k_line_solve", "probed_launches": solve["count"],
-                        "ms_per_launch": solve["ms"] / solve["count"] if solve["count"] else None}
-    # dominant kernel by measured time share (probes sample 1/probe_every of the solves)
-    far_ms = totals[1]["ms"] + totals[0]["ms"] * probe_every
-    solve_ms_est = (solve["ms"] / max(solve["count"], 1)) * prob.steps * args.steps
-    main_kernel = kernels.get("far_tc") or kernels.get("hist_gemv")
-    roofline = dict(main_kernel) if main_kernel else {}
-    roofline["time_share_of_step"] = (totals[1]["ms"] if prec else totals[0]["ms"] * probe_every) / (ms * args.steps)
-    roofline["solve_time_share_of_step"] = solve_ms_est / (ms * args.steps)
-
-    out = {"metric": METRIC, "value": value, "unit": "node-steps/s", "n_gpus": world, "steps": args.steps,
+    peak, peak_src = measured_peaks()
+    out = {"metric": wl.metric, "value": value, "unit": "node-steps/s", "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": "f64" if prec == 0 else f"{pname}(tensor)+f64",
-           "data": "synthetic (seeded lognormal k, 8-Gaussian H0)",
-           "config": {"workload": f"1D Caputo line N={prob.N}, {prob.steps} steps, alpha 0.7, tau 1e-4, "
-                                  "lognormal k (sigma 0.5, ell 0.01), 8-Gaussian H0 (config 2)",
-                      "nodes": prob.N, "time_steps": prob.steps, "path": pname, "block": 64,
-                      "l2": "inputs larger than L2 (history 2.1-4.3 GB streamed)",
+           "data": "synthetic (seeded; no dataset exists for this operator)",
+           "config": {"workload": wl.desc, "path": pname,
+                      "l2": "inputs larger than L2 (the increment history, GBs, is streamed every step)",
                       "parallelism": f"replicas x{world}"},
-           "e2e": e2e, "gpu_launches": int(launches), "roofline": roofline, "kernels": kernels, "clocks": clk}
+           "e2e": e2e, "gpu_launches": int(launches), "clocks": clk}
 
-    if prec != 0 and not args.no_fp64_arm:
+    if is_line:
+        # kernel rooflines from one separate probed solve (events inside the graph)
+        every = max(1, steps // 32)
+        tot = _probe(obj, u0_dev, steps, every)
+        kernels = {}
+        if prec == 0:
+            kernels["hist_gemv"] = _kernel_entry(tot[0], "k_l1_partial (FP64 history GEMV)", peak, peak_src, every)
+        else:
+            kernels["far_tc"] = _kernel_entry(tot[1], "k_far_tc3/k_far_tc (tcgen05 far-history contraction)",
+                                              peak, peak_src, 1.0)
+        kernels["solve"] = _kernel_entry(tot[2], "k_line_solve (history fold + near history + Thomas)", peak,
+                                         peak_src, every)
+        kernels = {k: v for k, v in kernels.items() if v}
+        est = {k: v["est_ms_per_solve"] for k, v in kernels.items()}
+        tot_est = sum(est.values())
+        for k, v in kernels.items():
+            v["share_of_kernel_time"] = est[k] / tot_est if tot_est else None
+        dom = max(kernels, key=lambda k: est[k])
+        out["roofline"] = dict(kernels[dom])
+        out["kernels"] = kernels
+    else:
+        # whole-step HBM roofline: algorithmic history bytes 8 x nodes x lags, summed over steps
+        nodes = wl.node_steps / steps
+        alg = 8.0 * nodes * steps * (steps - 1) / 2
+        gbs = alg / (ms / 1e3) / 1e9
+        out["roofline"] = {"kernel": "whole step (FP64 history GEMV dominant)", "bound": "hbm", "achieved": gbs,
+                           "peak": peak, "unit": "GB/s", "frac": gbs / peak, "peak_source": peak_src,
+                           "traffic": None, "note": "algorithmic history bytes / whole solve time"}
+
+    if is_line and prec != 0 and not args.no_fp64_arm:
         # the plain FP64 kernel on the same workload: speed-up and accuracy of the split path
-        l64 = fp.Line(ctx, prob.N, prob.alpha, prob.tau, prob.Da, A, B, R, prob.u0, prob.steps,
-                      precision=fp.FPDE_PREC_FP64)
-        l64.set_probe(probe_every)
+        l64 = wl.build(ctx, fp.FPDE_PREC_FP64)
         l64.reset(u0_dev)
-        l64.run(prob.steps)
-        ms64, tot64 = _timed_runs(l64, u0_dev, prob.steps, 1, stream)
+        l64.run(steps)
+        ms64 = _timed(l64, u0_dev, steps, 1, stream)
         u64 = l64.state()
+        tot64 = _probe(l64, u0_dev, steps, max(1, steps // 32))
         l64.close()
         err = float(np.max(np.abs(u_main - u64)) / np.max(np.abs(u64)))
         rms = float(np.sqrt(np.mean((u_main - u64) ** 2)) / np.sqrt(np.mean(u64 ** 2)))
-        out["fp64_kernel"] = {"value": prob.node_steps / (ms64 / 1e3), "ms_per_step": ms64,
-                              "roofline": _roofline(tot64, 0, peak, peak_src, "k_l1_partial (FP64 history GEMV)",
-                                                    {"fp64_fma_ceiling_gbs": 4800.0})}
-        out["split_vs_fp64"] = {"speedup": ms64 / ms, "max_rel_err": err, "rms_rel_err": rms,
-                                "bound": 1e-7}
+        out["fp64_kernel"] = {"value": wl.node_steps / (ms64 / 1e3), "ms_per_step": ms64,
+                              "roofline": _kernel_entry(tot64[0], "k_l1_partial (FP64 history GEMV)", peak,
+                                                        peak_src, max(1, steps // 32))}
+        if out["fp64_kernel"]["roofline"]:
+            out["fp64_kernel"]["roofline"]["fp64_fma_ceiling_gbs"] = 4800.0
+        out["split_vs_fp64"] = {"speedup": ms64 / ms, "max_rel_err": err, "rms_rel_err": rms, "bound": 1e-7}
+    obj.close()
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        cb = cpu_port_rate(prob, os.cpu_count() or 1)
+        cb = wl.cpu_rate(os.cpu_count() or 1)
         out["cpu_baseline"] = {"value": cb["value"], "unit": "node-steps/s", "cores": os.cpu_count() or 1,
                                "kind": "port", "sample": cb["sample"]}
     ctx.close()
