@@ -62,7 +62,7 @@ struct LineSolveArgs {
     const double *Lf, *Mb, *Kb, *mb;      // chunk-carry rows: c_in = Lf Y, u_b = Mb U0 + Kb Y + mb U_N
     unsigned *barrier, *flags;
     double lam, g0, gN, dLN, AlN;
-    int KS, nr, N, G, rkind;
+    int KS, nr, N, G, rkind, chunk;
 };
 
 
@@ -90,10 +90,10 @@ __global__ void __launch_bounds__(LT) k_line_solve(LineSolveArgs p)
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int c = blockIdx.x;
     if (tid == 0) s_seq = *((volatile unsigned long long *)p.seq) + 1;
-    const int a = c * LT * SP;
-    const int b = min(a + LT * SP, p.N);
+    const int a = c * p.chunk;
+    const int b = min(a + p.chunk, p.N);
     const int i0 = a + tid * SP;
-    const int i1 = min(i0 + SP, p.N);
+    const int i1 = min(i0 + SP, b);
     const int cnt = max(0, i1 - i0);
 
     // ---- warp 0: the time-invariant chunk-carry rows of this chunk (used after the gather)
@@ -346,6 +346,395 @@ __global__ void __launch_bounds__(LT) k_line_solve(LineSolveArgs p)
     if (c == 0 && tid == 0) *((volatile unsigned long long *)p.seq) = s_seq;   // all CTAs have read it
 }
 
+// ---------------------------------------------------------------------------------------
+// Persistent form for the split path: one cooperative launch advances steps j0 .. j0+nsteps-1
+// of a 64-step block. Every CTA keeps its chunk's state and time-invariant data in registers
+// for the whole launch; per step the CTAs exchange only their two chunk aggregates (double-
+// buffered by step parity, published with a release flag carrying a monotonically growing
+// tag). While the exchange of step j is in flight, every thread already sums the far partials
+// and the near history of step j+1 except the newest increment, which is added once known.
+//
+// All products of the scans are time-invariant (they are products of the recurrence
+// coefficients), so they are precomputed on the host: a warp-scan level is one shuffle and
+// one FMA, the combination across the warps of a CTA is a dot product with precomputed
+// coefficients (no second barrier), and thread 0 forms the chunk's two aggregates from the
+// warp totals and publishes them itself. Three CTA barriers per step remain.
+struct ScanCoef {
+    const double *lane;       // [12][G*LT]: 5 forward level products, forward prefix, 5 backward, backward suffix
+    const double *warp;       // [G][4][NW][NW]: Cf, Cb (cross-warp), Yrow, U0row (chunk aggregates, first row)
+};
+
+struct LineBlockArgs {
+    const double *A, *g, *al, *cf, *cb, *CB, *GG;
+    const double *lamv, *eA, *eB;         // optional explicit part (theta != 0)
+    const double *src;                    // optional per-step source rows ((N+1) each)
+    int src_rows;
+    double *U;                            // state: read at start, written at the end
+    double *ring;                         // [P][64] node-major increments of the block
+    const double *cfar;                   // far partials [KS][64][P]
+    int KS;
+    int64_t P;
+    const double *wlag;                   // w[lag]
+    double *agg;                          // [2][2G+2] aggregates by step parity
+    double *halo;                         // [2][2G+2] chunk edge states by step parity
+    unsigned long long *cflag, *hflag, *seq;
+    const double *Lf, *Mb, *Kb, *mb;
+    ScanCoef sc;
+    unsigned *flags;
+    double lam, g0, gN, dLN, AlN;
+    int64_t n0;                           // global index of step j0
+    int j0, nsteps, N, G, rkind, chunk;
+};
+
+__device__ __forceinline__ unsigned long long ld_acquire(const unsigned long long *f)
+{
+    unsigned long long v;
+    asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(f) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ bool wait_flag(const unsigned long long *f, unsigned long long tag,
+                                          unsigned long long t0)
+{
+    while (ld_acquire(f) < tag)
+        if (gtimer_ns() - t0 > 1000000000ull) return false;
+    return true;
+}
+
+template <int SP>
+__global__ void __launch_bounds__(LT, 1) k_line_block(LineBlockArgs p)
+{
+    constexpr int NW = LT / 32;
+    __shared__ double wXf[NW], wXb[NW];
+    __shared__ double sCf[NW][NW], sCb[NW][NW], sY[NW], sU0[NW];
+    __shared__ double s_cin, s_ub, s_UN;
+    __shared__ double s_first[LT], s_last[LT];
+    __shared__ unsigned long long s_base;
+    __shared__ int s_abort;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int c = blockIdx.x, G = p.G, N = p.N;
+    if (tid == 0) { s_base = *((volatile unsigned long long *)p.seq); s_abort = 0; }
+    {
+        const double *wc = p.sc.warp + (size_t)c * (2 * NW * NW + 2 * NW);
+        for (int q = tid; q < NW * NW; q += LT) {
+            sCf[q / NW][q % NW] = wc[q];
+            sCb[q / NW][q % NW] = wc[NW * NW + q];
+        }
+        if (tid < NW) { sY[tid] = wc[2 * NW * NW + tid]; sU0[tid] = wc[2 * NW * NW + NW + tid]; }
+    }
+    const int a = c * p.chunk;
+    const int b = min(a + p.chunk, N);
+    const int i0 = a + tid * SP;
+    const int i1 = min(i0 + SP, b);
+    const int cnt = max(0, i1 - i0);
+    const bool expl = p.eA != nullptr;
+    // lane scan coefficients
+    double PF[5], PB[5], PeF, PeB;
+    {
+        const int64_t T = (int64_t)c * LT + tid, GT = (int64_t)G * LT;
+#pragma unroll
+        for (int k = 0; k < 5; ++k) {
+            PF[k] = __ldg(p.sc.lane + k * GT + T);
+            PB[k] = __ldg(p.sc.lane + (6 + k) * GT + T);
+        }
+        PeF = __ldg(p.sc.lane + 5 * GT + T);
+        PeB = __ldg(p.sc.lane + 11 * GT + T);
+    }
+    double lf[5], lfN[5], mbv[5], kbv[5], mbc = 0.0;
+    if (warp == 0) {
+#pragma unroll
+        for (int t = 0; t < 5; ++t) {
+            const int q = lane + 32 * t;
+            const bool in = q < G;
+            lf[t] = in ? __ldg(p.Lf + (int64_t)c * G + q) : 0.0;
+            lfN[t] = in ? __ldg(p.Lf + (int64_t)G * G + q) : 0.0;
+            mbv[t] = in ? __ldg(p.Mb + (int64_t)c * G + q) : 0.0;
+            kbv[t] = in ? __ldg(p.Kb + (int64_t)c * G + q) : 0.0;
+        }
+        mbc = __ldg(p.mb + c);
+    }
+    double u[SP], kA[SP], kg[SP], kal[SP], kcf[SP], kcb[SP], kCB[SP], kGG[SP], klam[SP], S[SP];
+#pragma unroll
+    for (int k = 0; k < SP; ++k) {
+        const bool in = k < cnt;
+        const int i = in ? i0 + k : 0;
+        u[k] = in ? p.U[i] : 0.0;
+        kA[k] = in ? __ldg(p.A + i) : 0.0;
+        kg[k] = in ? __ldg(p.g + i) : 0.0;
+        kal[k] = in ? __ldg(p.al + i) : 0.0;
+        kcf[k] = in ? __ldg(p.cf + i) : 0.0;
+        kcb[k] = in ? __ldg(p.cb + i) : 0.0;
+        kCB[k] = in ? __ldg(p.CB + i) : 0.0;
+        kGG[k] = in ? __ldg(p.GG + i) : 0.0;
+        klam[k] = (in && p.lamv) ? __ldg(p.lamv + i) : p.lam;
+        S[k] = 0.0;
+    }
+    const bool ownsN = cnt > 0 && i1 == N;
+    double uNv = ownsN ? p.U[N] : 0.0;
+    if (expl) {
+        s_first[tid] = cnt > 0 ? u[0] : 0.0;
+        double last = 0.0;
+#pragma unroll
+        for (int k = 0; k < SP; ++k)
+            if (k < cnt) last = u[k];
+        s_last[tid] = last;
+    }
+    {                                                    // history of the first step
+        const int j = p.j0;
+#pragma unroll
+        for (int k = 0; k < SP; ++k) {
+            if (k < cnt) {
+                const int64_t i = i0 + k;
+                double s0 = 0.0, s1 = 0.0;
+                for (int q = 0; q < p.KS; ++q) s0 += __ldcg(p.cfar + ((int64_t)q * BLK + j) * p.P + i);
+                for (int r = 0; r < j; ++r) s1 = fma(__ldg(p.wlag + (j - r)), p.ring[i * 64 + r], s1);
+                S[k] = s0 + s1;
+            }
+        }
+    }
+    __syncthreads();
+    const unsigned long long base = s_base;
+    double hl = 0.0, hr = 0.0;                           // neighbour edge states (explicit part)
+    if (expl) {
+        if (tid == 0 && c > 0) hl = p.U[a - 1];
+        if (i1 == b && cnt > 0 && b < N) hr = p.U[b];
+    }
+    for (int s = 0; s < p.nsteps; ++s) {
+        const int j = p.j0 + s;
+        const int64_t n = p.n0 + s;
+        const unsigned long long tag = base + (unsigned long long)s + 1;
+        double *agg = p.agg + (size_t)(tag & 1ull) * (2 * G + 2);
+        // ---- right-hand side
+        double om[SP];
+        const double *src = p.src ? p.src + (int64_t)(n < p.src_rows ? n : p.src_rows - 1) * (N + 1) : nullptr;
+#pragma unroll
+        for (int k = 0; k < SP; ++k)
+            om[k] = (-(klam[k] * u[k]) + ((src && k < cnt) ? __ldg(src + i0 + k) : 0.0)) + S[k];
+        if (expl) {
+            if (tid > 0) hl = s_last[tid - 1];
+            if (i1 < b && cnt > 0) hr = s_first[tid + 1];
+            if (ownsN) hr = uNv;
+            double ul = hl;
+#pragma unroll
+            for (int k = 0; k < SP; ++k) {
+                if (k < cnt) {
+                    const double un = k + 1 < cnt ? u[k + 1] : hr;
+                    om[k] -= fma(__ldg(p.eA + i0 + k), ul, __ldg(p.eB + i0 + k) * un);
+                    ul = u[k];
+                }
+            }
+        }
+        if (ownsN && p.rkind != FPDE_BC_DIRICHLET) agg[2 * G] = u[cnt - 1];    // old U[N-1], flux closure
+        // ---- forward: segment sweep from zero carry, warp scan, warp totals
+        double y[SP];
+        double yl = 0.0;
+#pragma unroll
+        for (int k = 0; k < SP; ++k) {
+            if (k < cnt) {
+                if (i0 + k == 0) yl = p.g0;
+                else yl = kg[k] * (kA[k] * yl - om[k]);
+                y[k] = yl;
+            }
+        }
+        double X = cnt > 0 ? yl : 0.0;
+#pragma unroll
+        for (int k = 0; k < 5; ++k) {
+            const double Xp = __shfl_up_sync(FULL, X, 1 << k);
+            if (lane >= (1 << k)) X = fma(PF[k], Xp, X);
+        }
+        double Xe = __shfl_up_sync(FULL, X, 1);
+        if (lane == 0) Xe = 0.0;
+        if (lane == 31) wXf[warp] = X;
+        __syncthreads();                                                      // (A)
+        {
+            double xin = 0.0;
+#pragma unroll
+            for (int w = 0; w < NW; ++w)
+                if (w < warp) xin = fma(sCf[warp][w], wXf[w], xin);
+            const double carry = fma(PeF, xin, Xe);
+#pragma unroll
+            for (int k = 0; k < SP; ++k)
+                if (k < cnt) y[k] = fma(kcf[k], carry, y[k]);
+        }
+        // ---- backward: segment sweep from zero carry, warp scan, warp totals
+        double ub[SP];
+        double ul = 0.0;
+#pragma unroll
+        for (int k = SP - 1; k >= 0; --k) {
+            if (k < cnt) {
+                ul = fma(kal[k], ul, y[k]);
+                ub[k] = ul;
+            }
+        }
+        X = cnt > 0 ? ul : 0.0;
+#pragma unroll
+        for (int k = 0; k < 5; ++k) {
+            const double Xn = __shfl_down_sync(FULL, X, 1 << k);
+            if (lane + (1 << k) < 32) X = fma(PB[k], Xn, X);
+        }
+        Xe = __shfl_down_sync(FULL, X, 1);
+        if (lane == 31) Xe = 0.0;
+        if (lane == 0) wXb[warp] = X;
+        __syncthreads();                                                      // (B)
+        {
+            double xin = 0.0;
+#pragma unroll
+            for (int w = 0; w < NW; ++w)
+                if (w > warp) xin = fma(sCb[warp][w], wXb[w], xin);
+            const double carry = fma(PeB, xin, Xe);
+#pragma unroll
+            for (int k = 0; k < SP; ++k)
+                if (k < cnt) ub[k] = fma(kcb[k], carry, ub[k]);
+        }
+        // ---- thread 0 publishes the chunk's last y and first u (zero carries)
+        if (tid == 0) {
+            double ylast = 0.0, u0 = 0.0;
+#pragma unroll
+            for (int w = 0; w < NW; ++w) {
+                ylast = fma(sY[w], wXf[w], ylast);
+                u0 = fma(sU0[w], wXb[w], u0);
+            }
+            agg[2 * c] = ylast;
+            agg[2 * c + 1] = u0;
+            if (G > 1) {
+                __threadfence();
+                asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p.cflag + c), "l"(tag) : "memory");
+            }
+        }
+        // ---- while the chunks publish: the next step's history except its newest row
+        double Sn[SP];
+#pragma unroll
+        for (int k = 0; k < SP; ++k) Sn[k] = 0.0;
+        if (s + 1 < p.nsteps) {
+            const int jn = j + 1;
+#pragma unroll
+            for (int k = 0; k < SP; ++k) {
+                if (k < cnt) {
+                    const int64_t i = i0 + k;
+                    double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
+                    for (int q = 0; q < p.KS; ++q) s0 += __ldcg(p.cfar + ((int64_t)q * BLK + jn) * p.P + i);
+                    const double *rr = p.ring + i * 64;
+                    int r = 0;
+                    for (; r + 4 <= j; r += 4) {
+                        const double2 v0 = *(const double2 *)(rr + r), v1 = *(const double2 *)(rr + r + 2);
+                        s1 = fma(__ldg(p.wlag + (jn - r)), v0.x, s1);
+                        s2 = fma(__ldg(p.wlag + (jn - r - 1)), v0.y, s2);
+                        s3 = fma(__ldg(p.wlag + (jn - r - 2)), v1.x, s3);
+                        s1 = fma(__ldg(p.wlag + (jn - r - 3)), v1.y, s1);
+                    }
+                    for (; r < j; ++r) s2 = fma(__ldg(p.wlag + (jn - r)), rr[r], s2);
+                    Sn[k] = s0 + ((s1 + s2) + s3);
+                }
+            }
+        }
+        // ---- warp 0: every chunk's aggregates (one polling round for all flags), carries
+        if (warp == 0) {
+            bool ok = true;
+            if (G > 1) {
+                const unsigned long long t0 = gtimer_ns();
+                while (true) {
+                    bool mine = true;
+#pragma unroll
+                    for (int t = 0; t < 5; ++t) {
+                        const int q = lane + 32 * t;
+                        if (q < G && ld_acquire(p.cflag + q) < tag) mine = false;
+                    }
+                    if (__all_sync(FULL, mine)) break;
+                    if (gtimer_ns() - t0 > 1000000000ull) { ok = false; break; }
+                }
+                ok = __all_sync(FULL, ok);
+            }
+            if (!ok) {
+                if (lane == 0) { atomicOr(p.flags, DEVERR_BARRIER_TIMEOUT); s_abort = 1; }
+            } else {
+                double sc = 0.0, syN = 0.0, sub = 0.0;
+#pragma unroll
+                for (int t = 0; t < 5; ++t) {
+                    const int q = lane + 32 * t;
+                    if (q < G) {
+                        const double ye = __ldcg(agg + 2 * q), u0 = __ldcg(agg + 2 * q + 1);
+                        sc = fma(lf[t], ye, sc);
+                        syN = fma(lfN[t], ye, syN);
+                        sub = fma(mbv[t], u0, fma(kbv[t], ye, sub));
+                    }
+                }
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) {
+                    sc += __shfl_xor_sync(FULL, sc, o);
+                    syN += __shfl_xor_sync(FULL, syN, o);
+                    sub += __shfl_xor_sync(FULL, sub, o);
+                }
+                double uN;                               // right end (U1 :4685-4719)
+                if (p.rkind == FPDE_BC_DIRICHLET) {
+                    uN = p.gN;
+                } else {
+                    const double uNm1 = __ldcg(agg + 2 * G);
+                    if (fabs(syN) > 1e-15) uN = (fabs(1.0 - p.AlN) > 1e-15) ? (syN + p.gN * p.dLN) / (1.0 - p.AlN) : uNm1;
+                    else uN = (fabs(1.0 - p.AlN) > 1e-15) ? 0.0 : uNm1;
+                }
+                if (lane == 0) { s_cin = sc; s_ub = fma(mbc, uN, sub); s_UN = uN; }
+            }
+        }
+        __syncthreads();                                                      // (D)
+        if (s_abort) return;
+        const double cin = s_cin, ubv = s_ub;
+        // ---- new state, increment into the ring, the newest history row of the next step
+        const double w1 = __ldg(p.wlag + 1);
+#pragma unroll
+        for (int k = 0; k < SP; ++k) {
+            if (k < cnt) {
+                const int64_t i = i0 + k;
+                const double un = fma(kCB[k], ubv, fma(kGG[k], cin, ub[k]));
+                const double d = un - u[k];
+                p.ring[i * 64 + j] = d;
+                u[k] = un;
+                S[k] = fma(w1, d, Sn[k]);
+            }
+        }
+        if (ownsN) {
+            const double UN = s_UN;
+            p.ring[(int64_t)N * 64 + j] = UN - uNv;
+            uNv = UN;
+        }
+        if (expl) {                                      // edge states for the next step
+            s_first[tid] = cnt > 0 ? u[0] : 0.0;
+            double last = 0.0;
+#pragma unroll
+            for (int k = 0; k < SP; ++k)
+                if (k < cnt) last = u[k];
+            s_last[tid] = last;
+            double *halo = p.halo + (size_t)(tag & 1ull) * (2 * G + 2);
+            if (cnt > 0 && i0 == a) halo[2 * c] = u[0];
+            if (cnt > 0 && i1 == b) halo[2 * c + 1] = last;
+            __syncthreads();
+            if (tid == 0 && G > 1) {
+                __threadfence();
+                asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p.hflag + c), "l"(tag) : "memory");
+            }
+            if (s + 1 < p.nsteps && G > 1) {             // neighbours' edge states of this step
+                const unsigned long long t0 = gtimer_ns();
+                bool ok = true;
+                if (tid == 0 && c > 0) {
+                    ok = wait_flag(p.hflag + c - 1, tag, t0);
+                    if (ok) hl = __ldcg(halo + 2 * (c - 1) + 1);
+                }
+                if (cnt > 0 && i1 == b && b < N) {
+                    ok = wait_flag(p.hflag + c + 1, tag, t0);
+                    if (ok) hr = __ldcg(halo + 2 * (c + 1));
+                }
+                if (!ok) { atomicOr(p.flags, DEVERR_BARRIER_TIMEOUT); s_abort = 1; }
+            }
+            __syncthreads();
+            if (s_abort) return;
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < SP; ++k)
+        if (k < cnt) p.U[i0 + k] = u[k];
+    if (ownsN) p.U[N] = uNv;
+    if (c == 0 && tid == 0) *((volatile unsigned long long *)p.seq) = base + (unsigned long long)p.nsteps;
+}
+
 }  // namespace fpde
 
 using namespace fpde;
@@ -354,13 +743,14 @@ struct fpde_line {
     fpde_ctx *ctx = nullptr;
     fpde_line_desc d{};
     int64_t N = 0, P = 0;
-    int G = 1, s = 1, max_steps = 0;
+    int G = 1, s = 1, chunk = 0, max_steps = 0;
     bool split = false;
     double lam = 0, lamR = 0, kkk0 = 0, AlN = 0;
     double *A = nullptr, *g = nullptr, *al = nullptr, *cf = nullptr, *cb = nullptr;
     double *CF = nullptr, *CB = nullptr, *GG = nullptr;
     double *Lf = nullptr, *Mb = nullptr, *Kb = nullptr, *mb = nullptr;
-    unsigned long long *cflag = nullptr, *seq = nullptr;
+    unsigned long long *cflag = nullptr, *seq = nullptr, *hflag = nullptr;
+    double *halo = nullptr, *sclane = nullptr, *scwarp = nullptr;
     double *U = nullptr, *D = nullptr, *part = nullptr, *wrev = nullptr;
     double *agg = nullptr;
     unsigned *barrier = nullptr;
@@ -384,7 +774,7 @@ struct fpde_line {
     std::map<std::pair<int64_t, int>, cudaGraphExec_t> graphs;
     std::map<std::pair<int64_t, int>, int64_t> graph_launches;
     // probes: CUDA events around kernels inside the captured graph
-    struct Probe { int kind; int64_t n; double bytes, flops; int ev; };
+    struct Probe { int kind; int64_t n; double bytes, flops; int ev; int steps; };
     int probe_every = 0;
     std::vector<cudaEvent_t> probe_ev;
     std::vector<Probe> probes;                            // recorded by the last enqueue
@@ -414,6 +804,7 @@ static int line_launch_solve(fpde_line *L, cudaStream_t st, int64_t n, const dou
     a.barrier = L->barrier; a.flags = L->ctx->d_flags;
     a.lam = L->lam; a.g0 = L->d.left_value; a.gN = L->d.right_value; a.dLN = L->d.dLN;
     a.AlN = L->AlN; a.KS = KS; a.nr = nr; a.N = (int)L->N; a.G = L->G; a.rkind = L->d.right_kind;
+    a.chunk = L->chunk;
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(L->G);
     cfg.blockDim = dim3(LT);
@@ -435,12 +826,53 @@ static int line_launch_solve(fpde_line *L, cudaStream_t st, int64_t n, const dou
     return FPDE_OK;
 }
 
-static cudaEvent_t *probe_begin(fpde_line *L, int kind, int64_t n, double bytes, double flops)
+static cudaEvent_t *probe_begin(fpde_line *L, int kind, int64_t n, double bytes, double flops, int steps = 1)
 {
     const size_t k = L->probes.size();
     if (2 * (k + 1) > L->probe_ev.size()) return nullptr;
-    L->probes.push_back({kind, n, bytes, flops, (int)(2 * k)});
+    L->probes.push_back({kind, n, bytes, flops, (int)(2 * k), steps});
     return &L->probe_ev[2 * k];
+}
+
+template <int SP>
+static cudaError_t launch_block_sp(const cudaLaunchConfig_t &cfg, const LineBlockArgs &a)
+{
+    return cudaLaunchKernelEx(&cfg, k_line_block<SP>, a);
+}
+
+// Steps j0 .. j0+nsteps-1 of the block starting at nb0 in one persistent launch.
+static int line_launch_block(fpde_line *L, cudaStream_t st, int64_t nb0, int j0, int nsteps, int KS)
+{
+    LineBlockArgs a;
+    a.A = L->A; a.g = L->g; a.al = L->al; a.cf = L->cf; a.cb = L->cb; a.CB = L->CB; a.GG = L->GG;
+    a.lamv = L->lamv; a.eA = L->eA; a.eB = L->eB;
+    a.src = L->srcd; a.src_rows = L->src_rows;
+    a.U = L->U; a.ring = L->ring; a.cfar = L->cfar; a.KS = KS; a.P = L->P; a.wlag = L->wlag;
+    a.agg = L->agg; a.halo = L->halo; a.cflag = L->cflag; a.hflag = L->hflag; a.seq = L->seq;
+    a.Lf = L->Lf; a.Mb = L->Mb; a.Kb = L->Kb; a.mb = L->mb; a.flags = L->ctx->d_flags;
+    a.sc.lane = L->sclane; a.sc.warp = L->scwarp;
+    a.lam = L->lam; a.g0 = L->d.left_value; a.gN = L->d.right_value; a.dLN = L->d.dLN; a.AlN = L->AlN;
+    a.n0 = nb0 + j0; a.j0 = j0; a.nsteps = nsteps; a.N = (int)L->N; a.G = L->G; a.rkind = L->d.right_kind;
+    a.chunk = L->chunk;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(L->G);
+    cfg.blockDim = dim3(LT);
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = L->G > 1 ? 1 : 0;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    cudaError_t e;
+    switch (L->s) {
+    case 1: e = launch_block_sp<1>(cfg, a); break;
+    case 2: e = launch_block_sp<2>(cfg, a); break;
+    case 4: e = launch_block_sp<4>(cfg, a); break;
+    default: e = launch_block_sp<8>(cfg, a); break;
+    }
+    if (e != cudaSuccess) return set_error(FPDE_ERR_CUDA, "line block launch: %s", cudaGetErrorString(e));
+    count_launches(1);
+    return FPDE_OK;
 }
 
 #define PROBE_REC(ev, i) \
@@ -511,14 +943,19 @@ static int line_enqueue(fpde_line *L, cudaStream_t st, int64_t n0, int steps, in
                 PROBE_REC(ev, 1);
                 ++k;
             }
-            const double *wn = L->wrev + (L->max_steps - j);       // wn[r] = w[j - r]
-            ev = probe_step ? probe_begin(L, 2, n, 0.0, 0.0) : nullptr;
+            // the rest of this block (or of the requested range) in one persistent launch
+            const int nst = (int)std::min<int64_t>(BLK - j, n0 + steps - n);
+            double bytes = 0.0, flops = 0.0;
+            for (int q = j; q < j + nst; ++q) {                  // far fold + near ring + state
+                bytes += 8.0 * nodes_hist * (splits + q + 2);
+                flops += (double)nodes_hist * (splits + 2.0 * q + 30.0);
+            }
+            ev = L->probe_every > 0 ? probe_begin(L, 2, n, bytes, flops, nst) : nullptr;
             PROBE_REC(ev, 0);
-            if ((rc = line_launch_solve(L, st, n, L->cfar + (int64_t)j * L->P, splits, (int64_t)BLK * L->P, L->ring, wn,
-                                        j, L->ring + j, BLK)))
-                return rc;
+            if ((rc = line_launch_block(L, st, nb0, j, nst, splits))) return rc;
             PROBE_REC(ev, 1);
             ++k;
+            n += nst - 1;
         }
     }
     if (nk) *nk = k;
@@ -553,7 +990,11 @@ int fpde_line_destroy(fpde_line *L)
     for (auto &kv : L->graphs) cudaGraphExecDestroy(kv.second);
     for (cudaEvent_t e : L->probe_ev) cudaEventDestroy(e);
     dev_free(L->cflag);
+    dev_free(L->hflag);
     dev_free(L->seq);
+    dev_free(L->halo);
+    dev_free(L->sclane);
+    dev_free(L->scwarp);
     for (double *p : {L->A, L->g, L->al, L->cf, L->cb, L->CF, L->CB, L->GG, L->Lf, L->Mb, L->Kb, L->mb, L->U, L->D,
                       L->part, L->wrev, L->agg, L->ring, L->cfar, L->wlag, L->out_scale, L->srcd, L->lamv, L->eA,
                       L->eB})
@@ -606,6 +1047,13 @@ int fpde_line_create(fpde_ctx *ctx, const fpde_line_desc *desc, const double *A,
                              (long long)N, (long long)ctx->sm_count * LT * LSEG, LT, LSEG);
         G = (int)((N + (int64_t)LT * sp - 1) / ((int64_t)LT * sp));
     }
+    // chunk of nodes per CTA: LT * sp, or (long lines) an even share of all SMs, rounded to sp
+    int64_t chunk = (int64_t)LT * sp;
+    if (G > 1 && N >= (int64_t)ctx->sm_count * LT) {
+        chunk = (N + ctx->sm_count - 1) / ctx->sm_count;
+        chunk = (chunk + sp - 1) / sp * sp;
+        G = (int)((N + chunk - 1) / chunk);
+    }
     if (G > 160) return set_error(FPDE_ERR_UNSUPPORTED, "line solve: at most 160 chunks");
     int per_sm = 0;
     FPDE_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_line_solve<LSEG>, LT, 0));
@@ -619,6 +1067,7 @@ int fpde_line_create(fpde_ctx *ctx, const fpde_line_desc *desc, const double *A,
     L->P = (N + 1 + 511) / 512 * 512;
     L->G = G;
     L->s = sp;
+    L->chunk = (int)chunk;
     L->max_steps = d.max_steps;
     L->split = d.precision != FPDE_PREC_FP64;
     L->x3 = d.precision == FPDE_PREC_SPLIT_BF16X3;
@@ -657,7 +1106,7 @@ int fpde_line_create(fpde_ctx *ctx, const fpde_line_desc *desc, const double *A,
     // backward sweep GG of CF, so that u = u^cta + c_in GG + u_b CB
     std::vector<double> hCF(N), hCB(N), hGG(N), hPend(G), hG0(G), hB0(G);
     for (int cc = 0; cc < G; ++cc) {
-        const int64_t a0 = (int64_t)cc * LT * sp, b0 = std::min<int64_t>(a0 + (int64_t)LT * sp, N);
+        const int64_t a0 = (int64_t)cc * chunk, b0 = std::min<int64_t>(a0 + chunk, N);
         double pr = 1.0;
         for (int64_t i = a0; i < b0; ++i) { pr *= hp[i]; hCF[i] = pr; }
         double cbv = 1.0, gg = 0.0;
@@ -688,6 +1137,63 @@ int fpde_line_create(fpde_ctx *ctx, const fpde_line_desc *desc, const double *A,
             for (int r = 0; r < q; ++r) hKb[(size_t)cc * G + r] += f * hLf[(size_t)q * G + r];
         }
     }
+    // scan coefficients of the persistent split-path kernel (all products are time-invariant):
+    // per thread the products of its segment (forward P, backward Q); per lane the products
+    // the five warp-scan levels multiply with and the exclusive prefix/suffix products; per
+    // CTA the cross-warp coefficients and the rows that give the chunk aggregates.
+    constexpr int NWc = LT / 32;
+    const int64_t GT = (int64_t)G * LT;
+    std::vector<double> hsl((size_t)12 * GT, 1.0), hsw((size_t)G * (2 * NWc * NWc + 2 * NWc), 0.0);
+    for (int cc = 0; cc < G; ++cc) {
+        double Pt[LT], Qt[LT];
+        const int64_t a0 = (int64_t)cc * chunk, b0 = std::min<int64_t>(a0 + chunk, N);
+        for (int t = 0; t < LT; ++t) {
+            const int64_t i0 = a0 + (int64_t)t * sp, i1 = std::min<int64_t>(i0 + sp, b0);
+            Pt[t] = i1 > i0 ? hcf[i1 - 1] : 1.0;
+            Qt[t] = i1 > i0 ? hcb[i0] : 1.0;
+        }
+        double PW[NWc], QW[NWc];
+        for (int w = 0; w < NWc; ++w) {
+            const double *pw = Pt + 32 * w, *qw = Qt + 32 * w;
+            for (int l = 0; l < 32; ++l) {
+                const int64_t T = (int64_t)cc * LT + 32 * w + l;
+                for (int k = 0; k < 5; ++k) {
+                    double pf = 1.0, pb = 1.0;
+                    for (int m = std::max(0, l - (1 << k) + 1); m <= l; ++m) pf *= pw[m];
+                    for (int m = l; m <= std::min(31, l + (1 << k) - 1); ++m) pb *= qw[m];
+                    hsl[(size_t)k * GT + T] = pf;
+                    hsl[(size_t)(6 + k) * GT + T] = pb;
+                }
+                double pe = 1.0, qe = 1.0;
+                for (int m = 0; m < l; ++m) pe *= pw[m];
+                for (int m = l + 1; m < 32; ++m) qe *= qw[m];
+                hsl[(size_t)5 * GT + T] = pe;
+                hsl[(size_t)11 * GT + T] = qe;
+            }
+            double pt = 1.0, qt = 1.0;
+            for (int l = 0; l < 32; ++l) { pt *= pw[l]; qt *= qw[l]; }
+            PW[w] = pt;
+            QW[w] = qt;
+        }
+        double *wc = hsw.data() + (size_t)cc * (2 * NWc * NWc + 2 * NWc);
+        for (int w = 0; w < NWc; ++w) {
+            for (int v = 0; v < w; ++v) {                 // Cf[w][v] = prod_{v < x < w} PW[x]
+                double pr = 1.0;
+                for (int x = v + 1; x < w; ++x) pr *= PW[x];
+                wc[w * NWc + v] = pr;
+            }
+            for (int v = w + 1; v < NWc; ++v) {           // Cb[w][v] = prod_{w < x < v} QW[x]
+                double pr = 1.0;
+                for (int x = w + 1; x < v; ++x) pr *= QW[x];
+                wc[NWc * NWc + w * NWc + v] = pr;
+            }
+            double py = 1.0, pu = 1.0;                    // Yrow[w], U0row[w]
+            for (int x = w + 1; x < NWc; ++x) py *= PW[x];
+            for (int x = 0; x < w; ++x) pu *= QW[x];
+            wc[2 * NWc * NWc + w] = py;
+            wc[2 * NWc * NWc + NWc + w] = pu;
+        }
+    }
     // lag weights w[j] = Da * kb(lag j) / tau with kb(lag j) = kkk0 * b_j; wrev[m] = w[L - m]
     const int64_t LW = L->max_steps + BLK + 1;
     std::vector<double> wlag(LW, 0.0);
@@ -707,7 +1213,11 @@ int fpde_line_create(fpde_ctx *ctx, const fpde_line_desc *desc, const double *A,
                 dev_alloc((void **)&L->seq, sizeof(unsigned long long)) ||
                 dev_alloc((void **)&L->U, L->P * sizeof(double)) ||
                 dev_alloc((void **)&L->wrev, wrev.size() * sizeof(double)) ||
-                dev_alloc((void **)&L->agg, (2 * G + 2) * sizeof(double)) ||
+                dev_alloc((void **)&L->agg, 2 * (2 * G + 2) * sizeof(double)) ||
+                dev_alloc((void **)&L->halo, 2 * (2 * G + 2) * sizeof(double)) ||
+                dev_alloc((void **)&L->hflag, (size_t)G * sizeof(unsigned long long)) ||
+                dev_alloc((void **)&L->sclane, hsl.size() * sizeof(double)) ||
+                dev_alloc((void **)&L->scwarp, hsw.size() * sizeof(double)) ||
                 dev_alloc((void **)&L->barrier, 2 * sizeof(unsigned));
     if (!fail && !L->split) {
         fail = dev_alloc((void **)&L->D, (size_t)L->max_steps * L->P * sizeof(double)) ||
@@ -799,6 +1309,9 @@ int fpde_line_create(fpde_ctx *ctx, const fpde_line_desc *desc, const double *A,
     cudaMemcpyAsync(L->Kb, hKb.data(), hKb.size() * sizeof(double), cudaMemcpyHostToDevice, st);
     cudaMemcpyAsync(L->mb, hmb.data(), gb, cudaMemcpyHostToDevice, st);
     cudaMemsetAsync(L->cflag, 0, (size_t)G * sizeof(unsigned long long), st);
+    cudaMemsetAsync(L->hflag, 0, (size_t)G * sizeof(unsigned long long), st);
+    cudaMemcpyAsync(L->sclane, hsl.data(), hsl.size() * sizeof(double), cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(L->scwarp, hsw.data(), hsw.size() * sizeof(double), cudaMemcpyHostToDevice, st);
     cudaMemsetAsync(L->seq, 0, sizeof(unsigned long long), st);
     cudaMemcpyAsync(L->wrev, wrev.data(), wrev.size() * sizeof(double), cudaMemcpyHostToDevice, st);
     cudaMemsetAsync(L->U, 0, L->P * sizeof(double), st);
@@ -938,7 +1451,7 @@ int fpde_line_set_probe(fpde_line *L, int every)
     L->probe_ev.clear();
     L->probe_every = every;
     if (every > 0) {
-        int64_t n = L->max_steps / every + L->max_steps / BLK + 2;
+        int64_t n = 2 * (L->max_steps / every) + 2 * (L->max_steps / BLK) + 4;
         if (n > 8192) n = 8192;
         L->probe_ev.resize(2 * n);
         for (auto &e : L->probe_ev) FPDE_CUDA(cudaEventCreate(&e));
@@ -962,7 +1475,7 @@ int fpde_line_probe_stats(fpde_line *L, int kind, double *ms, double *bytes, dou
         m += t;
         b += p.bytes;
         f += p.flops;
-        ++c;
+        c += p.steps;
     }
     *ms = m;
     *bytes = b;

@@ -265,8 +265,10 @@ int fpde_line_steps_done(const fpde_line *line, int64_t *n);
  * `every`-th step and around every far-history contraction. fpde_line_probe_stats returns,
  * for the last run and one kind of kernel (0 FP64 history GEMV, 1 tensor-core far
  * contraction, 2 line solve), the summed event time (ms), the summed algorithmic bytes
- * (GEMV: 8 * rows * (N+1); contraction: 4 * rows * (N+1) of hi/lo history), the summed
- * algorithmic flops and the number of probed launches. */
+ * (GEMV: 8 * rows * (N+1); contraction: 2 bytes per slice * rows * (N+1) of 16-bit history;
+ * solve: 8 * (N+1) * (far splits + near rows + 2)), the summed algorithmic flops and the
+ * number of time steps the probed launches cover (for the contraction: its launches). On
+ * the split paths every block's solve launch is probed; on the FP64 path every `every`-th. */
 int fpde_line_set_probe(fpde_line *line, int every);
 int fpde_line_probe_stats(fpde_line *line, int kind, double *ms, double *bytes, double *flops,
                           int *count);
