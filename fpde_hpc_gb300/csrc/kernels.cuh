@@ -23,7 +23,7 @@ namespace fpde {
 
 // Buffers of the split-precision path touched by the per-block preparation (split.cu).
 struct SplitPrep {
-    const double *ring = nullptr;        // [P][64] FP64 increments of the finished block (node-major)
+    const double *ring = nullptr;        // [64][P] FP64 increments of the finished block (time-major)
     int64_t P = 0, nvalid = 0;           // row pitch of the ring, nodes with history
     unsigned long long *slots = nullptr; // per block: max |increment| (double bits)
     int *exps = nullptr;                 // per block: scale exponent sexp

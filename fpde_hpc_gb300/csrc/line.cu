@@ -1,17 +1,17 @@
 // 1D line problem (fpde_line_*): the plain FP64 path and the split-precision path.
 //
 // Per time step n (fpde_hpc_1d.cpp calc_step / U1 with the history applied every step):
-//   FP64 path
+//   FP64 path (one launch each per step)
 //     1. k_l1_partial : part[ks][i] = sum_t w[n-t] D_t[i]        (FP64 history GEMV)
 //     2. k_line_solve : S = sum_ks part, Om = -lam U + src + S, Thomas solve, U <- U^{n+1},
-//                       D_n = U^{n+1} - U^n                       (one cooperative launch)
+//                       D_n = U^{n+1} - U^n
 //   split path (blocks of 64 steps starting at n0)
-//     at n0:  convert the finished block's FP64 increments into 16-bit hi/lo history,
+//     at n0:  convert the finished block's FP64 increments into 16-bit history slices,
 //             build the Toeplitz weight tile and run the tensor-core contraction for the
 //             far history t < n0 (tc_far.cu) -> FP64 partials C[split][j][i]
-//     each step j = n - n0:
-//             S = sum_split C[split][j][i] + sum_{n0 <= t < n} w[n-t] D_t[i]   (near: FP64)
-//             then the same solve; D_n goes to a 64-row FP64 ring.
+//     steps of the block: k_line_block, one persistent launch: S = sum_split C[split][j][i]
+//             + sum_{n0 <= t < n} w[n-t] D_t[i] (near history in FP64), the solve, and D_n
+//             into a 64-row FP64 ring.
 // The whole run is captured once into a CUDA graph and replayed.
 //
 // The Thomas solve of a long line runs on all SMs. The alpha recurrence
@@ -23,9 +23,10 @@
 // threads sweep segments of SP nodes sequentially, segments are joined by warp-shuffle
 // scans of (product, value) pairs and across warps through shared memory. Because the
 // recurrences are linear, the true solution is U = U^cta + c_in GG + u_b CB, with GG and CB
-// time-invariant per node. After one bounded grid barrier, warp 0 of every CTA solves the
-// two short chunk-level recurrences for all carries (c_in forward, u_b backward) from the
-// chunks' published end values, and every node takes two FMAs to finish.
+// time-invariant per node. Every CTA publishes two numbers per step (its last y and first u
+// with zero carries) behind a release flag; warp 0 of every CTA waits (bounded) for all
+// flags and forms its chunk's carries c_in and u_b as dot products with precomputed rows,
+// and every node takes two FMAs to finish.
 #include <map>
 #include <vector>
 #include <cmath>
@@ -54,15 +55,13 @@ struct LineSolveArgs {
     int64_t dstride;
     const double *part;                   // S += sum_{q<KS} part[q*pstride + i]
     int64_t pstride;
-    const double *ring;                   // S += sum_{r<nr} wn[r] * ring[i*64 + r]   (node-major)
-    const double *wn;
     double *agg;                          // [G][2] (chunk's last y, chunk's first u), agg[2G] = old U[N-1]
     unsigned long long *cflag;            // per chunk: launch sequence number of its published values
     unsigned long long *seq;              // launch sequence counter (read at start, advanced by CTA 0)
     const double *Lf, *Mb, *Kb, *mb;      // chunk-carry rows: c_in = Lf Y, u_b = Mb U0 + Kb Y + mb U_N
     unsigned *barrier, *flags;
     double lam, g0, gN, dLN, AlN;
-    int KS, nr, N, G, rkind, chunk;
+    int KS, N, G, rkind, chunk;
 };
 
 
@@ -151,35 +150,6 @@ __global__ void __launch_bounds__(LT) k_line_solve(LineSolveArgs p)
         }
 #pragma unroll
         for (int k = 0; k < SP; ++k) om[k] = (a0[k] + a1[k]) + (a2[k] + a3[k]);
-    }
-    if (p.nr > 0) {                                                  // FP64 near history, 4-way ILP
-        double a0[SP], a1[SP], a2[SP], a3[SP];
-#pragma unroll
-        for (int k = 0; k < SP; ++k) { a0[k] = 0.0; a1[k] = 0.0; a2[k] = 0.0; a3[k] = 0.0; }
-        int r = 0;
-        for (; r + 4 <= p.nr; r += 4) {
-            const double w0 = __ldg(p.wn + r), w1 = __ldg(p.wn + r + 1), w2 = __ldg(p.wn + r + 2),
-                         w3 = __ldg(p.wn + r + 3);
-#pragma unroll
-            for (int k = 0; k < SP; ++k) {
-                if (k < cnt) {
-                    const double2 *rp = (const double2 *)(p.ring + (int64_t)(i0 + k) * 64 + r);
-                    const double2 v = __ldg(rp), v2 = __ldg(rp + 1);
-                    a0[k] = fma(w0, v.x, a0[k]);
-                    a1[k] = fma(w1, v.y, a1[k]);
-                    a2[k] = fma(w2, v2.x, a2[k]);
-                    a3[k] = fma(w3, v2.y, a3[k]);
-                }
-            }
-        }
-        for (; r < p.nr; ++r) {
-            const double w0 = __ldg(p.wn + r);
-#pragma unroll
-            for (int k = 0; k < SP; ++k)
-                if (k < cnt) a0[k] = fma(w0, __ldg(p.ring + (int64_t)(i0 + k) * 64 + r), a0[k]);
-        }
-#pragma unroll
-        for (int k = 0; k < SP; ++k) om[k] += (a0[k] + a1[k]) + (a2[k] + a3[k]);
     }
 #pragma unroll
     for (int k = 0; k < SP; ++k) {
@@ -348,20 +318,28 @@ __global__ void __launch_bounds__(LT) k_line_solve(LineSolveArgs p)
 
 // ---------------------------------------------------------------------------------------
 // Persistent form for the split path: one cooperative launch advances steps j0 .. j0+nsteps-1
-// of a 64-step block. Every CTA keeps its chunk's state and time-invariant data in registers
-// for the whole launch; per step the CTAs exchange only their two chunk aggregates (double-
-// buffered by step parity, published with a release flag carrying a monotonically growing
-// tag). While the exchange of step j is in flight, every thread already sums the far partials
-// and the near history of step j+1 except the newest increment, which is added once known.
+// of a 64-step block, with two warp roles per CTA:
+//   solver warps (LTS threads, SP nodes each): the chunk's right-hand side, the two sweeps and
+//     scans, the exchange of the two chunk aggregates with all other chunks (double-buffered
+//     by step parity, release flags carrying a monotonically growing tag) and the new state;
+//     state and time-invariant data stay in registers for the whole launch;
+//   history warps (LTS threads): during step j, the far partials and the FP64 near history of
+//     step j+1 for every node of the chunk except the newest increment (which the solver
+//     adds), handed over in shared memory.
+// The two roles meet at one CTA barrier per step; the solver warps synchronise among
+// themselves with a named barrier. Near-history FP64 work thus overlaps the latency-bound
+// scans and the exchange.
 //
-// All products of the scans are time-invariant (they are products of the recurrence
-// coefficients), so they are precomputed on the host: a warp-scan level is one shuffle and
-// one FMA, the combination across the warps of a CTA is a dot product with precomputed
-// coefficients (no second barrier), and thread 0 forms the chunk's two aggregates from the
-// warp totals and publishes them itself. Three CTA barriers per step remain.
+// All products of the scans are time-invariant, so they are precomputed on the host: a
+// warp-scan level is one shuffle and one FMA, the combination across the solver warps is a
+// dot product with precomputed coefficients, and the chunk's aggregates are the last y and
+// first u of the chunk, published by the two threads that own them.
+constexpr int LTS = 128;                 // solver threads per CTA (= history threads)
+constexpr int NWS = LTS / 32;
+
 struct ScanCoef {
-    const double *lane;       // [12][G*LT]: 5 forward level products, forward prefix, 5 backward, backward suffix
-    const double *warp;       // [G][4][NW][NW]: Cf, Cb (cross-warp), Yrow, U0row (chunk aggregates, first row)
+    const double *lane;       // [12][G*LTS]: 5 forward level products, forward prefix, 5 backward, backward suffix
+    const double *warp;       // [G][2][NWS][NWS]: cross-warp coefficients (forward, backward)
 };
 
 struct LineBlockArgs {
@@ -370,7 +348,7 @@ struct LineBlockArgs {
     const double *src;                    // optional per-step source rows ((N+1) each)
     int src_rows;
     double *U;                            // state: read at start, written at the end
-    double *ring;                         // [P][64] node-major increments of the block
+    double *ring;                         // [64][P] time-major increments of the block
     const double *cfar;                   // far partials [KS][64][P]
     int KS;
     int64_t P;
@@ -401,37 +379,99 @@ __device__ __forceinline__ bool wait_flag(const unsigned long long *f, unsigned 
     return true;
 }
 
+__device__ __forceinline__ void solver_sync() { asm volatile("bar.sync 1, %0;" ::"n"(LTS) : "memory"); }
+
+// history warps: S[node] = far partials of step j + sum_{r < rmax} w[j - r] ring[r][node]
 template <int SP>
-__global__ void __launch_bounds__(LT, 1) k_line_block(LineBlockArgs p)
+__device__ __forceinline__ void history_sum(const LineBlockArgs &p, int ht, int a, int b, int j, int rmax,
+                                            double *out)
 {
-    constexpr int NW = LT / 32;
-    __shared__ double wXf[NW], wXb[NW];
-    __shared__ double sCf[NW][NW], sCb[NW][NW], sY[NW], sU0[NW];
+    double acc[SP], far[SP];
+    int64_t node[SP];
+#pragma unroll
+    for (int q = 0; q < SP; ++q) {
+        node[q] = a + ht + LTS * q;
+        acc[q] = 0.0;
+        far[q] = 0.0;
+    }
+    for (int k = 0; k < p.KS; ++k) {
+#pragma unroll
+        for (int q = 0; q < SP; ++q)
+            if (node[q] < b) far[q] += __ldcg(p.cfar + ((int64_t)k * BLK + j) * p.P + node[q]);
+    }
+    int r = 0;
+    for (; r + 8 <= rmax; r += 8) {                      // eight rows of loads in flight
+        double v[8][SP];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            const double *row = p.ring + (int64_t)(r + u) * p.P;
+#pragma unroll
+            for (int q = 0; q < SP; ++q) v[u][q] = node[q] < b ? row[node[q]] : 0.0;
+        }
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            const double w = __ldg(p.wlag + (j - r - u));
+#pragma unroll
+            for (int q = 0; q < SP; ++q) acc[q] = fma(w, v[u][q], acc[q]);
+        }
+    }
+    for (; r < rmax; ++r) {
+        const double w = __ldg(p.wlag + (j - r));
+        const double *row = p.ring + (int64_t)r * p.P;
+#pragma unroll
+        for (int q = 0; q < SP; ++q)
+            if (node[q] < b) acc[q] = fma(w, row[node[q]], acc[q]);
+    }
+#pragma unroll
+    for (int q = 0; q < SP; ++q)
+        if (node[q] < b) out[ht + LTS * q] = far[q] + acc[q];
+}
+
+template <int SP>
+__global__ void __launch_bounds__(2 * LTS, 1) k_line_block(LineBlockArgs p)
+{
+    __shared__ double sS[2][LTS * SP];                   // next step's history, by step parity
+    __shared__ double wXf[NWS], wXb[NWS];
+    __shared__ double sCf[NWS][NWS], sCb[NWS][NWS];
     __shared__ double s_cin, s_ub, s_UN;
-    __shared__ double s_first[LT], s_last[LT];
+    __shared__ double s_first[LTS], s_last[LTS];
     __shared__ unsigned long long s_base;
     __shared__ int s_abort;
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int tid = threadIdx.x;
+    const bool solver = tid < LTS;
     const int c = blockIdx.x, G = p.G, N = p.N;
-    if (tid == 0) { s_base = *((volatile unsigned long long *)p.seq); s_abort = 0; }
-    {
-        const double *wc = p.sc.warp + (size_t)c * (2 * NW * NW + 2 * NW);
-        for (int q = tid; q < NW * NW; q += LT) {
-            sCf[q / NW][q % NW] = wc[q];
-            sCb[q / NW][q % NW] = wc[NW * NW + q];
-        }
-        if (tid < NW) { sY[tid] = wc[2 * NW * NW + tid]; sU0[tid] = wc[2 * NW * NW + NW + tid]; }
-    }
     const int a = c * p.chunk;
     const int b = min(a + p.chunk, N);
+    if (tid == 0) { s_base = *((volatile unsigned long long *)p.seq); s_abort = 0; }
+    if (tid < NWS * NWS) {
+        const double *wc = p.sc.warp + (size_t)c * (2 * NWS * NWS);
+        sCf[tid / NWS][tid % NWS] = wc[tid];
+        sCb[tid / NWS][tid % NWS] = wc[NWS * NWS + tid];
+    }
+
+    if (!solver) {
+        // ======================================================= history warps
+        const int ht = tid - LTS;
+        history_sum<SP>(p, ht, a, b, p.j0, p.j0, sS[p.j0 & 1]);           // full history of step j0
+        __syncthreads();                                                    // start
+        for (int s = 0; s < p.nsteps; ++s) {
+            const int j = p.j0 + s;
+            if (s + 1 < p.nsteps) history_sum<SP>(p, ht, a, b, j + 1, j, sS[(j + 1) & 1]);
+            __syncthreads();                                                // end of step s
+            if (s_abort) return;
+        }
+        return;
+    }
+
+    // =========================================================== solver warps
+    const int lane = tid & 31, warp = tid >> 5;
     const int i0 = a + tid * SP;
     const int i1 = min(i0 + SP, b);
     const int cnt = max(0, i1 - i0);
     const bool expl = p.eA != nullptr;
-    // lane scan coefficients
     double PF[5], PB[5], PeF, PeB;
     {
-        const int64_t T = (int64_t)c * LT + tid, GT = (int64_t)G * LT;
+        const int64_t T = (int64_t)c * LTS + tid, GT = (int64_t)G * LTS;
 #pragma unroll
         for (int k = 0; k < 5; ++k) {
             PF[k] = __ldg(p.sc.lane + k * GT + T);
@@ -453,7 +493,7 @@ __global__ void __launch_bounds__(LT, 1) k_line_block(LineBlockArgs p)
         }
         mbc = __ldg(p.mb + c);
     }
-    double u[SP], kA[SP], kg[SP], kal[SP], kcf[SP], kcb[SP], kCB[SP], kGG[SP], klam[SP], S[SP];
+    double u[SP], kA[SP], kg[SP], kal[SP], kcf[SP], kcb[SP], kCB[SP], kGG[SP], klam[SP], dprev[SP];
 #pragma unroll
     for (int k = 0; k < SP; ++k) {
         const bool in = k < cnt;
@@ -467,7 +507,7 @@ __global__ void __launch_bounds__(LT, 1) k_line_block(LineBlockArgs p)
         kCB[k] = in ? __ldg(p.CB + i) : 0.0;
         kGG[k] = in ? __ldg(p.GG + i) : 0.0;
         klam[k] = (in && p.lamv) ? __ldg(p.lamv + i) : p.lam;
-        S[k] = 0.0;
+        dprev[k] = 0.0;
     }
     const bool ownsN = cnt > 0 && i1 == N;
     double uNv = ownsN ? p.U[N] : 0.0;
@@ -479,37 +519,28 @@ __global__ void __launch_bounds__(LT, 1) k_line_block(LineBlockArgs p)
             if (k < cnt) last = u[k];
         s_last[tid] = last;
     }
-    {                                                    // history of the first step
-        const int j = p.j0;
-#pragma unroll
-        for (int k = 0; k < SP; ++k) {
-            if (k < cnt) {
-                const int64_t i = i0 + k;
-                double s0 = 0.0, s1 = 0.0;
-                for (int q = 0; q < p.KS; ++q) s0 += __ldcg(p.cfar + ((int64_t)q * BLK + j) * p.P + i);
-                for (int r = 0; r < j; ++r) s1 = fma(__ldg(p.wlag + (j - r)), p.ring[i * 64 + r], s1);
-                S[k] = s0 + s1;
-            }
-        }
-    }
-    __syncthreads();
-    const unsigned long long base = s_base;
     double hl = 0.0, hr = 0.0;                           // neighbour edge states (explicit part)
     if (expl) {
         if (tid == 0 && c > 0) hl = p.U[a - 1];
         if (i1 == b && cnt > 0 && b < N) hr = p.U[b];
     }
+    __syncthreads();                                                        // start
+    const unsigned long long base = s_base;
+    const double w1 = __ldg(p.wlag + 1);
     for (int s = 0; s < p.nsteps; ++s) {
         const int j = p.j0 + s;
         const int64_t n = p.n0 + s;
         const unsigned long long tag = base + (unsigned long long)s + 1;
         double *agg = p.agg + (size_t)(tag & 1ull) * (2 * G + 2);
-        // ---- right-hand side
+        // ---- right-hand side: history (newest row added here) + local term (+ explicit part)
         double om[SP];
         const double *src = p.src ? p.src + (int64_t)(n < p.src_rows ? n : p.src_rows - 1) * (N + 1) : nullptr;
+        const double *hs = sS[j & 1];
 #pragma unroll
-        for (int k = 0; k < SP; ++k)
-            om[k] = (-(klam[k] * u[k]) + ((src && k < cnt) ? __ldg(src + i0 + k) : 0.0)) + S[k];
+        for (int k = 0; k < SP; ++k) {
+            const double S = k < cnt ? fma(w1, dprev[k], hs[i0 - a + k]) : 0.0;
+            om[k] = (-(klam[k] * u[k]) + ((src && k < cnt) ? __ldg(src + i0 + k) : 0.0)) + S;
+        }
         if (expl) {
             if (tid > 0) hl = s_last[tid - 1];
             if (i1 < b && cnt > 0) hr = s_first[tid + 1];
@@ -545,17 +576,20 @@ __global__ void __launch_bounds__(LT, 1) k_line_block(LineBlockArgs p)
         double Xe = __shfl_up_sync(FULL, X, 1);
         if (lane == 0) Xe = 0.0;
         if (lane == 31) wXf[warp] = X;
-        __syncthreads();                                                      // (A)
+        solver_sync();                                                      // (A)
         {
-            double xin = 0.0;
+            double x0 = 0.0, x1 = 0.0;
 #pragma unroll
-            for (int w = 0; w < NW; ++w)
-                if (w < warp) xin = fma(sCf[warp][w], wXf[w], xin);
-            const double carry = fma(PeF, xin, Xe);
+            for (int w = 0; w < NWS; w += 2) {
+                if (w < warp) x0 = fma(sCf[warp][w], wXf[w], x0);
+                if (w + 1 < warp) x1 = fma(sCf[warp][w + 1], wXf[w + 1], x1);
+            }
+            const double carry = fma(PeF, x0 + x1, Xe);
 #pragma unroll
             for (int k = 0; k < SP; ++k)
                 if (k < cnt) y[k] = fma(kcf[k], carry, y[k]);
         }
+        if (cnt > 0 && i1 == b) agg[2 * c] = y[cnt - 1];   // the chunk's last y (zero carry-in)
         // ---- backward: segment sweep from zero carry, warp scan, warp totals
         double ub[SP];
         double ul = 0.0;
@@ -575,57 +609,24 @@ __global__ void __launch_bounds__(LT, 1) k_line_block(LineBlockArgs p)
         Xe = __shfl_down_sync(FULL, X, 1);
         if (lane == 31) Xe = 0.0;
         if (lane == 0) wXb[warp] = X;
-        __syncthreads();                                                      // (B)
+        solver_sync();                                                      // (B)
         {
-            double xin = 0.0;
+            double x0 = 0.0, x1 = 0.0;
 #pragma unroll
-            for (int w = 0; w < NW; ++w)
-                if (w > warp) xin = fma(sCb[warp][w], wXb[w], xin);
-            const double carry = fma(PeB, xin, Xe);
+            for (int w = 0; w < NWS; w += 2) {
+                if (w > warp) x0 = fma(sCb[warp][w], wXb[w], x0);
+                if (w + 1 > warp) x1 = fma(sCb[warp][w + 1], wXb[w + 1], x1);
+            }
+            const double carry = fma(PeB, x0 + x1, Xe);
 #pragma unroll
             for (int k = 0; k < SP; ++k)
                 if (k < cnt) ub[k] = fma(kcb[k], carry, ub[k]);
         }
-        // ---- thread 0 publishes the chunk's last y and first u (zero carries)
+        // The chunk's first u, then the release: barrier (B) orders the last-y write of the other
+        // thread before this release, which is cumulative at gpu scope.
         if (tid == 0) {
-            double ylast = 0.0, u0 = 0.0;
-#pragma unroll
-            for (int w = 0; w < NW; ++w) {
-                ylast = fma(sY[w], wXf[w], ylast);
-                u0 = fma(sU0[w], wXb[w], u0);
-            }
-            agg[2 * c] = ylast;
-            agg[2 * c + 1] = u0;
-            if (G > 1) {
-                __threadfence();
-                asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p.cflag + c), "l"(tag) : "memory");
-            }
-        }
-        // ---- while the chunks publish: the next step's history except its newest row
-        double Sn[SP];
-#pragma unroll
-        for (int k = 0; k < SP; ++k) Sn[k] = 0.0;
-        if (s + 1 < p.nsteps) {
-            const int jn = j + 1;
-#pragma unroll
-            for (int k = 0; k < SP; ++k) {
-                if (k < cnt) {
-                    const int64_t i = i0 + k;
-                    double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
-                    for (int q = 0; q < p.KS; ++q) s0 += __ldcg(p.cfar + ((int64_t)q * BLK + jn) * p.P + i);
-                    const double *rr = p.ring + i * 64;
-                    int r = 0;
-                    for (; r + 4 <= j; r += 4) {
-                        const double2 v0 = *(const double2 *)(rr + r), v1 = *(const double2 *)(rr + r + 2);
-                        s1 = fma(__ldg(p.wlag + (jn - r)), v0.x, s1);
-                        s2 = fma(__ldg(p.wlag + (jn - r - 1)), v0.y, s2);
-                        s3 = fma(__ldg(p.wlag + (jn - r - 2)), v1.x, s3);
-                        s1 = fma(__ldg(p.wlag + (jn - r - 3)), v1.y, s1);
-                    }
-                    for (; r < j; ++r) s2 = fma(__ldg(p.wlag + (jn - r)), rr[r], s2);
-                    Sn[k] = s0 + ((s1 + s2) + s3);
-                }
-            }
+            agg[2 * c + 1] = ub[0];
+            if (G > 1) asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p.cflag + c), "l"(tag) : "memory");
         }
         // ---- warp 0: every chunk's aggregates (one polling round for all flags), carries
         if (warp == 0) {
@@ -675,58 +676,56 @@ __global__ void __launch_bounds__(LT, 1) k_line_block(LineBlockArgs p)
                 if (lane == 0) { s_cin = sc; s_ub = fma(mbc, uN, sub); s_UN = uN; }
             }
         }
-        __syncthreads();                                                      // (D)
+        solver_sync();                                                      // (D)
+        if (!s_abort) {
+            const double cin = s_cin, ubv = s_ub;
+            // ---- new state and its increment (into the ring; the solver keeps it for the next step)
+#pragma unroll
+            for (int k = 0; k < SP; ++k) {
+                if (k < cnt) {
+                    const int64_t i = i0 + k;
+                    const double un = fma(kCB[k], ubv, fma(kGG[k], cin, ub[k]));
+                    const double d = un - u[k];
+                    p.ring[(int64_t)j * p.P + i] = d;
+                    u[k] = un;
+                    dprev[k] = d;
+                }
+            }
+            if (ownsN) {
+                const double UN = s_UN;
+                p.ring[(int64_t)j * p.P + N] = UN - uNv;
+                uNv = UN;
+            }
+            if (expl) {                                  // edge states for the next step
+                s_first[tid] = cnt > 0 ? u[0] : 0.0;
+                double last = 0.0;
+#pragma unroll
+                for (int k = 0; k < SP; ++k)
+                    if (k < cnt) last = u[k];
+                s_last[tid] = last;
+                double *halo = p.halo + (size_t)(tag & 1ull) * (2 * G + 2);
+                if (cnt > 0 && i0 == a) halo[2 * c] = u[0];
+                if (cnt > 0 && i1 == b) halo[2 * c + 1] = last;
+                solver_sync();
+                if (tid == 0 && G > 1)
+                    asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p.hflag + c), "l"(tag) : "memory");
+                if (s + 1 < p.nsteps && G > 1) {         // neighbours' edge states of this step
+                    const unsigned long long t0 = gtimer_ns();
+                    bool ok = true;
+                    if (tid == 0 && c > 0) {
+                        ok = wait_flag(p.hflag + c - 1, tag, t0);
+                        if (ok) hl = __ldcg(halo + 2 * (c - 1) + 1);
+                    }
+                    if (cnt > 0 && i1 == b && b < N) {
+                        ok = wait_flag(p.hflag + c + 1, tag, t0);
+                        if (ok) hr = __ldcg(halo + 2 * (c + 1));
+                    }
+                    if (!ok) { atomicOr(p.flags, DEVERR_BARRIER_TIMEOUT); s_abort = 1; }
+                }
+            }
+        }
+        __syncthreads();                                                    // end of step s
         if (s_abort) return;
-        const double cin = s_cin, ubv = s_ub;
-        // ---- new state, increment into the ring, the newest history row of the next step
-        const double w1 = __ldg(p.wlag + 1);
-#pragma unroll
-        for (int k = 0; k < SP; ++k) {
-            if (k < cnt) {
-                const int64_t i = i0 + k;
-                const double un = fma(kCB[k], ubv, fma(kGG[k], cin, ub[k]));
-                const double d = un - u[k];
-                p.ring[i * 64 + j] = d;
-                u[k] = un;
-                S[k] = fma(w1, d, Sn[k]);
-            }
-        }
-        if (ownsN) {
-            const double UN = s_UN;
-            p.ring[(int64_t)N * 64 + j] = UN - uNv;
-            uNv = UN;
-        }
-        if (expl) {                                      // edge states for the next step
-            s_first[tid] = cnt > 0 ? u[0] : 0.0;
-            double last = 0.0;
-#pragma unroll
-            for (int k = 0; k < SP; ++k)
-                if (k < cnt) last = u[k];
-            s_last[tid] = last;
-            double *halo = p.halo + (size_t)(tag & 1ull) * (2 * G + 2);
-            if (cnt > 0 && i0 == a) halo[2 * c] = u[0];
-            if (cnt > 0 && i1 == b) halo[2 * c + 1] = last;
-            __syncthreads();
-            if (tid == 0 && G > 1) {
-                __threadfence();
-                asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p.hflag + c), "l"(tag) : "memory");
-            }
-            if (s + 1 < p.nsteps && G > 1) {             // neighbours' edge states of this step
-                const unsigned long long t0 = gtimer_ns();
-                bool ok = true;
-                if (tid == 0 && c > 0) {
-                    ok = wait_flag(p.hflag + c - 1, tag, t0);
-                    if (ok) hl = __ldcg(halo + 2 * (c - 1) + 1);
-                }
-                if (cnt > 0 && i1 == b && b < N) {
-                    ok = wait_flag(p.hflag + c + 1, tag, t0);
-                    if (ok) hr = __ldcg(halo + 2 * (c + 1));
-                }
-                if (!ok) { atomicOr(p.flags, DEVERR_BARRIER_TIMEOUT); s_abort = 1; }
-            }
-            __syncthreads();
-            if (s_abort) return;
-        }
     }
 #pragma unroll
     for (int k = 0; k < SP; ++k)
@@ -791,7 +790,7 @@ static cudaError_t launch_solve_sp(const cudaLaunchConfig_t &cfg, const LineSolv
 }
 
 static int line_launch_solve(fpde_line *L, cudaStream_t st, int64_t n, const double *part, int KS, int64_t pstride,
-                             const double *ring, const double *wn, int nr, double *Drow, int64_t dstride)
+                             double *Drow, int64_t dstride)
 {
     LineSolveArgs a;
     a.A = L->A; a.g = L->g; a.al = L->al; a.cf = L->cf; a.cb = L->cb;
@@ -799,11 +798,11 @@ static int line_launch_solve(fpde_line *L, cudaStream_t st, int64_t n, const dou
     a.lamv = L->lamv; a.eA = L->eA; a.eB = L->eB;
     a.CF = L->CF; a.CB = L->CB; a.GG = L->GG;
     a.Lf = L->Lf; a.Mb = L->Mb; a.Kb = L->Kb; a.mb = L->mb; a.cflag = L->cflag; a.seq = L->seq;
-    a.U = L->U; a.Drow = Drow; a.dstride = dstride; a.part = part; a.pstride = pstride; a.ring = ring; a.wn = wn;
+    a.U = L->U; a.Drow = Drow; a.dstride = dstride; a.part = part; a.pstride = pstride;
     a.agg = L->agg;
     a.barrier = L->barrier; a.flags = L->ctx->d_flags;
     a.lam = L->lam; a.g0 = L->d.left_value; a.gN = L->d.right_value; a.dLN = L->d.dLN;
-    a.AlN = L->AlN; a.KS = KS; a.nr = nr; a.N = (int)L->N; a.G = L->G; a.rkind = L->d.right_kind;
+    a.AlN = L->AlN; a.KS = KS; a.N = (int)L->N; a.G = L->G; a.rkind = L->d.right_kind;
     a.chunk = L->chunk;
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(L->G);
@@ -856,7 +855,7 @@ static int line_launch_block(fpde_line *L, cudaStream_t st, int64_t nb0, int j0,
     a.chunk = L->chunk;
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(L->G);
-    cfg.blockDim = dim3(LT);
+    cfg.blockDim = dim3(2 * LTS);
     cfg.stream = st;
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeCooperative;
@@ -901,7 +900,7 @@ static int line_enqueue(fpde_line *L, cudaStream_t st, int64_t n0, int steps, in
             }
             ev = probe_step ? probe_begin(L, 2, n, 0.0, 0.0) : nullptr;
             PROBE_REC(ev, 0);
-            if ((rc = line_launch_solve(L, st, n, L->part, KS, L->P, nullptr, nullptr, 0, L->D + n * L->P, 1))) return rc;
+            if ((rc = line_launch_solve(L, st, n, L->part, KS, L->P, L->D + n * L->P, 1))) return rc;
             PROBE_REC(ev, 1);
             ++k;
         } else {
@@ -1034,29 +1033,33 @@ int fpde_line_create(fpde_ctx *ctx, const fpde_line_desc *desc, const double *A,
     FPDE_CHECK_ARG(d.precision == FPDE_PREC_FP64 || d.block == 0 || d.block == BLK,
                    "split path: block must be 0 (auto) or 64");
     const int64_t N = d.N;
-    // partition of nodes 0..N-1 into G chunks (CTAs) of LT threads x sp nodes (sp a power of
-    // two): one CTA when the line fits in 8 nodes per thread, otherwise the smallest sp that
+    // partition of nodes 0..N-1 into G chunks (CTAs) of lt threads x sp nodes (sp a power of
+    // two; lt = LT for the per-step FP64 solve, LTS solver threads for the persistent split
+    // path): one CTA when the line fits in 8 nodes per thread, otherwise the smallest sp that
     // keeps G within the SM count
+    const bool split = d.precision != FPDE_PREC_FP64;
+    const int lt = split ? LTS : LT;
     int sp = 1, G = 1;
-    if (N <= (int64_t)LT * LSEG) {
-        while ((int64_t)LT * sp < N) sp <<= 1;
+    if (N <= (int64_t)lt * LSEG) {
+        while ((int64_t)lt * sp < N) sp <<= 1;
     } else {
-        while (sp <= LSEG && (N + (int64_t)LT * sp - 1) / ((int64_t)LT * sp) > ctx->sm_count) sp <<= 1;
+        while (sp <= LSEG && (N + (int64_t)lt * sp - 1) / ((int64_t)lt * sp) > ctx->sm_count) sp <<= 1;
         if (sp > LSEG)
             return set_error(FPDE_ERR_UNSUPPORTED, "line of %lld intervals exceeds %lld (SMs x %d x %d)",
-                             (long long)N, (long long)ctx->sm_count * LT * LSEG, LT, LSEG);
-        G = (int)((N + (int64_t)LT * sp - 1) / ((int64_t)LT * sp));
+                             (long long)N, (long long)ctx->sm_count * lt * LSEG, lt, LSEG);
+        G = (int)((N + (int64_t)lt * sp - 1) / ((int64_t)lt * sp));
     }
-    // chunk of nodes per CTA: LT * sp, or (long lines) an even share of all SMs, rounded to sp
-    int64_t chunk = (int64_t)LT * sp;
-    if (G > 1 && N >= (int64_t)ctx->sm_count * LT) {
+    // chunk of nodes per CTA: lt * sp, or (long lines) an even share of all SMs, rounded to sp
+    int64_t chunk = (int64_t)lt * sp;
+    if (G > 1 && N >= (int64_t)ctx->sm_count * lt) {
         chunk = (N + ctx->sm_count - 1) / ctx->sm_count;
         chunk = (chunk + sp - 1) / sp * sp;
         G = (int)((N + chunk - 1) / chunk);
     }
     if (G > 160) return set_error(FPDE_ERR_UNSUPPORTED, "line solve: at most 160 chunks");
     int per_sm = 0;
-    FPDE_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_line_solve<LSEG>, LT, 0));
+    if (split) FPDE_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_line_block<LSEG>, 2 * LTS, 0));
+    else FPDE_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_line_solve<LSEG>, LT, 0));
     if (G > 1 && G > per_sm * ctx->sm_count)
         return set_error(FPDE_ERR_UNSUPPORTED, "line solve grid of %d CTAs cannot be co-resident", G);
 
@@ -1069,7 +1072,7 @@ int fpde_line_create(fpde_ctx *ctx, const fpde_line_desc *desc, const double *A,
     L->s = sp;
     L->chunk = (int)chunk;
     L->max_steps = d.max_steps;
-    L->split = d.precision != FPDE_PREC_FP64;
+    L->split = split;
     L->x3 = d.precision == FPDE_PREC_SPLIT_BF16X3;
     // local weight kkk0 = tau^{1-alpha}/(1-alpha); lam as in Om1 (:4191), lamR as in R (:3120);
     // or the caller's lag weights (distributed order: w[0] = b0/tau of eq_init, fr_do.cpp:688-694)
@@ -1140,58 +1143,56 @@ int fpde_line_create(fpde_ctx *ctx, const fpde_line_desc *desc, const double *A,
     // scan coefficients of the persistent split-path kernel (all products are time-invariant):
     // per thread the products of its segment (forward P, backward Q); per lane the products
     // the five warp-scan levels multiply with and the exclusive prefix/suffix products; per
-    // CTA the cross-warp coefficients and the rows that give the chunk aggregates.
-    constexpr int NWc = LT / 32;
-    const int64_t GT = (int64_t)G * LT;
-    std::vector<double> hsl((size_t)12 * GT, 1.0), hsw((size_t)G * (2 * NWc * NWc + 2 * NWc), 0.0);
-    for (int cc = 0; cc < G; ++cc) {
-        double Pt[LT], Qt[LT];
-        const int64_t a0 = (int64_t)cc * chunk, b0 = std::min<int64_t>(a0 + chunk, N);
-        for (int t = 0; t < LT; ++t) {
-            const int64_t i0 = a0 + (int64_t)t * sp, i1 = std::min<int64_t>(i0 + sp, b0);
-            Pt[t] = i1 > i0 ? hcf[i1 - 1] : 1.0;
-            Qt[t] = i1 > i0 ? hcb[i0] : 1.0;
-        }
-        double PW[NWc], QW[NWc];
-        for (int w = 0; w < NWc; ++w) {
-            const double *pw = Pt + 32 * w, *qw = Qt + 32 * w;
-            for (int l = 0; l < 32; ++l) {
-                const int64_t T = (int64_t)cc * LT + 32 * w + l;
-                for (int k = 0; k < 5; ++k) {
-                    double pf = 1.0, pb = 1.0;
-                    for (int m = std::max(0, l - (1 << k) + 1); m <= l; ++m) pf *= pw[m];
-                    for (int m = l; m <= std::min(31, l + (1 << k) - 1); ++m) pb *= qw[m];
-                    hsl[(size_t)k * GT + T] = pf;
-                    hsl[(size_t)(6 + k) * GT + T] = pb;
+    // CTA the cross-warp coefficients of the solver warps.
+    const int64_t GT = (int64_t)G * LTS;
+    std::vector<double> hsl, hsw;
+    if (split) {
+        hsl.assign((size_t)12 * GT, 1.0);
+        hsw.assign((size_t)G * 2 * NWS * NWS, 0.0);
+        for (int cc = 0; cc < G; ++cc) {
+            double Pt[LTS], Qt[LTS];
+            const int64_t a0 = (int64_t)cc * chunk, b0 = std::min<int64_t>(a0 + chunk, N);
+            for (int t = 0; t < LTS; ++t) {
+                const int64_t i0 = std::min<int64_t>(a0 + (int64_t)t * sp, b0), i1 = std::min<int64_t>(i0 + sp, b0);
+                Pt[t] = i1 > i0 ? hcf[i1 - 1] : 1.0;
+                Qt[t] = i1 > i0 ? hcb[i0] : 1.0;
+            }
+            double PW[NWS], QW[NWS];
+            for (int w = 0; w < NWS; ++w) {
+                const double *pw = Pt + 32 * w, *qw = Qt + 32 * w;
+                for (int l = 0; l < 32; ++l) {
+                    const int64_t T = (int64_t)cc * LTS + 32 * w + l;
+                    for (int k = 0; k < 5; ++k) {
+                        double pf = 1.0, pb = 1.0;
+                        for (int m = std::max(0, l - (1 << k) + 1); m <= l; ++m) pf *= pw[m];
+                        for (int m = l; m <= std::min(31, l + (1 << k) - 1); ++m) pb *= qw[m];
+                        hsl[(size_t)k * GT + T] = pf;
+                        hsl[(size_t)(6 + k) * GT + T] = pb;
+                    }
+                    double pe = 1.0, qe = 1.0;
+                    for (int m = 0; m < l; ++m) pe *= pw[m];
+                    for (int m = l + 1; m < 32; ++m) qe *= qw[m];
+                    hsl[(size_t)5 * GT + T] = pe;
+                    hsl[(size_t)11 * GT + T] = qe;
                 }
-                double pe = 1.0, qe = 1.0;
-                for (int m = 0; m < l; ++m) pe *= pw[m];
-                for (int m = l + 1; m < 32; ++m) qe *= qw[m];
-                hsl[(size_t)5 * GT + T] = pe;
-                hsl[(size_t)11 * GT + T] = qe;
+                double pt = 1.0, qt = 1.0;
+                for (int l = 0; l < 32; ++l) { pt *= pw[l]; qt *= qw[l]; }
+                PW[w] = pt;
+                QW[w] = qt;
             }
-            double pt = 1.0, qt = 1.0;
-            for (int l = 0; l < 32; ++l) { pt *= pw[l]; qt *= qw[l]; }
-            PW[w] = pt;
-            QW[w] = qt;
-        }
-        double *wc = hsw.data() + (size_t)cc * (2 * NWc * NWc + 2 * NWc);
-        for (int w = 0; w < NWc; ++w) {
-            for (int v = 0; v < w; ++v) {                 // Cf[w][v] = prod_{v < x < w} PW[x]
-                double pr = 1.0;
-                for (int x = v + 1; x < w; ++x) pr *= PW[x];
-                wc[w * NWc + v] = pr;
+            double *wc = hsw.data() + (size_t)cc * 2 * NWS * NWS;
+            for (int w = 0; w < NWS; ++w) {
+                for (int v = 0; v < w; ++v) {             // Cf[w][v] = prod_{v < x < w} PW[x]
+                    double pr = 1.0;
+                    for (int x = v + 1; x < w; ++x) pr *= PW[x];
+                    wc[w * NWS + v] = pr;
+                }
+                for (int v = w + 1; v < NWS; ++v) {       // Cb[w][v] = prod_{w < x < v} QW[x]
+                    double pr = 1.0;
+                    for (int x = w + 1; x < v; ++x) pr *= QW[x];
+                    wc[NWS * NWS + w * NWS + v] = pr;
+                }
             }
-            for (int v = w + 1; v < NWc; ++v) {           // Cb[w][v] = prod_{w < x < v} QW[x]
-                double pr = 1.0;
-                for (int x = w + 1; x < v; ++x) pr *= QW[x];
-                wc[NWc * NWc + w * NWc + v] = pr;
-            }
-            double py = 1.0, pu = 1.0;                    // Yrow[w], U0row[w]
-            for (int x = w + 1; x < NWc; ++x) py *= PW[x];
-            for (int x = 0; x < w; ++x) pu *= QW[x];
-            wc[2 * NWc * NWc + w] = py;
-            wc[2 * NWc * NWc + NWc + w] = pu;
         }
     }
     // lag weights w[j] = Da * kb(lag j) / tau with kb(lag j) = kkk0 * b_j; wrev[m] = w[L - m]
@@ -1216,8 +1217,8 @@ int fpde_line_create(fpde_ctx *ctx, const fpde_line_desc *desc, const double *A,
                 dev_alloc((void **)&L->agg, 2 * (2 * G + 2) * sizeof(double)) ||
                 dev_alloc((void **)&L->halo, 2 * (2 * G + 2) * sizeof(double)) ||
                 dev_alloc((void **)&L->hflag, (size_t)G * sizeof(unsigned long long)) ||
-                dev_alloc((void **)&L->sclane, hsl.size() * sizeof(double)) ||
-                dev_alloc((void **)&L->scwarp, hsw.size() * sizeof(double)) ||
+                (split && (dev_alloc((void **)&L->sclane, hsl.size() * sizeof(double)) ||
+                           dev_alloc((void **)&L->scwarp, hsw.size() * sizeof(double)))) ||
                 dev_alloc((void **)&L->barrier, 2 * sizeof(unsigned));
     if (!fail && !L->split) {
         fail = dev_alloc((void **)&L->D, (size_t)L->max_steps * L->P * sizeof(double)) ||
@@ -1310,8 +1311,10 @@ int fpde_line_create(fpde_ctx *ctx, const fpde_line_desc *desc, const double *A,
     cudaMemcpyAsync(L->mb, hmb.data(), gb, cudaMemcpyHostToDevice, st);
     cudaMemsetAsync(L->cflag, 0, (size_t)G * sizeof(unsigned long long), st);
     cudaMemsetAsync(L->hflag, 0, (size_t)G * sizeof(unsigned long long), st);
-    cudaMemcpyAsync(L->sclane, hsl.data(), hsl.size() * sizeof(double), cudaMemcpyHostToDevice, st);
-    cudaMemcpyAsync(L->scwarp, hsw.data(), hsw.size() * sizeof(double), cudaMemcpyHostToDevice, st);
+    if (split) {
+        cudaMemcpyAsync(L->sclane, hsl.data(), hsl.size() * sizeof(double), cudaMemcpyHostToDevice, st);
+        cudaMemcpyAsync(L->scwarp, hsw.data(), hsw.size() * sizeof(double), cudaMemcpyHostToDevice, st);
+    }
     cudaMemsetAsync(L->seq, 0, sizeof(unsigned long long), st);
     cudaMemcpyAsync(L->wrev, wrev.data(), wrev.size() * sizeof(double), cudaMemcpyHostToDevice, st);
     cudaMemsetAsync(L->U, 0, L->P * sizeof(double), st);

@@ -1,6 +1,6 @@
 // Block preparation of the split-precision path (per block of 64 steps):
 //   k_absmax  : largest |increment| of the finished block (for the fp16 scale)
-//   k_convert : FP64 increments (node-major ring, 64 per node) -> 16-bit hi/lo pairs in the
+//   k_convert : FP64 increments (time-major ring, 64 rows of P) -> 16-bit hi/lo pairs in the
 //               node-major history used as the K-major A operand, scaled by 2^sexp
 //   k_wgen    : Toeplitz weight tile W[j][t] = w[n0+j-t] * 2^(kexp - sexp(t)), split hi/lo,
 //               and the output scale 2^-kexp of the contraction
@@ -71,7 +71,7 @@ __global__ void __launch_bounds__(256) k_convert(const double *__restrict__ ring
     for (int e = threadIdx.x; e < 64 * 64; e += 256) {
         const int r = e >> 6, c = e & 63;
         const int64_t node = node0 + c;
-        tile[c][r] = node < nvalid ? ring[node * 64 + r] * sc : 0.0;
+        tile[c][r] = node < nvalid ? ring[(int64_t)r * P + node] * sc : 0.0;
     }
     __syncthreads();
     for (int e = threadIdx.x; e < 64 * 8; e += 256) {
@@ -171,7 +171,8 @@ __device__ __forceinline__ int exp_of_maxbits(unsigned long long mbits)
     return p < -127 ? -127 : (p > 127 ? 127 : p);
 }
 
-// One thread per node: the node's 64 increments of the finished block (node-major ring).
+// One thread per node: the node's 64 increments of the finished block (time-major ring: the
+// threads of a warp read consecutive nodes of one row).
 __global__ void __launch_bounds__(128) k_convert3(const double *__restrict__ ring, int64_t P, int64_t nvalid,
                                                   uint16_t *__restrict__ h0, uint16_t *__restrict__ h1,
                                                   uint16_t *__restrict__ h2, int64_t ld, int64_t col0,
@@ -179,24 +180,21 @@ __global__ void __launch_bounds__(128) k_convert3(const double *__restrict__ rin
 {
     const int64_t node = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (node >= nvalid) return;
-    const ulonglong2 *src = (const ulonglong2 *)(ring + node * 64);
+    const unsigned long long *src = (const unsigned long long *)ring + node;
     unsigned long long mb = 0;
-#pragma unroll 8
-    for (int r = 0; r < 32; ++r) {
-        const ulonglong2 v = __ldg(src + r);
-        const unsigned long long m0 = v.x & 0x7FFFFFFFFFFFFFFFull, m1 = v.y & 0x7FFFFFFFFFFFFFFFull;
+#pragma unroll 16
+    for (int r = 0; r < 64; ++r) {
+        const unsigned long long m0 = __ldg(src + (int64_t)r * P) & 0x7FFFFFFFFFFFFFFFull;
         mb = m0 > mb ? m0 : mb;
-        mb = m1 > mb ? m1 : mb;
     }
     const int pe = exp_of_maxbits(mb);
     pA[node * ldp + blk] = (int8_t)pe;
     for (int g = 0; g < 8; ++g) {
         uint16_t a[8], b[8], c[8];
 #pragma unroll
-        for (int k = 0; k < 8; k += 2) {
-            const ulonglong2 v = __ldg(src + 4 * g + k / 2);
-            digits3(fixed16(__longlong_as_double((long long)v.x), pe), a[k], b[k], c[k]);
-            digits3(fixed16(__longlong_as_double((long long)v.y), pe), a[k + 1], b[k + 1], c[k + 1]);
+        for (int k = 0; k < 8; ++k) {
+            const unsigned long long v = __ldg(src + (int64_t)(8 * g + k) * P);
+            digits3(fixed16(__longlong_as_double((long long)v), pe), a[k], b[k], c[k]);
         }
         uint4 va, vb, vc;
         va.x = a[0] | ((uint32_t)a[1] << 16); va.y = a[2] | ((uint32_t)a[3] << 16);
