@@ -351,6 +351,7 @@ struct LineBlockArgs {
     double *ring;                         // [64][P] time-major increments of the block
     const double *cfar;                   // far partials [KS][64][P]
     int KS;
+    int far_pairs;                        // 1: partials are float pairs (three-slice contraction)
     int64_t P;
     const double *wlag;                   // w[lag]
     double *agg;                          // [2][2G+2] aggregates by step parity
@@ -394,10 +395,13 @@ __device__ __forceinline__ void history_sum(const LineBlockArgs &p, int ht, int 
         acc[q] = 0.0;
         far[q] = 0.0;
     }
-    for (int k = 0; k < p.KS; ++k) {
+    for (int k = 0; k < p.KS; ++k) {                     // far partials: float pairs, exact in FP64
 #pragma unroll
         for (int q = 0; q < SP; ++q)
-            if (node[q] < b) far[q] += __ldcg(p.cfar + ((int64_t)k * BLK + j) * p.P + node[q]);
+            if (node[q] < b) {
+                const double v = __ldcg(p.cfar + ((int64_t)k * BLK + j) * p.P + node[q]);
+                far[q] += p.far_pairs ? ff_to_double(v) : v;
+            }
     }
     int r = 0;
     for (; r + 8 <= rmax; r += 8) {                      // eight rows of loads in flight
@@ -847,6 +851,7 @@ static int line_launch_block(fpde_line *L, cudaStream_t st, int64_t nb0, int j0,
     a.lamv = L->lamv; a.eA = L->eA; a.eB = L->eB;
     a.src = L->srcd; a.src_rows = L->src_rows;
     a.U = L->U; a.ring = L->ring; a.cfar = L->cfar; a.KS = KS; a.P = L->P; a.wlag = L->wlag;
+    a.far_pairs = L->x3 ? 1 : 0;
     a.agg = L->agg; a.halo = L->halo; a.cflag = L->cflag; a.hflag = L->hflag; a.seq = L->seq;
     a.Lf = L->Lf; a.Mb = L->Mb; a.Kb = L->Kb; a.mb = L->mb; a.flags = L->ctx->d_flags;
     a.sc.lane = L->sclane; a.sc.warp = L->scwarp;

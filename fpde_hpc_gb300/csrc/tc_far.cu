@@ -18,6 +18,7 @@
 // warps 2-5 epilogue (TMEM lane quadrant = warp % 4).
 // Every wait is bounded (2 s of %globaltimer); on timeout the kernel raises
 // DEVERR_MBAR_TIMEOUT, stops issuing, drains its own copies (bounded) and frees its TMEM.
+#include <algorithm>
 #include <cuda.h>
 #include <cuda_runtime.h>
 
@@ -318,9 +319,20 @@ struct __align__(64) FarMaps3 {
     CUtensorMap a[3], w[3];
 };
 
+// 2^e as a float for e in [-127, 127], from the bits (exact; e = -127 is the subnormal 2^-127).
+__device__ __forceinline__ float pow2f(int e)
+{
+    return e >= -126 ? __int_as_float((e + 127) << 23) : __int_as_float(0x00400000);
+}
+
+// Persistent: gridDim.x CTAs (at most one per SM) walk the items (128-row tile mt, k-split
+// ks) = blockIdx.x, blockIdx.x + gridDim.x, ...; the TMA producer, the MMA issuer and the
+// epilogue follow the same static sequence of k-tiles, so the pipeline runs on across item
+// boundaries and TMEM is allocated once. Every item writes its partial (zeros if its k range
+// is empty).
 __global__ void __launch_bounds__(THREADS, 1)
     k_far_tc3(const __grid_constant__ FarMaps3 maps, double *__restrict__ C, int64_t ldc_split, int64_t ldc_col,
-              int64_t rows, int kt_total, int kt_per, uint32_t idesc, const int8_t *__restrict__ pA,
+              int64_t rows, int kt_total, int kt_per, int n_split, uint32_t idesc, const int8_t *__restrict__ pA,
               const int8_t *__restrict__ pW, int64_t ldp, unsigned *flags)
 {
     extern __shared__ uint8_t smem_raw[];
@@ -333,10 +345,8 @@ __global__ void __launch_bounds__(THREADS, 1)
     volatile int *abort_s = (volatile int *)(bars + 2 * STAGES3 + 6);
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int mt = blockIdx.x, split = blockIdx.y;
-    const int kt0 = split * kt_per;
-    const int kt1 = min(kt0 + kt_per, kt_total);
-    const int nkt = max(0, kt1 - kt0);
+    const int n_mt = (int)(rows / BM);
+    const int n_items = n_mt * n_split;
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < STAGES3; ++s) { mbar_init(&full[s], 1); mbar_init(&empty[s], 1); }
@@ -358,21 +368,25 @@ __global__ void __launch_bounds__(THREADS, 1)
 
     if (warp == 0) {
         if (lane == 0) {                                   // TMA producer
-            int issued = 0;
-            for (int it = 0; it < nkt; ++it) {
-                const int s = it % STAGES3;
-                const uint32_t ph = (uint32_t)(it / STAGES3) & 1u;
-                if (!mbar_wait(&empty[s], ph ^ 1u, flags, abort_s)) break;
-                uint8_t *st = stage_base + s * STAGE3_BYTES;
-                mbar_expect_tx(&full[s], STAGE3_BYTES);
-                const int x = (kt0 + it) * BK, y = mt * BM;
+            int g = 0;
+            bool ok = true;
+            for (int item = blockIdx.x; item < n_items && ok; item += gridDim.x) {
+                const int mt = item / n_split, ks = item % n_split;
+                const int kt0 = ks * kt_per, kt1 = min(kt0 + kt_per, kt_total);
+                for (int kt = kt0; kt < kt1; ++kt, ++g) {
+                    const int s = g % STAGES3;
+                    const uint32_t ph = (uint32_t)(g / STAGES3) & 1u;
+                    if (!mbar_wait(&empty[s], ph ^ 1u, flags, abort_s)) { ok = false; break; }
+                    uint8_t *st = stage_base + s * STAGE3_BYTES;
+                    mbar_expect_tx(&full[s], STAGE3_BYTES);
+                    const int x = kt * BK, y = mt * BM;
 #pragma unroll
-                for (int q = 0; q < 3; ++q) tma_load_2d(st + q * A_BYTES, &maps.a[q], x, y, &full[s]);
+                    for (int q = 0; q < 3; ++q) tma_load_2d(st + q * A_BYTES, &maps.a[q], x, y, &full[s]);
 #pragma unroll
-                for (int q = 0; q < 3; ++q) tma_load_2d(st + 3 * A_BYTES + q * W_BYTES, &maps.w[q], x, 0, &full[s]);
-                ++issued;
+                    for (int q = 0; q < 3; ++q) tma_load_2d(st + 3 * A_BYTES + q * W_BYTES, &maps.w[q], x, 0, &full[s]);
+                }
             }
-            for (int it = (issued > STAGES3 ? issued - STAGES3 : 0); it < issued; ++it) {
+            for (int it = (g > STAGES3 ? g - STAGES3 : 0); it < g; ++it) {   // own copies in flight
                 const int s = it % STAGES3;
                 const uint32_t ph = (uint32_t)(it / STAGES3) & 1u;
                 unsigned long long t0 = gtimer();
@@ -381,32 +395,38 @@ __global__ void __launch_bounds__(THREADS, 1)
         }
     } else if (warp == 1) {
         if (lane == 0) {                                   // MMA issuer: one k-tile per chunk
-            for (int it = 0; it < nkt && !*abort_s; ++it) {
-                const int buf = it & 1;
-                const uint32_t use = (uint32_t)(it >> 1);
-                if (!mbar_wait(&tempty[buf], (use & 1u) ^ 1u, flags, abort_s)) break;
-                tc_fence_after();
-                const int s = it % STAGES3;
-                const uint32_t ph = (uint32_t)(it / STAGES3) & 1u;
-                if (!mbar_wait(&full[s], ph, flags, abort_s)) break;
-                tc_fence_after();
-                const uint32_t x0 = tmem + (uint32_t)(buf * 2 * BN), x12 = x0 + BN;
-                const uint32_t st = smem_u32(stage_base + s * STAGE3_BYTES);
-                const uint32_t a0 = st, a1 = st + A_BYTES, a2 = st + 2 * A_BYTES;
-                const uint32_t w0 = st + 3 * A_BYTES, w1 = w0 + W_BYTES, w2 = w0 + 2 * W_BYTES;
+            int g = 0;
+            bool ok = true;
+            for (int item = blockIdx.x; item < n_items && ok; item += gridDim.x) {
+                const int ks = item % n_split;
+                const int kt0 = ks * kt_per, kt1 = min(kt0 + kt_per, kt_total);
+                for (int kt = kt0; kt < kt1 && !*abort_s; ++kt, ++g) {
+                    const int buf = g & 1;
+                    const uint32_t use = (uint32_t)(g >> 1);
+                    if (!mbar_wait(&tempty[buf], (use & 1u) ^ 1u, flags, abort_s)) { ok = false; break; }
+                    tc_fence_after();
+                    const int s = g % STAGES3;
+                    const uint32_t ph = (uint32_t)(g / STAGES3) & 1u;
+                    if (!mbar_wait(&full[s], ph, flags, abort_s)) { ok = false; break; }
+                    tc_fence_after();
+                    const uint32_t x0 = tmem + (uint32_t)(buf * 2 * BN), x12 = x0 + BN;
+                    const uint32_t st = smem_u32(stage_base + s * STAGE3_BYTES);
+                    const uint32_t a0 = st, a1 = st + A_BYTES, a2 = st + 2 * A_BYTES;
+                    const uint32_t w0 = st + 3 * A_BYTES, w1 = w0 + W_BYTES, w2 = w0 + 2 * W_BYTES;
 #pragma unroll
-                for (int k = 0; k < BK / 16; ++k) {
-                    const uint32_t off = (uint32_t)(k * 32);
-                    const uint32_t acc = k ? 1u : 0u;
-                    umma(x0, sdesc_sw128(a0 + off), sdesc_sw128(w0 + off), idesc, acc);
-                    umma(x12, sdesc_sw128(a0 + off), sdesc_sw128(w1 + off), idesc, acc);
-                    umma(x12, sdesc_sw128(a1 + off), sdesc_sw128(w0 + off), idesc, 1u);
-                    umma(x12, sdesc_sw128(a0 + off), sdesc_sw128(w2 + off), idesc, 1u);
-                    umma(x12, sdesc_sw128(a1 + off), sdesc_sw128(w1 + off), idesc, 1u);
-                    umma(x12, sdesc_sw128(a2 + off), sdesc_sw128(w0 + off), idesc, 1u);
+                    for (int k = 0; k < BK / 16; ++k) {
+                        const uint32_t off = (uint32_t)(k * 32);
+                        const uint32_t acc = k ? 1u : 0u;
+                        umma(x0, sdesc_sw128(a0 + off), sdesc_sw128(w0 + off), idesc, acc);
+                        umma(x12, sdesc_sw128(a0 + off), sdesc_sw128(w1 + off), idesc, acc);
+                        umma(x12, sdesc_sw128(a1 + off), sdesc_sw128(w0 + off), idesc, 1u);
+                        umma(x12, sdesc_sw128(a0 + off), sdesc_sw128(w2 + off), idesc, 1u);
+                        umma(x12, sdesc_sw128(a1 + off), sdesc_sw128(w1 + off), idesc, 1u);
+                        umma(x12, sdesc_sw128(a2 + off), sdesc_sw128(w0 + off), idesc, 1u);
+                    }
+                    umma_commit(&empty[s]);
+                    umma_commit(&tfull[buf]);
                 }
-                umma_commit(&empty[s]);
-                umma_commit(&tfull[buf]);
             }
             umma_commit(mma_done);
             const unsigned long long t0 = gtimer();
@@ -414,50 +434,55 @@ __global__ void __launch_bounds__(THREADS, 1)
         }
     } else {
         const int q = warp & 3;                            // TMEM lane quadrant
-        const int64_t row = (int64_t)mt * BM + q * 32 + lane;
-        const int64_t row_c = row < rows ? row : rows - 1;
-        float hi[BN], lo[BN];
-#pragma unroll
-        for (int j = 0; j < BN; ++j) { hi[j] = 0.f; lo[j] = 0.f; }
+        int g = 0;
         bool ok = true;
-        for (int it = 0; it < nkt; ++it) {
-            const int buf = it & 1;
-            const uint32_t use = (uint32_t)(it >> 1);
-            if (!mbar_wait(&tfull[buf], use & 1u, flags, abort_s)) { ok = false; break; }
-            tc_fence_after();
-            const int kt = kt0 + it;
-            const int ea = (int)pA[row_c * ldp + kt];
-            const uint32_t tb = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(buf * 2 * BN);
+        for (int item = blockIdx.x; item < n_items && ok; item += gridDim.x) {
+            const int mt = item / n_split, ks = item % n_split;
+            const int kt0 = ks * kt_per, kt1 = min(kt0 + kt_per, kt_total);
+            const int64_t row = (int64_t)mt * BM + q * 32 + lane;
+            const int64_t row_c = row < rows ? row : rows - 1;
+            float hi[BN], lo[BN];
 #pragma unroll
-            for (int h = 0; h < BN / 16; ++h) {
-                float v0[16], v1[16];
-                tmem_ld16(tb + 16 * h, v0);
-                tmem_ld16(tb + BN + 16 * h, v1);
-                tmem_ld_wait();
+            for (int j = 0; j < BN; ++j) { hi[j] = 0.f; lo[j] = 0.f; }
+            for (int kt = kt0; kt < kt1; ++kt, ++g) {
+                const int buf = g & 1;
+                const uint32_t use = (uint32_t)(g >> 1);
+                if (!mbar_wait(&tfull[buf], use & 1u, flags, abort_s)) { ok = false; break; }
+                tc_fence_after();
+                const float sa = pow2f((int)pA[row_c * ldp + kt]);
+                const uint32_t tb = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(buf * 2 * BN);
 #pragma unroll
-                for (int jj = 0; jj < 16; ++jj) {
-                    const int j = 16 * h + jj;
-                    const float sc = ldexpf(1.0f, ea + (int)__ldg(pW + (int64_t)j * ldp + kt));
-                    float x = v0[jj] * sc;                     // exact (power-of-two scaling)
-                    float s = hi[j] + x, bb = s - hi[j];
-                    float e = (hi[j] - (s - bb)) + (x - bb);
-                    hi[j] = s;
-                    lo[j] += e;
-                    x = v1[jj] * sc;
-                    s = hi[j] + x;
-                    bb = s - hi[j];
-                    e = (hi[j] - (s - bb)) + (x - bb);
-                    hi[j] = s;
-                    lo[j] += e;
+                for (int h = 0; h < BN / 16; ++h) {
+                    float v0[16], v1[16];
+                    tmem_ld16(tb + 16 * h, v0);
+                    tmem_ld16(tb + BN + 16 * h, v1);
+                    tmem_ld_wait();
+#pragma unroll
+                    for (int jj = 0; jj < 16; ++jj) {
+                        const int j = 16 * h + jj;
+                        // 2^pA * 2^pW: a product of powers of two, exact while it stays normal
+                        const float sc = sa * pow2f((int)__ldg(pW + (int64_t)j * ldp + kt));
+                        float x = v0[jj] * sc;                 // exact (power-of-two scaling)
+                        float s = hi[j] + x, bb = s - hi[j];
+                        float e = (hi[j] - (s - bb)) + (x - bb);
+                        hi[j] = s;
+                        lo[j] += e;
+                        x = v1[jj] * sc;
+                        s = hi[j] + x;
+                        bb = s - hi[j];
+                        e = (hi[j] - (s - bb)) + (x - bb);
+                        hi[j] = s;
+                        lo[j] += e;
+                    }
                 }
+                tc_fence_before();
+                mbar_arrive(&tempty[buf]);
             }
-            tc_fence_before();
-            mbar_arrive(&tempty[buf]);
-        }
-        if (ok && row < rows && nkt > 0) {
-            double *out = C + (int64_t)split * ldc_split + row;
+            if (ok && row < rows) {                   // float pairs: no FP64 work here
+                float2 *out = reinterpret_cast<float2 *>(C + (int64_t)ks * ldc_split + row);
 #pragma unroll
-            for (int j = 0; j < BN; ++j) out[(int64_t)j * ldc_col] = (double)hi[j] + (double)lo[j];
+                for (int j = 0; j < BN; ++j) out[(int64_t)j * ldc_col] = make_float2(hi[j], lo[j]);
+            }
         }
     }
     tc_fence_before();
@@ -562,22 +587,43 @@ int far3_launch(cudaStream_t st, const FarPlan3 *p, int k_cols, double *C, int64
     const int kt_total = k_cols / tc::BK;
     if (splits < 1) splits = 1;
     if (splits > FAR_MAX_SPLITS) splits = FAR_MAX_SPLITS;
-    const int kt_per = (kt_total + splits - 1) / splits;
-    splits = (kt_total + kt_per - 1) / kt_per;
-    dim3 grid((unsigned)(p->rows / tc::BM), (unsigned)splits);
+    const int kt_per = (kt_total + splits - 1) / splits;     // every split is written, possibly with zeros
+    const int64_t items = (p->rows / tc::BM) * splits;
+    int sms = 152;
+    {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    }
+    const unsigned grid = (unsigned)std::min<int64_t>(items, sms);
     const tc::FarMaps3 *m = (const tc::FarMaps3 *)p->maps;
     tc::k_far_tc3<<<grid, tc::THREADS, tc::SMEM3_BYTES, st>>>(*m, C, ldc_split, ldc_col, p->rows, kt_total, kt_per,
-                                                             p->idesc, pA, pW, ldp, flags);
+                                                             splits, p->idesc, pA, pW, ldp, flags);
     FPDE_LAUNCHED(1);
     return FPDE_OK;
 }
 
 int far_splits(int kt_total, int64_t rows)
 {
-    int64_t tiles = rows / tc::BM;
-    int s = 1;
-    while (s < FAR_MAX_SPLITS && tiles * s < 152 * 6 && kt_total / (s + 1) >= 8) ++s;
-    return s;
+    // Splits of K only for balance of the persistent grid (one CTA per SM): the fewest splits
+    // whose items fill the SMs within 5% (each split keeps at least 2 k-tiles).
+    int sms = 152;
+    {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    }
+    const int64_t tiles = rows / tc::BM;
+    int best = 1;
+    double best_waste = 1e30;
+    for (int s = 1; s <= FAR_MAX_SPLITS && (s == 1 || kt_total / s >= 2); ++s) {
+        const int64_t items = tiles * s;
+        const double waves = (double)items / sms, full = (double)((items + sms - 1) / sms);
+        const double waste = full / waves;
+        if (waste < best_waste - 1e-9) { best_waste = waste; best = s; }
+        if (waste <= 1.05) break;
+    }
+    return best;
 }
 
 int far_launch(cudaStream_t st, const FarPlan *p, int k_cols, double *C, int64_t ldc_split, int64_t ldc_col,
@@ -621,6 +667,15 @@ extern "C" int fpde_far_contract(fpde_ctx *ctx, const void *a_hi, const void *a_
     return ctx_check_flags(ctx, "far contraction");
 }
 
+namespace fpde {
+// In place: float-pair slots of a far contraction -> FP64 values.
+__global__ void k_ff_to_double(double *C, int64_t n)
+{
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) C[i] = ff_to_double(C[i]);
+}
+}  // namespace fpde
+
 extern "C" int fpde_far_contract3(fpde_ctx *ctx, const void *const a[3], int64_t rows, int64_t lda,
                                   const void *const w[3], int64_t ldw, int k_cols, const int8_t *pA,
                                   const int8_t *pW, int64_t ldp, double *C, int splits)
@@ -633,8 +688,14 @@ extern "C" int fpde_far_contract3(fpde_ctx *ctx, const void *const a[3], int64_t
     FarPlan3 plan;
     if ((rc = far_plan3_init(&plan, a, rows, lda, w, ldw))) return rc;
     if (splits <= 0) splits = far_splits(k_cols / 64, rows);
+    if (splits > FAR_MAX_SPLITS) splits = FAR_MAX_SPLITS;
     if ((rc = far3_launch(ctx->stream, &plan, k_cols, C, rows * 64, rows, splits, pA, pW, ldp, ctx->d_flags)))
         return rc;
+    const int64_t n = (int64_t)splits * 64 * rows;
+    if (k_cols > 0) {
+        k_ff_to_double<<<(unsigned)((n + 255) / 256), 256, 0, ctx->stream>>>(C, n);
+        FPDE_LAUNCHED(1);
+    }
     FPDE_CUDA(cudaStreamSynchronize(ctx->stream));
     return ctx_check_flags(ctx, "far contraction (three slices)");
 }

@@ -31,7 +31,37 @@ struct FarPlan3 {
 };
 int far_plan3_init(FarPlan3 *p, const void *const a[3], int64_t rows, int64_t lda, const void *const w[3],
                    int64_t ldw);
+// Writes each partial as a float pair (hi, lo) into the 8-byte slot of C (the fold's float-
+// float value; hi + lo is exact in FP64): read it with ff_to_double.
 int far3_launch(cudaStream_t st, const FarPlan3 *p, int k_cols, double *C, int64_t ldc_split, int64_t ldc_col,
                 int splits, const int8_t *pA, const int8_t *pW, int64_t ldp, unsigned *flags);
+
+// float -> double from the bits (integer instructions only; exact for every float).
+__device__ __forceinline__ double f2d_bits(float x)
+{
+    const uint32_t b = (uint32_t)__float_as_int(x);
+    const uint64_t sign = (uint64_t)(b >> 31) << 63;
+    const uint32_t e = (b >> 23) & 0xFFu, m = b & 0x7FFFFFu;
+    uint64_t r;
+    if (e == 0) {
+        if (m == 0) {
+            r = sign;
+        } else {                                        // subnormal: m * 2^-149
+            const int k = 31 - __clz((int)m);           // highest set bit, 0..22
+            r = sign | ((uint64_t)(k - 149 + 1023) << 52) | (((uint64_t)m << (52 - k)) & 0xFFFFFFFFFFFFFull);
+        }
+    } else if (e == 0xFFu) {
+        r = sign | (0x7FFull << 52) | ((uint64_t)m << 29);
+    } else {
+        r = sign | ((uint64_t)(e - 127 + 1023) << 52) | ((uint64_t)m << 29);
+    }
+    return __longlong_as_double((long long)r);
+}
+// A far-contraction slot (float pair) as one double: hi + lo, exact.
+__device__ __forceinline__ double ff_to_double(double slot)
+{
+    const float2 v = *reinterpret_cast<const float2 *>(&slot);
+    return f2d_bits(v.x) + f2d_bits(v.y);
+}
 
 }  // namespace fpde
