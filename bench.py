@@ -410,10 +410,13 @@ def run_ours(args):
     ctx.set_stream(stream.cuda_stream)
     lib = ctx.lib
     is_line = isinstance(wl, LineWorkload)
-    prec = {"auto": fp.FPDE_PREC_SPLIT_BF16X3 if is_line else fp.FPDE_PREC_FP64, "fp64": fp.FPDE_PREC_FP64,
+    splittable = is_line or isinstance(wl, LodWorkload)
+    prec = {"auto": fp.FPDE_PREC_SPLIT_BF16X3 if splittable else fp.FPDE_PREC_FP64, "fp64": fp.FPDE_PREC_FP64,
             "bf16": fp.FPDE_PREC_SPLIT_BF16, "f16": fp.FPDE_PREC_SPLIT_F16,
             "bf16x3": fp.FPDE_PREC_SPLIT_BF16X3}[args.precision]
-    if not is_line and prec != fp.FPDE_PREC_FP64:
+    if not is_line and prec not in (fp.FPDE_PREC_FP64, fp.FPDE_PREC_SPLIT_BF16X3):
+        raise SystemExit(f"{wl.name} runs in FP64 or the exact three-slice split")
+    if not splittable and prec != fp.FPDE_PREC_FP64:
         raise SystemExit(f"{wl.name} runs in FP64 only")
     pname = {0: "fp64", 1: "split-bf16", 2: "split-fp16", 3: "split-bf16x3"}[prec]
 
@@ -446,7 +449,7 @@ def run_ours(args):
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms = float(t.item())
     value = wl.node_steps * world / (ms / 1e3)
-    u_main = obj.state() if is_line else None
+    u_main = obj.state() if splittable else None
 
     # end to end through the C ABI with host buffers (pinned)
     u0_h = torch.from_numpy(np.ascontiguousarray(wl.u0).copy()).pin_memory()
@@ -503,30 +506,41 @@ def run_ours(args):
         out["roofline"] = dict(kernels[dom])
         out["kernels"] = kernels
     else:
-        # whole-step HBM roofline: algorithmic history bytes 8 x nodes x lags, summed over steps
+        # whole-step HBM roofline from the algorithmic history bytes of the run:
+        #   FP64: 8 B x nodes x lags, summed over steps;
+        #   split: 6 B (three bf16 slices) x nodes x far lags per 64-step block + 8 B x nodes x
+        #          near lags per step (the FP64 ring)
         nodes = wl.node_steps / steps
-        alg = 8.0 * nodes * steps * (steps - 1) / 2
+        if prec == 0:
+            alg = 8.0 * nodes * steps * (steps - 1) / 2
+            name = "whole step (FP64 history GEMV dominant)"
+        else:
+            nb = steps // 64
+            alg = 6.0 * nodes * 64 * 64 * nb * (nb - 1) / 2 + 8.0 * nodes * sum(n % 64 for n in range(steps))
+            name = "whole step (tensor-core far history + FP64 near history + passes)"
         gbs = alg / (ms / 1e3) / 1e9
-        out["roofline"] = {"kernel": "whole step (FP64 history GEMV dominant)", "bound": "hbm", "achieved": gbs,
+        out["roofline"] = {"kernel": name, "bound": "hbm", "achieved": gbs,
                            "peak": peak, "unit": "GB/s", "frac": gbs / peak, "peak_source": peak_src,
                            "traffic": None, "note": "algorithmic history bytes / whole solve time"}
 
-    if is_line and prec != 0 and not args.no_fp64_arm:
+    if splittable and prec != 0 and not args.no_fp64_arm:
         # the plain FP64 kernel on the same workload: speed-up and accuracy of the split path
         l64 = wl.build(ctx, fp.FPDE_PREC_FP64)
         l64.reset(u0_dev)
         l64.run(steps)
         ms64 = _timed(l64, u0_dev, steps, 1, stream)
         u64 = l64.state()
-        tot64 = _probe(l64, u0_dev, steps, max(1, steps // 32))
-        l64.close()
         err = float(np.max(np.abs(u_main - u64)) / np.max(np.abs(u64)))
         rms = float(np.sqrt(np.mean((u_main - u64) ** 2)) / np.sqrt(np.mean(u64 ** 2)))
-        out["fp64_kernel"] = {"value": wl.node_steps / (ms64 / 1e3), "ms_per_step": ms64,
-                              "roofline": _kernel_entry(tot64[0], "k_l1_partial (FP64 history GEMV)", peak,
-                                                        peak_src, steps / max(tot64[0]["count"], 1))}
-        if out["fp64_kernel"]["roofline"]:
-            out["fp64_kernel"]["roofline"]["fp64_fma_ceiling_gbs"] = 4800.0
+        out["fp64_kernel"] = {"value": wl.node_steps / (ms64 / 1e3), "ms_per_step": ms64}
+        if is_line:
+            tot64 = _probe(l64, u0_dev, steps, max(1, steps // 32))
+            r64 = _kernel_entry(tot64[0], "k_l1_partial (FP64 history GEMV)", peak, peak_src,
+                                steps / max(tot64[0]["count"], 1))
+            if r64:
+                r64["fp64_fma_ceiling_gbs"] = 4800.0
+            out["fp64_kernel"]["roofline"] = r64
+        l64.close()
         out["split_vs_fp64"] = {"speedup": ms64 / ms, "max_rel_err": err, "rms_rel_err": rms, "bound": 1e-7}
     obj.close()
     if rank == 0 and world == 1 and not args.no_cpu_baseline:

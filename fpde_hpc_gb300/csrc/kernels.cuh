@@ -52,4 +52,10 @@ struct SplitPrep3 {
 };
 int launch_block_prep3(cudaStream_t st, const SplitPrep3 &p, int64_t n0);
 
+// Near history of step j of a block for every node (FP64):
+//   S[i] = sum_{q<KS} far_q[j][i] + sum_{r<j} wlag[j-r] ring[r][i],
+// ring [64][P] time-major, far partials [KS][64][P] (float pairs when pairs != 0).
+int launch_near_history(cudaStream_t st, const double *ring, int64_t P, int j, const double *wlag,
+                        const double *cfar, int KS, int pairs, double *S);
+
 }  // namespace fpde

@@ -8,6 +8,10 @@
 //   3. _M pass       : lines along j for every (i, k); Om = -lam U
 //   4. sN pass       : lines along i for every (j, k); Om = -lam U
 //   5. append        : D_n = U - U_old over the grid (the snapshot of the step, :5733-5745)
+// Split path (FPDE_PREC_SPLIT_BF16X3): step 1 becomes, per 64-step block, the exact
+// three-slice tensor-core contraction of all history before the block (tc_far.cu, as for
+// lines) and, per step, k_near_history: the far partials plus the FP64 near history from a
+// 64-row FP64 ring of the block's increments (step 5 writes that ring).
 // Each pass is a Thomas solve per line with R = Rlap + lam (A_/B/R :3095-3142). For a
 // uniform step the alpha recurrence Al[p+1] = B/(R - A Al[p]) is time-invariant, so it is
 // evaluated once on the host in the reference's order; a pass then needs two first-order
@@ -27,6 +31,7 @@
 
 #include "common.cuh"
 #include "kernels.cuh"
+#include "tc_far.cuh"
 
 namespace fpde {
 
@@ -45,6 +50,11 @@ struct LodPassArgs {
     double dLN;
 };
 
+// One thread per line. The loads of eight nodes are issued together before their
+// dependent recurrence steps (the in-place stores to U would otherwise keep the compiler
+// from hoisting them), so each line keeps eight nodes of memory traffic in flight.
+constexpr int LB = 8;
+
 __global__ void __launch_bounds__(128) k_lod_pass(LodPassArgs p)
 {
     const int line = blockIdx.x * blockDim.x + threadIdx.x;
@@ -55,18 +65,32 @@ __global__ void __launch_bounds__(128) k_lod_pass(LodPassArgs p)
     const double g0 = p.bc ? p.bc[base] : 0.0;
     // forward: y_q = Bt[q+1] = g_q (A_q y_{q-1} - Om_q), y_0 = Bt[1] = g0; y_q overwrites U_q
     double y = g0, uold_last = 0.0;
-    for (int q = 1; q < Nl; ++q) {
-        const int64_t id = base + (int64_t)q * p.st;
-        const double u = p.U[id];
-        if (q == Nl - 1) uold_last = u;
-        double om = -(p.lam * u) + (p.rp ? p.rp[id] : 0.0);
-        if (p.KS > 0) {
-            double s = 0.0;
-            for (int k = 0; k < p.KS; ++k) s += __ldcg(p.part + (int64_t)k * p.pstride + id);
-            om += s;
+    for (int q0 = 1; q0 < Nl; q0 += LB) {
+        double uu[LB], aa[LB], gg[LB], rr[LB], ss[LB];
+#pragma unroll
+        for (int t = 0; t < LB; ++t) {
+            const int q = q0 + t;
+            const bool in = q < Nl;
+            const int64_t id = base + (int64_t)(in ? q : 1) * p.st;
+            uu[t] = in ? p.U[id] : 0.0;
+            aa[t] = in ? __ldg(p.A + (int64_t)q * L + line) : 0.0;
+            gg[t] = in ? __ldg(p.g + (int64_t)q * L + line) : 0.0;
+            rr[t] = (in && p.rp) ? __ldg(p.rp + id) : 0.0;
+            double sv = 0.0;
+            for (int k = 0; k < p.KS; ++k)
+                if (in) sv += __ldcg(p.part + (int64_t)k * p.pstride + id);
+            ss[t] = sv;
         }
-        y = __ldg(p.g + (int64_t)q * L + line) * (__ldg(p.A + (int64_t)q * L + line) * y - om);
-        p.U[id] = y;
+#pragma unroll
+        for (int t = 0; t < LB; ++t) {
+            const int q = q0 + t;
+            if (q < Nl) {
+                if (q == Nl - 1) uold_last = uu[t];
+                const double om = (-(p.lam * uu[t]) + rr[t]) + ss[t];    // Om1 :4191, :4267
+                y = gg[t] * (aa[t] * y - om);
+                p.U[base + (int64_t)q * p.st] = y;
+            }
+        }
     }
     // right end: Dirichlet value or the flux closure of U1 (:4687-4719) with the old U[Nl-1]
     const double gN = p.bc ? p.bc[base + (int64_t)Nl * p.st] : 0.0;
@@ -81,12 +105,69 @@ __global__ void __launch_bounds__(128) k_lod_pass(LodPassArgs p)
     p.U[base + (int64_t)Nl * p.st] = uN;
     p.U[base + (int64_t)(Nl + 1) * p.st] = uN;                  // ghost copy (U1 :4792)
     double u = uN;
-    for (int q = Nl - 1; q >= 1; --q) {
-        const int64_t id = base + (int64_t)q * p.st;
-        u = fma(__ldg(p.al + (int64_t)q * L + line), u, p.U[id]);
-        p.U[id] = u;
+    for (int q1 = Nl - 1; q1 >= 1; q1 -= LB) {
+        double yy[LB], al[LB];
+#pragma unroll
+        for (int t = 0; t < LB; ++t) {
+            const int q = q1 - t;
+            const bool in = q >= 1;
+            yy[t] = in ? p.U[base + (int64_t)q * p.st] : 0.0;
+            al[t] = in ? __ldg(p.al + (int64_t)q * L + line) : 0.0;
+        }
+#pragma unroll
+        for (int t = 0; t < LB; ++t) {
+            const int q = q1 - t;
+            if (q >= 1) {
+                u = fma(al[t], u, yy[t]);
+                p.U[base + (int64_t)q * p.st] = u;
+            }
+        }
     }
     p.U[base] = fma(__ldg(p.al + line), u, g0);                   // Al[1] U[1] + Bt[1]
+}
+
+// Near history (split path): two nodes per thread, eight ring rows of loads in flight.
+__global__ void __launch_bounds__(256) k_near_history(const double2 *__restrict__ ring, int64_t P2, int j,
+                                                      const double *__restrict__ wlag,
+                                                      const double2 *__restrict__ cfar, int KS, int pairs,
+                                                      double2 *__restrict__ S)
+{
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P2) return;
+    double ax = 0.0, ay = 0.0, bx = 0.0, by = 0.0;
+    for (int q = 0; q < KS; ++q) {
+        const double2 v = __ldcs(cfar + ((int64_t)q * 64 + j) * P2 + i);
+        bx += pairs ? ff_to_double(v.x) : v.x;
+        by += pairs ? ff_to_double(v.y) : v.y;
+    }
+    int r = 0;
+    for (; r + 8 <= j; r += 8) {
+        double2 v[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) v[u] = __ldcg(ring + (int64_t)(r + u) * P2 + i);
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            const double w = __ldg(wlag + (j - r - u));
+            ax = fma(w, v[u].x, ax);
+            ay = fma(w, v[u].y, ay);
+        }
+    }
+    for (; r < j; ++r) {
+        const double2 v = __ldcg(ring + (int64_t)r * P2 + i);
+        const double w = __ldg(wlag + (j - r));
+        ax = fma(w, v.x, ax);
+        ay = fma(w, v.y, ay);
+    }
+    S[i] = make_double2(bx + ax, by + ay);
+}
+
+int launch_near_history(cudaStream_t st, const double *ring, int64_t P, int j, const double *wlag,
+                        const double *cfar, int KS, int pairs, double *S)
+{
+    k_near_history<<<(unsigned)((P / 2 + 255) / 256), 256, 0, st>>>((const double2 *)ring, P / 2, j, wlag,
+                                                                    (const double2 *)cfar, KS, pairs, (double2 *)S);
+    FPDE_LAUNCHED(1);
+    return FPDE_OK;
 }
 
 }  // namespace fpde
@@ -106,6 +187,13 @@ struct fpde_lod3d {
     double *cA[3] = {nullptr, nullptr, nullptr}, *cg[3] = {nullptr, nullptr, nullptr},
            *cal[3] = {nullptr, nullptr, nullptr};
     int lines[3] = {0, 0, 0};
+    // split path (exact three-slice far history on the tensor cores, FP64 near history)
+    bool split = false;
+    int64_t rows16 = 0, ld16 = 0, ldp = 0;
+    uint16_t *h3[3] = {nullptr, nullptr, nullptr}, *w3[3] = {nullptr, nullptr, nullptr};
+    int8_t *pA = nullptr, *pW = nullptr;
+    double *ring = nullptr, *cfar = nullptr, *wlag = nullptr, *Sn = nullptr;
+    FarPlan3 plan3;
     int64_t n_done = 0;
     std::map<std::pair<int64_t, int>, cudaGraphExec_t> graphs;
     std::map<std::pair<int64_t, int>, int64_t> graph_launches;
@@ -133,7 +221,7 @@ static int lod_launch_pass(fpde_lod3d *L, cudaStream_t st, int pass, int64_t n, 
     a.lines = L->lines[pass];
     a.U = L->U;
     a.A = L->cA[pass]; a.g = L->cg[pass]; a.al = L->cal[pass];
-    a.part = pass == 2 ? L->part : nullptr;
+    a.part = pass == 2 ? (L->split ? L->Sn : L->part) : nullptr;
     a.KS = pass == 2 ? KS : 0;
     a.pstride = L->P;
     a.rp = (pass == 2 && L->rp) ? L->rp + (n < L->rp_rows ? n : L->rp_rows - 1) * L->G : nullptr;
@@ -154,17 +242,46 @@ static int lod_enqueue(fpde_lod3d *L, cudaStream_t st, int64_t n0, int steps, in
     int rc;
     for (int64_t n = n0; n < n0 + steps; ++n) {
         int KS = 0;
-        if (n >= 1) {
-            KS = choose_splits((int)n, L->P);
-            const double *wt = L->wrev + (L->max_steps - n);         // wt[t] = w[n - t]
-            if ((rc = launch_l1_partial(st, L->D, L->P, (int)n, wt, L->part, KS))) return rc;
-            ++k;
+        double *Drow;
+        if (!L->split) {
+            if (n >= 1) {
+                KS = choose_splits((int)n, L->P);
+                const double *wt = L->wrev + (L->max_steps - n);     // wt[t] = w[n - t]
+                if ((rc = launch_l1_partial(st, L->D, L->P, (int)n, wt, L->part, KS))) return rc;
+                ++k;
+            }
+            Drow = L->D + n * L->P;
+        } else {
+            const int64_t nb0 = n - n % 64;                          // block of 64 steps
+            const int j = (int)(n - nb0);
+            int splits = 0;
+            if (nb0 > 0) {
+                splits = far_splits((int)(nb0 / 64), L->rows16);
+                if (j == 0) {                                        // far history t < nb0
+                    SplitPrep3 sp;
+                    sp.ring = L->ring; sp.P = L->P; sp.nvalid = L->G; sp.ld = L->ld16; sp.wlag = L->wlag;
+                    for (int q = 0; q < 3; ++q) { sp.hist[q] = L->h3[q]; sp.w[q] = L->w3[q]; }
+                    sp.pA = L->pA; sp.pW = L->pW; sp.ldp = L->ldp;
+                    if ((rc = launch_block_prep3(st, sp, nb0))) return rc;
+                    k += 2;
+                    if ((rc = far3_launch(st, &L->plan3, (int)nb0, L->cfar, (int64_t)64 * L->P, L->P, splits, L->pA,
+                                          L->pW, L->ldp, L->ctx->d_flags)))
+                        return rc;
+                    ++k;
+                }
+            }
+            if (n >= 1) {
+                if ((rc = launch_near_history(st, L->ring, L->P, j, L->wlag, L->cfar, splits, 1, L->Sn))) return rc;
+                ++k;
+                KS = 1;
+            }
+            Drow = L->ring + (int64_t)j * L->P;
         }
         for (int pass = 2; pass >= 0; --pass) {                      // K, _M, sN (calc_step order)
             if ((rc = lod_launch_pass(L, st, pass, n, KS))) return rc;
             ++k;
         }
-        if ((rc = launch_append(st, L->U, L->last, L->D + n * L->P, L->G, L->P))) return rc;
+        if ((rc = launch_append(st, L->U, L->last, Drow, L->G, L->P))) return rc;
         ++k;
     }
     *nk = k;
@@ -183,7 +300,14 @@ int fpde_lod3d_destroy(fpde_lod3d *L)
         cudaStreamSynchronize(L->ctx->stream);
     }
     for (auto &kv : L->graphs) cudaGraphExecDestroy(kv.second);
-    for (double *p : {L->U, L->last, L->D, L->part, L->wrev, L->rp, L->bc}) dev_free(p);
+    for (double *p : {L->U, L->last, L->D, L->part, L->wrev, L->rp, L->bc, L->ring, L->cfar, L->wlag, L->Sn})
+        dev_free(p);
+    for (int q = 0; q < 3; ++q) {
+        dev_free(L->h3[q]);
+        dev_free(L->w3[q]);
+    }
+    dev_free(L->pA);
+    dev_free(L->pW);
     for (int q = 0; q < 3; ++q) {
         dev_free(L->cA[q]);
         dev_free(L->cg[q]);
@@ -205,7 +329,8 @@ int fpde_lod3d_create(fpde_ctx *ctx, const fpde_lod3d_desc *desc, const double *
     FPDE_CHECK_ARG(d.sN >= 2 && d.M >= 2 && d.K >= 2, "every axis needs at least 2 intervals");
     FPDE_CHECK_ARG(d.lag_weights || (d.alpha > 0.0 && d.alpha < 1.0), "alpha must be in (0, 1)");
     FPDE_CHECK_ARG(d.tau > 0.0 && d.max_steps > 0, "tau and max_steps must be positive");
-    FPDE_CHECK_ARG(d.precision == FPDE_PREC_FP64, "the 3D LOD path computes in FP64");
+    FPDE_CHECK_ARG(d.precision == FPDE_PREC_FP64 || d.precision == FPDE_PREC_SPLIT_BF16X3,
+                   "3D LOD: precision must be FP64 or the exact three-slice split");
     FPDE_CHECK_ARG(!d.source || d.source_rows >= 1, "source needs source_rows >= 1");
     FPDE_CHECK_ARG(!d.bc || d.bc_rows >= 1, "bc needs bc_rows >= 1");
     for (int q = 0; q < 3; ++q)
@@ -233,10 +358,40 @@ int fpde_lod3d_create(fpde_ctx *ctx, const fpde_lod3d_desc *desc, const double *
         wrev[m] = d.lag_weights ? d.lag_weights[j] : d.Da * (kkk0 * l1_lag(d.alpha, j)) / d.tau;
     }
     const size_t gbytes = (size_t)L->G * sizeof(double), pbytes = (size_t)L->P * sizeof(double);
+    L->split = d.precision == FPDE_PREC_SPLIT_BF16X3;
     bool fail = dev_alloc((void **)&L->U, pbytes) || dev_alloc((void **)&L->last, pbytes) ||
-                dev_alloc((void **)&L->D, (size_t)L->max_steps * pbytes) ||
-                dev_alloc((void **)&L->part, (size_t)KS_MAX * pbytes) ||
                 dev_alloc((void **)&L->wrev, wrev.size() * sizeof(double));
+    std::vector<double> wlag;
+    if (!fail && !L->split) {
+        fail = dev_alloc((void **)&L->D, (size_t)L->max_steps * pbytes) ||
+               dev_alloc((void **)&L->part, (size_t)KS_MAX * pbytes);
+    } else if (!fail) {
+        L->rows16 = (L->G + 127) / 128 * 128;
+        L->ld16 = ((int64_t)L->max_steps + 63) / 64 * 64;
+        L->ldp = L->ld16 / 64;
+        const int64_t LW = L->max_steps + 64 + 1;
+        wlag.assign(LW, 0.0);
+        for (int64_t j = 1; j < LW; ++j)
+            wlag[j] = d.lag_weights ? (j <= L->max_steps ? d.lag_weights[j] : 0.0)
+                                    : d.Da * (kkk0 * l1_lag(d.alpha, j)) / d.tau;
+        for (int q = 0; q < 3 && !fail; ++q)
+            fail = dev_alloc((void **)&L->h3[q], (size_t)L->rows16 * L->ld16 * 2) ||
+                   dev_alloc((void **)&L->w3[q], (size_t)64 * L->ld16 * 2);
+        fail = fail || dev_alloc((void **)&L->pA, (size_t)L->rows16 * L->ldp) ||
+               dev_alloc((void **)&L->pW, (size_t)64 * L->ldp) ||
+               dev_alloc((void **)&L->ring, (size_t)64 * pbytes) ||
+               dev_alloc((void **)&L->cfar, (size_t)FAR_MAX_SPLITS * 64 * pbytes) ||
+               dev_alloc((void **)&L->wlag, LW * sizeof(double)) || dev_alloc((void **)&L->Sn, pbytes);
+        if (!fail) {
+            const void *a3[3] = {L->h3[0], L->h3[1], L->h3[2]}, *w3[3] = {L->w3[0], L->w3[1], L->w3[2]};
+            int rcp = far_plan3_init(&L->plan3, a3, L->rows16, L->ld16, w3, L->ld16);
+            if (rcp) {
+                std::string keep = fpde_last_error_string();
+                fpde_lod3d_destroy(L);
+                return set_error(rcp, "%s", keep.c_str());
+            }
+        }
+    }
     if (!fail && d.source) {
         L->rp_rows = std::min(d.source_rows, d.max_steps);
         fail = dev_alloc((void **)&L->rp, (size_t)L->rp_rows * gbytes);
@@ -294,7 +449,19 @@ int fpde_lod3d_create(fpde_ctx *ctx, const fpde_lod3d_desc *desc, const double *
     cudaMemcpyAsync(L->U, u0, gbytes, cudaMemcpyHostToDevice, st);
     cudaMemsetAsync(L->last, 0, pbytes, st);
     cudaMemcpyAsync(L->last, u0, gbytes, cudaMemcpyHostToDevice, st);
-    cudaMemsetAsync(L->D, 0, (size_t)L->max_steps * pbytes, st);
+    if (!L->split) {
+        cudaMemsetAsync(L->D, 0, (size_t)L->max_steps * pbytes, st);
+    } else {
+        for (int q = 0; q < 3; ++q) {
+            cudaMemsetAsync(L->h3[q], 0, (size_t)L->rows16 * L->ld16 * 2, st);
+            cudaMemsetAsync(L->w3[q], 0, (size_t)64 * L->ld16 * 2, st);
+        }
+        cudaMemsetAsync(L->pA, 0, (size_t)L->rows16 * L->ldp, st);
+        cudaMemsetAsync(L->pW, 0, (size_t)64 * L->ldp, st);
+        cudaMemsetAsync(L->ring, 0, (size_t)64 * pbytes, st);
+        cudaMemsetAsync(L->cfar, 0, (size_t)FAR_MAX_SPLITS * 64 * pbytes, st);
+        cudaMemcpyAsync(L->wlag, wlag.data(), wlag.size() * sizeof(double), cudaMemcpyHostToDevice, st);
+    }
     cudaMemcpyAsync(L->wrev, wrev.data(), wrev.size() * sizeof(double), cudaMemcpyHostToDevice, st);
     if (L->rp) cudaMemcpyAsync(L->rp, d.source, (size_t)L->rp_rows * gbytes, cudaMemcpyHostToDevice, st);
     if (L->bc) cudaMemcpyAsync(L->bc, d.bc, (size_t)L->bc_rows * gbytes, cudaMemcpyHostToDevice, st);

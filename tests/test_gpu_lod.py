@@ -95,3 +95,23 @@ def test_lod_runs_in_pieces_and_solve_host(ctx):
     lod.solve_host(p.u0, 20, out)
     lod.close()
     assert np.array_equal(u_two, out)
+
+
+@pytest.mark.parametrize("steps,tol", [(64, 1e-12), (230, 1e-7)])
+def test_lod_split_history_vs_fp64(ctx, steps, tol):
+    """Split path (far history as exact bf16 slices on the tensor cores, near history and
+    passes in FP64): equal to the FP64 path within one block, within 1e-7 across blocks."""
+    import fpde_hpc_gb300 as fp
+    from fpde_hpc_gb300 import problems
+    p = problems.config4(n=20, steps=steps)
+    cA, cB, cR = p.coefs()
+    kw = dict(left_kind=p.left_kind, right_kind=p.right_kind, dLN=p.dLN)
+    out = []
+    for prec in (0, 3):
+        lod = fp.Lod3D(ctx, p.dims, p.alpha, p.tau, p.Da, cA, cB, cR, p.u0, steps, precision=prec, **kw)
+        lod.run(steps)
+        out.append(lod.state())
+        lod.close()
+    err = relmax(out[1], out[0])
+    print(f"LOD 20^3 {steps} steps, split x3 vs FP64: max rel {err:.2e}")
+    assert err <= tol
