@@ -165,7 +165,6 @@ class LineWorkload:
             self.desc = (f"distributed-order line N={self.p.N}, {self.p.steps} steps, w(a)=6a(1-a), 16-node "
                          "Gauss-Legendre, tau 1e-4, lognormal k (seed 3), 8-Gaussian H0 (seed 4) (config 3)")
         self.node_steps = self.p.node_steps
-        self.paths = ["fp64", "split-bf16", "split-fp16", "split-bf16x3"]
 
     def weights(self, n):
         import fpde_hpc_gb300 as fp
@@ -226,7 +225,6 @@ class LodWorkload:
                        f"{self.p.steps} steps)")
         self.desc = (f"3D LOD {n}^3, {self.p.steps} steps, alpha 0.85, tau 1e-3, lognormal k (sigma 0.4, seed 5), "
                      "Gaussian blob, zero-flux sides, Dirichlet top/bottom (config 4)")
-        self.paths = ["fp64"]
 
     def build(self, ctx, prec):
         import fpde_hpc_gb300 as fp
@@ -275,7 +273,6 @@ class BatchWorkload:
         self.desc = (f"ensemble of {len(self.cols)} columns, N log-uniform [256, 16384] "
                      f"(sum N = {sum(c.N for c in self.cols)}), alpha U[0.5, 0.95], tau 1e-3, {self._steps} steps, "
                      "seeds 6.. (config 5)")
-        self.paths = ["fp64"]
         self._b = None
 
     def build(self, ctx, prec):
@@ -410,14 +407,11 @@ def run_ours(args):
     ctx.set_stream(stream.cuda_stream)
     lib = ctx.lib
     is_line = isinstance(wl, LineWorkload)
-    splittable = is_line or isinstance(wl, LodWorkload)
-    prec = {"auto": fp.FPDE_PREC_SPLIT_BF16X3 if splittable else fp.FPDE_PREC_FP64, "fp64": fp.FPDE_PREC_FP64,
-            "bf16": fp.FPDE_PREC_SPLIT_BF16, "f16": fp.FPDE_PREC_SPLIT_F16,
-            "bf16x3": fp.FPDE_PREC_SPLIT_BF16X3}[args.precision]
+    # default: the exact three-slice split path (every workload has it), with the FP64 arm beside it
+    prec = {"auto": fp.FPDE_PREC_SPLIT_BF16X3, "fp64": fp.FPDE_PREC_FP64, "bf16": fp.FPDE_PREC_SPLIT_BF16,
+            "f16": fp.FPDE_PREC_SPLIT_F16, "bf16x3": fp.FPDE_PREC_SPLIT_BF16X3}[args.precision]
     if not is_line and prec not in (fp.FPDE_PREC_FP64, fp.FPDE_PREC_SPLIT_BF16X3):
         raise SystemExit(f"{wl.name} runs in FP64 or the exact three-slice split")
-    if not splittable and prec != fp.FPDE_PREC_FP64:
-        raise SystemExit(f"{wl.name} runs in FP64 only")
     pname = {0: "fp64", 1: "split-bf16", 2: "split-fp16", 3: "split-bf16x3"}[prec]
 
     obj = wl.build(ctx, prec)
@@ -449,7 +443,7 @@ def run_ours(args):
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms = float(t.item())
     value = wl.node_steps * world / (ms / 1e3)
-    u_main = obj.state() if splittable else None
+    u_main = obj.state()
 
     # end to end through the C ABI with host buffers (pinned)
     u0_h = torch.from_numpy(np.ascontiguousarray(wl.u0).copy()).pin_memory()
@@ -523,7 +517,7 @@ def run_ours(args):
                            "peak": peak, "unit": "GB/s", "frac": gbs / peak, "peak_source": peak_src,
                            "traffic": None, "note": "algorithmic history bytes / whole solve time"}
 
-    if splittable and prec != 0 and not args.no_fp64_arm:
+    if prec != 0 and not args.no_fp64_arm:
         # the plain FP64 kernel on the same workload: speed-up and accuracy of the split path
         l64 = wl.build(ctx, fp.FPDE_PREC_FP64)
         l64.reset(u0_dev)

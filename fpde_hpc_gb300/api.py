@@ -342,7 +342,10 @@ class Batch:
     def run(self, steps):
         check(self.ctx.lib.fpde_batch_run(self.h, steps), "fpde_batch_run")
 
-    def state(self, col):
+    def state(self, col=None):
+        """Column col's state, or (col None) all columns' states concatenated."""
+        if col is None:
+            return np.concatenate([self.state(c) for c in range(self.n_cols)])
         out = np.zeros(self.layout[col][1] + 1)
         check(self.ctx.lib.fpde_batch_get_state(self.h, col, _ptr(out), 0), "fpde_batch_get_state")
         return out

@@ -9,9 +9,14 @@
 // Per time step n:
 //   1. k_batch_partial : part[ks][q] = sum_t w_c[n-t] D_t[q], the column's lag weights picked
 //                        per CTA (one flat grid over all nodes: balanced by construction)
-//   2. k_batch_solve   : one CTA per column, launched largest first; Thomas per column
-//                        (fpde_hpc_1d.cpp al1/bt1/U1 :4002-4027, :4585-4590, :4683-4724) as
-//                        segment sweeps joined by a CTA scan, then U and D_n written.
+//   2. k_batch_solve   : one persistent launch fed by a device work queue: each CTA takes the
+//                        next column (largest first) from an atomic counter of the step and runs
+//                        Thomas on it (fpde_hpc_1d.cpp al1/bt1/U1 :4002-4027, :4585-4590,
+//                        :4683-4724) as segment sweeps joined by a CTA scan, then writes U and D_n.
+// Split path (FPDE_PREC_SPLIT_BF16X3): step 1 becomes, per 64-step block, the exact
+// three-slice tensor-core contraction of all history before the block with one weight tile
+// per column (tc_far.cu; each 128-row tile picks its column's tile), and per step the FP64
+// near history from a 64-row ring (k_near_history); the increments go to that ring.
 // The alpha recurrence is time-invariant and precomputed on the host per column.
 #include <algorithm>
 #include <cmath>
@@ -23,6 +28,7 @@
 #include "common.cuh"
 #include "kernels.cuh"
 #include "scan.cuh"
+#include "tc_far.cuh"
 
 namespace fpde {
 
@@ -99,6 +105,7 @@ __device__ __forceinline__ void cta_scan_excl(double &P, double &X, double *wP, 
 }
 
 __global__ void __launch_bounds__(BT) k_batch_solve(const ColInfo *__restrict__ cols, const int *__restrict__ order,
+                                                    int n_cols, unsigned *__restrict__ queue,
                                                     const double *__restrict__ A, const double *__restrict__ g,
                                                     const double *__restrict__ al, const double *__restrict__ segP,
                                                     const double *__restrict__ segQ, const double *__restrict__ part,
@@ -107,7 +114,13 @@ __global__ void __launch_bounds__(BT) k_batch_solve(const ColInfo *__restrict__ 
 {
     __shared__ double wP[BW], wX[BW];
     __shared__ double s_y, s_uN;
-    const int col = order[blockIdx.x];
+    __shared__ int s_item;
+    while (true) {
+    if (threadIdx.x == 0) s_item = (int)atomicAdd(queue, 1u);
+    __syncthreads();
+    const int item = s_item;
+    if (item >= n_cols) return;
+    const int col = order[item];
     const ColInfo c = cols[col];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int64_t o = c.off;
@@ -172,6 +185,8 @@ __global__ void __launch_bounds__(BT) k_batch_solve(const ColInfo *__restrict__ 
         U[o + c.N] = uN;
         Drow[o + c.N] = uN - uo;
     }
+    __syncthreads();                                                // s_item, s_y, s_uN reused
+    }
 }
 
 }  // namespace fpde
@@ -188,6 +203,16 @@ struct fpde_batch {
     double *U = nullptr, *U0 = nullptr, *Y = nullptr, *D = nullptr, *part = nullptr, *wall = nullptr;
     ColInfo *cols = nullptr;
     int *order = nullptr, *cta_col = nullptr;
+    unsigned *queue = nullptr;                // per step: next work item of the solve
+    int solve_grid = 0;
+    // split path
+    bool split = false;
+    int64_t ld16 = 0, ldp = 0, LW = 0;
+    uint16_t *h3[3] = {nullptr, nullptr, nullptr}, *w3[3] = {nullptr, nullptr, nullptr};
+    int8_t *pA = nullptr, *pW = nullptr;
+    double *ring = nullptr, *cfar = nullptr, *wlag = nullptr, *Sn = nullptr;
+    int *wcol = nullptr;
+    FarPlan3 plan3;
     int64_t n_done = 0;
     std::map<std::pair<int64_t, int>, cudaGraphExec_t> graphs;
     std::map<std::pair<int64_t, int>, int64_t> graph_launches;
@@ -198,19 +223,54 @@ namespace fpde {
 static int batch_enqueue(fpde_batch *b, cudaStream_t st, int64_t n0, int steps, int64_t *nk)
 {
     int64_t k = 0;
+    int rc;
+    FPDE_CUDA(cudaMemsetAsync(b->queue + n0, 0, (size_t)steps * sizeof(unsigned), st));   // work queues of the run
     for (int64_t n = n0; n < n0 + steps; ++n) {
         int KS = 0;
-        if (n >= 1) {
-            KS = choose_splits((int)n, b->Ptot);
-            dim3 grid((unsigned)(b->Ptot / 512), (unsigned)KS);
-            k_batch_partial<<<grid, 256, 0, st>>>((const double2 *)b->D, b->Ptot / 2, (int)n, b->wall,
-                                                  b->max_steps + 1, b->max_steps - n, b->cta_col,
-                                                  (double2 *)b->part);
-            FPDE_LAUNCHED(1);
-            ++k;
+        const double *part = b->part;
+        double *Drow;
+        if (!b->split) {
+            if (n >= 1) {
+                KS = choose_splits((int)n, b->Ptot);
+                dim3 grid((unsigned)(b->Ptot / 512), (unsigned)KS);
+                k_batch_partial<<<grid, 256, 0, st>>>((const double2 *)b->D, b->Ptot / 2, (int)n, b->wall,
+                                                      b->max_steps + 1, b->max_steps - n, b->cta_col,
+                                                      (double2 *)b->part);
+                FPDE_LAUNCHED(1);
+                ++k;
+            }
+            Drow = b->D + n * b->Ptot;
+        } else {
+            const int64_t nb0 = n - n % 64;
+            const int j = (int)(n - nb0);
+            int splits = 0;
+            if (nb0 > 0) {
+                splits = far_splits((int)(nb0 / 64), b->Ptot);
+                if (j == 0) {                                        // far history t < nb0, per column
+                    SplitPrep3 sp;
+                    sp.ring = b->ring; sp.P = b->Ptot; sp.nvalid = b->Ptot; sp.ld = b->ld16; sp.wlag = b->wlag;
+                    for (int q = 0; q < 3; ++q) { sp.hist[q] = b->h3[q]; sp.w[q] = b->w3[q]; }
+                    sp.pA = b->pA; sp.pW = b->pW; sp.ldp = b->ldp; sp.ncols = b->n_cols; sp.wstride = b->LW;
+                    if ((rc = launch_block_prep3(st, sp, nb0))) return rc;
+                    k += 2;
+                    if ((rc = far3_launch(st, &b->plan3, (int)nb0, b->cfar, (int64_t)64 * b->Ptot, b->Ptot, splits,
+                                          b->pA, b->pW, b->ldp, b->ctx->d_flags, b->wcol)))
+                        return rc;
+                    ++k;
+                }
+            }
+            if (n >= 1) {
+                if ((rc = launch_near_history(st, b->ring, b->Ptot, j, b->wlag, b->cfar, splits, 1, b->Sn, b->cta_col,
+                                              b->LW)))
+                    return rc;
+                ++k;
+                KS = 1;
+                part = b->Sn;
+            }
+            Drow = b->ring + (int64_t)j * b->Ptot;
         }
-        k_batch_solve<<<b->n_cols, BT, 0, st>>>(b->cols, b->order, b->A, b->g, b->al, b->segP, b->segQ, b->part, KS,
-                                                b->Ptot, b->U, b->Y, b->D + n * b->Ptot);
+        k_batch_solve<<<b->solve_grid, BT, 0, st>>>(b->cols, b->order, b->n_cols, b->queue + n, b->A, b->g, b->al,
+                                                    b->segP, b->segQ, part, KS, b->Ptot, b->U, b->Y, Drow);
         FPDE_LAUNCHED(1);
         ++k;
     }
@@ -230,7 +290,17 @@ int fpde_batch_destroy(fpde_batch *b)
         cudaStreamSynchronize(b->ctx->stream);
     }
     for (auto &kv : b->graphs) cudaGraphExecDestroy(kv.second);
-    for (double *p : {b->A, b->g, b->al, b->segP, b->segQ, b->U, b->U0, b->Y, b->D, b->part, b->wall}) dev_free(p);
+    for (double *p : {b->A, b->g, b->al, b->segP, b->segQ, b->U, b->U0, b->Y, b->D, b->part, b->wall, b->ring,
+                      b->cfar, b->wlag, b->Sn})
+        dev_free(p);
+    for (int q = 0; q < 3; ++q) {
+        dev_free(b->h3[q]);
+        dev_free(b->w3[q]);
+    }
+    dev_free(b->pA);
+    dev_free(b->pW);
+    dev_free(b->wcol);
+    dev_free(b->queue);
     dev_free(b->cols);
     dev_free(b->order);
     dev_free(b->cta_col);
@@ -247,7 +317,8 @@ int fpde_batch_create(fpde_ctx *ctx, const fpde_column_desc *cols, int n_cols, i
     int rc = ctx_enter(ctx);
     if (rc) return rc;
     FPDE_CHECK_ARG(max_steps > 0, "max_steps must be positive");
-    FPDE_CHECK_ARG(precision == FPDE_PREC_FP64, "the ensemble computes in FP64");
+    FPDE_CHECK_ARG(precision == FPDE_PREC_FP64 || precision == FPDE_PREC_SPLIT_BF16X3,
+                   "ensemble: precision must be FP64 or the exact three-slice split");
     for (int c = 0; c < n_cols; ++c) {
         const fpde_column_desc &d = cols[c];
         FPDE_CHECK_ARG(d.N >= 2 && d.N <= (1 << 24), "column N out of range");
@@ -323,6 +394,24 @@ int fpde_batch_create(fpde_ctx *ctx, const fpde_column_desc *cols, int n_cols, i
         }
         for (int64_t q = o / 512; q < (o + (N + 1 + 511) / 512 * 512) / 512; ++q) cta_col[q] = c;
     }
+    const bool split = precision == FPDE_PREC_SPLIT_BF16X3;
+    b->split = split;
+    b->LW = (int64_t)max_steps + 64 + 1;
+    std::vector<double> hwl;                                           // split: w_c[lag], lag < LW
+    std::vector<int> hwcol;                                            // split: column of each 128-row tile
+    if (split) {
+        hwl.assign((size_t)n_cols * b->LW, 0.0);
+        hwcol.assign(tot / 128, 0);
+        for (int c = 0; c < n_cols; ++c) {
+            const fpde_column_desc &d = cols[c];
+            const double kkk0 = d.lag_weights ? 0.0 : l1_interval_weight(d.alpha, 0.0, d.tau);
+            for (int64_t j = 1; j < b->LW; ++j)
+                hwl[(size_t)c * b->LW + j] = d.lag_weights ? (j <= max_steps ? d.lag_weights[j] : 0.0)
+                                                           : d.Da * (kkk0 * l1_lag(d.alpha, j)) / d.tau;
+            const int64_t o = b->off[c], Pc = (cols[c].N + 1 + 511) / 512 * 512;
+            for (int64_t q = o / 128; q < (o + Pc) / 128; ++q) hwcol[q] = c;
+        }
+    }
     std::vector<int> order(n_cols);                                    // largest columns first
     std::iota(order.begin(), order.end(), 0);
     std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return b->N[x] > b->N[y]; });
@@ -331,11 +420,35 @@ int fpde_batch_create(fpde_ctx *ctx, const fpde_column_desc *cols, int n_cols, i
                 dev_alloc((void **)&b->segP, hP.size() * sizeof(double)) ||
                 dev_alloc((void **)&b->segQ, hQ.size() * sizeof(double)) || dev_alloc((void **)&b->U, tb) ||
                 dev_alloc((void **)&b->U0, tb) || dev_alloc((void **)&b->Y, tb) ||
-                dev_alloc((void **)&b->D, (size_t)max_steps * tb) || dev_alloc((void **)&b->part, (size_t)KS_MAX * tb) ||
-                dev_alloc((void **)&b->wall, hw.size() * sizeof(double)) ||
                 dev_alloc((void **)&b->cols, hc.size() * sizeof(ColInfo)) ||
                 dev_alloc((void **)&b->order, order.size() * sizeof(int)) ||
-                dev_alloc((void **)&b->cta_col, cta_col.size() * sizeof(int));
+                dev_alloc((void **)&b->cta_col, cta_col.size() * sizeof(int)) ||
+                dev_alloc((void **)&b->queue, (size_t)max_steps * sizeof(unsigned));
+    if (!fail && !split) {
+        fail = dev_alloc((void **)&b->D, (size_t)max_steps * tb) || dev_alloc((void **)&b->part, (size_t)KS_MAX * tb) ||
+               dev_alloc((void **)&b->wall, hw.size() * sizeof(double));
+    } else if (!fail) {
+        b->ld16 = ((int64_t)max_steps + 63) / 64 * 64;
+        b->ldp = b->ld16 / 64;
+        const int64_t wrows = (int64_t)n_cols * 64;
+        for (int q = 0; q < 3 && !fail; ++q)
+            fail = dev_alloc((void **)&b->h3[q], (size_t)tot * b->ld16 * 2) ||
+                   dev_alloc((void **)&b->w3[q], (size_t)wrows * b->ld16 * 2);
+        fail = fail || dev_alloc((void **)&b->pA, (size_t)tot * b->ldp) ||
+               dev_alloc((void **)&b->pW, (size_t)wrows * b->ldp) || dev_alloc((void **)&b->ring, (size_t)64 * tb) ||
+               dev_alloc((void **)&b->cfar, (size_t)FAR_MAX_SPLITS * 64 * tb) ||
+               dev_alloc((void **)&b->wlag, hwl.size() * sizeof(double)) || dev_alloc((void **)&b->Sn, tb) ||
+               dev_alloc((void **)&b->wcol, hwcol.size() * sizeof(int));
+        if (!fail) {
+            const void *a3[3] = {b->h3[0], b->h3[1], b->h3[2]}, *w3[3] = {b->w3[0], b->w3[1], b->w3[2]};
+            int rcp = far_plan3_init(&b->plan3, a3, tot, b->ld16, w3, b->ld16, n_cols);
+            if (rcp) {
+                std::string keep = fpde_last_error_string();
+                fpde_batch_destroy(b);
+                return set_error(rcp, "%s", keep.c_str());
+            }
+        }
+    }
     if (fail) {
         std::string keep = fpde_last_error_string();
         fpde_batch_destroy(b);
@@ -350,8 +463,28 @@ int fpde_batch_create(fpde_ctx *ctx, const fpde_column_desc *cols, int n_cols, i
     cudaMemcpyAsync(b->U, hU.data(), tb, cudaMemcpyHostToDevice, st);
     cudaMemcpyAsync(b->U0, hU.data(), tb, cudaMemcpyHostToDevice, st);
     cudaMemsetAsync(b->Y, 0, tb, st);
-    cudaMemsetAsync(b->D, 0, (size_t)max_steps * tb, st);
-    cudaMemcpyAsync(b->wall, hw.data(), hw.size() * sizeof(double), cudaMemcpyHostToDevice, st);
+    cudaMemsetAsync(b->queue, 0, (size_t)max_steps * sizeof(unsigned), st);
+    if (!split) {
+        cudaMemsetAsync(b->D, 0, (size_t)max_steps * tb, st);
+        cudaMemcpyAsync(b->wall, hw.data(), hw.size() * sizeof(double), cudaMemcpyHostToDevice, st);
+    } else {
+        const int64_t wrows = (int64_t)n_cols * 64;
+        for (int q = 0; q < 3; ++q) {
+            cudaMemsetAsync(b->h3[q], 0, (size_t)tot * b->ld16 * 2, st);
+            cudaMemsetAsync(b->w3[q], 0, (size_t)wrows * b->ld16 * 2, st);
+        }
+        cudaMemsetAsync(b->pA, 0, (size_t)tot * b->ldp, st);
+        cudaMemsetAsync(b->pW, 0, (size_t)wrows * b->ldp, st);
+        cudaMemsetAsync(b->ring, 0, (size_t)64 * tb, st);
+        cudaMemsetAsync(b->cfar, 0, (size_t)FAR_MAX_SPLITS * 64 * tb, st);
+        cudaMemcpyAsync(b->wlag, hwl.data(), hwl.size() * sizeof(double), cudaMemcpyHostToDevice, st);
+        cudaMemcpyAsync(b->wcol, hwcol.data(), hwcol.size() * sizeof(int), cudaMemcpyHostToDevice, st);
+    }
+    {                                                                  // persistent solve grid
+        int per_sm = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch_solve, BT, 0);
+        b->solve_grid = std::max(1, std::min(n_cols, std::max(1, per_sm) * ctx->sm_count));
+    }
     cudaMemcpyAsync(b->cols, hc.data(), hc.size() * sizeof(ColInfo), cudaMemcpyHostToDevice, st);
     cudaMemcpyAsync(b->order, order.data(), order.size() * sizeof(int), cudaMemcpyHostToDevice, st);
     cudaMemcpyAsync(b->cta_col, cta_col.data(), cta_col.size() * sizeof(int), cudaMemcpyHostToDevice, st);

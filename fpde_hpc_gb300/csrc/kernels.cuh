@@ -48,14 +48,18 @@ struct SplitPrep3 {
     int64_t ld = 0;
     int8_t *pA = nullptr, *pW = nullptr;
     int64_t ldp = 0;
-    const double *wlag = nullptr;
+    const double *wlag = nullptr;        // w[lag] (per column: ncols rows of wstride)
+    int ncols = 1;                       // weight tiles (columns of an ensemble)
+    int64_t wstride = 0;
 };
 int launch_block_prep3(cudaStream_t st, const SplitPrep3 &p, int64_t n0);
 
 // Near history of step j of a block for every node (FP64):
 //   S[i] = sum_{q<KS} far_q[j][i] + sum_{r<j} wlag[j-r] ring[r][i],
 // ring [64][P] time-major, far partials [KS][64][P] (float pairs when pairs != 0).
+// cta_col (may be null) gives each 512-node group its column's weights at wlag + col * wstride.
 int launch_near_history(cudaStream_t st, const double *ring, int64_t P, int j, const double *wlag,
-                        const double *cfar, int KS, int pairs, double *S);
+                        const double *cfar, int KS, int pairs, double *S, const int *cta_col = nullptr,
+                        int64_t wstride = 0);
 
 }  // namespace fpde

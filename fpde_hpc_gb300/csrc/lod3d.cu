@@ -128,12 +128,14 @@ __global__ void __launch_bounds__(128) k_lod_pass(LodPassArgs p)
 
 // Near history (split path): two nodes per thread, eight ring rows of loads in flight.
 __global__ void __launch_bounds__(256) k_near_history(const double2 *__restrict__ ring, int64_t P2, int j,
-                                                      const double *__restrict__ wlag,
+                                                      const double *__restrict__ wlag_all,
                                                       const double2 *__restrict__ cfar, int KS, int pairs,
-                                                      double2 *__restrict__ S)
+                                                      double2 *__restrict__ S, const int *__restrict__ cta_col,
+                                                      int64_t wstride)
 {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= P2) return;
+    const double *wlag = cta_col ? wlag_all + (int64_t)cta_col[blockIdx.x] * wstride : wlag_all;
     double ax = 0.0, ay = 0.0, bx = 0.0, by = 0.0;
     for (int q = 0; q < KS; ++q) {
         const double2 v = __ldcs(cfar + ((int64_t)q * 64 + j) * P2 + i);
@@ -162,10 +164,11 @@ __global__ void __launch_bounds__(256) k_near_history(const double2 *__restrict_
 }
 
 int launch_near_history(cudaStream_t st, const double *ring, int64_t P, int j, const double *wlag,
-                        const double *cfar, int KS, int pairs, double *S)
+                        const double *cfar, int KS, int pairs, double *S, const int *cta_col, int64_t wstride)
 {
     k_near_history<<<(unsigned)((P / 2 + 255) / 256), 256, 0, st>>>((const double2 *)ring, P / 2, j, wlag,
-                                                                    (const double2 *)cfar, KS, pairs, (double2 *)S);
+                                                                    (const double2 *)cfar, KS, pairs, (double2 *)S,
+                                                                    cta_col, wstride);
     FPDE_LAUNCHED(1);
     return FPDE_OK;
 }

@@ -209,15 +209,18 @@ __global__ void __launch_bounds__(128) k_convert3(const double *__restrict__ rin
     }
 }
 
-// grid = (n0/64 k-tiles, 64 steps j), 64 threads: W[j][t] = w[n0 + j - t] for the k-tile.
-__global__ void __launch_bounds__(64) k_wgen3(const double *__restrict__ wlag, int n0, uint16_t *__restrict__ w0,
-                                              uint16_t *__restrict__ w1, uint16_t *__restrict__ w2, int64_t ld,
-                                              int8_t *__restrict__ pW, int64_t ldp)
+// grid = (n0/64 k-tiles, 64 steps j, columns), 64 threads: W[c*64 + j][t] = w_c[n0 + j - t]
+// for the k-tile (one weight tile per column of an ensemble; one column for a line or a grid).
+__global__ void __launch_bounds__(64) k_wgen3(const double *__restrict__ wlag_all, int64_t wstride, int n0,
+                                              uint16_t *__restrict__ w0, uint16_t *__restrict__ w1,
+                                              uint16_t *__restrict__ w2, int64_t ld, int8_t *__restrict__ pW,
+                                              int64_t ldp)
 {
     __shared__ double red[2];
-    const int kt = blockIdx.x, j = blockIdx.y;
+    const int kt = blockIdx.x, j = blockIdx.y + 64 * blockIdx.z;
+    const double *wlag = wlag_all + (int64_t)blockIdx.z * wstride;
     const int t = kt * 64 + threadIdx.x;
-    const double v = wlag[n0 + j - t];
+    const double v = wlag[n0 + (int)blockIdx.y - t];
     double m = fabs(v);
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
@@ -239,8 +242,8 @@ int launch_block_prep3(cudaStream_t st, const SplitPrep3 &p, int64_t n0)
     k_convert3<<<(unsigned)((p.nvalid + 127) / 128), 128, 0, st>>>(p.ring, p.P, p.nvalid, p.hist[0], p.hist[1],
                                                                    p.hist[2], p.ld, n0 - 64, p.pA, p.ldp, blk);
     FPDE_LAUNCHED(1);
-    dim3 g((unsigned)(n0 / 64), 64);
-    k_wgen3<<<g, 64, 0, st>>>(p.wlag, (int)n0, p.w[0], p.w[1], p.w[2], p.ld, p.pW, p.ldp);
+    dim3 g((unsigned)(n0 / 64), 64, (unsigned)(p.ncols > 0 ? p.ncols : 1));
+    k_wgen3<<<g, 64, 0, st>>>(p.wlag, p.wstride, (int)n0, p.w[0], p.w[1], p.w[2], p.ld, p.pW, p.ldp);
     FPDE_LAUNCHED(1);
     return FPDE_OK;
 }

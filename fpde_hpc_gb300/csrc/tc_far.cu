@@ -333,7 +333,7 @@ __device__ __forceinline__ float pow2f(int e)
 __global__ void __launch_bounds__(THREADS, 1)
     k_far_tc3(const __grid_constant__ FarMaps3 maps, double *__restrict__ C, int64_t ldc_split, int64_t ldc_col,
               int64_t rows, int kt_total, int kt_per, int n_split, uint32_t idesc, const int8_t *__restrict__ pA,
-              const int8_t *__restrict__ pW, int64_t ldp, unsigned *flags)
+              const int8_t *__restrict__ pW, int64_t ldp, const int *__restrict__ wcol, unsigned *flags)
 {
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
@@ -379,11 +379,11 @@ __global__ void __launch_bounds__(THREADS, 1)
                     if (!mbar_wait(&empty[s], ph ^ 1u, flags, abort_s)) { ok = false; break; }
                     uint8_t *st = stage_base + s * STAGE3_BYTES;
                     mbar_expect_tx(&full[s], STAGE3_BYTES);
-                    const int x = kt * BK, y = mt * BM;
+                    const int x = kt * BK, y = mt * BM, yw = wcol ? wcol[mt] * BN : 0;
 #pragma unroll
                     for (int q = 0; q < 3; ++q) tma_load_2d(st + q * A_BYTES, &maps.a[q], x, y, &full[s]);
 #pragma unroll
-                    for (int q = 0; q < 3; ++q) tma_load_2d(st + 3 * A_BYTES + q * W_BYTES, &maps.w[q], x, 0, &full[s]);
+                    for (int q = 0; q < 3; ++q) tma_load_2d(st + 3 * A_BYTES + q * W_BYTES, &maps.w[q], x, yw, &full[s]);
                 }
             }
             for (int it = (g > STAGES3 ? g - STAGES3 : 0); it < g; ++it) {   // own copies in flight
@@ -441,6 +441,7 @@ __global__ void __launch_bounds__(THREADS, 1)
             const int kt0 = ks * kt_per, kt1 = min(kt0 + kt_per, kt_total);
             const int64_t row = (int64_t)mt * BM + q * 32 + lane;
             const int64_t row_c = row < rows ? row : rows - 1;
+            const int8_t *pWc = pW + (wcol ? (int64_t)wcol[mt] * BN * ldp : 0);
             float hi[BN], lo[BN];
 #pragma unroll
             for (int j = 0; j < BN; ++j) { hi[j] = 0.f; lo[j] = 0.f; }
@@ -461,7 +462,7 @@ __global__ void __launch_bounds__(THREADS, 1)
                     for (int jj = 0; jj < 16; ++jj) {
                         const int j = 16 * h + jj;
                         // 2^pA * 2^pW: a product of powers of two, exact while it stays normal
-                        const float sc = sa * pow2f((int)__ldg(pW + (int64_t)j * ldp + kt));
+                        const float sc = sa * pow2f((int)__ldg(pWc + (int64_t)j * ldp + kt));
                         float x = v0[jj] * sc;                 // exact (power-of-two scaling)
                         float s = hi[j] + x, bb = s - hi[j];
                         float e = (hi[j] - (s - bb)) + (x - bb);
@@ -556,7 +557,7 @@ int far_plan_init(FarPlan *p, const void *a_hi, const void *a_lo, int64_t rows, 
 }
 
 int far_plan3_init(FarPlan3 *p, const void *const a[3], int64_t rows, int64_t lda, const void *const w[3],
-                   int64_t ldw)
+                   int64_t ldw, int w_tiles)
 {
     if (rows % tc::BM != 0 || lda % tc::BK != 0 || ldw % tc::BK != 0)
         return set_error(FPDE_ERR_ARG, "far contraction: rows must be a multiple of 128, pitches of 64");
@@ -565,7 +566,7 @@ int far_plan3_init(FarPlan3 *p, const void *const a[3], int64_t rows, int64_t ld
     int rc;
     for (int q = 0; q < 3; ++q) {
         if ((rc = tc::make_map(&m->a[q], a[q], rows, lda, tc::BM))) return rc;
-        if ((rc = tc::make_map(&m->w[q], w[q], tc::BN, ldw, tc::BN))) return rc;
+        if ((rc = tc::make_map(&m->w[q], w[q], (int64_t)tc::BN * (w_tiles > 0 ? w_tiles : 1), ldw, tc::BN))) return rc;
     }
     p->rows = rows;
     p->idesc = tc::idesc_f16(1, tc::BM, tc::BN);
@@ -580,7 +581,7 @@ int far_plan3_init(FarPlan3 *p, const void *const a[3], int64_t rows, int64_t ld
 }
 
 int far3_launch(cudaStream_t st, const FarPlan3 *p, int k_cols, double *C, int64_t ldc_split, int64_t ldc_col,
-                int splits, const int8_t *pA, const int8_t *pW, int64_t ldp, unsigned *flags)
+                int splits, const int8_t *pA, const int8_t *pW, int64_t ldp, unsigned *flags, const int *wcol)
 {
     if (k_cols % tc::BK != 0) return set_error(FPDE_ERR_ARG, "far contraction: K must be a multiple of 64");
     if (k_cols == 0) return FPDE_OK;
@@ -598,7 +599,7 @@ int far3_launch(cudaStream_t st, const FarPlan3 *p, int k_cols, double *C, int64
     const unsigned grid = (unsigned)std::min<int64_t>(items, sms);
     const tc::FarMaps3 *m = (const tc::FarMaps3 *)p->maps;
     tc::k_far_tc3<<<grid, tc::THREADS, tc::SMEM3_BYTES, st>>>(*m, C, ldc_split, ldc_col, p->rows, kt_total, kt_per,
-                                                             splits, p->idesc, pA, pW, ldp, flags);
+                                                             splits, p->idesc, pA, pW, ldp, wcol, flags);
     FPDE_LAUNCHED(1);
     return FPDE_OK;
 }

@@ -29,12 +29,16 @@ struct FarPlan3 {
     int64_t rows = 0;
     uint32_t idesc = 0;
 };
+// w_tiles: number of 64-row weight tiles in the W slices (columns of an ensemble; 1 otherwise).
 int far_plan3_init(FarPlan3 *p, const void *const a[3], int64_t rows, int64_t lda, const void *const w[3],
-                   int64_t ldw);
+                   int64_t ldw, int w_tiles = 1);
 // Writes each partial as a float pair (hi, lo) into the 8-byte slot of C (the fold's float-
 // float value; hi + lo is exact in FP64): read it with ff_to_double.
+// wcol (device, may be null): per 128-row tile the weight tile (column of an ensemble) it uses,
+// whose 64 rows start at row wcol[tile] * 64 of the W slices and of pW.
 int far3_launch(cudaStream_t st, const FarPlan3 *p, int k_cols, double *C, int64_t ldc_split, int64_t ldc_col,
-                int splits, const int8_t *pA, const int8_t *pW, int64_t ldp, unsigned *flags);
+                int splits, const int8_t *pA, const int8_t *pW, int64_t ldp, unsigned *flags,
+                const int *wcol = nullptr);
 
 // float -> double from the bits (integer instructions only; exact for every float).
 __device__ __forceinline__ double f2d_bits(float x)

@@ -99,3 +99,22 @@ def test_batch_pieces_reset_and_host_call(ctx):
     b.close()
     for x, y, z in zip(two, again, host):
         assert np.array_equal(x, y) and np.array_equal(x, z)
+
+
+@pytest.mark.parametrize("steps,tol", [(64, 1e-11), (200, 1e-7)])
+def test_batch_split_history_vs_fp64(ctx, steps, tol):
+    """Split path of the ensemble (per-column weight tiles in one tensor-core contraction, FP64
+    near history, work-queue solve) against the FP64 ensemble: within the first block the same
+    up to rounding, across blocks within 1e-7, column by column."""
+    import fpde_hpc_gb300 as fp
+    from fpde_hpc_gb300 import problems
+    cols = [_col(p) for p in problems.config5(n_cols=20, steps=steps, n_max=3000)]
+    res = []
+    for prec in (0, 3):
+        b = fp.Batch(ctx, cols, steps, precision=prec)
+        b.run(steps)
+        res.append([b.state(i) for i in range(len(cols))])
+        b.close()
+    worst = max(relmax(x, y) for x, y in zip(res[1], res[0]))
+    print(f"ensemble of {len(cols)} columns, {steps} steps, split x3 vs FP64: max rel {worst:.2e}")
+    assert worst <= tol
