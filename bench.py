@@ -510,7 +510,8 @@ def run_ours(args):
             name = "whole step (FP64 history GEMV dominant)"
         else:
             nb = steps // 64
-            alg = 6.0 * nodes * 64 * 64 * nb * (nb - 1) / 2 + 8.0 * nodes * sum(n % 64 for n in range(steps))
+            # far: every block b reads 64 b lags of 6 B per node; near: n % 64 ring rows of 8 B per step
+            alg = 6.0 * nodes * 64 * nb * (nb - 1) / 2 + 8.0 * nodes * sum(n % 64 for n in range(steps))
             name = "whole step (tensor-core far history + FP64 near history + passes)"
         gbs = alg / (ms / 1e3) / 1e9
         out["roofline"] = {"kernel": name, "bound": "hbm", "achieved": gbs,
