@@ -48,6 +48,7 @@ def parse():
     ap.add_argument("--nodes", type=int, default=None, help="override the workload's size")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64-arm", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true", help="built-in launch rules instead of fpde_line_autotune")
     return ap.parse_args()
 
 
@@ -170,14 +171,24 @@ class LineWorkload:
         import fpde_hpc_gb300 as fp
         return fp.do_weights(self.p.orders, self.p.qw, self.p.tau, n, self.p.gnorm) / self.p.tau
 
-    def build(self, ctx, prec):
+    def build(self, ctx, prec, tuning=None):
         import fpde_hpc_gb300 as fp
         p = self.p
         A, B, R = p.coefs()
         if self.do:
             return fp.Line(ctx, p.N, 0.5, p.tau, 1.0, A, B, R, p.u0, p.steps, precision=prec,
-                           lag_weights=self.weights(p.steps + 1), theta=1.0)
-        return fp.Line(ctx, p.N, p.alpha, p.tau, p.Da, A, B, R, p.u0, p.steps, precision=prec)
+                           lag_weights=self.weights(p.steps + 1), theta=1.0, tuning=tuning)
+        return fp.Line(ctx, p.N, p.alpha, p.tau, p.Da, A, B, R, p.u0, p.steps, precision=prec, tuning=tuning)
+
+    def autotune(self, ctx, prec):
+        """fpde_line_autotune for this line (partition of the solve, far split depth, GEMV splits)."""
+        import fpde_hpc_gb300 as fp
+        p = self.p
+        A, B, R = p.coefs()
+        if self.do:
+            return fp.autotune_line(ctx, p.N, 0.5, p.tau, 1.0, A, B, R, p.u0, p.steps, precision=prec,
+                                    lag_weights=self.weights(p.steps + 1), theta=1.0)
+        return fp.autotune_line(ctx, p.N, p.alpha, p.tau, p.Da, A, B, R, p.u0, p.steps, precision=prec)
 
     @property
     def u0(self):
@@ -414,7 +425,12 @@ def run_ours(args):
         raise SystemExit(f"{wl.name} runs in FP64 or the exact three-slice split")
     pname = {0: "fp64", 1: "split-bf16", 2: "split-fp16", 3: "split-bf16x3"}[prec]
 
-    obj = wl.build(ctx, prec)
+    tuning = None
+    if is_line and not args.no_autotune:
+        t0 = time.perf_counter()
+        tuning = wl.autotune(ctx, prec)
+        tune_s = time.perf_counter() - t0
+    obj = wl.build(ctx, prec, tuning) if is_line else wl.build(ctx, prec)
     u0_dev = torch.from_numpy(np.ascontiguousarray(wl.u0)).cuda()
     steps = wl.steps
     for _ in range(args.warmup):
@@ -474,6 +490,11 @@ def run_ours(args):
                       "l2": "inputs larger than L2 (the increment history, GBs, is streamed every step)",
                       "parallelism": f"replicas x{world}"},
            "e2e": e2e, "gpu_launches": int(launches), "clocks": clk}
+    if tuning is not None:
+        out["config"]["tuning"] = {"solve_sp": tuning.solve_sp, "chunks": tuning.chunks,
+                                   "far_splits": tuning.far_splits, "gemv_splits": tuning.gemv_splits,
+                                   "tuned_ms_per_step": tuning.ms_per_step, "autotune_seconds": tune_s,
+                                   "block_steps": 64}
 
     if is_line:
         # kernel rooflines from one separate probed solve (events inside the graph)
@@ -520,7 +541,8 @@ def run_ours(args):
 
     if prec != 0 and not args.no_fp64_arm:
         # the plain FP64 kernel on the same workload: speed-up and accuracy of the split path
-        l64 = wl.build(ctx, fp.FPDE_PREC_FP64)
+        t64 = wl.autotune(ctx, fp.FPDE_PREC_FP64) if (is_line and not args.no_autotune) else None
+        l64 = wl.build(ctx, fp.FPDE_PREC_FP64, t64) if is_line else wl.build(ctx, fp.FPDE_PREC_FP64)
         l64.reset(u0_dev)
         l64.run(steps)
         ms64 = _timed(l64, u0_dev, steps, 1, stream)

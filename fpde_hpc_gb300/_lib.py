@@ -18,12 +18,17 @@ class FpdeError(RuntimeError):
         self.code = code
 
 
+class LineTuning(C.Structure):
+    _fields_ = [("solve_sp", c_int), ("chunks", c_int), ("far_splits", c_int), ("gemv_splits", c_int),
+                ("ms_per_step", c_dbl)]
+
+
 class LineDesc(C.Structure):
     _fields_ = [("N", c_i64), ("alpha", c_dbl), ("tau", c_dbl), ("Da", c_dbl),
                 ("left_kind", c_int), ("left_value", c_dbl), ("right_kind", c_int),
                 ("right_value", c_dbl), ("dLN", c_dbl), ("precision", c_int), ("block", c_int),
                 ("max_steps", c_int), ("lag_weights", c_vp), ("theta", c_dbl), ("source", c_vp),
-                ("source_rows", c_int)]
+                ("source_rows", c_int), ("tuning", C.POINTER(LineTuning))]
 
 
 class Lod3dDesc(C.Structure):
@@ -52,6 +57,7 @@ _SIGS = {
     "fpde_weights_l1_lags": (c_int, [c_dbl, c_int, c_vp]),
     "fpde_gamma": (c_int, [c_dbl, P_dbl]),
     "fpde_do_weights": (c_int, [c_int, c_vp, c_vp, c_vp, c_dbl, c_int, c_vp]),
+    "fpde_line_autotune": (c_int, [c_vp, C.POINTER(LineDesc), c_vp, c_vp, c_vp, c_vp, C.POINTER(LineTuning)]),
     "fpde_batch_create": (c_int, [c_vp, C.POINTER(ColumnDesc), c_int, c_int, c_int, C.POINTER(c_vp)]),
     "fpde_batch_destroy": (c_int, [c_vp]),
     "fpde_batch_run": (c_int, [c_vp, c_int]),

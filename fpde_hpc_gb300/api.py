@@ -3,7 +3,7 @@ import ctypes as C
 
 import numpy as np
 
-from ._lib import ColumnDesc, LineDesc, Lod3dDesc, check, load
+from ._lib import ColumnDesc, LineDesc, LineTuning, Lod3dDesc, check, load
 
 FP64, SPLIT_BF16, SPLIT_F16 = 0, 1, 2
 
@@ -57,6 +57,28 @@ def do_weights(orders, qw, tau, n, gnorm=None):
     check(load().fpde_do_weights(len(a), _ptr(a), _ptr(q), None if g is None else _ptr(g), tau, n, _ptr(c)),
           "fpde_do_weights")
     return c
+
+
+def autotune_line(ctx, N, alpha, tau, Da, A, B, Rlap, u0, max_steps, left=(0, 0.0), right=(0, 0.0), dLN=0.0,
+                  precision=FP64, lag_weights=None, theta=0.0, source=None):
+    """fpde_line_autotune: the fastest launch parameters for this line (a LineTuning to pass as
+    Line(..., tuning=...))."""
+    d = LineDesc(N=N, alpha=alpha, tau=tau, Da=Da, left_kind=left[0], left_value=left[1], right_kind=right[0],
+                 right_value=right[1], dLN=dLN, precision=precision, max_steps=max_steps, theta=theta)
+    keep = []
+    if lag_weights is not None:
+        w = np.ascontiguousarray(lag_weights, dtype=np.float64)
+        keep.append(w)
+        d.lag_weights = w.ctypes.data
+    if source is not None:
+        src = np.ascontiguousarray(np.atleast_2d(source), dtype=np.float64)
+        keep.append(src)
+        d.source, d.source_rows = src.ctypes.data, src.shape[0]
+    arrs = [np.ascontiguousarray(x, dtype=np.float64) for x in (A, B, Rlap, u0)]
+    out = LineTuning()
+    check(ctx.lib.fpde_line_autotune(ctx.h, C.byref(d), *(_ptr(x) for x in arrs), C.byref(out)),
+          "fpde_line_autotune")
+    return out
 
 
 def line_coefs(k, dL, iw=None):
@@ -162,7 +184,7 @@ class Line:
     """A 1D Caputo line problem advanced on the GPU (fpde_line_*)."""
 
     def __init__(self, ctx, N, alpha, tau, Da, A, B, Rlap, u0, max_steps, left=(0, 0.0), right=(0, 0.0),
-                 dLN=0.0, precision=FP64, block=0, lag_weights=None, theta=0.0, source=None):
+                 dLN=0.0, precision=FP64, block=0, lag_weights=None, theta=0.0, source=None, tuning=None):
         """lag_weights (max_steps+1 values, w[0] local) replace the Caputo L1 weights (the
         distributed-order equation passes fused weights / tau); theta is the explicit fraction
         of the space operator; source is one row or a (rows, N+1) array of per-step rows."""
@@ -184,6 +206,9 @@ class Line:
             self._keep.append(src)
             d.source = src.ctypes.data
             d.source_rows = src.shape[0]
+        if tuning is not None:
+            self._keep.append(tuning)
+            d.tuning = C.pointer(tuning)
         self.desc = d
         arrs = [np.ascontiguousarray(x, dtype=np.float64) for x in (A, B, Rlap, u0)]
         self.h = C.c_void_p()

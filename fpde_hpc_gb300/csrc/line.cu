@@ -747,6 +747,7 @@ struct fpde_line {
     fpde_line_desc d{};
     int64_t N = 0, P = 0;
     int G = 1, s = 1, chunk = 0, max_steps = 0;
+    int far_splits = 0, gemv_splits = 0;      // tuned values (0: built-in rules)
     bool split = false;
     double lam = 0, lamR = 0, kkk0 = 0, AlN = 0;
     double *A = nullptr, *g = nullptr, *al = nullptr, *cf = nullptr, *cb = nullptr;
@@ -895,7 +896,8 @@ static int line_enqueue(fpde_line *L, cudaStream_t st, int64_t n0, int steps, in
         if (!L->split) {
             int KS = 0;
             if (n >= 1) {
-                KS = choose_splits((int)n, L->P);
+                KS = L->gemv_splits > 0 ? std::max(1, std::min<int>(L->gemv_splits, (int)std::min<int64_t>(n, KS_MAX)))
+                                        : choose_splits((int)n, L->P);
                 const double *wt = L->wrev + (L->max_steps - n);   // wt[t] = w[n - t]
                 ev = probe_step ? probe_begin(L, 0, n, 8.0 * (double)n * nodes_hist, 2.0 * n * nodes_hist) : nullptr;
                 PROBE_REC(ev, 0);
@@ -912,7 +914,8 @@ static int line_enqueue(fpde_line *L, cudaStream_t st, int64_t n0, int steps, in
             const int64_t nb0 = n - n % BLK;                     // block start
             const int j = (int)(n - nb0);
             int splits = 0;
-            if (nb0 > 0) splits = far_splits((int)(nb0 / 64), L->rows16);
+            if (nb0 > 0)
+                splits = L->far_splits > 0 ? std::min(L->far_splits, (int)(nb0 / 64)) : far_splits((int)(nb0 / 64), L->rows16);
             if (j == 0 && nb0 > 0 && L->x3) {
                 SplitPrep3 sp;
                 sp.ring = L->ring; sp.P = L->P; sp.nvalid = nodes_hist; sp.ld = L->ld16; sp.wlag = L->wlag;
@@ -1044,22 +1047,36 @@ int fpde_line_create(fpde_ctx *ctx, const fpde_line_desc *desc, const double *A,
     // keeps G within the SM count
     const bool split = d.precision != FPDE_PREC_FP64;
     const int lt = split ? LTS : LT;
+    const fpde_line_tuning *tu = d.tuning;
     int sp = 1, G = 1;
-    if (N <= (int64_t)lt * LSEG) {
-        while ((int64_t)lt * sp < N) sp <<= 1;
-    } else {
-        while (sp <= LSEG && (N + (int64_t)lt * sp - 1) / ((int64_t)lt * sp) > ctx->sm_count) sp <<= 1;
-        if (sp > LSEG)
-            return set_error(FPDE_ERR_UNSUPPORTED, "line of %lld intervals exceeds %lld (SMs x %d x %d)",
-                             (long long)N, (long long)ctx->sm_count * lt * LSEG, lt, LSEG);
-        G = (int)((N + (int64_t)lt * sp - 1) / ((int64_t)lt * sp));
-    }
-    // chunk of nodes per CTA: lt * sp, or (long lines) an even share of all SMs, rounded to sp
-    int64_t chunk = (int64_t)lt * sp;
-    if (G > 1 && N >= (int64_t)ctx->sm_count * lt) {
-        chunk = (N + ctx->sm_count - 1) / ctx->sm_count;
+    int64_t chunk;
+    if (tu && (tu->solve_sp > 0 || tu->chunks > 0)) {
+        // tuned partition: sp nodes per thread, `chunks` CTAs (or the fewest that fit)
+        sp = tu->solve_sp > 0 ? tu->solve_sp : LSEG;
+        FPDE_CHECK_ARG(sp == 1 || sp == 2 || sp == 4 || sp == 8, "tuning: solve_sp must be 1, 2, 4 or 8");
+        const int64_t gmin = (N + (int64_t)lt * sp - 1) / ((int64_t)lt * sp);
+        G = tu->chunks > 0 ? tu->chunks : (int)gmin;
+        FPDE_CHECK_ARG(G >= gmin && G <= ctx->sm_count, "tuning: chunks out of range for this line and solve_sp");
+        chunk = (N + G - 1) / G;
         chunk = (chunk + sp - 1) / sp * sp;
         G = (int)((N + chunk - 1) / chunk);
+    } else {
+        if (N <= (int64_t)lt * LSEG) {
+            while ((int64_t)lt * sp < N) sp <<= 1;
+        } else {
+            while (sp <= LSEG && (N + (int64_t)lt * sp - 1) / ((int64_t)lt * sp) > ctx->sm_count) sp <<= 1;
+            if (sp > LSEG)
+                return set_error(FPDE_ERR_UNSUPPORTED, "line of %lld intervals exceeds %lld (SMs x %d x %d)",
+                                 (long long)N, (long long)ctx->sm_count * lt * LSEG, lt, LSEG);
+            G = (int)((N + (int64_t)lt * sp - 1) / ((int64_t)lt * sp));
+        }
+        // chunk of nodes per CTA: lt * sp, or (long lines) an even share of all SMs, rounded to sp
+        chunk = (int64_t)lt * sp;
+        if (G > 1 && N >= (int64_t)ctx->sm_count * lt) {
+            chunk = (N + ctx->sm_count - 1) / ctx->sm_count;
+            chunk = (chunk + sp - 1) / sp * sp;
+            G = (int)((N + chunk - 1) / chunk);
+        }
     }
     if (G > 160) return set_error(FPDE_ERR_UNSUPPORTED, "line solve: at most 160 chunks");
     int per_sm = 0;
@@ -1076,6 +1093,11 @@ int fpde_line_create(fpde_ctx *ctx, const fpde_line_desc *desc, const double *A,
     L->G = G;
     L->s = sp;
     L->chunk = (int)chunk;
+    if (tu) {
+        L->far_splits = std::min(std::max(tu->far_splits, 0), FAR_MAX_SPLITS);
+        L->gemv_splits = std::min(std::max(tu->gemv_splits, 0), KS_MAX);
+    }
+    L->d.tuning = nullptr;                     // not kept
     L->max_steps = d.max_steps;
     L->split = split;
     L->x3 = d.precision == FPDE_PREC_SPLIT_BF16X3;
@@ -1500,3 +1522,173 @@ int fpde_line_steps_done(const fpde_line *L, int64_t *n)
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------------- autotuner
+namespace fpde {
+
+// Time `fn` (which enqueues work on st) reps times after one warm-up; ms per call.
+template <class F>
+static float time_on_stream(cudaStream_t st, int reps, F fn)
+{
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    fn();
+    cudaEventRecord(e0, st);
+    for (int r = 0; r < reps; ++r) fn();
+    cudaEventRecord(e1, st);
+    cudaEventSynchronize(e1);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return ms / reps;
+}
+
+}  // namespace fpde
+
+extern "C" int fpde_line_autotune(fpde_ctx *ctx, const fpde_line_desc *desc, const double *A, const double *B,
+                                  const double *Rlap, const double *u0, fpde_line_tuning *out)
+{
+    clear_error();
+    FPDE_CHECK_ARG(desc && A && B && Rlap && u0 && out, "null argument");
+    int rc = ctx_enter(ctx);
+    if (rc) return rc;
+    const fpde_line_desc &d = *desc;
+    const bool split = d.precision != FPDE_PREC_FP64;
+    const int lt = split ? LTS : LT;
+    const int64_t N = d.N;
+    cudaStream_t st = ctx->stream;
+    fpde_line_tuning best{};
+    double best_ms = 1e300;
+
+    // 1. partition of the solve: solve_sp x chunks, timed on the second 64-step block of a short run
+    const int tsteps = std::min(d.max_steps, 128);
+    const int first = std::min(64, tsteps / 2);
+    std::vector<std::pair<int, int>> cands;
+    for (int sp = 1; sp <= LSEG; sp <<= 1) {
+        const int64_t gmin = (N + (int64_t)lt * sp - 1) / ((int64_t)lt * sp);
+        if (gmin > ctx->sm_count) continue;
+        std::vector<int> gs = {(int)gmin};
+        if (gmin > 1) {
+            gs.push_back(ctx->sm_count);
+            gs.push_back((int)((gmin + ctx->sm_count) / 2));
+        }
+        std::sort(gs.begin(), gs.end());
+        gs.erase(std::unique(gs.begin(), gs.end()), gs.end());
+        for (int g : gs) cands.emplace_back(sp, g);
+    }
+    for (const auto &cd : cands) {
+        fpde_line_tuning t{};
+        t.solve_sp = cd.first;
+        t.chunks = cd.second;
+        fpde_line_desc td = d;
+        td.max_steps = tsteps;
+        td.tuning = &t;
+        fpde_line *L = nullptr;
+        if (fpde_line_create(ctx, &td, A, B, Rlap, u0, &L) != FPDE_OK) {   // e.g. not co-resident
+            clear_error();
+            continue;
+        }
+        bool ok = fpde_line_run(L, first) == FPDE_OK && fpde_line_run(L, tsteps - first) == FPDE_OK &&
+                  fpde_line_reset(L, u0, 0) == FPDE_OK && fpde_line_run(L, first) == FPDE_OK;
+        float ms = 0.f;
+        if (ok) {
+            cudaEvent_t e0, e1;
+            cudaEventCreate(&e0);
+            cudaEventCreate(&e1);
+            cudaEventRecord(e0, st);
+            ok = fpde_line_run(L, tsteps - first) == FPDE_OK;
+            cudaEventRecord(e1, st);
+            cudaEventSynchronize(e1);
+            cudaEventElapsedTime(&ms, e0, e1);
+            cudaEventDestroy(e0);
+            cudaEventDestroy(e1);
+        }
+        unsigned flags = 0;
+        cudaMemcpy(&flags, ctx->d_flags, sizeof flags, cudaMemcpyDeviceToHost);
+        if (flags) {                                            // a bounded wait gave up: not a candidate
+            cudaMemset(ctx->d_flags, 0, sizeof(unsigned));
+            ok = false;
+        }
+        fpde_line_destroy(L);
+        if (!ok) {
+            clear_error();
+            continue;
+        }
+        const double per = ms / (tsteps - first);
+        if (per < best_ms) {
+            best_ms = per;
+            best.solve_sp = cd.first;
+            best.chunks = cd.second;
+        }
+    }
+    if (best_ms >= 1e300) return set_error(FPDE_ERR_UNSUPPORTED, "autotune: no partition of this line could run");
+    best.ms_per_step = best_ms;
+
+    const int64_t kt_steps = std::min<int64_t>((int64_t)d.max_steps / 64 * 64, 2048);
+    if (split && d.precision == FPDE_PREC_SPLIT_BF16X3 && kt_steps >= 128) {
+        // 2. split depth of the far contraction at a history of kt_steps columns (zero data)
+        const int64_t rows = (N + 1 + 127) / 128 * 128, ldp = kt_steps / 64;
+        uint16_t *a3[3] = {nullptr, nullptr, nullptr}, *w3[3] = {nullptr, nullptr, nullptr};
+        int8_t *pA = nullptr, *pW = nullptr;
+        double *C = nullptr;
+        bool fail = false;
+        for (int q = 0; q < 3 && !fail; ++q)
+            fail = dev_alloc((void **)&a3[q], (size_t)rows * kt_steps * 2) ||
+                   dev_alloc((void **)&w3[q], (size_t)64 * kt_steps * 2);
+        fail = fail || dev_alloc((void **)&pA, (size_t)rows * ldp) || dev_alloc((void **)&pW, (size_t)64 * ldp) ||
+               dev_alloc((void **)&C, (size_t)FAR_MAX_SPLITS * 64 * rows * sizeof(double));
+        if (!fail) {
+            for (int q = 0; q < 3; ++q) {
+                cudaMemsetAsync(a3[q], 0, (size_t)rows * kt_steps * 2, st);
+                cudaMemsetAsync(w3[q], 0, (size_t)64 * kt_steps * 2, st);
+            }
+            cudaMemsetAsync(pA, 0, (size_t)rows * ldp, st);
+            cudaMemsetAsync(pW, 0, (size_t)64 * ldp, st);
+            FarPlan3 plan;
+            const void *ap[3] = {a3[0], a3[1], a3[2]}, *wp[3] = {w3[0], w3[1], w3[2]};
+            if (far_plan3_init(&plan, ap, rows, kt_steps, wp, kt_steps) == FPDE_OK) {
+                double bms = 1e300;
+                for (int s = 1; s <= FAR_MAX_SPLITS; ++s) {
+                    const float ms = time_on_stream(st, 3, [&] {
+                        far3_launch(st, &plan, (int)kt_steps, C, 64 * rows, rows, s, pA, pW, ldp, ctx->d_flags);
+                    });
+                    if (ms < bms) { bms = ms; best.far_splits = s; }
+                }
+            }
+        }
+        cudaStreamSynchronize(st);
+        for (int q = 0; q < 3; ++q) { dev_free(a3[q]); dev_free(w3[q]); }
+        dev_free(pA);
+        dev_free(pW);
+        dev_free(C);
+        clear_error();
+    }
+    if (!split) {
+        // 3. row splits of the FP64 history sum at min(max_steps, 2048) rows (zero data)
+        const int64_t P = (N + 1 + 511) / 512 * 512;
+        const int nrow = std::min(d.max_steps, 2048);
+        double *D = nullptr, *part = nullptr, *w = nullptr;
+        if (nrow >= 8 && !dev_alloc((void **)&D, (size_t)nrow * P * sizeof(double)) &&
+            !dev_alloc((void **)&part, (size_t)KS_MAX * P * sizeof(double)) &&
+            !dev_alloc((void **)&w, (size_t)nrow * sizeof(double))) {
+            cudaMemsetAsync(D, 0, (size_t)nrow * P * sizeof(double), st);
+            cudaMemsetAsync(w, 0, (size_t)nrow * sizeof(double), st);
+            const int k0 = choose_splits(nrow, P);
+            const int ks_c[3] = {std::max(1, k0 / 2), k0, std::min(KS_MAX, 2 * k0)};
+            double bms = 1e300;
+            for (int ks : ks_c) {
+                const float ms = time_on_stream(st, 3, [&] { launch_l1_partial(st, D, P, nrow, w, part, ks); });
+                if (ms < bms) { bms = ms; best.gemv_splits = ks; }
+            }
+        }
+        cudaStreamSynchronize(st);
+        dev_free(D);
+        dev_free(part);
+        dev_free(w);
+        clear_error();
+    }
+    *out = best;
+    return ctx_check_flags(ctx, "autotune");
+}

@@ -211,6 +211,17 @@ int fpde_tridiag_solve(fpde_ctx *ctx, const double *a, const double *b, const do
 
 /* ------------------------------------------------------- 1D line problem */
 
+/* Launch parameters of a line chosen by fpde_line_autotune (or by hand); 0 = the built-in rule.
+ * No counterpart in the reference, whose OpenCL path fixes one work-group shape
+ * (opencl_cuda_base.cpp:626-649). */
+typedef struct fpde_line_tuning {
+    int solve_sp;       /* nodes per solve thread: 1, 2, 4 or 8 */
+    int chunks;         /* CTAs the line is split into for the solve (at most the SM count) */
+    int far_splits;     /* K splits of the tensor-core far contraction: 1..4 (split paths) */
+    int gemv_splits;    /* row splits of the FP64 history sum: 1..64 (FP64 path) */
+    double ms_per_step; /* output of fpde_line_autotune: measured time per step of the choice */
+} fpde_line_tuning;
+
 /* A time-fractional diffusion line  D_t^alpha U = d/dx(k dU/dx) (+ source)  discretised as in
  * fpde_hpc_1d.cpp (L1 Caputo in time, implicit 3-point FD in space, Thomas per step):
  *   Om[i] = -Da*(kkk0/tau) U[i] + src[i] + Da*S[i],  R[i] = Rlap[i] + Da*kkk0/tau.
@@ -238,6 +249,7 @@ typedef struct fpde_line_desc {
     const double *source; /* host, source_rows x (N+1): step n adds row min(n, source_rows-1)
                              to Om (fr_do's -(f(t_n,x)+f(t_{n+1},x))/2; Rp of Om1) */
     int source_rows;
+    const fpde_line_tuning *tuning; /* optional launch parameters (NULL: built-in rules) */
 } fpde_line_desc;
 
 /* Set up a line: A, B, Rlap (N+1 host values, entries 1..N-1 used; see fpde_line_coefs)
@@ -272,6 +284,15 @@ int fpde_line_steps_done(const fpde_line *line, int64_t *n);
 int fpde_line_set_probe(fpde_line *line, int every);
 int fpde_line_probe_stats(fpde_line *line, int kind, double *ms, double *bytes, double *flops,
                           int *count);
+
+/* Autotuner (no counterpart in the reference): for the line that desc and the arrays describe,
+ * time candidate launch parameters on short runs and on the far contraction / FP64 history
+ * sum at a history of min(max_steps, 2048) steps, and return the fastest in *out (pass it as
+ * desc->tuning to fpde_line_create). Candidates: solve_sp x chunks (solve time per step of the
+ * second 64-step block), far_splits 1..4, gemv_splits {k/2, k, 2k} around the built-in rule k.
+ * Allocates and frees temporary device buffers; takes a fraction of a second to seconds. */
+int fpde_line_autotune(fpde_ctx *ctx, const fpde_line_desc *desc, const double *A, const double *B,
+                       const double *Rlap, const double *u0, fpde_line_tuning *out);
 
 /* Line coefficients of the H equation with gamma = 1 (A_ / B / R, fpde_hpc_1d.cpp:3095-3142):
  * A[i] = k[i-1] iw[i]/(dL[i] dL[i-1]), B[i] = k[i] iw[i]/dL[i]^2,
