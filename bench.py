@@ -388,6 +388,15 @@ def _probe(line, u0_dev, steps, every):
     return tot
 
 
+# DRAM traffic per launch from ncu captures (profiles/), as bytes per unit the launch processes:
+#   k_line_block: per node-step (79.8 MB for 64 steps x 65,537 nodes, 2 far splits)
+#   k_far_tc3   : per node x history step (629.2 MB for 65,664 rows x 1,344 steps)
+NCU_TRAFFIC = {
+    "solve_split": (79.76e6 / (64 * 65537), "profiles/k_line_block_N65536_2048steps.md"),
+    "far_tc": (629.24e6 / (65664 * 1344), "profiles/k_far_tc3_N65536_K1344.md"),
+}
+
+
 def _kernel_entry(t, name, peak, peak_src, scale=1.0):
     if t["count"] <= 0 or t["ms"] <= 0:
         return None
@@ -513,6 +522,19 @@ def run_ours(args):
             solve_name = "k_line_block (far fold + FP64 near history + Thomas, one launch per 64-step block)"
         kernels["solve"] = _kernel_entry(tot[2], solve_name, peak, peak_src, per(tot[2]))
         kernels = {k: v for k, v in kernels.items() if v}
+        if prec == fp.FPDE_PREC_SPLIT_BF16X3 and not wl.do:   # traffic per launch, scaled to this line
+            nodes = wl.p.N + 1
+            if "solve" in kernels:
+                per, src = NCU_TRAFFIC["solve_split"]
+                kernels["solve"]["traffic"] = per * nodes
+                kernels["solve"]["traffic_unit"] = "bytes per step (ncu, scaled by nodes)"
+                kernels["solve"]["traffic_source"] = src
+            if "far_tc" in kernels:
+                per, src = NCU_TRAFFIC["far_tc"]
+                avg_k = 64 * (steps // 64 - 1) / 2.0
+                kernels["far_tc"]["traffic"] = per * nodes * avg_k
+                kernels["far_tc"]["traffic_unit"] = "bytes per launch at the average history (ncu, scaled)"
+                kernels["far_tc"]["traffic_source"] = src
         est = {k: v["est_ms_per_solve"] for k, v in kernels.items()}
         tot_est = sum(est.values())
         for k, v in kernels.items():
