@@ -311,6 +311,8 @@ __global__ void __launch_bounds__(THREADS, 1)
 // float-float every k-tile. The leading product is therefore free of accumulation error,
 // whatever the rounding of the tensor core's FP32 adder.
 constexpr int STAGES3 = 3;
+constexpr int THREADS3 = 64 + 8 * 32;                         // TMA warp, MMA warp, 8 epilogue warps
+constexpr int EPI_COLS = BN / 2;                              // columns per epilogue warp
 constexpr int STAGE3_BYTES = 3 * A_BYTES + 3 * W_BYTES;      // 72 KB
 constexpr int TMEM3_COLS = 256;                               // 2 buffers x (X0, X12)
 constexpr int SMEM3_BYTES = 1024 + STAGES3 * STAGE3_BYTES + 256;
@@ -330,7 +332,7 @@ __device__ __forceinline__ float pow2f(int e)
 // epilogue follow the same static sequence of k-tiles, so the pipeline runs on across item
 // boundaries and TMEM is allocated once. Every item writes its partial (zeros if its k range
 // is empty).
-__global__ void __launch_bounds__(THREADS, 1)
+__global__ void __launch_bounds__(THREADS3, 1)
     k_far_tc3(const __grid_constant__ FarMaps3 maps, double *__restrict__ C, int64_t ldc_split, int64_t ldc_col,
               int64_t rows, int kt_total, int kt_per, int n_split, uint32_t idesc, const int8_t *__restrict__ pA,
               const int8_t *__restrict__ pW, int64_t ldp, const int *__restrict__ wcol, unsigned *flags)
@@ -350,7 +352,7 @@ __global__ void __launch_bounds__(THREADS, 1)
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < STAGES3; ++s) { mbar_init(&full[s], 1); mbar_init(&empty[s], 1); }
-        for (int b = 0; b < 2; ++b) { mbar_init(&tfull[b], 1); mbar_init(&tempty[b], 128); }
+        for (int b = 0; b < 2; ++b) { mbar_init(&tfull[b], 1); mbar_init(&tempty[b], 256); }
         mbar_init(mma_done, 1);
         *abort_s = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -433,7 +435,10 @@ __global__ void __launch_bounds__(THREADS, 1)
             while (!mbar_try_wait(mma_done, 0) && gtimer() - t0 < WAIT_NS) {}
         }
     } else {
-        const int q = warp & 3;                            // TMEM lane quadrant
+        // 8 epilogue warps: warp w reads TMEM lane quadrant w % 4 (the hardware's rule) and
+        // folds columns [c0, c0 + 32) with c0 = 32 * ((w - 2) / 4)
+        const int q = warp & 3;
+        const int c0 = EPI_COLS * ((warp - 2) >> 2);
         int g = 0;
         bool ok = true;
         for (int item = blockIdx.x; item < n_items && ok; item += gridDim.x) {
@@ -441,19 +446,19 @@ __global__ void __launch_bounds__(THREADS, 1)
             const int kt0 = ks * kt_per, kt1 = min(kt0 + kt_per, kt_total);
             const int64_t row = (int64_t)mt * BM + q * 32 + lane;
             const int64_t row_c = row < rows ? row : rows - 1;
-            const int8_t *pWc = pW + (wcol ? (int64_t)wcol[mt] * BN * ldp : 0);
-            float hi[BN], lo[BN];
+            const int8_t *pWc = pW + (wcol ? (int64_t)wcol[mt] * BN * ldp : 0) + (int64_t)c0 * ldp;
+            float hi[EPI_COLS], lo[EPI_COLS];
 #pragma unroll
-            for (int j = 0; j < BN; ++j) { hi[j] = 0.f; lo[j] = 0.f; }
+            for (int j = 0; j < EPI_COLS; ++j) { hi[j] = 0.f; lo[j] = 0.f; }
             for (int kt = kt0; kt < kt1; ++kt, ++g) {
                 const int buf = g & 1;
                 const uint32_t use = (uint32_t)(g >> 1);
                 if (!mbar_wait(&tfull[buf], use & 1u, flags, abort_s)) { ok = false; break; }
                 tc_fence_after();
                 const float sa = pow2f((int)pA[row_c * ldp + kt]);
-                const uint32_t tb = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(buf * 2 * BN);
+                const uint32_t tb = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(buf * 2 * BN + c0);
 #pragma unroll
-                for (int h = 0; h < BN / 16; ++h) {
+                for (int h = 0; h < EPI_COLS / 16; ++h) {
                     float v0[16], v1[16];
                     tmem_ld16(tb + 16 * h, v0);
                     tmem_ld16(tb + BN + 16 * h, v1);
@@ -480,9 +485,9 @@ __global__ void __launch_bounds__(THREADS, 1)
                 mbar_arrive(&tempty[buf]);
             }
             if (ok && row < rows) {                   // float pairs: no FP64 work here
-                float2 *out = reinterpret_cast<float2 *>(C + (int64_t)ks * ldc_split + row);
+                float2 *out = reinterpret_cast<float2 *>(C + (int64_t)ks * ldc_split + row) + (int64_t)c0 * ldc_col;
 #pragma unroll
-                for (int j = 0; j < BN; ++j) out[(int64_t)j * ldc_col] = make_float2(hi[j], lo[j]);
+                for (int j = 0; j < EPI_COLS; ++j) out[(int64_t)j * ldc_col] = make_float2(hi[j], lo[j]);
             }
         }
     }
@@ -598,7 +603,7 @@ int far3_launch(cudaStream_t st, const FarPlan3 *p, int k_cols, double *C, int64
     }
     const unsigned grid = (unsigned)std::min<int64_t>(items, sms);
     const tc::FarMaps3 *m = (const tc::FarMaps3 *)p->maps;
-    tc::k_far_tc3<<<grid, tc::THREADS, tc::SMEM3_BYTES, st>>>(*m, C, ldc_split, ldc_col, p->rows, kt_total, kt_per,
+    tc::k_far_tc3<<<grid, tc::THREADS3, tc::SMEM3_BYTES, st>>>(*m, C, ldc_split, ldc_col, p->rows, kt_total, kt_per,
                                                              splits, p->idesc, pA, pW, ldp, wcol, flags);
     FPDE_LAUNCHED(1);
     return FPDE_OK;
