@@ -354,7 +354,7 @@ struct LineBlockArgs {
     int far_pairs;                        // 1: partials are float pairs (three-slice contraction)
     int64_t P;
     const double *wlag;                   // w[lag]
-    double *agg;                          // [2][2G+2] aggregates by step parity
+    double *agg;                          // [nsteps][2G+2] aggregates, one row of slots per step
     double *halo;                         // [2][2G+2] chunk edge states by step parity
     unsigned long long *cflag, *hflag, *seq;
     const double *Lf, *Mb, *Kb, *mb;
@@ -370,6 +370,21 @@ __device__ __forceinline__ unsigned long long ld_acquire(const unsigned long lon
     unsigned long long v;
     asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(f) : "memory");
     return v;
+}
+
+constexpr unsigned long long SLOT_EMPTY = ~0ull;        // exchange slot not yet written (a NaN pattern)
+
+__device__ __forceinline__ unsigned long long ld_relaxed_u64(const double *p)
+{
+    unsigned long long v;
+    asm volatile("ld.relaxed.gpu.global.b64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ void st_relaxed_f64(double *p, double v)
+{
+    asm volatile("st.relaxed.gpu.global.b64 [%0], %1;" ::"l"(p), "l"((unsigned long long)__double_as_longlong(v))
+                 : "memory");
 }
 
 __device__ __forceinline__ bool wait_flag(const unsigned long long *f, unsigned long long tag,
@@ -535,7 +550,7 @@ __global__ void __launch_bounds__(2 * LTS, 1) k_line_block(LineBlockArgs p)
         const int j = p.j0 + s;
         const int64_t n = p.n0 + s;
         const unsigned long long tag = base + (unsigned long long)s + 1;
-        double *agg = p.agg + (size_t)(tag & 1ull) * (2 * G + 2);
+        double *agg = p.agg + (size_t)s * (2 * G + 2);       // this step's slots (all bits set until written)
         // ---- right-hand side: history (newest row added here) + local term (+ explicit part)
         double om[SP];
         const double *src = p.src ? p.src + (int64_t)(n < p.src_rows ? n : p.src_rows - 1) * (N + 1) : nullptr;
@@ -559,7 +574,7 @@ __global__ void __launch_bounds__(2 * LTS, 1) k_line_block(LineBlockArgs p)
                 }
             }
         }
-        if (ownsN && p.rkind != FPDE_BC_DIRICHLET) agg[2 * G] = u[cnt - 1];    // old U[N-1], flux closure
+        if (ownsN && p.rkind != FPDE_BC_DIRICHLET) st_relaxed_f64(agg + 2 * G, u[cnt - 1]);  // old U[N-1], flux
         // ---- forward: segment sweep from zero carry, warp scan, warp totals
         double y[SP];
         double yl = 0.0;
@@ -593,7 +608,7 @@ __global__ void __launch_bounds__(2 * LTS, 1) k_line_block(LineBlockArgs p)
             for (int k = 0; k < SP; ++k)
                 if (k < cnt) y[k] = fma(kcf[k], carry, y[k]);
         }
-        if (cnt > 0 && i1 == b) agg[2 * c] = y[cnt - 1];   // the chunk's last y (zero carry-in)
+        if (cnt > 0 && i1 == b) st_relaxed_f64(agg + 2 * c, y[cnt - 1]);   // the chunk's last y (zero carry-in)
         // ---- backward: segment sweep from zero carry, warp scan, warp totals
         double ub[SP];
         double ul = 0.0;
@@ -626,42 +641,47 @@ __global__ void __launch_bounds__(2 * LTS, 1) k_line_block(LineBlockArgs p)
             for (int k = 0; k < SP; ++k)
                 if (k < cnt) ub[k] = fma(kcb[k], carry, ub[k]);
         }
-        // The chunk's first u, then the release: barrier (B) orders the last-y write of the other
-        // thread before this release, which is cumulative at gpu scope.
-        if (tid == 0) {
-            agg[2 * c + 1] = ub[0];
-            if (G > 1) asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p.cflag + c), "l"(tag) : "memory");
-        }
-        // ---- warp 0: every chunk's aggregates (one polling round for all flags), carries
+        if (tid == 0) st_relaxed_f64(agg + 2 * c + 1, ub[0]);   // the chunk's first u (zero carries)
+        // ---- warp 0: every chunk's aggregates, polled as values: each slot is written once per
+        // launch and holds the all-bits-set pattern until then (a NaN no arithmetic produces);
+        // a 64-bit load is single-copy atomic, so a slot that differs from it is the final value
         if (warp == 0) {
+            double ye[5], u0[5], uNm1 = 0.0;
             bool ok = true;
-            if (G > 1) {
-                const unsigned long long t0 = gtimer_ns();
-                while (true) {
-                    bool mine = true;
+            const bool need_nm1 = p.rkind != FPDE_BC_DIRICHLET;
+            const unsigned long long t0 = gtimer_ns();
+            while (true) {
+                bool mine = true;
 #pragma unroll
-                    for (int t = 0; t < 5; ++t) {
-                        const int q = lane + 32 * t;
-                        if (q < G && ld_acquire(p.cflag + q) < tag) mine = false;
+                for (int t = 0; t < 5; ++t) {
+                    const int q = lane + 32 * t;
+                    ye[t] = 0.0;
+                    u0[t] = 0.0;
+                    if (q < G) {
+                        const unsigned long long by = ld_relaxed_u64(agg + 2 * q), bu = ld_relaxed_u64(agg + 2 * q + 1);
+                        if (by == SLOT_EMPTY || bu == SLOT_EMPTY) mine = false;
+                        ye[t] = __longlong_as_double((long long)by);
+                        u0[t] = __longlong_as_double((long long)bu);
                     }
-                    if (__all_sync(FULL, mine)) break;
-                    if (gtimer_ns() - t0 > 1000000000ull) { ok = false; break; }
                 }
-                ok = __all_sync(FULL, ok);
+                if (need_nm1 && lane == 0) {
+                    const unsigned long long bn = ld_relaxed_u64(agg + 2 * G);
+                    if (bn == SLOT_EMPTY) mine = false;
+                    uNm1 = __longlong_as_double((long long)bn);
+                }
+                if (__all_sync(FULL, mine)) break;
+                if (gtimer_ns() - t0 > 1000000000ull) { ok = false; break; }
             }
+            ok = __all_sync(FULL, ok);
             if (!ok) {
                 if (lane == 0) { atomicOr(p.flags, DEVERR_BARRIER_TIMEOUT); s_abort = 1; }
             } else {
                 double sc = 0.0, syN = 0.0, sub = 0.0;
 #pragma unroll
                 for (int t = 0; t < 5; ++t) {
-                    const int q = lane + 32 * t;
-                    if (q < G) {
-                        const double ye = __ldcg(agg + 2 * q), u0 = __ldcg(agg + 2 * q + 1);
-                        sc = fma(lf[t], ye, sc);
-                        syN = fma(lfN[t], ye, syN);
-                        sub = fma(mbv[t], u0, fma(kbv[t], ye, sub));
-                    }
+                    sc = fma(lf[t], ye[t], sc);
+                    syN = fma(lfN[t], ye[t], syN);
+                    sub = fma(mbv[t], u0[t], fma(kbv[t], ye[t], sub));
                 }
 #pragma unroll
                 for (int o = 16; o > 0; o >>= 1) {
@@ -672,8 +692,7 @@ __global__ void __launch_bounds__(2 * LTS, 1) k_line_block(LineBlockArgs p)
                 double uN;                               // right end (U1 :4685-4719)
                 if (p.rkind == FPDE_BC_DIRICHLET) {
                     uN = p.gN;
-                } else {
-                    const double uNm1 = __ldcg(agg + 2 * G);
+                } else {                                 // lane 0 holds the old U[N-1]
                     if (fabs(syN) > 1e-15) uN = (fabs(1.0 - p.AlN) > 1e-15) ? (syN + p.gN * p.dLN) / (1.0 - p.AlN) : uNm1;
                     else uN = (fabs(1.0 - p.AlN) > 1e-15) ? 0.0 : uNm1;
                 }
@@ -868,6 +887,8 @@ static int line_launch_block(fpde_line *L, cudaStream_t st, int64_t nb0, int j0,
     attr[0].val.cooperative = L->G > 1 ? 1 : 0;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
+    // the launch's exchange slots start as SLOT_EMPTY (all bits set)
+    FPDE_CUDA(cudaMemsetAsync(L->agg, 0xFF, (size_t)nsteps * (2 * L->G + 2) * sizeof(double), st));
     cudaError_t e;
     switch (L->s) {
     case 1: e = launch_block_sp<1>(cfg, a); break;
@@ -1241,7 +1262,7 @@ int fpde_line_create(fpde_ctx *ctx, const fpde_line_desc *desc, const double *A,
                 dev_alloc((void **)&L->seq, sizeof(unsigned long long)) ||
                 dev_alloc((void **)&L->U, L->P * sizeof(double)) ||
                 dev_alloc((void **)&L->wrev, wrev.size() * sizeof(double)) ||
-                dev_alloc((void **)&L->agg, 2 * (2 * G + 2) * sizeof(double)) ||
+                dev_alloc((void **)&L->agg, (size_t)BLK * (2 * G + 2) * sizeof(double)) ||
                 dev_alloc((void **)&L->halo, 2 * (2 * G + 2) * sizeof(double)) ||
                 dev_alloc((void **)&L->hflag, (size_t)G * sizeof(unsigned long long)) ||
                 (split && (dev_alloc((void **)&L->sclane, hsl.size() * sizeof(double)) ||
