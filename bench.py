@@ -198,10 +198,11 @@ class LineWorkload:
     def steps(self):
         return self.p.steps
 
-    def cpu_rate(self, threads, s1=48, s2=144):
+    def cpu_rate(self, threads, s1=512, s2=1536):
         os.environ["OMP_NUM_THREADS"] = str(threads)
         oracle = _oracle()
         p = self.p
+        s1, s2 = min(s1, p.steps // 3), min(s2, p.steps)
         A, B, R = p.coefs()
         ts = []
         w = self.weights_host(s2 + 1) if self.do else None
