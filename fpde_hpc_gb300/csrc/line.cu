@@ -359,6 +359,7 @@ struct LineBlockArgs {
     unsigned long long *cflag, *hflag, *seq;
     const double *Lf, *Mb, *Kb, *mb;
     ScanCoef sc;
+    const double *RB1, *RB2, *RY1, *RY2;  // speculative kernel: sweep responses to E1, E2
     unsigned *flags;
     double lam, g0, gN, dLN, AlN;
     int64_t n0;                           // global index of step j0
@@ -757,6 +758,330 @@ __global__ void __launch_bounds__(2 * LTS, 1) k_line_block(LineBlockArgs p)
     if (c == 0 && tid == 0) *((volatile unsigned long long *)p.seq) = base + (unsigned long long)p.nsteps;
 }
 
+
+// ---------------------------------------------------------------------------------------
+// Speculative form of the block solve (split path, no explicit part). Everything in a step is
+// linear, so step t+1's right-hand side is known up to step t's two chunk carries:
+//   Om^{t+1} = Omega0 + c_in E1 + u_b E2,   E1 = (w1 - lam) GG,  E2 = (w1 - lam) CB,
+//   Omega0   = (w1 - lam) ub_t - w1 u^t + src + H_{t+1} + w2 D_{t-1}
+// (ub_t: the chunk's zero-carry backward result of step t, H: far partials plus every history
+// row but the two newest). The solver warps therefore run step t+1's sweeps and scans on
+// Omega0 while step t's aggregates are exchanged, and correct them afterwards with the
+// time-invariant chunk-local responses to E1, E2 (RB: backward, RY: forward at the chunk's last
+// node). Per step the critical path is: carries of step t -> corrected aggregates of step t+1
+// published -> exchange; the sweeps of the next step fill the exchange's latency.
+template <int SP>
+__global__ void __launch_bounds__(2 * LTS, 1) k_line_block_spec(LineBlockArgs p)
+{
+    __shared__ double sS[2][LTS * SP];                   // H_t by parity of t
+    __shared__ double wXf[NWS], wXb[NWS];
+    __shared__ double sCf[NWS][NWS], sCb[NWS][NWS];
+    __shared__ double s_cin, s_ub, s_UN;
+    __shared__ int s_abort;
+    const int tid = threadIdx.x;
+    const bool solver = tid < LTS;
+    const int c = blockIdx.x, G = p.G, N = p.N;
+    const int a = c * p.chunk;
+    const int b = min(a + p.chunk, N);
+    const int jend = p.j0 + p.nsteps;
+    if (tid == 0) s_abort = 0;
+    if (tid < NWS * NWS) {
+        const double *wc = p.sc.warp + (size_t)c * (2 * NWS * NWS);
+        sCf[tid / NWS][tid % NWS] = wc[tid];
+        sCb[tid / NWS][tid % NWS] = wc[NWS * NWS + tid];
+    }
+
+    if (!solver) {
+        // ============== history warps: H_t = far^t + sum_{0 <= r <= t-3} w[t-r] D_r
+        const int ht = tid - LTS;
+        history_sum<SP>(p, ht, a, b, p.j0, max(p.j0 - 2, 0), sS[p.j0 & 1]);
+        if (p.j0 + 1 < jend) history_sum<SP>(p, ht, a, b, p.j0 + 1, max(p.j0 - 1, 0), sS[(p.j0 + 1) & 1]);
+        __syncthreads();                                                    // start
+        for (int s = 0; s < p.nsteps; ++s) {
+            __syncthreads();                                                // X(s): row t-1 is in the ring
+            if (s_abort) return;
+            const int t = p.j0 + s;
+            if (t + 2 < jend) history_sum<SP>(p, ht, a, b, t + 2, t, sS[t & 1]);
+        }
+        return;
+    }
+
+    // ===================================================================== solver warps
+    const int lane = tid & 31, warp = tid >> 5;
+    const int i0 = a + tid * SP;
+    const int i1 = min(i0 + SP, b);
+    const int cnt = max(0, i1 - i0);
+    double PF[5], PB[5], PeF, PeB;
+    {
+        const int64_t T = (int64_t)c * LTS + tid, GT = (int64_t)G * LTS;
+#pragma unroll
+        for (int k = 0; k < 5; ++k) {
+            PF[k] = __ldg(p.sc.lane + k * GT + T);
+            PB[k] = __ldg(p.sc.lane + (6 + k) * GT + T);
+        }
+        PeF = __ldg(p.sc.lane + 5 * GT + T);
+        PeB = __ldg(p.sc.lane + 11 * GT + T);
+    }
+    double lf[5], lfN[5], mbv[5], kbv[5], mbc = 0.0;
+    if (warp == 0) {
+#pragma unroll
+        for (int t = 0; t < 5; ++t) {
+            const int q = lane + 32 * t;
+            const bool in = q < G;
+            lf[t] = in ? __ldg(p.Lf + (int64_t)c * G + q) : 0.0;
+            lfN[t] = in ? __ldg(p.Lf + (int64_t)G * G + q) : 0.0;
+            mbv[t] = in ? __ldg(p.Mb + (int64_t)c * G + q) : 0.0;
+            kbv[t] = in ? __ldg(p.Kb + (int64_t)c * G + q) : 0.0;
+        }
+        mbc = __ldg(p.mb + c);
+    }
+    double u[SP], kA[SP], kg[SP], kal[SP], kcf[SP], kcb[SP], kCB[SP], kGG[SP], rb1[SP], rb2[SP];
+    double dm1[SP], dm2[SP];                             // D_{t-1}, D_{t-2}
+#pragma unroll
+    for (int k = 0; k < SP; ++k) {
+        const bool in = k < cnt;
+        const int i = in ? i0 + k : 0;
+        u[k] = in ? p.U[i] : 0.0;
+        kA[k] = in ? __ldg(p.A + i) : 0.0;
+        kg[k] = in ? __ldg(p.g + i) : 0.0;
+        kal[k] = in ? __ldg(p.al + i) : 0.0;
+        kcf[k] = in ? __ldg(p.cf + i) : 0.0;
+        kcb[k] = in ? __ldg(p.cb + i) : 0.0;
+        kCB[k] = in ? __ldg(p.CB + i) : 0.0;
+        kGG[k] = in ? __ldg(p.GG + i) : 0.0;
+        rb1[k] = in ? __ldg(p.RB1 + i) : 0.0;
+        rb2[k] = in ? __ldg(p.RB2 + i) : 0.0;
+        dm1[k] = (in && p.j0 >= 1) ? p.ring[(int64_t)(p.j0 - 1) * p.P + i] : 0.0;
+        dm2[k] = (in && p.j0 >= 2) ? p.ring[(int64_t)(p.j0 - 2) * p.P + i] : 0.0;
+    }
+    const bool ownsN = cnt > 0 && i1 == N;
+    const bool last = cnt > 0 && i1 == b;                // owns the chunk's last node
+    const double ry1 = last ? __ldg(p.RY1 + i1 - 1) : 0.0, ry2 = last ? __ldg(p.RY2 + i1 - 1) : 0.0;
+    double uNv = ownsN ? p.U[N] : 0.0;
+    const double lam = p.lam, w1 = __ldg(p.wlag + 1), w2 = __ldg(p.wlag + 2);
+
+    double om[SP], yv[SP], ubw[SP];
+    // chunk-local zero-carry sweeps of om: forward y (+ scans), backward ub (+ scans)
+    auto sweeps = [&]() {
+        double yl = 0.0;
+#pragma unroll
+        for (int k = 0; k < SP; ++k) {
+            if (k < cnt) {
+                if (i0 + k == 0) yl = p.g0;
+                else yl = kg[k] * (kA[k] * yl - om[k]);
+                yv[k] = yl;
+            }
+        }
+        double X = cnt > 0 ? yl : 0.0;
+#pragma unroll
+        for (int k = 0; k < 5; ++k) {
+            const double Xp = __shfl_up_sync(FULL, X, 1 << k);
+            if (lane >= (1 << k)) X = fma(PF[k], Xp, X);
+        }
+        double Xe = __shfl_up_sync(FULL, X, 1);
+        if (lane == 0) Xe = 0.0;
+        if (lane == 31) wXf[warp] = X;
+        solver_sync();                                                      // (A)
+        {
+            double x0 = 0.0, x1 = 0.0;
+#pragma unroll
+            for (int w = 0; w < NWS; w += 2) {
+                if (w < warp) x0 = fma(sCf[warp][w], wXf[w], x0);
+                if (w + 1 < warp) x1 = fma(sCf[warp][w + 1], wXf[w + 1], x1);
+            }
+            const double carry = fma(PeF, x0 + x1, Xe);
+#pragma unroll
+            for (int k = 0; k < SP; ++k)
+                if (k < cnt) yv[k] = fma(kcf[k], carry, yv[k]);
+        }
+        double ul = 0.0;
+#pragma unroll
+        for (int k = SP - 1; k >= 0; --k) {
+            if (k < cnt) {
+                ul = fma(kal[k], ul, yv[k]);
+                ubw[k] = ul;
+            }
+        }
+        X = cnt > 0 ? ul : 0.0;
+#pragma unroll
+        for (int k = 0; k < 5; ++k) {
+            const double Xn = __shfl_down_sync(FULL, X, 1 << k);
+            if (lane + (1 << k) < 32) X = fma(PB[k], Xn, X);
+        }
+        Xe = __shfl_down_sync(FULL, X, 1);
+        if (lane == 31) Xe = 0.0;
+        if (lane == 0) wXb[warp] = X;
+        solver_sync();                                                      // (B)
+        {
+            double x0 = 0.0, x1 = 0.0;
+#pragma unroll
+            for (int w = 0; w < NWS; w += 2) {
+                if (w > warp) x0 = fma(sCb[warp][w], wXb[w], x0);
+                if (w + 1 > warp) x1 = fma(sCb[warp][w + 1], wXb[w + 1], x1);
+            }
+            const double carry = fma(PeB, x0 + x1, Xe);
+#pragma unroll
+            for (int k = 0; k < SP; ++k)
+                if (k < cnt) ubw[k] = fma(kcb[k], carry, ubw[k]);
+        }
+    };
+    // warp 0: step t's aggregates of every chunk (polled values), this chunk's carries
+    auto gather = [&](int s) {
+        if (warp != 0) return;
+        const double *agg = p.agg + (size_t)s * (2 * G + 2);
+        double ye[5], u0[5], uNm1 = 0.0;
+        bool ok = true;
+        const bool need_nm1 = p.rkind != FPDE_BC_DIRICHLET;
+        const unsigned long long t0 = gtimer_ns();
+        while (true) {
+            bool mine = true;
+#pragma unroll
+            for (int t = 0; t < 5; ++t) {
+                const int q = lane + 32 * t;
+                ye[t] = 0.0;
+                u0[t] = 0.0;
+                if (q < G) {
+                    const unsigned long long by = ld_relaxed_u64(agg + 2 * q), bu = ld_relaxed_u64(agg + 2 * q + 1);
+                    if (by == SLOT_EMPTY || bu == SLOT_EMPTY) mine = false;
+                    ye[t] = __longlong_as_double((long long)by);
+                    u0[t] = __longlong_as_double((long long)bu);
+                }
+            }
+            if (need_nm1 && lane == 0) {
+                const unsigned long long bn = ld_relaxed_u64(agg + 2 * G);
+                if (bn == SLOT_EMPTY) mine = false;
+                uNm1 = __longlong_as_double((long long)bn);
+            }
+            if (__all_sync(FULL, mine)) break;
+            if (gtimer_ns() - t0 > 1000000000ull) { ok = false; break; }
+        }
+        ok = __all_sync(FULL, ok);
+        if (!ok) {
+            if (lane == 0) { atomicOr(p.flags, DEVERR_BARRIER_TIMEOUT); s_abort = 1; }
+            return;
+        }
+        double sc = 0.0, syN = 0.0, s1 = 0.0, s2 = 0.0;
+#pragma unroll
+        for (int t = 0; t < 5; ++t) {
+            sc = fma(lf[t], ye[t], sc);
+            syN = fma(lfN[t], ye[t], syN);
+            s1 = fma(mbv[t], u0[t], s1);
+            s2 = fma(kbv[t], ye[t], s2);
+        }
+        double sub = s1 + s2;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            sc += __shfl_xor_sync(FULL, sc, o);
+            syN += __shfl_xor_sync(FULL, syN, o);
+            sub += __shfl_xor_sync(FULL, sub, o);
+        }
+        double uN;                                       // right end (U1 :4685-4719)
+        if (p.rkind == FPDE_BC_DIRICHLET) {
+            uN = p.gN;
+        } else {                                         // lane 0 holds the old U[N-1]
+            if (fabs(syN) > 1e-15) uN = (fabs(1.0 - p.AlN) > 1e-15) ? (syN + p.gN * p.dLN) / (1.0 - p.AlN) : uNm1;
+            else uN = (fabs(1.0 - p.AlN) > 1e-15) ? 0.0 : uNm1;
+        }
+        if (lane == 0) { s_cin = sc; s_ub = fma(mbc, uN, sub); s_UN = uN; }
+    };
+    auto src_row = [&](int64_t n) -> const double * {
+        return p.src ? p.src + (int64_t)(n < p.src_rows ? n : p.src_rows - 1) * (N + 1) : nullptr;
+    };
+
+    __syncthreads();                                                        // start: H_j0, H_j0+1 ready
+    // ---- prologue: step j0 from its full right-hand side
+    {
+        const double *src = src_row(p.n0);
+        const double *hs = sS[p.j0 & 1];
+#pragma unroll
+        for (int k = 0; k < SP; ++k) {
+            const double S = k < cnt ? fma(w1, dm1[k], fma(w2, dm2[k], hs[i0 - a + k])) : 0.0;
+            om[k] = (-(lam * u[k]) + ((src && k < cnt) ? __ldg(src + i0 + k) : 0.0)) + S;
+        }
+        sweeps();
+        double *agg = p.agg;
+        if (ownsN && p.rkind != FPDE_BC_DIRICHLET) st_relaxed_f64(agg + 2 * G, u[cnt - 1]);
+        if (last) st_relaxed_f64(agg + 2 * c, yv[cnt - 1]);
+        if (tid == 0) st_relaxed_f64(agg + 2 * c + 1, ubw[0]);
+    }
+    double ubc[SP], ubp[SP], ubprev[SP];                 // ub_t corrected, ub'_{t+1}, ub_{t-1}
+#pragma unroll
+    for (int k = 0; k < SP; ++k) { ubc[k] = ubw[k]; ubp[k] = 0.0; ubprev[k] = 0.0; }
+    double ypl = 0.0;                                    // y'_{t+1} at the chunk's last node
+    for (int s = 0; s < p.nsteps; ++s) {
+        const int t = p.j0 + s;
+        if (s > 0) {
+            // ---- carries of step t-1: state u^t, increment D_{t-1}; step t's corrected results
+            const double cin = s_cin, ubv = s_ub;
+#pragma unroll
+            for (int k = 0; k < SP; ++k) {
+                if (k < cnt) {
+                    const double un = fma(kCB[k], ubv, fma(kGG[k], cin, ubprev[k]));
+                    const double d = un - u[k];
+                    p.ring[(int64_t)(t - 1) * p.P + i0 + k] = d;
+                    dm2[k] = dm1[k];
+                    dm1[k] = d;
+                    u[k] = un;
+                    ubc[k] = fma(rb2[k], ubv, fma(rb1[k], cin, ubp[k]));
+                }
+            }
+            if (ownsN) {
+                const double UN = s_UN;
+                p.ring[(int64_t)(t - 1) * p.P + N] = UN - uNv;
+                uNv = UN;
+            }
+            double *agg = p.agg + (size_t)s * (2 * G + 2);
+            if (ownsN && p.rkind != FPDE_BC_DIRICHLET) st_relaxed_f64(agg + 2 * G, u[cnt - 1]);
+            if (last) st_relaxed_f64(agg + 2 * c, fma(ry2, ubv, fma(ry1, cin, ypl)));
+            if (tid == 0) st_relaxed_f64(agg + 2 * c + 1, ubc[0]);
+        }
+        __syncthreads();                                                    // X(s)
+        if (t + 1 < jend) {
+            // ---- step t+1 on Omega0, while the aggregates of step t are exchanged
+            const double *src = src_row(p.n0 + s + 1);
+            const double *hs = sS[(t + 1) & 1];
+#pragma unroll
+            for (int k = 0; k < SP; ++k) {
+                om[k] = 0.0;
+                if (k < cnt) {
+                    const double h = fma(w2, dm1[k], hs[i0 - a + k]) + (src ? __ldg(src + i0 + k) : 0.0);
+                    om[k] = fma(w1 - lam, ubc[k], fma(-w1, u[k], h));
+                }
+            }
+            sweeps();
+            ypl = last ? yv[cnt - 1] : 0.0;
+#pragma unroll
+            for (int k = 0; k < SP; ++k) ubp[k] = ubw[k];
+        }
+        gather(s);
+        solver_sync();                                                      // (D)
+        if (s_abort) {
+            if (s + 1 < p.nsteps) __syncthreads();      // release the history warps at X(s+1)
+            return;
+        }
+#pragma unroll
+        for (int k = 0; k < SP; ++k) ubprev[k] = ubc[k];
+    }
+    // ---- carries of the last step: the final state and increment
+    {
+        const int t = jend;
+        const double cin = s_cin, ubv = s_ub;
+#pragma unroll
+        for (int k = 0; k < SP; ++k) {
+            if (k < cnt) {
+                const double un = fma(kCB[k], ubv, fma(kGG[k], cin, ubprev[k]));
+                p.ring[(int64_t)(t - 1) * p.P + i0 + k] = un - u[k];
+                p.U[i0 + k] = un;
+            }
+        }
+        if (ownsN) {
+            const double UN = s_UN;
+            p.ring[(int64_t)(t - 1) * p.P + N] = UN - uNv;
+            p.U[N] = UN;
+        }
+    }
+}
+
 }  // namespace fpde
 
 using namespace fpde;
@@ -771,6 +1096,9 @@ struct fpde_line {
     double lam = 0, lamR = 0, kkk0 = 0, AlN = 0;
     double *A = nullptr, *g = nullptr, *al = nullptr, *cf = nullptr, *cb = nullptr;
     double *CF = nullptr, *CB = nullptr, *GG = nullptr;
+    // speculative block solve (split path, theta == 0): chunk-local responses of the sweeps
+    bool spec = false;
+    double *RB1 = nullptr, *RB2 = nullptr, *RY1 = nullptr, *RY2 = nullptr;
     double *Lf = nullptr, *Mb = nullptr, *Kb = nullptr, *mb = nullptr;
     unsigned long long *cflag = nullptr, *seq = nullptr, *hflag = nullptr;
     double *halo = nullptr, *sclane = nullptr, *scwarp = nullptr;
@@ -858,9 +1186,9 @@ static cudaEvent_t *probe_begin(fpde_line *L, int kind, int64_t n, double bytes,
 }
 
 template <int SP>
-static cudaError_t launch_block_sp(const cudaLaunchConfig_t &cfg, const LineBlockArgs &a)
+static cudaError_t launch_block_sp(const cudaLaunchConfig_t &cfg, const LineBlockArgs &a, bool spec)
 {
-    return cudaLaunchKernelEx(&cfg, k_line_block<SP>, a);
+    return spec ? cudaLaunchKernelEx(&cfg, k_line_block_spec<SP>, a) : cudaLaunchKernelEx(&cfg, k_line_block<SP>, a);
 }
 
 // Steps j0 .. j0+nsteps-1 of the block starting at nb0 in one persistent launch.
@@ -875,6 +1203,7 @@ static int line_launch_block(fpde_line *L, cudaStream_t st, int64_t nb0, int j0,
     a.agg = L->agg; a.halo = L->halo; a.cflag = L->cflag; a.hflag = L->hflag; a.seq = L->seq;
     a.Lf = L->Lf; a.Mb = L->Mb; a.Kb = L->Kb; a.mb = L->mb; a.flags = L->ctx->d_flags;
     a.sc.lane = L->sclane; a.sc.warp = L->scwarp;
+    a.RB1 = L->RB1; a.RB2 = L->RB2; a.RY1 = L->RY1; a.RY2 = L->RY2;
     a.lam = L->lam; a.g0 = L->d.left_value; a.gN = L->d.right_value; a.dLN = L->d.dLN; a.AlN = L->AlN;
     a.n0 = nb0 + j0; a.j0 = j0; a.nsteps = nsteps; a.N = (int)L->N; a.G = L->G; a.rkind = L->d.right_kind;
     a.chunk = L->chunk;
@@ -891,10 +1220,10 @@ static int line_launch_block(fpde_line *L, cudaStream_t st, int64_t nb0, int j0,
     FPDE_CUDA(cudaMemsetAsync(L->agg, 0xFF, (size_t)nsteps * (2 * L->G + 2) * sizeof(double), st));
     cudaError_t e;
     switch (L->s) {
-    case 1: e = launch_block_sp<1>(cfg, a); break;
-    case 2: e = launch_block_sp<2>(cfg, a); break;
-    case 4: e = launch_block_sp<4>(cfg, a); break;
-    default: e = launch_block_sp<8>(cfg, a); break;
+    case 1: e = launch_block_sp<1>(cfg, a, L->spec); break;
+    case 2: e = launch_block_sp<2>(cfg, a, L->spec); break;
+    case 4: e = launch_block_sp<4>(cfg, a, L->spec); break;
+    default: e = launch_block_sp<8>(cfg, a, L->spec); break;
     }
     if (e != cudaSuccess) return set_error(FPDE_ERR_CUDA, "line block launch: %s", cudaGetErrorString(e));
     count_launches(1);
@@ -1025,7 +1354,7 @@ int fpde_line_destroy(fpde_line *L)
     dev_free(L->scwarp);
     for (double *p : {L->A, L->g, L->al, L->cf, L->cb, L->CF, L->CB, L->GG, L->Lf, L->Mb, L->Kb, L->mb, L->U, L->D,
                       L->part, L->wrev, L->agg, L->ring, L->cfar, L->wlag, L->out_scale, L->srcd, L->lamv, L->eA,
-                      L->eB})
+                      L->eB, L->RB1, L->RB2, L->RY1, L->RY2})
         dev_free(p);
     for (uint16_t *p : {L->h_hi, L->h_lo, L->w_hi, L->w_lo, L->h3[0], L->h3[1], L->h3[2], L->w3[0], L->w3[1],
                         L->w3[2]})
@@ -1101,7 +1430,12 @@ int fpde_line_create(fpde_ctx *ctx, const fpde_line_desc *desc, const double *A,
     }
     if (G > 160) return set_error(FPDE_ERR_UNSUPPORTED, "line solve: at most 160 chunks");
     int per_sm = 0;
-    if (split) FPDE_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_line_block<LSEG>, 2 * LTS, 0));
+    if (split) {
+        int per_sm2 = 0;
+        FPDE_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_line_block<LSEG>, 2 * LTS, 0));
+        FPDE_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm2, k_line_block_spec<LSEG>, 2 * LTS, 0));
+        per_sm = std::min(per_sm, per_sm2);
+    }
     else FPDE_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_line_solve<LSEG>, LT, 0));
     if (G > 1 && G > per_sm * ctx->sm_count)
         return set_error(FPDE_ERR_UNSUPPORTED, "line solve grid of %d CTAs cannot be co-resident", G);
@@ -1251,6 +1585,36 @@ int fpde_line_create(fpde_ctx *ctx, const fpde_line_desc *desc, const double *A,
                                 : d.Da * (L->kkk0 * l1_lag(d.alpha, j)) / d.tau;
     std::vector<double> wrev(L->max_steps + 1, 0.0);
     for (int64_t m = 0; m < L->max_steps; ++m) wrev[m] = wlag[L->max_steps - m];
+    // Speculative block solve (split path without an explicit part): step n+1's right-hand side
+    // is affine in step n's chunk carries (c_in, u_b) through E1 = (w1 - lam) GG and
+    // E2 = (w1 - lam) CB; the chunk-local zero-carry sweeps of E1, E2 (forward y -> RY, backward
+    // u -> RB) are time-invariant.
+    L->spec = split && d.theta == 0.0;
+    std::vector<double> hRB1, hRB2, hRY1, hRY2;
+    if (L->spec) {
+        hRB1.assign(N, 0.0); hRB2.assign(N, 0.0); hRY1.assign(N, 0.0); hRY2.assign(N, 0.0);
+        const double cE = wlag[1] - L->lam;
+        for (int cc = 0; cc < G; ++cc) {
+            const int64_t a0 = (int64_t)cc * chunk, b0 = std::min<int64_t>(a0 + chunk, N);
+            double y1 = 0.0, y2 = 0.0;
+            for (int64_t i = a0; i < b0; ++i) {
+                if (i == 0) { y1 = 0.0; y2 = 0.0; }
+                else {
+                    y1 = hg[i] * (hA[i] * y1 - cE * hGG[i]);
+                    y2 = hg[i] * (hA[i] * y2 - cE * hCB[i]);
+                }
+                hRY1[i] = y1;
+                hRY2[i] = y2;
+            }
+            double u1 = 0.0, u2 = 0.0;
+            for (int64_t i = b0 - 1; i >= a0; --i) {
+                u1 = hal[i] * u1 + hRY1[i];
+                u2 = hal[i] * u2 + hRY2[i];
+                hRB1[i] = u1;
+                hRB2[i] = u2;
+            }
+        }
+    }
     const size_t nb = N * sizeof(double);
     const size_t gb = (size_t)G * sizeof(double);
     bool fail = dev_alloc((void **)&L->A, nb) || dev_alloc((void **)&L->g, nb) || dev_alloc((void **)&L->al, nb) ||
@@ -1323,6 +1687,9 @@ int fpde_line_create(fpde_ctx *ctx, const fpde_line_desc *desc, const double *A,
     }
     if (!fail && d.theta != 0.0)
         fail = dev_alloc((void **)&L->lamv, nb) || dev_alloc((void **)&L->eA, nb) || dev_alloc((void **)&L->eB, nb);
+    if (!fail && L->spec)
+        fail = dev_alloc((void **)&L->RB1, nb) || dev_alloc((void **)&L->RB2, nb) || dev_alloc((void **)&L->RY1, nb) ||
+               dev_alloc((void **)&L->RY2, nb);
     if (fail) {
         std::string keep = fpde_last_error_string();
         fpde_line_destroy(L);
@@ -1342,6 +1709,12 @@ int fpde_line_create(fpde_ctx *ctx, const fpde_line_desc *desc, const double *A,
         cudaMemcpyAsync(L->lamv, hlamv.data(), nb, cudaMemcpyHostToDevice, st);
         cudaMemcpyAsync(L->eA, heA.data(), nb, cudaMemcpyHostToDevice, st);
         cudaMemcpyAsync(L->eB, heB.data(), nb, cudaMemcpyHostToDevice, st);
+    }
+    if (L->spec) {
+        cudaMemcpyAsync(L->RB1, hRB1.data(), nb, cudaMemcpyHostToDevice, st);
+        cudaMemcpyAsync(L->RB2, hRB2.data(), nb, cudaMemcpyHostToDevice, st);
+        cudaMemcpyAsync(L->RY1, hRY1.data(), nb, cudaMemcpyHostToDevice, st);
+        cudaMemcpyAsync(L->RY2, hRY2.data(), nb, cudaMemcpyHostToDevice, st);
     }
     if (L->srcd)
         cudaMemcpyAsync(L->srcd, d.source, (size_t)L->src_rows * (N + 1) * sizeof(double), cudaMemcpyHostToDevice, st);
