@@ -37,6 +37,7 @@
 #include "kernels.cuh"
 #include "tc_far.cuh"
 #include "scan.cuh"
+#include "ff.cuh"
 
 namespace fpde {
 
@@ -360,6 +361,8 @@ struct LineBlockArgs {
     const double *Lf, *Mb, *Kb, *mb;
     ScanCoef sc;
     const double *RB1, *RB2, *RY1, *RY2;  // speculative kernel: sweep responses to E1, E2
+    float2 *ringf;                        // speculative kernel: the ring as float pairs
+    const float2 *wff;                    // speculative kernel: w[lag] as float pairs
     unsigned *flags;
     double lam, g0, gN, dLN, AlN;
     int64_t n0;                           // global index of step j0
@@ -445,6 +448,61 @@ __device__ __forceinline__ void history_sum(const LineBlockArgs &p, int ht, int 
 #pragma unroll
     for (int q = 0; q < SP; ++q)
         if (node[q] < b) out[ht + LTS * q] = far[q] + acc[q];
+}
+
+// history warps of the speculative solve: the same sum in float-float arithmetic on the FP32
+// pipe (one FP64 add per node), from the float-pair copy of the ring and float-pair weights.
+// GB300 issues 2 DFMA/clk/SM, so the FP64 form of this sum (up to 63 rows a step) occupied the
+// FP64 pipe the solver's recurrences wait on.
+template <int SP>
+__device__ __forceinline__ void history_sum_ff(const LineBlockArgs &p, int ht, int a, int b, int j, int rmax,
+                                               double *out)
+{
+    float ah[SP], al[SP];
+    int64_t node[SP];
+#pragma unroll
+    for (int q = 0; q < SP; ++q) {
+        node[q] = a + ht + LTS * q;
+        ah[q] = 0.f;
+        al[q] = 0.f;
+    }
+    for (int k = 0; k < p.KS; ++k) {
+#pragma unroll
+        for (int q = 0; q < SP; ++q)
+            if (node[q] < b) {
+                const double v = __ldcg(p.cfar + ((int64_t)k * BLK + j) * p.P + node[q]);
+                const float2 f = p.far_pairs ? *reinterpret_cast<const float2 *>(&v) : d2ff(v);
+                ff_add(ah[q], al[q], f.x, f.y);
+            }
+    }
+    int r = 0;
+    for (; r + 8 <= rmax; r += 8) {
+        float2 v[8][SP];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            const float2 *row = p.ringf + (int64_t)(r + u) * p.P;
+#pragma unroll
+            for (int q = 0; q < SP; ++q) v[u][q] = node[q] < b ? row[node[q]] : make_float2(0.f, 0.f);
+        }
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            const float2 w = __ldg(p.wff + (j - r - u));
+#pragma unroll
+            for (int q = 0; q < SP; ++q) ff_fma(ah[q], al[q], w, v[u][q]);
+        }
+#pragma unroll
+        for (int q = 0; q < SP; ++q) ff_renorm(ah[q], al[q]);
+    }
+    for (; r < rmax; ++r) {
+        const float2 w = __ldg(p.wff + (j - r));
+        const float2 *row = p.ringf + (int64_t)r * p.P;
+#pragma unroll
+        for (int q = 0; q < SP; ++q)
+            if (node[q] < b) ff_fma(ah[q], al[q], w, row[node[q]]);
+    }
+#pragma unroll
+    for (int q = 0; q < SP; ++q)
+        if (node[q] < b) out[ht + LTS * q] = f2d_bits(ah[q]) + f2d_bits(al[q]);
 }
 
 template <int SP>
@@ -770,13 +828,19 @@ __global__ void __launch_bounds__(2 * LTS, 1) k_line_block(LineBlockArgs p)
 // time-invariant chunk-local responses to E1, E2 (RB: backward, RY: forward at the chunk's last
 // node). Per step the critical path is: carries of step t -> corrected aggregates of step t+1
 // published -> exchange; the sweeps of the next step fill the exchange's latency.
+// GB300 runs FP64 at 2 DFMA/clk/SM (a warp's FP64 instruction holds its scheduler's FP64 pipe
+// for ~64 cycles), so the history warps sum in float-float on the FP32 pipe (ringf, wff: the
+// increments and weights as float pairs; the solver hands each new FP64 row over in shared
+// memory and the history warps convert it), and the four solver warps form the four carry dot
+// products of a step side by side.
 template <int SP>
 __global__ void __launch_bounds__(2 * LTS, 1) k_line_block_spec(LineBlockArgs p)
 {
     __shared__ double sS[2][LTS * SP];                   // H_t by parity of t
+    __shared__ double sD[2][LTS * SP];                   // D_t (FP64) by parity of t
     __shared__ double wXf[NWS], wXb[NWS];
     __shared__ double sCf[NWS][NWS], sCb[NWS][NWS];
-    __shared__ double s_cin, s_ub, s_UN;
+    __shared__ double s_red[4];                          // c_in, Mb.U0, Kb.Y, right end value
     __shared__ int s_abort;
     const int tid = threadIdx.x;
     const bool solver = tid < LTS;
@@ -794,14 +858,23 @@ __global__ void __launch_bounds__(2 * LTS, 1) k_line_block_spec(LineBlockArgs p)
     if (!solver) {
         // ============== history warps: H_t = far^t + sum_{0 <= r <= t-3} w[t-r] D_r
         const int ht = tid - LTS;
-        history_sum<SP>(p, ht, a, b, p.j0, max(p.j0 - 2, 0), sS[p.j0 & 1]);
-        if (p.j0 + 1 < jend) history_sum<SP>(p, ht, a, b, p.j0 + 1, max(p.j0 - 1, 0), sS[(p.j0 + 1) & 1]);
+        history_sum_ff<SP>(p, ht, a, b, p.j0, max(p.j0 - 2, 0), sS[p.j0 & 1]);
+        if (p.j0 + 1 < jend) history_sum_ff<SP>(p, ht, a, b, p.j0 + 1, max(p.j0 - 1, 0), sS[(p.j0 + 1) & 1]);
         __syncthreads();                                                    // start
         for (int s = 0; s < p.nsteps; ++s) {
-            __syncthreads();                                                // X(s): row t-1 is in the ring
+            __syncthreads();                                                // X(s): D_{t-1} is in sD
             if (s_abort) return;
             const int t = p.j0 + s;
-            if (t + 2 < jend) history_sum<SP>(p, ht, a, b, t + 2, t, sS[t & 1]);
+            if (s > 0) {                                                    // row t-1 as float pairs
+                const double *dd = sD[(t - 1) & 1];
+                float2 *row = p.ringf + (int64_t)(t - 1) * p.P;
+#pragma unroll
+                for (int q = 0; q < SP; ++q) {
+                    const int i = a + ht + LTS * q;
+                    if (i < b) row[i] = d2ff(dd[ht + LTS * q]);
+                }
+            }
+            if (t + 2 < jend) history_sum_ff<SP>(p, ht, a, b, t + 2, t, sS[t & 1]);
         }
         return;
     }
@@ -822,21 +895,24 @@ __global__ void __launch_bounds__(2 * LTS, 1) k_line_block_spec(LineBlockArgs p)
         PeF = __ldg(p.sc.lane + 5 * GT + T);
         PeB = __ldg(p.sc.lane + 11 * GT + T);
     }
-    double lf[5], lfN[5], mbv[5], kbv[5], mbc = 0.0;
-    if (warp == 0) {
+    // warp w's carry dot product over the chunks' aggregates: 0 Lf[c].Y (c_in), 1 Mb[c].U0,
+    // 2 Kb[c].Y, 3 Lf[G].Y (the flux end's y; unused at a Dirichlet end)
+    const bool flux = p.rkind != FPDE_BC_DIRICHLET;
+    const double *cvec = warp == 0 ? p.Lf + (int64_t)c * G
+                       : warp == 1 ? p.Mb + (int64_t)c * G
+                       : warp == 2 ? p.Kb + (int64_t)c * G
+                                   : p.Lf + (int64_t)G * G;
+    const int slot_off = warp == 1 ? 1 : 0;              // U0 slots for warp 1, Y slots otherwise
+    double cv[5];
 #pragma unroll
-        for (int t = 0; t < 5; ++t) {
-            const int q = lane + 32 * t;
-            const bool in = q < G;
-            lf[t] = in ? __ldg(p.Lf + (int64_t)c * G + q) : 0.0;
-            lfN[t] = in ? __ldg(p.Lf + (int64_t)G * G + q) : 0.0;
-            mbv[t] = in ? __ldg(p.Mb + (int64_t)c * G + q) : 0.0;
-            kbv[t] = in ? __ldg(p.Kb + (int64_t)c * G + q) : 0.0;
-        }
-        mbc = __ldg(p.mb + c);
+    for (int t = 0; t < 5; ++t) {
+        const int q = lane + 32 * t;
+        cv[t] = q < G ? __ldg(cvec + q) : 0.0;
     }
+    const double mbc = __ldg(p.mb + c);
     double u[SP], kA[SP], kg[SP], kal[SP], kcf[SP], kcb[SP], kCB[SP], kGG[SP], rb1[SP], rb2[SP];
-    double dm1[SP], dm2[SP];                             // D_{t-1}, D_{t-2}
+    double dm1[SP];                                      // D_{t-1}
+    double dm2[SP];                                      // D_{t-2} (prologue only)
 #pragma unroll
     for (int k = 0; k < SP; ++k) {
         const bool in = k < cnt;
@@ -925,29 +1001,31 @@ __global__ void __launch_bounds__(2 * LTS, 1) k_line_block_spec(LineBlockArgs p)
                 if (k < cnt) ubw[k] = fma(kcb[k], carry, ubw[k]);
         }
     };
-    // warp 0: step t's aggregates of every chunk (polled values), this chunk's carries
+    // step s's aggregates of every chunk, polled as values (each slot holds the all-bits-set
+    // pattern until its one write of the launch; a 64-bit load is single-copy atomic); each
+    // warp forms its dot product, warp 3 the right end value (U1 :4685-4719)
     auto gather = [&](int s) {
-        if (warp != 0) return;
         const double *agg = p.agg + (size_t)s * (2 * G + 2);
-        double ye[5], u0[5], uNm1 = 0.0;
+        if (warp == 3 && !flux) {
+            if (lane == 0) s_red[3] = p.gN;
+            return;
+        }
+        double v[5], uNm1 = 0.0;
         bool ok = true;
-        const bool need_nm1 = p.rkind != FPDE_BC_DIRICHLET;
         const unsigned long long t0 = gtimer_ns();
         while (true) {
             bool mine = true;
 #pragma unroll
             for (int t = 0; t < 5; ++t) {
                 const int q = lane + 32 * t;
-                ye[t] = 0.0;
-                u0[t] = 0.0;
+                v[t] = 0.0;
                 if (q < G) {
-                    const unsigned long long by = ld_relaxed_u64(agg + 2 * q), bu = ld_relaxed_u64(agg + 2 * q + 1);
-                    if (by == SLOT_EMPTY || bu == SLOT_EMPTY) mine = false;
-                    ye[t] = __longlong_as_double((long long)by);
-                    u0[t] = __longlong_as_double((long long)bu);
+                    const unsigned long long bv = ld_relaxed_u64(agg + 2 * q + slot_off);
+                    if (bv == SLOT_EMPTY) mine = false;
+                    v[t] = __longlong_as_double((long long)bv);
                 }
             }
-            if (need_nm1 && lane == 0) {
+            if (warp == 3 && lane == 0) {
                 const unsigned long long bn = ld_relaxed_u64(agg + 2 * G);
                 if (bn == SLOT_EMPTY) mine = false;
                 uNm1 = __longlong_as_double((long long)bn);
@@ -960,29 +1038,21 @@ __global__ void __launch_bounds__(2 * LTS, 1) k_line_block_spec(LineBlockArgs p)
             if (lane == 0) { atomicOr(p.flags, DEVERR_BARRIER_TIMEOUT); s_abort = 1; }
             return;
         }
-        double sc = 0.0, syN = 0.0, s1 = 0.0, s2 = 0.0;
+        double sum = 0.0;
 #pragma unroll
-        for (int t = 0; t < 5; ++t) {
-            sc = fma(lf[t], ye[t], sc);
-            syN = fma(lfN[t], ye[t], syN);
-            s1 = fma(mbv[t], u0[t], s1);
-            s2 = fma(kbv[t], ye[t], s2);
-        }
-        double sub = s1 + s2;
+        for (int t = 0; t < 5; ++t) sum = fma(cv[t], v[t], sum);
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            sc += __shfl_xor_sync(FULL, sc, o);
-            syN += __shfl_xor_sync(FULL, syN, o);
-            sub += __shfl_xor_sync(FULL, sub, o);
+        for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(FULL, sum, o);
+        if (lane == 0) {
+            if (warp == 3) {                             // flux end: lane 0 holds the old U[N-1]
+                double uN;
+                if (fabs(sum) > 1e-15) uN = (fabs(1.0 - p.AlN) > 1e-15) ? (sum + p.gN * p.dLN) / (1.0 - p.AlN) : uNm1;
+                else uN = (fabs(1.0 - p.AlN) > 1e-15) ? 0.0 : uNm1;
+                s_red[3] = uN;
+            } else {
+                s_red[warp] = sum;
+            }
         }
-        double uN;                                       // right end (U1 :4685-4719)
-        if (p.rkind == FPDE_BC_DIRICHLET) {
-            uN = p.gN;
-        } else {                                         // lane 0 holds the old U[N-1]
-            if (fabs(syN) > 1e-15) uN = (fabs(1.0 - p.AlN) > 1e-15) ? (syN + p.gN * p.dLN) / (1.0 - p.AlN) : uNm1;
-            else uN = (fabs(1.0 - p.AlN) > 1e-15) ? 0.0 : uNm1;
-        }
-        if (lane == 0) { s_cin = sc; s_ub = fma(mbc, uN, sub); s_UN = uN; }
     };
     auto src_row = [&](int64_t n) -> const double * {
         return p.src ? p.src + (int64_t)(n < p.src_rows ? n : p.src_rows - 1) * (N + 1) : nullptr;
@@ -1000,7 +1070,7 @@ __global__ void __launch_bounds__(2 * LTS, 1) k_line_block_spec(LineBlockArgs p)
         }
         sweeps();
         double *agg = p.agg;
-        if (ownsN && p.rkind != FPDE_BC_DIRICHLET) st_relaxed_f64(agg + 2 * G, u[cnt - 1]);
+        if (ownsN && flux) st_relaxed_f64(agg + 2 * G, u[cnt - 1]);
         if (last) st_relaxed_f64(agg + 2 * c, yv[cnt - 1]);
         if (tid == 0) st_relaxed_f64(agg + 2 * c + 1, ubw[0]);
     }
@@ -1008,30 +1078,31 @@ __global__ void __launch_bounds__(2 * LTS, 1) k_line_block_spec(LineBlockArgs p)
 #pragma unroll
     for (int k = 0; k < SP; ++k) { ubc[k] = ubw[k]; ubp[k] = 0.0; ubprev[k] = 0.0; }
     double ypl = 0.0;                                    // y'_{t+1} at the chunk's last node
+    double cin = 0.0, ubv = 0.0;                         // carries of the last gathered step
     for (int s = 0; s < p.nsteps; ++s) {
         const int t = p.j0 + s;
         if (s > 0) {
             // ---- carries of step t-1: state u^t, increment D_{t-1}; step t's corrected results
-            const double cin = s_cin, ubv = s_ub;
+            double *dsh = sD[(t - 1) & 1];
 #pragma unroll
             for (int k = 0; k < SP; ++k) {
                 if (k < cnt) {
                     const double un = fma(kCB[k], ubv, fma(kGG[k], cin, ubprev[k]));
                     const double d = un - u[k];
                     p.ring[(int64_t)(t - 1) * p.P + i0 + k] = d;
-                    dm2[k] = dm1[k];
+                    dsh[i0 - a + k] = d;
                     dm1[k] = d;
                     u[k] = un;
                     ubc[k] = fma(rb2[k], ubv, fma(rb1[k], cin, ubp[k]));
                 }
             }
             if (ownsN) {
-                const double UN = s_UN;
+                const double UN = s_red[3];
                 p.ring[(int64_t)(t - 1) * p.P + N] = UN - uNv;
                 uNv = UN;
             }
             double *agg = p.agg + (size_t)s * (2 * G + 2);
-            if (ownsN && p.rkind != FPDE_BC_DIRICHLET) st_relaxed_f64(agg + 2 * G, u[cnt - 1]);
+            if (ownsN && flux) st_relaxed_f64(agg + 2 * G, u[cnt - 1]);
             if (last) st_relaxed_f64(agg + 2 * c, fma(ry2, ubv, fma(ry1, cin, ypl)));
             if (tid == 0) st_relaxed_f64(agg + 2 * c + 1, ubc[0]);
         }
@@ -1040,12 +1111,21 @@ __global__ void __launch_bounds__(2 * LTS, 1) k_line_block_spec(LineBlockArgs p)
             // ---- step t+1 on Omega0, while the aggregates of step t are exchanged
             const double *src = src_row(p.n0 + s + 1);
             const double *hs = sS[(t + 1) & 1];
+            const double cE = w1 - lam;
+            if (src) {
 #pragma unroll
-            for (int k = 0; k < SP; ++k) {
-                om[k] = 0.0;
-                if (k < cnt) {
-                    const double h = fma(w2, dm1[k], hs[i0 - a + k]) + (src ? __ldg(src + i0 + k) : 0.0);
-                    om[k] = fma(w1 - lam, ubc[k], fma(-w1, u[k], h));
+                for (int k = 0; k < SP; ++k) {
+                    om[k] = 0.0;
+                    if (k < cnt) {
+                        const double h = fma(w2, dm1[k], hs[i0 - a + k]) + __ldg(src + i0 + k);
+                        om[k] = fma(cE, ubc[k], fma(-w1, u[k], h));
+                    }
+                }
+            } else {
+#pragma unroll
+                for (int k = 0; k < SP; ++k) {
+                    om[k] = 0.0;
+                    if (k < cnt) om[k] = fma(cE, ubc[k], fma(-w1, u[k], fma(w2, dm1[k], hs[i0 - a + k])));
                 }
             }
             sweeps();
@@ -1059,24 +1139,27 @@ __global__ void __launch_bounds__(2 * LTS, 1) k_line_block_spec(LineBlockArgs p)
             if (s + 1 < p.nsteps) __syncthreads();      // release the history warps at X(s+1)
             return;
         }
+        cin = s_red[0];
+        ubv = fma(mbc, s_red[3], s_red[1] + s_red[2]);
 #pragma unroll
         for (int k = 0; k < SP; ++k) ubprev[k] = ubc[k];
     }
-    // ---- carries of the last step: the final state and increment
+    // ---- carries of the last step: the final state and increment (FP64 ring and float pairs)
     {
-        const int t = jend;
-        const double cin = s_cin, ubv = s_ub;
+        const int64_t row = (int64_t)(jend - 1) * p.P;
 #pragma unroll
         for (int k = 0; k < SP; ++k) {
             if (k < cnt) {
                 const double un = fma(kCB[k], ubv, fma(kGG[k], cin, ubprev[k]));
-                p.ring[(int64_t)(t - 1) * p.P + i0 + k] = un - u[k];
+                const double d = un - u[k];
+                p.ring[row + i0 + k] = d;
+                p.ringf[row + i0 + k] = d2ff(d);
                 p.U[i0 + k] = un;
             }
         }
         if (ownsN) {
-            const double UN = s_UN;
-            p.ring[(int64_t)(t - 1) * p.P + N] = UN - uNv;
+            const double UN = s_red[3];
+            p.ring[row + N] = UN - uNv;
             p.U[N] = UN;
         }
     }
@@ -1099,6 +1182,7 @@ struct fpde_line {
     // speculative block solve (split path, theta == 0): chunk-local responses of the sweeps
     bool spec = false;
     double *RB1 = nullptr, *RB2 = nullptr, *RY1 = nullptr, *RY2 = nullptr;
+    float2 *ringf = nullptr, *wff = nullptr;  // the ring and the lag weights as float pairs
     double *Lf = nullptr, *Mb = nullptr, *Kb = nullptr, *mb = nullptr;
     unsigned long long *cflag = nullptr, *seq = nullptr, *hflag = nullptr;
     double *halo = nullptr, *sclane = nullptr, *scwarp = nullptr;
@@ -1204,6 +1288,7 @@ static int line_launch_block(fpde_line *L, cudaStream_t st, int64_t nb0, int j0,
     a.Lf = L->Lf; a.Mb = L->Mb; a.Kb = L->Kb; a.mb = L->mb; a.flags = L->ctx->d_flags;
     a.sc.lane = L->sclane; a.sc.warp = L->scwarp;
     a.RB1 = L->RB1; a.RB2 = L->RB2; a.RY1 = L->RY1; a.RY2 = L->RY2;
+    a.ringf = L->ringf; a.wff = L->wff;
     a.lam = L->lam; a.g0 = L->d.left_value; a.gN = L->d.right_value; a.dLN = L->d.dLN; a.AlN = L->AlN;
     a.n0 = nb0 + j0; a.j0 = j0; a.nsteps = nsteps; a.N = (int)L->N; a.G = L->G; a.rkind = L->d.right_kind;
     a.chunk = L->chunk;
@@ -1356,6 +1441,8 @@ int fpde_line_destroy(fpde_line *L)
                       L->part, L->wrev, L->agg, L->ring, L->cfar, L->wlag, L->out_scale, L->srcd, L->lamv, L->eA,
                       L->eB, L->RB1, L->RB2, L->RY1, L->RY2})
         dev_free(p);
+    dev_free(L->ringf);
+    dev_free(L->wff);
     for (uint16_t *p : {L->h_hi, L->h_lo, L->w_hi, L->w_lo, L->h3[0], L->h3[1], L->h3[2], L->w3[0], L->w3[1],
                         L->w3[2]})
         dev_free(p);
@@ -1591,7 +1678,13 @@ int fpde_line_create(fpde_ctx *ctx, const fpde_line_desc *desc, const double *A,
     // u -> RB) are time-invariant.
     L->spec = split && d.theta == 0.0;
     std::vector<double> hRB1, hRB2, hRY1, hRY2;
+    std::vector<float2> hwff;
     if (L->spec) {
+        hwff.resize(LW);                           // w = hi + lo, hi the nearest float
+        for (int64_t j = 0; j < LW; ++j) {
+            const float hi = (float)wlag[j];
+            hwff[j] = make_float2(hi, (float)(wlag[j] - (double)hi));
+        }
         hRB1.assign(N, 0.0); hRB2.assign(N, 0.0); hRY1.assign(N, 0.0); hRY2.assign(N, 0.0);
         const double cE = wlag[1] - L->lam;
         for (int cc = 0; cc < G; ++cc) {
@@ -1689,7 +1782,8 @@ int fpde_line_create(fpde_ctx *ctx, const fpde_line_desc *desc, const double *A,
         fail = dev_alloc((void **)&L->lamv, nb) || dev_alloc((void **)&L->eA, nb) || dev_alloc((void **)&L->eB, nb);
     if (!fail && L->spec)
         fail = dev_alloc((void **)&L->RB1, nb) || dev_alloc((void **)&L->RB2, nb) || dev_alloc((void **)&L->RY1, nb) ||
-               dev_alloc((void **)&L->RY2, nb);
+               dev_alloc((void **)&L->RY2, nb) || dev_alloc((void **)&L->ringf, (size_t)BLK * L->P * sizeof(float2)) ||
+               dev_alloc((void **)&L->wff, (size_t)LW * sizeof(float2));
     if (fail) {
         std::string keep = fpde_last_error_string();
         fpde_line_destroy(L);
@@ -1715,6 +1809,8 @@ int fpde_line_create(fpde_ctx *ctx, const fpde_line_desc *desc, const double *A,
         cudaMemcpyAsync(L->RB2, hRB2.data(), nb, cudaMemcpyHostToDevice, st);
         cudaMemcpyAsync(L->RY1, hRY1.data(), nb, cudaMemcpyHostToDevice, st);
         cudaMemcpyAsync(L->RY2, hRY2.data(), nb, cudaMemcpyHostToDevice, st);
+        cudaMemcpyAsync(L->wff, hwff.data(), (size_t)LW * sizeof(float2), cudaMemcpyHostToDevice, st);
+        cudaMemsetAsync(L->ringf, 0, (size_t)BLK * L->P * sizeof(float2), st);
     }
     if (L->srcd)
         cudaMemcpyAsync(L->srcd, d.source, (size_t)L->src_rows * (N + 1) * sizeof(double), cudaMemcpyHostToDevice, st);
