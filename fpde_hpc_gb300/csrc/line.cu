@@ -450,39 +450,115 @@ __device__ __forceinline__ void history_sum(const LineBlockArgs &p, int ht, int 
         if (node[q] < b) out[ht + LTS * q] = far[q] + acc[q];
 }
 
-// history warps of the speculative solve: the same sum in float-float arithmetic on the FP32
-// pipe (one FP64 add per node), from the float-pair copy of the ring and float-pair weights.
-// GB300 issues 2 DFMA/clk/SM, so the FP64 form of this sum (up to 63 rows a step) occupied the
-// FP64 pipe the solver's recurrences wait on.
-template <int SP>
-__device__ __forceinline__ void history_sum_ff(const LineBlockArgs &p, int ht, int a, int b, int j, int rmax,
-                                               double *out)
+// history warps of the speculative solve: the same sums in float-float arithmetic on the FP32
+// pipe (one FP64 add per node at the end), from the float-pair copy of the ring and float-pair
+// weights. GB300 issues 2 DFMA/clk/SM, so the FP64 form of these sums (up to 63 rows a step)
+// occupied the FP64 pipe the solver's recurrences wait on.
+// (ah, al) += far partials of steps j .. j+NJ-1 (NJ accumulators; every load issued first).
+template <int SP, int NJ>
+__device__ __forceinline__ void far_fold_ff(const LineBlockArgs &p, int ht, int a, int b, int j, float (&ah)[NJ][SP],
+                                            float (&al)[NJ][SP])
 {
-    float ah[SP], al[SP];
+    double v[NJ][FAR_MAX_SPLITS][SP];
+#pragma unroll
+    for (int m = 0; m < NJ; ++m)
+#pragma unroll
+        for (int k = 0; k < FAR_MAX_SPLITS; ++k)
+#pragma unroll
+            for (int q = 0; q < SP; ++q) {
+                const int64_t node = a + ht + LTS * q;
+                v[m][k][q] = (k < p.KS && node < b && j + m < BLK)
+                                 ? __ldcg(p.cfar + ((int64_t)k * BLK + j + m) * p.P + node) : 0.0;
+            }
+#pragma unroll
+    for (int m = 0; m < NJ; ++m)
+#pragma unroll
+        for (int k = 0; k < FAR_MAX_SPLITS; ++k)
+#pragma unroll
+            for (int q = 0; q < SP; ++q) {
+                const float2 f = p.far_pairs ? *reinterpret_cast<const float2 *>(&v[m][k][q]) : d2ff(v[m][k][q]);
+                ff_add(ah[m][q], al[m][q], f.x, f.y);
+            }
+}
+
+// (ah, al) += sum_{r < rmax} w[j - r] D_r for this thread's nodes (rows of the float-pair ring,
+// two batches of rows in flight).
+template <int SP>
+__device__ __forceinline__ void rows_ff(const LineBlockArgs &p, int ht, int a, int b, int j, int rmax, float *ah,
+                                        float *al)
+{
+    constexpr int RB = SP <= 4 ? 8 : 4;                  // rows per batch
     int64_t node[SP];
 #pragma unroll
-    for (int q = 0; q < SP; ++q) {
-        node[q] = a + ht + LTS * q;
-        ah[q] = 0.f;
-        al[q] = 0.f;
+    for (int q = 0; q < SP; ++q) node[q] = a + ht + LTS * q;
+    float2 va[RB][SP], vb[RB][SP];
+    auto load = [&](float2 (&v)[RB][SP], int r0) {
+#pragma unroll
+        for (int u = 0; u < RB; ++u) {
+            const float2 *row = p.ringf + (int64_t)(r0 + u) * p.P;
+#pragma unroll
+            for (int q = 0; q < SP; ++q) v[u][q] = node[q] < b ? row[node[q]] : make_float2(0.f, 0.f);
+        }
+    };
+    auto accumulate = [&](const float2 (&v)[RB][SP], int r0) {
+#pragma unroll
+        for (int u = 0; u < RB; ++u) {
+            const float2 w = __ldg(p.wff + (j - r0 - u));
+#pragma unroll
+            for (int q = 0; q < SP; ++q) ff_fma(ah[q], al[q], w, v[u][q]);
+        }
+#pragma unroll
+        for (int q = 0; q < SP; ++q) ff_renorm(ah[q], al[q]);
+    };
+    int r = 0;
+    if (RB <= rmax) load(va, 0);
+    while (r + RB <= rmax) {                             // batch r in registers, the next one loading
+        const bool more = r + 2 * RB <= rmax;
+        if (more) load(vb, r + RB);
+        accumulate(va, r);
+        r += RB;
+        if (!more) break;
+        const bool more2 = r + 2 * RB <= rmax;
+        if (more2) load(va, r + RB);
+        accumulate(vb, r);
+        r += RB;
+        if (!more2) break;
     }
-    for (int k = 0; k < p.KS; ++k) {
+    for (; r < rmax; ++r) {
+        const float2 w = __ldg(p.wff + (j - r));
+        const float2 *row = p.ringf + (int64_t)r * p.P;
 #pragma unroll
         for (int q = 0; q < SP; ++q)
-            if (node[q] < b) {
-                const double v = __ldcg(p.cfar + ((int64_t)k * BLK + j) * p.P + node[q]);
-                const float2 f = p.far_pairs ? *reinterpret_cast<const float2 *>(&v) : d2ff(v);
-                ff_add(ah[q], al[q], f.x, f.y);
-            }
+            if (node[q] < b) ff_fma(ah[q], al[q], w, row[node[q]]);
     }
-    int r = 0;
-    for (; r + 8 <= rmax; r += 8) {
+}
+
+// The speculative kernel keeps the block's newest NR increment rows (float pairs, this chunk's
+// nodes) in dynamic shared memory, so the per-step history sums read them from shared memory
+// instead of re-reading every earlier row of the block from L2 each step; older rows come from
+// the float-pair ring in global memory.
+template <int SP>
+struct SpecRing {
+    static constexpr int NR = SP <= 2 ? 64 : (SP == 4 ? 48 : 24);
+    static constexpr size_t bytes = (size_t)NR * LTS * SP * sizeof(float2);
+};
+
+// (ah, al) += sum_{r0 <= r < r1} w[j - r] D_r from the shared-memory row ring (slot r mod NR).
+template <int SP>
+__device__ __forceinline__ void rows_smem_ff(const LineBlockArgs &p, const float2 *sR, int ht, int j, int r0, int r1,
+                                             float *ah, float *al)
+{
+    constexpr int NR = SpecRing<SP>::NR;
+    int slot = r0 % NR;
+    int r = r0;
+    for (; r + 8 <= r1; r += 8) {
         float2 v[8][SP];
 #pragma unroll
         for (int u = 0; u < 8; ++u) {
-            const float2 *row = p.ringf + (int64_t)(r + u) * p.P;
+            int sl = slot + u;
+            if (sl >= NR) sl -= NR;
 #pragma unroll
-            for (int q = 0; q < SP; ++q) v[u][q] = node[q] < b ? row[node[q]] : make_float2(0.f, 0.f);
+            for (int q = 0; q < SP; ++q) v[u][q] = sR[sl * (LTS * SP) + ht + LTS * q];
         }
 #pragma unroll
         for (int u = 0; u < 8; ++u) {
@@ -492,17 +568,46 @@ __device__ __forceinline__ void history_sum_ff(const LineBlockArgs &p, int ht, i
         }
 #pragma unroll
         for (int q = 0; q < SP; ++q) ff_renorm(ah[q], al[q]);
+        slot += 8;
+        if (slot >= NR) slot -= NR;
     }
-    for (; r < rmax; ++r) {
+    for (; r < r1; ++r) {
         const float2 w = __ldg(p.wff + (j - r));
-        const float2 *row = p.ringf + (int64_t)r * p.P;
 #pragma unroll
-        for (int q = 0; q < SP; ++q)
-            if (node[q] < b) ff_fma(ah[q], al[q], w, row[node[q]]);
+        for (int q = 0; q < SP; ++q) ff_fma(ah[q], al[q], w, sR[slot * (LTS * SP) + ht + LTS * q]);
+        if (++slot == NR) slot = 0;
     }
+}
+
+// (ah, al) += sum_{r < rmax} w[j - r] D_r: rows below rlo from the global float-pair ring, the
+// rest from the shared-memory row ring.
+template <int SP>
+__device__ __forceinline__ void rows_split_ff(const LineBlockArgs &p, const float2 *sR, int ht, int a, int b, int j,
+                                              int rmax, int rlo, float *ah, float *al)
+{
+    const int rg = min(rlo, rmax);
+    if (rg > 0) rows_ff<SP>(p, ht, a, b, j, rg, ah, al);
+    if (rmax > rg) rows_smem_ff<SP>(p, sR, ht, j, rg, rmax, ah, al);
+}
+
+// v[n - 1] for a register array and a run-time n (1..SP) without indexing it dynamically,
+// which would move the array to local memory.
+template <int SP>
+__device__ __forceinline__ double last_of(const double (&v)[SP], int n)
+{
+    double r = v[0];
+#pragma unroll
+    for (int k = 1; k < SP; ++k)
+        if (k == n - 1) r = v[k];
+    return r;
+}
+
+template <int SP>
+__device__ __forceinline__ void history_store_ff(int ht, int a, int b, const float *ah, const float *al, double *out)
+{
 #pragma unroll
     for (int q = 0; q < SP; ++q)
-        if (node[q] < b) out[ht + LTS * q] = f2d_bits(ah[q]) + f2d_bits(al[q]);
+        if (a + ht + LTS * q < b) out[ht + LTS * q] = f2d_bits(ah[q]) + f2d_bits(al[q]);
 }
 
 template <int SP>
@@ -633,7 +738,7 @@ __global__ void __launch_bounds__(2 * LTS, 1) k_line_block(LineBlockArgs p)
                 }
             }
         }
-        if (ownsN && p.rkind != FPDE_BC_DIRICHLET) st_relaxed_f64(agg + 2 * G, u[cnt - 1]);  // old U[N-1], flux
+        if (ownsN && p.rkind != FPDE_BC_DIRICHLET) st_relaxed_f64(agg + 2 * G, last_of<SP>(u, cnt));  // old U[N-1], flux
         // ---- forward: segment sweep from zero carry, warp scan, warp totals
         double y[SP];
         double yl = 0.0;
@@ -667,7 +772,7 @@ __global__ void __launch_bounds__(2 * LTS, 1) k_line_block(LineBlockArgs p)
             for (int k = 0; k < SP; ++k)
                 if (k < cnt) y[k] = fma(kcf[k], carry, y[k]);
         }
-        if (cnt > 0 && i1 == b) st_relaxed_f64(agg + 2 * c, y[cnt - 1]);   // the chunk's last y (zero carry-in)
+        if (cnt > 0 && i1 == b) st_relaxed_f64(agg + 2 * c, last_of<SP>(y, cnt));   // the chunk's last y (zero carry-in)
         // ---- backward: segment sweep from zero carry, warp scan, warp totals
         double ub[SP];
         double ul = 0.0;
@@ -826,13 +931,15 @@ __global__ void __launch_bounds__(2 * LTS, 1) k_line_block(LineBlockArgs p)
 // row but the two newest). The solver warps therefore run step t+1's sweeps and scans on
 // Omega0 while step t's aggregates are exchanged, and correct them afterwards with the
 // time-invariant chunk-local responses to E1, E2 (RB: backward, RY: forward at the chunk's last
-// node). Per step the critical path is: carries of step t -> corrected aggregates of step t+1
-// published -> exchange; the sweeps of the next step fill the exchange's latency.
+// node). The history warps poll step t's aggregates of every chunk and form this chunk's carry
+// dot products while the solver warps sweep step t+1, and hand the carries over through a
+// named barrier (bar.arrive / bar.sync): per step the solver's path is finalise + publish ->
+// sweeps -> carries, and the exchange's latency is hidden behind the sweeps.
 // GB300 runs FP64 at 2 DFMA/clk/SM (a warp's FP64 instruction holds its scheduler's FP64 pipe
 // for ~64 cycles), so the history warps sum in float-float on the FP32 pipe (ringf, wff: the
 // increments and weights as float pairs; the solver hands each new FP64 row over in shared
-// memory and the history warps convert it), and the four solver warps form the four carry dot
-// products of a step side by side.
+// memory and the history warps convert it), and the four history warps form the four carry
+// dot products side by side.
 template <int SP>
 __global__ void __launch_bounds__(2 * LTS, 1) k_line_block_spec(LineBlockArgs p)
 {
@@ -842,6 +949,7 @@ __global__ void __launch_bounds__(2 * LTS, 1) k_line_block_spec(LineBlockArgs p)
     __shared__ double sCf[NWS][NWS], sCb[NWS][NWS];
     __shared__ double s_red[4];                          // c_in, Mb.U0, Kb.Y, right end value
     __shared__ int s_abort;
+    extern __shared__ float2 spec_rows[];                // [NR][LTS * SP]: the newest increment rows
     const int tid = threadIdx.x;
     const bool solver = tid < LTS;
     const int c = blockIdx.x, G = p.G, N = p.N;
@@ -856,11 +964,106 @@ __global__ void __launch_bounds__(2 * LTS, 1) k_line_block_spec(LineBlockArgs p)
     }
 
     if (!solver) {
-        // ============== history warps: H_t = far^t + sum_{0 <= r <= t-3} w[t-r] D_r
+        // ============== history warps: H_t = far^t + sum_{0 <= r <= t-3} w[t-r] D_r.
+        // H_{t+3} is summed before X(s+1) from every row but D_t; after X(s+1) D_t arrives in
+        // sD, is converted into the float-pair ring and its one term completes H_{t+3}.
         const int ht = tid - LTS;
-        history_sum_ff<SP>(p, ht, a, b, p.j0, max(p.j0 - 2, 0), sS[p.j0 & 1]);
-        if (p.j0 + 1 < jend) history_sum_ff<SP>(p, ht, a, b, p.j0 + 1, max(p.j0 - 1, 0), sS[(p.j0 + 1) & 1]);
-        __syncthreads();                                                    // start
+        const int lane = tid & 31, hw = ht >> 5;
+        // history warp hw's carry dot product over the chunks' aggregates: 0 Lf[c].Y (c_in),
+        // 1 Mb[c].U0, 2 Kb[c].Y, 3 Lf[G].Y (the flux end's y; unused at a Dirichlet end)
+        const bool flux = p.rkind != FPDE_BC_DIRICHLET;
+        const double *cvec = hw == 0 ? p.Lf + (int64_t)c * G
+                           : hw == 1 ? p.Mb + (int64_t)c * G
+                           : hw == 2 ? p.Kb + (int64_t)c * G
+                                     : p.Lf + (int64_t)G * G;
+        const int slot_off = hw == 1 ? 1 : 0;            // U0 slots for warp 1, Y slots otherwise
+        double cv[5];
+#pragma unroll
+        for (int k = 0; k < 5; ++k) {
+            const int q = lane + 32 * k;
+            cv[k] = q < G ? __ldg(cvec + q) : 0.0;
+        }
+        // step s's aggregates of every chunk, polled as values (each slot holds the all-bits-set
+        // pattern until its one write of the launch; a 64-bit load is single-copy atomic); warp 3
+        // forms the right end value (U1 :4685-4719)
+        auto carries = [&](int s) {
+            const double *agg = p.agg + (size_t)s * (2 * G + 2);
+            if (hw == 3 && !flux) {
+                if (lane == 0) s_red[3] = p.gN;
+                return;
+            }
+            double v[5], uNm1 = 0.0;
+            bool ok = true;
+            const unsigned long long t0 = gtimer_ns();
+            while (true) {
+                bool mine = true;
+#pragma unroll
+                for (int k = 0; k < 5; ++k) {
+                    const int q = lane + 32 * k;
+                    v[k] = 0.0;
+                    if (q < G) {
+                        const unsigned long long bv = ld_relaxed_u64(agg + 2 * q + slot_off);
+                        if (bv == SLOT_EMPTY) mine = false;
+                        v[k] = __longlong_as_double((long long)bv);
+                    }
+                }
+                if (hw == 3 && lane == 0) {
+                    const unsigned long long bn = ld_relaxed_u64(agg + 2 * G);
+                    if (bn == SLOT_EMPTY) mine = false;
+                    uNm1 = __longlong_as_double((long long)bn);
+                }
+                if (__all_sync(FULL, mine)) break;
+                if (gtimer_ns() - t0 > 1000000000ull) { ok = false; break; }
+            }
+            ok = __all_sync(FULL, ok);
+            if (!ok) {
+                if (lane == 0) { atomicOr(p.flags, DEVERR_BARRIER_TIMEOUT); s_abort = 1; }
+                return;
+            }
+            double sum = 0.0;
+#pragma unroll
+            for (int k = 0; k < 5; ++k) sum = fma(cv[k], v[k], sum);
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(FULL, sum, o);
+            if (lane == 0) {
+                if (hw == 3) {                           // flux end: lane 0 holds the old U[N-1]
+                    double uN;
+                    if (fabs(sum) > 1e-15) uN = (fabs(1.0 - p.AlN) > 1e-15) ? (sum + p.gN * p.dLN) / (1.0 - p.AlN) : uNm1;
+                    else uN = (fabs(1.0 - p.AlN) > 1e-15) ? 0.0 : uNm1;
+                    s_red[3] = uN;
+                } else {
+                    s_red[hw] = sum;
+                }
+            }
+        };
+        constexpr int NR = SpecRing<SP>::NR;
+        float2 *sR = spec_rows;
+        const int rlo0 = max(0, p.j0 - NR);              // rows of earlier launches into the ring
+        for (int r = rlo0; r < p.j0; ++r) {
+#pragma unroll
+            for (int q = 0; q < SP; ++q) {
+                const int i = a + ht + LTS * q;
+                if (i < b) sR[(r % NR) * (LTS * SP) + ht + LTS * q] = p.ringf[(int64_t)r * p.P + i];
+            }
+        }
+        float h3[3][SP], l3[3][SP];                      // H_j0, H_j0+1, H_j0+2
+#pragma unroll
+        for (int m = 0; m < 3; ++m)
+#pragma unroll
+            for (int q = 0; q < SP; ++q) { h3[m][q] = 0.f; l3[m][q] = 0.f; }
+        far_fold_ff<SP, 3>(p, ht, a, b, p.j0, h3, l3);
+        rows_split_ff<SP>(p, sR, ht, a, b, p.j0, max(p.j0 - 2, 0), rlo0, h3[0], l3[0]);
+        history_store_ff<SP>(ht, a, b, h3[0], l3[0], sS[p.j0 & 1]);
+        __syncthreads();                                                    // start: the solver's prologue
+        if (p.j0 + 1 < jend) {                                              // runs beside the rest
+            rows_split_ff<SP>(p, sR, ht, a, b, p.j0 + 1, max(p.j0 - 1, 0), rlo0, h3[1], l3[1]);
+            history_store_ff<SP>(ht, a, b, h3[1], l3[1], sS[(p.j0 + 1) & 1]);
+        }
+        float ah[SP], al[SP];
+#pragma unroll
+        for (int q = 0; q < SP; ++q) { ah[q] = h3[2][q]; al[q] = l3[2][q]; }
+        if (p.j0 + 2 < jend) rows_split_ff<SP>(p, sR, ht, a, b, p.j0 + 2, p.j0, rlo0, ah, al);   // complete
+        const float2 w3 = __ldg(p.wff + 3);
         for (int s = 0; s < p.nsteps; ++s) {
             __syncthreads();                                                // X(s): D_{t-1} is in sD
             if (s_abort) return;
@@ -868,13 +1071,30 @@ __global__ void __launch_bounds__(2 * LTS, 1) k_line_block_spec(LineBlockArgs p)
             if (s > 0) {                                                    // row t-1 as float pairs
                 const double *dd = sD[(t - 1) & 1];
                 float2 *row = p.ringf + (int64_t)(t - 1) * p.P;
+                float2 *srow = sR + ((t - 1) % NR) * (LTS * SP);
 #pragma unroll
                 for (int q = 0; q < SP; ++q) {
                     const int i = a + ht + LTS * q;
-                    if (i < b) row[i] = d2ff(dd[ht + LTS * q]);
+                    if (i < b) {
+                        const float2 f = d2ff(dd[ht + LTS * q]);
+                        row[i] = f;
+                        srow[ht + LTS * q] = f;
+                        if (t + 2 < jend) ff_fma(ah[q], al[q], w3, f);
+                    }
                 }
             }
-            if (t + 2 < jend) history_sum_ff<SP>(p, ht, a, b, t + 2, t, sS[t & 1]);
+            if (t + 2 < jend) history_store_ff<SP>(ht, a, b, ah, al, sS[t & 1]);
+            carries(s);
+            asm volatile("bar.arrive 2, %0;" ::"n"(2 * LTS) : "memory");      // (C): carries of step t
+            if (t + 3 < jend) {
+                float fh[1][SP], fl[1][SP];
+#pragma unroll
+                for (int q = 0; q < SP; ++q) { fh[0][q] = 0.f; fl[0][q] = 0.f; }
+                far_fold_ff<SP, 1>(p, ht, a, b, t + 3, fh, fl);
+#pragma unroll
+                for (int q = 0; q < SP; ++q) { ah[q] = fh[0][q]; al[q] = fl[0][q]; }
+                rows_split_ff<SP>(p, sR, ht, a, b, t + 3, t, max(0, t - NR), ah, al);
+            }
         }
         return;
     }
@@ -895,20 +1115,7 @@ __global__ void __launch_bounds__(2 * LTS, 1) k_line_block_spec(LineBlockArgs p)
         PeF = __ldg(p.sc.lane + 5 * GT + T);
         PeB = __ldg(p.sc.lane + 11 * GT + T);
     }
-    // warp w's carry dot product over the chunks' aggregates: 0 Lf[c].Y (c_in), 1 Mb[c].U0,
-    // 2 Kb[c].Y, 3 Lf[G].Y (the flux end's y; unused at a Dirichlet end)
     const bool flux = p.rkind != FPDE_BC_DIRICHLET;
-    const double *cvec = warp == 0 ? p.Lf + (int64_t)c * G
-                       : warp == 1 ? p.Mb + (int64_t)c * G
-                       : warp == 2 ? p.Kb + (int64_t)c * G
-                                   : p.Lf + (int64_t)G * G;
-    const int slot_off = warp == 1 ? 1 : 0;              // U0 slots for warp 1, Y slots otherwise
-    double cv[5];
-#pragma unroll
-    for (int t = 0; t < 5; ++t) {
-        const int q = lane + 32 * t;
-        cv[t] = q < G ? __ldg(cvec + q) : 0.0;
-    }
     const double mbc = __ldg(p.mb + c);
     double u[SP], kA[SP], kg[SP], kal[SP], kcf[SP], kcb[SP], kCB[SP], kGG[SP], rb1[SP], rb2[SP];
     double dm1[SP];                                      // D_{t-1}
@@ -1001,64 +1208,11 @@ __global__ void __launch_bounds__(2 * LTS, 1) k_line_block_spec(LineBlockArgs p)
                 if (k < cnt) ubw[k] = fma(kcb[k], carry, ubw[k]);
         }
     };
-    // step s's aggregates of every chunk, polled as values (each slot holds the all-bits-set
-    // pattern until its one write of the launch; a 64-bit load is single-copy atomic); each
-    // warp forms its dot product, warp 3 the right end value (U1 :4685-4719)
-    auto gather = [&](int s) {
-        const double *agg = p.agg + (size_t)s * (2 * G + 2);
-        if (warp == 3 && !flux) {
-            if (lane == 0) s_red[3] = p.gN;
-            return;
-        }
-        double v[5], uNm1 = 0.0;
-        bool ok = true;
-        const unsigned long long t0 = gtimer_ns();
-        while (true) {
-            bool mine = true;
-#pragma unroll
-            for (int t = 0; t < 5; ++t) {
-                const int q = lane + 32 * t;
-                v[t] = 0.0;
-                if (q < G) {
-                    const unsigned long long bv = ld_relaxed_u64(agg + 2 * q + slot_off);
-                    if (bv == SLOT_EMPTY) mine = false;
-                    v[t] = __longlong_as_double((long long)bv);
-                }
-            }
-            if (warp == 3 && lane == 0) {
-                const unsigned long long bn = ld_relaxed_u64(agg + 2 * G);
-                if (bn == SLOT_EMPTY) mine = false;
-                uNm1 = __longlong_as_double((long long)bn);
-            }
-            if (__all_sync(FULL, mine)) break;
-            if (gtimer_ns() - t0 > 1000000000ull) { ok = false; break; }
-        }
-        ok = __all_sync(FULL, ok);
-        if (!ok) {
-            if (lane == 0) { atomicOr(p.flags, DEVERR_BARRIER_TIMEOUT); s_abort = 1; }
-            return;
-        }
-        double sum = 0.0;
-#pragma unroll
-        for (int t = 0; t < 5; ++t) sum = fma(cv[t], v[t], sum);
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(FULL, sum, o);
-        if (lane == 0) {
-            if (warp == 3) {                             // flux end: lane 0 holds the old U[N-1]
-                double uN;
-                if (fabs(sum) > 1e-15) uN = (fabs(1.0 - p.AlN) > 1e-15) ? (sum + p.gN * p.dLN) / (1.0 - p.AlN) : uNm1;
-                else uN = (fabs(1.0 - p.AlN) > 1e-15) ? 0.0 : uNm1;
-                s_red[3] = uN;
-            } else {
-                s_red[warp] = sum;
-            }
-        }
-    };
     auto src_row = [&](int64_t n) -> const double * {
         return p.src ? p.src + (int64_t)(n < p.src_rows ? n : p.src_rows - 1) * (N + 1) : nullptr;
     };
 
-    __syncthreads();                                                        // start: H_j0, H_j0+1 ready
+    __syncthreads();                                                        // start: H_j0 ready
     // ---- prologue: step j0 from its full right-hand side
     {
         const double *src = src_row(p.n0);
@@ -1070,8 +1224,8 @@ __global__ void __launch_bounds__(2 * LTS, 1) k_line_block_spec(LineBlockArgs p)
         }
         sweeps();
         double *agg = p.agg;
-        if (ownsN && flux) st_relaxed_f64(agg + 2 * G, u[cnt - 1]);
-        if (last) st_relaxed_f64(agg + 2 * c, yv[cnt - 1]);
+        if (ownsN && flux) st_relaxed_f64(agg + 2 * G, last_of<SP>(u, cnt));
+        if (last) st_relaxed_f64(agg + 2 * c, last_of<SP>(yv, cnt));
         if (tid == 0) st_relaxed_f64(agg + 2 * c + 1, ubw[0]);
     }
     double ubc[SP], ubp[SP], ubprev[SP];                 // ub_t corrected, ub'_{t+1}, ub_{t-1}
@@ -1082,7 +1236,15 @@ __global__ void __launch_bounds__(2 * LTS, 1) k_line_block_spec(LineBlockArgs p)
     for (int s = 0; s < p.nsteps; ++s) {
         const int t = p.j0 + s;
         if (s > 0) {
-            // ---- carries of step t-1: state u^t, increment D_{t-1}; step t's corrected results
+            // ---- carries of step t-1: first step t's corrected aggregates (the chunk's last y,
+            // first u; at a flux end the new U[N-1]) go out, then state u^t, increment D_{t-1}
+            // and the corrected backward results
+            double *agg = p.agg + (size_t)s * (2 * G + 2);
+            if (last) st_relaxed_f64(agg + 2 * c, fma(ry2, ubv, fma(ry1, cin, ypl)));
+            if (tid == 0) st_relaxed_f64(agg + 2 * c + 1, fma(rb2[0], ubv, fma(rb1[0], cin, ubp[0])));
+            if (ownsN && flux)
+                st_relaxed_f64(agg + 2 * G, fma(last_of<SP>(kCB, cnt), ubv,
+                                                fma(last_of<SP>(kGG, cnt), cin, last_of<SP>(ubprev, cnt))));
             double *dsh = sD[(t - 1) & 1];
 #pragma unroll
             for (int k = 0; k < SP; ++k) {
@@ -1101,10 +1263,6 @@ __global__ void __launch_bounds__(2 * LTS, 1) k_line_block_spec(LineBlockArgs p)
                 p.ring[(int64_t)(t - 1) * p.P + N] = UN - uNv;
                 uNv = UN;
             }
-            double *agg = p.agg + (size_t)s * (2 * G + 2);
-            if (ownsN && flux) st_relaxed_f64(agg + 2 * G, u[cnt - 1]);
-            if (last) st_relaxed_f64(agg + 2 * c, fma(ry2, ubv, fma(ry1, cin, ypl)));
-            if (tid == 0) st_relaxed_f64(agg + 2 * c + 1, ubc[0]);
         }
         __syncthreads();                                                    // X(s)
         if (t + 1 < jend) {
@@ -1129,12 +1287,11 @@ __global__ void __launch_bounds__(2 * LTS, 1) k_line_block_spec(LineBlockArgs p)
                 }
             }
             sweeps();
-            ypl = last ? yv[cnt - 1] : 0.0;
+            ypl = last ? last_of<SP>(yv, cnt) : 0.0;
 #pragma unroll
             for (int k = 0; k < SP; ++k) ubp[k] = ubw[k];
         }
-        gather(s);
-        solver_sync();                                                      // (D)
+        asm volatile("bar.sync 2, %0;" ::"n"(2 * LTS) : "memory");         // (C): carries of step t
         if (s_abort) {
             if (s + 1 < p.nsteps) __syncthreads();      // release the history warps at X(s+1)
             return;
@@ -1269,10 +1426,32 @@ static cudaEvent_t *probe_begin(fpde_line *L, int kind, int64_t n, double bytes,
     return &L->probe_ev[2 * k];
 }
 
-template <int SP>
-static cudaError_t launch_block_sp(const cudaLaunchConfig_t &cfg, const LineBlockArgs &a, bool spec)
+// Opt the speculative kernels in to their dynamic shared memory (the row ring) once.
+static cudaError_t spec_smem_attrs()
 {
-    return spec ? cudaLaunchKernelEx(&cfg, k_line_block_spec<SP>, a) : cudaLaunchKernelEx(&cfg, k_line_block<SP>, a);
+    static cudaError_t done = [] {
+        cudaError_t e = cudaFuncSetAttribute(k_line_block_spec<1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)SpecRing<1>::bytes);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(k_line_block_spec<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)SpecRing<2>::bytes);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(k_line_block_spec<4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)SpecRing<4>::bytes);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(k_line_block_spec<8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)SpecRing<8>::bytes);
+        return e;
+    }();
+    return done;
+}
+
+template <int SP>
+static cudaError_t launch_block_sp(cudaLaunchConfig_t cfg, const LineBlockArgs &a, bool spec)
+{
+    if (!spec) return cudaLaunchKernelEx(&cfg, k_line_block<SP>, a);
+    cfg.dynamicSmemBytes = SpecRing<SP>::bytes;
+    return cudaLaunchKernelEx(&cfg, k_line_block_spec<SP>, a);
 }
 
 // Steps j0 .. j0+nsteps-1 of the block starting at nb0 in one persistent launch.
@@ -1520,7 +1699,9 @@ int fpde_line_create(fpde_ctx *ctx, const fpde_line_desc *desc, const double *A,
     if (split) {
         int per_sm2 = 0;
         FPDE_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_line_block<LSEG>, 2 * LTS, 0));
-        FPDE_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm2, k_line_block_spec<LSEG>, 2 * LTS, 0));
+        FPDE_CUDA(spec_smem_attrs());
+        FPDE_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm2, k_line_block_spec<LSEG>, 2 * LTS,
+                                                                SpecRing<LSEG>::bytes));
         per_sm = std::min(per_sm, per_sm2);
     }
     else FPDE_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_line_solve<LSEG>, LT, 0));
