@@ -390,12 +390,16 @@ def _probe(line, u0_dev, steps, every):
 
 
 # DRAM traffic per launch from ncu captures (profiles/), as bytes per unit the launch processes:
-#   k_line_block: per node-step (79.8 MB for 64 steps x 65,537 nodes, 2 far splits)
-#   k_far_tc3   : per node x history step (629.2 MB for 65,664 rows x 1,344 steps)
+#   k_line_block_spec: per node-step (107.5 MB for 64 steps x 65,537 nodes, 2 far splits)
+#   k_far_tc3        : per node x history step (587.3 MB for 65,664 rows x 1,344 steps)
 NCU_TRAFFIC = {
-    "solve_split": (79.76e6 / (64 * 65537), "profiles/k_line_block_N65536_2048steps.md"),
-    "far_tc": (629.24e6 / (65664 * 1344), "profiles/k_far_tc3_N65536_K1344.md"),
+    "solve_split": ((79.91e6 + 27.61e6) / (64 * 65537), "profiles/k_line_block_spec_N65536_2048steps.md"),
+    "far_tc": ((533.41e6 + 53.86e6) / (65664 * 1344), "profiles/k_far_tc3_N65536_K1344.md"),
 }
+# The speculative block solve is bound by neither HBM nor the tensor cores but by GB300's FP64
+# pipe (2 DFMA/clk/SM) and its per-step synchronisation: ncu's sm__pipe_fp64_cycles_active for
+# one launch (same capture as its traffic).
+SOLVE_FP64_PIPE = (0.5196, "profiles/k_line_block_spec_N65536_2048steps.md")
 
 
 def _kernel_entry(t, name, peak, peak_src, scale=1.0):
@@ -520,7 +524,9 @@ def run_ours(args):
         else:
             kernels["far_tc"] = _kernel_entry(tot[1], "k_far_tc3/k_far_tc (tcgen05 far-history contraction)",
                                               peak, peak_src, 1.0)
-            solve_name = "k_line_block (far fold + FP64 near history + Thomas, one launch per 64-step block)"
+            solve_name = ("k_line_block_spec (far fold, float-float near history, speculative FP64 Thomas; "
+                          "one launch per 64-step block)" if not wl.do else
+                          "k_line_block (far fold + FP64 near history + Thomas, one launch per 64-step block)")
         kernels["solve"] = _kernel_entry(tot[2], solve_name, peak, peak_src, per(tot[2]))
         kernels = {k: v for k, v in kernels.items() if v}
         if prec == fp.FPDE_PREC_SPLIT_BF16X3 and not wl.do:   # traffic per launch, scaled to this line
@@ -530,6 +536,9 @@ def run_ours(args):
                 kernels["solve"]["traffic"] = per * nodes
                 kernels["solve"]["traffic_unit"] = "bytes per step (ncu, scaled by nodes)"
                 kernels["solve"]["traffic_source"] = src
+                kernels["solve"]["limiter"] = "fp64 pipe + per-step synchronisation (not HBM)"
+                kernels["solve"]["fp64_pipe_active"] = SOLVE_FP64_PIPE[0]
+                kernels["solve"]["fp64_pipe_source"] = SOLVE_FP64_PIPE[1]
             if "far_tc" in kernels:
                 per, src = NCU_TRAFFIC["far_tc"]
                 avg_k = 64 * (steps // 64 - 1) / 2.0
