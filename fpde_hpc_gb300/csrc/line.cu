@@ -363,6 +363,10 @@ struct LineBlockArgs {
     const double *RB1, *RB2, *RY1, *RY2;  // speculative kernel: sweep responses to E1, E2
     float2 *ringf;                        // speculative kernel: the ring as float pairs
     const float2 *wff;                    // speculative kernel: w[lag] as float pairs
+    // speculative kernel: right-hand side pre-scaled by -g so the forward sweep is one FMA
+    // (y = ga y + Om', ga = g A, Om' = -g Om): ng = -g, c1 = -g (w1 - lam), c2 = g w1, c3 = -g w2
+    const double *ga, *ng, *c1, *c2, *c3;
+    const float2 *ngf;                    // -g as float pairs (the history warps deliver -g H)
     unsigned *flags;
     double lam, g0, gN, dLN, AlN;
     int64_t n0;                           // global index of step j0
@@ -608,6 +612,22 @@ __device__ __forceinline__ void history_store_ff(int ht, int a, int b, const flo
 #pragma unroll
     for (int q = 0; q < SP; ++q)
         if (a + ht + LTS * q < b) out[ht + LTS * q] = f2d_bits(ah[q]) + f2d_bits(al[q]);
+}
+
+// The same, times the per-node factor sg (a float pair): (ah + al) sg in float-float, one FP64 add.
+template <int SP>
+__device__ __forceinline__ void history_store_scaled_ff(int ht, int a, int b, const float *ah, const float *al,
+                                                        const float2 *sg, double *out)
+{
+#pragma unroll
+    for (int q = 0; q < SP; ++q)
+        if (a + ht + LTS * q < b) {
+            const float ph = __fmul_rn(ah[q], sg[q].x);
+            float pe = __fmaf_rn(ah[q], sg[q].x, -ph);
+            pe = __fmaf_rn(ah[q], sg[q].y, pe);
+            pe = __fmaf_rn(al[q], sg[q].x, pe);
+            out[ht + LTS * q] = f2d_bits(ph) + f2d_bits(pe);
+        }
 }
 
 template <int SP>
@@ -1046,6 +1066,12 @@ __global__ void __launch_bounds__(2 * LTS, 1) k_line_block_spec(LineBlockArgs p)
                 if (i < b) sR[(r % NR) * (LTS * SP) + ht + LTS * q] = p.ringf[(int64_t)r * p.P + i];
             }
         }
+        float2 sg[SP];                                   // -g of this thread's nodes
+#pragma unroll
+        for (int q = 0; q < SP; ++q) {
+            const int i = a + ht + LTS * q;
+            sg[q] = i < b ? __ldg(p.ngf + i) : make_float2(0.f, 0.f);
+        }
         float h3[3][SP], l3[3][SP];                      // H_j0, H_j0+1, H_j0+2
 #pragma unroll
         for (int m = 0; m < 3; ++m)
@@ -1053,11 +1079,11 @@ __global__ void __launch_bounds__(2 * LTS, 1) k_line_block_spec(LineBlockArgs p)
             for (int q = 0; q < SP; ++q) { h3[m][q] = 0.f; l3[m][q] = 0.f; }
         far_fold_ff<SP, 3>(p, ht, a, b, p.j0, h3, l3);
         rows_split_ff<SP>(p, sR, ht, a, b, p.j0, max(p.j0 - 2, 0), rlo0, h3[0], l3[0]);
-        history_store_ff<SP>(ht, a, b, h3[0], l3[0], sS[p.j0 & 1]);
+        history_store_scaled_ff<SP>(ht, a, b, h3[0], l3[0], sg, sS[p.j0 & 1]);
         __syncthreads();                                                    // start: the solver's prologue
         if (p.j0 + 1 < jend) {                                              // runs beside the rest
             rows_split_ff<SP>(p, sR, ht, a, b, p.j0 + 1, max(p.j0 - 1, 0), rlo0, h3[1], l3[1]);
-            history_store_ff<SP>(ht, a, b, h3[1], l3[1], sS[(p.j0 + 1) & 1]);
+            history_store_scaled_ff<SP>(ht, a, b, h3[1], l3[1], sg, sS[(p.j0 + 1) & 1]);
         }
         float ah[SP], al[SP];
 #pragma unroll
@@ -1083,7 +1109,7 @@ __global__ void __launch_bounds__(2 * LTS, 1) k_line_block_spec(LineBlockArgs p)
                     }
                 }
             }
-            if (t + 2 < jend) history_store_ff<SP>(ht, a, b, ah, al, sS[t & 1]);
+            if (t + 2 < jend) history_store_scaled_ff<SP>(ht, a, b, ah, al, sg, sS[t & 1]);
             carries(s);
             asm volatile("bar.arrive 2, %0;" ::"n"(2 * LTS) : "memory");      // (C): carries of step t
             if (t + 3 < jend) {
@@ -1117,7 +1143,8 @@ __global__ void __launch_bounds__(2 * LTS, 1) k_line_block_spec(LineBlockArgs p)
     }
     const bool flux = p.rkind != FPDE_BC_DIRICHLET;
     const double mbc = __ldg(p.mb + c);
-    double u[SP], kA[SP], kg[SP], kal[SP], kcf[SP], kcb[SP], kCB[SP], kGG[SP], rb1[SP], rb2[SP];
+    double u[SP], kga[SP], kng[SP], kc1[SP], kc2[SP], kc3[SP], kal[SP], kcf[SP], kcb[SP], kCB[SP], kGG[SP];
+    double rb1[SP], rb2[SP];
     double dm1[SP];                                      // D_{t-1}
     double dm2[SP];                                      // D_{t-2} (prologue only)
 #pragma unroll
@@ -1125,8 +1152,11 @@ __global__ void __launch_bounds__(2 * LTS, 1) k_line_block_spec(LineBlockArgs p)
         const bool in = k < cnt;
         const int i = in ? i0 + k : 0;
         u[k] = in ? p.U[i] : 0.0;
-        kA[k] = in ? __ldg(p.A + i) : 0.0;
-        kg[k] = in ? __ldg(p.g + i) : 0.0;
+        kga[k] = in ? __ldg(p.ga + i) : 0.0;
+        kng[k] = in ? __ldg(p.ng + i) : 0.0;
+        kc1[k] = in ? __ldg(p.c1 + i) : 0.0;
+        kc2[k] = in ? __ldg(p.c2 + i) : 0.0;
+        kc3[k] = in ? __ldg(p.c3 + i) : 0.0;
         kal[k] = in ? __ldg(p.al + i) : 0.0;
         kcf[k] = in ? __ldg(p.cf + i) : 0.0;
         kcb[k] = in ? __ldg(p.cb + i) : 0.0;
@@ -1151,7 +1181,7 @@ __global__ void __launch_bounds__(2 * LTS, 1) k_line_block_spec(LineBlockArgs p)
         for (int k = 0; k < SP; ++k) {
             if (k < cnt) {
                 if (i0 + k == 0) yl = p.g0;
-                else yl = kg[k] * (kA[k] * yl - om[k]);
+                else yl = fma(kga[k], yl, om[k]);           // om holds -g Om
                 yv[k] = yl;
             }
         }
@@ -1216,11 +1246,14 @@ __global__ void __launch_bounds__(2 * LTS, 1) k_line_block_spec(LineBlockArgs p)
     // ---- prologue: step j0 from its full right-hand side
     {
         const double *src = src_row(p.n0);
-        const double *hs = sS[p.j0 & 1];
+        const double *hs = sS[p.j0 & 1];                 // -g H_j0
 #pragma unroll
         for (int k = 0; k < SP; ++k) {
-            const double S = k < cnt ? fma(w1, dm1[k], fma(w2, dm2[k], hs[i0 - a + k])) : 0.0;
-            om[k] = (-(lam * u[k]) + ((src && k < cnt) ? __ldg(src + i0 + k) : 0.0)) + S;
+            om[k] = 0.0;
+            if (k < cnt) {
+                const double rest = (-(lam * u[k]) + (src ? __ldg(src + i0 + k) : 0.0)) + fma(w1, dm1[k], w2 * dm2[k]);
+                om[k] = fma(kng[k], rest, hs[i0 - a + k]);
+            }
         }
         sweeps();
         double *agg = p.agg;
@@ -1268,22 +1301,21 @@ __global__ void __launch_bounds__(2 * LTS, 1) k_line_block_spec(LineBlockArgs p)
         if (t + 1 < jend) {
             // ---- step t+1 on Omega0, while the aggregates of step t are exchanged
             const double *src = src_row(p.n0 + s + 1);
-            const double *hs = sS[(t + 1) & 1];
-            const double cE = w1 - lam;
+            const double *hs = sS[(t + 1) & 1];          // -g H_{t+1}
             if (src) {
 #pragma unroll
                 for (int k = 0; k < SP; ++k) {
                     om[k] = 0.0;
                     if (k < cnt) {
-                        const double h = fma(w2, dm1[k], hs[i0 - a + k]) + __ldg(src + i0 + k);
-                        om[k] = fma(cE, ubc[k], fma(-w1, u[k], h));
+                        const double h = fma(kng[k], __ldg(src + i0 + k), fma(kc3[k], dm1[k], hs[i0 - a + k]));
+                        om[k] = fma(kc1[k], ubc[k], fma(kc2[k], u[k], h));
                     }
                 }
             } else {
 #pragma unroll
                 for (int k = 0; k < SP; ++k) {
                     om[k] = 0.0;
-                    if (k < cnt) om[k] = fma(cE, ubc[k], fma(-w1, u[k], fma(w2, dm1[k], hs[i0 - a + k])));
+                    if (k < cnt) om[k] = fma(kc1[k], ubc[k], fma(kc2[k], u[k], fma(kc3[k], dm1[k], hs[i0 - a + k])));
                 }
             }
             sweeps();
@@ -1340,6 +1372,8 @@ struct fpde_line {
     bool spec = false;
     double *RB1 = nullptr, *RB2 = nullptr, *RY1 = nullptr, *RY2 = nullptr;
     float2 *ringf = nullptr, *wff = nullptr;  // the ring and the lag weights as float pairs
+    double *sga = nullptr, *sng = nullptr, *sc1 = nullptr, *sc2 = nullptr, *sc3 = nullptr;  // -g pre-scaling
+    float2 *sngf = nullptr;
     double *Lf = nullptr, *Mb = nullptr, *Kb = nullptr, *mb = nullptr;
     unsigned long long *cflag = nullptr, *seq = nullptr, *hflag = nullptr;
     double *halo = nullptr, *sclane = nullptr, *scwarp = nullptr;
@@ -1468,6 +1502,7 @@ static int line_launch_block(fpde_line *L, cudaStream_t st, int64_t nb0, int j0,
     a.sc.lane = L->sclane; a.sc.warp = L->scwarp;
     a.RB1 = L->RB1; a.RB2 = L->RB2; a.RY1 = L->RY1; a.RY2 = L->RY2;
     a.ringf = L->ringf; a.wff = L->wff;
+    a.ga = L->sga; a.ng = L->sng; a.c1 = L->sc1; a.c2 = L->sc2; a.c3 = L->sc3; a.ngf = L->sngf;
     a.lam = L->lam; a.g0 = L->d.left_value; a.gN = L->d.right_value; a.dLN = L->d.dLN; a.AlN = L->AlN;
     a.n0 = nb0 + j0; a.j0 = j0; a.nsteps = nsteps; a.N = (int)L->N; a.G = L->G; a.rkind = L->d.right_kind;
     a.chunk = L->chunk;
@@ -1622,6 +1657,8 @@ int fpde_line_destroy(fpde_line *L)
         dev_free(p);
     dev_free(L->ringf);
     dev_free(L->wff);
+    for (double *q : {L->sga, L->sng, L->sc1, L->sc2, L->sc3}) dev_free(q);
+    dev_free(L->sngf);
     for (uint16_t *p : {L->h_hi, L->h_lo, L->w_hi, L->w_lo, L->h3[0], L->h3[1], L->h3[2], L->w3[0], L->w3[1],
                         L->w3[2]})
         dev_free(p);
@@ -1964,7 +2001,9 @@ int fpde_line_create(fpde_ctx *ctx, const fpde_line_desc *desc, const double *A,
     if (!fail && L->spec)
         fail = dev_alloc((void **)&L->RB1, nb) || dev_alloc((void **)&L->RB2, nb) || dev_alloc((void **)&L->RY1, nb) ||
                dev_alloc((void **)&L->RY2, nb) || dev_alloc((void **)&L->ringf, (size_t)BLK * L->P * sizeof(float2)) ||
-               dev_alloc((void **)&L->wff, (size_t)LW * sizeof(float2));
+               dev_alloc((void **)&L->wff, (size_t)LW * sizeof(float2)) || dev_alloc((void **)&L->sga, nb) ||
+               dev_alloc((void **)&L->sng, nb) || dev_alloc((void **)&L->sc1, nb) || dev_alloc((void **)&L->sc2, nb) ||
+               dev_alloc((void **)&L->sc3, nb) || dev_alloc((void **)&L->sngf, (size_t)N * sizeof(float2));
     if (fail) {
         std::string keep = fpde_last_error_string();
         fpde_line_destroy(L);
@@ -1991,6 +2030,24 @@ int fpde_line_create(fpde_ctx *ctx, const fpde_line_desc *desc, const double *A,
         cudaMemcpyAsync(L->RY1, hRY1.data(), nb, cudaMemcpyHostToDevice, st);
         cudaMemcpyAsync(L->RY2, hRY2.data(), nb, cudaMemcpyHostToDevice, st);
         cudaMemcpyAsync(L->wff, hwff.data(), (size_t)LW * sizeof(float2), cudaMemcpyHostToDevice, st);
+        std::vector<double> h1(N), h2(N), h3(N), h4(N), h5(N);
+        std::vector<float2> hngf(N);
+        const double w1 = wlag[1], w2 = wlag[2], cE = w1 - L->lam;
+        for (int64_t i = 0; i < N; ++i) {
+            h1[i] = hp[i];                         // g A
+            h2[i] = -hg[i];
+            h3[i] = -hg[i] * cE;
+            h4[i] = hg[i] * w1;
+            h5[i] = -hg[i] * w2;
+            const float hi = (float)h2[i];
+            hngf[i] = make_float2(hi, (float)(h2[i] - (double)hi));
+        }
+        cudaMemcpyAsync(L->sga, h1.data(), nb, cudaMemcpyHostToDevice, st);
+        cudaMemcpyAsync(L->sng, h2.data(), nb, cudaMemcpyHostToDevice, st);
+        cudaMemcpyAsync(L->sc1, h3.data(), nb, cudaMemcpyHostToDevice, st);
+        cudaMemcpyAsync(L->sc2, h4.data(), nb, cudaMemcpyHostToDevice, st);
+        cudaMemcpyAsync(L->sc3, h5.data(), nb, cudaMemcpyHostToDevice, st);
+        cudaMemcpyAsync(L->sngf, hngf.data(), (size_t)N * sizeof(float2), cudaMemcpyHostToDevice, st);
         cudaMemsetAsync(L->ringf, 0, (size_t)BLK * L->P * sizeof(float2), st);
     }
     if (L->srcd)

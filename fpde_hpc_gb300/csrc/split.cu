@@ -172,7 +172,8 @@ __device__ __forceinline__ int exp_of_maxbits(unsigned long long mbits)
 }
 
 // One thread per node: the node's 64 increments of the finished block (time-major ring: the
-// threads of a warp read consecutive nodes of one row).
+// threads of a warp read consecutive nodes of one row). All 64 are loaded at once (the ring was
+// just written and sits in L2) and kept in registers for both passes.
 __global__ void __launch_bounds__(128) k_convert3(const double *__restrict__ ring, int64_t P, int64_t nvalid,
                                                   uint16_t *__restrict__ h0, uint16_t *__restrict__ h1,
                                                   uint16_t *__restrict__ h2, int64_t ld, int64_t col0,
@@ -181,21 +182,23 @@ __global__ void __launch_bounds__(128) k_convert3(const double *__restrict__ rin
     const int64_t node = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (node >= nvalid) return;
     const unsigned long long *src = (const unsigned long long *)ring + node;
+    unsigned long long v[64];
+#pragma unroll
+    for (int r = 0; r < 64; ++r) v[r] = __ldcg(src + (int64_t)r * P);
     unsigned long long mb = 0;
-#pragma unroll 16
+#pragma unroll
     for (int r = 0; r < 64; ++r) {
-        const unsigned long long m0 = __ldg(src + (int64_t)r * P) & 0x7FFFFFFFFFFFFFFFull;
+        const unsigned long long m0 = v[r] & 0x7FFFFFFFFFFFFFFFull;
         mb = m0 > mb ? m0 : mb;
     }
     const int pe = exp_of_maxbits(mb);
     pA[node * ldp + blk] = (int8_t)pe;
+#pragma unroll
     for (int g = 0; g < 8; ++g) {
         uint16_t a[8], b[8], c[8];
 #pragma unroll
-        for (int k = 0; k < 8; ++k) {
-            const unsigned long long v = __ldg(src + (int64_t)(8 * g + k) * P);
-            digits3(fixed16(__longlong_as_double((long long)v), pe), a[k], b[k], c[k]);
-        }
+        for (int k = 0; k < 8; ++k)
+            digits3(fixed16(__longlong_as_double((long long)v[8 * g + k]), pe), a[k], b[k], c[k]);
         uint4 va, vb, vc;
         va.x = a[0] | ((uint32_t)a[1] << 16); va.y = a[2] | ((uint32_t)a[3] << 16);
         va.z = a[4] | ((uint32_t)a[5] << 16); va.w = a[6] | ((uint32_t)a[7] << 16);
