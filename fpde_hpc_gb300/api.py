@@ -259,6 +259,12 @@ class Line:
         check(self.ctx.lib.fpde_line_steps_done(self.h, C.byref(n)), "fpde_line_steps_done")
         return n.value
 
+    def step_block(self):
+        """fpde_step_block: advance to the next 64-step block boundary; returns the steps run."""
+        n = C.c_int()
+        check(self.ctx.lib.fpde_step_block(self.h, C.byref(n)), "fpde_step_block")
+        return n.value
+
 
 class Lod3D:
     """The 3D LOD step of the reference (fpde_lod3d_*): grids are numpy arrays of shape

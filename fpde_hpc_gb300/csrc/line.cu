@@ -2249,6 +2249,17 @@ int fpde_line_steps_done(const fpde_line *L, int64_t *n)
     return FPDE_OK;
 }
 
+int fpde_step_block(fpde_line *L, int *steps_run)
+{
+    clear_error();
+    FPDE_CHECK_ARG(L && steps_run, "null argument");
+    static_assert(FPDE_BLOCK_STEPS == BLK, "block length");
+    const int64_t to_end = BLK - L->n_done % BLK;
+    const int steps = (int)std::min<int64_t>(to_end, (int64_t)L->max_steps - L->n_done);
+    *steps_run = steps > 0 ? steps : 0;
+    return steps > 0 ? fpde_line_run(L, steps) : FPDE_OK;
+}
+
 }  // extern "C"
 
 // ---------------------------------------------------------------------------------- autotuner

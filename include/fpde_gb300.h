@@ -271,6 +271,13 @@ int fpde_line_state_ptr(fpde_line *line, double **u_dev);
 int fpde_line_solve_host(fpde_line *line, const double *u0_host, int steps, double *u_out_host);
 /* Current step count. */
 int fpde_line_steps_done(const fpde_line *line, int64_t *n);
+/* One block of the blocked schedule: advance to the next multiple of FPDE_BLOCK_STEPS (64) steps
+ * (or to max_steps), i.e. append -> far history of the block -> near history -> RHS -> solve for
+ * every step of the block, as one captured graph; *steps_run receives the count (0 when the
+ * history is full). Replaces the per-step `calc_step` -> `fr_ocl_call_sum` -> `time_summing`
+ * sequence (fpde_hpc_1d.cpp:5156-5157, :1835-1880, :4100-4104) for a whole block at once. */
+#define FPDE_BLOCK_STEPS 64
+int fpde_step_block(fpde_line *line, int *steps_run);
 /* Kernel timing probes (no counterpart in the reference, which times whole calls with
  * clock_gettime, opencl_cuda_base.cpp:708-716): with every > 0, later runs record CUDA
  * events inside the captured graph around the history-sum and solve kernels of every

@@ -75,3 +75,25 @@ def test_split_config1_vs_oracle(ctx):
     err = relmax(us, uref)
     print(f"bf16 x3 split, config 1 (N=1000, 1000 steps) vs oracle: max rel {err:.3e}")
     assert err <= 1e-7
+
+
+def test_step_block_walks_the_blocks(ctx):
+    """fpde_step_block advances to each 64-step boundary (the last block ends at max_steps):
+    from step 0 it makes the same launches as one run over all steps (bit-identical state);
+    from step 10 the first call runs the 54 steps to the boundary (the restarted launch sums
+    its first history rows in another float-float order, so the states agree to rounding)."""
+    import fpde_hpc_gb300 as fp
+    from fpde_hpc_gb300 import problems
+    p = problems.config2(N=4096, steps=200)
+    A, B, R = p.coefs()
+    u_run = _run(ctx, p, p.steps, 3)
+    line = fp.Line(ctx, p.N, p.alpha, p.tau, p.Da, A, B, R, p.u0, p.steps, precision=3)
+    got = [line.step_block() for _ in range(5)]
+    assert got == [64, 64, 64, 8, 0]
+    assert np.array_equal(line.state(), u_run)
+    line.reset(p.u0)
+    line.run(10)
+    got = [line.step_block() for _ in range(4)]
+    assert got == [54, 64, 64, 8]
+    assert relmax(line.state(), u_run) <= 1e-9
+    line.close()
