@@ -209,7 +209,8 @@ struct fpde_batch {
     bool split = false;
     int64_t ld16 = 0, ldp = 0, LW = 0;
     uint16_t *h3[3] = {nullptr, nullptr, nullptr}, *w3[3] = {nullptr, nullptr, nullptr};
-    int8_t *pA = nullptr, *pW = nullptr;
+    int8_t *pA = nullptr;
+    float *pW = nullptr;
     double *ring = nullptr, *cfar = nullptr, *wlag = nullptr, *Sn = nullptr;
     int *wcol = nullptr;
     FarPlan3 plan3;
@@ -435,7 +436,7 @@ int fpde_batch_create(fpde_ctx *ctx, const fpde_column_desc *cols, int n_cols, i
             fail = dev_alloc((void **)&b->h3[q], (size_t)tot * b->ld16 * 2) ||
                    dev_alloc((void **)&b->w3[q], (size_t)wrows * b->ld16 * 2);
         fail = fail || dev_alloc((void **)&b->pA, (size_t)tot * b->ldp) ||
-               dev_alloc((void **)&b->pW, (size_t)wrows * b->ldp) || dev_alloc((void **)&b->ring, (size_t)64 * tb) ||
+               dev_alloc((void **)&b->pW, (size_t)wrows * b->ldp * sizeof(float)) || dev_alloc((void **)&b->ring, (size_t)64 * tb) ||
                dev_alloc((void **)&b->cfar, (size_t)FAR_MAX_SPLITS * 64 * tb) ||
                dev_alloc((void **)&b->wlag, hwl.size() * sizeof(double)) || dev_alloc((void **)&b->Sn, tb) ||
                dev_alloc((void **)&b->wcol, hwcol.size() * sizeof(int));
@@ -474,7 +475,7 @@ int fpde_batch_create(fpde_ctx *ctx, const fpde_column_desc *cols, int n_cols, i
             cudaMemsetAsync(b->w3[q], 0, (size_t)wrows * b->ld16 * 2, st);
         }
         cudaMemsetAsync(b->pA, 0, (size_t)tot * b->ldp, st);
-        cudaMemsetAsync(b->pW, 0, (size_t)wrows * b->ldp, st);
+        cudaMemsetAsync(b->pW, 0, (size_t)wrows * b->ldp * sizeof(float), st);
         cudaMemsetAsync(b->ring, 0, (size_t)64 * tb, st);
         cudaMemsetAsync(b->cfar, 0, (size_t)FAR_MAX_SPLITS * 64 * tb, st);
         cudaMemcpyAsync(b->wlag, hwl.data(), hwl.size() * sizeof(double), cudaMemcpyHostToDevice, st);

@@ -46,7 +46,8 @@ struct SplitPrep3 {
     uint16_t *hist[3] = {nullptr, nullptr, nullptr};
     uint16_t *w[3] = {nullptr, nullptr, nullptr};
     int64_t ld = 0;
-    int8_t *pA = nullptr, *pW = nullptr;
+    int8_t *pA = nullptr;                // per (node, k-tile) exponents
+    float *pW = nullptr;                 // per (step, k-tile) scales 2^e of the weight tiles
     int64_t ldp = 0;
     const double *wlag = nullptr;        // w[lag] (per column: ncols rows of wstride)
     int ncols = 1;                       // weight tiles (columns of an ensemble)

@@ -1393,7 +1393,8 @@ struct fpde_line {
     // exact three-slice form
     bool x3 = false;
     uint16_t *h3[3] = {nullptr, nullptr, nullptr}, *w3[3] = {nullptr, nullptr, nullptr};
-    int8_t *pA = nullptr, *pW = nullptr;
+    int8_t *pA = nullptr;
+    float *pW = nullptr;
     int64_t ldp = 0;
     FarPlan3 plan3;
     int64_t n_done = 0;
@@ -1955,7 +1956,7 @@ int fpde_line_create(fpde_ctx *ctx, const fpde_line_desc *desc, const double *A,
             fail = dev_alloc((void **)&L->h3[q], (size_t)L->rows16 * L->ld16 * 2) ||
                    dev_alloc((void **)&L->w3[q], (size_t)BLK * L->ld16 * 2);
         fail = fail || dev_alloc((void **)&L->pA, (size_t)L->rows16 * L->ldp) ||
-               dev_alloc((void **)&L->pW, (size_t)BLK * L->ldp) ||
+               dev_alloc((void **)&L->pW, (size_t)BLK * L->ldp * sizeof(float)) ||
                dev_alloc((void **)&L->ring, (size_t)BLK * L->P * sizeof(double)) ||
                dev_alloc((void **)&L->cfar, (size_t)FAR_MAX_SPLITS * BLK * L->P * sizeof(double)) ||
                dev_alloc((void **)&L->wlag, LW * sizeof(double));
@@ -2083,7 +2084,7 @@ int fpde_line_create(fpde_ctx *ctx, const fpde_line_desc *desc, const double *A,
             cudaMemsetAsync(L->w3[q], 0, (size_t)BLK * L->ld16 * 2, st);
         }
         cudaMemsetAsync(L->pA, 0, (size_t)L->rows16 * L->ldp, st);
-        cudaMemsetAsync(L->pW, 0, (size_t)BLK * L->ldp, st);
+        cudaMemsetAsync(L->pW, 0, (size_t)BLK * L->ldp * sizeof(float), st);
         cudaMemsetAsync(L->ring, 0, (size_t)BLK * L->P * sizeof(double), st);
         cudaMemsetAsync(L->cfar, 0, (size_t)FAR_MAX_SPLITS * BLK * L->P * sizeof(double), st);
         cudaMemcpyAsync(L->wlag, wlag.data(), LW * sizeof(double), cudaMemcpyHostToDevice, st);
@@ -2370,13 +2371,14 @@ extern "C" int fpde_line_autotune(fpde_ctx *ctx, const fpde_line_desc *desc, con
         // 2. split depth of the far contraction at a history of kt_steps columns (zero data)
         const int64_t rows = (N + 1 + 127) / 128 * 128, ldp = kt_steps / 64;
         uint16_t *a3[3] = {nullptr, nullptr, nullptr}, *w3[3] = {nullptr, nullptr, nullptr};
-        int8_t *pA = nullptr, *pW = nullptr;
+        int8_t *pA = nullptr;
+        float *pW = nullptr;
         double *C = nullptr;
         bool fail = false;
         for (int q = 0; q < 3 && !fail; ++q)
             fail = dev_alloc((void **)&a3[q], (size_t)rows * kt_steps * 2) ||
                    dev_alloc((void **)&w3[q], (size_t)64 * kt_steps * 2);
-        fail = fail || dev_alloc((void **)&pA, (size_t)rows * ldp) || dev_alloc((void **)&pW, (size_t)64 * ldp) ||
+        fail = fail || dev_alloc((void **)&pA, (size_t)rows * ldp) || dev_alloc((void **)&pW, (size_t)64 * ldp * sizeof(float)) ||
                dev_alloc((void **)&C, (size_t)FAR_MAX_SPLITS * 64 * rows * sizeof(double));
         if (!fail) {
             for (int q = 0; q < 3; ++q) {
@@ -2384,7 +2386,7 @@ extern "C" int fpde_line_autotune(fpde_ctx *ctx, const fpde_line_desc *desc, con
                 cudaMemsetAsync(w3[q], 0, (size_t)64 * kt_steps * 2, st);
             }
             cudaMemsetAsync(pA, 0, (size_t)rows * ldp, st);
-            cudaMemsetAsync(pW, 0, (size_t)64 * ldp, st);
+            cudaMemsetAsync(pW, 0, (size_t)64 * ldp * sizeof(float), st);
             FarPlan3 plan;
             const void *ap[3] = {a3[0], a3[1], a3[2]}, *wp[3] = {w3[0], w3[1], w3[2]};
             if (far_plan3_init(&plan, ap, rows, kt_steps, wp, kt_steps) == FPDE_OK) {

@@ -194,7 +194,8 @@ struct fpde_lod3d {
     bool split = false;
     int64_t rows16 = 0, ld16 = 0, ldp = 0;
     uint16_t *h3[3] = {nullptr, nullptr, nullptr}, *w3[3] = {nullptr, nullptr, nullptr};
-    int8_t *pA = nullptr, *pW = nullptr;
+    int8_t *pA = nullptr;
+    float *pW = nullptr;
     double *ring = nullptr, *cfar = nullptr, *wlag = nullptr, *Sn = nullptr;
     FarPlan3 plan3;
     int64_t n_done = 0;
@@ -381,7 +382,7 @@ int fpde_lod3d_create(fpde_ctx *ctx, const fpde_lod3d_desc *desc, const double *
             fail = dev_alloc((void **)&L->h3[q], (size_t)L->rows16 * L->ld16 * 2) ||
                    dev_alloc((void **)&L->w3[q], (size_t)64 * L->ld16 * 2);
         fail = fail || dev_alloc((void **)&L->pA, (size_t)L->rows16 * L->ldp) ||
-               dev_alloc((void **)&L->pW, (size_t)64 * L->ldp) ||
+               dev_alloc((void **)&L->pW, (size_t)64 * L->ldp * sizeof(float)) ||
                dev_alloc((void **)&L->ring, (size_t)64 * pbytes) ||
                dev_alloc((void **)&L->cfar, (size_t)FAR_MAX_SPLITS * 64 * pbytes) ||
                dev_alloc((void **)&L->wlag, LW * sizeof(double)) || dev_alloc((void **)&L->Sn, pbytes);
@@ -460,7 +461,7 @@ int fpde_lod3d_create(fpde_ctx *ctx, const fpde_lod3d_desc *desc, const double *
             cudaMemsetAsync(L->w3[q], 0, (size_t)64 * L->ld16 * 2, st);
         }
         cudaMemsetAsync(L->pA, 0, (size_t)L->rows16 * L->ldp, st);
-        cudaMemsetAsync(L->pW, 0, (size_t)64 * L->ldp, st);
+        cudaMemsetAsync(L->pW, 0, (size_t)64 * L->ldp * sizeof(float), st);
         cudaMemsetAsync(L->ring, 0, (size_t)64 * pbytes, st);
         cudaMemsetAsync(L->cfar, 0, (size_t)FAR_MAX_SPLITS * 64 * pbytes, st);
         cudaMemcpyAsync(L->wlag, wlag.data(), wlag.size() * sizeof(double), cudaMemcpyHostToDevice, st);

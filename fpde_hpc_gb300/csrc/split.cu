@@ -216,7 +216,7 @@ __global__ void __launch_bounds__(128) k_convert3(const double *__restrict__ rin
 // for the k-tile (one weight tile per column of an ensemble; one column for a line or a grid).
 __global__ void __launch_bounds__(64) k_wgen3(const double *__restrict__ wlag_all, int64_t wstride, int n0,
                                               uint16_t *__restrict__ w0, uint16_t *__restrict__ w1,
-                                              uint16_t *__restrict__ w2, int64_t ld, int8_t *__restrict__ pW,
+                                              uint16_t *__restrict__ w2, int64_t ld, float *__restrict__ pW,
                                               int64_t ldp)
 {
     __shared__ double red[2];
@@ -231,7 +231,8 @@ __global__ void __launch_bounds__(64) k_wgen3(const double *__restrict__ wlag_al
     __syncthreads();
     m = fmax(red[0], red[1]);
     const int pe = exp_of_maxbits((unsigned long long)__double_as_longlong(m));
-    if (threadIdx.x == 0) pW[(int64_t)j * ldp + kt] = (int8_t)pe;
+    if (threadIdx.x == 0)                                // the scale 2^pe, exact (pe in [-127, 127])
+        pW[(int64_t)j * ldp + kt] = pe >= -126 ? __int_as_float((pe + 127) << 23) : __int_as_float(0x00400000);
     uint16_t a, b, c;
     digits3(fixed16(v, pe), a, b, c);
     w0[(int64_t)j * ld + t] = a;

@@ -335,7 +335,7 @@ __device__ __forceinline__ float pow2f(int e)
 __global__ void __launch_bounds__(THREADS3, 1)
     k_far_tc3(const __grid_constant__ FarMaps3 maps, double *__restrict__ C, int64_t ldc_split, int64_t ldc_col,
               int64_t rows, int kt_total, int kt_per, int n_split, uint32_t idesc, const int8_t *__restrict__ pA,
-              const int8_t *__restrict__ pW, int64_t ldp, const int *__restrict__ wcol, unsigned *flags)
+              const float *__restrict__ pW, int64_t ldp, const int *__restrict__ wcol, unsigned *flags)
 {
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
@@ -446,7 +446,7 @@ __global__ void __launch_bounds__(THREADS3, 1)
             const int kt0 = ks * kt_per, kt1 = min(kt0 + kt_per, kt_total);
             const int64_t row = (int64_t)mt * BM + q * 32 + lane;
             const int64_t row_c = row < rows ? row : rows - 1;
-            const int8_t *pWc = pW + (wcol ? (int64_t)wcol[mt] * BN * ldp : 0) + (int64_t)c0 * ldp;
+            const float *pWc = pW + (wcol ? (int64_t)wcol[mt] * BN * ldp : 0) + (int64_t)c0 * ldp;
             float hi[EPI_COLS], lo[EPI_COLS];
 #pragma unroll
             for (int j = 0; j < EPI_COLS; ++j) { hi[j] = 0.f; lo[j] = 0.f; }
@@ -467,7 +467,7 @@ __global__ void __launch_bounds__(THREADS3, 1)
                     for (int jj = 0; jj < 16; ++jj) {
                         const int j = 16 * h + jj;
                         // 2^pA * 2^pW: a product of powers of two, exact while it stays normal
-                        const float sc = sa * pow2f((int)__ldg(pWc + (int64_t)j * ldp + kt));
+                        const float sc = sa * __ldg(pWc + (int64_t)j * ldp + kt);
                         float x = v0[jj] * sc;                 // exact (power-of-two scaling)
                         float s = hi[j] + x, bb = s - hi[j];
                         float e = (hi[j] - (s - bb)) + (x - bb);
@@ -586,7 +586,7 @@ int far_plan3_init(FarPlan3 *p, const void *const a[3], int64_t rows, int64_t ld
 }
 
 int far3_launch(cudaStream_t st, const FarPlan3 *p, int k_cols, double *C, int64_t ldc_split, int64_t ldc_col,
-                int splits, const int8_t *pA, const int8_t *pW, int64_t ldp, unsigned *flags, const int *wcol)
+                int splits, const int8_t *pA, const float *pW, int64_t ldp, unsigned *flags, const int *wcol)
 {
     if (k_cols % tc::BK != 0) return set_error(FPDE_ERR_ARG, "far contraction: K must be a multiple of 64");
     if (k_cols == 0) return FPDE_OK;
@@ -674,6 +674,12 @@ extern "C" int fpde_far_contract(fpde_ctx *ctx, const void *a_hi, const void *a_
 }
 
 namespace fpde {
+// Weight-tile exponents -> their scales 2^e (the far kernel takes the scales).
+__global__ void k_exp_to_scale(const int8_t *e, float *s, int64_t n)
+{
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) s[i] = tc::pow2f((int)e[i]);
+}
 // In place: float-pair slots of a far contraction -> FP64 values.
 __global__ void k_ff_to_double(double *C, int64_t n)
 {
@@ -695,13 +701,23 @@ extern "C" int fpde_far_contract3(fpde_ctx *ctx, const void *const a[3], int64_t
     if ((rc = far_plan3_init(&plan, a, rows, lda, w, ldw))) return rc;
     if (splits <= 0) splits = far_splits(k_cols / 64, rows);
     if (splits > FAR_MAX_SPLITS) splits = FAR_MAX_SPLITS;
-    if ((rc = far3_launch(ctx->stream, &plan, k_cols, C, rows * 64, rows, splits, pA, pW, ldp, ctx->d_flags)))
+    float *pWs = nullptr;
+    const int64_t nw = 64 * ldp;
+    if (dev_alloc((void **)&pWs, (size_t)nw * sizeof(float))) return FPDE_ERR_NOMEM;
+    k_exp_to_scale<<<(unsigned)((nw + 255) / 256), 256, 0, ctx->stream>>>(pW, pWs, nw);
+    FPDE_LAUNCHED(1);
+    rc = far3_launch(ctx->stream, &plan, k_cols, C, rows * 64, rows, splits, pA, pWs, ldp, ctx->d_flags);
+    if (rc) {
+        cudaStreamSynchronize(ctx->stream);
+        dev_free(pWs);
         return rc;
+    }
     const int64_t n = (int64_t)splits * 64 * rows;
     if (k_cols > 0) {
         k_ff_to_double<<<(unsigned)((n + 255) / 256), 256, 0, ctx->stream>>>(C, n);
         FPDE_LAUNCHED(1);
     }
     FPDE_CUDA(cudaStreamSynchronize(ctx->stream));
+    dev_free(pWs);
     return ctx_check_flags(ctx, "far contraction (three slices)");
 }

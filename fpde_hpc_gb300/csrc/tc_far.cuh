@@ -23,7 +23,8 @@ int far_launch(cudaStream_t st, const FarPlan *p, int k_cols, double *C, int64_t
 int far_splits(int kt_total, int64_t rows);
 
 // Exact-slice variant: three bf16 slices per operand, per-(row, k-tile) exponents pA
-// ([rows][ldp] int8) and per-(j, k-tile) exponents pW ([64][ldp] int8).
+// ([rows][ldp] int8) and per-(j, k-tile) scales pW = 2^e ([64][ldp] float: the epilogue
+// multiplies by them without rebuilding each power of two).
 struct FarPlan3 {
     alignas(64) unsigned char maps[6 * 128];
     int64_t rows = 0;
@@ -37,7 +38,7 @@ int far_plan3_init(FarPlan3 *p, const void *const a[3], int64_t rows, int64_t ld
 // wcol (device, may be null): per 128-row tile the weight tile (column of an ensemble) it uses,
 // whose 64 rows start at row wcol[tile] * 64 of the W slices and of pW.
 int far3_launch(cudaStream_t st, const FarPlan3 *p, int k_cols, double *C, int64_t ldc_split, int64_t ldc_col,
-                int splits, const int8_t *pA, const int8_t *pW, int64_t ldp, unsigned *flags,
+                int splits, const int8_t *pA, const float *pW, int64_t ldp, unsigned *flags,
                 const int *wcol = nullptr);
 
 // float -> double from the bits (integer instructions only; exact for every float).
