@@ -390,16 +390,16 @@ def _probe(line, u0_dev, steps, every):
 
 
 # DRAM traffic per launch from ncu captures (profiles/), as bytes per unit the launch processes:
-#   k_line_block_spec: per node-step (107.5 MB for 64 steps x 65,537 nodes, 2 far splits)
-#   k_far_tc3        : per node x history step (587.3 MB for 65,664 rows x 1,344 steps)
+#   k_line_block_spec: per node-step (109.5 MB for 64 steps x 65,537 nodes, 2 far splits)
+#   k_far_tc3        : per node x history step (630.4 MB for 65,664 rows x 1,344 steps)
 NCU_TRAFFIC = {
-    "solve_split": ((79.91e6 + 27.61e6) / (64 * 65537), "profiles/k_line_block_spec_N65536_2048steps.md"),
-    "far_tc": ((533.41e6 + 53.86e6) / (65664 * 1344), "profiles/k_far_tc3_N65536_K1344.md"),
+    "solve_split": ((82.01e6 + 27.51e6) / (64 * 65537), "profiles/k_line_block_spec_N65536_2048steps.md"),
+    "far_tc": ((576.33e6 + 54.06e6) / (65664 * 1344), "profiles/k_far_tc3_N65536_K1344.md"),
 }
 # The speculative block solve is bound by neither HBM nor the tensor cores but by GB300's FP64
 # pipe (2 DFMA/clk/SM) and its per-step synchronisation: ncu's sm__pipe_fp64_cycles_active for
 # one launch (same capture as its traffic).
-SOLVE_FP64_PIPE = (0.5196, "profiles/k_line_block_spec_N65536_2048steps.md")
+SOLVE_FP64_PIPE = (0.4844, "profiles/k_line_block_spec_N65536_2048steps.md")
 
 
 def _kernel_entry(t, name, peak, peak_src, scale=1.0):
