@@ -29,6 +29,7 @@
 #include "kernels.cuh"
 #include "scan.cuh"
 #include "tc_far.cuh"
+#include "ff.cuh"
 
 namespace fpde {
 
@@ -110,7 +111,8 @@ __global__ void __launch_bounds__(BT) k_batch_solve(const ColInfo *__restrict__ 
                                                     const double *__restrict__ al, const double *__restrict__ segP,
                                                     const double *__restrict__ segQ, const double *__restrict__ part,
                                                     int KS, int64_t pstride, double *__restrict__ U,
-                                                    double *__restrict__ Y, double *__restrict__ Drow)
+                                                    double *__restrict__ Y, double *__restrict__ Drow,
+                                                    float2 *__restrict__ Drowf)
 {
     __shared__ double wP[BW], wX[BW];
     __shared__ double s_y, s_uN;
@@ -179,11 +181,13 @@ __global__ void __launch_bounds__(BT) k_batch_solve(const ColInfo *__restrict__ 
         const double uo = U[q];
         U[q] = u;
         Drow[q] = u - uo;
+        if (Drowf) Drowf[q] = d2ff(u - uo);            // split path: the float-pair ring row
     }
     if (tid == 0) {
         const double uo = U[o + c.N];
         U[o + c.N] = uN;
         Drow[o + c.N] = uN - uo;
+        if (Drowf) Drowf[o + c.N] = d2ff(uN - uo);
     }
     __syncthreads();                                                // s_item, s_y, s_uN reused
     }
@@ -212,6 +216,7 @@ struct fpde_batch {
     int8_t *pA = nullptr;
     float *pW = nullptr;
     double *ring = nullptr, *cfar = nullptr, *wlag = nullptr, *Sn = nullptr;
+    float2 *ringf = nullptr, *wff = nullptr;  // the ring and every column's lag weights as float pairs
     int *wcol = nullptr;
     FarPlan3 plan3;
     int64_t n_done = 0;
@@ -230,6 +235,7 @@ static int batch_enqueue(fpde_batch *b, cudaStream_t st, int64_t n0, int steps, 
         int KS = 0;
         const double *part = b->part;
         double *Drow;
+        float2 *Drowf = nullptr;                                     // split: the float-pair ring row
         if (!b->split) {
             if (n >= 1) {
                 KS = choose_splits((int)n, b->Ptot);
@@ -261,7 +267,7 @@ static int batch_enqueue(fpde_batch *b, cudaStream_t st, int64_t n0, int steps, 
                 }
             }
             if (n >= 1) {
-                if ((rc = launch_near_history(st, b->ring, b->Ptot, j, b->wlag, b->cfar, splits, 1, b->Sn, b->cta_col,
+                if ((rc = launch_near_history_ff(st, b->ringf, b->Ptot, j, b->wff, b->cfar, splits, 1, b->Sn, b->cta_col,
                                               b->LW)))
                     return rc;
                 ++k;
@@ -269,9 +275,10 @@ static int batch_enqueue(fpde_batch *b, cudaStream_t st, int64_t n0, int steps, 
                 part = b->Sn;
             }
             Drow = b->ring + (int64_t)j * b->Ptot;
+            Drowf = b->ringf + (int64_t)j * b->Ptot;
         }
         k_batch_solve<<<b->solve_grid, BT, 0, st>>>(b->cols, b->order, b->n_cols, b->queue + n, b->A, b->g, b->al,
-                                                    b->segP, b->segQ, part, KS, b->Ptot, b->U, b->Y, Drow);
+                                                    b->segP, b->segQ, part, KS, b->Ptot, b->U, b->Y, Drow, Drowf);
         FPDE_LAUNCHED(1);
         ++k;
     }
@@ -300,6 +307,8 @@ int fpde_batch_destroy(fpde_batch *b)
     }
     dev_free(b->pA);
     dev_free(b->pW);
+    dev_free(b->ringf);
+    dev_free(b->wff);
     dev_free(b->wcol);
     dev_free(b->queue);
     dev_free(b->cols);
@@ -439,6 +448,8 @@ int fpde_batch_create(fpde_ctx *ctx, const fpde_column_desc *cols, int n_cols, i
                dev_alloc((void **)&b->pW, (size_t)wrows * b->ldp * sizeof(float)) || dev_alloc((void **)&b->ring, (size_t)64 * tb) ||
                dev_alloc((void **)&b->cfar, (size_t)FAR_MAX_SPLITS * 64 * tb) ||
                dev_alloc((void **)&b->wlag, hwl.size() * sizeof(double)) || dev_alloc((void **)&b->Sn, tb) ||
+               dev_alloc((void **)&b->ringf, (size_t)64 * tot * sizeof(float2)) ||
+               dev_alloc((void **)&b->wff, hwl.size() * sizeof(float2)) ||
                dev_alloc((void **)&b->wcol, hwcol.size() * sizeof(int));
         if (!fail) {
             const void *a3[3] = {b->h3[0], b->h3[1], b->h3[2]}, *w3[3] = {b->w3[0], b->w3[1], b->w3[2]};
@@ -479,6 +490,13 @@ int fpde_batch_create(fpde_ctx *ctx, const fpde_column_desc *cols, int n_cols, i
         cudaMemsetAsync(b->ring, 0, (size_t)64 * tb, st);
         cudaMemsetAsync(b->cfar, 0, (size_t)FAR_MAX_SPLITS * 64 * tb, st);
         cudaMemcpyAsync(b->wlag, hwl.data(), hwl.size() * sizeof(double), cudaMemcpyHostToDevice, st);
+        std::vector<float2> hwff(hwl.size());            // w = hi + lo, hi the nearest float
+        for (size_t q = 0; q < hwl.size(); ++q) {
+            const float hi = (float)hwl[q];
+            hwff[q] = make_float2(hi, (float)(hwl[q] - (double)hi));
+        }
+        cudaMemcpyAsync(b->wff, hwff.data(), hwff.size() * sizeof(float2), cudaMemcpyHostToDevice, st);
+        cudaMemsetAsync(b->ringf, 0, (size_t)64 * tot * sizeof(float2), st);
         cudaMemcpyAsync(b->wcol, hwcol.data(), hwcol.size() * sizeof(int), cudaMemcpyHostToDevice, st);
     }
     {                                                                  // persistent solve grid

@@ -13,6 +13,7 @@
 
 #include "common.cuh"
 #include "kernels.cuh"
+#include "ff.cuh"
 
 namespace fpde {
 
@@ -178,6 +179,30 @@ int launch_l1_partial(cudaStream_t st, const double *D, int64_t P, int n, const 
     if (n <= 0) return FPDE_OK;
     dim3 grid((unsigned)((P / 2 + 255) / 256), (unsigned)KS);
     k_l1_partial<<<grid, 256, 0, st>>>((const double2 *)D, P / 2, n, wt, (double2 *)part);
+    FPDE_LAUNCHED(1);
+    return FPDE_OK;
+}
+
+// u - last -> D row (FP64 and float pairs); last <- u
+__global__ void k_append_ff(const double *__restrict__ u, double *__restrict__ last, double *__restrict__ row,
+                            float2 *__restrict__ rowf, int64_t nodes, int64_t P)
+{
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P) return;
+    double d = 0.0;
+    if (i < nodes) {
+        const double v = u[i];
+        d = v - last[i];
+        last[i] = v;
+    }
+    row[i] = d;
+    rowf[i] = d2ff(d);
+}
+
+int launch_append_ff(cudaStream_t st, const double *u, double *last, double *row, float2 *rowf, int64_t nodes,
+                     int64_t P)
+{
+    k_append_ff<<<(unsigned)((P + 255) / 256), 256, 0, st>>>(u, last, row, rowf, nodes, P);
     FPDE_LAUNCHED(1);
     return FPDE_OK;
 }

@@ -16,6 +16,9 @@ int launch_l1_partial(cudaStream_t st, const double *D, int64_t P, int n, const 
 int choose_splits(int n, int64_t P);
 // row[i] = u[i] - last[i], last[i] = u[i] for i < nodes; row[i] = 0 up to P.
 int launch_append(cudaStream_t st, const double *u, double *last, double *row, int64_t nodes, int64_t P);
+// The same, also writing the increment row as float pairs (rowf, for the float-float near history).
+int launch_append_ff(cudaStream_t st, const double *u, double *last, double *row, float2 *rowf, int64_t nodes,
+                     int64_t P);
 
 }  // namespace fpde
 
@@ -59,6 +62,12 @@ int launch_block_prep3(cudaStream_t st, const SplitPrep3 &p, int64_t n0);
 //   S[i] = sum_{q<KS} far_q[j][i] + sum_{r<j} wlag[j-r] ring[r][i],
 // ring [64][P] time-major, far partials [KS][64][P] (float pairs when pairs != 0).
 // cta_col (may be null) gives each 512-node group its column's weights at wlag + col * wstride.
+// The same sum in float-float arithmetic on the FP32 pipe (GB300 issues 2 DFMA/clk/SM) from the
+// float-pair copy of the ring (ringf [64][P]) and float-pair lag weights (wff, per column at
+// wff + col * wstride when cta_col is given); one FP64 add per node.
+int launch_near_history_ff(cudaStream_t st, const float2 *ringf, int64_t P, int j, const float2 *wff,
+                           const double *cfar, int KS, int pairs, double *S, const int *cta_col = nullptr,
+                           int64_t wstride = 0);
 int launch_near_history(cudaStream_t st, const double *ring, int64_t P, int j, const double *wlag,
                         const double *cfar, int KS, int pairs, double *S, const int *cta_col = nullptr,
                         int64_t wstride = 0);

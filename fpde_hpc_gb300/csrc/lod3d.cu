@@ -32,6 +32,7 @@
 #include "common.cuh"
 #include "kernels.cuh"
 #include "tc_far.cuh"
+#include "ff.cuh"
 
 namespace fpde {
 
@@ -163,6 +164,57 @@ __global__ void __launch_bounds__(256) k_near_history(const double2 *__restrict_
     S[i] = make_double2(bx + ax, by + ay);
 }
 
+// Two nodes per thread: S = far partials of step j + sum_{r<j} w[j-r] ring[r] in float-float.
+__global__ void __launch_bounds__(256) k_near_history_ff(const float4 *__restrict__ ringf, int64_t P2, int j,
+                                                         const float2 *__restrict__ wff_all,
+                                                         const double2 *__restrict__ cfar, int KS, int pairs,
+                                                         double2 *__restrict__ S, const int *__restrict__ cta_col,
+                                                         int64_t wstride)
+{
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P2) return;
+    const float2 *wff = cta_col ? wff_all + (int64_t)cta_col[blockIdx.x] * wstride : wff_all;
+    float h0 = 0.f, l0 = 0.f, h1 = 0.f, l1 = 0.f;
+    for (int q = 0; q < KS; ++q) {
+        const double2 v = __ldcs(cfar + ((int64_t)q * 64 + j) * P2 + i);
+        const float2 f0 = pairs ? *reinterpret_cast<const float2 *>(&v.x) : d2ff(v.x);
+        const float2 f1 = pairs ? *reinterpret_cast<const float2 *>(&v.y) : d2ff(v.y);
+        ff_add(h0, l0, f0.x, f0.y);
+        ff_add(h1, l1, f1.x, f1.y);
+    }
+    int r = 0;
+    for (; r + 8 <= j; r += 8) {
+        float4 v[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) v[u] = __ldcg(ringf + (int64_t)(r + u) * P2 + i);
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            const float2 w = __ldg(wff + (j - r - u));
+            ff_fma(h0, l0, w, make_float2(v[u].x, v[u].y));
+            ff_fma(h1, l1, w, make_float2(v[u].z, v[u].w));
+        }
+        ff_renorm(h0, l0);
+        ff_renorm(h1, l1);
+    }
+    for (; r < j; ++r) {
+        const float4 v = __ldcg(ringf + (int64_t)r * P2 + i);
+        const float2 w = __ldg(wff + (j - r));
+        ff_fma(h0, l0, w, make_float2(v.x, v.y));
+        ff_fma(h1, l1, w, make_float2(v.z, v.w));
+    }
+    S[i] = make_double2(f2d_bits(h0) + f2d_bits(l0), f2d_bits(h1) + f2d_bits(l1));
+}
+
+int launch_near_history_ff(cudaStream_t st, const float2 *ringf, int64_t P, int j, const float2 *wff,
+                           const double *cfar, int KS, int pairs, double *S, const int *cta_col, int64_t wstride)
+{
+    k_near_history_ff<<<(unsigned)((P / 2 + 255) / 256), 256, 0, st>>>((const float4 *)ringf, P / 2, j, wff,
+                                                                       (const double2 *)cfar, KS, pairs,
+                                                                       (double2 *)S, cta_col, wstride);
+    FPDE_LAUNCHED(1);
+    return FPDE_OK;
+}
+
 int launch_near_history(cudaStream_t st, const double *ring, int64_t P, int j, const double *wlag,
                         const double *cfar, int KS, int pairs, double *S, const int *cta_col, int64_t wstride)
 {
@@ -197,6 +249,7 @@ struct fpde_lod3d {
     int8_t *pA = nullptr;
     float *pW = nullptr;
     double *ring = nullptr, *cfar = nullptr, *wlag = nullptr, *Sn = nullptr;
+    float2 *ringf = nullptr, *wff = nullptr;  // the ring and the lag weights as float pairs
     FarPlan3 plan3;
     int64_t n_done = 0;
     std::map<std::pair<int64_t, int>, cudaGraphExec_t> graphs;
@@ -247,6 +300,7 @@ static int lod_enqueue(fpde_lod3d *L, cudaStream_t st, int64_t n0, int steps, in
     for (int64_t n = n0; n < n0 + steps; ++n) {
         int KS = 0;
         double *Drow;
+        float2 *Drowf = nullptr;                                         // split: the float-pair ring row
         if (!L->split) {
             if (n >= 1) {
                 KS = choose_splits((int)n, L->P);
@@ -275,17 +329,20 @@ static int lod_enqueue(fpde_lod3d *L, cudaStream_t st, int64_t n0, int steps, in
                 }
             }
             if (n >= 1) {
-                if ((rc = launch_near_history(st, L->ring, L->P, j, L->wlag, L->cfar, splits, 1, L->Sn))) return rc;
+                if ((rc = launch_near_history_ff(st, L->ringf, L->P, j, L->wff, L->cfar, splits, 1, L->Sn))) return rc;
                 ++k;
                 KS = 1;
             }
             Drow = L->ring + (int64_t)j * L->P;
+            Drowf = L->ringf + (int64_t)j * L->P;
         }
         for (int pass = 2; pass >= 0; --pass) {                      // K, _M, sN (calc_step order)
             if ((rc = lod_launch_pass(L, st, pass, n, KS))) return rc;
             ++k;
         }
-        if ((rc = launch_append(st, L->U, L->last, Drow, L->G, L->P))) return rc;
+        if ((rc = Drowf ? launch_append_ff(st, L->U, L->last, Drow, Drowf, L->G, L->P)
+                        : launch_append(st, L->U, L->last, Drow, L->G, L->P)))
+            return rc;
         ++k;
     }
     *nk = k;
@@ -304,6 +361,8 @@ int fpde_lod3d_destroy(fpde_lod3d *L)
         cudaStreamSynchronize(L->ctx->stream);
     }
     for (auto &kv : L->graphs) cudaGraphExecDestroy(kv.second);
+    dev_free(L->ringf);
+    dev_free(L->wff);
     for (double *p : {L->U, L->last, L->D, L->part, L->wrev, L->rp, L->bc, L->ring, L->cfar, L->wlag, L->Sn})
         dev_free(p);
     for (int q = 0; q < 3; ++q) {
@@ -385,7 +444,9 @@ int fpde_lod3d_create(fpde_ctx *ctx, const fpde_lod3d_desc *desc, const double *
                dev_alloc((void **)&L->pW, (size_t)64 * L->ldp * sizeof(float)) ||
                dev_alloc((void **)&L->ring, (size_t)64 * pbytes) ||
                dev_alloc((void **)&L->cfar, (size_t)FAR_MAX_SPLITS * 64 * pbytes) ||
-               dev_alloc((void **)&L->wlag, LW * sizeof(double)) || dev_alloc((void **)&L->Sn, pbytes);
+               dev_alloc((void **)&L->wlag, LW * sizeof(double)) || dev_alloc((void **)&L->Sn, pbytes) ||
+               dev_alloc((void **)&L->ringf, (size_t)64 * L->P * sizeof(float2)) ||
+               dev_alloc((void **)&L->wff, LW * sizeof(float2));
         if (!fail) {
             const void *a3[3] = {L->h3[0], L->h3[1], L->h3[2]}, *w3[3] = {L->w3[0], L->w3[1], L->w3[2]};
             int rcp = far_plan3_init(&L->plan3, a3, L->rows16, L->ld16, w3, L->ld16);
@@ -465,6 +526,13 @@ int fpde_lod3d_create(fpde_ctx *ctx, const fpde_lod3d_desc *desc, const double *
         cudaMemsetAsync(L->ring, 0, (size_t)64 * pbytes, st);
         cudaMemsetAsync(L->cfar, 0, (size_t)FAR_MAX_SPLITS * 64 * pbytes, st);
         cudaMemcpyAsync(L->wlag, wlag.data(), wlag.size() * sizeof(double), cudaMemcpyHostToDevice, st);
+        std::vector<float2> wff(wlag.size());          // w = hi + lo, hi the nearest float
+        for (size_t q = 0; q < wlag.size(); ++q) {
+            const float hi = (float)wlag[q];
+            wff[q] = make_float2(hi, (float)(wlag[q] - (double)hi));
+        }
+        cudaMemcpyAsync(L->wff, wff.data(), wff.size() * sizeof(float2), cudaMemcpyHostToDevice, st);
+        cudaMemsetAsync(L->ringf, 0, (size_t)64 * L->P * sizeof(float2), st);
     }
     cudaMemcpyAsync(L->wrev, wrev.data(), wrev.size() * sizeof(double), cudaMemcpyHostToDevice, st);
     if (L->rp) cudaMemcpyAsync(L->rp, d.source, (size_t)L->rp_rows * gbytes, cudaMemcpyHostToDevice, st);
