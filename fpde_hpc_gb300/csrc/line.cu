@@ -654,12 +654,54 @@ __global__ void __launch_bounds__(2 * LTS, 1) k_line_block(LineBlockArgs p)
 
     if (!solver) {
         // ======================================================= history warps
+        // Float-float sums on the FP32 pipe (as in the speculative kernel): every FP64 row the
+        // solver appends is converted once into the float-pair ring and the shared-memory ring
+        // of the block's newest rows; the far partials fold in as float pairs.
         const int ht = tid - LTS;
-        history_sum<SP>(p, ht, a, b, p.j0, p.j0, sS[p.j0 & 1]);           // full history of step j0
+        constexpr int NR = SpecRing<SP>::NR;
+        extern __shared__ float2 spec_rows[];
+        float2 *sR = spec_rows;
+        auto convert_row = [&](int r) {                  // FP64 ring row r -> float pairs
+#pragma unroll
+            for (int q = 0; q < SP; ++q) {
+                const int i = a + ht + LTS * q;
+                if (i < b) p.ringf[(int64_t)r * p.P + i] = d2ff(p.ring[(int64_t)r * p.P + i]);
+            }
+        };
+        if (p.j0 >= 1) convert_row(p.j0 - 1);           // the previous launch's last row
+        const int rlo0 = max(0, p.j0 - NR);
+        for (int r = rlo0; r < p.j0; ++r) {
+#pragma unroll
+            for (int q = 0; q < SP; ++q) {
+                const int i = a + ht + LTS * q;
+                if (i < b) sR[(r % NR) * (LTS * SP) + ht + LTS * q] = p.ringf[(int64_t)r * p.P + i];
+            }
+        }
+        auto history = [&](int j, int rmax, int rlo, double *out) {
+            float h[1][SP], l[1][SP];
+#pragma unroll
+            for (int q = 0; q < SP; ++q) { h[0][q] = 0.f; l[0][q] = 0.f; }
+            far_fold_ff<SP, 1>(p, ht, a, b, j, h, l);
+            rows_split_ff<SP>(p, sR, ht, a, b, j, rmax, rlo, h[0], l[0]);
+            history_store_ff<SP>(ht, a, b, h[0], l[0], out);
+        };
+        history(p.j0, p.j0, rlo0, sS[p.j0 & 1]);                            // full history of step j0
         __syncthreads();                                                    // start
         for (int s = 0; s < p.nsteps; ++s) {
             const int j = p.j0 + s;
-            if (s + 1 < p.nsteps) history_sum<SP>(p, ht, a, b, j + 1, j, sS[(j + 1) & 1]);
+            if (s >= 1) {                                // row j-1 (appended at the end of step s-1)
+                float2 *srow = sR + ((j - 1) % NR) * (LTS * SP);
+#pragma unroll
+                for (int q = 0; q < SP; ++q) {
+                    const int i = a + ht + LTS * q;
+                    if (i < b) {
+                        const float2 f = d2ff(p.ring[(int64_t)(j - 1) * p.P + i]);
+                        p.ringf[(int64_t)(j - 1) * p.P + i] = f;
+                        srow[ht + LTS * q] = f;
+                    }
+                }
+            }
+            if (s + 1 < p.nsteps) history(j + 1, j, max(0, j - NR), sS[(j + 1) & 1]);
             __syncthreads();                                                // end of step s
             if (s_abort) return;
         }
@@ -1476,6 +1518,18 @@ static cudaError_t spec_smem_attrs()
         if (e == cudaSuccess)
             e = cudaFuncSetAttribute(k_line_block_spec<8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      (int)SpecRing<8>::bytes);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(k_line_block<1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)SpecRing<1>::bytes);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(k_line_block<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)SpecRing<2>::bytes);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(k_line_block<4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)SpecRing<4>::bytes);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(k_line_block<8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)SpecRing<8>::bytes);
         return e;
     }();
     return done;
@@ -1484,9 +1538,8 @@ static cudaError_t spec_smem_attrs()
 template <int SP>
 static cudaError_t launch_block_sp(cudaLaunchConfig_t cfg, const LineBlockArgs &a, bool spec)
 {
-    if (!spec) return cudaLaunchKernelEx(&cfg, k_line_block<SP>, a);
-    cfg.dynamicSmemBytes = SpecRing<SP>::bytes;
-    return cudaLaunchKernelEx(&cfg, k_line_block_spec<SP>, a);
+    cfg.dynamicSmemBytes = SpecRing<SP>::bytes;     // both keep the newest rows in shared memory
+    return spec ? cudaLaunchKernelEx(&cfg, k_line_block_spec<SP>, a) : cudaLaunchKernelEx(&cfg, k_line_block<SP>, a);
 }
 
 // Steps j0 .. j0+nsteps-1 of the block starting at nb0 in one persistent launch.
@@ -1736,8 +1789,9 @@ int fpde_line_create(fpde_ctx *ctx, const fpde_line_desc *desc, const double *A,
     int per_sm = 0;
     if (split) {
         int per_sm2 = 0;
-        FPDE_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_line_block<LSEG>, 2 * LTS, 0));
         FPDE_CUDA(spec_smem_attrs());
+        FPDE_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_line_block<LSEG>, 2 * LTS,
+                                                                SpecRing<LSEG>::bytes));
         FPDE_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm2, k_line_block_spec<LSEG>, 2 * LTS,
                                                                 SpecRing<LSEG>::bytes));
         per_sm = std::min(per_sm, per_sm2);
@@ -1898,12 +1952,14 @@ int fpde_line_create(fpde_ctx *ctx, const fpde_line_desc *desc, const double *A,
     L->spec = split && d.theta == 0.0;
     std::vector<double> hRB1, hRB2, hRY1, hRY2;
     std::vector<float2> hwff;
-    if (L->spec) {
-        hwff.resize(LW);                           // w = hi + lo, hi the nearest float
+    if (split) {                                   // w = hi + lo, hi the nearest float
+        hwff.resize(LW);
         for (int64_t j = 0; j < LW; ++j) {
             const float hi = (float)wlag[j];
             hwff[j] = make_float2(hi, (float)(wlag[j] - (double)hi));
         }
+    }
+    if (L->spec) {
         hRB1.assign(N, 0.0); hRB2.assign(N, 0.0); hRY1.assign(N, 0.0); hRY2.assign(N, 0.0);
         const double cE = wlag[1] - L->lam;
         for (int cc = 0; cc < G; ++cc) {
@@ -1999,10 +2055,12 @@ int fpde_line_create(fpde_ctx *ctx, const fpde_line_desc *desc, const double *A,
     }
     if (!fail && d.theta != 0.0)
         fail = dev_alloc((void **)&L->lamv, nb) || dev_alloc((void **)&L->eA, nb) || dev_alloc((void **)&L->eB, nb);
+    if (!fail && split)
+        fail = dev_alloc((void **)&L->ringf, (size_t)BLK * L->P * sizeof(float2)) ||
+               dev_alloc((void **)&L->wff, (size_t)LW * sizeof(float2));
     if (!fail && L->spec)
         fail = dev_alloc((void **)&L->RB1, nb) || dev_alloc((void **)&L->RB2, nb) || dev_alloc((void **)&L->RY1, nb) ||
-               dev_alloc((void **)&L->RY2, nb) || dev_alloc((void **)&L->ringf, (size_t)BLK * L->P * sizeof(float2)) ||
-               dev_alloc((void **)&L->wff, (size_t)LW * sizeof(float2)) || dev_alloc((void **)&L->sga, nb) ||
+               dev_alloc((void **)&L->RY2, nb) || dev_alloc((void **)&L->sga, nb) ||
                dev_alloc((void **)&L->sng, nb) || dev_alloc((void **)&L->sc1, nb) || dev_alloc((void **)&L->sc2, nb) ||
                dev_alloc((void **)&L->sc3, nb) || dev_alloc((void **)&L->sngf, (size_t)N * sizeof(float2));
     if (fail) {
@@ -2025,12 +2083,15 @@ int fpde_line_create(fpde_ctx *ctx, const fpde_line_desc *desc, const double *A,
         cudaMemcpyAsync(L->eA, heA.data(), nb, cudaMemcpyHostToDevice, st);
         cudaMemcpyAsync(L->eB, heB.data(), nb, cudaMemcpyHostToDevice, st);
     }
+    if (split) {
+        cudaMemcpyAsync(L->wff, hwff.data(), (size_t)LW * sizeof(float2), cudaMemcpyHostToDevice, st);
+        cudaMemsetAsync(L->ringf, 0, (size_t)BLK * L->P * sizeof(float2), st);
+    }
     if (L->spec) {
         cudaMemcpyAsync(L->RB1, hRB1.data(), nb, cudaMemcpyHostToDevice, st);
         cudaMemcpyAsync(L->RB2, hRB2.data(), nb, cudaMemcpyHostToDevice, st);
         cudaMemcpyAsync(L->RY1, hRY1.data(), nb, cudaMemcpyHostToDevice, st);
         cudaMemcpyAsync(L->RY2, hRY2.data(), nb, cudaMemcpyHostToDevice, st);
-        cudaMemcpyAsync(L->wff, hwff.data(), (size_t)LW * sizeof(float2), cudaMemcpyHostToDevice, st);
         std::vector<double> h1(N), h2(N), h3(N), h4(N), h5(N);
         std::vector<float2> hngf(N);
         const double w1 = wlag[1], w2 = wlag[2], cE = w1 - L->lam;
@@ -2049,7 +2110,6 @@ int fpde_line_create(fpde_ctx *ctx, const fpde_line_desc *desc, const double *A,
         cudaMemcpyAsync(L->sc2, h4.data(), nb, cudaMemcpyHostToDevice, st);
         cudaMemcpyAsync(L->sc3, h5.data(), nb, cudaMemcpyHostToDevice, st);
         cudaMemcpyAsync(L->sngf, hngf.data(), (size_t)N * sizeof(float2), cudaMemcpyHostToDevice, st);
-        cudaMemsetAsync(L->ringf, 0, (size_t)BLK * L->P * sizeof(float2), st);
     }
     if (L->srcd)
         cudaMemcpyAsync(L->srcd, d.source, (size_t)L->src_rows * (N + 1) * sizeof(double), cudaMemcpyHostToDevice, st);
