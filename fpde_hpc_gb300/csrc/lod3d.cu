@@ -127,6 +127,138 @@ __global__ void __launch_bounds__(128) k_lod_pass(LodPassArgs p)
     p.U[base] = fma(__ldg(p.al + line), u, g0);                   // Al[1] U[1] + Bt[1]
 }
 
+// Segmented pass: LSEGS threads (adjacent lanes) per line, each sweeping one segment of up to
+// LSEGLEN nodes from zero carries, the segments joined by affine scans over the group's lanes.
+// One thread per line left only ~3 warps per SM for a chain of dependent FP64 operations; four
+// per line give the FP64 pipe four times the independent work. With the segment's prefix
+// product of a = g A (its end value PF), the backward sweep's responses KF (to that prefix
+// product) and CB (suffix product of al) precomputed per node on the host:
+//   y = y0 + c_in CF,  u = ub0 + c_in KF + c_out CB,
+// where y0, ub0 are the zero-carry sweeps, c_in the true y before the segment and c_out the
+// true u after it.
+constexpr int LSEGS = 4, LSEGLEN = 32;
+constexpr int LSB = 4;                    // nodes of loads issued together (register budget: one wave)
+struct LodSegArgs {
+    const double *KF, *CB;           // (Nl+1) x lines, pass-line-major
+    const double *PF;                // [lines][LSEGS]: product of a = g A over each segment
+    int seglen;                      // nodes per segment (<= LSEGLEN)
+};
+
+__global__ void __launch_bounds__(128, 4) k_lod_pass_seg(LodPassArgs p, LodSegArgs sg)
+{
+    const int gt = blockIdx.x * blockDim.x + threadIdx.x;
+    const int line = gt / LSEGS, sgi = gt % LSEGS;
+    const bool live = line < p.lines;
+    const int ln = live ? line : 0;
+    const int a = ln % p.n1, b = ln / p.n1;
+    const int64_t base = (int64_t)(1 + a) * p.s1 + (int64_t)(1 + b) * p.s2;
+    const int Nl = p.Nl, L = p.lines;
+    const int q0 = 1 + sgi * sg.seglen, q1 = min(q0 + sg.seglen, Nl);   // nodes [q0, q1)
+    const double g0 = p.bc ? p.bc[base] : 0.0;
+    const double uold_last = p.U[base + (int64_t)(Nl - 1) * p.st];       // read before any write
+    // forward from a zero carry: y0_q = g_q (A_q y0_{q-1} - Om_q)
+    double yv[LSEGLEN];
+    double y = 0.0;
+#pragma unroll
+    for (int t0 = 0; t0 < LSEGLEN; t0 += LSB) {
+        double uu[LSB], aa[LSB], gg[LSB], rr[LSB], ss[LSB];
+#pragma unroll
+        for (int t = 0; t < LSB; ++t) {
+            const int q = q0 + t0 + t;
+            const bool in = live && q < q1;
+            const int64_t id = base + (int64_t)(in ? q : 1) * p.st;
+            uu[t] = in ? p.U[id] : 0.0;
+            aa[t] = in ? __ldg(p.A + (int64_t)q * L + line) : 0.0;
+            gg[t] = in ? __ldg(p.g + (int64_t)q * L + line) : 0.0;
+            rr[t] = (in && p.rp) ? __ldg(p.rp + id) : 0.0;
+            double sv = 0.0;
+            for (int k = 0; k < p.KS; ++k)
+                if (in) sv += __ldcg(p.part + (int64_t)k * p.pstride + id);
+            ss[t] = sv;
+        }
+#pragma unroll
+        for (int t = 0; t < LSB; ++t) {
+            if (q0 + t0 + t < q1) {
+                const double om = (-(p.lam * uu[t]) + rr[t]) + ss[t];    // Om1 :4191, :4267
+                y = gg[t] * (aa[t] * y - om);
+            }
+            yv[t0 + t] = y;
+        }
+    }
+    // forward carries: compose (PF, y0_end) over segments 0..sgi; c_in of this segment
+    double Pc = (live && q1 > q0) ? __ldg(sg.PF + (int64_t)line * LSEGS + sgi) : 1.0;
+    double Yc = (q1 > q0) ? y : 0.0;
+#pragma unroll
+    for (int d = 1; d < LSEGS; d <<= 1) {
+        const double Pp = __shfl_up_sync(0xffffffffu, Pc, d, LSEGS), Yp = __shfl_up_sync(0xffffffffu, Yc, d, LSEGS);
+        if (sgi >= d) { Yc = fma(Pc, Yp, Yc); Pc *= Pp; }
+    }
+    const double yend = fma(Pc, g0, Yc);                 // true y at this segment's end
+    double cin = __shfl_up_sync(0xffffffffu, yend, 1, LSEGS);
+    if (sgi == 0) cin = g0;
+    const double ylast = __shfl_sync(0xffffffffu, yend, LSEGS - 1, LSEGS);   // y_{Nl-1}
+    // right end: Dirichlet value or the flux closure of U1 (:4687-4719) with the old U[Nl-1]
+    const double gN = p.bc ? p.bc[base + (int64_t)Nl * p.st] : 0.0;
+    double uN;
+    if (p.rkind == FPDE_BC_DIRICHLET) {
+        uN = gN;
+    } else {
+        const double AlN = __ldg(p.al + (int64_t)(Nl - 1) * L + ln);
+        if (fabs(ylast) > 1e-15) uN = (fabs(1.0 - AlN) > 1e-15) ? (ylast + gN * p.dLN) / (1.0 - AlN) : uold_last;
+        else uN = (fabs(1.0 - AlN) > 1e-15) ? 0.0 : uold_last;
+    }
+    // backward from a zero carry over y0: ub0_q = al_q ub0_{q+1} + y0_q
+    double u = 0.0;
+#pragma unroll
+    for (int t0 = LSEGLEN - LSB; t0 >= 0; t0 -= LSB) {
+        double al[LSB];
+#pragma unroll
+        for (int t = LSB - 1; t >= 0; --t) {
+            const int q = q0 + t0 + t;
+            al[t] = (live && q < q1) ? __ldg(p.al + (int64_t)q * L + line) : 0.0;
+        }
+#pragma unroll
+        for (int t = LSB - 1; t >= 0; --t) {
+            if (q0 + t0 + t < q1) u = fma(al[t], u, yv[t0 + t]);
+            yv[t0 + t] = u;
+        }
+    }
+    // backward carries: u at this segment's start = ub0_start + c_in KF_start + c_out CB_start
+    const double kf0 = (live && q1 > q0) ? __ldg(sg.KF + (int64_t)q0 * L + line) : 0.0;
+    double Qc = (live && q1 > q0) ? __ldg(sg.CB + (int64_t)q0 * L + line) : 1.0;
+    double Uc = (q1 > q0) ? fma(cin, kf0, u) : 0.0;
+#pragma unroll
+    for (int d = 1; d < LSEGS; d <<= 1) {
+        const double Qn = __shfl_down_sync(0xffffffffu, Qc, d, LSEGS), Un = __shfl_down_sync(0xffffffffu, Uc, d, LSEGS);
+        if (sgi + d < LSEGS) { Uc = fma(Qc, Un, Uc); Qc *= Qn; }
+    }
+    const double ustart = fma(Qc, uN, Uc);               // true u at this segment's start
+    double cout = __shfl_down_sync(0xffffffffu, ustart, 1, LSEGS);
+    if (sgi == LSEGS - 1) cout = uN;
+    const double u1 = __shfl_sync(0xffffffffu, ustart, 0, LSEGS);        // U[1]
+    if (!live) return;
+#pragma unroll
+    for (int t0 = 0; t0 < LSEGLEN; t0 += LSB) {
+        double kf[LSB], cb[LSB];
+#pragma unroll
+        for (int t = 0; t < LSB; ++t) {
+            const int q = q0 + t0 + t;
+            kf[t] = q < q1 ? __ldg(sg.KF + (int64_t)q * L + line) : 0.0;
+            cb[t] = q < q1 ? __ldg(sg.CB + (int64_t)q * L + line) : 0.0;
+        }
+#pragma unroll
+        for (int t = 0; t < LSB; ++t) {
+            const int q = q0 + t0 + t;
+            if (q < q1) p.U[base + (int64_t)q * p.st] = fma(cout, cb[t], fma(cin, kf[t], yv[t0 + t]));
+        }
+    }
+    if (sgi == LSEGS - 1) {
+        p.U[base + (int64_t)Nl * p.st] = uN;
+        p.U[base + (int64_t)(Nl + 1) * p.st] = uN;                  // ghost copy (U1 :4792)
+    }
+    if (sgi == 0) p.U[base] = fma(__ldg(p.al + line), u1, g0);    // Al[1] U[1] + Bt[1]
+}
+
 // Near history (split path): two nodes per thread, eight ring rows of loads in flight.
 __global__ void __launch_bounds__(256) k_near_history(const double2 *__restrict__ ring, int64_t P2, int j,
                                                       const double *__restrict__ wlag_all,
@@ -241,6 +373,11 @@ struct fpde_lod3d {
     int rp_rows = 0, bc_rows = 0;
     double *cA[3] = {nullptr, nullptr, nullptr}, *cg[3] = {nullptr, nullptr, nullptr},
            *cal[3] = {nullptr, nullptr, nullptr};
+    // segmented passes (lines of up to LSEGS x LSEGLEN interior nodes): per-node responses KF, CB
+    // and per-segment products PF; seglen 0 runs the one-thread-per-line kernel
+    double *cKF[3] = {nullptr, nullptr, nullptr}, *cCB[3] = {nullptr, nullptr, nullptr},
+           *cPF[3] = {nullptr, nullptr, nullptr};
+    int seglen[3] = {0, 0, 0};
     int lines[3] = {0, 0, 0};
     // split path (exact three-slice far history on the tensor cores, FP64 near history)
     bool split = false;
@@ -288,7 +425,14 @@ static int lod_launch_pass(fpde_lod3d *L, cudaStream_t st, int pass, int64_t n, 
     a.rkind = L->d.right_kind[pass];
     a.dLN = L->d.dLN[pass];
     if (a.lines <= 0) return FPDE_OK;
-    k_lod_pass<<<(unsigned)((a.lines + 127) / 128), 128, 0, st>>>(a);
+    if (L->seglen[pass] > 0) {
+        LodSegArgs sg;
+        sg.KF = L->cKF[pass]; sg.CB = L->cCB[pass]; sg.PF = L->cPF[pass]; sg.seglen = L->seglen[pass];
+        const int64_t threads = (int64_t)a.lines * LSEGS;
+        k_lod_pass_seg<<<(unsigned)((threads + 127) / 128), 128, 0, st>>>(a, sg);
+    } else {
+        k_lod_pass<<<(unsigned)((a.lines + 127) / 128), 128, 0, st>>>(a);
+    }
     FPDE_LAUNCHED(1);
     return FPDE_OK;
 }
@@ -375,6 +519,9 @@ int fpde_lod3d_destroy(fpde_lod3d *L)
         dev_free(L->cA[q]);
         dev_free(L->cg[q]);
         dev_free(L->cal[q]);
+        dev_free(L->cKF[q]);
+        dev_free(L->cCB[q]);
+        dev_free(L->cPF[q]);
     }
     delete L;
     return FPDE_OK;
@@ -503,6 +650,41 @@ int fpde_lod3d_create(fpde_ctx *ctx, const fpde_lod3d_desc *desc, const double *
                    cudaMemcpy(L->cg[pass], hg.data(), cnt * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess ||
                    cudaMemcpy(L->cal[pass], hal.data(), cnt * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess;
             if (fail) set_error(FPDE_ERR_CUDA, "lod3d: coefficient upload failed");
+        }
+        // segmented pass data: segment s holds nodes [1 + s seglen, 1 + (s+1) seglen) of 1..Nl-1
+        const int sl = (Nl - 1 + LSEGS - 1) / LSEGS;
+        if (!fail && Nl >= 2 && sl <= LSEGLEN) {
+            std::vector<double> hKF(cnt, 0.0), hCB(cnt, 0.0), hPF((size_t)lines * LSEGS, 1.0), cf(LSEGLEN);
+            for (int line = 0; line < lines; ++line) {
+                for (int sgi = 0; sgi < LSEGS; ++sgi) {
+                    const int q0 = 1 + sgi * sl, q1 = std::min(q0 + sl, Nl);
+                    double pr = 1.0;
+                    for (int q = q0; q < q1; ++q) {
+                        const size_t o = (size_t)q * lines + line;
+                        pr *= hg[o] * hA[o];                               // prefix product of a = g A
+                        cf[q - q0] = pr;
+                    }
+                    hPF[(size_t)line * LSEGS + sgi] = pr;
+                    double kf = 0.0, cb = 1.0;
+                    for (int q = q1 - 1; q >= q0; --q) {
+                        const size_t o = (size_t)q * lines + line;
+                        kf = hal[o] * kf + cf[q - q0];                      // backward sweep of CF
+                        cb = hal[o] * cb;                                  // suffix product of al
+                        hKF[o] = kf;
+                        hCB[o] = cb;
+                    }
+                }
+            }
+            fail = dev_alloc((void **)&L->cKF[pass], cnt * sizeof(double)) ||
+                   dev_alloc((void **)&L->cCB[pass], cnt * sizeof(double)) ||
+                   dev_alloc((void **)&L->cPF[pass], hPF.size() * sizeof(double));
+            if (!fail) {
+                fail = cudaMemcpy(L->cKF[pass], hKF.data(), cnt * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess ||
+                       cudaMemcpy(L->cCB[pass], hCB.data(), cnt * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess ||
+                       cudaMemcpy(L->cPF[pass], hPF.data(), hPF.size() * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess;
+                if (fail) set_error(FPDE_ERR_CUDA, "lod3d: coefficient upload failed");
+            }
+            if (!fail) L->seglen[pass] = sl;
         }
     }
     if (fail) {
