@@ -109,7 +109,8 @@ __global__ void __launch_bounds__(BT) k_batch_solve(const ColInfo *__restrict__ 
                                                     int n_cols, unsigned *__restrict__ queue,
                                                     const double *__restrict__ A, const double *__restrict__ g,
                                                     const double *__restrict__ al, const double *__restrict__ segP,
-                                                    const double *__restrict__ segQ, const double *__restrict__ part,
+                                                    const double *__restrict__ segQ, const double *__restrict__ KF,
+                                                    const double *__restrict__ CB, const double *__restrict__ part,
                                                     int KS, int64_t pstride, double *__restrict__ U,
                                                     double *__restrict__ Y, double *__restrict__ Drow,
                                                     float2 *__restrict__ Drowf)
@@ -127,32 +128,47 @@ __global__ void __launch_bounds__(BT) k_batch_solve(const ColInfo *__restrict__ 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int64_t o = c.off;
     const int i0 = min(tid * c.seg, c.N), i1 = min(i0 + c.seg, c.N);
-    // forward, pass 1: Om into Y and the segment's sweep from a zero carry
+    // Segment sweeps from zero carries joined by CTA scans; the carries are applied in one
+    // independent pass, u = ub0 + c_in KF + c_out CB (KF: the segment's backward response to its
+    // forward prefix products, CB: suffix products of al; time-invariant, from the host), so two
+    // dependent FP64 chains per step instead of four. Loads are issued eight nodes at a time.
+    // forward: y0 from a zero carry (y_0 = g0 at the column's first node) into Y
     double yl = 0.0;
-    for (int i = i0; i < i1; ++i) {
-        const int64_t q = o + i;
-        double om = 0.0;
-        if (i == 0) {
-            yl = c.g0;                                                  // Bt[1]
-        } else {
-            double s = 0.0;
-            for (int k = 0; k < KS; ++k) s += __ldcg(part + (int64_t)k * pstride + q);
-            om = -(c.lam * U[q]) + s;
-            yl = __ldg(g + q) * (__ldg(A + q) * yl - om);
+    for (int ib = i0; ib < i1; ib += 8) {
+        double uu[8], gg[8], aa[8], ss[8];
+#pragma unroll
+        for (int t = 0; t < 8; ++t) {
+            const int i = ib + t;
+            const bool in = i < i1 && i > 0;
+            const int64_t q = o + (in ? i : 0);
+            uu[t] = in ? U[q] : 0.0;
+            gg[t] = in ? __ldg(g + q) : 0.0;
+            aa[t] = in ? __ldg(A + q) : 0.0;
+            double sv = 0.0;
+            for (int k = 0; k < KS; ++k)
+                if (in) sv += __ldcg(part + (int64_t)k * pstride + q);
+            ss[t] = sv;
         }
-        Y[q] = om;
+#pragma unroll
+        for (int t = 0; t < 8; ++t) {
+            const int i = ib + t;
+            if (i < i1) {
+                if (i == 0) {
+                    yl = c.g0;                                          // Bt[1]
+                } else {
+                    const double om = -(c.lam * uu[t]) + ss[t];
+                    yl = gg[t] * (aa[t] * yl - om);
+                }
+                Y[o + i] = yl;
+            }
+        }
     }
-    double P = i1 > i0 ? __ldg(segP + (int64_t)col * BT + tid) : 1.0;
+    const double pf = i1 > i0 ? __ldg(segP + (int64_t)col * BT + tid) : 1.0;
+    double P = pf;
     double X = i1 > i0 ? yl : 0.0;
     cta_scan_excl<true>(P, X, wP, wX, lane, warp);
-    // forward, pass 2: the exact sweep from the true carry y_{i0-1} = X
-    double y = X;
-    for (int i = i0; i < i1; ++i) {
-        const int64_t q = o + i;
-        y = (i == 0) ? c.g0 : __ldg(g + q) * (__ldg(A + q) * y - Y[q]);
-        Y[q] = y;
-    }
-    if (i1 == c.N && i1 > i0) s_y = y;                                  // Bt[N]
+    const double cin = X;                                               // true y before the segment
+    if (i1 == c.N && i1 > i0) s_y = fma(pf, cin, yl);                   // Bt[N]
     __syncthreads();
     if (tid == 0) {
         double uN;
@@ -164,24 +180,55 @@ __global__ void __launch_bounds__(BT) k_batch_solve(const ColInfo *__restrict__ 
     }
     __syncthreads();
     const double uN = s_uN;
-    // backward, pass 1: the segment's sweep from a zero carry
+    // backward: ub0 from a zero carry over y0, into Y
     double ul = 0.0;
-    for (int i = i1 - 1; i >= i0; --i) {
-        const int64_t q = o + i;
-        ul = fma(__ldg(al + q), ul, Y[q]);
+    for (int ie = i1 - 1; ie >= i0; ie -= 8) {
+        double yy[8], la[8];
+#pragma unroll
+        for (int t = 0; t < 8; ++t) {
+            const int i = ie - t;
+            const bool in = i >= i0;
+            const int64_t q = o + (in ? i : i0);
+            yy[t] = in ? Y[q] : 0.0;
+            la[t] = in ? __ldg(al + q) : 0.0;
+        }
+#pragma unroll
+        for (int t = 0; t < 8; ++t) {
+            const int i = ie - t;
+            if (i >= i0) {
+                ul = fma(la[t], ul, yy[t]);
+                Y[o + i] = ul;
+            }
+        }
     }
     P = i1 > i0 ? __ldg(segQ + (int64_t)col * BT + tid) : 1.0;
-    X = i1 > i0 ? ul : 0.0;
+    X = i1 > i0 ? fma(cin, __ldg(KF + o + i0), ul) : 0.0;              // u at the segment start, c_out = 0
     cta_scan_excl<false>(P, X, wP, wX, lane, warp);
-    // backward, pass 2: U_{i1} = P uN + X, exact sweep, write U and the increment
-    double u = fma(P, uN, X);
-    for (int i = i1 - 1; i >= i0; --i) {
-        const int64_t q = o + i;
-        u = fma(__ldg(al + q), u, Y[q]);
-        const double uo = U[q];
-        U[q] = u;
-        Drow[q] = u - uo;
-        if (Drowf) Drowf[q] = d2ff(u - uo);            // split path: the float-pair ring row
+    const double cout = fma(P, uN, X);                                  // true u after the segment
+    // carries applied; U and the increment written
+    for (int ib = i0; ib < i1; ib += 8) {
+        double ub[8], kf[8], cb[8], uo[8];
+#pragma unroll
+        for (int t = 0; t < 8; ++t) {
+            const int i = ib + t;
+            const bool in = i < i1;
+            const int64_t q = o + (in ? i : i0);
+            ub[t] = in ? Y[q] : 0.0;
+            kf[t] = in ? __ldg(KF + q) : 0.0;
+            cb[t] = in ? __ldg(CB + q) : 0.0;
+            uo[t] = in ? U[q] : 0.0;
+        }
+#pragma unroll
+        for (int t = 0; t < 8; ++t) {
+            const int i = ib + t;
+            if (i < i1) {
+                const int64_t q = o + i;
+                const double u = fma(cout, cb[t], fma(cin, kf[t], ub[t]));
+                U[q] = u;
+                Drow[q] = u - uo[t];
+                if (Drowf) Drowf[q] = d2ff(u - uo[t]);          // split path: the float-pair ring row
+            }
+        }
     }
     if (tid == 0) {
         const double uo = U[o + c.N];
@@ -204,6 +251,7 @@ struct fpde_batch {
     std::vector<int64_t> off;
     std::vector<int> N;
     double *A = nullptr, *g = nullptr, *al = nullptr, *segP = nullptr, *segQ = nullptr;
+    double *KF = nullptr, *CB = nullptr;      // per node: segment responses KF and suffix products CB
     double *U = nullptr, *U0 = nullptr, *Y = nullptr, *D = nullptr, *part = nullptr, *wall = nullptr;
     ColInfo *cols = nullptr;
     int *order = nullptr, *cta_col = nullptr;
@@ -278,7 +326,8 @@ static int batch_enqueue(fpde_batch *b, cudaStream_t st, int64_t n0, int steps, 
             Drowf = b->ringf + (int64_t)j * b->Ptot;
         }
         k_batch_solve<<<b->solve_grid, BT, 0, st>>>(b->cols, b->order, b->n_cols, b->queue + n, b->A, b->g, b->al,
-                                                    b->segP, b->segQ, part, KS, b->Ptot, b->U, b->Y, Drow, Drowf);
+                                                    b->segP, b->segQ, b->KF, b->CB, part, KS, b->Ptot, b->U, b->Y, Drow,
+                                                    Drowf);
         FPDE_LAUNCHED(1);
         ++k;
     }
@@ -298,7 +347,7 @@ int fpde_batch_destroy(fpde_batch *b)
         cudaStreamSynchronize(b->ctx->stream);
     }
     for (auto &kv : b->graphs) cudaGraphExecDestroy(kv.second);
-    for (double *p : {b->A, b->g, b->al, b->segP, b->segQ, b->U, b->U0, b->Y, b->D, b->part, b->wall, b->ring,
+    for (double *p : {b->A, b->g, b->al, b->segP, b->segQ, b->KF, b->CB, b->U, b->U0, b->Y, b->D, b->part, b->wall, b->ring,
                       b->cfar, b->wlag, b->Sn})
         dev_free(p);
     for (int q = 0; q < 3; ++q) {
@@ -353,6 +402,7 @@ int fpde_batch_create(fpde_ctx *ctx, const fpde_column_desc *cols, int n_cols, i
     b->Ptot = tot;
     std::vector<double> hA(tot, 0.0), hg(tot, 0.0), hal(tot, 0.0), hU(tot, 0.0);
     std::vector<double> hP((size_t)n_cols * BT, 1.0), hQ((size_t)n_cols * BT, 1.0);
+    std::vector<double> hKF(tot, 0.0), hCB(tot, 0.0);
     std::vector<double> hw((size_t)n_cols * (max_steps + 1), 0.0);
     std::vector<ColInfo> hc(n_cols);
     std::vector<int> cta_col(tot / 512);
@@ -392,10 +442,18 @@ int fpde_batch_create(fpde_ctx *ctx, const fpde_column_desc *cols, int n_cols, i
             double pf = 1.0, pb = 1.0;
             for (int64_t i = i0; i < i1; ++i) {
                 pf *= hg[o + i] * hA[o + i];
+                hKF[o + i] = pf;                                       // forward prefix product (CF)
                 pb *= hal[o + i];
             }
             hP[(size_t)c * BT + t] = pf;
             hQ[(size_t)c * BT + t] = pb;
+            double kf = 0.0, cb = 1.0;                                  // backward sweep of CF, suffix of al
+            for (int64_t i = i1 - 1; i >= i0; --i) {
+                kf = hal[o + i] * kf + hKF[o + i];
+                cb = hal[o + i] * cb;
+                hKF[o + i] = kf;
+                hCB[o + i] = cb;
+            }
         }
         double *w = hw.data() + (size_t)c * (max_steps + 1);          // w[m] = w_c[max_steps - m]
         for (int64_t m = 0; m < max_steps; ++m) {
@@ -429,6 +487,7 @@ int fpde_batch_create(fpde_ctx *ctx, const fpde_column_desc *cols, int n_cols, i
     bool fail = dev_alloc((void **)&b->A, tb) || dev_alloc((void **)&b->g, tb) || dev_alloc((void **)&b->al, tb) ||
                 dev_alloc((void **)&b->segP, hP.size() * sizeof(double)) ||
                 dev_alloc((void **)&b->segQ, hQ.size() * sizeof(double)) || dev_alloc((void **)&b->U, tb) ||
+                dev_alloc((void **)&b->KF, tb) || dev_alloc((void **)&b->CB, tb) ||
                 dev_alloc((void **)&b->U0, tb) || dev_alloc((void **)&b->Y, tb) ||
                 dev_alloc((void **)&b->cols, hc.size() * sizeof(ColInfo)) ||
                 dev_alloc((void **)&b->order, order.size() * sizeof(int)) ||
@@ -472,6 +531,8 @@ int fpde_batch_create(fpde_ctx *ctx, const fpde_column_desc *cols, int n_cols, i
     cudaMemcpyAsync(b->al, hal.data(), tb, cudaMemcpyHostToDevice, st);
     cudaMemcpyAsync(b->segP, hP.data(), hP.size() * sizeof(double), cudaMemcpyHostToDevice, st);
     cudaMemcpyAsync(b->segQ, hQ.data(), hQ.size() * sizeof(double), cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(b->KF, hKF.data(), tb, cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(b->CB, hCB.data(), tb, cudaMemcpyHostToDevice, st);
     cudaMemcpyAsync(b->U, hU.data(), tb, cudaMemcpyHostToDevice, st);
     cudaMemcpyAsync(b->U0, hU.data(), tb, cudaMemcpyHostToDevice, st);
     cudaMemsetAsync(b->Y, 0, tb, st);
