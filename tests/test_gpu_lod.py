@@ -115,3 +115,27 @@ def test_lod_split_history_vs_fp64(ctx, steps, tol):
     err = relmax(out[1], out[0])
     print(f"LOD 20^3 {steps} steps, split x3 vs FP64: max rel {err:.2e}")
     assert err <= tol
+
+
+@pytest.mark.parametrize("dims,steps", [((129, 6, 5), 12), ((141, 5, 7), 10)])
+def test_lod_long_lines_vs_oracle(ctx, dims, steps):
+    """Lines of exactly 4 x 32 interior nodes (the segmented pass at its limit) and longer lines
+    (the one-thread-per-line pass) in the same grid as short ones: every pass against the
+    oracle's LOD restatement, 1e-12 or 4x its one-ulp rounding envelope."""
+    import fpde_hpc_gb300 as fp
+    from fpde_hpc_gb300 import problems
+    base = problems.config4(n=max(dims), steps=steps)
+    sN, M, K = dims
+    p = problems.LodProblem("lod", dims, base.alpha, base.tau, steps, base.k[:K + 2, :M + 2, :sN + 2].copy(),
+                            base.u0[:K + 2, :M + 2, :sN + 2].copy(), base.left_kind, base.right_kind)
+    p.u0[K:] = 0.0
+    cA, cB, cR = p.coefs()
+    lod = fp.Lod3D(ctx, dims, p.alpha, p.tau, p.Da, cA, cB, cR, p.u0, steps, left_kind=p.left_kind,
+                   right_kind=p.right_kind, dLN=p.dLN)
+    lod.run(steps)
+    u = lod.state()
+    lod.close()
+    uref, env = _envelope(p, cA, cB, cR)
+    err = relmax(u, uref)
+    print(f"LOD {dims} {steps} steps vs oracle: {err:.2e} (one-ulp envelope {env:.2e})")
+    assert err <= max(1e-12, 4 * env)
