@@ -15,8 +15,9 @@
 //                        :4683-4724) as segment sweeps joined by a CTA scan, then writes U and D_n.
 // Split path (FPDE_PREC_SPLIT_BF16X3): step 1 becomes, per 64-step block, the exact
 // three-slice tensor-core contraction of all history before the block with one weight tile
-// per column (tc_far.cu; each 128-row tile picks its column's tile), and per step the FP64
-// near history from a 64-row ring (k_near_history); the increments go to that ring.
+// per column (tc_far.cu; each 128-row tile picks its column's tile), and per step the near
+// history in float-float from a 64-row float-pair ring (k_near_history_ff); the solve writes
+// each increment to that ring and to the FP64 one the conversion reads.
 // The alpha recurrence is time-invariant and precomputed on the host per column.
 #include <algorithm>
 #include <cmath>

@@ -58,18 +58,14 @@ struct SplitPrep3 {
 };
 int launch_block_prep3(cudaStream_t st, const SplitPrep3 &p, int64_t n0);
 
-// Near history of step j of a block for every node (FP64):
-//   S[i] = sum_{q<KS} far_q[j][i] + sum_{r<j} wlag[j-r] ring[r][i],
-// ring [64][P] time-major, far partials [KS][64][P] (float pairs when pairs != 0).
-// cta_col (may be null) gives each 512-node group its column's weights at wlag + col * wstride.
-// The same sum in float-float arithmetic on the FP32 pipe (GB300 issues 2 DFMA/clk/SM) from the
-// float-pair copy of the ring (ringf [64][P]) and float-pair lag weights (wff, per column at
-// wff + col * wstride when cta_col is given); one FP64 add per node.
+// Near history of step j of a block for every node:
+//   S[i] = sum_{q<KS} far_q[j][i] + sum_{r<j} w[j-r] D_r[i],
+// far partials [KS][64][P] (float pairs when pairs != 0), in float-float arithmetic on the FP32
+// pipe (GB300 issues 2 DFMA/clk/SM) from the float-pair ring (ringf [64][P]) and float-pair lag
+// weights (wff, per column at wff + col * wstride when cta_col is given: each 512-node group's
+// column); one FP64 add per node.
 int launch_near_history_ff(cudaStream_t st, const float2 *ringf, int64_t P, int j, const float2 *wff,
                            const double *cfar, int KS, int pairs, double *S, const int *cta_col = nullptr,
                            int64_t wstride = 0);
-int launch_near_history(cudaStream_t st, const double *ring, int64_t P, int j, const double *wlag,
-                        const double *cfar, int KS, int pairs, double *S, const int *cta_col = nullptr,
-                        int64_t wstride = 0);
 
 }  // namespace fpde

@@ -405,58 +405,9 @@ __device__ __forceinline__ bool wait_flag(const unsigned long long *f, unsigned 
 
 __device__ __forceinline__ void solver_sync() { asm volatile("bar.sync 1, %0;" ::"n"(LTS) : "memory"); }
 
-// history warps: S[node] = far partials of step j + sum_{r < rmax} w[j - r] ring[r][node]
-template <int SP>
-__device__ __forceinline__ void history_sum(const LineBlockArgs &p, int ht, int a, int b, int j, int rmax,
-                                            double *out)
-{
-    double acc[SP], far[SP];
-    int64_t node[SP];
-#pragma unroll
-    for (int q = 0; q < SP; ++q) {
-        node[q] = a + ht + LTS * q;
-        acc[q] = 0.0;
-        far[q] = 0.0;
-    }
-    for (int k = 0; k < p.KS; ++k) {                     // far partials: float pairs, exact in FP64
-#pragma unroll
-        for (int q = 0; q < SP; ++q)
-            if (node[q] < b) {
-                const double v = __ldcg(p.cfar + ((int64_t)k * BLK + j) * p.P + node[q]);
-                far[q] += p.far_pairs ? ff_to_double(v) : v;
-            }
-    }
-    int r = 0;
-    for (; r + 8 <= rmax; r += 8) {                      // eight rows of loads in flight
-        double v[8][SP];
-#pragma unroll
-        for (int u = 0; u < 8; ++u) {
-            const double *row = p.ring + (int64_t)(r + u) * p.P;
-#pragma unroll
-            for (int q = 0; q < SP; ++q) v[u][q] = node[q] < b ? row[node[q]] : 0.0;
-        }
-#pragma unroll
-        for (int u = 0; u < 8; ++u) {
-            const double w = __ldg(p.wlag + (j - r - u));
-#pragma unroll
-            for (int q = 0; q < SP; ++q) acc[q] = fma(w, v[u][q], acc[q]);
-        }
-    }
-    for (; r < rmax; ++r) {
-        const double w = __ldg(p.wlag + (j - r));
-        const double *row = p.ring + (int64_t)r * p.P;
-#pragma unroll
-        for (int q = 0; q < SP; ++q)
-            if (node[q] < b) acc[q] = fma(w, row[node[q]], acc[q]);
-    }
-#pragma unroll
-    for (int q = 0; q < SP; ++q)
-        if (node[q] < b) out[ht + LTS * q] = far[q] + acc[q];
-}
-
-// history warps of the speculative solve: the same sums in float-float arithmetic on the FP32
-// pipe (one FP64 add per node at the end), from the float-pair copy of the ring and float-pair
-// weights. GB300 issues 2 DFMA/clk/SM, so the FP64 form of these sums (up to 63 rows a step)
+// history warps of the block solves: S[node] = far partials of step j + sum_{r < rmax} w[j - r]
+// D_r[node], in float-float arithmetic on the FP32 pipe (one FP64 add per node at the end), from
+// the float-pair copy of the ring and float-pair weights. GB300 issues 2 DFMA/clk/SM, so the FP64 form of these sums (up to 63 rows a step)
 // occupied the FP64 pipe the solver's recurrences wait on.
 // (ah, al) += far partials of steps j .. j+NJ-1 (NJ accumulators; every load issued first).
 template <int SP, int NJ>

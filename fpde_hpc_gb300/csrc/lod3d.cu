@@ -10,12 +10,14 @@
 //   5. append        : D_n = U - U_old over the grid (the snapshot of the step, :5733-5745)
 // Split path (FPDE_PREC_SPLIT_BF16X3): step 1 becomes, per 64-step block, the exact
 // three-slice tensor-core contraction of all history before the block (tc_far.cu, as for
-// lines) and, per step, k_near_history: the far partials plus the FP64 near history from a
-// 64-row FP64 ring of the block's increments (step 5 writes that ring).
+// lines) and, per step, k_near_history_ff: the far partials plus the near history in
+// float-float from the 64-row float-pair ring of the block's increments (step 5 writes it
+// beside the FP64 ring that the conversion reads).
 // Each pass is a Thomas solve per line with R = Rlap + lam (A_/B/R :3095-3142). For a
 // uniform step the alpha recurrence Al[p+1] = B/(R - A Al[p]) is time-invariant, so it is
 // evaluated once on the host in the reference's order; a pass then needs two first-order
-// recurrences per line (y forward into U in place, U backward).
+// recurrences per line (forward y, backward U), swept by four lanes per line in segments
+// (k_lod_pass_seg) or, for lines over 128 interior nodes, by one thread (k_lod_pass).
 //
 // HBM layout: the state and every grid input keep the reference's index
 // idx = i + j (sN+2) + k (sN+2)(M+2) (:1181). The per-pass line coefficients (A, g =
@@ -259,43 +261,6 @@ __global__ void __launch_bounds__(128, 4) k_lod_pass_seg(LodPassArgs p, LodSegAr
     if (sgi == 0) p.U[base] = fma(__ldg(p.al + line), u1, g0);    // Al[1] U[1] + Bt[1]
 }
 
-// Near history (split path): two nodes per thread, eight ring rows of loads in flight.
-__global__ void __launch_bounds__(256) k_near_history(const double2 *__restrict__ ring, int64_t P2, int j,
-                                                      const double *__restrict__ wlag_all,
-                                                      const double2 *__restrict__ cfar, int KS, int pairs,
-                                                      double2 *__restrict__ S, const int *__restrict__ cta_col,
-                                                      int64_t wstride)
-{
-    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= P2) return;
-    const double *wlag = cta_col ? wlag_all + (int64_t)cta_col[blockIdx.x] * wstride : wlag_all;
-    double ax = 0.0, ay = 0.0, bx = 0.0, by = 0.0;
-    for (int q = 0; q < KS; ++q) {
-        const double2 v = __ldcs(cfar + ((int64_t)q * 64 + j) * P2 + i);
-        bx += pairs ? ff_to_double(v.x) : v.x;
-        by += pairs ? ff_to_double(v.y) : v.y;
-    }
-    int r = 0;
-    for (; r + 8 <= j; r += 8) {
-        double2 v[8];
-#pragma unroll
-        for (int u = 0; u < 8; ++u) v[u] = __ldcg(ring + (int64_t)(r + u) * P2 + i);
-#pragma unroll
-        for (int u = 0; u < 8; ++u) {
-            const double w = __ldg(wlag + (j - r - u));
-            ax = fma(w, v[u].x, ax);
-            ay = fma(w, v[u].y, ay);
-        }
-    }
-    for (; r < j; ++r) {
-        const double2 v = __ldcg(ring + (int64_t)r * P2 + i);
-        const double w = __ldg(wlag + (j - r));
-        ax = fma(w, v.x, ax);
-        ay = fma(w, v.y, ay);
-    }
-    S[i] = make_double2(bx + ax, by + ay);
-}
-
 // Two nodes per thread: S = far partials of step j + sum_{r<j} w[j-r] ring[r] in float-float.
 __global__ void __launch_bounds__(256) k_near_history_ff(const float4 *__restrict__ ringf, int64_t P2, int j,
                                                          const float2 *__restrict__ wff_all,
@@ -347,15 +312,6 @@ int launch_near_history_ff(cudaStream_t st, const float2 *ringf, int64_t P, int 
     return FPDE_OK;
 }
 
-int launch_near_history(cudaStream_t st, const double *ring, int64_t P, int j, const double *wlag,
-                        const double *cfar, int KS, int pairs, double *S, const int *cta_col, int64_t wstride)
-{
-    k_near_history<<<(unsigned)((P / 2 + 255) / 256), 256, 0, st>>>((const double2 *)ring, P / 2, j, wlag,
-                                                                    (const double2 *)cfar, KS, pairs, (double2 *)S,
-                                                                    cta_col, wstride);
-    FPDE_LAUNCHED(1);
-    return FPDE_OK;
-}
 
 }  // namespace fpde
 
