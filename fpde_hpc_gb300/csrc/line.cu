@@ -356,7 +356,9 @@ struct LineBlockArgs {
     int64_t P;
     const double *wlag;                   // w[lag]
     double *agg;                          // [nsteps][2G+2] aggregates, one row of slots per step
-    double *halo;                         // [2][2G+2] chunk edge states by step parity
+    double *halo;                         // [2][2G+2] chunk edge states by step parity (unused)
+    double *hslot;                        // [nsteps][2G] chunk edge states (first, last) of each step,
+                                          // all bits set until written (theta != 0)
     unsigned long long *cflag, *hflag, *seq;
     const double *Lf, *Mb, *Kb, *mb;
     ScanCoef sc;
@@ -404,6 +406,19 @@ __device__ __forceinline__ bool wait_flag(const unsigned long long *f, unsigned 
 }
 
 __device__ __forceinline__ void solver_sync() { asm volatile("bar.sync 1, %0;" ::"n"(LTS) : "memory"); }
+
+// Poll a value slot (all bits set until its one write) with the 1 s bound; false on timeout.
+__device__ __forceinline__ bool poll_slot(const double *slot, unsigned long long t0, double &v)
+{
+    while (true) {
+        const unsigned long long bits = ld_relaxed_u64(slot);
+        if (bits != SLOT_EMPTY) {
+            v = __longlong_as_double((long long)bits);
+            return true;
+        }
+        if (gtimer_ns() - t0 > 1000000000ull) return false;
+    }
+}
 
 // history warps of the block solves: S[node] = far partials of step j + sum_{r < rmax} w[j - r]
 // D_r[node], in float-float arithmetic on the FP32 pipe (one FP64 add per node at the end), from
@@ -903,23 +918,16 @@ __global__ void __launch_bounds__(2 * LTS, 1) k_line_block(LineBlockArgs p)
                 for (int k = 0; k < SP; ++k)
                     if (k < cnt) last = u[k];
                 s_last[tid] = last;
-                double *halo = p.halo + (size_t)(tag & 1ull) * (2 * G + 2);
-                if (cnt > 0 && i0 == a) halo[2 * c] = u[0];
-                if (cnt > 0 && i1 == b) halo[2 * c + 1] = last;
-                solver_sync();
-                if (tid == 0 && G > 1)
-                    asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p.hflag + c), "l"(tag) : "memory");
+                // edge states published as values in this step's slots (each written once per
+                // launch; a 64-bit load is single-copy atomic), polled by the neighbours
+                double *hrow = p.hslot + (size_t)s * (2 * G);
+                if (cnt > 0 && i0 == a) st_relaxed_f64(hrow + 2 * c, u[0]);
+                if (cnt > 0 && i1 == b) st_relaxed_f64(hrow + 2 * c + 1, last);
                 if (s + 1 < p.nsteps && G > 1) {         // neighbours' edge states of this step
                     const unsigned long long t0 = gtimer_ns();
                     bool ok = true;
-                    if (tid == 0 && c > 0) {
-                        ok = wait_flag(p.hflag + c - 1, tag, t0);
-                        if (ok) hl = __ldcg(halo + 2 * (c - 1) + 1);
-                    }
-                    if (cnt > 0 && i1 == b && b < N) {
-                        ok = wait_flag(p.hflag + c + 1, tag, t0);
-                        if (ok) hr = __ldcg(halo + 2 * (c + 1));
-                    }
+                    if (tid == 0 && c > 0) ok = poll_slot(hrow + 2 * (c - 1) + 1, t0, hl);
+                    if (cnt > 0 && i1 == b && b < N) ok = poll_slot(hrow + 2 * (c + 1), t0, hr) && ok;
                     if (!ok) { atomicOr(p.flags, DEVERR_BARRIER_TIMEOUT); s_abort = 1; }
                 }
             }
@@ -1370,6 +1378,7 @@ struct fpde_line {
     double *Lf = nullptr, *Mb = nullptr, *Kb = nullptr, *mb = nullptr;
     unsigned long long *cflag = nullptr, *seq = nullptr, *hflag = nullptr;
     double *halo = nullptr, *sclane = nullptr, *scwarp = nullptr;
+    double *hslot = nullptr;                  // edge-state slots of the block solve (theta != 0)
     double *U = nullptr, *D = nullptr, *part = nullptr, *wrev = nullptr;
     double *agg = nullptr;
     unsigned *barrier = nullptr;
@@ -1502,7 +1511,7 @@ static int line_launch_block(fpde_line *L, cudaStream_t st, int64_t nb0, int j0,
     a.src = L->srcd; a.src_rows = L->src_rows;
     a.U = L->U; a.ring = L->ring; a.cfar = L->cfar; a.KS = KS; a.P = L->P; a.wlag = L->wlag;
     a.far_pairs = L->x3 ? 1 : 0;
-    a.agg = L->agg; a.halo = L->halo; a.cflag = L->cflag; a.hflag = L->hflag; a.seq = L->seq;
+    a.agg = L->agg; a.halo = L->halo; a.cflag = L->cflag; a.hflag = L->hflag; a.seq = L->seq; a.hslot = L->hslot;
     a.Lf = L->Lf; a.Mb = L->Mb; a.Kb = L->Kb; a.mb = L->mb; a.flags = L->ctx->d_flags;
     a.sc.lane = L->sclane; a.sc.warp = L->scwarp;
     a.RB1 = L->RB1; a.RB2 = L->RB2; a.RY1 = L->RY1; a.RY2 = L->RY2;
@@ -1522,6 +1531,7 @@ static int line_launch_block(fpde_line *L, cudaStream_t st, int64_t nb0, int j0,
     cfg.numAttrs = 1;
     // the launch's exchange slots start as SLOT_EMPTY (all bits set)
     FPDE_CUDA(cudaMemsetAsync(L->agg, 0xFF, (size_t)nsteps * (2 * L->G + 2) * sizeof(double), st));
+    if (L->hslot) FPDE_CUDA(cudaMemsetAsync(L->hslot, 0xFF, (size_t)nsteps * 2 * L->G * sizeof(double), st));
     cudaError_t e;
     switch (L->s) {
     case 1: e = launch_block_sp<1>(cfg, a, L->spec); break;
@@ -1654,6 +1664,7 @@ int fpde_line_destroy(fpde_line *L)
     dev_free(L->hflag);
     dev_free(L->seq);
     dev_free(L->halo);
+    dev_free(L->hslot);
     dev_free(L->sclane);
     dev_free(L->scwarp);
     for (double *p : {L->A, L->g, L->al, L->cf, L->cb, L->CF, L->CB, L->GG, L->Lf, L->Mb, L->Kb, L->mb, L->U, L->D,
@@ -1946,6 +1957,7 @@ int fpde_line_create(fpde_ctx *ctx, const fpde_line_desc *desc, const double *A,
                 dev_alloc((void **)&L->U, L->P * sizeof(double)) ||
                 dev_alloc((void **)&L->wrev, wrev.size() * sizeof(double)) ||
                 dev_alloc((void **)&L->agg, (size_t)BLK * (2 * G + 2) * sizeof(double)) ||
+                (d.theta != 0.0 && dev_alloc((void **)&L->hslot, (size_t)BLK * 2 * G * sizeof(double))) ||
                 dev_alloc((void **)&L->halo, 2 * (2 * G + 2) * sizeof(double)) ||
                 dev_alloc((void **)&L->hflag, (size_t)G * sizeof(unsigned long long)) ||
                 (split && (dev_alloc((void **)&L->sclane, hsl.size() * sizeof(double)) ||
