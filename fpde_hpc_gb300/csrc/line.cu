@@ -321,14 +321,15 @@ __global__ void __launch_bounds__(LT) k_line_solve(LineSolveArgs p)
 // Persistent form for the split path: one cooperative launch advances steps j0 .. j0+nsteps-1
 // of a 64-step block, with two warp roles per CTA:
 //   solver warps (LTS threads, SP nodes each): the chunk's right-hand side, the two sweeps and
-//     scans, the exchange of the two chunk aggregates with all other chunks (double-buffered
-//     by step parity, release flags carrying a monotonically growing tag) and the new state;
-//     state and time-invariant data stay in registers for the whole launch;
-//   history warps (LTS threads): during step j, the far partials and the FP64 near history of
+//     scans, the exchange of the two chunk aggregates with all other chunks (one row of value
+//     slots per step, each written once per launch and polled until it leaves the all-bits-set
+//     pattern) and the new state; state and time-invariant data stay in registers for the
+//     whole launch;
+//   history warps (LTS threads): during step j, the far partials and the near history of
 //     step j+1 for every node of the chunk except the newest increment (which the solver
 //     adds), handed over in shared memory.
 // The two roles meet at one CTA barrier per step; the solver warps synchronise among
-// themselves with a named barrier. Near-history FP64 work thus overlaps the latency-bound
+// themselves with a named barrier. The near-history work thus overlaps the latency-bound
 // scans and the exchange.
 //
 // All products of the scans are time-invariant, so they are precomputed on the host: a
@@ -356,10 +357,9 @@ struct LineBlockArgs {
     int64_t P;
     const double *wlag;                   // w[lag]
     double *agg;                          // [nsteps][2G+2] aggregates, one row of slots per step
-    double *halo;                         // [2][2G+2] chunk edge states by step parity (unused)
     double *hslot;                        // [nsteps][2G] chunk edge states (first, last) of each step,
                                           // all bits set until written (theta != 0)
-    unsigned long long *cflag, *hflag, *seq;
+    unsigned long long *cflag, *seq;
     const double *Lf, *Mb, *Kb, *mb;
     ScanCoef sc;
     const double *RB1, *RB2, *RY1, *RY2;  // speculative kernel: sweep responses to E1, E2
@@ -395,14 +395,6 @@ __device__ __forceinline__ void st_relaxed_f64(double *p, double v)
 {
     asm volatile("st.relaxed.gpu.global.b64 [%0], %1;" ::"l"(p), "l"((unsigned long long)__double_as_longlong(v))
                  : "memory");
-}
-
-__device__ __forceinline__ bool wait_flag(const unsigned long long *f, unsigned long long tag,
-                                          unsigned long long t0)
-{
-    while (ld_acquire(f) < tag)
-        if (gtimer_ns() - t0 > 1000000000ull) return false;
-    return true;
 }
 
 __device__ __forceinline__ void solver_sync() { asm volatile("bar.sync 1, %0;" ::"n"(LTS) : "memory"); }
@@ -604,14 +596,13 @@ __global__ void __launch_bounds__(2 * LTS, 1) k_line_block(LineBlockArgs p)
     __shared__ double sCf[NWS][NWS], sCb[NWS][NWS];
     __shared__ double s_cin, s_ub, s_UN;
     __shared__ double s_first[LTS], s_last[LTS];
-    __shared__ unsigned long long s_base;
     __shared__ int s_abort;
     const int tid = threadIdx.x;
     const bool solver = tid < LTS;
     const int c = blockIdx.x, G = p.G, N = p.N;
     const int a = c * p.chunk;
     const int b = min(a + p.chunk, N);
-    if (tid == 0) { s_base = *((volatile unsigned long long *)p.seq); s_abort = 0; }
+    if (tid == 0) s_abort = 0;
     if (tid < NWS * NWS) {
         const double *wc = p.sc.warp + (size_t)c * (2 * NWS * NWS);
         sCf[tid / NWS][tid % NWS] = wc[tid];
@@ -736,12 +727,10 @@ __global__ void __launch_bounds__(2 * LTS, 1) k_line_block(LineBlockArgs p)
         if (i1 == b && cnt > 0 && b < N) hr = p.U[b];
     }
     __syncthreads();                                                        // start
-    const unsigned long long base = s_base;
     const double w1 = __ldg(p.wlag + 1);
     for (int s = 0; s < p.nsteps; ++s) {
         const int j = p.j0 + s;
         const int64_t n = p.n0 + s;
-        const unsigned long long tag = base + (unsigned long long)s + 1;
         double *agg = p.agg + (size_t)s * (2 * G + 2);       // this step's slots (all bits set until written)
         // ---- right-hand side: history (newest row added here) + local term (+ explicit part)
         double om[SP];
@@ -939,7 +928,6 @@ __global__ void __launch_bounds__(2 * LTS, 1) k_line_block(LineBlockArgs p)
     for (int k = 0; k < SP; ++k)
         if (k < cnt) p.U[i0 + k] = u[k];
     if (ownsN) p.U[N] = uNv;
-    if (c == 0 && tid == 0) *((volatile unsigned long long *)p.seq) = base + (unsigned long long)p.nsteps;
 }
 
 
@@ -1376,8 +1364,8 @@ struct fpde_line {
     double *sga = nullptr, *sng = nullptr, *sc1 = nullptr, *sc2 = nullptr, *sc3 = nullptr;  // -g pre-scaling
     float2 *sngf = nullptr;
     double *Lf = nullptr, *Mb = nullptr, *Kb = nullptr, *mb = nullptr;
-    unsigned long long *cflag = nullptr, *seq = nullptr, *hflag = nullptr;
-    double *halo = nullptr, *sclane = nullptr, *scwarp = nullptr;
+    unsigned long long *cflag = nullptr, *seq = nullptr;
+    double *sclane = nullptr, *scwarp = nullptr;
     double *hslot = nullptr;                  // edge-state slots of the block solve (theta != 0)
     double *U = nullptr, *D = nullptr, *part = nullptr, *wrev = nullptr;
     double *agg = nullptr;
@@ -1511,7 +1499,7 @@ static int line_launch_block(fpde_line *L, cudaStream_t st, int64_t nb0, int j0,
     a.src = L->srcd; a.src_rows = L->src_rows;
     a.U = L->U; a.ring = L->ring; a.cfar = L->cfar; a.KS = KS; a.P = L->P; a.wlag = L->wlag;
     a.far_pairs = L->x3 ? 1 : 0;
-    a.agg = L->agg; a.halo = L->halo; a.cflag = L->cflag; a.hflag = L->hflag; a.seq = L->seq; a.hslot = L->hslot;
+    a.agg = L->agg; a.cflag = L->cflag; a.seq = L->seq; a.hslot = L->hslot;
     a.Lf = L->Lf; a.Mb = L->Mb; a.Kb = L->Kb; a.mb = L->mb; a.flags = L->ctx->d_flags;
     a.sc.lane = L->sclane; a.sc.warp = L->scwarp;
     a.RB1 = L->RB1; a.RB2 = L->RB2; a.RY1 = L->RY1; a.RY2 = L->RY2;
@@ -1661,9 +1649,7 @@ int fpde_line_destroy(fpde_line *L)
     for (auto &kv : L->graphs) cudaGraphExecDestroy(kv.second);
     for (cudaEvent_t e : L->probe_ev) cudaEventDestroy(e);
     dev_free(L->cflag);
-    dev_free(L->hflag);
     dev_free(L->seq);
-    dev_free(L->halo);
     dev_free(L->hslot);
     dev_free(L->sclane);
     dev_free(L->scwarp);
@@ -1958,8 +1944,6 @@ int fpde_line_create(fpde_ctx *ctx, const fpde_line_desc *desc, const double *A,
                 dev_alloc((void **)&L->wrev, wrev.size() * sizeof(double)) ||
                 dev_alloc((void **)&L->agg, (size_t)BLK * (2 * G + 2) * sizeof(double)) ||
                 (d.theta != 0.0 && dev_alloc((void **)&L->hslot, (size_t)BLK * 2 * G * sizeof(double))) ||
-                dev_alloc((void **)&L->halo, 2 * (2 * G + 2) * sizeof(double)) ||
-                dev_alloc((void **)&L->hflag, (size_t)G * sizeof(unsigned long long)) ||
                 (split && (dev_alloc((void **)&L->sclane, hsl.size() * sizeof(double)) ||
                            dev_alloc((void **)&L->scwarp, hsw.size() * sizeof(double)))) ||
                 dev_alloc((void **)&L->barrier, 2 * sizeof(unsigned));
@@ -2089,7 +2073,6 @@ int fpde_line_create(fpde_ctx *ctx, const fpde_line_desc *desc, const double *A,
     cudaMemcpyAsync(L->Kb, hKb.data(), hKb.size() * sizeof(double), cudaMemcpyHostToDevice, st);
     cudaMemcpyAsync(L->mb, hmb.data(), gb, cudaMemcpyHostToDevice, st);
     cudaMemsetAsync(L->cflag, 0, (size_t)G * sizeof(unsigned long long), st);
-    cudaMemsetAsync(L->hflag, 0, (size_t)G * sizeof(unsigned long long), st);
     if (split) {
         cudaMemcpyAsync(L->sclane, hsl.data(), hsl.size() * sizeof(double), cudaMemcpyHostToDevice, st);
         cudaMemcpyAsync(L->scwarp, hsw.data(), hsw.size() * sizeof(double), cudaMemcpyHostToDevice, st);
