@@ -524,11 +524,12 @@ def run_ours(args):
         else:
             kernels["far_tc"] = _kernel_entry(tot[1], "k_far_tc3/k_far_tc (tcgen05 far-history contraction)",
                                               peak, peak_src, 1.0)
-            solve_name = ("k_line_block_spec (far fold, float-float near history, speculative FP64 Thomas; "
-                          "one launch per 64-step block)" if not wl.do else
-                          "k_line_block (far fold + FP64 near history + Thomas, one launch per 64-step block)")
+            solve_name = ("k_line_block_spec (far fold, float-float near history, speculative FP64 Thomas"
+                          + (" with the explicit half" if wl.do else "") + "; one launch per 64-step block)")
         kernels["solve"] = _kernel_entry(tot[2], solve_name, peak, peak_src, per(tot[2]))
         kernels = {k: v for k, v in kernels.items() if v}
+        if prec != 0 and "solve" in kernels:
+            kernels["solve"]["limiter"] = "fp64 pipe + per-step synchronisation (not HBM)"
         if prec == fp.FPDE_PREC_SPLIT_BF16X3 and not wl.do:   # traffic per launch, scaled to this line
             nodes = wl.p.N + 1
             if "solve" in kernels:
@@ -536,7 +537,6 @@ def run_ours(args):
                 kernels["solve"]["traffic"] = per * nodes
                 kernels["solve"]["traffic_unit"] = "bytes per step (ncu, scaled by nodes)"
                 kernels["solve"]["traffic_source"] = src
-                kernels["solve"]["limiter"] = "fp64 pipe + per-step synchronisation (not HBM)"
                 kernels["solve"]["fp64_pipe_active"] = SOLVE_FP64_PIPE[0]
                 kernels["solve"]["fp64_pipe_source"] = SOLVE_FP64_PIPE[1]
             if "far_tc" in kernels:

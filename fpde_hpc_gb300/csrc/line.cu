@@ -369,6 +369,9 @@ struct LineBlockArgs {
     // (y = ga y + Om', ga = g A, Om' = -g Om): ng = -g, c1 = -g (w1 - lam), c2 = g w1, c3 = -g w2
     const double *ga, *ng, *c1, *c2, *c3;
     const float2 *ngf;                    // -g as float pairs (the history warps deliver -g H)
+    // speculative kernel with an explicit part: the pre-scaled weights g theta A (on ub at i-1,
+    // i > a) and g theta B (on ub at i+1, i < b-1) of the chunk's own zero-carry backward result
+    const double *xa, *xb;
     unsigned *flags;
     double lam, g0, gN, dLN, AlN;
     int64_t n0;                           // global index of step j0
@@ -932,12 +935,15 @@ __global__ void __launch_bounds__(2 * LTS, 1) k_line_block(LineBlockArgs p)
 
 
 // ---------------------------------------------------------------------------------------
-// Speculative form of the block solve (split path, no explicit part). Everything in a step is
-// linear, so step t+1's right-hand side is known up to step t's two chunk carries:
+// Speculative form of the block solve (split path). Everything in a step is linear, so step
+// t+1's right-hand side is known up to step t's two chunk carries:
 //   Om^{t+1} = Omega0 + c_in E1 + u_b E2,   E1 = (w1 - lam) GG,  E2 = (w1 - lam) CB,
 //   Omega0   = (w1 - lam) ub_t - w1 u^t + src + H_{t+1} + w2 D_{t-1}
 // (ub_t: the chunk's zero-carry backward result of step t, H: far partials plus every history
-// row but the two newest). The solver warps therefore run step t+1's sweeps and scans on
+// row but the two newest). With an explicit part (EXPL: Om -= theta (A u_{i-1} - Rlap u_i +
+// B u_{i+1}) on the state before the step) lam becomes the per-node lam - theta Rlap, the
+// neighbours' ub_t enter Omega0 (xa, xb; at the chunk's first node the term on u_{a-1} =
+// al_{a-1} u_a + c_in folds into c1) and E1, E2 carry the neighbours' GG, CB (host-built). The solver warps therefore run step t+1's sweeps and scans on
 // Omega0 while step t's aggregates are exchanged, and correct them afterwards with the
 // time-invariant chunk-local responses to E1, E2 (RB: backward, RY: forward at the chunk's last
 // node). The history warps poll step t's aggregates of every chunk and form this chunk's carry
@@ -949,10 +955,11 @@ __global__ void __launch_bounds__(2 * LTS, 1) k_line_block(LineBlockArgs p)
 // increments and weights as float pairs; the solver hands each new FP64 row over in shared
 // memory and the history warps convert it), and the four history warps form the four carry
 // dot products side by side.
-template <int SP>
+template <int SP, bool EXPL>
 __global__ void __launch_bounds__(2 * LTS, 1) k_line_block_spec(LineBlockArgs p)
 {
     __shared__ double sS[2][LTS * SP];                   // H_t by parity of t
+    __shared__ double sUf[EXPL ? LTS : 1], sUl[EXPL ? LTS : 1];   // per solver thread: first, last ub
     __shared__ double sD[2][LTS * SP];                   // D_t (FP64) by parity of t
     __shared__ double wXf[NWS], wXb[NWS];
     __shared__ double sCf[NWS][NWS], sCb[NWS][NWS];
@@ -1134,6 +1141,7 @@ __global__ void __launch_bounds__(2 * LTS, 1) k_line_block_spec(LineBlockArgs p)
     const double mbc = __ldg(p.mb + c);
     double u[SP], kga[SP], kng[SP], kc1[SP], kc2[SP], kc3[SP], kal[SP], kcf[SP], kcb[SP], kCB[SP], kGG[SP];
     double rb1[SP], rb2[SP];
+    double kxa[EXPL ? SP : 1], kxb[EXPL ? SP : 1];
     double dm1[SP];                                      // D_{t-1}
     double dm2[SP];                                      // D_{t-2} (prologue only)
 #pragma unroll
@@ -1153,6 +1161,10 @@ __global__ void __launch_bounds__(2 * LTS, 1) k_line_block_spec(LineBlockArgs p)
         kGG[k] = in ? __ldg(p.GG + i) : 0.0;
         rb1[k] = in ? __ldg(p.RB1 + i) : 0.0;
         rb2[k] = in ? __ldg(p.RB2 + i) : 0.0;
+        if constexpr (EXPL) {
+            kxa[k] = in ? __ldg(p.xa + i) : 0.0;
+            kxb[k] = in ? __ldg(p.xb + i) : 0.0;
+        }
         dm1[k] = (in && p.j0 >= 1) ? p.ring[(int64_t)(p.j0 - 1) * p.P + i] : 0.0;
         dm2[k] = (in && p.j0 >= 2) ? p.ring[(int64_t)(p.j0 - 2) * p.P + i] : 0.0;
     }
@@ -1231,16 +1243,36 @@ __global__ void __launch_bounds__(2 * LTS, 1) k_line_block_spec(LineBlockArgs p)
         return p.src ? p.src + (int64_t)(n < p.src_rows ? n : p.src_rows - 1) * (N + 1) : nullptr;
     };
 
+    if constexpr (EXPL) {                                // edge states of the threads' segments
+        sUf[tid] = cnt > 0 ? u[0] : 0.0;
+        sUl[tid] = cnt > 0 ? last_of<SP>(u, cnt) : 0.0;
+    }
     __syncthreads();                                                        // start: H_j0 ready
     // ---- prologue: step j0 from its full right-hand side
     {
         const double *src = src_row(p.n0);
         const double *hs = sS[p.j0 & 1];                 // -g H_j0
+        double ul = 0.0, hr = 0.0;                       // explicit part: the neighbours of the segment
+        if constexpr (EXPL) {
+            if (cnt > 0) {
+                ul = tid > 0 ? sUl[tid - 1] : (a > 0 ? p.U[a - 1] : 0.0);
+                hr = i1 < b ? sUf[tid + 1] : (b < N ? p.U[b] : uNv);
+            }
+        }
 #pragma unroll
         for (int k = 0; k < SP; ++k) {
             om[k] = 0.0;
             if (k < cnt) {
-                const double rest = (-(lam * u[k]) + (src ? __ldg(src + i0 + k) : 0.0)) + fma(w1, dm1[k], w2 * dm2[k]);
+                double rest;
+                if constexpr (EXPL) {
+                    const int i = i0 + k;
+                    const double un = k + 1 < cnt ? u[k + 1] : hr;
+                    rest = (-(__ldg(p.lamv + i) * u[k]) + (src ? __ldg(src + i) : 0.0)) + fma(w1, dm1[k], w2 * dm2[k]);
+                    rest -= fma(__ldg(p.eA + i), ul, __ldg(p.eB + i) * un);
+                    ul = u[k];
+                } else {
+                    rest = (-(lam * u[k]) + (src ? __ldg(src + i0 + k) : 0.0)) + fma(w1, dm1[k], w2 * dm2[k]);
+                }
                 om[k] = fma(kng[k], rest, hs[i0 - a + k]);
             }
         }
@@ -1286,6 +1318,10 @@ __global__ void __launch_bounds__(2 * LTS, 1) k_line_block_spec(LineBlockArgs p)
                 uNv = UN;
             }
         }
+        if constexpr (EXPL) {                            // the segment's first and last ub_t
+            sUf[tid] = cnt > 0 ? ubc[0] : 0.0;
+            sUl[tid] = cnt > 0 ? last_of<SP>(ubc, cnt) : 0.0;
+        }
         __syncthreads();                                                    // X(s)
         if (t + 1 < jend) {
             // ---- step t+1 on Omega0, while the aggregates of step t are exchanged
@@ -1305,6 +1341,18 @@ __global__ void __launch_bounds__(2 * LTS, 1) k_line_block_spec(LineBlockArgs p)
                 for (int k = 0; k < SP; ++k) {
                     om[k] = 0.0;
                     if (k < cnt) om[k] = fma(kc1[k], ubc[k], fma(kc2[k], u[k], fma(kc3[k], dm1[k], hs[i0 - a + k])));
+                }
+            }
+            if constexpr (EXPL) {                        // neighbours' ub_t inside the chunk
+                const double xl = (cnt > 0 && tid > 0) ? sUl[tid - 1] : 0.0;
+                const double xr = (cnt > 0 && i1 < b) ? sUf[tid + 1] : 0.0;
+#pragma unroll
+                for (int k = 0; k < SP; ++k) {
+                    if (k < cnt) {
+                        const double ul = k > 0 ? ubc[k - 1] : xl;
+                        const double ur = k + 1 < cnt ? ubc[k + 1] : xr;
+                        om[k] = fma(kxa[k], ul, fma(kxb[k], ur, om[k]));
+                    }
                 }
             }
             sweeps();
@@ -1363,6 +1411,7 @@ struct fpde_line {
     float2 *ringf = nullptr, *wff = nullptr;  // the ring and the lag weights as float pairs
     double *sga = nullptr, *sng = nullptr, *sc1 = nullptr, *sc2 = nullptr, *sc3 = nullptr;  // -g pre-scaling
     float2 *sngf = nullptr;
+    double *sxa = nullptr, *sxb = nullptr;    // pre-scaled neighbour weights (explicit part)
     double *Lf = nullptr, *Mb = nullptr, *Kb = nullptr, *mb = nullptr;
     unsigned long long *cflag = nullptr, *seq = nullptr;
     double *sclane = nullptr, *scwarp = nullptr;
@@ -1455,29 +1504,22 @@ static cudaEvent_t *probe_begin(fpde_line *L, int kind, int64_t n, double bytes,
 static cudaError_t spec_smem_attrs()
 {
     static cudaError_t done = [] {
-        cudaError_t e = cudaFuncSetAttribute(k_line_block_spec<1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)SpecRing<1>::bytes);
-        if (e == cudaSuccess)
-            e = cudaFuncSetAttribute(k_line_block_spec<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)SpecRing<2>::bytes);
-        if (e == cudaSuccess)
-            e = cudaFuncSetAttribute(k_line_block_spec<4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)SpecRing<4>::bytes);
-        if (e == cudaSuccess)
-            e = cudaFuncSetAttribute(k_line_block_spec<8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)SpecRing<8>::bytes);
-        if (e == cudaSuccess)
-            e = cudaFuncSetAttribute(k_line_block<1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)SpecRing<1>::bytes);
-        if (e == cudaSuccess)
-            e = cudaFuncSetAttribute(k_line_block<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)SpecRing<2>::bytes);
-        if (e == cudaSuccess)
-            e = cudaFuncSetAttribute(k_line_block<4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)SpecRing<4>::bytes);
-        if (e == cudaSuccess)
-            e = cudaFuncSetAttribute(k_line_block<8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)SpecRing<8>::bytes);
+        cudaError_t e = cudaSuccess;
+        auto opt = [&e](const void *fn, size_t bytes) {
+            if (e == cudaSuccess) e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+        };
+        opt((const void *)k_line_block_spec<1, false>, SpecRing<1>::bytes);
+        opt((const void *)k_line_block_spec<2, false>, SpecRing<2>::bytes);
+        opt((const void *)k_line_block_spec<4, false>, SpecRing<4>::bytes);
+        opt((const void *)k_line_block_spec<8, false>, SpecRing<8>::bytes);
+        opt((const void *)k_line_block_spec<1, true>, SpecRing<1>::bytes);
+        opt((const void *)k_line_block_spec<2, true>, SpecRing<2>::bytes);
+        opt((const void *)k_line_block_spec<4, true>, SpecRing<4>::bytes);
+        opt((const void *)k_line_block_spec<8, true>, SpecRing<8>::bytes);
+        opt((const void *)k_line_block<1>, SpecRing<1>::bytes);
+        opt((const void *)k_line_block<2>, SpecRing<2>::bytes);
+        opt((const void *)k_line_block<4>, SpecRing<4>::bytes);
+        opt((const void *)k_line_block<8>, SpecRing<8>::bytes);
         return e;
     }();
     return done;
@@ -1487,7 +1529,9 @@ template <int SP>
 static cudaError_t launch_block_sp(cudaLaunchConfig_t cfg, const LineBlockArgs &a, bool spec)
 {
     cfg.dynamicSmemBytes = SpecRing<SP>::bytes;     // both keep the newest rows in shared memory
-    return spec ? cudaLaunchKernelEx(&cfg, k_line_block_spec<SP>, a) : cudaLaunchKernelEx(&cfg, k_line_block<SP>, a);
+    if (!spec) return cudaLaunchKernelEx(&cfg, k_line_block<SP>, a);
+    return a.xa ? cudaLaunchKernelEx(&cfg, k_line_block_spec<SP, true>, a)
+                : cudaLaunchKernelEx(&cfg, k_line_block_spec<SP, false>, a);
 }
 
 // Steps j0 .. j0+nsteps-1 of the block starting at nb0 in one persistent launch.
@@ -1505,6 +1549,7 @@ static int line_launch_block(fpde_line *L, cudaStream_t st, int64_t nb0, int j0,
     a.RB1 = L->RB1; a.RB2 = L->RB2; a.RY1 = L->RY1; a.RY2 = L->RY2;
     a.ringf = L->ringf; a.wff = L->wff;
     a.ga = L->sga; a.ng = L->sng; a.c1 = L->sc1; a.c2 = L->sc2; a.c3 = L->sc3; a.ngf = L->sngf;
+    a.xa = L->sxa; a.xb = L->sxb;
     a.lam = L->lam; a.g0 = L->d.left_value; a.gN = L->d.right_value; a.dLN = L->d.dLN; a.AlN = L->AlN;
     a.n0 = nb0 + j0; a.j0 = j0; a.nsteps = nsteps; a.N = (int)L->N; a.G = L->G; a.rkind = L->d.right_kind;
     a.chunk = L->chunk;
@@ -1661,6 +1706,8 @@ int fpde_line_destroy(fpde_line *L)
     dev_free(L->wff);
     for (double *q : {L->sga, L->sng, L->sc1, L->sc2, L->sc3}) dev_free(q);
     dev_free(L->sngf);
+    dev_free(L->sxa);
+    dev_free(L->sxb);
     for (uint16_t *p : {L->h_hi, L->h_lo, L->w_hi, L->w_lo, L->h3[0], L->h3[1], L->h3[2], L->w3[0], L->w3[1],
                         L->w3[2]})
         dev_free(p);
@@ -1740,7 +1787,10 @@ int fpde_line_create(fpde_ctx *ctx, const fpde_line_desc *desc, const double *A,
         FPDE_CUDA(spec_smem_attrs());
         FPDE_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_line_block<LSEG>, 2 * LTS,
                                                                 SpecRing<LSEG>::bytes));
-        FPDE_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm2, k_line_block_spec<LSEG>, 2 * LTS,
+        FPDE_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm2, k_line_block_spec<LSEG, false>, 2 * LTS,
+                                                                SpecRing<LSEG>::bytes));
+        per_sm = std::min(per_sm, per_sm2);
+        FPDE_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm2, k_line_block_spec<LSEG, true>, 2 * LTS,
                                                                 SpecRing<LSEG>::bytes));
         per_sm = std::min(per_sm, per_sm2);
     }
@@ -1897,8 +1947,8 @@ int fpde_line_create(fpde_ctx *ctx, const fpde_line_desc *desc, const double *A,
     // is affine in step n's chunk carries (c_in, u_b) through E1 = (w1 - lam) GG and
     // E2 = (w1 - lam) CB; the chunk-local zero-carry sweeps of E1, E2 (forward y -> RY, backward
     // u -> RB) are time-invariant.
-    L->spec = split && d.theta == 0.0;
-    std::vector<double> hRB1, hRB2, hRY1, hRY2;
+    L->spec = split;
+    std::vector<double> hRB1, hRB2, hRY1, hRY2, hklam, hXA, hXB, hfold;
     std::vector<float2> hwff;
     if (split) {                                   // w = hi + lo, hi the nearest float
         hwff.resize(LW);
@@ -1908,16 +1958,47 @@ int fpde_line_create(fpde_ctx *ctx, const fpde_line_desc *desc, const double *A,
         }
     }
     if (L->spec) {
+        // E1, E2: Omega0's coefficients on the carries (c_in, u_b) of the step before. With an
+        // explicit part (theta != 0) the new state at the neighbours enters too: inside the
+        // chunk u = ub + c_in GG + u_b CB; before it u_{a-1} = al_{a-1} u_a + c_in (the backward
+        // recurrence with the chunk's carry-in); after it u_b is the carry-out itself. The terms
+        // on the neighbours' ub stay in Omega0 (XA, XB; node a's term folds into its own ub).
         hRB1.assign(N, 0.0); hRB2.assign(N, 0.0); hRY1.assign(N, 0.0); hRY2.assign(N, 0.0);
-        const double cE = wlag[1] - L->lam;
+        hklam.assign(N, L->lam); hXA.assign(N, 0.0); hXB.assign(N, 0.0); hfold.assign(N, 0.0);
+        std::vector<double> hE1(N, 0.0), hE2(N, 0.0);
+        const double w1 = wlag[1], th = d.theta;
+        if (th != 0.0)
+            for (int64_t i = 1; i < N; ++i) hklam[i] = L->lam - th * Rlap[i];
         for (int cc = 0; cc < G; ++cc) {
             const int64_t a0 = (int64_t)cc * chunk, b0 = std::min<int64_t>(a0 + chunk, N);
+            for (int64_t i = std::max<int64_t>(a0, 1); i < b0; ++i) {
+                hE1[i] = (w1 - hklam[i]) * hGG[i];
+                hE2[i] = (w1 - hklam[i]) * hCB[i];
+                if (th == 0.0) continue;
+                const double eA = th * A[i], eB = th * B[i];
+                if (i > a0) {
+                    hE1[i] -= eA * hGG[i - 1];
+                    hE2[i] -= eA * hCB[i - 1];
+                    hXA[i] = -eA;
+                } else {                           // i == a0 > 0
+                    hE1[i] -= eA * (hal[a0 - 1] * hGG[a0] + 1.0);
+                    hE2[i] -= eA * hal[a0 - 1] * hCB[a0];
+                    hfold[i] = -eA * hal[a0 - 1];  // on node a's own ub
+                }
+                if (i < b0 - 1) {
+                    hE1[i] -= eB * hGG[i + 1];
+                    hE2[i] -= eB * hCB[i + 1];
+                    hXB[i] = -eB;
+                } else {
+                    hE2[i] -= eB;                  // u_b = the chunk's carry-out
+                }
+            }
             double y1 = 0.0, y2 = 0.0;
             for (int64_t i = a0; i < b0; ++i) {
                 if (i == 0) { y1 = 0.0; y2 = 0.0; }
                 else {
-                    y1 = hg[i] * (hA[i] * y1 - cE * hGG[i]);
-                    y2 = hg[i] * (hA[i] * y2 - cE * hCB[i]);
+                    y1 = hg[i] * (hA[i] * y1 - hE1[i]);
+                    y2 = hg[i] * (hA[i] * y2 - hE2[i]);
                 }
                 hRY1[i] = y1;
                 hRY2[i] = y2;
@@ -2010,6 +2091,8 @@ int fpde_line_create(fpde_ctx *ctx, const fpde_line_desc *desc, const double *A,
                dev_alloc((void **)&L->RY2, nb) || dev_alloc((void **)&L->sga, nb) ||
                dev_alloc((void **)&L->sng, nb) || dev_alloc((void **)&L->sc1, nb) || dev_alloc((void **)&L->sc2, nb) ||
                dev_alloc((void **)&L->sc3, nb) || dev_alloc((void **)&L->sngf, (size_t)N * sizeof(float2));
+    if (!fail && L->spec && d.theta != 0.0)
+        fail = dev_alloc((void **)&L->sxa, nb) || dev_alloc((void **)&L->sxb, nb);
     if (fail) {
         std::string keep = fpde_last_error_string();
         fpde_line_destroy(L);
@@ -2039,15 +2122,17 @@ int fpde_line_create(fpde_ctx *ctx, const fpde_line_desc *desc, const double *A,
         cudaMemcpyAsync(L->RB2, hRB2.data(), nb, cudaMemcpyHostToDevice, st);
         cudaMemcpyAsync(L->RY1, hRY1.data(), nb, cudaMemcpyHostToDevice, st);
         cudaMemcpyAsync(L->RY2, hRY2.data(), nb, cudaMemcpyHostToDevice, st);
-        std::vector<double> h1(N), h2(N), h3(N), h4(N), h5(N);
+        std::vector<double> h1(N), h2(N), h3(N), h4(N), h5(N), h6(N), h7(N);
         std::vector<float2> hngf(N);
-        const double w1 = wlag[1], w2 = wlag[2], cE = w1 - L->lam;
+        const double w1 = wlag[1], w2 = wlag[2];
         for (int64_t i = 0; i < N; ++i) {
             h1[i] = hp[i];                         // g A
             h2[i] = -hg[i];
-            h3[i] = -hg[i] * cE;
+            h3[i] = -hg[i] * ((w1 - hklam[i]) + hfold[i]);
             h4[i] = hg[i] * w1;
             h5[i] = -hg[i] * w2;
+            h6[i] = -hg[i] * hXA[i];
+            h7[i] = -hg[i] * hXB[i];
             const float hi = (float)h2[i];
             hngf[i] = make_float2(hi, (float)(h2[i] - (double)hi));
         }
@@ -2057,6 +2142,10 @@ int fpde_line_create(fpde_ctx *ctx, const fpde_line_desc *desc, const double *A,
         cudaMemcpyAsync(L->sc2, h4.data(), nb, cudaMemcpyHostToDevice, st);
         cudaMemcpyAsync(L->sc3, h5.data(), nb, cudaMemcpyHostToDevice, st);
         cudaMemcpyAsync(L->sngf, hngf.data(), (size_t)N * sizeof(float2), cudaMemcpyHostToDevice, st);
+        if (L->sxa) {
+            cudaMemcpyAsync(L->sxa, h6.data(), nb, cudaMemcpyHostToDevice, st);
+            cudaMemcpyAsync(L->sxb, h7.data(), nb, cudaMemcpyHostToDevice, st);
+        }
     }
     if (L->srcd)
         cudaMemcpyAsync(L->srcd, d.source, (size_t)L->src_rows * (N + 1) * sizeof(double), cudaMemcpyHostToDevice, st);

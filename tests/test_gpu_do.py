@@ -101,6 +101,37 @@ def test_do_line_split_x3_vs_oracle(ctx):
     assert err <= 1e-7
 
 
+
+@pytest.mark.parametrize("sp,chunks,theta,right", [
+    (1, 0, 1.0, (0, 0.0)),      # one node per solver thread, built-in chunks
+    (2, 30, 0.5, (1, 0.0)),     # ragged chunks of 200 nodes (idle solver threads), flux end
+    (4, 13, 1.0, (1, 0.3)),     # four nodes per thread, 116 of 128 threads busy, boundary flux
+])
+def test_do_line_split_explicit_partitions_vs_oracle(ctx, sp, chunks, theta, right):
+    """The speculative block solve with an explicit part (theta != 0): its right-hand side
+    takes the neighbours' zero-carry results inside each chunk, the previous chunk's carry
+    at the chunk's first node and the carry-out at its last, under every partition shape
+    (nodes per thread, ragged chunks, idle threads) and both right-end kinds, with per-step
+    sources, against the oracle to 1e-7 over 300 steps (5 blocks)."""
+    import fpde_hpc_gb300 as fp
+    from fpde_hpc_gb300 import problems
+    p = problems.config3(N=6000, steps=300)
+    A, B, R = p.coefs()
+    c = fp.do_weights(p.orders, p.qw, p.tau, p.steps + 1, p.gnorm)
+    rng = np.random.default_rng(11)
+    src = 0.1 * rng.standard_normal((40, p.N + 1))
+    tuning = fp.LineTuning(solve_sp=sp, chunks=chunks, far_splits=0, gemv_splits=0)
+    line = fp.Line(ctx, p.N, 0.5, p.tau, 1.0, A, B, R, p.u0, p.steps, right=right, dLN=1.0 / p.N,
+                   lag_weights=c / p.tau, theta=theta, source=src, precision=3, tuning=tuning)
+    line.run(p.steps)
+    u = line.state()
+    line.close()
+    uref, _ = oracle.line_run_general(p.u0, p.steps, c / p.tau, theta, A, B, R, src, rtype=right[0],
+                                      gN=right[1], dLN=1.0 / p.N)
+    err = relmax(u, uref)
+    print(f"DO line N=6000 300 steps bf16x3, sp={sp} chunks={chunks} theta={theta} right={right}: {err:.2e}")
+    assert err <= 1e-7
+
 def _derivative(ctx, F, tau, c, t0=1, j0=0, maxt=-1, DF0=None, append=0):
     import torch
     import fpde_hpc_gb300 as fp
