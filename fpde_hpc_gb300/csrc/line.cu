@@ -9,9 +9,9 @@
 //     at n0:  convert the finished block's FP64 increments into 16-bit history slices,
 //             build the Toeplitz weight tile and run the tensor-core contraction for the
 //             far history t < n0 (tc_far.cu) -> FP64 partials C[split][j][i]
-//     steps of the block: k_line_block, one persistent launch: S = sum_split C[split][j][i]
-//             + sum_{n0 <= t < n} w[n-t] D_t[i] (near history in FP64), the solve, and D_n
-//             into a 64-row FP64 ring.
+//     steps of the block: k_line_block_spec, one persistent launch: S = sum_split C[split][j][i]
+//             + sum_{n0 <= t < n} w[n-t] D_t[i] (near history in float-float), the solve
+//             (speculated one step ahead), and D_n into a 64-row FP64 ring.
 // The whole run is captured once into a CUDA graph and replayed.
 //
 // The Thomas solve of a long line runs on all SMs. The alpha recurrence
@@ -357,8 +357,6 @@ struct LineBlockArgs {
     int64_t P;
     const double *wlag;                   // w[lag]
     double *agg;                          // [nsteps][2G+2] aggregates, one row of slots per step
-    double *hslot;                        // [nsteps][2G] chunk edge states (first, last) of each step,
-                                          // all bits set until written (theta != 0)
     unsigned long long *cflag, *seq;
     const double *Lf, *Mb, *Kb, *mb;
     ScanCoef sc;
@@ -378,13 +376,6 @@ struct LineBlockArgs {
     int j0, nsteps, N, G, rkind, chunk;
 };
 
-__device__ __forceinline__ unsigned long long ld_acquire(const unsigned long long *f)
-{
-    unsigned long long v;
-    asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(f) : "memory");
-    return v;
-}
-
 constexpr unsigned long long SLOT_EMPTY = ~0ull;        // exchange slot not yet written (a NaN pattern)
 
 __device__ __forceinline__ unsigned long long ld_relaxed_u64(const double *p)
@@ -401,19 +392,6 @@ __device__ __forceinline__ void st_relaxed_f64(double *p, double v)
 }
 
 __device__ __forceinline__ void solver_sync() { asm volatile("bar.sync 1, %0;" ::"n"(LTS) : "memory"); }
-
-// Poll a value slot (all bits set until its one write) with the 1 s bound; false on timeout.
-__device__ __forceinline__ bool poll_slot(const double *slot, unsigned long long t0, double &v)
-{
-    while (true) {
-        const unsigned long long bits = ld_relaxed_u64(slot);
-        if (bits != SLOT_EMPTY) {
-            v = __longlong_as_double((long long)bits);
-            return true;
-        }
-        if (gtimer_ns() - t0 > 1000000000ull) return false;
-    }
-}
 
 // history warps of the block solves: S[node] = far partials of step j + sum_{r < rmax} w[j - r]
 // D_r[node], in float-float arithmetic on the FP32 pipe (one FP64 add per node at the end), from
@@ -567,15 +545,7 @@ __device__ __forceinline__ double last_of(const double (&v)[SP], int n)
     return r;
 }
 
-template <int SP>
-__device__ __forceinline__ void history_store_ff(int ht, int a, int b, const float *ah, const float *al, double *out)
-{
-#pragma unroll
-    for (int q = 0; q < SP; ++q)
-        if (a + ht + LTS * q < b) out[ht + LTS * q] = f2d_bits(ah[q]) + f2d_bits(al[q]);
-}
-
-// The same, times the per-node factor sg (a float pair): (ah + al) sg in float-float, one FP64 add.
+// out = (ah + al) sg for this thread's nodes, sg a per-node float pair: float-float, one FP64 add.
 template <int SP>
 __device__ __forceinline__ void history_store_scaled_ff(int ht, int a, int b, const float *ah, const float *al,
                                                         const float2 *sg, double *out)
@@ -590,349 +560,6 @@ __device__ __forceinline__ void history_store_scaled_ff(int ht, int a, int b, co
             out[ht + LTS * q] = f2d_bits(ph) + f2d_bits(pe);
         }
 }
-
-template <int SP>
-__global__ void __launch_bounds__(2 * LTS, 1) k_line_block(LineBlockArgs p)
-{
-    __shared__ double sS[2][LTS * SP];                   // next step's history, by step parity
-    __shared__ double wXf[NWS], wXb[NWS];
-    __shared__ double sCf[NWS][NWS], sCb[NWS][NWS];
-    __shared__ double s_cin, s_ub, s_UN;
-    __shared__ double s_first[LTS], s_last[LTS];
-    __shared__ int s_abort;
-    const int tid = threadIdx.x;
-    const bool solver = tid < LTS;
-    const int c = blockIdx.x, G = p.G, N = p.N;
-    const int a = c * p.chunk;
-    const int b = min(a + p.chunk, N);
-    if (tid == 0) s_abort = 0;
-    if (tid < NWS * NWS) {
-        const double *wc = p.sc.warp + (size_t)c * (2 * NWS * NWS);
-        sCf[tid / NWS][tid % NWS] = wc[tid];
-        sCb[tid / NWS][tid % NWS] = wc[NWS * NWS + tid];
-    }
-
-    if (!solver) {
-        // ======================================================= history warps
-        // Float-float sums on the FP32 pipe (as in the speculative kernel): every FP64 row the
-        // solver appends is converted once into the float-pair ring and the shared-memory ring
-        // of the block's newest rows; the far partials fold in as float pairs.
-        const int ht = tid - LTS;
-        constexpr int NR = SpecRing<SP>::NR;
-        extern __shared__ float2 spec_rows[];
-        float2 *sR = spec_rows;
-        auto convert_row = [&](int r) {                  // FP64 ring row r -> float pairs
-#pragma unroll
-            for (int q = 0; q < SP; ++q) {
-                const int i = a + ht + LTS * q;
-                if (i < b) p.ringf[(int64_t)r * p.P + i] = d2ff(p.ring[(int64_t)r * p.P + i]);
-            }
-        };
-        if (p.j0 >= 1) convert_row(p.j0 - 1);           // the previous launch's last row
-        const int rlo0 = max(0, p.j0 - NR);
-        for (int r = rlo0; r < p.j0; ++r) {
-#pragma unroll
-            for (int q = 0; q < SP; ++q) {
-                const int i = a + ht + LTS * q;
-                if (i < b) sR[(r % NR) * (LTS * SP) + ht + LTS * q] = p.ringf[(int64_t)r * p.P + i];
-            }
-        }
-        auto history = [&](int j, int rmax, int rlo, double *out) {
-            float h[1][SP], l[1][SP];
-#pragma unroll
-            for (int q = 0; q < SP; ++q) { h[0][q] = 0.f; l[0][q] = 0.f; }
-            far_fold_ff<SP, 1>(p, ht, a, b, j, h, l);
-            rows_split_ff<SP>(p, sR, ht, a, b, j, rmax, rlo, h[0], l[0]);
-            history_store_ff<SP>(ht, a, b, h[0], l[0], out);
-        };
-        history(p.j0, p.j0, rlo0, sS[p.j0 & 1]);                            // full history of step j0
-        __syncthreads();                                                    // start
-        for (int s = 0; s < p.nsteps; ++s) {
-            const int j = p.j0 + s;
-            if (s >= 1) {                                // row j-1 (appended at the end of step s-1)
-                float2 *srow = sR + ((j - 1) % NR) * (LTS * SP);
-#pragma unroll
-                for (int q = 0; q < SP; ++q) {
-                    const int i = a + ht + LTS * q;
-                    if (i < b) {
-                        const float2 f = d2ff(p.ring[(int64_t)(j - 1) * p.P + i]);
-                        p.ringf[(int64_t)(j - 1) * p.P + i] = f;
-                        srow[ht + LTS * q] = f;
-                    }
-                }
-            }
-            if (s + 1 < p.nsteps) history(j + 1, j, max(0, j - NR), sS[(j + 1) & 1]);
-            __syncthreads();                                                // end of step s
-            if (s_abort) return;
-        }
-        return;
-    }
-
-    // =========================================================== solver warps
-    const int lane = tid & 31, warp = tid >> 5;
-    const int i0 = a + tid * SP;
-    const int i1 = min(i0 + SP, b);
-    const int cnt = max(0, i1 - i0);
-    const bool expl = p.eA != nullptr;
-    double PF[5], PB[5], PeF, PeB;
-    {
-        const int64_t T = (int64_t)c * LTS + tid, GT = (int64_t)G * LTS;
-#pragma unroll
-        for (int k = 0; k < 5; ++k) {
-            PF[k] = __ldg(p.sc.lane + k * GT + T);
-            PB[k] = __ldg(p.sc.lane + (6 + k) * GT + T);
-        }
-        PeF = __ldg(p.sc.lane + 5 * GT + T);
-        PeB = __ldg(p.sc.lane + 11 * GT + T);
-    }
-    double lf[5], lfN[5], mbv[5], kbv[5], mbc = 0.0;
-    if (warp == 0) {
-#pragma unroll
-        for (int t = 0; t < 5; ++t) {
-            const int q = lane + 32 * t;
-            const bool in = q < G;
-            lf[t] = in ? __ldg(p.Lf + (int64_t)c * G + q) : 0.0;
-            lfN[t] = in ? __ldg(p.Lf + (int64_t)G * G + q) : 0.0;
-            mbv[t] = in ? __ldg(p.Mb + (int64_t)c * G + q) : 0.0;
-            kbv[t] = in ? __ldg(p.Kb + (int64_t)c * G + q) : 0.0;
-        }
-        mbc = __ldg(p.mb + c);
-    }
-    double u[SP], kA[SP], kg[SP], kal[SP], kcf[SP], kcb[SP], kCB[SP], kGG[SP], klam[SP], dprev[SP];
-#pragma unroll
-    for (int k = 0; k < SP; ++k) {
-        const bool in = k < cnt;
-        const int i = in ? i0 + k : 0;
-        u[k] = in ? p.U[i] : 0.0;
-        kA[k] = in ? __ldg(p.A + i) : 0.0;
-        kg[k] = in ? __ldg(p.g + i) : 0.0;
-        kal[k] = in ? __ldg(p.al + i) : 0.0;
-        kcf[k] = in ? __ldg(p.cf + i) : 0.0;
-        kcb[k] = in ? __ldg(p.cb + i) : 0.0;
-        kCB[k] = in ? __ldg(p.CB + i) : 0.0;
-        kGG[k] = in ? __ldg(p.GG + i) : 0.0;
-        klam[k] = (in && p.lamv) ? __ldg(p.lamv + i) : p.lam;
-        dprev[k] = 0.0;
-    }
-    const bool ownsN = cnt > 0 && i1 == N;
-    double uNv = ownsN ? p.U[N] : 0.0;
-    if (expl) {
-        s_first[tid] = cnt > 0 ? u[0] : 0.0;
-        double last = 0.0;
-#pragma unroll
-        for (int k = 0; k < SP; ++k)
-            if (k < cnt) last = u[k];
-        s_last[tid] = last;
-    }
-    double hl = 0.0, hr = 0.0;                           // neighbour edge states (explicit part)
-    if (expl) {
-        if (tid == 0 && c > 0) hl = p.U[a - 1];
-        if (i1 == b && cnt > 0 && b < N) hr = p.U[b];
-    }
-    __syncthreads();                                                        // start
-    const double w1 = __ldg(p.wlag + 1);
-    for (int s = 0; s < p.nsteps; ++s) {
-        const int j = p.j0 + s;
-        const int64_t n = p.n0 + s;
-        double *agg = p.agg + (size_t)s * (2 * G + 2);       // this step's slots (all bits set until written)
-        // ---- right-hand side: history (newest row added here) + local term (+ explicit part)
-        double om[SP];
-        const double *src = p.src ? p.src + (int64_t)(n < p.src_rows ? n : p.src_rows - 1) * (N + 1) : nullptr;
-        const double *hs = sS[j & 1];
-#pragma unroll
-        for (int k = 0; k < SP; ++k) {
-            const double S = k < cnt ? fma(w1, dprev[k], hs[i0 - a + k]) : 0.0;
-            om[k] = (-(klam[k] * u[k]) + ((src && k < cnt) ? __ldg(src + i0 + k) : 0.0)) + S;
-        }
-        if (expl) {
-            if (tid > 0) hl = s_last[tid - 1];
-            if (i1 < b && cnt > 0) hr = s_first[tid + 1];
-            if (ownsN) hr = uNv;
-            double ul = hl;
-#pragma unroll
-            for (int k = 0; k < SP; ++k) {
-                if (k < cnt) {
-                    const double un = k + 1 < cnt ? u[k + 1] : hr;
-                    om[k] -= fma(__ldg(p.eA + i0 + k), ul, __ldg(p.eB + i0 + k) * un);
-                    ul = u[k];
-                }
-            }
-        }
-        if (ownsN && p.rkind != FPDE_BC_DIRICHLET) st_relaxed_f64(agg + 2 * G, last_of<SP>(u, cnt));  // old U[N-1], flux
-        // ---- forward: segment sweep from zero carry, warp scan, warp totals
-        double y[SP];
-        double yl = 0.0;
-#pragma unroll
-        for (int k = 0; k < SP; ++k) {
-            if (k < cnt) {
-                if (i0 + k == 0) yl = p.g0;
-                else yl = kg[k] * (kA[k] * yl - om[k]);
-                y[k] = yl;
-            }
-        }
-        double X = cnt > 0 ? yl : 0.0;
-#pragma unroll
-        for (int k = 0; k < 5; ++k) {
-            const double Xp = __shfl_up_sync(FULL, X, 1 << k);
-            if (lane >= (1 << k)) X = fma(PF[k], Xp, X);
-        }
-        double Xe = __shfl_up_sync(FULL, X, 1);
-        if (lane == 0) Xe = 0.0;
-        if (lane == 31) wXf[warp] = X;
-        solver_sync();                                                      // (A)
-        {
-            double x0 = 0.0, x1 = 0.0;
-#pragma unroll
-            for (int w = 0; w < NWS; w += 2) {
-                if (w < warp) x0 = fma(sCf[warp][w], wXf[w], x0);
-                if (w + 1 < warp) x1 = fma(sCf[warp][w + 1], wXf[w + 1], x1);
-            }
-            const double carry = fma(PeF, x0 + x1, Xe);
-#pragma unroll
-            for (int k = 0; k < SP; ++k)
-                if (k < cnt) y[k] = fma(kcf[k], carry, y[k]);
-        }
-        if (cnt > 0 && i1 == b) st_relaxed_f64(agg + 2 * c, last_of<SP>(y, cnt));   // the chunk's last y (zero carry-in)
-        // ---- backward: segment sweep from zero carry, warp scan, warp totals
-        double ub[SP];
-        double ul = 0.0;
-#pragma unroll
-        for (int k = SP - 1; k >= 0; --k) {
-            if (k < cnt) {
-                ul = fma(kal[k], ul, y[k]);
-                ub[k] = ul;
-            }
-        }
-        X = cnt > 0 ? ul : 0.0;
-#pragma unroll
-        for (int k = 0; k < 5; ++k) {
-            const double Xn = __shfl_down_sync(FULL, X, 1 << k);
-            if (lane + (1 << k) < 32) X = fma(PB[k], Xn, X);
-        }
-        Xe = __shfl_down_sync(FULL, X, 1);
-        if (lane == 31) Xe = 0.0;
-        if (lane == 0) wXb[warp] = X;
-        solver_sync();                                                      // (B)
-        {
-            double x0 = 0.0, x1 = 0.0;
-#pragma unroll
-            for (int w = 0; w < NWS; w += 2) {
-                if (w > warp) x0 = fma(sCb[warp][w], wXb[w], x0);
-                if (w + 1 > warp) x1 = fma(sCb[warp][w + 1], wXb[w + 1], x1);
-            }
-            const double carry = fma(PeB, x0 + x1, Xe);
-#pragma unroll
-            for (int k = 0; k < SP; ++k)
-                if (k < cnt) ub[k] = fma(kcb[k], carry, ub[k]);
-        }
-        if (tid == 0) st_relaxed_f64(agg + 2 * c + 1, ub[0]);   // the chunk's first u (zero carries)
-        // ---- warp 0: every chunk's aggregates, polled as values: each slot is written once per
-        // launch and holds the all-bits-set pattern until then (a NaN no arithmetic produces);
-        // a 64-bit load is single-copy atomic, so a slot that differs from it is the final value
-        if (warp == 0) {
-            double ye[5], u0[5], uNm1 = 0.0;
-            bool ok = true;
-            const bool need_nm1 = p.rkind != FPDE_BC_DIRICHLET;
-            const unsigned long long t0 = gtimer_ns();
-            while (true) {
-                bool mine = true;
-#pragma unroll
-                for (int t = 0; t < 5; ++t) {
-                    const int q = lane + 32 * t;
-                    ye[t] = 0.0;
-                    u0[t] = 0.0;
-                    if (q < G) {
-                        const unsigned long long by = ld_relaxed_u64(agg + 2 * q), bu = ld_relaxed_u64(agg + 2 * q + 1);
-                        if (by == SLOT_EMPTY || bu == SLOT_EMPTY) mine = false;
-                        ye[t] = __longlong_as_double((long long)by);
-                        u0[t] = __longlong_as_double((long long)bu);
-                    }
-                }
-                if (need_nm1 && lane == 0) {
-                    const unsigned long long bn = ld_relaxed_u64(agg + 2 * G);
-                    if (bn == SLOT_EMPTY) mine = false;
-                    uNm1 = __longlong_as_double((long long)bn);
-                }
-                if (__all_sync(FULL, mine)) break;
-                if (gtimer_ns() - t0 > 1000000000ull) { ok = false; break; }
-            }
-            ok = __all_sync(FULL, ok);
-            if (!ok) {
-                if (lane == 0) { atomicOr(p.flags, DEVERR_BARRIER_TIMEOUT); s_abort = 1; }
-            } else {
-                double sc = 0.0, syN = 0.0, sub = 0.0;
-#pragma unroll
-                for (int t = 0; t < 5; ++t) {
-                    sc = fma(lf[t], ye[t], sc);
-                    syN = fma(lfN[t], ye[t], syN);
-                    sub = fma(mbv[t], u0[t], fma(kbv[t], ye[t], sub));
-                }
-#pragma unroll
-                for (int o = 16; o > 0; o >>= 1) {
-                    sc += __shfl_xor_sync(FULL, sc, o);
-                    syN += __shfl_xor_sync(FULL, syN, o);
-                    sub += __shfl_xor_sync(FULL, sub, o);
-                }
-                double uN;                               // right end (U1 :4685-4719)
-                if (p.rkind == FPDE_BC_DIRICHLET) {
-                    uN = p.gN;
-                } else {                                 // lane 0 holds the old U[N-1]
-                    if (fabs(syN) > 1e-15) uN = (fabs(1.0 - p.AlN) > 1e-15) ? (syN + p.gN * p.dLN) / (1.0 - p.AlN) : uNm1;
-                    else uN = (fabs(1.0 - p.AlN) > 1e-15) ? 0.0 : uNm1;
-                }
-                if (lane == 0) { s_cin = sc; s_ub = fma(mbc, uN, sub); s_UN = uN; }
-            }
-        }
-        solver_sync();                                                      // (D)
-        if (!s_abort) {
-            const double cin = s_cin, ubv = s_ub;
-            // ---- new state and its increment (into the ring; the solver keeps it for the next step)
-#pragma unroll
-            for (int k = 0; k < SP; ++k) {
-                if (k < cnt) {
-                    const int64_t i = i0 + k;
-                    const double un = fma(kCB[k], ubv, fma(kGG[k], cin, ub[k]));
-                    const double d = un - u[k];
-                    p.ring[(int64_t)j * p.P + i] = d;
-                    u[k] = un;
-                    dprev[k] = d;
-                }
-            }
-            if (ownsN) {
-                const double UN = s_UN;
-                p.ring[(int64_t)j * p.P + N] = UN - uNv;
-                uNv = UN;
-            }
-            if (expl) {                                  // edge states for the next step
-                s_first[tid] = cnt > 0 ? u[0] : 0.0;
-                double last = 0.0;
-#pragma unroll
-                for (int k = 0; k < SP; ++k)
-                    if (k < cnt) last = u[k];
-                s_last[tid] = last;
-                // edge states published as values in this step's slots (each written once per
-                // launch; a 64-bit load is single-copy atomic), polled by the neighbours
-                double *hrow = p.hslot + (size_t)s * (2 * G);
-                if (cnt > 0 && i0 == a) st_relaxed_f64(hrow + 2 * c, u[0]);
-                if (cnt > 0 && i1 == b) st_relaxed_f64(hrow + 2 * c + 1, last);
-                if (s + 1 < p.nsteps && G > 1) {         // neighbours' edge states of this step
-                    const unsigned long long t0 = gtimer_ns();
-                    bool ok = true;
-                    if (tid == 0 && c > 0) ok = poll_slot(hrow + 2 * (c - 1) + 1, t0, hl);
-                    if (cnt > 0 && i1 == b && b < N) ok = poll_slot(hrow + 2 * (c + 1), t0, hr) && ok;
-                    if (!ok) { atomicOr(p.flags, DEVERR_BARRIER_TIMEOUT); s_abort = 1; }
-                }
-            }
-        }
-        __syncthreads();                                                    // end of step s
-        if (s_abort) return;
-    }
-#pragma unroll
-    for (int k = 0; k < SP; ++k)
-        if (k < cnt) p.U[i0 + k] = u[k];
-    if (ownsN) p.U[N] = uNv;
-}
-
 
 // ---------------------------------------------------------------------------------------
 // Speculative form of the block solve (split path). Everything in a step is linear, so step
@@ -1405,8 +1032,7 @@ struct fpde_line {
     double lam = 0, lamR = 0, kkk0 = 0, AlN = 0;
     double *A = nullptr, *g = nullptr, *al = nullptr, *cf = nullptr, *cb = nullptr;
     double *CF = nullptr, *CB = nullptr, *GG = nullptr;
-    // speculative block solve (split path, theta == 0): chunk-local responses of the sweeps
-    bool spec = false;
+    // speculative block solve (split path): chunk-local responses of the sweeps
     double *RB1 = nullptr, *RB2 = nullptr, *RY1 = nullptr, *RY2 = nullptr;
     float2 *ringf = nullptr, *wff = nullptr;  // the ring and the lag weights as float pairs
     double *sga = nullptr, *sng = nullptr, *sc1 = nullptr, *sc2 = nullptr, *sc3 = nullptr;  // -g pre-scaling
@@ -1415,7 +1041,6 @@ struct fpde_line {
     double *Lf = nullptr, *Mb = nullptr, *Kb = nullptr, *mb = nullptr;
     unsigned long long *cflag = nullptr, *seq = nullptr;
     double *sclane = nullptr, *scwarp = nullptr;
-    double *hslot = nullptr;                  // edge-state slots of the block solve (theta != 0)
     double *U = nullptr, *D = nullptr, *part = nullptr, *wrev = nullptr;
     double *agg = nullptr;
     unsigned *barrier = nullptr;
@@ -1516,20 +1141,15 @@ static cudaError_t spec_smem_attrs()
         opt((const void *)k_line_block_spec<2, true>, SpecRing<2>::bytes);
         opt((const void *)k_line_block_spec<4, true>, SpecRing<4>::bytes);
         opt((const void *)k_line_block_spec<8, true>, SpecRing<8>::bytes);
-        opt((const void *)k_line_block<1>, SpecRing<1>::bytes);
-        opt((const void *)k_line_block<2>, SpecRing<2>::bytes);
-        opt((const void *)k_line_block<4>, SpecRing<4>::bytes);
-        opt((const void *)k_line_block<8>, SpecRing<8>::bytes);
         return e;
     }();
     return done;
 }
 
 template <int SP>
-static cudaError_t launch_block_sp(cudaLaunchConfig_t cfg, const LineBlockArgs &a, bool spec)
+static cudaError_t launch_block_sp(cudaLaunchConfig_t cfg, const LineBlockArgs &a)
 {
     cfg.dynamicSmemBytes = SpecRing<SP>::bytes;     // both keep the newest rows in shared memory
-    if (!spec) return cudaLaunchKernelEx(&cfg, k_line_block<SP>, a);
     return a.xa ? cudaLaunchKernelEx(&cfg, k_line_block_spec<SP, true>, a)
                 : cudaLaunchKernelEx(&cfg, k_line_block_spec<SP, false>, a);
 }
@@ -1543,7 +1163,7 @@ static int line_launch_block(fpde_line *L, cudaStream_t st, int64_t nb0, int j0,
     a.src = L->srcd; a.src_rows = L->src_rows;
     a.U = L->U; a.ring = L->ring; a.cfar = L->cfar; a.KS = KS; a.P = L->P; a.wlag = L->wlag;
     a.far_pairs = L->x3 ? 1 : 0;
-    a.agg = L->agg; a.cflag = L->cflag; a.seq = L->seq; a.hslot = L->hslot;
+    a.agg = L->agg; a.cflag = L->cflag; a.seq = L->seq;
     a.Lf = L->Lf; a.Mb = L->Mb; a.Kb = L->Kb; a.mb = L->mb; a.flags = L->ctx->d_flags;
     a.sc.lane = L->sclane; a.sc.warp = L->scwarp;
     a.RB1 = L->RB1; a.RB2 = L->RB2; a.RY1 = L->RY1; a.RY2 = L->RY2;
@@ -1564,13 +1184,12 @@ static int line_launch_block(fpde_line *L, cudaStream_t st, int64_t nb0, int j0,
     cfg.numAttrs = 1;
     // the launch's exchange slots start as SLOT_EMPTY (all bits set)
     FPDE_CUDA(cudaMemsetAsync(L->agg, 0xFF, (size_t)nsteps * (2 * L->G + 2) * sizeof(double), st));
-    if (L->hslot) FPDE_CUDA(cudaMemsetAsync(L->hslot, 0xFF, (size_t)nsteps * 2 * L->G * sizeof(double), st));
     cudaError_t e;
     switch (L->s) {
-    case 1: e = launch_block_sp<1>(cfg, a, L->spec); break;
-    case 2: e = launch_block_sp<2>(cfg, a, L->spec); break;
-    case 4: e = launch_block_sp<4>(cfg, a, L->spec); break;
-    default: e = launch_block_sp<8>(cfg, a, L->spec); break;
+    case 1: e = launch_block_sp<1>(cfg, a); break;
+    case 2: e = launch_block_sp<2>(cfg, a); break;
+    case 4: e = launch_block_sp<4>(cfg, a); break;
+    default: e = launch_block_sp<8>(cfg, a); break;
     }
     if (e != cudaSuccess) return set_error(FPDE_ERR_CUDA, "line block launch: %s", cudaGetErrorString(e));
     count_launches(1);
@@ -1695,7 +1314,6 @@ int fpde_line_destroy(fpde_line *L)
     for (cudaEvent_t e : L->probe_ev) cudaEventDestroy(e);
     dev_free(L->cflag);
     dev_free(L->seq);
-    dev_free(L->hslot);
     dev_free(L->sclane);
     dev_free(L->scwarp);
     for (double *p : {L->A, L->g, L->al, L->cf, L->cb, L->CF, L->CB, L->GG, L->Lf, L->Mb, L->Kb, L->mb, L->U, L->D,
@@ -1785,11 +1403,8 @@ int fpde_line_create(fpde_ctx *ctx, const fpde_line_desc *desc, const double *A,
     if (split) {
         int per_sm2 = 0;
         FPDE_CUDA(spec_smem_attrs());
-        FPDE_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_line_block<LSEG>, 2 * LTS,
+        FPDE_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_line_block_spec<LSEG, false>, 2 * LTS,
                                                                 SpecRing<LSEG>::bytes));
-        FPDE_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm2, k_line_block_spec<LSEG, false>, 2 * LTS,
-                                                                SpecRing<LSEG>::bytes));
-        per_sm = std::min(per_sm, per_sm2);
         FPDE_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm2, k_line_block_spec<LSEG, true>, 2 * LTS,
                                                                 SpecRing<LSEG>::bytes));
         per_sm = std::min(per_sm, per_sm2);
@@ -1943,11 +1558,10 @@ int fpde_line_create(fpde_ctx *ctx, const fpde_line_desc *desc, const double *A,
                                 : d.Da * (L->kkk0 * l1_lag(d.alpha, j)) / d.tau;
     std::vector<double> wrev(L->max_steps + 1, 0.0);
     for (int64_t m = 0; m < L->max_steps; ++m) wrev[m] = wlag[L->max_steps - m];
-    // Speculative block solve (split path without an explicit part): step n+1's right-hand side
-    // is affine in step n's chunk carries (c_in, u_b) through E1 = (w1 - lam) GG and
-    // E2 = (w1 - lam) CB; the chunk-local zero-carry sweeps of E1, E2 (forward y -> RY, backward
+    // Speculative block solve (split path): step n+1's right-hand side is affine in step n's
+    // chunk carries (c_in, u_b) through E1 and E2 (without an explicit part (w1 - lam) GG and
+    // (w1 - lam) CB); the chunk-local zero-carry sweeps of E1, E2 (forward y -> RY, backward
     // u -> RB) are time-invariant.
-    L->spec = split;
     std::vector<double> hRB1, hRB2, hRY1, hRY2, hklam, hXA, hXB, hfold;
     std::vector<float2> hwff;
     if (split) {                                   // w = hi + lo, hi the nearest float
@@ -1957,7 +1571,7 @@ int fpde_line_create(fpde_ctx *ctx, const fpde_line_desc *desc, const double *A,
             hwff[j] = make_float2(hi, (float)(wlag[j] - (double)hi));
         }
     }
-    if (L->spec) {
+    if (split) {
         // E1, E2: Omega0's coefficients on the carries (c_in, u_b) of the step before. With an
         // explicit part (theta != 0) the new state at the neighbours enters too: inside the
         // chunk u = ub + c_in GG + u_b CB; before it u_{a-1} = al_{a-1} u_a + c_in (the backward
@@ -2024,7 +1638,6 @@ int fpde_line_create(fpde_ctx *ctx, const fpde_line_desc *desc, const double *A,
                 dev_alloc((void **)&L->U, L->P * sizeof(double)) ||
                 dev_alloc((void **)&L->wrev, wrev.size() * sizeof(double)) ||
                 dev_alloc((void **)&L->agg, (size_t)BLK * (2 * G + 2) * sizeof(double)) ||
-                (d.theta != 0.0 && dev_alloc((void **)&L->hslot, (size_t)BLK * 2 * G * sizeof(double))) ||
                 (split && (dev_alloc((void **)&L->sclane, hsl.size() * sizeof(double)) ||
                            dev_alloc((void **)&L->scwarp, hsw.size() * sizeof(double)))) ||
                 dev_alloc((void **)&L->barrier, 2 * sizeof(unsigned));
@@ -2086,12 +1699,12 @@ int fpde_line_create(fpde_ctx *ctx, const fpde_line_desc *desc, const double *A,
     if (!fail && split)
         fail = dev_alloc((void **)&L->ringf, (size_t)BLK * L->P * sizeof(float2)) ||
                dev_alloc((void **)&L->wff, (size_t)LW * sizeof(float2));
-    if (!fail && L->spec)
+    if (!fail && split)
         fail = dev_alloc((void **)&L->RB1, nb) || dev_alloc((void **)&L->RB2, nb) || dev_alloc((void **)&L->RY1, nb) ||
                dev_alloc((void **)&L->RY2, nb) || dev_alloc((void **)&L->sga, nb) ||
                dev_alloc((void **)&L->sng, nb) || dev_alloc((void **)&L->sc1, nb) || dev_alloc((void **)&L->sc2, nb) ||
                dev_alloc((void **)&L->sc3, nb) || dev_alloc((void **)&L->sngf, (size_t)N * sizeof(float2));
-    if (!fail && L->spec && d.theta != 0.0)
+    if (!fail && split && d.theta != 0.0)
         fail = dev_alloc((void **)&L->sxa, nb) || dev_alloc((void **)&L->sxb, nb);
     if (fail) {
         std::string keep = fpde_last_error_string();
@@ -2117,7 +1730,7 @@ int fpde_line_create(fpde_ctx *ctx, const fpde_line_desc *desc, const double *A,
         cudaMemcpyAsync(L->wff, hwff.data(), (size_t)LW * sizeof(float2), cudaMemcpyHostToDevice, st);
         cudaMemsetAsync(L->ringf, 0, (size_t)BLK * L->P * sizeof(float2), st);
     }
-    if (L->spec) {
+    if (split) {
         cudaMemcpyAsync(L->RB1, hRB1.data(), nb, cudaMemcpyHostToDevice, st);
         cudaMemcpyAsync(L->RB2, hRB2.data(), nb, cudaMemcpyHostToDevice, st);
         cudaMemcpyAsync(L->RY1, hRY1.data(), nb, cudaMemcpyHostToDevice, st);
