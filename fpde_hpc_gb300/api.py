@@ -137,6 +137,34 @@ class Context:
                                           1 if dev else 0), "fpde_sum_snapshots")
         return S
 
+    def sum_alg(self, sum_alg, old, tau, kb=None, sum_param=0.0, bs=0, Htmp=None, row2=None, gtj=0.0, gt=0.0,
+                alpha=0.0, tstep=0, nodes=None):
+        """The reference Sum kernel in history mode sum_alg (0 full, 1 restricted, 2 series
+        expansion; fpde_sum). old: (old_size, OS) time-major snapshots (the two newest for
+        sum_alg 2); Htmp: (nodes, ceil(sum_param)) moments, updated in place. Returns S."""
+        dev = _is_dev(old)
+        old = _f64(old)
+        nold, OS = old.shape
+        nodes = OS if nodes is None else nodes
+        if dev:
+            import torch
+            S = torch.zeros(nodes, dtype=torch.float64, device=old.device)
+        else:
+            S = np.zeros(nodes)
+        if sum_alg == 2:
+            P = int(np.ceil(sum_param))
+            if Htmp is None or tuple(Htmp.shape) != (nodes, P):
+                raise ValueError("Htmp must be (nodes, ceil(sum_param))")
+            if not (Htmp.flags["C_CONTIGUOUS"] if not dev else Htmp.is_contiguous()):
+                raise ValueError("Htmp must be contiguous")
+            row2 = _f64(row2)
+        tau = _f64(tau) if tau is not None else None
+        kb = _f64(kb) if kb is not None else None
+        check(self.lib.fpde_sum(self.h, sum_alg, bs, OS, nodes, _ptr(S), _ptr(old), nold, _ptr(tau), _ptr(Htmp),
+                                _ptr(row2), _ptr(kb), float(sum_param), float(gtj), float(gt), float(alpha),
+                                int(tstep), 1 if dev else 0), "fpde_sum")
+        return S
+
     def tridiag_solve(self, a, b, r, om, u, n_lines, N, stride_elem, stride_line, left_kind=0,
                       left_val=None, right_kind=0, right_val=None, dLN=0.0):
         dev = _is_dev(u)

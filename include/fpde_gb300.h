@@ -157,6 +157,36 @@ int fpde_l1_sum(fpde_hist *h, const double *kb, const double *tau, double scale,
 int fpde_sum_snapshots(fpde_ctx *ctx, double *S, const double *old, int old_size, int64_t OS,
                        int64_t nodes, const double *tau, const double *kb_3_cache, int on_device);
 
+/* The reference's Sum kernel with every history mode it compiles in (fpde_hpc_1d.cpp:1407-1478,
+ * the sum_alg and BS defines; its arguments S, old, old_size, tau, Htmp, row2_precalc,
+ * kb_3_cache, sum_param, gtj, gt, alpha, tstep in the reference's order, args set :1851-1868;
+ * CPU form time_summing :4108-4151). Snapshots are time-major, old[t*OS + id], id < nodes.
+ *   sum_alg 0: S[id] = sum_{t=old_size-2..0} kb_3_cache[t]*(old[t+1]-old[t])/tau[t]
+ *              (fpde_sum_snapshots).
+ *   sum_alg 1: restricted summing, the same terms from the newest down while the weight stays
+ *              at or above sum_param:
+ *                bs == 0: time_summing's rule (:4117-4131): stop before the first term with
+ *                         |kb_3_cache[t]| < sum_param;
+ *                bs  > 0: the GPU kernel's rule with BS = bs: whole chunks of bs terms (weights
+ *                         before t = 0 count as 0), stopping after the first chunk whose bs
+ *                         weights are all below sum_param.
+ *   sum_alg 2: series expansion (:4137-4151, :1457-1475) with P = ceil(sum_param) (1..128)
+ *              moments per node in Htmp[id*P + j] (updated in place), from the two snapshots
+ *              old[0..OS) and old[OS..2*OS) (old_size >= 2; otherwise S = 0 and Htmp unchanged):
+ *                d = old[OS+id] - old[id]
+ *                Htmp[id*P+j] += gt^(j+1) * row2_precalc[j] * d,            j < P
+ *                S[id] = sum_j v_j * Htmp[id*P+j] / tau[tstep],
+ *                v_0 = gtj^-alpha,  v_j = v_{j-1} * (alpha + j - 1) / (j * gtj),
+ *              with the GPU kernel's guards (a non-finite d, row2_precalc[j], power or v_j
+ *              counts as 0). gt, gtj: g(t) at the step's two ends.
+ * Arrays per on_device: old (old_size rows; 2 for sum_alg 2), tau (old_size-1 values, or at
+ * least tstep+1 for sum_alg 2), kb_3_cache (old_size-1), Htmp (nodes*P), row2_precalc (P), S
+ * (nodes). Unused pointers may be NULL. Synchronous, like the reference's launch. */
+int fpde_sum(fpde_ctx *ctx, int sum_alg, int bs, int64_t OS, int64_t nodes, double *S, const double *old,
+             int old_size, const double *tau, double *Htmp, const double *row2_precalc,
+             const double *kb_3_cache, double sum_param, double gtj, double gt, double alpha, int tstep,
+             int on_device);
+
 /* The history sum of fpde_l1_sum from caller-owned device buffers, allocating nothing.
  * No counterpart in the reference. For callers that cannot call cudaMalloc while they run
  * (a host framework that owns all device memory, a fixed device-memory budget, a step loop

@@ -63,6 +63,66 @@ void fo_l1_sum_snapshots(const double *old, int64_t OS, int nold, const double *
     }
 }
 
+void fo_sum_restricted(const double *old, int64_t OS, int nold, const double *kb, const double *tau,
+                       double thr, int bs, int64_t nodes, double *S)
+{
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < nodes; i++) {
+        double s = 0.0;
+        if (bs == 0) {
+            for (int t = nold - 2; t >= 0; t--) {          /* :4110-4131 */
+                double kv = kb[t];
+                double diff = old[(int64_t)(t + 1) * OS + i] - old[(int64_t)t * OS + i];
+                if (fabs(kv) < thr) break;
+                s += kv * diff / tau[t];
+            }
+        } else {
+            for (int t = nold - 2; t >= 0; t -= bs) {       /* :1422-1455, one chunk per pass */
+                int br = 0;
+                for (int q = 0; q < bs; q++) {
+                    double kv = t - q >= 0 ? kb[t - q] : 0.0;
+                    if (t - q >= 0) {
+                        double diff = old[(int64_t)(t - q + 1) * OS + i] - old[(int64_t)(t - q) * OS + i];
+                        s += kv * diff / tau[t - q];
+                    }
+                    if (fabs(kv) < thr) br++;
+                }
+                if (br == bs) break;
+            }
+        }
+        S[i] = s;
+    }
+}
+
+void fo_sum_series(const double *prev, const double *cur, int64_t nodes, double *H, int P, const double *row2,
+                   double gt, double gtj, double alpha, double tau_t, double *S)
+{
+    double *pw = (double *)malloc((size_t)P * sizeof(double));
+    double *v = (double *)malloc((size_t)P * sizeof(double));
+    double mult = gt, vv = pow(gtj, -alpha);
+    for (int j = 0; j < P; j++) {
+        pw[j] = isfinite(mult) ? mult : 0.0;                /* mult = g^(j+1), :4143-4148 */
+        v[j] = isfinite(vv) ? vv : 0.0;                     /* v1, :1165-1178 */
+        mult *= gt;
+        double ii = (double)(j + 1);
+        vv *= -(-alpha - ii + 1.0) / (ii * gtj);
+    }
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < nodes; i++) {
+        double d = cur[i] - prev[i];
+        if (!isfinite(d)) d = 0.0;
+        double sum = 0.0;
+        for (int j = 0; j < P; j++) {
+            double r = isfinite(row2[j]) ? row2[j] : 0.0;
+            H[i * P + j] += pw[j] * r * d;
+            sum += v[j] * H[i * P + j];
+        }
+        S[i] = sum / tau_t;
+    }
+    free(pw);
+    free(v);
+}
+
 /* ------------------------------------------------------------------ Thomas */
 
 static void thomas_core(int N, const double *A, const double *B, const double *R,

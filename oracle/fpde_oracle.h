@@ -39,6 +39,22 @@ void fo_l1_sum(const double *D, int64_t P, int n, const double *kb, const double
 void fo_l1_sum_snapshots(const double *old, int64_t OS, int nold, const double *kb,
                          const double *tau, int64_t nodes, double *S);
 
+/* Restricted summing (sum_alg 1, time_summing fpde_hpc_1d.cpp:4110-4131): the terms of
+ * fo_l1_sum_snapshots from the newest down, stopping before the first |kb[t]| < thr
+ * (bs == 0); or the GPU Sum kernel's rule (:1422-1455, bs == BS > 0): chunks of bs terms
+ * are added whole (weights before t = 0 count as 0), stopping after the first chunk whose
+ * bs weights are all below thr. */
+void fo_sum_restricted(const double *old, int64_t OS, int nold, const double *kb, const double *tau,
+                       double thr, int bs, int64_t nodes, double *S);
+
+/* Series expansion (sum_alg 2, time_summing :4137-4151 with _kb_row2_fixed_coefs
+ * :1159-1180; the GPU kernel's finiteness guards :1459-1469): P moments per node in
+ * H[i*P + j], updated with d = cur[i] - prev[i]:
+ *   H[i*P+j] += gt^(j+1) * row2[j] * d;  S[i] = sum_j v_j H[i*P+j] / tau_t,
+ *   v_0 = pow(gtj, -alpha), v_j = v_{j-1} * (-(-alpha - j + 1) / (j * gtj)). */
+void fo_sum_series(const double *prev, const double *cur, int64_t nodes, double *H, int P, const double *row2,
+                   double gt, double gtj, double alpha, double tau_t, double *S);
+
 /* Thomas solve of one line (al1 :4002-4027, bt1 :4585-4590, back-substitution in U1
  * :4678-4725): A[i] U[i-1] - R[i] U[i] + B[i] U[i+1] = Om[i], i = 1..N-1.
  * Left boundary: ltype 0 -> U[0] = g0 (Al[1] = 0, Bt[1] = g0); ltype 1 -> flux form

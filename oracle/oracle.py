@@ -36,6 +36,8 @@ def load():
     lib.fo_l1_weights.argtypes = [d, _dp, i32, _dp, C.POINTER(d)]
     lib.fo_l1_sum.argtypes = [_dp, i64, i32, _dp, _dp, i64, i64, _dp]
     lib.fo_l1_sum_snapshots.argtypes = [_dp, i64, i32, _dp, _dp, i64, _dp]
+    lib.fo_sum_restricted.argtypes = [_dp, i64, i32, _dp, _dp, d, i32, i64, _dp]
+    lib.fo_sum_series.argtypes = [_dp, _dp, i64, _dp, i32, _dp, d, d, d, d, _dp]
     lib.fo_thomas_line.argtypes = [i32, _dp, _dp, _dp, _dp, i32, d, i32, d, d, _dp]
     lib.fo_line_coefs.argtypes = [i32, _dp, _dp, _dp, _dp, _dp, _dp]
     lib.fo_line_step.argtypes = [i32, _dp, _dp, i64, i32, _dp, _dp, d, d, _dp, _dp, _dp, vp,
@@ -98,6 +100,28 @@ def l1_sum_snapshots(old, kb, tau):
     S = np.zeros(OS)
     lib.fo_l1_sum_snapshots(old.reshape(-1), OS, nold, np.ascontiguousarray(kb, dtype=np.float64),
                             np.ascontiguousarray(tau, dtype=np.float64), OS, S)
+    return S
+
+
+def sum_restricted(old, kb, tau, thr, bs=0):
+    lib = load()
+    old = np.ascontiguousarray(old, dtype=np.float64)
+    nold, OS = old.shape
+    S = np.zeros(OS)
+    lib.fo_sum_restricted(old.reshape(-1), OS, nold, np.ascontiguousarray(kb, dtype=np.float64),
+                          np.ascontiguousarray(tau, dtype=np.float64), thr, bs, OS, S)
+    return S
+
+
+def sum_series(prev, cur, H, row2, gt, gtj, alpha, tau_t):
+    """One step of the series-expansion history; H (nodes, P) is updated in place."""
+    lib = load()
+    assert H.dtype == np.float64 and H.flags["C_CONTIGUOUS"]
+    nodes, P = H.shape
+    S = np.zeros(nodes)
+    lib.fo_sum_series(np.ascontiguousarray(prev, dtype=np.float64), np.ascontiguousarray(cur, dtype=np.float64),
+                      nodes, H.reshape(-1), P, np.ascontiguousarray(row2, dtype=np.float64), gt, gtj, alpha,
+                      tau_t, S)
     return S
 
 

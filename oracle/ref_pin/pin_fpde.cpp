@@ -12,6 +12,10 @@
  *     hard-coded analytic problems: the tridiagonal coefficients A_/B/R of every line of
  *     every pass (:3095-3142), the source Rp of the K pass (:2724) and the Dirichlet
  *     boundary values bc0/bcN of every line (:4491-4583).
+ * Two more scenarios run the column with the reference's other history modes
+ * (time_summing :4108-4151): sum_alg 1 (restricted summing) and sum_alg 2 (series
+ * expansion, with the per-step coefficient row row2_precalc[time_i1][0] and g(t) at the
+ * step's ends, the inputs of the Sum kernel's series branch).
  * The oracle and the GPU path replay the same steps from those inputs and must match the
  * recorded grids to 1e-12. Scenarios are listed in main().
  */
@@ -172,6 +176,57 @@ static void run_lod(const char *path, int analytic, int bs, int nb, int mb, int 
     printf("wrote %s (%zu steps, grid %dx%dx%d)\n", path, taus.size(), sN, _M, K);
 }
 
+/* The column (analytic 2) with sum_alg 1 or 2: per step the history sum b_Utimesum, the grid,
+ * the weights kb_3_cache (sum_alg 1) or the series inputs (sum_alg 2: row2_precalc[time_i1][0]
+ * padded with zeros to sum_param values, gt = g(Time[tstep]), gtj = g(Time[tstep+1]),
+ * tau[tstep]). Old snapshots are kept (dont_clear_sum_alg1) so that the record is complete. */
+static void run_sumalg(const char *path, int alg, double param, int kcells, double alpha, double tau, int steps)
+{
+    set_dims(1, 3, 3, kcells);
+    varT = 0; varZ = 0; varXY = 0;
+    implicit = 0; implicit3d = 0; rp_split_3d = 0;
+    sum_alg = alg; sum_param = param; dont_clear_sum_alg1 = 1;
+    global_eps = 1e-15; global_eps2 = 1e-15;
+    FILE *lg = fopen("/dev/null", "w");
+    H_solver *s = new H_solver(2, 1, 5, 0, 1, alpha, 1.0, 0, 0, 0, 3, lg, 2);
+    size_t G = (size_t)(sN + 2) * (_M + 2) * (K + 2);
+    FgvWriter w(path);
+    w.scalar("sN", sN); w.scalar("M", _M); w.scalar("K", K);
+    w.scalar("alpha", alpha); w.scalar("sum_alg", alg); w.scalar("sum_param", param);
+    std::vector<uint64_t> gdims = {(uint64_t)(K + 2), (uint64_t)(_M + 2), (uint64_t)(sN + 2)};
+    w.put("U0", gdims, s->b_U);
+    const int P = (int)ceil(param);
+    std::vector<double> kb_all, kb_off, tauv, S_all, U_all, row2, gt, gtj;
+    for (int n = 0; n < steps; n++) {
+        s->calc_step(tau);
+        kb_off.push_back((double)kb_all.size());
+        kb_all.insert(kb_all.end(), s->kb_3_cache.begin(), s->kb_3_cache.end());
+        tauv.push_back(s->tau[s->tstep]);
+        S_all.insert(S_all.end(), s->b_Utimesum, s->b_Utimesum + G);
+        U_all.insert(U_all.end(), s->b_U, s->b_U + G);
+        if (alg == 2) {
+            const std::vector<double> &r = s->row2_precalc[s->time_i1][0];
+            for (int j = 0; j < P; j++) row2.push_back(j < (int)r.size() ? r[j] : 0.0);
+            gt.push_back(s->g(s->Time[s->tstep]));
+            gtj.push_back(s->g(s->Time[s->tstep + 1]));
+        }
+    }
+    kb_off.push_back((double)kb_all.size());
+    uint64_t ns = steps;
+    w.put("tau", tauv);
+    w.put("kb_flat", kb_all); w.put("kb_off", kb_off);
+    w.put("S", {ns, (uint64_t)(K + 2), (uint64_t)(_M + 2), (uint64_t)(sN + 2)}, S_all.data());
+    w.put("U", {ns, (uint64_t)(K + 2), (uint64_t)(_M + 2), (uint64_t)(sN + 2)}, U_all.data());
+    if (alg == 2) {
+        w.put("row2", {ns, (uint64_t)P}, row2.data());
+        w.put("gt", gt); w.put("gtj", gtj);
+    }
+    delete s;
+    fclose(lg);
+    sum_alg = 0; sum_param = 1e-5; dont_clear_sum_alg1 = 0;
+    printf("wrote %s (sum_alg %d, %d steps)\n", path, alg, steps);
+}
+
 /* Wall-clock timing of the reference's column run, for the CPU baseline
  * (mode 3 BS 1 NB 3 M 3 K <n>, analytic 2, sum_alg 0, EPS 1e-15). */
 static void time_column(int kcells, double alpha, double tau, int steps)
@@ -236,6 +291,14 @@ int main(int argc, char **argv)
         std::vector<double> taus(256, 1e-3);
         snprintf(p, sizeof p, "%s/fpde_weights_long.fgv", dir);
         run_lod(p, 2, 1, 3, 3, 4, 0.3, taus, 0);
+    }
+    /* History modes: restricted summing below kb = 0.05 (about the 10 newest lags at alpha
+     * 0.8, tau 0.0025) and a 16-term series expansion. */
+    {
+        snprintf(p, sizeof p, "%s/fpde_column_alg1.fgv", dir);
+        run_sumalg(p, 1, 0.05, 32, 0.8, 0.0025, 40);
+        snprintf(p, sizeof p, "%s/fpde_column_alg2.fgv", dir);
+        run_sumalg(p, 2, 16, 32, 0.8, 0.0025, 40);
     }
     return 0;
 }

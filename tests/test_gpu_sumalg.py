@@ -1,0 +1,161 @@
+"""The reference's Sum kernel in its other history modes (fpde_sum) on the GPU:
+
+  * sum_alg 1 (restricted summing) and sum_alg 2 (series expansion) replay the reference's
+    own column runs (golden vectors of time_summing) to 1e-13 at every step; the GPU path
+    uses FMAs and kb/tau per weight, the reference separate roundings, hence not bit for bit;
+  * against the oracle on larger seeded cases: windows longer than a 256-term chunk, the
+    GPU kernel's chunk rule for several BS, no truncation and an empty window; moment counts
+    from 1 to 128, node counts that leave a partial CTA, non-finite coefficients;
+  * sum_alg 0 equals fpde_sum_snapshots; host and device buffers give the same result.
+"""
+import numpy as np
+import pytest
+
+import fgv
+import oracle
+from conftest import golden_path
+
+pytestmark = pytest.mark.gpu
+RTOL = 1e-13
+
+
+def relmax(a, b):
+    return float(np.max(np.abs(a - b)) / np.max(np.abs(b)))
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    import fpde_hpc_gb300 as fp
+    c = fp.Context(0)
+    yield c
+    c.close()
+
+
+def _interior(g):
+    sN, M, K = int(g["sN"]), int(g["M"]), int(g["K"])
+    m = np.zeros(g["U0"].shape, dtype=bool)
+    m[1:K + 1, 1:M, 1:sN] = True
+    return m.reshape(-1)
+
+
+def test_restricted_replays_reference_run(ctx):
+    import torch
+    g = fgv.load(golden_path("fpde_column_alg1"))
+    U, m = g["U"], _interior(g)
+    off = g["kb_off"].astype(int)
+    worst = 0.0
+    for n in range(1, U.shape[0]):
+        old = torch.from_numpy(np.concatenate([g["U0"][None], U[:n]]).reshape(n + 1, -1)).cuda()
+        kb = torch.from_numpy(g["kb_flat"][off[n]:off[n + 1]].copy()).cuda()
+        tau = torch.from_numpy(g["tau"][:n].copy()).cuda()
+        S = ctx.sum_alg(1, old, tau, kb=kb, sum_param=g["sum_param"]).cpu().numpy()
+        worst = max(worst, relmax(S[m], g["S"][n].reshape(-1)[m]))
+    print(f"sum_alg 1 vs the reference's run: max rel {worst:.2e}")
+    assert worst <= RTOL
+
+
+def test_series_replays_reference_run(ctx):
+    """Moments stay on the device from step to step, as the reference's Htmp buffer."""
+    import torch
+    g = fgv.load(golden_path("fpde_column_alg2"))
+    U, m = g["U"], _interior(g)
+    P = int(np.ceil(g["sum_param"]))
+    G = U.shape[1] * U.shape[2] * U.shape[3]
+    H = torch.zeros((G, P), dtype=torch.float64, device="cuda")
+    tau = torch.from_numpy(g["tau"].copy()).cuda()
+    worst = 0.0
+    for n in range(1, U.shape[0]):
+        prev = g["U0"] if n == 1 else U[n - 2]
+        old = torch.from_numpy(np.stack([prev.reshape(-1), U[n - 1].reshape(-1)])).cuda()
+        row2 = torch.from_numpy(g["row2"][n].copy()).cuda()
+        S = ctx.sum_alg(2, old, tau, sum_param=g["sum_param"], Htmp=H, row2=row2, gtj=g["gtj"][n], gt=g["gt"][n],
+                        alpha=g["alpha"], tstep=n).cpu().numpy()
+        worst = max(worst, relmax(S[m], g["S"][n].reshape(-1)[m]))
+    print(f"sum_alg 2 vs the reference's run: max rel {worst:.2e}")
+    assert worst <= RTOL
+
+
+@pytest.mark.parametrize("nt,nodes,thr,bs", [
+    (700, 3001, 0.0, 0),          # no truncation: every term (three 256-term chunks)
+    (700, 3001, 5e-4, 0),         # time_summing's rule, window of 564 terms (three chunks)
+    (700, 3001, 5e-4, 16),        # the GPU kernel's rule, BS = 16
+    (700, 3001, 5e-4, 256),
+    (700, 3001, 5e-4, 300),       # BS not a divisor of the window
+    (40, 257, 10.0, 0),           # the newest weight is already below: empty window, S = 0
+    (1, 100, 0.0, 0),             # one term
+])
+def test_restricted_vs_oracle(ctx, nt, nodes, thr, bs):
+    rng = np.random.default_rng(nt + nodes + bs)
+    old = np.cumsum(0.01 * rng.standard_normal((nt + 1, nodes)), axis=0) + 1.0
+    lag = nt - np.arange(nt)
+    kb = 1.0 / lag ** 1.2
+    tau = 1e-3 * (1.0 + 0.3 * rng.random(nt))
+    ref = oracle.sum_restricted(old, kb, tau, thr, bs)
+    S = ctx.sum_alg(1, old, tau, kb=kb, sum_param=thr, bs=bs)
+    if np.max(np.abs(ref)) == 0.0:
+        assert np.max(np.abs(S)) == 0.0
+    else:
+        assert relmax(S, ref) <= RTOL
+
+
+def test_full_mode_equals_sum_snapshots(ctx):
+    rng = np.random.default_rng(5)
+    old = rng.standard_normal((300, 1000))
+    kb = rng.random(299)
+    tau = 1e-3 + rng.random(299) * 1e-3
+    S0 = ctx.sum_alg(0, old, tau, kb=kb)
+    S1 = ctx.sum_snapshots(old, kb, tau)
+    assert relmax(S0, S1) <= RTOL
+
+
+@pytest.mark.parametrize("P,nodes", [(1, 129), (7, 1000), (16, 65536 + 77), (75, 5000), (128, 300)])
+def test_series_vs_oracle(ctx, P, nodes):
+    """Five steps carried in the moments; host buffers (the entry copies them each call)."""
+    rng = np.random.default_rng(P * 7 + nodes)
+    alpha = 0.7
+    H = np.zeros((nodes, P))
+    Href = np.zeros((nodes, P))
+    u = rng.standard_normal(nodes)
+    tau = np.full(10, 2e-3)
+    for n in range(1, 6):
+        un = u + 0.01 * rng.standard_normal(nodes)
+        gt, gtj = n * 2e-3, (n + 1) * 2e-3
+        row2 = 1.0 / (np.arange(P) + 1.0) * (1.0 - (gt / gtj) ** (np.arange(P) + 1.0))
+        ref = oracle.sum_series(u, un, Href, row2, gt, gtj, alpha, tau[n])
+        S = ctx.sum_alg(2, np.stack([u, un]), tau, sum_param=P, Htmp=H, row2=row2, gtj=gtj, gt=gt, alpha=alpha,
+                        tstep=n)
+        assert relmax(S, ref) <= RTOL, n
+        assert relmax(H, Href) <= RTOL, n
+        u = un
+
+
+def test_series_guards_and_device_buffers(ctx):
+    """A non-finite row2 entry counts as 0 (the GPU kernel's guard, also in the oracle);
+    device buffers give the same moments and sums as host buffers."""
+    import torch
+    rng = np.random.default_rng(9)
+    nodes, P = 1000, 16
+    prev, cur = rng.standard_normal(nodes), rng.standard_normal(nodes)
+    row2 = rng.random(P)
+    row2[3] = np.nan
+    row2[9] = np.inf
+    Hh = rng.standard_normal((nodes, P))
+    Href = Hh.copy()
+    tau = np.array([1e-3, 2e-3])
+    ref = oracle.sum_series(prev, cur, Href, row2, 0.01, 0.012, 0.6, tau[1])
+    assert np.isfinite(ref).all()
+    Hd = torch.from_numpy(Hh.copy()).cuda()
+    Sd = ctx.sum_alg(2, torch.from_numpy(np.stack([prev, cur])).cuda(), torch.from_numpy(tau).cuda(), sum_param=P,
+                     Htmp=Hd, row2=torch.from_numpy(row2).cuda(), gtj=0.012, gt=0.01, alpha=0.6, tstep=1)
+    Sh = ctx.sum_alg(2, np.stack([prev, cur]), tau, sum_param=P, Htmp=Hh, row2=row2, gtj=0.012, gt=0.01, alpha=0.6,
+                     tstep=1)
+    assert relmax(Sh, ref) <= RTOL and relmax(Hh, Href) <= RTOL
+    np.testing.assert_array_equal(Sd.cpu().numpy(), Sh)
+    np.testing.assert_array_equal(Hd.cpu().numpy(), Hh)
+
+
+def test_series_first_step_has_no_history(ctx):
+    H = np.ones((50, 4))
+    S = ctx.sum_alg(2, np.ones((1, 50)), np.ones(3), sum_param=4, Htmp=H, row2=np.ones(4), gtj=1.0, gt=1.0,
+                    alpha=0.5, tstep=0)
+    assert np.all(S == 0.0) and np.all(H == 1.0)

@@ -144,3 +144,53 @@ def test_do_equation_as_general_line_run(name):
     for n in range(1, steps + 1):            # compare every time level
         U, _ = oracle.line_run_general(u0, n, w, theta, A, B, Rl, src)
         assert _relmax(U, Cref[:, n]) <= RTOL, (n, _relmax(U, Cref[:, n]))
+
+
+def _interior(g):
+    sN, M, K = int(g["sN"]), int(g["M"]), int(g["K"])
+    m = np.zeros(g["U0"].shape, dtype=bool)
+    m[1:K + 1, 1:M, 1:sN] = True
+    return m.reshape(-1)
+
+
+def test_sum_restricted_matches_reference_run():
+    """sum_alg 1 (time_summing's restricted summing, threshold 0.05: the 8 newest lags) on the
+    reference's own column run: every step's history sum, bit for bit. Step 0 has no history
+    and the reference leaves its b_Utimesum unwritten, so it is skipped."""
+    g = fgv.load(golden_path("fpde_column_alg1"))
+    U, m = g["U"], _interior(g)
+    off = g["kb_off"].astype(int)
+    for n in range(1, U.shape[0]):
+        old = np.concatenate([g["U0"][None], U[:n]]).reshape(n + 1, -1)
+        S = oracle.sum_restricted(old, g["kb_flat"][off[n]:off[n + 1]], g["tau"], g["sum_param"], 0)
+        np.testing.assert_array_equal(S[m], g["S"][n].reshape(-1)[m])
+
+
+def test_sum_series_matches_reference_run():
+    """sum_alg 2 (16-term series expansion) on the reference's own column run: the moments are
+    carried from step to step from zero, every step's history sum bit for bit."""
+    g = fgv.load(golden_path("fpde_column_alg2"))
+    U, m = g["U"], _interior(g)
+    H = np.zeros((U.shape[1] * U.shape[2] * U.shape[3], int(np.ceil(g["sum_param"]))))
+    for n in range(1, U.shape[0]):
+        prev = (g["U0"] if n == 1 else U[n - 2]).reshape(-1)
+        S = oracle.sum_series(prev, U[n - 1].reshape(-1), H, g["row2"][n], g["gt"][n], g["gtj"][n], g["alpha"],
+                              g["tau"][n])
+        np.testing.assert_array_equal(S[m], g["S"][n].reshape(-1)[m])
+
+
+def test_sum_restricted_chunk_rule():
+    """The GPU kernel's chunked rule (BS terms at a time, stop after the first all-small chunk)
+    against the window it implies, on weights decreasing with lag."""
+    rng = np.random.default_rng(3)
+    nt, nodes = 50, 9
+    old = rng.standard_normal((nt + 1, nodes))
+    tau = 0.5 + rng.random(nt)
+    kb = 1.0 / (1.0 + np.arange(nt)[::-1])          # kb[t] for lag nt - t: 1, 1/2, 1/3, ...
+    thr = 1.0 / 7.5                                  # lags 1..7 are >= thr
+    def window(L):
+        return sum(kb[t] * (old[t + 1] - old[t]) / tau[t] for t in range(nt - 1, nt - 1 - L, -1))
+    np.testing.assert_allclose(oracle.sum_restricted(old, kb, tau, thr, 0), window(7), rtol=1e-14)
+    for bs, L in ((1, 8), (4, 12), (7, 14), (8, 16), (64, 50)):
+        np.testing.assert_allclose(oracle.sum_restricted(old, kb, tau, thr, bs), window(L), rtol=1e-14,
+                                   err_msg=f"bs={bs}")
