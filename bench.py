@@ -7,6 +7,10 @@ L1 history sum and a Thomas solve. Other workloads of the same operator:
   config3  distributed-order line, N=16,384, 4,096 steps, 16-node Gauss-Legendre orders
   config4  3D LOD 128^3, 1,024 steps, alpha 0.85 (history in the K pass, three Thomas passes)
   config5  ensemble of 512 columns, N log-uniform [256, 16384], alpha U[0.5, 0.95], 2,048 steps
+  sum1     the Sum kernel contract with restricted summing (sum_alg 1) over config 4's 130^3
+           grid: 1,024 stored snapshots, a threshold that keeps the 256 newest lags
+  sum2     the Sum kernel contract with the series expansion (sum_alg 2, 16 moments per point)
+           over config 4's 130^3 grid
 `value` is measured with inputs resident in HBM (CUDA events on the library's stream, the
 run replayed from a captured CUDA graph, no probes); `e2e` goes through the C ABI with host
 buffers (the *_solve_host calls: upload the initial state, solve, download the state).
@@ -42,7 +46,8 @@ def parse():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="config2", choices=["config2", "config3", "config4", "config5"])
+    ap.add_argument("--workload", default="config2",
+                    choices=["config2", "config3", "config4", "config5", "sum1", "sum2"])
     ap.add_argument("--precision", default="auto", choices=["auto", "fp64", "bf16", "f16", "bf16x3"])
     ap.add_argument("--time-steps", type=int, default=None, help="override the workload's step count")
     ap.add_argument("--nodes", type=int, default=None, help="override the workload's size")
@@ -328,7 +333,178 @@ class BatchWorkload:
         return n, n
 
 
+class SumWorkload:
+    """The reference's Sum kernel contract in its other history modes (fpde_sum) over the
+    grid of config 4 (130^3 points with ghosts, as the reference's Sum runs over the whole
+    snapshot). One bench step = `calls` consecutive time steps (one Sum call each)."""
+
+    def __init__(self, args):
+        self.alg = 1 if args.workload == "sum1" else 2
+        self.name = args.workload
+        n = args.nodes or 130
+        self.points = n ** 3
+        self.calls = 64
+        self.alpha, self.tau = 0.85, 1e-3
+        self.node_steps = self.points * self.calls
+        if self.alg == 1:
+            self.nt = args.time_steps or 1024          # stored increments at the timed steps
+            self.window = 256
+            import fpde_hpc_gb300 as fp
+            b = fp.weights_l1_lags(self.alpha, self.nt + 1)
+            kkk0 = self.tau ** (1 - self.alpha) / (1 - self.alpha)
+            lagw = kkk0 * b                                # kb of lag l = kkk0 b[l-1]
+            self.kb = np.ascontiguousarray(lagw[:self.nt][::-1])          # kb[t], t = 0..nt-1 (lag nt-t)
+            self.thr = 0.5 * (lagw[self.window - 1] + lagw[self.window])  # keeps lags 1..window
+            self.metric = (f"node-steps/s (Sum kernel, restricted summing: newest {self.window} of {self.nt} lags, "
+                           f"{n}^3 points)")
+            self.desc = (f"Sum contract sum_alg 1 over {n}^3 points (config 4's grid), {self.nt} stored snapshots, "
+                         f"L1 weights alpha {self.alpha}, tau {self.tau}, threshold keeping the newest {self.window} "
+                         f"lags (time_summing's rule), {self.calls} calls per step")
+            self.bytes_per_point = 8.0 * (self.window + 1) + 8.0
+        else:
+            self.P = 16
+            self.metric = f"node-steps/s (Sum kernel, series expansion with {self.P} moments, {n}^3 points)"
+            self.desc = (f"Sum contract sum_alg 2 over {n}^3 points (config 4's grid), {self.P} moments per point "
+                         f"(the reference's GPU default), alpha {self.alpha}, tau {self.tau}, {self.calls} calls "
+                         "per step")
+            self.bytes_per_point = 16.0 * self.P + 16.0 + 8.0
+
+    def series_inputs(self, n):
+        """row2, gt, gtj of time step n (g(t) = t): the normalised interval moments."""
+        t0, t1, t2 = (n - 1) * self.tau, n * self.tau, (n + 1) * self.tau
+        j = np.arange(self.P) + 1.0
+        return (1.0 - (t0 / t1) ** j) / j, t1, t2
+
+    def cpu_rate(self, threads):
+        os.environ["OMP_NUM_THREADS"] = str(threads)
+        oracle = _oracle()
+        rng = np.random.default_rng(1)
+        m = min(1 << 16 if self.alg == 1 else 1 << 18, self.points)
+        if self.alg == 1:
+            old = rng.standard_normal((self.nt + 1, m))
+            t0 = time.perf_counter()
+            oracle.sum_restricted(old, self.kb, np.full(self.nt, self.tau), self.thr, 0)
+            dt = time.perf_counter() - t0
+        else:
+            H = np.zeros((m, self.P))
+            prev, cur = rng.standard_normal(m), rng.standard_normal(m)
+            row2, gt, gtj = self.series_inputs(100)
+            t0 = time.perf_counter()
+            reps = 8
+            for _ in range(reps):
+                oracle.sum_series(prev, cur, H, row2, gt, gtj, self.alpha, self.tau)
+            dt = (time.perf_counter() - t0) / reps
+        return {"value": m / dt, "sample_seconds": dt,
+                "sample": f"one call over {m} of the {self.points} points (the oracle's restatement, "
+                          f"{threads} threads)"}
+
+
+def run_sum(args, wl):
+    """Our arm for the Sum-contract workloads: device-resident calls timed with CUDA events on
+    the context's stream (stream-ordered mode), and end to end as the reference drives its
+    kernel: upload the newest snapshot, one synchronous call, read S back."""
+    import torch
+    import fpde_hpc_gb300 as fp
+    rank, world, local = dist_info()
+    torch.cuda.set_device(local)
+    ctx = fp.Context(local)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    ctx.set_stream(stream.cuda_stream)
+    lib = ctx.lib
+    dev = "cuda"
+    G = wl.points
+    S = torch.empty(G, dtype=torch.float64, device=dev)
+    if wl.alg == 1:
+        old = torch.rand((wl.nt + 1, G), dtype=torch.float64, device=dev)
+        kb = torch.from_numpy(wl.kb).to(dev)
+        tau = torch.full((wl.nt,), wl.tau, dtype=torch.float64, device=dev)
+        call = lambda c, sync=False: ctx.sum_alg(1, old, tau, kb=kb, sum_param=wl.thr, out=S, sync=sync)
+    else:
+        old = torch.rand((2, G), dtype=torch.float64, device=dev)
+        H = torch.zeros((G, wl.P), dtype=torch.float64, device=dev)
+        tau = torch.full((wl.calls + 2,), wl.tau, dtype=torch.float64, device=dev)
+        ins = [wl.series_inputs(100 + c) for c in range(wl.calls)]
+        row2 = torch.from_numpy(np.stack([r for r, _, _ in ins])).to(dev)
+
+        def call(c, sync=False):
+            _, gt, gtj = ins[c]
+            return ctx.sum_alg(2, old, tau, sum_param=wl.P, Htmp=H, row2=row2[c], gtj=gtj, gt=gt, alpha=wl.alpha,
+                               tstep=c + 1, out=S, sync=sync)
+
+    def step():
+        for c in range(wl.calls):
+            call(c)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    launches0 = lib.fpde_kernel_launch_count()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    launches = lib.fpde_kernel_launch_count() - launches0
+    clk = clocks.stop()
+    value = wl.node_steps * world / (ms / 1e3)
+    per_call_ms = ms / wl.calls
+
+    # end to end: newest snapshot up (pinned), one synchronous call, S down (pinned)
+    snap_h = torch.rand(G, dtype=torch.float64).pin_memory()
+    S_h = torch.empty(G, dtype=torch.float64).pin_memory()
+    dst = old[-1]
+
+    def e2e_step():
+        for c in range(wl.calls):
+            dst.copy_(snap_h, non_blocking=True)
+            call(c, sync=True)
+            S_h.copy_(S, non_blocking=True)
+            torch.cuda.current_stream().synchronize()
+    e2e_step()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        e2e_step()
+    e2e_s = (time.perf_counter() - t0) / args.steps
+    nb = 8 * G * wl.calls
+    e2e = {"value": wl.node_steps / e2e_s, "unit": "node-steps/s", "h2d_bytes_per_step": nb,
+           "d2h_bytes_per_step": nb, "ms_per_step": e2e_s * 1e3}
+
+    peak, peak_src = measured_peaks()
+    alg_bytes = wl.bytes_per_point * G
+    gbs = alg_bytes / (per_call_ms / 1e3) / 1e9
+    kname = "k_sum_window (+ k_window_len)" if wl.alg == 1 else "k_sum_series"
+    fp64_per_point = 2 * (wl.window) + 1 if wl.alg == 1 else 2 * wl.P + 1
+    roof = {"kernel": kname, "bound": "hbm", "achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak,
+            "peak_source": peak_src, "traffic": None, "ms_per_call": per_call_ms,
+            "algorithmic_bytes_per_call": alg_bytes,
+            "fp64_ops_per_point": fp64_per_point,
+            "limiter": "fp64 pipe (GB300 issues ~1.7 FP64 lane-ops/clk/SM); see the profile"}
+    out = {"metric": wl.metric, "value": value, "unit": "node-steps/s", "n_gpus": world, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded snapshots; no dataset exists)",
+           "config": {"workload": wl.desc, "path": f"sum_alg {wl.alg}",
+                      "l2": "inputs larger than L2 (snapshots / moments of 2.2 M points, GBs)",
+                      "parallelism": f"replicas x{world}"},
+           "e2e": e2e, "gpu_launches": int(launches), "clocks": clk, "roofline": roof}
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cb = wl.cpu_rate(os.cpu_count() or 1)
+        out["cpu_baseline"] = {"value": cb["value"], "unit": "node-steps/s", "cores": os.cpu_count() or 1,
+                               "kind": "port", "sample": cb["sample"]}
+    ctx.close()
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+
+
 def make_workload(args):
+    if args.workload in ("sum1", "sum2"):
+        return SumWorkload(args)
     if args.workload in ("config2", "config3"):
         return LineWorkload(args.workload, args)
     if args.workload == "config4":
@@ -608,6 +784,8 @@ def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload in ("sum1", "sum2"):
+        run_sum(args, SumWorkload(args))
     else:
         run_ours(args)
 

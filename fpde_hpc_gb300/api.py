@@ -138,15 +138,19 @@ class Context:
         return S
 
     def sum_alg(self, sum_alg, old, tau, kb=None, sum_param=0.0, bs=0, Htmp=None, row2=None, gtj=0.0, gt=0.0,
-                alpha=0.0, tstep=0, nodes=None):
+                alpha=0.0, tstep=0, nodes=None, out=None, sync=True):
         """The reference Sum kernel in history mode sum_alg (0 full, 1 restricted, 2 series
         expansion; fpde_sum). old: (old_size, OS) time-major snapshots (the two newest for
-        sum_alg 2); Htmp: (nodes, ceil(sum_param)) moments, updated in place. Returns S."""
+        sum_alg 2); Htmp: (nodes, ceil(sum_param)) moments, updated in place. Returns S (into
+        `out` when given). With device tensors and sync=False the call is stream-ordered on the
+        context's stream and returns after launching."""
         dev = _is_dev(old)
         old = _f64(old)
         nold, OS = old.shape
         nodes = OS if nodes is None else nodes
-        if dev:
+        if out is not None:
+            S = out
+        elif dev:
             import torch
             S = torch.zeros(nodes, dtype=torch.float64, device=old.device)
         else:
@@ -162,7 +166,7 @@ class Context:
         kb = _f64(kb) if kb is not None else None
         check(self.lib.fpde_sum(self.h, sum_alg, bs, OS, nodes, _ptr(S), _ptr(old), nold, _ptr(tau), _ptr(Htmp),
                                 _ptr(row2), _ptr(kb), float(sum_param), float(gtj), float(gt), float(alpha),
-                                int(tstep), 1 if dev else 0), "fpde_sum")
+                                int(tstep), (1 if sync else 2) if dev else 0), "fpde_sum")
         return S
 
     def tridiag_solve(self, a, b, r, om, u, n_lines, N, stride_elem, stride_line, left_kind=0,

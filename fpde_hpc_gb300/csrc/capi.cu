@@ -275,8 +275,10 @@ int fpde_ctx_create(int device, fpde_ctx **out)
     cudaError_t e = cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking);
     if (e != cudaSuccess) { delete c; return set_error(FPDE_ERR_CUDA, "stream create: %s", cudaGetErrorString(e)); }
     c->stream = c->own_stream;
-    if (dev_alloc((void **)&c->d_flags, 64) || dev_alloc((void **)&c->d_barrier, 64 * 2 * sizeof(unsigned))) {
+    if (dev_alloc((void **)&c->d_flags, 64) || dev_alloc((void **)&c->d_barrier, 64 * 2 * sizeof(unsigned)) ||
+        dev_alloc((void **)&c->d_scratch, 16 * sizeof(int))) {
         dev_free(c->d_flags);
+        dev_free(c->d_barrier);
         cudaStreamDestroy(c->own_stream);
         delete c;
         return FPDE_ERR_NOMEM;
@@ -297,6 +299,7 @@ int fpde_ctx_destroy(fpde_ctx *ctx)
     while (!ctx->hists.empty()) fpde_history_destroy(*ctx->hists.begin());
     dev_free(ctx->d_flags);
     dev_free(ctx->d_barrier);
+    dev_free(ctx->d_scratch);
     cudaStreamDestroy(ctx->own_stream);
     delete ctx;
     return FPDE_OK;

@@ -64,6 +64,7 @@ struct fpde_ctx {
     cudaStream_t stream = nullptr;
     unsigned *d_flags = nullptr;       // device error flags
     unsigned *d_barrier = nullptr;     // grid barrier state (count, generation) x 64 slots
+    int *d_scratch = nullptr;          // 16 ints of per-call device scratch (one call at a time)
     std::set<fpde_hist *> hists;
     std::set<fpde_line *> lines;
     std::set<void *> extra;            // other objects registered by modules (freed by them)

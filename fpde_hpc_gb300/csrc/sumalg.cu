@@ -7,11 +7,14 @@
 //   sum_alg 2  series expansion: P moments per node updated with the newest increment, and
 //              the history sum as their dot product with the binomial series coefficients.
 //
-// k_sum_window (sum_alg 0/1): the window (terms from the newest) is the same for every node and
-// is found on the host from the weights. One thread per node; the CTA's 256 threads first turn
+// k_sum_window (sum_alg 0/1): the window (terms from the newest) is the same for every node; for
+// sum_alg 1 a one-CTA kernel finds it from the weights on the device (no host round trip). One thread per node; the CTA's 256 threads first turn
 // a chunk of 256 weights into kb/tau (one division per weight and CTA, not per node), then
-// every thread walks the chunk's terms carrying the newer snapshot in a register (one 8-byte
-// load, one subtraction and one FMA per node and term).
+// every thread walks the chunk's terms carrying the newer snapshot in a register: one 8-byte
+// load, one FP64 subtraction and one FP64 FMA per node and term. GB300 issues FP64 at about
+// two lanes per clock per SM, so the two FP64 operations per term, not HBM, bound the kernel
+// (ncu: FP64 pipe ~90% busy, DRAM ~1/3). The snapshots are close, so the difference needs FP64;
+// a float-float accumulation of the products (tried) was slower and ~10x less accurate.
 //
 // k_sum_series (sum_alg 2): 128 nodes per CTA. The CTA's moment tile (128 x P doubles,
 // node-major as the reference's Htmp[id*P + j]) is staged through shared memory with
@@ -19,6 +22,7 @@
 // product in the reference's order j = 0 .. P-1. Rows of the tile are padded to an odd
 // number of doubles so the per-node accesses are free of bank conflicts.
 #include <algorithm>
+#include <climits>
 #include <cmath>
 
 #include "common.cuh"
@@ -29,14 +33,15 @@ constexpr int SW_T = 256;         // threads (nodes) per CTA and weights per chu
 constexpr int SS_T = 128;         // nodes per CTA of k_sum_series
 constexpr int SERIES_PMAX = 128;  // most moments per node
 
-// S[id] = sum over the newest L terms (t = nt-1 .. nt-L, nt = old_size - 1) of
+// S[id] = sum over the newest L terms (L = *Ld when Ld is given, else Lh) (t = nt-1 .. nt-L, nt = old_size - 1) of
 // kb[t] (old[t+1] - old[t]) / tau[t], newest first.
 __global__ void __launch_bounds__(SW_T) k_sum_window(double *__restrict__ S, const double *__restrict__ old,
                                                      int old_size, int64_t OS, int64_t nodes,
                                                      const double *__restrict__ tau, const double *__restrict__ kb,
-                                                     int L)
+                                                     int Lh, const int *__restrict__ Ld)
 {
     __shared__ double sw[SW_T];
+    const int L = Ld ? *Ld : Lh;
     const int64_t id = (int64_t)blockIdx.x * SW_T + threadIdx.x;
     const bool in = id < nodes;
     const int nt = old_size - 1;
@@ -60,27 +65,38 @@ __global__ void __launch_bounds__(SW_T) k_sum_window(double *__restrict__ S, con
     if (in) S[id] = s;
 }
 
-// Terms the restricted rules use, counted from the newest (kb: the nt weights on the host).
+// Terms the restricted rules use, counted from the newest, into *L (one CTA):
 //   bs == 0: time_summing (:4110-4131): stop before the first |kb[t]| < thr;
 //   bs  > 0: the GPU Sum kernel (:1422-1455): whole chunks of bs terms (weights before t = 0
 //            count as 0), stopping after the first chunk whose bs weights are all below thr.
-static int restricted_terms(const double *kb, int nt, double thr, int bs)
+constexpr int WL_T = 1024;
+__global__ void __launch_bounds__(WL_T) k_window_len(const double *__restrict__ kb, int nt, double thr, int bs,
+                                                     int *__restrict__ L)
 {
+    __shared__ int first;
+    if (threadIdx.x == 0) first = INT_MAX;
+    __syncthreads();
     if (bs == 0) {
-        for (int g = 0; g < nt; ++g)
-            if (std::fabs(kb[nt - 1 - g]) < thr) return g;
-        return nt;
-    }
-    for (int m0 = 0; m0 < nt; m0 += bs) {
-        bool all_small = true;
-        for (int q = 0; q < bs && all_small; ++q) {
-            const int t = nt - 1 - (m0 + q);
-            const double kv = t >= 0 ? kb[t] : 0.0;
-            if (!(std::fabs(kv) < thr)) all_small = false;
+        for (int g = threadIdx.x; g < nt; g += WL_T)
+            if (fabs(kb[nt - 1 - g]) < thr) atomicMin(&first, g);
+    } else {
+        const int nchunks = (nt + bs - 1) / bs;
+        for (int m = threadIdx.x; m < nchunks; m += WL_T) {
+            bool all_small = true;
+            for (int q = 0; q < bs && all_small; ++q) {
+                const int t = nt - 1 - (m * bs + q);
+                const double kv = t >= 0 ? kb[t] : 0.0;
+                if (!(fabs(kv) < thr)) all_small = false;
+            }
+            if (all_small) atomicMin(&first, m);
         }
-        if (all_small) return std::min(nt, m0 + bs);
     }
-    return nt;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int n = nt;
+        if (first != INT_MAX) n = bs == 0 ? first : (int)min((long long)nt, ((long long)first + 1) * bs);
+        *L = n;
+    }
 }
 
 struct SeriesCoef {
@@ -141,6 +157,7 @@ int fpde_sum(fpde_ctx *ctx, int sum_alg, int bs, int64_t OS, int64_t nodes, doub
     int rc = ctx_enter(ctx);
     if (rc) return rc;
     FPDE_CHECK_ARG(sum_alg >= 0 && sum_alg <= 2, "sum_alg must be 0, 1 or 2");
+    FPDE_CHECK_ARG(on_device >= 0 && on_device <= 2, "on_device must be 0, 1 or 2");
     FPDE_CHECK_ARG(S && old && old_size >= 1 && nodes > 0 && OS >= nodes, "bad arguments");
     FPDE_CHECK_ARG(sum_alg != 1 || bs >= 0, "bs must be >= 0");
     const int P = sum_alg == 2 ? (int)std::ceil(sum_param) : 0;
@@ -212,25 +229,22 @@ int fpde_sum(fpde_ctx *ctx, int sum_alg, int bs, int64_t OS, int64_t nodes, doub
             }
         }
     } else {
-        int L = nt;
-        if (sum_alg == 1 && nt > 0) {                    // the window is the same for every node
-            std::vector<double> hkb(nt);
-            if (on_device) {
-                e = cudaMemcpyAsync(hkb.data(), kb_3_cache, (size_t)nt * sizeof(double), cudaMemcpyDeviceToHost, st);
-                if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-            } else {
-                std::copy(kb_3_cache, kb_3_cache + nt, hkb.begin());
-            }
-            if (e == cudaSuccess) L = restricted_terms(hkb.data(), nt, sum_param, bs);
+        // the window is the same for every node; sum_alg 1 finds it on the device
+        const int *Ld = nullptr;
+        if (sum_alg == 1 && nt > 0) {
+            k_window_len<<<1, WL_T, 0, st>>>(dkb, nt, sum_param, bs, ctx->d_scratch);
+            e = cudaGetLastError();
+            Ld = ctx->d_scratch;
+            launched = 1;
         }
         if (e == cudaSuccess) {
             k_sum_window<<<(unsigned)((nodes + SW_T - 1) / SW_T), SW_T, 0, st>>>(dS, dold, old_size, OS, nodes, dtau,
-                                                                                dkb, L);
+                                                                                dkb, nt, Ld);
             e = cudaGetLastError();
-            launched = 1;
+            launched += 1;
         }
     }
-    if (e == cudaSuccess && launched) count_launches(1);
+    if (e == cudaSuccess && launched) count_launches(launched);
     if (!on_device) {
         cudaMemcpyAsync(S, dS, (size_t)nodes * sizeof(double), cudaMemcpyDeviceToHost, st);
         if (sum_alg == 2) cudaMemcpyAsync(Htmp, dH, (size_t)nodes * P * sizeof(double), cudaMemcpyDeviceToHost, st);
@@ -238,7 +252,7 @@ int fpde_sum(fpde_ctx *ctx, int sum_alg, int bs, int64_t OS, int64_t nodes, doub
         release();
     }
     if (e != cudaSuccess) return set_error(FPDE_ERR_CUDA, "Sum (sum_alg %d) launch: %s", sum_alg, cudaGetErrorString(e));
-    FPDE_CUDA(cudaStreamSynchronize(st));
+    if (on_device != 2) FPDE_CUDA(cudaStreamSynchronize(st));
     return FPDE_OK;
 }
 

@@ -162,7 +162,7 @@ int fpde_sum_snapshots(fpde_ctx *ctx, double *S, const double *old, int old_size
  * kb_3_cache, sum_param, gtj, gt, alpha, tstep in the reference's order, args set :1851-1868;
  * CPU form time_summing :4108-4151). Snapshots are time-major, old[t*OS + id], id < nodes.
  *   sum_alg 0: S[id] = sum_{t=old_size-2..0} kb_3_cache[t]*(old[t+1]-old[t])/tau[t]
- *              (fpde_sum_snapshots).
+ *              (as fpde_sum_snapshots, with kb/tau formed once per weight and FMAs).
  *   sum_alg 1: restricted summing, the same terms from the newest down while the weight stays
  *              at or above sum_param:
  *                bs == 0: time_summing's rule (:4117-4131): stop before the first term with
@@ -179,9 +179,11 @@ int fpde_sum_snapshots(fpde_ctx *ctx, double *S, const double *old, int old_size
  *                v_0 = gtj^-alpha,  v_j = v_{j-1} * (alpha + j - 1) / (j * gtj),
  *              with the GPU kernel's guards (a non-finite d, row2_precalc[j], power or v_j
  *              counts as 0). gt, gtj: g(t) at the step's two ends.
- * Arrays per on_device: old (old_size rows; 2 for sum_alg 2), tau (old_size-1 values, or at
- * least tstep+1 for sum_alg 2), kb_3_cache (old_size-1), Htmp (nodes*P), row2_precalc (P), S
- * (nodes). Unused pointers may be NULL. Synchronous, like the reference's launch. */
+ * Arrays: old (old_size rows; 2 for sum_alg 2), tau (old_size-1 values, or at least tstep+1 for
+ * sum_alg 2), kb_3_cache (old_size-1), Htmp (nodes*P), row2_precalc (P), S (nodes); unused
+ * pointers may be NULL. on_device: 0 host arrays, 1 device arrays (both synchronous, like the
+ * reference's launch), 2 device arrays, stream-ordered on the context's stream: the call
+ * returns after launching (launch errors are reported; nothing is read back). */
 int fpde_sum(fpde_ctx *ctx, int sum_alg, int bs, int64_t OS, int64_t nodes, double *S, const double *old,
              int old_size, const double *tau, double *Htmp, const double *row2_precalc,
              const double *kb_3_cache, double sum_param, double gtj, double gt, double alpha, int tstep,

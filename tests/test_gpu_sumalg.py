@@ -2,7 +2,10 @@
 
   * sum_alg 1 (restricted summing) and sum_alg 2 (series expansion) replay the reference's
     own column runs (golden vectors of time_summing) to 1e-13 at every step; the GPU path
-    uses FMAs and kb/tau per weight, the reference separate roundings, hence not bit for bit;
+    forms kb/tau once per weight and sums with FMAs, the reference with separate roundings,
+    hence not bit for bit;
+  * windowed sums are checked per node against 1e-13 x the sum of the terms' magnitudes (the
+    scale of any summation-order difference: FP64's own sequential bound is n 2^-53 of it);
   * against the oracle on larger seeded cases: windows longer than a 256-term chunk, the
     GPU kernel's chunk rule for several BS, no truncation and an empty window; moment counts
     from 1 to 128, node counts that leave a partial CTA, non-finite coefficients;
@@ -91,11 +94,16 @@ def test_restricted_vs_oracle(ctx, nt, nodes, thr, bs):
     kb = 1.0 / lag ** 1.2
     tau = 1e-3 * (1.0 + 0.3 * rng.random(nt))
     ref = oracle.sum_restricted(old, kb, tau, thr, bs)
+    # the same window over |increments|: the sum of the terms' magnitudes per node
+    mag = oracle.sum_restricted(np.concatenate([[np.zeros(nodes)], np.cumsum(np.abs(np.diff(old, axis=0)), axis=0)]),
+                                kb, tau, thr, bs)
     S = ctx.sum_alg(1, old, tau, kb=kb, sum_param=thr, bs=bs)
     if np.max(np.abs(ref)) == 0.0:
         assert np.max(np.abs(S)) == 0.0
     else:
-        assert relmax(S, ref) <= RTOL
+        err = np.abs(S - ref)
+        print(f"nt={nt} thr={thr} bs={bs}: max err / sum|terms| {np.max(err / np.maximum(mag, 1e-300)):.2e}")
+        assert np.all(err <= RTOL * mag)
 
 
 def test_full_mode_equals_sum_snapshots(ctx):
@@ -159,3 +167,19 @@ def test_series_first_step_has_no_history(ctx):
     S = ctx.sum_alg(2, np.ones((1, 50)), np.ones(3), sum_param=4, Htmp=H, row2=np.ones(4), gtj=1.0, gt=1.0,
                     alpha=0.5, tstep=0)
     assert np.all(S == 0.0) and np.all(H == 1.0)
+
+
+def test_stream_ordered_mode(ctx):
+    """on_device = 2 returns after launching; after the context's stream drains the results equal
+    the synchronous call's (restricted window found on the device in both)."""
+    import torch
+    rng = np.random.default_rng(12)
+    nt, nodes = 600, 4000
+    old = torch.from_numpy(rng.standard_normal((nt + 1, nodes))).cuda()
+    kb = torch.from_numpy(1.0 / (nt - np.arange(nt)) ** 1.1).cuda()
+    tau = torch.from_numpy(1e-3 * (1 + rng.random(nt))).cuda()
+    S1 = ctx.sum_alg(1, old, tau, kb=kb, sum_param=1e-3, bs=32)
+    S2 = torch.empty_like(S1)
+    ctx.sum_alg(1, old, tau, kb=kb, sum_param=1e-3, bs=32, out=S2, sync=False)
+    ctx.synchronize()
+    assert torch.equal(S1, S2)
