@@ -169,6 +169,23 @@ class Context:
                                 int(tstep), (1 if sync else 2) if dev else 0), "fpde_sum")
         return S
 
+    def weights_g(self, p, alpha, time, n0, n1, out=None, sync=True):
+        """Generalized-kernel L1 weights (g(t) = t^p) of steps n0..n1 (fpde_weights_g): row
+        n - n0 holds kb_0..kb_{n-1} and kkk0 at column n. time: n1 + 2 points (host array or
+        device tensor); returns a (n1 - n0 + 1, n1 + 1) array (device tensor for device time)."""
+        dev = _is_dev(time)
+        time = _f64(time)
+        rows, ld = n1 - n0 + 1, n1 + 1
+        if out is None:
+            if dev:
+                import torch
+                out = torch.zeros((rows, ld), dtype=torch.float64, device=time.device)
+            else:
+                out = np.zeros((rows, ld))
+        check(self.lib.fpde_weights_g(self.h, float(p), float(alpha), _ptr(time), int(n0), int(n1), _ptr(out),
+                                      ld, (1 if sync else 2) if dev else 0), "fpde_weights_g")
+        return out
+
     def tridiag_solve(self, a, b, r, om, u, n_lines, N, stride_elem, stride_line, left_kind=0,
                       left_val=None, right_kind=0, right_val=None, dLN=0.0):
         dev = _is_dev(u)

@@ -99,6 +99,20 @@ int fpde_weights_l1(double alpha, const double *time, int n, double *kb, double 
  * cancellation-free (so kb[t] of step n = tau^{1-alpha}/(1-alpha) * b[n-t]). Host. */
 int fpde_weights_l1_lags(double alpha, int n, double *b);
 
+/* Generalized-kernel L1 weights on the device, any time points (kb :2167-2301 with the
+ * generalized Caputo kernel g(t) = t^p of func_in_kernel, g :1889-1930: 0 -> p = 1,
+ * 1 -> p = 0.5, 2 -> p = 2, 3 -> p = func_power; variable steps as varT). For every step n in
+ * [n0, n1], with T = time[n+1]:
+ *   out[(n-n0)*ld + t] = int_{time[t]}^{time[t+1]} (T^p - s^p)^{-alpha} ds,  t = 0..n-1 (kb_3_cache)
+ *   out[(n-n0)*ld + n] = the same over [time[n], T]                       (kkk0)
+ * evaluated in FP64 by quadrature (the reference sums truncated series, which converge
+ * slowly on intervals that start at t = 0 when p is not 1). Entries past t = n are left
+ * unchanged. time: n1 + 2 strictly increasing points with time[0] = 0, ld >= n1 + 1,
+ * 0 < p, 0 <= alpha <= 1 (alpha = 1: kb = 0, kkk0 = 1 as the reference). on_device: 0 host
+ * arrays, 1 device arrays, 2 device arrays stream-ordered (returns after launching). */
+int fpde_weights_g(fpde_ctx *ctx, double p, double alpha, const double *time, int n0, int n1, double *out,
+                   int64_t ld, int on_device);
+
 /* Gamma function (FP64, host). Used for Da = 1/Gamma(1-alpha) (fpde_hpc_1d.cpp:3598-3605)
  * and the distributed-order normalisers Gamma(2-alpha) (fr_do.cpp:337-341). */
 int fpde_gamma(double x, double *out);

@@ -35,6 +35,109 @@ void fo_l1_weights(double alpha, const double *time, int n, double *kb, double *
     if (kkk0) *kkk0 = l1_interval_weight(alpha, 0.0, T1 - time[n]);
 }
 
+/* Quadrature rules of fo_weights_g: double-exponential nodes t = k/8, |k| <= 28, mapped to
+ * (0, 1) by u = 1/(1 + e^{-pi sinh t}) (v = 1 - u formed directly), and 16-point
+ * Gauss-Legendre on (0, 1) by Newton iteration on P_16. */
+#define WG_DE 57
+#define WG_GL 16
+static double wg_u[WG_DE], wg_v[WG_DE], wg_w[WG_DE], wg_x[WG_GL], wg_gw[WG_GL];
+static int wg_ready = 0;
+
+static void wg_init(void)
+{
+    if (wg_ready) return;
+    const double pi = 3.14159265358979323846;
+    for (int k = 0; k < WG_DE; k++) {
+        double t = (k - 28) / 8.0;
+        double e = exp(pi * sinh(t));
+        wg_u[k] = e / (1.0 + e);
+        wg_v[k] = 1.0 / (1.0 + e);
+        wg_w[k] = (pi / 8.0) * cosh(t) * wg_u[k] * wg_v[k];
+    }
+    for (int i = 0; i < WG_GL; i++) {
+        double x = cos(pi * (i + 0.75) / (WG_GL + 0.5)), dp = 1.0;
+        for (int it = 0; it < 100; it++) {
+            double p0 = 1.0, p1 = x;
+            for (int k = 2; k <= WG_GL; k++) {
+                double p2 = ((2.0 * k - 1.0) * x * p1 - (k - 1.0) * p0) / k;
+                p0 = p1;
+                p1 = p2;
+            }
+            dp = WG_GL * (x * p1 - p0) / (x * x - 1.0);
+            double dx = p1 / dp;
+            x -= dx;
+            if (fabs(dx) < 1e-17) break;
+        }
+        {
+            double p0 = 1.0, p1 = x;
+            for (int k = 2; k <= WG_GL; k++) {
+                double p2 = ((2.0 * k - 1.0) * x * p1 - (k - 1.0) * p0) / k;
+                p0 = p1;
+                p1 = p2;
+            }
+            dp = WG_GL * (x * p1 - p0) / (x * x - 1.0);
+        }
+        wg_x[i] = 0.5 * (x + 1.0);
+        wg_gw[i] = 1.0 / ((1.0 - x * x) * dp * dp);   /* 2/((1-x^2)P'^2) on (-1,1), halved */
+    }
+    wg_ready = 1;
+}
+
+/* T^p - s^p with delta = T - s (both given; no cancellation for small delta) */
+static double wg_gdiff(double delta, double s, double T, double p, double Tp)
+{
+    if (p == 1.0) return delta;
+    if (delta < 0.5 * T) return -Tp * expm1(p * log1p(-delta / T));
+    return Tp - pow(s, p);
+}
+
+static double wg_interval(double s0, double s1, double T, double p, double alpha)
+{
+    const double wdt = s1 - s0, d1 = T - s1, Tp = pow(T, p);
+    double sum = 0.0;
+    if (d1 == 0.0) {                                   /* newest: delta^-alpha on [0, wdt/16] */
+        const double hw = wdt / 16.0, q = 1.0 / (1.0 - alpha), R0 = pow(p * pow(T, p - 1.0), -alpha);
+        double a = 0.0, b = 0.0;
+        for (int k = 0; k < WG_DE; k++) {
+            double delta = hw * pow(wg_u[k], q);
+            double R = delta > 0.0 ? pow(wg_gdiff(delta, T - delta, T, p, Tp) / delta, -alpha) : R0;
+            a += wg_w[k] * R;
+        }
+        const double rest = wdt - hw;
+        for (int k = 0; k < WG_DE; k++) {
+            double delta = hw + rest * wg_u[k], s = s0 + rest * wg_v[k];
+            b += wg_w[k] * pow(wg_gdiff(delta, s, T, p, Tp), -alpha);
+        }
+        return pow(hw, 1.0 - alpha) / (1.0 - alpha) * a + rest * b;
+    }
+    const int smooth0 = p >= 1.0 && p == floor(p);
+    if (d1 < 4.0 * wdt || (!smooth0 && s0 < 4.0 * wdt)) {
+        for (int k = 0; k < WG_DE; k++) {
+            double delta = d1 + wdt * wg_u[k], s = s0 + wdt * wg_v[k];
+            sum += wg_w[k] * pow(wg_gdiff(delta, s, T, p, Tp), -alpha);
+        }
+        return wdt * sum;
+    }
+    for (int i = 0; i < WG_GL; i++) {
+        double s = s0 + wdt * wg_x[i], delta = d1 + wdt * (1.0 - wg_x[i]);
+        sum += wg_gw[i] * pow(wg_gdiff(delta, s, T, p, Tp), -alpha);
+    }
+    return wdt * sum;
+}
+
+void fo_weights_g(double p, double alpha, const double *time, int n, double *kb, double *kkk0)
+{
+    wg_init();
+    const double T = time[n + 1];
+    if (alpha == 1.0) {                                /* kb :2169-2175 */
+        for (int t = 0; t < n; t++) kb[t] = 0.0;
+        if (kkk0) *kkk0 = 1.0;
+        return;
+    }
+    for (int t = 0; t < n; t++) kb[t] = wg_interval(time[t], time[t + 1], T, p, alpha);
+    if (kkk0) *kkk0 = wg_interval(time[n], T, T, p, alpha);
+}
+
 /* ------------------------------------------------------------ history sum */
 
 void fo_l1_sum(const double *D, int64_t P, int n, const double *kb, const double *tau,

@@ -47,6 +47,17 @@ void fo_l1_sum_snapshots(const double *old, int64_t OS, int nold, const double *
 void fo_sum_restricted(const double *old, int64_t OS, int nold, const double *kb, const double *tau,
                        double thr, int bs, int64_t nodes, double *S);
 
+/* Generalized-kernel L1 weights (kb :2167-2301 with g(t) = t^p, g :1889-1930: func_in_kernel
+ * 0 -> p = 1, 1 -> 0.5, 2 -> 2, 3 -> func_power): for step n with T = time[n+1],
+ *   kb[t] = int_{time[t]}^{time[t+1]} (T^p - s^p)^{-alpha} ds,  t = 0..n-1,  kkk0 = the same over
+ *   [time[n], T]. The reference sums truncated Taylor/binomial series (_kb_row :1933,
+ *   _kb_row2 :2000); this evaluates the integral by quadrature: 16-point Gauss-Legendre on
+ *   intervals at least 4 widths from both singular points (s = T, and s = 0 when p is not a
+ *   positive integer), the double-exponential rule elsewhere, and on the newest interval the
+ *   factor delta^-alpha (delta = T - s) integrated analytically on its last 1/16 (delta =
+ *   h y^(1/(1-alpha))). T^p - s^p is formed as -T^p expm1(p log1p(-delta/T)) for small delta. */
+void fo_weights_g(double p, double alpha, const double *time, int n, double *kb, double *kkk0);
+
 /* Series expansion (sum_alg 2, time_summing :4137-4151 with _kb_row2_fixed_coefs
  * :1159-1180; the GPU kernel's finiteness guards :1459-1469): P moments per node in
  * H[i*P + j], updated with d = cur[i] - prev[i]:

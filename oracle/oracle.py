@@ -36,6 +36,7 @@ def load():
     lib.fo_l1_weights.argtypes = [d, _dp, i32, _dp, C.POINTER(d)]
     lib.fo_l1_sum.argtypes = [_dp, i64, i32, _dp, _dp, i64, i64, _dp]
     lib.fo_l1_sum_snapshots.argtypes = [_dp, i64, i32, _dp, _dp, i64, _dp]
+    lib.fo_weights_g.argtypes = [d, d, _dp, i32, _dp, C.POINTER(d)]
     lib.fo_sum_restricted.argtypes = [_dp, i64, i32, _dp, _dp, d, i32, i64, _dp]
     lib.fo_sum_series.argtypes = [_dp, _dp, i64, _dp, i32, _dp, d, d, d, d, _dp]
     lib.fo_thomas_line.argtypes = [i32, _dp, _dp, _dp, _dp, i32, d, i32, d, d, _dp]
@@ -101,6 +102,15 @@ def l1_sum_snapshots(old, kb, tau):
     lib.fo_l1_sum_snapshots(old.reshape(-1), OS, nold, np.ascontiguousarray(kb, dtype=np.float64),
                             np.ascontiguousarray(tau, dtype=np.float64), OS, S)
     return S
+
+
+def weights_g(p, alpha, time, n):
+    """kb (n values) and kkk0 of step n for g(t) = t^p (fo_weights_g)."""
+    lib = load()
+    kb = np.zeros(max(n, 1))
+    k0 = C.c_double()
+    lib.fo_weights_g(p, alpha, np.ascontiguousarray(time, dtype=np.float64), n, kb, C.byref(k0))
+    return kb[:n], k0.value
 
 
 def sum_restricted(old, kb, tau, thr, bs=0):

@@ -12,6 +12,8 @@
  *     hard-coded analytic problems: the tridiagonal coefficients A_/B/R of every line of
  *     every pass (:3095-3142), the source Rp of the K pass (:2724) and the Dirichlet
  *     boundary values bc0/bcN of every line (:4491-4583).
+ * Weights-only scenarios also cover the generalized Caputo kernels (func_in_kernel 1-3,
+ * g(t) = sqrt(t), t^2, t^p; g :1889-1930) with uniform and variable steps.
  * Two more scenarios run the column with the reference's other history modes
  * (time_summing :4108-4151): sum_alg 1 (restricted summing) and sum_alg 2 (series
  * expansion, with the per-step coefficient row row2_precalc[time_i1][0] and g(t) at the
@@ -291,6 +293,24 @@ int main(int argc, char **argv)
         std::vector<double> taus(256, 1e-3);
         snprintf(p, sizeof p, "%s/fpde_weights_long.fgv", dir);
         run_lod(p, 2, 1, 3, 3, 4, 0.3, taus, 0);
+    }
+    /* Weights only, generalized kernels g(t) = sqrt(t), t^2, t^1.5 (func_in_kernel 1, 2, 3),
+     * uniform and variable steps. */
+    {
+        const int fk[3] = {1, 2, 3};
+        const double fpw[3] = {0.5, 2.0, 1.5};
+        for (int q = 0; q < 3; q++) {
+            func_in_kernel = fk[q];
+            func_power = fpw[q];
+            std::vector<double> tu(40, 2e-3), tv;
+            for (int n = 0; n < 40; n++) tv.push_back(2e-3 * (1.0 + 0.5 * sin(0.9 * n)));
+            snprintf(p, sizeof p, "%s/fpde_weights_fk%d.fgv", dir, fk[q]);
+            run_lod(p, 2, 1, 3, 3, 4, 0.6, tu, 0);
+            snprintf(p, sizeof p, "%s/fpde_weights_fk%d_vartau.fgv", dir, fk[q]);
+            run_lod(p, 2, 1, 3, 3, 4, 0.6, tv, 0);
+        }
+        func_in_kernel = 0;
+        func_power = 0.6;
     }
     /* History modes: restricted summing below kb = 0.05 (about the 10 newest lags at alpha
      * 0.8, tau 0.0025) and a 16-term series expansion. */
