@@ -11,6 +11,8 @@ L1 history sum and a Thomas solve. Other workloads of the same operator:
            grid: 1,024 stored snapshots, a threshold that keeps the 256 newest lags
   sum2     the Sum kernel contract with the series expansion (sum_alg 2, 16 moments per point)
            over config 4's 130^3 grid
+  weights  every L1 weight row of a 4,096-step run with the generalized kernel g(t) = t^1.5 and
+           variable steps (fpde_weights_g: 8.4 M weights per call)
 `value` is measured with inputs resident in HBM (CUDA events on the library's stream, the
 run replayed from a captured CUDA graph, no probes); `e2e` goes through the C ABI with host
 buffers (the *_solve_host calls: upload the initial state, solve, download the state).
@@ -47,7 +49,7 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="config2",
-                    choices=["config2", "config3", "config4", "config5", "sum1", "sum2"])
+                    choices=["config2", "config3", "config4", "config5", "sum1", "sum2", "weights"])
     ap.add_argument("--precision", default="auto", choices=["auto", "fp64", "bf16", "f16", "bf16x3"])
     ap.add_argument("--time-steps", type=int, default=None, help="override the workload's step count")
     ap.add_argument("--nodes", type=int, default=None, help="override the workload's size")
@@ -502,7 +504,98 @@ def run_sum(args, wl):
         print(json.dumps(out), flush=True)
 
 
+class WeightsWorkload:
+    """All weight rows of a run with the generalized kernel g(t) = t^p and variable steps."""
+
+    def __init__(self, args):
+        self.name = "weights"
+        self.steps = args.time_steps or 4096
+        self.p, self.alpha = 1.5, 0.85
+        rng = np.random.default_rng(7)
+        tau = 1e-3 * (1.0 + 0.5 * np.sin(0.7 * np.arange(self.steps)) + 0.1 * rng.random(self.steps))
+        self.time = np.concatenate([[0.0], np.cumsum(tau)])
+        self.node_steps = self.steps * (self.steps + 1) // 2          # weights per call
+        self.metric = f"weights/s (generalized L1 kernel g(t)=t^{self.p}, variable steps, all rows of {self.steps} steps)"
+        self.desc = (f"fpde_weights_g rows 0..{self.steps - 1}: g(t) = t^{self.p}, alpha {self.alpha}, tau 1e-3 x "
+                     "(1 + 0.5 sin(0.7 n) + 0.1 U[0,1)) (seed 7), one call per step")
+
+    def cpu_rate(self, threads, rows=24):
+        os.environ["OMP_NUM_THREADS"] = str(threads)
+        oracle = _oracle()
+        ns = list(range(self.steps - rows, self.steps))
+        t0 = time.perf_counter()
+        for n in ns:
+            oracle.weights_g(self.p, self.alpha, self.time, n)
+        dt = time.perf_counter() - t0
+        cnt = sum(n + 1 for n in ns)
+        return {"value": cnt / dt, "sample_seconds": dt,
+                "sample": f"the last {rows} rows ({cnt} weights) by the oracle's quadrature, {threads} threads"}
+
+
+def run_weights(args, wl):
+    import torch
+    import fpde_hpc_gb300 as fp
+    rank, world, local = dist_info()
+    torch.cuda.set_device(local)
+    ctx = fp.Context(local)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    ctx.set_stream(stream.cuda_stream)
+    lib = ctx.lib
+    S = wl.steps
+    tdev = torch.from_numpy(wl.time).cuda()
+    out = torch.zeros((S, S), dtype=torch.float64, device="cuda")
+    call = lambda: ctx.weights_g(wl.p, wl.alpha, tdev, 0, S - 1, out=out, sync=False)
+    for _ in range(args.warmup):
+        call()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    launches0 = lib.fpde_kernel_launch_count()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        call()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    launches = lib.fpde_kernel_launch_count() - launches0
+    clk = clocks.stop()
+    value = wl.node_steps * world / (ms / 1e3)
+    host = np.zeros((S, S))
+    ctx.weights_g(wl.p, wl.alpha, wl.time, 0, S - 1, out=host)       # end to end: host time points and rows
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        ctx.weights_g(wl.p, wl.alpha, wl.time, 0, S - 1, out=host)
+    e2e_s = (time.perf_counter() - t0) / args.steps
+    peak, peak_src = measured_peaks()
+    gbs = 8.0 * wl.node_steps / (ms / 1e3) / 1e9
+    out_j = {"metric": wl.metric, "value": value, "unit": "weights/s", "n_gpus": world, "steps": args.steps,
+             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+             "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded time steps)",
+             "config": {"workload": wl.desc, "path": "fpde_weights_g",
+                        "l2": "output rows (134 MB) exceed L2; every call recomputes them",
+                        "parallelism": f"replicas x{world}"},
+             "e2e": {"value": wl.node_steps / e2e_s, "unit": "weights/s", "h2d_bytes_per_step": 8 * (S + 1),
+                     "d2h_bytes_per_step": 8 * S * S, "ms_per_step": e2e_s * 1e3},
+             "gpu_launches": int(launches), "clocks": clk,
+             "roofline": {"kernel": "k_weights_g", "bound": "hbm", "achieved": gbs, "peak": peak, "unit": "GB/s",
+                          "frac": gbs / peak, "peak_source": peak_src, "traffic": None,
+                          "limiter": "FP64 transcendentals (pow/expm1/log1p per quadrature node), not HBM",
+                          "note": "achieved = 8 B written per weight / kernel time"}}
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cb = wl.cpu_rate(os.cpu_count() or 1)
+        out_j["cpu_baseline"] = {"value": cb["value"], "unit": "weights/s", "cores": os.cpu_count() or 1,
+                                 "kind": "port", "sample": cb["sample"]}
+    ctx.close()
+    if rank == 0:
+        print(json.dumps(out_j), flush=True)
+
+
 def make_workload(args):
+    if args.workload == "weights":
+        return WeightsWorkload(args)
     if args.workload in ("sum1", "sum2"):
         return SumWorkload(args)
     if args.workload in ("config2", "config3"):
@@ -526,13 +619,14 @@ def run_reference(args):
         if it >= args.warmup:
             vals.append(r)
     v = float(np.median([r["value"] for r in vals]))
-    out = {"impl": "reference", "metric": wl.metric, "value": v, "unit": "node-steps/s", "n_gpus": args.gpus,
+    unit = "weights/s" if isinstance(wl, WeightsWorkload) else "node-steps/s"
+    out = {"impl": "reference", "metric": wl.metric, "value": v, "unit": unit, "n_gpus": args.gpus,
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": wl.node_steps / v * 1e3,
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
            "config": {"workload": wl.desc},
-           "cpu_baseline": {"value": v, "unit": "node-steps/s", "cores": threads, "kind": "port",
+           "cpu_baseline": {"value": v, "unit": unit, "cores": threads, "kind": "port",
                             "sample": vals[0]["sample"]},
-           "e2e": {"value": v, "unit": "node-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+           "e2e": {"value": v, "unit": unit, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out), flush=True)
 
 
@@ -786,6 +880,8 @@ def main():
         run_reference(args)
     elif args.workload in ("sum1", "sum2"):
         run_sum(args, SumWorkload(args))
+    elif args.workload == "weights":
+        run_weights(args, WeightsWorkload(args))
     else:
         run_ours(args)
 

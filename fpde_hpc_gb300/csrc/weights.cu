@@ -7,8 +7,9 @@
 // step needs a fresh row. The reference evaluates each weight by truncated series
 // (_kb_row :1933, _kb_row2 :2000) on the host, one at a time under an OpenMP critical
 // section; here one thread evaluates one weight by quadrature in FP64:
-//   - 16-point Gauss-Legendre when the interval lies at least 4 widths from both points where
-//     the integrand is not smooth (s = T, and s = 0 when p is not a positive integer);
+//   - Gauss-Legendre when the interval lies at least 4 widths from both points where the
+//     integrand is not smooth (s = T, and s = 0 when p is not a positive integer): 16 points,
+//     8 beyond 32 widths (the error falls like rho^-2m, rho ~ 4 x the distance in widths);
 //   - the double-exponential rule (nodes k/8, |k| <= 28) otherwise: it absorbs endpoint
 //     singularities of the derivatives;
 //   - on the newest interval the factor delta^-alpha (delta = T - s) is integrated
@@ -24,10 +25,12 @@ namespace fpde {
 
 constexpr int WG_DE = 57;
 constexpr int WG_GL = 16;
+constexpr int WG_GL8 = 8;
 
 struct WeightRule {
     double u[WG_DE], v[WG_DE], w[WG_DE];   // double-exponential: u in (0,1), v = 1 - u, weights
-    double x[WG_GL], gw[WG_GL];            // Gauss-Legendre on (0,1)
+    double x[WG_GL], gw[WG_GL];            // Gauss-Legendre on (0,1), 16 points
+    double x8[WG_GL8], gw8[WG_GL8];        // and 8 points
 };
 
 __device__ __forceinline__ double wg_gdiff(double delta, double s, double T, double p, double Tp)
@@ -61,9 +64,16 @@ __device__ double wg_interval(const WeightRule &r, double s0, double s1, double 
         }
         return wdt * sum;
     }
-    for (int i = 0; i < WG_GL; ++i) {
-        const double s = s0 + wdt * r.x[i], delta = d1 + wdt * (1.0 - r.x[i]);
-        sum += r.gw[i] * pow(wg_gdiff(delta, s, T, p, Tp), -alpha);
+    if (d1 < 32.0 * wdt || (!smooth0 && s0 < 32.0 * wdt)) {
+        for (int i = 0; i < WG_GL; ++i) {
+            const double s = s0 + wdt * r.x[i], delta = d1 + wdt * (1.0 - r.x[i]);
+            sum += r.gw[i] * pow(wg_gdiff(delta, s, T, p, Tp), -alpha);
+        }
+        return wdt * sum;
+    }
+    for (int i = 0; i < WG_GL8; ++i) {
+        const double s = s0 + wdt * r.x8[i], delta = d1 + wdt * (1.0 - r.x8[i]);
+        sum += r.gw8[i] * pow(wg_gdiff(delta, s, T, p, Tp), -alpha);
     }
     return wdt * sum;
 }
@@ -86,6 +96,33 @@ __global__ void __launch_bounds__(256) k_weights_g(const double *__restrict__ ti
     out[(int64_t)blockIdx.y * ld + t] = v;
 }
 
+// m-point Gauss-Legendre nodes and weights on (0, 1): Newton on P_m from the usual guesses.
+static void gauss_legendre(int m, double *x01, double *w01)
+{
+    const double pi = 3.14159265358979323846;
+    for (int i = 0; i < m; ++i) {
+        double x = std::cos(pi * (i + 0.75) / (m + 0.5)), dp = 1.0;
+        auto legendre = [m](double z, double &d) {
+            double p0 = 1.0, p1 = z;
+            for (int k = 2; k <= m; ++k) {
+                const double p2 = ((2.0 * k - 1.0) * z * p1 - (k - 1.0) * p0) / k;
+                p0 = p1;
+                p1 = p2;
+            }
+            d = m * (z * p1 - p0) / (z * z - 1.0);
+            return p1;
+        };
+        for (int it = 0; it < 100; ++it) {
+            const double dx = legendre(x, dp) / dp;
+            x -= dx;
+            if (std::fabs(dx) < 1e-17) break;
+        }
+        legendre(x, dp);
+        x01[i] = 0.5 * (x + 1.0);
+        w01[i] = 1.0 / ((1.0 - x * x) * dp * dp);
+    }
+}
+
 static const WeightRule &weight_rule()
 {
     static WeightRule r = [] {
@@ -97,30 +134,8 @@ static const WeightRule &weight_rule()
             q.v[k] = 1.0 / (1.0 + e);
             q.w[k] = (pi / 8.0) * std::cosh(t) * q.u[k] * q.v[k];
         }
-        for (int i = 0; i < WG_GL; ++i) {               // Newton on P_16 from the usual guesses
-            double x = std::cos(pi * (i + 0.75) / (WG_GL + 0.5)), dp = 1.0;
-            for (int it = 0; it < 100; ++it) {
-                double p0 = 1.0, p1 = x;
-                for (int k = 2; k <= WG_GL; ++k) {
-                    const double p2 = ((2.0 * k - 1.0) * x * p1 - (k - 1.0) * p0) / k;
-                    p0 = p1;
-                    p1 = p2;
-                }
-                dp = WG_GL * (x * p1 - p0) / (x * x - 1.0);
-                const double dx = p1 / dp;
-                x -= dx;
-                if (std::fabs(dx) < 1e-17) break;
-            }
-            double p0 = 1.0, p1 = x;
-            for (int k = 2; k <= WG_GL; ++k) {
-                const double p2 = ((2.0 * k - 1.0) * x * p1 - (k - 1.0) * p0) / k;
-                p0 = p1;
-                p1 = p2;
-            }
-            dp = WG_GL * (x * p1 - p0) / (x * x - 1.0);
-            q.x[i] = 0.5 * (x + 1.0);
-            q.gw[i] = 1.0 / ((1.0 - x * x) * dp * dp);
-        }
+        gauss_legendre(WG_GL, q.x, q.gw);
+        gauss_legendre(WG_GL8, q.x8, q.gw8);
         return q;
     }();
     return r;
@@ -155,6 +170,8 @@ int fpde_weights_g(fpde_ctx *ctx, double p, double alpha, const double *time, in
         dtime = (const double *)mine[0];
         dout = (double *)mine[1];
         cudaMemcpyAsync(mine[0], time, (size_t)(n1 + 2) * sizeof(double), cudaMemcpyHostToDevice, st);
+        // the caller's rows go up too, so that entries past t = n come back unchanged
+        cudaMemcpyAsync(mine[1], out, (size_t)rows * ld * sizeof(double), cudaMemcpyHostToDevice, st);
     }
     const dim3 grid((unsigned)((n1 + 1 + 255) / 256), (unsigned)rows);
     k_weights_g<<<grid, 256, 0, st>>>(dtime, n0, p, alpha, dout, ld, weight_rule());

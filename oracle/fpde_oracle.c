@@ -36,12 +36,41 @@ void fo_l1_weights(double alpha, const double *time, int n, double *kb, double *
 }
 
 /* Quadrature rules of fo_weights_g: double-exponential nodes t = k/8, |k| <= 28, mapped to
- * (0, 1) by u = 1/(1 + e^{-pi sinh t}) (v = 1 - u formed directly), and 16-point
- * Gauss-Legendre on (0, 1) by Newton iteration on P_16. */
+ * (0, 1) by u = 1/(1 + e^{-pi sinh t}) (v = 1 - u formed directly), and 16- and 8-point
+ * Gauss-Legendre on (0, 1) by Newton iteration on P_m. */
 #define WG_DE 57
 #define WG_GL 16
-static double wg_u[WG_DE], wg_v[WG_DE], wg_w[WG_DE], wg_x[WG_GL], wg_gw[WG_GL];
+#define WG_GL8 8
+static double wg_u[WG_DE], wg_v[WG_DE], wg_w[WG_DE], wg_x[WG_GL], wg_gw[WG_GL], wg_x8[WG_GL8], wg_gw8[WG_GL8];
 static int wg_ready = 0;
+
+static double wg_legendre(int m, double z, double *d)
+{
+    double p0 = 1.0, p1 = z;
+    for (int k = 2; k <= m; k++) {
+        double p2 = ((2.0 * k - 1.0) * z * p1 - (k - 1.0) * p0) / k;
+        p0 = p1;
+        p1 = p2;
+    }
+    *d = m * (z * p1 - p0) / (z * z - 1.0);
+    return p1;
+}
+
+static void wg_gauss_legendre(int m, double *x01, double *w01)
+{
+    const double pi = 3.14159265358979323846;
+    for (int i = 0; i < m; i++) {
+        double x = cos(pi * (i + 0.75) / (m + 0.5)), dp = 1.0;
+        for (int it = 0; it < 100; it++) {
+            double dx = wg_legendre(m, x, &dp) / dp;
+            x -= dx;
+            if (fabs(dx) < 1e-17) break;
+        }
+        wg_legendre(m, x, &dp);
+        x01[i] = 0.5 * (x + 1.0);
+        w01[i] = 1.0 / ((1.0 - x * x) * dp * dp);   /* 2/((1-x^2)P'^2) on (-1,1), halved */
+    }
+}
 
 static void wg_init(void)
 {
@@ -54,32 +83,8 @@ static void wg_init(void)
         wg_v[k] = 1.0 / (1.0 + e);
         wg_w[k] = (pi / 8.0) * cosh(t) * wg_u[k] * wg_v[k];
     }
-    for (int i = 0; i < WG_GL; i++) {
-        double x = cos(pi * (i + 0.75) / (WG_GL + 0.5)), dp = 1.0;
-        for (int it = 0; it < 100; it++) {
-            double p0 = 1.0, p1 = x;
-            for (int k = 2; k <= WG_GL; k++) {
-                double p2 = ((2.0 * k - 1.0) * x * p1 - (k - 1.0) * p0) / k;
-                p0 = p1;
-                p1 = p2;
-            }
-            dp = WG_GL * (x * p1 - p0) / (x * x - 1.0);
-            double dx = p1 / dp;
-            x -= dx;
-            if (fabs(dx) < 1e-17) break;
-        }
-        {
-            double p0 = 1.0, p1 = x;
-            for (int k = 2; k <= WG_GL; k++) {
-                double p2 = ((2.0 * k - 1.0) * x * p1 - (k - 1.0) * p0) / k;
-                p0 = p1;
-                p1 = p2;
-            }
-            dp = WG_GL * (x * p1 - p0) / (x * x - 1.0);
-        }
-        wg_x[i] = 0.5 * (x + 1.0);
-        wg_gw[i] = 1.0 / ((1.0 - x * x) * dp * dp);   /* 2/((1-x^2)P'^2) on (-1,1), halved */
-    }
+    wg_gauss_legendre(WG_GL, wg_x, wg_gw);
+    wg_gauss_legendre(WG_GL8, wg_x8, wg_gw8);
     wg_ready = 1;
 }
 
@@ -118,9 +123,16 @@ static double wg_interval(double s0, double s1, double T, double p, double alpha
         }
         return wdt * sum;
     }
-    for (int i = 0; i < WG_GL; i++) {
-        double s = s0 + wdt * wg_x[i], delta = d1 + wdt * (1.0 - wg_x[i]);
-        sum += wg_gw[i] * pow(wg_gdiff(delta, s, T, p, Tp), -alpha);
+    if (d1 < 32.0 * wdt || (!smooth0 && s0 < 32.0 * wdt)) {
+        for (int i = 0; i < WG_GL; i++) {
+            double s = s0 + wdt * wg_x[i], delta = d1 + wdt * (1.0 - wg_x[i]);
+            sum += wg_gw[i] * pow(wg_gdiff(delta, s, T, p, Tp), -alpha);
+        }
+        return wdt * sum;
+    }
+    for (int i = 0; i < WG_GL8; i++) {
+        double s = s0 + wdt * wg_x8[i], delta = d1 + wdt * (1.0 - wg_x8[i]);
+        sum += wg_gw8[i] * pow(wg_gdiff(delta, s, T, p, Tp), -alpha);
     }
     return wdt * sum;
 }
@@ -134,6 +146,7 @@ void fo_weights_g(double p, double alpha, const double *time, int n, double *kb,
         if (kkk0) *kkk0 = 1.0;
         return;
     }
+#pragma omp parallel for schedule(dynamic, 64)
     for (int t = 0; t < n; t++) kb[t] = wg_interval(time[t], time[t + 1], T, p, alpha);
     if (kkk0) *kkk0 = wg_interval(time[n], T, T, p, alpha);
 }

@@ -51,9 +51,9 @@ void fo_sum_restricted(const double *old, int64_t OS, int nold, const double *kb
  * 0 -> p = 1, 1 -> 0.5, 2 -> 2, 3 -> func_power): for step n with T = time[n+1],
  *   kb[t] = int_{time[t]}^{time[t+1]} (T^p - s^p)^{-alpha} ds,  t = 0..n-1,  kkk0 = the same over
  *   [time[n], T]. The reference sums truncated Taylor/binomial series (_kb_row :1933,
- *   _kb_row2 :2000); this evaluates the integral by quadrature: 16-point Gauss-Legendre on
- *   intervals at least 4 widths from both singular points (s = T, and s = 0 when p is not a
- *   positive integer), the double-exponential rule elsewhere, and on the newest interval the
+ *   _kb_row2 :2000); this evaluates the integral by quadrature: Gauss-Legendre on intervals at
+ *   least 4 widths from both singular points (s = T, and s = 0 when p is not a positive
+ *   integer; 16 points, 8 beyond 32 widths), the double-exponential rule elsewhere, and on the newest interval the
  *   factor delta^-alpha (delta = T - s) integrated analytically on its last 1/16 (delta =
  *   h y^(1/(1-alpha))). T^p - s^p is formed as -T^p expm1(p log1p(-delta/T)) for small delta. */
 void fo_weights_g(double p, double alpha, const double *time, int n, double *kb, double *kkk0);
