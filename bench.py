@@ -56,6 +56,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64-arm", action="store_true")
     ap.add_argument("--no-autotune", action="store_true", help="built-in launch rules instead of fpde_line_autotune")
+    ap.add_argument("--max-lag", type=int, default=0,
+                    help="config2: restricted summing (the reference's sum_alg 1) keeping the newest MAX_LAG lags")
     return ap.parse_args()
 
 
@@ -160,6 +162,16 @@ class LineWorkload:
             self.metric = f"node-steps/s (1D Caputo L1 history sum + Thomas, N={self.p.N}, {self.p.steps} steps)"
             self.desc = (f"1D Caputo line N={self.p.N}, {self.p.steps} steps, alpha 0.7, tau 1e-4, lognormal k "
                          "(sigma 0.5, ell 0.01), 8-Gaussian H0 (config 2)")
+            self.restrict_eps = 0.0
+            if args.max_lag:
+                # threshold between the kb of lags max_lag and max_lag + 1 (kb_l = kkk0 b_l)
+                import fpde_hpc_gb300 as fp
+                b = fp.weights_l1_lags(self.p.alpha, args.max_lag + 2)
+                kkk0 = self.p.tau ** (1 - self.p.alpha) / (1 - self.p.alpha)
+                self.restrict_eps = 0.5 * kkk0 * (b[args.max_lag] + b[args.max_lag + 1])
+                self.metric = self.metric[:-1] + f", restricted summing: newest {args.max_lag} lags)"
+                self.desc += (f"; restricted summing (the reference's sum_alg 1) with sum_param "
+                              f"{self.restrict_eps:.6g}: the newest {args.max_lag} lags")
         else:
             kw = {}
             if args.nodes:
@@ -185,7 +197,8 @@ class LineWorkload:
         if self.do:
             return fp.Line(ctx, p.N, 0.5, p.tau, 1.0, A, B, R, p.u0, p.steps, precision=prec,
                            lag_weights=self.weights(p.steps + 1), theta=1.0, tuning=tuning)
-        return fp.Line(ctx, p.N, p.alpha, p.tau, p.Da, A, B, R, p.u0, p.steps, precision=prec, tuning=tuning)
+        return fp.Line(ctx, p.N, p.alpha, p.tau, p.Da, A, B, R, p.u0, p.steps, precision=prec, tuning=tuning,
+                       restrict_eps=self.restrict_eps)
 
     def autotune(self, ctx, prec):
         """fpde_line_autotune for this line (partition of the solve, far split depth, GEMV splits)."""
@@ -862,7 +875,7 @@ def run_ours(args):
         l64.close()
         out["split_vs_fp64"] = {"speedup": ms64 / ms, "max_rel_err": err, "rms_rel_err": rms, "bound": 1e-7}
     obj.close()
-    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+    if rank == 0 and world == 1 and not args.no_cpu_baseline and not getattr(args, "max_lag", 0):
         cb = wl.cpu_rate(os.cpu_count() or 1)
         out["cpu_baseline"] = {"value": cb["value"], "unit": "node-steps/s", "cores": os.cpu_count() or 1,
                                "kind": "port", "sample": cb["sample"]}

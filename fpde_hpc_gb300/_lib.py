@@ -28,7 +28,7 @@ class LineDesc(C.Structure):
                 ("left_kind", c_int), ("left_value", c_dbl), ("right_kind", c_int),
                 ("right_value", c_dbl), ("dLN", c_dbl), ("precision", c_int), ("block", c_int),
                 ("max_steps", c_int), ("lag_weights", c_vp), ("theta", c_dbl), ("source", c_vp),
-                ("source_rows", c_int), ("tuning", C.POINTER(LineTuning))]
+                ("source_rows", c_int), ("tuning", C.POINTER(LineTuning)), ("restrict_eps", c_dbl)]
 
 
 class Lod3dDesc(C.Structure):

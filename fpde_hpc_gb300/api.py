@@ -233,14 +233,17 @@ class Line:
     """A 1D Caputo line problem advanced on the GPU (fpde_line_*)."""
 
     def __init__(self, ctx, N, alpha, tau, Da, A, B, Rlap, u0, max_steps, left=(0, 0.0), right=(0, 0.0),
-                 dLN=0.0, precision=FP64, block=0, lag_weights=None, theta=0.0, source=None, tuning=None):
+                 dLN=0.0, precision=FP64, block=0, lag_weights=None, theta=0.0, source=None, tuning=None,
+                 restrict_eps=0.0):
         """lag_weights (max_steps+1 values, w[0] local) replace the Caputo L1 weights (the
         distributed-order equation passes fused weights / tau); theta is the explicit fraction
-        of the space operator; source is one row or a (rows, N+1) array of per-step rows."""
+        of the space operator; source is one row or a (rows, N+1) array of per-step rows;
+        restrict_eps > 0 drops the lags from the first one whose kb = w tau / Da is below it
+        (the reference's restricted summing)."""
         self.ctx, self.N = ctx, N
         d = LineDesc(N=N, alpha=alpha, tau=tau, Da=Da, left_kind=left[0], left_value=left[1],
                      right_kind=right[0], right_value=right[1], dLN=dLN, precision=precision, block=block,
-                     max_steps=max_steps, theta=theta)
+                     max_steps=max_steps, theta=theta, restrict_eps=restrict_eps)
         self._keep = []
         if lag_weights is not None:
             w = np.ascontiguousarray(lag_weights, dtype=np.float64)

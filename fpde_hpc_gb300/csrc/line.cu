@@ -27,6 +27,7 @@
 // with zero carries) behind a release flag; warp 0 of every CTA waits (bounded) for all
 // flags and forms its chunk's carries c_in and u_b as dot products with precomputed rows,
 // and every node takes two FMAs to finish.
+#include <climits>
 #include <map>
 #include <vector>
 #include <cmath>
@@ -1028,6 +1029,7 @@ struct fpde_line {
     int64_t N = 0, P = 0;
     int G = 1, s = 1, chunk = 0, max_steps = 0;
     int far_splits = 0, gemv_splits = 0;      // tuned values (0: built-in rules)
+    int max_lag = INT_MAX;                    // restricted summing: lags above are dropped
     bool split = false;
     double lam = 0, lamR = 0, kkk0 = 0, AlN = 0;
     double *A = nullptr, *g = nullptr, *al = nullptr, *cf = nullptr, *cb = nullptr;
@@ -1211,13 +1213,15 @@ static int line_enqueue(fpde_line *L, cudaStream_t st, int64_t n0, int steps, in
         cudaEvent_t *ev;
         if (!L->split) {
             int KS = 0;
-            if (n >= 1) {
-                KS = L->gemv_splits > 0 ? std::max(1, std::min<int>(L->gemv_splits, (int)std::min<int64_t>(n, KS_MAX)))
-                                        : choose_splits((int)n, L->P);
+            const int64_t t0 = n > L->max_lag ? n - L->max_lag : 0;   // oldest row of the window
+            const int64_t nr = n - t0;
+            if (nr >= 1) {
+                KS = L->gemv_splits > 0 ? std::max(1, std::min<int>(L->gemv_splits, (int)std::min<int64_t>(nr, KS_MAX)))
+                                        : choose_splits((int)nr, L->P);
                 const double *wt = L->wrev + (L->max_steps - n);   // wt[t] = w[n - t]
-                ev = probe_step ? probe_begin(L, 0, n, 8.0 * (double)n * nodes_hist, 2.0 * n * nodes_hist) : nullptr;
+                ev = probe_step ? probe_begin(L, 0, n, 8.0 * (double)nr * nodes_hist, 2.0 * nr * nodes_hist) : nullptr;
                 PROBE_REC(ev, 0);
-                if ((rc = launch_l1_partial(st, L->D, L->P, (int)n, wt, L->part, KS))) return rc;
+                if ((rc = launch_l1_partial(st, L->D + t0 * L->P, L->P, (int)nr, wt + t0, L->part, KS))) return rc;
                 PROBE_REC(ev, 1);
                 ++k;
             }
@@ -1229,9 +1233,13 @@ static int line_enqueue(fpde_line *L, cudaStream_t st, int64_t n0, int steps, in
         } else {
             const int64_t nb0 = n - n % BLK;                     // block start
             const int j = (int)(n - nb0);
+            // far history columns [kb0, nb0): the 64-step tiles the window reaches (lags up to
+            // max_lag from step nb0 go back to column nb0 - max_lag)
+            const int64_t kb0 = nb0 > L->max_lag ? (nb0 - L->max_lag) / 64 * 64 : 0;
+            const int far_kt = (int)((nb0 - kb0) / 64);
             int splits = 0;
-            if (nb0 > 0)
-                splits = L->far_splits > 0 ? std::min(L->far_splits, (int)(nb0 / 64)) : far_splits((int)(nb0 / 64), L->rows16);
+            if (far_kt > 0)
+                splits = L->far_splits > 0 ? std::min(L->far_splits, far_kt) : far_splits(far_kt, L->rows16);
             if (j == 0 && nb0 > 0 && L->x3) {
                 SplitPrep3 sp;
                 sp.ring = L->ring; sp.P = L->P; sp.nvalid = nodes_hist; sp.ld = L->ld16; sp.wlag = L->wlag;
@@ -1239,15 +1247,17 @@ static int line_enqueue(fpde_line *L, cudaStream_t st, int64_t n0, int steps, in
                 sp.pA = L->pA; sp.pW = L->pW; sp.ldp = L->ldp;
                 if ((rc = launch_block_prep3(st, sp, nb0))) return rc;
                 k += 2;
-                ev = L->probe_every > 0 ? probe_begin(L, 1, nb0, 6.0 * (double)nb0 * nodes_hist,
-                                                      6.0 * 2.0 * (double)nodes_hist * nb0 * BLK)
-                                        : nullptr;
-                PROBE_REC(ev, 0);
-                if ((rc = far3_launch(st, &L->plan3, (int)nb0, L->cfar, (int64_t)BLK * L->P, L->P, splits, L->pA,
-                                      L->pW, L->ldp, L->ctx->d_flags)))
-                    return rc;
-                PROBE_REC(ev, 1);
-                ++k;
+                if (far_kt > 0) {
+                    ev = L->probe_every > 0 ? probe_begin(L, 1, nb0, 6.0 * (double)(nb0 - kb0) * nodes_hist,
+                                                          6.0 * 2.0 * (double)nodes_hist * (nb0 - kb0) * BLK)
+                                            : nullptr;
+                    PROBE_REC(ev, 0);
+                    if ((rc = far3_launch(st, &L->plan3, (int)nb0, L->cfar, (int64_t)BLK * L->P, L->P, splits, L->pA,
+                                          L->pW, L->ldp, L->ctx->d_flags, nullptr, (int)kb0)))
+                        return rc;
+                    PROBE_REC(ev, 1);
+                    ++k;
+                }
             } else if (j == 0 && nb0 > 0) {
                 SplitPrep sp;
                 sp.ring = L->ring; sp.P = L->P; sp.nvalid = nodes_hist; sp.slots = L->slots; sp.exps = L->exps;
@@ -1360,6 +1370,9 @@ int fpde_line_create(fpde_ctx *ctx, const fpde_line_desc *desc, const double *A,
                    "bad precision mode");
     FPDE_CHECK_ARG(d.precision == FPDE_PREC_FP64 || d.block == 0 || d.block == BLK,
                    "split path: block must be 0 (auto) or 64");
+    FPDE_CHECK_ARG(std::isfinite(d.restrict_eps) && d.restrict_eps >= 0.0, "restrict_eps must be >= 0");
+    if (d.restrict_eps > 0.0 && (d.precision == FPDE_PREC_SPLIT_BF16 || d.precision == FPDE_PREC_SPLIT_F16))
+        return set_error(FPDE_ERR_UNSUPPORTED, "restricted summing runs on the FP64 and the three-slice split paths");
     const int64_t N = d.N;
     // partition of nodes 0..N-1 into G chunks (CTAs) of lt threads x sp nodes (sp a power of
     // two; lt = LT for the per-step FP64 solve, LTS solver threads for the persistent split
@@ -1556,6 +1569,16 @@ int fpde_line_create(fpde_ctx *ctx, const fpde_line_desc *desc, const double *A,
     for (int64_t j = 1; j < LW; ++j)
         wlag[j] = d.lag_weights ? (j <= L->max_steps ? d.lag_weights[j] : 0.0)
                                 : d.Da * (L->kkk0 * l1_lag(d.alpha, j)) / d.tau;
+    // restricted summing (time_summing :4117-4131, newest first): the history stops before the
+    // first lag whose kb = w tau / Da falls below restrict_eps; later lags get weight 0
+    if (d.restrict_eps > 0.0) {
+        int64_t j = 1;
+        while (j <= L->max_steps && !(std::fabs(wlag[j] * d.tau / d.Da) < d.restrict_eps)) ++j;
+        if (j <= L->max_steps) {
+            L->max_lag = (int)(j - 1);
+            for (int64_t q = j; q < LW; ++q) wlag[q] = 0.0;
+        }
+    }
     std::vector<double> wrev(L->max_steps + 1, 0.0);
     for (int64_t m = 0; m < L->max_steps; ++m) wrev[m] = wlag[L->max_steps - m];
     // Speculative block solve (split path): step n+1's right-hand side is affine in step n's

@@ -334,8 +334,9 @@ __device__ __forceinline__ float pow2f(int e)
 // is empty).
 __global__ void __launch_bounds__(THREADS3, 1)
     k_far_tc3(const __grid_constant__ FarMaps3 maps, double *__restrict__ C, int64_t ldc_split, int64_t ldc_col,
-              int64_t rows, int kt_total, int kt_per, int n_split, uint32_t idesc, const int8_t *__restrict__ pA,
-              const float *__restrict__ pW, int64_t ldp, const int *__restrict__ wcol, unsigned *flags)
+              int64_t rows, int kt_begin, int kt_total, int kt_per, int n_split, uint32_t idesc,
+              const int8_t *__restrict__ pA, const float *__restrict__ pW, int64_t ldp, const int *__restrict__ wcol,
+              unsigned *flags)
 {
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
@@ -374,7 +375,7 @@ __global__ void __launch_bounds__(THREADS3, 1)
             bool ok = true;
             for (int item = blockIdx.x; item < n_items && ok; item += gridDim.x) {
                 const int mt = item / n_split, ks = item % n_split;
-                const int kt0 = ks * kt_per, kt1 = min(kt0 + kt_per, kt_total);
+                const int kt0 = kt_begin + ks * kt_per, kt1 = min(kt0 + kt_per, kt_total);
                 for (int kt = kt0; kt < kt1; ++kt, ++g) {
                     const int s = g % STAGES3;
                     const uint32_t ph = (uint32_t)(g / STAGES3) & 1u;
@@ -401,7 +402,7 @@ __global__ void __launch_bounds__(THREADS3, 1)
             bool ok = true;
             for (int item = blockIdx.x; item < n_items && ok; item += gridDim.x) {
                 const int ks = item % n_split;
-                const int kt0 = ks * kt_per, kt1 = min(kt0 + kt_per, kt_total);
+                const int kt0 = kt_begin + ks * kt_per, kt1 = min(kt0 + kt_per, kt_total);
                 for (int kt = kt0; kt < kt1 && !*abort_s; ++kt, ++g) {
                     const int buf = g & 1;
                     const uint32_t use = (uint32_t)(g >> 1);
@@ -443,7 +444,7 @@ __global__ void __launch_bounds__(THREADS3, 1)
         bool ok = true;
         for (int item = blockIdx.x; item < n_items && ok; item += gridDim.x) {
             const int mt = item / n_split, ks = item % n_split;
-            const int kt0 = ks * kt_per, kt1 = min(kt0 + kt_per, kt_total);
+            const int kt0 = kt_begin + ks * kt_per, kt1 = min(kt0 + kt_per, kt_total);
             const int64_t row = (int64_t)mt * BM + q * 32 + lane;
             const int64_t row_c = row < rows ? row : rows - 1;
             const float *pWc = pW + (wcol ? (int64_t)wcol[mt] * BN * ldp : 0) + (int64_t)c0 * ldp;
@@ -586,14 +587,16 @@ int far_plan3_init(FarPlan3 *p, const void *const a[3], int64_t rows, int64_t ld
 }
 
 int far3_launch(cudaStream_t st, const FarPlan3 *p, int k_cols, double *C, int64_t ldc_split, int64_t ldc_col,
-                int splits, const int8_t *pA, const float *pW, int64_t ldp, unsigned *flags, const int *wcol)
+                int splits, const int8_t *pA, const float *pW, int64_t ldp, unsigned *flags, const int *wcol,
+                int k_begin)
 {
-    if (k_cols % tc::BK != 0) return set_error(FPDE_ERR_ARG, "far contraction: K must be a multiple of 64");
-    if (k_cols == 0) return FPDE_OK;
-    const int kt_total = k_cols / tc::BK;
+    if (k_cols % tc::BK != 0 || k_begin % tc::BK != 0 || k_begin < 0 || k_begin > k_cols)
+        return set_error(FPDE_ERR_ARG, "far contraction: K range must be in multiples of 64");
+    if (k_cols == k_begin) return FPDE_OK;
+    const int kt_total = k_cols / tc::BK, kt_begin = k_begin / tc::BK;
     if (splits < 1) splits = 1;
     if (splits > FAR_MAX_SPLITS) splits = FAR_MAX_SPLITS;
-    const int kt_per = (kt_total + splits - 1) / splits;     // every split is written, possibly with zeros
+    const int kt_per = (kt_total - kt_begin + splits - 1) / splits;   // every split is written, possibly with zeros
     const int64_t items = (p->rows / tc::BM) * splits;
     int sms = 152;
     {
@@ -603,8 +606,8 @@ int far3_launch(cudaStream_t st, const FarPlan3 *p, int k_cols, double *C, int64
     }
     const unsigned grid = (unsigned)std::min<int64_t>(items, sms);
     const tc::FarMaps3 *m = (const tc::FarMaps3 *)p->maps;
-    tc::k_far_tc3<<<grid, tc::THREADS3, tc::SMEM3_BYTES, st>>>(*m, C, ldc_split, ldc_col, p->rows, kt_total, kt_per,
-                                                             splits, p->idesc, pA, pW, ldp, wcol, flags);
+    tc::k_far_tc3<<<grid, tc::THREADS3, tc::SMEM3_BYTES, st>>>(*m, C, ldc_split, ldc_col, p->rows, kt_begin, kt_total,
+                                                             kt_per, splits, p->idesc, pA, pW, ldp, wcol, flags);
     FPDE_LAUNCHED(1);
     return FPDE_OK;
 }

@@ -37,9 +37,11 @@ int far_plan3_init(FarPlan3 *p, const void *const a[3], int64_t rows, int64_t ld
 // float value; hi + lo is exact in FP64): read it with ff_to_double.
 // wcol (device, may be null): per 128-row tile the weight tile (column of an ensemble) it uses,
 // whose 64 rows start at row wcol[tile] * 64 of the W slices and of pW.
+// k_begin (a multiple of 64): the contraction covers history columns [k_begin, k_cols) only
+// (a restricted history window); the splits divide that range.
 int far3_launch(cudaStream_t st, const FarPlan3 *p, int k_cols, double *C, int64_t ldc_split, int64_t ldc_col,
                 int splits, const int8_t *pA, const float *pW, int64_t ldp, unsigned *flags,
-                const int *wcol = nullptr);
+                const int *wcol = nullptr, int k_begin = 0);
 
 // float -> double from the bits (integer instructions only; exact for every float).
 __device__ __forceinline__ double f2d_bits(float x)

@@ -296,6 +296,12 @@ typedef struct fpde_line_desc {
                              to Om (fr_do's -(f(t_n,x)+f(t_{n+1},x))/2; Rp of Om1) */
     int source_rows;
     const fpde_line_tuning *tuning; /* optional launch parameters (NULL: built-in rules) */
+    double restrict_eps;  /* restricted summing, the reference's sum_alg 1 with sum_param =
+                             restrict_eps (time_summing :4117-4131): newest first, the history
+                             stops before the first lag l whose kb = w[l]*tau/Da is below it;
+                             0 keeps every lag. FPDE_PREC_FP64 and FPDE_PREC_SPLIT_BF16X3: the
+                             GEMV reads only the window's rows, the far contraction only the
+                             64-step blocks the window reaches. */
 } fpde_line_desc;
 
 /* Set up a line: A, B, Rlap (N+1 host values, entries 1..N-1 used; see fpde_line_coefs)
