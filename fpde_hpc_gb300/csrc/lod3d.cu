@@ -26,6 +26,7 @@
 // numbered with i fastest, so their state accesses are coalesced too; the sN pass walks
 // along the contiguous axis and relies on L1 for reuse of each line's cache lines.
 // The whole run is captured once into a CUDA graph and replayed.
+#include <climits>
 #include <map>
 #include <vector>
 #include <cmath>
@@ -323,6 +324,7 @@ struct fpde_lod3d {
     int dims[3] = {0, 0, 0};                 // sN, M, K
     int64_t G = 0, P = 0;
     int max_steps = 0;
+    int max_lag = INT_MAX;                    // restricted summing: lags above are dropped
     double lam = 0.0, lamR = 0.0;
     double *U = nullptr, *last = nullptr, *D = nullptr, *part = nullptr, *wrev = nullptr;
     double *rp = nullptr, *bc = nullptr;
@@ -402,19 +404,24 @@ static int lod_enqueue(fpde_lod3d *L, cudaStream_t st, int64_t n0, int steps, in
         double *Drow;
         float2 *Drowf = nullptr;                                         // split: the float-pair ring row
         if (!L->split) {
-            if (n >= 1) {
-                KS = choose_splits((int)n, L->P);
+            const int64_t t0 = n > L->max_lag ? n - L->max_lag : 0;    // oldest row of the window
+            if (n - t0 >= 1) {
+                KS = choose_splits((int)(n - t0), L->P);
                 const double *wt = L->wrev + (L->max_steps - n);     // wt[t] = w[n - t]
-                if ((rc = launch_l1_partial(st, L->D, L->P, (int)n, wt, L->part, KS))) return rc;
+                if ((rc = launch_l1_partial(st, L->D + t0 * L->P, L->P, (int)(n - t0), wt + t0, L->part, KS)))
+                    return rc;
                 ++k;
             }
             Drow = L->D + n * L->P;
         } else {
             const int64_t nb0 = n - n % 64;                          // block of 64 steps
             const int j = (int)(n - nb0);
+            // far history columns [kb0, nb0): the 64-step tiles the window reaches
+            const int64_t kb0 = nb0 > L->max_lag ? (nb0 - L->max_lag) / 64 * 64 : 0;
+            const int far_kt = (int)((nb0 - kb0) / 64);
             int splits = 0;
             if (nb0 > 0) {
-                splits = far_splits((int)(nb0 / 64), L->rows16);
+                splits = far_kt > 0 ? far_splits(far_kt, L->rows16) : 0;
                 if (j == 0) {                                        // far history t < nb0
                     SplitPrep3 sp;
                     sp.ring = L->ring; sp.P = L->P; sp.nvalid = L->G; sp.ld = L->ld16; sp.wlag = L->wlag;
@@ -422,10 +429,12 @@ static int lod_enqueue(fpde_lod3d *L, cudaStream_t st, int64_t n0, int steps, in
                     sp.pA = L->pA; sp.pW = L->pW; sp.ldp = L->ldp;
                     if ((rc = launch_block_prep3(st, sp, nb0))) return rc;
                     k += 2;
-                    if ((rc = far3_launch(st, &L->plan3, (int)nb0, L->cfar, (int64_t)64 * L->P, L->P, splits, L->pA,
-                                          L->pW, L->ldp, L->ctx->d_flags)))
-                        return rc;
-                    ++k;
+                    if (far_kt > 0) {
+                        if ((rc = far3_launch(st, &L->plan3, (int)nb0, L->cfar, (int64_t)64 * L->P, L->P, splits,
+                                              L->pA, L->pW, L->ldp, L->ctx->d_flags, nullptr, (int)kb0)))
+                            return rc;
+                        ++k;
+                    }
                 }
             }
             if (n >= 1) {
@@ -494,6 +503,7 @@ int fpde_lod3d_create(fpde_ctx *ctx, const fpde_lod3d_desc *desc, const double *
     const fpde_lod3d_desc &d = *desc;
     FPDE_CHECK_ARG(d.sN >= 2 && d.M >= 2 && d.K >= 2, "every axis needs at least 2 intervals");
     FPDE_CHECK_ARG(d.lag_weights || (d.alpha > 0.0 && d.alpha < 1.0), "alpha must be in (0, 1)");
+    FPDE_CHECK_ARG(std::isfinite(d.restrict_eps) && d.restrict_eps >= 0.0, "restrict_eps must be >= 0");
     FPDE_CHECK_ARG(d.tau > 0.0 && d.max_steps > 0, "tau and max_steps must be positive");
     FPDE_CHECK_ARG(d.precision == FPDE_PREC_FP64 || d.precision == FPDE_PREC_SPLIT_BF16X3,
                    "3D LOD: precision must be FP64 or the exact three-slice split");
@@ -518,11 +528,20 @@ int fpde_lod3d_create(fpde_ctx *ctx, const fpde_lod3d_desc *desc, const double *
         L->lamR = d.Da * kkk0 / d.tau;
     }
     const double kkk0 = d.lag_weights ? 0.0 : l1_interval_weight(d.alpha, 0.0, d.tau);
-    std::vector<double> wrev(L->max_steps + 1, 0.0);               // wrev[m] = w[max_steps - m]
-    for (int64_t m = 0; m < L->max_steps; ++m) {
-        const int64_t j = L->max_steps - m;
-        wrev[m] = d.lag_weights ? d.lag_weights[j] : d.Da * (kkk0 * l1_lag(d.alpha, j)) / d.tau;
+    auto wlag_of = [&](int64_t j) {
+        return d.lag_weights ? (j <= L->max_steps ? d.lag_weights[j] : 0.0)
+                             : d.Da * (kkk0 * l1_lag(d.alpha, j)) / d.tau;
+    };
+    // restricted summing (time_summing :4117-4131, newest first): the history stops before the
+    // first lag whose kb = w tau / Da falls below restrict_eps; later lags get weight 0
+    if (d.restrict_eps > 0.0) {
+        int64_t j = 1;
+        while (j <= L->max_steps && !(std::fabs(wlag_of(j) * d.tau / d.Da) < d.restrict_eps)) ++j;
+        if (j <= L->max_steps) L->max_lag = (int)(j - 1);
     }
+    auto wlag_at = [&](int64_t j) { return j > L->max_lag ? 0.0 : wlag_of(j); };
+    std::vector<double> wrev(L->max_steps + 1, 0.0);               // wrev[m] = w[max_steps - m]
+    for (int64_t m = 0; m < L->max_steps; ++m) wrev[m] = wlag_at(L->max_steps - m);
     const size_t gbytes = (size_t)L->G * sizeof(double), pbytes = (size_t)L->P * sizeof(double);
     L->split = d.precision == FPDE_PREC_SPLIT_BF16X3;
     bool fail = dev_alloc((void **)&L->U, pbytes) || dev_alloc((void **)&L->last, pbytes) ||
@@ -537,9 +556,7 @@ int fpde_lod3d_create(fpde_ctx *ctx, const fpde_lod3d_desc *desc, const double *
         L->ldp = L->ld16 / 64;
         const int64_t LW = L->max_steps + 64 + 1;
         wlag.assign(LW, 0.0);
-        for (int64_t j = 1; j < LW; ++j)
-            wlag[j] = d.lag_weights ? (j <= L->max_steps ? d.lag_weights[j] : 0.0)
-                                    : d.Da * (kkk0 * l1_lag(d.alpha, j)) / d.tau;
+        for (int64_t j = 1; j < LW; ++j) wlag[j] = wlag_at(j);
         for (int q = 0; q < 3 && !fail; ++q)
             fail = dev_alloc((void **)&L->h3[q], (size_t)L->rows16 * L->ld16 * 2) ||
                    dev_alloc((void **)&L->w3[q], (size_t)64 * L->ld16 * 2);

@@ -382,6 +382,8 @@ typedef struct fpde_lod3d_desc {
     const double *bc;       /* optional host grids of boundary data (Dirichlet values / fluxes at the
                                line ends), bc_rows x grid; NULL = 0 */
     int bc_rows;
+    double restrict_eps;    /* restricted summing as in fpde_line_desc (the reference's sum_alg 1 in
+                               the K pass, time_summing :4117-4131); 0 keeps every lag */
 } fpde_lod3d_desc;
 
 /* coefA/B/Rlap: three host grids each (pass 0 = sN, 1 = _M, 2 = K) of the line coefficients at

@@ -139,3 +139,51 @@ def test_lod_long_lines_vs_oracle(ctx, dims, steps):
     err = relmax(u, uref)
     print(f"LOD {dims} {steps} steps vs oracle: {err:.2e} (one-ulp envelope {env:.2e})")
     assert err <= max(1e-12, 4 * env)
+
+
+def test_lod_restricted_replays_reference_run(ctx):
+    """The reference's own mode-3 column run with restricted summing (sum_alg 1, sum_param
+    0.05: the 8 newest lags) replayed by the GPU LOD with restrict_eps = 0.05, every level to
+    1e-12. The run is the column problem of fpde_column_a2 (coefficient grids, sources and
+    boundary values recorded there)."""
+    import fpde_hpc_gb300 as fp
+    g = fgv.load(golden_path("fpde_column_alg1"))
+    a2 = fgv.load(golden_path("fpde_column_a2"))
+    dims = (int(g["sN"]), int(g["M"]), int(g["K"]))
+    cA = np.stack([a2["coefA_pass%d" % p] for p in range(3)])
+    cB = np.stack([a2["coefB_pass%d" % p] for p in range(3)])
+    cR = np.stack([a2["coefRlap_pass%d" % p] for p in range(3)])
+    taus = g["tau"]
+    steps = len(taus)
+    lod = fp.Lod3D(ctx, dims, g["alpha"], taus[0], a2["Da"], cA, cB, cR, g["U0"], steps, source=a2["Rp"],
+                   bc=a2["BC"], restrict_eps=g["sum_param"])
+    worst = 0.0
+    for n in range(steps):
+        lod.run(1)
+        worst = max(worst, relmax(lod.state(), g["U"][n]))
+    lod.close()
+    print(f"LOD restricted replay (sum_alg 1), {steps} steps: max rel {worst:.2e}")
+    assert worst <= 1e-12
+
+
+@pytest.mark.parametrize("max_lag", [0, 10, 70])
+def test_lod_restricted_split_vs_fp64(ctx, max_lag):
+    """The three-slice split LOD with a history window against the FP64 LOD with the same
+    window (far contraction from the first tile the window reaches), 150 steps."""
+    import fpde_hpc_gb300 as fp
+    from fpde_hpc_gb300 import problems
+    p = problems.config4(n=24, steps=150)
+    cA, cB, cR = p.coefs()
+    b = fp.weights_l1_lags(p.alpha, p.steps + 2)
+    kkk0 = p.tau ** (1 - p.alpha) / (1 - p.alpha)
+    eps = 0.5 * kkk0 * (b[max_lag] + b[max_lag + 1])
+    out = []
+    for prec in (0, 3):
+        lod = fp.Lod3D(ctx, p.dims, p.alpha, p.tau, p.Da, cA, cB, cR, p.u0, p.steps, left_kind=p.left_kind,
+                       right_kind=p.right_kind, dLN=p.dLN, precision=prec, restrict_eps=eps)
+        lod.run(p.steps)
+        out.append(lod.state())
+        lod.close()
+    err = relmax(out[1], out[0])
+    print(f"LOD 24^3 restricted to {max_lag} lags: split vs FP64 {err:.2e}")
+    assert err <= 1e-7

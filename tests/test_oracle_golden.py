@@ -244,3 +244,28 @@ def test_weights_g_linear_kernel_is_the_l1_closed_form():
             assert abs(k0 - kc0) / kc0 <= 2e-15
             if n:
                 assert np.max(np.abs(kb - kc) / kc) <= 2e-15
+
+
+def test_lod_restricted_replay_matches_reference_run():
+    """The reference's mode-3 column run with restricted summing (sum_alg 1, sum_param 0.05)
+    replayed step by step by the oracle: the same column problem as fpde_column_a2 (its
+    coefficient grids, sources and boundary values), each step's history cut by time_summing's
+    rule on the reference's own kb_3_cache."""
+    g = fgv.load(golden_path("fpde_column_alg1"))
+    a2 = fgv.load(golden_path("fpde_column_a2"))
+    dims = (int(g["sN"]), int(g["M"]), int(g["K"]))
+    assert dims == (int(a2["sN"]), int(a2["M"]), int(a2["K"])) and g["alpha"] == a2["alpha"]
+    assert np.array_equal(g["tau"], a2["tau"])
+    G, cA, cB, cR = _grids(a2)
+    taus = g["tau"]
+    U = g["U0"].copy()
+    hist = np.zeros((len(taus),) + G)
+    for n in range(len(taus)):
+        kb = _weights_of(g, n).copy()
+        for t in range(n - 1, -1, -1):                 # newest first: stop at the first small weight
+            if abs(kb[t]) < g["sum_param"]:
+                kb[:t + 1] = 0.0
+                break
+        oracle.lod_step_dirichlet(dims, U, hist, n, kb if n else np.zeros(1), taus, a2["Da"], a2["kkk0"][n],
+                                  cA, cB, cR, a2["Rp"][n], a2["BC"][n])
+        assert _relmax(U, g["U"][n]) <= RTOL, (n, _relmax(U, g["U"][n]))
