@@ -325,12 +325,12 @@ class Lod3D:
 
     def __init__(self, ctx, dims, alpha, tau, Da, coefA, coefB, coefRlap, u0, max_steps, left_kind=(0, 0, 0),
                  right_kind=(0, 0, 0), dLN=(0.0, 0.0, 0.0), source=None, bc=None, lag_weights=None,
-                 precision=FP64, restrict_eps=0.0):
+                 precision=FP64, restrict_eps=0.0, series_terms=0):
         sN, M, K = dims
         self.ctx, self.dims = ctx, dims
         self.shape = (K + 2, M + 2, sN + 2)
         d = Lod3dDesc(sN=sN, M=M, K=K, alpha=alpha, tau=tau, Da=Da, precision=precision, max_steps=max_steps,
-                      restrict_eps=restrict_eps)
+                      restrict_eps=restrict_eps, series_terms=series_terms)
         for q in range(3):
             d.left_kind[q], d.right_kind[q], d.dLN[q] = left_kind[q], right_kind[q], dLN[q]
         keep = []

@@ -325,6 +325,9 @@ struct fpde_lod3d {
     int64_t G = 0, P = 0;
     int max_steps = 0;
     int max_lag = INT_MAX;                    // restricted summing: lags above are dropped
+    int series = 0;                           // series expansion: moments per point (0: off)
+    double *H = nullptr;                      // [series][P] moments, moment-major
+    std::vector<double> time;                 // Time[k], accumulated as the reference does
     double lam = 0.0, lamR = 0.0;
     double *U = nullptr, *last = nullptr, *D = nullptr, *part = nullptr, *wrev = nullptr;
     double *rp = nullptr, *bc = nullptr;
@@ -395,6 +398,55 @@ static int lod_launch_pass(fpde_lod3d *L, cudaStream_t st, int pass, int64_t n, 
     return FPDE_OK;
 }
 
+// Series expansion in the K pass (the reference's sum_alg 2, time_summing :4137-4151): with the
+// newest increment d of every point, H_j += c_j d and part = Da sum_j v_j H_j / tau, in the
+// reference's order j = 0 .. P-1. The moments are moment-major (row j over all points), so
+// every access is coalesced; the step's coefficients come by value.
+constexpr int LOD_SERIES_MAX = 128;
+struct SeriesStep {
+    double c[LOD_SERIES_MAX];   // g(Time[n])^(j+1) row2_j
+    double v[LOD_SERIES_MAX];   // binomial series coefficients of (g(Time[n+1]) - s)^-alpha
+    double Da, tau;
+};
+
+__global__ void __launch_bounds__(256) k_lod_series(const double *__restrict__ dnew, double *__restrict__ H,
+                                                    int64_t ld, int P, const SeriesStep cf, double *__restrict__ part,
+                                                    int64_t G)
+{
+    const int64_t id = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (id >= G) return;
+    const double d = dnew[id];
+    double acc = 0.0;
+    for (int j = 0; j < P; ++j) {
+        const double h = fma(cf.c[j], d, H[(int64_t)j * ld + id]);
+        H[(int64_t)j * ld + id] = h;
+        acc = fma(cf.v[j], h, acc);
+    }
+    part[id] = cf.Da * (acc / cf.tau);
+}
+
+// Coefficients of step n (g(t) = t): row2_j = int_{t0}^{t1} s^j ds / t1^(j+1) over the newest
+// interval [t0, t1] = [Time[n-1], Time[n]] (the reference's row2_precalc, _kb_row2 :2000-2131:
+// (t1 - t0)/t1 for j = 0, (1 - (t0/t1)^(j+1))/(j+1) beyond), c_j = t1^(j+1) row2_j with the power
+// formed by repeated multiplication, v_0 = T^-alpha and v_j = v_{j-1} (alpha + j - 1)/(j T),
+// T = Time[n+1] (_kb_row2_fixed_coefs :1159-1180).
+static void series_step(const fpde_lod3d *L, int64_t n, SeriesStep &cf)
+{
+    const int P = L->series;
+    const double t0 = L->time[n - 1], t1 = L->time[n], T = L->time[n + 1], alpha = L->d.alpha;
+    double mult = t1, v = std::pow(T, -alpha);
+    for (int j = 0; j < P; ++j) {
+        const double r = j == 0 ? (t1 - t0) / t1 : (1.0 - std::pow(t0 / t1, (double)(j + 1))) / (double)(j + 1);
+        cf.c[j] = mult * r;
+        cf.v[j] = v;
+        mult *= t1;
+        const double i = (double)(j + 1);
+        v *= -(-alpha - i + 1.0) / (i * T);
+    }
+    cf.Da = L->d.Da;
+    cf.tau = L->d.tau;
+}
+
 static int lod_enqueue(fpde_lod3d *L, cudaStream_t st, int64_t n0, int steps, int64_t *nk)
 {
     int64_t k = 0;
@@ -403,7 +455,18 @@ static int lod_enqueue(fpde_lod3d *L, cudaStream_t st, int64_t n0, int steps, in
         int KS = 0;
         double *Drow;
         float2 *Drowf = nullptr;                                         // split: the float-pair ring row
-        if (!L->split) {
+        if (L->series) {                                             // moments, newest increment only
+            if (n >= 1) {
+                SeriesStep cf;
+                series_step(L, n, cf);
+                k_lod_series<<<(unsigned)((L->G + 255) / 256), 256, 0, st>>>(L->D + ((n - 1) & 1) * L->P, L->H, L->P,
+                                                                            L->series, cf, L->part, L->G);
+                FPDE_LAUNCHED(1);
+                ++k;
+                KS = 1;
+            }
+            Drow = L->D + (n & 1) * L->P;
+        } else if (!L->split) {
             const int64_t t0 = n > L->max_lag ? n - L->max_lag : 0;    // oldest row of the window
             if (n - t0 >= 1) {
                 KS = choose_splits((int)(n - t0), L->P);
@@ -472,7 +535,7 @@ int fpde_lod3d_destroy(fpde_lod3d *L)
     for (auto &kv : L->graphs) cudaGraphExecDestroy(kv.second);
     dev_free(L->ringf);
     dev_free(L->wff);
-    for (double *p : {L->U, L->last, L->D, L->part, L->wrev, L->rp, L->bc, L->ring, L->cfar, L->wlag, L->Sn})
+    for (double *p : {L->U, L->last, L->D, L->part, L->wrev, L->rp, L->bc, L->ring, L->cfar, L->wlag, L->Sn, L->H})
         dev_free(p);
     for (int q = 0; q < 3; ++q) {
         dev_free(L->h3[q]);
@@ -504,6 +567,9 @@ int fpde_lod3d_create(fpde_ctx *ctx, const fpde_lod3d_desc *desc, const double *
     FPDE_CHECK_ARG(d.sN >= 2 && d.M >= 2 && d.K >= 2, "every axis needs at least 2 intervals");
     FPDE_CHECK_ARG(d.lag_weights || (d.alpha > 0.0 && d.alpha < 1.0), "alpha must be in (0, 1)");
     FPDE_CHECK_ARG(std::isfinite(d.restrict_eps) && d.restrict_eps >= 0.0, "restrict_eps must be >= 0");
+    FPDE_CHECK_ARG(d.series_terms >= 0 && d.series_terms <= LOD_SERIES_MAX, "series_terms must be 0 .. 128");
+    FPDE_CHECK_ARG(d.series_terms == 0 || (d.precision == FPDE_PREC_FP64 && !d.lag_weights && d.restrict_eps == 0.0),
+                   "series expansion: FP64 path, Caputo weights, no restricted summing");
     FPDE_CHECK_ARG(d.tau > 0.0 && d.max_steps > 0, "tau and max_steps must be positive");
     FPDE_CHECK_ARG(d.precision == FPDE_PREC_FP64 || d.precision == FPDE_PREC_SPLIT_BF16X3,
                    "3D LOD: precision must be FP64 or the exact three-slice split");
@@ -544,10 +610,18 @@ int fpde_lod3d_create(fpde_ctx *ctx, const fpde_lod3d_desc *desc, const double *
     for (int64_t m = 0; m < L->max_steps; ++m) wrev[m] = wlag_at(L->max_steps - m);
     const size_t gbytes = (size_t)L->G * sizeof(double), pbytes = (size_t)L->P * sizeof(double);
     L->split = d.precision == FPDE_PREC_SPLIT_BF16X3;
+    L->series = d.series_terms;
+    if (L->series) {                                               // Time[k+1] = Time[k] + tau (init_time_step)
+        L->time.assign((size_t)L->max_steps + 2, 0.0);
+        for (int64_t q = 1; q < (int64_t)L->time.size(); ++q) L->time[q] = L->time[q - 1] + d.tau;
+    }
     bool fail = dev_alloc((void **)&L->U, pbytes) || dev_alloc((void **)&L->last, pbytes) ||
                 dev_alloc((void **)&L->wrev, wrev.size() * sizeof(double));
     std::vector<double> wlag;
-    if (!fail && !L->split) {
+    if (!fail && L->series) {                                      // two increment rows and the moments
+        fail = dev_alloc((void **)&L->D, 2 * pbytes) || dev_alloc((void **)&L->part, pbytes) ||
+               dev_alloc((void **)&L->H, (size_t)L->series * pbytes);
+    } else if (!fail && !L->split) {
         fail = dev_alloc((void **)&L->D, (size_t)L->max_steps * pbytes) ||
                dev_alloc((void **)&L->part, (size_t)KS_MAX * pbytes);
     } else if (!fail) {
@@ -669,7 +743,10 @@ int fpde_lod3d_create(fpde_ctx *ctx, const fpde_lod3d_desc *desc, const double *
     cudaMemcpyAsync(L->U, u0, gbytes, cudaMemcpyHostToDevice, st);
     cudaMemsetAsync(L->last, 0, pbytes, st);
     cudaMemcpyAsync(L->last, u0, gbytes, cudaMemcpyHostToDevice, st);
-    if (!L->split) {
+    if (L->series) {
+        cudaMemsetAsync(L->D, 0, 2 * pbytes, st);
+        cudaMemsetAsync(L->H, 0, (size_t)L->series * pbytes, st);
+    } else if (!L->split) {
         cudaMemsetAsync(L->D, 0, (size_t)L->max_steps * pbytes, st);
     } else {
         for (int q = 0; q < 3; ++q) {
@@ -762,6 +839,8 @@ int fpde_lod3d_reset(fpde_lod3d *L, const double *u0, int on_device)
     const cudaMemcpyKind kind = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
     FPDE_CUDA(cudaMemcpyAsync(L->U, u0, L->G * sizeof(double), kind, L->ctx->stream));
     FPDE_CUDA(cudaMemcpyAsync(L->last, u0, L->G * sizeof(double), kind, L->ctx->stream));
+    if (L->series)                                   // an empty history: the moments start at zero
+        FPDE_CUDA(cudaMemsetAsync(L->H, 0, (size_t)L->series * L->P * sizeof(double), L->ctx->stream));
     if (!on_device) FPDE_CUDA(cudaStreamSynchronize(L->ctx->stream));
     L->n_done = 0;
     return FPDE_OK;

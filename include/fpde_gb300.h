@@ -384,6 +384,11 @@ typedef struct fpde_lod3d_desc {
     int bc_rows;
     double restrict_eps;    /* restricted summing as in fpde_line_desc (the reference's sum_alg 1 in
                                the K pass, time_summing :4117-4131); 0 keeps every lag */
+    int series_terms;       /* > 0: the reference's sum_alg 2 with sum_param = series_terms (at most
+                               128) in the K pass (time_summing :4137-4151): P moments per grid point
+                               carried from step to step instead of the stored history, S = sum_j
+                               v_j H_j / tau (FPDE_PREC_FP64, Caputo weights, g(t) = t; the history
+                               then keeps only the newest increment) */
 } fpde_lod3d_desc;
 
 /* coefA/B/Rlap: three host grids each (pass 0 = sN, 1 = _M, 2 = K) of the line coefficients at

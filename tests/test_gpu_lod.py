@@ -187,3 +187,46 @@ def test_lod_restricted_split_vs_fp64(ctx, max_lag):
     err = relmax(out[1], out[0])
     print(f"LOD 24^3 restricted to {max_lag} lags: split vs FP64 {err:.2e}")
     assert err <= 1e-7
+
+
+def test_lod_series_replays_reference_run(ctx):
+    """The reference's own mode-3 column run with the series expansion (sum_alg 2, 16 moments)
+    replayed by the GPU LOD with series_terms = 16 (moments carried on the device, the step's
+    coefficients in closed form for g(t) = t), every level to 1e-12. The run is the column
+    problem of fpde_column_a2 (coefficient grids, sources and boundary values recorded there)."""
+    import fpde_hpc_gb300 as fp
+    g = fgv.load(golden_path("fpde_column_alg2"))
+    a2 = fgv.load(golden_path("fpde_column_a2"))
+    dims = (int(g["sN"]), int(g["M"]), int(g["K"]))
+    cA = np.stack([a2["coefA_pass%d" % p] for p in range(3)])
+    cB = np.stack([a2["coefB_pass%d" % p] for p in range(3)])
+    cR = np.stack([a2["coefRlap_pass%d" % p] for p in range(3)])
+    taus = g["tau"]
+    steps = len(taus)
+    lod = fp.Lod3D(ctx, dims, g["alpha"], taus[0], a2["Da"], cA, cB, cR, g["U0"], steps, source=a2["Rp"],
+                   bc=a2["BC"], series_terms=int(g["sum_param"]))
+    worst = 0.0
+    for n in range(steps):
+        lod.run(1)
+        worst = max(worst, relmax(lod.state(), g["U"][n]))
+    lod.close()
+    print(f"LOD series replay (sum_alg 2), {steps} steps: max rel {worst:.2e}")
+    assert worst <= 1e-12
+
+
+def test_lod_series_runs_in_pieces(ctx):
+    """A series-expansion LOD run in one call equals the same run in pieces (the moments
+    persist across graphs) and after a reset (the moments restart from zero)."""
+    import fpde_hpc_gb300 as fp
+    from fpde_hpc_gb300 import problems
+    p = problems.config4(n=20, steps=30)
+    cA, cB, cR = p.coefs()
+    lod = fp.Lod3D(ctx, p.dims, p.alpha, p.tau, p.Da, cA, cB, cR, p.u0, p.steps, left_kind=p.left_kind,
+                   right_kind=p.right_kind, dLN=p.dLN, series_terms=12)
+    lod.run(30)
+    u_one = lod.state()
+    lod.reset(p.u0)
+    for m in (7, 13, 10):
+        lod.run(m)
+    np.testing.assert_array_equal(lod.state(), u_one)
+    lod.close()
