@@ -183,3 +183,23 @@ def test_stream_ordered_mode(ctx):
     ctx.sum_alg(1, old, tau, kb=kb, sum_param=1e-3, bs=32, out=S2, sync=False)
     ctx.synchronize()
     assert torch.equal(S1, S2)
+
+
+def test_snapshot_pitch_larger_than_nodes(ctx):
+    """Snapshots with a row pitch OS above the node count (the reference rounds ocl_sol_size up
+    to its block size): only the first `nodes` entries of each row are read and written."""
+    rng = np.random.default_rng(21)
+    nt, nodes, OS = 90, 1000, 1024
+    old = rng.standard_normal((nt + 1, OS))
+    kb = 1.0 / (nt - np.arange(nt)) ** 0.9
+    tau = np.full(nt, 1e-3)
+    S = ctx.sum_alg(1, old, tau, kb=kb, sum_param=0.02, nodes=nodes)
+    ref = oracle.sum_restricted(old[:, :nodes], kb, tau, 0.02, 0)
+    assert S.shape == (nodes,) and relmax(S, ref) <= RTOL
+    H = np.zeros((nodes, 8))
+    Href = np.zeros((nodes, 8))
+    row2 = 1.0 / np.arange(1.0, 9.0)
+    S2 = ctx.sum_alg(2, old[:2], tau, sum_param=8, Htmp=H, row2=row2, gtj=0.02, gt=0.01, alpha=0.5, tstep=3,
+                     nodes=nodes)
+    ref2 = oracle.sum_series(old[0, :nodes], old[1, :nodes], Href, row2, 0.01, 0.02, 0.5, tau[3])
+    assert relmax(S2, ref2) <= RTOL and relmax(H, Href) <= RTOL
