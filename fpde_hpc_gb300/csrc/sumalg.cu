@@ -159,7 +159,7 @@ int fpde_sum(fpde_ctx *ctx, int sum_alg, int bs, int64_t OS, int64_t nodes, doub
     FPDE_CHECK_ARG(sum_alg >= 0 && sum_alg <= 2, "sum_alg must be 0, 1 or 2");
     FPDE_CHECK_ARG(on_device >= 0 && on_device <= 2, "on_device must be 0, 1 or 2");
     FPDE_CHECK_ARG(S && old && old_size >= 1 && nodes > 0 && OS >= nodes, "bad arguments");
-    FPDE_CHECK_ARG(sum_alg != 1 || bs >= 0, "bs must be >= 0");
+    FPDE_CHECK_ARG(sum_alg != 1 || (bs >= 0 && bs <= 65536), "bs must be 0 .. 65536");
     const int P = sum_alg == 2 ? (int)std::ceil(sum_param) : 0;
     if (sum_alg == 2) {
         FPDE_CHECK_ARG(std::isfinite(sum_param) && P >= 1 && P <= SERIES_PMAX,
