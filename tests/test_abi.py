@@ -106,3 +106,10 @@ def test_do_weights_match_oracle(lib_path):
     assert np.allclose(c2, c, rtol=1e-14, atol=0)
     with pytest.raises(fp.FpdeError):
         fp.do_weights([1.5], [1.0], 0.1, 3)
+
+
+def test_python_binding_covers_every_declared_symbol():
+    """Every entry point of include/*.h has a ctypes signature in the Python layer."""
+    from fpde_hpc_gb300 import _lib
+    missing = sorted(_declared() - set(_lib._SIGS))
+    assert not missing, missing
