@@ -86,6 +86,7 @@ _SIGS = {
     "fpde_far_contract3": (c_int, [c_vp, C.POINTER(c_vp), c_i64, c_i64, C.POINTER(c_vp), c_i64, c_int, c_vp, c_vp,
                                    c_i64, c_vp, c_int]),
     "fpde_sum_snapshots": (c_int, [c_vp, c_vp, c_vp, c_int, c_i64, c_i64, c_vp, c_vp, c_int]),
+    "fpde_restricted_lags": (c_int, [c_vp, c_int, c_dbl, C.POINTER(c_int)]),
     "fpde_weights_g": (c_int, [c_vp, c_dbl, c_dbl, c_vp, c_int, c_int, c_vp, c_i64, c_int]),
     "fpde_sum": (c_int, [c_vp, c_int, c_int, c_i64, c_i64, c_vp, c_vp, c_int, c_vp, c_vp, c_vp, c_vp, c_dbl,
                          c_dbl, c_dbl, c_dbl, c_int, c_int]),

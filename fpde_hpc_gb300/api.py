@@ -48,6 +48,15 @@ def gamma(x):
     return out.value
 
 
+def restricted_lags(kb_lag, eps):
+    """Lags kept by restricted summing (fpde_restricted_lags): kb_lag[j] is the weight of lag j+1."""
+    kb = np.ascontiguousarray(kb_lag, dtype=np.float64)
+    out = C.c_int()
+    check(load().fpde_restricted_lags(_ptr(kb) if kb.size else None, int(kb.size), float(eps), C.byref(out)),
+          "fpde_restricted_lags")
+    return out.value
+
+
 def do_weights(orders, qw, tau, n, gnorm=None):
     """Fused distributed-order lag weights c[0..n-1] (fpde_do_weights)."""
     a = np.ascontiguousarray(orders, dtype=np.float64)

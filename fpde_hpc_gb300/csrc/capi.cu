@@ -351,6 +351,16 @@ int fpde_weights_l1_lags(double alpha, int n, double *b)
     return FPDE_OK;
 }
 
+int fpde_restricted_lags(const double *kb_lag, int n, double eps, int *max_lag)
+{
+    FPDE_CHECK_ARG(max_lag && n >= 0 && (kb_lag || n == 0), "bad arguments");
+    FPDE_CHECK_ARG(std::isfinite(eps) && eps >= 0.0, "eps must be >= 0");
+    int j = 0;
+    while (j < n && !(std::fabs(kb_lag[j]) < eps)) ++j;    // kb_lag[j]: lag j + 1
+    *max_lag = j;
+    return FPDE_OK;
+}
+
 int fpde_gamma(double x, double *out)
 {
     FPDE_CHECK_ARG(out, "null output");

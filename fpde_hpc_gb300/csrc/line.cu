@@ -1572,11 +1572,13 @@ int fpde_line_create(fpde_ctx *ctx, const fpde_line_desc *desc, const double *A,
     // restricted summing (time_summing :4117-4131, newest first): the history stops before the
     // first lag whose kb = w tau / Da falls below restrict_eps; later lags get weight 0
     if (d.restrict_eps > 0.0) {
-        int64_t j = 1;
-        while (j <= L->max_steps && !(std::fabs(wlag[j] * d.tau / d.Da) < d.restrict_eps)) ++j;
-        if (j <= L->max_steps) {
-            L->max_lag = (int)(j - 1);
-            for (int64_t q = j; q < LW; ++q) wlag[q] = 0.0;
+        std::vector<double> kbl(L->max_steps);
+        for (int64_t j = 1; j <= L->max_steps; ++j) kbl[j - 1] = wlag[j] * d.tau / d.Da;
+        int keep = 0;
+        fpde_restricted_lags(kbl.data(), L->max_steps, d.restrict_eps, &keep);
+        if (keep < L->max_steps) {
+            L->max_lag = keep;
+            for (int64_t q = keep + 1; q < LW; ++q) wlag[q] = 0.0;
         }
     }
     std::vector<double> wrev(L->max_steps + 1, 0.0);

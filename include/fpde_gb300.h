@@ -113,6 +113,13 @@ int fpde_weights_l1_lags(double alpha, int n, double *b);
 int fpde_weights_g(fpde_ctx *ctx, double p, double alpha, const double *time, int n0, int n1, double *out,
                    int64_t ld, int on_device);
 
+/* Restricted summing's window (the reference's sum_alg 1, time_summing :4117-4131: newest
+ * first, the sum stops before the first term whose |kb| is below sum_param): with kb_lag[j] the
+ * weight of lag j + 1 (j = 0..n-1), *max_lag = the number of lags kept (n when none is below
+ * eps). Host function; fpde_line_create and fpde_lod3d_create apply it to their lag weights
+ * (kb = w tau / Da) when restrict_eps > 0. */
+int fpde_restricted_lags(const double *kb_lag, int n, double eps, int *max_lag);
+
 /* Gamma function (FP64, host). Used for Da = 1/Gamma(1-alpha) (fpde_hpc_1d.cpp:3598-3605)
  * and the distributed-order normalisers Gamma(2-alpha) (fr_do.cpp:337-341). */
 int fpde_gamma(double x, double *out);

@@ -269,3 +269,26 @@ def test_lod_restricted_replay_matches_reference_run():
         oracle.lod_step_dirichlet(dims, U, hist, n, kb if n else np.zeros(1), taus, a2["Da"], a2["kkk0"][n],
                                   cA, cB, cR, a2["Rp"][n], a2["BC"][n])
         assert _relmax(U, g["U"][n]) <= RTOL, (n, _relmax(U, g["U"][n]))
+
+
+def test_restricted_window_rule_matches_reference_run():
+    """fpde_restricted_lags (host, the rule the line and LOD set-up apply to their weights) on
+    the reference's own sum_alg 1 run: at every step the window it gives from that step's
+    kb_3_cache is the one the reference summed (the replayed history sums match bit for bit),
+    and the Caputo lag weights kkk0 b_l give the same 8 lags."""
+    import fpde_hpc_gb300 as fp
+    g = fgv.load(golden_path("fpde_column_alg1"))
+    U = g["U"]
+    m = _interior(g)
+    off = g["kb_off"].astype(int)
+    eps = g["sum_param"]
+    for n in range(1, U.shape[0]):
+        kb = g["kb_flat"][off[n]:off[n + 1]]
+        L = fp.restricted_lags(kb[::-1], eps)          # kb[t] is the weight of lag n - t
+        old = np.concatenate([g["U0"][None], U[:n]]).reshape(n + 1, -1)
+        S = sum(kb[t] * (old[t + 1] - old[t]) / g["tau"][t] for t in range(n - 1, n - 1 - L, -1)) if L else 0.0 * old[0]
+        np.testing.assert_allclose(S[m], g["S"][n].reshape(-1)[m], rtol=0, atol=1e-13 * np.abs(g["S"][n]).max())
+    b = fp.weights_l1_lags(g["alpha"], 40)
+    kkk0 = g["tau"][0] ** (1 - g["alpha"]) / (1 - g["alpha"])
+    assert fp.restricted_lags(kkk0 * b[1:], eps) == 8
+    assert fp.restricted_lags(kkk0 * b[1:], 0.0) == 39 and fp.restricted_lags(kkk0 * b[1:], 10.0) == 0
