@@ -174,3 +174,30 @@ def test_do_derivative_windows_many_nodes(ctx, t0, j0, maxt):
         ref[pt, t0:] += d[t0:]
     assert relmax(DF[:, t0:] - DF0[:, t0:], ref[:, t0:] - DF0[:, t0:]) <= 1e-12
     assert np.array_equal(DF[:, :t0], DF0[:, :t0])
+
+
+def test_do_line_split_in_pieces(ctx):
+    """The speculative solve with the explicit half restarted mid-block: a run split into
+    pieces of 37, 64, 99 and 50 steps (launches that start inside a 64-step block, with the
+    edge states taken from the stored state) against one run of all 250 steps. A restarted
+    launch sums its first history rows in another float-float order, so the states agree to
+    rounding, and both stay within 1e-7 of the oracle."""
+    import fpde_hpc_gb300 as fp
+    from fpde_hpc_gb300 import problems
+    p = problems.config3(N=3000, steps=250)
+    A, B, R = p.coefs()
+    c = fp.do_weights(p.orders, p.qw, p.tau, p.steps + 1, p.gnorm) / p.tau
+    mk = lambda: fp.Line(ctx, p.N, 0.5, p.tau, 1.0, A, B, R, p.u0, p.steps, lag_weights=c, theta=1.0, precision=3)
+    line = mk()
+    line.run(p.steps)
+    u_one = line.state()
+    line.close()
+    line = mk()
+    for m in (37, 64, 99, 50):
+        line.run(m)
+    u_pieces = line.state()
+    line.close()
+    uref, _ = oracle.line_run_general(p.u0, p.steps, c, 1.0, A, B, R)
+    print(f"DO line in pieces: vs one run {relmax(u_pieces, u_one):.2e}, vs oracle {relmax(u_pieces, uref):.2e}")
+    assert relmax(u_pieces, u_one) <= 1e-9
+    assert relmax(u_pieces, uref) <= 1e-7
