@@ -60,3 +60,34 @@ def test_restricted_two_term_split_is_unsupported(ctx):
     with pytest.raises(fp.FpdeError) as e:
         fp.Line(ctx, p.N, p.alpha, p.tau, p.Da, A, B, R, p.u0, 10, precision=1, restrict_eps=0.01)
     assert e.value.code == 6
+
+
+@pytest.mark.parametrize("precision,tol", [(0, 1e-12), (3, 1e-7)])
+def test_restricted_do_line_vs_oracle(ctx, precision, tol):
+    """Restricted summing on the distributed-order line (fused lag weights, theta = 1): the
+    window comes from kb = w tau / Da of the fused weights; 200 steps, a 90-lag window."""
+    import fpde_hpc_gb300 as fp
+    from fpde_hpc_gb300 import problems
+    p = problems.config3(N=3000, steps=200)
+    A, B, R = p.coefs()
+    c = fp.do_weights(p.orders, p.qw, p.tau, p.steps + 1, p.gnorm)      # kb of lag l (Da = 1)
+    keep = 90
+    eps = 0.5 * (abs(c[keep]) + abs(c[keep + 1]))
+    assert fp.restricted_lags(c[1:], eps) == keep
+    line = fp.Line(ctx, p.N, 0.5, p.tau, 1.0, A, B, R, p.u0, p.steps, lag_weights=c / p.tau, theta=1.0,
+                   precision=precision, restrict_eps=eps)
+    line.run(p.steps)
+    u = line.state()
+    line.close()
+    w = c / p.tau
+    w[keep + 1:] = 0.0
+    uref, _ = oracle.line_run_general(p.u0, p.steps, w, 1.0, A, B, R)
+    # the explicit half makes this line ill-conditioned: FP64 is held to 4x the oracle's own
+    # movement under one-ulp changes of its inputs (as the unrestricted FP64 DO test)
+    rng = np.random.default_rng(0)
+    pert = lambda x: x * (1 + 2.2e-16 * rng.choice([-1, 1], size=x.shape))
+    u2, _ = oracle.line_run_general(p.u0, p.steps, pert(w), 1.0, pert(A), pert(B), pert(R))
+    env = relmax(u2, uref)
+    err = relmax(u, uref)
+    print(f"DO line restricted to {keep} lags, precision {precision}: {err:.2e} (one-ulp envelope {env:.2e})")
+    assert err <= max(tol, 4 * env)
