@@ -1,0 +1,57 @@
+"""bench.py's reference arm on small cases (CPU only): one JSON line with the keys the
+benchmark contract asks for, for every workload family, and the restricted-summing option of
+the line workload."""
+import json
+import os
+import subprocess
+import sys
+
+import pytest
+
+from conftest import ROOT
+
+CASES = [
+    ["--workload", "config2", "--nodes", "1024", "--time-steps", "96"],
+    ["--workload", "config3", "--nodes", "1024", "--time-steps", "96"],
+    ["--workload", "config4", "--nodes", "12", "--time-steps", "24"],
+    ["--workload", "sum2", "--nodes", "24"],
+    ["--workload", "weights", "--time-steps", "256"],
+]
+
+
+@pytest.mark.parametrize("args", CASES, ids=[c[1] for c in CASES])
+def test_reference_arm_json(args):
+    env = dict(os.environ, OMP_NUM_THREADS="2")
+    out = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--steps", "1",
+                          "--warmup", "0"] + args, stdout=subprocess.PIPE, stderr=subprocess.PIPE, text=True,
+                         env=env, timeout=600, cwd=ROOT)
+    assert out.returncode == 0, out.stderr[-2000:]
+    lines = [ln for ln in out.stdout.splitlines() if ln.startswith("{")]
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    for k in ("impl", "metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better",
+              "scaling", "vs_baseline", "dtype", "data", "config", "cpu_baseline", "e2e"):
+        assert k in d, k
+    assert d["impl"] == "reference" and d["value"] > 0 and d["higher_is_better"] is True
+    cb = d["cpu_baseline"]
+    assert cb["kind"] in ("port", "reference") and cb["cores"] >= 1 and cb["sample"] and cb["value"] == d["value"]
+    assert d["e2e"]["value"] == d["value"] and d["e2e"]["unit"] == d["unit"]
+    assert "workload" in d["config"]
+
+
+def test_line_workload_restricted_threshold():
+    """--max-lag turns into the threshold that keeps exactly that many lags."""
+    sys.path.insert(0, ROOT)
+    import bench
+    import fpde_hpc_gb300 as fp
+    old = sys.argv
+    try:
+        sys.argv = ["bench.py", "--max-lag", "300", "--nodes", "1024", "--time-steps", "1000"]
+        a = bench.parse()
+    finally:
+        sys.argv = old
+    w = bench.LineWorkload("config2", a)
+    b = fp.weights_l1_lags(w.p.alpha, 1001)
+    kkk0 = w.p.tau ** (1 - w.p.alpha) / (1 - w.p.alpha)
+    assert fp.restricted_lags(kkk0 * b[1:], w.restrict_eps) == 300
+    assert "newest 300 lags" in w.metric
