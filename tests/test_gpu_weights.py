@@ -87,3 +87,18 @@ def test_weights_g_bad_arguments(ctx):
     assert lib.fpde_weights_g(ctx.h, 1.0, 1.5, p_t, 8, 10, p_o, 11, 0) == FPDE_ERR_ARG      # alpha > 1
     assert lib.fpde_weights_g(ctx.h, 1.0, 0.5, p_t, 8, 10, p_o, 10, 0) == FPDE_ERR_ARG      # ld < n1 + 1
     assert lib.fpde_weights_g(ctx.h, 1.0, 0.5, p_t, 9, 8, p_o, 11, 0) == FPDE_ERR_ARG       # n1 < n0
+
+
+@pytest.mark.parametrize("p", [0.5, 1.5, 3.0])
+def test_weights_g_rows_sum_to_the_beta_integral(ctx, p):
+    """Every row (a step's weights and its local weight) covers [0, T]: the row sums equal
+    T^(1 - p alpha) B(1/p, 1 - alpha) / p, for 200 rows of a random variable-step grid."""
+    from scipy.special import beta
+    rng = np.random.default_rng(int(10 * p))
+    time = oracle.time_points(1e-2 * (0.2 + rng.random(201)))
+    alpha = 0.7
+    W = ctx.weights_g(p, alpha, time, 0, 199)
+    T = time[1:201]
+    exact = T ** (1.0 - p * alpha) * beta(1.0 / p, 1.0 - alpha) / p
+    err = np.max(np.abs(W.sum(axis=1) - exact) / exact)
+    assert err <= 1e-14, err

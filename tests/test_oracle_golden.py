@@ -292,3 +292,18 @@ def test_restricted_window_rule_matches_reference_run():
     kkk0 = g["tau"][0] ** (1 - g["alpha"]) / (1 - g["alpha"])
     assert fp.restricted_lags(kkk0 * b[1:], eps) == 8
     assert fp.restricted_lags(kkk0 * b[1:], 0.0) == 39 and fp.restricted_lags(kkk0 * b[1:], 10.0) == 0
+
+
+@pytest.mark.parametrize("p", [0.5, 1.0, 1.5, 2.0, 3.0])
+@pytest.mark.parametrize("alpha", [0.05, 0.4, 0.8, 0.95])
+def test_weights_g_sum_to_the_beta_integral(p, alpha):
+    """A step's weights and its local weight cover [0, T]: sum_t kb_t + kkk0 =
+    int_0^T (T^p - s^p)^-alpha ds = T^(1 - p alpha) B(1/p, 1 - alpha) / p, on random time grids."""
+    from scipy.special import beta
+    rng = np.random.default_rng(int(100 * p + 1000 * alpha))
+    time = oracle.time_points(1e-2 * (0.2 + rng.random(60)))
+    for n in (0, 1, 7, 59):
+        kb, k0 = oracle.weights_g(p, alpha, time, n)
+        T = time[n + 1]
+        exact = T ** (1.0 - p * alpha) * beta(1.0 / p, 1.0 - alpha) / p
+        assert abs((kb.sum() + k0) - exact) <= 1e-14 * exact, (n, (kb.sum() + k0) / exact - 1)
