@@ -1,7 +1,7 @@
 """Parity of the plain FP64 GPU path with the CPU oracle (and the reference's golden runs).
 
 Tolerance: 1e-12 relative to the maximum magnitude of the reference value (normwise), the
-spec bar for the FP64 path. All calls go through the C ABI.
+parity bar of the FP64 path. All calls go through the C ABI.
 """
 import numpy as np
 import pytest
