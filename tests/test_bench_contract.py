@@ -55,3 +55,24 @@ def test_line_workload_restricted_threshold():
     kkk0 = w.p.tau ** (1 - w.p.alpha) / (1 - w.p.alpha)
     assert fp.restricted_lags(kkk0 * b[1:], w.restrict_eps) == 300
     assert "newest 300 lags" in w.metric
+
+
+def test_reference_arm_under_two_ranks():
+    """Launched as the multi-GPU runs are (torch.distributed.run, two ranks, 127.0.0.1): rank 0
+    alone measures and prints one JSON line; the other rank exits 0 without work."""
+    import socket
+    with socket.socket() as sk:                      # a free port for the rendezvous
+        sk.bind(("127.0.0.1", 0))
+        port = sk.getsockname()[1]
+    env = dict(os.environ, OMP_NUM_THREADS="1")
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", "2",
+           "--master-addr", "127.0.0.1", "--master-port", str(port), os.path.join(ROOT, "bench.py"), "--impl",
+           "reference", "--gpus", "2", "--steps", "1", "--warmup", "0", "--workload", "config2", "--nodes", "512",
+           "--time-steps", "48"]
+    out = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.PIPE, text=True, env=env, timeout=600,
+                         cwd=ROOT)
+    assert out.returncode == 0, out.stderr[-2000:]
+    lines = [ln for ln in out.stdout.splitlines() if ln.strip().startswith("{")]
+    assert len(lines) == 1, out.stdout
+    d = json.loads(lines[0])
+    assert d["impl"] == "reference" and d["n_gpus"] == 2 and d["value"] > 0
