@@ -61,6 +61,15 @@ def parse():
     return ap.parse_args()
 
 
+def max_over_ranks(x, device):
+    """The largest value of x over all ranks of the process group (the slowest replica's time)."""
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def dist_info():
     return (int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")),
             int(os.environ.get("LOCAL_RANK", "0")))
@@ -751,10 +760,7 @@ def run_ours(args):
     launches = lib.fpde_kernel_launch_count() - launches0
     clk = clocks.stop()
     if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+        ms = max_over_ranks(ms, "cuda")
     value = wl.node_steps * world / (ms / 1e3)
     u_main = obj.state()
 
@@ -770,10 +776,7 @@ def run_ours(args):
         obj.solve_host(u0_np, steps, out_np)
     e2e_s = (time.perf_counter() - t0) / args.steps
     if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([e2e_s], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
+        e2e_s = max_over_ranks(e2e_s, "cuda")
     bi, bo = wl.bytes_io()
     e2e = {"value": wl.node_steps * world / e2e_s, "unit": "node-steps/s", "h2d_bytes_per_step": bi,
            "d2h_bytes_per_step": bo, "ms_per_step": e2e_s * 1e3}

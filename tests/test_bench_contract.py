@@ -76,3 +76,33 @@ def test_reference_arm_under_two_ranks():
     assert len(lines) == 1, out.stdout
     d = json.loads(lines[0])
     assert d["impl"] == "reference" and d["n_gpus"] == 2 and d["value"] > 0
+
+
+def _rank_main(rank, port, out):
+    import torch.distributed as dist
+    sys.path.insert(0, ROOT)
+    import bench
+    dist.init_process_group("gloo", init_method=f"tcp://127.0.0.1:{port}", rank=rank, world_size=2)
+    try:
+        out[rank] = bench.max_over_ranks(1.5 + rank, "cpu")     # rank 1 is the slower replica
+    finally:
+        dist.destroy_process_group()
+
+
+def test_max_over_ranks_gloo():
+    """The N > 1 timing rule (each rank's time reduced to the maximum) on two gloo ranks."""
+    import socket
+    import torch.multiprocessing as mp
+    with socket.socket() as sk:
+        sk.bind(("127.0.0.1", 0))
+        port = sk.getsockname()[1]
+    ctx = mp.get_context("spawn")
+    with ctx.Manager() as mgr:
+        out = mgr.dict()
+        procs = [ctx.Process(target=_rank_main, args=(r, port, out)) for r in range(2)]
+        for p in procs:
+            p.start()
+        for p in procs:
+            p.join(timeout=300)
+        assert all(p.exitcode == 0 for p in procs)
+        assert dict(out) == {0: 2.5, 1: 2.5}
