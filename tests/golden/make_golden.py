@@ -7,6 +7,9 @@ mount used when these fixtures were made); the fixtures themselves are committed
 tests never need it.
 
     python tests/golden/make_golden.py [REF_DIR]
+
+The 40-digit weights fixture (fpde_weights_g_exact.fgv.gz) is computed from the time grids of
+the fpde_weights_fk* fixtures written here: rerun make_weights_exact.py after this script.
 """
 import gzip
 import os
