@@ -20,7 +20,7 @@ class FpdeError(RuntimeError):
 
 class LineTuning(C.Structure):
     _fields_ = [("solve_sp", c_int), ("chunks", c_int), ("far_splits", c_int), ("gemv_splits", c_int),
-                ("ms_per_step", c_dbl)]
+                ("far_super", c_int), ("ms_per_step", c_dbl)]
 
 
 class LineDesc(C.Structure):

@@ -214,12 +214,24 @@ int launch_append(cudaStream_t st, const double *u, double *last, double *row, i
     return FPDE_OK;
 }
 
+int device_sm_count()
+{
+    static int cached[64] = {0};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0) return 1;
+    if (dev < 64 && cached[dev] > 0) return cached[dev];
+    int sms = 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms < 1) sms = 1;
+    if (dev < 64) cached[dev] = sms;
+    return sms;
+}
+
 int choose_splits(int n, int64_t P)
 {
     // Split the rows so that ~32 CTAs per SM are in flight (the stream needs many loads
     // outstanding), with at least 64 rows per split.
     int64_t ctas_per_split = (P / 2 + 255) / 256;
-    int64_t ks_par = (152 * 32 + ctas_per_split - 1) / ctas_per_split;
+    int64_t ks_par = ((int64_t)device_sm_count() * 32 + ctas_per_split - 1) / ctas_per_split;
     int64_t ks_rows = (n + 63) / 64;
     int64_t ks = ks_par < ks_rows ? ks_par : ks_rows;
     if (ks > KS_MAX) ks = KS_MAX;

@@ -74,6 +74,8 @@ namespace fpde {
 
 // Make ctx's device current for the calling thread.
 int ctx_enter(fpde_ctx *ctx);
+// Streaming multiprocessors of the current device (queried once per device).
+int device_sm_count();
 // Allocate/free device memory (returns FPDE_ERR_NOMEM on failure).
 int dev_alloc(void **p, size_t bytes);
 void dev_free(void *p);

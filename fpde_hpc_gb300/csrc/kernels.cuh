@@ -55,8 +55,11 @@ struct SplitPrep3 {
     const double *wlag = nullptr;        // w[lag] (per column: ncols rows of wstride)
     int ncols = 1;                       // weight tiles (columns of an ensemble)
     int64_t wstride = 0;
+    int n_grp = 1;                       // weight groups of 64 steps per column (a super-block)
 };
-int launch_block_prep3(cudaStream_t st, const SplitPrep3 &p, int64_t n0);
+// Convert the block ending at n0 (n0 % 64 == 0; nothing to convert at n0 = 0); with `weights`,
+// also build the weight slices for the n_grp * 64 steps from n0 (rows c*64*n_grp + r of column c).
+int launch_block_prep3(cudaStream_t st, const SplitPrep3 &p, int64_t n0, bool weights = true);
 
 // Near history of step j of a block for every node:
 //   S[i] = sum_{q<KS} far_q[j][i] + sum_{r<j} w[j-r] D_r[i],

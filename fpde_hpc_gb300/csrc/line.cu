@@ -352,8 +352,9 @@ struct LineBlockArgs {
     int src_rows;
     double *U;                            // state: read at start, written at the end
     double *ring;                         // [64][P] time-major increments of the block
-    const double *cfar;                   // far partials [KS][64][P]
+    const double *cfar;                   // far partials: split k, step j at row k*far_ld + far_row0 + j of P
     int KS;
+    int far_ld, far_row0;
     int far_pairs;                        // 1: partials are float pairs (three-slice contraction)
     int64_t P;
     const double *wlag;                   // w[lag]
@@ -412,7 +413,8 @@ __device__ __forceinline__ void far_fold_ff(const LineBlockArgs &p, int ht, int 
             for (int q = 0; q < SP; ++q) {
                 const int64_t node = a + ht + LTS * q;
                 v[m][k][q] = (k < p.KS && node < b && j + m < BLK)
-                                 ? __ldcg(p.cfar + ((int64_t)k * BLK + j + m) * p.P + node) : 0.0;
+                                 ? __ldcg(p.cfar + ((int64_t)k * p.far_ld + p.far_row0 + j + m) * p.P + node)
+                                 : 0.0;
             }
 #pragma unroll
     for (int m = 0; m < NJ; ++m)
@@ -1029,6 +1031,7 @@ struct fpde_line {
     int64_t N = 0, P = 0;
     int G = 1, s = 1, chunk = 0, max_steps = 0;
     int far_splits = 0, gemv_splits = 0;      // tuned values (0: built-in rules)
+    int sbk = 4;                              // blocks per far super-block (three-slice path)
     int max_lag = INT_MAX;                    // restricted summing: lags above are dropped
     bool split = false;
     double lam = 0, lamR = 0, kkk0 = 0, AlN = 0;
@@ -1157,13 +1160,15 @@ static cudaError_t launch_block_sp(cudaLaunchConfig_t cfg, const LineBlockArgs &
 }
 
 // Steps j0 .. j0+nsteps-1 of the block starting at nb0 in one persistent launch.
-static int line_launch_block(fpde_line *L, cudaStream_t st, int64_t nb0, int j0, int nsteps, int KS)
+static int line_launch_block(fpde_line *L, cudaStream_t st, int64_t nb0, int j0, int nsteps, int KS, int far_ld,
+                             int far_row0)
 {
     LineBlockArgs a;
     a.A = L->A; a.g = L->g; a.al = L->al; a.cf = L->cf; a.cb = L->cb; a.CB = L->CB; a.GG = L->GG;
     a.lamv = L->lamv; a.eA = L->eA; a.eB = L->eB;
     a.src = L->srcd; a.src_rows = L->src_rows;
     a.U = L->U; a.ring = L->ring; a.cfar = L->cfar; a.KS = KS; a.P = L->P; a.wlag = L->wlag;
+    a.far_ld = far_ld; a.far_row0 = far_row0;
     a.far_pairs = L->x3 ? 1 : 0;
     a.agg = L->agg; a.cflag = L->cflag; a.seq = L->seq;
     a.Lf = L->Lf; a.Mb = L->Mb; a.Kb = L->Kb; a.mb = L->mb; a.flags = L->ctx->d_flags;
@@ -1237,26 +1242,63 @@ static int line_enqueue(fpde_line *L, cudaStream_t st, int64_t n0, int steps, in
             // max_lag from step nb0 go back to column nb0 - max_lag)
             const int64_t kb0 = nb0 > L->max_lag ? (nb0 - L->max_lag) / 64 * 64 : 0;
             const int far_kt = (int)((nb0 - kb0) / 64);
-            int splits = 0;
-            if (far_kt > 0)
+            int splits = 0, far_ld = BLK, far_row0 = 0;
+            if (far_kt > 0 && !L->x3)
                 splits = L->far_splits > 0 ? std::min(L->far_splits, far_kt) : far_splits(far_kt, L->rows16);
-            if (j == 0 && nb0 > 0 && L->x3) {
-                SplitPrep3 sp;
-                sp.ring = L->ring; sp.P = L->P; sp.nvalid = nodes_hist; sp.ld = L->ld16; sp.wlag = L->wlag;
-                for (int q = 0; q < 3; ++q) { sp.hist[q] = L->h3[q]; sp.w[q] = L->w3[q]; }
-                sp.pA = L->pA; sp.pW = L->pW; sp.ldp = L->ldp;
-                if ((rc = launch_block_prep3(st, sp, nb0))) return rc;
-                k += 2;
-                if (far_kt > 0) {
-                    ev = L->probe_every > 0 ? probe_begin(L, 1, nb0, 6.0 * (double)(nb0 - kb0) * nodes_hist,
-                                                          6.0 * 2.0 * (double)nodes_hist * (nb0 - kb0) * BLK)
-                                            : nullptr;
-                    PROBE_REC(ev, 0);
-                    if ((rc = far3_launch(st, &L->plan3, (int)nb0, L->cfar, (int64_t)BLK * L->P, L->P, splits, L->pA,
-                                          L->pW, L->ldp, L->ctx->d_flags, nullptr, (int)kb0)))
-                        return rc;
-                    PROBE_REC(ev, 1);
-                    ++k;
+            if (L->x3) {
+                // Two-level blocking: super-blocks of sbk blocks starting at s0. The history older
+                // than s0 is contracted once for all sbk*64 steps of the super-block (the "super"
+                // partials, splits 0..sup-1, rows [0, sbk*64) of every split); each block adds the
+                // contraction over the super-block's own older blocks [s0, nb0) (the "near-far"
+                // partial in split slot sup, rows of this block). Both are pure functions of s0
+                // and nb0, so a run may start at any block.
+                const int sbk = L->sbk;
+                const int m = (int)((nb0 / BLK) % sbk);
+                const int64_t s0 = nb0 - (int64_t)BLK * m;
+                const int64_t kbs = s0 > L->max_lag ? (s0 - L->max_lag) / 64 * 64 : 0;
+                const int sup_kt = (int)((s0 - kbs) / 64);
+                const int sup = sup_kt > 0 ? std::min(FAR_MAX_SPLITS - 1,
+                                                      L->far_splits > 0 ? std::min(L->far_splits, sup_kt)
+                                                                        : far_splits(sup_kt, L->rows16 * sbk))
+                                           : 0;
+                const int64_t kn0 = std::max(s0, kb0);
+                const int near_kt = (int)((nb0 - kn0) / 64);
+                splits = sup + (near_kt > 0 ? 1 : 0);
+                far_ld = BLK * sbk;
+                far_row0 = BLK * m;
+                if (j == 0 && (nb0 > 0 || sbk > 1)) {
+                    // convert the finished block; at a super-block start also the weight slices of
+                    // all its steps (the first super-block's later blocks need them too)
+                    SplitPrep3 sp;
+                    sp.ring = L->ring; sp.P = L->P; sp.nvalid = nodes_hist; sp.ld = L->ld16; sp.wlag = L->wlag;
+                    for (int q = 0; q < 3; ++q) { sp.hist[q] = L->h3[q]; sp.w[q] = L->w3[q]; }
+                    sp.pA = L->pA; sp.pW = L->pW; sp.ldp = L->ldp; sp.n_grp = sbk;
+                    if ((rc = launch_block_prep3(st, sp, nb0, m == 0))) return rc;
+                    k += (nb0 > 0 ? 1 : 0) + (m == 0 ? 1 : 0);
+                    if (m == 0 && sup_kt > 0) {
+                        ev = L->probe_every > 0
+                                 ? probe_begin(L, 1, nb0, 6.0 * (double)(s0 - kbs) * nodes_hist,
+                                               6.0 * 2.0 * (double)nodes_hist * (s0 - kbs) * BLK * sbk)
+                                 : nullptr;
+                        PROBE_REC(ev, 0);
+                        if ((rc = far3_launch(st, &L->plan3, (int)s0, L->cfar, (int64_t)far_ld * L->P, L->P, sup,
+                                              L->pA, L->pW, L->ldp, L->ctx->d_flags, nullptr, (int)kbs, sbk, 0)))
+                            return rc;
+                        PROBE_REC(ev, 1);
+                        ++k;
+                    }
+                    if (near_kt > 0) {
+                        ev = L->probe_every > 0 ? probe_begin(L, 3, nb0, 6.0 * (double)(nb0 - kn0) * nodes_hist,
+                                                              6.0 * 2.0 * (double)nodes_hist * (nb0 - kn0) * BLK)
+                                                : nullptr;
+                        PROBE_REC(ev, 0);
+                        if ((rc = far3_launch(st, &L->plan3, (int)nb0, L->cfar + ((int64_t)sup * far_ld + far_row0) * L->P,
+                                              (int64_t)far_ld * L->P, L->P, 1, L->pA, L->pW, L->ldp, L->ctx->d_flags,
+                                              nullptr, (int)kn0, 1, m)))
+                            return rc;
+                        PROBE_REC(ev, 1);
+                        ++k;
+                    }
                 }
             } else if (j == 0 && nb0 > 0) {
                 SplitPrep sp;
@@ -1285,7 +1327,7 @@ static int line_enqueue(fpde_line *L, cudaStream_t st, int64_t n0, int steps, in
             }
             ev = L->probe_every > 0 ? probe_begin(L, 2, n, bytes, flops, nst) : nullptr;
             PROBE_REC(ev, 0);
-            if ((rc = line_launch_block(L, st, nb0, j, nst, splits))) return rc;
+            if ((rc = line_launch_block(L, st, nb0, j, nst, splits, far_ld, far_row0))) return rc;
             PROBE_REC(ev, 1);
             ++k;
             n += nst - 1;
@@ -1435,8 +1477,9 @@ int fpde_line_create(fpde_ctx *ctx, const fpde_line_desc *desc, const double *A,
     L->s = sp;
     L->chunk = (int)chunk;
     if (tu) {
-        L->far_splits = std::min(std::max(tu->far_splits, 0), FAR_MAX_SPLITS);
+        L->far_splits = std::min(std::max(tu->far_splits, 0), FAR_MAX_SPLITS - 1);
         L->gemv_splits = std::min(std::max(tu->gemv_splits, 0), KS_MAX);
+        if (tu->far_super > 0) L->sbk = std::min(tu->far_super, FAR_MAX_SUPER);
     }
     L->d.tuning = nullptr;                     // not kept
     L->max_steps = d.max_steps;
@@ -1564,7 +1607,7 @@ int fpde_line_create(fpde_ctx *ctx, const fpde_line_desc *desc, const double *A,
         }
     }
     // lag weights w[j] = Da * kb(lag j) / tau with kb(lag j) = kkk0 * b_j; wrev[m] = w[L - m]
-    const int64_t LW = L->max_steps + BLK + 1;
+    const int64_t LW = L->max_steps + (int64_t)BLK * FAR_MAX_SUPER + 1;
     std::vector<double> wlag(LW, 0.0);
     for (int64_t j = 1; j < LW; ++j)
         wlag[j] = d.lag_weights ? (j <= L->max_steps ? d.lag_weights[j] : 0.0)
@@ -1676,15 +1719,15 @@ int fpde_line_create(fpde_ctx *ctx, const fpde_line_desc *desc, const double *A,
         L->ldp = L->ld16 / 64;
         for (int q = 0; q < 3 && !fail; ++q)
             fail = dev_alloc((void **)&L->h3[q], (size_t)L->rows16 * L->ld16 * 2) ||
-                   dev_alloc((void **)&L->w3[q], (size_t)BLK * L->ld16 * 2);
+                   dev_alloc((void **)&L->w3[q], (size_t)BLK * L->sbk * L->ld16 * 2);
         fail = fail || dev_alloc((void **)&L->pA, (size_t)L->rows16 * L->ldp) ||
-               dev_alloc((void **)&L->pW, (size_t)BLK * L->ldp * sizeof(float)) ||
+               dev_alloc((void **)&L->pW, (size_t)BLK * L->sbk * L->ldp * sizeof(float)) ||
                dev_alloc((void **)&L->ring, (size_t)BLK * L->P * sizeof(double)) ||
-               dev_alloc((void **)&L->cfar, (size_t)FAR_MAX_SPLITS * BLK * L->P * sizeof(double)) ||
+               dev_alloc((void **)&L->cfar, (size_t)FAR_MAX_SPLITS * BLK * L->sbk * L->P * sizeof(double)) ||
                dev_alloc((void **)&L->wlag, LW * sizeof(double));
         if (!fail) {
             const void *a[3] = {L->h3[0], L->h3[1], L->h3[2]}, *w[3] = {L->w3[0], L->w3[1], L->w3[2]};
-            int rcp = far_plan3_init(&L->plan3, a, L->rows16, L->ld16, w, L->ld16);
+            int rcp = far_plan3_init(&L->plan3, a, L->rows16, L->ld16, w, L->ld16, L->sbk);
             if (rcp) {
                 std::string keep = fpde_last_error_string();
                 fpde_line_destroy(L);
@@ -1814,12 +1857,12 @@ int fpde_line_create(fpde_ctx *ctx, const fpde_line_desc *desc, const double *A,
     } else if (L->x3) {
         for (int q = 0; q < 3; ++q) {
             cudaMemsetAsync(L->h3[q], 0, (size_t)L->rows16 * L->ld16 * 2, st);
-            cudaMemsetAsync(L->w3[q], 0, (size_t)BLK * L->ld16 * 2, st);
+            cudaMemsetAsync(L->w3[q], 0, (size_t)BLK * L->sbk * L->ld16 * 2, st);
         }
         cudaMemsetAsync(L->pA, 0, (size_t)L->rows16 * L->ldp, st);
-        cudaMemsetAsync(L->pW, 0, (size_t)BLK * L->ldp * sizeof(float), st);
+        cudaMemsetAsync(L->pW, 0, (size_t)BLK * L->sbk * L->ldp * sizeof(float), st);
         cudaMemsetAsync(L->ring, 0, (size_t)BLK * L->P * sizeof(double), st);
-        cudaMemsetAsync(L->cfar, 0, (size_t)FAR_MAX_SPLITS * BLK * L->P * sizeof(double), st);
+        cudaMemsetAsync(L->cfar, 0, (size_t)FAR_MAX_SPLITS * BLK * L->sbk * L->P * sizeof(double), st);
         cudaMemcpyAsync(L->wlag, wlag.data(), LW * sizeof(double), cudaMemcpyHostToDevice, st);
     } else {
         cudaMemsetAsync(L->h_hi, 0, (size_t)L->rows16 * L->ld16 * 2, st);

@@ -7,6 +7,7 @@
 // The power-of-two scales keep fp16 operands inside its normal range; they are exact, and
 // A*W keeps its value up to the single global factor 2^kexp undone in the epilogue.
 // bf16 has float's exponent range and runs unscaled (sexp = kexp = 0).
+#include <algorithm>
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
 
@@ -212,18 +213,24 @@ __global__ void __launch_bounds__(128) k_convert3(const double *__restrict__ rin
     }
 }
 
-// grid = (n0/64 k-tiles, 64 steps j, columns), 64 threads: W[c*64 + j][t] = w_c[n0 + j - t]
-// for the k-tile (one weight tile per column of an ensemble; one column for a line or a grid).
+// grid = (n0/64 + n_grp - 1 k-tiles, 64 n_grp steps r, columns), 64 threads:
+// W[c*64*n_grp + r][t] = w_c[n0 + r - t] for the k-tile (one weight tile per column of an
+// ensemble; one column for a line or a grid). Row r (of weight group r/64) gets the columns
+// t < n0 + 64 (r/64): every lag n0 + r - t it holds is at least 1. With n_grp > 1 the groups past
+// the first serve the steps of the later blocks of a super-block starting at n0, the columns
+// past n0 their contraction over the super-block's own history.
 __global__ void __launch_bounds__(64) k_wgen3(const double *__restrict__ wlag_all, int64_t wstride, int n0,
                                               uint16_t *__restrict__ w0, uint16_t *__restrict__ w1,
                                               uint16_t *__restrict__ w2, int64_t ld, float *__restrict__ pW,
-                                              int64_t ldp)
+                                              int64_t ldp, int n_grp, int kt_lim)
 {
     __shared__ double red[2];
-    const int kt = blockIdx.x, j = blockIdx.y + 64 * blockIdx.z;
+    const int kt = blockIdx.x, r = blockIdx.y;
+    if (kt >= n0 / 64 + r / 64 || kt >= kt_lim) return;  // the whole CTA (uniform)
+    const int j = r + 64 * n_grp * blockIdx.z;
     const double *wlag = wlag_all + (int64_t)blockIdx.z * wstride;
     const int t = kt * 64 + threadIdx.x;
-    const double v = wlag[n0 + (int)blockIdx.y - t];
+    const double v = wlag[n0 + r - t];
     double m = fabs(v);
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
@@ -240,15 +247,23 @@ __global__ void __launch_bounds__(64) k_wgen3(const double *__restrict__ wlag_al
     w2[(int64_t)j * ld + t] = c;
 }
 
-int launch_block_prep3(cudaStream_t st, const SplitPrep3 &p, int64_t n0)
+int launch_block_prep3(cudaStream_t st, const SplitPrep3 &p, int64_t n0, bool weights)
 {
-    const int blk = (int)(n0 / 64) - 1;
-    k_convert3<<<(unsigned)((p.nvalid + 127) / 128), 128, 0, st>>>(p.ring, p.P, p.nvalid, p.hist[0], p.hist[1],
-                                                                   p.hist[2], p.ld, n0 - 64, p.pA, p.ldp, blk);
-    FPDE_LAUNCHED(1);
-    dim3 g((unsigned)(n0 / 64), 64, (unsigned)(p.ncols > 0 ? p.ncols : 1));
-    k_wgen3<<<g, 64, 0, st>>>(p.wlag, p.wstride, (int)n0, p.w[0], p.w[1], p.w[2], p.ld, p.pW, p.ldp);
-    FPDE_LAUNCHED(1);
+    if (n0 >= 64) {
+        const int blk = (int)(n0 / 64) - 1;
+        k_convert3<<<(unsigned)((p.nvalid + 127) / 128), 128, 0, st>>>(p.ring, p.P, p.nvalid, p.hist[0], p.hist[1],
+                                                                       p.hist[2], p.ld, n0 - 64, p.pA, p.ldp, blk);
+        FPDE_LAUNCHED(1);
+    }
+    if (weights && n0 / 64 + (p.n_grp > 0 ? p.n_grp : 1) - 1 > 0) {
+        const int ng = p.n_grp > 0 ? p.n_grp : 1;
+        dim3 g((unsigned)(n0 / 64 + ng - 1), 64 * ng, (unsigned)(p.ncols > 0 ? p.ncols : 1));
+        // columns stop at the slices' pitch: a later block of the super-block exists only below the
+        // step capacity, so its contraction never reaches past it
+        const int kt_lim = (int)std::min<int64_t>(p.ld / 64, p.ldp);
+        k_wgen3<<<g, 64, 0, st>>>(p.wlag, p.wstride, (int)n0, p.w[0], p.w[1], p.w[2], p.ld, p.pW, p.ldp, ng, kt_lim);
+        FPDE_LAUNCHED(1);
+    }
     return FPDE_OK;
 }
 

@@ -125,6 +125,21 @@ __device__ __forceinline__ void umma(uint32_t dtm, uint64_t ad, uint64_t bd, uin
         "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n"
         ::"r"(dtm), "l"(ad), "l"(bd), "r"(idesc), "r"(acc));
 }
+// Same MMA with both smem descriptors given as (low, high) 32-bit words: the high words are
+// constant and the low words differ from a stage's base only by the operand offset >> 4 (the
+// 14-bit start-address field cannot carry: shared memory ends below 256 KB), so the issuing
+// thread forms each descriptor with one integer add.
+__device__ __forceinline__ void umma_lo(uint32_t dtm, uint32_t alo, uint32_t blo, uint32_t dhi, uint32_t idesc,
+                                        uint32_t acc)
+{
+    asm volatile(
+        "{\n\t.reg .b64 da, db;\n\t.reg .pred p;\n\t"
+        "mov.b64 da, {%1, %3};\n\t"
+        "mov.b64 db, {%2, %3};\n\t"
+        "setp.ne.b32 p, %5, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], da, db, %4, p;\n\t}\n"
+        ::"r"(dtm), "r"(alo), "r"(blo), "r"(dhi), "r"(idesc), "r"(acc));
+}
 __device__ __forceinline__ void umma_commit(uint64_t *bar)
 {
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
@@ -307,9 +322,11 @@ __global__ void __launch_bounds__(THREADS, 1)
 //   X0  = sum a0 w0                                  (integers < 2^16, 64 of them < 2^22:
 //                                                    exact in the FP32 accumulator)
 //   X12 = sum a0 w1' + a1' w0 + a0 w2' + a1' w1' + a2' w0     (2^-8 below X0)
-// go to two TMEM accumulators; the epilogue scales both by 2^(pA+pW) and folds them into
-// float-float every k-tile. The leading product is therefore free of accumulation error,
-// whatever the rounding of the tensor core's FP32 adder.
+// go to two TMEM accumulators; the epilogue scales both by 2^(pA+pW) every k-tile and folds them
+// into a float-float pair (hi, lo): X0 by an error-free TwoSum into hi, X12 (2^-8 of X0) added
+// into lo together with that sum's rounding error. The leading product is therefore free of
+// accumulation error, whatever the rounding of the tensor core's FP32 adder, and the FP32
+// rounding of lo stays near 2^-31 of the partial per k-tile.
 constexpr int STAGES3 = 3;
 constexpr int THREADS3 = 64 + 8 * 32;                         // TMA warp, MMA warp, 8 epilogue warps
 constexpr int EPI_COLS = BN / 2;                              // columns per epilogue warp
@@ -336,7 +353,7 @@ __global__ void __launch_bounds__(THREADS3, 1)
     k_far_tc3(const __grid_constant__ FarMaps3 maps, double *__restrict__ C, int64_t ldc_split, int64_t ldc_col,
               int64_t rows, int kt_begin, int kt_total, int kt_per, int n_split, uint32_t idesc,
               const int8_t *__restrict__ pA, const float *__restrict__ pW, int64_t ldp, const int *__restrict__ wcol,
-              unsigned *flags)
+              int n_grp, int grp0, int64_t ldc_grp, unsigned *flags)
 {
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
@@ -349,7 +366,7 @@ __global__ void __launch_bounds__(THREADS3, 1)
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int n_mt = (int)(rows / BM);
-    const int n_items = n_mt * n_split;
+    const int n_items = n_mt * n_split * n_grp;
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < STAGES3; ++s) { mbar_init(&full[s], 1); mbar_init(&empty[s], 1); }
@@ -374,7 +391,8 @@ __global__ void __launch_bounds__(THREADS3, 1)
             int g = 0;
             bool ok = true;
             for (int item = blockIdx.x; item < n_items && ok; item += gridDim.x) {
-                const int mt = item / n_split, ks = item % n_split;
+                const int grp = item % n_grp, mk = item / n_grp;
+                const int mt = mk / n_split, ks = mk % n_split;
                 const int kt0 = kt_begin + ks * kt_per, kt1 = min(kt0 + kt_per, kt_total);
                 for (int kt = kt0; kt < kt1; ++kt, ++g) {
                     const int s = g % STAGES3;
@@ -382,7 +400,7 @@ __global__ void __launch_bounds__(THREADS3, 1)
                     if (!mbar_wait(&empty[s], ph ^ 1u, flags, abort_s)) { ok = false; break; }
                     uint8_t *st = stage_base + s * STAGE3_BYTES;
                     mbar_expect_tx(&full[s], STAGE3_BYTES);
-                    const int x = kt * BK, y = mt * BM, yw = wcol ? wcol[mt] * BN : 0;
+                    const int x = kt * BK, y = mt * BM, yw = ((wcol ? wcol[mt] : 0) + grp0 + grp) * BN;
 #pragma unroll
                     for (int q = 0; q < 3; ++q) tma_load_2d(st + q * A_BYTES, &maps.a[q], x, y, &full[s]);
 #pragma unroll
@@ -401,7 +419,7 @@ __global__ void __launch_bounds__(THREADS3, 1)
             int g = 0;
             bool ok = true;
             for (int item = blockIdx.x; item < n_items && ok; item += gridDim.x) {
-                const int ks = item % n_split;
+                const int ks = (item / n_grp) % n_split;
                 const int kt0 = kt_begin + ks * kt_per, kt1 = min(kt0 + kt_per, kt_total);
                 for (int kt = kt0; kt < kt1 && !*abort_s; ++kt, ++g) {
                     const int buf = g & 1;
@@ -413,19 +431,20 @@ __global__ void __launch_bounds__(THREADS3, 1)
                     if (!mbar_wait(&full[s], ph, flags, abort_s)) { ok = false; break; }
                     tc_fence_after();
                     const uint32_t x0 = tmem + (uint32_t)(buf * 2 * BN), x12 = x0 + BN;
-                    const uint32_t st = smem_u32(stage_base + s * STAGE3_BYTES);
-                    const uint32_t a0 = st, a1 = st + A_BYTES, a2 = st + 2 * A_BYTES;
-                    const uint32_t w0 = st + 3 * A_BYTES, w1 = w0 + W_BYTES, w2 = w0 + 2 * W_BYTES;
+                    const uint64_t dst = sdesc_sw128(smem_u32(stage_base + s * STAGE3_BYTES));
+                    const uint32_t dlo = (uint32_t)dst, dhi = (uint32_t)(dst >> 32);
+                    constexpr uint32_t A1 = A_BYTES >> 4, A2 = 2 * A_BYTES >> 4;
+                    constexpr uint32_t W0 = 3 * A_BYTES >> 4, W1 = W0 + (W_BYTES >> 4), W2 = W0 + (2 * W_BYTES >> 4);
 #pragma unroll
                     for (int k = 0; k < BK / 16; ++k) {
-                        const uint32_t off = (uint32_t)(k * 32);
+                        const uint32_t o = dlo + (uint32_t)(k * 2);      // +32 bytes per K=16 step
                         const uint32_t acc = k ? 1u : 0u;
-                        umma(x0, sdesc_sw128(a0 + off), sdesc_sw128(w0 + off), idesc, acc);
-                        umma(x12, sdesc_sw128(a0 + off), sdesc_sw128(w1 + off), idesc, acc);
-                        umma(x12, sdesc_sw128(a1 + off), sdesc_sw128(w0 + off), idesc, 1u);
-                        umma(x12, sdesc_sw128(a0 + off), sdesc_sw128(w2 + off), idesc, 1u);
-                        umma(x12, sdesc_sw128(a1 + off), sdesc_sw128(w1 + off), idesc, 1u);
-                        umma(x12, sdesc_sw128(a2 + off), sdesc_sw128(w0 + off), idesc, 1u);
+                        umma_lo(x0, o, o + W0, dhi, idesc, acc);
+                        umma_lo(x12, o, o + W1, dhi, idesc, acc);
+                        umma_lo(x12, o + A1, o + W0, dhi, idesc, 1u);
+                        umma_lo(x12, o, o + W2, dhi, idesc, 1u);
+                        umma_lo(x12, o + A1, o + W1, dhi, idesc, 1u);
+                        umma_lo(x12, o + A2, o + W0, dhi, idesc, 1u);
                     }
                     umma_commit(&empty[s]);
                     umma_commit(&tfull[buf]);
@@ -443,20 +462,35 @@ __global__ void __launch_bounds__(THREADS3, 1)
         int g = 0;
         bool ok = true;
         for (int item = blockIdx.x; item < n_items && ok; item += gridDim.x) {
-            const int mt = item / n_split, ks = item % n_split;
+            const int grp = item % n_grp, mk = item / n_grp;
+            const int mt = mk / n_split, ks = mk % n_split;
             const int kt0 = kt_begin + ks * kt_per, kt1 = min(kt0 + kt_per, kt_total);
             const int64_t row = (int64_t)mt * BM + q * 32 + lane;
             const int64_t row_c = row < rows ? row : rows - 1;
-            const float *pWc = pW + (wcol ? (int64_t)wcol[mt] * BN * ldp : 0) + (int64_t)c0 * ldp;
+            // this lane's row exponents and its column's (c0 + lane) weight-tile scales; the next
+            // k-tile's pair is loaded while the current one is folded (both miss L1 often: shared
+            // memory takes most of it), and each column's scale reaches the warp by a shuffle
+            static_assert(EPI_COLS == 32, "one column per lane");
+            const int8_t *pAr = pA + row_c * ldp;
+            const float *pWl = pW + ((int64_t)((wcol ? wcol[mt] : 0) + grp0 + grp) * BN + c0 + lane) * ldp;
+            int e_nx = kt0 < kt1 ? (int)pAr[kt0] : 0;
+            float w_nx = kt0 < kt1 ? __ldg(pWl + kt0) : 0.f;
             float hi[EPI_COLS], lo[EPI_COLS];
 #pragma unroll
             for (int j = 0; j < EPI_COLS; ++j) { hi[j] = 0.f; lo[j] = 0.f; }
             for (int kt = kt0; kt < kt1; ++kt, ++g) {
                 const int buf = g & 1;
                 const uint32_t use = (uint32_t)(g >> 1);
+                const int e_cur = e_nx;
+                const float w_cur = w_nx;
+                if (kt + 1 < kt1) {
+                    e_nx = (int)pAr[kt + 1];
+                    w_nx = __ldg(pWl + kt + 1);
+                }
                 if (!mbar_wait(&tfull[buf], use & 1u, flags, abort_s)) { ok = false; break; }
                 tc_fence_after();
-                const float sa = pow2f((int)pA[row_c * ldp + kt]);
+                // 2^pA * 2^pW: a product of powers of two, exact while it stays normal
+                const float sa = pow2f(e_cur);
                 const uint32_t tb = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(buf * 2 * BN + c0);
 #pragma unroll
                 for (int h = 0; h < EPI_COLS / 16; ++h) {
@@ -467,26 +501,23 @@ __global__ void __launch_bounds__(THREADS3, 1)
 #pragma unroll
                     for (int jj = 0; jj < 16; ++jj) {
                         const int j = 16 * h + jj;
-                        // 2^pA * 2^pW: a product of powers of two, exact while it stays normal
-                        const float sc = sa * __ldg(pWc + (int64_t)j * ldp + kt);
-                        float x = v0[jj] * sc;                 // exact (power-of-two scaling)
-                        float s = hi[j] + x, bb = s - hi[j];
-                        float e = (hi[j] - (s - bb)) + (x - bb);
+                        const float sc = sa * __shfl_sync(0xffffffffu, w_cur, j);
+                        // X0 (exact integer sum) enters hi by TwoSum; X12, 2^-8 of it, goes
+                        // straight into lo with the rounding error (FP32 rounding of lo is
+                        // ~2^-31 of hi per k-tile)
+                        const float x = v0[jj] * sc;           // exact (power-of-two scaling)
+                        const float s = hi[j] + x, bb = s - hi[j];
+                        const float e = (hi[j] - (s - bb)) + (x - bb);
                         hi[j] = s;
-                        lo[j] += e;
-                        x = v1[jj] * sc;
-                        s = hi[j] + x;
-                        bb = s - hi[j];
-                        e = (hi[j] - (s - bb)) + (x - bb);
-                        hi[j] = s;
-                        lo[j] += e;
+                        lo[j] = fmaf(v1[jj], sc, lo[j] + e);
                     }
                 }
                 tc_fence_before();
                 mbar_arrive(&tempty[buf]);
             }
             if (ok && row < rows) {                   // float pairs: no FP64 work here
-                float2 *out = reinterpret_cast<float2 *>(C + (int64_t)ks * ldc_split + row) + (int64_t)c0 * ldc_col;
+                float2 *out = reinterpret_cast<float2 *>(C + (int64_t)ks * ldc_split + (int64_t)grp * ldc_grp + row) +
+                              (int64_t)c0 * ldc_col;
 #pragma unroll
                 for (int j = 0; j < EPI_COLS; ++j) out[(int64_t)j * ldc_col] = make_float2(hi[j], lo[j]);
             }
@@ -575,6 +606,7 @@ int far_plan3_init(FarPlan3 *p, const void *const a[3], int64_t rows, int64_t ld
         if ((rc = tc::make_map(&m->w[q], w[q], (int64_t)tc::BN * (w_tiles > 0 ? w_tiles : 1), ldw, tc::BN))) return rc;
     }
     p->rows = rows;
+    p->w_rows = (int64_t)tc::BN * (w_tiles > 0 ? w_tiles : 1);
     p->idesc = tc::idesc_f16(1, tc::BM, tc::BN);
     static bool attr_set = false;
     if (!attr_set) {
@@ -588,8 +620,10 @@ int far_plan3_init(FarPlan3 *p, const void *const a[3], int64_t rows, int64_t ld
 
 int far3_launch(cudaStream_t st, const FarPlan3 *p, int k_cols, double *C, int64_t ldc_split, int64_t ldc_col,
                 int splits, const int8_t *pA, const float *pW, int64_t ldp, unsigned *flags, const int *wcol,
-                int k_begin)
+                int k_begin, int n_grp, int grp0)
 {
+    if (n_grp < 1 || grp0 < 0 || (int64_t)(grp0 + n_grp) * tc::BN > p->w_rows)
+        return set_error(FPDE_ERR_ARG, "far contraction: weight rows out of range");
     if (k_cols % tc::BK != 0 || k_begin % tc::BK != 0 || k_begin < 0 || k_begin > k_cols)
         return set_error(FPDE_ERR_ARG, "far contraction: K range must be in multiples of 64");
     if (k_cols == k_begin) return FPDE_OK;
@@ -597,17 +631,17 @@ int far3_launch(cudaStream_t st, const FarPlan3 *p, int k_cols, double *C, int64
     if (splits < 1) splits = 1;
     if (splits > FAR_MAX_SPLITS) splits = FAR_MAX_SPLITS;
     const int kt_per = (kt_total - kt_begin + splits - 1) / splits;   // every split is written, possibly with zeros
-    const int64_t items = (p->rows / tc::BM) * splits;
-    int sms = 152;
-    {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    }
-    const unsigned grid = (unsigned)std::min<int64_t>(items, sms);
+    const int64_t items = (p->rows / tc::BM) * splits * n_grp;
+    const int sms = device_sm_count();
+    // The n_grp weight groups of one (row tile, split) are consecutive items; a grid that is a
+    // multiple of n_grp keeps them on neighbouring CTAs for the whole walk, so the history tiles
+    // they share stream from HBM once and are re-read from L2.
+    int64_t grid = std::min<int64_t>(items, sms);
+    if (grid > n_grp) grid -= grid % n_grp;
     const tc::FarMaps3 *m = (const tc::FarMaps3 *)p->maps;
-    tc::k_far_tc3<<<grid, tc::THREADS3, tc::SMEM3_BYTES, st>>>(*m, C, ldc_split, ldc_col, p->rows, kt_begin, kt_total,
-                                                             kt_per, splits, p->idesc, pA, pW, ldp, wcol, flags);
+    tc::k_far_tc3<<<(unsigned)grid, tc::THREADS3, tc::SMEM3_BYTES, st>>>(
+        *m, C, ldc_split, ldc_col, p->rows, kt_begin, kt_total, kt_per, splits, p->idesc, pA, pW, ldp, wcol, n_grp,
+        grp0, (int64_t)tc::BN * ldc_col, flags);
     FPDE_LAUNCHED(1);
     return FPDE_OK;
 }
@@ -616,12 +650,7 @@ int far_splits(int kt_total, int64_t rows)
 {
     // Splits of K only for balance of the persistent grid (one CTA per SM): the fewest splits
     // whose items fill the SMs within 5% (each split keeps at least 2 k-tiles).
-    int sms = 152;
-    {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    }
+    const int sms = device_sm_count();
     const int64_t tiles = rows / tc::BM;
     int best = 1;
     double best_waste = 1e30;

@@ -6,6 +6,7 @@
 namespace fpde {
 
 constexpr int FAR_MAX_SPLITS = 4;   // K splits (FP64 partial slices) per contraction
+constexpr int FAR_MAX_SUPER = 4;    // 64-step weight groups per far super-block
 
 struct FarPlan {
     alignas(64) unsigned char maps[4 * 128];   // four CUtensorMap (a_hi, a_lo, w_hi, w_lo)
@@ -28,6 +29,7 @@ int far_splits(int kt_total, int64_t rows);
 struct FarPlan3 {
     alignas(64) unsigned char maps[6 * 128];
     int64_t rows = 0;
+    int64_t w_rows = 0;                        // rows of the W slices (64 per weight tile)
     uint32_t idesc = 0;
 };
 // w_tiles: number of 64-row weight tiles in the W slices (columns of an ensemble; 1 otherwise).
@@ -39,9 +41,12 @@ int far_plan3_init(FarPlan3 *p, const void *const a[3], int64_t rows, int64_t ld
 // whose 64 rows start at row wcol[tile] * 64 of the W slices and of pW.
 // k_begin (a multiple of 64): the contraction covers history columns [k_begin, k_cols) only
 // (a restricted history window); the splits divide that range.
+// n_grp, grp0: every row tile is contracted against the n_grp weight tiles grp0 .. grp0+n_grp-1
+// (64 steps each, W rows (grp0+g)*64 ..; plus wcol's tile) and writes group g's 64 steps at
+// C + g*64*ldc_col: one launch covers n_grp*64 upcoming steps (a super-block).
 int far3_launch(cudaStream_t st, const FarPlan3 *p, int k_cols, double *C, int64_t ldc_split, int64_t ldc_col,
                 int splits, const int8_t *pA, const float *pW, int64_t ldp, unsigned *flags,
-                const int *wcol = nullptr, int k_begin = 0);
+                const int *wcol = nullptr, int k_begin = 0, int n_grp = 1, int grp0 = 0);
 
 // float -> double from the bits (integer instructions only; exact for every float).
 __device__ __forceinline__ double f2d_bits(float x)

@@ -1,7 +1,7 @@
 """Run one line solve of the benchmark family from the command line (for profiling runs and as a
 usage example):
 
-    python -m fpde_hpc_gb300.run_line N STEPS [PRECISION] [--sp SP --chunks G --far-splits S] [--do]
+    python -m fpde_hpc_gb300.run_line N STEPS [PRECISION] [--sp SP --chunks G --far-splits S --far-super B] [--do]
 
 builds the lognormal-k, 8-Gaussian line of N intervals (problems.config2; with --do the
 distributed-order line of problems.config3: fused 16-order weights, the explicit half of the
@@ -24,13 +24,15 @@ def main(argv=None):
     ap.add_argument("--sp", type=int, default=0, help="nodes per solver thread (0: built-in rule)")
     ap.add_argument("--chunks", type=int, default=0, help="CTAs of the block solve (0: built-in rule)")
     ap.add_argument("--far-splits", type=int, default=0, help="K splits of the far contraction (0: built-in)")
+    ap.add_argument("--far-super", type=int, default=0, help="64-step blocks per far super-block (0: built-in)")
     ap.add_argument("--do", action="store_true", help="the distributed-order line (theta = 1)")
     a = ap.parse_args(argv)
     p = problems.config3(N=a.N, steps=a.steps) if a.do else problems.config2(N=a.N, steps=a.steps)
     A, B, R = p.coefs()
     tuning = None
-    if a.sp or a.chunks or a.far_splits:
-        tuning = api.LineTuning(solve_sp=a.sp, chunks=a.chunks, far_splits=a.far_splits, gemv_splits=0)
+    if a.sp or a.chunks or a.far_splits or a.far_super:
+        tuning = api.LineTuning(solve_sp=a.sp, chunks=a.chunks, far_splits=a.far_splits, gemv_splits=0,
+                                far_super=a.far_super)
     with api.Context(0) as ctx:
         if a.do:
             c = api.do_weights(p.orders, p.qw, p.tau, a.steps + 1, p.gnorm)

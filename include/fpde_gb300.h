@@ -270,8 +270,11 @@ int fpde_tridiag_solve(fpde_ctx *ctx, const double *a, const double *b, const do
 typedef struct fpde_line_tuning {
     int solve_sp;       /* nodes per solve thread: 1, 2, 4 or 8 */
     int chunks;         /* CTAs the line is split into for the solve (at most the SM count) */
-    int far_splits;     /* K splits of the tensor-core far contraction: 1..4 (split paths) */
+    int far_splits;     /* K splits of the tensor-core far contraction: 1..4 (split paths; the
+                           three-slice path keeps one slot for its super-block partial: 1..3) */
     int gemv_splits;    /* row splits of the FP64 history sum: 1..64 (FP64 path) */
+    int far_super;      /* three-slice path: 64-step blocks per far super-block, 1..4 (the history
+                           older than a super-block is contracted once for all its steps) */
     double ms_per_step; /* output of fpde_line_autotune: measured time per step of the choice */
 } fpde_line_tuning;
 
