@@ -159,6 +159,24 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float *v)
 #pragma unroll
     for (int k = 0; k < 16; ++k) v[k] = __uint_as_float(r[k]);
 }
+__device__ __forceinline__ void tmem_ld8(uint32_t taddr, float *v)
+{
+    uint32_t r[8];
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+                 : "r"(taddr));
+#pragma unroll
+    for (int k = 0; k < 8; ++k) v[k] = __uint_as_float(r[k]);
+}
+__device__ __forceinline__ void tmem_ld4(uint32_t taddr, float *v)
+{
+    uint32_t r[4];
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0,%1,%2,%3}, [%4];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+                 : "r"(taddr));
+#pragma unroll
+    for (int k = 0; k < 4; ++k) v[k] = __uint_as_float(r[k]);
+}
 __device__ __forceinline__ void tmem_ld_wait() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
 struct __align__(64) FarMaps {
@@ -327,15 +345,25 @@ __global__ void __launch_bounds__(THREADS, 1)
 // into lo together with that sum's rounding error. The leading product is therefore free of
 // accumulation error, whatever the rounding of the tensor core's FP32 adder, and the FP32
 // rounding of lo stays near 2^-31 of the partial per k-tile.
-constexpr int STAGES3 = 3;
 constexpr int THREADS3 = 64 + 8 * 32;                         // TMA warp, MMA warp, 8 epilogue warps
-constexpr int EPI_COLS = BN / 2;                              // columns per epilogue warp
-constexpr int STAGE3_BYTES = 3 * A_BYTES + 3 * W_BYTES;      // 72 KB
-constexpr int TMEM3_COLS = 256;                               // 2 buffers x (X0, X12)
-constexpr int SMEM3_BYTES = 1024 + STAGES3 * STAGE3_BYTES + 256;
+
+// Shape of the three-slice kernel for NG weight groups (64 steps each) per item: one MMA of
+// N = 64 NG columns reads the item's history tile once for all NG groups, so the shared-memory
+// traffic per group (TMA writes + MMA operand reads) falls with NG.
+template <int NG>
+struct Far3Cfg {
+    static constexpr int N = BN * NG;                         // MMA N: steps per item
+    static constexpr int WB = N * BK * 2;                     // one weight slice of a stage
+    static constexpr int STAGE = 3 * A_BYTES + 3 * WB;        // 72 KB (NG 1), 96 KB (NG 2)
+    static constexpr int STAGES = NG == 1 ? 3 : 2;
+    static constexpr int TMEM = 4 * N;                        // 2 buffers x (X0, X12)
+    static constexpr int SMEM = 1024 + STAGES * STAGE + 256;
+    static constexpr int COLS = N / 2;                        // columns per epilogue warp
+    static constexpr int CH = NG == 1 ? 32 : 4;               // columns per TMEM read batch
+};
 
 struct __align__(64) FarMaps3 {
-    CUtensorMap a[3], w[3];
+    CUtensorMap a[3], w[3], w2[3];                            // w: 64-row weight boxes, w2: 128-row
 };
 
 // 2^e as a float for e in [-127, 127], from the bits (exact; e = -127 is the subnormal 2^-127).
@@ -344,32 +372,35 @@ __device__ __forceinline__ float pow2f(int e)
     return e >= -126 ? __int_as_float((e + 127) << 23) : __int_as_float(0x00400000);
 }
 
-// Persistent: gridDim.x CTAs (at most one per SM) walk the items (128-row tile mt, k-split
-// ks) = blockIdx.x, blockIdx.x + gridDim.x, ...; the TMA producer, the MMA issuer and the
-// epilogue follow the same static sequence of k-tiles, so the pipeline runs on across item
-// boundaries and TMEM is allocated once. Every item writes its partial (zeros if its k range
-// is empty).
+// Persistent: gridDim.x CTAs (at most one per SM) walk the items (128-row tile mt, k-split ks,
+// weight-group set gi of NG groups) = blockIdx.x, blockIdx.x + gridDim.x, ...; the TMA producer,
+// the MMA issuer and the epilogue follow the same static sequence of k-tiles, so the pipeline runs
+// on across item boundaries and TMEM is allocated once. Every item writes its partial (zeros if
+// its k range is empty).
+template <int NG>
 __global__ void __launch_bounds__(THREADS3, 1)
     k_far_tc3(const __grid_constant__ FarMaps3 maps, double *__restrict__ C, int64_t ldc_split, int64_t ldc_col,
               int64_t rows, int kt_begin, int kt_total, int kt_per, int n_split, uint32_t idesc,
               const int8_t *__restrict__ pA, const float *__restrict__ pW, int64_t ldp, const int *__restrict__ wcol,
-              int n_grp, int grp0, int64_t ldc_grp, unsigned *flags)
+              int n_sets, int grp0, int64_t ldc_grp, unsigned *flags)
 {
+    using Cfg = Far3Cfg<NG>;
+    constexpr int STAGES = Cfg::STAGES, STAGE_BYTES3 = Cfg::STAGE, N = Cfg::N, COLS = Cfg::COLS, CH = Cfg::CH;
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     uint8_t *stage_base = smem;
-    uint64_t *bars = (uint64_t *)(smem + STAGES3 * STAGE3_BYTES);
-    uint64_t *full = bars, *empty = bars + STAGES3, *tfull = bars + 2 * STAGES3, *tempty = bars + 2 * STAGES3 + 2;
-    uint64_t *mma_done = bars + 2 * STAGES3 + 4;
-    volatile uint32_t *tmem_slot = (volatile uint32_t *)(bars + 2 * STAGES3 + 5);
-    volatile int *abort_s = (volatile int *)(bars + 2 * STAGES3 + 6);
+    uint64_t *bars = (uint64_t *)(smem + STAGES * STAGE_BYTES3);
+    uint64_t *full = bars, *empty = bars + STAGES, *tfull = bars + 2 * STAGES, *tempty = bars + 2 * STAGES + 2;
+    uint64_t *mma_done = bars + 2 * STAGES + 4;
+    volatile uint32_t *tmem_slot = (volatile uint32_t *)(bars + 2 * STAGES + 5);
+    volatile int *abort_s = (volatile int *)(bars + 2 * STAGES + 6);
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int n_mt = (int)(rows / BM);
-    const int n_items = n_mt * n_split * n_grp;
+    const int n_items = n_mt * n_split * n_sets;
 
     if (threadIdx.x == 0) {
-        for (int s = 0; s < STAGES3; ++s) { mbar_init(&full[s], 1); mbar_init(&empty[s], 1); }
+        for (int s = 0; s < STAGES; ++s) { mbar_init(&full[s], 1); mbar_init(&empty[s], 1); }
         for (int b = 0; b < 2; ++b) { mbar_init(&tfull[b], 1); mbar_init(&tempty[b], 256); }
         mbar_init(mma_done, 1);
         *abort_s = 0;
@@ -378,7 +409,7 @@ __global__ void __launch_bounds__(THREADS3, 1)
     if (warp == 1) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
                          smem_u32((const void *)tmem_slot)),
-                     "r"(TMEM3_COLS));
+                     "r"(Cfg::TMEM));
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
     }
     tc_fence_before();
@@ -388,28 +419,29 @@ __global__ void __launch_bounds__(THREADS3, 1)
 
     if (warp == 0) {
         if (lane == 0) {                                   // TMA producer
+            const CUtensorMap *wm = NG == 1 ? maps.w : maps.w2;
             int g = 0;
             bool ok = true;
             for (int item = blockIdx.x; item < n_items && ok; item += gridDim.x) {
-                const int grp = item % n_grp, mk = item / n_grp;
+                const int gi = item % n_sets, mk = item / n_sets;
                 const int mt = mk / n_split, ks = mk % n_split;
                 const int kt0 = kt_begin + ks * kt_per, kt1 = min(kt0 + kt_per, kt_total);
                 for (int kt = kt0; kt < kt1; ++kt, ++g) {
-                    const int s = g % STAGES3;
-                    const uint32_t ph = (uint32_t)(g / STAGES3) & 1u;
+                    const int s = g % STAGES;
+                    const uint32_t ph = (uint32_t)(g / STAGES) & 1u;
                     if (!mbar_wait(&empty[s], ph ^ 1u, flags, abort_s)) { ok = false; break; }
-                    uint8_t *st = stage_base + s * STAGE3_BYTES;
-                    mbar_expect_tx(&full[s], STAGE3_BYTES);
-                    const int x = kt * BK, y = mt * BM, yw = ((wcol ? wcol[mt] : 0) + grp0 + grp) * BN;
+                    uint8_t *st = stage_base + s * STAGE_BYTES3;
+                    mbar_expect_tx(&full[s], STAGE_BYTES3);
+                    const int x = kt * BK, y = mt * BM, yw = ((wcol ? wcol[mt] : 0) + grp0 + NG * gi) * BN;
 #pragma unroll
                     for (int q = 0; q < 3; ++q) tma_load_2d(st + q * A_BYTES, &maps.a[q], x, y, &full[s]);
 #pragma unroll
-                    for (int q = 0; q < 3; ++q) tma_load_2d(st + 3 * A_BYTES + q * W_BYTES, &maps.w[q], x, yw, &full[s]);
+                    for (int q = 0; q < 3; ++q) tma_load_2d(st + 3 * A_BYTES + q * Cfg::WB, &wm[q], x, yw, &full[s]);
                 }
             }
-            for (int it = (g > STAGES3 ? g - STAGES3 : 0); it < g; ++it) {   // own copies in flight
-                const int s = it % STAGES3;
-                const uint32_t ph = (uint32_t)(it / STAGES3) & 1u;
+            for (int it = (g > STAGES ? g - STAGES : 0); it < g; ++it) {   // own copies in flight
+                const int s = it % STAGES;
+                const uint32_t ph = (uint32_t)(it / STAGES) & 1u;
                 unsigned long long t0 = gtimer();
                 while (!mbar_try_wait(&full[s], ph) && gtimer() - t0 < WAIT_NS) {}
             }
@@ -419,22 +451,22 @@ __global__ void __launch_bounds__(THREADS3, 1)
             int g = 0;
             bool ok = true;
             for (int item = blockIdx.x; item < n_items && ok; item += gridDim.x) {
-                const int ks = (item / n_grp) % n_split;
+                const int ks = (item / n_sets) % n_split;
                 const int kt0 = kt_begin + ks * kt_per, kt1 = min(kt0 + kt_per, kt_total);
                 for (int kt = kt0; kt < kt1 && !*abort_s; ++kt, ++g) {
                     const int buf = g & 1;
                     const uint32_t use = (uint32_t)(g >> 1);
                     if (!mbar_wait(&tempty[buf], (use & 1u) ^ 1u, flags, abort_s)) { ok = false; break; }
                     tc_fence_after();
-                    const int s = g % STAGES3;
-                    const uint32_t ph = (uint32_t)(g / STAGES3) & 1u;
+                    const int s = g % STAGES;
+                    const uint32_t ph = (uint32_t)(g / STAGES) & 1u;
                     if (!mbar_wait(&full[s], ph, flags, abort_s)) { ok = false; break; }
                     tc_fence_after();
-                    const uint32_t x0 = tmem + (uint32_t)(buf * 2 * BN), x12 = x0 + BN;
-                    const uint64_t dst = sdesc_sw128(smem_u32(stage_base + s * STAGE3_BYTES));
+                    const uint32_t x0 = tmem + (uint32_t)(buf * 2 * N), x12 = x0 + N;
+                    const uint64_t dst = sdesc_sw128(smem_u32(stage_base + s * STAGE_BYTES3));
                     const uint32_t dlo = (uint32_t)dst, dhi = (uint32_t)(dst >> 32);
                     constexpr uint32_t A1 = A_BYTES >> 4, A2 = 2 * A_BYTES >> 4;
-                    constexpr uint32_t W0 = 3 * A_BYTES >> 4, W1 = W0 + (W_BYTES >> 4), W2 = W0 + (2 * W_BYTES >> 4);
+                    constexpr uint32_t W0 = 3 * A_BYTES >> 4, W1 = W0 + (Cfg::WB >> 4), W2 = W0 + (2 * Cfg::WB >> 4);
 #pragma unroll
                     for (int k = 0; k < BK / 16; ++k) {
                         const uint32_t o = dlo + (uint32_t)(k * 2);      // +32 bytes per K=16 step
@@ -456,55 +488,69 @@ __global__ void __launch_bounds__(THREADS3, 1)
         }
     } else {
         // 8 epilogue warps: warp w reads TMEM lane quadrant w % 4 (the hardware's rule) and
-        // folds columns [c0, c0 + 32) with c0 = 32 * ((w - 2) / 4)
+        // folds columns [c0, c0 + COLS) with c0 = COLS * ((w - 2) / 4)
         const int q = warp & 3;
-        const int c0 = EPI_COLS * ((warp - 2) >> 2);
+        const int c0 = COLS * ((warp - 2) >> 2);
         int g = 0;
         bool ok = true;
         for (int item = blockIdx.x; item < n_items && ok; item += gridDim.x) {
-            const int grp = item % n_grp, mk = item / n_grp;
+            const int gi = item % n_sets, mk = item / n_sets;
             const int mt = mk / n_split, ks = mk % n_split;
             const int kt0 = kt_begin + ks * kt_per, kt1 = min(kt0 + kt_per, kt_total);
             const int64_t row = (int64_t)mt * BM + q * 32 + lane;
             const int64_t row_c = row < rows ? row : rows - 1;
-            // this lane's row exponents and its column's (c0 + lane) weight-tile scales; the next
-            // k-tile's pair is loaded while the current one is folded (both miss L1 often: shared
-            // memory takes most of it), and each column's scale reaches the warp by a shuffle
-            static_assert(EPI_COLS == 32, "one column per lane");
+            // this lane's row exponents and its columns' (c0 + 32u + lane) weight-tile scales; the
+            // next k-tile's set is loaded while the current one is folded (both miss L1 often:
+            // shared memory takes most of it), and each column's scale reaches the warp by a shuffle
+            constexpr int NU = COLS / 32;
             const int8_t *pAr = pA + row_c * ldp;
-            const float *pWl = pW + ((int64_t)((wcol ? wcol[mt] : 0) + grp0 + grp) * BN + c0 + lane) * ldp;
+            const float *pWl = pW + ((int64_t)((wcol ? wcol[mt] : 0) + grp0 + NG * gi) * BN + c0 + lane) * ldp;
             int e_nx = kt0 < kt1 ? (int)pAr[kt0] : 0;
-            float w_nx = kt0 < kt1 ? __ldg(pWl + kt0) : 0.f;
-            float hi[EPI_COLS], lo[EPI_COLS];
+            float w_nx[NU];
 #pragma unroll
-            for (int j = 0; j < EPI_COLS; ++j) { hi[j] = 0.f; lo[j] = 0.f; }
+            for (int u = 0; u < NU; ++u) w_nx[u] = kt0 < kt1 ? __ldg(pWl + (int64_t)32 * u * ldp + kt0) : 0.f;
+            float hi[COLS], lo[COLS];
+#pragma unroll
+            for (int j = 0; j < COLS; ++j) { hi[j] = 0.f; lo[j] = 0.f; }
             for (int kt = kt0; kt < kt1; ++kt, ++g) {
                 const int buf = g & 1;
                 const uint32_t use = (uint32_t)(g >> 1);
                 const int e_cur = e_nx;
-                const float w_cur = w_nx;
+                float w_cur[NU];
+#pragma unroll
+                for (int u = 0; u < NU; ++u) w_cur[u] = w_nx[u];
                 if (kt + 1 < kt1) {
                     e_nx = (int)pAr[kt + 1];
-                    w_nx = __ldg(pWl + kt + 1);
+#pragma unroll
+                    for (int u = 0; u < NU; ++u) w_nx[u] = __ldg(pWl + (int64_t)32 * u * ldp + kt + 1);
                 }
                 if (!mbar_wait(&tfull[buf], use & 1u, flags, abort_s)) { ok = false; break; }
                 tc_fence_after();
                 // 2^pA * 2^pW: a product of powers of two, exact while it stays normal
                 const float sa = pow2f(e_cur);
-                const uint32_t tb = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(buf * 2 * BN + c0);
+                const uint32_t tb = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(buf * 2 * N + c0);
 #pragma unroll
-                for (int h = 0; h < EPI_COLS / 16; ++h) {
-                    float v0[16], v1[16];
-                    tmem_ld16(tb + 16 * h, v0);
-                    tmem_ld16(tb + BN + 16 * h, v1);
+                for (int h = 0; h < COLS / CH; ++h) {
+                    // a batch of CH columns of both accumulators in flight before one wait
+                    float v0[CH], v1[CH];
+                    if constexpr (CH == 4) {
+                        tmem_ld4(tb + CH * h, v0);
+                        tmem_ld4(tb + N + CH * h, v1);
+                    } else {
+#pragma unroll
+                        for (int b = 0; b < CH / 16; ++b) {
+                            tmem_ld16(tb + CH * h + 16 * b, v0 + 16 * b);
+                            tmem_ld16(tb + N + CH * h + 16 * b, v1 + 16 * b);
+                        }
+                    }
                     tmem_ld_wait();
 #pragma unroll
-                    for (int jj = 0; jj < 16; ++jj) {
-                        const int j = 16 * h + jj;
-                        const float sc = sa * __shfl_sync(0xffffffffu, w_cur, j);
-                        // X0 (exact integer sum) enters hi by TwoSum; X12, 2^-8 of it, goes
-                        // straight into lo with the rounding error (FP32 rounding of lo is
-                        // ~2^-31 of hi per k-tile)
+                    for (int jj = 0; jj < CH; ++jj) {
+                        const int j = CH * h + jj;
+                        const float sc = sa * __shfl_sync(0xffffffffu, w_cur[j >> 5], j & 31);
+                        // X0 (exact integer sum) enters hi by TwoSum; X12, 2^-8 of it, goes straight
+                        // into lo with the rounding error (FP32 rounding of lo is ~2^-31 of hi per
+                        // k-tile)
                         const float x = v0[jj] * sc;           // exact (power-of-two scaling)
                         const float s = hi[j] + x, bb = s - hi[j];
                         const float e = (hi[j] - (s - bb)) + (x - bb);
@@ -516,10 +562,12 @@ __global__ void __launch_bounds__(THREADS3, 1)
                 mbar_arrive(&tempty[buf]);
             }
             if (ok && row < rows) {                   // float pairs: no FP64 work here
-                float2 *out = reinterpret_cast<float2 *>(C + (int64_t)ks * ldc_split + (int64_t)grp * ldc_grp + row) +
+                // column c of the item is step c % 64 of group NG gi + c / 64, i.e. at
+                // C + (NG gi) ldc_grp + c ldc_col (ldc_grp = 64 ldc_col)
+                float2 *out = reinterpret_cast<float2 *>(C + (int64_t)ks * ldc_split + (int64_t)NG * gi * ldc_grp + row) +
                               (int64_t)c0 * ldc_col;
 #pragma unroll
-                for (int j = 0; j < EPI_COLS; ++j) out[(int64_t)j * ldc_col] = make_float2(hi[j], lo[j]);
+                for (int j = 0; j < COLS; ++j) out[(int64_t)j * ldc_col] = make_float2(hi[j], lo[j]);
             }
         }
     }
@@ -527,7 +575,7 @@ __global__ void __launch_bounds__(THREADS3, 1)
     __syncthreads();
     if (warp == 1) {
         tc_fence_after();
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM3_COLS));
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(Cfg::TMEM));
     }
 }
 
@@ -601,19 +649,33 @@ int far_plan3_init(FarPlan3 *p, const void *const a[3], int64_t rows, int64_t ld
     static_assert(sizeof(tc::FarMaps3) <= sizeof(p->maps), "map storage");
     tc::FarMaps3 *m = (tc::FarMaps3 *)p->maps;
     int rc;
+    const int64_t w_rows = (int64_t)tc::BN * (w_tiles > 0 ? w_tiles : 1);
     for (int q = 0; q < 3; ++q) {
         if ((rc = tc::make_map(&m->a[q], a[q], rows, lda, tc::BM))) return rc;
-        if ((rc = tc::make_map(&m->w[q], w[q], (int64_t)tc::BN * (w_tiles > 0 ? w_tiles : 1), ldw, tc::BN))) return rc;
+        if ((rc = tc::make_map(&m->w[q], w[q], w_rows, ldw, tc::BN))) return rc;
+        // 128-row weight boxes (two groups per item) exist only when the slices hold two tiles
+        if (w_rows >= 2 * tc::BN) {
+            if ((rc = tc::make_map(&m->w2[q], w[q], w_rows, ldw, 2 * tc::BN))) return rc;
+        } else {
+            m->w2[q] = m->w[q];
+        }
     }
     p->rows = rows;
-    p->w_rows = (int64_t)tc::BN * (w_tiles > 0 ? w_tiles : 1);
+    p->w_rows = w_rows;
     p->idesc = tc::idesc_f16(1, tc::BM, tc::BN);
-    static bool attr_set = false;
-    if (!attr_set) {
-        cudaError_t e = cudaFuncSetAttribute(tc::k_far_tc3, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             tc::SMEM3_BYTES);
+    p->idesc2 = tc::idesc_f16(1, tc::BM, 2 * tc::BN);
+    // the dynamic shared memory opt-in is a per-device attribute
+    static bool attr_set[64] = {false};
+    int dev = 0;
+    FPDE_CUDA(cudaGetDevice(&dev));
+    if (dev >= 64 || !attr_set[dev]) {
+        cudaError_t e = cudaFuncSetAttribute(tc::k_far_tc3<1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             tc::Far3Cfg<1>::SMEM);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(tc::k_far_tc3<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     tc::Far3Cfg<2>::SMEM);
         if (e != cudaSuccess) return set_error(FPDE_ERR_CUDA, "far kernel smem attribute: %s", cudaGetErrorString(e));
-        attr_set = true;
+        if (dev < 64) attr_set[dev] = true;
     }
     return FPDE_OK;
 }
@@ -631,17 +693,26 @@ int far3_launch(cudaStream_t st, const FarPlan3 *p, int k_cols, double *C, int64
     if (splits < 1) splits = 1;
     if (splits > FAR_MAX_SPLITS) splits = FAR_MAX_SPLITS;
     const int kt_per = (kt_total - kt_begin + splits - 1) / splits;   // every split is written, possibly with zeros
-    const int64_t items = (p->rows / tc::BM) * splits * n_grp;
+    // Two weight groups per item (one N = 128 MMA reads the history tile once for both) when the
+    // groups pair up; the item sets of one (row tile, split) are consecutive items, and a grid that
+    // is a multiple of their count keeps them on neighbouring CTAs for the whole walk, so the
+    // history tiles they share stream from HBM once and are re-read from L2.
+    const int ng = (n_grp % 2 == 0) ? 2 : 1;
+    const int n_sets = n_grp / ng;
+    const int64_t items = (p->rows / tc::BM) * splits * n_sets;
     const int sms = device_sm_count();
-    // The n_grp weight groups of one (row tile, split) are consecutive items; a grid that is a
-    // multiple of n_grp keeps them on neighbouring CTAs for the whole walk, so the history tiles
-    // they share stream from HBM once and are re-read from L2.
     int64_t grid = std::min<int64_t>(items, sms);
-    if (grid > n_grp) grid -= grid % n_grp;
+    if (grid > n_sets) grid -= grid % n_sets;
     const tc::FarMaps3 *m = (const tc::FarMaps3 *)p->maps;
-    tc::k_far_tc3<<<(unsigned)grid, tc::THREADS3, tc::SMEM3_BYTES, st>>>(
-        *m, C, ldc_split, ldc_col, p->rows, kt_begin, kt_total, kt_per, splits, p->idesc, pA, pW, ldp, wcol, n_grp,
-        grp0, (int64_t)tc::BN * ldc_col, flags);
+    const int64_t ldc_grp = (int64_t)tc::BN * ldc_col;
+    if (ng == 2)
+        tc::k_far_tc3<2><<<(unsigned)grid, tc::THREADS3, tc::Far3Cfg<2>::SMEM, st>>>(
+            *m, C, ldc_split, ldc_col, p->rows, kt_begin, kt_total, kt_per, splits, p->idesc2, pA, pW, ldp, wcol,
+            n_sets, grp0, ldc_grp, flags);
+    else
+        tc::k_far_tc3<1><<<(unsigned)grid, tc::THREADS3, tc::Far3Cfg<1>::SMEM, st>>>(
+            *m, C, ldc_split, ldc_col, p->rows, kt_begin, kt_total, kt_per, splits, p->idesc, pA, pW, ldp, wcol,
+            n_sets, grp0, ldc_grp, flags);
     FPDE_LAUNCHED(1);
     return FPDE_OK;
 }

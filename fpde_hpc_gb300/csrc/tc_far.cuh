@@ -27,10 +27,10 @@ int far_splits(int kt_total, int64_t rows);
 // ([rows][ldp] int8) and per-(j, k-tile) scales pW = 2^e ([64][ldp] float: the epilogue
 // multiplies by them without rebuilding each power of two).
 struct FarPlan3 {
-    alignas(64) unsigned char maps[6 * 128];
+    alignas(64) unsigned char maps[9 * 128];
     int64_t rows = 0;
     int64_t w_rows = 0;                        // rows of the W slices (64 per weight tile)
-    uint32_t idesc = 0;
+    uint32_t idesc = 0, idesc2 = 0;            // MMA instruction descriptors for N = 64 and 128
 };
 // w_tiles: number of 64-row weight tiles in the W slices (columns of an ensemble; 1 otherwise).
 int far_plan3_init(FarPlan3 *p, const void *const a[3], int64_t rows, int64_t lda, const void *const w[3],
