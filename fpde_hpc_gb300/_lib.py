@@ -100,6 +100,7 @@ _SIGS = {
     "fpde_line_state_ptr": (c_int, [c_vp, C.POINTER(c_vp)]),
     "fpde_line_solve_host": (c_int, [c_vp, c_vp, c_int, c_vp]),
     "fpde_line_steps_done": (c_int, [c_vp, C.POINTER(c_i64)]),
+    "fpde_line_graph_stats": (c_int, [c_vp, C.POINTER(c_int), C.POINTER(c_i64)]),
     "fpde_step_block": (c_int, [c_vp, C.POINTER(c_int)]),
     "fpde_line_coefs": (c_int, [c_i64, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]),
     "fpde_line_set_probe": (c_int, [c_vp, c_int]),

@@ -150,7 +150,8 @@ class Context:
                 alpha=0.0, tstep=0, nodes=None, out=None, sync=True):
         """The reference Sum kernel in history mode sum_alg (0 full, 1 restricted, 2 series
         expansion; fpde_sum). old: (old_size, OS) time-major snapshots (the two newest for
-        sum_alg 2); Htmp: (nodes, ceil(sum_param)) moments, updated in place. Returns S (into
+        sum_alg 2); Htmp: (nodes, int(sum_param)) moments (the reference truncates sum_param),
+        updated in place. Returns S (into
         `out` when given). With device tensors and sync=False the call is stream-ordered on the
         context's stream and returns after launching."""
         dev = _is_dev(old)
@@ -165,9 +166,9 @@ class Context:
         else:
             S = np.zeros(nodes)
         if sum_alg == 2:
-            P = int(np.ceil(sum_param))
+            P = int(sum_param)
             if Htmp is None or tuple(Htmp.shape) != (nodes, P):
-                raise ValueError("Htmp must be (nodes, ceil(sum_param))")
+                raise ValueError("Htmp must be (nodes, int(sum_param))")
             if not (Htmp.flags["C_CONTIGUOUS"] if not dev else Htmp.is_contiguous()):
                 raise ValueError("Htmp must be contiguous")
             row2 = _f64(row2)
@@ -319,6 +320,12 @@ class Line:
         n = C.c_int64()
         check(self.ctx.lib.fpde_line_steps_done(self.h, C.byref(n)), "fpde_line_steps_done")
         return n.value
+
+    def graph_stats(self):
+        """fpde_line_graph_stats: (graphs cached now, graphs instantiated since creation)."""
+        c, n = C.c_int(), C.c_int64()
+        check(self.ctx.lib.fpde_line_graph_stats(self.h, C.byref(c), C.byref(n)), "fpde_line_graph_stats")
+        return c.value, n.value
 
     def step_block(self):
         """fpde_step_block: advance to the next 64-step block boundary; returns the steps run."""

@@ -28,6 +28,7 @@
 
 #include "common.cuh"
 #include "kernels.cuh"
+#include "graph_cache.cuh"
 #include "scan.cuh"
 #include "tc_far.cuh"
 #include "ff.cuh"
@@ -269,8 +270,7 @@ struct fpde_batch {
     int *wcol = nullptr;
     FarPlan3 plan3;
     int64_t n_done = 0;
-    std::map<std::pair<int64_t, int>, cudaGraphExec_t> graphs;
-    std::map<std::pair<int64_t, int>, int64_t> graph_launches;
+    GraphCache<int> graphs;                        // captured runs (at least GRAPH_MIN_STEPS steps)
 };
 
 namespace fpde {
@@ -347,7 +347,7 @@ int fpde_batch_destroy(fpde_batch *b)
         cudaSetDevice(b->ctx->device);
         cudaStreamSynchronize(b->ctx->stream);
     }
-    for (auto &kv : b->graphs) cudaGraphExecDestroy(kv.second);
+    b->graphs.clear();
     for (double *p : {b->A, b->g, b->al, b->segP, b->segQ, b->KF, b->CB, b->U, b->U0, b->Y, b->D, b->part, b->wall, b->ring,
                       b->cfar, b->wlag, b->Sn})
         dev_free(p);
@@ -587,30 +587,20 @@ int fpde_batch_run(fpde_batch *b, int steps)
     if (steps == 0) return FPDE_OK;
     if (b->n_done + steps > b->max_steps)
         return set_error(FPDE_ERR_CAPACITY, "run of %d steps exceeds the history capacity %d", steps, b->max_steps);
-    auto key = std::make_pair(b->n_done, steps);
-    auto it = b->graphs.find(key);
-    if (it == b->graphs.end()) {
-        cudaStream_t cs;
-        FPDE_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
-        cudaGraph_t graph;
-        FPDE_CUDA(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
+    if (steps < GRAPH_MIN_STEPS) {                 // short runs: enqueued directly, no graph
         int64_t nk = 0;
-        const int64_t before = fpde_kernel_launch_count();
-        rc = batch_enqueue(b, cs, b->n_done, steps, &nk);
-        cudaError_t e = cudaStreamEndCapture(cs, &graph);
-        count_launches(-(fpde_kernel_launch_count() - before));           // counted at replay
-        cudaStreamDestroy(cs);
-        if (rc) return rc;
-        if (e != cudaSuccess) return set_error(FPDE_ERR_CUDA, "graph capture: %s", cudaGetErrorString(e));
-        cudaGraphExec_t exec;
-        e = cudaGraphInstantiate(&exec, graph, 0);
-        cudaGraphDestroy(graph);
-        if (e != cudaSuccess) return set_error(FPDE_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(e));
-        it = b->graphs.emplace(key, exec).first;
-        b->graph_launches[key] = nk;
+        if ((rc = batch_enqueue(b, b->ctx->stream, b->n_done, steps, &nk))) return rc;
+    } else {
+        auto *g = b->graphs.find(b->n_done, steps);
+        if (!g) {
+            rc = b->graphs.capture(b->n_done, steps,
+                                   [&](cudaStream_t cs, int64_t *nk, int *) { return batch_enqueue(b, cs, b->n_done, steps, nk); },
+                                   &g);
+            if (rc) return rc;
+        }
+        FPDE_CUDA(cudaGraphLaunch(g->exec, b->ctx->stream));
+        count_launches(g->launches);
     }
-    FPDE_CUDA(cudaGraphLaunch(it->second, b->ctx->stream));
-    count_launches(b->graph_launches[key]);
     b->n_done += steps;
     return FPDE_OK;
 }

@@ -226,6 +226,20 @@ int device_sm_count()
     return sms;
 }
 
+cudaError_t smem_opt_in(const void *fn, int bytes)
+{
+    static std::mutex mu;
+    static std::set<std::pair<int, const void *>> done;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    std::lock_guard<std::mutex> lock(mu);
+    if (done.count({dev, fn})) return cudaSuccess;
+    e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    if (e == cudaSuccess) done.insert({dev, fn});
+    return e;
+}
+
 int choose_splits(int n, int64_t P)
 {
     // Split the rows so that ~32 CTAs per SM are in flight (the stream needs many loads

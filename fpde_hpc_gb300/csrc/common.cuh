@@ -76,6 +76,9 @@ namespace fpde {
 int ctx_enter(fpde_ctx *ctx);
 // Streaming multiprocessors of the current device (queried once per device).
 int device_sm_count();
+// Opt kernel `fn` in to `bytes` of dynamic shared memory on the current device (the attribute is
+// per device: done once per (device, kernel) and remembered).
+cudaError_t smem_opt_in(const void *fn, int bytes);
 // Allocate/free device memory (returns FPDE_ERR_NOMEM on failure).
 int dev_alloc(void **p, size_t bytes);
 void dev_free(void *p);

@@ -36,6 +36,7 @@
 
 #include "common.cuh"
 #include "kernels.cuh"
+#include "graph_cache.cuh"
 #include "tc_far.cuh"
 #include "scan.cuh"
 #include "ff.cuh"
@@ -1067,14 +1068,13 @@ struct fpde_line {
     int64_t ldp = 0;
     FarPlan3 plan3;
     int64_t n_done = 0;
-    std::map<std::pair<int64_t, int>, cudaGraphExec_t> graphs;
-    std::map<std::pair<int64_t, int>, int64_t> graph_launches;
+    int graph_min = GRAPH_MIN_STEPS;          // shortest run replayed from a graph
     // probes: CUDA events around kernels inside the captured graph
     struct Probe { int kind; int64_t n; double bytes, flops; int ev; int steps; };
     int probe_every = 0;
     std::vector<cudaEvent_t> probe_ev;
     std::vector<Probe> probes;                            // recorded by the last enqueue
-    std::map<std::pair<int64_t, int>, std::vector<Probe>> graph_probes;
+    GraphCache<std::vector<Probe>> graphs;                // captured runs and their probe records
     std::vector<Probe> last_probes;
 };
 
@@ -1130,25 +1130,22 @@ static cudaEvent_t *probe_begin(fpde_line *L, int kind, int64_t n, double bytes,
     return &L->probe_ev[2 * k];
 }
 
-// Opt the speculative kernels in to their dynamic shared memory (the row ring) once.
+// Opt the speculative kernels in to their dynamic shared memory (the row ring) on this device.
 static cudaError_t spec_smem_attrs()
 {
-    static cudaError_t done = [] {
-        cudaError_t e = cudaSuccess;
-        auto opt = [&e](const void *fn, size_t bytes) {
-            if (e == cudaSuccess) e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
-        };
-        opt((const void *)k_line_block_spec<1, false>, SpecRing<1>::bytes);
-        opt((const void *)k_line_block_spec<2, false>, SpecRing<2>::bytes);
-        opt((const void *)k_line_block_spec<4, false>, SpecRing<4>::bytes);
-        opt((const void *)k_line_block_spec<8, false>, SpecRing<8>::bytes);
-        opt((const void *)k_line_block_spec<1, true>, SpecRing<1>::bytes);
-        opt((const void *)k_line_block_spec<2, true>, SpecRing<2>::bytes);
-        opt((const void *)k_line_block_spec<4, true>, SpecRing<4>::bytes);
-        opt((const void *)k_line_block_spec<8, true>, SpecRing<8>::bytes);
-        return e;
-    }();
-    return done;
+    cudaError_t e = cudaSuccess;
+    auto opt = [&e](const void *fn, size_t bytes) {
+        if (e == cudaSuccess) e = smem_opt_in(fn, (int)bytes);
+    };
+    opt((const void *)k_line_block_spec<1, false>, SpecRing<1>::bytes);
+    opt((const void *)k_line_block_spec<2, false>, SpecRing<2>::bytes);
+    opt((const void *)k_line_block_spec<4, false>, SpecRing<4>::bytes);
+    opt((const void *)k_line_block_spec<8, false>, SpecRing<8>::bytes);
+    opt((const void *)k_line_block_spec<1, true>, SpecRing<1>::bytes);
+    opt((const void *)k_line_block_spec<2, true>, SpecRing<2>::bytes);
+    opt((const void *)k_line_block_spec<4, true>, SpecRing<4>::bytes);
+    opt((const void *)k_line_block_spec<8, true>, SpecRing<8>::bytes);
+    return e;
 }
 
 template <int SP>
@@ -1204,7 +1201,7 @@ static int line_launch_block(fpde_line *L, cudaStream_t st, int64_t nb0, int j0,
 }
 
 #define PROBE_REC(ev, i) \
-    do { if (ev) FPDE_CUDA(cudaEventRecordWithFlags((ev)[i], st, cudaEventRecordExternal)); } while (0)
+    do { if (ev) FPDE_CUDA(record_probe_event((ev)[i], st)); } while (0)
 
 // Enqueue steps [n0, n0+steps) on st; returns the number of kernels enqueued via *nk.
 static int line_enqueue(fpde_line *L, cudaStream_t st, int64_t n0, int steps, int64_t *nk)
@@ -1362,7 +1359,7 @@ int fpde_line_destroy(fpde_line *L)
         cudaStreamSynchronize(L->ctx->stream);
         L->ctx->lines.erase(L);
     }
-    for (auto &kv : L->graphs) cudaGraphExecDestroy(kv.second);
+    L->graphs.clear();
     for (cudaEvent_t e : L->probe_ev) cudaEventDestroy(e);
     dev_free(L->cflag);
     dev_free(L->seq);
@@ -1906,32 +1903,27 @@ int fpde_line_run(fpde_line *L, int steps)
     if (L->n_done + steps > L->max_steps)
         return set_error(FPDE_ERR_CAPACITY, "run of %d steps exceeds the history capacity %d", steps, L->max_steps);
     cudaStream_t st = L->ctx->stream;
-    auto key = std::make_pair(L->n_done, steps);
-    auto it = L->graphs.find(key);
-    if (it == L->graphs.end()) {
-        cudaStream_t cs;
-        FPDE_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
-        cudaGraph_t graph;
-        FPDE_CUDA(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
+    if (steps < L->graph_min) {                  // short runs: enqueued directly, no graph
         int64_t nk = 0;
-        int64_t before = fpde_kernel_launch_count();
-        rc = line_enqueue(L, cs, L->n_done, steps, &nk);
-        cudaError_t e = cudaStreamEndCapture(cs, &graph);
-        fpde::count_launches(-(fpde_kernel_launch_count() - before));   // counted at replay
-        cudaStreamDestroy(cs);
-        if (rc) return rc;
-        if (e != cudaSuccess) return set_error(FPDE_ERR_CUDA, "graph capture: %s", cudaGetErrorString(e));
-        cudaGraphExec_t exec;
-        e = cudaGraphInstantiate(&exec, graph, 0);
-        cudaGraphDestroy(graph);
-        if (e != cudaSuccess) return set_error(FPDE_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(e));
-        it = L->graphs.emplace(key, exec).first;
-        L->graph_launches[key] = nk;
-        L->graph_probes[key] = L->probes;
+        if ((rc = line_enqueue(L, st, L->n_done, steps, &nk))) return rc;
+        L->last_probes = L->probes;
+        L->n_done += steps;
+        return FPDE_OK;
     }
-    L->last_probes = L->graph_probes[key];
-    FPDE_CUDA(cudaGraphLaunch(it->second, st));
-    count_launches(L->graph_launches[key]);
+    auto *g = L->graphs.find(L->n_done, steps);
+    if (!g) {
+        rc = L->graphs.capture(L->n_done, steps,
+                               [&](cudaStream_t cs, int64_t *nk, std::vector<fpde_line::Probe> *probes) {
+                                   const int r = line_enqueue(L, cs, L->n_done, steps, nk);
+                                   *probes = L->probes;
+                                   return r;
+                               },
+                               &g);
+        if (rc) return rc;
+    }
+    L->last_probes = g->aux;
+    FPDE_CUDA(cudaGraphLaunch(g->exec, st));
+    count_launches(g->launches);
     L->n_done += steps;
     return FPDE_OK;
 }
@@ -1977,10 +1969,7 @@ int fpde_line_set_probe(fpde_line *L, int every)
     int rc = ctx_enter(L->ctx);
     if (rc) return rc;
     FPDE_CUDA(cudaStreamSynchronize(L->ctx->stream));
-    for (auto &kv : L->graphs) cudaGraphExecDestroy(kv.second);
     L->graphs.clear();
-    L->graph_launches.clear();
-    L->graph_probes.clear();
     L->last_probes.clear();
     for (cudaEvent_t e : L->probe_ev) cudaEventDestroy(e);
     L->probe_ev.clear();
@@ -2016,6 +2005,14 @@ int fpde_line_probe_stats(fpde_line *L, int kind, double *ms, double *bytes, dou
     *bytes = b;
     *flops = f;
     *count = c;
+    return FPDE_OK;
+}
+
+int fpde_line_graph_stats(const fpde_line *L, int *cached, int64_t *instantiated)
+{
+    FPDE_CHECK_ARG(L && cached && instantiated, "null argument");
+    *cached = (int)L->graphs.entries.size();
+    *instantiated = L->graphs.instantiated;
     return FPDE_OK;
 }
 
@@ -2106,6 +2103,7 @@ extern "C" int fpde_line_autotune(fpde_ctx *ctx, const fpde_line_desc *desc, con
             clear_error();
             continue;
         }
+        L->graph_min = 1;                                       // time graph replays, not launches
         bool ok = fpde_line_run(L, first) == FPDE_OK && fpde_line_run(L, tsteps - first) == FPDE_OK &&
                   fpde_line_reset(L, u0, 0) == FPDE_OK && fpde_line_run(L, first) == FPDE_OK;
         float ms = 0.f;

@@ -34,6 +34,7 @@
 
 #include "common.cuh"
 #include "kernels.cuh"
+#include "graph_cache.cuh"
 #include "tc_far.cuh"
 #include "ff.cuh"
 
@@ -350,8 +351,7 @@ struct fpde_lod3d {
     float2 *ringf = nullptr, *wff = nullptr;  // the ring and the lag weights as float pairs
     FarPlan3 plan3;
     int64_t n_done = 0;
-    std::map<std::pair<int64_t, int>, cudaGraphExec_t> graphs;
-    std::map<std::pair<int64_t, int>, int64_t> graph_launches;
+    GraphCache<int> graphs;                        // captured runs (at least GRAPH_MIN_STEPS steps)
 };
 
 namespace fpde {
@@ -532,7 +532,7 @@ int fpde_lod3d_destroy(fpde_lod3d *L)
         cudaSetDevice(L->ctx->device);
         cudaStreamSynchronize(L->ctx->stream);
     }
-    for (auto &kv : L->graphs) cudaGraphExecDestroy(kv.second);
+    L->graphs.clear();
     dev_free(L->ringf);
     dev_free(L->wff);
     for (double *p : {L->U, L->last, L->D, L->part, L->wrev, L->rp, L->bc, L->ring, L->cfar, L->wlag, L->Sn, L->H})
@@ -792,30 +792,20 @@ int fpde_lod3d_run(fpde_lod3d *L, int steps)
     if (steps == 0) return FPDE_OK;
     if (L->n_done + steps > L->max_steps)
         return set_error(FPDE_ERR_CAPACITY, "run of %d steps exceeds the history capacity %d", steps, L->max_steps);
-    auto key = std::make_pair(L->n_done, steps);
-    auto it = L->graphs.find(key);
-    if (it == L->graphs.end()) {
-        cudaStream_t cs;
-        FPDE_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
-        cudaGraph_t graph;
-        FPDE_CUDA(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
+    if (steps < GRAPH_MIN_STEPS) {                 // short runs: enqueued directly, no graph
         int64_t nk = 0;
-        const int64_t before = fpde_kernel_launch_count();
-        rc = lod_enqueue(L, cs, L->n_done, steps, &nk);
-        cudaError_t e = cudaStreamEndCapture(cs, &graph);
-        count_launches(-(fpde_kernel_launch_count() - before));         // counted at replay
-        cudaStreamDestroy(cs);
-        if (rc) return rc;
-        if (e != cudaSuccess) return set_error(FPDE_ERR_CUDA, "graph capture: %s", cudaGetErrorString(e));
-        cudaGraphExec_t exec;
-        e = cudaGraphInstantiate(&exec, graph, 0);
-        cudaGraphDestroy(graph);
-        if (e != cudaSuccess) return set_error(FPDE_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(e));
-        it = L->graphs.emplace(key, exec).first;
-        L->graph_launches[key] = nk;
+        if ((rc = lod_enqueue(L, L->ctx->stream, L->n_done, steps, &nk))) return rc;
+    } else {
+        auto *g = L->graphs.find(L->n_done, steps);
+        if (!g) {
+            rc = L->graphs.capture(L->n_done, steps,
+                                   [&](cudaStream_t cs, int64_t *nk, int *) { return lod_enqueue(L, cs, L->n_done, steps, nk); },
+                                   &g);
+            if (rc) return rc;
+        }
+        FPDE_CUDA(cudaGraphLaunch(g->exec, L->ctx->stream));
+        count_launches(g->launches);
     }
-    FPDE_CUDA(cudaGraphLaunch(it->second, L->ctx->stream));
-    count_launches(L->graph_launches[key]);
     L->n_done += steps;
     return FPDE_OK;
 }

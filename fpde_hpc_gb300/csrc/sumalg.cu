@@ -160,9 +160,11 @@ int fpde_sum(fpde_ctx *ctx, int sum_alg, int bs, int64_t OS, int64_t nodes, doub
     FPDE_CHECK_ARG(on_device >= 0 && on_device <= 2, "on_device must be 0, 1 or 2");
     FPDE_CHECK_ARG(S && old && old_size >= 1 && nodes > 0 && OS >= nodes, "bad arguments");
     FPDE_CHECK_ARG(sum_alg != 1 || (bs >= 0 && bs <= 65536), "bs must be 0 .. 65536");
-    const int P = sum_alg == 2 ? (int)std::ceil(sum_param) : 0;
+    // the reference truncates: (int)sum_param moments (time_summing :4137, Sum kernel :1462-1474)
+    const int P = (sum_alg == 2 && std::isfinite(sum_param) && sum_param >= 1.0 && sum_param < 1e9)
+                      ? (int)sum_param : 0;
     if (sum_alg == 2) {
-        FPDE_CHECK_ARG(std::isfinite(sum_param) && P >= 1 && P <= SERIES_PMAX,
+        FPDE_CHECK_ARG(P >= 1 && P <= SERIES_PMAX,
                        "sum_alg 2: sum_param (moments per node) must be 1 .. 128");
         FPDE_CHECK_ARG(Htmp && row2_precalc && tau && tstep >= 0, "sum_alg 2: Htmp, row2_precalc and tau required");
     } else {
@@ -214,12 +216,7 @@ int fpde_sum(fpde_ctx *ctx, int sum_alg, int bs, int64_t OS, int64_t nodes, doub
                 v *= -(-alpha - i + 1.0) / (i * gtj);
             }
             const size_t smem = series_smem(P);
-            static bool opted = false;
-            if (!opted) {
-                e = cudaFuncSetAttribute(k_sum_series, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)series_smem(SERIES_PMAX));
-                opted = e == cudaSuccess;
-            }
+            e = smem_opt_in((const void *)k_sum_series, (int)series_smem(SERIES_PMAX));
             if (e == cudaSuccess) {
                 const double *tt = on_device ? dtau + tstep : dtau;
                 k_sum_series<<<(unsigned)((nodes + SS_T - 1) / SS_T), SS_T, smem, st>>>(dS, dold, OS, nodes, dH, P,

@@ -632,12 +632,8 @@ int far_plan_init(FarPlan *p, const void *a_hi, const void *a_lo, int64_t rows, 
         return rc;
     p->rows = rows;
     p->idesc = tc::idesc_f16(bf16 ? 1 : 0, tc::BM, tc::BN);
-    static bool attr_set = false;
-    if (!attr_set) {
-        cudaError_t e = cudaFuncSetAttribute(tc::k_far_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, tc::SMEM_BYTES);
-        if (e != cudaSuccess) return set_error(FPDE_ERR_CUDA, "far kernel smem attribute: %s", cudaGetErrorString(e));
-        attr_set = true;
-    }
+    cudaError_t e = smem_opt_in((const void *)tc::k_far_tc, tc::SMEM_BYTES);
+    if (e != cudaSuccess) return set_error(FPDE_ERR_CUDA, "far kernel smem attribute: %s", cudaGetErrorString(e));
     return FPDE_OK;
 }
 
@@ -664,19 +660,9 @@ int far_plan3_init(FarPlan3 *p, const void *const a[3], int64_t rows, int64_t ld
     p->w_rows = w_rows;
     p->idesc = tc::idesc_f16(1, tc::BM, tc::BN);
     p->idesc2 = tc::idesc_f16(1, tc::BM, 2 * tc::BN);
-    // the dynamic shared memory opt-in is a per-device attribute
-    static bool attr_set[64] = {false};
-    int dev = 0;
-    FPDE_CUDA(cudaGetDevice(&dev));
-    if (dev >= 64 || !attr_set[dev]) {
-        cudaError_t e = cudaFuncSetAttribute(tc::k_far_tc3<1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             tc::Far3Cfg<1>::SMEM);
-        if (e == cudaSuccess)
-            e = cudaFuncSetAttribute(tc::k_far_tc3<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     tc::Far3Cfg<2>::SMEM);
-        if (e != cudaSuccess) return set_error(FPDE_ERR_CUDA, "far kernel smem attribute: %s", cudaGetErrorString(e));
-        if (dev < 64) attr_set[dev] = true;
-    }
+    cudaError_t e = smem_opt_in((const void *)tc::k_far_tc3<1>, tc::Far3Cfg<1>::SMEM);
+    if (e == cudaSuccess) e = smem_opt_in((const void *)tc::k_far_tc3<2>, tc::Far3Cfg<2>::SMEM);
+    if (e != cudaSuccess) return set_error(FPDE_ERR_CUDA, "far kernel smem attribute: %s", cudaGetErrorString(e));
     return FPDE_OK;
 }
 

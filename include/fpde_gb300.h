@@ -191,7 +191,8 @@ int fpde_sum_snapshots(fpde_ctx *ctx, double *S, const double *old, int old_size
  *                bs  > 0: the GPU kernel's rule with BS = bs: whole chunks of bs terms (weights
  *                         before t = 0 count as 0), stopping after the first chunk whose bs
  *                         weights are all below sum_param.
- *   sum_alg 2: series expansion (:4137-4151, :1457-1475) with P = ceil(sum_param) (1..128)
+ *   sum_alg 2: series expansion (:4137-4151, :1457-1475) with P = (int)sum_param (1..128; the
+ *              reference's truncation)
  *              moments per node in Htmp[id*P + j] (updated in place), from the two snapshots
  *              old[0..OS) and old[OS..2*OS) (old_size >= 2; otherwise S = 0 and Htmp unchanged):
  *                d = old[OS+id] - old[id]
@@ -323,7 +324,8 @@ int fpde_line_destroy(fpde_line *line);
 /* Reset to the state u0 (N+1 values, host or device) and an empty history. */
 int fpde_line_reset(fpde_line *line, const double *u0, int on_device);
 /* Advance `steps` time steps (calc_step / U1 per step, fpde_hpc_1d.cpp:5100-5135, with the
- * history applied every step). The whole loop is one CUDA graph. */
+ * history applied every step). Runs of at least 128 steps replay one CUDA graph (see
+ * fpde_line_graph_stats); shorter runs are enqueued directly on the context's stream. */
 int fpde_line_run(fpde_line *line, int steps);
 /* Copy the state (N+1 values) out. */
 int fpde_line_get_state(fpde_line *line, double *u, int on_device);
@@ -331,6 +333,12 @@ int fpde_line_get_state(fpde_line *line, double *u, int on_device);
 int fpde_line_state_ptr(fpde_line *line, double **u_dev);
 /* End-to-end call: upload u0 from host, run `steps`, download the final state to host. */
 int fpde_line_solve_host(fpde_line *line, const double *u0_host, int steps, double *u_out_host);
+/* CUDA graphs of the line (no counterpart in the reference, which launches every kernel itself):
+ * runs of at least 128 steps are captured once per (first step, steps) and replayed; at most 8
+ * instantiated graphs are kept (least recently used evicted). Shorter runs are enqueued directly,
+ * so a per-step or per-block caller instantiates none. *cached = graphs held now, *instantiated =
+ * graphs instantiated since the line was created. */
+int fpde_line_graph_stats(const fpde_line *line, int *cached, int64_t *instantiated);
 /* Current step count. */
 int fpde_line_steps_done(const fpde_line *line, int64_t *n);
 /* One block of the blocked schedule: advance to the next multiple of FPDE_BLOCK_STEPS (64) steps
@@ -407,7 +415,8 @@ typedef struct fpde_lod3d_desc {
 int fpde_lod3d_create(fpde_ctx *ctx, const fpde_lod3d_desc *desc, const double *coefA, const double *coefB,
                       const double *coefRlap, const double *u0, fpde_lod3d **out);
 int fpde_lod3d_destroy(fpde_lod3d *lod);
-/* Advance `steps` steps (one CUDA graph per (start, steps)). */
+/* Advance `steps` steps (runs of at least 128 steps replay a cached CUDA graph per (start, steps),
+ * at most 8 kept; shorter runs are enqueued directly). */
 int fpde_lod3d_run(fpde_lod3d *lod, int steps);
 int fpde_lod3d_get_state(fpde_lod3d *lod, double *u, int on_device);
 /* New initial grid and an empty history. */

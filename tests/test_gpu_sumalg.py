@@ -62,7 +62,7 @@ def test_series_replays_reference_run(ctx):
     import torch
     g = fgv.load(golden_path("fpde_column_alg2"))
     U, m = g["U"], _interior(g)
-    P = int(np.ceil(g["sum_param"]))
+    P = int(g["sum_param"])
     G = U.shape[1] * U.shape[2] * U.shape[3]
     H = torch.zeros((G, P), dtype=torch.float64, device="cuda")
     tau = torch.from_numpy(g["tau"].copy()).cuda()
@@ -135,6 +135,22 @@ def test_series_vs_oracle(ctx, P, nodes):
         assert relmax(S, ref) <= RTOL, n
         assert relmax(H, Href) <= RTOL, n
         u = un
+
+
+def test_series_truncates_fractional_sum_param(ctx):
+    """sum_param = 16.5 keeps 16 moments, as the reference's (int)sum_param (time_summing :4137,
+    Sum kernel :1462-1474): the same sums and moments as sum_param = 16."""
+    rng = np.random.default_rng(5)
+    nodes, alpha, tau = 2000, 0.6, np.full(4, 1e-3)
+    u, un = rng.standard_normal(nodes), rng.standard_normal(nodes)
+    row2 = 1.0 / np.arange(1.0, 17.0)
+    H1, H2 = np.zeros((nodes, 16)), np.zeros((nodes, 16))
+    S1 = ctx.sum_alg(2, np.stack([u, un]), tau, sum_param=16, Htmp=H1, row2=row2, gtj=0.003, gt=0.002,
+                     alpha=alpha, tstep=2)
+    S2 = ctx.sum_alg(2, np.stack([u, un]), tau, sum_param=16.5, Htmp=H2, row2=row2, gtj=0.003, gt=0.002,
+                     alpha=alpha, tstep=2)
+    np.testing.assert_array_equal(S1, S2)
+    np.testing.assert_array_equal(H1, H2)
 
 
 def test_series_guards_and_device_buffers(ctx):

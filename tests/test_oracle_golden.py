@@ -171,7 +171,7 @@ def test_sum_series_matches_reference_run():
     carried from step to step from zero, every step's history sum bit for bit."""
     g = fgv.load(golden_path("fpde_column_alg2"))
     U, m = g["U"], _interior(g)
-    H = np.zeros((U.shape[1] * U.shape[2] * U.shape[3], int(np.ceil(g["sum_param"]))))
+    H = np.zeros((U.shape[1] * U.shape[2] * U.shape[3], int(g["sum_param"])))
     for n in range(1, U.shape[0]):
         prev = (g["U0"] if n == 1 else U[n - 2]).reshape(-1)
         S = oracle.sum_series(prev, U[n - 1].reshape(-1), H, g["row2"][n], g["gt"][n], g["gtj"][n], g["alpha"],

@@ -6,7 +6,8 @@ cudaMalloc/cudaFree) pass their own device buffers; the library keeps its split-
 in a fixed array compiled into it. This file is named so that pytest collects it last.
 The check: through the C ABI, two calls in a row (different history lengths and weights,
 so the second call runs over the first call's leftover partials) must equal the allocating
-entry point fpde_l1_sum within the FP64 tolerance of the other parity tests (1e-12).
+entry point fpde_l1_sum within the FP64 tolerance of the other parity tests (1e-12), and
+later calls must leave the device's free memory unchanged.
 """
 import ctypes as C
 
@@ -53,6 +54,17 @@ def test_noalloc_sum_equals_allocating_entry_point_twice():
             fp.check(rc, "fpde_l1_sum_noalloc")
             torch.cuda.synchronize()
             assert relmax(Sdev.cpu().numpy(), Sref) <= RTOL, n
+        # after the first call (which looked up the scratch array's address), further calls take
+        # no device memory: the free memory the driver reports does not move
+        w = torch.from_numpy(np.linspace(0.5, 1.5, steps)).cuda()
+        torch.cuda.synchronize()
+        free0 = torch.cuda.mem_get_info()[0]
+        for nrows in (steps, 17, steps // 2):
+            rc = lib.fpde_l1_sum_noalloc(C.c_void_p(Ddev.data_ptr()), nrows, P, nodes,
+                                         C.c_void_p(w.data_ptr()), C.c_void_p(Sdev.data_ptr()), None)
+            fp.check(rc, "fpde_l1_sum_noalloc")
+        torch.cuda.synchronize()
+        assert torch.cuda.mem_get_info()[0] == free0
 
 
 def test_noalloc_rejects_pitch_beyond_scratch():
