@@ -396,24 +396,24 @@ int fo_lod_step(int sN, int M, int K, double *U, double *hist, int n,
     int L = sN; if (M > L) L = M; if (K > L) L = K;
     double *Uold = (double *)malloc(sizeof(double) * (size_t)G);
     double *S = (double *)calloc((size_t)G, sizeof(double));
-    double *la = (double *)malloc(sizeof(double) * (size_t)(L + 2));
-    double *lb = (double *)malloc(sizeof(double) * (size_t)(L + 2));
-    double *lr = (double *)malloc(sizeof(double) * (size_t)(L + 2));
-    double *lo = (double *)malloc(sizeof(double) * (size_t)(L + 2));
-    double *lu = (double *)malloc(sizeof(double) * (size_t)(L + 2));
-    double *Al = (double *)malloc(sizeof(double) * (size_t)(L + 2));
-    double *Bt = (double *)malloc(sizeof(double) * (size_t)(L + 2));
     memcpy(Uold, U, sizeof(double) * (size_t)G);
-    /* history sum on the K-pass nodes (time_summing is evaluated for k = 1..K) */
-    if (n > 0)
-        for (int i = 1; i < sN; i++)
-            for (int j = 1; j < M; j++)
-                for (int k = 1; k <= K; k++) {
-                    int64_t id = i * sx + j * sy + k * sz;
-                    double s = 0.0;
-                    for (int t = n - 1; t >= 0; t--) s += kb[t] * hist[(int64_t)t * G + id] / tau[t];
-                    S[id] = s;
-                }
+    /* history sum on the K-pass nodes (time_summing is evaluated for k = 1..K): every node's sum
+     * runs from t = n-1 down to 0 in the reference's order, s = 0 then s += kb[t]*D/tau[t]; the
+     * loops visit t outside the nodes so that each row is read contiguously (same per-node order
+     * and rounding), k-planes in parallel */
+    if (n > 0) {
+#pragma omp parallel for schedule(static)
+        for (int k = 1; k <= K; k++)
+            for (int t = n - 1; t >= 0; t--) {
+                const double *h = hist + (int64_t)t * G;
+                const double c = kb[t], tt = tau[t];
+                for (int j = 1; j < M; j++)
+                    for (int i = 1; i < sN; i++) {
+                        const int64_t id = i * sx + j * sy + k * sz;
+                        S[id] += c * h[id] / tt;
+                    }
+            }
+    }
     /* passes in the order of calc_step: K (c=2), _M (c=1), sN (c=0) */
     for (int pass = 2; pass >= 0; pass--) {
         int Nl = pass == 2 ? K : (pass == 1 ? M : sN);
@@ -422,6 +422,17 @@ int fo_lod_step(int sN, int M, int K, double *U, double *hist, int n,
         const double *cR = coefRlap + (int64_t)pass * G;
         int na = pass == 2 ? sN : (pass == 1 ? sN : M);     /* first line index range */
         int nb = pass == 2 ? M : K;                          /* second line index range */
+        /* the lines of a pass are independent: in parallel, each thread with its own line arrays */
+#pragma omp parallel
+        {
+        double *la = (double *)malloc(sizeof(double) * (size_t)(L + 2));
+        double *lb = (double *)malloc(sizeof(double) * (size_t)(L + 2));
+        double *lr = (double *)malloc(sizeof(double) * (size_t)(L + 2));
+        double *lo = (double *)malloc(sizeof(double) * (size_t)(L + 2));
+        double *lu = (double *)malloc(sizeof(double) * (size_t)(L + 2));
+        double *Al = (double *)malloc(sizeof(double) * (size_t)(L + 2));
+        double *Bt = (double *)malloc(sizeof(double) * (size_t)(L + 2));
+#pragma omp for schedule(static) collapse(2)
         for (int a = 1; a < na; a++)
             for (int b = 1; b < nb; b++) {
                 int64_t base;
@@ -440,11 +451,13 @@ int fo_lod_step(int sN, int M, int K, double *U, double *hist, int n,
                 lu[Nl + 1] = lu[Nl];                                 /* U1 :4792 */
                 for (int p = 0; p <= Nl + 1; p++) U[base + p * st] = lu[p];
             }
+        free(la); free(lb); free(lr); free(lo); free(lu); free(Al); free(Bt);
+        }
     }
     double *row = hist + (int64_t)n * G;
     for (int64_t q = 0; q < G; q++) row[q] = U[q] - Uold[q];
     if (S_out) memcpy(S_out, S, sizeof(double) * (size_t)G);
-    free(Uold); free(S); free(la); free(lb); free(lr); free(lo); free(lu); free(Al); free(Bt);
+    free(Uold); free(S);
     return 0;
 }
 
