@@ -138,13 +138,33 @@ class ClockSampler:
 
 # ------------------------------------------------------------------ workloads
 
-def _fit_quadratic(ts, ss, S):
-    (t1, t2), (s1, s2) = ts, ss
-    b = (t2 / s2 - t1 / s1) / (s2 - s1)
-    a = t1 / s1 - b * s1
-    if b <= 0:          # timing noise: linear model through the longer sample
-        a, b = t2 / s2, 0.0
-    return a * S + b * S * S
+def cpu_fit(samples, S):
+    """Least-squares fit of t(s) = a s + b s^2 to timed samples [(s, seconds), ...] (the history
+    term makes the cost quadratic in the step count) and its extrapolation to S steps. Returns
+    (T(S), a, b, relative rms residual of the samples)."""
+    s = np.array([x for x, _ in samples], dtype=np.float64)
+    t = np.array([y for _, y in samples], dtype=np.float64)
+    M = np.stack([s, s * s], axis=1)
+    (a, b), *_ = np.linalg.lstsq(M / t[:, None], np.ones_like(t), rcond=None)   # relative residuals
+    if b < 0:                                   # timing noise: linear model
+        a, b = float(np.sum(t * s) / np.sum(s * s)), 0.0
+    fit = a * s + b * s * s
+    resid = float(np.sqrt(np.mean(((fit - t) / t) ** 2)))
+    return float(a * S + b * S * S), float(a), float(b), resid
+
+
+def cpu_record(wl, samples, threads):
+    """cpu_baseline / reference-arm record from timed samples of the workload's CPU oracle."""
+    T, a, b, resid = cpu_fit(samples, wl.steps)
+    scale = getattr(wl, "sample_scale", 1.0)
+    T *= scale
+    lens = sorted({s for s, _ in samples})
+    return {"value": wl.node_steps / T, "unit": "node-steps/s", "cores": threads, "kind": "port",
+            "sample": wl.sample_desc(lens), "extrapolated": True,
+            "fit": {"model": "t(S) = a S + b S^2 (seconds)", "a": a, "b": b, "relative_rms_residual": resid,
+                    "samples": [{"steps": int(s), "seconds": float(t)} for s, t in samples],
+                    "extrapolated_to_steps": wl.steps, "scale": scale, "seconds_per_solve": T},
+            "seconds_timed": float(sum(t for _, t in samples))}
 
 
 def _oracle():
@@ -227,25 +247,28 @@ class LineWorkload:
     def steps(self):
         return self.p.steps
 
-    def cpu_rate(self, threads, s1=512, s2=1536):
+    def sample_lengths(self):
+        """Step counts of the timed CPU samples (the first steps of the full-size line)."""
+        S = self.p.steps
+        return [max(1, min(256, S // 8)), max(2, min(512, S // 4)), max(3, min(1024, S // 2))]
+
+    def run_sample(self, s, threads):
+        """Seconds for the oracle to run the first s steps at full size on `threads` host threads."""
         os.environ["OMP_NUM_THREADS"] = str(threads)
         oracle = _oracle()
         p = self.p
-        s1, s2 = min(s1, p.steps // 3), min(s2, p.steps)
         A, B, R = p.coefs()
-        ts = []
-        w = self.weights_host(s2 + 1) if self.do else None
-        for s in (s1, s2):
-            t0 = time.perf_counter()
-            if self.do:
-                oracle.line_run_general(p.u0, s, w, 1.0, A, B, R)
-            else:
-                oracle.line_run(p.u0, s, p.tau, p.alpha, p.Da, A, B, R)
-            ts.append(time.perf_counter() - t0)
-        T = _fit_quadratic(ts, (s1, s2), p.steps)
-        return {"value": self.node_steps / T, "sample_seconds": sum(ts),
-                "sample": f"first {s1} and {s2} steps of the {p.N}-node line (full history), fit t(S)=aS+bS^2, "
-                          f"extrapolated to {p.steps} steps"}
+        w = self.weights_host(s + 1) if self.do else None
+        t0 = time.perf_counter()
+        if self.do:
+            oracle.line_run_general(p.u0, s, w, 1.0, A, B, R)
+        else:
+            oracle.line_run(p.u0, s, p.tau, p.alpha, p.Da, A, B, R)
+        return time.perf_counter() - t0
+
+    def sample_desc(self, lens):
+        return (f"the first {', '.join(map(str, lens))} steps of the {self.p.N}-node line (full history), "
+                f"least-squares fit t(S) = aS + bS^2, extrapolated to {self.p.steps} steps")
 
     def weights_host(self, n):
         oracle = _oracle()
@@ -282,21 +305,23 @@ class LodWorkload:
     def steps(self):
         return self.p.steps
 
-    def cpu_rate(self, threads, s1=8, s2=32):
+    def sample_lengths(self):
+        S = self.p.steps
+        return [max(1, min(16, S // 8)), max(2, min(32, S // 4)), max(3, min(64, S // 2))]
+
+    def run_sample(self, s, threads):
         os.environ["OMP_NUM_THREADS"] = str(threads)
         oracle = _oracle()
         p = self.p
         cA, cB, cR = p.coefs()
-        ts = []
-        for s in (s1, s2):
-            t0 = time.perf_counter()
-            oracle.lod_run(p.dims, p.u0, s, p.tau, p.alpha, p.Da, cA, cB, cR, None, None, p.left_kind,
-                           p.right_kind, p.dLN)
-            ts.append(time.perf_counter() - t0)
-        T = _fit_quadratic(ts, (s1, s2), p.steps)
-        return {"value": self.node_steps / T, "sample_seconds": sum(ts),
-                "sample": f"first {s1} and {s2} steps of the {p.dims[0]}^3 grid, fit t(S)=aS+bS^2, "
-                          f"extrapolated to {p.steps} steps"}
+        t0 = time.perf_counter()
+        oracle.lod_run(p.dims, p.u0, s, p.tau, p.alpha, p.Da, cA, cB, cR, None, None, p.left_kind,
+                       p.right_kind, p.dLN)
+        return time.perf_counter() - t0
+
+    def sample_desc(self, lens):
+        return (f"the first {', '.join(map(str, lens))} steps of the {self.p.dims[0]}^3 grid, least-squares "
+                f"fit t(S) = aS + bS^2, extrapolated to {self.p.steps} steps")
 
     def bytes_io(self):
         return 8 * self.p.u0.size, 8 * self.p.u0.size
@@ -333,24 +358,33 @@ class BatchWorkload:
     def steps(self):
         return self._steps
 
-    def cpu_rate(self, threads, s1=48, s2=144, sample=16):
+    SAMPLE_COLS = 16
+
+    def _sample_idx(self):
+        return np.linspace(0, len(self.cols) - 1, self.SAMPLE_COLS).astype(int)
+
+    @property
+    def sample_scale(self):
+        """Total nodes over the sampled columns' nodes (the fit is per sampled column set)."""
+        return sum(c.N for c in self.cols) / sum(self.cols[i].N for i in self._sample_idx())
+
+    def sample_lengths(self):
+        S = self._steps
+        return [max(1, min(64, S // 8)), max(2, min(128, S // 4)), max(3, min(256, S // 2))]
+
+    def run_sample(self, s, threads):
         os.environ["OMP_NUM_THREADS"] = str(threads)
         oracle = _oracle()
-        idx = np.linspace(0, len(self.cols) - 1, sample).astype(int)
-        ts = []
-        for s in (s1, s2):
-            t0 = time.perf_counter()
-            for i in idx:
-                c = self.cols[i]
-                A, B, R = c.coefs()
-                oracle.line_run(c.u0, s, c.tau, c.alpha, c.Da, A, B, R)
-            ts.append(time.perf_counter() - t0)
-        T = _fit_quadratic(ts, (s1, s2), self._steps)
-        scale = sum(c.N for c in self.cols) / sum(self.cols[i].N for i in idx)
-        T *= scale
-        return {"value": self.node_steps / T, "sample_seconds": sum(ts),
-                "sample": f"{sample} of the {len(self.cols)} columns, first {s1} and {s2} steps, fit t(S)=aS+bS^2, "
-                          f"extrapolated to {self._steps} steps and scaled by total nodes"}
+        t0 = time.perf_counter()
+        for i in self._sample_idx():
+            c = self.cols[i]
+            A, B, R = c.coefs()
+            oracle.line_run(c.u0, s, c.tau, c.alpha, c.Da, A, B, R)
+        return time.perf_counter() - t0
+
+    def sample_desc(self, lens):
+        return (f"{self.SAMPLE_COLS} of the {len(self.cols)} columns, the first {', '.join(map(str, lens))} steps, "
+                f"least-squares fit t(S) = aS + bS^2, extrapolated to {self._steps} steps and scaled by total nodes")
 
     def bytes_io(self):
         n = 8 * sum(c.N + 1 for c in self.cols)
@@ -513,9 +547,7 @@ def run_sum(args, wl):
     out = {"metric": wl.metric, "value": value, "unit": "node-steps/s", "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded snapshots; no dataset exists)",
-           "config": {"workload": wl.desc, "path": f"sum_alg {wl.alg}",
-                      "l2": "inputs larger than L2 (snapshots / moments of 2.2 M points, GBs)",
-                      "parallelism": f"replicas x{world}"},
+           "config": bench_config(wl, world), "path": f"sum_alg {wl.alg}",
            "e2e": e2e, "gpu_launches": int(launches), "clocks": clk, "roofline": roof}
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cb = wl.cpu_rate(os.cpu_count() or 1)
@@ -596,9 +628,7 @@ def run_weights(args, wl):
     out_j = {"metric": wl.metric, "value": value, "unit": "weights/s", "n_gpus": world, "steps": args.steps,
              "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
              "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded time steps)",
-             "config": {"workload": wl.desc, "path": "fpde_weights_g",
-                        "l2": "output rows (134 MB) exceed L2; every call recomputes them",
-                        "parallelism": f"replicas x{world}"},
+             "config": bench_config(wl, world), "path": "fpde_weights_g",
              "e2e": {"value": wl.node_steps / e2e_s, "unit": "weights/s", "h2d_bytes_per_step": 8 * (S + 1),
                      "d2h_bytes_per_step": 8 * S * S, "ms_per_step": e2e_s * 1e3},
              "gpu_launches": int(launches), "clocks": clk,
@@ -613,6 +643,17 @@ def run_weights(args, wl):
     ctx.close()
     if rank == 0:
         print(json.dumps(out_j), flush=True)
+
+
+def bench_config(wl, world):
+    """The `config` of both arms (same dict: same workload, same inputs)."""
+    if isinstance(wl, WeightsWorkload):
+        l2 = "output rows (134 MB) exceed L2; every call recomputes them"
+    elif isinstance(wl, SumWorkload):
+        l2 = "inputs larger than L2 (snapshots / moments of 2.2 M points, GBs)"
+    else:
+        l2 = "inputs larger than L2 (the increment history, GBs, is streamed every step)"
+    return {"workload": wl.desc, "l2": l2, "parallelism": f"replicas x{world}"}
 
 
 def make_workload(args):
@@ -630,25 +671,48 @@ def make_workload(args):
 # ------------------------------------------------------------------ reference arm
 
 def run_reference(args):
+    """The reference algorithm on the host cores: the oracle (the CPU restatement of the reference's
+    FP64 path) on all host threads. For the time-stepping workloads each bench step is one timed
+    sample - the first s steps of the full-size problem, s cycling through three lengths - and the
+    value is the full solve's rate from a least-squares fit t(S) = aS + bS^2 of the samples
+    (extrapolated; the fit, its residual and the seconds timed are printed). The Sum and weights
+    workloads time one bounded call per step directly."""
     rank, world, _ = dist_info()
     if rank != 0:
         return
     wl = make_workload(args)
     threads = os.cpu_count() or 1
-    vals = []
-    for it in range(args.warmup + args.steps):
-        r = wl.cpu_rate(threads)
-        if it >= args.warmup:
-            vals.append(r)
-    v = float(np.median([r["value"] for r in vals]))
     unit = "weights/s" if isinstance(wl, WeightsWorkload) else "node-steps/s"
-    out = {"impl": "reference", "metric": wl.metric, "value": v, "unit": unit, "n_gpus": args.gpus,
-           "steps": args.steps, "warmup": args.warmup, "ms_per_step": wl.node_steps / v * 1e3,
+    if hasattr(wl, "run_sample"):
+        lens = wl.sample_lengths()
+        for _ in range(args.warmup):
+            wl.run_sample(lens[0], threads)
+        samples = []
+        for it in range(args.steps):
+            s = lens[it % len(lens)]
+            samples.append((s, wl.run_sample(s, threads)))
+        extra = [(s, wl.run_sample(s, threads)) for s in lens if not any(x == s for x, _ in samples)]
+        cb = cpu_record(wl, samples + extra, threads)
+        cb["timed_steps"] = [{"steps": int(x), "seconds": float(t)} for x, t in samples]
+        cb["extra_samples_for_fit"] = len(extra)
+        value = cb["value"]
+        ms_step = 1e3 * float(np.mean([t for _, t in samples])) if samples else None
+        note = ("each step is one timed sample (the first s steps at full size); value is the full solve's "
+                "rate extrapolated from the samples (cpu_baseline.fit)")
+    else:
+        for _ in range(args.warmup):
+            wl.cpu_rate(threads)
+        vals = [wl.cpu_rate(threads) for _ in range(args.steps)]
+        value = float(np.median([r["value"] for r in vals]))
+        ms_step = 1e3 * float(np.mean([r["sample_seconds"] for r in vals]))
+        cb = {"value": value, "unit": unit, "cores": threads, "kind": "port", "sample": vals[0]["sample"],
+              "extrapolated": False}
+        note = "each step is one timed bounded call of the oracle; value is measured directly"
+    out = {"impl": "reference", "metric": wl.metric, "value": value, "unit": unit, "n_gpus": args.gpus,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step, "step_note": note,
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-           "config": {"workload": wl.desc},
-           "cpu_baseline": {"value": v, "unit": unit, "cores": threads, "kind": "port",
-                            "sample": vals[0]["sample"]},
-           "e2e": {"value": v, "unit": unit, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+           "config": bench_config(wl, world), "cpu_baseline": cb,
+           "e2e": {"value": value, "unit": unit, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out), flush=True)
 
 
@@ -668,7 +732,8 @@ def _timed(obj, u0_dev, steps, reps, stream):
 
 
 def _probe(line, u0_dev, steps, every):
-    """One probed solve: per-kind event sums (0 FP64 GEMV, 1 tensor-core far contraction, 2 solve)."""
+    """One probed solve: per-kind event sums (0 FP64 GEMV, 1 tensor-core far contraction over the
+    history older than a super-block, 2 solve, 3 contraction over the super-block's own blocks)."""
     import torch
     line.set_probe(every)
     line.reset(u0_dev)
@@ -676,22 +741,20 @@ def _probe(line, u0_dev, steps, every):
     line.reset(u0_dev)
     line.run(steps)
     torch.cuda.synchronize()
-    tot = {k: line.probe_stats(k) for k in (0, 1, 2)}
+    tot = {k: line.probe_stats(k) for k in (0, 1, 2, 3)}
     line.set_probe(0)
     return tot
 
 
-# DRAM traffic per launch from ncu captures (profiles/), as bytes per unit the launch processes:
-#   k_line_block_spec: per node-step (109.5 MB for 64 steps x 65,537 nodes, 2 far splits)
-#   k_far_tc3        : per node x history step (630.4 MB for 65,664 rows x 1,344 steps)
-NCU_TRAFFIC = {
-    "solve_split": ((82.01e6 + 27.51e6) / (64 * 65537), "profiles/k_line_block_spec_N65536_2048steps.md"),
-    "far_tc": ((576.33e6 + 54.06e6) / (65664 * 1344), "profiles/k_far_tc3_N65536_K1344.md"),
-}
-# The speculative block solve is bound by neither HBM nor the tensor cores but by GB300's FP64
-# pipe (2 DFMA/clk/SM) and its per-step synchronisation: ncu's sm__pipe_fp64_cycles_active for
-# one launch (same capture as its traffic).
-SOLVE_FP64_PIPE = (0.4844, "profiles/k_line_block_spec_N65536_2048steps.md")
+# DRAM traffic per launch from ncu captures (profiles/), split into what scales with the
+# history length K of a launch and what does not:
+#   k_far_tc3 (two weight groups per item, a 256-step super-block): reads per row x history
+#     column, writes (the float-pair partials) per launch and row;
+#   k_line_block_spec: bytes per node-step (64 steps x 65,537 nodes per launch).
+NCU_FAR = {"read_per_row_col": 623.12e6 / (65664 * 1536), "write_per_row": 122.56e6 / 65664,
+           "source": "profiles/k_far_tc3_super_N65536_K1536.md"}
+NCU_SOLVE = {"per_node_step": (82.01e6 + 27.51e6) / (64 * 65537), "fp64_pipe_active": 0.4844,
+             "source": "profiles/k_line_block_spec_N65536_2048steps.md"}
 
 
 def _kernel_entry(t, name, peak, peak_src, scale=1.0):
@@ -704,6 +767,117 @@ def _kernel_entry(t, name, peak, peak_src, scale=1.0):
     if t["flops"]:
         e["achieved_tflops"] = t["flops"] / (t["ms"] / 1e3) / 1e12
     return e
+
+
+def split_line_rooflines(tot, steps, nodes, rows, sbk, ms_solve, hbm, hbm_src):
+    """Kernel records of the split (bf16x3) line from one probed solve.
+
+    far_tc: k_far_tc3 over the history older than each 256-step super-block (one launch per
+    super-block): bound by the tensor cores' operand traffic, reported in TFLOP/s of the six bf16
+    products against the sustained dense bf16 peak, with its HBM rate beside it for the bytes it
+    reads (6 B per row and history column, three bf16 slices) and for the hi+lo count of the
+    benchmark's byte model (4 B); traffic = ncu reads scaled by the mean K plus ncu writes.
+    near_far: the same kernel over a super-block's own earlier blocks (every block).
+    solve: k_line_block_spec, bound by GB300's FP64 pipe and the per-step chain, not by HBM:
+    microseconds per step, with the profile's FP64-pipe activity.
+    whole_solve: the benchmark's blocked byte model (history read once per block of B = 64 steps as
+    hi+lo bf16 plus the near history and state; and the same at the super-block length) over the
+    whole solve time."""
+    peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
+        os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
+    tflops_peak = peaks.get("bf16_tflops_sustained", 1700.0)
+    tsrc = ("of measured (MEASURED_PEAKS.json bf16_tflops_sustained: the kernel runs inside a long solve)"
+            if "bf16_tflops_sustained" in peaks else "of fallback 1.7 PFLOP/s sustained")
+    out = {}
+    t1, t3, t2 = tot[1], tot[3], tot[2]
+    if t1["count"] > 0 and t1["ms"] > 0:
+        sec = t1["ms"] / 1e3
+        n = t1["count"]
+        b6 = t1["bytes"]                                      # 6 B x nodes x K, summed over the launches
+        b4 = b6 * 4.0 / 6.0
+        k_mean = b6 / (6.0 * nodes * n)
+        tf = t1["flops"] / sec / 1e12
+        out["far_tc"] = {
+            "kernel": "k_far_tc3 (tcgen05 far-history contraction, super-block of %d steps)" % (64 * sbk),
+            "bound": "tensor", "achieved": tf, "peak": tflops_peak, "unit": "TFLOP/s", "frac": tf / tflops_peak,
+            "peak_source": tsrc, "flops_counted": "6 bf16 products x 2 x rows x K x %d steps per launch" % (64 * sbk),
+            "launches": n, "ms_per_launch": t1["ms"] / n, "mean_k": k_mean, "est_ms_per_solve": t1["ms"],
+            "hbm_6B": {"achieved": b6 / sec / 1e9, "frac": b6 / sec / 1e9 / hbm, "unit": "GB/s",
+                       "bytes_per_launch": b6 / n, "note": "three bf16 slices per history element"},
+            "hbm_4B": {"achieved": b4 / sec / 1e9, "frac": b4 / sec / 1e9 / hbm, "unit": "GB/s",
+                       "bytes_per_launch": b4 / n, "note": "hi+lo bf16 count of the benchmark's byte model"},
+            "hbm_peak": hbm, "hbm_peak_source": hbm_src,
+            "traffic": NCU_FAR["read_per_row_col"] * rows * k_mean + NCU_FAR["write_per_row"] * rows,
+            "traffic_unit": "DRAM bytes per launch at the mean K (ncu reads scaled by K, writes per launch)",
+            "traffic_source": NCU_FAR["source"]}
+    if t3["count"] > 0 and t3["ms"] > 0:
+        out["near_far"] = {"kernel": "k_far_tc3 (contraction over the super-block's own earlier blocks)",
+                           "bound": "tensor", "launches": t3["count"], "ms_per_launch": t3["ms"] / t3["count"],
+                           "est_ms_per_solve": t3["ms"],
+                           "achieved": t3["flops"] / (t3["ms"] / 1e3) / 1e12, "unit": "TFLOP/s",
+                           "peak": tflops_peak, "frac": t3["flops"] / (t3["ms"] / 1e3) / 1e12 / tflops_peak,
+                           "peak_source": tsrc}
+    if t2["count"] > 0 and t2["ms"] > 0:
+        us = 1e3 * t2["ms"] / t2["count"]
+        out["solve"] = {"kernel": "k_line_block_spec (far fold, float-float near history, speculative FP64 "
+                                  "Thomas; one launch per 64-step block)",
+                        "bound": "fp64-latency", "achieved": us, "unit": "us/step", "frac": None,
+                        "limiter": "GB300's FP64 pipe (about one FP64 warp instruction per 19 cycles per SM) "
+                                   "along the per-step chain of dependent operations, plus the per-step exchange",
+                        "fp64_pipe_active": NCU_SOLVE["fp64_pipe_active"],
+                        "fp64_pipe_source": NCU_SOLVE["source"] + " (ncu sm__pipe_fp64_cycles_active)",
+                        "steps": t2["count"], "est_ms_per_solve": t2["ms"] * steps / t2["count"],
+                        "traffic": NCU_SOLVE["per_node_step"] * nodes,
+                        "traffic_unit": "DRAM bytes per step (ncu, scaled by nodes)",
+                        "traffic_source": NCU_SOLVE["source"]}
+    # the benchmark's blocked byte model, whole solve
+    def model(B):
+        tot_b = 0.0
+        for n0 in range(0, steps, B):
+            tot_b += 4.0 * n0 * nodes
+            for t in range(n0, min(n0 + B, steps)):
+                tot_b += (8.0 * (t - n0) + 60.0) * nodes
+        return tot_b
+    m64 = model(64)
+    m_sb = 0.0
+    for n0 in range(0, steps, 64):
+        s0 = n0 - n0 % (64 * sbk)
+        m_sb += (4.0 * s0 * nodes if n0 == s0 else 0.0) + 4.0 * (n0 - s0) * nodes
+        for t in range(n0, min(n0 + 64, steps)):
+            m_sb += (8.0 * (t - n0) + 60.0) * nodes
+    sec = ms_solve / 1e3
+    out["whole_solve"] = {"bound": "hbm", "unit": "GB/s", "peak": hbm, "peak_source": hbm_src,
+                          "model_B64": {"bytes": m64, "achieved": m64 / sec / 1e9, "frac": m64 / sec / 1e9 / hbm,
+                                        "note": "history as hi+lo bf16 read once per 64-step block + 8 B per near "
+                                                "lag + 60 B per node-step"},
+                          "model_superblock": {"bytes": m_sb, "achieved": m_sb / sec / 1e9,
+                                               "frac": m_sb / sec / 1e9 / hbm,
+                                               "note": "the same with the far history read once per %d-step "
+                                                       "super-block (this build's schedule)" % (64 * sbk)}}
+    return out
+
+
+def checkpoint_errors(a, b):
+    """Max and RMS relative error of state list a against b (normwise by max |b|)."""
+    out = []
+    for x, y in zip(a, b):
+        x, y = np.concatenate([np.ravel(v) for v in x]), np.concatenate([np.ravel(v) for v in y])
+        m = np.max(np.abs(y))
+        out.append({"max_rel_err": float(np.max(np.abs(x - y)) / m),
+                    "rms_rel_err": float(np.sqrt(np.mean((x - y) ** 2)) / m)})
+    return out
+
+
+def run_pieces(obj, u0_dev, steps, state, k=8):
+    """A solve in k pieces; the state after each piece (the checkpoints)."""
+    cps = [int(round((i + 1) * steps / k)) for i in range(k)]
+    obj.reset(u0_dev)
+    out, t = [], 0
+    for c in cps:
+        obj.run(c - t)
+        t = c
+        out.append(state())
+    return cps, out
 
 
 def run_ours(args):
@@ -786,58 +960,39 @@ def run_ours(args):
            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": "f64" if prec == 0 else f"{pname}(tensor)+f64",
            "data": "synthetic (seeded; no dataset exists for this operator)",
-           "config": {"workload": wl.desc, "path": pname,
-                      "l2": "inputs larger than L2 (the increment history, GBs, is streamed every step)",
-                      "parallelism": f"replicas x{world}"},
+           "config": bench_config(wl, world), "path": pname,
            "e2e": e2e, "gpu_launches": int(launches), "clocks": clk}
     if tuning is not None:
-        out["config"]["tuning"] = {"solve_sp": tuning.solve_sp, "chunks": tuning.chunks,
-                                   "far_splits": tuning.far_splits, "gemv_splits": tuning.gemv_splits,
-                                   "tuned_ms_per_step": tuning.ms_per_step, "autotune_seconds": tune_s,
-                                   "block_steps": 64}
+        out["tuning"] = {"solve_sp": tuning.solve_sp, "chunks": tuning.chunks,
+                         "far_splits": tuning.far_splits, "gemv_splits": tuning.gemv_splits,
+                         "far_super_blocks": tuning.far_super, "tuned_ms_per_step": tuning.ms_per_step,
+                         "autotune_seconds": tune_s, "block_steps": 64}
 
     if is_line:
         # kernel rooflines from one separate probed solve (events inside the graph)
         every = max(1, steps // 32)
         tot = _probe(obj, u0_dev, steps, every)
-        kernels = {}
-        # probe counts are time steps covered (all far contractions are probed)
-        per = lambda t: steps / t["count"] if t["count"] else 0.0
+        nodes = wl.p.N + 1
         if prec == 0:
-            kernels["hist_gemv"] = _kernel_entry(tot[0], "k_l1_partial (FP64 history GEMV)", peak, peak_src,
-                                                 per(tot[0]))
-            solve_name = "k_line_solve (history fold + Thomas, one launch per step)"
+            k = _kernel_entry(tot[0], "k_l1_partial (FP64 history GEMV)", peak, peak_src,
+                              steps / max(tot[0]["count"], 1))
+            kernels = {"hist_gemv": k} if k else {}
+        elif prec == fp.FPDE_PREC_SPLIT_BF16X3:
+            sbk = tuning.far_super if (tuning is not None and tuning.far_super) else 4
+            rows = (nodes + 127) // 128 * 128
+            kernels = split_line_rooflines(tot, steps, nodes, rows, sbk, ms, peak, peak_src)
         else:
-            kernels["far_tc"] = _kernel_entry(tot[1], "k_far_tc3/k_far_tc (tcgen05 far-history contraction)",
-                                              peak, peak_src, 1.0)
-            solve_name = ("k_line_block_spec (far fold, float-float near history, speculative FP64 Thomas"
-                          + (" with the explicit half" if wl.do else "") + "; one launch per 64-step block)")
-        kernels["solve"] = _kernel_entry(tot[2], solve_name, peak, peak_src, per(tot[2]))
-        kernels = {k: v for k, v in kernels.items() if v}
-        if prec != 0 and "solve" in kernels:
-            kernels["solve"]["limiter"] = "fp64 pipe + per-step synchronisation (not HBM)"
-        if prec == fp.FPDE_PREC_SPLIT_BF16X3 and not wl.do:   # traffic per launch, scaled to this line
-            nodes = wl.p.N + 1
-            if "solve" in kernels:
-                per, src = NCU_TRAFFIC["solve_split"]
-                kernels["solve"]["traffic"] = per * nodes
-                kernels["solve"]["traffic_unit"] = "bytes per step (ncu, scaled by nodes)"
-                kernels["solve"]["traffic_source"] = src
-                kernels["solve"]["fp64_pipe_active"] = SOLVE_FP64_PIPE[0]
-                kernels["solve"]["fp64_pipe_source"] = SOLVE_FP64_PIPE[1]
-            if "far_tc" in kernels:
-                per, src = NCU_TRAFFIC["far_tc"]
-                avg_k = 64 * (steps // 64 - 1) / 2.0
-                kernels["far_tc"]["traffic"] = per * nodes * avg_k
-                kernels["far_tc"]["traffic_unit"] = "bytes per launch at the average history (ncu, scaled)"
-                kernels["far_tc"]["traffic_source"] = src
-        est = {k: v["est_ms_per_solve"] for k, v in kernels.items()}
-        tot_est = sum(est.values())
-        for k, v in kernels.items():
-            v["share_of_kernel_time"] = est[k] / tot_est if tot_est else None
-        dom = max(kernels, key=lambda k: est[k])
-        out["roofline"] = dict(kernels[dom])
+            k = _kernel_entry(tot[1], "k_far_tc (tcgen05 far-history contraction, two-term split)", peak,
+                              peak_src, 1.0)
+            kernels = {"far_tc": k} if k else {}
         out["kernels"] = kernels
+        if "far_tc" in kernels:
+            out["roofline"] = dict(kernels["far_tc"])
+            out["roofline_note"] = ("the tensor-core far contraction (the split path's HBM/tensor kernel); the "
+                                    "block solve (kernels.solve) takes a comparable share but is bound by the "
+                                    "FP64 pipe and its per-step chain, not by HBM or the tensor cores")
+        elif "hist_gemv" in kernels:
+            out["roofline"] = dict(kernels["hist_gemv"])
     else:
         # whole-step HBM roofline from the algorithmic history bytes of the run:
         #   FP64: 8 B x nodes x lags, summed over steps;
@@ -861,12 +1016,17 @@ def run_ours(args):
         # the plain FP64 kernel on the same workload: speed-up and accuracy of the split path
         t64 = wl.autotune(ctx, fp.FPDE_PREC_FP64) if (is_line and not args.no_autotune) else None
         l64 = wl.build(ctx, fp.FPDE_PREC_FP64, t64) if is_line else wl.build(ctx, fp.FPDE_PREC_FP64)
-        l64.reset(u0_dev)
-        l64.run(steps)
+        # both paths in eight pieces (untimed; the FP64 one is also its warm-up): max and RMS
+        # relative error of the split path against FP64 at the 8 checkpoints and the final step
+        cps, s64 = run_pieces(l64, u0_dev, steps, l64.state)
+        _, ssp = run_pieces(obj, u0_dev, steps, obj.state)
         ms64 = _timed(l64, u0_dev, steps, 1, stream)
         u64 = l64.state()
         err = float(np.max(np.abs(u_main - u64)) / np.max(np.abs(u64)))
-        rms = float(np.sqrt(np.mean((u_main - u64) ** 2)) / np.sqrt(np.mean(u64 ** 2)))
+        rms = float(np.sqrt(np.mean((u_main - u64) ** 2)) / np.max(np.abs(u64)))
+        cp_err = checkpoint_errors(ssp, s64)
+        for c, e in zip(cps, cp_err):
+            e["step"] = c
         out["fp64_kernel"] = {"value": wl.node_steps / (ms64 / 1e3), "ms_per_step": ms64}
         if is_line:
             tot64 = _probe(l64, u0_dev, steps, max(1, steps // 32))
@@ -876,12 +1036,14 @@ def run_ours(args):
                 r64["fp64_fma_ceiling_gbs"] = 4800.0
             out["fp64_kernel"]["roofline"] = r64
         l64.close()
-        out["split_vs_fp64"] = {"speedup": ms64 / ms, "max_rel_err": err, "rms_rel_err": rms, "bound": 1e-7}
+        out["split_vs_fp64"] = {"speedup": ms64 / ms, "max_rel_err": max([err] + [e["max_rel_err"] for e in cp_err]),
+                                "final_max_rel_err": err, "final_rms_rel_err": rms, "checkpoints": cp_err,
+                                "bound": 1e-7, "norm": "relative to max |u_fp64| at the same step"}
     obj.close()
     if rank == 0 and world == 1 and not args.no_cpu_baseline and not getattr(args, "max_lag", 0):
-        cb = wl.cpu_rate(os.cpu_count() or 1)
-        out["cpu_baseline"] = {"value": cb["value"], "unit": "node-steps/s", "cores": os.cpu_count() or 1,
-                               "kind": "port", "sample": cb["sample"]}
+        threads = os.cpu_count() or 1
+        out["cpu_baseline"] = cpu_record(wl, [(s, wl.run_sample(s, threads)) for s in wl.sample_lengths()],
+                                         threads)
     ctx.close()
     if rank == 0:
         print(json.dumps(out), flush=True)

@@ -153,15 +153,23 @@ void fo_weights_g(double p, double alpha, const double *time, int n, double *kb,
 
 /* ------------------------------------------------------------ history sum */
 
+/* Every node's sum starts at 0 and adds its terms from t = n-1 down to 0 (time_summing :4111,
+ * newest first) in the reference's order and rounding; the loops visit t outside a block of nodes
+ * so that each history row is read contiguously, node blocks in parallel. */
+#define FO_NODE_BLOCK 2048
 void fo_l1_sum(const double *D, int64_t P, int n, const double *kb, const double *tau,
                int64_t i0, int64_t i1, double *S)
 {
+    const int64_t nblk = (i1 - i0 + FO_NODE_BLOCK - 1) / FO_NODE_BLOCK;
 #pragma omp parallel for schedule(static)
-    for (int64_t i = i0; i < i1; i++) {
-        double s = 0.0;
-        for (int t = n - 1; t >= 0; t--)          /* time_summing :4111, newest first */
-            s += kb[t] * D[(int64_t)t * P + i] / tau[t];
-        S[i] = s;
+    for (int64_t b = 0; b < nblk; b++) {
+        const int64_t a = i0 + b * FO_NODE_BLOCK, e = a + FO_NODE_BLOCK < i1 ? a + FO_NODE_BLOCK : i1;
+        for (int64_t i = a; i < e; i++) S[i] = 0.0;
+        for (int t = n - 1; t >= 0; t--) {
+            const double *row = D + (int64_t)t * P;
+            const double c = kb[t], tt = tau[t];
+            for (int64_t i = a; i < e; i++) S[i] += c * row[i] / tt;
+        }
     }
 }
 
@@ -346,13 +354,19 @@ int fo_line_run_general(int N, double *U, double *hist, int64_t P, int steps, co
     double *wl = (double *)malloc(sizeof(double) * (size_t)(steps + 1));
     for (int n = 0; n < steps; n++) {
         memcpy(Uold, U, sizeof(double) * (size_t)(N + 1));
-        /* history: S[i] = sum_{t<n} w[n-t] D_t[i] (lag weights, eq_DF of fr_do.cpp :737-771) */
+        /* history: S[i] = sum_{t<n} w[n-t] D_t[i] (lag weights, eq_DF of fr_do.cpp :737-771), each
+         * node from t = n-1 down, rows read contiguously per block of nodes */
         for (int t = 0; t < n; t++) wl[t] = w[n - t];
+        const int64_t nblk = ((int64_t)N - 1 + FO_NODE_BLOCK - 1) / FO_NODE_BLOCK;
 #pragma omp parallel for schedule(static)
-        for (int i = 1; i < N; i++) {
-            double s = 0.0;
-            for (int t = n - 1; t >= 0; t--) s += wl[t] * hist[(int64_t)t * P + i];
-            S[i] = s;
+        for (int64_t b = 0; b < nblk; b++) {
+            const int64_t a = 1 + b * FO_NODE_BLOCK, e = a + FO_NODE_BLOCK < N ? a + FO_NODE_BLOCK : N;
+            for (int64_t i = a; i < e; i++) S[i] = 0.0;
+            for (int t = n - 1; t >= 0; t--) {
+                const double *row = hist + (int64_t)t * P;
+                const double c = wl[t];
+                for (int64_t i = a; i < e; i++) S[i] += c * row[i];
+            }
         }
         const double *sr = src ? src + (int64_t)(n < src_rows ? n : src_rows - 1) * (N + 1) : NULL;
         for (int i = 1; i < N; i++) {

@@ -14,6 +14,7 @@ CASES = [
     ["--workload", "config2", "--nodes", "1024", "--time-steps", "96"],
     ["--workload", "config3", "--nodes", "1024", "--time-steps", "96"],
     ["--workload", "config4", "--nodes", "12", "--time-steps", "24"],
+    ["--workload", "config5", "--nodes", "6", "--time-steps", "64"],
     ["--workload", "sum2", "--nodes", "24"],
     ["--workload", "weights", "--time-steps", "256"],
 ]
@@ -37,6 +38,15 @@ def test_reference_arm_json(args):
     assert cb["kind"] in ("port", "reference") and cb["cores"] >= 1 and cb["sample"] and cb["value"] == d["value"]
     assert d["e2e"]["value"] == d["value"] and d["e2e"]["unit"] == d["unit"]
     assert "workload" in d["config"]
+    if args[1].startswith("config"):
+        # time-stepping workloads: an extrapolation from at least three timed sample lengths, with
+        # the fit, its residual and the seconds timed in the record; one timed sample per step
+        assert cb["extrapolated"] is True
+        fit = cb["fit"]
+        assert len({x["steps"] for x in fit["samples"]}) >= 3 and fit["relative_rms_residual"] >= 0
+        assert fit["a"] >= 0 and fit["b"] >= 0 and cb["seconds_timed"] > 0
+        assert len(cb["timed_steps"]) == d["steps"]
+        assert d["ms_per_step"] > 0
 
 
 def test_line_workload_restricted_threshold():
