@@ -251,8 +251,32 @@ static void time_column(int kcells, double alpha, double tau, int steps)
     fclose(lg);
 }
 
+/* The reference's Gamma (fpde_hpc_1d.cpp:70-252: exp(LogGamma), its own series and
+ * asymptotic forms, memoised) at the orders the benchmark configurations use: 1 - alpha for
+ * Da = 1/Gamma(1 - alpha) (:3598-3605) and 2 - a for the distributed-order normalisers, plus a
+ * sweep over (0, 4]. */
+static void run_gamma(const char *path)
+{
+    std::vector<double> x;
+    const double alphas[] = {0.5, 0.55, 0.6, 0.65, 0.7, 0.75, 0.8, 0.85, 0.9, 0.95, 0.3, 0.1};
+    for (double a : alphas) { x.push_back(1.0 - a); x.push_back(2.0 - a); }
+    for (int q = 1; q <= 400; q++) x.push_back(0.01 * q);
+    std::vector<double> g;
+    for (double v : x) g.push_back(Gamma(v));
+    FgvWriter w(path);
+    w.put("x", x);
+    w.put("gamma", g);
+    printf("wrote %s (%zu values)\n", path, x.size());
+}
+
 int main(int argc, char **argv)
 {
+    if (argc >= 3 && strcmp(argv[1], "gamma") == 0) {
+        char q[4096];
+        snprintf(q, sizeof q, "%s/fpde_gamma.fgv", argv[2]);
+        run_gamma(q);
+        return 0;
+    }
     if (argc >= 2 && strcmp(argv[1], "time") == 0) {
         int kc = argc > 2 ? atoi(argv[2]) : 1000;
         int st = argc > 3 ? atoi(argv[3]) : 200;
@@ -312,6 +336,8 @@ int main(int argc, char **argv)
         func_in_kernel = 0;
         func_power = 0.6;
     }
+    snprintf(p, sizeof p, "%s/fpde_gamma.fgv", dir);
+    run_gamma(p);
     /* History modes: restricted summing below kb = 0.05 (about the 10 newest lags at alpha
      * 0.8, tau 0.0025) and a 16-term series expansion. */
     {

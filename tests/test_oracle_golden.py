@@ -307,3 +307,17 @@ def test_weights_g_sum_to_the_beta_integral(p, alpha):
         T = time[n + 1]
         exact = T ** (1.0 - p * alpha) * beta(1.0 / p, 1.0 - alpha) / p
         assert abs((kb.sum() + k0) - exact) <= 1e-14 * exact, (n, (kb.sum() + k0) / exact - 1)
+
+
+def test_gamma_matches_reference_gamma():
+    """fpde_gamma against the reference's own Gamma (fpde_hpc_1d.cpp:70-252, exp(LogGamma) with
+    its series and asymptotic branches), recorded by the pin harness at the orders the
+    configurations use (1 - alpha for Da, 2 - a for the distributed-order normalisers) and over
+    (0, 4]: the C library's tgamma and the reference's evaluation agree to a few ulps, far inside
+    the 1e-12 parity bar they feed."""
+    import fpde_hpc_gb300 as fp
+    g = fgv.load(golden_path("fpde_gamma"))
+    mine = np.array([fp.gamma(v) for v in g["x"]])
+    rel = np.abs(mine - g["gamma"]) / np.abs(g["gamma"])
+    assert rel.max() <= 4e-15, (rel.max(), g["x"][np.argmax(rel)])
+    assert rel[:24].max() <= 4e-15          # the configurations' orders come first
