@@ -475,6 +475,154 @@ int fo_lod_step(int sN, int M, int K, double *U, double *hist, int n,
     return 0;
 }
 
+/* ------------------------------------------------- Richards (solution-dependent coefficients) */
+
+/* The reference's closures of its Richards problem (analytic_test 0, cv_form 4): water content
+ * wetness :2493-2522, its inverse derivative inv_dw_dh :2523-2566 and the conductivity KK
+ * :2625-2655 (k_form 1 van Genuchten-Mualem, 2 Averianov), as functions of the suction P
+ * (metres). The expressions keep the reference's operation order, so the values are bitwise
+ * the reference's. */
+static double rich_wetness(double P)
+{
+    const double n = 1.25, s0 = 0.0736, s1 = 0.55, a = 0.066;
+    double Ch;
+    P *= 100.0;
+    if (P <= 0.0)
+        Ch = s1;
+    else
+        Ch = s0 + ((s1 - s0) / pow(1 + pow(a * P, n), (1 - 1 / n)));
+    return Ch;
+}
+
+static double rich_inv_dw_dh(double P)
+{
+    const double n = 1.25, s0 = 0.0736, s1 = 0.55, a = 0.066;
+    double Ch = 0.0;
+    if (P <= 0.0) {
+        Ch = 0.0;
+    } else {
+        double hn = pow(100.0, n), h2n = pow(100.0, 2.0 * n);
+        Ch = ((((1 - n) * hn * s0 + (n - 1) * hn * s1) * pow(a * P, n) * pow(1 + hn * pow(a * P, n), (1 / n))) /
+              (h2n * P * pow(a * P, 2 * n) + 2 * hn * P * pow(a * P, n) + P));
+    }
+    if (Ch != 0.0) return 1.0 / Ch;
+    return 1e20;
+}
+
+static double rich_KK(double P, int kform, double ksat)
+{
+    const double n = 1.25, s0 = 0.0736, s1 = 0.55;
+    double Kr = 1.0;
+    if (kform == 1)
+        Kr = pow(((rich_wetness(P) - s0) / (s1 - s0)), 0.5) *
+             pow(1.0 - pow(1.0 - pow(((rich_wetness(P) - s0) / (s1 - s0)), (1.0 / (1.0 - 1.0 / n))), (1.0 - 1.0 / n)),
+                 2.0);
+    if (kform == 2) Kr = pow(((rich_wetness(P) - s0) / (s1 - s0)), 3.5);
+    return Kr * ksat;
+}
+
+void fo_richards_closures(int n, const double *P, int kform, double ksat, double *w, double *iw, double *kk)
+{
+    for (int i = 0; i < n; i++) {
+        if (w) w[i] = rich_wetness(P[i]);
+        if (iw) iw[i] = rich_inv_dw_dh(P[i]);
+        if (kk) kk[i] = rich_KK(P[i], kform, ksat);
+    }
+}
+
+/* One LOD step of the reference's Richards problem in its 3D mode (calc_step :5144-5779 with
+ * analytic_test 0, no irrigation, bottom_cond 0): the passes of fo_lod_step, with every line's
+ * coefficients A_/B/R (:3095-3142) formed from the line's current values before its solve. The
+ * suction of a node follows the reference's mode-3 wetness/inv_dw_dh (:2504-2512, :2546-2554):
+ * P = -(U - i sZ[p]) with i the node's index along the sN axis and p its position along the pass.
+ * Left ends: the sN pass takes the first-order surface condition (al1 :4004-4012, bc0 :4493-4500)
+ * with Uc = dL[0] E / KK(1) (:3036-3070, no irrigation); the other passes zero flux (Al[1] = 1,
+ * Bt[1] = 0). Right ends: the flux closure of U1 with bcN = 0. rp: the K-pass source grid. */
+int fo_lod_step_richards(int sN, int M, int K, double *U, double *hist, int n, const double *kb, const double *tau,
+                         double Da, double kkk0, const double *sZ, const double *sdL, const double *dLx,
+                         const double *dLy, int kform, double ksat, double E, const double *rp, double *S_out)
+{
+    const double lam = Da * (kkk0 / tau[n]);      /* Om1 :4191 */
+    const double lamR = Da * kkk0 / tau[n];       /* R :3120 */
+    const int64_t sx = 1, sy = sN + 2, sz = (int64_t)(sN + 2) * (M + 2);
+    const int64_t G = sz * (K + 2);
+    int L = sN; if (M > L) L = M; if (K > L) L = K;
+    double *Uold = (double *)malloc(sizeof(double) * (size_t)G);
+    double *S = (double *)calloc((size_t)G, sizeof(double));
+    memcpy(Uold, U, sizeof(double) * (size_t)G);
+    if (n > 0) {
+#pragma omp parallel for schedule(static)
+        for (int k = 1; k <= K; k++)
+            for (int t = n - 1; t >= 0; t--) {
+                const double *h = hist + (int64_t)t * G;
+                const double c = kb[t], tt = tau[t];
+                for (int j = 1; j < M; j++)
+                    for (int i = 1; i < sN; i++) {
+                        const int64_t id = i * sx + j * sy + k * sz;
+                        S[id] += c * h[id] / tt;
+                    }
+            }
+    }
+    for (int pass = 2; pass >= 0; pass--) {
+        const int Nl = pass == 2 ? K : (pass == 1 ? M : sN);
+        const int64_t st = pass == 2 ? sz : (pass == 1 ? sy : sx);
+        const double *dL = pass == 2 ? dLy : (pass == 1 ? dLx : sdL);
+        const int na = pass == 2 ? sN : (pass == 1 ? sN : M);
+        const int nb = pass == 2 ? M : K;
+#pragma omp parallel
+        {
+        double *la = (double *)malloc(sizeof(double) * (size_t)(L + 2));
+        double *lb = (double *)malloc(sizeof(double) * (size_t)(L + 2));
+        double *lr = (double *)malloc(sizeof(double) * (size_t)(L + 2));
+        double *lo = (double *)malloc(sizeof(double) * (size_t)(L + 2));
+        double *lu = (double *)malloc(sizeof(double) * (size_t)(L + 2));
+        double *kk = (double *)malloc(sizeof(double) * (size_t)(L + 2));
+        double *iw = (double *)malloc(sizeof(double) * (size_t)(L + 2));
+        double *Al = (double *)malloc(sizeof(double) * (size_t)(L + 2));
+        double *Bt = (double *)malloc(sizeof(double) * (size_t)(L + 2));
+#pragma omp for schedule(static) collapse(2)
+        for (int a = 1; a < na; a++)
+            for (int b = 1; b < nb; b++) {
+                int64_t base;
+                if (pass == 2) base = a * sx + b * sy;
+                else if (pass == 1) base = a * sx + b * sz;
+                else base = a * sy + b * sz;
+                for (int p = 0; p <= Nl + 1; p++) lu[p] = U[base + p * st];
+                for (int p = 0; p <= Nl; p++) {           /* closures at the line's nodes */
+                    const int inode = pass == 0 ? p : a;
+                    const double P = -(lu[p] - inode * sZ[p]);
+                    kk[p] = rich_KK(P, kform, ksat);
+                    iw[p] = rich_inv_dw_dh(P);
+                }
+                for (int p = 1; p < Nl; p++) {
+                    la[p] = kk[p - 1] * iw[p] / (dL[p] * dL[p - 1]);
+                    lb[p] = kk[p] * iw[p] / (dL[p] * dL[p]);
+                    lr[p] = iw[p] * ((kk[p] / (dL[p] * dL[p])) + (kk[p - 1] / (dL[p] * dL[p - 1]))) + lamR;
+                    const int64_t id = base + p * st;
+                    lo[p] = -(lam * lu[p]) + ((pass == 2 && rp) ? rp[id] : 0.0);
+                    if (pass == 2) lo[p] += Da * S[id];
+                }
+                int lkind = 1;
+                double g0 = 0.0;
+                if (pass == 0) {                           /* surface: al1 :4006-4012, bc0 :4495-4500 */
+                    const double Uc = dL[0] * (E - 0.0) / kk[1];
+                    if (iw[0] != 1e20) { lkind = 1; g0 = -Uc; }
+                    else { lkind = 0; g0 = -Uc * kk[1] / dL[0]; }
+                }
+                thomas_core(Nl, la, lb, lr, lo, lkind, g0, 1, 0.0, dL[Nl - 1], lu, Al, Bt);
+                lu[Nl + 1] = lu[Nl];                                 /* U1 :4792 */
+                for (int p = 0; p <= Nl + 1; p++) U[base + p * st] = lu[p];
+            }
+        free(la); free(lb); free(lr); free(lo); free(lu); free(kk); free(iw); free(Al); free(Bt);
+        }
+    }
+    double *row = hist + (int64_t)n * G;
+    for (int64_t q = 0; q < G; q++) row[q] = U[q] - Uold[q];
+    if (S_out) memcpy(S_out, S, sizeof(double) * (size_t)G);
+    free(Uold); free(S);
+    return 0;
+}
+
 /* ------------------------------------------------------ distributed order */
 
 static double bk_pow(double d1, double d2, double beta)   /* fr_do.cpp:129-134 */

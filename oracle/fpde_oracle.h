@@ -140,6 +140,20 @@ int fo_lod_step(int sN, int M, int K, double *U, double *hist, int n,
                 const double *rp, const double *bc, const int *lkind, const int *rkind, const double *dLN,
                 double *S_out);
 
+/* ---- Richards problem: solution-dependent coefficients ---- */
+
+/* The reference's closures at suctions P[0..n-1] (metres): water content (wetness, cv_form 4),
+ * 1/(dw/dh) (inv_dw_dh; 1e20 where saturated) and the conductivity KK (k_form 1 VGM, 2
+ * Averianov, times ksat). Any output may be NULL. */
+void fo_richards_closures(int n, const double *P, int kform, double ksat, double *w, double *iw, double *kk);
+
+/* One 3D LOD step of the reference's Richards problem (analytic_test 0, no irrigation,
+ * bottom_cond 0): coefficients from each line's current values, the surface condition of the
+ * sN pass from the evaporation rate E, zero flux elsewhere; rp the K-pass source grid. */
+int fo_lod_step_richards(int sN, int M, int K, double *U, double *hist, int n, const double *kb, const double *tau,
+                         double Da, double kkk0, const double *sZ, const double *sdL, const double *dLx,
+                         const double *dLy, int kform, double ksat, double E, const double *rp, double *S_out);
+
 /* ---- distributed order (fr_do.cpp) ---- */
 
 /* Caputo derivative of sampled F (Cder :74-86 with an F array): DF[t] for t = 1..ntau-1,

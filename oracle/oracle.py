@@ -54,6 +54,10 @@ def load():
     lib.fo_lod_step.argtypes = [i32, i32, i32, _dp, _dp, i32, _dp, _dp, d, d, _dp, _dp, _dp, vp, _dp,
                                 _ip, _ip, _dp, vp]
     lib.fo_lod_step.restype = i32
+    lib.fo_richards_closures.argtypes = [i32, _dp, i32, d, vp, vp, vp]
+    lib.fo_lod_step_richards.argtypes = [i32, i32, i32, _dp, _dp, i32, _dp, _dp, d, d, _dp, _dp, _dp, _dp, i32, d,
+                                         d, vp, vp]
+    lib.fo_lod_step_richards.restype = i32
     lib.fo_caputo_derivative.argtypes = [i32, d, d, d, _dp, _dp]
     lib.fo_do_derivative.argtypes = [i32, d, i32, _dp, _dp, _dp, i32, i32, i32, _dp]
     lib.fo_do_fused_weights.argtypes = [i32, _dp, _dp, _dp, d, i32, _dp]
@@ -232,6 +236,29 @@ def lod_run(dims, U0, steps, tau, alpha, Da, coefA, coefB, coefRlap, rp=None, bc
         lod_step(dims, U, hist, n, kb if n else np.zeros(1), taus, Da, k0, coefA, coefB, coefRlap, rp, bc,
                  lkind, rkind, dLN)
     return U
+
+
+def richards_closures(P, kform, ksat):
+    """(wetness, inv_dw_dh, KK) of the reference's Richards problem at suctions P (metres)."""
+    lib = load()
+    P = np.ascontiguousarray(P, dtype=np.float64)
+    w, iw, kk = np.zeros_like(P), np.zeros_like(P), np.zeros_like(P)
+    lib.fo_richards_closures(len(P), P, kform, ksat, _ptr(w), _ptr(iw), _ptr(kk))
+    return w, iw, kk
+
+
+def lod_step_richards(dims, U, hist, n, kb, tau, Da, kkk0, sZ, sdL, dLx, dLy, kform, ksat, E, rp=None,
+                      want_S=False):
+    """fo_lod_step_richards: one LOD step of the Richards problem (coefficients from the grid)."""
+    lib = load()
+    sN, M, K = dims
+    S = np.zeros_like(U) if want_S else None
+    f = lambda x: np.ascontiguousarray(x, dtype=np.float64)
+    rpp = None if rp is None else f(rp).reshape(-1)
+    lib.fo_lod_step_richards(sN, M, K, U.reshape(-1), hist.reshape(-1), n, f(kb), f(tau), Da, kkk0, f(sZ), f(sdL),
+                             f(dLx), f(dLy), kform, ksat, E,
+                             None if rpp is None else rpp.ctypes.data_as(C.c_void_p), _ptr(S))
+    return S
 
 
 def caputo_derivative(F, tau, a, g2a):

@@ -251,6 +251,77 @@ static void time_column(int kcells, double alpha, double tau, int steps)
     fclose(lg);
 }
 
+/* The Richards problem of the reference (analytic_test 0: van Genuchten-Mualem water content
+ * cv_form 4 and conductivity k_form 1 or Averianov k_form 2, wetness / inv_dw_dh / KK
+ * :2493-2657) in its 3D LOD mode with the history, no irrigation (no_irr 1), zero-flux bottom
+ * and sides (bottom_cond 0): the tridiagonal coefficients A_/B/R (:3095-3142) change with the
+ * solution every step. Recorded per step, besides the weights, history sums and grids:
+ *   Rp - the K-pass source (root water uptake, :2724-2978), evaluated at the state and time the
+ *        step's K pass sees (the grid at the start of the step, Time[tstep] of the step);
+ *   E  - the evaporation rate of the step (Uc :3036-3070 with no irrigation is dL[0] E / KK(1)).
+ * A replay computes the coefficients and the top boundary value from its own grid. */
+static void run_richards(const char *path, int kform, int rpform, int bs, int nb, int mb, int kb, double alpha,
+                         double tau, int steps)
+{
+    set_dims(bs, nb, mb, kb);
+    varT = 0; varZ = 0; varXY = 0;
+    implicit = 0; implicit3d = 0; rp_split_3d = 0; sum_alg = 0;
+    global_eps = 1e-15; global_eps2 = 1e-15;
+    FILE *lg = fopen("/dev/null", "w");
+    H_solver *s = new H_solver(0, rpform, 4, 1, 0, alpha, 1.0, 0, 0, 0, 3, lg, kform);
+    size_t G = (size_t)(sN + 2) * (_M + 2) * (K + 2);
+    FgvWriter w(path);
+    w.scalar("sN", sN); w.scalar("M", _M); w.scalar("K", K);
+    w.scalar("alpha", alpha); w.scalar("Da", s->Da); w.scalar("k_form", kform); w.scalar("rp_form", rpform);
+    w.scalar("k_sat", s->k);
+    std::vector<uint64_t> gdims = {(uint64_t)(K + 2), (uint64_t)(_M + 2), (uint64_t)(sN + 2)};
+    w.put("U0", gdims, s->b_U);
+    w.put("sZ", std::vector<double>(s->sZ, s->sZ + sN + 2));
+    w.put("sdL", std::vector<double>(s->sdL, s->sdL + sN + 2));
+    w.put("dLx", std::vector<double>(s->dLx, s->dLx + _M + 2));
+    w.put("dLy", std::vector<double>(s->dLy, s->dLy + K + 2));
+    std::vector<double> kb_all, kb_off, kkk0, tauv, S_all, U_all, rp, Ev;
+    for (int n = 0; n < steps; n++) {
+        /* the inputs as the step sees them: advance Time/tau/tstep as init_time_step does,
+         * evaluate, and put them back before the step itself */
+        s->Time.push_back(s->Time[s->Time.size() - 1] + tau);
+        s->tau.push_back(tau);
+        s->tstep++;
+        size_t o = rp.size();
+        rp.resize(o + G, 0.0);
+        PassState st = save_state(s);
+        for (int i = 1; i < sN; i++) for (int j = 1; j < _M; j++) {
+            enter_line(s, 2, i, j);
+            for (int k = 1; k < K; k++) rp[o + gidx(i, j, k)] = s->Rp(k);
+        }
+        restore_state(s, st);
+        double E = s->Ev * s->day_night_coef();
+        if (rpform == 3) E += s->Tr * s->day_night_coef();
+        Ev.push_back(E);
+        s->Time.pop_back();
+        s->tau.pop_back();
+        s->tstep--;
+        s->calc_step(tau);
+        kb_off.push_back((double)kb_all.size());
+        kb_all.insert(kb_all.end(), s->kb_3_cache.begin(), s->kb_3_cache.end());
+        kkk0.push_back(s->kkk0);
+        tauv.push_back(s->tau[s->tstep]);
+        S_all.insert(S_all.end(), s->b_Utimesum, s->b_Utimesum + G);
+        U_all.insert(U_all.end(), s->b_U, s->b_U + G);
+    }
+    kb_off.push_back((double)kb_all.size());
+    uint64_t ns = steps;
+    w.put("tau", tauv); w.put("kkk0", kkk0);
+    w.put("kb_flat", kb_all); w.put("kb_off", kb_off);
+    w.put("E", Ev);
+    w.put("S", {ns, (uint64_t)(K + 2), (uint64_t)(_M + 2), (uint64_t)(sN + 2)}, S_all.data());
+    w.put("U", {ns, (uint64_t)(K + 2), (uint64_t)(_M + 2), (uint64_t)(sN + 2)}, U_all.data());
+    w.put("Rp", {ns, (uint64_t)(K + 2), (uint64_t)(_M + 2), (uint64_t)(sN + 2)}, rp.data());
+    delete s;
+    fclose(lg);
+    printf("wrote %s (Richards k_form %d, %d steps, grid %dx%dx%d)\n", path, kform, steps, sN, _M, K);
+}
+
 /* The reference's Gamma (fpde_hpc_1d.cpp:70-252: exp(LogGamma), its own series and
  * asymptotic forms, memoised) at the orders the benchmark configurations use: 1 - alpha for
  * Da = 1/Gamma(1 - alpha) (:3598-3605) and 2 - a for the distributed-order normalisers, plus a
@@ -271,6 +342,16 @@ static void run_gamma(const char *path)
 
 int main(int argc, char **argv)
 {
+    if (argc >= 3 && strcmp(argv[1], "richards") == 0) {
+        char q[4096];
+        snprintf(q, sizeof q, "%s/fpde_richards_k1.fgv", argv[2]);
+        /* sN = M = K: the reference indexes its root mask rp_mult[i][j] (allocated M+2 x K+2) with
+         * the K-pass line and sZ (sN+2 values) with positions along the other passes */
+        run_richards(q, 1, 1, 2, 3, 3, 3, 0.8, 900.0, 40);
+        snprintf(q, sizeof q, "%s/fpde_richards_k2.fgv", argv[2]);
+        run_richards(q, 2, 2, 2, 3, 3, 3, 0.6, 900.0, 40);
+        return 0;
+    }
     if (argc >= 3 && strcmp(argv[1], "gamma") == 0) {
         char q[4096];
         snprintf(q, sizeof q, "%s/fpde_gamma.fgv", argv[2]);

@@ -321,3 +321,31 @@ def test_gamma_matches_reference_gamma():
     rel = np.abs(mine - g["gamma"]) / np.abs(g["gamma"])
     assert rel.max() <= 4e-15, (rel.max(), g["x"][np.argmax(rel)])
     assert rel[:24].max() <= 4e-15          # the configurations' orders come first
+
+
+@pytest.mark.parametrize("kform", [1, 2])
+def test_richards_lod_replays_reference_run(kform):
+    """The reference's Richards problem (analytic_test 0: van Genuchten-Mualem water content,
+    k_form 1 VGM or 2 Averianov conductivity, no irrigation, zero-flux bottom and sides) in its 3D
+    LOD mode with the history, 40 steps on 6^3 cells: the oracle forms every line's coefficients
+    from the grid as the reference's A_/B/R do (fpde_hpc_1d.cpp:3095-3142 with KK/inv_dw_dh
+    :2493-2657) and the surface condition from the step's evaporation rate, and replays every
+    grid - bit for bit for k_form 2; for k_form 1 one value of step 10 rounds one ulp apart,
+    4e-16 at most over the run."""
+    g = fgv.load(golden_path(f"fpde_richards_k{kform}"))
+    dims = (int(g["sN"]), int(g["M"]), int(g["K"]))
+    U = g["U0"].copy()
+    steps = len(g["tau"])
+    hist = np.zeros((steps,) + U.shape)
+    off = g["kb_off"].astype(int)
+    worst = 0.0
+    for n in range(steps):
+        kb = g["kb_flat"][off[n]:off[n + 1]]
+        S = oracle.lod_step_richards(dims, U, hist, n, kb if n else np.zeros(1), g["tau"], g["Da"], g["kkk0"][n],
+                                     g["sZ"], g["sdL"], g["dLx"], g["dLy"], kform, g["k_sat"], g["E"][n], g["Rp"][n],
+                                     want_S=True)
+        worst = max(worst, float(np.max(np.abs(U - g["U"][n])) / np.max(np.abs(g["U"][n]))))
+        if n > 0:                                   # the history sums on the K-pass nodes
+            sl = (slice(1, dims[2] + 1), slice(1, dims[1]), slice(1, dims[0]))
+            assert np.allclose(S[sl], g["S"][n][sl], rtol=1e-13, atol=1e-13 * np.max(np.abs(g["S"][n][sl])))
+    assert worst <= (0.0 if kform == 2 else 1e-14), worst
