@@ -31,11 +31,17 @@ class LineDesc(C.Structure):
                 ("source_rows", c_int), ("tuning", C.POINTER(LineTuning)), ("restrict_eps", c_dbl)]
 
 
+class Richards(C.Structure):
+    _fields_ = [("k_form", c_int), ("k_sat", c_dbl), ("sZ", c_vp), ("dL", c_vp * 3), ("evaporation", c_vp),
+                ("evaporation_rows", c_int)]
+
+
 class Lod3dDesc(C.Structure):
     _fields_ = [("sN", c_int), ("M", c_int), ("K", c_int), ("alpha", c_dbl), ("tau", c_dbl), ("Da", c_dbl),
                 ("left_kind", c_int * 3), ("right_kind", c_int * 3), ("dLN", c_dbl * 3), ("precision", c_int),
                 ("max_steps", c_int), ("lag_weights", c_vp), ("source", c_vp), ("source_rows", c_int),
-                ("bc", c_vp), ("bc_rows", c_int), ("restrict_eps", c_dbl), ("series_terms", c_int)]
+                ("bc", c_vp), ("bc_rows", c_int), ("restrict_eps", c_dbl), ("series_terms", c_int),
+                ("richards", C.POINTER(Richards))]
 
 
 class ColumnDesc(C.Structure):

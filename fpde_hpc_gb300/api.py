@@ -3,7 +3,7 @@ import ctypes as C
 
 import numpy as np
 
-from ._lib import ColumnDesc, LineDesc, LineTuning, Lod3dDesc, check, load
+from ._lib import ColumnDesc, LineDesc, LineTuning, Lod3dDesc, Richards, check, load
 
 FP64, SPLIT_BF16, SPLIT_F16 = 0, 1, 2
 
@@ -341,7 +341,10 @@ class Lod3D:
 
     def __init__(self, ctx, dims, alpha, tau, Da, coefA, coefB, coefRlap, u0, max_steps, left_kind=(0, 0, 0),
                  right_kind=(0, 0, 0), dLN=(0.0, 0.0, 0.0), source=None, bc=None, lag_weights=None,
-                 precision=FP64, restrict_eps=0.0, series_terms=0):
+                 precision=FP64, restrict_eps=0.0, series_terms=0, richards=None):
+        """richards: optional dict(k_form, k_sat, sZ, dL=(sdL, dLx, dLy), evaporation) - the
+        reference's Richards problem, coefficients formed from the grid every step (coefA/B/Rlap
+        may then be None)."""
         sN, M, K = dims
         self.ctx, self.dims = ctx, dims
         self.shape = (K + 2, M + 2, sN + 2)
@@ -370,10 +373,26 @@ class Lod3D:
                 raise ValueError("lag_weights needs max_steps + 1 values")
             keep.append(w)
             d.lag_weights = w.ctypes.data
-        cs = [np.ascontiguousarray(x, dtype=np.float64) for x in (coefA, coefB, coefRlap)]
-        for c in cs:
-            if c.shape != (3,) + self.shape:
-                raise ValueError("coefficient grids need shape (3, K+2, M+2, sN+2)")
+        if richards is not None:
+            arrs = [np.ascontiguousarray(richards[k], dtype=np.float64) for k in ("sZ", "evaporation")]
+            dls = [np.ascontiguousarray(x, dtype=np.float64) for x in richards["dL"]]
+            if len(arrs[0]) < sN + 2 or any(len(x) < n + 2 for x, n in zip(dls, (sN, M, K))):
+                raise ValueError("richards: sZ needs sN+2 values, dL[p] intervals+2")
+            keep.extend(arrs + dls)
+            r = Richards(k_form=int(richards["k_form"]), k_sat=float(richards["k_sat"]), sZ=arrs[0].ctypes.data,
+                         evaporation=arrs[1].ctypes.data, evaporation_rows=len(arrs[1]))
+            for q in range(3):
+                r.dL[q] = dls[q].ctypes.data
+            keep.append(r)
+            d.richards = C.pointer(r)
+        if coefA is None and richards is not None:
+            cs = [None, None, None]
+        else:
+            cs = [np.ascontiguousarray(x, dtype=np.float64) for x in (coefA, coefB, coefRlap)]
+            for c in cs:
+                if c.shape != (3,) + self.shape:
+                    raise ValueError("coefficient grids need shape (3, K+2, M+2, sN+2)")
+        self._keep = keep
         u0 = np.ascontiguousarray(u0, dtype=np.float64)
         self.h = C.c_void_p()
         check(ctx.lib.fpde_lod3d_create(ctx.h, C.byref(d), *(_ptr(x) for x in cs), _ptr(u0), C.byref(self.h)),

@@ -35,6 +35,7 @@
 #include "common.cuh"
 #include "kernels.cuh"
 #include "graph_cache.cuh"
+#include "richards.cuh"
 #include "tc_far.cuh"
 #include "ff.cuh"
 
@@ -129,6 +130,85 @@ __global__ void __launch_bounds__(128) k_lod_pass(LodPassArgs p)
         }
     }
     p.U[base] = fma(__ldg(p.al + line), u, g0);                   // Al[1] U[1] + Bt[1]
+}
+
+// The reference's Richards problem (analytic_test 0): every line's coefficients change with the
+// solution, so nothing is precomputed. One thread per line forms, node by node, the suction
+// P = -(U - i sZ[q]) (i the node's sN index: q in the sN pass, the line's first index otherwise;
+// wetness / inv_dw_dh :2504-2512, :2546-2554), the closures KK and inv_dw_dh (richards.cuh) and
+// A_ = KK(q-1) iw(q) / (dL_q dL_{q-1}), B = KK(q) iw(q) / dL_q^2,
+// R = iw(q) (KK(q)/dL_q^2 + KK(q-1)/(dL_q dL_{q-1})) + Da kkk0/tau (:3095-3142), and runs the
+// Thomas recurrences of al1 / bt1 / U1 on them in the reference's order, without contracted
+// multiply-adds. Left end: the sN pass takes the first-order surface condition (al1 :4004-4012,
+// bc0 :4493-4500) with Uc = dL_0 E / KK(1) (Uc :3036-3070, no irrigation); the other passes
+// zero flux. Right end: U1's flux closure (:4687-4719) with zero flux.
+struct LodRichArgs {
+    const double *sZ;       // sN+2 coordinates along the sN axis
+    const double *dL;       // this pass's steps, Nl+2 values
+    double *al;             // scratch: Al[q+1] at q * lines + line
+    double ksat, lamR, E;
+    int kform, pass;
+};
+
+__global__ void __launch_bounds__(128) k_lod_pass_rich(LodPassArgs p, LodRichArgs r)
+{
+    const int line = blockIdx.x * blockDim.x + threadIdx.x;
+    if (line >= p.lines) return;
+    const int a = line % p.n1, b = line / p.n1;
+    const int64_t base = (int64_t)(1 + a) * p.s1 + (int64_t)(1 + b) * p.s2;
+    const int Nl = p.Nl, L = p.lines;
+    auto suction = [&](int q, double u) {
+        const double i = r.pass == 0 ? (double)q : (double)(1 + a);
+        return -__dadd_rn(u, -__dmul_rn(i, r.sZ[q]));
+    };
+    const double P0 = suction(0, p.U[base]);
+    double kk_prev = rich_KK(P0, r.kform, r.ksat);                       // KK(0)
+    double al = 1.0, y = 0.0;                                           // Al[1], Bt[1]
+    if (r.pass == 0) {
+        const double kk1 = rich_KK(suction(1, p.U[base + p.st]), r.kform, r.ksat);
+        const double Uc = __ddiv_rn(__dmul_rn(r.dL[0], r.E - 0.0), kk1);
+        if (rich_inv_dw_dh(P0) != RICH_SATURATED) {
+            y = -Uc;
+        } else {
+            al = 0.0;
+            y = __ddiv_rn(__dmul_rn(-Uc, kk1), r.dL[0]);
+        }
+    }
+    const double al1 = al, g0 = y;
+    double uold_last = 0.0;
+    for (int q = 1; q < Nl; ++q) {
+        const int64_t id = base + (int64_t)q * p.st;
+        const double u = p.U[id];
+        if (q == Nl - 1) uold_last = u;
+        const double P = suction(q, u);
+        const double kk = rich_KK(P, r.kform, r.ksat), iw = rich_inv_dw_dh(P);
+        const double dq = r.dL[q], dm = r.dL[q - 1];
+        const double dqq = __dmul_rn(dq, dq), dqm = __dmul_rn(dq, dm);
+        const double A = __ddiv_rn(__dmul_rn(kk_prev, iw), dqm);
+        const double B = __ddiv_rn(__dmul_rn(kk, iw), dqq);
+        const double R = __dadd_rn(__dmul_rn(iw, __dadd_rn(__ddiv_rn(kk, dqq), __ddiv_rn(kk_prev, dqm))), r.lamR);
+        const double aln = __ddiv_rn(B, __dadd_rn(R, -__dmul_rn(A, al)));    // Al[q+1]
+        double sv = 0.0;
+        for (int k = 0; k < p.KS; ++k) sv += __ldcg(p.part + (int64_t)k * p.pstride + id);
+        const double om = __dadd_rn(__dadd_rn(-__dmul_rn(p.lam, u), p.rp ? __ldg(p.rp + id) : 0.0), sv);
+        y = __dmul_rn(__ddiv_rn(aln, B), __dadd_rn(__dmul_rn(A, y), -om));  // Bt[q+1]
+        r.al[(int64_t)q * L + line] = aln;
+        p.U[id] = y;
+        al = aln;
+        kk_prev = kk;
+    }
+    double uN;                                                          // flux closure, zero flux
+    if (fabs(y) > 1e-15) uN = (fabs(1.0 - al) > 1e-15) ? __ddiv_rn(y + 0.0, 1.0 - al) : uold_last;
+    else uN = (fabs(1.0 - al) > 1e-15) ? 0.0 : uold_last;
+    p.U[base + (int64_t)Nl * p.st] = uN;
+    p.U[base + (int64_t)(Nl + 1) * p.st] = uN;                          // ghost copy (U1 :4792)
+    double u = uN;
+    for (int q = Nl - 1; q >= 1; --q) {
+        const int64_t id = base + (int64_t)q * p.st;
+        u = __dadd_rn(__dmul_rn(r.al[(int64_t)q * L + line], u), p.U[id]);
+        p.U[id] = u;
+    }
+    p.U[base] = __dadd_rn(__dmul_rn(al1, u), g0);                       // Al[1] U[1] + Bt[1]
 }
 
 // Segmented pass: LSEGS threads (adjacent lanes) per line, each sweeping one segment of up to
@@ -350,6 +430,12 @@ struct fpde_lod3d {
     double *ring = nullptr, *cfar = nullptr, *wlag = nullptr, *Sn = nullptr;
     float2 *ringf = nullptr, *wff = nullptr;  // the ring and the lag weights as float pairs
     FarPlan3 plan3;
+    // Richards problem (desc.richards): coefficients from the solution every step
+    bool rich = false;
+    int rkform = 0;
+    double rksat = 0.0;
+    double *rsZ = nullptr, *rdL[3] = {nullptr, nullptr, nullptr}, *ral = nullptr;
+    std::vector<double> rE;                   // evaporation rate per step
     int64_t n_done = 0;
     GraphCache<int> graphs;                        // captured runs (at least GRAPH_MIN_STEPS steps)
 };
@@ -386,7 +472,13 @@ static int lod_launch_pass(fpde_lod3d *L, cudaStream_t st, int pass, int64_t n, 
     a.rkind = L->d.right_kind[pass];
     a.dLN = L->d.dLN[pass];
     if (a.lines <= 0) return FPDE_OK;
-    if (L->seglen[pass] > 0) {
+    if (L->rich) {
+        LodRichArgs r;
+        r.sZ = L->rsZ; r.dL = L->rdL[pass]; r.al = L->ral;
+        r.ksat = L->rksat; r.lamR = L->lamR; r.kform = L->rkform; r.pass = pass;
+        r.E = L->rE[(size_t)std::min<int64_t>(n, (int64_t)L->rE.size() - 1)];
+        k_lod_pass_rich<<<(unsigned)((a.lines + 127) / 128), 128, 0, st>>>(a, r);
+    } else if (L->seglen[pass] > 0) {
         LodSegArgs sg;
         sg.KF = L->cKF[pass]; sg.CB = L->cCB[pass]; sg.PF = L->cPF[pass]; sg.seglen = L->seglen[pass];
         const int64_t threads = (int64_t)a.lines * LSEGS;
@@ -550,7 +642,10 @@ int fpde_lod3d_destroy(fpde_lod3d *L)
         dev_free(L->cKF[q]);
         dev_free(L->cCB[q]);
         dev_free(L->cPF[q]);
+        dev_free(L->rdL[q]);
     }
+    dev_free(L->rsZ);
+    dev_free(L->ral);
     delete L;
     return FPDE_OK;
 }
@@ -559,11 +654,22 @@ int fpde_lod3d_create(fpde_ctx *ctx, const fpde_lod3d_desc *desc, const double *
                       const double *coefRlap, const double *u0, fpde_lod3d **out)
 {
     clear_error();
-    FPDE_CHECK_ARG(out && desc && coefA && coefB && coefRlap && u0, "null argument");
+    FPDE_CHECK_ARG(out && desc && u0, "null argument");
     *out = nullptr;
     int rc = ctx_enter(ctx);
     if (rc) return rc;
     const fpde_lod3d_desc &d = *desc;
+    const fpde_richards *rich = d.richards;
+    FPDE_CHECK_ARG(rich || (coefA && coefB && coefRlap), "null coefficient grids");
+    if (rich) {
+        FPDE_CHECK_ARG(rich->k_form == 1 || rich->k_form == 2, "richards: k_form must be 1 or 2");
+        FPDE_CHECK_ARG(rich->k_sat > 0.0 && std::isfinite(rich->k_sat), "richards: k_sat must be positive");
+        FPDE_CHECK_ARG(rich->sZ && rich->dL[0] && rich->dL[1] && rich->dL[2], "richards: sZ and dL[3] required");
+        FPDE_CHECK_ARG(rich->evaporation && rich->evaporation_rows >= 1, "richards: evaporation rows required");
+        FPDE_CHECK_ARG(d.series_terms == 0, "richards: no series expansion");
+        FPDE_CHECK_ARG(d.M <= d.sN + 1 && d.K <= d.sN + 1,
+                       "richards: M and K at most sN + 1 (suctions index sZ by positions along every pass)");
+    }
     FPDE_CHECK_ARG(d.sN >= 2 && d.M >= 2 && d.K >= 2, "every axis needs at least 2 intervals");
     FPDE_CHECK_ARG(d.lag_weights || (d.alpha > 0.0 && d.alpha < 1.0), "alpha must be in (0, 1)");
     FPDE_CHECK_ARG(std::isfinite(d.restrict_eps) && d.restrict_eps >= 0.0, "restrict_eps must be >= 0");
@@ -661,10 +767,31 @@ int fpde_lod3d_create(fpde_ctx *ctx, const fpde_lod3d_desc *desc, const double *
         L->bc_rows = std::min(d.bc_rows, d.max_steps);
         fail = dev_alloc((void **)&L->bc, (size_t)L->bc_rows * gbytes);
     }
+    cudaStream_t st = ctx->stream;
+    if (!fail && rich) {                       // closures' inputs; no precomputed coefficients
+        L->rich = true;
+        L->rkform = rich->k_form;
+        L->rksat = rich->k_sat;
+        L->rE.assign(rich->evaporation, rich->evaporation + std::min(rich->evaporation_rows, d.max_steps));
+        const int dims[3] = {d.sN, d.M, d.K};
+        int64_t scratch = 0;
+        for (int pass = 0; pass < 3 && !fail; ++pass) {
+            int Nl, n1, n2;
+            int64_t s1, s2, stp;
+            pass_geometry(L, pass, &Nl, &n1, &n2, &s1, &s2, &stp);
+            L->lines[pass] = n1 * n2;
+            scratch = std::max<int64_t>(scratch, (int64_t)(Nl + 1) * n1 * n2);
+            fail = dev_alloc((void **)&L->rdL[pass], (size_t)(dims[pass] + 2) * sizeof(double)) ||
+                   cudaMemcpy(L->rdL[pass], rich->dL[pass], (size_t)(dims[pass] + 2) * sizeof(double),
+                              cudaMemcpyHostToDevice) != cudaSuccess;
+        }
+        fail = fail || dev_alloc((void **)&L->rsZ, (size_t)(d.sN + 2) * sizeof(double)) ||
+               cudaMemcpy(L->rsZ, rich->sZ, (size_t)(d.sN + 2) * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess ||
+               dev_alloc((void **)&L->ral, (size_t)scratch * sizeof(double));
+    }
     // per-pass line coefficients, evaluated in the reference's order (al1 :4002-4027)
     std::vector<double> hA, hg, hal;
-    cudaStream_t st = ctx->stream;
-    for (int pass = 0; pass < 3 && !fail; ++pass) {
+    for (int pass = 0; pass < 3 && !fail && !rich; ++pass) {
         int Nl, n1, n2;
         int64_t s1, s2, stp;
         pass_geometry(L, pass, &Nl, &n1, &n2, &s1, &s2, &stp);
@@ -779,6 +906,7 @@ int fpde_lod3d_create(fpde_ctx *ctx, const fpde_lod3d_desc *desc, const double *
     L->d.lag_weights = nullptr;                 // host pointers are not kept
     L->d.source = nullptr;
     L->d.bc = nullptr;
+    L->d.richards = nullptr;
     *out = L;
     return FPDE_OK;
 }

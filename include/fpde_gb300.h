@@ -379,6 +379,25 @@ int fpde_line_coefs(int64_t N, const double *k, const double *iw, const double *
 
 /* ------------------------------------------------------------------ 3D LOD */
 
+/* The reference's Richards problem (fpde_hpc_1d.cpp with analytic_test 0: water transport with
+ * the van Genuchten-Mualem water content of cv_form 4, wetness / inv_dw_dh :2493-2566, and the
+ * conductivity KK = Kr(wetness) k_sat :2625-2655; no irrigation, bottom_cond 0). Its line
+ * coefficients A_/B/R (:3095-3142) depend on the solution and are formed on the device from the
+ * grid before every line solve, with the reference's mode-3 suction P = -(U - i sZ[p]) (i the
+ * node's index along the sN axis, p its position along the pass; :2504-2512, :2546-2554). The sN
+ * pass starts with the reference's first-order surface condition (al1 :4004-4012, bc0
+ * :4493-4500: flux -Uc with Uc = dL[0] E / KK(1), or Dirichlet -Uc KK(1)/dL[0] where node 0 is
+ * saturated); every other line end has zero flux (al1's Al[1] = 1, U1's flux closure). */
+typedef struct fpde_richards {
+    int k_form;                 /* 1: van Genuchten-Mualem Kr, 2: Averianov Kr = S^3.5 */
+    double k_sat;               /* saturated filtration coefficient (the reference's k) */
+    const double *sZ;           /* host, sN+2 node coordinates along the sN axis */
+    const double *dL[3];        /* host, per pass (0 sN, 1 _M, 2 K) the steps dL[p], intervals+2 values */
+    const double *evaporation;  /* host, evaporation rate E of every step (Ev * day_night_coef);
+                                   step n uses row min(n, evaporation_rows-1) */
+    int evaporation_rows;
+} fpde_richards;
+
 /* The 3D locally-one-dimensional step of the reference (calc_step, mode 3 with implicit3d 0
  * and split3d 0, fpde_hpc_1d.cpp:5144-5779): per time step the history sum, then Thomas
  * passes along k (K, with the history and the source Rp, Om1 :4165-4268 for m3d_c == 2),
@@ -407,6 +426,9 @@ typedef struct fpde_lod3d_desc {
                                carried from step to step instead of the stored history, S = sum_j
                                v_j H_j / tau (FPDE_PREC_FP64, Caputo weights, g(t) = t; the history
                                then keeps only the newest increment) */
+    const fpde_richards *richards; /* optional: the Richards problem (coefficients from the solution
+                               every step; coefA/B/Rlap, the boundary kinds and bc are then unused
+                               and may be NULL; needs M, K <= sN + 1) */
 } fpde_lod3d_desc;
 
 /* coefA/B/Rlap: three host grids each (pass 0 = sN, 1 = _M, 2 = K) of the line coefficients at

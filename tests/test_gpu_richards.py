@@ -1,0 +1,83 @@
+"""The reference's Richards problem on the GPU: solution-dependent line coefficients.
+
+The reference's analytic_test 0 (van Genuchten-Mualem water content, k_form 1 VGM and 2 Averianov
+conductivity, no irrigation, zero-flux bottom and sides; fpde_hpc_1d.cpp:2493-2657, :3095-3142)
+changes every line's A_/B/R with the solution, so the 3D LOD forms them on the device before
+each line solve (fpde_richards). Checks:
+  * replay of the reference's own 40-step run on 6^3 cells (fixtures fpde_richards_k1/k2, the
+    K-pass source and the evaporation rate of every step recorded by the pin harness): every grid
+    within 1e-12 of the reference's (the device's pow and the host's differ by an ulp or two);
+  * the split path (far history on the tensor cores) within 1e-7 of FP64 on the same run.
+"""
+import numpy as np
+import pytest
+
+import fgv
+from conftest import golden_path
+
+pytestmark = pytest.mark.gpu
+
+
+def relmax(a, b):
+    return float(np.max(np.abs(a - b)) / np.max(np.abs(b)))
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    import fpde_hpc_gb300 as fp
+    c = fp.Context(0)
+    yield c
+    c.close()
+
+
+def _lod(ctx, g, kform, precision=0, steps=None):
+    import fpde_hpc_gb300 as fp
+    dims = (int(g["sN"]), int(g["M"]), int(g["K"]))
+    steps = steps or len(g["tau"])
+    rich = dict(k_form=kform, k_sat=g["k_sat"], sZ=g["sZ"], dL=(g["sdL"], g["dLx"], g["dLy"]), evaporation=g["E"])
+    return fp.Lod3D(ctx, dims, g["alpha"], g["tau"][0], g["Da"], None, None, None, g["U0"], steps,
+                    source=g["Rp"], richards=rich, precision=precision)
+
+
+@pytest.mark.parametrize("kform", [1, 2])
+def test_richards_lod_replays_reference_run(ctx, kform):
+    g = fgv.load(golden_path(f"fpde_richards_k{kform}"))
+    lod = _lod(ctx, g, kform)
+    worst = 0.0
+    for n in range(len(g["tau"])):
+        lod.run(1)
+        worst = max(worst, relmax(lod.state(), g["U"][n]))
+    lod.close()
+    print(f"Richards k_form {kform}: every level vs the reference's run, max rel {worst:.2e}")
+    assert worst <= 1e-12
+
+
+@pytest.mark.parametrize("kform", [1, 2])
+def test_richards_lod_runs_in_one_call(ctx, kform):
+    g = fgv.load(golden_path(f"fpde_richards_k{kform}"))
+    steps = len(g["tau"])
+    lod = _lod(ctx, g, kform)
+    lod.run(steps)
+    e64 = relmax(lod.state(), g["U"][-1])
+    lod.close()
+    print(f"Richards k_form {kform}, {steps} steps in one call: FP64 vs reference {e64:.2e}")
+    assert e64 <= 1e-12
+
+
+@pytest.mark.parametrize("kform", [1, 2])
+def test_richards_lod_split_history_vs_fp64(ctx, kform):
+    """200 steps (the recorded source and evaporation rate of the last step repeat): the far
+    history of three 64-step blocks on the tensor cores, the coefficients from the solution."""
+    g = fgv.load(golden_path(f"fpde_richards_k{kform}"))
+    out = []
+    for prec in (0, 3):
+        lod = _lod(ctx, g, kform, prec, steps=200)
+        states = []
+        for _ in range(8):
+            lod.run(25)
+            states.append(lod.state())
+        out.append(states)
+        lod.close()
+    errs = [relmax(x, y) for x, y in zip(out[1], out[0])]
+    print(f"Richards k_form {kform}, 200 steps, split vs FP64 at 8 checkpoints: max {max(errs):.2e}")
+    assert max(errs) <= 1e-7
