@@ -23,17 +23,18 @@ class LineTuning(C.Structure):
                 ("far_super", c_int), ("ms_per_step", c_dbl)]
 
 
+class Richards(C.Structure):
+    _fields_ = [("k_form", c_int), ("k_sat", c_dbl), ("sZ", c_vp), ("dL", c_vp * 3), ("evaporation", c_vp),
+                ("evaporation_rows", c_int)]
+
+
 class LineDesc(C.Structure):
     _fields_ = [("N", c_i64), ("alpha", c_dbl), ("tau", c_dbl), ("Da", c_dbl),
                 ("left_kind", c_int), ("left_value", c_dbl), ("right_kind", c_int),
                 ("right_value", c_dbl), ("dLN", c_dbl), ("precision", c_int), ("block", c_int),
                 ("max_steps", c_int), ("lag_weights", c_vp), ("theta", c_dbl), ("source", c_vp),
-                ("source_rows", c_int), ("tuning", C.POINTER(LineTuning)), ("restrict_eps", c_dbl)]
-
-
-class Richards(C.Structure):
-    _fields_ = [("k_form", c_int), ("k_sat", c_dbl), ("sZ", c_vp), ("dL", c_vp * 3), ("evaporation", c_vp),
-                ("evaporation_rows", c_int)]
+                ("source_rows", c_int), ("tuning", C.POINTER(LineTuning)), ("restrict_eps", c_dbl),
+                ("richards", C.POINTER(Richards))]
 
 
 class Lod3dDesc(C.Structure):

@@ -244,12 +244,14 @@ class Line:
 
     def __init__(self, ctx, N, alpha, tau, Da, A, B, Rlap, u0, max_steps, left=(0, 0.0), right=(0, 0.0),
                  dLN=0.0, precision=FP64, block=0, lag_weights=None, theta=0.0, source=None, tuning=None,
-                 restrict_eps=0.0):
+                 restrict_eps=0.0, richards=None):
         """lag_weights (max_steps+1 values, w[0] local) replace the Caputo L1 weights (the
         distributed-order equation passes fused weights / tau); theta is the explicit fraction
         of the space operator; source is one row or a (rows, N+1) array of per-step rows;
         restrict_eps > 0 drops the lags from the first one whose kb = w tau / Da is below it
-        (the reference's restricted summing)."""
+        (the reference's restricted summing); richards = dict(k_form, k_sat, Z, dL, evaporation)
+        selects the Richards problem (A, B, Rlap formed from the state every step; they may be
+        None)."""
         self.ctx, self.N = ctx, N
         d = LineDesc(N=N, alpha=alpha, tau=tau, Da=Da, left_kind=left[0], left_value=left[1],
                      right_kind=right[0], right_value=right[1], dLN=dLN, precision=precision, block=block,
@@ -271,8 +273,17 @@ class Line:
         if tuning is not None:
             self._keep.append(tuning)
             d.tuning = C.pointer(tuning)
+        if richards is not None:
+            z, dl, ev = (np.ascontiguousarray(richards[k], dtype=np.float64) for k in ("Z", "dL", "evaporation"))
+            if len(z) < N + 1 or len(dl) < N + 1:
+                raise ValueError("richards: Z and dL need N + 1 values")
+            r = Richards(k_form=int(richards["k_form"]), k_sat=float(richards["k_sat"]), sZ=z.ctypes.data,
+                         evaporation=ev.ctypes.data, evaporation_rows=len(np.atleast_1d(ev)))
+            r.dL[0] = dl.ctypes.data
+            self._keep.extend([z, dl, ev, r])
+            d.richards = C.pointer(r)
         self.desc = d
-        arrs = [np.ascontiguousarray(x, dtype=np.float64) for x in (A, B, Rlap, u0)]
+        arrs = [None if x is None else np.ascontiguousarray(x, dtype=np.float64) for x in (A, B, Rlap, u0)]
         self.h = C.c_void_p()
         check(ctx.lib.fpde_line_create(ctx.h, C.byref(d), *(_ptr(x) for x in arrs), C.byref(self.h)),
               "fpde_line_create")

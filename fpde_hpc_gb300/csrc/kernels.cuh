@@ -72,3 +72,22 @@ int launch_near_history_ff(cudaStream_t st, const float2 *ringf, int64_t P, int 
                            int64_t wstride = 0);
 
 }  // namespace fpde
+
+namespace fpde {
+
+// One step of a line with solution-dependent coefficients (the Richards problem, rich_line.cu).
+struct RichLineArgs {
+    double *U;                           // N+1 values, advanced in place
+    const double *Z, *dL;                // node coordinates and steps (N+1)
+    const double *part;                  // history partials (S = sum over KS rows of pstride), or KS = 0
+    int KS = 0;
+    int64_t pstride = 0;
+    const double *src = nullptr;         // optional source row (N+1)
+    double *cA, *cB, *cR, *cOm, *al, *bt;   // scratch, N+1 each (al/bt: Al[i], Bt[i])
+    double lam = 0, lamR = 0, E = 0, ksat = 0;
+    int kform = 1, N = 0, rkind = 0;
+    double gN = 0, dLN = 0;              // right end: Dirichlet value, or the flux and last step
+};
+int launch_rich_line_step(cudaStream_t st, const RichLineArgs &a);
+
+}  // namespace fpde

@@ -1069,6 +1069,13 @@ struct fpde_line {
     FarPlan3 plan3;
     int64_t n_done = 0;
     int graph_min = GRAPH_MIN_STEPS;          // shortest run replayed from a graph
+    // Richards problem (desc.richards): coefficients from the solution every step (rich_line.cu)
+    bool rich = false;
+    int rkform = 1;
+    double rksat = 0.0;
+    double *rZ = nullptr, *rdL = nullptr, *rA = nullptr, *rB = nullptr, *rR = nullptr, *rOm = nullptr,
+           *ral = nullptr, *rbt = nullptr, *last = nullptr, *Sn = nullptr;
+    std::vector<double> rE;
     // probes: CUDA events around kernels inside the captured graph
     struct Probe { int kind; int64_t n; double bytes, flops; int ev; int steps; };
     int probe_every = 0;
@@ -1203,6 +1210,20 @@ static int line_launch_block(fpde_line *L, cudaStream_t st, int64_t nb0, int j0,
 #define PROBE_REC(ev, i) \
     do { if (ev) FPDE_CUDA(record_probe_event((ev)[i], st)); } while (0)
 
+// One Richards step (rich_line.cu): coefficients from the current state, then the solve.
+static int rich_step(fpde_line *L, cudaStream_t st, int64_t n, const double *part, int KS)
+{
+    RichLineArgs a;
+    a.U = L->U; a.Z = L->rZ; a.dL = L->rdL;
+    a.part = part; a.KS = KS; a.pstride = L->P;
+    a.src = L->srcd ? L->srcd + (n < L->src_rows ? n : L->src_rows - 1) * (L->N + 1) : nullptr;
+    a.cA = L->rA; a.cB = L->rB; a.cR = L->rR; a.cOm = L->rOm; a.al = L->ral; a.bt = L->rbt;
+    a.lam = L->lam; a.lamR = L->lamR; a.ksat = L->rksat; a.kform = L->rkform;
+    a.E = L->rE[(size_t)std::min<int64_t>(n, (int64_t)L->rE.size() - 1)];
+    a.N = (int)L->N; a.rkind = L->d.right_kind; a.gN = L->d.right_value; a.dLN = L->d.dLN;
+    return launch_rich_line_step(st, a);
+}
+
 // Enqueue steps [n0, n0+steps) on st; returns the number of kernels enqueued via *nk.
 static int line_enqueue(fpde_line *L, cudaStream_t st, int64_t n0, int steps, int64_t *nk)
 {
@@ -1229,7 +1250,13 @@ static int line_enqueue(fpde_line *L, cudaStream_t st, int64_t n0, int steps, in
             }
             ev = probe_step ? probe_begin(L, 2, n, 0.0, 0.0) : nullptr;
             PROBE_REC(ev, 0);
-            if ((rc = line_launch_solve(L, st, n, L->part, KS, L->P, L->D + n * L->P, 1))) return rc;
+            if (L->rich) {                             // coefficients from the solution, then the increment
+                if ((rc = rich_step(L, st, n, L->part, KS))) return rc;
+                if ((rc = launch_append(st, L->U, L->last, L->D + n * L->P, L->N + 1, L->P))) return rc;
+                k += 2;
+            } else if ((rc = line_launch_solve(L, st, n, L->part, KS, L->P, L->D + n * L->P, 1))) {
+                return rc;
+            }
             PROBE_REC(ev, 1);
             ++k;
         } else {
@@ -1315,8 +1342,29 @@ static int line_enqueue(fpde_line *L, cudaStream_t st, int64_t n0, int steps, in
                 PROBE_REC(ev, 1);
                 ++k;
             }
-            // the rest of this block (or of the requested range) in one persistent launch
             const int nst = (int)std::min<int64_t>(BLK - j, n0 + steps - n);
+            if (L->rich) {
+                // per step: far partials + the block's earlier rows (float-float), the solve with
+                // coefficients from the solution, the increment into the ring
+                for (int q = j; q < j + nst; ++q) {
+                    const int64_t m = nb0 + q;
+                    int KSn = 0;
+                    if (m >= 1) {
+                        if ((rc = launch_near_history_ff(st, L->ringf, L->P, q, L->wff, L->cfar, splits, 1, L->Sn)))
+                            return rc;
+                        KSn = 1;
+                        ++k;
+                    }
+                    if ((rc = rich_step(L, st, m, L->Sn, KSn))) return rc;
+                    if ((rc = launch_append_ff(st, L->U, L->last, L->ring + (int64_t)q * L->P,
+                                               L->ringf + (int64_t)q * L->P, L->N + 1, L->P)))
+                        return rc;
+                    k += 3;
+                }
+                n += nst - 1;
+                continue;
+            }
+            // the rest of this block (or of the requested range) in one persistent launch
             double bytes = 0.0, flops = 0.0;
             for (int q = j; q < j + nst; ++q) {                  // far fold + near ring + state
                 bytes += 8.0 * nodes_hist * (splits + q + 2);
@@ -1383,6 +1431,7 @@ int fpde_line_destroy(fpde_line *L)
     dev_free(L->slots);
     dev_free(L->exps);
     dev_free(L->barrier);
+    for (double *p : {L->rZ, L->rdL, L->rA, L->rB, L->rR, L->rOm, L->ral, L->rbt, L->last, L->Sn}) dev_free(p);
     delete L;
     return FPDE_OK;
 }
@@ -1391,12 +1440,32 @@ int fpde_line_create(fpde_ctx *ctx, const fpde_line_desc *desc, const double *A,
                      const double *Rlap, const double *u0, fpde_line **out)
 {
     clear_error();
-    FPDE_CHECK_ARG(out && desc && A && B && Rlap && u0, "null argument");
+    FPDE_CHECK_ARG(out && desc && u0, "null argument");
     *out = nullptr;
     int rc = ctx_enter(ctx);
     if (rc) return rc;
     const fpde_line_desc &d = *desc;
     FPDE_CHECK_ARG(d.N >= 2, "N must be >= 2");
+    const fpde_richards *rich = d.richards;
+    std::vector<double> placeholder;
+    if (rich) {
+        FPDE_CHECK_ARG(rich->k_form == 1 || rich->k_form == 2, "richards: k_form must be 1 or 2");
+        FPDE_CHECK_ARG(rich->k_sat > 0.0 && std::isfinite(rich->k_sat), "richards: k_sat must be positive");
+        FPDE_CHECK_ARG(rich->sZ && rich->dL[0], "richards: node coordinates (sZ) and steps (dL[0]) required");
+        FPDE_CHECK_ARG(rich->evaporation && rich->evaporation_rows >= 1, "richards: evaporation rows required");
+        FPDE_CHECK_ARG(d.precision == FPDE_PREC_FP64 || d.precision == FPDE_PREC_SPLIT_BF16X3,
+                       "richards: FP64 or the exact three-slice split");
+        FPDE_CHECK_ARG(!d.lag_weights && d.theta == 0.0 && d.restrict_eps == 0.0,
+                       "richards: Caputo weights, no explicit part, no restricted summing");
+        if (!A || !B || !Rlap) {       // time-invariant data of the linear solves: unused, kept regular
+            placeholder.assign(3 * (size_t)(d.N + 1), 1.0);
+            for (int64_t i = 0; i <= d.N; ++i) placeholder[2 * (d.N + 1) + i] = 2.0;
+            A = placeholder.data();
+            B = A + d.N + 1;
+            Rlap = B + d.N + 1;
+        }
+    }
+    FPDE_CHECK_ARG(A && B && Rlap, "null coefficient arrays");
     FPDE_CHECK_ARG(d.lag_weights || (d.alpha > 0.0 && d.alpha < 1.0), "alpha must be in (0, 1)");
     FPDE_CHECK_ARG(!d.source || d.source_rows >= 1, "source needs source_rows >= 1");
     FPDE_CHECK_ARG(std::isfinite(d.theta), "theta must be finite");
@@ -1479,6 +1548,7 @@ int fpde_line_create(fpde_ctx *ctx, const fpde_line_desc *desc, const double *A,
         if (tu->far_super > 0) L->sbk = std::min(tu->far_super, FAR_MAX_SUPER);
     }
     L->d.tuning = nullptr;                     // not kept
+    if (rich) L->sbk = 1;                      // per-block far history; the near history per step
     L->max_steps = d.max_steps;
     L->split = split;
     L->x3 = d.precision == FPDE_PREC_SPLIT_BF16X3;
@@ -1870,6 +1940,29 @@ int fpde_line_create(fpde_ctx *ctx, const fpde_line_desc *desc, const double *A,
         cudaMemsetAsync(L->cfar, 0, (size_t)FAR_MAX_SPLITS * BLK * L->P * sizeof(double), st);
         cudaMemcpyAsync(L->wlag, wlag.data(), LW * sizeof(double), cudaMemcpyHostToDevice, st);
     }
+    if (rich) {                                // closures' inputs and the per-step scratch
+        L->rich = true;
+        L->rkform = rich->k_form;
+        L->rksat = rich->k_sat;
+        L->rE.assign(rich->evaporation, rich->evaporation + std::min(rich->evaporation_rows, d.max_steps));
+        const size_t nb1 = (size_t)(N + 1) * sizeof(double);
+        bool f2 = dev_alloc((void **)&L->rZ, nb1) || dev_alloc((void **)&L->rdL, nb1) ||
+                  dev_alloc((void **)&L->rA, nb1) || dev_alloc((void **)&L->rB, nb1) ||
+                  dev_alloc((void **)&L->rR, nb1) || dev_alloc((void **)&L->rOm, nb1) ||
+                  dev_alloc((void **)&L->ral, nb1 + sizeof(double)) || dev_alloc((void **)&L->rbt, nb1 + sizeof(double)) ||
+                  dev_alloc((void **)&L->last, L->P * sizeof(double)) ||
+                  (L->split && dev_alloc((void **)&L->Sn, L->P * sizeof(double)));
+        if (f2) {
+            std::string keep = fpde_last_error_string();
+            fpde_line_destroy(L);
+            return set_error(FPDE_ERR_NOMEM, "%s", keep.c_str());
+        }
+        cudaMemcpyAsync(L->rZ, rich->sZ, nb1, cudaMemcpyHostToDevice, st);
+        cudaMemcpyAsync(L->rdL, rich->dL[0], nb1, cudaMemcpyHostToDevice, st);
+        cudaMemsetAsync(L->last, 0, L->P * sizeof(double), st);
+        cudaMemcpyAsync(L->last, u0, nb1, cudaMemcpyHostToDevice, st);
+    }
+    L->d.richards = nullptr;                   // host pointers are not kept
     cudaError_t e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) {
         fpde_line_destroy(L);
@@ -1888,6 +1981,9 @@ int fpde_line_reset(fpde_line *L, const double *u0, int on_device)
     if (rc) return rc;
     FPDE_CUDA(cudaMemcpyAsync(L->U, u0, (L->N + 1) * sizeof(double),
                               on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, L->ctx->stream));
+    if (L->last)                               // the Richards line's previous state (increments)
+        FPDE_CUDA(cudaMemcpyAsync(L->last, L->U, (L->N + 1) * sizeof(double), cudaMemcpyDeviceToDevice,
+                                  L->ctx->stream));
     if (!on_device) FPDE_CUDA(cudaStreamSynchronize(L->ctx->stream));
     L->n_done = 0;
     return FPDE_OK;
@@ -1955,6 +2051,8 @@ int fpde_line_solve_host(fpde_line *L, const double *u0_host, int steps, double 
     if (rc) return rc;
     cudaStream_t st = L->ctx->stream;
     FPDE_CUDA(cudaMemcpyAsync(L->U, u0_host, (L->N + 1) * sizeof(double), cudaMemcpyHostToDevice, st));
+    if (L->last)
+        FPDE_CUDA(cudaMemcpyAsync(L->last, L->U, (L->N + 1) * sizeof(double), cudaMemcpyDeviceToDevice, st));
     L->n_done = 0;
     if ((rc = fpde_line_run(L, steps))) return rc;
     FPDE_CUDA(cudaMemcpyAsync(u_out_host, L->U, (L->N + 1) * sizeof(double), cudaMemcpyDeviceToHost, st));

@@ -265,6 +265,31 @@ int fpde_tridiag_solve(fpde_ctx *ctx, const double *a, const double *b, const do
 
 /* ------------------------------------------------------- 1D line problem */
 
+/* The reference's Richards problem (fpde_hpc_1d.cpp with analytic_test 0: water transport with
+ * the van Genuchten-Mualem water content of cv_form 4, wetness / inv_dw_dh :2493-2566, and the
+ * conductivity KK = Kr(wetness) k_sat :2625-2655; no irrigation, bottom_cond 0). Its line
+ * coefficients A_/B/R (:3095-3142) depend on the solution and are formed on the device from the
+ * grid before every line solve, with the reference's mode-3 suction P = -(U - i sZ[p]) (i the
+ * node's index along the sN axis, p its position along the pass; :2504-2512, :2546-2554). The sN
+ * pass starts with the reference's first-order surface condition (al1 :4004-4012, bc0
+ * :4493-4500: flux -Uc with Uc = dL[0] E / KK(1), or Dirichlet -Uc KK(1)/dL[0] where node 0 is
+ * saturated); every other line end has zero flux (al1's Al[1] = 1, U1's flux closure).
+ * A 1D line (fpde_line_desc.richards) has the same surface condition at node 0 and its own
+ * right end (right_kind / right_value / dLN: the reference's bottom_cond 1 is Dirichlet H0 - Z[N]). */
+typedef struct fpde_richards {
+    int k_form;                 /* 1: van Genuchten-Mualem Kr, 2: Averianov Kr = S^3.5 */
+    double k_sat;               /* saturated filtration coefficient (the reference's k) */
+    const double *sZ;           /* host: 3D LOD, sN+2 node coordinates along the sN axis; line, the N+1
+                                   node coordinates Z (suction P = -(U - Z), the reference's mode-1
+                                   wetness / inv_dw_dh :2499-2500, :2529) */
+    const double *dL[3];        /* host: 3D LOD, per pass (0 sN, 1 _M, 2 K) the steps dL[p],
+                                   intervals+2 values; line, dL[0] only (N+1 steps) */
+    const double *evaporation;  /* host, evaporation rate E of every step (Ev * day_night_coef);
+                                   step n uses row min(n, evaporation_rows-1) */
+    int evaporation_rows;
+} fpde_richards;
+
+
 /* Launch parameters of a line chosen by fpde_line_autotune (or by hand); 0 = the built-in rule.
  * No counterpart in the reference, whose OpenCL path fixes one work-group shape
  * (opencl_cuda_base.cpp:626-649). */
@@ -313,6 +338,9 @@ typedef struct fpde_line_desc {
                              0 keeps every lag. FPDE_PREC_FP64 and FPDE_PREC_SPLIT_BF16X3: the
                              GEMV reads only the window's rows, the far contraction only the
                              64-step blocks the window reaches. */
+    const fpde_richards *richards; /* optional: the Richards problem - A, B, Rlap formed from the state
+                             every step (those arguments of fpde_line_create may be NULL);
+                             FPDE_PREC_FP64 or FPDE_PREC_SPLIT_BF16X3, Caputo weights, theta 0 */
 } fpde_line_desc;
 
 /* Set up a line: A, B, Rlap (N+1 host values, entries 1..N-1 used; see fpde_line_coefs)
@@ -379,24 +407,6 @@ int fpde_line_coefs(int64_t N, const double *k, const double *iw, const double *
 
 /* ------------------------------------------------------------------ 3D LOD */
 
-/* The reference's Richards problem (fpde_hpc_1d.cpp with analytic_test 0: water transport with
- * the van Genuchten-Mualem water content of cv_form 4, wetness / inv_dw_dh :2493-2566, and the
- * conductivity KK = Kr(wetness) k_sat :2625-2655; no irrigation, bottom_cond 0). Its line
- * coefficients A_/B/R (:3095-3142) depend on the solution and are formed on the device from the
- * grid before every line solve, with the reference's mode-3 suction P = -(U - i sZ[p]) (i the
- * node's index along the sN axis, p its position along the pass; :2504-2512, :2546-2554). The sN
- * pass starts with the reference's first-order surface condition (al1 :4004-4012, bc0
- * :4493-4500: flux -Uc with Uc = dL[0] E / KK(1), or Dirichlet -Uc KK(1)/dL[0] where node 0 is
- * saturated); every other line end has zero flux (al1's Al[1] = 1, U1's flux closure). */
-typedef struct fpde_richards {
-    int k_form;                 /* 1: van Genuchten-Mualem Kr, 2: Averianov Kr = S^3.5 */
-    double k_sat;               /* saturated filtration coefficient (the reference's k) */
-    const double *sZ;           /* host, sN+2 node coordinates along the sN axis */
-    const double *dL[3];        /* host, per pass (0 sN, 1 _M, 2 K) the steps dL[p], intervals+2 values */
-    const double *evaporation;  /* host, evaporation rate E of every step (Ev * day_night_coef);
-                                   step n uses row min(n, evaporation_rows-1) */
-    int evaporation_rows;
-} fpde_richards;
 
 /* The 3D locally-one-dimensional step of the reference (calc_step, mode 3 with implicit3d 0
  * and split3d 0, fpde_hpc_1d.cpp:5144-5779): per time step the history sum, then Thomas

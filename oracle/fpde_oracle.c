@@ -623,6 +623,65 @@ int fo_lod_step_richards(int sN, int M, int K, double *U, double *hist, int n, c
     return 0;
 }
 
+/* A 1D line of the Richards problem with the history (the reference's column form; mode-1
+ * closures: the suction of node i is P = -(U[i] - Z[i]), wetness / inv_dw_dh :2499-2500,
+ * :2529): per step the L1 history sum, the coefficients A_/B/R from the current values, the
+ * surface condition of al1 / bc0 (first-order flux -Uc with Uc = dL[0] E / KK(1), or Dirichlet
+ * -Uc KK(1)/dL[0] where node 0 is saturated) and the right end of U1 (rtype 0 Dirichlet gN,
+ * 1 flux closure). E: the evaporation rate of every step (row min(n, erows-1)); src: optional
+ * source rows. hist receives the increments (rows of P). */
+int fo_line_run_richards(int N, double *U, double *hist, int64_t P, int steps, double tau, double alpha, double Da,
+                         const double *Z, const double *dL, int kform, double ksat, const double *E, int erows,
+                         const double *src, int src_rows, int rtype, double gN, double dLN)
+{
+    double *time = (double *)malloc(sizeof(double) * (size_t)(steps + 2));
+    double *taus = (double *)malloc(sizeof(double) * (size_t)(steps + 1));
+    double *kb = (double *)malloc(sizeof(double) * (size_t)(steps + 1));
+    double *S = (double *)calloc((size_t)N + 1, sizeof(double));
+    double *Om = (double *)calloc((size_t)N + 1, sizeof(double));
+    double *A = (double *)calloc((size_t)N + 1, sizeof(double));
+    double *B = (double *)calloc((size_t)N + 1, sizeof(double));
+    double *R = (double *)calloc((size_t)N + 1, sizeof(double));
+    double *kk = (double *)malloc(sizeof(double) * (size_t)(N + 1));
+    double *iw = (double *)malloc(sizeof(double) * (size_t)(N + 1));
+    double *Uold = (double *)malloc(sizeof(double) * (size_t)(N + 1));
+    double *Al = (double *)malloc(sizeof(double) * (size_t)(N + 2));
+    double *Bt = (double *)malloc(sizeof(double) * (size_t)(N + 2));
+    time[0] = 0.0;
+    for (int n = 0; n <= steps; n++) { taus[n] = tau; time[n + 1] = time[n] + tau; }
+    for (int n = 0; n < steps; n++) {
+        double kkk0;
+        fo_l1_weights(alpha, time, n, kb, &kkk0);
+        const double lam = Da * (kkk0 / tau), lamR = Da * kkk0 / tau;
+        memcpy(Uold, U, sizeof(double) * (size_t)(N + 1));
+        if (n > 0) fo_l1_sum(hist, P, n, kb, taus, 1, N, S);
+        for (int i = 0; i <= N; i++) {
+            const double Pi = -(U[i] - Z[i]);
+            kk[i] = rich_KK(Pi, kform, ksat);
+            iw[i] = rich_inv_dw_dh(Pi);
+        }
+        const double *sr = src ? src + (int64_t)(n < src_rows ? n : src_rows - 1) * (N + 1) : NULL;
+        for (int i = 1; i < N; i++) {
+            A[i] = kk[i - 1] * iw[i] / (dL[i] * dL[i - 1]);
+            B[i] = kk[i] * iw[i] / (dL[i] * dL[i]);
+            R[i] = iw[i] * ((kk[i] / (dL[i] * dL[i])) + (kk[i - 1] / (dL[i] * dL[i - 1]))) + lamR;
+            Om[i] = -(lam * U[i]) + (sr ? sr[i] : 0.0);
+            Om[i] += Da * S[i];
+        }
+        const double En = E[n < erows ? n : erows - 1];
+        const double Uc = dL[0] * (En - 0.0) / kk[1];
+        int lkind = 1;
+        double g0 = -Uc;
+        if (iw[0] == 1e20) { lkind = 0; g0 = -Uc * kk[1] / dL[0]; }
+        thomas_core(N, A, B, R, Om, lkind, g0, rtype, gN, dLN, U, Al, Bt);
+        double *row = hist + (int64_t)n * P;
+        for (int64_t i = 0; i < P; i++) row[i] = (i <= N) ? U[i] - Uold[i] : 0.0;
+    }
+    free(time); free(taus); free(kb); free(S); free(Om); free(A); free(B); free(R); free(kk); free(iw);
+    free(Uold); free(Al); free(Bt);
+    return 0;
+}
+
 /* ------------------------------------------------------ distributed order */
 
 static double bk_pow(double d1, double d2, double beta)   /* fr_do.cpp:129-134 */

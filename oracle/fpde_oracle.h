@@ -154,6 +154,13 @@ int fo_lod_step_richards(int sN, int M, int K, double *U, double *hist, int n, c
                          double Da, double kkk0, const double *sZ, const double *sdL, const double *dLx,
                          const double *dLy, int kform, double ksat, double E, const double *rp, double *S_out);
 
+/* A 1D Richards line with the history (mode-1 closures, P = -(U[i] - Z[i])): per step the L1
+ * sum, coefficients from the current values, the surface condition from the step's evaporation
+ * rate E[min(n, erows-1)], the right end rtype (0 Dirichlet gN, 1 flux closure). */
+int fo_line_run_richards(int N, double *U, double *hist, int64_t P, int steps, double tau, double alpha, double Da,
+                         const double *Z, const double *dL, int kform, double ksat, const double *E, int erows,
+                         const double *src, int src_rows, int rtype, double gN, double dLN);
+
 /* ---- distributed order (fr_do.cpp) ---- */
 
 /* Caputo derivative of sampled F (Cder :74-86 with an F array): DF[t] for t = 1..ntau-1,

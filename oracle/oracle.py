@@ -58,6 +58,9 @@ def load():
     lib.fo_lod_step_richards.argtypes = [i32, i32, i32, _dp, _dp, i32, _dp, _dp, d, d, _dp, _dp, _dp, _dp, i32, d,
                                          d, vp, vp]
     lib.fo_lod_step_richards.restype = i32
+    lib.fo_line_run_richards.argtypes = [i32, _dp, _dp, i64, i32, d, d, d, _dp, _dp, i32, d, _dp, i32, vp, i32,
+                                         i32, d, d]
+    lib.fo_line_run_richards.restype = i32
     lib.fo_caputo_derivative.argtypes = [i32, d, d, d, _dp, _dp]
     lib.fo_do_derivative.argtypes = [i32, d, i32, _dp, _dp, _dp, i32, i32, i32, _dp]
     lib.fo_do_fused_weights.argtypes = [i32, _dp, _dp, _dp, d, i32, _dp]
@@ -259,6 +262,23 @@ def lod_step_richards(dims, U, hist, n, kb, tau, Da, kkk0, sZ, sdL, dLx, dLy, kf
                              f(dLx), f(dLy), kform, ksat, E,
                              None if rpp is None else rpp.ctypes.data_as(C.c_void_p), _ptr(S))
     return S
+
+
+def line_run_richards(U0, steps, tau, alpha, Da, Z, dL, kform, ksat, E, src=None, rtype=0, gN=0.0, dLN=0.0):
+    """fo_line_run_richards: a Richards line with the history. Returns (U, hist)."""
+    lib = load()
+    U = np.array(U0, dtype=np.float64)
+    N = len(U) - 1
+    hist = np.zeros((steps, N + 1))
+    f = lambda x: np.ascontiguousarray(x, dtype=np.float64)
+    E = np.atleast_1d(f(E))
+    rows, sp = 0, None
+    if src is not None:
+        src = f(np.atleast_2d(src))
+        rows, sp = src.shape[0], src.ctypes.data_as(C.c_void_p)
+    lib.fo_line_run_richards(N, U, hist.reshape(-1), N + 1, steps, tau, alpha, Da, f(Z), f(dL), kform, ksat, E, len(E),
+                             sp, rows, rtype, gN, dLN)
+    return U, hist
 
 
 def caputo_derivative(F, tau, a, g2a):

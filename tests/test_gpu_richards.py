@@ -81,3 +81,58 @@ def test_richards_lod_split_history_vs_fp64(ctx, kform):
     errs = [relmax(x, y) for x, y in zip(out[1], out[0])]
     print(f"Richards k_form {kform}, 200 steps, split vs FP64 at 8 checkpoints: max {max(errs):.2e}")
     assert max(errs) <= 1e-7
+
+
+def _rich_line(N, steps, kform):
+    """A Richards column in the reference's units: depth 3 m in N intervals, H0 = -0.8 - Z,
+    Dirichlet H0 - Z[N] at the bottom (bottom_cond 1), the surface condition from the recorded
+    evaporation rates of the pinned 3D run, tau 900 s."""
+    import math
+    g = fgv.load(golden_path(f"fpde_richards_k{kform}"))
+    Z = np.arange(N + 1) * 3.0 / N
+    dL = np.full(N + 1, 3.0 / N)
+    u0 = -0.8 - Z
+    alpha = float(g["alpha"])
+    return dict(Z=Z, dL=dL, u0=u0, alpha=alpha, Da=1.0 / math.gamma(1.0 - alpha), tau=900.0, E=g["E"],
+                ksat=float(g["k_sat"]), kform=kform, N=N, steps=steps)
+
+
+def _gpu_line(ctx, c, precision, pieces=1):
+    import fpde_hpc_gb300 as fp
+    rich = dict(k_form=c["kform"], k_sat=c["ksat"], Z=c["Z"], dL=c["dL"], evaporation=c["E"])
+    line = fp.Line(ctx, c["N"], c["alpha"], c["tau"], c["Da"], None, None, None, c["u0"], c["steps"],
+                   right=(0, c["u0"][-1]), precision=precision, richards=rich)
+    out = []
+    for k in range(pieces):
+        line.run(c["steps"] // pieces)
+        out.append(line.state())
+    line.close()
+    return out
+
+
+@pytest.mark.parametrize("kform,N", [(1, 2000), (2, 2000), (2, 50000)])
+def test_richards_line_fp64_vs_oracle(ctx, kform, N):
+    """The line's coefficients from its state every step (k_rich_coefs) and the scan-based Thomas
+    solve (k_rich_thomas) against the oracle's sequential restatement: 1e-12, or 4x the oracle's
+    one-ulp envelope (node coordinates and steps moved by one ulp) where that is larger."""
+    import oracle
+    c = _rich_line(N, 100, kform)
+    u = _gpu_line(ctx, c, 0)[0]
+    ref, _ = oracle.line_run_richards(c["u0"], c["steps"], c["tau"], c["alpha"], c["Da"], c["Z"], c["dL"], kform,
+                                      c["ksat"], c["E"], rtype=0, gN=c["u0"][-1])
+    rng = np.random.default_rng(0)
+    pert = lambda x: x * (1 + 2.2e-16 * rng.choice([-1, 1], size=x.shape))
+    ref2, _ = oracle.line_run_richards(c["u0"], c["steps"], c["tau"], c["alpha"], c["Da"], pert(c["Z"]),
+                                       pert(c["dL"]), kform, c["ksat"], c["E"], rtype=0, gN=c["u0"][-1])
+    env, err = relmax(ref2, ref), relmax(u, ref)
+    print(f"Richards line k_form {kform} N={N}, 100 steps: GPU vs oracle {err:.2e} (one-ulp envelope {env:.2e})")
+    assert err <= max(1e-12, 4 * env)
+
+
+@pytest.mark.parametrize("kform", [1, 2])
+def test_richards_line_split_vs_fp64(ctx, kform):
+    c = _rich_line(4000, 256, kform)
+    a, b = _gpu_line(ctx, c, 0, 8), _gpu_line(ctx, c, 3, 8)
+    errs = [relmax(x, y) for x, y in zip(b, a)]
+    print(f"Richards line k_form {kform}, 256 steps, split vs FP64 at 8 checkpoints: max {max(errs):.2e}")
+    assert max(errs) <= 1e-7
