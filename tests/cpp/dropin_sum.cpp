@@ -4,8 +4,8 @@
 // step's weights kb_3_cache with precalc_kb_3 (:4069-4085) and, before the K pass of every step,
 // calls fr_ocl_call_sum (:1819-1883, from calc_step :5155-5158), whose results time_summing
 // returns (:4100-4104). This program is that caller with fr_ocl_call_sum replaced by the
-// gb300_call_sum adapter of INTEGRATION.md, line for line: a C++ host program linked against
-// libfpde_gb300.so, no Python in between.
+// gb300_call_sum adapter (fpde_history_append of each new snapshot, then fpde_l1_sum with the
+// step's kb_3_cache): a C++ host program linked against libfpde_gb300.so, no Python in between.
 //
 // Input (little-endian, written by tests/test_cpp_dropin.py from the reference's recorded column
 // run): int64 nodes, int64 steps; U0[nodes]; U[steps][nodes] (the grid after each step);
@@ -29,7 +29,7 @@ struct Column {
     int64_t nodes = 0;
     std::vector<double *> oldH;          // snapshots, oldest first (the reference's oldH)
     std::vector<double> kb_3_cache, tau; // precalc_kb_3's output for the current step
-    // gb300_call_sum state
+    // gb300_call_sum state: the library context and the device snapshot history
     fpde_ctx *gb_ctx = nullptr;
     fpde_hist *gb_hist = nullptr;
     double *Sums = nullptr;

@@ -1,8 +1,8 @@
 """C++ host programs calling the library through include/fpde_gb300.h, as the reference would.
 
 tests/cpp/dropin_sum.cpp is the reference's caller (calc_step -> fr_ocl_call_sum ->
-time_summing, fpde_hpc_1d.cpp:5155-5158, :1819-1883, :4100-4104) with the INTEGRATION.md
-adapter in place of fr_ocl_call_sum, replayed on the reference's own recorded column run
+time_summing, fpde_hpc_1d.cpp:5155-5158, :1819-1883, :4100-4104) with the
+library's gb300_call_sum adapter in place of fr_ocl_call_sum, replayed on the reference's own recorded column run
 (tests/golden/fpde_column_a2: its snapshots, kb_3_cache and tau of every step); its Sums must
 equal the reference's to 1e-12. tests/cpp/dropin_line.cpp advances a column on the device in one
 call, block by block (fpde_step_block) and step by step, each compared with the oracle.
