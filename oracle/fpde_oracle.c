@@ -682,6 +682,182 @@ int fo_line_run_richards(int N, double *U, double *hist, int64_t P, int steps, d
     return 0;
 }
 
+/* ------------------------------------------ implicit space-fractional operator (impl 2) */
+
+/* vmul_T, fpde_hpc_1d.cpp:6662-6686 (toeplitz_mult_alg 0; the C/T branch :6704-6746 is not
+ * restated). The interior rows are the reference's s->rb..s->re-1 = 1..n-1 of a line. */
+void fo_sf_matvec(int n, const double *mat, const double *mc, const double *Tm, const double *iw,
+                  const double *rs, int space_der, const double *x, double *r, double *bt)
+{
+    const double *m0 = mat, *m1 = mat + (n + 1), *m2 = mat + 2 * (n + 1);
+    const double *c0 = mc, *c1 = mc + (n + 1), *c2 = mc + 2 * (n + 1);
+    for (int i = 1; i < n; i++) r[i] = m0[i] * x[i - 1] + m1[i] * x[i] + m2[i] * x[i + 1];   /* :6662-6663 */
+    r[0] = m1[0] * x[0] + m2[0] * x[1];
+    r[n] = m0[n] * x[n - 1] + m1[n] * x[n];
+    for (int j = 1; j < n; j++) bt[j] = c0[j] * x[j - 1] + c1[j] * x[j] + c2[j] * x[j + 1];  /* :6668-6669 */
+    for (int i = 1; i < n; i++) {                                                              /* :6674-6686 */
+        double v = 0.0;
+        for (int j = 1; j < i; j++) v += bt[j] * Tm[i - j + 1];
+        if (space_der == 1)
+            for (int j = i + 1; j < n; j++) v -= bt[j] * Tm[j - i + 1];
+        if (rs) v /= rs[i];
+        r[i] += v * (iw ? iw[i] : 1.0);
+    }
+}
+
+static double sf_dot(int m, const double *a, const double *b)
+{
+    double s = 0.0;
+    for (int i = 0; i < m; i++) s += a[i] * b[i];
+    return s;
+}
+
+/* solve_mln<1>, fpde_hpc_1d.cpp:812-1157, for n = 1: rn(k) = 1 and qn(k) = k - 1 for every k, so
+ * each iteration takes the rn == 1 branch (:868-915), recomputes the residual (:943-947) and the
+ * rn == n branch (:1053-1098); q[0] is the initial residual (no random vectors for n = 1). */
+int fo_sf_solve(int n, const double *mat, const double *mc, const double *Tm, const double *iw,
+                const double *rs, int space_der, const double *B, double *x, double thr, int maxiter)
+{
+    const int m = n + 1;
+    double *q0 = (double *)malloc(sizeof(double) * (size_t)m), *r = (double *)malloc(sizeof(double) * (size_t)m);
+    double *g[2], *w[2];
+    for (int k = 0; k < 2; k++) {
+        g[k] = (double *)malloc(sizeof(double) * (size_t)m);
+        w[k] = (double *)malloc(sizeof(double) * (size_t)m);
+    }
+    double *u = (double *)malloc(sizeof(double) * (size_t)m), *Au = (double *)malloc(sizeof(double) * (size_t)m);
+    double *zw = (double *)malloc(sizeof(double) * (size_t)m), *bt = (double *)malloc(sizeof(double) * (size_t)m);
+    double c[2] = {0.0, 0.0}, al, ro1 = 0.0, beta, norm;
+    int iter = 1;
+restart:
+    fo_sf_matvec(n, mat, mc, Tm, iw, rs, space_der, x, r, bt);                 /* :841-844 */
+    for (int i = 0; i < m; i++) r[i] = B[i] - r[i];
+    memcpy(g[1], r, sizeof(double) * (size_t)m);
+    memcpy(q0, r, sizeof(double) * (size_t)m);
+    fo_sf_matvec(n, mat, mc, Tm, iw, rs, space_der, g[1], w[1], bt);            /* :851 */
+    c[1] = sf_dot(m, q0, w[1]);
+    norm = sf_dot(m, r, r);
+    if (fabs(norm / m) < thr) goto done;
+    for (;;) {
+        al = sf_dot(m, q0, r);                                                   /* :871-877 */
+        al /= c[1];
+        if (c[1] != 0.0) {
+            for (int i = 0; i < m; i++) u[i] = r[i] - al * w[1][i];
+            for (int i = 0; i < m; i++) x[i] = x[i] + al * g[1][i];
+            fo_sf_matvec(n, mat, mc, Tm, iw, rs, space_der, u, Au, bt);      /* :890 */
+            norm = sf_dot(m, Au, Au);
+            ro1 = sf_dot(m, Au, u);
+            ro1 = -ro1 / norm;
+            if (norm == 0.0) goto restart;
+            for (int i = 0; i < m; i++) x[i] = x[i] - ro1 * u[i];
+        } else {
+            goto restart;
+        }
+        fo_sf_matvec(n, mat, mc, Tm, iw, rs, space_der, x, r, bt);             /* :943-947 */
+        for (int i = 0; i < m; i++) r[i] = B[i] - r[i];
+        beta = 0.0;                                                              /* :1056-1065 */
+        for (int i = 0; i < m; i++) beta -= q0[i] * r[i];
+        beta /= c[1];
+        if (c[1] == 0.0) beta = 0.0;
+        for (int i = 0; i < m; i++) zw[i] = r[i] + beta * w[1][i];
+        for (int i = 0; i < m; i++) g[0][i] = zw[i] + (beta / ro1) * g[1][i];
+        fo_sf_matvec(n, mat, mc, Tm, iw, rs, space_der, g[0], w[0], bt);       /* :1094 */
+        c[0] = sf_dot(m, q0, w[0]);
+        {                                                                        /* :1104-1121 */
+            double *t = g[1]; g[1] = g[0]; g[0] = t;
+            t = w[1]; w[1] = w[0]; w[0] = t;
+            double tc = c[1]; c[1] = c[0]; c[0] = tc;
+        }
+        norm = sf_dot(m, r, r);
+        if (fabs(norm / m) < thr) break;
+        iter++;
+        if (iter == maxiter) break;
+    }
+done:
+    free(q0); free(r); free(u); free(Au); free(zw); free(bt);
+    for (int k = 0; k < 2; k++) { free(g[k]); free(w[k]); }
+    return iter;
+}
+
+int fo_lod_step_sf(int sN, int M, int K, double *U, double *hist, int n, const double *kb, const double *tau,
+                   double Da, double kkk0, const double *coefA, const double *coefB, const double *coefRlap,
+                   const double *mc, const double *iw, const double *Tm, int ldt, int space_der, double thr,
+                   int maxiter, const double *rp, const double *bc, double *S_out, int64_t *iters)
+{
+    const double lam = Da * (kkk0 / tau[n]);      /* Om1_impl :4441 */
+    const double lamR = Da * kkk0 / tau[n];       /* R :3120 */
+    const int64_t sx = 1, sy = sN + 2, sz = (int64_t)(sN + 2) * (M + 2);
+    const int64_t G = sz * (K + 2);
+    int L = sN; if (M > L) L = M; if (K > L) L = K;
+    double *Uold = (double *)malloc(sizeof(double) * (size_t)G);
+    double *S = (double *)calloc((size_t)G, sizeof(double));
+    int64_t it_total = 0;
+    memcpy(Uold, U, sizeof(double) * (size_t)G);
+    if (n > 0) {                                  /* time_summing on the K-pass nodes, as fo_lod_step */
+#pragma omp parallel for schedule(static)
+        for (int k = 1; k <= K; k++)
+            for (int t = n - 1; t >= 0; t--) {
+                const double *h = hist + (int64_t)t * G;
+                const double c = kb[t], tt = tau[t];
+                for (int j = 1; j < M; j++)
+                    for (int i = 1; i < sN; i++) {
+                        const int64_t id = i * sx + j * sy + k * sz;
+                        S[id] += c * h[id] / tt;
+                    }
+            }
+    }
+    for (int pass = 2; pass >= 0; pass--) {       /* K, _M, sN as calc_step */
+        int Nl = pass == 2 ? K : (pass == 1 ? M : sN);
+        int64_t st = pass == 2 ? sz : (pass == 1 ? sy : sx);
+        const double *cA = coefA + (int64_t)pass * G, *cB = coefB + (int64_t)pass * G;
+        const double *cR = coefRlap + (int64_t)pass * G;
+        const double *pm = mc + (int64_t)pass * 3 * G, *piw = iw + (int64_t)pass * G;
+        const double *pT = Tm + (int64_t)pass * ldt;
+        int na = pass == 2 ? sN : (pass == 1 ? sN : M);
+        int nb = pass == 2 ? M : K;
+#pragma omp parallel reduction(+ : it_total)
+        {
+        double *mat = (double *)malloc(sizeof(double) * (size_t)3 * (L + 2));
+        double *lmc = (double *)calloc((size_t)3 * (L + 2), sizeof(double));
+        double *liw = (double *)calloc((size_t)(L + 2), sizeof(double));
+        double *om = (double *)malloc(sizeof(double) * (size_t)(L + 2));
+        double *lu = (double *)malloc(sizeof(double) * (size_t)(L + 2));
+#pragma omp for schedule(static) collapse(2)
+        for (int a = 1; a < na; a++)
+            for (int b = 1; b < nb; b++) {
+                int64_t base;
+                if (pass == 2) base = a * sx + b * sy;
+                else if (pass == 1) base = a * sx + b * sz;
+                else base = a * sy + b * sz;
+                const int m = Nl + 1;
+                double *m0 = mat, *m1 = mat + m, *m2 = mat + 2 * m;
+                for (int p = 0; p <= Nl + 1; p++) lu[p] = U[base + p * st];
+                for (int p = 1; p < Nl; p++) {                                 /* implicit2_gen :4633-4638 */
+                    int64_t id = base + p * st;
+                    m0[p] = cA[id]; m1[p] = -(cR[id] + lamR); m2[p] = cB[id];
+                    lmc[p] = pm[id]; lmc[m + p] = pm[G + id]; lmc[2 * m + p] = pm[2 * G + id];
+                    liw[p] = piw[id];
+                    om[p] = -(lam * lu[p]) + ((pass == 2 && rp) ? rp[id] : 0.0);   /* Om1_impl :4441 */
+                    if (pass == 2) om[p] += Da * S[id];                             /* :4507-4510 */
+                }
+                m0[0] = 0.0; m1[0] = 1.0; m2[0] = 0.0;                             /* :4643-4648 */
+                m0[Nl] = 0.0; m1[Nl] = 1.0; m2[Nl] = 0.0;
+                om[0] = bc[base]; om[Nl] = bc[base + Nl * st];                     /* :4650-4651 */
+                it_total += fo_sf_solve(Nl, mat, lmc, pT, liw, NULL, space_der, om, lu, thr, maxiter);
+                lu[Nl + 1] = lu[Nl];                                               /* U1 :4792 */
+                for (int p = 0; p <= Nl + 1; p++) U[base + p * st] = lu[p];
+            }
+        free(mat); free(lmc); free(liw); free(om); free(lu);
+        }
+    }
+    double *row = hist + (int64_t)n * G;
+    for (int64_t q = 0; q < G; q++) row[q] = U[q] - Uold[q];
+    if (S_out) memcpy(S_out, S, sizeof(double) * (size_t)G);
+    if (iters) *iters = it_total;
+    free(Uold); free(S);
+    return 0;
+}
+
 /* ------------------------------------------------------ distributed order */
 
 static double bk_pow(double d1, double d2, double beta)   /* fr_do.cpp:129-134 */

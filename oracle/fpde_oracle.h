@@ -161,6 +161,33 @@ int fo_line_run_richards(int N, double *U, double *hist, int64_t P, int steps, d
                          const double *Z, const double *dL, int kform, double ksat, const double *E, int erows,
                          const double *src, int src_rows, int rtype, double gN, double dLN);
 
+/* ---- implicit space-fractional operator (impl 2, TMA 0) ---- */
+
+/* vmul_T (fpde_hpc_1d.cpp:6618-6747, toeplitz_mult_alg 0, equation 0) on one line of n
+ * intervals (n+1 unknowns): r = tridiag(mat) x + iw * (T * (tridiag(mc) x)) with the Toeplitz sum
+ * over interior rows i = 1..n-1: sum_{j=1}^{i-1} bt[j] Tm[i-j+1], minus (space_der 1)
+ * sum_{j=i+1}^{n-1} bt[j] Tm[j-i+1]; divided by rs[i] when rs is given (implicit_row_scaling).
+ * mat and mc are 3 x (n+1) (rows 0 = lower, 1 = diagonal, 2 = upper); mc is read at rows 1..n-1,
+ * iw at 1..n-1 (NULL: 1.0, the C/T equations), Tm at 2..n. bt is scratch of n+1 values. */
+void fo_sf_matvec(int n, const double *mat, const double *mc, const double *Tm, const double *iw,
+                  const double *rs, int space_der, const double *x, double *r, double *bt);
+
+/* solve_mln<1> (:812-1157) with vmul_T on the same operands over the whole line (rb = 0,
+ * re = n+1): x holds the initial guess and receives the solution; stops when
+ * |r.r / (n+1)| < thr or after maxiter - 1 iterations. Returns the iteration count. */
+int fo_sf_solve(int n, const double *mat, const double *mc, const double *Tm, const double *iw,
+                const double *rs, int space_der, const double *B, double *x, double thr, int maxiter);
+
+/* One LOD step (mode 3, implicit3d 0) with impl 2: as fo_lod_step with Dirichlet line ends, but
+ * every line is solved with fo_sf_solve on the system implicit2_gen forms (:4630-4663): interior
+ * rows (A_, -(Rlap + Da kkk0/tau), B), identity rows at both ends with the right-hand side
+ * bc0 / bcN, the operand grids mc (3 passes x 3 x G), iw (3 x G) and the Toeplitz rows Tm
+ * (3 x ldt, pass p's row at p*ldt). *iters (may be NULL) receives the total iteration count. */
+int fo_lod_step_sf(int sN, int M, int K, double *U, double *hist, int n, const double *kb, const double *tau,
+                   double Da, double kkk0, const double *coefA, const double *coefB, const double *coefRlap,
+                   const double *mc, const double *iw, const double *Tm, int ldt, int space_der, double thr,
+                   int maxiter, const double *rp, const double *bc, double *S_out, int64_t *iters);
+
 /* ---- distributed order (fr_do.cpp) ---- */
 
 /* Caputo derivative of sampled F (Cder :74-86 with an F array): DF[t] for t = 1..ntau-1,

@@ -61,6 +61,12 @@ def load():
     lib.fo_line_run_richards.argtypes = [i32, _dp, _dp, i64, i32, d, d, d, _dp, _dp, i32, d, _dp, i32, vp, i32,
                                          i32, d, d]
     lib.fo_line_run_richards.restype = i32
+    lib.fo_sf_matvec.argtypes = [i32, _dp, _dp, _dp, vp, vp, i32, _dp, _dp, _dp]
+    lib.fo_sf_solve.argtypes = [i32, _dp, _dp, _dp, vp, vp, i32, _dp, _dp, d, i32]
+    lib.fo_sf_solve.restype = i32
+    lib.fo_lod_step_sf.argtypes = [i32, i32, i32, _dp, _dp, i32, _dp, _dp, d, d, _dp, _dp, _dp, _dp, _dp, _dp, i32,
+                                   i32, d, i32, vp, _dp, vp, C.POINTER(i64)]
+    lib.fo_lod_step_sf.restype = i32
     lib.fo_caputo_derivative.argtypes = [i32, d, d, d, _dp, _dp]
     lib.fo_do_derivative.argtypes = [i32, d, i32, _dp, _dp, _dp, i32, i32, i32, _dp]
     lib.fo_do_fused_weights.argtypes = [i32, _dp, _dp, _dp, d, i32, _dp]
@@ -279,6 +285,51 @@ def line_run_richards(U0, steps, tau, alpha, Da, Z, dL, kform, ksat, E, src=None
     lib.fo_line_run_richards(N, U, hist.reshape(-1), N + 1, steps, tau, alpha, Da, f(Z), f(dL), kform, ksat, E, len(E),
                              sp, rows, rtype, gN, dLN)
     return U, hist
+
+
+def _f64(a):
+    return None if a is None else np.ascontiguousarray(a, dtype=np.float64)
+
+
+def sf_matvec(mat, mc, Tm, x, iw=None, rs=None, space_der=0):
+    """fo_sf_matvec (vmul_T, toeplitz_mult_alg 0) on one line: mat, mc are 3 x (n+1)."""
+    lib = load()
+    x = _f64(x)
+    n = x.size - 1
+    r = np.zeros(n + 1)
+    bt = np.zeros(n + 1)
+    iw, rs = _f64(iw), _f64(rs)
+    lib.fo_sf_matvec(n, _f64(mat).reshape(-1), _f64(mc).reshape(-1), _f64(Tm), _ptr(iw), _ptr(rs), space_der, x,
+                     r, bt)
+    return r
+
+
+def sf_solve(mat, mc, Tm, B, x0, thr, maxiter, iw=None, rs=None, space_der=0):
+    """fo_sf_solve (solve_mln<1> with vmul_T): returns (solution, iterations)."""
+    lib = load()
+    x = _f64(x0).copy()
+    n = x.size - 1
+    iw, rs = _f64(iw), _f64(rs)
+    it = lib.fo_sf_solve(n, _f64(mat).reshape(-1), _f64(mc).reshape(-1), _f64(Tm), _ptr(iw), _ptr(rs), space_der,
+                         _f64(B), x, thr, maxiter)
+    return x, it
+
+
+def lod_step_sf(dims, U, hist, n, kb, tau, Da, kkk0, coefA, coefB, coefRlap, mc, iw, Tm, space_der, thr, maxiter,
+                rp, bc, want_S=False):
+    """fo_lod_step_sf: one LOD step with the implicit space-fractional line solves.
+    mc: (3 passes, 3, G), iw: (3, G), Tm: (3, ldt). Returns (S or None, iterations)."""
+    lib = load()
+    sN, M, K = dims
+    S = np.zeros_like(U) if want_S else None
+    Tm = _f64(Tm)
+    it = C.c_int64()
+    rpp = None if rp is None else _f64(rp).reshape(-1)
+    lib.fo_lod_step_sf(sN, M, K, U.reshape(-1), hist.reshape(-1), n, _f64(kb), _f64(tau), Da, kkk0,
+                       _f64(coefA).reshape(-1), _f64(coefB).reshape(-1), _f64(coefRlap).reshape(-1),
+                       _f64(mc).reshape(-1), _f64(iw).reshape(-1), Tm.reshape(-1), Tm.shape[1], space_der, thr,
+                       maxiter, _ptr(rpp), _f64(bc).reshape(-1), _ptr(S), C.byref(it))
+    return S, it.value
 
 
 def caputo_derivative(F, tau, a, g2a):

@@ -322,6 +322,114 @@ static void run_richards(const char *path, int kform, int rpform, int bs, int nb
     printf("wrote %s (Richards k_form %d, %d steps, grid %dx%dx%d)\n", path, kform, steps, sN, _M, K);
 }
 
+/* The implicit space-fractional LOD (impl 2, TMA 0: implicit2_gen :4630-4663 builds each line's
+ * tridiagonal Mat and right-hand side, U1 :4769-4791 solves tridiag(Mat) + iw * T * tridiag(Mcoefs)
+ * with solve_mln<1> :812-1157 and the product vmul_T :6618-6747), analytic problem 2, Dirichlet
+ * line ends (bottom_cond 1). Recorded once: per pass the coefficient grids A_/B/R (Da = 0 as in
+ * record_coefs), the Mcoefs diagonals of Om1T :4362-4376 and inv_dw_dh at every line node, and
+ * the Toeplitz row Tm[pass][1..] (:3670-3694). Per step: the grid, the history sum, Rp and the line
+ * ends. After the run, for the first line of each pass: one product vmul_T(x) of a fixed x and one
+ * solve_mln<1> of the line's own system from its state, with their operands. */
+static void run_spacefrac(const char *path, int sd, double gam, double alpha, int bs, int nb, int mb, int kb,
+                          double tau, int steps, double ieps, int initer)
+{
+    set_dims(bs, nb, mb, kb);
+    varT = 0; varZ = 0; varXY = 0;
+    implicit = 2; implicit3d = 0; rp_split_3d = 0; sum_alg = 0;
+    toeplitz_mult_alg = 0; space_der = sd; implicit_row_scaling = 0;
+    impl_err = ieps; impl_niter = initer;
+    global_eps = 1e-15; global_eps2 = 1e-15;
+    FILE *lg = fopen("/dev/null", "w");
+    H_solver *s = new H_solver(2, 1, 5, 0, 1, alpha, gam, 0, 0, 0, 3, lg, 2);
+    size_t G = (size_t)(sN + 2) * (_M + 2) * (K + 2);
+    FgvWriter w(path);
+    w.scalar("sN", sN); w.scalar("M", _M); w.scalar("K", K);
+    w.scalar("alpha", alpha); w.scalar("gamma", gam); w.scalar("Da", s->Da); w.scalar("Dg", s->Dg);
+    w.scalar("space_der", sd); w.scalar("impl_err", ieps); w.scalar("impl_niter", initer);
+    std::vector<uint64_t> gdims = {(uint64_t)(K + 2), (uint64_t)(_M + 2), (uint64_t)(sN + 2)};
+    w.put("U0", gdims, s->b_U);
+    std::vector<double> kb_all, kb_off, kkk0, tauv, S_all, U_all, rp, bc;
+    for (int n = 0; n < steps; n++) {
+        s->calc_step(tau);
+        kb_off.push_back((double)kb_all.size());
+        kb_all.insert(kb_all.end(), s->kb_3_cache.begin(), s->kb_3_cache.end());
+        kkk0.push_back(s->kkk0);
+        tauv.push_back(s->tau[s->tstep]);
+        if (n == 0) record_coefs(s, w);
+        S_all.insert(S_all.end(), s->b_Utimesum, s->b_Utimesum + G);
+        U_all.insert(U_all.end(), s->b_U, s->b_U + G);
+        record_step_inputs(s, rp, bc);
+    }
+    kb_off.push_back((double)kb_all.size());
+    uint64_t ns = steps;
+    w.put("tau", tauv); w.put("kkk0", kkk0);
+    w.put("kb_flat", kb_all); w.put("kb_off", kb_off);
+    w.put("S", {ns, (uint64_t)(K + 2), (uint64_t)(_M + 2), (uint64_t)(sN + 2)}, S_all.data());
+    w.put("U", {ns, (uint64_t)(K + 2), (uint64_t)(_M + 2), (uint64_t)(sN + 2)}, U_all.data());
+    w.put("Rp", {ns, (uint64_t)(K + 2), (uint64_t)(_M + 2), (uint64_t)(sN + 2)}, rp.data());
+    w.put("BC", {ns, (uint64_t)(K + 2), (uint64_t)(_M + 2), (uint64_t)(sN + 2)}, bc.data());
+
+    /* per pass: Mcoefs and inv_dw_dh at every interior line node, and the Toeplitz row */
+    PassState st = save_state(s);
+    for (int pass = 0; pass < 3; pass++) {
+        std::vector<double> m0(G, 0.0), m1(G, 0.0), m2(G, 0.0), iw(G, 0.0);
+        int na = pass == 2 ? sN : (pass == 1 ? sN : _M), nbl = pass == 2 ? _M : K;
+        int Nl = pass == 2 ? K : (pass == 1 ? _M : sN);
+        for (int a = 1; a < na; a++) for (int b = 1; b < nbl; b++) {
+            enter_line(s, pass, a, b);
+            s->rb = 1; s->re = N;
+            s->Om1T();
+            for (int q = 1; q < Nl; q++) {
+                size_t id = pass == 2 ? gidx(a, b, q) : (pass == 1 ? gidx(a, q, b) : gidx(q, a, b));
+                m0[id] = s->Mcoefs[0][q]; m1[id] = s->Mcoefs[1][q]; m2[id] = s->Mcoefs[2][q];
+                iw[id] = s->inv_dw_dh(q);
+            }
+        }
+        char nm[32];
+        snprintf(nm, sizeof nm, "mc0_pass%d", pass); w.put(nm, gdims, m0.data());
+        snprintf(nm, sizeof nm, "mc1_pass%d", pass); w.put(nm, gdims, m1.data());
+        snprintf(nm, sizeof nm, "mc2_pass%d", pass); w.put(nm, gdims, m2.data());
+        snprintf(nm, sizeof nm, "iw_pass%d", pass); w.put(nm, gdims, iw.data());
+        snprintf(nm, sizeof nm, "Tm_pass%d", pass);
+        w.put(nm, std::vector<double>(s->Tm[pass], s->Tm[pass] + Nl + 1));
+    }
+    /* one product and one solve on the first line of each pass, with the system implicit2_gen
+     * forms for it now (after the last step) */
+    for (int pass = 0; pass < 3; pass++) {
+        enter_line(s, pass, 1, 1);
+        s->rb = 1; s->re = N;
+        const int Ns = N + 1;
+        s->implicit2_gen(s->Mat, s->Om);
+        std::vector<double> x(Ns), r(Ns, 0.0), mat((size_t)3 * Ns), x0(Ns), xs(Ns);
+        for (int q = 0; q < Ns; q++) x[q] = std::sin(1.0 + 0.37 * q) + 0.25 * std::cos(3.1 * q * q);
+        vmul_T((double **)s, x.data(), r.data(), Ns);
+        for (int d = 0; d < 3; d++) for (int q = 0; q < Ns; q++) mat[(size_t)d * Ns + q] = s->Mat[d][q];
+        std::vector<double> mc((size_t)3 * Ns, 0.0), iwl(Ns, 0.0);
+        for (int d = 0; d < 3; d++) for (int q = 1; q < N; q++) mc[(size_t)d * Ns + q] = s->Mcoefs[d][q];
+        for (int q = 1; q < N; q++) iwl[q] = s->inv_dw_dh(q);
+        std::vector<double> om(s->Om, s->Om + Ns);
+        for (int q = 0; q < Ns; q++) x0[q] = xs[q] = s->U[q];
+        solve_mln<1>((double **)s, s->Om, xs.data(), Ns, impl_err, impl_niter, vmul_T, 0, Ns);
+        char nm[32];
+        snprintf(nm, sizeof nm, "mv%d_x", pass); w.put(nm, x);
+        snprintf(nm, sizeof nm, "mv%d_r", pass); w.put(nm, r);
+        snprintf(nm, sizeof nm, "mv%d_mat", pass); w.put(nm, {3, (uint64_t)Ns}, mat.data());
+        snprintf(nm, sizeof nm, "mv%d_mc", pass); w.put(nm, {3, (uint64_t)Ns}, mc.data());
+        snprintf(nm, sizeof nm, "mv%d_iw", pass); w.put(nm, iwl);
+        snprintf(nm, sizeof nm, "mv%d_Tm", pass);
+        w.put(nm, std::vector<double>(s->Tm[pass], s->Tm[pass] + Ns));
+        snprintf(nm, sizeof nm, "mv%d_B", pass); w.put(nm, om);
+        snprintf(nm, sizeof nm, "mv%d_x0", pass); w.put(nm, x0);
+        snprintf(nm, sizeof nm, "mv%d_sol", pass); w.put(nm, xs);
+    }
+    restore_state(s, st);
+    delete s;
+    fclose(lg);
+    implicit = 0; toeplitz_mult_alg = 0; space_der = 0;
+    printf("wrote %s (space-fractional LOD, SD %d, gamma %g, %d steps, grid %dx%dx%d)\n", path, sd, gam, steps, sN,
+           _M, K);
+}
+
 /* The reference's Gamma (fpde_hpc_1d.cpp:70-252: exp(LogGamma), its own series and
  * asymptotic forms, memoised) at the orders the benchmark configurations use: 1 - alpha for
  * Da = 1/Gamma(1 - alpha) (:3598-3605) and 2 - a for the distributed-order normalisers, plus a
@@ -350,6 +458,18 @@ int main(int argc, char **argv)
         run_richards(q, 1, 1, 2, 3, 3, 3, 0.8, 900.0, 40);
         snprintf(q, sizeof q, "%s/fpde_richards_k2.fgv", argv[2]);
         run_richards(q, 2, 2, 2, 3, 3, 3, 0.6, 900.0, 40);
+        return 0;
+    }
+    if (argc >= 3 && strcmp(argv[1], "spacefrac") == 0) {
+        char q[4096];
+        /* 6 x 4 x 8 cells, one- and two-sided, the reference's default tolerance */
+        snprintf(q, sizeof q, "%s/fpde_sf_sd0.fgv", argv[2]);
+        run_spacefrac(q, 0, 0.8, 0.8, 2, 3, 2, 4, 0.0025, 12, 1e-9, 5000);
+        snprintf(q, sizeof q, "%s/fpde_sf_sd1.fgv", argv[2]);
+        run_spacefrac(q, 1, 0.7, 0.85, 2, 3, 2, 4, 0.0025, 12, 1e-9, 5000);
+        /* a column of 40 nodes, two-sided, solved to a tight tolerance */
+        snprintf(q, sizeof q, "%s/fpde_sf_col.fgv", argv[2]);
+        run_spacefrac(q, 1, 0.75, 0.8, 1, 3, 3, 40, 0.002, 10, 1e-26, 400);
         return 0;
     }
     if (argc >= 3 && strcmp(argv[1], "gamma") == 0) {
