@@ -37,12 +37,17 @@ class LineDesc(C.Structure):
                 ("richards", C.POINTER(Richards))]
 
 
+class SpaceFrac(C.Structure):
+    _fields_ = [("space_der", c_int), ("tol", c_dbl), ("max_iter", c_int), ("Tm", c_vp * 3), ("mc", c_vp * 3),
+                ("iw", c_vp * 3)]
+
+
 class Lod3dDesc(C.Structure):
     _fields_ = [("sN", c_int), ("M", c_int), ("K", c_int), ("alpha", c_dbl), ("tau", c_dbl), ("Da", c_dbl),
                 ("left_kind", c_int * 3), ("right_kind", c_int * 3), ("dLN", c_dbl * 3), ("precision", c_int),
                 ("max_steps", c_int), ("lag_weights", c_vp), ("source", c_vp), ("source_rows", c_int),
                 ("bc", c_vp), ("bc_rows", c_int), ("restrict_eps", c_dbl), ("series_terms", c_int),
-                ("richards", C.POINTER(Richards))]
+                ("richards", C.POINTER(Richards)), ("space_frac", C.POINTER(SpaceFrac))]
 
 
 class ColumnDesc(C.Structure):
@@ -79,6 +84,11 @@ _SIGS = {
     "fpde_lod3d_reset": (c_int, [c_vp, c_vp, c_int]),
     "fpde_lod3d_solve_host": (c_int, [c_vp, c_vp, c_int, c_vp]),
     "fpde_lod3d_steps_done": (c_int, [c_vp, C.POINTER(c_i64)]),
+    "fpde_lod3d_sf_iterations": (c_int, [c_vp, C.POINTER(c_i64)]),
+    "fpde_sf_matvec": (c_int, [c_vp, c_int, c_int, c_vp, c_vp, c_vp, c_vp, c_vp, c_int, c_vp, c_vp, c_int]),
+    "fpde_sf_solve": (c_int, [c_vp, c_int, c_int, c_vp, c_vp, c_vp, c_vp, c_vp, c_int, c_vp, c_vp, c_dbl, c_int,
+                              c_vp, c_int]),
+    "fpde_sf_toeplitz_row": (c_int, [c_dbl, c_vp, c_int, c_vp]),
     "fpde_do_derivative": (c_int, [c_vp, c_vp, c_i64, c_i64, c_int, c_dbl, c_vp, c_int, c_int, c_int, c_vp, c_i64,
                                    c_int]),
     "fpde_history_create": (c_int, [c_vp, c_i64, c_i64, c_int, C.POINTER(c_vp)]),

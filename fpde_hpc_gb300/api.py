@@ -3,7 +3,7 @@ import ctypes as C
 
 import numpy as np
 
-from ._lib import ColumnDesc, LineDesc, LineTuning, Lod3dDesc, Richards, check, load
+from ._lib import ColumnDesc, LineDesc, LineTuning, Lod3dDesc, Richards, SpaceFrac, check, load
 
 FP64, SPLIT_BF16, SPLIT_F16 = 0, 1, 2
 
@@ -88,6 +88,17 @@ def autotune_line(ctx, N, alpha, tau, Da, A, B, Rlap, u0, max_steps, left=(0, 0.
     check(ctx.lib.fpde_line_autotune(ctx.h, C.byref(d), *(_ptr(x) for x in arrs), C.byref(out)),
           "fpde_line_autotune")
     return out
+
+
+def sf_toeplitz_row(gamma_, Z, n):
+    """The Toeplitz row Tm[0..n] of a uniform axis with n+2 coordinates Z (fpde_sf_toeplitz_row)."""
+    Z = np.ascontiguousarray(Z, dtype=np.float64)
+    if Z.size < n + 2:
+        raise ValueError("Z needs n+2 coordinates")
+    Tm = np.zeros(n + 1)
+    check(load().fpde_sf_toeplitz_row(float(gamma_), Z.ctypes.data_as(C.c_void_p), int(n),
+                                      Tm.ctypes.data_as(C.c_void_p)), "fpde_sf_toeplitz_row")
+    return Tm
 
 
 def line_coefs(k, dL, iw=None):
@@ -195,6 +206,47 @@ class Context:
         check(self.lib.fpde_weights_g(self.h, float(p), float(alpha), _ptr(time), int(n0), int(n1), _ptr(out),
                                       ld, (1 if sync else 2) if dev else 0), "fpde_weights_g")
         return out
+
+    def _sf_args(self, mat, mc, Tm, x, iw, rs):
+        dev = _is_dev(x)
+        x = _f64(x)
+        lines, m = (1, x.shape[0]) if x.ndim == 1 else x.shape
+        mat, mc, Tm = _f64(mat), _f64(mc), _f64(Tm)
+        if tuple(mat.shape[-1:]) != (m,) or mat.shape[0] != 3 or tuple(mc.shape) != tuple(mat.shape):
+            raise ValueError("mat and mc need shape (3, lines, n+1) (or (3, n+1) for one line)")
+        iw = None if iw is None else _f64(iw)
+        rs = None if rs is None else _f64(rs)
+        return dev, x, lines, m - 1, mat, mc, Tm, iw, rs
+
+    def sf_matvec(self, mat, mc, Tm, x, iw=None, rs=None, space_der=0):
+        """The reference's vmul_T (impl 2, toeplitz_mult_alg 0) on one line (x: n+1 values) or a
+        batch (x: lines x (n+1)); mat, mc: (3, [lines,] n+1); bitwise the reference's product."""
+        dev, x, lines, n, mat, mc, Tm, iw, rs = self._sf_args(mat, mc, Tm, x, iw, rs)
+        if dev:
+            import torch
+            r = torch.empty_like(x)
+        else:
+            r = np.zeros_like(x)
+        check(self.lib.fpde_sf_matvec(self.h, lines, n, _ptr(mat), _ptr(mc), _ptr(Tm), _ptr(iw), _ptr(rs),
+                                      int(space_der), _ptr(x), _ptr(r), 1 if dev else 0), "fpde_sf_matvec")
+        return r
+
+    def sf_solve(self, mat, mc, Tm, B, x0, thr, maxiter, iw=None, rs=None, space_der=0):
+        """solve_mln<1> with vmul_T on every line from the guesses x0: returns (x, iterations)."""
+        dev, x, lines, n, mat, mc, Tm, iw, rs = self._sf_args(mat, mc, Tm, x0, iw, rs)
+        x = x.clone() if dev else x.copy()
+        B = _f64(B)
+        if dev:
+            import torch
+            it = torch.zeros(lines, dtype=torch.int32, device=x.device)
+            itp = C.c_void_p(it.data_ptr())
+        else:
+            it = np.zeros(lines, dtype=np.int32)
+            itp = it.ctypes.data_as(C.c_void_p)
+        check(self.lib.fpde_sf_solve(self.h, lines, n, _ptr(mat), _ptr(mc), _ptr(Tm), _ptr(iw), _ptr(rs),
+                                     int(space_der), _ptr(B), _ptr(x), float(thr), int(maxiter), itp,
+                                     1 if dev else 0), "fpde_sf_solve")
+        return x, it
 
     def tridiag_solve(self, a, b, r, om, u, n_lines, N, stride_elem, stride_line, left_kind=0,
                       left_val=None, right_kind=0, right_val=None, dLN=0.0):
@@ -352,10 +404,12 @@ class Lod3D:
 
     def __init__(self, ctx, dims, alpha, tau, Da, coefA, coefB, coefRlap, u0, max_steps, left_kind=(0, 0, 0),
                  right_kind=(0, 0, 0), dLN=(0.0, 0.0, 0.0), source=None, bc=None, lag_weights=None,
-                 precision=FP64, restrict_eps=0.0, series_terms=0, richards=None):
+                 precision=FP64, restrict_eps=0.0, series_terms=0, richards=None, space_frac=None):
         """richards: optional dict(k_form, k_sat, sZ, dL=(sdL, dLx, dLy), evaporation) - the
         reference's Richards problem, coefficients formed from the grid every step (coefA/B/Rlap
-        may then be None)."""
+        may then be None).
+        space_frac: optional dict(space_der, tol, max_iter, Tm=(3 rows), mc=(3 passes x 3 grids),
+        iw=(3 grids)) - the reference's implicit space-fractional line solves (impl 2)."""
         sN, M, K = dims
         self.ctx, self.dims = ctx, dims
         self.shape = (K + 2, M + 2, sN + 2)
@@ -396,6 +450,19 @@ class Lod3D:
                 r.dL[q] = dls[q].ctypes.data
             keep.append(r)
             d.richards = C.pointer(r)
+        if space_frac is not None:
+            f = SpaceFrac(space_der=int(space_frac.get("space_der", 0)), tol=float(space_frac.get("tol", 1e-9)),
+                          max_iter=int(space_frac.get("max_iter", 5000)))
+            for q, nl in enumerate((sN, M, K)):
+                tm = np.ascontiguousarray(space_frac["Tm"][q], dtype=np.float64)
+                mc = np.ascontiguousarray(space_frac["mc"][q], dtype=np.float64)
+                iw = np.ascontiguousarray(space_frac["iw"][q], dtype=np.float64)
+                if tm.size < nl + 1 or mc.shape != (3,) + self.shape or iw.shape != self.shape:
+                    raise ValueError("space_frac: Tm[p] needs Nl+1 values, mc[p] (3,)+grid, iw[p] one grid")
+                keep.extend([tm, mc, iw])
+                f.Tm[q], f.mc[q], f.iw[q] = tm.ctypes.data, mc.ctypes.data, iw.ctypes.data
+            keep.append(f)
+            d.space_frac = C.pointer(f)
         if coefA is None and richards is not None:
             cs = [None, None, None]
         else:
@@ -431,6 +498,12 @@ class Lod3D:
     def solve_host(self, u0, steps, out):
         check(self.ctx.lib.fpde_lod3d_solve_host(self.h, _ptr(u0), steps, _ptr(out)), "fpde_lod3d_solve_host")
         return out
+
+    def sf_iterations(self):
+        """Solver iterations of every space-fractional line solve so far."""
+        v = C.c_int64()
+        check(self.ctx.lib.fpde_lod3d_sf_iterations(self.h, C.byref(v)), "fpde_lod3d_sf_iterations")
+        return v.value
 
 
 class Batch:

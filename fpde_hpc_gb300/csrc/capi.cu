@@ -69,6 +69,9 @@ int ctx_check_flags(fpde_ctx *ctx, const char *where)
         FPDE_CUDA(cudaStreamSynchronize(ctx->stream));
         if (flags & (DEVERR_BARRIER_TIMEOUT | DEVERR_MBAR_TIMEOUT))
             return set_error(FPDE_ERR_TIMEOUT, "%s: device wait timed out (flags 0x%x)", where, flags);
+        if (flags & DEVERR_SOLVER)
+            return set_error(FPDE_ERR_NUMERIC, "%s: iterative solve broke down or ran past its time limit (flags 0x%x)",
+                             where, flags);
         return set_error(FPDE_ERR_ARG, "%s: device reported a bad shape (flags 0x%x)", where, flags);
     }
     return FPDE_OK;

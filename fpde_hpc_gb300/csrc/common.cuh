@@ -49,6 +49,7 @@ enum : unsigned {
     DEVERR_BARRIER_TIMEOUT = 1u,
     DEVERR_MBAR_TIMEOUT = 2u,
     DEVERR_BAD_SHAPE = 4u,
+    DEVERR_SOLVER = 8u,           // an iterative solve broke down repeatedly or ran past its time limit
 };
 
 }  // namespace fpde

@@ -91,3 +91,26 @@ struct RichLineArgs {
 int launch_rich_line_step(cudaStream_t st, const RichLineArgs &a);
 
 }  // namespace fpde
+
+namespace fpde {
+
+// One pass of the 3D LOD with the implicit space-fractional line solves (impl 2, spacefrac.cu):
+// one CTA per line; coef holds per line 7 rows of Nl+1 values (A, B, Rlap, mc0, mc1, mc2, iw).
+struct LodSfArgs {
+    double *U;
+    const double *coef, *Tm;             // Tm: Nl+1 values, entries 2..Nl-1 read
+    const double *part = nullptr;        // history partials of the K pass, or KS = 0
+    int KS = 0;
+    int64_t pstride = 0;
+    const double *rp = nullptr, *bc = nullptr;
+    double lam = 0, lamR = 0, thr = 0, dLN = 0;
+    int Nl = 0, lines = 0, n1 = 0, sd = 0, maxiter = 1, rkind = 0;
+    int64_t s1 = 0, s2 = 0, st = 0;
+    unsigned long long *iters = nullptr; // total iterations (may be null)
+    unsigned *flags = nullptr;
+};
+int launch_lod_pass_sf(cudaStream_t st, const LodSfArgs &a);
+size_t sf_smem_bytes(int n);
+int sf_prepare();
+
+}  // namespace fpde

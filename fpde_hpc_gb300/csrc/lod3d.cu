@@ -436,6 +436,13 @@ struct fpde_lod3d {
     double rksat = 0.0;
     double *rsZ = nullptr, *rdL[3] = {nullptr, nullptr, nullptr}, *ral = nullptr;
     std::vector<double> rE;                   // evaporation rate per step
+    // implicit space-fractional line solves (desc.space_frac): per pass the line-major operands
+    // (per line A, B, Rlap, mc0, mc1, mc2, iw, Nl+1 values each) and the Toeplitz row
+    bool sf = false;
+    int sf_sd = 0, sf_maxit = 1;
+    double sf_thr = 0.0;
+    double *sfc[3] = {nullptr, nullptr, nullptr}, *sfT[3] = {nullptr, nullptr, nullptr};
+    unsigned long long *sf_iters = nullptr;   // iterations of every line solve since creation
     int64_t n_done = 0;
     GraphCache<int> graphs;                        // captured runs (at least GRAPH_MIN_STEPS steps)
 };
@@ -472,6 +479,22 @@ static int lod_launch_pass(fpde_lod3d *L, cudaStream_t st, int pass, int64_t n, 
     a.rkind = L->d.right_kind[pass];
     a.dLN = L->d.dLN[pass];
     if (a.lines <= 0) return FPDE_OK;
+    if (L->sf) {
+        LodSfArgs f;
+        int n2s;
+        pass_geometry(L, pass, &f.Nl, &f.n1, &n2s, &f.s1, &f.s2, &f.st);
+        f.lines = a.lines;
+        f.U = L->U;
+        f.coef = L->sfc[pass];
+        f.Tm = L->sfT[pass];
+        f.part = a.part; f.KS = a.KS; f.pstride = a.pstride;
+        f.rp = a.rp; f.bc = a.bc;
+        f.lam = L->lam; f.lamR = L->lamR; f.thr = L->sf_thr; f.dLN = a.dLN;
+        f.sd = L->sf_sd; f.maxiter = L->sf_maxit; f.rkind = a.rkind;
+        f.iters = L->sf_iters;
+        f.flags = L->ctx->d_flags;
+        return launch_lod_pass_sf(st, f);
+    }
     if (L->rich) {
         LodRichArgs r;
         r.sZ = L->rsZ; r.dL = L->rdL[pass]; r.al = L->ral;
@@ -643,7 +666,10 @@ int fpde_lod3d_destroy(fpde_lod3d *L)
         dev_free(L->cCB[q]);
         dev_free(L->cPF[q]);
         dev_free(L->rdL[q]);
+        dev_free(L->sfc[q]);
+        dev_free(L->sfT[q]);
     }
+    dev_free(L->sf_iters);
     dev_free(L->rsZ);
     dev_free(L->ral);
     delete L;
@@ -669,6 +695,17 @@ int fpde_lod3d_create(fpde_ctx *ctx, const fpde_lod3d_desc *desc, const double *
         FPDE_CHECK_ARG(d.series_terms == 0, "richards: no series expansion");
         FPDE_CHECK_ARG(d.M <= d.sN + 1 && d.K <= d.sN + 1,
                        "richards: M and K at most sN + 1 (suctions index sZ by positions along every pass)");
+    }
+    const fpde_space_frac *sfd = d.space_frac;
+    if (sfd) {
+        FPDE_CHECK_ARG(!rich, "space_frac: not with the Richards problem");
+        FPDE_CHECK_ARG(sfd->space_der == 0 || sfd->space_der == 1, "space_frac: space_der must be 0 or 1");
+        FPDE_CHECK_ARG(std::isfinite(sfd->tol) && sfd->tol >= 0.0, "space_frac: tol must be >= 0");
+        FPDE_CHECK_ARG(sfd->max_iter >= 1 && sfd->max_iter <= FPDE_SF_MAX_ITER, "space_frac: max_iter out of range");
+        FPDE_CHECK_ARG(d.sN <= FPDE_SF_MAX_N && d.M <= FPDE_SF_MAX_N && d.K <= FPDE_SF_MAX_N,
+                       "space_frac: lines longer than FPDE_SF_MAX_N intervals");
+        for (int q = 0; q < 3; ++q)
+            FPDE_CHECK_ARG(sfd->Tm[q] && sfd->mc[q] && sfd->iw[q], "space_frac: Tm, mc and iw of every pass required");
     }
     FPDE_CHECK_ARG(d.sN >= 2 && d.M >= 2 && d.K >= 2, "every axis needs at least 2 intervals");
     FPDE_CHECK_ARG(d.lag_weights || (d.alpha > 0.0 && d.alpha < 1.0), "alpha must be in (0, 1)");
@@ -789,9 +826,42 @@ int fpde_lod3d_create(fpde_ctx *ctx, const fpde_lod3d_desc *desc, const double *
                cudaMemcpy(L->rsZ, rich->sZ, (size_t)(d.sN + 2) * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess ||
                dev_alloc((void **)&L->ral, (size_t)scratch * sizeof(double));
     }
+    if (!fail && sfd) {                        // operands of the space-fractional line systems
+        L->sf = true;
+        L->sf_sd = sfd->space_der;
+        L->sf_thr = sfd->tol;
+        L->sf_maxit = sfd->max_iter;
+        fail = sf_prepare() != FPDE_OK || dev_alloc((void **)&L->sf_iters, sizeof(unsigned long long)) ||
+               cudaMemset(L->sf_iters, 0, sizeof(unsigned long long)) != cudaSuccess;
+        std::vector<double> hc;
+        for (int pass = 0; pass < 3 && !fail; ++pass) {
+            int Nl, n1, n2;
+            int64_t s1, s2, stp;
+            pass_geometry(L, pass, &Nl, &n1, &n2, &s1, &s2, &stp);
+            const int lines = n1 * n2, m = Nl + 1;
+            L->lines[pass] = lines;
+            hc.assign((size_t)lines * 7 * m, 0.0);
+            const double *src[7] = {coefA + (int64_t)pass * L->G, coefB + (int64_t)pass * L->G,
+                                    coefRlap + (int64_t)pass * L->G, sfd->mc[pass], sfd->mc[pass] + L->G,
+                                    sfd->mc[pass] + 2 * L->G, sfd->iw[pass]};
+            for (int line = 0; line < lines; ++line) {
+                const int a = line % n1, b = line / n1;
+                const int64_t base = (int64_t)(1 + a) * s1 + (int64_t)(1 + b) * s2;
+                double *dst = hc.data() + (size_t)line * 7 * m;
+                for (int r = 0; r < 7; ++r)
+                    for (int q = 1; q < Nl; ++q) dst[(size_t)r * m + q] = src[r][base + (int64_t)q * stp];
+            }
+            std::vector<double> tm(sfd->Tm[pass], sfd->Tm[pass] + m);
+            tm[0] = tm[1] = 0.0;                                      // never read
+            fail = dev_alloc((void **)&L->sfc[pass], hc.size() * sizeof(double)) ||
+                   dev_alloc((void **)&L->sfT[pass], (size_t)m * sizeof(double)) ||
+                   cudaMemcpy(L->sfc[pass], hc.data(), hc.size() * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess ||
+                   cudaMemcpy(L->sfT[pass], tm.data(), (size_t)m * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess;
+        }
+    }
     // per-pass line coefficients, evaluated in the reference's order (al1 :4002-4027)
     std::vector<double> hA, hg, hal;
-    for (int pass = 0; pass < 3 && !fail && !rich; ++pass) {
+    for (int pass = 0; pass < 3 && !fail && !rich && !sfd; ++pass) {
         int Nl, n1, n2;
         int64_t s1, s2, stp;
         pass_geometry(L, pass, &Nl, &n1, &n2, &s1, &s2, &stp);
@@ -907,6 +977,7 @@ int fpde_lod3d_create(fpde_ctx *ctx, const fpde_lod3d_desc *desc, const double *
     L->d.source = nullptr;
     L->d.bc = nullptr;
     L->d.richards = nullptr;
+    L->d.space_frac = nullptr;
     *out = L;
     return FPDE_OK;
 }
@@ -976,6 +1047,21 @@ int fpde_lod3d_solve_host(fpde_lod3d *L, const double *u0_host, int steps, doubl
     FPDE_CUDA(cudaMemcpyAsync(u_out_host, L->U, L->G * sizeof(double), cudaMemcpyDeviceToHost, L->ctx->stream));
     FPDE_CUDA(cudaStreamSynchronize(L->ctx->stream));
     return ctx_check_flags(L->ctx, "lod3d");
+}
+
+int fpde_lod3d_sf_iterations(fpde_lod3d *L, int64_t *iters)
+{
+    clear_error();
+    FPDE_CHECK_ARG(L && iters, "null argument");
+    *iters = 0;
+    if (!L->sf) return FPDE_OK;
+    int rc = ctx_enter(L->ctx);
+    if (rc) return rc;
+    unsigned long long v = 0;
+    FPDE_CUDA(cudaMemcpyAsync(&v, L->sf_iters, sizeof v, cudaMemcpyDeviceToHost, L->ctx->stream));
+    FPDE_CUDA(cudaStreamSynchronize(L->ctx->stream));
+    *iters = (int64_t)v;
+    return FPDE_OK;
 }
 
 int fpde_lod3d_steps_done(const fpde_lod3d *L, int64_t *n)

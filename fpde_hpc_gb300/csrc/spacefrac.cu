@@ -1,0 +1,396 @@
+// The implicit space-fractional operator of fpde_hpc_1d.cpp (impl 2, toeplitz_mult_alg 0): the
+// product vmul_T (:6618-6747) of tridiag(Mat) + iw * T * tridiag(Mcoefs), with T the Toeplitz
+// matrix of the space-fractional integral (row Tm, one- or two-sided), and the solver solve_mln<1>
+// (:812-1157) that U1 (:4769-4791) runs on it for every line of every pass.
+//
+// One CTA owns one line: the line's operands and the solver's vectors live in shared memory, every
+// product and every vector update is spread over the CTA's threads, and each CTA iterates to its
+// own convergence. Every value is formed with the reference's operations in the reference's order
+// and without contracted multiply-adds (its x86-64 build rounds each product): each output of the
+// product is one thread's sequential sum over j, and each dot product one thread's sequential sum
+// over the line, so the iterates, the iteration count and the solution equal the reference's bit
+// for bit on the same inputs. Products and dot products are FP64-pipe work (GB300: about two FP64
+// lanes per cycle per SM), so a pass keeps many lines in flight per SM (20 vectors of n+1 doubles
+// per CTA: 21 KB at n = 128).
+#include <cmath>
+#include <vector>
+
+#include "common.cuh"
+#include "kernels.cuh"
+#include "scan.cuh"
+
+namespace fpde {
+
+__device__ __forceinline__ double dm(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double da(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double ds(double a, double b) { return __dsub_rn(a, b); }
+
+// Shared-memory vectors of one line, n+1 doubles each.
+struct SfVec {
+    double *Tm, *m0, *m1, *m2, *c0, *c1, *c2, *iw, *rs, *B, *x, *r, *q0, *g0, *g1, *w0, *w1, *u, *Au, *bt;
+};
+constexpr int SF_NVEC = 20;
+constexpr int SF_THREADS = 128;
+constexpr uint64_t SF_TIME_LIMIT_NS = 10ull * 1000000000ull;   // per line solve
+
+__device__ __forceinline__ SfVec sf_carve(double *sm, int m)
+{
+    SfVec v;
+    double **f[SF_NVEC] = {&v.Tm, &v.m0, &v.m1, &v.m2, &v.c0, &v.c1, &v.c2, &v.iw, &v.rs, &v.B,
+                           &v.x,  &v.r,  &v.q0, &v.g0, &v.g1, &v.w0, &v.w1, &v.u,  &v.Au, &v.bt};
+#pragma unroll
+    for (int k = 0; k < SF_NVEC; ++k) *f[k] = sm + (size_t)k * m;
+    return v;
+}
+
+// rv = vmul_T(xv) on the line's operands (:6662-6686). All threads; ends with a barrier.
+__device__ void sf_apply(const SfVec &s, int n, int sd, bool has_iw, bool has_rs, const double *xv, double *rv)
+{
+    const int T = blockDim.x, tid = threadIdx.x;
+    for (int j = 1 + tid; j < n; j += T)
+        s.bt[j] = da(da(dm(s.c0[j], xv[j - 1]), dm(s.c1[j], xv[j])), dm(s.c2[j], xv[j + 1]));
+    __syncthreads();
+    for (int i = tid; i <= n; i += T) {
+        double r;
+        if (i == 0) {
+            r = da(dm(s.m1[0], xv[0]), dm(s.m2[0], xv[1]));
+        } else if (i == n) {
+            r = da(dm(s.m0[n], xv[n - 1]), dm(s.m1[n], xv[n]));
+        } else {
+            r = da(da(dm(s.m0[i], xv[i - 1]), dm(s.m1[i], xv[i])), dm(s.m2[i], xv[i + 1]));
+            double v = 0.0;
+            for (int j = 1; j < i; ++j) v = da(v, dm(s.bt[j], s.Tm[i - j + 1]));
+            if (sd)
+                for (int j = i + 1; j < n; ++j) v = ds(v, dm(s.bt[j], s.Tm[j - i + 1]));
+            if (has_rs) v = __ddiv_rn(v, s.rs[i]);
+            r = da(r, has_iw ? dm(v, s.iw[i]) : v);
+        }
+        rv[i] = r;
+    }
+    __syncthreads();
+}
+
+// Sequential dot products in the reference's order (one thread).
+__device__ __forceinline__ double sf_dot(const double *a, const double *b, int m)
+{
+    double s = 0.0;
+    for (int i = 0; i < m; ++i) s = da(s, dm(a[i], b[i]));
+    return s;
+}
+__device__ __forceinline__ double sf_negdot(const double *a, const double *b, int m)
+{
+    double s = 0.0;
+    for (int i = 0; i < m; ++i) s = ds(s, dm(a[i], b[i]));
+    return s;
+}
+
+// solve_mln<1> on the line in s (x: initial guess in, solution out). All threads; returns the
+// iteration count. A solve that restarts more than maxiter times without an iteration in between,
+// or runs past the time limit, stops and sets DEVERR_SOLVER.
+__device__ int sf_solve_cta(SfVec s, int n, int sd, bool has_iw, bool has_rs, double thr, int maxiter,
+                            double *scal, unsigned *flags)
+{
+    const int m = n + 1, T = blockDim.x, tid = threadIdx.x;
+    const double md = (double)m;
+    const unsigned long long t0 = gtimer_ns();
+    int iter = 1, restarts = 0;
+    double c1, norm, al, ro1 = 0.0, beta;
+restart:
+    if (++restarts > maxiter + 1) {
+        if (tid == 0) atomicOr(flags, DEVERR_SOLVER);
+        return iter;
+    }
+    sf_apply(s, n, sd, has_iw, has_rs, s.x, s.r);                            // :841-844
+    for (int i = tid; i < m; i += T) {
+        const double v = ds(s.B[i], s.r[i]);
+        s.r[i] = v;
+        s.g1[i] = v;
+        s.q0[i] = v;
+    }
+    __syncthreads();
+    sf_apply(s, n, sd, has_iw, has_rs, s.g1, s.w1);                          // :851
+    if (tid == 0) scal[0] = sf_dot(s.q0, s.w1, m);
+    if (tid == 32 % T) scal[1] = sf_dot(s.r, s.r, m);
+    __syncthreads();
+    c1 = scal[0];
+    norm = scal[1];
+    if (fabs(__ddiv_rn(norm, md)) < thr) return iter;
+    for (;;) {
+        if (tid == 0) scal[2] = __ddiv_rn(sf_dot(s.q0, s.r, m), c1);          // :871-877
+        __syncthreads();
+        al = scal[2];
+        if (!(c1 != 0.0)) goto restart;
+        for (int i = tid; i < m; i += T) {
+            s.u[i] = ds(s.r[i], dm(al, s.w1[i]));
+            s.x[i] = da(s.x[i], dm(al, s.g1[i]));
+        }
+        __syncthreads();
+        sf_apply(s, n, sd, has_iw, has_rs, s.u, s.Au);                       // :890
+        if (tid == 0) scal[3] = sf_dot(s.Au, s.Au, m);
+        if (tid == 32 % T) scal[4] = sf_dot(s.Au, s.u, m);
+        __syncthreads();
+        norm = scal[3];
+        ro1 = __ddiv_rn(-scal[4], norm);
+        if (norm == 0.0) goto restart;
+        for (int i = tid; i < m; i += T) s.x[i] = ds(s.x[i], dm(ro1, s.u[i]));
+        __syncthreads();
+        sf_apply(s, n, sd, has_iw, has_rs, s.x, s.r);                        // :943-947
+        for (int i = tid; i < m; i += T) s.r[i] = ds(s.B[i], s.r[i]);
+        __syncthreads();
+        if (tid == 0) {                                                        // :1056-1065
+            double b = __ddiv_rn(sf_negdot(s.q0, s.r, m), c1);
+            if (c1 == 0.0) b = 0.0;
+            scal[5] = b;
+        }
+        __syncthreads();
+        beta = scal[5];
+        const double bro = __ddiv_rn(beta, ro1);
+        for (int i = tid; i < m; i += T) {
+            const double zw = da(s.r[i], dm(beta, s.w1[i]));
+            s.g0[i] = da(zw, dm(bro, s.g1[i]));
+        }
+        __syncthreads();
+        sf_apply(s, n, sd, has_iw, has_rs, s.g0, s.w0);                      // :1094
+        if (tid == 0) {
+            scal[6] = sf_dot(s.q0, s.w0, m);
+            scal[8] = gtimer_ns() - t0 > SF_TIME_LIMIT_NS ? 1.0 : 0.0;           // one decision for all
+        }
+        if (tid == 32 % T) scal[7] = sf_dot(s.r, s.r, m);
+        __syncthreads();
+        c1 = scal[6];
+        norm = scal[7];
+        const bool late = scal[8] != 0.0;
+        {                                                                      // :1104-1121
+            double *t = s.g0; s.g0 = s.g1; s.g1 = t;
+            t = s.w0; s.w0 = s.w1; s.w1 = t;
+        }
+        restarts = 0;
+        if (fabs(__ddiv_rn(norm, md)) < thr) break;
+        ++iter;
+        if (iter == maxiter) break;
+        if (late) {
+            if (tid == 0) atomicOr(flags, DEVERR_SOLVER);
+            break;
+        }
+    }
+    return iter;
+}
+
+__device__ __forceinline__ void sf_copy(double *dst, const double *src, int m)
+{
+    for (int i = threadIdx.x; i < m; i += blockDim.x) dst[i] = src[i];
+}
+
+// ------------------------------------------------------------- batch of lines (the C ABI)
+
+struct SfBatchArgs {
+    int lines, n, sd;
+    const double *mat, *mc, *Tm, *iw, *rs, *B;   // mat, mc: 3 planes of lines x (n+1)
+    const double *x;
+    double *r;                                   // product output (matvec) or solution (solve)
+    double thr;
+    int maxiter;
+    int *iters;
+    unsigned *flags;
+};
+
+__global__ void __launch_bounds__(SF_THREADS) k_sf_batch(SfBatchArgs a, int solve)
+{
+    extern __shared__ __align__(16) double sf_sm[];
+    __shared__ double scal[9];
+    const int m = a.n + 1, line = blockIdx.x;
+    const int64_t o = (int64_t)line * m, plane = (int64_t)a.lines * m;
+    SfVec s = sf_carve(sf_sm, m);
+    sf_copy(s.Tm, a.Tm, m);
+    sf_copy(s.m0, a.mat + o, m);
+    sf_copy(s.m1, a.mat + plane + o, m);
+    sf_copy(s.m2, a.mat + 2 * plane + o, m);
+    sf_copy(s.c0, a.mc + o, m);
+    sf_copy(s.c1, a.mc + plane + o, m);
+    sf_copy(s.c2, a.mc + 2 * plane + o, m);
+    if (a.iw) sf_copy(s.iw, a.iw + o, m);
+    if (a.rs) sf_copy(s.rs, a.rs + o, m);
+    sf_copy(s.x, a.x + o, m);
+    if (solve) sf_copy(s.B, a.B + o, m);
+    __syncthreads();
+    if (!solve) {
+        sf_apply(s, a.n, a.sd, a.iw != nullptr, a.rs != nullptr, s.x, s.r);
+        sf_copy(a.r + o, s.r, m);
+        return;
+    }
+    const int it = sf_solve_cta(s, a.n, a.sd, a.iw != nullptr, a.rs != nullptr, a.thr, a.maxiter, scal, a.flags);
+    sf_copy(a.r + o, s.x, m);
+    if (a.iters && threadIdx.x == 0) a.iters[line] = it;
+}
+
+// ------------------------------------------------------------------ LOD pass with impl 2
+
+// One line of one pass: the system implicit2_gen forms (:4630-4663) from the coefficient grids of
+// the pass (line-major: per line A, B, Rlap, mc0, mc1, mc2, iw, each Nl+1 values), the state and
+// this step's source, history and line ends; solved in place and written back with the ghost copy
+// U[Nl+1] = U[Nl] (U1 :4792).
+__global__ void __launch_bounds__(SF_THREADS) k_lod_pass_sf(LodSfArgs a)
+{
+    extern __shared__ __align__(16) double sf_sm[];
+    __shared__ double scal[9];
+    const int n = a.Nl, m = n + 1, line = blockIdx.x, tid = threadIdx.x, T = blockDim.x;
+    const int la = line % a.n1, lb = line / a.n1;
+    const int64_t base = (int64_t)(1 + la) * a.s1 + (int64_t)(1 + lb) * a.s2;
+    const double *cf = a.coef + (int64_t)line * 7 * m;
+    SfVec s = sf_carve(sf_sm, m);
+    sf_copy(s.Tm, a.Tm, m);
+    for (int p = tid; p < m; p += T) {
+        const int64_t id = base + (int64_t)p * a.st;
+        const double u = a.U[id];
+        s.x[p] = u;
+        if (p >= 1 && p < n) {
+            s.m0[p] = cf[p];
+            s.m2[p] = cf[m + p];
+            s.m1[p] = -da(cf[2 * m + p], a.lamR);                                  // -R :3117-3123
+            s.c0[p] = cf[3 * m + p];
+            s.c1[p] = cf[4 * m + p];
+            s.c2[p] = cf[5 * m + p];
+            s.iw[p] = cf[6 * m + p];
+            double om = ds(a.rp ? a.rp[id] : 0.0, dm(a.lam, u));                     // Om1_impl :4441
+            if (a.KS) {
+                double sv = 0.0;
+                for (int k = 0; k < a.KS; ++k) sv = da(sv, __ldcg(a.part + (int64_t)k * a.pstride + id));
+                om = da(om, sv);                                                     // :4507-4510
+            }
+            s.B[p] = om;
+        } else if (p == 0) {                                                         // :4643-4651
+            s.m0[0] = 0.0; s.m1[0] = 1.0; s.m2[0] = 0.0;
+            s.B[0] = a.bc ? a.bc[id] : 0.0;
+        } else {
+            const double g = a.bc ? a.bc[id] : 0.0;
+            s.m2[n] = 0.0; s.m1[n] = 1.0;
+            if (a.rkind == FPDE_BC_FLUX) { s.m0[n] = -1.0; s.B[n] = dm(g, a.dLN); } // bottom_cond 0
+            else { s.m0[n] = 0.0; s.B[n] = g; }
+        }
+    }
+    __syncthreads();
+    const int it = sf_solve_cta(s, n, a.sd, true, false, a.thr, a.maxiter, scal, a.flags);
+    for (int p = tid; p < m; p += T) a.U[base + (int64_t)p * a.st] = s.x[p];
+    if (tid == 0) {
+        a.U[base + (int64_t)m * a.st] = s.x[n];
+        if (a.iters) atomicAdd(a.iters, (unsigned long long)it);
+    }
+}
+
+size_t sf_smem_bytes(int n) { return (size_t)SF_NVEC * (size_t)(n + 1) * sizeof(double); }
+
+// Opt both kernels in to the shared memory of the longest line once per device (outside any graph
+// capture: fpde_lod3d_create calls this before its first run).
+int sf_prepare()
+{
+    const int bytes = (int)sf_smem_bytes(FPDE_SF_MAX_N);
+    if (smem_opt_in((const void *)k_lod_pass_sf, bytes) != cudaSuccess ||
+        smem_opt_in((const void *)k_sf_batch, bytes) != cudaSuccess)
+        return set_error(FPDE_ERR_CUDA, "space-fractional kernels: shared memory opt-in failed");
+    return FPDE_OK;
+}
+
+int launch_lod_pass_sf(cudaStream_t st, const LodSfArgs &a)
+{
+    const size_t smem = sf_smem_bytes(a.Nl);
+    k_lod_pass_sf<<<(unsigned)a.lines, SF_THREADS, smem, st>>>(a);
+    FPDE_LAUNCHED(1);
+    return FPDE_OK;
+}
+
+}  // namespace fpde
+
+using namespace fpde;
+
+static int sf_batch(fpde_ctx *ctx, int lines, int n, const double *mat, const double *mc, const double *Tm,
+                    const double *iw, const double *rs, int space_der, const double *B, const double *x, double *out,
+                    double thr, int maxiter, int *iters, int on_device, int solve)
+{
+    clear_error();
+    FPDE_CHECK_ARG(mat && mc && Tm && x && out, "null argument");
+    FPDE_CHECK_ARG(!solve || B, "null right-hand side");
+    FPDE_CHECK_ARG(lines >= 1 && n >= 1 && n <= FPDE_SF_MAX_N, "lines >= 1 and 1 <= n <= FPDE_SF_MAX_N");
+    FPDE_CHECK_ARG(space_der == 0 || space_der == 1, "space_der must be 0 or 1");
+    FPDE_CHECK_ARG(!solve || (maxiter >= 1 && maxiter <= FPDE_SF_MAX_ITER), "maxiter must be 1 .. FPDE_SF_MAX_ITER");
+    int rc = ctx_enter(ctx);
+    if (rc) return rc;
+    cudaStream_t st = ctx->stream;
+    const size_t m = (size_t)n + 1, vec = (size_t)lines * m * sizeof(double);
+    const size_t smem = sf_smem_bytes(n);
+    if ((rc = sf_prepare())) return rc;
+    SfBatchArgs a{};
+    a.lines = lines; a.n = n; a.sd = space_der; a.thr = thr; a.maxiter = maxiter; a.flags = ctx->d_flags;
+    std::vector<void *> own;
+    auto stage = [&](const double *src, size_t bytes, bool copy_in) -> double * {
+        if (on_device) return const_cast<double *>(src);
+        void *p = nullptr;
+        if (dev_alloc(&p, bytes)) return nullptr;
+        own.push_back(p);
+        if (copy_in && src) cudaMemcpyAsync(p, src, bytes, cudaMemcpyHostToDevice, st);
+        return (double *)p;
+    };
+    bool fail = false;
+    a.mat = stage(mat, 3 * vec, true);
+    a.mc = stage(mc, 3 * vec, true);
+    a.Tm = stage(Tm, m * sizeof(double), true);
+    a.iw = iw ? stage(iw, vec, true) : nullptr;
+    a.rs = rs ? stage(rs, vec, true) : nullptr;
+    a.B = (solve && B) ? stage(B, vec, true) : nullptr;
+    a.x = stage(x, vec, true);
+    a.r = stage(out, vec, false);
+    int *d_it = nullptr;
+    fail = !a.mat || !a.mc || !a.Tm || (iw && !a.iw) || (rs && !a.rs) || (solve && !a.B) || !a.x || !a.r;
+    if (!fail && iters) {
+        if (on_device) d_it = iters;
+        else fail = dev_alloc((void **)&d_it, (size_t)lines * sizeof(int)) != 0;
+        if (!on_device && d_it) own.push_back(d_it);
+    }
+    a.iters = d_it;
+    if (!fail) {
+        k_sf_batch<<<(unsigned)lines, SF_THREADS, smem, st>>>(a, solve);
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) rc = set_error(FPDE_ERR_CUDA, "space-fractional batch launch: %s", cudaGetErrorString(e));
+        else count_launches(1);
+        if (!rc && !on_device) {
+            cudaMemcpyAsync(out, a.r, vec, cudaMemcpyDeviceToHost, st);
+            if (iters) cudaMemcpyAsync(iters, d_it, (size_t)lines * sizeof(int), cudaMemcpyDeviceToHost, st);
+        }
+        if (!rc) rc = ctx_check_flags(ctx, solve ? "fpde_sf_solve" : "fpde_sf_matvec");
+    } else {
+        rc = set_error(FPDE_ERR_NOMEM, "space-fractional batch: device allocation failed");
+    }
+    cudaStreamSynchronize(st);
+    for (void *p : own) dev_free(p);
+    return rc;
+}
+
+extern "C" {
+
+int fpde_sf_matvec(fpde_ctx *ctx, int lines, int n, const double *mat, const double *mc, const double *Tm,
+                   const double *iw, const double *rs, int space_der, const double *x, double *r, int on_device)
+{
+    return sf_batch(ctx, lines, n, mat, mc, Tm, iw, rs, space_der, nullptr, x, r, 0.0, 1, nullptr, on_device, 0);
+}
+
+int fpde_sf_solve(fpde_ctx *ctx, int lines, int n, const double *mat, const double *mc, const double *Tm,
+                  const double *iw, const double *rs, int space_der, const double *B, double *x, double thr,
+                  int maxiter, int *iters, int on_device)
+{
+    return sf_batch(ctx, lines, n, mat, mc, Tm, iw, rs, space_der, B, x, x, thr, maxiter, iters, on_device, 1);
+}
+
+int fpde_sf_toeplitz_row(double gamma, const double *Z, int n, double *Tm)
+{
+    clear_error();
+    FPDE_CHECK_ARG(Z && Tm && n >= 1, "null argument or n < 1");
+    FPDE_CHECK_ARG(gamma > 0.0 && gamma <= 1.0, "gamma must be in (0, 1]");
+    const double A = 1.0 - gamma;                                // :3675-3681
+    const double Dg2 = 1.0 / std::tgamma(2.0 - gamma);           // 1 / g2g, g2g = Gamma(2 - gamma) (:2715)
+    Tm[0] = 0.0;
+    for (int i = 1; i <= n; ++i)
+        Tm[i] = A != 0.0 ? Dg2 * std::fabs(std::pow(std::fabs(Z[1] - Z[i]), A) - std::pow(std::fabs(Z[1] - Z[i + 1]), A))
+                         : (i == 1 ? 1.0 : 0.0);
+    return FPDE_OK;
+}
+
+}  // extern "C"

@@ -414,6 +414,52 @@ int fpde_line_coefs(int64_t N, const double *k, const double *iw, const double *
  * along j (_M) and along i (sN), each with R = Rlap + Da*kkk0/tau and Om = -Da*(kkk0/tau) U
  * (+ Rp + Da S in the K pass), and a ghost copy at the far end of every line (U1 :4792).
  * The grid has (sN+2)(M+2)(K+2) points with idx = i + j (sN+2) + k (sN+2)(M+2) (:1181). */
+/* ---------------------------------------------------------------------------------------------
+ * Implicit space-fractional operator (the reference's impl 2 with toeplitz_mult_alg 0).
+ *
+ * With a space-fractional order gamma < 1, U1 (fpde_hpc_1d.cpp:4769-4791) solves every line's
+ * system tridiag(Mat) + iw * T * tridiag(Mcoefs) with solve_mln<1> (:812-1157) and the product
+ * vmul_T (:6618-6747): T is the Toeplitz matrix of the space-fractional integral, strictly lower
+ * (space_der 0: row i sums j = 1..i-1 with Tm[i-j+1]) or two-sided (space_der 1: minus the sum over
+ * j = i+1..n-1 with Tm[j-i+1]) over the interior rows 1..n-1 of a line of n intervals; iw is
+ * inv_dw_dh (equation 0). The library forms every value with the reference's operations in its
+ * order and without contracted multiply-adds, so products, iterates and solutions equal the
+ * reference's (an x86-64 build) bit for bit on the same inputs.
+ * ------------------------------------------------------------------------------------------- */
+#define FPDE_SF_MAX_N 1400          /* longest line (intervals): one CTA holds a line in shared memory */
+#define FPDE_SF_MAX_ITER 1000000
+
+/* vmul_T on a batch of lines of n intervals: mat and mc are three planes (0 lower, 1 diagonal,
+ * 2 upper) of lines x (n+1) values (plane d at mat + d*lines*(n+1)); rows 0 and n of mat are the
+ * boundary rows, mc is read at rows 1..n-1; iw and rs (implicit_row_scaling: RS) are lines x (n+1)
+ * or NULL (1.0 / no scaling); Tm has n+1 entries of which 2..n-1 are read; x, r are lines x (n+1). */
+int fpde_sf_matvec(fpde_ctx *ctx, int lines, int n, const double *mat, const double *mc, const double *Tm,
+                   const double *iw, const double *rs, int space_der, const double *x, double *r, int on_device);
+/* solve_mln<1> on every line (rb = 0, re = n+1): x holds the initial guesses and receives the
+ * solutions; a line stops when |r.r / (n+1)| < thr (the reference's impl_err) or after maxiter - 1
+ * iterations (impl_niter); iters (lines ints, may be NULL) receives each line's count. A line whose
+ * solve breaks down maxiter times in a row, or runs for more than 10 s, stops: FPDE_ERR_NUMERIC. */
+int fpde_sf_solve(fpde_ctx *ctx, int lines, int n, const double *mat, const double *mc, const double *Tm,
+                  const double *iw, const double *rs, int space_der, const double *B, double *x, double thr,
+                  int maxiter, int *iters, int on_device);
+/* The Toeplitz row of a uniform axis Z (n+2 coordinates): Tm[i] = |(Z1-Zi)^(1-gamma) -
+ * (Z1-Z(i+1))^(1-gamma)| / Gamma(2-gamma), i = 1..n, Tm[0] = 0 (the reference's fill :3670-3694,
+ * with C tgamma for its Gamma). Host function. */
+int fpde_sf_toeplitz_row(double gamma, const double *Z, int n, double *Tm);
+
+/* The implicit space-fractional solves of a 3D LOD (fpde_lod3d_desc.space_frac): per pass p the
+ * Toeplitz row Tm[p] (Nl+1 values), the Mcoefs grids mc[p] (three host grids: lower, diagonal,
+ * upper, at every interior line node) and inv_dw_dh iw[p] (one grid), and the solver's threshold
+ * and iteration cap. Line lengths at most FPDE_SF_MAX_N. */
+typedef struct fpde_space_frac {
+    int space_der;              /* 0 one-sided, 1 two-sided */
+    double tol;                 /* impl_err (default 1e-9 in the reference) */
+    int max_iter;               /* impl_niter (5000) */
+    const double *Tm[3];
+    const double *mc[3];        /* each 3 x grid */
+    const double *iw[3];        /* each one grid */
+} fpde_space_frac;
+
 typedef struct fpde_lod3d_desc {
     int sN, M, K;           /* intervals along i, j, k */
     double alpha, tau, Da;  /* as for lines; tau uniform */
@@ -439,6 +485,9 @@ typedef struct fpde_lod3d_desc {
     const fpde_richards *richards; /* optional: the Richards problem (coefficients from the solution
                                every step; coefA/B/Rlap, the boundary kinds and bc are then unused
                                and may be NULL; needs M, K <= sN + 1) */
+    const fpde_space_frac *space_frac; /* optional: implicit space-fractional line solves (impl 2);
+                               coefA/B/Rlap are then the reference's A_/B/R with its space-fractional
+                               local weights, every pass has a Dirichlet start, right_kind per pass */
 } fpde_lod3d_desc;
 
 /* coefA/B/Rlap: three host grids each (pass 0 = sN, 1 = _M, 2 = K) of the line coefficients at
@@ -456,6 +505,8 @@ int fpde_lod3d_reset(fpde_lod3d *lod, const double *u0, int on_device);
 /* End-to-end call: upload u0 from host, run `steps`, download the grid to host. */
 int fpde_lod3d_solve_host(fpde_lod3d *lod, const double *u0_host, int steps, double *u_out_host);
 int fpde_lod3d_steps_done(const fpde_lod3d *lod, int64_t *n);
+/* With space_frac: the solver iterations of every line solve since creation (0 otherwise). */
+int fpde_lod3d_sf_iterations(fpde_lod3d *lod, int64_t *iters);
 
 /* --------------------------------------------------------------- ensembles */
 

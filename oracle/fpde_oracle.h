@@ -168,7 +168,7 @@ int fo_line_run_richards(int N, double *U, double *hist, int64_t P, int steps, d
  * over interior rows i = 1..n-1: sum_{j=1}^{i-1} bt[j] Tm[i-j+1], minus (space_der 1)
  * sum_{j=i+1}^{n-1} bt[j] Tm[j-i+1]; divided by rs[i] when rs is given (implicit_row_scaling).
  * mat and mc are 3 x (n+1) (rows 0 = lower, 1 = diagonal, 2 = upper); mc is read at rows 1..n-1,
- * iw at 1..n-1 (NULL: 1.0, the C/T equations), Tm at 2..n. bt is scratch of n+1 values. */
+ * iw at 1..n-1 (NULL: 1.0, the C/T equations), Tm at 2..n-1. bt is scratch of n+1 values. */
 void fo_sf_matvec(int n, const double *mat, const double *mc, const double *Tm, const double *iw,
                   const double *rs, int space_der, const double *x, double *r, double *bt);
 

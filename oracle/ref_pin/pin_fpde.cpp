@@ -348,6 +348,9 @@ static void run_spacefrac(const char *path, int sd, double gam, double alpha, in
     w.scalar("space_der", sd); w.scalar("impl_err", ieps); w.scalar("impl_niter", initer);
     std::vector<uint64_t> gdims = {(uint64_t)(K + 2), (uint64_t)(_M + 2), (uint64_t)(sN + 2)};
     w.put("U0", gdims, s->b_U);
+    w.put("Z_pass0", std::vector<double>(s->sZ, s->sZ + sN + 2));   /* node coordinates of each axis */
+    w.put("Z_pass1", std::vector<double>(s->X, s->X + _M + 2));
+    w.put("Z_pass2", std::vector<double>(s->Y, s->Y + K + 2));
     std::vector<double> kb_all, kb_off, kkk0, tauv, S_all, U_all, rp, bc;
     for (int n = 0; n < steps; n++) {
         s->calc_step(tau);

@@ -1,0 +1,151 @@
+"""The implicit space-fractional operator on the GPU (fpde_sf_matvec, fpde_sf_solve and the LOD's
+impl-2 passes) against the reference's own runs and the oracle.
+
+The kernels form every value with the reference's operations in its order, without contracted
+multiply-adds, so the product and the solver reproduce the reference (an x86-64 build: every
+product rounded) bit for bit on the same inputs. A whole LOD step differs from the reference's
+only through its history sum (the GPU sums the history in another order, a few ulps), which the
+solver then carries: with the reference's default threshold (r.r/(n+1) < 1e-9) the solutions are
+iterates a few ulps apart, with a tight threshold they are the converged solution."""
+import numpy as np
+import pytest
+
+import oracle
+import sf_cases
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    import fpde_hpc_gb300 as fp
+    c = fp.Context(0)
+    yield c
+    c.close()
+
+
+@pytest.mark.parametrize("name", sf_cases.NAMES)
+@pytest.mark.parametrize("p", [0, 1, 2])
+def test_matvec_and_solve_bitwise_vs_reference(ctx, name, p):
+    c = sf_cases.load(name)
+    lc = sf_cases.line_case(c, p)
+    r = ctx.sf_matvec(lc["mat"], lc["mc"], lc["Tm"], lc["x"], iw=lc["iw"], space_der=c["space_der"])
+    assert np.array_equal(r, lc["r"])
+    x, it = ctx.sf_solve(lc["mat"], lc["mc"], lc["Tm"], lc["B"], lc["x0"], c["thr"], c["maxiter"], iw=lc["iw"],
+                         space_der=c["space_der"])
+    assert np.array_equal(x, lc["sol"])
+    _, it_o = oracle.sf_solve(lc["mat"], lc["mc"], lc["Tm"], lc["B"], lc["x0"], c["thr"], c["maxiter"], iw=lc["iw"],
+                              space_der=c["space_der"])
+    assert int(it[0]) == it_o
+
+
+def _random_batch(rng, lines, n):
+    """Diagonally dominant interior rows, identity boundary rows, a decaying Toeplitz row."""
+    m = n + 1
+    mat = np.zeros((3, lines, m))
+    mat[0, :, 1:n] = 1.0 + rng.random((lines, n - 1))
+    mat[2, :, 1:n] = 1.0 + rng.random((lines, n - 1))
+    mat[1, :, 1:n] = -(mat[0, :, 1:n] + mat[2, :, 1:n] + 50.0 + 10 * rng.random((lines, n - 1)))
+    mat[1, :, 0] = mat[1, :, n] = 1.0
+    mc = np.zeros((3, lines, m))
+    mc[0, :, 1:n] = 0.5 + rng.random((lines, n - 1))
+    mc[2, :, 1:n] = 0.5 + rng.random((lines, n - 1))
+    mc[1, :, 1:n] = -(mc[0, :, 1:n] + mc[2, :, 1:n])
+    iw = 1.0 + 0.5 * rng.random((lines, m))
+    Tm = np.zeros(m)
+    k = np.arange(2, m)
+    Tm[2:] = 0.3 * (k ** 0.25 - (k - 1) ** 0.25)
+    return mat, mc, iw, Tm
+
+
+@pytest.mark.parametrize("sd", [0, 1])
+@pytest.mark.parametrize("n,lines", [(1, 3), (2, 4), (64, 37), (129, 300), (700, 5), (1400, 2)])
+def test_batch_bitwise_vs_oracle(ctx, sd, n, lines):
+    rng = np.random.default_rng(n * 7 + sd)
+    mat, mc, iw, Tm = _random_batch(rng, lines, n)
+    x = rng.standard_normal((lines, n + 1))
+    B = rng.standard_normal((lines, n + 1))
+    r = ctx.sf_matvec(mat, mc, Tm, x, iw=iw, space_der=sd)
+    xs, its = ctx.sf_solve(mat, mc, Tm, B, x, 1e-20, 60, iw=iw, space_der=sd)
+    for L in range(lines):
+        ro = oracle.sf_matvec(mat[:, L], mc[:, L], Tm, x[L], iw=iw[L], space_der=sd)
+        assert np.array_equal(r[L], ro), f"line {L}"
+        xo, ito = oracle.sf_solve(mat[:, L], mc[:, L], Tm, B[L], x[L], 1e-20, 60, iw=iw[L], space_der=sd)
+        assert np.array_equal(xs[L], xo) and int(its[L]) == ito, f"line {L}"
+
+
+def test_row_scaling_and_device_buffers(ctx):
+    import torch
+    rng = np.random.default_rng(5)
+    mat, mc, iw, Tm = _random_batch(rng, 6, 90)
+    rs = 1.0 + rng.random((6, 91))
+    x = rng.standard_normal((6, 91))
+    r_host = ctx.sf_matvec(mat, mc, Tm, x, iw=iw, rs=rs, space_der=1)
+    dev = [torch.tensor(a, device="cuda") for a in (mat, mc, Tm, x, iw, rs)]
+    r_dev = ctx.sf_matvec(dev[0], dev[1], dev[2], dev[3], iw=dev[4], rs=dev[5], space_der=1)
+    assert np.array_equal(r_dev.cpu().numpy(), r_host)
+    for L in range(6):
+        ro = oracle.sf_matvec(mat[:, L], mc[:, L], Tm, x[L], iw=iw[L], rs=rs[L], space_der=1)
+        assert np.array_equal(r_host[L], ro)
+
+
+def test_breakdown_is_bounded_and_reported(ctx):
+    """A zero operator makes solve_mln<1> restart for ever (c[1] = 0 every time); the library stops
+    after max_iter restarts in a row and reports FPDE_ERR_NUMERIC."""
+    import fpde_hpc_gb300 as fp
+    n = 8
+    z = np.zeros((3, n + 1))
+    with pytest.raises(fp.FpdeError) as e:
+        ctx.sf_solve(z, z, np.zeros(n + 1), np.ones(n + 1), np.zeros(n + 1), 1e-12, 5)
+    assert e.value.code == 7
+    x, it = ctx.sf_solve(z, z, np.zeros(n + 1), np.zeros(n + 1), np.zeros(n + 1), 1e-12, 5)   # r = 0: done
+    assert int(it[0]) == 1
+
+
+def test_bad_sizes_are_errors(ctx):
+    import fpde_hpc_gb300 as fp
+    n = 1401
+    z = np.zeros((3, n + 1))
+    with pytest.raises(fp.FpdeError) as e:
+        ctx.sf_matvec(z, z, np.zeros(n + 1), np.zeros(n + 1))
+    assert e.value.code == 1
+
+
+def _lod(ctx, c, precision=0, max_steps=None):
+    import fpde_hpc_gb300 as fp
+    g = c["g"]
+    sN, M, K = c["dims"]
+    sf = dict(space_der=c["space_der"], tol=c["thr"], max_iter=c["maxiter"], Tm=[c["Tm"][p] for p in range(3)],
+              mc=[c["mc"][p] for p in range(3)], iw=[c["iw"][p] for p in range(3)])
+    steps = c["steps"]
+    return fp.Lod3D(ctx, c["dims"], float(g["alpha"]), float(g["tau"][0]), c["Da"], c["coefA"], c["coefB"],
+                    c["coefRlap"], g["U0"], max_steps or steps, source=g["Rp"], bc=g["BC"], precision=precision,
+                    space_frac=sf)
+
+
+@pytest.mark.parametrize("name,tol", [("fpde_sf_sd0", 1e-12), ("fpde_sf_sd1", 1e-12), ("fpde_sf_col", 1e-13)])
+def test_lod_replay_vs_reference(ctx, name, tol):
+    c = sf_cases.load(name)
+    g = c["g"]
+    lod = _lod(ctx, c)
+    worst = 0.0
+    for n in range(c["steps"]):
+        lod.run(1)
+        U = lod.state()
+        worst = max(worst, float(np.abs(U - g["U"][n]).max() / np.abs(g["U"][n]).max()))
+    assert lod.sf_iterations() > 0
+    lod.close()
+    assert worst <= tol, worst
+
+
+def test_lod_one_call_equals_step_by_step(ctx):
+    """A run captured as one graph gives the same grid as per-step calls."""
+    c = sf_cases.load("fpde_sf_col")
+    a = _lod(ctx, c)
+    for _ in range(c["steps"]):
+        a.run(1)
+    b = _lod(ctx, c)
+    b.run(c["steps"])
+    assert np.array_equal(a.state(), b.state())
+    a.close()
+    b.close()
