@@ -123,10 +123,30 @@ def _lod(ctx, c, precision=0, max_steps=None):
                     space_frac=sf)
 
 
-@pytest.mark.parametrize("name,tol", [("fpde_sf_sd0", 1e-12), ("fpde_sf_sd1", 1e-12), ("fpde_sf_col", 1e-13)])
-def test_lod_replay_vs_reference(ctx, name, tol):
+def _oracle_envelope(c, rel):
+    """How far the reference's own run moves when its source is scaled by 1 + rel (the oracle
+    reproduces the reference bit for bit, so this is the reference's sensitivity)."""
+    g = c["g"]
+    U = g["U0"].copy()
+    hist = np.zeros((c["steps"],) + U.shape)
+    worst = 0.0
+    for n in range(c["steps"]):
+        oracle.lod_step_sf(c["dims"], U, hist, n, c["kb_rows"][n], g["tau"], c["Da"], float(g["kkk0"][n]),
+                           c["coefA"], c["coefB"], c["coefRlap"], c["mc"], c["iw"], c["Tm"], c["space_der"], c["thr"],
+                           c["maxiter"], g["Rp"][n] * (1.0 + rel), g["BC"][n])
+        worst = max(worst, float(np.abs(U - g["U"][n]).max() / np.abs(g["U"][n]).max()))
+    return worst
+
+
+@pytest.mark.parametrize("name", sf_cases.NAMES)
+def test_lod_replay_vs_reference(ctx, name):
+    """The GPU's history sum differs from the reference's in the last bits, and the solver carries
+    that: the bar is ten times the reference's own response to a 1e-15 change of its source (with
+    the default threshold 1e-9 that response is 3e-5 on fpde_sf_sd0: the solution is an iterate;
+    with the tight threshold of fpde_sf_col it is 3.4e-12: the converged solution), and 1e-12."""
     c = sf_cases.load(name)
     g = c["g"]
+    env = max(_oracle_envelope(c, 1e-15), _oracle_envelope(c, -1e-15))
     lod = _lod(ctx, c)
     worst = 0.0
     for n in range(c["steps"]):
@@ -135,7 +155,69 @@ def test_lod_replay_vs_reference(ctx, name, tol):
         worst = max(worst, float(np.abs(U - g["U"][n]).max() / np.abs(g["U"][n]).max()))
     assert lod.sf_iterations() > 0
     lod.close()
-    assert worst <= tol, worst
+    assert worst <= max(10.0 * env, 1e-12), (worst, env)
+
+
+def _synthetic(dims, gam, seed):
+    """A larger well-posed impl-2 problem: Laplacian-like line coefficients, Mcoefs of a second
+    difference, iw = 1 + sin/2, the Toeplitz rows of uniform axes, a random source."""
+    import fpde_hpc_gb300 as fp
+    sN, M, K = dims
+    shape = (K + 2, M + 2, sN + 2)
+    rng = np.random.default_rng(seed)
+    coefA, coefB, coefR = (np.zeros((3,) + shape) for _ in range(3))
+    mc = np.zeros((3, 3) + shape)
+    iw = np.zeros((3,) + shape)
+    Tm = np.zeros((3, max(dims) + 2))
+    for p, nl in enumerate(dims):
+        h = 1.0 / nl
+        a = (1.0 + rng.random(shape)) / h ** 2
+        b = (1.0 + rng.random(shape)) / h ** 2
+        coefA[p], coefB[p], coefR[p] = a, b, a + b
+        mc[p, 0] = mc[p, 2] = 1.0 / h ** 2
+        mc[p, 1] = -2.0 / h ** 2
+        iw[p] = 1.0 + 0.5 * np.sin(np.arange(shape[0] * shape[1] * shape[2]).reshape(shape) * 0.37)
+        Tm[p, :nl + 1] = fp.sf_toeplitz_row(gam, np.arange(nl + 2) * h, nl)
+    rp = 0.1 * rng.standard_normal(shape)
+    u0 = rng.random(shape)
+    return coefA, coefB, coefR, mc, iw, Tm, rp, u0
+
+
+@pytest.mark.parametrize("sd", [0, 1])
+def test_lod_larger_grid_vs_oracle(ctx, sd):
+    """20 x 16 x 40 cells, 12 steps, both solved to a tight threshold: the GPU against the oracle.
+    The two sum the history in different orders (last bits); the bar is ten times the oracle's own
+    response to a 1e-15 change of the source (measured here: a few 1e-12)."""
+    import fpde_hpc_gb300 as fp
+    dims, alpha, tau, steps, thr, mx = (20, 16, 40), 0.75, 1e-3, 12, 1e-24, 300
+    coefA, coefB, coefR, mc, iw, Tm, rp, u0 = _synthetic(dims, 0.7, 3 + sd)
+    Da = 1.0 / fp.gamma(1.0 - alpha)
+    sf = dict(space_der=sd, tol=thr, max_iter=mx, Tm=list(Tm), mc=list(mc), iw=list(iw))
+    lod = fp.Lod3D(ctx, dims, alpha, tau, Da, coefA, coefB, coefR, u0, steps, source=rp, space_frac=sf)
+    t = oracle.time_points(np.full(steps, tau))
+    bc = np.zeros_like(u0)
+
+    def oracle_run(scale):
+        U = u0.copy()
+        hist = np.zeros((steps,) + U.shape)
+        out = []
+        for n in range(steps):
+            kb, k0 = oracle.l1_weights(alpha, t, n)
+            oracle.lod_step_sf(dims, U, hist, n, kb, np.full(steps, tau), Da, k0, coefA, coefB, coefR, mc, iw, Tm,
+                               sd, thr, mx, rp * scale, bc)
+            out.append(U.copy())
+        return out
+
+    ref = oracle_run(1.0)
+    env = max(max(float(np.abs(a - b).max() / np.abs(b).max()) for a, b in zip(oracle_run(1.0 + e), ref))
+              for e in (1e-15, -1e-15))
+    worst = 0.0
+    for n in range(steps):
+        lod.run(1)
+        G = lod.state()
+        worst = max(worst, float(np.abs(G - ref[n]).max() / np.abs(ref[n]).max()))
+    lod.close()
+    assert worst <= max(10.0 * env, 1e-12), (worst, env)
 
 
 def test_lod_one_call_equals_step_by_step(ctx):
