@@ -49,7 +49,9 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="config2",
-                    choices=["config2", "config3", "config4", "config5", "sum1", "sum2", "weights"])
+                    choices=["config2", "config3", "config4", "config5", "sum1", "sum2", "weights", "sf3d"])
+    ap.add_argument("--space-der", type=int, default=0, choices=[0, 1],
+                    help="sf3d: one-sided (0) or two-sided (1) space-fractional operator")
     ap.add_argument("--precision", default="auto", choices=["auto", "fp64", "bf16", "f16", "bf16x3"])
     ap.add_argument("--time-steps", type=int, default=None, help="override the workload's step count")
     ap.add_argument("--nodes", type=int, default=None, help="override the workload's size")
@@ -325,6 +327,72 @@ class LodWorkload:
 
     def bytes_io(self):
         return 8 * self.p.u0.size, 8 * self.p.u0.size
+
+
+class SfWorkload(LodWorkload):
+    """The 3D LOD with the reference's implicit space-fractional line solves (impl 2, TMA 0): every
+    line of every pass solved by solve_mln<1> with vmul_T (problems.sf3d)."""
+
+    def __init__(self, args):
+        from fpde_hpc_gb300 import problems
+        n = args.nodes or 64
+        self.p = problems.sf3d(n=n, steps=args.time_steps or 32, space_der=args.space_der)
+        self.name = "sf3d"
+        self.node_steps = self.p.node_steps
+        side = "two-sided" if args.space_der else "one-sided"
+        self.metric = (f"node-steps/s (3D LOD with implicit space-fractional line solves, vmul_T + solve_mln<1>, "
+                       f"{n}^3, {self.p.steps} steps)")
+        self.desc = (f"3D LOD {n}^3, {self.p.steps} steps, alpha 0.8, gamma {self.p.gamma} {side}, tau 1e-3, "
+                     "lognormal k (sigma 0.4, seed 11), Gaussian blob and source, Dirichlet 0 line ends, "
+                     "solver threshold 1e-9 / 5000 iterations (the reference's defaults)")
+        self._ops = None
+
+    def operands(self):
+        if self._ops is None:
+            p = self.p
+            cA, cB, cR = p.coefs()
+            Tm, mc, iw = p.sf_operands()
+            self._ops = (cA, cB, cR, Tm, mc, iw, p.source())
+        return self._ops
+
+    def build(self, ctx, prec):
+        import fpde_hpc_gb300 as fp
+        p = self.p
+        cA, cB, cR, Tm, mc, iw, src = self.operands()
+        sf = dict(space_der=p.space_der, tol=p.tol, max_iter=p.max_iter, Tm=list(Tm), mc=list(mc), iw=list(iw))
+        return fp.Lod3D(ctx, p.dims, p.alpha, p.tau, p.Da, cA, cB, cR, p.u0, p.steps, source=src, precision=prec,
+                        space_frac=sf)
+
+    def sample_lengths(self):
+        S = self.p.steps
+        return [max(1, S // 8), max(2, S // 4), max(3, S // 2)]
+
+    def run_sample(self, s, threads):
+        os.environ["OMP_NUM_THREADS"] = str(threads)
+        oracle = _oracle()
+        p = self.p
+        cA, cB, cR, Tm, mc, iw, src = self.operands()
+        taus = np.full(p.steps, p.tau)
+        t = oracle.time_points(taus)
+        U = p.u0.copy()
+        hist = np.zeros((s,) + U.shape)
+        bc = np.zeros_like(U)
+        t0 = time.perf_counter()
+        for n in range(s):
+            kb, k0 = oracle.l1_weights(p.alpha, t, n)
+            oracle.lod_step_sf(p.dims, U, hist, n, kb, taus, p.Da, k0, cA, cB, cR, mc, iw, Tm, p.space_der, p.tol,
+                               p.max_iter, src, bc)
+        return time.perf_counter() - t0
+
+    def line_iteration_ops(self):
+        """FP64 operations (multiplies and adds, one each per lane) of one solver iteration on a line
+        of n intervals: three products vmul_T (bt 5(n-1), tridiagonal 5(n-1)+6, Toeplitz
+        (n-1)(n-2) one-sided or twice that two-sided, iw 2(n-1)), five dot products (2 (n+1)
+        each) and the vector updates (11 (n+1))."""
+        n = self.p.dims[0]
+        toe = (n - 1) * (n - 2) * (2 if self.p.space_der else 1)
+        mv = 5 * (n - 1) + 5 * (n - 1) + 6 + toe + 2 * (n - 1)
+        return 3 * mv + 10 * (n + 1) + 11 * (n + 1)
 
 
 class BatchWorkload:
@@ -665,6 +733,8 @@ def make_workload(args):
         return LineWorkload(args.workload, args)
     if args.workload == "config4":
         return LodWorkload(args)
+    if args.workload == "sf3d":
+        return SfWorkload(args)
     return BatchWorkload(args)
 
 
@@ -898,9 +968,12 @@ def run_ours(args):
     ctx.set_stream(stream.cuda_stream)
     lib = ctx.lib
     is_line = isinstance(wl, LineWorkload)
-    # default: the exact three-slice split path (every workload has it), with the FP64 arm beside it
-    prec = {"auto": fp.FPDE_PREC_SPLIT_BF16X3, "fp64": fp.FPDE_PREC_FP64, "bf16": fp.FPDE_PREC_SPLIT_BF16,
-            "f16": fp.FPDE_PREC_SPLIT_F16, "bf16x3": fp.FPDE_PREC_SPLIT_BF16X3}[args.precision]
+    is_sf = isinstance(wl, SfWorkload)
+    # default: the exact three-slice split path (every workload has it), with the FP64 arm beside it;
+    # the space-fractional workload defaults to FP64, the path that reproduces the reference bit for bit
+    prec = {"auto": fp.FPDE_PREC_FP64 if is_sf else fp.FPDE_PREC_SPLIT_BF16X3, "fp64": fp.FPDE_PREC_FP64,
+            "bf16": fp.FPDE_PREC_SPLIT_BF16, "f16": fp.FPDE_PREC_SPLIT_F16,
+            "bf16x3": fp.FPDE_PREC_SPLIT_BF16X3}[args.precision]
     if not is_line and prec not in (fp.FPDE_PREC_FP64, fp.FPDE_PREC_SPLIT_BF16X3):
         raise SystemExit(f"{wl.name} runs in FP64 or the exact three-slice split")
     pname = {0: "fp64", 1: "split-bf16", 2: "split-fp16", 3: "split-bf16x3"}[prec]
@@ -929,9 +1002,11 @@ def run_ours(args):
     barrier()
     torch.cuda.synchronize()
     launches0 = lib.fpde_kernel_launch_count()
+    it0 = obj.sf_iterations() if is_sf else 0
     ms = _timed(obj, u0_dev, steps, args.steps, stream)
     barrier()
     launches = lib.fpde_kernel_launch_count() - launches0
+    sf_iters = (obj.sf_iterations() - it0) / args.steps if is_sf else 0
     clk = clocks.stop()
     if world > 1:
         ms = max_over_ranks(ms, "cuda")
@@ -993,6 +1068,20 @@ def run_ours(args):
                                     "FP64 pipe and its per-step chain, not by HBM or the tensor cores")
         elif "hist_gemv" in kernels:
             out["roofline"] = dict(kernels["hist_gemv"])
+    elif is_sf:
+        # the line solves are FP64-pipe work: every multiply and add of vmul_T, the dot products and
+        # the updates is one FP64 operation per lane (no contracted FMAs: they would change the
+        # reference's roundings); achieved = operations of the iterations run / solve time
+        ops = sf_iters * wl.line_iteration_ops()
+        gops = ops / (ms / 1e3) / 1e9
+        lines = 3 * (wl.p.dims[0] - 1) ** 2 * steps
+        out["roofline"] = {"kernel": "k_lod_pass_sf (vmul_T + solve_mln<1>, one CTA per line)", "bound": "fp64",
+                           "achieved": gops, "peak": 625.0, "unit": "G FP64 ops/s", "frac": gops / 625.0,
+                           "peak_source": "nominal GB300 FP64 1.25 TFLOP/s counting an FMA as 2 (625 G lane-ops/s)",
+                           "traffic": None,
+                           "note": (f"{sf_iters:.0f} solver iterations per solve ({sf_iters / lines:.1f} per line "
+                                    f"solve) x {wl.line_iteration_ops()} FP64 ops per line-iteration; the "
+                                    "dot products' sequential sums (the reference's order) run on one lane")}
     else:
         # whole-step HBM roofline from the algorithmic history bytes of the run:
         #   FP64: 8 B x nodes x lags, summed over steps;

@@ -43,13 +43,21 @@ __device__ __forceinline__ SfVec sf_carve(double *sm, int m)
     return v;
 }
 
-// rv = vmul_T(xv) on the line's operands (:6662-6686). All threads; ends with a barrier.
-__device__ void sf_apply(const SfVec &s, int n, int sd, bool has_iw, bool has_rs, const double *xv, double *rv)
+// rv = vmul_T(xv) on the line's operands (:6662-6686). All threads; ends with a barrier. When side
+// is given, thread 0 (whose own output has no Toeplitz sum) also forms *side_out = the sequential
+// sum of the m products in side, overlapping it with the other threads' products.
+__device__ void sf_apply(const SfVec &s, int n, int sd, bool has_iw, bool has_rs, const double *xv, double *rv,
+                         const double *side = nullptr, double *side_out = nullptr)
 {
     const int T = blockDim.x, tid = threadIdx.x;
     for (int j = 1 + tid; j < n; j += T)
         s.bt[j] = da(da(dm(s.c0[j], xv[j - 1]), dm(s.c1[j], xv[j])), dm(s.c2[j], xv[j + 1]));
     __syncthreads();
+    if (side && tid == 0) {
+        double a = 0.0;
+        for (int i = 0; i <= n; ++i) a = da(a, side[i]);
+        *side_out = a;
+    }
     for (int i = tid; i <= n; i += T) {
         double r;
         if (i == 0) {
@@ -70,23 +78,30 @@ __device__ void sf_apply(const SfVec &s, int n, int sd, bool has_iw, bool has_rs
     __syncthreads();
 }
 
-// Sequential dot products in the reference's order (one thread).
-__device__ __forceinline__ double sf_dot(const double *a, const double *b, int m)
+// The reference's dot products (:860-1102) accumulate a[i]*b[i] from 0.0 in index order, each
+// product rounded. The products are formed by all threads into a scratch vector; one thread adds
+// them in order (sf_sum), or subtracts them in order for beta's "beta -= q*r" (sf_negsum): the
+// same roundings as the reference's loop.
+__device__ __forceinline__ double sf_sum(const double *p, int m)
 {
     double s = 0.0;
-    for (int i = 0; i < m; ++i) s = da(s, dm(a[i], b[i]));
+    for (int i = 0; i < m; ++i) s = da(s, p[i]);
     return s;
 }
-__device__ __forceinline__ double sf_negdot(const double *a, const double *b, int m)
+__device__ __forceinline__ double sf_negsum(const double *p, int m)
 {
     double s = 0.0;
-    for (int i = 0; i < m; ++i) s = ds(s, dm(a[i], b[i]));
+    for (int i = 0; i < m; ++i) s = ds(s, p[i]);
     return s;
 }
 
 // solve_mln<1> on the line in s (x: initial guess in, solution out). All threads; returns the
-// iteration count. A solve that restarts more than maxiter times without an iteration in between,
-// or runs past the time limit, stops and sets DEVERR_SOLVER.
+// iteration count. Scratch: bt (free outside sf_apply's first phase), u and g0 where the
+// iteration does not hold them. q.r of an iteration equals minus the previous iteration's beta
+// numerator (same r, and a sum subtracted from 0.0 in order is the negated sum added: rounding to
+// nearest is symmetric), so it is reused unless that numerator was zero (whose sign could differ).
+// A solve that restarts more than maxiter times without an iteration in between, or runs past the
+// time limit, stops and sets DEVERR_SOLVER.
 __device__ int sf_solve_cta(SfVec s, int n, int sd, bool has_iw, bool has_rs, double thr, int maxiter,
                             double *scal, unsigned *flags)
 {
@@ -94,31 +109,41 @@ __device__ int sf_solve_cta(SfVec s, int n, int sd, bool has_iw, bool has_rs, do
     const double md = (double)m;
     const unsigned long long t0 = gtimer_ns();
     int iter = 1, restarts = 0;
-    double c1, norm, al, ro1 = 0.0, beta;
+    double c1, norm, al, ro1 = 0.0, beta, qr_neg = 0.0;
+    bool have_qr = false;
 restart:
     if (++restarts > maxiter + 1) {
         if (tid == 0) atomicOr(flags, DEVERR_SOLVER);
         return iter;
     }
+    have_qr = false;
     sf_apply(s, n, sd, has_iw, has_rs, s.x, s.r);                            // :841-844
     for (int i = tid; i < m; i += T) {
         const double v = ds(s.B[i], s.r[i]);
         s.r[i] = v;
         s.g1[i] = v;
         s.q0[i] = v;
+        s.u[i] = dm(v, v);                                                   // r.r products (:864)
     }
     __syncthreads();
-    sf_apply(s, n, sd, has_iw, has_rs, s.g1, s.w1);                          // :851
-    if (tid == 0) scal[0] = sf_dot(s.q0, s.w1, m);
-    if (tid == 32 % T) scal[1] = sf_dot(s.r, s.r, m);
+    sf_apply(s, n, sd, has_iw, has_rs, s.g1, s.w1, s.u, &scal[1]);           // :851, norm on the side
+    for (int i = tid; i < m; i += T) s.bt[i] = dm(s.q0[i], s.w1[i]);         // c[1] = q0.w1 (:853-856)
+    __syncthreads();
+    if (tid == 0) scal[0] = sf_sum(s.bt, m);
     __syncthreads();
     c1 = scal[0];
     norm = scal[1];
     if (fabs(__ddiv_rn(norm, md)) < thr) return iter;
     for (;;) {
-        if (tid == 0) scal[2] = __ddiv_rn(sf_dot(s.q0, s.r, m), c1);          // :871-877
-        __syncthreads();
-        al = scal[2];
+        if (have_qr) {                                                         // :871-877
+            al = __ddiv_rn(-qr_neg, c1);
+        } else {
+            for (int i = tid; i < m; i += T) s.bt[i] = dm(s.q0[i], s.r[i]);
+            __syncthreads();
+            if (tid == 0) scal[2] = sf_sum(s.bt, m);
+            __syncthreads();
+            al = __ddiv_rn(scal[2], c1);
+        }
         if (!(c1 != 0.0)) goto restart;
         for (int i = tid; i < m; i += T) {
             s.u[i] = ds(s.r[i], dm(al, s.w1[i]));
@@ -126,8 +151,13 @@ restart:
         }
         __syncthreads();
         sf_apply(s, n, sd, has_iw, has_rs, s.u, s.Au);                       // :890
-        if (tid == 0) scal[3] = sf_dot(s.Au, s.Au, m);
-        if (tid == 32 % T) scal[4] = sf_dot(s.Au, s.u, m);
+        for (int i = tid; i < m; i += T) {
+            s.bt[i] = dm(s.Au[i], s.Au[i]);
+            s.g0[i] = dm(s.Au[i], s.u[i]);                                   // g0 is free until :1091
+        }
+        __syncthreads();
+        if (tid == 0) scal[3] = sf_sum(s.bt, m);
+        if (tid == 32 % T) scal[4] = sf_sum(s.g0, m);
         __syncthreads();
         norm = scal[3];
         ro1 = __ddiv_rn(-scal[4], norm);
@@ -135,27 +165,36 @@ restart:
         for (int i = tid; i < m; i += T) s.x[i] = ds(s.x[i], dm(ro1, s.u[i]));
         __syncthreads();
         sf_apply(s, n, sd, has_iw, has_rs, s.x, s.r);                        // :943-947
-        for (int i = tid; i < m; i += T) s.r[i] = ds(s.B[i], s.r[i]);
+        for (int i = tid; i < m; i += T) {
+            const double v = ds(s.B[i], s.r[i]);
+            s.r[i] = v;
+            s.bt[i] = dm(s.q0[i], v);                                        // beta's q.r (:1056-1059)
+            s.u[i] = dm(v, v);                                               // r.r for the check (:1127)
+        }
         __syncthreads();
-        if (tid == 0) {                                                        // :1056-1065
-            double b = __ddiv_rn(sf_negdot(s.q0, s.r, m), c1);
+        if (tid == 0) {                                                        // :1060-1065
+            const double nq = sf_negsum(s.bt, m);
+            double b = __ddiv_rn(nq, c1);
             if (c1 == 0.0) b = 0.0;
             scal[5] = b;
+            scal[2] = nq;
         }
         __syncthreads();
         beta = scal[5];
+        qr_neg = scal[2];
         const double bro = __ddiv_rn(beta, ro1);
         for (int i = tid; i < m; i += T) {
             const double zw = da(s.r[i], dm(beta, s.w1[i]));
             s.g0[i] = da(zw, dm(bro, s.g1[i]));
         }
         __syncthreads();
-        sf_apply(s, n, sd, has_iw, has_rs, s.g0, s.w0);                      // :1094
+        sf_apply(s, n, sd, has_iw, has_rs, s.g0, s.w0, s.u, &scal[7]);       // :1094, r.r on the side
+        for (int i = tid; i < m; i += T) s.bt[i] = dm(s.q0[i], s.w0[i]);     // c[0] (:1096-1099)
+        __syncthreads();
         if (tid == 0) {
-            scal[6] = sf_dot(s.q0, s.w0, m);
+            scal[6] = sf_sum(s.bt, m);
             scal[8] = gtimer_ns() - t0 > SF_TIME_LIMIT_NS ? 1.0 : 0.0;           // one decision for all
         }
-        if (tid == 32 % T) scal[7] = sf_dot(s.r, s.r, m);
         __syncthreads();
         c1 = scal[6];
         norm = scal[7];
@@ -165,6 +204,7 @@ restart:
             t = s.w0; s.w0 = s.w1; s.w1 = t;
         }
         restarts = 0;
+        have_qr = qr_neg != 0.0;
         if (fabs(__ddiv_rn(norm, md)) < thr) break;
         ++iter;
         if (iter == maxiter) break;
@@ -194,7 +234,7 @@ struct SfBatchArgs {
     unsigned *flags;
 };
 
-__global__ void __launch_bounds__(SF_THREADS) k_sf_batch(SfBatchArgs a, int solve)
+__global__ void __launch_bounds__(SF_THREADS, 6) k_sf_batch(SfBatchArgs a, int solve)
 {
     extern __shared__ __align__(16) double sf_sm[];
     __shared__ double scal[9];
@@ -229,7 +269,7 @@ __global__ void __launch_bounds__(SF_THREADS) k_sf_batch(SfBatchArgs a, int solv
 // the pass (line-major: per line A, B, Rlap, mc0, mc1, mc2, iw, each Nl+1 values), the state and
 // this step's source, history and line ends; solved in place and written back with the ghost copy
 // U[Nl+1] = U[Nl] (U1 :4792).
-__global__ void __launch_bounds__(SF_THREADS) k_lod_pass_sf(LodSfArgs a)
+__global__ void __launch_bounds__(SF_THREADS, 6) k_lod_pass_sf(LodSfArgs a)
 {
     extern __shared__ __align__(16) double sf_sm[];
     __shared__ double scal[9];

@@ -230,3 +230,74 @@ def config5(n_cols=512, steps=2048, tau=1e-3, n_min=256, n_max=16384, seed=6):
         u0[0] = u0[-1] = 0.0
         cols.append(LineProblem(f"col{c}", int(N), float(a), tau, steps, k, u0))
     return cols
+
+
+@dataclass
+class SfLodProblem(LodProblem):
+    """A 3D LOD problem with the implicit space-fractional line solves (the reference's impl 2,
+    toeplitz_mult_alg 0) of order gamma: per pass the line coefficients of A_/B/R with the
+    space-fractional local weight Dg kb(gamma) = h^(1-gamma) / Gamma(2-gamma) of a uniform axis
+    (:3095-3142), Mcoefs of Om1T (:4362-4376, equation 0: k / h^2 stencils), inv_dw_dh
+    iw = 1.5 + sin(z / 4) (the analytic problems' form, :2534-2545) and the Toeplitz rows of
+    fpde_sf_toeplitz_row; Dirichlet line ends (bc 0), a Gaussian source in the K pass."""
+    gamma: float = 0.7
+    space_der: int = 0
+    tol: float = 1e-9
+    max_iter: int = 5000
+
+    def iw(self):
+        z = np.arange(self.u0.shape[0])[:, None, None] / self.dims[2]
+        return np.broadcast_to(1.5 + np.sin(z / 4.0), self.u0.shape).copy()
+
+    def coefs(self):
+        shape = self.u0.shape
+        iw = self.iw()
+        cA, cB, cR = (np.zeros((3,) + shape) for _ in range(3))
+        for pss, axis in ((0, 2), (1, 1), (2, 0)):
+            hh = self.h[pss]
+            w = hh ** (1.0 - self.gamma) / math.gamma(2.0 - self.gamma)
+            km = np.roll(self.k, 1, axis=axis)
+            cA[pss] = w * km * iw / (hh * hh)
+            cB[pss] = w * self.k * iw / (hh * hh)
+            cR[pss] = w * iw * ((self.k / (hh * hh)) + (km / (hh * hh)))
+        return cA, cB, cR
+
+    def sf_operands(self):
+        """(Tm rows (3, max+2), mc (3 passes, 3, grid), iw (3, grid)) for fpde_lod3d_desc.space_frac."""
+        from .api import sf_toeplitz_row
+        shape = self.u0.shape
+        mc = np.zeros((3, 3) + shape)
+        iw = np.stack([self.iw()] * 3)
+        Tm = np.zeros((3, max(self.dims) + 2))
+        for pss, axis in ((0, 2), (1, 1), (2, 0)):
+            hh = self.h[pss]
+            km = np.roll(self.k, 1, axis=axis)
+            mc[pss, 0] = km / (hh * hh)
+            mc[pss, 1] = -((self.k / (hh * hh)) + (km / (hh * hh)))
+            mc[pss, 2] = self.k / (hh * hh)
+            nl = self.dims[pss]
+            Tm[pss, :nl + 1] = sf_toeplitz_row(self.gamma, np.arange(nl + 2) * hh, nl)
+        return Tm, mc, iw
+
+    def source(self):
+        z, y, x = np.meshgrid(*(np.arange(s) / (s - 2) for s in self.u0.shape), indexing="ij")
+        return 5.0 * np.exp(-((x - 0.4) ** 2 + (y - 0.5) ** 2 + (z - 0.5) ** 2) / (2 * 0.15 ** 2))
+
+
+def sf3d(n=64, steps=32, tau=1e-3, gamma=0.7, space_der=0):
+    """The space-fractional LOD workload: n^3, alpha 0.8, lognormal k (mu 0, sigma 0.4, ell 0.05,
+    seed 11), Gaussian blob initial state, Dirichlet 0 at every line end, space-fractional order
+    gamma (one-sided for space_der 0), the reference's default solver threshold (1e-9) and
+    iteration cap (5000)."""
+    shape = (n + 2, n + 2, n + 2)
+    k = lognormal_field_3d(shape, 0.0, 0.4, 0.05, 11, 1.0 / n)
+    z, y, x = np.meshgrid(*(np.arange(n + 2) / n for _ in range(3)), indexing="ij")
+    u0 = np.exp(-((x - 0.5) ** 2 + (y - 0.5) ** 2 + (z - 0.5) ** 2) / (2 * 0.12 ** 2))
+    for a in range(3):
+        idx = [slice(None)] * 3
+        idx[a] = 0
+        u0[tuple(idx)] = 0.0
+        idx[a] = slice(n, None)
+        u0[tuple(idx)] = 0.0
+    return SfLodProblem(f"sf3d_{n}^3", (n, n, n), 0.8, tau, steps, k, u0, (0, 0, 0), (0, 0, 0),
+                        gamma=gamma, space_der=space_der)
