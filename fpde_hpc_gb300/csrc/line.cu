@@ -2302,6 +2302,52 @@ extern "C" int fpde_line_autotune(fpde_ctx *ctx, const fpde_line_desc *desc, con
         dev_free(w);
         clear_error();
     }
+    if (d.precision == FPDE_PREC_SPLIT_BF16X3 && !d.richards && d.max_steps >= 512) {
+        // 4. depth of the far super-blocks (64-step blocks contracted together against the older
+        // history): a whole run of min(max_steps, 2048) steps per choice, replayed from its graph
+        const int ks = std::min(d.max_steps, 2048) / 256 * 256;
+        double bms = 1e300;
+        int bsup = 0;
+        for (int sup : {1, 2, 4}) {
+            fpde_line_tuning t = best;
+            t.far_super = sup;
+            fpde_line_desc td = d;
+            td.max_steps = ks;
+            td.tuning = &t;
+            fpde_line *L = nullptr;
+            if (fpde_line_create(ctx, &td, A, B, Rlap, u0, &L) != FPDE_OK) {
+                clear_error();
+                continue;
+            }
+            bool ok = fpde_line_run(L, ks) == FPDE_OK && fpde_line_reset(L, u0, 0) == FPDE_OK;
+            float ms = 0.f;
+            if (ok) {
+                cudaEvent_t e0, e1;
+                cudaEventCreate(&e0);
+                cudaEventCreate(&e1);
+                cudaEventRecord(e0, st);
+                ok = fpde_line_run(L, ks) == FPDE_OK;
+                cudaEventRecord(e1, st);
+                cudaEventSynchronize(e1);
+                cudaEventElapsedTime(&ms, e0, e1);
+                cudaEventDestroy(e0);
+                cudaEventDestroy(e1);
+            }
+            unsigned flags = 0;
+            cudaMemcpy(&flags, ctx->d_flags, sizeof flags, cudaMemcpyDeviceToHost);
+            if (flags) {
+                cudaMemset(ctx->d_flags, 0, sizeof(unsigned));
+                ok = false;
+            }
+            fpde_line_destroy(L);
+            clear_error();
+            if (ok && ms < bms) {
+                bms = ms;
+                bsup = sup;
+            }
+        }
+        if (bsup) best.far_super = bsup;
+    }
     *out = best;
     return ctx_check_flags(ctx, "autotune");
 }

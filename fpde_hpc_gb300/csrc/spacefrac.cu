@@ -43,9 +43,25 @@ __device__ __forceinline__ SfVec sf_carve(double *sm, int m)
     return v;
 }
 
-// rv = vmul_T(xv) on the line's operands (:6662-6686). All threads; ends with a barrier. When side
-// is given, thread 0 (whose own output has no Toeplitz sum) also forms *side_out = the sequential
-// sum of the m products in side, overlapping it with the other threads' products.
+// Row i (1..n-1) of vmul_T: the tridiagonal part, then the Toeplitz sum in the reference's order.
+__device__ __forceinline__ double sf_row(const SfVec &s, int n, int sd, bool has_iw, bool has_rs, const double *xv,
+                                         int i)
+{
+    const double r = da(da(dm(s.m0[i], xv[i - 1]), dm(s.m1[i], xv[i])), dm(s.m2[i], xv[i + 1]));
+    double v = 0.0;
+    for (int j = 1; j < i; ++j) v = da(v, dm(s.bt[j], s.Tm[i - j + 1]));
+    if (sd)
+        for (int j = i + 1; j < n; ++j) v = ds(v, dm(s.bt[j], s.Tm[j - i + 1]));
+    if (has_rs) v = __ddiv_rn(v, s.rs[i]);
+    return da(r, has_iw ? dm(v, s.iw[i]) : v);
+}
+
+// rv = vmul_T(xv) on the line's operands (:6662-6686). All threads; ends with a barrier.
+// Row i's one-sided sum has i-1 terms, so a thread takes the pair of rows k+1 and n-1-k: every
+// thread then runs n-2 terms and a warp issues no lanes idle on a shorter row. When side is given,
+// the CTA's last thread also forms *side_out = the sequential sum of the m products in side (one of
+// the reference's dot products), overlapping it with the rows; the second-to-last thread forms
+// the two boundary rows.
 __device__ void sf_apply(const SfVec &s, int n, int sd, bool has_iw, bool has_rs, const double *xv, double *rv,
                          const double *side = nullptr, double *side_out = nullptr)
 {
@@ -53,27 +69,20 @@ __device__ void sf_apply(const SfVec &s, int n, int sd, bool has_iw, bool has_rs
     for (int j = 1 + tid; j < n; j += T)
         s.bt[j] = da(da(dm(s.c0[j], xv[j - 1]), dm(s.c1[j], xv[j])), dm(s.c2[j], xv[j + 1]));
     __syncthreads();
-    if (side && tid == 0) {
+    if (side && tid == T - 1) {
         double a = 0.0;
         for (int i = 0; i <= n; ++i) a = da(a, side[i]);
         *side_out = a;
     }
-    for (int i = tid; i <= n; i += T) {
-        double r;
-        if (i == 0) {
-            r = da(dm(s.m1[0], xv[0]), dm(s.m2[0], xv[1]));
-        } else if (i == n) {
-            r = da(dm(s.m0[n], xv[n - 1]), dm(s.m1[n], xv[n]));
-        } else {
-            r = da(da(dm(s.m0[i], xv[i - 1]), dm(s.m1[i], xv[i])), dm(s.m2[i], xv[i + 1]));
-            double v = 0.0;
-            for (int j = 1; j < i; ++j) v = da(v, dm(s.bt[j], s.Tm[i - j + 1]));
-            if (sd)
-                for (int j = i + 1; j < n; ++j) v = ds(v, dm(s.bt[j], s.Tm[j - i + 1]));
-            if (has_rs) v = __ddiv_rn(v, s.rs[i]);
-            r = da(r, has_iw ? dm(v, s.iw[i]) : v);
-        }
-        rv[i] = r;
+    if (tid == T - 2) {
+        rv[0] = da(dm(s.m1[0], xv[0]), dm(s.m2[0], xv[1]));
+        rv[n] = da(dm(s.m0[n], xv[n - 1]), dm(s.m1[n], xv[n]));
+    }
+    const int pairs = n / 2;
+    for (int k = tid; k < pairs; k += T) {
+        const int a = k + 1, b = n - 1 - k;
+        rv[a] = sf_row(s, n, sd, has_iw, has_rs, xv, a);
+        if (b != a) rv[b] = sf_row(s, n, sd, has_iw, has_rs, xv, b);
     }
     __syncthreads();
 }
@@ -96,12 +105,16 @@ __device__ __forceinline__ double sf_negsum(const double *p, int m)
 }
 
 // solve_mln<1> on the line in s (x: initial guess in, solution out). All threads; returns the
-// iteration count. Scratch: bt (free outside sf_apply's first phase), u and g0 where the
-// iteration does not hold them. q.r of an iteration equals minus the previous iteration's beta
-// numerator (same r, and a sum subtracted from 0.0 in order is the negated sum added: rounding to
-// nearest is symmetric), so it is reused unless that numerator was zero (whose sign could differ).
-// A solve that restarts more than maxiter times without an iteration in between, or runs past the
-// time limit, stops and sets DEVERR_SOLVER.
+// iteration count. The scalars (dot products, divisions, the convergence test) are formed by
+// thread 0 and read by all after a barrier, so the FP64 pipe runs each once. Scratch: bt (free
+// outside sf_apply's first phase), u and g0 where the iteration does not hold them. q.r of an
+// iteration equals minus the previous iteration's beta numerator (same r, and a sum subtracted
+// from 0.0 in order is the negated sum added: rounding to nearest is symmetric), so it is reused
+// unless that numerator was zero (whose sign could differ). A solve that restarts more than
+// maxiter times without an iteration in between, or runs past the time limit, stops and sets
+// DEVERR_SOLVER.
+//   scal: 0 c1, 1 norm (r.r), 2 al, 3 ro1, 4 ro sum (Au.u), 5 beta, 6 beta/ro1, 7 norm at the
+//   iteration's end, 8 state (0 go on, 1 converged, 2 restart, 3 time limit), 9 q.r numerator
 __device__ int sf_solve_cta(SfVec s, int n, int sd, bool has_iw, bool has_rs, double thr, int maxiter,
                             double *scal, unsigned *flags)
 {
@@ -109,7 +122,6 @@ __device__ int sf_solve_cta(SfVec s, int n, int sd, bool has_iw, bool has_rs, do
     const double md = (double)m;
     const unsigned long long t0 = gtimer_ns();
     int iter = 1, restarts = 0;
-    double c1, norm, al, ro1 = 0.0, beta, qr_neg = 0.0;
     bool have_qr = false;
 restart:
     if (++restarts > maxiter + 1) {
@@ -129,25 +141,26 @@ restart:
     sf_apply(s, n, sd, has_iw, has_rs, s.g1, s.w1, s.u, &scal[1]);           // :851, norm on the side
     for (int i = tid; i < m; i += T) s.bt[i] = dm(s.q0[i], s.w1[i]);         // c[1] = q0.w1 (:853-856)
     __syncthreads();
-    if (tid == 0) scal[0] = sf_sum(s.bt, m);
+    if (tid == 0) {
+        scal[0] = sf_sum(s.bt, m);
+        scal[8] = fabs(__ddiv_rn(scal[1], md)) < thr ? 1.0 : 0.0;           // :866
+    }
     __syncthreads();
-    c1 = scal[0];
-    norm = scal[1];
-    if (fabs(__ddiv_rn(norm, md)) < thr) return iter;
+    if (scal[8] != 0.0) return iter;
     for (;;) {
-        if (have_qr) {                                                         // :871-877
-            al = __ddiv_rn(-qr_neg, c1);
-        } else {
+        if (!have_qr) {                                                        // :871-877
             for (int i = tid; i < m; i += T) s.bt[i] = dm(s.q0[i], s.r[i]);
             __syncthreads();
-            if (tid == 0) scal[2] = sf_sum(s.bt, m);
+            if (tid == 0) scal[2] = __ddiv_rn(sf_sum(s.bt, m), scal[0]);
             __syncthreads();
-            al = __ddiv_rn(scal[2], c1);
         }
-        if (!(c1 != 0.0)) goto restart;
-        for (int i = tid; i < m; i += T) {
-            s.u[i] = ds(s.r[i], dm(al, s.w1[i]));
-            s.x[i] = da(s.x[i], dm(al, s.g1[i]));
+        if (!(scal[0] != 0.0)) goto restart;                                   // c[1] (:878, :913)
+        {
+            const double al = scal[2];
+            for (int i = tid; i < m; i += T) {
+                s.u[i] = ds(s.r[i], dm(al, s.w1[i]));
+                s.x[i] = da(s.x[i], dm(al, s.g1[i]));
+            }
         }
         __syncthreads();
         sf_apply(s, n, sd, has_iw, has_rs, s.u, s.Au);                       // :890
@@ -156,13 +169,16 @@ restart:
             s.g0[i] = dm(s.Au[i], s.u[i]);                                   // g0 is free until :1091
         }
         __syncthreads();
-        if (tid == 0) scal[3] = sf_sum(s.bt, m);
+        if (tid == 0) scal[1] = sf_sum(s.bt, m);
         if (tid == 32 % T) scal[4] = sf_sum(s.g0, m);
         __syncthreads();
-        norm = scal[3];
-        ro1 = __ddiv_rn(-scal[4], norm);
-        if (norm == 0.0) goto restart;
-        for (int i = tid; i < m; i += T) s.x[i] = ds(s.x[i], dm(ro1, s.u[i]));
+        if (tid == 0) scal[3] = __ddiv_rn(-scal[4], scal[1]);                 // ro1 (:903)
+        __syncthreads();
+        if (scal[1] == 0.0) goto restart;                                      // :904-905
+        {
+            const double ro1 = scal[3];
+            for (int i = tid; i < m; i += T) s.x[i] = ds(s.x[i], dm(ro1, s.u[i]));
+        }
         __syncthreads();
         sf_apply(s, n, sd, has_iw, has_rs, s.x, s.r);                        // :943-947
         for (int i = tid; i < m; i += T) {
@@ -174,41 +190,45 @@ restart:
         __syncthreads();
         if (tid == 0) {                                                        // :1060-1065
             const double nq = sf_negsum(s.bt, m);
-            double b = __ddiv_rn(nq, c1);
-            if (c1 == 0.0) b = 0.0;
+            double b = __ddiv_rn(nq, scal[0]);
+            if (scal[0] == 0.0) b = 0.0;
             scal[5] = b;
-            scal[2] = nq;
+            scal[6] = __ddiv_rn(b, scal[3]);
+            scal[9] = nq;
         }
         __syncthreads();
-        beta = scal[5];
-        qr_neg = scal[2];
-        const double bro = __ddiv_rn(beta, ro1);
-        for (int i = tid; i < m; i += T) {
-            const double zw = da(s.r[i], dm(beta, s.w1[i]));
-            s.g0[i] = da(zw, dm(bro, s.g1[i]));
+        {
+            const double beta = scal[5], bro = scal[6];
+            for (int i = tid; i < m; i += T) {
+                const double zw = da(s.r[i], dm(beta, s.w1[i]));
+                s.g0[i] = da(zw, dm(bro, s.g1[i]));
+            }
         }
         __syncthreads();
         sf_apply(s, n, sd, has_iw, has_rs, s.g0, s.w0, s.u, &scal[7]);       // :1094, r.r on the side
         for (int i = tid; i < m; i += T) s.bt[i] = dm(s.q0[i], s.w0[i]);     // c[0] (:1096-1099)
         __syncthreads();
         if (tid == 0) {
-            scal[6] = sf_sum(s.bt, m);
-            scal[8] = gtimer_ns() - t0 > SF_TIME_LIMIT_NS ? 1.0 : 0.0;           // one decision for all
+            const double c0 = sf_sum(s.bt, m), nq = scal[9];
+            scal[0] = c0;                                                      // the shift :1104-1121
+            if (nq != 0.0) scal[2] = __ddiv_rn(-nq, c0);                       // next iteration's al
+            double st = 0.0;
+            if (fabs(__ddiv_rn(scal[7], md)) < thr) st = 1.0;                  // :1126-1132
+            else if (gtimer_ns() - t0 > SF_TIME_LIMIT_NS) st = 3.0;
+            scal[8] = st;
         }
         __syncthreads();
-        c1 = scal[6];
-        norm = scal[7];
-        const bool late = scal[8] != 0.0;
-        {                                                                      // :1104-1121
+        {
             double *t = s.g0; s.g0 = s.g1; s.g1 = t;
             t = s.w0; s.w0 = s.w1; s.w1 = t;
         }
         restarts = 0;
-        have_qr = qr_neg != 0.0;
-        if (fabs(__ddiv_rn(norm, md)) < thr) break;
+        have_qr = scal[9] != 0.0;
+        const double st = scal[8];
+        if (st == 1.0) break;
         ++iter;
         if (iter == maxiter) break;
-        if (late) {
+        if (st == 3.0) {
             if (tid == 0) atomicOr(flags, DEVERR_SOLVER);
             break;
         }
@@ -237,7 +257,7 @@ struct SfBatchArgs {
 __global__ void __launch_bounds__(SF_THREADS, 6) k_sf_batch(SfBatchArgs a, int solve)
 {
     extern __shared__ __align__(16) double sf_sm[];
-    __shared__ double scal[9];
+    __shared__ double scal[10];
     const int m = a.n + 1, line = blockIdx.x;
     const int64_t o = (int64_t)line * m, plane = (int64_t)a.lines * m;
     SfVec s = sf_carve(sf_sm, m);
@@ -272,7 +292,7 @@ __global__ void __launch_bounds__(SF_THREADS, 6) k_sf_batch(SfBatchArgs a, int s
 __global__ void __launch_bounds__(SF_THREADS, 6) k_lod_pass_sf(LodSfArgs a)
 {
     extern __shared__ __align__(16) double sf_sm[];
-    __shared__ double scal[9];
+    __shared__ double scal[10];
     const int n = a.Nl, m = n + 1, line = blockIdx.x, tid = threadIdx.x, T = blockDim.x;
     const int la = line % a.n1, lb = line / a.n1;
     const int64_t base = (int64_t)(1 + la) * a.s1 + (int64_t)(1 + lb) * a.s2;

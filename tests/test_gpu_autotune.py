@@ -21,7 +21,8 @@ def ctx():
 
 
 @pytest.mark.parametrize("N,steps,prec,tol", [(1000, 160, 0, 1e-12), (20000, 160, 0, 1e-9),
-                                              (20000, 200, 3, 1e-9), (65536, 192, 3, 3e-9)])
+                                              (20000, 200, 3, 1e-9), (65536, 192, 3, 3e-9),
+                                              (16384, 768, 3, 3e-9)])
 def test_autotuned_line_matches_default(ctx, N, steps, prec, tol):
     import fpde_hpc_gb300 as fp
     from fpde_hpc_gb300 import problems
@@ -29,9 +30,11 @@ def test_autotuned_line_matches_default(ctx, N, steps, prec, tol):
     A, B, R = p.coefs()
     t = fp.autotune_line(ctx, p.N, p.alpha, p.tau, p.Da, A, B, R, p.u0, steps, precision=prec)
     print(f"N={N} prec={prec}: solve_sp={t.solve_sp} chunks={t.chunks} far_splits={t.far_splits} "
-          f"gemv_splits={t.gemv_splits} ms/step={t.ms_per_step:.4f}")
+          f"gemv_splits={t.gemv_splits} far_super={t.far_super} ms/step={t.ms_per_step:.4f}")
     assert t.solve_sp in (1, 2, 4, 8) and 1 <= t.chunks <= ctx.sm_count and t.ms_per_step > 0
     assert 0 <= t.far_splits <= 4 and 0 <= t.gemv_splits <= 64
+    if prec == 3 and steps >= 512:                  # the super-block depth is timed, not left at 0
+        assert t.far_super in (1, 2, 4)
     out = []
     for tuning in (None, t):
         line = fp.Line(ctx, p.N, p.alpha, p.tau, p.Da, A, B, R, p.u0, steps, precision=prec, tuning=tuning)
