@@ -53,7 +53,8 @@ class Lod3dDesc(C.Structure):
 class ColumnDesc(C.Structure):
     _fields_ = [("N", c_i64), ("alpha", c_dbl), ("tau", c_dbl), ("Da", c_dbl), ("left_kind", c_int),
                 ("left_value", c_dbl), ("right_kind", c_int), ("right_value", c_dbl), ("dLN", c_dbl),
-                ("A", c_vp), ("B", c_vp), ("Rlap", c_vp), ("u0", c_vp), ("lag_weights", c_vp)]
+                ("A", c_vp), ("B", c_vp), ("Rlap", c_vp), ("u0", c_vp), ("lag_weights", c_vp),
+                ("restrict_eps", c_dbl)]
 
 
 # name -> (restype, argtypes)

@@ -508,7 +508,8 @@ class Lod3D:
 
 class Batch:
     """An ensemble of independent 1D Caputo columns (fpde_batch_*). columns: list of dicts with
-    N, alpha, tau, Da, A, B, Rlap, u0 and optional left/right (kind, value), dLN, lag_weights."""
+    N, alpha, tau, Da, A, B, Rlap, u0 and optional left/right (kind, value), dLN, lag_weights,
+    restrict_eps (restricted summing per column)."""
 
     def __init__(self, ctx, columns, max_steps, precision=FP64):
         self.ctx = ctx
@@ -521,6 +522,7 @@ class Batch:
             d.N, d.alpha, d.tau, d.Da = c["N"], c.get("alpha", 0.5), c["tau"], c.get("Da", 1.0)
             d.left_kind, d.left_value, d.right_kind, d.right_value = left[0], left[1], right[0], right[1]
             d.dLN = c.get("dLN", 0.0)
+            d.restrict_eps = float(c.get("restrict_eps", 0.0))
             d.A, d.B, d.Rlap, d.u0 = (a.ctypes.data for a in arrs)
             if c.get("lag_weights") is not None:
                 w = np.ascontiguousarray(c["lag_weights"], dtype=np.float64)

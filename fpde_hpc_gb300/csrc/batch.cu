@@ -47,18 +47,21 @@ struct ColInfo {
     int pad;
 };
 
+// col_lag (may be null): the lags each column keeps under restricted summing; rows older than
+// n - col_lag[c] carry zero weights and are skipped (adding a zero-weight term changes nothing).
 __global__ void __launch_bounds__(256) k_batch_partial(const double2 *__restrict__ D, int64_t P2, int n,
                                                        const double *__restrict__ wall, int64_t wstride,
                                                        int64_t woff, const int *__restrict__ cta_col,
-                                                       double2 *__restrict__ part)
+                                                       const int *__restrict__ col_lag, double2 *__restrict__ part)
 {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const int ks = blockIdx.y, KS = gridDim.y;
     const int t0 = (int)((int64_t)n * ks / KS), t1 = (int)((int64_t)n * (ks + 1) / KS);
     if (i >= P2) return;
-    const double *wt = wall + (int64_t)cta_col[blockIdx.x] * wstride + woff;   // wt[t] = w_c[n - t]
+    const int c = cta_col[blockIdx.x];
+    const double *wt = wall + (int64_t)c * wstride + woff;                       // wt[t] = w_c[n - t]
     double ax = 0.0, ay = 0.0;
-    int t = t0;
+    int t = col_lag ? max(t0, n - col_lag[c]) : t0;
     for (; t + 8 <= t1; t += 8) {
         double2 v[8];
 #pragma unroll
@@ -257,6 +260,7 @@ struct fpde_batch {
     double *U = nullptr, *U0 = nullptr, *Y = nullptr, *D = nullptr, *part = nullptr, *wall = nullptr;
     ColInfo *cols = nullptr;
     int *order = nullptr, *cta_col = nullptr;
+    int *col_lag = nullptr;                   // restricted summing: lags kept per column (null: all)
     unsigned *queue = nullptr;                // per step: next work item of the solve
     int solve_grid = 0;
     // split path
@@ -291,7 +295,7 @@ static int batch_enqueue(fpde_batch *b, cudaStream_t st, int64_t n0, int steps, 
                 dim3 grid((unsigned)(b->Ptot / 512), (unsigned)KS);
                 k_batch_partial<<<grid, 256, 0, st>>>((const double2 *)b->D, b->Ptot / 2, (int)n, b->wall,
                                                       b->max_steps + 1, b->max_steps - n, b->cta_col,
-                                                      (double2 *)b->part);
+                                                      b->col_lag, (double2 *)b->part);
                 FPDE_LAUNCHED(1);
                 ++k;
             }
@@ -364,6 +368,7 @@ int fpde_batch_destroy(fpde_batch *b)
     dev_free(b->cols);
     dev_free(b->order);
     dev_free(b->cta_col);
+    dev_free(b->col_lag);
     delete b;
     return FPDE_OK;
 }
@@ -387,7 +392,27 @@ int fpde_batch_create(fpde_ctx *ctx, const fpde_column_desc *cols, int n_cols, i
         FPDE_CHECK_ARG(d.tau > 0.0, "tau must be positive");
         FPDE_CHECK_ARG((d.left_kind == 0 || d.left_kind == 1) && (d.right_kind == 0 || d.right_kind == 1),
                        "bad boundary kind");
+        FPDE_CHECK_ARG(std::isfinite(d.restrict_eps) && d.restrict_eps >= 0.0, "restrict_eps must be >= 0");
     }
+    // restricted summing per column (time_summing :4117-4131, newest first): the lags before the
+    // first one whose kb = w tau / Da falls below restrict_eps; later lags get weight 0
+    std::vector<int> lag_keep(n_cols, max_steps);
+    bool any_restrict = false;
+    for (int c = 0; c < n_cols; ++c) {
+        const fpde_column_desc &d = cols[c];
+        if (d.restrict_eps <= 0.0) continue;
+        const double kkk0 = d.lag_weights ? 0.0 : l1_interval_weight(d.alpha, 0.0, d.tau);
+        std::vector<double> kbl(max_steps);
+        for (int64_t j = 1; j <= max_steps; ++j) {
+            const double w = d.lag_weights ? d.lag_weights[j] : d.Da * (kkk0 * l1_lag(d.alpha, j)) / d.tau;
+            kbl[j - 1] = w * d.tau / d.Da;
+        }
+        int keep = max_steps;
+        fpde_restricted_lags(kbl.data(), max_steps, d.restrict_eps, &keep);
+        lag_keep[c] = keep;
+        any_restrict = any_restrict || keep < max_steps;
+    }
+    clear_error();
     fpde_batch *b = new fpde_batch();
     b->ctx = ctx;
     b->n_cols = n_cols;
@@ -459,7 +484,8 @@ int fpde_batch_create(fpde_ctx *ctx, const fpde_column_desc *cols, int n_cols, i
         double *w = hw.data() + (size_t)c * (max_steps + 1);          // w[m] = w_c[max_steps - m]
         for (int64_t m = 0; m < max_steps; ++m) {
             const int64_t j = max_steps - m;
-            w[m] = d.lag_weights ? d.lag_weights[j] : d.Da * (kkk0 * l1_lag(d.alpha, j)) / d.tau;
+            w[m] = j > lag_keep[c] ? 0.0
+                                   : d.lag_weights ? d.lag_weights[j] : d.Da * (kkk0 * l1_lag(d.alpha, j)) / d.tau;
         }
         for (int64_t q = o / 512; q < (o + (N + 1 + 511) / 512 * 512) / 512; ++q) cta_col[q] = c;
     }
@@ -475,8 +501,9 @@ int fpde_batch_create(fpde_ctx *ctx, const fpde_column_desc *cols, int n_cols, i
             const fpde_column_desc &d = cols[c];
             const double kkk0 = d.lag_weights ? 0.0 : l1_interval_weight(d.alpha, 0.0, d.tau);
             for (int64_t j = 1; j < b->LW; ++j)
-                hwl[(size_t)c * b->LW + j] = d.lag_weights ? (j <= max_steps ? d.lag_weights[j] : 0.0)
-                                                           : d.Da * (kkk0 * l1_lag(d.alpha, j)) / d.tau;
+                hwl[(size_t)c * b->LW + j] = j > lag_keep[c] ? 0.0
+                                             : d.lag_weights ? (j <= max_steps ? d.lag_weights[j] : 0.0)
+                                                             : d.Da * (kkk0 * l1_lag(d.alpha, j)) / d.tau;
             const int64_t o = b->off[c], Pc = (cols[c].N + 1 + 511) / 512 * 512;
             for (int64_t q = o / 128; q < (o + Pc) / 128; ++q) hwcol[q] = c;
         }
@@ -493,6 +520,7 @@ int fpde_batch_create(fpde_ctx *ctx, const fpde_column_desc *cols, int n_cols, i
                 dev_alloc((void **)&b->cols, hc.size() * sizeof(ColInfo)) ||
                 dev_alloc((void **)&b->order, order.size() * sizeof(int)) ||
                 dev_alloc((void **)&b->cta_col, cta_col.size() * sizeof(int)) ||
+                (any_restrict && dev_alloc((void **)&b->col_lag, (size_t)n_cols * sizeof(int))) ||
                 dev_alloc((void **)&b->queue, (size_t)max_steps * sizeof(unsigned));
     if (!fail && !split) {
         fail = dev_alloc((void **)&b->D, (size_t)max_steps * tb) || dev_alloc((void **)&b->part, (size_t)KS_MAX * tb) ||
@@ -569,6 +597,7 @@ int fpde_batch_create(fpde_ctx *ctx, const fpde_column_desc *cols, int n_cols, i
     cudaMemcpyAsync(b->cols, hc.data(), hc.size() * sizeof(ColInfo), cudaMemcpyHostToDevice, st);
     cudaMemcpyAsync(b->order, order.data(), order.size() * sizeof(int), cudaMemcpyHostToDevice, st);
     cudaMemcpyAsync(b->cta_col, cta_col.data(), cta_col.size() * sizeof(int), cudaMemcpyHostToDevice, st);
+    if (b->col_lag) cudaMemcpyAsync(b->col_lag, lag_keep.data(), (size_t)n_cols * sizeof(int), cudaMemcpyHostToDevice, st);
     cudaError_t e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) {
         fpde_batch_destroy(b);

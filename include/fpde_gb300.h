@@ -524,6 +524,9 @@ typedef struct fpde_column_desc {
     double dLN;
     const double *A, *B, *Rlap, *u0;   /* N+1 values each (as for fpde_line_create) */
     const double *lag_weights;         /* optional, max_steps+1 values (fpde_line_desc) */
+    double restrict_eps;               /* restricted summing of this column (the reference's sum_alg 1,
+                                          time_summing :4117-4131, as fpde_line_desc.restrict_eps);
+                                          0 keeps every lag */
 } fpde_column_desc;
 
 /* An ensemble of columns of any lengths and orders advanced together: per step one history

@@ -118,3 +118,35 @@ def test_batch_split_history_vs_fp64(ctx, steps, tol):
     worst = max(relmax(x, y) for x, y in zip(res[1], res[0]))
     print(f"ensemble of {len(cols)} columns, {steps} steps, split x3 vs FP64: max rel {worst:.2e}")
     assert worst <= tol
+
+
+@pytest.mark.parametrize("precision,tol", [(0, 1e-12), (3, 1e-7)])
+def test_batch_restricted_summing_vs_oracle(ctx, precision, tol):
+    """Restricted summing per column (restrict_eps, the reference's sum_alg 1): columns with
+    windows of 0, 5, 63, 64 and 100 lags and one untruncated share the ensemble; each equals the
+    oracle's general line run with its lag weights from the window on set to zero."""
+    import fpde_hpc_gb300 as fp
+    from fpde_hpc_gb300 import problems
+    steps = 200
+    cols, refs = [], []
+    for j, (N, max_lag) in enumerate([(300, 0), (1000, 5), (2049, 63), (700, 64), (4096, 100), (513, 1000)]):
+        p = problems.config2(N=N, steps=steps)
+        p.alpha = 0.6 + 0.05 * j
+        A, B, R = p.coefs()
+        b = fp.weights_l1_lags(p.alpha, steps + 2)
+        kkk0 = p.tau ** (1 - p.alpha) / (1 - p.alpha)
+        kb = kkk0 * b
+        eps = 0.5 * (kb[max_lag] + kb[max_lag + 1]) if max_lag < steps else 0.5 * kb[steps + 1]
+        c = dict(N=p.N, alpha=p.alpha, tau=p.tau, Da=p.Da, A=A, B=B, Rlap=R, u0=p.u0, restrict_eps=eps)
+        cols.append(c)
+        w = np.zeros(steps + 1)
+        keep = min(max_lag, steps)
+        w[:keep + 1] = p.Da * kb[:keep + 1] / p.tau
+        refs.append(oracle.line_run_general(p.u0, steps, w, 0.0, A, B, R)[0])
+    bt = fp.Batch(ctx, cols, steps, precision=precision)
+    bt.run(steps)
+    for i, uref in enumerate(refs):
+        err = relmax(bt.state(i), uref)
+        print(f"precision {precision}, column {i}: {err:.2e}")
+        assert err <= tol, (i, err)
+    bt.close()
