@@ -2304,8 +2304,9 @@ extern "C" int fpde_line_autotune(fpde_ctx *ctx, const fpde_line_desc *desc, con
     }
     if (d.precision == FPDE_PREC_SPLIT_BF16X3 && !d.richards && d.max_steps >= 512) {
         // 4. depth of the far super-blocks (64-step blocks contracted together against the older
-        // history): a whole run of min(max_steps, 2048) steps per choice, replayed from its graph
-        const int ks = std::min(d.max_steps, 2048) / 256 * 256;
+        // history, whose benefit grows with the history): a whole run of min(max_steps, 4096) steps
+        // per choice, replayed from its graph
+        const int ks = std::min(d.max_steps, 4096) / 256 * 256;
         double bms = 1e300;
         int bsup = 0;
         for (int sup : {1, 2, 4}) {

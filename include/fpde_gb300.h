@@ -395,7 +395,7 @@ int fpde_line_probe_stats(fpde_line *line, int kind, double *ms, double *bytes, 
  * sum at a history of min(max_steps, 2048) steps, and return the fastest in *out (pass it as
  * desc->tuning to fpde_line_create). Candidates: solve_sp x chunks (solve time per step of the
  * second 64-step block), far_splits 1..4, gemv_splits {k/2, k, 2k} around the built-in rule k,
- * and on the three-slice path far_super 1, 2, 4 (a whole run of min(max_steps, 2048) steps each).
+ * and on the three-slice path far_super 1, 2, 4 (a whole run of min(max_steps, 4096) steps each).
  * Allocates and frees temporary device buffers; takes a fraction of a second to seconds. */
 int fpde_line_autotune(fpde_ctx *ctx, const fpde_line_desc *desc, const double *A, const double *B,
                        const double *Rlap, const double *u0, fpde_line_tuning *out);
