@@ -35,7 +35,8 @@
 
 namespace fpde {
 
-constexpr int BT = 256;       // threads per column CTA
+constexpr int BT = 512;       // threads per column CTA (halves the sequential segment of the longest columns,
+                              // which set the step time of a skewed ensemble)
 constexpr int BW = BT / 32;
 
 struct ColInfo {
@@ -271,6 +272,7 @@ struct fpde_batch {
     float *pW = nullptr;
     double *ring = nullptr, *cfar = nullptr, *wlag = nullptr, *Sn = nullptr;
     float2 *ringf = nullptr, *wff = nullptr;  // the ring and every column's lag weights as float pairs
+    float2 *pre = nullptr;                    // near-history sums of the current 8-step sub-block
     int *wcol = nullptr;
     FarPlan3 plan3;
     int64_t n_done = 0;
@@ -320,8 +322,17 @@ static int batch_enqueue(fpde_batch *b, cudaStream_t st, int64_t n0, int steps, 
                 }
             }
             if (n >= 1) {
+                // rows older than the step's 8-step sub-block (and the far partials) once per sub-block
+                const int j0 = j - j % NEAR_SUB;
+                const bool use_pre = splits > 0 || j0 > 0;
+                if (use_pre && j == j0) {
+                    if ((rc = launch_near_pre_ff(st, b->ringf, b->Ptot, j0, b->wff, b->cfar, splits, 1, b->pre,
+                                                 b->cta_col, b->LW)))
+                        return rc;
+                    ++k;
+                }
                 if ((rc = launch_near_history_ff(st, b->ringf, b->Ptot, j, b->wff, b->cfar, splits, 1, b->Sn, b->cta_col,
-                                              b->LW)))
+                                                 b->LW, use_pre ? b->pre : nullptr, j0)))
                     return rc;
                 ++k;
                 KS = 1;
@@ -362,6 +373,7 @@ int fpde_batch_destroy(fpde_batch *b)
     dev_free(b->pA);
     dev_free(b->pW);
     dev_free(b->ringf);
+    dev_free(b->pre);
     dev_free(b->wff);
     dev_free(b->wcol);
     dev_free(b->queue);
@@ -537,6 +549,7 @@ int fpde_batch_create(fpde_ctx *ctx, const fpde_column_desc *cols, int n_cols, i
                dev_alloc((void **)&b->cfar, (size_t)FAR_MAX_SPLITS * 64 * tb) ||
                dev_alloc((void **)&b->wlag, hwl.size() * sizeof(double)) || dev_alloc((void **)&b->Sn, tb) ||
                dev_alloc((void **)&b->ringf, (size_t)64 * tot * sizeof(float2)) ||
+               dev_alloc((void **)&b->pre, (size_t)NEAR_SUB * tot * sizeof(float2)) ||
                dev_alloc((void **)&b->wff, hwl.size() * sizeof(float2)) ||
                dev_alloc((void **)&b->wcol, hwcol.size() * sizeof(int));
         if (!fail) {

@@ -69,7 +69,12 @@ int launch_block_prep3(cudaStream_t st, const SplitPrep3 &p, int64_t n0, bool we
 // column); one FP64 add per node.
 int launch_near_history_ff(cudaStream_t st, const float2 *ringf, int64_t P, int j, const float2 *wff,
                            const double *cfar, int KS, int pairs, double *S, const int *cta_col = nullptr,
-                           int64_t wstride = 0);
+                           int64_t wstride = 0, const float2 *pre = nullptr, int r0 = 0);
+// Sub-blocks of the near history: the partial sums of NEAR_SUB steps from the rows before j0
+// (pre: NEAR_SUB rows of P float pairs).
+constexpr int NEAR_SUB = 8;
+int launch_near_pre_ff(cudaStream_t st, const float2 *ringf, int64_t P, int j0, const float2 *wff, const double *cfar,
+                       int KS, int pairs, float2 *pre, const int *cta_col = nullptr, int64_t wstride = 0);
 
 }  // namespace fpde
 

@@ -211,8 +211,8 @@ __global__ void __launch_bounds__(128) k_lod_pass_rich(LodPassArgs p, LodRichArg
     p.U[base] = __dadd_rn(__dmul_rn(al1, u), g0);                       // Al[1] U[1] + Bt[1]
 }
 
-// Segmented pass: LSEGS threads (adjacent lanes) per line, each sweeping one segment of up to
-// LSEGLEN nodes from zero carries, the segments joined by affine scans over the group's lanes.
+// Segmented pass: SEGS threads (adjacent lanes) per line, each sweeping one segment of up to
+// SEGLEN nodes from zero carries, the segments joined by affine scans over the group's lanes.
 // One thread per line left only ~3 warps per SM for a chain of dependent FP64 operations; four
 // per line give the FP64 pipe four times the independent work. With the segment's prefix
 // product of a = g A (its end value PF), the backward sweep's responses KF (to that prefix
@@ -220,18 +220,30 @@ __global__ void __launch_bounds__(128) k_lod_pass_rich(LodPassArgs p, LodRichArg
 //   y = y0 + c_in CF,  u = ub0 + c_in KF + c_out CB,
 // where y0, ub0 are the zero-carry sweeps, c_in the true y before the segment and c_out the
 // true u after it.
-constexpr int LSEGS = 4, LSEGLEN = 32;
+// (segments per line, nodes per segment) by line length: 8 x 16 up to 129 intervals, 16 x 16 up to
+// 257, 16 x 32 up to 513; longer lines run one thread per line. More, shorter segments keep more
+// lines' loads in flight (the pass is bound by memory latency, not bandwidth).
+constexpr int LSEG_MAXSEGS = 16;
+static inline void seg_shape(int Nl, int *segs, int *seglen)
+{
+    const int interior = Nl - 1;
+    if (interior <= 8 * 16) { *segs = 8; *seglen = 16; }
+    else if (interior <= 16 * 16) { *segs = 16; *seglen = 16; }
+    else if (interior <= 16 * 32) { *segs = 16; *seglen = 32; }
+    else { *segs = 0; *seglen = 0; }
+}
 constexpr int LSB = 4;                    // nodes of loads issued together (register budget: one wave)
 struct LodSegArgs {
     const double *KF, *CB;           // (Nl+1) x lines, pass-line-major
-    const double *PF;                // [lines][LSEGS]: product of a = g A over each segment
-    int seglen;                      // nodes per segment (<= LSEGLEN)
+    const double *PF;                // [lines][segs]: product of a = g A over each segment
+    int seglen;                      // nodes per segment (<= the kernel's SEGLEN)
 };
 
-__global__ void __launch_bounds__(128, 4) k_lod_pass_seg(LodPassArgs p, LodSegArgs sg)
+template <int SEGS, int SEGLEN>
+__global__ void __launch_bounds__(128, SEGLEN <= 16 ? 5 : 4) k_lod_pass_seg(LodPassArgs p, LodSegArgs sg)
 {
     const int gt = blockIdx.x * blockDim.x + threadIdx.x;
-    const int line = gt / LSEGS, sgi = gt % LSEGS;
+    const int line = gt / SEGS, sgi = gt % SEGS;
     const bool live = line < p.lines;
     const int ln = live ? line : 0;
     const int a = ln % p.n1, b = ln / p.n1;
@@ -241,10 +253,10 @@ __global__ void __launch_bounds__(128, 4) k_lod_pass_seg(LodPassArgs p, LodSegAr
     const double g0 = p.bc ? p.bc[base] : 0.0;
     const double uold_last = p.U[base + (int64_t)(Nl - 1) * p.st];       // read before any write
     // forward from a zero carry: y0_q = g_q (A_q y0_{q-1} - Om_q)
-    double yv[LSEGLEN];
+    double yv[SEGLEN];
     double y = 0.0;
 #pragma unroll
-    for (int t0 = 0; t0 < LSEGLEN; t0 += LSB) {
+    for (int t0 = 0; t0 < SEGLEN; t0 += LSB) {
         double uu[LSB], aa[LSB], gg[LSB], rr[LSB], ss[LSB];
 #pragma unroll
         for (int t = 0; t < LSB; ++t) {
@@ -270,17 +282,17 @@ __global__ void __launch_bounds__(128, 4) k_lod_pass_seg(LodPassArgs p, LodSegAr
         }
     }
     // forward carries: compose (PF, y0_end) over segments 0..sgi; c_in of this segment
-    double Pc = (live && q1 > q0) ? __ldg(sg.PF + (int64_t)line * LSEGS + sgi) : 1.0;
+    double Pc = (live && q1 > q0) ? __ldg(sg.PF + (int64_t)line * SEGS + sgi) : 1.0;
     double Yc = (q1 > q0) ? y : 0.0;
 #pragma unroll
-    for (int d = 1; d < LSEGS; d <<= 1) {
-        const double Pp = __shfl_up_sync(0xffffffffu, Pc, d, LSEGS), Yp = __shfl_up_sync(0xffffffffu, Yc, d, LSEGS);
+    for (int d = 1; d < SEGS; d <<= 1) {
+        const double Pp = __shfl_up_sync(0xffffffffu, Pc, d, SEGS), Yp = __shfl_up_sync(0xffffffffu, Yc, d, SEGS);
         if (sgi >= d) { Yc = fma(Pc, Yp, Yc); Pc *= Pp; }
     }
     const double yend = fma(Pc, g0, Yc);                 // true y at this segment's end
-    double cin = __shfl_up_sync(0xffffffffu, yend, 1, LSEGS);
+    double cin = __shfl_up_sync(0xffffffffu, yend, 1, SEGS);
     if (sgi == 0) cin = g0;
-    const double ylast = __shfl_sync(0xffffffffu, yend, LSEGS - 1, LSEGS);   // y_{Nl-1}
+    const double ylast = __shfl_sync(0xffffffffu, yend, SEGS - 1, SEGS);   // y_{Nl-1}
     // right end: Dirichlet value or the flux closure of U1 (:4687-4719) with the old U[Nl-1]
     const double gN = p.bc ? p.bc[base + (int64_t)Nl * p.st] : 0.0;
     double uN;
@@ -294,7 +306,7 @@ __global__ void __launch_bounds__(128, 4) k_lod_pass_seg(LodPassArgs p, LodSegAr
     // backward from a zero carry over y0: ub0_q = al_q ub0_{q+1} + y0_q
     double u = 0.0;
 #pragma unroll
-    for (int t0 = LSEGLEN - LSB; t0 >= 0; t0 -= LSB) {
+    for (int t0 = SEGLEN - LSB; t0 >= 0; t0 -= LSB) {
         double al[LSB];
 #pragma unroll
         for (int t = LSB - 1; t >= 0; --t) {
@@ -312,17 +324,17 @@ __global__ void __launch_bounds__(128, 4) k_lod_pass_seg(LodPassArgs p, LodSegAr
     double Qc = (live && q1 > q0) ? __ldg(sg.CB + (int64_t)q0 * L + line) : 1.0;
     double Uc = (q1 > q0) ? fma(cin, kf0, u) : 0.0;
 #pragma unroll
-    for (int d = 1; d < LSEGS; d <<= 1) {
-        const double Qn = __shfl_down_sync(0xffffffffu, Qc, d, LSEGS), Un = __shfl_down_sync(0xffffffffu, Uc, d, LSEGS);
-        if (sgi + d < LSEGS) { Uc = fma(Qc, Un, Uc); Qc *= Qn; }
+    for (int d = 1; d < SEGS; d <<= 1) {
+        const double Qn = __shfl_down_sync(0xffffffffu, Qc, d, SEGS), Un = __shfl_down_sync(0xffffffffu, Uc, d, SEGS);
+        if (sgi + d < SEGS) { Uc = fma(Qc, Un, Uc); Qc *= Qn; }
     }
     const double ustart = fma(Qc, uN, Uc);               // true u at this segment's start
-    double cout = __shfl_down_sync(0xffffffffu, ustart, 1, LSEGS);
-    if (sgi == LSEGS - 1) cout = uN;
-    const double u1 = __shfl_sync(0xffffffffu, ustart, 0, LSEGS);        // U[1]
+    double cout = __shfl_down_sync(0xffffffffu, ustart, 1, SEGS);
+    if (sgi == SEGS - 1) cout = uN;
+    const double u1 = __shfl_sync(0xffffffffu, ustart, 0, SEGS);        // U[1]
     if (!live) return;
 #pragma unroll
-    for (int t0 = 0; t0 < LSEGLEN; t0 += LSB) {
+    for (int t0 = 0; t0 < SEGLEN; t0 += LSB) {
         double kf[LSB], cb[LSB];
 #pragma unroll
         for (int t = 0; t < LSB; ++t) {
@@ -336,24 +348,78 @@ __global__ void __launch_bounds__(128, 4) k_lod_pass_seg(LodPassArgs p, LodSegAr
             if (q < q1) p.U[base + (int64_t)q * p.st] = fma(cout, cb[t], fma(cin, kf[t], yv[t0 + t]));
         }
     }
-    if (sgi == LSEGS - 1) {
+    if (sgi == SEGS - 1) {
         p.U[base + (int64_t)Nl * p.st] = uN;
         p.U[base + (int64_t)(Nl + 1) * p.st] = uN;                  // ghost copy (U1 :4792)
     }
     if (sgi == 0) p.U[base] = fma(__ldg(p.al + line), u1, g0);    // Al[1] U[1] + Bt[1]
 }
 
-// Two nodes per thread: S = far partials of step j + sum_{r<j} w[j-r] ring[r] in float-float.
+// The near history of the NEAR_SUB steps j0 .. j0+NEAR_SUB-1 of a 64-step block from the block's
+// rows older than j0, with those steps' far partials: pre[u][i] = far(j0+u) + sum_{r<j0}
+// w[j0+u-r] ring[r], in float-float (two nodes per thread, (hi, lo) of each). Each row is read
+// once per NEAR_SUB steps instead of once per step; a step then adds only the rows of its own
+// sub-block (k_near_history_ff with pre).
+__global__ void __launch_bounds__(256) k_near_pre_ff(const float4 *__restrict__ ringf, int64_t P2, int j0,
+                                                     const float2 *__restrict__ wff_all,
+                                                     const double2 *__restrict__ cfar, int KS, int pairs,
+                                                     float4 *__restrict__ pre, const int *__restrict__ cta_col,
+                                                     int64_t wstride)
+{
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= P2) return;
+    const float2 *wff = cta_col ? wff_all + (int64_t)cta_col[blockIdx.x] * wstride : wff_all;
+    float h[NEAR_SUB][2], l[NEAR_SUB][2];
+#pragma unroll
+    for (int u = 0; u < NEAR_SUB; ++u) h[u][0] = h[u][1] = l[u][0] = l[u][1] = 0.f;
+    for (int q = 0; q < KS; ++q) {
+#pragma unroll
+        for (int u = 0; u < NEAR_SUB; ++u) {
+            const double2 v = __ldcs(cfar + ((int64_t)q * 64 + j0 + u) * P2 + i);
+            const float2 f0 = pairs ? *reinterpret_cast<const float2 *>(&v.x) : d2ff(v.x);
+            const float2 f1 = pairs ? *reinterpret_cast<const float2 *>(&v.y) : d2ff(v.y);
+            ff_add(h[u][0], l[u][0], f0.x, f0.y);
+            ff_add(h[u][1], l[u][1], f1.x, f1.y);
+        }
+    }
+    for (int r = 0; r < j0; ++r) {
+        const float4 v = __ldcg(ringf + (int64_t)r * P2 + i);
+#pragma unroll
+        for (int u = 0; u < NEAR_SUB; ++u) {
+            const float2 w = __ldg(wff + (j0 + u - r));
+            ff_fma(h[u][0], l[u][0], w, make_float2(v.x, v.y));
+            ff_fma(h[u][1], l[u][1], w, make_float2(v.z, v.w));
+        }
+        if ((r & 7) == 7) {
+#pragma unroll
+            for (int u = 0; u < NEAR_SUB; ++u) {
+                ff_renorm(h[u][0], l[u][0]);
+                ff_renorm(h[u][1], l[u][1]);
+            }
+        }
+    }
+#pragma unroll
+    for (int u = 0; u < NEAR_SUB; ++u) pre[(int64_t)u * P2 + i] = make_float4(h[u][0], l[u][0], h[u][1], l[u][1]);
+}
+
+// Two nodes per thread: S = far partials of step j + sum_{r<j} w[j-r] ring[r] in float-float; with
+// pre (the sub-block's partial sums of k_near_pre_ff, sub-block start r0), S = pre[j-r0] + the rows
+// r0 .. j-1.
 __global__ void __launch_bounds__(256) k_near_history_ff(const float4 *__restrict__ ringf, int64_t P2, int j,
                                                          const float2 *__restrict__ wff_all,
                                                          const double2 *__restrict__ cfar, int KS, int pairs,
                                                          double2 *__restrict__ S, const int *__restrict__ cta_col,
-                                                         int64_t wstride)
+                                                         int64_t wstride, const float4 *__restrict__ pre, int r0)
 {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= P2) return;
     const float2 *wff = cta_col ? wff_all + (int64_t)cta_col[blockIdx.x] * wstride : wff_all;
     float h0 = 0.f, l0 = 0.f, h1 = 0.f, l1 = 0.f;
+    if (pre) {
+        const float4 v = __ldcs(pre + (int64_t)(j - r0) * P2 + i);
+        h0 = v.x; l0 = v.y; h1 = v.z; l1 = v.w;
+        KS = 0;
+    }
     for (int q = 0; q < KS; ++q) {
         const double2 v = __ldcs(cfar + ((int64_t)q * 64 + j) * P2 + i);
         const float2 f0 = pairs ? *reinterpret_cast<const float2 *>(&v.x) : d2ff(v.x);
@@ -361,7 +427,7 @@ __global__ void __launch_bounds__(256) k_near_history_ff(const float4 *__restric
         ff_add(h0, l0, f0.x, f0.y);
         ff_add(h1, l1, f1.x, f1.y);
     }
-    int r = 0;
+    int r = pre ? r0 : 0;
     for (; r + 8 <= j; r += 8) {
         float4 v[8];
 #pragma unroll
@@ -385,11 +451,23 @@ __global__ void __launch_bounds__(256) k_near_history_ff(const float4 *__restric
 }
 
 int launch_near_history_ff(cudaStream_t st, const float2 *ringf, int64_t P, int j, const float2 *wff,
-                           const double *cfar, int KS, int pairs, double *S, const int *cta_col, int64_t wstride)
+                           const double *cfar, int KS, int pairs, double *S, const int *cta_col, int64_t wstride,
+                           const float2 *pre, int r0)
 {
     k_near_history_ff<<<(unsigned)((P / 2 + 255) / 256), 256, 0, st>>>((const float4 *)ringf, P / 2, j, wff,
                                                                        (const double2 *)cfar, KS, pairs,
-                                                                       (double2 *)S, cta_col, wstride);
+                                                                       (double2 *)S, cta_col, wstride,
+                                                                       (const float4 *)pre, r0);
+    FPDE_LAUNCHED(1);
+    return FPDE_OK;
+}
+
+int launch_near_pre_ff(cudaStream_t st, const float2 *ringf, int64_t P, int j0, const float2 *wff, const double *cfar,
+                       int KS, int pairs, float2 *pre, const int *cta_col, int64_t wstride)
+{
+    k_near_pre_ff<<<(unsigned)((P / 2 + 255) / 256), 256, 0, st>>>((const float4 *)ringf, P / 2, j0, wff,
+                                                                   (const double2 *)cfar, KS, pairs, (float4 *)pre,
+                                                                   cta_col, wstride);
     FPDE_LAUNCHED(1);
     return FPDE_OK;
 }
@@ -415,11 +493,12 @@ struct fpde_lod3d {
     int rp_rows = 0, bc_rows = 0;
     double *cA[3] = {nullptr, nullptr, nullptr}, *cg[3] = {nullptr, nullptr, nullptr},
            *cal[3] = {nullptr, nullptr, nullptr};
-    // segmented passes (lines of up to LSEGS x LSEGLEN interior nodes): per-node responses KF, CB
+    // segmented passes (seg_shape: lines of up to 16 x 32 interior nodes): per-node responses KF, CB
     // and per-segment products PF; seglen 0 runs the one-thread-per-line kernel
     double *cKF[3] = {nullptr, nullptr, nullptr}, *cCB[3] = {nullptr, nullptr, nullptr},
            *cPF[3] = {nullptr, nullptr, nullptr};
     int seglen[3] = {0, 0, 0};
+    int segs[3] = {0, 0, 0};
     int lines[3] = {0, 0, 0};
     // split path (exact three-slice far history on the tensor cores, FP64 near history)
     bool split = false;
@@ -429,6 +508,7 @@ struct fpde_lod3d {
     float *pW = nullptr;
     double *ring = nullptr, *cfar = nullptr, *wlag = nullptr, *Sn = nullptr;
     float2 *ringf = nullptr, *wff = nullptr;  // the ring and the lag weights as float pairs
+    float2 *pre = nullptr;                    // near-history sums of the current 8-step sub-block
     FarPlan3 plan3;
     // Richards problem (desc.richards): coefficients from the solution every step
     bool rich = false;
@@ -504,8 +584,11 @@ static int lod_launch_pass(fpde_lod3d *L, cudaStream_t st, int pass, int64_t n, 
     } else if (L->seglen[pass] > 0) {
         LodSegArgs sg;
         sg.KF = L->cKF[pass]; sg.CB = L->cCB[pass]; sg.PF = L->cPF[pass]; sg.seglen = L->seglen[pass];
-        const int64_t threads = (int64_t)a.lines * LSEGS;
-        k_lod_pass_seg<<<(unsigned)((threads + 127) / 128), 128, 0, st>>>(a, sg);
+        const int SG = L->segs[pass];
+        const unsigned blocks = (unsigned)(((int64_t)a.lines * SG + 127) / 128);
+        if (SG == 8) k_lod_pass_seg<8, 16><<<blocks, 128, 0, st>>>(a, sg);
+        else if (L->seglen[pass] <= 16) k_lod_pass_seg<16, 16><<<blocks, 128, 0, st>>>(a, sg);
+        else k_lod_pass_seg<16, 32><<<blocks, 128, 0, st>>>(a, sg);
     } else {
         k_lod_pass<<<(unsigned)((a.lines + 127) / 128), 128, 0, st>>>(a);
     }
@@ -616,7 +699,17 @@ static int lod_enqueue(fpde_lod3d *L, cudaStream_t st, int64_t n0, int steps, in
                 }
             }
             if (n >= 1) {
-                if ((rc = launch_near_history_ff(st, L->ringf, L->P, j, L->wff, L->cfar, splits, 1, L->Sn))) return rc;
+                // rows older than the step's 8-step sub-block (and the far partials) are summed once
+                // per sub-block; each step adds its sub-block's rows
+                const int j0 = j - j % NEAR_SUB;
+                const bool use_pre = splits > 0 || j0 > 0;
+                if (use_pre && j == j0) {
+                    if ((rc = launch_near_pre_ff(st, L->ringf, L->P, j0, L->wff, L->cfar, splits, 1, L->pre))) return rc;
+                    ++k;
+                }
+                if ((rc = launch_near_history_ff(st, L->ringf, L->P, j, L->wff, L->cfar, splits, 1, L->Sn, nullptr, 0,
+                                                 use_pre ? L->pre : nullptr, j0)))
+                    return rc;
                 ++k;
                 KS = 1;
             }
@@ -650,6 +743,7 @@ int fpde_lod3d_destroy(fpde_lod3d *L)
     L->graphs.clear();
     dev_free(L->ringf);
     dev_free(L->wff);
+    dev_free(L->pre);
     for (double *p : {L->U, L->last, L->D, L->part, L->wrev, L->rp, L->bc, L->ring, L->cfar, L->wlag, L->Sn, L->H})
         dev_free(p);
     for (int q = 0; q < 3; ++q) {
@@ -785,6 +879,7 @@ int fpde_lod3d_create(fpde_ctx *ctx, const fpde_lod3d_desc *desc, const double *
                dev_alloc((void **)&L->cfar, (size_t)FAR_MAX_SPLITS * 64 * pbytes) ||
                dev_alloc((void **)&L->wlag, LW * sizeof(double)) || dev_alloc((void **)&L->Sn, pbytes) ||
                dev_alloc((void **)&L->ringf, (size_t)64 * L->P * sizeof(float2)) ||
+               dev_alloc((void **)&L->pre, (size_t)NEAR_SUB * L->P * sizeof(float2)) ||
                dev_alloc((void **)&L->wff, LW * sizeof(float2));
         if (!fail) {
             const void *a3[3] = {L->h3[0], L->h3[1], L->h3[2]}, *w3[3] = {L->w3[0], L->w3[1], L->w3[2]};
@@ -898,11 +993,13 @@ int fpde_lod3d_create(fpde_ctx *ctx, const fpde_lod3d_desc *desc, const double *
             if (fail) set_error(FPDE_ERR_CUDA, "lod3d: coefficient upload failed");
         }
         // segmented pass data: segment s holds nodes [1 + s seglen, 1 + (s+1) seglen) of 1..Nl-1
-        const int sl = (Nl - 1 + LSEGS - 1) / LSEGS;
-        if (!fail && Nl >= 2 && sl <= LSEGLEN) {
-            std::vector<double> hKF(cnt, 0.0), hCB(cnt, 0.0), hPF((size_t)lines * LSEGS, 1.0), cf(LSEGLEN);
+        int SG = 0, SL = 0;
+        seg_shape(Nl, &SG, &SL);
+        const int sl = SG ? (Nl - 1 + SG - 1) / SG : 0;
+        if (!fail && Nl >= 2 && SG > 0 && sl <= SL) {
+            std::vector<double> hKF(cnt, 0.0), hCB(cnt, 0.0), hPF((size_t)lines * SG, 1.0), cf(SL);
             for (int line = 0; line < lines; ++line) {
-                for (int sgi = 0; sgi < LSEGS; ++sgi) {
+                for (int sgi = 0; sgi < SG; ++sgi) {
                     const int q0 = 1 + sgi * sl, q1 = std::min(q0 + sl, Nl);
                     double pr = 1.0;
                     for (int q = q0; q < q1; ++q) {
@@ -910,7 +1007,7 @@ int fpde_lod3d_create(fpde_ctx *ctx, const fpde_lod3d_desc *desc, const double *
                         pr *= hg[o] * hA[o];                               // prefix product of a = g A
                         cf[q - q0] = pr;
                     }
-                    hPF[(size_t)line * LSEGS + sgi] = pr;
+                    hPF[(size_t)line * SG + sgi] = pr;
                     double kf = 0.0, cb = 1.0;
                     for (int q = q1 - 1; q >= q0; --q) {
                         const size_t o = (size_t)q * lines + line;
@@ -930,7 +1027,10 @@ int fpde_lod3d_create(fpde_ctx *ctx, const fpde_lod3d_desc *desc, const double *
                        cudaMemcpy(L->cPF[pass], hPF.data(), hPF.size() * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess;
                 if (fail) set_error(FPDE_ERR_CUDA, "lod3d: coefficient upload failed");
             }
-            if (!fail) L->seglen[pass] = sl;
+            if (!fail) {
+                L->seglen[pass] = sl;
+                L->segs[pass] = SG;
+            }
         }
     }
     if (fail) {

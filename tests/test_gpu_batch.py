@@ -1,6 +1,6 @@
 """Ensembles of columns (fpde_batch_*) on the GPU against the oracle, column by column.
 
-Columns of very different lengths (2 .. 5000 intervals, around the 256-thread segment
+Columns of very different lengths (2 .. 5000 intervals, around the 512-thread segment
 boundaries), orders and boundary kinds share one history sum and one solve kernel per step;
 each must equal the oracle's own run of that column to 1e-12, or to 4x the oracle's one-ulp
 rounding envelope where the column is long and ill-conditioned.
@@ -60,7 +60,7 @@ def _check(ctx, cols, steps):
 def test_batch_mixed_columns_vs_oracle(ctx):
     from fpde_hpc_gb300 import problems
     rng = np.random.default_rng(11)
-    sizes = [2, 3, 17, 255, 256, 257, 511, 512, 1000, 2049, 5000, 40, 700, 1300]
+    sizes = [2, 3, 17, 255, 256, 257, 511, 512, 513, 1000, 1025, 2049, 5000, 40, 700, 1300]
     cols = []
     for j, N in enumerate(sizes):
         p = problems.config2(N=N, steps=90)
