@@ -538,9 +538,40 @@ void fo_richards_closures(int n, const double *P, int kform, double ksat, double
  * Left ends: the sN pass takes the first-order surface condition (al1 :4004-4012, bc0 :4493-4500)
  * with Uc = dL[0] E / KK(1) (:3036-3070, no irrigation); the other passes zero flux (Al[1] = 1,
  * Bt[1] = 0). Right ends: the flux closure of U1 with bcN = 0. rp: the K-pass source grid. */
+/* time_summing of the K-pass nodes (:4086-4164) in the reference's order: s = 0, then
+ * s += kb[t] D_t / tau[t] for t = n-1 .. 0 (rows read contiguously, k-planes in parallel) */
+static void lod_history_sum(int sN, int M, int K, const double *hist, int n, const double *kb, const double *tau,
+                            double *S)
+{
+    const int64_t sx = 1, sy = sN + 2, sz = (int64_t)(sN + 2) * (M + 2);
+    const int64_t G = sz * (K + 2);
+    if (n <= 0) return;
+#pragma omp parallel for schedule(static)
+    for (int k = 1; k <= K; k++)
+        for (int t = n - 1; t >= 0; t--) {
+            const double *h = hist + (int64_t)t * G;
+            const double c = kb[t], tt = tau[t];
+            for (int j = 1; j < M; j++)
+                for (int i = 1; i < sN; i++) {
+                    const int64_t id = i * sx + j * sy + k * sz;
+                    S[id] += c * h[id] / tt;
+                }
+        }
+}
+
 int fo_lod_step_richards(int sN, int M, int K, double *U, double *hist, int n, const double *kb, const double *tau,
                          double Da, double kkk0, const double *sZ, const double *sdL, const double *dLx,
                          const double *dLy, int kform, double ksat, double E, const double *rp, double *S_out)
+{
+    return fo_lod_step_richards_salt(sN, M, K, U, hist, n, kb, tau, Da, kkk0, sZ, sdL, dLx, dLy, kform, ksat, E, rp,
+                                     S_out, NULL, NULL, NULL, NULL, NULL, 0.0, 0.0, NULL);
+}
+
+int fo_lod_step_richards_salt(int sN, int M, int K, double *U, double *hist, int n, const double *kb,
+                              const double *tau, double Da, double kkk0, const double *sZ, const double *sdL,
+                              const double *dLx, const double *dLy, int kform, double ksat, double E,
+                              const double *rp, double *S_out, double *C, double *histC, const double *cA,
+                              const double *cB, const double *cR, double nu, double sigma, double *SC_out)
 {
     const double lam = Da * (kkk0 / tau[n]);      /* Om1 :4191 */
     const double lamR = Da * kkk0 / tau[n];       /* R :3120 */
@@ -549,19 +580,13 @@ int fo_lod_step_richards(int sN, int M, int K, double *U, double *hist, int n, c
     int L = sN; if (M > L) L = M; if (K > L) L = K;
     double *Uold = (double *)malloc(sizeof(double) * (size_t)G);
     double *S = (double *)calloc((size_t)G, sizeof(double));
+    double *Cold = C ? (double *)malloc(sizeof(double) * (size_t)G) : NULL;
+    double *SC = C ? (double *)calloc((size_t)G, sizeof(double)) : NULL;
     memcpy(Uold, U, sizeof(double) * (size_t)G);
-    if (n > 0) {
-#pragma omp parallel for schedule(static)
-        for (int k = 1; k <= K; k++)
-            for (int t = n - 1; t >= 0; t--) {
-                const double *h = hist + (int64_t)t * G;
-                const double c = kb[t], tt = tau[t];
-                for (int j = 1; j < M; j++)
-                    for (int i = 1; i < sN; i++) {
-                        const int64_t id = i * sx + j * sy + k * sz;
-                        S[id] += c * h[id] / tt;
-                    }
-            }
+    lod_history_sum(sN, M, K, hist, n, kb, tau, S);
+    if (C) {
+        memcpy(Cold, C, sizeof(double) * (size_t)G);
+        lod_history_sum(sN, M, K, histC, n, kb, tau, SC);
     }
     for (int pass = 2; pass >= 0; pass--) {
         const int Nl = pass == 2 ? K : (pass == 1 ? M : sN);
@@ -600,6 +625,12 @@ int fo_lod_step_richards(int sN, int M, int K, double *U, double *hist, int n, c
                     lr[p] = iw[p] * ((kk[p] / (dL[p] * dL[p])) + (kk[p - 1] / (dL[p] * dL[p - 1]))) + lamR;
                     const int64_t id = base + p * st;
                     lo[p] = -(lam * lu[p]) + ((pass == 2 && rp) ? rp[id] : 0.0);
+                    if (C && nu != 0.0) {                  /* chemical osmosis, Om1 :4211-4223 (old C) */
+                        const double d2 = dL[p] * dL[p], d1 = dL[p] * dL[p - 1];
+                        const int64_t s1 = st;
+                        const double f = nu * (((C[id + s1] / d2) - ((1.0 / d2) + (1.0 / d1)) * C[id]) + (C[id - s1] / d1));
+                        lo[p] += f * iw[p];
+                    }
                     if (pass == 2) lo[p] += Da * S[id];
                 }
                 int lkind = 1;
@@ -612,14 +643,52 @@ int fo_lod_step_richards(int sN, int M, int K, double *U, double *hist, int n, c
                 thomas_core(Nl, la, lb, lr, lo, lkind, g0, 1, 0.0, dL[Nl - 1], lu, Al, Bt);
                 lu[Nl + 1] = lu[Nl];                                 /* U1 :4792 */
                 for (int p = 0; p <= Nl + 1; p++) U[base + p * st] = lu[p];
+                if (!C) continue;
+                /* equation 1 on the same line (U1(1) after U1(0), :5270-5278): the coefficients of
+                 * A_/B/R (:3099-3136), Om1's local and coupling terms (:4175-4229) with the new H
+                 * and its KK, the old C; Dirichlet Cu() = 0 at the surface of the sN pass (al1
+                 * :4014-4017, no irrigation), zero flux elsewhere (Al[1] = 1, Bt[1] = 0), the flux
+                 * closure with bcN = 0 at the far end (bottom_cond 0) */
+                for (int p = 0; p <= Nl; p++) {                      /* KK of the new H */
+                    const int inode = pass == 0 ? p : a;
+                    kk[p] = rich_KK(-(lu[p] - inode * sZ[p]), kform, ksat);
+                }
+                double *lc = iw;                                       /* reuse: the C line */
+                for (int p = 0; p <= Nl + 1; p++) lc[p] = C[base + p * st];
+                for (int p = 1; p < Nl; p++) {
+                    const int64_t id = base + p * st;
+                    la[p] = cA[(int64_t)pass * G + id];
+                    lb[p] = cB[(int64_t)pass * G + id];
+                    lr[p] = cR[(int64_t)pass * G + id] + lamR;
+                    const double d2 = dL[p] * dL[p], d1 = dL[p] * dL[p - 1];
+                    const double fh = (1.0 / sigma) * ((((kk[p] * lc[p]) * lu[p + 1]) / d2) -
+                                                       (((kk[p] * lc[p]) / d2) + ((kk[p - 1] * lc[p - 1]) / d1)) * lu[p] +
+                                                       (((kk[p - 1] * lc[p - 1]) * lu[p - 1]) / d1));
+                    const double fc = (nu / sigma) * (((lc[p] * lc[p + 1]) / d2) -
+                                                      ((lc[p] / d2) + (lc[p - 1] / d1)) * lc[p] +
+                                                      ((lc[p - 1] * lc[p - 1]) / d1));
+                    double om = -(lam * lc[p]) + 0.0;                  /* Rp = 0 for equation 1 */
+                    om -= fh;
+                    if (nu != 0.0) om += fc;
+                    if (pass == 2) om += Da * SC[id];
+                    lo[p] = om;
+                }
+                thomas_core(Nl, la, lb, lr, lo, pass == 0 ? 0 : 1, 0.0, 1, 0.0, dL[Nl - 1], lc, Al, Bt);
+                lc[Nl + 1] = lu[Nl];                                 /* U1 :4792 copies H's U[N] */
+                for (int p = 0; p <= Nl + 1; p++) C[base + p * st] = lc[p];
             }
         free(la); free(lb); free(lr); free(lo); free(lu); free(kk); free(iw); free(Al); free(Bt);
         }
     }
     double *row = hist + (int64_t)n * G;
     for (int64_t q = 0; q < G; q++) row[q] = U[q] - Uold[q];
+    if (C) {
+        double *rc = histC + (int64_t)n * G;
+        for (int64_t q = 0; q < G; q++) rc[q] = C[q] - Cold[q];
+    }
     if (S_out) memcpy(S_out, S, sizeof(double) * (size_t)G);
-    free(Uold); free(S);
+    if (SC_out && SC) memcpy(SC_out, SC, sizeof(double) * (size_t)G);
+    free(Uold); free(S); free(Cold); free(SC);
     return 0;
 }
 

@@ -154,6 +154,16 @@ int fo_lod_step_richards(int sN, int M, int K, double *U, double *hist, int n, c
                          double Da, double kkk0, const double *sZ, const double *sdL, const double *dLx,
                          const double *dLy, int kform, double ksat, double E, const double *rp, double *S_out);
 
+/* The same step with the salt concentration C (equation 1, is_c): on every line of every pass, after
+ * the H solve, C's solve with the constant coefficient grids cA/cB/cR (3 passes x grid: the
+ * reference's A_/B/R of equation 1 with Da = 0), the coupling terms of Om1 with the new H and its
+ * KK and the old C, C's own history histC (rows of the grid) and sum. C = NULL: H alone. */
+int fo_lod_step_richards_salt(int sN, int M, int K, double *U, double *hist, int n, const double *kb,
+                              const double *tau, double Da, double kkk0, const double *sZ, const double *sdL,
+                              const double *dLx, const double *dLy, int kform, double ksat, double E,
+                              const double *rp, double *S_out, double *C, double *histC, const double *cA,
+                              const double *cB, const double *cR, double nu, double sigma, double *SC_out);
+
 /* A 1D Richards line with the history (mode-1 closures, P = -(U[i] - Z[i])): per step the L1
  * sum, coefficients from the current values, the surface condition from the step's evaporation
  * rate E[min(n, erows-1)], the right end rtype (0 Dirichlet gN, 1 flux closure). */

@@ -58,6 +58,9 @@ def load():
     lib.fo_lod_step_richards.argtypes = [i32, i32, i32, _dp, _dp, i32, _dp, _dp, d, d, _dp, _dp, _dp, _dp, i32, d,
                                          d, vp, vp]
     lib.fo_lod_step_richards.restype = i32
+    lib.fo_lod_step_richards_salt.argtypes = [i32, i32, i32, _dp, _dp, i32, _dp, _dp, d, d, _dp, _dp, _dp, _dp, i32,
+                                              d, d, vp, vp, vp, vp, vp, vp, vp, d, d, vp]
+    lib.fo_lod_step_richards_salt.restype = i32
     lib.fo_line_run_richards.argtypes = [i32, _dp, _dp, i64, i32, d, d, d, _dp, _dp, i32, d, _dp, i32, vp, i32,
                                          i32, d, d]
     lib.fo_line_run_richards.restype = i32
@@ -268,6 +271,23 @@ def lod_step_richards(dims, U, hist, n, kb, tau, Da, kkk0, sZ, sdL, dLx, dLy, kf
                              f(dLx), f(dLy), kform, ksat, E,
                              None if rpp is None else rpp.ctypes.data_as(C.c_void_p), _ptr(S))
     return S
+
+
+def lod_step_richards_salt(dims, U, hist, n, kb, tau, Da, kkk0, sZ, sdL, dLx, dLy, kform, ksat, E, C, histC, cA, cB,
+                           cR, nu, sigma, rp=None, want_S=False):
+    """fo_lod_step_richards_salt: one LOD step of H and the salt concentration C (equation 1),
+    both advanced in place; cA/cB/cR: equation 1's coefficient grids (3 passes). Returns
+    (S_H, S_C) when want_S."""
+    lib = load()
+    sN, M, K = dims
+    S = np.zeros_like(U) if want_S else None
+    SC = np.zeros_like(U) if want_S else None
+    rpp = None if rp is None else _f64(rp).reshape(-1)
+    lib.fo_lod_step_richards_salt(sN, M, K, U.reshape(-1), hist.reshape(-1), n, _f64(kb), _f64(tau), Da, kkk0,
+                                  _f64(sZ), _f64(sdL), _f64(dLx), _f64(dLy), kform, ksat, E, _ptr(rpp), _ptr(S),
+                                  _ptr(C), _ptr(histC), _ptr(_f64(cA)), _ptr(_f64(cB)), _ptr(_f64(cR)), nu, sigma,
+                                  _ptr(SC))
+    return (S, SC) if want_S else None
 
 
 def line_run_richards(U0, steps, tau, alpha, Da, Z, dL, kform, ksat, E, src=None, rtype=0, gN=0.0, dLN=0.0):

@@ -322,6 +322,100 @@ static void run_richards(const char *path, int kform, int rpform, int bs, int nb
     printf("wrote %s (Richards k_form %d, %d steps, grid %dx%dx%d)\n", path, kform, steps, sN, _M, K);
 }
 
+/* The Richards problem coupled with salt concentration C (analytic_test 0 with is_c = 1: nu
+ * nonzero, :3515): on every line of every pass calc_step solves H (U1(0)) and then C (U1(1))
+ * (:5270-5278), each with its own L1 history (oldC, time_summing :4086-4164). (With is_t = 1 the
+ * reference's mode-3 constructor writes T0 through a row that is not set yet, :3640, and stops
+ * with a null dereference, so no 3D run with temperature exists.) Records, besides the Richards
+ * inputs: the initial and per-step C grids with their history sums, the constant line
+ * coefficients of equation 1 per pass (as record_coefs, Da = 0) and the physical constants of the
+ * coupling terms (Om1 :4195-4256). */
+static void run_richards_ct(const char *path, int kform, int bs, int nb, int mb, int kb, double alpha, double tau,
+                            int steps)
+{
+    set_dims(bs, nb, mb, kb);
+    varT = 0; varZ = 0; varXY = 0;
+    implicit = 0; implicit3d = 0; rp_split_3d = 0; sum_alg = 0;
+    global_eps = 1e-15; global_eps2 = 1e-15;
+    FILE *lg = fopen("/dev/null", "w");
+    H_solver *s = new H_solver(0, 1, 4, 1, 0, alpha, 1.0, 1, 0, 0, 3, lg, kform);
+    size_t G = (size_t)(sN + 2) * (_M + 2) * (K + 2);
+    /* the reference starts from C0 = 0 everywhere and, without irrigation, nothing makes C nonzero:
+     * start from a smooth salt field instead (the reference's own steps then move it) */
+    for (int i = 0; i <= sN + 1; i++) for (int j = 0; j <= _M + 1; j++) for (int k = 0; k <= K + 1; k++)
+        s->b_C[gidx(i, j, k)] = 2.0 + std::sin(0.9 * i + 0.4 * j) * std::cos(0.6 * k);
+    FgvWriter w(path);
+    w.scalar("sN", sN); w.scalar("M", _M); w.scalar("K", K);
+    w.scalar("alpha", alpha); w.scalar("Da", s->Da); w.scalar("Dg", s->Dg); w.scalar("k_form", kform);
+    w.scalar("k_sat", s->k);
+    w.scalar("nu", s->nu); w.scalar("kt", s->kt); w.scalar("sigma", s->sigma); w.scalar("D", s->D);
+    w.scalar("lambda", s->lambda); w.scalar("Ct", s->Ct); w.scalar("p_water", s->p_water);
+    std::vector<uint64_t> gdims = {(uint64_t)(K + 2), (uint64_t)(_M + 2), (uint64_t)(sN + 2)};
+    w.put("U0", gdims, s->b_U);
+    w.put("C0", gdims, s->b_C);
+    w.put("sZ", std::vector<double>(s->sZ, s->sZ + sN + 2));
+    w.put("sdL", std::vector<double>(s->sdL, s->sdL + sN + 2));
+    w.put("dLx", std::vector<double>(s->dLx, s->dLx + _M + 2));
+    w.put("dLy", std::vector<double>(s->dLy, s->dLy + K + 2));
+    std::vector<double> kb_all, kb_off, kkk0, tauv, Ev, U_all, C_all, SU, SC;
+    for (int n = 0; n < steps; n++) {
+        s->Time.push_back(s->Time[s->Time.size() - 1] + tau);
+        s->tau.push_back(tau);
+        s->tstep++;
+        Ev.push_back(s->Ev * s->day_night_coef());
+        s->Time.pop_back();
+        s->tau.pop_back();
+        s->tstep--;
+        s->calc_step(tau);
+        if (n == 0) {   /* equation 1: A_/B/R per pass with Da = 0 (constant: D/sigma and the steps) */
+            PassState st = save_state(s);
+            double Da_saved = s->Da;
+            s->Da = 0.0;
+            for (int eq = 1; eq <= 1; eq++)
+                for (int pass = 0; pass < 3; pass++) {
+                    std::vector<double> A(G, 0.0), B(G, 0.0), R(G, 0.0);
+                    int na = pass == 2 ? sN : (pass == 1 ? sN : _M), nbl = pass == 2 ? _M : K;
+                    int Nl = pass == 2 ? K : (pass == 1 ? _M : sN);
+                    for (int a = 1; a < na; a++) for (int b = 1; b < nbl; b++) {
+                        enter_line(s, pass, a, b);
+                        s->equation = eq;
+                        for (int q = 1; q < Nl; q++) {
+                            size_t id = pass == 2 ? gidx(a, b, q) : (pass == 1 ? gidx(a, q, b) : gidx(q, a, b));
+                            A[id] = s->A_(q); B[id] = s->B(q); R[id] = s->R(q);
+                        }
+                    }
+                    char nm[32];
+                    snprintf(nm, sizeof nm, "eq%d_A_pass%d", eq, pass); w.put(nm, gdims, A.data());
+                    snprintf(nm, sizeof nm, "eq%d_B_pass%d", eq, pass); w.put(nm, gdims, B.data());
+                    snprintf(nm, sizeof nm, "eq%d_R_pass%d", eq, pass); w.put(nm, gdims, R.data());
+                }
+            s->Da = Da_saved;
+            s->equation = 0;
+            restore_state(s, st);
+        }
+        kb_off.push_back((double)kb_all.size());
+        kb_all.insert(kb_all.end(), s->kb_3_cache.begin(), s->kb_3_cache.end());
+        kkk0.push_back(s->kkk0);
+        tauv.push_back(s->tau[s->tstep]);
+        U_all.insert(U_all.end(), s->b_U, s->b_U + G);
+        C_all.insert(C_all.end(), s->b_C, s->b_C + G);
+        SU.insert(SU.end(), s->b_Utimesum, s->b_Utimesum + G);
+        SC.insert(SC.end(), s->b_Ctimesum, s->b_Ctimesum + G);
+    }
+    kb_off.push_back((double)kb_all.size());
+    uint64_t ns = steps;
+    std::vector<uint64_t> sdims = {ns, (uint64_t)(K + 2), (uint64_t)(_M + 2), (uint64_t)(sN + 2)};
+    w.put("tau", tauv); w.put("kkk0", kkk0);
+    w.put("kb_flat", kb_all); w.put("kb_off", kb_off);
+    w.put("E", Ev);
+    w.put("U", sdims, U_all.data()); w.put("C", sdims, C_all.data());
+    w.put("SU", sdims, SU.data()); w.put("SC", sdims, SC.data());
+    delete s;
+    fclose(lg);
+    printf("wrote %s (Richards with salt concentration, k_form %d, %d steps, grid %dx%dx%d)\n", path, kform, steps,
+           sN, _M, K);
+}
+
 /* The implicit space-fractional LOD (impl 2, TMA 0: implicit2_gen :4630-4663 builds each line's
  * tridiagonal Mat and right-hand side, U1 :4769-4791 solves tridiag(Mat) + iw * T * tridiag(Mcoefs)
  * with solve_mln<1> :812-1157 and the product vmul_T :6618-6747), analytic problem 2, Dirichlet
@@ -461,6 +555,12 @@ int main(int argc, char **argv)
         run_richards(q, 1, 1, 2, 3, 3, 3, 0.8, 900.0, 40);
         snprintf(q, sizeof q, "%s/fpde_richards_k2.fgv", argv[2]);
         run_richards(q, 2, 2, 2, 3, 3, 3, 0.6, 900.0, 40);
+        return 0;
+    }
+    if (argc >= 3 && strcmp(argv[1], "richards_ct") == 0) {
+        char q[4096];
+        snprintf(q, sizeof q, "%s/fpde_richards_ct.fgv", argv[2]);
+        run_richards_ct(q, 1, 2, 3, 3, 3, 0.8, 900.0, 24);
         return 0;
     }
     if (argc >= 3 && strcmp(argv[1], "spacefrac") == 0) {

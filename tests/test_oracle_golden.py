@@ -349,3 +349,53 @@ def test_richards_lod_replays_reference_run(kform):
             sl = (slice(1, dims[2] + 1), slice(1, dims[1]), slice(1, dims[0]))
             assert np.allclose(S[sl], g["S"][n][sl], rtol=1e-13, atol=1e-13 * np.max(np.abs(g["S"][n][sl])))
     assert worst <= (0.0 if kform == 2 else 1e-14), worst
+
+
+def _salt_case():
+    g = fgv.load(golden_path("fpde_richards_ct"))
+    dims = (int(g["sN"]), int(g["M"]), int(g["K"]))
+    cA = np.stack([g[f"eq1_A_pass{p}"] for p in range(3)])
+    cB = np.stack([g[f"eq1_B_pass{p}"] for p in range(3)])
+    cR = np.stack([g[f"eq1_R_pass{p}"] for p in range(3)])
+    return g, dims, cA, cB, cR
+
+
+def test_richards_salt_lod_replays_reference_run():
+    """The reference's Richards run with the salt concentration C (equation 1: chemical osmosis in
+    the H equation, the H-driven and osmotic terms in C's, C's own history) replayed by the oracle
+    bit for bit, H and C at every step (6^3 cells, 24 steps, k_form 1)."""
+    g, dims, cA, cB, cR = _salt_case()
+    U, C = g["U0"].copy(), g["C0"].copy()
+    steps = g["U"].shape[0]
+    hist, histC = np.zeros((steps,) + U.shape), np.zeros((steps,) + U.shape)
+    kbo = g["kb_off"].astype(np.int64)
+    for n in range(steps):
+        kb = g["kb_flat"][kbo[n]:kbo[n + 1]]
+        oracle.lod_step_richards_salt(dims, U, hist, n, kb if n else np.zeros(1), g["tau"], float(g["Da"]),
+                                      float(g["kkk0"][n]), g["sZ"], g["sdL"], g["dLx"], g["dLy"], int(g["k_form"]),
+                                      float(g["k_sat"]), float(g["E"][n]), C, histC, cA, cB, cR, float(g["nu"]),
+                                      float(g["sigma"]))
+        assert np.array_equal(U, g["U"][n]), f"H at step {n}"
+        assert np.array_equal(C, g["C"][n]), f"C at step {n}"
+    assert np.abs(C - g["C0"])[1:-1, 1:-1, 1:-1].max() > 0.05      # the concentration moved
+
+
+def test_salt_coefficients_match_the_reference_formula():
+    """Equation 1's constant coefficients (A_/B/R :3099-3136 with Dg = kb = 1, Da = 0) from D, sigma
+    and the steps, as the device forms them, equal the reference's recorded grids."""
+    g, dims, cA, cB, cR = _salt_case()
+    sN, M, K = dims
+    D, sigma = float(g["D"]), float(g["sigma"])
+    for p, (dl, nl) in enumerate(((g["sdL"], sN), (g["dLx"], M), (g["dLy"], K))):
+        ref = (cA[p], cB[p], cR[p])
+        ax = 2 - p                                   # grid axis of the pass (k, j, i order)
+        for q in range(1, nl):
+            a = (D * (1.0 / (dl[q] * dl[q - 1]))) / sigma
+            b = (D * (1.0 / (dl[q] * dl[q]))) / sigma
+            r = (D * ((1.0 / (dl[q] * dl[q])) + (1.0 / (dl[q] * dl[q - 1])))) / sigma
+            sl = [slice(1, -1)] * 3
+            sl[ax] = q
+            for got, want in zip((a, b, r), ref):
+                vals = np.unique(want[tuple(sl)])
+                vals = vals[vals != 0]                   # nodes off the pass's lines hold 0
+                assert vals.size == 1 and vals[0] == got, (p, q)
