@@ -25,7 +25,8 @@ class LineTuning(C.Structure):
 
 class Richards(C.Structure):
     _fields_ = [("k_form", c_int), ("k_sat", c_dbl), ("sZ", c_vp), ("dL", c_vp * 3), ("evaporation", c_vp),
-                ("evaporation_rows", c_int)]
+                ("evaporation_rows", c_int), ("salt_c0", c_vp), ("salt_nu", c_dbl), ("salt_sigma", c_dbl),
+                ("salt_D", c_dbl)]
 
 
 class LineDesc(C.Structure):
@@ -86,6 +87,7 @@ _SIGS = {
     "fpde_lod3d_solve_host": (c_int, [c_vp, c_vp, c_int, c_vp]),
     "fpde_lod3d_steps_done": (c_int, [c_vp, C.POINTER(c_i64)]),
     "fpde_lod3d_sf_iterations": (c_int, [c_vp, C.POINTER(c_i64)]),
+    "fpde_lod3d_get_concentration": (c_int, [c_vp, c_vp, c_int]),
     "fpde_sf_matvec": (c_int, [c_vp, c_int, c_int, c_vp, c_vp, c_vp, c_vp, c_vp, c_int, c_vp, c_vp, c_int]),
     "fpde_sf_solve": (c_int, [c_vp, c_int, c_int, c_vp, c_vp, c_vp, c_vp, c_vp, c_int, c_vp, c_vp, c_dbl, c_int,
                               c_vp, c_int]),

@@ -407,7 +407,7 @@ class Lod3D:
                  precision=FP64, restrict_eps=0.0, series_terms=0, richards=None, space_frac=None):
         """richards: optional dict(k_form, k_sat, sZ, dL=(sdL, dLx, dLy), evaporation) - the
         reference's Richards problem, coefficients formed from the grid every step (coefA/B/Rlap
-        may then be None).
+        may then be None); with c0 (and nu, sigma, D) also the salt concentration (equation 1).
         space_frac: optional dict(space_der, tol, max_iter, Tm=(3 rows), mc=(3 passes x 3 grids),
         iw=(3 grids)) - the reference's implicit space-fractional line solves (impl 2)."""
         sN, M, K = dims
@@ -448,6 +448,13 @@ class Lod3D:
                          evaporation=arrs[1].ctypes.data, evaporation_rows=len(arrs[1]))
             for q in range(3):
                 r.dL[q] = dls[q].ctypes.data
+            if richards.get("c0") is not None:            # salt concentration (equation 1)
+                c0 = np.ascontiguousarray(richards["c0"], dtype=np.float64)
+                if c0.shape != self.shape:
+                    raise ValueError("richards: c0 needs the grid's shape")
+                keep.append(c0)
+                r.salt_c0 = c0.ctypes.data
+                r.salt_nu, r.salt_sigma, r.salt_D = (float(richards[k]) for k in ("nu", "sigma", "D"))
             keep.append(r)
             d.richards = C.pointer(r)
         if space_frac is not None:
@@ -497,6 +504,14 @@ class Lod3D:
 
     def solve_host(self, u0, steps, out):
         check(self.ctx.lib.fpde_lod3d_solve_host(self.h, _ptr(u0), steps, _ptr(out)), "fpde_lod3d_solve_host")
+        return out
+
+    def concentration(self, out=None):
+        """The salt concentration grid (Richards problem with richards['c0'])."""
+        if out is None:
+            out = np.zeros(self.shape)
+        check(self.ctx.lib.fpde_lod3d_get_concentration(self.h, _ptr(out), 1 if _is_dev(out) else 0),
+              "fpde_lod3d_get_concentration")
         return out
 
     def sf_iterations(self):

@@ -1453,6 +1453,7 @@ int fpde_line_create(fpde_ctx *ctx, const fpde_line_desc *desc, const double *A,
         FPDE_CHECK_ARG(rich->k_sat > 0.0 && std::isfinite(rich->k_sat), "richards: k_sat must be positive");
         FPDE_CHECK_ARG(rich->sZ && rich->dL[0], "richards: node coordinates (sZ) and steps (dL[0]) required");
         FPDE_CHECK_ARG(rich->evaporation && rich->evaporation_rows >= 1, "richards: evaporation rows required");
+        FPDE_CHECK_ARG(!rich->salt_c0, "richards: the salt concentration is a 3D LOD option");
         FPDE_CHECK_ARG(d.precision == FPDE_PREC_FP64 || d.precision == FPDE_PREC_SPLIT_BF16X3,
                        "richards: FP64 or the exact three-slice split");
         FPDE_CHECK_ARG(!d.lag_weights && d.theta == 0.0 && d.restrict_eps == 0.0,

@@ -148,6 +148,11 @@ struct LodRichArgs {
     double *al;             // scratch: Al[q+1] at q * lines + line
     double ksat, lamR, E;
     int kform, pass;
+    // salt concentration (equation 1), or C = null
+    double *C = nullptr;
+    const double *partC = nullptr;   // C's history partials (K pass), KSC rows of pstride
+    int KSC = 0;
+    double nu = 0.0, sigma = 1.0, Dc = 0.0;
 };
 
 __global__ void __launch_bounds__(128) k_lod_pass_rich(LodPassArgs p, LodRichArgs r)
@@ -190,7 +195,16 @@ __global__ void __launch_bounds__(128) k_lod_pass_rich(LodPassArgs p, LodRichArg
         const double aln = __ddiv_rn(B, __dadd_rn(R, -__dmul_rn(A, al)));    // Al[q+1]
         double sv = 0.0;
         for (int k = 0; k < p.KS; ++k) sv += __ldcg(p.part + (int64_t)k * p.pstride + id);
-        const double om = __dadd_rn(__dadd_rn(-__dmul_rn(p.lam, u), p.rp ? __ldg(p.rp + id) : 0.0), sv);
+        double om = __dadd_rn(-__dmul_rn(p.lam, u), p.rp ? __ldg(p.rp + id) : 0.0);
+        if (r.C && r.nu != 0.0) {              // chemical osmosis from the old C (Om1 :4211-4223)
+            const double cm = r.C[id - p.st], cq = r.C[id], cp = r.C[id + p.st];
+            const double f = __dmul_rn(r.nu, __dadd_rn(__dadd_rn(__ddiv_rn(cp, dqq),
+                                                                 -__dmul_rn(__dadd_rn(__ddiv_rn(1.0, dqq),
+                                                                                      __ddiv_rn(1.0, dqm)), cq)),
+                                                       __ddiv_rn(cm, dqm)));
+            om = __dadd_rn(om, __dmul_rn(f, iw));
+        }
+        om = __dadd_rn(om, sv);
         y = __dmul_rn(__ddiv_rn(aln, B), __dadd_rn(__dmul_rn(A, y), -om));  // Bt[q+1]
         r.al[(int64_t)q * L + line] = aln;
         p.U[id] = y;
@@ -209,6 +223,67 @@ __global__ void __launch_bounds__(128) k_lod_pass_rich(LodPassArgs p, LodRichArg
         p.U[id] = u;
     }
     p.U[base] = __dadd_rn(__dmul_rn(al1, u), g0);                       // Al[1] U[1] + Bt[1]
+    if (!r.C) return;
+    // ---- equation 1 on the same line (U1(1) after U1(0), :5270-5278): constant coefficients
+    // A_/B/R (:3099-3136: D/sigma over the steps, Dg = kb = 1), Om1 (:4175-4229) with the new H
+    // and its KK and the old C: -(lam C) - F_H + F_C + history. Dirichlet Cu() = 0 at the sN
+    // pass's surface (al1 :4014-4017), zero flux elsewhere; the flux closure with bcN = 0 at the
+    // far end; the ghost node takes H's U[N] (U1 :4792 copies U, the H row, into the C row).
+    double *C = r.C;
+    double hprev = p.U[base], hcur = p.U[base + p.st];
+    double kkm = rich_KK(suction(0, hprev), r.kform, r.ksat);
+    double cprev = C[base], ccur = C[base + p.st];
+    double alc = r.pass == 0 ? 0.0 : 1.0, yc = 0.0;
+    const double alc1 = alc;
+    double cold_last = ccur;
+    for (int q = 1; q < Nl; ++q) {
+        const int64_t id = base + (int64_t)q * p.st;
+        const double hnext = p.U[id + p.st], cnext = C[id + p.st];
+        if (q == Nl - 1) cold_last = ccur;
+        const double kk = rich_KK(suction(q, hcur), r.kform, r.ksat);
+        const double dq = r.dL[q], dm = r.dL[q - 1];
+        const double dqq = __dmul_rn(dq, dq), dqm = __dmul_rn(dq, dm);
+        const double iqq = __ddiv_rn(1.0, dqq), iqm = __ddiv_rn(1.0, dqm);
+        const double A = __ddiv_rn(__dmul_rn(r.Dc, iqm), r.sigma);
+        const double B = __ddiv_rn(__dmul_rn(r.Dc, iqq), r.sigma);
+        const double R = __dadd_rn(__ddiv_rn(__dmul_rn(r.Dc, __dadd_rn(iqq, iqm)), r.sigma), r.lamR);
+        const double aln = __ddiv_rn(B, __dadd_rn(R, -__dmul_rn(A, alc)));
+        const double kc = __dmul_rn(kk, ccur), kcm = __dmul_rn(kkm, cprev);
+        const double fh = __dmul_rn(__ddiv_rn(1.0, r.sigma),
+                                    __dadd_rn(__dadd_rn(__ddiv_rn(__dmul_rn(kc, hnext), dqq),
+                                                        -__dmul_rn(__dadd_rn(__ddiv_rn(kc, dqq), __ddiv_rn(kcm, dqm)), hcur)),
+                                              __ddiv_rn(__dmul_rn(kcm, hprev), dqm)));
+        double om = __dadd_rn(__dadd_rn(-__dmul_rn(p.lam, ccur), 0.0), -fh);
+        if (r.nu != 0.0) {
+            const double fc = __dmul_rn(__ddiv_rn(r.nu, r.sigma),
+                                        __dadd_rn(__dadd_rn(__ddiv_rn(__dmul_rn(ccur, cnext), dqq),
+                                                            -__dmul_rn(__dadd_rn(__ddiv_rn(ccur, dqq), __ddiv_rn(cprev, dqm)), ccur)),
+                                                  __ddiv_rn(__dmul_rn(cprev, cprev), dqm)));
+            om = __dadd_rn(om, fc);
+        }
+        double svc = 0.0;
+        for (int k = 0; k < r.KSC; ++k) svc += __ldcg(r.partC + (int64_t)k * p.pstride + id);
+        om = __dadd_rn(om, svc);
+        yc = __dmul_rn(__ddiv_rn(aln, B), __dadd_rn(__dmul_rn(A, yc), -om));
+        r.al[(int64_t)q * L + line] = aln;
+        C[id] = yc;
+        alc = aln;
+        kkm = kk;
+        hprev = hcur; hcur = hnext;
+        cprev = ccur; ccur = cnext;
+    }
+    double cN;
+    if (fabs(yc) > 1e-15) cN = (fabs(1.0 - alc) > 1e-15) ? __ddiv_rn(yc + 0.0, 1.0 - alc) : cold_last;
+    else cN = (fabs(1.0 - alc) > 1e-15) ? 0.0 : cold_last;
+    C[base + (int64_t)Nl * p.st] = cN;
+    C[base + (int64_t)(Nl + 1) * p.st] = uN;
+    double c = cN;
+    for (int q = Nl - 1; q >= 1; --q) {
+        const int64_t id = base + (int64_t)q * p.st;
+        c = __dadd_rn(__dmul_rn(r.al[(int64_t)q * L + line], c), C[id]);
+        C[id] = c;
+    }
+    C[base] = __dadd_rn(__dmul_rn(alc1, c), 0.0);
 }
 
 // Segmented pass: SEGS threads (adjacent lanes) per line, each sweeping one segment of up to
@@ -516,6 +591,10 @@ struct fpde_lod3d {
     double rksat = 0.0;
     double *rsZ = nullptr, *rdL[3] = {nullptr, nullptr, nullptr}, *ral = nullptr;
     std::vector<double> rE;                   // evaporation rate per step
+    // salt concentration C (equation 1) beside H: state, snapshot, its history and partials
+    bool salt = false;
+    double snu = 0.0, ssig = 1.0, sDc = 0.0;
+    double *C = nullptr, *lastC = nullptr, *DC = nullptr, *partC = nullptr, *C0 = nullptr;
     // implicit space-fractional line solves (desc.space_frac): per pass the line-major operands
     // (per line A, B, Rlap, mc0, mc1, mc2, iw, Nl+1 values each) and the Toeplitz row
     bool sf = false;
@@ -580,6 +659,12 @@ static int lod_launch_pass(fpde_lod3d *L, cudaStream_t st, int pass, int64_t n, 
         r.sZ = L->rsZ; r.dL = L->rdL[pass]; r.al = L->ral;
         r.ksat = L->rksat; r.lamR = L->lamR; r.kform = L->rkform; r.pass = pass;
         r.E = L->rE[(size_t)std::min<int64_t>(n, (int64_t)L->rE.size() - 1)];
+        if (L->salt) {
+            r.C = L->C;
+            r.partC = pass == 2 ? L->partC : nullptr;
+            r.KSC = pass == 2 ? KS : 0;
+            r.nu = L->snu; r.sigma = L->ssig; r.Dc = L->sDc;
+        }
         k_lod_pass_rich<<<(unsigned)((a.lines + 127) / 128), 128, 0, st>>>(a, r);
     } else if (L->seglen[pass] > 0) {
         LodSegArgs sg;
@@ -672,6 +757,11 @@ static int lod_enqueue(fpde_lod3d *L, cudaStream_t st, int64_t n0, int steps, in
                 if ((rc = launch_l1_partial(st, L->D + t0 * L->P, L->P, (int)(n - t0), wt + t0, L->part, KS)))
                     return rc;
                 ++k;
+                if (L->salt) {                                           // C's own history, same weights
+                    if ((rc = launch_l1_partial(st, L->DC + t0 * L->P, L->P, (int)(n - t0), wt + t0, L->partC, KS)))
+                        return rc;
+                    ++k;
+                }
             }
             Drow = L->D + n * L->P;
         } else {
@@ -724,6 +814,10 @@ static int lod_enqueue(fpde_lod3d *L, cudaStream_t st, int64_t n0, int steps, in
                         : launch_append(st, L->U, L->last, Drow, L->G, L->P)))
             return rc;
         ++k;
+        if (L->salt) {
+            if ((rc = launch_append(st, L->C, L->lastC, L->DC + n * L->P, L->G, L->P))) return rc;
+            ++k;
+        }
     }
     *nk = k;
     return FPDE_OK;
@@ -764,6 +858,7 @@ int fpde_lod3d_destroy(fpde_lod3d *L)
         dev_free(L->sfT[q]);
     }
     dev_free(L->sf_iters);
+    for (double *p : {L->C, L->lastC, L->DC, L->partC, L->C0}) dev_free(p);
     dev_free(L->rsZ);
     dev_free(L->ral);
     delete L;
@@ -789,6 +884,11 @@ int fpde_lod3d_create(fpde_ctx *ctx, const fpde_lod3d_desc *desc, const double *
         FPDE_CHECK_ARG(d.series_terms == 0, "richards: no series expansion");
         FPDE_CHECK_ARG(d.M <= d.sN + 1 && d.K <= d.sN + 1,
                        "richards: M and K at most sN + 1 (suctions index sZ by positions along every pass)");
+        if (rich->salt_c0) {
+            FPDE_CHECK_ARG(d.precision == FPDE_PREC_FP64, "richards salt: FP64 path only");
+            FPDE_CHECK_ARG(std::isfinite(rich->salt_nu) && rich->salt_sigma > 0.0 && std::isfinite(rich->salt_D),
+                           "richards salt: nu, sigma > 0 and D required");
+        }
     }
     const fpde_space_frac *sfd = d.space_frac;
     if (sfd) {
@@ -916,6 +1016,20 @@ int fpde_lod3d_create(fpde_ctx *ctx, const fpde_lod3d_desc *desc, const double *
             fail = dev_alloc((void **)&L->rdL[pass], (size_t)(dims[pass] + 2) * sizeof(double)) ||
                    cudaMemcpy(L->rdL[pass], rich->dL[pass], (size_t)(dims[pass] + 2) * sizeof(double),
                               cudaMemcpyHostToDevice) != cudaSuccess;
+        }
+        if (!fail && rich->salt_c0) {
+            L->salt = true;
+            L->snu = rich->salt_nu; L->ssig = rich->salt_sigma; L->sDc = rich->salt_D;
+            fail = dev_alloc((void **)&L->C, pbytes) || dev_alloc((void **)&L->lastC, pbytes) ||
+                   dev_alloc((void **)&L->C0, pbytes) || dev_alloc((void **)&L->DC, (size_t)L->max_steps * pbytes) ||
+                   dev_alloc((void **)&L->partC, (size_t)KS_MAX * pbytes);
+            if (!fail) {
+                cudaMemset(L->C0, 0, pbytes);
+                fail = cudaMemcpy(L->C0, rich->salt_c0, gbytes, cudaMemcpyHostToDevice) != cudaSuccess ||
+                       cudaMemcpy(L->C, L->C0, pbytes, cudaMemcpyDeviceToDevice) != cudaSuccess ||
+                       cudaMemcpy(L->lastC, L->C0, pbytes, cudaMemcpyDeviceToDevice) != cudaSuccess ||
+                       cudaMemset(L->DC, 0, (size_t)L->max_steps * pbytes) != cudaSuccess;
+            }
         }
         fail = fail || dev_alloc((void **)&L->rsZ, (size_t)(d.sN + 2) * sizeof(double)) ||
                cudaMemcpy(L->rsZ, rich->sZ, (size_t)(d.sN + 2) * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess ||
@@ -1121,6 +1235,19 @@ int fpde_lod3d_get_state(fpde_lod3d *L, double *u, int on_device)
     return ctx_check_flags(L->ctx, "lod3d");
 }
 
+int fpde_lod3d_get_concentration(fpde_lod3d *L, double *c, int on_device)
+{
+    clear_error();
+    FPDE_CHECK_ARG(L && c, "null argument");
+    if (!L->salt) return set_error(FPDE_ERR_ARG, "lod3d: no salt concentration (richards.salt_c0 not given)");
+    int rc = ctx_enter(L->ctx);
+    if (rc) return rc;
+    FPDE_CUDA(cudaMemcpyAsync(c, L->C, L->G * sizeof(double),
+                              on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, L->ctx->stream));
+    FPDE_CUDA(cudaStreamSynchronize(L->ctx->stream));
+    return ctx_check_flags(L->ctx, "lod3d");
+}
+
 int fpde_lod3d_reset(fpde_lod3d *L, const double *u0, int on_device)
 {
     clear_error();
@@ -1132,6 +1259,10 @@ int fpde_lod3d_reset(fpde_lod3d *L, const double *u0, int on_device)
     FPDE_CUDA(cudaMemcpyAsync(L->last, u0, L->G * sizeof(double), kind, L->ctx->stream));
     if (L->series)                                   // an empty history: the moments start at zero
         FPDE_CUDA(cudaMemsetAsync(L->H, 0, (size_t)L->series * L->P * sizeof(double), L->ctx->stream));
+    if (L->salt) {                                   // the salt field starts again from its initial grid
+        FPDE_CUDA(cudaMemcpyAsync(L->C, L->C0, L->P * sizeof(double), cudaMemcpyDeviceToDevice, L->ctx->stream));
+        FPDE_CUDA(cudaMemcpyAsync(L->lastC, L->C0, L->P * sizeof(double), cudaMemcpyDeviceToDevice, L->ctx->stream));
+    }
     if (!on_device) FPDE_CUDA(cudaStreamSynchronize(L->ctx->stream));
     L->n_done = 0;
     return FPDE_OK;

@@ -287,6 +287,15 @@ typedef struct fpde_richards {
     const double *evaporation;  /* host, evaporation rate E of every step (Ev * day_night_coef);
                                    step n uses row min(n, evaporation_rows-1) */
     int evaporation_rows;
+    /* Salt concentration C (3D LOD only, FPDE_PREC_FP64; the reference's is_c: equation 1): with
+     * salt_c0 (the initial grid) every line of every pass also solves C after H, as calc_step does
+     * (:5270-5278): C's coefficients D/sigma over the steps (A_/B/R :3099-3136), the H-driven
+     * transport div(K C grad H)/sigma with the new H and chemical osmosis (nu/sigma) in C's
+     * right-hand side, chemical osmosis nu in H's (Om1 :4175-4229), C's own L1 history; C is
+     * Dirichlet Cu() = 0 at the surface (no irrigation), zero-flux elsewhere. The reference's
+     * temperature equation (is_t) is not available: its 3D set-up stops on a null row (:3640). */
+    const double *salt_c0;
+    double salt_nu, salt_sigma, salt_D;   /* nu, sigma, D of the reference (:3515-3518) */
 } fpde_richards;
 
 
@@ -506,6 +515,8 @@ int fpde_lod3d_reset(fpde_lod3d *lod, const double *u0, int on_device);
 /* End-to-end call: upload u0 from host, run `steps`, download the grid to host. */
 int fpde_lod3d_solve_host(fpde_lod3d *lod, const double *u0_host, int steps, double *u_out_host);
 int fpde_lod3d_steps_done(const fpde_lod3d *lod, int64_t *n);
+/* With richards.salt_c0: the salt concentration grid out. */
+int fpde_lod3d_get_concentration(fpde_lod3d *lod, double *c, int on_device);
 /* With space_frac: the solver iterations of every line solve since creation (0 otherwise). */
 int fpde_lod3d_sf_iterations(fpde_lod3d *lod, int64_t *iters);
 

@@ -136,3 +136,52 @@ def test_richards_line_split_vs_fp64(ctx, kform):
     errs = [relmax(x, y) for x, y in zip(b, a)]
     print(f"Richards line k_form {kform}, 256 steps, split vs FP64 at 8 checkpoints: max {max(errs):.2e}")
     assert max(errs) <= 1e-7
+
+
+def _salt_lod(ctx, g, steps=None):
+    import fpde_hpc_gb300 as fp
+    dims = (int(g["sN"]), int(g["M"]), int(g["K"]))
+    steps = steps or len(g["tau"])
+    rich = dict(k_form=int(g["k_form"]), k_sat=g["k_sat"], sZ=g["sZ"], dL=(g["sdL"], g["dLx"], g["dLy"]),
+                evaporation=g["E"], c0=g["C0"], nu=g["nu"], sigma=g["sigma"], D=g["D"])
+    return fp.Lod3D(ctx, dims, g["alpha"], g["tau"][0], g["Da"], None, None, None, g["U0"], steps, richards=rich)
+
+
+def test_richards_salt_lod_replays_reference_run(ctx):
+    """The reference's run with the salt concentration (equation 1 beside H on every line: chemical
+    osmosis in H, the H-driven transport and osmosis in C, C's own history; 6^3 cells, 24 steps):
+    H and C at every level within 1e-12 of the reference's (device and host pow differ by an ulp)."""
+    g = fgv.load(golden_path("fpde_richards_ct"))
+    lod = _salt_lod(ctx, g)
+    wu = wc = 0.0
+    for n in range(len(g["tau"])):
+        lod.run(1)
+        wu = max(wu, relmax(lod.state(), g["U"][n]))
+        wc = max(wc, relmax(lod.concentration(), g["C"][n]))
+    lod.close()
+    print(f"Richards with salt: H {wu:.2e}, C {wc:.2e} vs the reference's run")
+    assert wu <= 1e-12 and wc <= 1e-12
+
+
+def test_richards_salt_one_call_reset_and_errors(ctx):
+    """One call equals step by step; a reset restores the salt field; the options the salt field does
+    not support are refused."""
+    import fpde_hpc_gb300 as fp
+    g = fgv.load(golden_path("fpde_richards_ct"))
+    steps = len(g["tau"])
+    lod = _salt_lod(ctx, g)
+    lod.run(steps)
+    u1, c1 = lod.state(), lod.concentration()
+    lod.reset(g["U0"])
+    np.testing.assert_array_equal(lod.concentration(), g["C0"])
+    lod.run(steps)
+    np.testing.assert_array_equal(lod.state(), u1)
+    np.testing.assert_array_equal(lod.concentration(), c1)
+    lod.close()
+    assert relmax(c1, g["C"][-1]) <= 1e-12
+    dims = (int(g["sN"]), int(g["M"]), int(g["K"]))
+    rich = dict(k_form=1, k_sat=g["k_sat"], sZ=g["sZ"], dL=(g["sdL"], g["dLx"], g["dLy"]), evaporation=g["E"],
+                c0=g["C0"], nu=g["nu"], sigma=g["sigma"], D=g["D"])
+    with pytest.raises(fp.FpdeError):           # the salt field runs on the FP64 path only
+        fp.Lod3D(ctx, dims, g["alpha"], g["tau"][0], g["Da"], None, None, None, g["U0"], 70, richards=rich,
+                 precision=3)
