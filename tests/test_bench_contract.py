@@ -17,6 +17,7 @@ CASES = [
     ["--workload", "config5", "--nodes", "6", "--time-steps", "64"],
     ["--workload", "sum2", "--nodes", "24"],
     ["--workload", "weights", "--time-steps", "256"],
+    ["--workload", "sf3d", "--nodes", "12", "--time-steps", "8"],
 ]
 
 
