@@ -43,7 +43,7 @@ namespace fpde {
 
 struct LodPassArgs {
     double *U;
-    const double *A, *g, *al;        // (Nl+1) x lines, pass-line-major
+    const double *A, *g, *al;        // (Nl+1) x lines, pass-line-major: A holds gA = g A_
     const double *part;              // history partials [KS][pstride] (K pass), or KS = 0
     int KS;
     int64_t pstride;
@@ -92,8 +92,11 @@ __global__ void __launch_bounds__(128) k_lod_pass(LodPassArgs p)
             const int q = q0 + t;
             if (q < Nl) {
                 if (q == Nl - 1) uold_last = uu[t];
-                const double om = (-(p.lam * uu[t]) + rr[t]) + ss[t];    // Om1 :4191, :4267
-                y = gg[t] * (aa[t] * y - om);
+                // y = g (A y - Om) with Om = -(lam u) + Rp + S (Om1 :4191, :4267), as gA y + g (-Om)
+                double mo = p.lam * uu[t];                               // -Om, term by term
+                if (p.rp) mo -= rr[t];
+                if (p.KS) mo -= ss[t];
+                y = fma(aa[t], y, gg[t] * mo);
                 p.U[base + (int64_t)q * p.st] = y;
             }
         }
@@ -350,8 +353,10 @@ __global__ void __launch_bounds__(128, SEGLEN <= 16 ? 5 : 4) k_lod_pass_seg(LodP
 #pragma unroll
         for (int t = 0; t < LSB; ++t) {
             if (q0 + t0 + t < q1) {
-                const double om = (-(p.lam * uu[t]) + rr[t]) + ss[t];    // Om1 :4191, :4267
-                y = gg[t] * (aa[t] * y - om);
+                double mo = p.lam * uu[t];                               // -Om (Om1 :4191, :4267)
+                if (p.rp) mo -= rr[t];
+                if (p.KS) mo -= ss[t];
+                y = fma(aa[t], y, gg[t] * mo);                           // g (A y - Om) as gA y + g (-Om)
             }
             yv[t0 + t] = y;
         }
@@ -1094,7 +1099,7 @@ int fpde_lod3d_create(fpde_ctx *ctx, const fpde_lod3d_desc *desc, const double *
                 Al = Bq / (R - Aq * Al);                                           // Al[q+1]
                 hal[(size_t)q * lines + line] = Al;
                 hg[(size_t)q * lines + line] = Al / Bq;
-                hA[(size_t)q * lines + line] = Aq;
+                hA[(size_t)q * lines + line] = (Al / Bq) * Aq;                      // gA = g A
             }
         }
         fail = dev_alloc((void **)&L->cA[pass], cnt * sizeof(double)) ||
@@ -1118,7 +1123,7 @@ int fpde_lod3d_create(fpde_ctx *ctx, const fpde_lod3d_desc *desc, const double *
                     double pr = 1.0;
                     for (int q = q0; q < q1; ++q) {
                         const size_t o = (size_t)q * lines + line;
-                        pr *= hg[o] * hA[o];                               // prefix product of a = g A
+                        pr *= hA[o];                                       // prefix product of a = g A
                         cf[q - q0] = pr;
                     }
                     hPF[(size_t)line * SG + sgi] = pr;

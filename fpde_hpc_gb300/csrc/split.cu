@@ -172,30 +172,41 @@ __device__ __forceinline__ int exp_of_maxbits(unsigned long long mbits)
     return p < -127 ? -127 : (p > 127 ? 127 : p);
 }
 
-// One thread per node: the node's 64 increments of the finished block (time-major ring: the
-// threads of a warp read consecutive nodes of one row). All 64 are loaded at once (the ring was
-// just written and sits in L2) and kept in registers for both passes.
-__global__ void __launch_bounds__(128) k_convert3(const double *__restrict__ ring, int64_t P, int64_t nvalid,
+// Four adjacent lanes per node, each with 16 of the node's 64 increments of the finished block
+// (time-major ring: for each row the lanes of a warp read eight consecutive nodes). The block
+// exponent is the maximum over the four lanes (shuffles); each lane then writes its 16 columns of
+// the three slices. Sixteen values per thread keep the registers low and many nodes' loads in
+// flight (one thread per node with all 64 values had left the kernel latency-bound).
+constexpr int CONV_LANES = 4, CONV_ROWS = 64 / CONV_LANES;
+__global__ void __launch_bounds__(256) k_convert3(const double *__restrict__ ring, int64_t P, int64_t nvalid,
                                                   uint16_t *__restrict__ h0, uint16_t *__restrict__ h1,
                                                   uint16_t *__restrict__ h2, int64_t ld, int64_t col0,
                                                   int8_t *__restrict__ pA, int64_t ldp, int blk)
 {
-    const int64_t node = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (node >= nvalid) return;
-    const unsigned long long *src = (const unsigned long long *)ring + node;
-    unsigned long long v[64];
-#pragma unroll
-    for (int r = 0; r < 64; ++r) v[r] = __ldcg(src + (int64_t)r * P);
+    const int64_t gt = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t node = gt / CONV_LANES;
+    const int part = (int)(gt % CONV_LANES);
+    const bool live = node < nvalid;
+    const int r0 = part * CONV_ROWS;
+    unsigned long long v[CONV_ROWS];
     unsigned long long mb = 0;
+    const unsigned long long *src = (const unsigned long long *)ring + (live ? node : 0);
 #pragma unroll
-    for (int r = 0; r < 64; ++r) {
+    for (int r = 0; r < CONV_ROWS; ++r) {
+        v[r] = live ? __ldcg(src + (int64_t)(r0 + r) * P) : 0ull;
         const unsigned long long m0 = v[r] & 0x7FFFFFFFFFFFFFFFull;
         mb = m0 > mb ? m0 : mb;
     }
-    const int pe = exp_of_maxbits(mb);
-    pA[node * ldp + blk] = (int8_t)pe;
 #pragma unroll
-    for (int g = 0; g < 8; ++g) {
+    for (int o = 1; o < CONV_LANES; o <<= 1) {
+        const unsigned long long other = __shfl_xor_sync(0xffffffffu, mb, o, CONV_LANES);
+        mb = other > mb ? other : mb;
+    }
+    if (!live) return;
+    const int pe = exp_of_maxbits(mb);
+    if (part == 0) pA[node * ldp + blk] = (int8_t)pe;
+#pragma unroll
+    for (int g = 0; g < CONV_ROWS / 8; ++g) {
         uint16_t a[8], b[8], c[8];
 #pragma unroll
         for (int k = 0; k < 8; ++k)
@@ -207,9 +218,10 @@ __global__ void __launch_bounds__(128) k_convert3(const double *__restrict__ rin
         vb.z = b[4] | ((uint32_t)b[5] << 16); vb.w = b[6] | ((uint32_t)b[7] << 16);
         vc.x = c[0] | ((uint32_t)c[1] << 16); vc.y = c[2] | ((uint32_t)c[3] << 16);
         vc.z = c[4] | ((uint32_t)c[5] << 16); vc.w = c[6] | ((uint32_t)c[7] << 16);
-        *(uint4 *)(h0 + node * ld + col0 + 8 * g) = va;
-        *(uint4 *)(h1 + node * ld + col0 + 8 * g) = vb;
-        *(uint4 *)(h2 + node * ld + col0 + 8 * g) = vc;
+        const int64_t o = node * ld + col0 + r0 + 8 * g;
+        *(uint4 *)(h0 + o) = va;
+        *(uint4 *)(h1 + o) = vb;
+        *(uint4 *)(h2 + o) = vc;
     }
 }
 
@@ -251,8 +263,9 @@ int launch_block_prep3(cudaStream_t st, const SplitPrep3 &p, int64_t n0, bool we
 {
     if (n0 >= 64) {
         const int blk = (int)(n0 / 64) - 1;
-        k_convert3<<<(unsigned)((p.nvalid + 127) / 128), 128, 0, st>>>(p.ring, p.P, p.nvalid, p.hist[0], p.hist[1],
-                                                                       p.hist[2], p.ld, n0 - 64, p.pA, p.ldp, blk);
+        const int64_t threads = p.nvalid * CONV_LANES;
+        k_convert3<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(p.ring, p.P, p.nvalid, p.hist[0], p.hist[1],
+                                                                      p.hist[2], p.ld, n0 - 64, p.pA, p.ldp, blk);
         FPDE_LAUNCHED(1);
     }
     if (weights && n0 / 64 + (p.n_grp > 0 ? p.n_grp : 1) - 1 > 0) {
