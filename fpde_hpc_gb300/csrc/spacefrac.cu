@@ -30,11 +30,7 @@ struct SfVec {
     double *Tm, *m0, *m1, *m2, *c0, *c1, *c2, *iw, *rs, *B, *x, *r, *q0, *g0, *g1, *w0, *w1, *u, *Au, *bt;
 };
 constexpr int SF_NVEC = 20;
-constexpr int SF_THREADS = 128;
-// Threads per line CTA: a thread takes a pair of rows of the product, so n/2 threads carry it;
-// lines of up to 128 intervals run 64 threads and twice as many lines per SM (more independent
-// chains for the FP64 pipe), longer lines 128.
-static inline int sf_threads(int n) { return n <= 128 ? 64 : SF_THREADS; }
+constexpr int SF_THREADS = 128;   // (64-thread CTAs for short lines measured no faster on 64^3)
 constexpr uint64_t SF_TIME_LIMIT_NS = 10ull * 1000000000ull;   // per line solve
 
 __device__ __forceinline__ SfVec sf_carve(double *sm, int m)
@@ -357,7 +353,7 @@ int sf_prepare()
 int launch_lod_pass_sf(cudaStream_t st, const LodSfArgs &a)
 {
     const size_t smem = sf_smem_bytes(a.Nl);
-    k_lod_pass_sf<<<(unsigned)a.lines, sf_threads(a.Nl), smem, st>>>(a);
+    k_lod_pass_sf<<<(unsigned)a.lines, SF_THREADS, smem, st>>>(a);
     FPDE_LAUNCHED(1);
     return FPDE_OK;
 }
@@ -411,7 +407,7 @@ static int sf_batch(fpde_ctx *ctx, int lines, int n, const double *mat, const do
     }
     a.iters = d_it;
     if (!fail) {
-        k_sf_batch<<<(unsigned)lines, sf_threads(n), smem, st>>>(a, solve);
+        k_sf_batch<<<(unsigned)lines, SF_THREADS, smem, st>>>(a, solve);
         cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) rc = set_error(FPDE_ERR_CUDA, "space-fractional batch launch: %s", cudaGetErrorString(e));
         else count_launches(1);
