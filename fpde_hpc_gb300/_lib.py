@@ -48,7 +48,8 @@ class Lod3dDesc(C.Structure):
                 ("left_kind", c_int * 3), ("right_kind", c_int * 3), ("dLN", c_dbl * 3), ("precision", c_int),
                 ("max_steps", c_int), ("lag_weights", c_vp), ("source", c_vp), ("source_rows", c_int),
                 ("bc", c_vp), ("bc_rows", c_int), ("restrict_eps", c_dbl), ("series_terms", c_int),
-                ("richards", C.POINTER(Richards)), ("space_frac", C.POINTER(SpaceFrac))]
+                ("richards", C.POINTER(Richards)), ("time_steps", c_vp), ("weight_rows", c_vp),
+                ("kernel_power", c_dbl), ("space_frac", C.POINTER(SpaceFrac))]
 
 
 class ColumnDesc(C.Structure):

@@ -404,12 +404,16 @@ class Lod3D:
 
     def __init__(self, ctx, dims, alpha, tau, Da, coefA, coefB, coefRlap, u0, max_steps, left_kind=(0, 0, 0),
                  right_kind=(0, 0, 0), dLN=(0.0, 0.0, 0.0), source=None, bc=None, lag_weights=None,
-                 precision=FP64, restrict_eps=0.0, series_terms=0, richards=None, space_frac=None):
+                 precision=FP64, restrict_eps=0.0, series_terms=0, richards=None, space_frac=None,
+                 time_steps=None, weight_rows=None, kernel_power=0.0):
         """richards: optional dict(k_form, k_sat, sZ, dL=(sdL, dLx, dLy), evaporation) - the
         reference's Richards problem, coefficients formed from the grid every step (coefA/B/Rlap
         may then be None); with c0 (and nu, sigma, D) also the salt concentration (equation 1).
         space_frac: optional dict(space_der, tol, max_iter, Tm=(3 rows), mc=(3 passes x 3 grids),
-        iw=(3 grids)) - the reference's implicit space-fractional line solves (impl 2)."""
+        iw=(3 grids)) - the reference's implicit space-fractional line solves (impl 2).
+        time_steps: optional tau_n of every step (variable steps); weight_rows: optional
+        (max_steps, max_steps+1) matrix of the steps' kb_3_cache rows with kkk0 on the diagonal
+        (else computed for g(t) = t^kernel_power)."""
         sN, M, K = dims
         self.ctx, self.dims = ctx, dims
         self.shape = (K + 2, M + 2, sN + 2)
@@ -457,6 +461,19 @@ class Lod3D:
                 r.salt_nu, r.salt_sigma, r.salt_D = (float(richards[k]) for k in ("nu", "sigma", "D"))
             keep.append(r)
             d.richards = C.pointer(r)
+        if time_steps is not None:
+            ts = np.ascontiguousarray(time_steps, dtype=np.float64)
+            if ts.size < max_steps:
+                raise ValueError("time_steps needs max_steps values")
+            keep.append(ts)
+            d.time_steps = ts.ctypes.data
+            d.kernel_power = float(kernel_power)
+            if weight_rows is not None:
+                wr = np.ascontiguousarray(weight_rows, dtype=np.float64)
+                if wr.shape != (max_steps, max_steps + 1):
+                    raise ValueError("weight_rows needs shape (max_steps, max_steps + 1)")
+                keep.append(wr)
+                d.weight_rows = wr.ctypes.data
         if space_frac is not None:
             f = SpaceFrac(space_der=int(space_frac.get("space_der", 0)), tol=float(space_frac.get("tol", 1e-9)),
                           max_iter=int(space_frac.get("max_iter", 5000)))

@@ -26,6 +26,7 @@
 // numbered with i fastest, so their state accesses are coalesced too; the sN pass walks
 // along the contiguous axis and relies on L1 for reuse of each line's cache lines.
 // The whole run is captured once into a CUDA graph and replayed.
+#include <algorithm>
 #include <climits>
 #include <map>
 #include <vector>
@@ -133,6 +134,60 @@ __global__ void __launch_bounds__(128) k_lod_pass(LodPassArgs p)
         }
     }
     p.U[base] = fma(__ldg(p.al + line), u, g0);                   // Al[1] U[1] + Bt[1]
+}
+
+// Variable steps (the reference's varT): the local term Da kkk0_n / tau_n of R changes every step,
+// so one thread per line runs al1 / bt1 / U1 (:4002-4027, :4585-4590, :4683-4724) from the raw
+// coefficients A_, B, Rlap (pass-line-major) and the step's lamR, in the reference's order.
+struct LodVarArgs {
+    const double *A, *B, *Rl;        // (Nl+1) x lines, pass-line-major
+    double *al;                      // scratch: Al[q+1] at q * lines + line
+    double lamR;
+};
+
+__global__ void __launch_bounds__(128) k_lod_pass_var(LodPassArgs p, LodVarArgs v)
+{
+    const int line = blockIdx.x * blockDim.x + threadIdx.x;
+    if (line >= p.lines) return;
+    const int a = line % p.n1, b = line / p.n1;
+    const int64_t base = (int64_t)(1 + a) * p.s1 + (int64_t)(1 + b) * p.s2;
+    const int Nl = p.Nl, L = p.lines;
+    const double g0 = p.bc ? p.bc[base] : 0.0;
+    const double al1 = p.lkind == FPDE_BC_FLUX ? 1.0 : 0.0;             // Al[1]
+    double al = al1, y = g0, uold_last = 0.0;
+    for (int q = 1; q < Nl; ++q) {
+        const int64_t id = base + (int64_t)q * p.st;
+        const double u = p.U[id];
+        if (q == Nl - 1) uold_last = u;
+        const int64_t o = (int64_t)q * L + line;
+        const double A = __ldg(v.A + o), B = __ldg(v.B + o), R = __dadd_rn(__ldg(v.Rl + o), v.lamR);
+        const double aln = __ddiv_rn(B, __dsub_rn(R, __dmul_rn(A, al)));   // Al[q+1]
+        double sv = 0.0;
+        for (int k = 0; k < p.KS; ++k) sv += __ldcg(p.part + (int64_t)k * p.pstride + id);
+        const double om = __dadd_rn(__dadd_rn(-__dmul_rn(p.lam, u), p.rp ? __ldg(p.rp + id) : 0.0), sv);
+        y = __dmul_rn(__ddiv_rn(aln, B), __dsub_rn(__dmul_rn(A, y), om));   // Bt[q+1]
+        v.al[o] = aln;
+        p.U[id] = y;
+        al = aln;
+    }
+    const double gN = p.bc ? p.bc[base + (int64_t)Nl * p.st] : 0.0;
+    double uN;
+    if (p.rkind == FPDE_BC_DIRICHLET) {
+        uN = gN;
+    } else if (fabs(y) > 1e-15) {
+        uN = (fabs(1.0 - al) > 1e-15) ? __ddiv_rn(__dadd_rn(y, __dmul_rn(gN, p.dLN)), 1.0 - al) : uold_last;
+    } else {
+        uN = (fabs(1.0 - al) > 1e-15) ? 0.0 : uold_last;
+    }
+    p.U[base + (int64_t)Nl * p.st] = uN;
+    p.U[base + (int64_t)(Nl + 1) * p.st] = uN;                          // ghost copy (U1 :4792)
+    double u = uN;
+    for (int q = Nl - 1; q >= 1; --q) {
+        const int64_t id = base + (int64_t)q * p.st;
+        u = __dadd_rn(__dmul_rn(v.al[(int64_t)q * L + line], u), p.U[id]);
+        p.U[id] = u;
+    }
+    p.U[base] = __dadd_rn(__dmul_rn(al1, u), g0);                       // Al[1] U[1] + Bt[1]
 }
 
 // The reference's Richards problem (analytic_test 0): every line's coefficients change with the
@@ -596,6 +651,14 @@ struct fpde_lod3d {
     double rksat = 0.0;
     double *rsZ = nullptr, *rdL[3] = {nullptr, nullptr, nullptr}, *ral = nullptr;
     std::vector<double> rE;                   // evaporation rate per step
+    // variable steps: per-step local terms, the scaled weight rows (row n: Da kb_n[t] / tau_t) and
+    // the raw coefficients of every pass (the alpha recurrence is formed on the fly)
+    bool vart = false;
+    std::vector<double> lamv, lamRv;
+    int64_t wld = 0;
+    double *wrows = nullptr;
+    double *vA[3] = {nullptr, nullptr, nullptr}, *vB[3] = {nullptr, nullptr, nullptr},
+           *vR[3] = {nullptr, nullptr, nullptr}, *val = nullptr;
     // salt concentration C (equation 1) beside H: state, snapshot, its history and partials
     bool salt = false;
     double snu = 0.0, ssig = 1.0, sDc = 0.0;
@@ -638,11 +701,19 @@ static int lod_launch_pass(fpde_lod3d *L, cudaStream_t st, int pass, int64_t n, 
     a.pstride = L->P;
     a.rp = (pass == 2 && L->rp) ? L->rp + (n < L->rp_rows ? n : L->rp_rows - 1) * L->G : nullptr;
     a.bc = L->bc ? L->bc + (n < L->bc_rows ? n : L->bc_rows - 1) * L->G : nullptr;
-    a.lam = L->lam;
+    a.lam = L->vart ? L->lamv[(size_t)n] : L->lam;
     a.lkind = L->d.left_kind[pass];
     a.rkind = L->d.right_kind[pass];
     a.dLN = L->d.dLN[pass];
     if (a.lines <= 0) return FPDE_OK;
+    if (L->vart) {
+        LodVarArgs v;
+        v.A = L->vA[pass]; v.B = L->vB[pass]; v.Rl = L->vR[pass]; v.al = L->val;
+        v.lamR = L->lamRv[(size_t)n];
+        k_lod_pass_var<<<(unsigned)((a.lines + 127) / 128), 128, 0, st>>>(a, v);
+        FPDE_LAUNCHED(1);
+        return FPDE_OK;
+    }
     if (L->sf) {
         LodSfArgs f;
         int n2s;
@@ -758,7 +829,8 @@ static int lod_enqueue(fpde_lod3d *L, cudaStream_t st, int64_t n0, int steps, in
             const int64_t t0 = n > L->max_lag ? n - L->max_lag : 0;    // oldest row of the window
             if (n - t0 >= 1) {
                 KS = choose_splits((int)(n - t0), L->P);
-                const double *wt = L->wrev + (L->max_steps - n);     // wt[t] = w[n - t]
+                const double *wt = L->vart ? L->wrows + n * L->wld     // variable steps: row n
+                                           : L->wrev + (L->max_steps - n);     // wt[t] = w[n - t]
                 if ((rc = launch_l1_partial(st, L->D + t0 * L->P, L->P, (int)(n - t0), wt + t0, L->part, KS)))
                     return rc;
                 ++k;
@@ -864,6 +936,13 @@ int fpde_lod3d_destroy(fpde_lod3d *L)
     }
     dev_free(L->sf_iters);
     for (double *p : {L->C, L->lastC, L->DC, L->partC, L->C0}) dev_free(p);
+    for (int q = 0; q < 3; ++q) {
+        dev_free(L->vA[q]);
+        dev_free(L->vB[q]);
+        dev_free(L->vR[q]);
+    }
+    dev_free(L->val);
+    dev_free(L->wrows);
     dev_free(L->rsZ);
     dev_free(L->ral);
     delete L;
@@ -905,6 +984,17 @@ int fpde_lod3d_create(fpde_ctx *ctx, const fpde_lod3d_desc *desc, const double *
                        "space_frac: lines longer than FPDE_SF_MAX_N intervals");
         for (int q = 0; q < 3; ++q)
             FPDE_CHECK_ARG(sfd->Tm[q] && sfd->mc[q] && sfd->iw[q], "space_frac: Tm, mc and iw of every pass required");
+    }
+    const bool vart = d.time_steps != nullptr;
+    if (vart) {
+        FPDE_CHECK_ARG(d.precision == FPDE_PREC_FP64, "time_steps: FP64 path only (per-step weight rows)");
+        FPDE_CHECK_ARG(!d.lag_weights && d.series_terms == 0 && d.restrict_eps == 0.0 && !rich && !sfd,
+                       "time_steps: not with lag_weights, series, restricted summing, richards or space_frac");
+        for (int n = 0; n < d.max_steps; ++n)
+            FPDE_CHECK_ARG(d.time_steps[n] > 0.0 && std::isfinite(d.time_steps[n]), "time_steps must be positive");
+        FPDE_CHECK_ARG(std::isfinite(d.kernel_power) && d.kernel_power >= 0.0, "kernel_power must be >= 0");
+    } else {
+        FPDE_CHECK_ARG(!d.weight_rows, "weight_rows needs time_steps");
     }
     FPDE_CHECK_ARG(d.sN >= 2 && d.M >= 2 && d.K >= 2, "every axis needs at least 2 intervals");
     FPDE_CHECK_ARG(d.lag_weights || (d.alpha > 0.0 && d.alpha < 1.0), "alpha must be in (0, 1)");
@@ -1073,9 +1163,63 @@ int fpde_lod3d_create(fpde_ctx *ctx, const fpde_lod3d_desc *desc, const double *
                    cudaMemcpy(L->sfT[pass], tm.data(), (size_t)m * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess;
         }
     }
+    if (!fail && vart) {
+        // weight rows of every step: the caller's (its kb_3_cache and kkk0), or fpde_weights_g on the
+        // accumulated time points; then the local terms Da kkk0_n / tau_n (Om1 :4191, R :3120) and the
+        // GEMV rows Da kb_n[t] / tau_t
+        L->vart = true;
+        const int S = d.max_steps;
+        const int64_t ld = (int64_t)S + 1;
+        L->wld = ld;
+        std::vector<double> W((size_t)S * ld, 0.0);
+        if (d.weight_rows) {
+            std::copy(d.weight_rows, d.weight_rows + (size_t)S * ld, W.begin());
+        } else {
+            std::vector<double> T((size_t)S + 1, 0.0);
+            for (int k = 0; k < S; ++k) T[k + 1] = T[k] + d.time_steps[k];
+            const double pw = d.kernel_power > 0.0 ? d.kernel_power : 1.0;
+            if (fpde_weights_g(ctx, pw, d.alpha, T.data(), 0, S - 1, W.data(), ld, 0) != FPDE_OK) fail = true;
+        }
+        L->lamv.assign(S, 0.0);
+        L->lamRv.assign(S, 0.0);
+        std::vector<double> Ws((size_t)S * ld, 0.0);
+        for (int n = 0; n < S; ++n) {
+            const double k0 = W[(size_t)n * ld + n], tn = d.time_steps[n];
+            L->lamv[n] = d.Da * (k0 / tn);
+            L->lamRv[n] = d.Da * k0 / tn;
+            for (int t = 0; t < n; ++t) Ws[(size_t)n * ld + t] = (d.Da * W[(size_t)n * ld + t]) / d.time_steps[t];
+        }
+        fail = fail || dev_alloc((void **)&L->wrows, Ws.size() * sizeof(double)) ||
+               cudaMemcpy(L->wrows, Ws.data(), Ws.size() * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess;
+        int64_t scratch = 0;
+        std::vector<double> h[3];
+        for (int pass = 0; pass < 3 && !fail; ++pass) {
+            int Nl, n1, n2;
+            int64_t s1, s2, stp;
+            pass_geometry(L, pass, &Nl, &n1, &n2, &s1, &s2, &stp);
+            const int lines = n1 * n2;
+            L->lines[pass] = lines;
+            const size_t cnt = (size_t)(Nl + 1) * lines;
+            scratch = std::max<int64_t>(scratch, (int64_t)cnt);
+            const double *src[3] = {coefA + (int64_t)pass * L->G, coefB + (int64_t)pass * L->G,
+                                    coefRlap + (int64_t)pass * L->G};
+            double **dst[3] = {&L->vA[pass], &L->vB[pass], &L->vR[pass]};
+            for (int r = 0; r < 3 && !fail; ++r) {
+                h[r].assign(cnt, 0.0);
+                for (int line = 0; line < lines; ++line) {
+                    const int a = line % n1, b = line / n1;
+                    const int64_t base = (int64_t)(1 + a) * s1 + (int64_t)(1 + b) * s2;
+                    for (int q = 1; q < Nl; ++q) h[r][(size_t)q * lines + line] = src[r][base + (int64_t)q * stp];
+                }
+                fail = dev_alloc((void **)dst[r], cnt * sizeof(double)) ||
+                       cudaMemcpy(*dst[r], h[r].data(), cnt * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess;
+            }
+        }
+        fail = fail || dev_alloc((void **)&L->val, (size_t)scratch * sizeof(double));
+    }
     // per-pass line coefficients, evaluated in the reference's order (al1 :4002-4027)
     std::vector<double> hA, hg, hal;
-    for (int pass = 0; pass < 3 && !fail && !rich && !sfd; ++pass) {
+    for (int pass = 0; pass < 3 && !fail && !rich && !sfd && !vart; ++pass) {
         int Nl, n1, n2;
         int64_t s1, s2, stp;
         pass_geometry(L, pass, &Nl, &n1, &n2, &s1, &s2, &stp);
@@ -1197,6 +1341,8 @@ int fpde_lod3d_create(fpde_ctx *ctx, const fpde_lod3d_desc *desc, const double *
     L->d.bc = nullptr;
     L->d.richards = nullptr;
     L->d.space_frac = nullptr;
+    L->d.time_steps = nullptr;
+    L->d.weight_rows = nullptr;
     *out = L;
     return FPDE_OK;
 }

@@ -495,6 +495,20 @@ typedef struct fpde_lod3d_desc {
     const fpde_richards *richards; /* optional: the Richards problem (coefficients from the solution
                                every step; coefA/B/Rlap, the boundary kinds and bc are then unused
                                and may be NULL; needs M, K <= sN + 1) */
+    const double *time_steps;   /* optional: variable steps (the reference's varT), tau_n of every step
+                                   (max_steps values; Time accumulated as Time[n+1] = Time[n] + tau_n).
+                                   The L1 weights are then a row per step (no Toeplitz structure): the
+                                   history is summed by the FP64 GEMV with row n, and the line
+                                   coefficients' local term Da kkk0_n / tau_n changes every step, so
+                                   the passes form the alpha recurrence on the fly (FPDE_PREC_FP64;
+                                   not with lag_weights, series, restricted summing, richards,
+                                   space_frac) */
+    const double *weight_rows;  /* optional with time_steps: the weights of every step as the caller's
+                                   time_summing uses them: row n (max_steps+1 values) holds
+                                   kb_3_cache[0..n-1] and kkk0 at column n (precalc_kb_3 :4069-4085,
+                                   init_time_step :3942-3949); NULL: computed by fpde_weights_g */
+    double kernel_power;        /* with time_steps and no weight_rows: g(t) = t^p of the generalized
+                                   Caputo kernel (func_in_kernel 1-3; 0 means p = 1) */
     const fpde_space_frac *space_frac; /* optional: implicit space-fractional line solves (impl 2);
                                coefA/B/Rlap are then the reference's A_/B/R with its space-fractional
                                local weights, every pass has a Dirichlet start, right_kind per pass */

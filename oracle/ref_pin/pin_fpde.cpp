@@ -557,6 +557,23 @@ int main(int argc, char **argv)
         run_richards(q, 2, 2, 2, 3, 3, 3, 0.6, 900.0, 40);
         return 0;
     }
+    if (argc >= 3 && strcmp(argv[1], "lod_vartau") == 0) {
+        /* the 3D LOD (6 x 4 x 8 cells, analytic problem 2, alpha 0.8) with variable steps, for the
+         * device time loop with per-step weight rows: g(t) = t (func_in_kernel 0) and the
+         * generalized kernel g(t) = t^1.5 (func_in_kernel 3) */
+        char q[4096];
+        std::vector<double> tv;
+        for (int n = 0; n < 24; n++) tv.push_back(2.5e-3 * (1.0 + 0.5 * sin(0.7 * n)));
+        snprintf(q, sizeof q, "%s/fpde_lod3d_vartau.fgv", argv[2]);
+        run_lod(q, 2, 2, 3, 2, 4, 0.8, tv, 1);
+        func_in_kernel = 3;
+        func_power = 1.5;
+        snprintf(q, sizeof q, "%s/fpde_lod3d_fk3_vartau.fgv", argv[2]);
+        run_lod(q, 2, 2, 3, 2, 4, 0.8, tv, 1);
+        func_in_kernel = 0;
+        func_power = 0.6;
+        return 0;
+    }
     if (argc >= 3 && strcmp(argv[1], "richards_ct") == 0) {
         char q[4096];
         snprintf(q, sizeof q, "%s/fpde_richards_ct.fgv", argv[2]);

@@ -399,3 +399,22 @@ def test_salt_coefficients_match_the_reference_formula():
                 vals = np.unique(want[tuple(sl)])
                 vals = vals[vals != 0]                   # nodes off the pass's lines hold 0
                 assert vals.size == 1 and vals[0] == got, (p, q)
+
+
+@pytest.mark.parametrize("name", ["fpde_lod3d_vartau", "fpde_lod3d_fk3_vartau"])
+def test_variable_step_lod_replays_reference_run(name):
+    """The reference's 3D LOD with variable steps (its varT step sequence, g(t) = t and the
+    generalized kernel t^1.5) replayed by the oracle from its recorded weight rows, bit for bit."""
+    g = fgv.load(golden_path(name))
+    dims = (int(g["sN"]), int(g["M"]), int(g["K"]))
+    cA, cB, cR = (np.stack([g[f"{k}_pass{p}"] for p in range(3)]) for k in ("coefA", "coefB", "coefRlap"))
+    U = g["U0"].copy()
+    steps = g["U"].shape[0]
+    hist = np.zeros((steps,) + U.shape)
+    kbo = g["kb_off"].astype(np.int64)
+    assert np.ptp(g["tau"]) > 0                           # the steps do vary
+    for n in range(steps):
+        kb = g["kb_flat"][kbo[n]:kbo[n + 1]]
+        oracle.lod_step_dirichlet(dims, U, hist, n, kb if n else np.zeros(1), g["tau"], float(g["Da"]),
+                                  float(g["kkk0"][n]), cA, cB, cR, g["Rp"][n], g["BC"][n])
+        assert np.array_equal(U, g["U"][n]), f"step {n}"
