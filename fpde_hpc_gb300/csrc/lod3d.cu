@@ -517,20 +517,23 @@ __global__ void __launch_bounds__(256) k_near_pre_ff(const float4 *__restrict__ 
             ff_add(h[u][1], l[u][1], f1.x, f1.y);
         }
     }
-    for (int r = 0; r < j0; ++r) {
-        const float4 v = __ldcg(ringf + (int64_t)r * P2 + i);
+    for (int r0 = 0; r0 < j0; r0 += NEAR_SUB) {          // j0 is a multiple of NEAR_SUB
+        float4 v[NEAR_SUB];                                // the sub-block's rows, loaded together
 #pragma unroll
-        for (int u = 0; u < NEAR_SUB; ++u) {
-            const float2 w = __ldg(wff + (j0 + u - r));
-            ff_fma(h[u][0], l[u][0], w, make_float2(v.x, v.y));
-            ff_fma(h[u][1], l[u][1], w, make_float2(v.z, v.w));
-        }
-        if ((r & 7) == 7) {
+        for (int q = 0; q < NEAR_SUB; ++q) v[q] = __ldcg(ringf + (int64_t)(r0 + q) * P2 + i);
+#pragma unroll
+        for (int q = 0; q < NEAR_SUB; ++q) {
 #pragma unroll
             for (int u = 0; u < NEAR_SUB; ++u) {
-                ff_renorm(h[u][0], l[u][0]);
-                ff_renorm(h[u][1], l[u][1]);
+                const float2 w = __ldg(wff + (j0 + u - r0 - q));
+                ff_fma(h[u][0], l[u][0], w, make_float2(v[q].x, v[q].y));
+                ff_fma(h[u][1], l[u][1], w, make_float2(v[q].z, v[q].w));
             }
+        }
+#pragma unroll
+        for (int u = 0; u < NEAR_SUB; ++u) {
+            ff_renorm(h[u][0], l[u][0]);
+            ff_renorm(h[u][1], l[u][1]);
         }
     }
 #pragma unroll
