@@ -579,11 +579,19 @@ __global__ void __launch_bounds__(256) k_near_history_ff(const float4 *__restric
         ff_renorm(h0, l0);
         ff_renorm(h1, l1);
     }
-    for (; r < j; ++r) {
-        const float4 v = __ldcg(ringf + (int64_t)r * P2 + i);
-        const float2 w = __ldg(wff + (j - r));
-        ff_fma(h0, l0, w, make_float2(v.x, v.y));
-        ff_fma(h1, l1, w, make_float2(v.z, v.w));
+    if (r < j) {                                           // the last (< 8) rows, loaded together
+        const int rem = j - r;
+        float4 v[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) v[u] = u < rem ? __ldcg(ringf + (int64_t)(r + u) * P2 + i) : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            if (u < rem) {
+                const float2 w = __ldg(wff + (j - r - u));
+                ff_fma(h0, l0, w, make_float2(v[u].x, v[u].y));
+                ff_fma(h1, l1, w, make_float2(v[u].z, v[u].w));
+            }
+        }
     }
     S[i] = make_double2(f2d_bits(h0) + f2d_bits(l0), f2d_bits(h1) + f2d_bits(l1));
 }
