@@ -322,6 +322,68 @@ static void run_richards(const char *path, int kform, int rpform, int bs, int nb
     printf("wrote %s (Richards k_form %d, %d steps, grid %dx%dx%d)\n", path, kform, steps, sN, _M, K);
 }
 
+/* The reference's known answer for its column (mode 3, BS 1, NB 3, M 3, K kc, analytic problem 2):
+ * the squared error against the exact solution that its run prints (analytic_compare
+ * :3277-3312), for a run too long to record step by step. Its inputs separate into space and
+ * time parts, so the record stays small: the K-pass source is S1(node) - p2(t) (Rp :2766-2795;
+ * S1 = Rp with Time = 0, where p2 vanishes; p2(n) read at one node) and every line-end value is
+ * V(node) + vt(t) (bc0/bcN = testF3d :3181-3231; vt(n) read at the sN line start, where V = 0;
+ * V from the first step). Also the final grid and the exact solution at the final time. */
+static void run_kat(const char *path, int kc, double alpha, double tau, int steps)
+{
+    set_dims(1, 3, 3, kc);
+    varT = 0; varZ = 0; varXY = 0;
+    implicit = 0; implicit3d = 0; rp_split_3d = 0; sum_alg = 0;
+    global_eps = 1e-15; global_eps2 = 1e-15;
+    FILE *lg = fopen("/dev/null", "w");
+    H_solver *s = new H_solver(2, 1, 5, 0, 1, alpha, 1.0, 0, 0, 0, 3, lg, 2);
+    size_t G = (size_t)(sN + 2) * (_M + 2) * (K + 2);
+    FgvWriter w(path);
+    w.scalar("sN", sN); w.scalar("M", _M); w.scalar("K", K);
+    w.scalar("alpha", alpha); w.scalar("Da", s->Da); w.scalar("tau", tau);
+    std::vector<uint64_t> gdims = {(uint64_t)(K + 2), (uint64_t)(_M + 2), (uint64_t)(sN + 2)};
+    w.put("U0", gdims, s->b_U);
+    std::vector<double> p2, vt, kkk0, rp0, bc0g, S1(G, 0.0);
+    for (int n = 0; n < steps; n++) {
+        s->calc_step(tau);
+        kkk0.push_back(s->kkk0);
+        if (n == 0) {
+            record_coefs(s, w);
+            std::vector<double> bcv;
+            record_step_inputs(s, rp0, bcv);
+            bc0g = bcv;
+            const double t_saved = s->Time[s->tstep];             /* S1: the source at Time 0 */
+            s->Time[s->tstep] = 0.0;
+            PassState st = save_state(s);
+            for (int i = 1; i < sN; i++) for (int j = 1; j < _M; j++) {
+                enter_line(s, 2, i, j);
+                for (int k = 1; k < K; k++) S1[gidx(i, j, k)] = s->Rp(k);
+            }
+            restore_state(s, st);
+            s->Time[s->tstep] = t_saved;
+        }
+        PassState st = save_state(s);
+        enter_line(s, 2, 1, 1);
+        p2.push_back(S1[gidx(1, 1, 1)] - s->Rp(1));
+        enter_line(s, 0, 1, 1);
+        vt.push_back(s->bc0());
+        restore_state(s, st);
+    }
+    std::vector<double> exact(G, 0.0);
+    for (int i = 1; i < sN; i++) for (int j = 1; j < _M; j++) for (int k = 1; k < K; k++)
+        exact[gidx(i, j, k)] = s->testF3d(i, j, k, s->tstep + 1);
+    const double err = s->analytic_compare(NULL);
+    w.put("S1", gdims, S1.data());
+    w.put("BC0", gdims, bc0g.data());
+    w.put("p2", p2); w.put("vt", vt); w.put("kkk0", kkk0);
+    w.put("U_final", gdims, s->b_U);
+    w.put("exact_final", gdims, exact.data());
+    w.scalar("analytic_sq_err", err);
+    delete s;
+    fclose(lg);
+    printf("wrote %s (column K %d, %d steps, analytic squared error %.6g)\n", path, kc, steps, err);
+}
+
 /* The Richards problem coupled with salt concentration C (analytic_test 0 with is_c = 1: nu
  * nonzero, :3515): on every line of every pass calc_step solves H (U1(0)) and then C (U1(1))
  * (:5270-5278), each with its own L1 history (oldC, time_summing :4086-4164). (With is_t = 1 the
@@ -555,6 +617,12 @@ int main(int argc, char **argv)
         run_richards(q, 1, 1, 2, 3, 3, 3, 0.8, 900.0, 40);
         snprintf(q, sizeof q, "%s/fpde_richards_k2.fgv", argv[2]);
         run_richards(q, 2, 2, 2, 3, 3, 3, 0.6, 900.0, 40);
+        return 0;
+    }
+    if (argc >= 3 && strcmp(argv[1], "kat") == 0) {
+        char q[4096];
+        snprintf(q, sizeof q, "%s/fpde_column_kat.fgv", argv[2]);
+        run_kat(q, 1000, 0.8, 1e-3, 1000);
         return 0;
     }
     if (argc >= 3 && strcmp(argv[1], "lod_vartau") == 0) {
