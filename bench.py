@@ -923,7 +923,7 @@ def split_line_rooflines(tot, steps, nodes, rows, sbk, ms_solve, hbm, hbm_src):
                           "model_superblock": {"bytes": m_sb, "achieved": m_sb / sec / 1e9,
                                                "frac": m_sb / sec / 1e9 / hbm,
                                                "note": "the same with the far history read once per %d-step "
-                                                       "super-block (this build's schedule)" % (64 * sbk)}}
+                                                       "super-block (the library's schedule)" % (64 * sbk)}}
     return out
 
 

@@ -1,6 +1,6 @@
 /* fpde_oracle -- CPU restatement of FPDE_HPC's L1 history sum and tridiagonal line
- * solves, used ONLY as the checker (tests, the smoke check, and the CPU-baseline leg of
- * the benchmark). It is never linked into, called by or shipped with the GPU library.
+ * solves, used ONLY to check results (tests, the smoke check) and as the CPU baseline of
+ * the benchmark. It is never linked into, called by or shipped with the GPU library.
  *
  * Parity status: pinned. tests/golden/*.fgv.gz hold outputs of the reference's own FP64
  * code (built from its sources by oracle/Makefile + oracle/ref_pin), and the CPU test

@@ -1,7 +1,7 @@
 """ctypes binding of the CPU oracle (oracle/fpde_oracle.c).
 
 Test infrastructure: imported only by tests/, the smoke check and the CPU-baseline leg
-of bench.py, as the checker. The GPU library never loads it. ``load()`` builds the
+of bench.py, to check results. The GPU library never loads it. ``load()`` builds the
 shared object with ``make -C oracle`` on first use (a second or two with gcc).
 """
 import ctypes as C

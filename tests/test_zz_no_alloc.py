@@ -55,7 +55,7 @@ def test_noalloc_sum_equals_allocating_entry_point_twice():
             torch.cuda.synchronize()
             assert relmax(Sdev.cpu().numpy(), Sref) <= RTOL, n
         # after the first call (which looked up the scratch array's address), further calls take
-        # no device memory: the free memory the driver reports does not move
+        # no device memory: the free memory cudaMemGetInfo reports does not move
         w = torch.from_numpy(np.linspace(0.5, 1.5, steps)).cuda()
         torch.cuda.synchronize()
         free0 = torch.cuda.mem_get_info()[0]
