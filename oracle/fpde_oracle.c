@@ -774,36 +774,39 @@ void fo_sf_matvec(int n, const double *mat, const double *mc, const double *Tm, 
     }
 }
 
-static double sf_dot(int m, const double *a, const double *b)
+static double sf_dot(int64_t m, const double *a, const double *b)
 {
     double s = 0.0;
-    for (int i = 0; i < m; i++) s += a[i] * b[i];
+    for (int64_t i = 0; i < m; i++) s += a[i] * b[i];
     return s;
 }
 
+/* The product a solve runs on: apply(op, x, r) sets r = A x. */
+typedef void (*sf_apply_fn)(const void *op, const double *x, double *r);
+
 /* solve_mln<1>, fpde_hpc_1d.cpp:812-1157, for n = 1: rn(k) = 1 and qn(k) = k - 1 for every k, so
  * each iteration takes the rn == 1 branch (:868-915), recomputes the residual (:943-947) and the
- * rn == n branch (:1053-1098); q[0] is the initial residual (no random vectors for n = 1). */
-int fo_sf_solve(int n, const double *mat, const double *mc, const double *Tm, const double *iw,
-                const double *rs, int space_der, const double *B, double *x, double thr, int maxiter)
+ * rn == n branch (:1053-1098); q[0] is the initial residual (no random vectors for n = 1). The
+ * vectors have m values (the reference's N, rb = 0, re = N). */
+static int sf_bicgstab(int64_t m, sf_apply_fn apply, const void *op, const double *B, double *x, double thr,
+                       int maxiter)
 {
-    const int m = n + 1;
-    double *q0 = (double *)malloc(sizeof(double) * (size_t)m), *r = (double *)malloc(sizeof(double) * (size_t)m);
+    const size_t bytes = sizeof(double) * (size_t)m;
+    double *q0 = (double *)malloc(bytes), *r = (double *)malloc(bytes);
     double *g[2], *w[2];
     for (int k = 0; k < 2; k++) {
-        g[k] = (double *)malloc(sizeof(double) * (size_t)m);
-        w[k] = (double *)malloc(sizeof(double) * (size_t)m);
+        g[k] = (double *)malloc(bytes);
+        w[k] = (double *)malloc(bytes);
     }
-    double *u = (double *)malloc(sizeof(double) * (size_t)m), *Au = (double *)malloc(sizeof(double) * (size_t)m);
-    double *zw = (double *)malloc(sizeof(double) * (size_t)m), *bt = (double *)malloc(sizeof(double) * (size_t)m);
+    double *u = (double *)malloc(bytes), *Au = (double *)malloc(bytes), *zw = (double *)malloc(bytes);
     double c[2] = {0.0, 0.0}, al, ro1 = 0.0, beta, norm;
     int iter = 1;
 restart:
-    fo_sf_matvec(n, mat, mc, Tm, iw, rs, space_der, x, r, bt);                 /* :841-844 */
-    for (int i = 0; i < m; i++) r[i] = B[i] - r[i];
-    memcpy(g[1], r, sizeof(double) * (size_t)m);
-    memcpy(q0, r, sizeof(double) * (size_t)m);
-    fo_sf_matvec(n, mat, mc, Tm, iw, rs, space_der, g[1], w[1], bt);            /* :851 */
+    apply(op, x, r);                                                           /* :841-844 */
+    for (int64_t i = 0; i < m; i++) r[i] = B[i] - r[i];
+    memcpy(g[1], r, bytes);
+    memcpy(q0, r, bytes);
+    apply(op, g[1], w[1]);                                                     /* :851 */
     c[1] = sf_dot(m, q0, w[1]);
     norm = sf_dot(m, r, r);
     if (fabs(norm / m) < thr) goto done;
@@ -811,26 +814,26 @@ restart:
         al = sf_dot(m, q0, r);                                                   /* :871-877 */
         al /= c[1];
         if (c[1] != 0.0) {
-            for (int i = 0; i < m; i++) u[i] = r[i] - al * w[1][i];
-            for (int i = 0; i < m; i++) x[i] = x[i] + al * g[1][i];
-            fo_sf_matvec(n, mat, mc, Tm, iw, rs, space_der, u, Au, bt);      /* :890 */
+            for (int64_t i = 0; i < m; i++) u[i] = r[i] - al * w[1][i];
+            for (int64_t i = 0; i < m; i++) x[i] = x[i] + al * g[1][i];
+            apply(op, u, Au);                                                    /* :890 */
             norm = sf_dot(m, Au, Au);
             ro1 = sf_dot(m, Au, u);
             ro1 = -ro1 / norm;
             if (norm == 0.0) goto restart;
-            for (int i = 0; i < m; i++) x[i] = x[i] - ro1 * u[i];
+            for (int64_t i = 0; i < m; i++) x[i] = x[i] - ro1 * u[i];
         } else {
             goto restart;
         }
-        fo_sf_matvec(n, mat, mc, Tm, iw, rs, space_der, x, r, bt);             /* :943-947 */
-        for (int i = 0; i < m; i++) r[i] = B[i] - r[i];
+        apply(op, x, r);                                                         /* :943-947 */
+        for (int64_t i = 0; i < m; i++) r[i] = B[i] - r[i];
         beta = 0.0;                                                              /* :1056-1065 */
-        for (int i = 0; i < m; i++) beta -= q0[i] * r[i];
+        for (int64_t i = 0; i < m; i++) beta -= q0[i] * r[i];
         beta /= c[1];
         if (c[1] == 0.0) beta = 0.0;
-        for (int i = 0; i < m; i++) zw[i] = r[i] + beta * w[1][i];
-        for (int i = 0; i < m; i++) g[0][i] = zw[i] + (beta / ro1) * g[1][i];
-        fo_sf_matvec(n, mat, mc, Tm, iw, rs, space_der, g[0], w[0], bt);       /* :1094 */
+        for (int64_t i = 0; i < m; i++) zw[i] = r[i] + beta * w[1][i];
+        for (int64_t i = 0; i < m; i++) g[0][i] = zw[i] + (beta / ro1) * g[1][i];
+        apply(op, g[0], w[0]);                                                   /* :1094 */
         c[0] = sf_dot(m, q0, w[0]);
         {                                                                        /* :1104-1121 */
             double *t = g[1]; g[1] = g[0]; g[0] = t;
@@ -843,9 +846,29 @@ restart:
         if (iter == maxiter) break;
     }
 done:
-    free(q0); free(r); free(u); free(Au); free(zw); free(bt);
+    free(q0); free(r); free(u); free(Au); free(zw);
     for (int k = 0; k < 2; k++) { free(g[k]); free(w[k]); }
     return iter;
+}
+
+struct sf_line_op {
+    int n, space_der;
+    const double *mat, *mc, *Tm, *iw, *rs;
+    double *bt;
+};
+static void sf_line_apply(const void *op, const double *x, double *r)
+{
+    const struct sf_line_op *o = (const struct sf_line_op *)op;
+    fo_sf_matvec(o->n, o->mat, o->mc, o->Tm, o->iw, o->rs, o->space_der, x, r, o->bt);
+}
+
+int fo_sf_solve(int n, const double *mat, const double *mc, const double *Tm, const double *iw,
+                const double *rs, int space_der, const double *B, double *x, double thr, int maxiter)
+{
+    struct sf_line_op op = {n, space_der, mat, mc, Tm, iw, rs, (double *)malloc(sizeof(double) * (size_t)(n + 1))};
+    const int it = sf_bicgstab(n + 1, sf_line_apply, &op, B, x, thr, maxiter);
+    free(op.bt);
+    return it;
 }
 
 int fo_lod_step_sf(int sN, int M, int K, double *U, double *hist, int n, const double *kb, const double *tau,
@@ -924,6 +947,185 @@ int fo_lod_step_sf(int sN, int M, int K, double *U, double *hist, int n, const d
     if (S_out) memcpy(S_out, S, sizeof(double) * (size_t)G);
     if (iters) *iters = it_total;
     free(Uold); free(S);
+    return 0;
+}
+
+/* ------------------------------ fully implicit 3D space-fractional operator (implicit3d 1) */
+
+/* vmul_T_3d, fpde_hpc_1d.cpp:6801-8722, without MPI, toeplitz_mult_alg 0 and for equation 0 (the
+ * C/T branch :8501-8676 is not restated). The vector has V = G + 1 values, G = (sN+2)(M+2)(K+2)
+ * nodes with i fastest (idx :1649). mat: 7 planes of V (Mat_3d[0..6]: K-, K+ neighbours in 0 and 2,
+ * the diagonal in 1, _M-, _M+ in 3 and 4, sN-, sN+ in 5 and 6); mc: 9 planes of V (Mcoefs_3d[c][d]
+ * at plane 3c+d, axis c = 0 sN, 1 _M, 2 K); Tm[c]: the Toeplitz row of axis c; iw: 3 planes of V
+ * (inv_dw_dh of the axis-c line through the node) or NULL for 1; rs: V values or NULL; bt: V
+ * scratch. */
+void fo_sf3d_matvec(int sN, int M, int K, const double *mat, const double *mc, const double *const *Tm,
+                    const double *iw, const double *rs, int space_der, const double *x, double *r, double *bt)
+{
+    const int64_t sy = sN + 2, sz = (int64_t)(sN + 2) * (M + 2), V = sz * (K + 2) + 1;
+    const double *M0 = mat, *M1 = mat + V, *M2 = mat + 2 * V, *M3 = mat + 3 * V, *M4 = mat + 4 * V;
+    const double *M5 = mat + 5 * V, *M6 = mat + 6 * V;
+    for (int64_t i = 0; i < V; i++) {                                              /* :6857-6877 */
+        r[i] = M1[i] * x[i];
+        if (sN > 2) {
+            if (i - 1 >= 0) r[i] += M5[i] * x[i - 1];
+            if (i + 1 < V) r[i] += M6[i] * x[i + 1];
+        }
+        if (M > 2) {
+            if (i - sy >= 0) r[i] += M3[i] * x[i - sy];
+            if (i + sy < V) r[i] += M4[i] * x[i + sy];
+        }
+        if (K > 2) {
+            if (i - sz >= 0) r[i] += M0[i] * x[i - sz];
+            if (i + sz < V) r[i] += M2[i] * x[i + sz];
+        }
+    }
+    /* the axes in the reference's order: K (:7248-7574), _M (:7665-7995), sN (:8085-8411) */
+    for (int a = 0; a < 3; a++) {
+        const int c = 2 - a;
+        const int n = c == 2 ? K : (c == 1 ? M : sN);
+        const int64_t st = c == 2 ? sz : (c == 1 ? sy : 1);
+        if (n <= 2) continue;
+        const double *c0 = mc + (3 * c) * V, *c1 = mc + (3 * c + 1) * V, *c2 = mc + (3 * c + 2) * V;
+        const double *T = Tm[c];
+        for (int64_t i = 0; i < V; i++) {
+            bt[i] = c1[i] * x[i];
+            if (i - st >= 0) bt[i] += c0[i] * x[i - st];
+            if (i + st < V) bt[i] += c2[i] * x[i + st];
+        }
+        /* lines: the other two coordinates over 1..len-1 */
+        const int na = c == 0 ? M : sN, nb = c == 2 ? M : K;
+        const int64_t sa = c == 0 ? sy : 1, sb = c == 2 ? sy : sz;
+        for (int la = 1; la < na; la++)
+            for (int lb = 1; lb < nb; lb++) {
+                const int64_t base = la * sa + lb * sb;
+                for (int p = 1; p < n; p++) {
+                    double v = 0.0;
+                    for (int q = 1; q < p; q++) v += bt[base + q * st] * T[p - q + 1];
+                    if (space_der == 1)
+                        for (int q = p + 1; q < n; q++) v -= bt[base + q * st] * T[q - p + 1];
+                    const int64_t id = base + p * st;
+                    if (rs) v /= rs[id];
+                    r[id] += v * (iw ? iw[c * V + id] : 1.0);
+                }
+            }
+    }
+}
+
+struct sf3d_op {
+    int sN, M, K, space_der;
+    const double *mat, *mc, *const *Tm, *iw, *rs;
+    double *bt;
+};
+static void sf3d_apply(const void *op, const double *x, double *r)
+{
+    const struct sf3d_op *o = (const struct sf3d_op *)op;
+    fo_sf3d_matvec(o->sN, o->M, o->K, o->mat, o->mc, o->Tm, o->iw, o->rs, o->space_der, x, r, o->bt);
+}
+
+/* solve_mln<1> with vmul_T_3d over the V values (calc_step :5705). */
+int fo_sf3d_solve(int sN, int M, int K, const double *mat, const double *mc, const double *const *Tm,
+                  const double *iw, const double *rs, int space_der, const double *B, double *x, double thr,
+                  int maxiter)
+{
+    const int64_t V = (int64_t)(sN + 2) * (M + 2) * (K + 2) + 1;
+    struct sf3d_op op = {sN, M, K, space_der, mat, mc, Tm, iw, rs, (double *)malloc(sizeof(double) * (size_t)V)};
+    const int it = sf_bicgstab(V, sf3d_apply, &op, B, x, thr, maxiter);
+    free(op.bt);
+    return it;
+}
+
+/* One step of the fully implicit scheme (mode 3, implicit3d 1, impl 2; calc_step :5160-5716):
+ * Mat_3d and Om are zeroed (:5160-5178) and every line of the K, _M and sN passes, in that order,
+ * adds its implicit2_gen system (:4630-4663): interior rows (A_, -R, B) with R's time term
+ * Da kkk0/tau only in the K pass (:3117-3123), right-hand side -lam U + Rp + Da S in the K pass and
+ * Rp = 0 in the others (Om1_impl :4434-4445, Rp :2730-2733, :4493-4498), identity rows at both line
+ * ends with bc0 / bcN. Mcoefs_3d[c] is the operand grid mc of pass c at its line nodes. Then one
+ * solve over the V = G + 1 values from the grid (U[G], past the grid, is *u_end) and the
+ * history row. mat_out (7 x V) / om_out (V) / S_out (G) / iters may be NULL. */
+int fo_lod_step_sf3d(int sN, int M, int K, double *U, double *u_end, double *hist, int n, const double *kb,
+                     const double *tau, double Da, double kkk0, const double *coefA, const double *coefB,
+                     const double *coefRlap, const double *mc, const double *iw, const double *Tm, int ldt,
+                     int space_der, double thr, int maxiter, const double *rp, const double *bc, double *mat_out,
+                     double *om_out, double *S_out, int64_t *iters)
+{
+    const double lam = Da * (kkk0 / tau[n]);
+    const double lamR = Da * kkk0 / tau[n];
+    const int64_t sx = 1, sy = sN + 2, sz = (int64_t)(sN + 2) * (M + 2);
+    const int64_t G = sz * (K + 2), V = G + 1;
+    double *Uold = (double *)malloc(sizeof(double) * (size_t)G);
+    double *S = (double *)calloc((size_t)G, sizeof(double));
+    double *mat = (double *)calloc((size_t)(7 * V), sizeof(double));
+    double *mc3 = (double *)calloc((size_t)(9 * V), sizeof(double));
+    double *iw3 = (double *)calloc((size_t)(3 * V), sizeof(double));
+    double *Om = (double *)calloc((size_t)V, sizeof(double));
+    double *x = (double *)malloc(sizeof(double) * (size_t)V);
+    memcpy(Uold, U, sizeof(double) * (size_t)G);
+    if (n > 0) {
+        for (int k = 1; k <= K; k++)
+            for (int t = n - 1; t >= 0; t--) {
+                const double *h = hist + (int64_t)t * G;
+                const double c = kb[t], tt = tau[t];
+                for (int j = 1; j < M; j++)
+                    for (int i = 1; i < sN; i++) {
+                        const int64_t id = i * sx + j * sy + k * sz;
+                        S[id] += c * h[id] / tt;
+                    }
+            }
+    }
+    for (int pass = 2; pass >= 0; pass--) {
+        const int Nl = pass == 2 ? K : (pass == 1 ? M : sN);
+        const int64_t st = pass == 2 ? sz : (pass == 1 ? sy : sx);
+        const int lo = pass == 2 ? 0 : (pass == 1 ? 3 : 5), hi = pass == 2 ? 2 : (pass == 1 ? 4 : 6);
+        const double *cA = coefA + (int64_t)pass * G, *cB = coefB + (int64_t)pass * G;
+        const double *cR = coefRlap + (int64_t)pass * G;
+        const double *pm = mc + (int64_t)pass * 3 * G, *piw = iw + (int64_t)pass * G;
+        const int na = pass == 2 ? sN : (pass == 1 ? sN : M);
+        const int nb = pass == 2 ? M : K;
+        const double tR = pass == 2 ? lamR : 0.0;
+        for (int a = 1; a < na; a++)
+            for (int b = 1; b < nb; b++) {
+                int64_t base;
+                if (pass == 2) base = a * sx + b * sy;
+                else if (pass == 1) base = a * sx + b * sz;
+                else base = a * sy + b * sz;
+                for (int p = 0; p <= Nl; p++) {
+                    const int64_t id = base + p * st;
+                    double ml, md, mh, om;
+                    if (p == 0 || p == Nl) {
+                        ml = 0.0; md = 1.0; mh = 0.0;
+                        om = bc[id];
+                    } else {
+                        ml = cA[id]; md = -(cR[id] + tR); mh = cB[id];
+                        if (pass == 2) {
+                            om = -(lam * U[id]) + (rp ? rp[id] : 0.0);
+                            om += Da * S[id];
+                        } else {
+                            om = 0.0;
+                        }
+                        for (int d = 0; d < 3; d++) mc3[(3 * pass + d) * V + id] += pm[d * G + id];
+                        iw3[pass * V + id] = piw[id];
+                    }
+                    mat[lo * V + id] += ml;
+                    mat[V + id] += md;
+                    mat[hi * V + id] += mh;
+                    Om[id] += om;
+                }
+            }
+    }
+    const double *T3[3] = {Tm, Tm + ldt, Tm + 2 * ldt};
+    memcpy(x, U, sizeof(double) * (size_t)G);
+    x[G] = u_end ? *u_end : 0.0;
+    const int it = fo_sf3d_solve(sN, M, K, mat, mc3, T3, iw3, NULL, space_der, Om, x, thr, maxiter);
+    memcpy(U, x, sizeof(double) * (size_t)G);
+    if (u_end) *u_end = x[G];
+    double *row = hist + (int64_t)n * G;
+    for (int64_t q = 0; q < G; q++) row[q] = U[q] - Uold[q];
+    if (mat_out) memcpy(mat_out, mat, sizeof(double) * (size_t)(7 * V));
+    if (om_out) memcpy(om_out, Om, sizeof(double) * (size_t)V);
+    if (S_out) memcpy(S_out, S, sizeof(double) * (size_t)G);
+    if (iters) *iters = it;
+    free(Uold); free(S); free(mat); free(mc3); free(iw3); free(Om); free(x);
     return 0;
 }
 

@@ -198,6 +198,29 @@ int fo_lod_step_sf(int sN, int M, int K, double *U, double *hist, int n, const d
                    const double *mc, const double *iw, const double *Tm, int ldt, int space_der, double thr,
                    int maxiter, const double *rp, const double *bc, double *S_out, int64_t *iters);
 
+/* ---- fully implicit 3D space-fractional operator (implicit3d 1) ---- */
+
+/* vmul_T_3d (:6801-8722, toeplitz_mult_alg 0, equation 0) on V = (sN+2)(M+2)(K+2) + 1 values:
+ * mat 7 x V (Mat_3d), mc 9 x V (Mcoefs_3d[c][d] at plane 3c+d), Tm[c] the Toeplitz row of axis c
+ * (0 sN, 1 _M, 2 K), iw 3 x V or NULL, rs V or NULL, bt V scratch. */
+void fo_sf3d_matvec(int sN, int M, int K, const double *mat, const double *mc, const double *const *Tm,
+                    const double *iw, const double *rs, int space_der, const double *x, double *r, double *bt);
+
+/* solve_mln<1> with vmul_T_3d over the V values (calc_step :5705); returns the iteration count. */
+int fo_sf3d_solve(int sN, int M, int K, const double *mat, const double *mc, const double *const *Tm,
+                  const double *iw, const double *rs, int space_der, const double *B, double *x, double thr,
+                  int maxiter);
+
+/* One step of the fully implicit scheme (calc_step :5160-5716 with implicit3d 1, impl 2): the
+ * system assembled from every line's implicit2_gen system of the three passes, one solve, the
+ * history row. Operands as fo_lod_step_sf; *u_end is the value past the grid (may be NULL: 0);
+ * mat_out (7 x V), om_out (V), S_out (G) and iters may be NULL. */
+int fo_lod_step_sf3d(int sN, int M, int K, double *U, double *u_end, double *hist, int n, const double *kb,
+                     const double *tau, double Da, double kkk0, const double *coefA, const double *coefB,
+                     const double *coefRlap, const double *mc, const double *iw, const double *Tm, int ldt,
+                     int space_der, double thr, int maxiter, const double *rp, const double *bc, double *mat_out,
+                     double *om_out, double *S_out, int64_t *iters);
+
 /* ---- distributed order (fr_do.cpp) ---- */
 
 /* Caputo derivative of sampled F (Cder :74-86 with an F array): DF[t] for t = 1..ntau-1,

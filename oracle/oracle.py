@@ -70,6 +70,11 @@ def load():
     lib.fo_lod_step_sf.argtypes = [i32, i32, i32, _dp, _dp, i32, _dp, _dp, d, d, _dp, _dp, _dp, _dp, _dp, _dp, i32,
                                    i32, d, i32, vp, _dp, vp, C.POINTER(i64)]
     lib.fo_lod_step_sf.restype = i32
+    lib.fo_sf3d_matvec.argtypes = [i32, i32, i32, _dp, _dp, C.POINTER(C.c_void_p), vp, vp, i32, _dp, _dp, _dp]
+    lib.fo_sf3d_solve.argtypes = [i32, i32, i32, _dp, _dp, C.POINTER(C.c_void_p), vp, vp, i32, _dp, _dp, d, i32]
+    lib.fo_sf3d_solve.restype = i32
+    lib.fo_lod_step_sf3d.argtypes = [i32, i32, i32, _dp, C.POINTER(d), _dp, i32, _dp, _dp, d, d, _dp, _dp, _dp,
+                                     _dp, _dp, _dp, i32, i32, d, i32, vp, _dp, vp, vp, vp, C.POINTER(i64)]
     lib.fo_caputo_derivative.argtypes = [i32, d, d, d, _dp, _dp]
     lib.fo_do_derivative.argtypes = [i32, d, i32, _dp, _dp, _dp, i32, i32, i32, _dp]
     lib.fo_do_fused_weights.argtypes = [i32, _dp, _dp, _dp, d, i32, _dp]
@@ -350,6 +355,62 @@ def lod_step_sf(dims, U, hist, n, kb, tau, Da, kkk0, coefA, coefB, coefRlap, mc,
                        _f64(mc).reshape(-1), _f64(iw).reshape(-1), Tm.reshape(-1), Tm.shape[1], space_der, thr,
                        maxiter, _ptr(rpp), _f64(bc).reshape(-1), _ptr(S), C.byref(it))
     return S, it.value
+
+
+def _rows3(Tm):
+    """Three Toeplitz rows (one per axis: sN, _M, K) as a C array of pointers; keeps the arrays alive."""
+    rows = [_f64(t) for t in Tm]
+    arr = (C.c_void_p * 3)(*[r.ctypes.data_as(C.c_void_p).value for r in rows])
+    return arr, rows
+
+
+def sf3d_matvec(dims, mat, mc, Tm, x, iw=None, rs=None, space_der=0):
+    """fo_sf3d_matvec (vmul_T_3d): mat 7 x V, mc 9 x V, Tm three rows, iw 3 x V, V = G + 1."""
+    lib = load()
+    sN, M, K = dims
+    x = _f64(x).reshape(-1)
+    r = np.zeros_like(x)
+    bt = np.zeros_like(x)
+    arr, keep = _rows3(Tm)
+    iw, rs = _f64(iw), _f64(rs)
+    lib.fo_sf3d_matvec(sN, M, K, _f64(mat).reshape(-1), _f64(mc).reshape(-1), arr,
+                       _ptr(None if iw is None else iw.reshape(-1)), _ptr(rs), space_der, x, r, bt)
+    return r
+
+
+def sf3d_solve(dims, mat, mc, Tm, B, x0, thr, maxiter, iw=None, rs=None, space_der=0):
+    """fo_sf3d_solve (solve_mln<1> with vmul_T_3d): returns (solution, iterations)."""
+    lib = load()
+    sN, M, K = dims
+    x = _f64(x0).reshape(-1).copy()
+    arr, keep = _rows3(Tm)
+    iw, rs = _f64(iw), _f64(rs)
+    it = lib.fo_sf3d_solve(sN, M, K, _f64(mat).reshape(-1), _f64(mc).reshape(-1), arr,
+                           _ptr(None if iw is None else iw.reshape(-1)), _ptr(rs), space_der,
+                           _f64(B).reshape(-1), x, thr, maxiter)
+    return x, it
+
+
+def lod_step_sf3d(dims, U, u_end, hist, n, kb, tau, Da, kkk0, coefA, coefB, coefRlap, mc, iw, Tm, space_der, thr,
+                  maxiter, rp, bc, want_system=False):
+    """fo_lod_step_sf3d: one step of the fully implicit 3D scheme. U (G values) is advanced in place.
+    Returns (u_end, iterations, mat 7 x V or None, Om or None, S or None)."""
+    lib = load()
+    sN, M, K = dims
+    G = U.size
+    V = G + 1
+    Tm = _f64(Tm)
+    it = C.c_int64()
+    ue = C.c_double(u_end)
+    mat = np.zeros((7, V)) if want_system else None
+    om = np.zeros(V) if want_system else None
+    S = np.zeros(G) if want_system else None
+    rpp = None if rp is None else _f64(rp).reshape(-1)
+    lib.fo_lod_step_sf3d(sN, M, K, U.reshape(-1), C.byref(ue), hist.reshape(-1), n, _f64(kb), _f64(tau), Da, kkk0,
+                         _f64(coefA).reshape(-1), _f64(coefB).reshape(-1), _f64(coefRlap).reshape(-1),
+                         _f64(mc).reshape(-1), _f64(iw).reshape(-1), Tm.reshape(-1), Tm.shape[1], space_der, thr,
+                         maxiter, _ptr(rpp), _f64(bc).reshape(-1), _ptr(mat), _ptr(om), _ptr(S), C.byref(it))
+    return ue.value, it.value, mat, om, S
 
 
 def caputo_derivative(F, tau, a, g2a):

@@ -478,6 +478,38 @@ static void run_richards_ct(const char *path, int kform, int bs, int nb, int mb,
            sN, _M, K);
 }
 
+/* Per pass of a space-fractional run: Mcoefs (Om1T :4362-4389) and inv_dw_dh (:2527) at every
+ * interior line node, and the Toeplitz row Tm (:3670-3694). */
+static void record_sf_operands(H_solver *s, FgvWriter &w)
+{
+    size_t G = (size_t)(sN + 2) * (_M + 2) * (K + 2);
+    std::vector<uint64_t> gdims = {(uint64_t)(K + 2), (uint64_t)(_M + 2), (uint64_t)(sN + 2)};
+    PassState st = save_state(s);
+    for (int pass = 0; pass < 3; pass++) {
+        std::vector<double> m0(G, 0.0), m1(G, 0.0), m2(G, 0.0), iw(G, 0.0);
+        int na = pass == 2 ? sN : (pass == 1 ? sN : _M), nbl = pass == 2 ? _M : K;
+        int Nl = pass == 2 ? K : (pass == 1 ? _M : sN);
+        for (int a = 1; a < na; a++) for (int b = 1; b < nbl; b++) {
+            enter_line(s, pass, a, b);
+            s->rb = 1; s->re = N;
+            s->Om1T();
+            for (int q = 1; q < Nl; q++) {
+                size_t id = pass == 2 ? gidx(a, b, q) : (pass == 1 ? gidx(a, q, b) : gidx(q, a, b));
+                m0[id] = s->Mcoefs[0][q]; m1[id] = s->Mcoefs[1][q]; m2[id] = s->Mcoefs[2][q];
+                iw[id] = s->inv_dw_dh(q);
+            }
+        }
+        char nm[32];
+        snprintf(nm, sizeof nm, "mc0_pass%d", pass); w.put(nm, gdims, m0.data());
+        snprintf(nm, sizeof nm, "mc1_pass%d", pass); w.put(nm, gdims, m1.data());
+        snprintf(nm, sizeof nm, "mc2_pass%d", pass); w.put(nm, gdims, m2.data());
+        snprintf(nm, sizeof nm, "iw_pass%d", pass); w.put(nm, gdims, iw.data());
+        snprintf(nm, sizeof nm, "Tm_pass%d", pass);
+        w.put(nm, std::vector<double>(s->Tm[pass], s->Tm[pass] + Nl + 1));
+    }
+    restore_state(s, st);
+}
+
 /* The implicit space-fractional LOD (impl 2, TMA 0: implicit2_gen :4630-4663 builds each line's
  * tridiagonal Mat and right-hand side, U1 :4769-4791 solves tridiag(Mat) + iw * T * tridiag(Mcoefs)
  * with solve_mln<1> :812-1157 and the product vmul_T :6618-6747), analytic problem 2, Dirichlet
@@ -528,30 +560,8 @@ static void run_spacefrac(const char *path, int sd, double gam, double alpha, in
     w.put("Rp", {ns, (uint64_t)(K + 2), (uint64_t)(_M + 2), (uint64_t)(sN + 2)}, rp.data());
     w.put("BC", {ns, (uint64_t)(K + 2), (uint64_t)(_M + 2), (uint64_t)(sN + 2)}, bc.data());
 
-    /* per pass: Mcoefs and inv_dw_dh at every interior line node, and the Toeplitz row */
     PassState st = save_state(s);
-    for (int pass = 0; pass < 3; pass++) {
-        std::vector<double> m0(G, 0.0), m1(G, 0.0), m2(G, 0.0), iw(G, 0.0);
-        int na = pass == 2 ? sN : (pass == 1 ? sN : _M), nbl = pass == 2 ? _M : K;
-        int Nl = pass == 2 ? K : (pass == 1 ? _M : sN);
-        for (int a = 1; a < na; a++) for (int b = 1; b < nbl; b++) {
-            enter_line(s, pass, a, b);
-            s->rb = 1; s->re = N;
-            s->Om1T();
-            for (int q = 1; q < Nl; q++) {
-                size_t id = pass == 2 ? gidx(a, b, q) : (pass == 1 ? gidx(a, q, b) : gidx(q, a, b));
-                m0[id] = s->Mcoefs[0][q]; m1[id] = s->Mcoefs[1][q]; m2[id] = s->Mcoefs[2][q];
-                iw[id] = s->inv_dw_dh(q);
-            }
-        }
-        char nm[32];
-        snprintf(nm, sizeof nm, "mc0_pass%d", pass); w.put(nm, gdims, m0.data());
-        snprintf(nm, sizeof nm, "mc1_pass%d", pass); w.put(nm, gdims, m1.data());
-        snprintf(nm, sizeof nm, "mc2_pass%d", pass); w.put(nm, gdims, m2.data());
-        snprintf(nm, sizeof nm, "iw_pass%d", pass); w.put(nm, gdims, iw.data());
-        snprintf(nm, sizeof nm, "Tm_pass%d", pass);
-        w.put(nm, std::vector<double>(s->Tm[pass], s->Tm[pass] + Nl + 1));
-    }
+    record_sf_operands(s, w);
     /* one product and one solve on the first line of each pass, with the system implicit2_gen
      * forms for it now (after the last step) */
     for (int pass = 0; pass < 3; pass++) {
@@ -587,6 +597,102 @@ static void run_spacefrac(const char *path, int sd, double gam, double alpha, in
     implicit = 0; toeplitz_mult_alg = 0; space_der = 0;
     printf("wrote %s (space-fractional LOD, SD %d, gamma %g, %d steps, grid %dx%dx%d)\n", path, sd, gam, steps, sN,
            _M, K);
+}
+
+/* vmul_T_3d with a count of the products a solve_mln<1> call takes (two per start or restart,
+ * three per iteration). */
+static long sf3d_products = 0;
+static void vmul_T_3d_counted(double **Kp, double *x, double *r, int Nv)
+{
+    sf3d_products++;
+    vmul_T_3d(Kp, x, r, Nv);
+}
+
+/* The fully implicit 3D space-fractional scheme (implicit3d 1, impl 2, TMA 0): every step
+ * calc_step (:5160-5716) zeroes Mat_3d / Mcoefs_3d / Om, adds each line's implicit2_gen system of
+ * the K, _M and sN passes into them (the time term and the history only in the K pass: R :3121,
+ * Om1_impl :4434-4445, :4493-4498) and runs one solve_mln<1> over the (G+1)-vector with vmul_T_3d
+ * (:6801-8722, the 7-diagonal product plus each axis's Toeplitz sums). Recorded like run_spacefrac,
+ * plus the assembled system (Mat_3d, Om) of the first and the last step, Mcoefs_3d at the nodes the
+ * product reads, one product vmul_T_3d(x) of a fixed x, and the last step's solve repeated from its
+ * starting grid with the count of its products. The solve runs over G+1 values: the harness sets
+ * the one past the grid (b_U[G], never assigned by the reference) to 0. */
+static void run_spacefrac3d(const char *path, int sd, double gam, double alpha, int bs, int nb, int mb, int kb,
+                            double tau, int steps, double ieps, int initer)
+{
+    set_dims(bs, nb, mb, kb);
+    varT = 0; varZ = 0; varXY = 0;
+    implicit = 2; implicit3d = 1; rp_split_3d = 0; sum_alg = 0;
+    toeplitz_mult_alg = 0; space_der = sd; implicit_row_scaling = 0;
+    impl_err = ieps; impl_niter = initer;
+    global_eps = 1e-15; global_eps2 = 1e-15;
+    FILE *lg = fopen("/dev/null", "w");
+    H_solver *s = new H_solver(2, 1, 5, 0, 1, alpha, gam, 0, 0, 0, 3, lg, 2);
+    const size_t G = (size_t)(sN + 2) * (_M + 2) * (K + 2), V = G + 1;
+    s->b_U[G] = 0.0;
+    FgvWriter w(path);
+    w.scalar("sN", sN); w.scalar("M", _M); w.scalar("K", K);
+    w.scalar("alpha", alpha); w.scalar("gamma", gam); w.scalar("Da", s->Da); w.scalar("Dg", s->Dg);
+    w.scalar("space_der", sd); w.scalar("impl_err", ieps); w.scalar("impl_niter", initer);
+    std::vector<uint64_t> gdims = {(uint64_t)(K + 2), (uint64_t)(_M + 2), (uint64_t)(sN + 2)};
+    w.put("U0", gdims, s->b_U);
+    w.put("Z_pass0", std::vector<double>(s->sZ, s->sZ + sN + 2));
+    w.put("Z_pass1", std::vector<double>(s->X, s->X + _M + 2));
+    w.put("Z_pass2", std::vector<double>(s->Y, s->Y + K + 2));
+    std::vector<double> kb_all, kb_off, kkk0, tauv, S_all, U_all, rp, bc, Uprev(V);
+    for (int n = 0; n < steps; n++) {
+        Uprev.assign(s->b_U, s->b_U + V);
+        s->calc_step(tau);
+        kb_off.push_back((double)kb_all.size());
+        kb_all.insert(kb_all.end(), s->kb_3_cache.begin(), s->kb_3_cache.end());
+        kkk0.push_back(s->kkk0);
+        tauv.push_back(s->tau[s->tstep]);
+        if (n == 0) record_coefs(s, w);
+        S_all.insert(S_all.end(), s->b_Utimesum, s->b_Utimesum + G);
+        U_all.insert(U_all.end(), s->b_U, s->b_U + G);
+        record_step_inputs(s, rp, bc);
+        if (n == 0 || n == steps - 1) {
+            std::vector<double> mat((size_t)7 * V);
+            for (int d = 0; d < 7; d++) for (size_t v = 0; v < V; v++) mat[(size_t)d * V + v] = s->Mat_3d[d][v];
+            w.put(n == 0 ? "sys_first_mat" : "sys_last_mat", {7, (uint64_t)V}, mat.data());
+            w.put(n == 0 ? "sys_first_om" : "sys_last_om", std::vector<double>(s->Om, s->Om + V));
+        }
+    }
+    kb_off.push_back((double)kb_all.size());
+    uint64_t ns = steps;
+    w.put("tau", tauv); w.put("kkk0", kkk0);
+    w.put("kb_flat", kb_all); w.put("kb_off", kb_off);
+    w.put("S", {ns, (uint64_t)(K + 2), (uint64_t)(_M + 2), (uint64_t)(sN + 2)}, S_all.data());
+    w.put("U", {ns, (uint64_t)(K + 2), (uint64_t)(_M + 2), (uint64_t)(sN + 2)}, U_all.data());
+    w.put("Rp", {ns, (uint64_t)(K + 2), (uint64_t)(_M + 2), (uint64_t)(sN + 2)}, rp.data());
+    w.put("BC", {ns, (uint64_t)(K + 2), (uint64_t)(_M + 2), (uint64_t)(sN + 2)}, bc.data());
+    w.scalar("U_end", s->b_U[G]);
+    record_sf_operands(s, w);
+    /* Mcoefs_3d at the nodes whose Bt the product reads (1..n-1 along every axis); each line's
+     * Mcoefs at its two ends is left unset by Om1T and never read */
+    std::vector<double> mc3((size_t)9 * V, 0.0);
+    for (int k = 1; k < K; k++) for (int j = 1; j < _M; j++) for (int i = 1; i < sN; i++) {
+        const size_t v = gidx(i, j, k);
+        for (int c = 0; c < 3; c++) for (int d = 0; d < 3; d++) mc3[(size_t)(3 * c + d) * V + v] = s->Mcoefs_3d[c][d][v];
+    }
+    w.put("mc3d", {9, (uint64_t)V}, mc3.data());
+    s->equation = 0;
+    std::vector<double> x(V), r(V, 0.0);
+    for (size_t v = 0; v < V; v++) x[v] = std::sin(1.0 + 0.37 * v) + 0.25 * std::cos(3.1 * (double)v * v);
+    vmul_T_3d((double **)s, x.data(), r.data(), (int)V);
+    w.put("mv_x", x);
+    w.put("mv_r", r);
+    std::vector<double> xs(Uprev);
+    sf3d_products = 0;
+    solve_mln<1>((double **)s, s->Om, xs.data(), (int)V, impl_err, impl_niter, vmul_T_3d_counted, 0, (int)V);
+    w.put("solve_x0", Uprev);
+    w.put("solve_sol", xs);
+    w.scalar("solve_products", (double)sf3d_products);
+    delete s;
+    fclose(lg);
+    implicit = 0; implicit3d = 0; toeplitz_mult_alg = 0; space_der = 0;
+    printf("wrote %s (implicit 3D space-fractional, SD %d, gamma %g, %d steps, grid %dx%dx%d, %ld products)\n",
+           path, sd, gam, steps, sN, _M, K, sf3d_products);
 }
 
 /* The reference's Gamma (fpde_hpc_1d.cpp:70-252: exp(LogGamma), its own series and
@@ -658,6 +764,18 @@ int main(int argc, char **argv)
         /* a column of 40 nodes, two-sided, solved to a tight tolerance */
         snprintf(q, sizeof q, "%s/fpde_sf_col.fgv", argv[2]);
         run_spacefrac(q, 1, 0.75, 0.8, 1, 3, 3, 40, 0.002, 10, 1e-26, 400);
+        return 0;
+    }
+    if (argc >= 3 && strcmp(argv[1], "spacefrac3d") == 0) {
+        char q[4096];
+        /* 6 x 4 x 8 cells, one- and two-sided, the reference's default tolerance; and 4 x 6 x 6
+         * cells two-sided with a tight tolerance */
+        snprintf(q, sizeof q, "%s/fpde_sf3d_sd0.fgv", argv[2]);
+        run_spacefrac3d(q, 0, 0.8, 0.8, 2, 3, 2, 4, 0.0025, 10, 1e-9, 5000);
+        snprintf(q, sizeof q, "%s/fpde_sf3d_sd1.fgv", argv[2]);
+        run_spacefrac3d(q, 1, 0.7, 0.85, 2, 3, 2, 4, 0.0025, 10, 1e-9, 5000);
+        snprintf(q, sizeof q, "%s/fpde_sf3d_tight.fgv", argv[2]);
+        run_spacefrac3d(q, 1, 0.75, 0.8, 2, 2, 3, 3, 0.002, 8, 1e-24, 400);
         return 0;
     }
     if (argc >= 3 && strcmp(argv[1], "gamma") == 0) {

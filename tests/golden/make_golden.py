@@ -6,9 +6,10 @@ gzips their output here. Needs the reference checkout: REF_DIR on the command li
 $FPDE_REFERENCE_DIR, else a directory named "reference" beside the repository; the fixtures
 themselves are committed so tests never need it.
 
-    python tests/golden/make_golden.py [REF_DIR] [--only gamma|richards|richards_ct|spacefrac|lod_vartau|kat]
+    python tests/golden/make_golden.py [REF_DIR] [--only gamma|richards|richards_ct|spacefrac|spacefrac3d|lod_vartau|kat]
 
-The richards, richards_ct, spacefrac, lod_vartau and kat scenarios run only with --only (each sets its own solver mode).
+The richards, richards_ct, spacefrac, spacefrac3d, lod_vartau and kat scenarios run only with --only
+(each sets its own solver mode).
 
 The 40-digit weights fixture (fpde_weights_g_exact.fgv.gz) is computed from the time grids of
 the fpde_weights_fk* fixtures written here: rerun make_weights_exact.py after this script.
