@@ -40,7 +40,12 @@ class LineDesc(C.Structure):
 
 class SpaceFrac(C.Structure):
     _fields_ = [("space_der", c_int), ("tol", c_dbl), ("max_iter", c_int), ("Tm", c_vp * 3), ("mc", c_vp * 3),
-                ("iw", c_vp * 3)]
+                ("iw", c_vp * 3), ("implicit3d", c_int), ("exact", c_int)]
+
+
+class Sf3dSystem(C.Structure):
+    _fields_ = [("sN", c_int), ("M", c_int), ("K", c_int), ("space_der", c_int), ("mat", c_vp), ("mc", c_vp),
+                ("Tm", c_vp * 3), ("iw", c_vp), ("rs", c_vp)]
 
 
 class Lod3dDesc(C.Structure):
@@ -93,6 +98,9 @@ _SIGS = {
     "fpde_sf_solve": (c_int, [c_vp, c_int, c_int, c_vp, c_vp, c_vp, c_vp, c_vp, c_int, c_vp, c_vp, c_dbl, c_int,
                               c_vp, c_int]),
     "fpde_sf_toeplitz_row": (c_int, [c_dbl, c_vp, c_int, c_vp]),
+    "fpde_sf3d_matvec": (c_int, [c_vp, C.POINTER(Sf3dSystem), c_vp, c_vp, c_int]),
+    "fpde_sf3d_solve": (c_int, [c_vp, C.POINTER(Sf3dSystem), c_vp, c_vp, c_dbl, c_int, c_int, C.POINTER(c_int),
+                                c_int]),
     "fpde_do_derivative": (c_int, [c_vp, c_vp, c_i64, c_i64, c_int, c_dbl, c_vp, c_int, c_int, c_int, c_vp, c_i64,
                                    c_int]),
     "fpde_history_create": (c_int, [c_vp, c_i64, c_i64, c_int, C.POINTER(c_vp)]),

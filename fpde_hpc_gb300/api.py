@@ -3,7 +3,7 @@ import ctypes as C
 
 import numpy as np
 
-from ._lib import ColumnDesc, LineDesc, LineTuning, Lod3dDesc, Richards, SpaceFrac, check, load
+from ._lib import ColumnDesc, LineDesc, LineTuning, Lod3dDesc, Richards, Sf3dSystem, SpaceFrac, check, load
 
 FP64, SPLIT_BF16, SPLIT_F16 = 0, 1, 2
 
@@ -248,6 +248,59 @@ class Context:
                                      1 if dev else 0), "fpde_sf_solve")
         return x, it
 
+    def _sf3d_system(self, dims, mat, mc, Tm, iw, rs, space_der, dev):
+        sN, M, K = dims
+        V = (sN + 2) * (M + 2) * (K + 2) + 1
+        conv = (lambda a: a.contiguous()) if dev else _f64
+        mat, mc = conv(mat), conv(mc)
+        rows = [conv(t) for t in Tm]
+        iw = None if iw is None else conv(iw)
+        rs = None if rs is None else conv(rs)
+        if tuple(mat.shape) not in ((7, V), (7 * V,)) or tuple(mc.shape) not in ((9, V), (9 * V,)):
+            raise ValueError("mat needs 7 x V values and mc 9 x V, V = (sN+2)(M+2)(K+2) + 1")
+        if any((t.numel() if dev else t.size) < nl + 1 for t, nl in zip(rows, dims)):
+            raise ValueError("Tm[c] needs len_c + 1 values")
+        s = Sf3dSystem(sN=sN, M=M, K=K, space_der=int(space_der), mat=_ptr(mat), mc=_ptr(mc), iw=_ptr(iw),
+                       rs=_ptr(rs))
+        for c in range(3):
+            s.Tm[c] = _ptr(rows[c])
+        keep = [mat, mc, iw, rs] + rows
+        return s, keep, V
+
+    def sf3d_matvec(self, dims, mat, mc, Tm, x, iw=None, rs=None, space_der=0):
+        """vmul_T_3d (implicit3d 1) on the V = (sN+2)(M+2)(K+2) + 1 values of x: mat (7, V), mc (9, V),
+        Tm three rows (axis sN, _M, K), iw (3, V); bitwise the reference's product. Host arrays or
+        CUDA tensors (then the result is a tensor on the same device)."""
+        dev = _is_dev(x)
+        s, keep, V = self._sf3d_system(dims, mat, mc, Tm, iw, rs, space_der, dev)
+        if dev:
+            import torch
+            x = x.contiguous()
+            r = torch.empty_like(x)
+        else:
+            x = _f64(x)
+            r = np.zeros_like(x)
+        if (x.numel() if dev else x.size) != V:
+            raise ValueError("x needs V values")
+        check(self.lib.fpde_sf3d_matvec(self.h, C.byref(s), _ptr(x), _ptr(r), 1 if dev else 0), "fpde_sf3d_matvec")
+        return r
+
+    def sf3d_solve(self, dims, mat, mc, Tm, B, x0, thr, maxiter, iw=None, rs=None, space_der=0, exact=False):
+        """solve_mln<1> with vmul_T_3d over the V values from x0: returns (x, iterations). exact: the
+        reference's sequential dot products (bitwise its iterates); else deterministic tree sums."""
+        dev = _is_dev(x0)
+        s, keep, V = self._sf3d_system(dims, mat, mc, Tm, iw, rs, space_der, dev)
+        if dev:
+            x = x0.contiguous().clone()
+            B = B.contiguous()
+        else:
+            x = _f64(x0).copy()
+            B = _f64(B)
+        it = C.c_int(0)
+        check(self.lib.fpde_sf3d_solve(self.h, C.byref(s), _ptr(B), _ptr(x), float(thr), int(maxiter),
+                                       1 if exact else 0, C.byref(it), 1 if dev else 0), "fpde_sf3d_solve")
+        return x, it.value
+
     def tridiag_solve(self, a, b, r, om, u, n_lines, N, stride_elem, stride_line, left_kind=0,
                       left_val=None, right_kind=0, right_val=None, dLN=0.0):
         dev = _is_dev(u)
@@ -410,7 +463,9 @@ class Lod3D:
         reference's Richards problem, coefficients formed from the grid every step (coefA/B/Rlap
         may then be None); with c0 (and nu, sigma, D) also the salt concentration (equation 1).
         space_frac: optional dict(space_der, tol, max_iter, Tm=(3 rows), mc=(3 passes x 3 grids),
-        iw=(3 grids)) - the reference's implicit space-fractional line solves (impl 2).
+        iw=(3 grids)) - the reference's implicit space-fractional line solves (impl 2); with
+        implicit3d=1 its fully implicit scheme instead (one 3D solve per step; exact=1 for the
+        reference's sequential dot products).
         time_steps: optional tau_n of every step (variable steps); weight_rows: optional
         (max_steps, max_steps+1) matrix of the steps' kb_3_cache rows with kkk0 on the diagonal
         (else computed for g(t) = t^kernel_power)."""
@@ -476,7 +531,8 @@ class Lod3D:
                 d.weight_rows = wr.ctypes.data
         if space_frac is not None:
             f = SpaceFrac(space_der=int(space_frac.get("space_der", 0)), tol=float(space_frac.get("tol", 1e-9)),
-                          max_iter=int(space_frac.get("max_iter", 5000)))
+                          max_iter=int(space_frac.get("max_iter", 5000)),
+                          implicit3d=int(space_frac.get("implicit3d", 0)), exact=int(space_frac.get("exact", 0)))
             for q, nl in enumerate((sN, M, K)):
                 tm = np.ascontiguousarray(space_frac["Tm"][q], dtype=np.float64)
                 mc = np.ascontiguousarray(space_frac["mc"][q], dtype=np.float64)

@@ -119,3 +119,52 @@ size_t sf_smem_bytes(int n);
 int sf_prepare();
 
 }  // namespace fpde
+
+#include <vector>
+
+namespace fpde {
+
+// The fully implicit 3D space-fractional operator (implicit3d 1, spacefrac3d.cu) on the
+// V = (sN+2)(M+2)(K+2) + 1 values of a grid (i fastest) and the one past it. Device pointers.
+struct Sf3dSystem {
+    int sN = 0, M = 0, K = 0, sd = 0;
+    const double *mat = nullptr;         // 7 x V: Mat_3d[0..6]
+    const double *mc = nullptr;          // 9 x V: Mcoefs_3d[c][d] at plane 3c+d (c = 0 sN, 1 _M, 2 K)
+    const double *Tm[3] = {nullptr, nullptr, nullptr};   // axis c: len_c + 1 values
+    const double *iw = nullptr;          // 3 x V, or null (1.0)
+    const double *rs = nullptr;          // V row scales, or null
+};
+struct Sf3dWork;                         // the solve's device vectors
+int sf3d_work_create(const Sf3dSystem &s, Sf3dWork **w);
+void sf3d_work_destroy(Sf3dWork *w);
+// r = A x (bt: 3V scratch); two launches.
+int sf3d_enqueue_matvec(cudaStream_t st, const Sf3dSystem &s, double *bt, const double *x, double *r);
+// solve_mln<1> of A x = B from x (V values each), one cooperative launch; exact: the reference's
+// sequential dot products. iters_total (device, may be null) += iterations; iters_out (device int,
+// may be null) = iterations.
+int sf3d_enqueue_solve(cudaStream_t st, const Sf3dSystem &s, Sf3dWork *w, const double *B, double *x, double thr,
+                       int maxiter, bool exact, unsigned long long *iters_total, int *iters_out, unsigned *flags);
+
+// Right-hand side of one implicit3d LOD step (and the grid copied into the solve's x).
+struct Sf3dRhsArgs {
+    int sN = 0, M = 0, K = 0;
+    const double *U = nullptr;
+    double *x = nullptr, *Om = nullptr;
+    const double *rp = nullptr, *bc = nullptr;   // this step's rows (may be null)
+    const double *part = nullptr;        // history partials of the K pass, or KS = 0
+    int KS = 0;
+    int64_t pstride = 0;
+    double lam = 0;
+    int rkind[3] = {0, 0, 0};
+    double dLN[3] = {0, 0, 0};
+};
+int launch_sf3d_rhs(cudaStream_t st, const Sf3dRhsArgs &a);
+// U[v] = x[v] for the G grid nodes.
+int launch_sf3d_store(cudaStream_t st, const double *x, double *U, int64_t G);
+// Mat_3d (7 x V), Mcoefs_3d (9 x V) and the inv_dw_dh planes (3 x V) of a LOD with implicit3d, from
+// the per-pass coefficient grids (coefA/B/Rlap: 3 x G; mc[pass]: 3 x G; iw[pass]: G).
+void sf3d_assemble_host(int sN, int M, int K, const double *coefA, const double *coefB, const double *coefRlap,
+                        const double *const *mc, const double *const *iw, const int *rkind, double lamR,
+                        std::vector<double> &mat, std::vector<double> &mc3, std::vector<double> &iw3);
+
+}  // namespace fpde

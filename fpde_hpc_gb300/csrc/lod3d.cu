@@ -681,6 +681,12 @@ struct fpde_lod3d {
     double sf_thr = 0.0;
     double *sfc[3] = {nullptr, nullptr, nullptr}, *sfT[3] = {nullptr, nullptr, nullptr};
     unsigned long long *sf_iters = nullptr;   // iterations of every line solve since creation
+    // implicit3d (space_frac.implicit3d): the 3D system (Mat_3d, Mcoefs_3d, iw planes, Toeplitz rows),
+    // the solve's right-hand side and iterate (V = G + 1 values) and its workspace
+    bool sf3d = false, sf3d_exact = false;
+    Sf3dSystem s3;
+    Sf3dWork *s3work = nullptr;
+    double *s3buf = nullptr;                  // mat 7V, mc 9V, iw 3V, Om V, x V, Tm rows
     int64_t n_done = 0;
     GraphCache<int> graphs;                        // captured runs (at least GRAPH_MIN_STEPS steps)
 };
@@ -817,6 +823,30 @@ static void series_step(const fpde_lod3d *L, int64_t n, SeriesStep &cf)
     cf.tau = L->d.tau;
 }
 
+// One step of the fully implicit scheme (calc_step :5160-5716 with implicit3d 1): the right-hand
+// side (and the grid as the initial guess), the solve over the G + 1 values, the grid back.
+static int lod_sf3d_step(fpde_lod3d *L, cudaStream_t st, int64_t n, int KS)
+{
+    const int64_t V = L->G + 1;
+    double *Om = L->s3buf + 19 * V, *x = L->s3buf + 20 * V;
+    Sf3dRhsArgs r;
+    r.sN = L->dims[0]; r.M = L->dims[1]; r.K = L->dims[2];
+    r.U = L->U; r.x = x; r.Om = Om;
+    r.rp = L->rp ? L->rp + (n < L->rp_rows ? n : L->rp_rows - 1) * L->G : nullptr;
+    r.bc = L->bc ? L->bc + (n < L->bc_rows ? n : L->bc_rows - 1) * L->G : nullptr;
+    r.part = L->split ? L->Sn : L->part;
+    r.KS = KS;
+    r.pstride = L->P;
+    r.lam = L->lam;
+    for (int q = 0; q < 3; ++q) { r.rkind[q] = L->d.right_kind[q]; r.dLN[q] = L->d.dLN[q]; }
+    int rc;
+    if ((rc = launch_sf3d_rhs(st, r))) return rc;
+    if ((rc = sf3d_enqueue_solve(st, L->s3, L->s3work, Om, x, L->sf_thr, L->sf_maxit, L->sf3d_exact, L->sf_iters, nullptr,
+                                 L->ctx->d_flags)))
+        return rc;
+    return launch_sf3d_store(st, x, L->U, L->G);
+}
+
 static int lod_enqueue(fpde_lod3d *L, cudaStream_t st, int64_t n0, int steps, int64_t *nk)
 {
     int64_t k = 0;
@@ -894,9 +924,14 @@ static int lod_enqueue(fpde_lod3d *L, cudaStream_t st, int64_t n0, int steps, in
             Drow = L->ring + (int64_t)j * L->P;
             Drowf = L->ringf + (int64_t)j * L->P;
         }
-        for (int pass = 2; pass >= 0; --pass) {                      // K, _M, sN (calc_step order)
-            if ((rc = lod_launch_pass(L, st, pass, n, KS))) return rc;
-            ++k;
+        if (L->sf3d) {                                               // one 3D solve (implicit3d 1)
+            if ((rc = lod_sf3d_step(L, st, n, KS))) return rc;
+            k += 3;
+        } else {
+            for (int pass = 2; pass >= 0; --pass) {                  // K, _M, sN (calc_step order)
+                if ((rc = lod_launch_pass(L, st, pass, n, KS))) return rc;
+                ++k;
+            }
         }
         if ((rc = Drowf ? launch_append_ff(st, L->U, L->last, Drow, Drowf, L->G, L->P)
                         : launch_append(st, L->U, L->last, Drow, L->G, L->P)))
@@ -946,6 +981,8 @@ int fpde_lod3d_destroy(fpde_lod3d *L)
         dev_free(L->sfT[q]);
     }
     dev_free(L->sf_iters);
+    sf3d_work_destroy(L->s3work);
+    dev_free(L->s3buf);
     for (double *p : {L->C, L->lastC, L->DC, L->partC, L->C0}) dev_free(p);
     for (int q = 0; q < 3; ++q) {
         dev_free(L->vA[q]);
@@ -995,6 +1032,10 @@ int fpde_lod3d_create(fpde_ctx *ctx, const fpde_lod3d_desc *desc, const double *
                        "space_frac: lines longer than FPDE_SF_MAX_N intervals");
         for (int q = 0; q < 3; ++q)
             FPDE_CHECK_ARG(sfd->Tm[q] && sfd->mc[q] && sfd->iw[q], "space_frac: Tm, mc and iw of every pass required");
+        FPDE_CHECK_ARG(sfd->implicit3d == 0 || sfd->implicit3d == 1, "space_frac: implicit3d must be 0 or 1");
+        FPDE_CHECK_ARG(!sfd->exact || sfd->implicit3d, "space_frac: exact needs implicit3d");
+        FPDE_CHECK_ARG(!sfd->exact || (int64_t)(d.sN + 2) * (d.M + 2) * (d.K + 2) + 1 <= FPDE_SF3D_MAX_EXACT,
+                       "space_frac: exact dot products need at most FPDE_SF3D_MAX_EXACT values");
     }
     const bool vart = d.time_steps != nullptr;
     if (vart) {
@@ -1149,7 +1190,7 @@ int fpde_lod3d_create(fpde_ctx *ctx, const fpde_lod3d_desc *desc, const double *
         fail = sf_prepare() != FPDE_OK || dev_alloc((void **)&L->sf_iters, sizeof(unsigned long long)) ||
                cudaMemset(L->sf_iters, 0, sizeof(unsigned long long)) != cudaSuccess;
         std::vector<double> hc;
-        for (int pass = 0; pass < 3 && !fail; ++pass) {
+        for (int pass = 0; pass < 3 && !fail && !sfd->implicit3d; ++pass) {
             int Nl, n1, n2;
             int64_t s1, s2, stp;
             pass_geometry(L, pass, &Nl, &n1, &n2, &s1, &s2, &stp);
@@ -1172,6 +1213,36 @@ int fpde_lod3d_create(fpde_ctx *ctx, const fpde_lod3d_desc *desc, const double *
                    dev_alloc((void **)&L->sfT[pass], (size_t)m * sizeof(double)) ||
                    cudaMemcpy(L->sfc[pass], hc.data(), hc.size() * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess ||
                    cudaMemcpy(L->sfT[pass], tm.data(), (size_t)m * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess;
+        }
+        if (!fail && sfd->implicit3d) {        // the 3D system, constant over the steps (uniform tau)
+            L->sf3d = true;
+            L->sf3d_exact = sfd->exact != 0;
+            const int64_t V = L->G + 1;
+            const int len[3] = {d.sN, d.M, d.K};
+            std::vector<double> mat, mc3, iw3;
+            sf3d_assemble_host(d.sN, d.M, d.K, coefA, coefB, coefRlap, sfd->mc, sfd->iw, d.right_kind, L->lamR, mat,
+                               mc3, iw3);
+            const size_t rows = (size_t)(d.sN + d.M + d.K + 3);
+            std::vector<double> buf((size_t)21 * V + rows, 0.0);
+            std::copy(mat.begin(), mat.end(), buf.begin());
+            std::copy(mc3.begin(), mc3.end(), buf.begin() + 7 * V);
+            std::copy(iw3.begin(), iw3.end(), buf.begin() + 16 * V);
+            size_t o = (size_t)21 * V;
+            for (int c = 0; c < 3; ++c) {
+                for (int q = 2; q <= len[c]; ++q) buf[o + q] = sfd->Tm[c][q];   // entries 0 and 1 never read
+                o += (size_t)len[c] + 1;
+            }
+            fail = dev_alloc((void **)&L->s3buf, buf.size() * sizeof(double)) ||
+                   cudaMemcpy(L->s3buf, buf.data(), buf.size() * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess;
+            if (!fail) {
+                Sf3dSystem &S3 = L->s3;
+                S3.sN = d.sN; S3.M = d.M; S3.K = d.K; S3.sd = sfd->space_der;
+                S3.mat = L->s3buf; S3.mc = L->s3buf + 7 * V; S3.iw = L->s3buf + 16 * V; S3.rs = nullptr;
+                S3.Tm[0] = L->s3buf + 21 * V;
+                S3.Tm[1] = S3.Tm[0] + d.sN + 1;
+                S3.Tm[2] = S3.Tm[1] + d.M + 1;
+                fail = sf3d_work_create(S3, &L->s3work) != FPDE_OK;
+            }
         }
     }
     if (!fail && vart) {

@@ -457,10 +457,46 @@ int fpde_sf_solve(fpde_ctx *ctx, int lines, int n, const double *mat, const doub
  * with C tgamma for its Gamma). Host function. */
 int fpde_sf_toeplitz_row(double gamma, const double *Z, int n, double *Tm);
 
+/* The fully implicit 3D operator (the reference's implicit3d 1): vmul_T_3d (fpde_hpc_1d.cpp:
+ * 6801-8722, toeplitz_mult_alg 0, equation 0) on the V = (sN+2)(M+2)(K+2) + 1 values of a grid
+ * (i fastest, idx :1649) and the one past it, the vector solve_mln<1> runs over in calc_step
+ * (:5705). The product is the 7-diagonal Mat_3d (flat-index neighbours: planes 0/2 at -/+ (sN+2)(M+2),
+ * 3/4 at -/+ (sN+2), 5/6 at -/+ 1, the diagonal in 1, each pair applied when that axis has more
+ * than 2 intervals) plus, for each axis c = K, _M, sN in that order and at the nodes inside
+ * 1..len-1 on every axis, iw_c * T_c * tridiag(Mcoefs_3d[c]) along the node's axis-c line. Products
+ * equal the reference's bit for bit. */
+typedef struct fpde_sf3d_system {
+    int sN, M, K;               /* intervals along i, j, k (each 1 .. FPDE_SF_MAX_N) */
+    int space_der;              /* 0 one-sided, 1 two-sided */
+    const double *mat;          /* 7 x V: Mat_3d[0..6] */
+    const double *mc;           /* 9 x V: Mcoefs_3d[c][d] at plane 3c+d (c = 0 sN, 1 _M, 2 K; d = 0
+                                   lower, 1 diagonal, 2 upper); read at the interior nodes */
+    const double *Tm[3];        /* Toeplitz row of axis c: len_c + 1 values, entries 2..len_c-1 read */
+    const double *iw;           /* 3 x V: inv_dw_dh of the axis-c line through the node, or NULL (1.0) */
+    const double *rs;           /* V row scales (implicit_row_scaling: RS), or NULL */
+} fpde_sf3d_system;
+#define FPDE_SF3D_MAX_EXACT (1 << 22)   /* largest V of a solve with exact (sequential) dot products */
+
+/* r = A x over the V values (x, r: V each). */
+int fpde_sf3d_matvec(fpde_ctx *ctx, const fpde_sf3d_system *sys, const double *x, double *r, int on_device);
+/* solve_mln<1> of A x = B over the V values (rb = 0, re = V): x holds the initial guess and receives
+ * the solution; stops when |r.r / V| < thr or after maxiter - 1 iterations; *iters (host, may be
+ * NULL) receives the count. exact != 0: every dot product is the reference's sequential sum, so the
+ * iterates, the count and the solution equal the reference's bit for bit (one GPU thread adds each
+ * dot product: V <= FPDE_SF3D_MAX_EXACT); exact = 0: dot products are deterministic tree sums (the
+ * same on every run on a device; they differ from the reference's only in the order of the adds). A
+ * solve that breaks down maxiter times in a row or runs longer than 30 s stops: FPDE_ERR_NUMERIC. */
+int fpde_sf3d_solve(fpde_ctx *ctx, const fpde_sf3d_system *sys, const double *B, double *x, double thr, int maxiter,
+                    int exact, int *iters, int on_device);
+
 /* The implicit space-fractional solves of a 3D LOD (fpde_lod3d_desc.space_frac): per pass p the
  * Toeplitz row Tm[p] (Nl+1 values), the Mcoefs grids mc[p] (three host grids: lower, diagonal,
  * upper, at every interior line node) and inv_dw_dh iw[p] (one grid), and the solver's threshold
- * and iteration cap. Line lengths at most FPDE_SF_MAX_N. */
+ * and iteration cap. Line lengths at most FPDE_SF_MAX_N.
+ * implicit3d = 1 replaces the three passes of line solves by the reference's fully implicit scheme
+ * (calc_step :5160-5716 with implicit3d 1): each step adds every line's system of the K, _M and sN
+ * passes into one 3D system (the time term and the history in the K pass only) and solves it with
+ * fpde_sf3d_solve's solver over the G + 1 values (exact as in fpde_sf3d_solve). */
 typedef struct fpde_space_frac {
     int space_der;              /* 0 one-sided, 1 two-sided */
     double tol;                 /* impl_err (default 1e-9 in the reference) */
@@ -468,6 +504,8 @@ typedef struct fpde_space_frac {
     const double *Tm[3];
     const double *mc[3];        /* each 3 x grid */
     const double *iw[3];        /* each one grid */
+    int implicit3d;             /* 0: line solves per pass (LOD); 1: one 3D solve per step */
+    int exact;                  /* with implicit3d: sequential dot products */
 } fpde_space_frac;
 
 typedef struct fpde_lod3d_desc {
