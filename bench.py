@@ -52,6 +52,8 @@ def parse():
                     choices=["config2", "config3", "config4", "config5", "sum1", "sum2", "weights", "sf3d"])
     ap.add_argument("--space-der", type=int, default=0, choices=[0, 1],
                     help="sf3d: one-sided (0) or two-sided (1) space-fractional operator")
+    ap.add_argument("--implicit3d", type=int, default=0, choices=[0, 1],
+                    help="sf3d: line solves per pass (0) or the fully implicit scheme, one 3D solve per step (1)")
     ap.add_argument("--precision", default="auto", choices=["auto", "fp64", "bf16", "f16", "bf16x3"])
     ap.add_argument("--time-steps", type=int, default=None, help="override the workload's step count")
     ap.add_argument("--nodes", type=int, default=None, help="override the workload's size")
@@ -336,13 +338,20 @@ class SfWorkload(LodWorkload):
     def __init__(self, args):
         from fpde_hpc_gb300 import problems
         n = args.nodes or 64
+        self.impl3d = bool(args.implicit3d)
         self.p = problems.sf3d(n=n, steps=args.time_steps or 32, space_der=args.space_der)
-        self.name = "sf3d"
+        self.name = "sf3d_implicit3d" if self.impl3d else "sf3d"
         self.node_steps = self.p.node_steps
         side = "two-sided" if args.space_der else "one-sided"
-        self.metric = (f"node-steps/s (3D LOD with implicit space-fractional line solves, vmul_T + solve_mln<1>, "
-                       f"{n}^3, {self.p.steps} steps)")
-        self.desc = (f"3D LOD {n}^3, {self.p.steps} steps, alpha 0.8, gamma {self.p.gamma} {side}, tau 1e-3, "
+        if self.impl3d:
+            self.metric = (f"node-steps/s (fully implicit 3D space-fractional scheme, vmul_T_3d + solve_mln<1> over "
+                           f"the grid, {n}^3, {self.p.steps} steps)")
+            scheme = "fully implicit (implicit3d 1: one 3D solve per step, tree dot products)"
+        else:
+            self.metric = (f"node-steps/s (3D LOD with implicit space-fractional line solves, vmul_T + "
+                           f"solve_mln<1>, {n}^3, {self.p.steps} steps)")
+            scheme = "LOD (line solves per pass)"
+        self.desc = (f"3D {scheme} {n}^3, {self.p.steps} steps, alpha 0.8, gamma {self.p.gamma} {side}, tau 1e-3, "
                      "lognormal k (sigma 0.4, seed 11), Gaussian blob and source, Dirichlet 0 line ends, "
                      "solver threshold 1e-9 / 5000 iterations (the reference's defaults)")
         self._ops = None
@@ -359,12 +368,15 @@ class SfWorkload(LodWorkload):
         import fpde_hpc_gb300 as fp
         p = self.p
         cA, cB, cR, Tm, mc, iw, src = self.operands()
-        sf = dict(space_der=p.space_der, tol=p.tol, max_iter=p.max_iter, Tm=list(Tm), mc=list(mc), iw=list(iw))
+        sf = dict(space_der=p.space_der, tol=p.tol, max_iter=p.max_iter, Tm=list(Tm), mc=list(mc), iw=list(iw),
+                  implicit3d=1 if self.impl3d else 0)
         return fp.Lod3D(ctx, p.dims, p.alpha, p.tau, p.Da, cA, cB, cR, p.u0, p.steps, source=src, precision=prec,
                         space_frac=sf)
 
     def sample_lengths(self):
         S = self.p.steps
+        if self.impl3d:                  # the oracle's 3D solve is one thread's work: seconds per step at 64^3
+            return [1, 2, 3]
         return [max(1, S // 8), max(2, S // 4), max(3, S // 2)]
 
     def run_sample(self, s, threads):
@@ -380,9 +392,25 @@ class SfWorkload(LodWorkload):
         t0 = time.perf_counter()
         for n in range(s):
             kb, k0 = oracle.l1_weights(p.alpha, t, n)
-            oracle.lod_step_sf(p.dims, U, hist, n, kb, taus, p.Da, k0, cA, cB, cR, mc, iw, Tm, p.space_der, p.tol,
-                               p.max_iter, src, bc)
+            if self.impl3d:
+                oracle.lod_step_sf3d(p.dims, U.reshape(-1), 0.0, hist.reshape(s, -1), n, kb, taus, p.Da, k0, cA, cB,
+                                     cR, mc, iw, Tm, p.space_der, p.tol, p.max_iter, src, bc)
+            else:
+                oracle.lod_step_sf(p.dims, U, hist, n, kb, taus, p.Da, k0, cA, cB, cR, mc, iw, Tm, p.space_der,
+                                   p.tol, p.max_iter, src, bc)
         return time.perf_counter() - t0
+
+    def grid_iteration_ops(self):
+        """FP64 flops of one iteration of the 3D solve over V = (n+2)^3 + 1 values: three products
+        vmul_T_3d (seven diagonals 13 per value; Bt 5 per interior node and axis; per interior node and
+        axis the Toeplitz sum, 2 per term: n-2 terms two-sided, (n-2)/2 on average one-sided, plus the
+        iw product and the add), five dot products (2 per value) and the vector updates (11 per value)."""
+        n = self.p.dims[0]
+        V = (n + 2) ** 3 + 1
+        inner = (n - 1) ** 3
+        terms = (n - 2) if self.p.space_der else (n - 2) / 2.0
+        mv = 13 * V + 3 * inner * (5 + 2 * terms + 2)
+        return 3 * mv + 10 * V + 11 * V
 
     def line_iteration_ops(self):
         """FP64 operations (multiplies and adds, one each per lane) of one solver iteration on a line
@@ -1068,6 +1096,20 @@ def run_ours(args):
                                     "FP64 pipe and its per-step chain, not by HBM or the tensor cores")
         elif "hist_gemv" in kernels:
             out["roofline"] = dict(kernels["hist_gemv"])
+    elif is_sf and wl.impl3d:
+        # one persistent cooperative kernel per step, FP64-pipe bound: the products' Toeplitz terms are
+        # fused multiply-adds (2 flops each), the rest separate multiplies and adds; the tree dot
+        # products and the updates are L2-resident traffic
+        ops = sf_iters * wl.grid_iteration_ops()
+        gops = ops / (ms / 1e3) / 1e9
+        out["roofline"] = {"kernel": "k_sf3d_solve (vmul_T_3d + solve_mln<1>, persistent cooperative)",
+                           "bound": "fp64", "achieved": gops, "peak": 1250.0, "unit": "GFLOP/s (FP64)",
+                           "frac": gops / 1250.0,
+                           "peak_source": "nominal GB300 FP64 1.25 TFLOP/s (an FMA counted as 2 flops)",
+                           "traffic": None,
+                           "note": (f"{sf_iters:.0f} solver iterations per run ({sf_iters / steps:.1f} per step) x "
+                                    f"{wl.grid_iteration_ops():.3g} FP64 flops per iteration; ncu on 64^3: FP64 "
+                                    "pipe 69% active (profiles/k_sf3d_solve_64cube.md)")}
     elif is_sf:
         # the line solves are FP64-pipe work: every multiply and add of vmul_T, the dot products and
         # the updates is one FP64 operation per lane (no contracted FMAs: they would change the

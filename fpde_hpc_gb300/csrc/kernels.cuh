@@ -137,8 +137,8 @@ struct Sf3dSystem {
 struct Sf3dWork;                         // the solve's device vectors
 int sf3d_work_create(const Sf3dSystem &s, Sf3dWork **w);
 void sf3d_work_destroy(Sf3dWork *w);
-// r = A x (bt: 3V scratch); two launches.
-int sf3d_enqueue_matvec(cudaStream_t st, const Sf3dSystem &s, double *bt, const double *x, double *r);
+// r = A x (tc: 3V scratch for the axes' Toeplitz terms); two launches.
+int sf3d_enqueue_matvec(cudaStream_t st, const Sf3dSystem &s, double *tc, const double *x, double *r);
 // solve_mln<1> of A x = B from x (V values each), one cooperative launch; exact: the reference's
 // sequential dot products. iters_total (device, may be null) += iterations; iters_out (device int,
 // may be null) = iterations.

@@ -1034,6 +1034,8 @@ int fpde_lod3d_create(fpde_ctx *ctx, const fpde_lod3d_desc *desc, const double *
             FPDE_CHECK_ARG(sfd->Tm[q] && sfd->mc[q] && sfd->iw[q], "space_frac: Tm, mc and iw of every pass required");
         FPDE_CHECK_ARG(sfd->implicit3d == 0 || sfd->implicit3d == 1, "space_frac: implicit3d must be 0 or 1");
         FPDE_CHECK_ARG(!sfd->exact || sfd->implicit3d, "space_frac: exact needs implicit3d");
+        FPDE_CHECK_ARG(!sfd->implicit3d || (int64_t)(d.sN + 2) * (d.M + 2) * (d.K + 2) + 1 < ((int64_t)1 << 31),
+                       "space_frac: implicit3d needs (sN+2)(M+2)(K+2) + 1 below 2^31");
         FPDE_CHECK_ARG(!sfd->exact || (int64_t)(d.sN + 2) * (d.M + 2) * (d.K + 2) + 1 <= FPDE_SF3D_MAX_EXACT,
                        "space_frac: exact dot products need at most FPDE_SF3D_MAX_EXACT values");
     }

@@ -4,12 +4,13 @@
 // solve_mln<1> (:812-1157) that calc_step (:5681-5716) runs on it once per step over the V = G + 1
 // values of the grid (G = (sN+2)(M+2)(K+2) nodes, i fastest, plus the one past the grid).
 //
-// The product is node-parallel. A first phase forms each axis's Bt = tridiag(Mcoefs_3d[axis]) x at
-// the interior nodes (the only ones the Toeplitz sums read); a second forms every output in the
-// reference's order: the seven diagonals with its flat-index bounds, then the K, _M and sN Toeplitz
-// terms, each one thread's sequential sum over its line without contracted multiply-adds. So a
-// product equals the reference's bit for bit. All vectors are node-major and stay in L2 for the
-// grids this scheme is run on (a 64^3 grid is 2.3 MB per vector).
+// The product runs in two phases. In the first a warp owns one line of one axis: it forms the
+// line's Bt = tridiag(Mcoefs_3d[axis]) x in shared memory and each lane sums the Toeplitz terms of
+// two rows (p and n - p, so every lane runs a chain of equal length), each term one lane's
+// sequential sum without contracted multiply-adds. The second forms every output in the reference's
+// order: the seven diagonals with its flat-index bounds, then the K, _M and sN terms. So a product
+// equals the reference's bit for bit. All vectors are node-major and stay in L2 for the grids this
+// scheme is run on (a 64^3 grid is 2.3 MB per vector); the sums are FP64-pipe work.
 //
 // A solve is one persistent cooperative kernel: every thread owns a fixed set of nodes, the vector
 // updates need no synchronisation, and a bounded grid barrier separates the phases whose reads cross
@@ -19,7 +20,10 @@
 //          reference's bit for bit; the add chain runs on one thread (use on small grids);
 //   fast:  each thread adds its nodes, each CTA folds its threads in a fixed tree and every CTA
 //          folds the CTA partials in the same fixed order, so the result is deterministic and
-//          identical in every CTA, and differs from the reference's only by the order of the adds.
+//          identical in every CTA, and differs from the reference's only by the order of the adds;
+//          the products' Toeplitz terms are fused multiply-adds (one FP64 instruction per term
+//          instead of two, the pipe the sums are bound by; each term rounds once instead of twice).
+#include <algorithm>
 #include <cmath>
 #include <vector>
 
@@ -35,6 +39,9 @@ __device__ __forceinline__ double dm(double a, double b) { return __dmul_rn(a, b
 __device__ __forceinline__ double da(double a, double b) { return __dadd_rn(a, b); }
 __device__ __forceinline__ double ds(double a, double b) { return __dsub_rn(a, b); }
 
+#ifndef SF3_MIN_CTAS
+#define SF3_MIN_CTAS 2        // co-resident CTAs per SM the solve's register budget is cut for
+#endif
 constexpr int SF3_THREADS = 256;
 constexpr int SF3_WARPS = SF3_THREADS / 32;
 constexpr uint64_t SF3_TIME_LIMIT_NS = 30ull * 1000000000ull;   // per solve
@@ -59,52 +66,114 @@ __device__ __forceinline__ Geo geo_of(const Sf3dSystem &s)
 __device__ __forceinline__ bool interior(const Geo &g, int64_t v, int *i, int *j, int *k)
 {
     if (v >= g.G) return false;
-    const int64_t kk = v / g.sz, rem = v - kk * g.sz;
-    const int64_t jj = rem / g.sy, ii = rem - jj * g.sy;
+    const unsigned u = (unsigned)v, sz = (unsigned)g.sz, sy = (unsigned)g.sy;   // V < 2^31
+    const unsigned kk = u / sz, rem = u - kk * sz;
+    const unsigned jj = rem / sy, ii = rem - jj * sy;
     *i = (int)ii; *j = (int)jj; *k = (int)kk;
-    return ii >= 1 && ii < g.sN && jj >= 1 && jj < g.M && kk >= 1 && kk < g.K;
+    return ii >= 1 && (int)ii < g.sN && jj >= 1 && (int)jj < g.M && kk >= 1 && (int)kk < g.K;
 }
 
-// Bt of the three axes at node v (:7254-7261, :7677-7684, :8097-8104): Mcoefs_3d[c][1] x, then the
-// lower and the upper neighbour along the axis (always inside the vector at an interior node).
-__device__ __forceinline__ void bt_node(const Sf3dSystem &s, const Geo &g, const double *x, double *bt, int64_t v)
+// The lines of the product's Toeplitz terms: axis 2 (K) over (i, j), axis 1 (_M) over (i, k), axis 0
+// (sN) over (j, k), each coordinate 1..len-1, an axis only when it has more than 2 intervals. Line l
+// of the concatenation as its axis, first node (position 0) and node stride.
+struct LineSet {
+    int64_t n2, n1, n0;                  // lines of each axis
+};
+__device__ __forceinline__ LineSet lines_of(const Geo &g)
 {
-    int i, j, k;
-    if (!interior(g, v, &i, &j, &k)) return;
+    LineSet L;
+    L.n2 = g.K > 2 ? (int64_t)(g.sN - 1) * (g.M - 1) : 0;
+    L.n1 = g.M > 2 ? (int64_t)(g.sN - 1) * (g.K - 1) : 0;
+    L.n0 = g.sN > 2 ? (int64_t)(g.M - 1) * (g.K - 1) : 0;
+    return L;
+}
+__device__ __forceinline__ void line_at(const Geo &g, const LineSet &L, int64_t l, int *c, int64_t *base,
+                                        int64_t *st, int *n)
+{
+    unsigned u = (unsigned)l;
+    if (l < L.n2) {
+        const unsigned d = (unsigned)(g.sN - 1), b = u / d, i = 1 + u - b * d, j = 1 + b;
+        *c = 2; *base = i + (int64_t)j * g.sy; *st = g.sz; *n = g.K;
+    } else if (l < L.n2 + L.n1) {
+        u -= (unsigned)L.n2;
+        const unsigned d = (unsigned)(g.sN - 1), b = u / d, i = 1 + u - b * d, k = 1 + b;
+        *c = 1; *base = i + (int64_t)k * g.sz; *st = g.sy; *n = g.M;
+    } else {
+        u -= (unsigned)(L.n2 + L.n1);
+        const unsigned d = (unsigned)(g.M - 1), b = u / d, j = 1 + u - b * d, k = 1 + b;
+        *c = 0; *base = (int64_t)j * g.sy + (int64_t)k * g.sz; *st = 1; *n = g.sN;
+    }
+}
+
+// One warp, one line of axis c (FUSED: each term a fused multiply-add, the fast solve's form; else
+// the reference's separately rounded product and sum): Bt = tridiag(Mcoefs_3d[c]) x at positions 1..n-1 (:7254-7261,
+// :7677-7684, :8097-8104: the diagonal term, then the lower and the upper neighbour along the axis)
+// into the warp's shared slice, then every row's Toeplitz term (:7562-7574 and the other axes):
+// the sum over j < p in increasing j, then (two-sided) the subtraction over j > p, one lane's
+// sequential chain per row, row scaling and inv_dw_dh as the reference applies them; tc[c][node] =
+// the term. A lane takes the rows p and n - p (one-sided: p - 1 and n - p - 1 terms, n - 2 together;
+// two-sided: n - 2 each), so the lanes of a warp run equal chains.
+template <bool FUSED>
+__device__ __forceinline__ void line_terms(const Sf3dSystem &s, const Geo &g, const double *rows, double *sl,
+                                           const double *x, double *tc, int c, int64_t base, int64_t st, int n)
+{
+    const int lane = threadIdx.x & 31;
     const int64_t V = g.V;
-    const double xv = __ldcg(x + v);
-#pragma unroll
-    for (int c = 2; c >= 0; --c) {
-        const int n = c == 2 ? g.K : (c == 1 ? g.M : g.sN);
-        if (n <= 2) continue;
-        const int64_t st = c == 2 ? g.sz : (c == 1 ? g.sy : 1);
-        const double *mc = s.mc + (int64_t)(3 * c) * V;
-        double b = dm(__ldg(mc + V + v), xv);
+    const double *mc = s.mc + (int64_t)(3 * c) * V;
+    for (int q = 1 + lane; q < n; q += 32) {
+        const int64_t v = base + (int64_t)q * st;
+        double b = dm(__ldg(mc + V + v), __ldcg(x + v));
         b = da(b, dm(__ldg(mc + v), __ldcg(x + v - st)));
         b = da(b, dm(__ldg(mc + 2 * V + v), __ldcg(x + v + st)));
-        bt[(int64_t)c * V + v] = b;
+        sl[q] = b;
     }
+    __syncwarp();
+    // row c of the Toeplitz rows and of their negated copy (load_rows): a term subtracted is the
+    // product with -Tm, the same rounding as the subtraction of the product
+    const int off = c == 0 ? 0 : (c == 1 ? g.sN + 1 : g.sN + g.M + 2);
+    const double *Tp = rows + off, *Tn = rows + (g.sN + g.M + g.K + 3) + off;
+    const double *iw = s.iw ? s.iw + (int64_t)c * V : nullptr;
+    double *out = tc + (int64_t)c * V;
+    const int pairs = n / 2;                                 // rows 1..n-1 as (k+1, n-1-k)
+    for (int k = lane; k < pairs; k += 32) {
+        const int a = k + 1, b = n - 1 - k;
+        const int na = s.sd ? n - 2 : a - 1;
+        const int nb = a == b ? 0 : (s.sd ? n - 2 : b - 1);
+        // the lane's terms in up to four runs of consecutive j: row a below (j = 1..a-1, Tm[a-j+1]),
+        // row a above (two-sided: j = a+1..n-1, -Tm[j-a+1]), then the same for row b
+        double t = 0.0, ta = 0.0;
+        int seg = 0, q = 1, ti = a, dti = -1, cnt = a - 1;
+        const double *T = Tp;
+        for (int r = 0; r < na + nb; ++r) {
+            while (cnt == 0 && seg < 3) {
+                ++seg;
+                if (seg == 1) { q = a + 1; ti = 2; dti = 1; T = Tn; cnt = s.sd ? n - 1 - a : 0; }
+                else if (seg == 2) { ta = t; t = 0.0; q = 1; ti = b; dti = -1; T = Tp; cnt = b - 1; }
+                else { q = b + 1; ti = 2; dti = 1; T = Tn; cnt = s.sd ? n - 1 - b : 0; }
+            }
+            if (FUSED) t = fma(sl[q], T[ti], t);             // one rounding per term
+            else t = da(t, dm(sl[q], T[ti]));
+            ++q; ti += dti; --cnt;
+        }
+        double tb = t;
+        if (nb == 0) ta = t;
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            if (h == 1 && nb == 0) break;
+            const int p = h == 0 ? a : b;
+            const int64_t v = base + (int64_t)p * st;
+            double val = h == 0 ? ta : tb;
+            if (s.rs) val = __ddiv_rn(val, __ldg(s.rs + v));
+            out[v] = iw ? dm(val, __ldg(iw + v)) : val;
+        }
+    }
+    __syncwarp();
 }
 
-// One axis's Toeplitz term at position p of its line (:7562-7574): the sum over j < p, then (two-sided)
-// the subtraction over j > p, in increasing j; row scaling and inv_dw_dh as the reference applies them.
-__device__ __forceinline__ double axis_term(const double *bt, int64_t base, int64_t st, int p, int n, int sd,
-                                            const double *T, const double *rs, const double *iw, int64_t v)
-{
-    double t = 0.0;
-    const int qe = sd ? n : p;
-    for (int q = 1; q < qe; ++q) {
-        if (q == p) continue;
-        const double pr = dm(__ldcg(bt + base + (int64_t)q * st), T[q < p ? p - q + 1 : q - p + 1]);
-        t = q < p ? da(t, pr) : ds(t, pr);
-    }
-    if (rs) t = __ddiv_rn(t, __ldg(rs + v));
-    return iw ? dm(t, __ldg(iw + v)) : t;
-}
-
-// Output v of the product (:6857-6877 and the three axes' sums). Tm: the three rows in shared memory.
-__device__ __forceinline__ double row_node(const Sf3dSystem &s, const Geo &g, const double *const *Tm,
-                                           const double *x, const double *bt, int64_t v)
+// Output v of the product (:6857-6877), then the K, _M and sN terms in that order at the nodes
+// inside 1..len-1 on every axis.
+__device__ __forceinline__ double row_node(const Sf3dSystem &s, const Geo &g, const double *x, const double *tc,
+                                           int64_t v)
 {
     const int64_t V = g.V;
     const double *M = s.mat;
@@ -123,49 +192,53 @@ __device__ __forceinline__ double row_node(const Sf3dSystem &s, const Geo &g, co
     }
     int i, j, k;
     if (!interior(g, v, &i, &j, &k)) return r;
-    if (g.K > 2)
-        r = da(r, axis_term(bt + 2 * V, v - (int64_t)k * g.sz, g.sz, k, g.K, s.sd, Tm[2], s.rs,
-                            s.iw ? s.iw + 2 * V : nullptr, v));
-    if (g.M > 2)
-        r = da(r, axis_term(bt + V, v - (int64_t)j * g.sy, g.sy, j, g.M, s.sd, Tm[1], s.rs,
-                            s.iw ? s.iw + V : nullptr, v));
-    if (g.sN > 2)
-        r = da(r, axis_term(bt, v - i, 1, i, g.sN, s.sd, Tm[0], s.rs, s.iw, v));
+    if (g.K > 2) r = da(r, __ldcg(tc + 2 * V + v));
+    if (g.M > 2) r = da(r, __ldcg(tc + V + v));
+    if (g.sN > 2) r = da(r, __ldcg(tc + v));
     return r;
 }
 
-// The three Toeplitz rows into shared memory (lengths sN, M, K; entries 2..len-1 are read).
-__device__ __forceinline__ void load_rows(const Sf3dSystem &s, double *sm, const double **Tm)
+// Shared memory of a CTA: the three Toeplitz rows (lengths sN, M, K + 1; entries 2..len-1 are read)
+// and their negated copy, then one line slice of max(sN, M, K) + 1 values per warp.
+__device__ __forceinline__ double *load_rows(const Sf3dSystem &s, double *sm)
 {
-    const int n0 = s.sN + 1, n1 = s.M + 1, n2 = s.K + 1;
-    Tm[0] = sm; Tm[1] = sm + n0; Tm[2] = sm + n0 + n1;
-    for (int q = threadIdx.x; q < n0 + n1 + n2; q += blockDim.x) {
+    const int n0 = s.sN + 1, n1 = s.M + 1, n2 = s.K + 1, nr = n0 + n1 + n2;
+    for (int q = threadIdx.x; q < nr; q += blockDim.x) {
         double v;
         if (q < n0) v = s.Tm[0][q];
         else if (q < n0 + n1) v = s.Tm[1][q - n0];
         else v = s.Tm[2][q - n0 - n1];
         sm[q] = v;
+        sm[nr + q] = -v;
     }
     __syncthreads();
+    const int nmax = max(s.sN, max(s.M, s.K));
+    return sm + 2 * nr + (size_t)(threadIdx.x >> 5) * (nmax + 1);
 }
 
 // -------------------------------------------------------------------- standalone product
 
-__global__ void __launch_bounds__(SF3_THREADS) k_sf3d_bt(Sf3dSystem s, const double *x, double *bt)
-{
-    const Geo g = geo_of(s);
-    for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < g.V; v += (int64_t)gridDim.x * blockDim.x)
-        bt_node(s, g, x, bt, v);
-}
-
-__global__ void __launch_bounds__(SF3_THREADS) k_sf3d_rows(Sf3dSystem s, const double *x, const double *bt, double *r)
+__global__ void __launch_bounds__(SF3_THREADS) k_sf3d_terms(Sf3dSystem s, const double *x, double *tc)
 {
     extern __shared__ double sf3_sm[];
-    const double *Tm[3];
-    load_rows(s, sf3_sm, Tm);
+    double *sl = load_rows(s, sf3_sm);
+    const Geo g = geo_of(s);
+    const LineSet L = lines_of(g);
+    const int64_t nl = L.n2 + L.n1 + L.n0;
+    const int64_t w0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5, W = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t l = w0; l < nl; l += W) {
+        int c, n;
+        int64_t base, st;
+        line_at(g, L, l, &c, &base, &st, &n);
+        line_terms<false>(s, g, sf3_sm, sl, x, tc, c, base, st, n);
+    }
+}
+
+__global__ void __launch_bounds__(SF3_THREADS) k_sf3d_rows(Sf3dSystem s, const double *x, const double *tc, double *r)
+{
     const Geo g = geo_of(s);
     for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < g.V; v += (int64_t)gridDim.x * blockDim.x)
-        r[v] = row_node(s, g, Tm, x, bt, v);
+        r[v] = row_node(s, g, x, tc, v);
 }
 
 // -------------------------------------------------------------------------- the solve
@@ -174,7 +247,7 @@ struct SolveArgs {
     Sf3dSystem s;
     double *x;                 // initial guess in, solution out
     const double *B;
-    double *r, *q0, *g0, *g1, *w0, *w1, *u, *Au, *bt;   // V each (bt: 3V)
+    double *r, *q0, *g0, *g1, *w0, *w1, *u, *Au, *tc;   // V each (tc: the axes' terms, 3V)
     double *prod;              // exact: 2V products
     double *part;              // fast: 2 x gridDim partials
     double *gscal;             // exact: the sums (2)
@@ -191,63 +264,81 @@ template <bool EXACT>
 struct Solver {
     const SolveArgs &a;
     Geo g;
-    const double *Tm[3];
+    const double *rows;        // the Toeplitz rows (shared)
+    double *sl;                // the warp's line slice (shared)
     int64_t gt, GT;
     double *wsum;              // shared: 2 x SF3_WARPS
     double *res;               // shared: 2
 
     __device__ bool sync() { return grid_barrier(a.bar, gridDim.x, a.flags); }
 
-    // y = A x (two phases, one barrier between them); the caller has synchronised x.
+    // y = A x: the lines' Toeplitz terms (a warp per line), a barrier, the rows; the caller has
+    // synchronised x.
     __device__ bool apply(const double *x, double *y)
     {
-        for (int64_t v = gt; v < g.V; v += GT) bt_node(a.s, g, x, a.bt, v);
+        const LineSet L = lines_of(g);
+        const int64_t nl = L.n2 + L.n1 + L.n0;
+        for (int64_t l = gt >> 5; l < nl; l += GT >> 5) {
+            int c, n;
+            int64_t base, st;
+            line_at(g, L, l, &c, &base, &st, &n);
+            line_terms<!EXACT>(a.s, g, rows, sl, x, a.tc, c, base, st, n);
+        }
         if (!sync()) return false;
-        for (int64_t v = gt; v < g.V; v += GT) y[v] = row_node(a.s, g, Tm, x, a.bt, v);
+        for (int64_t v = gt; v < g.V; v += GT) y[v] = row_node(a.s, g, x, a.tc, v);
         return true;
     }
 
-    // A product term of dot slot q: exact stores it, fast adds it to the thread's partial.
-    __device__ __forceinline__ void term(int q, int64_t v, double p, double *acc, bool neg)
+    // A term of dot product Q: exact stores it, fast adds it to (NEG: subtracts it from) the
+    // thread's partial.
+    template <int Q, bool NEG>
+    __device__ __forceinline__ void term(int64_t v, double p, double &acc)
     {
-        if (EXACT) a.prod[(int64_t)q * g.V + v] = p;
-        else acc[q] = neg ? ds(acc[q], p) : da(acc[q], p);
+        if (EXACT) a.prod[(int64_t)Q * g.V + v] = p;
+        else acc = NEG ? ds(acc, p) : da(acc, p);
     }
 
-    // The nd dot products whose terms every thread has just produced; out[q] in every thread.
-    // neg[q]: the reference subtracts the terms from 0.0 (beta's "beta -= q*r").
-    __device__ bool dots(int nd, const double *acc, const bool *neg, double *out)
+    // Dot product slot q of a CTA (fast form): fold the threads' partials in a fixed tree.
+    __device__ __forceinline__ void fold_cta(int q, double t)
+    {
+        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+        for (int o = 16; o >= 1; o >>= 1) t = da(t, __shfl_down_sync(0xffffffffu, t, o));
+        if (lane == 0) wsum[q * SF3_WARPS + warp] = t;
+    }
+
+    // The ND dot products whose terms every thread has just produced (acc0, acc1: the thread's
+    // partials in the fast form); o0, o1 in every thread. NEG0: the first is the reference's
+    // "beta -= q*r" (terms subtracted from 0.0).
+    template <int ND, bool NEG0>
+    __device__ bool dots(double acc0, double acc1, double &o0, double &o1)
     {
         const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
         if (EXACT) {
             if (!sync()) return false;
-            if (blockIdx.x == 0 && lane == 0 && warp < nd) {
+            if (blockIdx.x == 0 && lane == 0 && warp < ND) {
                 const double *p = a.prod + (int64_t)warp * g.V;
                 double t = 0.0;
-                if (neg[warp])
+                if (NEG0 && warp == 0)
                     for (int64_t v = 0; v < g.V; ++v) t = ds(t, __ldcg(p + v));
                 else
                     for (int64_t v = 0; v < g.V; ++v) t = da(t, __ldcg(p + v));
                 a.gscal[warp] = t;
             }
             if (!sync()) return false;
-            if (tid < nd) res[tid] = __ldcg(a.gscal + tid);
+            if (tid < ND) res[tid] = __ldcg(a.gscal + tid);
             __syncthreads();
         } else {
-            for (int q = 0; q < nd; ++q) {
-                double t = acc[q];
-#pragma unroll
-                for (int o = 16; o >= 1; o >>= 1) t = da(t, __shfl_down_sync(0xffffffffu, t, o));
-                if (lane == 0) wsum[q * SF3_WARPS + warp] = t;
-            }
+            fold_cta(0, acc0);
+            if (ND > 1) fold_cta(1, acc1);
             __syncthreads();
-            if (tid < nd) {
+            if (tid < ND) {
                 double t = 0.0;
                 for (int w = 0; w < SF3_WARPS; ++w) t = da(t, wsum[tid * SF3_WARPS + w]);
                 a.part[(int64_t)tid * gridDim.x + blockIdx.x] = t;
             }
             if (!sync()) return false;
-            if (warp < nd) {
+            if (warp < ND) {
                 const double *p = a.part + (int64_t)warp * gridDim.x;
                 double t = 0.0;
                 for (unsigned b = lane; b < gridDim.x; b += 32) t = da(t, __ldcg(p + b));
@@ -257,7 +348,8 @@ struct Solver {
             }
             __syncthreads();
         }
-        for (int q = 0; q < nd; ++q) out[q] = res[q];
+        o0 = res[0];
+        if (ND > 1) o1 = res[1];
         __syncthreads();
         return true;
     }
@@ -268,14 +360,15 @@ struct Solver {
 // iteration with the q.r reuse and the w/g shift). A start repeated more than maxiter times without
 // an iteration between, the time limit or a barrier that times out ends the solve with a flag.
 template <bool EXACT>
-__global__ void __launch_bounds__(SF3_THREADS) k_sf3d_solve(SolveArgs a)
+__global__ void __launch_bounds__(SF3_THREADS, SF3_MIN_CTAS) k_sf3d_solve(SolveArgs a)
 {
     extern __shared__ double sf3_sm[];
     __shared__ double wsum[2 * SF3_WARPS];
     __shared__ double res[2];
     __shared__ unsigned stop_s;
     Solver<EXACT> S{a};
-    load_rows(a.s, sf3_sm, S.Tm);
+    S.rows = sf3_sm;
+    S.sl = load_rows(a.s, sf3_sm);
     S.g = geo_of(a.s);
     S.gt = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     S.GT = (int64_t)gridDim.x * blockDim.x;
@@ -287,8 +380,7 @@ __global__ void __launch_bounds__(SF3_THREADS) k_sf3d_solve(SolveArgs a)
     double *x = a.x, *r = a.r, *q0 = a.q0, *u = a.u, *Au = a.Au;
     double *g0 = a.g0, *g1 = a.g1, *w0 = a.w0, *w1 = a.w1;
     const double *B = a.B;
-    const bool pos[2] = {false, false}, negq[2] = {true, false};
-    double c1 = 0.0, al = 0.0, out[2], acc[2];
+    double c1 = 0.0, al = 0.0, o0 = 0.0, o1 = 0.0, acc0, acc1;
     int iter = 1, restarts = 0;
     bool have_qr = false;
 restart:
@@ -298,14 +390,14 @@ restart:
     }
     have_qr = false;
     if (!S.apply(x, r)) return;                                                       // :841-844
-    acc[0] = acc[1] = 0.0;
+    acc0 = 0.0;
     for (int64_t v = gt; v < V; v += GT) {
         const double e = ds(B[v], r[v]);
         r[v] = e; g1[v] = e; q0[v] = e;
-        S.term(0, v, dm(e, e), acc, false);                                           // norm (:864)
+        S.template term<0, false>(v, dm(e, e), acc0);                                 // norm (:864)
     }
     if (blockIdx.x == 0 && threadIdx.x == 0 && gtimer_ns() - t0 > SF3_TIME_LIMIT_NS) atomicExch(a.gstop, 1u);
-    if (!S.dots(1, acc, pos, out)) return;
+    if (!S.template dots<1, false>(acc0, 0.0, o0, o1)) return;
     if (threadIdx.x == 0) stop_s = __ldcg(a.gstop);
     __syncthreads();
     if (stop_s) {                                                                     // restarts past the limit
@@ -313,20 +405,20 @@ restart:
         goto out;
     }
     {
-        const double norm = out[0];
+        const double norm = o0;
         if (!S.apply(g1, w1)) return;                                                 // :851
-        acc[0] = 0.0;
-        for (int64_t v = gt; v < V; v += GT) S.term(0, v, dm(q0[v], w1[v]), acc, false);   // c[1] (:853-856)
-        if (!S.dots(1, acc, pos, out)) return;
-        c1 = out[0];
+        acc0 = 0.0;
+        for (int64_t v = gt; v < V; v += GT) S.template term<0, false>(v, dm(q0[v], w1[v]), acc0);   // c[1]
+        if (!S.template dots<1, false>(acc0, 0.0, o0, o1)) return;
+        c1 = o0;
         if (fabs(__ddiv_rn(norm, md)) < a.thr) goto out;                               // :866
     }
     for (;;) {
         if (!have_qr) {                                                                // :871-877
-            acc[0] = 0.0;
-            for (int64_t v = gt; v < V; v += GT) S.term(0, v, dm(q0[v], r[v]), acc, false);
-            if (!S.dots(1, acc, pos, out)) return;
-            al = __ddiv_rn(out[0], c1);
+            acc0 = 0.0;
+            for (int64_t v = gt; v < V; v += GT) S.template term<0, false>(v, dm(q0[v], r[v]), acc0);
+            if (!S.template dots<1, false>(acc0, 0.0, o0, o1)) return;
+            al = __ddiv_rn(o0, c1);
         }
         if (!(c1 != 0.0)) goto restart;                                                // :878, :913
         for (int64_t v = gt; v < V; v += GT) {
@@ -335,28 +427,28 @@ restart:
         }
         if (!S.sync()) return;
         if (!S.apply(u, Au)) return;                                                  // :890
-        acc[0] = acc[1] = 0.0;
+        acc0 = acc1 = 0.0;
         for (int64_t v = gt; v < V; v += GT) {
             const double av = Au[v];
-            S.term(0, v, dm(av, av), acc, false);
-            S.term(1, v, dm(av, u[v]), acc, false);
+            S.template term<0, false>(v, dm(av, av), acc0);
+            S.template term<1, false>(v, dm(av, u[v]), acc1);
         }
-        if (!S.dots(2, acc, pos, out)) return;
-        const double nrm = out[0];
-        const double ro1 = __ddiv_rn(-out[1], nrm);                                   // :903
+        if (!S.template dots<2, false>(acc0, acc1, o0, o1)) return;
+        const double nrm = o0;
+        const double ro1 = __ddiv_rn(-o1, nrm);                                       // :903
         if (nrm == 0.0) goto restart;                                                  // :904-905
         for (int64_t v = gt; v < V; v += GT) x[v] = ds(x[v], dm(ro1, u[v]));
         if (!S.sync()) return;
         if (!S.apply(x, r)) return;                                                   // :943-947
-        acc[0] = acc[1] = 0.0;
+        acc0 = acc1 = 0.0;
         for (int64_t v = gt; v < V; v += GT) {
             const double e = ds(B[v], r[v]);
             r[v] = e;
-            S.term(0, v, dm(q0[v], e), acc, true);                                   // beta's q.r (:1056-1059)
-            S.term(1, v, dm(e, e), acc, false);                                       // r.r (:1127)
+            S.template term<0, true>(v, dm(q0[v], e), acc0);                         // beta's q.r (:1056-1059)
+            S.template term<1, false>(v, dm(e, e), acc1);                             // r.r (:1127)
         }
-        if (!S.dots(2, acc, negq, out)) return;
-        const double nq = out[0], norm = out[1];
+        if (!S.template dots<2, true>(acc0, acc1, o0, o1)) return;
+        const double nq = o0, norm = o1;
         double beta = __ddiv_rn(nq, c1);                                               // :1060-1065
         if (c1 == 0.0) beta = 0.0;
         const double bro = __ddiv_rn(beta, ro1);
@@ -366,13 +458,13 @@ restart:
         }
         if (!S.sync()) return;
         if (!S.apply(g0, w0)) return;                                                 // :1094
-        acc[0] = 0.0;
-        for (int64_t v = gt; v < V; v += GT) S.term(0, v, dm(q0[v], w0[v]), acc, false);   // c[0] (:1096-1099)
+        acc0 = 0.0;
+        for (int64_t v = gt; v < V; v += GT) S.template term<0, false>(v, dm(q0[v], w0[v]), acc0);   // c[0]
         if (blockIdx.x == 0 && threadIdx.x == 0 && gtimer_ns() - t0 > SF3_TIME_LIMIT_NS) atomicExch(a.gstop, 1u);
-        if (!S.dots(1, acc, pos, out)) return;
+        if (!S.template dots<1, false>(acc0, 0.0, o0, o1)) return;
         if (threadIdx.x == 0) stop_s = __ldcg(a.gstop);
         __syncthreads();
-        c1 = out[0];                                                                   // the shift :1104-1121
+        c1 = o0;                                                                       // the shift :1104-1121
         if (nq != 0.0) al = __ddiv_rn(-nq, c1);                                        // next iteration's al
         have_qr = nq != 0.0;
         {
@@ -395,7 +487,13 @@ out:
     }
 }
 
-size_t rows_smem(const Sf3dSystem &s) { return (size_t)(s.sN + s.M + s.K + 3) * sizeof(double); }
+size_t rows_smem(const Sf3dSystem &s)
+{
+    const int nmax = std::max(s.sN, std::max(s.M, s.K));
+    return (size_t)(2 * (s.sN + s.M + s.K + 3) + SF3_WARPS * (nmax + 1)) * sizeof(double);
+}
+// The opt-in is made once per kernel and device, so for the largest axes allowed (157 KB).
+constexpr int SF3_SMEM_MAX = (6 * (FPDE_SF_MAX_N + 1) + SF3_WARPS * (FPDE_SF_MAX_N + 1)) * (int)sizeof(double);
 
 }  // namespace
 
@@ -405,7 +503,7 @@ struct Sf3dWork {
     int64_t V = 0;
     int blocks = 0;                      // the larger of the two
     int blocks_fast = 0, blocks_exact = 0;   // CTAs of each solve form (all co-resident)
-    double *vec = nullptr;               // r q0 g0 g1 w0 w1 u Au, bt (3V), prod (2V)
+    double *vec = nullptr;               // r q0 g0 g1 w0 w1 u Au, tc (3V), prod (2V)
     double *part = nullptr, *gscal = nullptr;
     unsigned *ctl = nullptr;             // barrier (2), stop (1)
     int exact_ok = 0;
@@ -417,10 +515,14 @@ static int solve_blocks(const Sf3dSystem &s, bool exact, int64_t V, int *blocks)
     FPDE_CUDA(cudaGetDevice(&dev));
     FPDE_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     const size_t smem = rows_smem(s);
+    FPDE_CUDA(exact ? smem_opt_in((const void *)k_sf3d_solve<true>, SF3_SMEM_MAX)
+                    : smem_opt_in((const void *)k_sf3d_solve<false>, SF3_SMEM_MAX));
     if (exact) FPDE_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_sf3d_solve<true>, SF3_THREADS, smem));
     else FPDE_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_sf3d_solve<false>, SF3_THREADS, smem));
     if (per < 1) return set_error(FPDE_ERR_CUDA, "space-fractional 3D solve: no co-resident CTA fits");
-    const int64_t need = (V + SF3_THREADS - 1) / SF3_THREADS;
+    // one thread per value or one warp per line, whichever asks more CTAs, at most all co-resident
+    const int64_t lines = (int64_t)(s.sN + 1) * (s.M + 1) + (int64_t)(s.sN + 1) * (s.K + 1) + (int64_t)(s.M + 1) * (s.K + 1);
+    const int64_t need = std::max((V + SF3_THREADS - 1) / SF3_THREADS, (lines + SF3_WARPS - 1) / SF3_WARPS);
     *blocks = (int)std::min<int64_t>((int64_t)per * sms, need);
     return FPDE_OK;
 }
@@ -453,13 +555,16 @@ void sf3d_work_destroy(Sf3dWork *w)
     delete w;
 }
 
-int sf3d_enqueue_matvec(cudaStream_t st, const Sf3dSystem &s, double *bt, const double *x, double *r)
+int sf3d_enqueue_matvec(cudaStream_t st, const Sf3dSystem &s, double *tc, const double *x, double *r)
 {
     const int64_t V = (int64_t)(s.sN + 2) * (s.M + 2) * (s.K + 2) + 1;
     const unsigned blocks = (unsigned)((V + SF3_THREADS - 1) / SF3_THREADS);
-    k_sf3d_bt<<<blocks, SF3_THREADS, 0, st>>>(s, x, bt);
+    const int64_t lines = (int64_t)(s.sN + 1) * (s.M + 1) + (int64_t)(s.sN + 1) * (s.K + 1) + (int64_t)(s.M + 1) * (s.K + 1);
+    const unsigned tblocks = (unsigned)std::max<int64_t>(1, (lines + SF3_WARPS - 1) / SF3_WARPS);
+    FPDE_CUDA(smem_opt_in((const void *)k_sf3d_terms, SF3_SMEM_MAX));
+    k_sf3d_terms<<<tblocks, SF3_THREADS, rows_smem(s), st>>>(s, x, tc);
     FPDE_LAUNCHED(1);
-    k_sf3d_rows<<<blocks, SF3_THREADS, rows_smem(s), st>>>(s, x, bt, r);
+    k_sf3d_rows<<<blocks, SF3_THREADS, 0, st>>>(s, x, tc, r);
     FPDE_LAUNCHED(1);
     return FPDE_OK;
 }
@@ -472,7 +577,7 @@ int sf3d_enqueue_solve(cudaStream_t st, const Sf3dSystem &s, Sf3dWork *w, const 
     a.s = s; a.x = x; a.B = B;
     double *p = w->vec;
     a.r = p; a.q0 = p + V; a.g0 = p + 2 * V; a.g1 = p + 3 * V; a.w0 = p + 4 * V; a.w1 = p + 5 * V;
-    a.u = p + 6 * V; a.Au = p + 7 * V; a.bt = p + 8 * V; a.prod = p + 11 * V;
+    a.u = p + 6 * V; a.Au = p + 7 * V; a.tc = p + 8 * V; a.prod = p + 11 * V;
     a.part = w->part; a.gscal = w->gscal;
     a.bar = w->ctl; a.gstop = w->ctl + 2;
     a.flags = flags; a.iters_total = iters_total; a.iters_out = iters_out;
@@ -627,6 +732,7 @@ static int sf3d_call(fpde_ctx *ctx, const fpde_sf3d_system *sys, const double *B
                    "1 <= sN, M, K <= FPDE_SF_MAX_N");
     FPDE_CHECK_ARG(sys->space_der == 0 || sys->space_der == 1, "space_der must be 0 or 1");
     const int64_t V = (int64_t)(sys->sN + 2) * (sys->M + 2) * (sys->K + 2) + 1;
+    FPDE_CHECK_ARG(V < ((int64_t)1 << 31), "(sN+2)(M+2)(K+2) + 1 must be below 2^31");
     FPDE_CHECK_ARG(!solve || (maxiter >= 1 && maxiter <= FPDE_SF_MAX_ITER), "maxiter must be 1 .. FPDE_SF_MAX_ITER");
     FPDE_CHECK_ARG(!solve || !exact || V <= FPDE_SF3D_MAX_EXACT, "exact dot products: at most FPDE_SF3D_MAX_EXACT values");
     int rc = ctx_enter(ctx);
@@ -657,7 +763,7 @@ static int sf3d_call(fpde_ctx *ctx, const fpde_sf3d_system *sys, const double *B
                 (solve && !dB) || !dx || !dout;
     int *d_it = nullptr;
     Sf3dWork *w = nullptr;
-    double *bt = nullptr;
+    double *tc = nullptr;
     if (!fail && solve) {
         fail = dev_alloc((void **)&d_it, sizeof(int)) != 0;
         if (!fail) {
@@ -665,12 +771,12 @@ static int sf3d_call(fpde_ctx *ctx, const fpde_sf3d_system *sys, const double *B
             if ((rc = sf3d_work_create(s, &w))) fail = true;
         }
     } else if (!fail) {
-        fail = dev_alloc((void **)&bt, 3 * vec) != 0;
-        if (!fail) own.push_back(bt);
+        fail = dev_alloc((void **)&tc, 3 * vec) != 0;
+        if (!fail) own.push_back(tc);
     }
     if (!fail) {
         if (solve) rc = sf3d_enqueue_solve(st, s, w, dB, dx, thr, maxiter, exact != 0, nullptr, d_it, ctx->d_flags);
-        else rc = sf3d_enqueue_matvec(st, s, bt, dx, dout);
+        else rc = sf3d_enqueue_matvec(st, s, tc, dx, dout);
         if (!rc && !on_device) cudaMemcpyAsync(out, dout, vec, cudaMemcpyDeviceToHost, st);
         if (!rc && iters) cudaMemcpyAsync(iters, d_it, sizeof(int), cudaMemcpyDeviceToHost, st);
         if (!rc) rc = ctx_check_flags(ctx, solve ? "fpde_sf3d_solve" : "fpde_sf3d_matvec");

@@ -466,7 +466,7 @@ int fpde_sf_toeplitz_row(double gamma, const double *Z, int n, double *Tm);
  * 1..len-1 on every axis, iw_c * T_c * tridiag(Mcoefs_3d[c]) along the node's axis-c line. Products
  * equal the reference's bit for bit. */
 typedef struct fpde_sf3d_system {
-    int sN, M, K;               /* intervals along i, j, k (each 1 .. FPDE_SF_MAX_N) */
+    int sN, M, K;               /* intervals along i, j, k (each 1 .. FPDE_SF_MAX_N; V below 2^31) */
     int space_der;              /* 0 one-sided, 1 two-sided */
     const double *mat;          /* 7 x V: Mat_3d[0..6] */
     const double *mc;           /* 9 x V: Mcoefs_3d[c][d] at plane 3c+d (c = 0 sN, 1 _M, 2 K; d = 0
@@ -484,7 +484,8 @@ int fpde_sf3d_matvec(fpde_ctx *ctx, const fpde_sf3d_system *sys, const double *x
  * NULL) receives the count. exact != 0: every dot product is the reference's sequential sum, so the
  * iterates, the count and the solution equal the reference's bit for bit (one GPU thread adds each
  * dot product: V <= FPDE_SF3D_MAX_EXACT); exact = 0: dot products are deterministic tree sums (the
- * same on every run on a device; they differ from the reference's only in the order of the adds). A
+ * same on every run on a device; they differ from the reference's only in the order of the adds) and
+ * the products' Toeplitz terms are fused multiply-adds (one rounding per term). A
  * solve that breaks down maxiter times in a row or runs longer than 30 s stops: FPDE_ERR_NUMERIC. */
 int fpde_sf3d_solve(fpde_ctx *ctx, const fpde_sf3d_system *sys, const double *B, double *x, double thr, int maxiter,
                     int exact, int *iters, int on_device);

@@ -965,6 +965,9 @@ void fo_sf3d_matvec(int sN, int M, int K, const double *mat, const double *mc, c
     const int64_t sy = sN + 2, sz = (int64_t)(sN + 2) * (M + 2), V = sz * (K + 2) + 1;
     const double *M0 = mat, *M1 = mat + V, *M2 = mat + 2 * V, *M3 = mat + 3 * V, *M4 = mat + 4 * V;
     const double *M5 = mat + 5 * V, *M6 = mat + 6 * V;
+    /* every output and every Bt value is one independent sequence of operations: the loops run
+     * on all threads without changing a bit */
+#pragma omp parallel for schedule(static)
     for (int64_t i = 0; i < V; i++) {                                              /* :6857-6877 */
         r[i] = M1[i] * x[i];
         if (sN > 2) {
@@ -988,6 +991,7 @@ void fo_sf3d_matvec(int sN, int M, int K, const double *mat, const double *mc, c
         if (n <= 2) continue;
         const double *c0 = mc + (3 * c) * V, *c1 = mc + (3 * c + 1) * V, *c2 = mc + (3 * c + 2) * V;
         const double *T = Tm[c];
+#pragma omp parallel for schedule(static)
         for (int64_t i = 0; i < V; i++) {
             bt[i] = c1[i] * x[i];
             if (i - st >= 0) bt[i] += c0[i] * x[i - st];
@@ -996,6 +1000,7 @@ void fo_sf3d_matvec(int sN, int M, int K, const double *mat, const double *mc, c
         /* lines: the other two coordinates over 1..len-1 */
         const int na = c == 0 ? M : sN, nb = c == 2 ? M : K;
         const int64_t sa = c == 0 ? sy : 1, sb = c == 2 ? sy : sz;
+#pragma omp parallel for schedule(static) collapse(2)
         for (int la = 1; la < na; la++)
             for (int lb = 1; lb < nb; lb++) {
                 const int64_t base = la * sa + lb * sb;

@@ -18,10 +18,11 @@ CASES = [
     ["--workload", "sum2", "--nodes", "24"],
     ["--workload", "weights", "--time-steps", "256"],
     ["--workload", "sf3d", "--nodes", "12", "--time-steps", "8"],
+    ["--workload", "sf3d", "--nodes", "12", "--time-steps", "8", "--implicit3d", "1"],
 ]
 
 
-@pytest.mark.parametrize("args", CASES, ids=[c[1] for c in CASES])
+@pytest.mark.parametrize("args", CASES, ids=[" ".join(c[1::2]) for c in CASES])
 def test_reference_arm_json(args):
     env = dict(os.environ, OMP_NUM_THREADS="2")
     out = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--steps", "1",

@@ -5,8 +5,9 @@ The product forms every output with the reference's operations in its order (vmu
 fpde_hpc_1d.cpp:6801-8722), so it equals the reference's bit for bit. The solve with exact dot
 products adds every dot product in index order on one thread, as solve_mln<1> does, so its iterates,
 iteration count and solution are the reference's bit for bit; the fast form sums its dot products in
-a fixed tree and is compared within the reference's own sensitivity: ten times how far the oracle
-(bitwise the reference) moves when the right-hand side changes by 1e-15."""
+a fixed tree and its Toeplitz terms as fused multiply-adds, and is compared within the reference's own
+sensitivity: ten times how far the oracle (bitwise the reference) moves when the right-hand side
+changes by 1e-15."""
 import numpy as np
 import pytest
 
