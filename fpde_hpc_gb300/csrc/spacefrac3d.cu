@@ -21,8 +21,9 @@
 //   fast:  each thread adds its nodes, each CTA folds its threads in a fixed tree and every CTA
 //          folds the CTA partials in the same fixed order, so the result is deterministic and
 //          identical in every CTA, and differs from the reference's only by the order of the adds;
-//          the products' Toeplitz terms are fused multiply-adds (one FP64 instruction per term
-//          instead of two, the pipe the sums are bound by; each term rounds once instead of twice).
+//          every product that feeds a sum (the Toeplitz terms, the diagonals, Bt, the updates, the dot
+//          partials) is a fused multiply-add (one FP64 instruction instead of two, on the pipe the
+//          solve is bound by; one rounding instead of two).
 #include <algorithm>
 #include <cmath>
 #include <vector>
@@ -38,6 +39,15 @@ namespace {
 __device__ __forceinline__ double dm(double a, double b) { return __dmul_rn(a, b); }
 __device__ __forceinline__ double da(double a, double b) { return __dadd_rn(a, b); }
 __device__ __forceinline__ double ds(double a, double b) { return __dsub_rn(a, b); }
+// c + a*b and c - a*b: fused (one rounding, the fast solve) or the reference's rounded product and sum
+template <bool F> __device__ __forceinline__ double madd(double a, double b, double c)
+{
+    return F ? fma(a, b, c) : da(c, dm(a, b));
+}
+template <bool F> __device__ __forceinline__ double msub(double c, double a, double b)
+{
+    return F ? fma(-a, b, c) : ds(c, dm(a, b));
+}
 
 #ifndef SF3_MIN_CTAS
 #define SF3_MIN_CTAS 2        // co-resident CTAs per SM the solve's register budget is cut for
@@ -123,8 +133,8 @@ __device__ __forceinline__ void line_terms(const Sf3dSystem &s, const Geo &g, co
     for (int q = 1 + lane; q < n; q += 32) {
         const int64_t v = base + (int64_t)q * st;
         double b = dm(__ldg(mc + V + v), __ldcg(x + v));
-        b = da(b, dm(__ldg(mc + v), __ldcg(x + v - st)));
-        b = da(b, dm(__ldg(mc + 2 * V + v), __ldcg(x + v + st)));
+        b = madd<FUSED>(__ldg(mc + v), __ldcg(x + v - st), b);
+        b = madd<FUSED>(__ldg(mc + 2 * V + v), __ldcg(x + v + st), b);
         sl[q] = b;
     }
     __syncwarp();
@@ -171,7 +181,8 @@ __device__ __forceinline__ void line_terms(const Sf3dSystem &s, const Geo &g, co
 }
 
 // Output v of the product (:6857-6877), then the K, _M and sN terms in that order at the nodes
-// inside 1..len-1 on every axis.
+// inside 1..len-1 on every axis (FUSED: the diagonals' products fused into their sums).
+template <bool FUSED>
 __device__ __forceinline__ double row_node(const Sf3dSystem &s, const Geo &g, const double *x, const double *tc,
                                            int64_t v)
 {
@@ -179,16 +190,16 @@ __device__ __forceinline__ double row_node(const Sf3dSystem &s, const Geo &g, co
     const double *M = s.mat;
     double r = dm(__ldg(M + V + v), __ldcg(x + v));
     if (g.sN > 2) {
-        if (v - 1 >= 0) r = da(r, dm(__ldg(M + 5 * V + v), __ldcg(x + v - 1)));
-        if (v + 1 < V) r = da(r, dm(__ldg(M + 6 * V + v), __ldcg(x + v + 1)));
+        if (v - 1 >= 0) r = madd<FUSED>(__ldg(M + 5 * V + v), __ldcg(x + v - 1), r);
+        if (v + 1 < V) r = madd<FUSED>(__ldg(M + 6 * V + v), __ldcg(x + v + 1), r);
     }
     if (g.M > 2) {
-        if (v - g.sy >= 0) r = da(r, dm(__ldg(M + 3 * V + v), __ldcg(x + v - g.sy)));
-        if (v + g.sy < V) r = da(r, dm(__ldg(M + 4 * V + v), __ldcg(x + v + g.sy)));
+        if (v - g.sy >= 0) r = madd<FUSED>(__ldg(M + 3 * V + v), __ldcg(x + v - g.sy), r);
+        if (v + g.sy < V) r = madd<FUSED>(__ldg(M + 4 * V + v), __ldcg(x + v + g.sy), r);
     }
     if (g.K > 2) {
-        if (v - g.sz >= 0) r = da(r, dm(__ldg(M + v), __ldcg(x + v - g.sz)));
-        if (v + g.sz < V) r = da(r, dm(__ldg(M + 2 * V + v), __ldcg(x + v + g.sz)));
+        if (v - g.sz >= 0) r = madd<FUSED>(__ldg(M + v), __ldcg(x + v - g.sz), r);
+        if (v + g.sz < V) r = madd<FUSED>(__ldg(M + 2 * V + v), __ldcg(x + v + g.sz), r);
     }
     int i, j, k;
     if (!interior(g, v, &i, &j, &k)) return r;
@@ -238,7 +249,7 @@ __global__ void __launch_bounds__(SF3_THREADS) k_sf3d_rows(Sf3dSystem s, const d
 {
     const Geo g = geo_of(s);
     for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < g.V; v += (int64_t)gridDim.x * blockDim.x)
-        r[v] = row_node(s, g, x, tc, v);
+        r[v] = row_node<false>(s, g, x, tc, v);
 }
 
 // -------------------------------------------------------------------------- the solve
@@ -285,17 +296,17 @@ struct Solver {
             line_terms<!EXACT>(a.s, g, rows, sl, x, a.tc, c, base, st, n);
         }
         if (!sync()) return false;
-        for (int64_t v = gt; v < g.V; v += GT) y[v] = row_node(a.s, g, x, a.tc, v);
+        for (int64_t v = gt; v < g.V; v += GT) y[v] = row_node<!EXACT>(a.s, g, x, a.tc, v);
         return true;
     }
 
-    // A term of dot product Q: exact stores it, fast adds it to (NEG: subtracts it from) the
-    // thread's partial.
+    // The term x*y of dot product Q: exact stores the rounded product, fast fuses it into (NEG: out
+    // of) the thread's partial.
     template <int Q, bool NEG>
-    __device__ __forceinline__ void term(int64_t v, double p, double &acc)
+    __device__ __forceinline__ void term(int64_t v, double x, double y, double &acc)
     {
-        if (EXACT) a.prod[(int64_t)Q * g.V + v] = p;
-        else acc = NEG ? ds(acc, p) : da(acc, p);
+        if (EXACT) a.prod[(int64_t)Q * g.V + v] = dm(x, y);
+        else acc = NEG ? fma(-x, y, acc) : fma(x, y, acc);
     }
 
     // Dot product slot q of a CTA (fast form): fold the threads' partials in a fixed tree.
@@ -394,7 +405,7 @@ restart:
     for (int64_t v = gt; v < V; v += GT) {
         const double e = ds(B[v], r[v]);
         r[v] = e; g1[v] = e; q0[v] = e;
-        S.template term<0, false>(v, dm(e, e), acc0);                                 // norm (:864)
+        S.template term<0, false>(v, e, e, acc0);                                 // norm (:864)
     }
     if (blockIdx.x == 0 && threadIdx.x == 0 && gtimer_ns() - t0 > SF3_TIME_LIMIT_NS) atomicExch(a.gstop, 1u);
     if (!S.template dots<1, false>(acc0, 0.0, o0, o1)) return;
@@ -408,7 +419,7 @@ restart:
         const double norm = o0;
         if (!S.apply(g1, w1)) return;                                                 // :851
         acc0 = 0.0;
-        for (int64_t v = gt; v < V; v += GT) S.template term<0, false>(v, dm(q0[v], w1[v]), acc0);   // c[1]
+        for (int64_t v = gt; v < V; v += GT) S.template term<0, false>(v, q0[v], w1[v], acc0);   // c[1]
         if (!S.template dots<1, false>(acc0, 0.0, o0, o1)) return;
         c1 = o0;
         if (fabs(__ddiv_rn(norm, md)) < a.thr) goto out;                               // :866
@@ -416,36 +427,36 @@ restart:
     for (;;) {
         if (!have_qr) {                                                                // :871-877
             acc0 = 0.0;
-            for (int64_t v = gt; v < V; v += GT) S.template term<0, false>(v, dm(q0[v], r[v]), acc0);
+            for (int64_t v = gt; v < V; v += GT) S.template term<0, false>(v, q0[v], r[v], acc0);
             if (!S.template dots<1, false>(acc0, 0.0, o0, o1)) return;
             al = __ddiv_rn(o0, c1);
         }
         if (!(c1 != 0.0)) goto restart;                                                // :878, :913
         for (int64_t v = gt; v < V; v += GT) {
-            u[v] = ds(r[v], dm(al, w1[v]));
-            x[v] = da(x[v], dm(al, g1[v]));
+            u[v] = msub<!EXACT>(r[v], al, w1[v]);
+            x[v] = madd<!EXACT>(al, g1[v], x[v]);
         }
         if (!S.sync()) return;
         if (!S.apply(u, Au)) return;                                                  // :890
         acc0 = acc1 = 0.0;
         for (int64_t v = gt; v < V; v += GT) {
             const double av = Au[v];
-            S.template term<0, false>(v, dm(av, av), acc0);
-            S.template term<1, false>(v, dm(av, u[v]), acc1);
+            S.template term<0, false>(v, av, av, acc0);
+            S.template term<1, false>(v, av, u[v], acc1);
         }
         if (!S.template dots<2, false>(acc0, acc1, o0, o1)) return;
         const double nrm = o0;
         const double ro1 = __ddiv_rn(-o1, nrm);                                       // :903
         if (nrm == 0.0) goto restart;                                                  // :904-905
-        for (int64_t v = gt; v < V; v += GT) x[v] = ds(x[v], dm(ro1, u[v]));
+        for (int64_t v = gt; v < V; v += GT) x[v] = msub<!EXACT>(x[v], ro1, u[v]);
         if (!S.sync()) return;
         if (!S.apply(x, r)) return;                                                   // :943-947
         acc0 = acc1 = 0.0;
         for (int64_t v = gt; v < V; v += GT) {
             const double e = ds(B[v], r[v]);
             r[v] = e;
-            S.template term<0, true>(v, dm(q0[v], e), acc0);                         // beta's q.r (:1056-1059)
-            S.template term<1, false>(v, dm(e, e), acc1);                             // r.r (:1127)
+            S.template term<0, true>(v, q0[v], e, acc0);                         // beta's q.r (:1056-1059)
+            S.template term<1, false>(v, e, e, acc1);                             // r.r (:1127)
         }
         if (!S.template dots<2, true>(acc0, acc1, o0, o1)) return;
         const double nq = o0, norm = o1;
@@ -453,13 +464,13 @@ restart:
         if (c1 == 0.0) beta = 0.0;
         const double bro = __ddiv_rn(beta, ro1);
         for (int64_t v = gt; v < V; v += GT) {
-            const double zw = da(r[v], dm(beta, w1[v]));
-            g0[v] = da(zw, dm(bro, g1[v]));
+            const double zw = madd<!EXACT>(beta, w1[v], r[v]);
+            g0[v] = madd<!EXACT>(bro, g1[v], zw);
         }
         if (!S.sync()) return;
         if (!S.apply(g0, w0)) return;                                                 // :1094
         acc0 = 0.0;
-        for (int64_t v = gt; v < V; v += GT) S.template term<0, false>(v, dm(q0[v], w0[v]), acc0);   // c[0]
+        for (int64_t v = gt; v < V; v += GT) S.template term<0, false>(v, q0[v], w0[v], acc0);   // c[0]
         if (blockIdx.x == 0 && threadIdx.x == 0 && gtimer_ns() - t0 > SF3_TIME_LIMIT_NS) atomicExch(a.gstop, 1u);
         if (!S.template dots<1, false>(acc0, 0.0, o0, o1)) return;
         if (threadIdx.x == 0) stop_s = __ldcg(a.gstop);
