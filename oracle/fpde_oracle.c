@@ -874,7 +874,8 @@ int fo_sf_solve(int n, const double *mat, const double *mc, const double *Tm, co
 int fo_lod_step_sf(int sN, int M, int K, double *U, double *hist, int n, const double *kb, const double *tau,
                    double Da, double kkk0, const double *coefA, const double *coefB, const double *coefRlap,
                    const double *mc, const double *iw, const double *Tm, int ldt, int space_der, double thr,
-                   int maxiter, const double *rp, const double *bc, double *S_out, int64_t *iters)
+                   int maxiter, const double *rp, const double *bc, double *S_out, int64_t *iters,
+                   const int *rkind, const double *dLN)
 {
     const double lam = Da * (kkk0 / tau[n]);      /* Om1_impl :4441 */
     const double lamR = Da * kkk0 / tau[n];       /* R :3120 */
@@ -935,6 +936,10 @@ int fo_lod_step_sf(int sN, int M, int K, double *U, double *hist, int n, const d
                 m0[0] = 0.0; m1[0] = 1.0; m2[0] = 0.0;                             /* :4643-4648 */
                 m0[Nl] = 0.0; m1[Nl] = 1.0; m2[Nl] = 0.0;
                 om[0] = bc[base]; om[Nl] = bc[base + Nl * st];                     /* :4650-4651 */
+                if (rkind && rkind[pass] == 1) {                                   /* bottom_cond 0 :4652-4655 */
+                    om[Nl] *= dLN[pass];
+                    m0[Nl] = -1.0;
+                }
                 it_total += fo_sf_solve(Nl, mat, lmc, pT, liw, NULL, space_der, om, lu, thr, maxiter);
                 lu[Nl + 1] = lu[Nl];                                               /* U1 :4792 */
                 for (int p = 0; p <= Nl + 1; p++) U[base + p * st] = lu[p];
@@ -1052,7 +1057,7 @@ int fo_lod_step_sf3d(int sN, int M, int K, double *U, double *u_end, double *his
                      const double *tau, double Da, double kkk0, const double *coefA, const double *coefB,
                      const double *coefRlap, const double *mc, const double *iw, const double *Tm, int ldt,
                      int space_der, double thr, int maxiter, const double *rp, const double *bc, double *mat_out,
-                     double *om_out, double *S_out, int64_t *iters)
+                     double *om_out, double *S_out, int64_t *iters, const int *rkind, const double *dLN)
 {
     const double lam = Da * (kkk0 / tau[n]);
     const double lamR = Da * kkk0 / tau[n];
@@ -1100,6 +1105,10 @@ int fo_lod_step_sf3d(int sN, int M, int K, double *U, double *u_end, double *his
                     if (p == 0 || p == Nl) {
                         ml = 0.0; md = 1.0; mh = 0.0;
                         om = bc[id];
+                        if (p == Nl && rkind && rkind[pass] == 1) {                 /* bottom_cond 0 :4652-4655 */
+                            om *= dLN[pass];
+                            ml = -1.0;
+                        }
                     } else {
                         ml = cA[id]; md = -(cR[id] + tR); mh = cB[id];
                         if (pass == 2) {

@@ -192,11 +192,14 @@ int fo_sf_solve(int n, const double *mat, const double *mc, const double *Tm, co
  * every line is solved with fo_sf_solve on the system implicit2_gen forms (:4630-4663): interior
  * rows (A_, -(Rlap + Da kkk0/tau), B), identity rows at both ends with the right-hand side
  * bc0 / bcN, the operand grids mc (3 passes x 3 x G), iw (3 x G) and the Toeplitz rows Tm
- * (3 x ldt, pass p's row at p*ldt). *iters (may be NULL) receives the total iteration count. */
+ * (3 x ldt, pass p's row at p*ldt). *iters (may be NULL) receives the total iteration count.
+ * rkind (3, may be NULL: Dirichlet) with 1 at a pass makes its lines' far ends the flux rows of
+ * bottom_cond 0, U[N] - U[N-1] = bcN dLN[pass] (:4652-4655). */
 int fo_lod_step_sf(int sN, int M, int K, double *U, double *hist, int n, const double *kb, const double *tau,
                    double Da, double kkk0, const double *coefA, const double *coefB, const double *coefRlap,
                    const double *mc, const double *iw, const double *Tm, int ldt, int space_der, double thr,
-                   int maxiter, const double *rp, const double *bc, double *S_out, int64_t *iters);
+                   int maxiter, const double *rp, const double *bc, double *S_out, int64_t *iters,
+                   const int *rkind, const double *dLN);
 
 /* ---- fully implicit 3D space-fractional operator (implicit3d 1) ---- */
 
@@ -214,12 +217,12 @@ int fo_sf3d_solve(int sN, int M, int K, const double *mat, const double *mc, con
 /* One step of the fully implicit scheme (calc_step :5160-5716 with implicit3d 1, impl 2): the
  * system assembled from every line's implicit2_gen system of the three passes, one solve, the
  * history row. Operands as fo_lod_step_sf; *u_end is the value past the grid (may be NULL: 0);
- * mat_out (7 x V), om_out (V), S_out (G) and iters may be NULL. */
+ * mat_out (7 x V), om_out (V), S_out (G) and iters may be NULL; rkind / dLN as fo_lod_step_sf. */
 int fo_lod_step_sf3d(int sN, int M, int K, double *U, double *u_end, double *hist, int n, const double *kb,
                      const double *tau, double Da, double kkk0, const double *coefA, const double *coefB,
                      const double *coefRlap, const double *mc, const double *iw, const double *Tm, int ldt,
                      int space_der, double thr, int maxiter, const double *rp, const double *bc, double *mat_out,
-                     double *om_out, double *S_out, int64_t *iters);
+                     double *om_out, double *S_out, int64_t *iters, const int *rkind, const double *dLN);
 
 /* ---- distributed order (fr_do.cpp) ---- */
 

@@ -68,13 +68,13 @@ def load():
     lib.fo_sf_solve.argtypes = [i32, _dp, _dp, _dp, vp, vp, i32, _dp, _dp, d, i32]
     lib.fo_sf_solve.restype = i32
     lib.fo_lod_step_sf.argtypes = [i32, i32, i32, _dp, _dp, i32, _dp, _dp, d, d, _dp, _dp, _dp, _dp, _dp, _dp, i32,
-                                   i32, d, i32, vp, _dp, vp, C.POINTER(i64)]
+                                   i32, d, i32, vp, _dp, vp, C.POINTER(i64), vp, vp]
     lib.fo_lod_step_sf.restype = i32
     lib.fo_sf3d_matvec.argtypes = [i32, i32, i32, _dp, _dp, C.POINTER(C.c_void_p), vp, vp, i32, _dp, _dp, _dp]
     lib.fo_sf3d_solve.argtypes = [i32, i32, i32, _dp, _dp, C.POINTER(C.c_void_p), vp, vp, i32, _dp, _dp, d, i32]
     lib.fo_sf3d_solve.restype = i32
     lib.fo_lod_step_sf3d.argtypes = [i32, i32, i32, _dp, C.POINTER(d), _dp, i32, _dp, _dp, d, d, _dp, _dp, _dp,
-                                     _dp, _dp, _dp, i32, i32, d, i32, vp, _dp, vp, vp, vp, C.POINTER(i64)]
+                                     _dp, _dp, _dp, i32, i32, d, i32, vp, _dp, vp, vp, vp, C.POINTER(i64), vp, vp]
     lib.fo_caputo_derivative.argtypes = [i32, d, d, d, _dp, _dp]
     lib.fo_do_derivative.argtypes = [i32, d, i32, _dp, _dp, _dp, i32, i32, i32, _dp]
     lib.fo_do_fused_weights.argtypes = [i32, _dp, _dp, _dp, d, i32, _dp]
@@ -340,20 +340,31 @@ def sf_solve(mat, mc, Tm, B, x0, thr, maxiter, iw=None, rs=None, space_der=0):
     return x, it
 
 
+def _ends(rkind, dLN):
+    """The far-end kinds (3 ints) and steps (3 doubles) of the passes as C arrays, or (None, None)."""
+    if rkind is None:
+        return None, None, None
+    rk = np.ascontiguousarray(rkind, dtype=np.int32)
+    dl = np.ascontiguousarray(dLN, dtype=np.float64)
+    return rk.ctypes.data_as(C.c_void_p), dl.ctypes.data_as(C.c_void_p), (rk, dl)
+
+
 def lod_step_sf(dims, U, hist, n, kb, tau, Da, kkk0, coefA, coefB, coefRlap, mc, iw, Tm, space_der, thr, maxiter,
-                rp, bc, want_S=False):
+                rp, bc, want_S=False, rkind=None, dLN=None):
     """fo_lod_step_sf: one LOD step with the implicit space-fractional line solves.
-    mc: (3 passes, 3, G), iw: (3, G), Tm: (3, ldt). Returns (S or None, iterations)."""
+    mc: (3 passes, 3, G), iw: (3, G), Tm: (3, ldt); rkind/dLN: far-end kinds and steps per pass
+    (1 = the flux row of bottom_cond 0). Returns (S or None, iterations)."""
     lib = load()
     sN, M, K = dims
     S = np.zeros_like(U) if want_S else None
     Tm = _f64(Tm)
     it = C.c_int64()
     rpp = None if rp is None else _f64(rp).reshape(-1)
+    ends = _ends(rkind, dLN)                   # keeps the arrays alive through the call
     lib.fo_lod_step_sf(sN, M, K, U.reshape(-1), hist.reshape(-1), n, _f64(kb), _f64(tau), Da, kkk0,
                        _f64(coefA).reshape(-1), _f64(coefB).reshape(-1), _f64(coefRlap).reshape(-1),
                        _f64(mc).reshape(-1), _f64(iw).reshape(-1), Tm.reshape(-1), Tm.shape[1], space_der, thr,
-                       maxiter, _ptr(rpp), _f64(bc).reshape(-1), _ptr(S), C.byref(it))
+                       maxiter, _ptr(rpp), _f64(bc).reshape(-1), _ptr(S), C.byref(it), *ends[:2])
     return S, it.value
 
 
@@ -392,7 +403,7 @@ def sf3d_solve(dims, mat, mc, Tm, B, x0, thr, maxiter, iw=None, rs=None, space_d
 
 
 def lod_step_sf3d(dims, U, u_end, hist, n, kb, tau, Da, kkk0, coefA, coefB, coefRlap, mc, iw, Tm, space_der, thr,
-                  maxiter, rp, bc, want_system=False):
+                  maxiter, rp, bc, want_system=False, rkind=None, dLN=None):
     """fo_lod_step_sf3d: one step of the fully implicit 3D scheme. U (G values) is advanced in place.
     Returns (u_end, iterations, mat 7 x V or None, Om or None, S or None)."""
     lib = load()
@@ -406,10 +417,12 @@ def lod_step_sf3d(dims, U, u_end, hist, n, kb, tau, Da, kkk0, coefA, coefB, coef
     om = np.zeros(V) if want_system else None
     S = np.zeros(G) if want_system else None
     rpp = None if rp is None else _f64(rp).reshape(-1)
+    ends = _ends(rkind, dLN)
     lib.fo_lod_step_sf3d(sN, M, K, U.reshape(-1), C.byref(ue), hist.reshape(-1), n, _f64(kb), _f64(tau), Da, kkk0,
                          _f64(coefA).reshape(-1), _f64(coefB).reshape(-1), _f64(coefRlap).reshape(-1),
                          _f64(mc).reshape(-1), _f64(iw).reshape(-1), Tm.reshape(-1), Tm.shape[1], space_der, thr,
-                         maxiter, _ptr(rpp), _f64(bc).reshape(-1), _ptr(mat), _ptr(om), _ptr(S), C.byref(it))
+                         maxiter, _ptr(rpp), _f64(bc).reshape(-1), _ptr(mat), _ptr(om), _ptr(S), C.byref(it),
+                         *ends[:2])
     return ue.value, it.value, mat, om, S
 
 

@@ -518,8 +518,18 @@ static void record_sf_operands(H_solver *s, FgvWriter &w)
  * the Toeplitz row Tm[pass][1..] (:3670-3694). Per step: the grid, the history sum, Rp and the line
  * ends. After the run, for the first line of each pass: one product vmul_T(x) of a fixed x and one
  * solve_mln<1> of the line's own system from its state, with their operands. */
+static void record_flux_steps(H_solver *s, FgvWriter &w)
+{
+    /* bottom_cond 0: every line's far end is the flux row U[N] - U[N-1] = bcN dL[N-1]
+     * (implicit2_gen :4652-4655); dL[N-1] of each pass's axis */
+    w.scalar("bottom_cond", 0.0);
+    w.scalar("dLN_pass0", s->sdL[sN - 1]);
+    w.scalar("dLN_pass1", s->dLx[_M - 1]);
+    w.scalar("dLN_pass2", s->dLy[K - 1]);
+}
+
 static void run_spacefrac(const char *path, int sd, double gam, double alpha, int bs, int nb, int mb, int kb,
-                          double tau, int steps, double ieps, int initer)
+                          double tau, int steps, double ieps, int initer, int bcond = 1)
 {
     set_dims(bs, nb, mb, kb);
     varT = 0; varZ = 0; varXY = 0;
@@ -528,12 +538,13 @@ static void run_spacefrac(const char *path, int sd, double gam, double alpha, in
     impl_err = ieps; impl_niter = initer;
     global_eps = 1e-15; global_eps2 = 1e-15;
     FILE *lg = fopen("/dev/null", "w");
-    H_solver *s = new H_solver(2, 1, 5, 0, 1, alpha, gam, 0, 0, 0, 3, lg, 2);
+    H_solver *s = new H_solver(2, 1, 5, 0, bcond, alpha, gam, 0, 0, 0, 3, lg, 2);
     size_t G = (size_t)(sN + 2) * (_M + 2) * (K + 2);
     FgvWriter w(path);
     w.scalar("sN", sN); w.scalar("M", _M); w.scalar("K", K);
     w.scalar("alpha", alpha); w.scalar("gamma", gam); w.scalar("Da", s->Da); w.scalar("Dg", s->Dg);
     w.scalar("space_der", sd); w.scalar("impl_err", ieps); w.scalar("impl_niter", initer);
+    if (bcond == 0) record_flux_steps(s, w);
     std::vector<uint64_t> gdims = {(uint64_t)(K + 2), (uint64_t)(_M + 2), (uint64_t)(sN + 2)};
     w.put("U0", gdims, s->b_U);
     w.put("Z_pass0", std::vector<double>(s->sZ, s->sZ + sN + 2));   /* node coordinates of each axis */
@@ -618,7 +629,7 @@ static void vmul_T_3d_counted(double **Kp, double *x, double *r, int Nv)
  * starting grid with the count of its products. The solve runs over G+1 values: the harness sets
  * the one past the grid (b_U[G], never assigned by the reference) to 0. */
 static void run_spacefrac3d(const char *path, int sd, double gam, double alpha, int bs, int nb, int mb, int kb,
-                            double tau, int steps, double ieps, int initer)
+                            double tau, int steps, double ieps, int initer, int bcond = 1)
 {
     set_dims(bs, nb, mb, kb);
     varT = 0; varZ = 0; varXY = 0;
@@ -627,13 +638,14 @@ static void run_spacefrac3d(const char *path, int sd, double gam, double alpha, 
     impl_err = ieps; impl_niter = initer;
     global_eps = 1e-15; global_eps2 = 1e-15;
     FILE *lg = fopen("/dev/null", "w");
-    H_solver *s = new H_solver(2, 1, 5, 0, 1, alpha, gam, 0, 0, 0, 3, lg, 2);
+    H_solver *s = new H_solver(2, 1, 5, 0, bcond, alpha, gam, 0, 0, 0, 3, lg, 2);
     const size_t G = (size_t)(sN + 2) * (_M + 2) * (K + 2), V = G + 1;
     s->b_U[G] = 0.0;
     FgvWriter w(path);
     w.scalar("sN", sN); w.scalar("M", _M); w.scalar("K", K);
     w.scalar("alpha", alpha); w.scalar("gamma", gam); w.scalar("Da", s->Da); w.scalar("Dg", s->Dg);
     w.scalar("space_der", sd); w.scalar("impl_err", ieps); w.scalar("impl_niter", initer);
+    if (bcond == 0) record_flux_steps(s, w);
     std::vector<uint64_t> gdims = {(uint64_t)(K + 2), (uint64_t)(_M + 2), (uint64_t)(sN + 2)};
     w.put("U0", gdims, s->b_U);
     w.put("Z_pass0", std::vector<double>(s->sZ, s->sZ + sN + 2));
@@ -764,6 +776,9 @@ int main(int argc, char **argv)
         /* a column of 40 nodes, two-sided, solved to a tight tolerance */
         snprintf(q, sizeof q, "%s/fpde_sf_col.fgv", argv[2]);
         run_spacefrac(q, 1, 0.75, 0.8, 1, 3, 3, 40, 0.002, 10, 1e-26, 400);
+        /* 6 x 4 x 8 cells, two-sided, flux rows at every line's far end (bottom_cond 0) */
+        snprintf(q, sizeof q, "%s/fpde_sf_flux.fgv", argv[2]);
+        run_spacefrac(q, 1, 0.7, 0.8, 2, 3, 2, 4, 0.0025, 12, 1e-9, 5000, 0);
         return 0;
     }
     if (argc >= 3 && strcmp(argv[1], "spacefrac3d") == 0) {
@@ -776,6 +791,9 @@ int main(int argc, char **argv)
         run_spacefrac3d(q, 1, 0.7, 0.85, 2, 3, 2, 4, 0.0025, 10, 1e-9, 5000);
         snprintf(q, sizeof q, "%s/fpde_sf3d_tight.fgv", argv[2]);
         run_spacefrac3d(q, 1, 0.75, 0.8, 2, 2, 3, 3, 0.002, 8, 1e-24, 400);
+        /* 6 x 4 x 8 cells, one-sided, flux rows at every line's far end (bottom_cond 0) */
+        snprintf(q, sizeof q, "%s/fpde_sf3d_flux.fgv", argv[2]);
+        run_spacefrac3d(q, 0, 0.8, 0.8, 2, 3, 2, 4, 0.0025, 10, 1e-9, 5000, 0);
         return 0;
     }
     if (argc >= 3 && strcmp(argv[1], "gamma") == 0) {

@@ -6,12 +6,13 @@ solve_mln<1> with vmul_T_3d over the G + 1 values (fpde_hpc_1d.cpp:5160-5716, :6
 the per-pass coefficient grids, Mcoefs, inv_dw_dh and Toeplitz rows (as in the line-solve fixtures),
 per step the grid, history sum, Rp and line ends, the assembled system of the first and last step,
 Mcoefs_3d at the nodes the product reads, one product of a fixed vector and the last step's solve
-repeated with its product count (tests/golden/make_golden.py --only spacefrac3d)."""
+repeated with its product count (tests/golden/make_golden.py --only spacefrac3d). fpde_sf3d_flux has flux
+rows at the lines' far ends (the reference's bottom_cond 0)."""
 import numpy as np
 
 import sf_cases
 
-NAMES = ["fpde_sf3d_sd0", "fpde_sf3d_sd1", "fpde_sf3d_tight"]
+NAMES = ["fpde_sf3d_sd0", "fpde_sf3d_sd1", "fpde_sf3d_tight", "fpde_sf3d_flux"]
 
 
 def load(name):

@@ -4,13 +4,13 @@ Each fixture is one run of the reference's LOD (impl 2, TMA 0, analytic problem 
 coefficient grids, the Mcoefs diagonals and inv_dw_dh of every line node, the Toeplitz rows
 Tm[pass], and per step the grid, the history sum, Rp and the line ends; plus one product vmul_T
 and one solve_mln<1> on the first line of each pass (tests/golden/make_golden.py --only
-spacefrac)."""
+spacefrac). fpde_sf_flux has flux rows at the lines' far ends (the reference's bottom_cond 0)."""
 import numpy as np
 
 import fgv
 from conftest import golden_path
 
-NAMES = ["fpde_sf_sd0", "fpde_sf_sd1", "fpde_sf_col"]
+NAMES = ["fpde_sf_sd0", "fpde_sf_sd1", "fpde_sf_col", "fpde_sf_flux"]
 
 
 def load(name):
@@ -32,6 +32,12 @@ def load(name):
     kbo = g["kb_off"].astype(np.int64)
     c["kb_rows"] = [g["kb_flat"][kbo[n]:kbo[n + 1]] for n in range(len(kbo) - 1)]
     c["steps"] = g["U"].shape[0]
+    # bottom_cond 0: every line's far end is the flux row U[N] - U[N-1] = bcN dL[N-1]
+    if "bottom_cond" in g:
+        c["rkind"] = (1, 1, 1)
+        c["dLN"] = tuple(float(g[f"dLN_pass{p}"]) for p in range(3))
+    else:
+        c["rkind"], c["dLN"] = None, None
     return c
 
 

@@ -118,9 +118,10 @@ def _lod(ctx, c, precision=0, max_steps=None):
     sf = dict(space_der=c["space_der"], tol=c["thr"], max_iter=c["maxiter"], Tm=[c["Tm"][p] for p in range(3)],
               mc=[c["mc"][p] for p in range(3)], iw=[c["iw"][p] for p in range(3)])
     steps = c["steps"]
+    ends = {} if c["rkind"] is None else dict(right_kind=c["rkind"], dLN=c["dLN"])
     return fp.Lod3D(ctx, c["dims"], float(g["alpha"]), float(g["tau"][0]), c["Da"], c["coefA"], c["coefB"],
                     c["coefRlap"], g["U0"], max_steps or steps, source=g["Rp"], bc=g["BC"], precision=precision,
-                    space_frac=sf)
+                    space_frac=sf, **ends)
 
 
 def _oracle_envelope(c, rel):
@@ -133,7 +134,7 @@ def _oracle_envelope(c, rel):
     for n in range(c["steps"]):
         oracle.lod_step_sf(c["dims"], U, hist, n, c["kb_rows"][n], g["tau"], c["Da"], float(g["kkk0"][n]),
                            c["coefA"], c["coefB"], c["coefRlap"], c["mc"], c["iw"], c["Tm"], c["space_der"], c["thr"],
-                           c["maxiter"], g["Rp"][n] * (1.0 + rel), g["BC"][n])
+                           c["maxiter"], g["Rp"][n] * (1.0 + rel), g["BC"][n], rkind=c["rkind"], dLN=c["dLN"])
         worst = max(worst, float(np.abs(U - g["U"][n]).max() / np.abs(g["U"][n]).max()))
     return worst
 

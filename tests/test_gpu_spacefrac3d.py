@@ -159,8 +159,9 @@ def _lod(ctx, c, exact):
     sf = dict(space_der=c["space_der"], tol=c["thr"], max_iter=c["maxiter"], Tm=[c["Tm"][p] for p in range(3)],
               mc=[c["mc"][p] for p in range(3)], iw=[c["iw"][p] for p in range(3)], implicit3d=1,
               exact=1 if exact else 0)
+    ends = {} if c["rkind"] is None else dict(right_kind=c["rkind"], dLN=c["dLN"])
     return fp.Lod3D(ctx, c["dims"], float(g["alpha"]), float(g["tau"][0]), c["Da"], c["coefA"], c["coefB"],
-                    c["coefRlap"], g["U0"], c["steps"], source=g["Rp"], bc=g["BC"], space_frac=sf)
+                    c["coefRlap"], g["U0"], c["steps"], source=g["Rp"], bc=g["BC"], space_frac=sf, **ends)
 
 
 def _lod_envelope(c, rel):
@@ -174,7 +175,7 @@ def _lod_envelope(c, rel):
         ue, *_ = oracle.lod_step_sf3d(c["dims"], U, ue, hist, n, c["kb_rows"][n], g["tau"], c["Da"],
                                       float(g["kkk0"][n]), c["coefA"], c["coefB"], c["coefRlap"], c["mc"], c["iw"],
                                       c["Tm"], c["space_der"], c["thr"], c["maxiter"], g["Rp"][n] * (1.0 + rel),
-                                      g["BC"][n])
+                                      g["BC"][n], rkind=c["rkind"], dLN=c["dLN"])
         worst = max(worst, relmax(U, g["U"][n].reshape(-1)))
     return worst
 

@@ -34,7 +34,8 @@ def test_lod_replay_bitwise(name):
     for n in range(c["steps"]):
         S, it = oracle.lod_step_sf(c["dims"], U, hist, n, c["kb_rows"][n], g["tau"], c["Da"], float(g["kkk0"][n]),
                                    c["coefA"], c["coefB"], c["coefRlap"], c["mc"], c["iw"], c["Tm"],
-                                   c["space_der"], c["thr"], c["maxiter"], g["Rp"][n], g["BC"][n], want_S=True)
+                                   c["space_der"], c["thr"], c["maxiter"], g["Rp"][n], g["BC"][n], want_S=True,
+                                   rkind=c["rkind"], dLN=c["dLN"])
         assert it > 0
         assert np.array_equal(U, g["U"][n]), f"step {n}"
         if n > 0:      # at step 0 there is no history and the reference leaves its buffer untouched
@@ -48,3 +49,18 @@ def test_two_sided_differs_from_one_sided():
     r1 = oracle.sf_matvec(lc["mat"], lc["mc"], lc["Tm"], lc["x"], iw=lc["iw"], space_der=1)
     r0 = oracle.sf_matvec(lc["mat"], lc["mc"], lc["Tm"], lc["x"], iw=lc["iw"], space_der=0)
     assert np.array_equal(r1, lc["r"]) and not np.array_equal(r0, lc["r"])
+
+
+def test_flux_rows_are_read():
+    """The flux fixture's first step needs the flux rows: replayed with Dirichlet far ends it moves."""
+    c = sf_cases.load("fpde_sf_flux")
+    g = c["g"]
+    out = []
+    for rk in (c["rkind"], None):
+        U = g["U0"].copy()
+        hist = np.zeros((c["steps"],) + U.shape)
+        oracle.lod_step_sf(c["dims"], U, hist, 0, c["kb_rows"][0], g["tau"], c["Da"], float(g["kkk0"][0]), c["coefA"],
+                           c["coefB"], c["coefRlap"], c["mc"], c["iw"], c["Tm"], c["space_der"], c["thr"],
+                           c["maxiter"], g["Rp"][0], g["BC"][0], rkind=rk, dLN=c["dLN"])
+        out.append(U)
+    assert np.array_equal(out[0], g["U"][0]) and not np.array_equal(out[1], out[0])

@@ -44,7 +44,7 @@ def test_lod_replay_bitwise(name):
         ue, it, mat, om, S = oracle.lod_step_sf3d(c["dims"], U, ue, hist, n, c["kb_rows"][n], g["tau"], c["Da"],
                                                   float(g["kkk0"][n]), c["coefA"], c["coefB"], c["coefRlap"], c["mc"],
                                                   c["iw"], c["Tm"], c["space_der"], c["thr"], c["maxiter"], g["Rp"][n],
-                                                  g["BC"][n], want_system=True)
+                                                  g["BC"][n], want_system=True, rkind=c["rkind"], dLN=c["dLN"])
         assert it >= 1
         if n == 0:
             assert np.array_equal(mat, g["sys_first_mat"]) and np.array_equal(om, g["sys_first_om"])
@@ -79,3 +79,18 @@ def test_axis_terms_are_read():
         assert not np.array_equal(r2, g["mv_r"]), f"axis {ax}"
     r0 = oracle.sf3d_matvec(c["dims"], g["sys_last_mat"], c["mc3d"], c["Tm3"], g["mv_x"], iw=c["iw3"], space_der=0)
     assert not np.array_equal(r0, g["mv_r"])
+
+
+def test_flux_rows_are_read():
+    """The flux fixture's first step needs the flux rows: replayed with Dirichlet far ends it moves."""
+    c = sf3d_cases.load("fpde_sf3d_flux")
+    g = c["g"]
+    out = []
+    for rk in (c["rkind"], None):
+        U = g["U0"].reshape(-1).copy()
+        hist = np.zeros((c["steps"], c["G"]))
+        oracle.lod_step_sf3d(c["dims"], U, 0.0, hist, 0, c["kb_rows"][0], g["tau"], c["Da"], float(g["kkk0"][0]),
+                             c["coefA"], c["coefB"], c["coefRlap"], c["mc"], c["iw"], c["Tm"], c["space_der"], c["thr"],
+                             c["maxiter"], g["Rp"][0], g["BC"][0], rkind=rk, dLN=c["dLN"])
+        out.append(U)
+    assert np.array_equal(out[0], g["U"][0].reshape(-1)) and not np.array_equal(out[1], out[0])
