@@ -234,3 +234,25 @@ def test_lod_implicit3d_larger_grid_vs_oracle(ctx, sd):
         worst = max(worst, relmax(lod.state().reshape(-1), ref[n]))
     lod.close()
     assert worst <= max(10.0 * env, 1e-12), (worst, env)
+
+
+@pytest.mark.parametrize("exact", [False, True])
+def test_lod_implicit3d_graph_replay(ctx, exact):
+    """A run of 130 steps is captured as a CUDA graph (the cooperative solve inside it); it must equal
+    130 single-step runs (enqueued directly) bit for bit: the dot products are deterministic."""
+    import fpde_hpc_gb300 as fp
+    from test_gpu_spacefrac import _synthetic
+    dims, alpha, tau, steps = (8, 6, 10), 0.75, 1e-3, 130
+    coefA, coefB, coefR, mc, iw, Tm, rp, u0 = _synthetic(dims, 0.7, 5)
+    Da = 1.0 / fp.gamma(1.0 - alpha)
+    sf = dict(space_der=1, tol=1e-20, max_iter=300, Tm=list(Tm), mc=list(mc), iw=list(iw), implicit3d=1,
+              exact=1 if exact else 0)
+    out = []
+    for chunk in (steps, 1):
+        lod = fp.Lod3D(ctx, dims, alpha, tau, Da, coefA, coefB, coefR, u0, steps, source=rp, space_frac=sf)
+        for _ in range(steps // chunk):
+            lod.run(chunk)
+        out.append((lod.state(), lod.sf_iterations()))
+        lod.close()
+    assert out[0][1] == out[1][1] and out[0][1] >= steps
+    assert np.array_equal(out[0][0], out[1][0])
