@@ -54,6 +54,8 @@ def parse():
                     help="sf3d: one-sided (0) or two-sided (1) space-fractional operator")
     ap.add_argument("--implicit3d", type=int, default=0, choices=[0, 1],
                     help="sf3d: line solves per pass (0) or the fully implicit scheme, one 3D solve per step (1)")
+    ap.add_argument("--sf-exact", action="store_true",
+                    help="sf3d: the reference's operation order (sequential dot products, separate roundings)")
     ap.add_argument("--precision", default="auto", choices=["auto", "fp64", "bf16", "f16", "bf16x3"])
     ap.add_argument("--time-steps", type=int, default=None, help="override the workload's step count")
     ap.add_argument("--nodes", type=int, default=None, help="override the workload's size")
@@ -339,18 +341,21 @@ class SfWorkload(LodWorkload):
         from fpde_hpc_gb300 import problems
         n = args.nodes or 64
         self.impl3d = bool(args.implicit3d)
+        self.exact = bool(args.sf_exact)
         self.p = problems.sf3d(n=n, steps=args.time_steps or 32, space_der=args.space_der)
         self.name = "sf3d_implicit3d" if self.impl3d else "sf3d"
         self.node_steps = self.p.node_steps
         side = "two-sided" if args.space_der else "one-sided"
+        form = ("the reference's operation order" if self.exact
+                else "tree dot products, fused multiply-adds")
         if self.impl3d:
             self.metric = (f"node-steps/s (fully implicit 3D space-fractional scheme, vmul_T_3d + solve_mln<1> over "
                            f"the grid, {n}^3, {self.p.steps} steps)")
-            scheme = "fully implicit (implicit3d 1: one 3D solve per step, tree dot products)"
+            scheme = f"fully implicit (implicit3d 1: one 3D solve per step; {form})"
         else:
             self.metric = (f"node-steps/s (3D LOD with implicit space-fractional line solves, vmul_T + "
                            f"solve_mln<1>, {n}^3, {self.p.steps} steps)")
-            scheme = "LOD (line solves per pass)"
+            scheme = f"LOD (line solves per pass; {form})"
         self.desc = (f"3D {scheme} {n}^3, {self.p.steps} steps, alpha 0.8, gamma {self.p.gamma} {side}, tau 1e-3, "
                      "lognormal k (sigma 0.4, seed 11), Gaussian blob and source, Dirichlet 0 line ends, "
                      "solver threshold 1e-9 / 5000 iterations (the reference's defaults)")
@@ -369,7 +374,7 @@ class SfWorkload(LodWorkload):
         p = self.p
         cA, cB, cR, Tm, mc, iw, src = self.operands()
         sf = dict(space_der=p.space_der, tol=p.tol, max_iter=p.max_iter, Tm=list(Tm), mc=list(mc), iw=list(iw),
-                  implicit3d=1 if self.impl3d else 0)
+                  implicit3d=1 if self.impl3d else 0, exact=1 if self.exact else 0)
         return fp.Lod3D(ctx, p.dims, p.alpha, p.tau, p.Da, cA, cB, cR, p.u0, p.steps, source=src, precision=prec,
                         space_frac=sf)
 
@@ -413,7 +418,7 @@ class SfWorkload(LodWorkload):
         return 3 * mv + 10 * V + 11 * V
 
     def line_iteration_ops(self):
-        """FP64 operations (multiplies and adds, one each per lane) of one solver iteration on a line
+        """FP64 flops (multiplies and adds) of one solver iteration on a line
         of n intervals: three products vmul_T (bt 5(n-1), tridiagonal 5(n-1)+6, Toeplitz
         (n-1)(n-2) one-sided or twice that two-sided, iw 2(n-1)), five dot products (2 (n+1)
         each) and the vector updates (11 (n+1))."""
@@ -1096,34 +1101,30 @@ def run_ours(args):
                                     "FP64 pipe and its per-step chain, not by HBM or the tensor cores")
         elif "hist_gemv" in kernels:
             out["roofline"] = dict(kernels["hist_gemv"])
-    elif is_sf and wl.impl3d:
-        # one persistent cooperative kernel per step, FP64-pipe bound: the products' Toeplitz terms are
-        # fused multiply-adds (2 flops each), the rest separate multiplies and adds; the tree dot
-        # products and the updates are L2-resident traffic
-        ops = sf_iters * wl.grid_iteration_ops()
-        gops = ops / (ms / 1e3) / 1e9
-        out["roofline"] = {"kernel": "k_sf3d_solve (vmul_T_3d + solve_mln<1>, persistent cooperative)",
-                           "bound": "fp64", "achieved": gops, "peak": 1250.0, "unit": "GFLOP/s (FP64)",
-                           "frac": gops / 1250.0,
-                           "peak_source": "nominal GB300 FP64 1.25 TFLOP/s (an FMA counted as 2 flops)",
-                           "traffic": None,
-                           "note": (f"{sf_iters:.0f} solver iterations per run ({sf_iters / steps:.1f} per step) x "
-                                    f"{wl.grid_iteration_ops():.3g} FP64 flops per iteration; ncu on 64^3: FP64 "
-                                    "pipe 69% active (profiles/k_sf3d_solve_64cube.md)")}
     elif is_sf:
-        # the line solves are FP64-pipe work: every multiply and add of vmul_T, the dot products and
-        # the updates is one FP64 operation per lane (no contracted FMAs: they would change the
-        # reference's roundings); achieved = operations of the iterations run / solve time
-        ops = sf_iters * wl.line_iteration_ops()
-        gops = ops / (ms / 1e3) / 1e9
-        lines = 3 * (wl.p.dims[0] - 1) ** 2 * steps
-        out["roofline"] = {"kernel": "k_lod_pass_sf (vmul_T + solve_mln<1>, one CTA per line)", "bound": "fp64",
-                           "achieved": gops, "peak": 625.0, "unit": "G FP64 ops/s", "frac": gops / 625.0,
-                           "peak_source": "nominal GB300 FP64 1.25 TFLOP/s counting an FMA as 2 (625 G lane-ops/s)",
-                           "traffic": None,
-                           "note": (f"{sf_iters:.0f} solver iterations per solve ({sf_iters / lines:.1f} per line "
-                                    f"solve) x {wl.line_iteration_ops()} FP64 ops per line-iteration; the "
-                                    "dot products' sequential sums (the reference's order) run on one lane")}
+        # FP64-pipe work. The fast form fuses every product into its sum (an FMA counted as 2 flops)
+        # and sums dot products in trees; the exact form issues every multiply and add on its own (it
+        # can reach at most half the nominal rate) and, on lines, adds each dot product on one lane.
+        peak = 1250.0
+        form = ("exact: the reference's order, separate multiplies and adds, at most 0.5 of the peak"
+                if wl.exact else "fast: fused multiply-adds, tree dot products")
+        if wl.impl3d:
+            ops = sf_iters * wl.grid_iteration_ops()
+            kern = "k_sf3d_solve (vmul_T_3d + solve_mln<1>, persistent cooperative)"
+            note = (f"{sf_iters:.0f} solver iterations per run ({sf_iters / steps:.1f} per step) x "
+                    f"{wl.grid_iteration_ops():.3g} FP64 flops per iteration; {form}; ncu on 64^3 "
+                    "(profiles/k_sf3d_solve_64cube.md)")
+        else:
+            ops = sf_iters * wl.line_iteration_ops()
+            lines = 3 * (wl.p.dims[0] - 1) ** 2 * steps
+            kern = "k_lod_pass_sf (vmul_T + solve_mln<1>, one CTA per line)"
+            note = (f"{sf_iters:.0f} solver iterations per solve ({sf_iters / lines:.1f} per line solve) x "
+                    f"{wl.line_iteration_ops()} FP64 flops per line-iteration; {form}")
+        gf = ops / (ms / 1e3) / 1e9
+        out["roofline"] = {"kernel": kern, "bound": "fp64", "achieved": gf, "peak": peak, "unit": "GFLOP/s (FP64)",
+                           "frac": gf / peak,
+                           "peak_source": "nominal GB300 FP64 1.25 TFLOP/s (an FMA counted as 2 flops)",
+                           "traffic": None, "note": note}
     else:
         # whole-step HBM roofline from the algorithmic history bytes of the run:
         #   FP64: 8 B x nodes x lags, summed over steps;

@@ -110,6 +110,7 @@ struct LodSfArgs {
     const double *rp = nullptr, *bc = nullptr;
     double lam = 0, lamR = 0, thr = 0, dLN = 0;
     int Nl = 0, lines = 0, n1 = 0, sd = 0, maxiter = 1, rkind = 0;
+    int fast = 0;                        // tree dot products and fused multiply-adds (else bitwise)
     int64_t s1 = 0, s2 = 0, st = 0;
     unsigned long long *iters = nullptr; // total iterations (may be null)
     unsigned *flags = nullptr;

@@ -676,7 +676,7 @@ struct fpde_lod3d {
     double *C = nullptr, *lastC = nullptr, *DC = nullptr, *partC = nullptr, *C0 = nullptr;
     // implicit space-fractional line solves (desc.space_frac): per pass the line-major operands
     // (per line A, B, Rlap, mc0, mc1, mc2, iw, Nl+1 values each) and the Toeplitz row
-    bool sf = false;
+    bool sf = false, sf_fast = false;
     int sf_sd = 0, sf_maxit = 1;
     double sf_thr = 0.0;
     double *sfc[3] = {nullptr, nullptr, nullptr}, *sfT[3] = {nullptr, nullptr, nullptr};
@@ -745,6 +745,7 @@ static int lod_launch_pass(fpde_lod3d *L, cudaStream_t st, int pass, int64_t n, 
         f.sd = L->sf_sd; f.maxiter = L->sf_maxit; f.rkind = a.rkind;
         f.iters = L->sf_iters;
         f.flags = L->ctx->d_flags;
+        f.fast = L->sf_fast ? 1 : 0;
         return launch_lod_pass_sf(st, f);
     }
     if (L->rich) {
@@ -1033,10 +1034,10 @@ int fpde_lod3d_create(fpde_ctx *ctx, const fpde_lod3d_desc *desc, const double *
         for (int q = 0; q < 3; ++q)
             FPDE_CHECK_ARG(sfd->Tm[q] && sfd->mc[q] && sfd->iw[q], "space_frac: Tm, mc and iw of every pass required");
         FPDE_CHECK_ARG(sfd->implicit3d == 0 || sfd->implicit3d == 1, "space_frac: implicit3d must be 0 or 1");
-        FPDE_CHECK_ARG(!sfd->exact || sfd->implicit3d, "space_frac: exact needs implicit3d");
         FPDE_CHECK_ARG(!sfd->implicit3d || (int64_t)(d.sN + 2) * (d.M + 2) * (d.K + 2) + 1 < ((int64_t)1 << 31),
                        "space_frac: implicit3d needs (sN+2)(M+2)(K+2) + 1 below 2^31");
-        FPDE_CHECK_ARG(!sfd->exact || (int64_t)(d.sN + 2) * (d.M + 2) * (d.K + 2) + 1 <= FPDE_SF3D_MAX_EXACT,
+        FPDE_CHECK_ARG(!sfd->exact || !sfd->implicit3d ||
+                           (int64_t)(d.sN + 2) * (d.M + 2) * (d.K + 2) + 1 <= FPDE_SF3D_MAX_EXACT,
                        "space_frac: exact dot products need at most FPDE_SF3D_MAX_EXACT values");
     }
     const bool vart = d.time_steps != nullptr;
@@ -1186,6 +1187,7 @@ int fpde_lod3d_create(fpde_ctx *ctx, const fpde_lod3d_desc *desc, const double *
     }
     if (!fail && sfd) {                        // operands of the space-fractional line systems
         L->sf = true;
+        L->sf_fast = sfd->exact == 0;
         L->sf_sd = sfd->space_der;
         L->sf_thr = sfd->tol;
         L->sf_maxit = sfd->max_iter;

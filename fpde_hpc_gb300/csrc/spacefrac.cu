@@ -236,6 +236,175 @@ restart:
     return iter;
 }
 
+// ----------------------------------------------------------------- the fast form of a line solve
+
+// The same solve with deterministic tree sums and fused multiply-adds: each dot product is every
+// thread's partial over its values folded by warp shuffles and then over the warps in a fixed
+// order (a few FP64 instructions per thread instead of m sequential adds on one lane), and every
+// product that feeds a sum is one fused multiply-add. The operation order differs from the
+// reference's (the LOD's default; space_frac.exact selects sf_solve_cta).
+
+// Sum of v over the CTA, the same value in every thread (red: one double per warp).
+__device__ __forceinline__ double cta_sum(double v, double *red)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, W = blockDim.x >> 5;
+#pragma unroll
+    for (int o = 16; o >= 1; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if (lane == 0) red[warp] = v;
+    __syncthreads();
+    double t = 0.0;
+    for (int w = 0; w < W; ++w) t += red[w];
+    __syncthreads();
+    return t;
+}
+__device__ __forceinline__ void cta_sum2(double a, double b, double *red, double *oa, double *ob)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, W = blockDim.x >> 5;
+#pragma unroll
+    for (int o = 16; o >= 1; o >>= 1) {
+        a += __shfl_down_sync(0xffffffffu, a, o);
+        b += __shfl_down_sync(0xffffffffu, b, o);
+    }
+    if (lane == 0) { red[warp] = a; red[W + warp] = b; }
+    __syncthreads();
+    double ta = 0.0, tb = 0.0;
+    for (int w = 0; w < W; ++w) { ta += red[w]; tb += red[W + w]; }
+    __syncthreads();
+    *oa = ta; *ob = tb;
+}
+
+// Row i of the product with fused multiply-adds (the reference's terms in its order).
+__device__ __forceinline__ double sf_row_fast(const SfVec &s, int n, int sd, bool has_iw, bool has_rs,
+                                              const double *xv, int i)
+{
+    const double r = fma(s.m2[i], xv[i + 1], fma(s.m1[i], xv[i], s.m0[i] * xv[i - 1]));
+    double v = 0.0;
+    for (int j = 1; j < i; ++j) v = fma(s.bt[j], s.Tm[i - j + 1], v);
+    if (sd)
+        for (int j = i + 1; j < n; ++j) v = fma(-s.bt[j], s.Tm[j - i + 1], v);
+    if (has_rs) v = v / s.rs[i];
+    return has_iw ? fma(v, s.iw[i], r) : r + v;
+}
+
+__device__ void sf_apply_fast(const SfVec &s, int n, int sd, bool has_iw, bool has_rs, const double *xv, double *rv)
+{
+    const int T = blockDim.x, tid = threadIdx.x;
+    for (int j = 1 + tid; j < n; j += T) s.bt[j] = fma(s.c2[j], xv[j + 1], fma(s.c1[j], xv[j], s.c0[j] * xv[j - 1]));
+    __syncthreads();
+    if (tid == T - 1) {
+        rv[0] = fma(s.m2[0], xv[1], s.m1[0] * xv[0]);
+        rv[n] = fma(s.m1[n], xv[n], s.m0[n] * xv[n - 1]);
+    }
+    const int pairs = n / 2;
+    for (int k = tid; k < pairs; k += T) {
+        const int a = k + 1, b = n - 1 - k;
+        rv[a] = sf_row_fast(s, n, sd, has_iw, has_rs, xv, a);
+        if (b != a) rv[b] = sf_row_fast(s, n, sd, has_iw, has_rs, xv, b);
+    }
+    __syncthreads();
+}
+
+// solve_mln<1> (the sequence of sf_solve_cta) with the fast sums. scal[8] carries thread 0's
+// time-limit decision to the CTA.
+__device__ int sf_solve_cta_fast(SfVec s, int n, int sd, bool has_iw, bool has_rs, double thr, int maxiter,
+                                 double *scal, double *red, unsigned *flags)
+{
+    const int m = n + 1, T = blockDim.x, tid = threadIdx.x;
+    const double md = (double)m;
+    const unsigned long long t0 = gtimer_ns();
+    int iter = 1, restarts = 0;
+    bool have_qr = false;
+    double c1 = 0.0, al = 0.0, norm = 0.0, nq = 0.0;
+restart:
+    if (++restarts > maxiter + 1) {
+        if (tid == 0) atomicOr(flags, DEVERR_SOLVER);
+        return iter;
+    }
+    have_qr = false;
+    sf_apply_fast(s, n, sd, has_iw, has_rs, s.x, s.r);                       // :841-844
+    {
+        double nr = 0.0;
+        for (int i = tid; i < m; i += T) {
+            const double v = s.B[i] - s.r[i];
+            s.r[i] = v; s.g1[i] = v; s.q0[i] = v;
+            nr = fma(v, v, nr);
+        }
+        norm = cta_sum(nr, red);                                               // (syncs: g1 complete)
+    }
+    sf_apply_fast(s, n, sd, has_iw, has_rs, s.g1, s.w1);                     // :851
+    {
+        double c = 0.0;
+        for (int i = tid; i < m; i += T) c = fma(s.q0[i], s.w1[i], c);
+        c1 = cta_sum(c, red);
+    }
+    if (fabs(norm / md) < thr) return iter;                                    // :866
+    for (;;) {
+        if (!have_qr) {                                                        // :871-877
+            double q = 0.0;
+            for (int i = tid; i < m; i += T) q = fma(s.q0[i], s.r[i], q);
+            al = cta_sum(q, red) / c1;
+        }
+        if (!(c1 != 0.0)) goto restart;
+        for (int i = tid; i < m; i += T) {
+            s.u[i] = fma(-al, s.w1[i], s.r[i]);
+            s.x[i] = fma(al, s.g1[i], s.x[i]);
+        }
+        __syncthreads();
+        sf_apply_fast(s, n, sd, has_iw, has_rs, s.u, s.Au);                  // :890
+        double nrm, ro;
+        {
+            double aa = 0.0, au = 0.0;
+            for (int i = tid; i < m; i += T) {
+                aa = fma(s.Au[i], s.Au[i], aa);
+                au = fma(s.Au[i], s.u[i], au);
+            }
+            cta_sum2(aa, au, red, &nrm, &ro);
+        }
+        const double ro1 = -ro / nrm;                                          // :903
+        if (nrm == 0.0) goto restart;
+        for (int i = tid; i < m; i += T) s.x[i] = fma(-ro1, s.u[i], s.x[i]);
+        __syncthreads();
+        sf_apply_fast(s, n, sd, has_iw, has_rs, s.x, s.r);                   // :943-947
+        {
+            double qn = 0.0, rr = 0.0;
+            for (int i = tid; i < m; i += T) {
+                const double v = s.B[i] - s.r[i];
+                s.r[i] = v;
+                qn = fma(-s.q0[i], v, qn);                                     // beta's -q.r (:1056-1059)
+                rr = fma(v, v, rr);
+            }
+            cta_sum2(qn, rr, red, &nq, &norm);
+        }
+        double beta = nq / c1;                                                 // :1060-1065
+        if (c1 == 0.0) beta = 0.0;
+        const double bro = beta / ro1;
+        for (int i = tid; i < m; i += T) s.g0[i] = fma(bro, s.g1[i], fma(beta, s.w1[i], s.r[i]));
+        __syncthreads();
+        sf_apply_fast(s, n, sd, has_iw, has_rs, s.g0, s.w0);                 // :1094
+        {
+            double c = 0.0;
+            for (int i = tid; i < m; i += T) c = fma(s.q0[i], s.w0[i], c);
+            if (tid == 0) scal[8] = gtimer_ns() - t0 > SF_TIME_LIMIT_NS ? 1.0 : 0.0;
+            c1 = cta_sum(c, red);                                              // c[0], the shift :1104-1121
+        }
+        if (nq != 0.0) al = -nq / c1;
+        have_qr = nq != 0.0;
+        {
+            double *t = s.g0; s.g0 = s.g1; s.g1 = t;
+            t = s.w0; s.w0 = s.w1; s.w1 = t;
+        }
+        restarts = 0;
+        if (fabs(norm / md) < thr) break;                                     // :1126-1132
+        ++iter;
+        if (iter == maxiter) break;
+        if (scal[8] != 0.0) {
+            if (tid == 0) atomicOr(flags, DEVERR_SOLVER);
+            break;
+        }
+    }
+    return iter;
+}
+
 __device__ __forceinline__ void sf_copy(double *dst, const double *src, int m)
 {
     for (int i = threadIdx.x; i < m; i += blockDim.x) dst[i] = src[i];
@@ -289,6 +458,7 @@ __global__ void __launch_bounds__(SF_THREADS, 6) k_sf_batch(SfBatchArgs a, int s
 // the pass (line-major: per line A, B, Rlap, mc0, mc1, mc2, iw, each Nl+1 values), the state and
 // this step's source, history and line ends; solved in place and written back with the ghost copy
 // U[Nl+1] = U[Nl] (U1 :4792).
+template <bool FAST>
 __global__ void __launch_bounds__(SF_THREADS, 6) k_lod_pass_sf(LodSfArgs a)
 {
     extern __shared__ __align__(16) double sf_sm[];
@@ -329,7 +499,9 @@ __global__ void __launch_bounds__(SF_THREADS, 6) k_lod_pass_sf(LodSfArgs a)
         }
     }
     __syncthreads();
-    const int it = sf_solve_cta(s, n, a.sd, true, false, a.thr, a.maxiter, scal, a.flags);
+    __shared__ double red[2 * SF_THREADS / 32];
+    const int it = FAST ? sf_solve_cta_fast(s, n, a.sd, true, false, a.thr, a.maxiter, scal, red, a.flags)
+                        : sf_solve_cta(s, n, a.sd, true, false, a.thr, a.maxiter, scal, a.flags);
     for (int p = tid; p < m; p += T) a.U[base + (int64_t)p * a.st] = s.x[p];
     if (tid == 0) {
         a.U[base + (int64_t)m * a.st] = s.x[n];
@@ -344,7 +516,8 @@ size_t sf_smem_bytes(int n) { return (size_t)SF_NVEC * (size_t)(n + 1) * sizeof(
 int sf_prepare()
 {
     const int bytes = (int)sf_smem_bytes(FPDE_SF_MAX_N);
-    if (smem_opt_in((const void *)k_lod_pass_sf, bytes) != cudaSuccess ||
+    if (smem_opt_in((const void *)k_lod_pass_sf<false>, bytes) != cudaSuccess ||
+        smem_opt_in((const void *)k_lod_pass_sf<true>, bytes) != cudaSuccess ||
         smem_opt_in((const void *)k_sf_batch, bytes) != cudaSuccess)
         return set_error(FPDE_ERR_CUDA, "space-fractional kernels: shared memory opt-in failed");
     return FPDE_OK;
@@ -353,7 +526,8 @@ int sf_prepare()
 int launch_lod_pass_sf(cudaStream_t st, const LodSfArgs &a)
 {
     const size_t smem = sf_smem_bytes(a.Nl);
-    k_lod_pass_sf<<<(unsigned)a.lines, SF_THREADS, smem, st>>>(a);
+    if (a.fast) k_lod_pass_sf<true><<<(unsigned)a.lines, SF_THREADS, smem, st>>>(a);
+    else k_lod_pass_sf<false><<<(unsigned)a.lines, SF_THREADS, smem, st>>>(a);
     FPDE_LAUNCHED(1);
     return FPDE_OK;
 }

@@ -493,7 +493,10 @@ int fpde_sf3d_solve(fpde_ctx *ctx, const fpde_sf3d_system *sys, const double *B,
 /* The implicit space-fractional solves of a 3D LOD (fpde_lod3d_desc.space_frac): per pass p the
  * Toeplitz row Tm[p] (Nl+1 values), the Mcoefs grids mc[p] (three host grids: lower, diagonal,
  * upper, at every interior line node) and inv_dw_dh iw[p] (one grid), and the solver's threshold
- * and iteration cap. Line lengths at most FPDE_SF_MAX_N.
+ * and iteration cap. Line lengths at most FPDE_SF_MAX_N. exact = 1 runs every line solve as
+ * fpde_sf_solve does (bit for bit the reference's); exact = 0 (faster) sums each dot product in a
+ * fixed tree over the line's CTA and fuses every product into its sum (deterministic; it differs
+ * from the reference's only in the order and rounding of those operations).
  * implicit3d = 1 replaces the three passes of line solves by the reference's fully implicit scheme
  * (calc_step :5160-5716 with implicit3d 1): each step adds every line's system of the K, _M and sN
  * passes into one 3D system (the time term and the history in the K pass only) and solves it with
@@ -506,7 +509,7 @@ typedef struct fpde_space_frac {
     const double *mc[3];        /* each 3 x grid */
     const double *iw[3];        /* each one grid */
     int implicit3d;             /* 0: line solves per pass (LOD); 1: one 3D solve per step */
-    int exact;                  /* with implicit3d: sequential dot products */
+    int exact;                  /* 1: the reference's operation order (sequential dot products) */
 } fpde_space_frac;
 
 typedef struct fpde_lod3d_desc {

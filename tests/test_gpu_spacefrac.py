@@ -111,12 +111,12 @@ def test_bad_sizes_are_errors(ctx):
     assert e.value.code == 1
 
 
-def _lod(ctx, c, precision=0, max_steps=None):
+def _lod(ctx, c, precision=0, max_steps=None, exact=False):
     import fpde_hpc_gb300 as fp
     g = c["g"]
     sN, M, K = c["dims"]
     sf = dict(space_der=c["space_der"], tol=c["thr"], max_iter=c["maxiter"], Tm=[c["Tm"][p] for p in range(3)],
-              mc=[c["mc"][p] for p in range(3)], iw=[c["iw"][p] for p in range(3)])
+              mc=[c["mc"][p] for p in range(3)], iw=[c["iw"][p] for p in range(3)], exact=1 if exact else 0)
     steps = c["steps"]
     ends = {} if c["rkind"] is None else dict(right_kind=c["rkind"], dLN=c["dLN"])
     return fp.Lod3D(ctx, c["dims"], float(g["alpha"]), float(g["tau"][0]), c["Da"], c["coefA"], c["coefB"],
@@ -139,16 +139,19 @@ def _oracle_envelope(c, rel):
     return worst
 
 
+@pytest.mark.parametrize("exact", [False, True])
 @pytest.mark.parametrize("name", sf_cases.NAMES)
-def test_lod_replay_vs_reference(ctx, name):
+def test_lod_replay_vs_reference(ctx, name, exact):
     """The GPU's history sum differs from the reference's in the last bits, and the solver carries
     that: the bar is ten times the reference's own response to a 1e-15 change of its source (with
     the default threshold 1e-9 that response is 3e-5 on fpde_sf_sd0: the solution is an iterate;
-    with the tight threshold of fpde_sf_col it is 3.4e-12: the converged solution), and 1e-12."""
+    with the tight threshold of fpde_sf_col it is 3.4e-12: the converged solution), and 1e-12. Both
+    forms: exact (the line solves bit for bit the reference's) and the fast one (tree dot products,
+    fused multiply-adds)."""
     c = sf_cases.load(name)
     g = c["g"]
     env = max(_oracle_envelope(c, 1e-15), _oracle_envelope(c, -1e-15))
-    lod = _lod(ctx, c)
+    lod = _lod(ctx, c, exact=exact)
     worst = 0.0
     for n in range(c["steps"]):
         lod.run(1)
@@ -184,8 +187,9 @@ def _synthetic(dims, gam, seed):
     return coefA, coefB, coefR, mc, iw, Tm, rp, u0
 
 
+@pytest.mark.parametrize("exact", [False, True])
 @pytest.mark.parametrize("sd", [0, 1])
-def test_lod_larger_grid_vs_oracle(ctx, sd):
+def test_lod_larger_grid_vs_oracle(ctx, sd, exact):
     """20 x 16 x 40 cells, 12 steps, both solved to a tight threshold: the GPU against the oracle.
     The two sum the history in different orders (last bits); the bar is ten times the oracle's own
     response to a 1e-15 change of the source (measured here: a few 1e-12)."""
@@ -193,7 +197,7 @@ def test_lod_larger_grid_vs_oracle(ctx, sd):
     dims, alpha, tau, steps, thr, mx = (20, 16, 40), 0.75, 1e-3, 12, 1e-24, 300
     coefA, coefB, coefR, mc, iw, Tm, rp, u0 = _synthetic(dims, 0.7, 3 + sd)
     Da = 1.0 / fp.gamma(1.0 - alpha)
-    sf = dict(space_der=sd, tol=thr, max_iter=mx, Tm=list(Tm), mc=list(mc), iw=list(iw))
+    sf = dict(space_der=sd, tol=thr, max_iter=mx, Tm=list(Tm), mc=list(mc), iw=list(iw), exact=1 if exact else 0)
     lod = fp.Lod3D(ctx, dims, alpha, tau, Da, coefA, coefB, coefR, u0, steps, source=rp, space_frac=sf)
     t = oracle.time_points(np.full(steps, tau))
     bc = np.zeros_like(u0)
@@ -221,13 +225,14 @@ def test_lod_larger_grid_vs_oracle(ctx, sd):
     assert worst <= max(10.0 * env, 1e-12), (worst, env)
 
 
-def test_lod_one_call_equals_step_by_step(ctx):
-    """A run captured as one graph gives the same grid as per-step calls."""
+@pytest.mark.parametrize("exact", [False, True])
+def test_lod_one_call_equals_step_by_step(ctx, exact):
+    """A run in one call gives the same grid as per-step calls (both forms are deterministic)."""
     c = sf_cases.load("fpde_sf_col")
-    a = _lod(ctx, c)
+    a = _lod(ctx, c, exact=exact)
     for _ in range(c["steps"]):
         a.run(1)
-    b = _lod(ctx, c)
+    b = _lod(ctx, c, exact=exact)
     b.run(c["steps"])
     assert np.array_equal(a.state(), b.state())
     a.close()
