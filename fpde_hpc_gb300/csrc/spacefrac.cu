@@ -238,39 +238,48 @@ restart:
 
 // ----------------------------------------------------------------- the fast form of a line solve
 
-// The same solve with deterministic tree sums and fused multiply-adds: each dot product is every
-// thread's partial over its values folded by warp shuffles and then over the warps in a fixed
-// order (a few FP64 instructions per thread instead of m sequential adds on one lane), and every
-// product that feeds a sum is one fused multiply-add. The operation order differs from the
+// The same solve with deterministic tree sums and fused multiply-adds: each dot product is one
+// warp's lane partials folded by shuffles in a fixed tree (a few warp-wide FP64 instructions instead
+// of m sequential adds on one lane), and every product that feeds a sum is one fused multiply-add. The operation order differs from the
 // reference's (the LOD's default; space_frac.exact selects sf_solve_cta).
 
-// Sum of v over the CTA, the same value in every thread (red: one double per warp).
-__device__ __forceinline__ double cta_sum(double v, double *red)
+// Dot products of the line by one warp each (warp q for product q): its lanes take the values
+// i = lane, lane + 32, ... as fused multiply-adds and fold them in a shuffle tree, and lane 0 puts
+// the sum in red[q]; the caller synchronises the CTA before and after. A dot product costs a few
+// warp-wide FP64 instructions instead of one per value on one lane.
+__device__ __forceinline__ double warp_dot(const double *a, const double *b, int m, bool neg)
 {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, W = blockDim.x >> 5;
-#pragma unroll
-    for (int o = 16; o >= 1; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-    if (lane == 0) red[warp] = v;
-    __syncthreads();
     double t = 0.0;
-    for (int w = 0; w < W; ++w) t += red[w];
+    for (int i = threadIdx.x & 31; i < m; i += 32) t = fma(neg ? -a[i] : a[i], b[i], t);
+#pragma unroll
+    for (int o = 16; o >= 1; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
+    return t;
+}
+// One dot product a.b (every thread gets it); the vectors must be complete (CTA synchronised).
+__device__ __forceinline__ double cta_dot(const double *a, const double *b, int m, double *red)
+{
+    if (threadIdx.x < 32) {
+        const double t = warp_dot(a, b, m, false);
+        if (threadIdx.x == 0) red[0] = t;
+    }
+    __syncthreads();
+    const double t = red[0];
     __syncthreads();
     return t;
 }
-__device__ __forceinline__ void cta_sum2(double a, double b, double *red, double *oa, double *ob)
+// Two dot products on two warps; neg0: the first is -(a0.b0) (beta's "beta -= q*r").
+__device__ __forceinline__ void cta_dot2(const double *a0, const double *b0, bool neg0, const double *a1,
+                                         const double *b1, int m, double *red, double *o0, double *o1)
 {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, W = blockDim.x >> 5;
-#pragma unroll
-    for (int o = 16; o >= 1; o >>= 1) {
-        a += __shfl_down_sync(0xffffffffu, a, o);
-        b += __shfl_down_sync(0xffffffffu, b, o);
+    const int warp = threadIdx.x >> 5;
+    if (warp < 2) {
+        const double t = warp == 0 ? warp_dot(a0, b0, m, neg0) : warp_dot(a1, b1, m, false);
+        if ((threadIdx.x & 31) == 0) red[warp] = t;
     }
-    if (lane == 0) { red[warp] = a; red[W + warp] = b; }
     __syncthreads();
-    double ta = 0.0, tb = 0.0;
-    for (int w = 0; w < W; ++w) { ta += red[w]; tb += red[W + w]; }
+    *o0 = red[0];
+    *o1 = red[1];
     __syncthreads();
-    *oa = ta; *ob = tb;
 }
 
 // Row i of the product with fused multiply-adds (the reference's terms in its order).
@@ -286,6 +295,9 @@ __device__ __forceinline__ double sf_row_fast(const SfVec &s, int n, int sd, boo
     return has_iw ? fma(v, s.iw[i], r) : r + v;
 }
 
+// rv = the product with fused multiply-adds; a thread takes the rows k+1 and n-1-k. (A walker that
+// evens out the lanes' loop lengths, as the 3D product does, measured slower here: its index
+// updates cost more than the divergent loop bounds.)
 __device__ void sf_apply_fast(const SfVec &s, int n, int sd, bool has_iw, bool has_rs, const double *xv, double *rv)
 {
     const int T = blockDim.x, tid = threadIdx.x;
@@ -322,28 +334,17 @@ restart:
     }
     have_qr = false;
     sf_apply_fast(s, n, sd, has_iw, has_rs, s.x, s.r);                       // :841-844
-    {
-        double nr = 0.0;
-        for (int i = tid; i < m; i += T) {
-            const double v = s.B[i] - s.r[i];
-            s.r[i] = v; s.g1[i] = v; s.q0[i] = v;
-            nr = fma(v, v, nr);
-        }
-        norm = cta_sum(nr, red);                                               // (syncs: g1 complete)
+    for (int i = tid; i < m; i += T) {
+        const double v = s.B[i] - s.r[i];
+        s.r[i] = v; s.g1[i] = v; s.q0[i] = v;
     }
+    __syncthreads();
+    norm = cta_dot(s.r, s.r, m, red);
     sf_apply_fast(s, n, sd, has_iw, has_rs, s.g1, s.w1);                     // :851
-    {
-        double c = 0.0;
-        for (int i = tid; i < m; i += T) c = fma(s.q0[i], s.w1[i], c);
-        c1 = cta_sum(c, red);
-    }
+    c1 = cta_dot(s.q0, s.w1, m, red);
     if (fabs(norm / md) < thr) return iter;                                    // :866
     for (;;) {
-        if (!have_qr) {                                                        // :871-877
-            double q = 0.0;
-            for (int i = tid; i < m; i += T) q = fma(s.q0[i], s.r[i], q);
-            al = cta_sum(q, red) / c1;
-        }
+        if (!have_qr) al = cta_dot(s.q0, s.r, m, red) / c1;                    // :871-877
         if (!(c1 != 0.0)) goto restart;
         for (int i = tid; i < m; i += T) {
             s.u[i] = fma(-al, s.w1[i], s.r[i]);
@@ -352,41 +353,23 @@ restart:
         __syncthreads();
         sf_apply_fast(s, n, sd, has_iw, has_rs, s.u, s.Au);                  // :890
         double nrm, ro;
-        {
-            double aa = 0.0, au = 0.0;
-            for (int i = tid; i < m; i += T) {
-                aa = fma(s.Au[i], s.Au[i], aa);
-                au = fma(s.Au[i], s.u[i], au);
-            }
-            cta_sum2(aa, au, red, &nrm, &ro);
-        }
+        cta_dot2(s.Au, s.Au, false, s.Au, s.u, m, red, &nrm, &ro);
         const double ro1 = -ro / nrm;                                          // :903
         if (nrm == 0.0) goto restart;
         for (int i = tid; i < m; i += T) s.x[i] = fma(-ro1, s.u[i], s.x[i]);
         __syncthreads();
         sf_apply_fast(s, n, sd, has_iw, has_rs, s.x, s.r);                   // :943-947
-        {
-            double qn = 0.0, rr = 0.0;
-            for (int i = tid; i < m; i += T) {
-                const double v = s.B[i] - s.r[i];
-                s.r[i] = v;
-                qn = fma(-s.q0[i], v, qn);                                     // beta's -q.r (:1056-1059)
-                rr = fma(v, v, rr);
-            }
-            cta_sum2(qn, rr, red, &nq, &norm);
-        }
+        for (int i = tid; i < m; i += T) s.r[i] = s.B[i] - s.r[i];
+        __syncthreads();
+        cta_dot2(s.q0, s.r, true, s.r, s.r, m, red, &nq, &norm);              // beta's -q.r, r.r
         double beta = nq / c1;                                                 // :1060-1065
         if (c1 == 0.0) beta = 0.0;
         const double bro = beta / ro1;
         for (int i = tid; i < m; i += T) s.g0[i] = fma(bro, s.g1[i], fma(beta, s.w1[i], s.r[i]));
         __syncthreads();
         sf_apply_fast(s, n, sd, has_iw, has_rs, s.g0, s.w0);                 // :1094
-        {
-            double c = 0.0;
-            for (int i = tid; i < m; i += T) c = fma(s.q0[i], s.w0[i], c);
-            if (tid == 0) scal[8] = gtimer_ns() - t0 > SF_TIME_LIMIT_NS ? 1.0 : 0.0;
-            c1 = cta_sum(c, red);                                              // c[0], the shift :1104-1121
-        }
+        if (tid == 0) scal[8] = gtimer_ns() - t0 > SF_TIME_LIMIT_NS ? 1.0 : 0.0;
+        c1 = cta_dot(s.q0, s.w0, m, red);                                      // c[0], the shift :1104-1121
         if (nq != 0.0) al = -nq / c1;
         have_qr = nq != 0.0;
         {
@@ -459,7 +442,7 @@ __global__ void __launch_bounds__(SF_THREADS, 6) k_sf_batch(SfBatchArgs a, int s
 // this step's source, history and line ends; solved in place and written back with the ghost copy
 // U[Nl+1] = U[Nl] (U1 :4792).
 template <bool FAST>
-__global__ void __launch_bounds__(SF_THREADS, 6) k_lod_pass_sf(LodSfArgs a)
+__global__ void __launch_bounds__(SF_THREADS, 6) k_lod_pass_sf(LodSfArgs a)   // (5 per SM measured slower)
 {
     extern __shared__ __align__(16) double sf_sm[];
     __shared__ double scal[10];
@@ -499,7 +482,7 @@ __global__ void __launch_bounds__(SF_THREADS, 6) k_lod_pass_sf(LodSfArgs a)
         }
     }
     __syncthreads();
-    __shared__ double red[2 * SF_THREADS / 32];
+    __shared__ double red[2];
     const int it = FAST ? sf_solve_cta_fast(s, n, a.sd, true, false, a.thr, a.maxiter, scal, red, a.flags)
                         : sf_solve_cta(s, n, a.sd, true, false, a.thr, a.maxiter, scal, a.flags);
     for (int p = tid; p < m; p += T) a.U[base + (int64_t)p * a.st] = s.x[p];
