@@ -13,12 +13,17 @@ L1 history sum and a Thomas solve. Other workloads of the same operator:
            over config 4's 130^3 grid
   weights  every L1 weight row of a 4,096-step run with the generalized kernel g(t) = t^1.5 and
            variable steps (fpde_weights_g: 8.4 M weights per call)
+  sf3d     3D 64^3, 32 steps with the implicit space-fractional operator (gamma 0.7): the LOD's
+           line solves (vmul_T + solve_mln<1>), or with --implicit3d 1 the fully implicit scheme
+           (one vmul_T_3d solve over the grid per step); --space-der 1 two-sided, --sf-exact the
+           reference's operation order (else tree dot products and fused multiply-adds)
 `value` is measured with inputs resident in HBM (CUDA events on the library's stream, the
 run replayed from a captured CUDA graph, no probes); `e2e` goes through the C ABI with host
 buffers (the *_solve_host calls: upload the initial state, solve, download the state).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload config2|config3|config4|config5] [--precision auto|fp64|bf16|f16|bf16x3]
+                    [--workload config2|config3|config4|config5|sum1|sum2|weights|sf3d]
+                    [--precision auto|fp64|bf16|f16|bf16x3] [--implicit3d 0|1] [--space-der 0|1] [--sf-exact]
 
 --impl reference times the reference algorithm on the host cores: the CPU restatement of the
 reference's FP64 path (oracle/), on all host threads, on a bounded sample of the same workload
