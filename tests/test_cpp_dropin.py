@@ -6,6 +6,9 @@ library's gb300_call_sum adapter in place of fr_ocl_call_sum, replayed on the re
 (tests/golden/fpde_column_a2: its snapshots, kb_3_cache and tau of every step); its Sums must
 equal the reference's to 1e-12. tests/cpp/dropin_line.cpp advances a column on the device in one
 call, block by block (fpde_step_block) and step by step, each compared with the oracle.
+tests/cpp/dropin_sf3d.cpp is calc_step's implicit3d solve_mln<1>(..., vmul_T_3d) call
+(fpde_hpc_1d.cpp:5705) with the library in its place, fed the reference's recorded system
+(tests/golden/fpde_sf3d_*): its product and solution must equal the reference's bit for bit.
 
 Without a GPU the programs are compiled and linked only (the -m "not gpu" run); on the GPU they
 run.
@@ -29,7 +32,7 @@ def programs(tmp_path_factory):
     lib = build.build()
     d = tmp_path_factory.mktemp("dropin")
     exe = {}
-    for name in ("dropin_sum", "dropin_line"):
+    for name in ("dropin_sum", "dropin_line", "dropin_sf3d"):
         out = str(d / name)
         cmd = ["g++", "-O2", "-std=c++17", "-Wall", "-I", os.path.join(ROOT, "include"),
                os.path.join(CPP, name + ".cpp"), "-L", os.path.dirname(lib), "-lfpde_gb300",
@@ -105,3 +108,25 @@ def test_cpp_column_whole_blockwise_stepwise(programs, precision, tol):
     # a block-by-block or step-by-step caller instantiates no CUDA graph
     assert "way 1: 200 steps, graphs cached 0, instantiated 0" in log
     assert "way 2: 200 steps, graphs cached 0, instantiated 0" in log
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["fpde_sf3d_sd1", "fpde_sf3d_tight"])
+def test_cpp_sf3d_solve_reproduces_reference(programs, name):
+    import sf3d_cases
+    exe, d = programs
+    c = sf3d_cases.load(name)
+    g = c["g"]
+    sN, M, K = c["dims"]
+    inp, out = str(d / f"{name}.in"), str(d / f"{name}.out")
+    with open(inp, "wb") as f:
+        np.array([sN, M, K, c["space_der"], c["maxiter"]], dtype="<i8").tofile(f)
+        np.array([c["thr"]], dtype="<f8").tofile(f)
+        for a in (g["sys_last_mat"], c["mc3d"], *c["Tm3"], c["iw3"], g["sys_last_om"], g["solve_x0"], g["mv_x"]):
+            np.ascontiguousarray(a, dtype="<f8").tofile(f)
+    _run(exe["dropin_sf3d"], inp, out)
+    V = c["V"]
+    res = np.fromfile(out, dtype="<f8", count=2 * V)
+    iters = int(np.fromfile(out, dtype="<i8", offset=16 * V)[0])
+    assert np.array_equal(res[:V], g["mv_r"])
+    assert np.array_equal(res[V:], g["solve_sol"]) and iters == c["solve_iters"]
