@@ -301,12 +301,21 @@ class LodWorkload:
         self.desc = (f"3D LOD {n}^3, {self.p.steps} steps, alpha 0.85, tau 1e-3, lognormal k (sigma 0.4, seed 5), "
                      "Gaussian blob, zero-flux sides, Dirichlet top/bottom (config 4)")
 
-    def build(self, ctx, prec):
+    def build(self, ctx, prec, segments=(0, 0, 0)):
         import fpde_hpc_gb300 as fp
         p = self.p
         cA, cB, cR = p.coefs()
         return fp.Lod3D(ctx, p.dims, p.alpha, p.tau, p.Da, cA, cB, cR, p.u0, p.steps, left_kind=p.left_kind,
-                        right_kind=p.right_kind, dLN=p.dLN, precision=prec)
+                        right_kind=p.right_kind, dLN=p.dLN, precision=prec, segments=segments)
+
+    def autotune(self, ctx, prec):
+        """fpde_lod3d_autotune over the first min(steps, 128) steps: the passes' segment counts."""
+        import fpde_hpc_gb300 as fp
+        p = self.p
+        cA, cB, cR = p.coefs()
+        s = min(p.steps, 128)
+        return fp.autotune_lod3d(ctx, p.dims, p.alpha, p.tau, p.Da, cA, cB, cR, p.u0, s, s, left_kind=p.left_kind,
+                                 right_kind=p.right_kind, dLN=p.dLN, precision=prec)
 
     @property
     def u0(self):
@@ -1017,11 +1026,17 @@ def run_ours(args):
     pname = {0: "fp64", 1: "split-bf16", 2: "split-fp16", 3: "split-bf16x3"}[prec]
 
     tuning = None
-    if is_line and not args.no_autotune:
+    lod_tuned = type(wl) is LodWorkload and not args.no_autotune
+    if (is_line or lod_tuned) and not args.no_autotune:
         t0 = time.perf_counter()
         tuning = wl.autotune(ctx, prec)
         tune_s = time.perf_counter() - t0
-    obj = wl.build(ctx, prec, tuning) if is_line else wl.build(ctx, prec)
+    if is_line:
+        obj = wl.build(ctx, prec, tuning)
+    elif lod_tuned:
+        obj = wl.build(ctx, prec, tuning[0])
+    else:
+        obj = wl.build(ctx, prec)
     u0_dev = torch.from_numpy(np.ascontiguousarray(wl.u0)).cuda()
     steps = wl.steps
     for _ in range(args.warmup):
@@ -1075,7 +1090,10 @@ def run_ours(args):
            "data": "synthetic (seeded; no dataset exists for this operator)",
            "config": bench_config(wl, world), "path": pname,
            "e2e": e2e, "gpu_launches": int(launches), "clocks": clk}
-    if tuning is not None:
+    if tuning is not None and lod_tuned:
+        out["tuning"] = {"segments": list(tuning[0]), "tuned_ms_per_step": tuning[1], "autotune_seconds": tune_s,
+                         "note": "segments per line of each pass (0 = the built-in rule), fpde_lod3d_autotune"}
+    elif tuning is not None:
         out["tuning"] = {"solve_sp": tuning.solve_sp, "chunks": tuning.chunks,
                          "far_splits": tuning.far_splits, "gemv_splits": tuning.gemv_splits,
                          "far_super_blocks": tuning.far_super, "tuned_ms_per_step": tuning.ms_per_step,

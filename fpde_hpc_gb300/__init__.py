@@ -6,7 +6,7 @@ problem generators of the benchmark configurations. Importing it does not need a
 creating a context does, and every compute call runs on the GPU (no CPU fallback).
 """
 from ._lib import FpdeError, LineDesc, LineTuning, load, check  # noqa: F401
-from .api import Batch, Context, History, Line, Lod3D, weights_l1, weights_l1_lags, restricted_lags, gamma, line_coefs, do_weights, autotune_line, sf_toeplitz_row  # noqa: F401
+from .api import Batch, Context, History, Line, Lod3D, weights_l1, weights_l1_lags, restricted_lags, gamma, line_coefs, do_weights, autotune_line, autotune_lod3d, sf_toeplitz_row  # noqa: F401
 
 FPDE_PREC_FP64 = 0
 FPDE_PREC_SPLIT_BF16 = 1

@@ -54,7 +54,7 @@ class Lod3dDesc(C.Structure):
                 ("max_steps", c_int), ("lag_weights", c_vp), ("source", c_vp), ("source_rows", c_int),
                 ("bc", c_vp), ("bc_rows", c_int), ("restrict_eps", c_dbl), ("series_terms", c_int),
                 ("richards", C.POINTER(Richards)), ("time_steps", c_vp), ("weight_rows", c_vp),
-                ("kernel_power", c_dbl), ("space_frac", C.POINTER(SpaceFrac))]
+                ("kernel_power", c_dbl), ("space_frac", C.POINTER(SpaceFrac)), ("segments", c_int * 3)]
 
 
 class ColumnDesc(C.Structure):
@@ -93,6 +93,8 @@ _SIGS = {
     "fpde_lod3d_solve_host": (c_int, [c_vp, c_vp, c_int, c_vp]),
     "fpde_lod3d_steps_done": (c_int, [c_vp, C.POINTER(c_i64)]),
     "fpde_lod3d_sf_iterations": (c_int, [c_vp, C.POINTER(c_i64)]),
+    "fpde_lod3d_autotune": (c_int, [c_vp, C.POINTER(Lod3dDesc), c_vp, c_vp, c_vp, c_vp, c_int, c_int * 3,
+                                    C.POINTER(c_dbl)]),
     "fpde_lod3d_get_concentration": (c_int, [c_vp, c_vp, c_int]),
     "fpde_sf_matvec": (c_int, [c_vp, c_int, c_int, c_vp, c_vp, c_vp, c_vp, c_vp, c_int, c_vp, c_vp, c_int]),
     "fpde_sf_solve": (c_int, [c_vp, c_int, c_int, c_vp, c_vp, c_vp, c_vp, c_vp, c_int, c_vp, c_vp, c_dbl, c_int,

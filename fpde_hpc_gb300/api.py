@@ -450,6 +450,94 @@ class Line:
         return n.value
 
 
+def _lod3d_desc(dims, alpha, tau, Da, coefA, coefB, coefRlap, max_steps, left_kind, right_kind, dLN, source, bc,
+                lag_weights, precision, restrict_eps, series_terms, richards, space_frac, time_steps, weight_rows,
+                kernel_power, segments):
+    """The fpde_lod3d_desc of Lod3D's arguments, the arrays it points into and the coefficient grids."""
+    sN, M, K = dims
+    shape = (K + 2, M + 2, sN + 2)
+    d = Lod3dDesc(sN=sN, M=M, K=K, alpha=alpha, tau=tau, Da=Da, precision=precision, max_steps=max_steps,
+                  restrict_eps=restrict_eps, series_terms=series_terms)
+    for q in range(3):
+        d.left_kind[q], d.right_kind[q], d.dLN[q] = left_kind[q], right_kind[q], dLN[q]
+        d.segments[q] = int(segments[q])
+    keep = []
+
+    def rows(x):
+        a = np.ascontiguousarray(x, dtype=np.float64)
+        if a.shape == shape:
+            a = a[None]
+        if a.shape[1:] != shape:
+            raise ValueError("grid inputs need shape (rows, K+2, M+2, sN+2)")
+        keep.append(a)
+        return a.ctypes.data, a.shape[0]
+
+    if source is not None:
+        d.source, d.source_rows = rows(source)
+    if bc is not None:
+        d.bc, d.bc_rows = rows(bc)
+    if lag_weights is not None:
+        w = np.ascontiguousarray(lag_weights, dtype=np.float64)
+        if len(w) < max_steps + 1:
+            raise ValueError("lag_weights needs max_steps + 1 values")
+        keep.append(w)
+        d.lag_weights = w.ctypes.data
+    if richards is not None:
+        arrs = [np.ascontiguousarray(richards[k], dtype=np.float64) for k in ("sZ", "evaporation")]
+        dls = [np.ascontiguousarray(x, dtype=np.float64) for x in richards["dL"]]
+        if len(arrs[0]) < sN + 2 or any(len(x) < n + 2 for x, n in zip(dls, (sN, M, K))):
+            raise ValueError("richards: sZ needs sN+2 values, dL[p] intervals+2")
+        keep.extend(arrs + dls)
+        r = Richards(k_form=int(richards["k_form"]), k_sat=float(richards["k_sat"]), sZ=arrs[0].ctypes.data,
+                     evaporation=arrs[1].ctypes.data, evaporation_rows=len(arrs[1]))
+        for q in range(3):
+            r.dL[q] = dls[q].ctypes.data
+        if richards.get("c0") is not None:            # salt concentration (equation 1)
+            c0 = np.ascontiguousarray(richards["c0"], dtype=np.float64)
+            if c0.shape != shape:
+                raise ValueError("richards: c0 needs the grid's shape")
+            keep.append(c0)
+            r.salt_c0 = c0.ctypes.data
+            r.salt_nu, r.salt_sigma, r.salt_D = (float(richards[k]) for k in ("nu", "sigma", "D"))
+        keep.append(r)
+        d.richards = C.pointer(r)
+    if time_steps is not None:
+        ts = np.ascontiguousarray(time_steps, dtype=np.float64)
+        if ts.size < max_steps:
+            raise ValueError("time_steps needs max_steps values")
+        keep.append(ts)
+        d.time_steps = ts.ctypes.data
+        d.kernel_power = float(kernel_power)
+        if weight_rows is not None:
+            wr = np.ascontiguousarray(weight_rows, dtype=np.float64)
+            if wr.shape != (max_steps, max_steps + 1):
+                raise ValueError("weight_rows needs shape (max_steps, max_steps + 1)")
+            keep.append(wr)
+            d.weight_rows = wr.ctypes.data
+    if space_frac is not None:
+        f = SpaceFrac(space_der=int(space_frac.get("space_der", 0)), tol=float(space_frac.get("tol", 1e-9)),
+                      max_iter=int(space_frac.get("max_iter", 5000)),
+                      implicit3d=int(space_frac.get("implicit3d", 0)), exact=int(space_frac.get("exact", 0)))
+        for q, nl in enumerate((sN, M, K)):
+            tm = np.ascontiguousarray(space_frac["Tm"][q], dtype=np.float64)
+            mc = np.ascontiguousarray(space_frac["mc"][q], dtype=np.float64)
+            iw = np.ascontiguousarray(space_frac["iw"][q], dtype=np.float64)
+            if tm.size < nl + 1 or mc.shape != (3,) + shape or iw.shape != shape:
+                raise ValueError("space_frac: Tm[p] needs Nl+1 values, mc[p] (3,)+grid, iw[p] one grid")
+            keep.extend([tm, mc, iw])
+            f.Tm[q], f.mc[q], f.iw[q] = tm.ctypes.data, mc.ctypes.data, iw.ctypes.data
+        keep.append(f)
+        d.space_frac = C.pointer(f)
+    if coefA is None and richards is not None:
+        cs = [None, None, None]
+    else:
+        cs = [np.ascontiguousarray(x, dtype=np.float64) for x in (coefA, coefB, coefRlap)]
+        for c in cs:
+            if c.shape != (3,) + shape:
+                raise ValueError("coefficient grids need shape (3, K+2, M+2, sN+2)")
+    return d, keep, cs
+
+
 class Lod3D:
     """The 3D LOD step of the reference (fpde_lod3d_*): grids are numpy arrays of shape
     (K+2, M+2, sN+2) (idx = i + j (sN+2) + k (sN+2)(M+2)); coefA/B/Rlap have a leading axis of 3
@@ -458,7 +546,7 @@ class Lod3D:
     def __init__(self, ctx, dims, alpha, tau, Da, coefA, coefB, coefRlap, u0, max_steps, left_kind=(0, 0, 0),
                  right_kind=(0, 0, 0), dLN=(0.0, 0.0, 0.0), source=None, bc=None, lag_weights=None,
                  precision=FP64, restrict_eps=0.0, series_terms=0, richards=None, space_frac=None,
-                 time_steps=None, weight_rows=None, kernel_power=0.0):
+                 time_steps=None, weight_rows=None, kernel_power=0.0, segments=(0, 0, 0)):
         """richards: optional dict(k_form, k_sat, sZ, dL=(sdL, dLx, dLy), evaporation) - the
         reference's Richards problem, coefficients formed from the grid every step (coefA/B/Rlap
         may then be None); with c0 (and nu, sigma, D) also the salt concentration (equation 1).
@@ -468,88 +556,15 @@ class Lod3D:
         reference's sequential dot products).
         time_steps: optional tau_n of every step (variable steps); weight_rows: optional
         (max_steps, max_steps+1) matrix of the steps' kb_3_cache rows with kkk0 on the diagonal
-        (else computed for g(t) = t^kernel_power)."""
+        (else computed for g(t) = t^kernel_power).
+        segments: threads per line of each pass's Thomas sweeps (0 = the built-in rule; see
+        autotune_lod3d)."""
         sN, M, K = dims
         self.ctx, self.dims = ctx, dims
         self.shape = (K + 2, M + 2, sN + 2)
-        d = Lod3dDesc(sN=sN, M=M, K=K, alpha=alpha, tau=tau, Da=Da, precision=precision, max_steps=max_steps,
-                      restrict_eps=restrict_eps, series_terms=series_terms)
-        for q in range(3):
-            d.left_kind[q], d.right_kind[q], d.dLN[q] = left_kind[q], right_kind[q], dLN[q]
-        keep = []
-
-        def rows(x):
-            a = np.ascontiguousarray(x, dtype=np.float64)
-            if a.shape == self.shape:
-                a = a[None]
-            if a.shape[1:] != self.shape:
-                raise ValueError("grid inputs need shape (rows, K+2, M+2, sN+2)")
-            keep.append(a)
-            return a.ctypes.data, a.shape[0]
-
-        if source is not None:
-            d.source, d.source_rows = rows(source)
-        if bc is not None:
-            d.bc, d.bc_rows = rows(bc)
-        if lag_weights is not None:
-            w = np.ascontiguousarray(lag_weights, dtype=np.float64)
-            if len(w) < max_steps + 1:
-                raise ValueError("lag_weights needs max_steps + 1 values")
-            keep.append(w)
-            d.lag_weights = w.ctypes.data
-        if richards is not None:
-            arrs = [np.ascontiguousarray(richards[k], dtype=np.float64) for k in ("sZ", "evaporation")]
-            dls = [np.ascontiguousarray(x, dtype=np.float64) for x in richards["dL"]]
-            if len(arrs[0]) < sN + 2 or any(len(x) < n + 2 for x, n in zip(dls, (sN, M, K))):
-                raise ValueError("richards: sZ needs sN+2 values, dL[p] intervals+2")
-            keep.extend(arrs + dls)
-            r = Richards(k_form=int(richards["k_form"]), k_sat=float(richards["k_sat"]), sZ=arrs[0].ctypes.data,
-                         evaporation=arrs[1].ctypes.data, evaporation_rows=len(arrs[1]))
-            for q in range(3):
-                r.dL[q] = dls[q].ctypes.data
-            if richards.get("c0") is not None:            # salt concentration (equation 1)
-                c0 = np.ascontiguousarray(richards["c0"], dtype=np.float64)
-                if c0.shape != self.shape:
-                    raise ValueError("richards: c0 needs the grid's shape")
-                keep.append(c0)
-                r.salt_c0 = c0.ctypes.data
-                r.salt_nu, r.salt_sigma, r.salt_D = (float(richards[k]) for k in ("nu", "sigma", "D"))
-            keep.append(r)
-            d.richards = C.pointer(r)
-        if time_steps is not None:
-            ts = np.ascontiguousarray(time_steps, dtype=np.float64)
-            if ts.size < max_steps:
-                raise ValueError("time_steps needs max_steps values")
-            keep.append(ts)
-            d.time_steps = ts.ctypes.data
-            d.kernel_power = float(kernel_power)
-            if weight_rows is not None:
-                wr = np.ascontiguousarray(weight_rows, dtype=np.float64)
-                if wr.shape != (max_steps, max_steps + 1):
-                    raise ValueError("weight_rows needs shape (max_steps, max_steps + 1)")
-                keep.append(wr)
-                d.weight_rows = wr.ctypes.data
-        if space_frac is not None:
-            f = SpaceFrac(space_der=int(space_frac.get("space_der", 0)), tol=float(space_frac.get("tol", 1e-9)),
-                          max_iter=int(space_frac.get("max_iter", 5000)),
-                          implicit3d=int(space_frac.get("implicit3d", 0)), exact=int(space_frac.get("exact", 0)))
-            for q, nl in enumerate((sN, M, K)):
-                tm = np.ascontiguousarray(space_frac["Tm"][q], dtype=np.float64)
-                mc = np.ascontiguousarray(space_frac["mc"][q], dtype=np.float64)
-                iw = np.ascontiguousarray(space_frac["iw"][q], dtype=np.float64)
-                if tm.size < nl + 1 or mc.shape != (3,) + self.shape or iw.shape != self.shape:
-                    raise ValueError("space_frac: Tm[p] needs Nl+1 values, mc[p] (3,)+grid, iw[p] one grid")
-                keep.extend([tm, mc, iw])
-                f.Tm[q], f.mc[q], f.iw[q] = tm.ctypes.data, mc.ctypes.data, iw.ctypes.data
-            keep.append(f)
-            d.space_frac = C.pointer(f)
-        if coefA is None and richards is not None:
-            cs = [None, None, None]
-        else:
-            cs = [np.ascontiguousarray(x, dtype=np.float64) for x in (coefA, coefB, coefRlap)]
-            for c in cs:
-                if c.shape != (3,) + self.shape:
-                    raise ValueError("coefficient grids need shape (3, K+2, M+2, sN+2)")
+        d, keep, cs = _lod3d_desc(dims, alpha, tau, Da, coefA, coefB, coefRlap, max_steps, left_kind, right_kind,
+                                  dLN, source, bc, lag_weights, precision, restrict_eps, series_terms, richards,
+                                  space_frac, time_steps, weight_rows, kernel_power, segments)
         self._keep = keep
         u0 = np.ascontiguousarray(u0, dtype=np.float64)
         self.h = C.c_void_p()
@@ -662,3 +677,23 @@ class Batch:
         check(self.ctx.lib.fpde_batch_solve_host(self.h, _ptr(u0_padded), steps, _ptr(out_padded)),
               "fpde_batch_solve_host")
         return out_padded
+
+
+def autotune_lod3d(ctx, dims, alpha, tau, Da, coefA, coefB, coefRlap, u0, max_steps, steps, **kw):
+    """fpde_lod3d_autotune: times `steps` steps with each segment count of the Thomas passes and
+    returns (segments, ms per step) of the fastest; Lod3D's keyword arguments describe the run."""
+    opts = dict(left_kind=(0, 0, 0), right_kind=(0, 0, 0), dLN=(0.0, 0.0, 0.0), source=None, bc=None,
+                lag_weights=None, precision=FP64, restrict_eps=0.0, series_terms=0, richards=None, space_frac=None,
+                time_steps=None, weight_rows=None, kernel_power=0.0, segments=(0, 0, 0))
+    opts.update(kw)
+    d, keep, cs = _lod3d_desc(dims, alpha, tau, Da, coefA, coefB, coefRlap, max_steps, opts["left_kind"],
+                              opts["right_kind"], opts["dLN"], opts["source"], opts["bc"], opts["lag_weights"],
+                              opts["precision"], opts["restrict_eps"], opts["series_terms"], opts["richards"],
+                              opts["space_frac"], opts["time_steps"], opts["weight_rows"], opts["kernel_power"],
+                              opts["segments"])
+    u0 = np.ascontiguousarray(u0, dtype=np.float64)
+    seg = (C.c_int * 3)()
+    ms = C.c_double()
+    check(ctx.lib.fpde_lod3d_autotune(ctx.h, C.byref(d), *(_ptr(x) for x in cs), _ptr(u0), int(steps), seg,
+                                      C.byref(ms)), "fpde_lod3d_autotune")
+    return tuple(seg), ms.value

@@ -356,14 +356,27 @@ __global__ void __launch_bounds__(128) k_lod_pass_rich(LodPassArgs p, LodRichArg
 // (segments per line, nodes per segment) by line length: 8 x 16 up to 129 intervals, 16 x 16 up to
 // 257, 16 x 32 up to 513; longer lines run one thread per line. More, shorter segments keep more
 // lines' loads in flight (the pass is bound by memory latency, not bandwidth).
-constexpr int LSEG_MAXSEGS = 16;
-static inline void seg_shape(int Nl, int *segs, int *seglen)
+// A requested count (fpde_lod3d_desc.segments: 4, 8, 16 or 32, at most 32 interior nodes each)
+// replaces the rule; *seglen is then the kernel's segment capacity (4, 8, 16 or 32, the smallest
+// that holds ceil((Nl-1)/segs) nodes).
+static inline void seg_shape(int Nl, int req, int *segs, int *seglen)
 {
     const int interior = Nl - 1;
+    if (req > 0) {
+        const int sl = (interior + req - 1) / req;
+        *segs = req;
+        *seglen = sl <= 4 ? 4 : sl <= 8 ? 8 : sl <= 16 ? 16 : 32;
+        if (sl > 32 || interior < 1) *segs = *seglen = 0;
+        return;
+    }
     if (interior <= 8 * 16) { *segs = 8; *seglen = 16; }
     else if (interior <= 16 * 16) { *segs = 16; *seglen = 16; }
     else if (interior <= 16 * 32) { *segs = 16; *seglen = 32; }
     else { *segs = 0; *seglen = 0; }
+}
+static inline bool seg_request_ok(int Nl, int req)
+{
+    return req == 0 || ((req == 4 || req == 8 || req == 16 || req == 32) && Nl >= 2 && (Nl - 1 + req - 1) / req <= 32);
 }
 constexpr int LSB = 4;                    // nodes of loads issued together (register budget: one wave)
 struct LodSegArgs {
@@ -645,6 +658,7 @@ struct fpde_lod3d {
            *cPF[3] = {nullptr, nullptr, nullptr};
     int seglen[3] = {0, 0, 0};
     int segs[3] = {0, 0, 0};
+    int segcap[3] = {0, 0, 0};                     // the pass kernel's segment capacity (SEGLEN)
     int lines[3] = {0, 0, 0};
     // split path (exact three-slice far history on the tensor cores, FP64 near history)
     bool split = false;
@@ -763,11 +777,26 @@ static int lod_launch_pass(fpde_lod3d *L, cudaStream_t st, int pass, int64_t n, 
     } else if (L->seglen[pass] > 0) {
         LodSegArgs sg;
         sg.KF = L->cKF[pass]; sg.CB = L->cCB[pass]; sg.PF = L->cPF[pass]; sg.seglen = L->seglen[pass];
-        const int SG = L->segs[pass];
+        const int SG = L->segs[pass], SLC = L->segcap[pass];
         const unsigned blocks = (unsigned)(((int64_t)a.lines * SG + 127) / 128);
-        if (SG == 8) k_lod_pass_seg<8, 16><<<blocks, 128, 0, st>>>(a, sg);
-        else if (L->seglen[pass] <= 16) k_lod_pass_seg<16, 16><<<blocks, 128, 0, st>>>(a, sg);
-        else k_lod_pass_seg<16, 32><<<blocks, 128, 0, st>>>(a, sg);
+        switch (SG * 64 + SLC) {
+        case 4 * 64 + 4: k_lod_pass_seg<4, 4><<<blocks, 128, 0, st>>>(a, sg); break;
+        case 4 * 64 + 8: k_lod_pass_seg<4, 8><<<blocks, 128, 0, st>>>(a, sg); break;
+        case 4 * 64 + 16: k_lod_pass_seg<4, 16><<<blocks, 128, 0, st>>>(a, sg); break;
+        case 4 * 64 + 32: k_lod_pass_seg<4, 32><<<blocks, 128, 0, st>>>(a, sg); break;
+        case 8 * 64 + 4: k_lod_pass_seg<8, 4><<<blocks, 128, 0, st>>>(a, sg); break;
+        case 8 * 64 + 8: k_lod_pass_seg<8, 8><<<blocks, 128, 0, st>>>(a, sg); break;
+        case 8 * 64 + 16: k_lod_pass_seg<8, 16><<<blocks, 128, 0, st>>>(a, sg); break;
+        case 8 * 64 + 32: k_lod_pass_seg<8, 32><<<blocks, 128, 0, st>>>(a, sg); break;
+        case 16 * 64 + 4: k_lod_pass_seg<16, 4><<<blocks, 128, 0, st>>>(a, sg); break;
+        case 16 * 64 + 8: k_lod_pass_seg<16, 8><<<blocks, 128, 0, st>>>(a, sg); break;
+        case 16 * 64 + 16: k_lod_pass_seg<16, 16><<<blocks, 128, 0, st>>>(a, sg); break;
+        case 16 * 64 + 32: k_lod_pass_seg<16, 32><<<blocks, 128, 0, st>>>(a, sg); break;
+        case 32 * 64 + 4: k_lod_pass_seg<32, 4><<<blocks, 128, 0, st>>>(a, sg); break;
+        case 32 * 64 + 8: k_lod_pass_seg<32, 8><<<blocks, 128, 0, st>>>(a, sg); break;
+        case 32 * 64 + 16: k_lod_pass_seg<32, 16><<<blocks, 128, 0, st>>>(a, sg); break;
+        default: k_lod_pass_seg<32, 32><<<blocks, 128, 0, st>>>(a, sg); break;
+        }
     } else {
         k_lod_pass<<<(unsigned)((a.lines + 127) / 128), 128, 0, st>>>(a);
     }
@@ -1052,6 +1081,9 @@ int fpde_lod3d_create(fpde_ctx *ctx, const fpde_lod3d_desc *desc, const double *
         FPDE_CHECK_ARG(!d.weight_rows, "weight_rows needs time_steps");
     }
     FPDE_CHECK_ARG(d.sN >= 2 && d.M >= 2 && d.K >= 2, "every axis needs at least 2 intervals");
+    FPDE_CHECK_ARG(seg_request_ok(d.sN, d.segments[0]) && seg_request_ok(d.M, d.segments[1]) &&
+                       seg_request_ok(d.K, d.segments[2]),
+                   "segments: 0, or 4, 8, 16 or 32 with at most 32 interior nodes per segment");
     FPDE_CHECK_ARG(d.lag_weights || (d.alpha > 0.0 && d.alpha < 1.0), "alpha must be in (0, 1)");
     FPDE_CHECK_ARG(std::isfinite(d.restrict_eps) && d.restrict_eps >= 0.0, "restrict_eps must be >= 0");
     FPDE_CHECK_ARG(d.series_terms >= 0 && d.series_terms <= LOD_SERIES_MAX, "series_terms must be 0 .. 128");
@@ -1343,7 +1375,7 @@ int fpde_lod3d_create(fpde_ctx *ctx, const fpde_lod3d_desc *desc, const double *
         }
         // segmented pass data: segment s holds nodes [1 + s seglen, 1 + (s+1) seglen) of 1..Nl-1
         int SG = 0, SL = 0;
-        seg_shape(Nl, &SG, &SL);
+        seg_shape(Nl, d.segments[pass], &SG, &SL);
         const int sl = SG ? (Nl - 1 + SG - 1) / SG : 0;
         if (!fail && Nl >= 2 && SG > 0 && sl <= SL) {
             std::vector<double> hKF(cnt, 0.0), hCB(cnt, 0.0), hPF((size_t)lines * SG, 1.0), cf(SL);
@@ -1379,6 +1411,7 @@ int fpde_lod3d_create(fpde_ctx *ctx, const fpde_lod3d_desc *desc, const double *
             if (!fail) {
                 L->seglen[pass] = sl;
                 L->segs[pass] = SG;
+                L->segcap[pass] = SL;
             }
         }
     }
@@ -1529,6 +1562,56 @@ int fpde_lod3d_sf_iterations(fpde_lod3d *L, int64_t *iters)
     FPDE_CUDA(cudaMemcpyAsync(&v, L->sf_iters, sizeof v, cudaMemcpyDeviceToHost, L->ctx->stream));
     FPDE_CUDA(cudaStreamSynchronize(L->ctx->stream));
     *iters = (int64_t)v;
+    return FPDE_OK;
+}
+
+int fpde_lod3d_autotune(fpde_ctx *ctx, const fpde_lod3d_desc *desc, const double *coefA, const double *coefB,
+                        const double *coefRlap, const double *u0, int steps, int segments[3], double *ms_per_step)
+{
+    clear_error();
+    FPDE_CHECK_ARG(ctx && desc && u0 && segments && ms_per_step, "null argument");
+    FPDE_CHECK_ARG(steps >= 1 && steps <= desc->max_steps, "steps must be 1 .. max_steps");
+    int rc = ctx_enter(ctx);
+    if (rc) return rc;
+    const int lens[3] = {desc->sN, desc->M, desc->K};
+    const int cand[5] = {0, 4, 8, 16, 32};
+    double best = -1.0;
+    int bestseg[3] = {0, 0, 0};
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    FPDE_CUDA(cudaEventCreate(&e0));
+    FPDE_CUDA(cudaEventCreate(&e1));
+    for (int ci = 0; ci < 5 && !rc; ++ci) {
+        fpde_lod3d_desc d = *desc;
+        bool takes = cand[ci] == 0;
+        for (int p = 0; p < 3; ++p) {
+            d.segments[p] = (cand[ci] > 0 && seg_request_ok(lens[p], cand[ci])) ? cand[ci] : 0;
+            takes = takes || d.segments[p] != 0;
+        }
+        if (!takes) continue;
+        fpde_lod3d *L = nullptr;
+        if ((rc = fpde_lod3d_create(ctx, &d, coefA, coefB, coefRlap, u0, &L))) break;
+        float ms = 0.f;
+        rc = fpde_lod3d_run(L, steps);                       // warm-up (and the graph's capture)
+        if (!rc) rc = fpde_lod3d_reset(L, u0, 0);
+        if (!rc) {
+            cudaEventRecord(e0, ctx->stream);
+            rc = fpde_lod3d_run(L, steps);
+            cudaEventRecord(e1, ctx->stream);
+        }
+        if (!rc && cudaEventSynchronize(e1) == cudaSuccess && cudaEventElapsedTime(&ms, e0, e1) == cudaSuccess) {
+            if (best < 0.0 || ms < best) {
+                best = ms;
+                for (int p = 0; p < 3; ++p) bestseg[p] = d.segments[p];
+            }
+        }
+        fpde_lod3d_destroy(L);
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc) return rc;
+    if (best < 0.0) return set_error(FPDE_ERR_CUDA, "lod3d autotune: no candidate could be timed");
+    for (int p = 0; p < 3; ++p) segments[p] = bestseg[p];
+    *ms_per_step = best / steps;
     return FPDE_OK;
 }
 

@@ -554,6 +554,9 @@ typedef struct fpde_lod3d_desc {
     const fpde_space_frac *space_frac; /* optional: implicit space-fractional line solves (impl 2);
                                coefA/B/Rlap are then the reference's A_/B/R with its space-fractional
                                local weights, every pass has a Dirichlet start, right_kind per pass */
+    int segments[3];            /* per pass: threads (segments) per line of the Thomas passes, 4, 8, 16
+                                   or 32 with at most 32 interior nodes each; 0 = the built-in rule
+                                   (fpde_lod3d_autotune times the choices) */
 } fpde_lod3d_desc;
 
 /* coefA/B/Rlap: three host grids each (pass 0 = sN, 1 = _M, 2 = K) of the line coefficients at
@@ -575,6 +578,12 @@ int fpde_lod3d_steps_done(const fpde_lod3d *lod, int64_t *n);
 int fpde_lod3d_get_concentration(fpde_lod3d *lod, double *c, int on_device);
 /* With space_frac: the solver iterations of every line solve since creation (0 otherwise). */
 int fpde_lod3d_sf_iterations(fpde_lod3d *lod, int64_t *iters);
+/* Times `steps` steps of the LOD desc describes (arguments as fpde_lod3d_create) with each
+ * segment count of the Thomas passes (the same count in every pass whose lines it fits: 4, 8, 16,
+ * 32, and the built-in rule) and returns the fastest in segments[3] (0 where the built-in rule won
+ * or a pass has no segmented form) with its milliseconds per step in *ms_per_step. */
+int fpde_lod3d_autotune(fpde_ctx *ctx, const fpde_lod3d_desc *desc, const double *coefA, const double *coefB,
+                        const double *coefRlap, const double *u0, int steps, int segments[3], double *ms_per_step);
 
 /* --------------------------------------------------------------- ensembles */
 

@@ -230,3 +230,48 @@ def test_lod_series_runs_in_pieces(ctx):
         lod.run(m)
     np.testing.assert_array_equal(lod.state(), u_one)
     lod.close()
+
+
+@pytest.mark.parametrize("segments", [(4, 4, 4), (8, 8, 8), (16, 16, 16), (32, 32, 32), (4, 16, 32)])
+def test_lod_segment_counts_vs_oracle(ctx, segments):
+    """Every segment count of the Thomas passes (fpde_lod3d_desc.segments) gives the oracle's run
+    (the segments join by exact affine scans; only the rounding order differs)."""
+    import fpde_hpc_gb300 as fp
+    from fpde_hpc_gb300 import problems
+    dims, steps = (24, 12, 18), 33
+    base = problems.config4(n=max(dims), steps=steps)
+    sN, M, K = dims
+    p = problems.LodProblem("lod", dims, base.alpha, base.tau, steps, base.k[:K + 2, :M + 2, :sN + 2].copy(),
+                            base.u0[:K + 2, :M + 2, :sN + 2].copy(), base.left_kind, base.right_kind)
+    p.u0[K:] = 0.0
+    cA, cB, cR = p.coefs()
+    lod = fp.Lod3D(ctx, dims, p.alpha, p.tau, p.Da, cA, cB, cR, p.u0, steps, left_kind=p.left_kind,
+                   right_kind=p.right_kind, dLN=p.dLN, segments=segments)
+    lod.run(steps)
+    u = lod.state()
+    lod.close()
+    uref, env = _envelope(p, cA, cB, cR)
+    err = relmax(u, uref)
+    print(f"LOD {dims} segments {segments}: {err:.2e} (one-ulp envelope {env:.2e})")
+    assert err <= max(1e-12, 4 * env)
+
+
+def test_lod_autotune_and_bad_segments(ctx):
+    import fpde_hpc_gb300 as fp
+    from fpde_hpc_gb300 import problems
+    p = problems.config4(n=40, steps=40)
+    cA, cB, cR = p.coefs()
+    seg, ms = fp.autotune_lod3d(ctx, p.dims, p.alpha, p.tau, p.Da, cA, cB, cR, p.u0, 40, 40, left_kind=p.left_kind,
+                                right_kind=p.right_kind, dLN=p.dLN, precision=fp.FPDE_PREC_SPLIT_BF16X3)
+    print(f"LOD 40^3 autotune: segments {seg}, {ms:.4f} ms per step")
+    assert all(s in (0, 4, 8, 16, 32) for s in seg) and ms > 0
+    for bad in ((3, 0, 0), (0, 0, 64), (1, 1, 1)):
+        with pytest.raises(fp.FpdeError) as e:
+            fp.Lod3D(ctx, p.dims, p.alpha, p.tau, p.Da, cA, cB, cR, p.u0, 8, left_kind=p.left_kind,
+                     right_kind=p.right_kind, dLN=p.dLN, segments=bad)
+        assert e.value.code == 1
+    shape = (6, 6, 202)                               # 4 segments of more than 32 nodes: 200 intervals
+    z = np.zeros((3,) + shape)
+    with pytest.raises(fp.FpdeError) as e:
+        fp.Lod3D(ctx, (200, 4, 4), p.alpha, p.tau, p.Da, z, z, z, np.zeros(shape), 2, segments=(4, 0, 0))
+    assert e.value.code == 1
