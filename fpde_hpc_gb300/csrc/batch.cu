@@ -35,8 +35,11 @@
 
 namespace fpde {
 
-constexpr int BT = 512;       // threads per column CTA (halves the sequential segment of the longest columns,
-                              // which set the step time of a skewed ensemble)
+#ifndef FPDE_BATCH_THREADS
+#define FPDE_BATCH_THREADS 512
+#endif
+constexpr int BT = FPDE_BATCH_THREADS;   // threads per column CTA (halves the sequential segment of the longest
+                                         // columns, which set the step time of a skewed ensemble)
 constexpr int BW = BT / 32;
 
 struct ColInfo {
