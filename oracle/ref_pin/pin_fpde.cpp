@@ -384,6 +384,76 @@ static void run_kat(const char *path, int kc, double alpha, double tau, int step
     printf("wrote %s (column K %d, %d steps, analytic squared error %.6g)\n", path, kc, steps, err);
 }
 
+/* The reference's 3D known answer of gpu_test.sh's error_tests (mode 3, NB M K 2 with BS 10: 20 x 20 x
+ * 20 cells, aa 0.8, bb 1.0, analytic problem 2, Dirichlet ends, FK 3 with FP 0.8: the generalized
+ * kernel g(t) = t^0.8, EPS2 1e-7 with the default EPS 1e-5, Tau 0.0025, Tm 0.1: 40 steps, impl 0,
+ * sum_alg 0): its run prints the squared error 0.157085 against the exact solution. Records as
+ * run_kat, plus the weight rows of every step (its series weights at EPS 1e-5: only its own rows
+ * reproduce the run). */
+static void run_kat3d(const char *path, int bs, int nb, double alpha, double tau, int steps)
+{
+    set_dims(bs, nb, nb, nb);
+    varT = 0; varZ = 0; varXY = 0;
+    implicit = 0; implicit3d = 0; rp_split_3d = 0; sum_alg = 0;
+    func_in_kernel = 3; func_power = 0.8;
+    global_eps = 1e-5; global_eps2 = 1e-7;
+    FILE *lg = fopen("/dev/null", "w");
+    H_solver *s = new H_solver(2, 1, 5, 0, 1, alpha, 1.0, 0, 0, 0, 3, lg, 2);
+    size_t G = (size_t)(sN + 2) * (_M + 2) * (K + 2);
+    FgvWriter w(path);
+    w.scalar("sN", sN); w.scalar("M", _M); w.scalar("K", K);
+    w.scalar("alpha", alpha); w.scalar("Da", s->Da); w.scalar("tau", tau); w.scalar("func_power", func_power);
+    std::vector<uint64_t> gdims = {(uint64_t)(K + 2), (uint64_t)(_M + 2), (uint64_t)(sN + 2)};
+    w.put("U0", gdims, s->b_U);
+    std::vector<double> p2, vt, kkk0, tauv, kb_all, kb_off, rp0, bc0g, S1(G, 0.0);
+    for (int n = 0; n < steps; n++) {
+        s->calc_step(tau);
+        kb_off.push_back((double)kb_all.size());
+        kb_all.insert(kb_all.end(), s->kb_3_cache.begin(), s->kb_3_cache.end());
+        kkk0.push_back(s->kkk0);
+        tauv.push_back(s->tau[s->tstep]);
+        if (n == 0) {
+            record_coefs(s, w);
+            std::vector<double> bcv;
+            record_step_inputs(s, rp0, bcv);
+            bc0g = bcv;
+            const double t_saved = s->Time[s->tstep];             /* S1: the source at Time 0 */
+            s->Time[s->tstep] = 0.0;
+            PassState st = save_state(s);
+            for (int i = 1; i < sN; i++) for (int j = 1; j < _M; j++) {
+                enter_line(s, 2, i, j);
+                for (int k = 1; k < K; k++) S1[gidx(i, j, k)] = s->Rp(k);
+            }
+            restore_state(s, st);
+            s->Time[s->tstep] = t_saved;
+        }
+        PassState st = save_state(s);
+        enter_line(s, 2, 1, 1);
+        p2.push_back(S1[gidx(1, 1, 1)] - s->Rp(1));
+        enter_line(s, 0, 1, 1);
+        vt.push_back(s->bc0());
+        restore_state(s, st);
+    }
+    kb_off.push_back((double)kb_all.size());
+    std::vector<double> exact(G, 0.0);
+    for (int i = 1; i < sN; i++) for (int j = 1; j < _M; j++) for (int k = 1; k < K; k++)
+        exact[gidx(i, j, k)] = s->testF3d(i, j, k, s->tstep + 1);
+    const double err = s->analytic_compare(NULL);
+    w.put("S1", gdims, S1.data());
+    w.put("BC0", gdims, bc0g.data());
+    w.put("p2", p2); w.put("vt", vt); w.put("kkk0", kkk0); w.put("tau_steps", tauv);
+    w.put("kb_flat", kb_all); w.put("kb_off", kb_off);
+    w.put("U_final", gdims, s->b_U);
+    w.put("exact_final", gdims, exact.data());
+    w.scalar("analytic_sq_err", err);
+    delete s;
+    fclose(lg);
+    func_in_kernel = 0; func_power = 0.6;
+    global_eps = 1e-15; global_eps2 = 1e-15;
+    printf("wrote %s (%d x %d x %d, FK 3 FP 0.8, %d steps, analytic squared error %.6g)\n", path, sN, _M, K, steps,
+           err);
+}
+
 /* The Richards problem coupled with salt concentration C (analytic_test 0 with is_c = 1: nu
  * nonzero, :3515): on every line of every pass calc_step solves H (U1(0)) and then C (U1(1))
  * (:5270-5278), each with its own L1 history (oldC, time_summing :4086-4164). (With is_t = 1 the
@@ -741,6 +811,8 @@ int main(int argc, char **argv)
         char q[4096];
         snprintf(q, sizeof q, "%s/fpde_column_kat.fgv", argv[2]);
         run_kat(q, 1000, 0.8, 1e-3, 1000);
+        snprintf(q, sizeof q, "%s/fpde_lod3d_kat.fgv", argv[2]);
+        run_kat3d(q, 10, 2, 0.8, 0.0025, 40);
         return 0;
     }
     if (argc >= 3 && strcmp(argv[1], "lod_vartau") == 0) {

@@ -8,7 +8,8 @@ themselves are committed so tests never need it.
 
     python tests/golden/make_golden.py [REF_DIR] [--only gamma|richards|richards_ct|spacefrac|spacefrac3d|lod_vartau|kat]
 
-The richards, richards_ct, spacefrac, spacefrac3d, lod_vartau and kat scenarios run only with --only
+The richards, richards_ct, spacefrac, spacefrac3d, lod_vartau and kat (the column and the 3D known answers)
+scenarios run only with --only
 (each sets its own solver mode).
 
 The 40-digit weights fixture (fpde_weights_g_exact.fgv.gz) is computed from the time grids of

@@ -1,4 +1,4 @@
-"""The reference's known answer for its column (fixture fpde_column_kat: mode 3, BS 1, NB 3, M 3,
+"""The reference's known answers. Its column (fixture fpde_column_kat: mode 3, BS 1, NB 3, M 3,
 K 1000, analytic problem 2, alpha 0.8, tau 1e-3, 1,000 steps): its run prints the squared error
 0.014446 against the exact solution (analytic_compare). The fixture keeps the inputs in separated
 form (source S1 - p2(t), line ends V + vt(t)); this module rebuilds the per-step grids."""
@@ -8,8 +8,11 @@ import fgv
 from conftest import golden_path
 
 
-def load():
-    g = fgv.load(golden_path("fpde_column_kat"))
+def load(name="fpde_column_kat"):
+    """The column KAT (fpde_column_kat) or the 3D one (fpde_lod3d_kat: gpu_test.sh's error_tests at
+    20 x 20 x 20, g(t) = t^0.8, 40 steps; its run prints 0.0472441, and it carries the reference's
+    weight rows of every step in `rows`)."""
+    g = fgv.load(golden_path(name))
     dims = (int(g["sN"]), int(g["M"]), int(g["K"]))
     sN, M, K = dims
     steps = g["p2"].size
@@ -25,7 +28,15 @@ def load():
     src = np.where(interior[None], g["S1"][None] - g["p2"][:, None, None, None], 0.0)
     bc = np.where(mask[None], V[None] + g["vt"][:, None, None, None], 0.0)
     coefs = [np.stack([g[f"{k}_pass{p}"] for p in range(3)]) for k in ("coefA", "coefB", "coefRlap")]
-    return dict(g=g, dims=dims, steps=steps, src=src, bc=bc, coefs=coefs, interior=interior)
+    c = dict(g=g, dims=dims, steps=steps, src=src, bc=bc, coefs=coefs, interior=interior)
+    if "kb_off" in g:                       # the reference's own weight rows (row n: kb_3_cache, kkk0)
+        kbo = g["kb_off"].astype(np.int64)
+        rows = np.zeros((steps, steps + 1))
+        for n in range(steps):
+            rows[n, :n] = g["kb_flat"][kbo[n]:kbo[n + 1]]
+            rows[n, n] = g["kkk0"][n]
+        c["rows"] = rows
+    return c
 
 
 def analytic_sq_err(U, c):

@@ -59,3 +59,22 @@ def test_known_answer_split(ctx, case):
     print(f"split x3: vs FP64 {relmax(U3, U64):.2e}, analytic squared error {err:.8g}")
     assert relmax(U3, U64) <= 1e-7
     assert abs(err - float(g["analytic_sq_err"])) <= 1e-6 * float(g["analytic_sq_err"])
+
+
+def test_reference_known_answer_3d_generalized_kernel(ctx):
+    """gpu_test.sh's error_tests at 20 x 20 x 20 with g(t) = t^0.8 (the reference prints 0.0472441):
+    the 3D LOD's variable-step time loop with the reference's weight rows reproduces its final grid
+    to 1e-12 and that error."""
+    import fpde_hpc_gb300 as fp
+    c = kat_case.load("fpde_lod3d_kat")
+    g = c["g"]
+    lod = fp.Lod3D(ctx, c["dims"], float(g["alpha"]), float(g["tau"]), float(g["Da"]), *c["coefs"], g["U0"],
+                   c["steps"], source=c["src"], bc=c["bc"], time_steps=g["tau_steps"], weight_rows=c["rows"])
+    lod.run(c["steps"])
+    U = lod.state()
+    lod.close()
+    assert relmax(U, g["U_final"]) <= 1e-12
+    err = kat_case.analytic_sq_err(U, c)
+    print(f"3D known answer: squared error {err:.6g} (reference {float(g['analytic_sq_err']):.6g})")
+    assert abs(err - float(g["analytic_sq_err"])) <= 1e-8 * float(g["analytic_sq_err"])
+    assert f"{err:.6g}" == "0.0472441"

@@ -440,3 +440,23 @@ def test_reference_known_answer_column_k1000():
     err = kat_case.analytic_sq_err(U, c)
     assert abs(err - float(g["analytic_sq_err"])) <= 1e-8 * float(g["analytic_sq_err"])   # printed: 6 digits
     assert abs(float(g["analytic_sq_err"]) - 0.014446) < 5e-7        # the value the reference prints
+
+
+def test_reference_known_answer_3d_generalized_kernel():
+    """gpu_test.sh's error_tests run at 20 x 20 x 20 (analytic problem 2, alpha 0.8, g(t) = t^0.8, 40
+    steps): the reference prints the squared error 0.0472441. The oracle, from the rebuilt inputs and
+    the reference's own weight rows (its series at EPS 1e-5), reproduces the final grid and that error."""
+    import kat_case
+    c = kat_case.load("fpde_lod3d_kat")
+    g = c["g"]
+    U = g["U0"].copy()
+    taus = g["tau_steps"]
+    hist = np.zeros((c["steps"],) + U.shape)
+    for n in range(c["steps"]):
+        kb = c["rows"][n, :n]
+        oracle.lod_step_dirichlet(c["dims"], U, hist, n, kb if n else np.zeros(1), taus, float(g["Da"]),
+                                  float(c["rows"][n, n]), *c["coefs"], c["src"][n], c["bc"][n])
+    assert _relmax(U, g["U_final"]) <= 1e-12
+    err = kat_case.analytic_sq_err(U, c)
+    assert abs(err - float(g["analytic_sq_err"])) <= 1e-8 * float(g["analytic_sq_err"])
+    assert f"{err:.6g}" == "0.0472441"
