@@ -13,6 +13,7 @@
 #include "fr_do.cpp"
 #undef main
 #include "fgv_write.h"
+#include <cstring>
 
 static void pin_derivative(const char *path, int n, int an)
 {
@@ -28,7 +29,12 @@ static void pin_derivative(const char *path, int n, int an)
     for (int i = 0; i < an; i++) gs[i] = Gamma(2.0 - (i / (T)(an - 1)));
     w.put("gs", gs);
     double err = 0.0;                           /* DOerr, as in main (:919-925) */
-    for (int i = 1; i < n; i++) err += (analytic(i * tau) - DF[i]) * (analytic(i * tau) - DF[i]);
+    std::vector<double> exact(n, 0.0);
+    for (int i = 1; i < n; i++) {
+        exact[i] = analytic(i * tau);
+        err += (analytic(i * tau) - DF[i]) * (analytic(i * tau) - DF[i]);
+    }
+    w.put("analytic", exact);
     w.scalar("DOerr", sqrt(err / n));
     printf("wrote %s DOerr %g\n", path, sqrt(err / n));
 }
@@ -61,6 +67,19 @@ static void pin_equation(const char *path, int ex, int nx, int na, int tb, int e
 
 int main(int argc, char **argv)
 {
+    if (argc >= 3 && strcmp(argv[1], "kat") == 0) {
+        /* fr_do's own runs at its defaults (main :868-928, eq_Nx 101, eq_Na 64, eq_tblock 16,
+         * eq_eNt 160, ex1 power 2 :435-446, :643-646): the derivative test prints DOerr, eq_solve
+         * its final err for eq_ex 0 and 1 */
+        char q[4096];
+        snprintf(q, sizeof q, "%s/frdo_derivative_kat.fgv", argv[2]);
+        pin_derivative(q, 1000, 32);
+        snprintf(q, sizeof q, "%s/frdo_eq_ex0_kat.fgv", argv[2]);
+        pin_equation(q, 0, 101, 64, 16, 160, 2.0);
+        snprintf(q, sizeof q, "%s/frdo_eq_ex1_kat.fgv", argv[2]);
+        pin_equation(q, 1, 101, 64, 16, 160, 2.0);
+        return 0;
+    }
     const char *dir = argc >= 2 ? argv[1] : ".";
     char p[4096];
     snprintf(p, sizeof p, "%s/frdo_derivative.fgv", dir);

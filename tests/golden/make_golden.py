@@ -6,10 +6,10 @@ gzips their output here. Needs the reference checkout: REF_DIR on the command li
 $FPDE_REFERENCE_DIR, else a directory named "reference" beside the repository; the fixtures
 themselves are committed so tests never need it.
 
-    python tests/golden/make_golden.py [REF_DIR] [--only gamma|richards|richards_ct|spacefrac|spacefrac3d|lod_vartau|kat]
+    python tests/golden/make_golden.py [REF_DIR] [--only gamma|richards|richards_ct|spacefrac|spacefrac3d|lod_vartau|kat|frdo_kat]
 
 The richards, richards_ct, spacefrac, spacefrac3d, lod_vartau and kat (the column and the 3D known answers)
-scenarios run only with --only
+scenarios, and frdo_kat (fr_do's runs at its defaults), run only with --only
 (each sets its own solver mode).
 
 The 40-digit weights fixture (fpde_weights_g_exact.fgv.gz) is computed from the time grids of
@@ -40,7 +40,9 @@ def main():
                            f"REF_DIR={ref_dir}"])
     tmp = tempfile.mkdtemp(prefix="fpde_golden_")
     try:
-        if only:                 # one scenario of the fpde harness (e.g. gamma)
+        if only == "frdo_kat":   # fr_do's default runs (pin_frdo kat)
+            subprocess.check_call([os.path.join(ROOT, "oracle", "_ref", "pin_frdo"), "kat", tmp], cwd=tmp)
+        elif only:               # one scenario of the fpde harness (e.g. gamma)
             subprocess.check_call([os.path.join(ROOT, "oracle", "_ref", "pin_fpde"), only, tmp], cwd=tmp)
         for exe in (() if only else ("pin_fpde", "pin_frdo")):
             # fr_do's eq_ex 1 caches series values in ./s_n_t.txt: run inside tmp.

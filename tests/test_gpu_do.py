@@ -37,7 +37,7 @@ def _do_weights(aq, qw, gq, tau, n):
     return fp.do_weights(aq, qw, tau, n, gq)
 
 
-@pytest.mark.parametrize("name", ["frdo_eq_ex0", "frdo_eq_ex1"])
+@pytest.mark.parametrize("name", ["frdo_eq_ex0", "frdo_eq_ex1", "frdo_eq_ex0_kat"])
 def test_do_equation_every_level_matches_fr_do(ctx, name):
     import fpde_hpc_gb300 as fp
     g = fgv.load(golden_path(name))
@@ -146,8 +146,9 @@ def _derivative(ctx, F, tau, c, t0=1, j0=0, maxt=-1, DF0=None, append=0):
     return DF.cpu().numpy()
 
 
-def test_do_derivative_matches_reference_and_oracle(ctx):
-    g = fgv.load(golden_path("frdo_derivative"))
+@pytest.mark.parametrize("name", ["frdo_derivative", "frdo_derivative_kat"])
+def test_do_derivative_matches_reference_and_oracle(ctx, name):
+    g = fgv.load(golden_path(name))
     n, tau = int(g["N"]), g["tau"]
     Na = len(g["WA"])
     F = (np.arange(n) * tau) ** 2
@@ -156,6 +157,9 @@ def test_do_derivative_matches_reference_and_oracle(ctx):
     assert relmax(DF[1:], g["DF_do"][1:]) <= 1e-12
     DFo = oracle.do_derivative(F, tau, g["WA"], g["gs"])
     assert relmax(DF[1:], DFo[1:]) <= 1e-12
+    if "analytic" in g:                        # fr_do's default run prints DOerr 0.000375753
+        err = float(np.sqrt(np.sum((g["analytic"][1:] - DF[1:]) ** 2) / n))
+        assert f"{err:.6g}" == "0.000375753"
 
 
 @pytest.mark.parametrize("t0,j0,maxt", [(1, 0, -1), (32, 0, 31), (40, 31, 39), (8, -1, 7)])

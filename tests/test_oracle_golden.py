@@ -102,19 +102,25 @@ def test_l1_sum_snapshot_form_equals_increment_form():
     assert _relmax(S1[grid.reshape(-1)], Sref[grid.reshape(-1)]) <= RTOL
 
 
-def test_do_derivative_matches_fr_do():
-    g = fgv.load(golden_path("frdo_derivative"))
+@pytest.mark.parametrize("name", ["frdo_derivative", "frdo_derivative_kat"])
+def test_do_derivative_matches_fr_do(name):
+    """fr_do's DO derivative of t^2 (DO_Cder); frdo_derivative_kat is its main's default run (N 1000,
+    aN 32), which prints DOerr 0.000375753: the oracle's derivative gives the same error."""
+    g = fgv.load(golden_path(name))
     n, tau = int(g["N"]), g["tau"]
     x = np.arange(n) * tau
     F = x * x
     DF = oracle.do_derivative(F, tau, g["WA"], g["gs"])
     assert _relmax(DF[1:], g["DF_do"][1:]) <= RTOL
+    if "analytic" in g:
+        err = float(np.sqrt(np.sum((g["analytic"][1:] - DF[1:]) ** 2) / n))
+        assert f"{err:.6g}" == f"{float(g['DOerr']):.6g}" == "0.000375753"
     from math import gamma
     DC = oracle.caputo_derivative(F, tau, 0.5, gamma(1.5))
     assert _relmax(DC[1:], g["DF_caputo05"][1:]) <= RTOL
 
 
-@pytest.mark.parametrize("name", ["frdo_eq_ex0", "frdo_eq_ex1"])
+@pytest.mark.parametrize("name", ["frdo_eq_ex0", "frdo_eq_ex1", "frdo_eq_ex0_kat"])
 def test_do_equation_matches_fr_do(name):
     g = fgv.load(golden_path(name))
     ex, Nx, Nt = int(g["ex"]), int(g["Nx"]), int(g["Nt"])
@@ -129,9 +135,11 @@ def test_do_equation_matches_fr_do(name):
     assert _relmax(Cm, g["C"]) <= RTOL, _relmax(Cm, g["C"])
     err = np.sqrt(np.mean((Cm[:, -1] - g["analytic_last"]) ** 2))
     assert abs(err - g["err"]) <= 1e-9 * max(g["err"], 1e-300) + 1e-15
+    if name.endswith("_kat"):                  # fr_do -1 (its defaults) prints err 0.0117073
+        assert f"{err:.6g}" == "0.0117073"
 
 
-@pytest.mark.parametrize("name", ["frdo_eq_ex0", "frdo_eq_ex1"])
+@pytest.mark.parametrize("name", ["frdo_eq_ex0", "frdo_eq_ex1", "frdo_eq_ex0_kat"])
 def test_do_equation_as_general_line_run(name):
     """fr_do's eq_solve, restated as a line run with fused DO lag weights, theta = 1 and a
     per-step source (the form the GPU line path runs), meets the reference's own output."""
