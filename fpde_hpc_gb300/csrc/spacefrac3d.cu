@@ -50,7 +50,8 @@ template <bool F> __device__ __forceinline__ double msub(double c, double a, dou
 }
 
 #ifndef SF3_MIN_CTAS
-#define SF3_MIN_CTAS 2        // co-resident CTAs per SM the solve's register budget is cut for
+#define SF3_MIN_CTAS 2        // co-resident CTAs per SM the solve's register budget is cut for (2 measured
+                              // fastest on 64^3: 3 and 4 per SM, with spills, were 16 % and 19 % slower)
 #endif
 constexpr int SF3_THREADS = 256;
 constexpr int SF3_WARPS = SF3_THREADS / 32;
