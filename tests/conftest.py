@@ -1,6 +1,8 @@
 import os
 import sys
 
+import numpy as np
+
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 for p in (ROOT, os.path.join(ROOT, "oracle"), os.path.join(ROOT, "tests", "golden")):
     if p not in sys.path:
@@ -15,3 +17,12 @@ def pytest_configure(config):
 
 def golden_path(name):
     return os.path.join(GOLDEN, name + ".fgv.gz")
+
+
+def relmax(a, b):
+    """max |a - b| / max |b|; inf when either side holds a NaN or an infinity, so that a test bar
+    fails instead of passing on a comparison with NaN."""
+    a, b = np.asarray(a, dtype=np.float64), np.asarray(b, dtype=np.float64)
+    if not (np.all(np.isfinite(a)) and np.all(np.isfinite(b))):
+        return float("inf")
+    return float(np.max(np.abs(a - b)) / max(float(np.max(np.abs(b))), 1e-300))

@@ -80,7 +80,7 @@ def test_reference_call_sequence_reproduces_reference_sums(programs):
     worst = 0.0
     for n in range(1, steps):
         ref = g["S"][n].reshape(-1)[mask]
-        worst = max(worst, float(np.max(np.abs(S[n - 1][mask] - ref)) / np.max(np.abs(ref))))
+        worst = float(np.maximum(worst, float(np.max(np.abs(S[n - 1][mask] - ref)) / np.max(np.abs(ref)))))
     print(f"C++ drop-in Sums over {steps - 1} steps vs the reference's: max rel err {worst:.2e}")
     assert worst <= 1e-12
 

@@ -4,12 +4,9 @@ rounding that a different order of the scans' operations gives: 1e-12, or 4x the
 one-ulp envelope on a long line)."""
 import numpy as np
 import pytest
+from conftest import relmax
 
 pytestmark = pytest.mark.gpu
-
-
-def relmax(a, b):
-    return float(np.max(np.abs(a - b)) / np.max(np.abs(b)))
 
 
 @pytest.fixture(scope="module")

@@ -16,12 +16,9 @@ import do_cases
 import fgv
 import oracle
 from conftest import golden_path
+from conftest import relmax
 
 pytestmark = pytest.mark.gpu
-
-
-def relmax(a, b):
-    return float(np.max(np.abs(a - b)) / np.max(np.abs(b)))
 
 
 @pytest.fixture(scope="module")
@@ -99,7 +96,6 @@ def test_do_line_split_x3_vs_oracle(ctx):
     err = relmax(u, uref)
     print(f"DO line N=4096 700 steps bf16x3 split vs oracle: {err:.2e}")
     assert err <= 1e-7
-
 
 
 @pytest.mark.parametrize("sp,chunks,theta,right", [

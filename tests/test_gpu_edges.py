@@ -5,12 +5,9 @@ import numpy as np
 import pytest
 
 import oracle
+from conftest import relmax
 
 pytestmark = pytest.mark.gpu
-
-
-def relmax(a, b):
-    return float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
 
 
 @pytest.fixture(scope="module")

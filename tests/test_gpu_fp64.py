@@ -9,14 +9,10 @@ import pytest
 import fgv
 import oracle
 from conftest import golden_path
+from conftest import relmax
 
 pytestmark = pytest.mark.gpu
 RTOL = 1e-12
-
-
-def relmax(a, b):
-    a, b = np.asarray(a), np.asarray(b)
-    return float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
 
 
 @pytest.fixture(scope="module")

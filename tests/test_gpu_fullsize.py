@@ -18,13 +18,10 @@ import numpy as np
 import pytest
 
 import oracle
+from conftest import relmax
 
 pytestmark = pytest.mark.gpu
 RTOL, SPLIT_TOL = 1e-12, 1e-7
-
-
-def relmax(a, b):
-    return float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
 
 
 def relrms(a, b):

@@ -9,12 +9,9 @@ import numpy as np
 import pytest
 
 import kat_case
+from conftest import relmax
 
 pytestmark = pytest.mark.gpu
-
-
-def relmax(a, b):
-    return float(np.max(np.abs(a - b)) / np.max(np.abs(b)))
 
 
 @pytest.fixture(scope="module")

@@ -11,12 +11,9 @@ import numpy as np
 import pytest
 
 import oracle
+from conftest import relmax
 
 pytestmark = pytest.mark.gpu
-
-
-def relmax(a, b):
-    return float(np.max(np.abs(a - b)) / np.max(np.abs(b)))
 
 
 @pytest.fixture(scope="module")

@@ -14,12 +14,9 @@ import pytest
 
 import fgv
 from conftest import golden_path
+from conftest import relmax
 
 pytestmark = pytest.mark.gpu
-
-
-def relmax(a, b):
-    return float(np.max(np.abs(a - b)) / np.max(np.abs(b)))
 
 
 @pytest.fixture(scope="module")

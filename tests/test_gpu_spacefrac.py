@@ -12,6 +12,7 @@ import pytest
 
 import oracle
 import sf_cases
+from conftest import relmax
 
 pytestmark = pytest.mark.gpu
 
@@ -135,7 +136,7 @@ def _oracle_envelope(c, rel):
         oracle.lod_step_sf(c["dims"], U, hist, n, c["kb_rows"][n], g["tau"], c["Da"], float(g["kkk0"][n]),
                            c["coefA"], c["coefB"], c["coefRlap"], c["mc"], c["iw"], c["Tm"], c["space_der"], c["thr"],
                            c["maxiter"], g["Rp"][n] * (1.0 + rel), g["BC"][n], rkind=c["rkind"], dLN=c["dLN"])
-        worst = max(worst, float(np.abs(U - g["U"][n]).max() / np.abs(g["U"][n]).max()))
+        worst = max(worst, relmax(U, g["U"][n]))
     return worst
 
 
@@ -156,7 +157,7 @@ def test_lod_replay_vs_reference(ctx, name, exact):
     for n in range(c["steps"]):
         lod.run(1)
         U = lod.state()
-        worst = max(worst, float(np.abs(U - g["U"][n]).max() / np.abs(g["U"][n]).max()))
+        worst = max(worst, relmax(U, g["U"][n]))
     assert lod.sf_iterations() > 0
     lod.close()
     assert worst <= max(10.0 * env, 1e-12), (worst, env)
@@ -214,13 +215,13 @@ def test_lod_larger_grid_vs_oracle(ctx, sd, exact):
         return out
 
     ref = oracle_run(1.0)
-    env = max(max(float(np.abs(a - b).max() / np.abs(b).max()) for a, b in zip(oracle_run(1.0 + e), ref))
+    env = max(max(relmax(a, b) for a, b in zip(oracle_run(1.0 + e), ref))
               for e in (1e-15, -1e-15))
     worst = 0.0
     for n in range(steps):
         lod.run(1)
         G = lod.state()
-        worst = max(worst, float(np.abs(G - ref[n]).max() / np.abs(ref[n]).max()))
+        worst = max(worst, relmax(G, ref[n]))
     lod.close()
     assert worst <= max(10.0 * env, 1e-12), (worst, env)
 

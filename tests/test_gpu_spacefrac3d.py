@@ -13,6 +13,7 @@ import pytest
 
 import oracle
 import sf3d_cases
+from conftest import relmax
 
 pytestmark = pytest.mark.gpu
 
@@ -23,10 +24,6 @@ def ctx():
     c = fp.Context(0)
     yield c
     c.close()
-
-
-def relmax(a, b):
-    return float(np.abs(np.asarray(a) - np.asarray(b)).max() / np.abs(np.asarray(b)).max())
 
 
 @pytest.mark.parametrize("name", sf3d_cases.NAMES)

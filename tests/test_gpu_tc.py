@@ -11,6 +11,7 @@ import ctypes as C
 
 import numpy as np
 import pytest
+from conftest import relmax
 
 pytestmark = pytest.mark.gpu
 
@@ -22,10 +23,6 @@ def split16(x, fmt):
     hi = t.to(dt)
     lo = (torch.from_numpy(x) - hi.double()).float().to(dt)
     return hi, lo
-
-
-def relmax(a, b):
-    return float(np.max(np.abs(a - b)) / np.max(np.abs(b)))
 
 
 @pytest.mark.parametrize("fmt", ["f16", "bf16"])

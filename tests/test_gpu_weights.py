@@ -55,7 +55,7 @@ def test_weights_g_vs_oracle(ctx, p, alpha):
         if alpha == 1.0:
             np.testing.assert_array_equal(got, ref)
             continue
-        worst = max(worst, float(np.max(np.abs(got - ref) / np.abs(ref))))
+        worst = float(np.maximum(worst, float(np.max(np.abs(got - ref) / np.abs(ref)))))
     assert worst <= 1e-14, worst
     assert np.all(W[0, n0 + 1:] == 0.0)                  # entries past t = n untouched
 

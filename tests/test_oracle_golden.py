@@ -12,14 +12,9 @@ import pytest
 import fgv
 import oracle
 from conftest import golden_path
+from conftest import relmax as _relmax
 
 RTOL = 1e-12
-
-
-def _relmax(a, b):
-    a, b = np.asarray(a), np.asarray(b)
-    scale = max(np.max(np.abs(b)), 1e-300)
-    return float(np.max(np.abs(a - b)) / scale)
 
 
 def _weights_of(g, n):
@@ -40,8 +35,8 @@ def test_l1_weights_closed_form_matches_reference_series(name):
         assert len(kb_ref) == n
         kb, k0 = oracle.l1_weights(alpha, time, n)
         if n:
-            worst = max(worst, float(np.max(np.abs(kb - kb_ref) / np.abs(kb_ref))))
-        worst = max(worst, abs(k0 - g["kkk0"][n]) / g["kkk0"][n])
+            worst = float(np.maximum(worst, float(np.max(np.abs(kb - kb_ref) / np.abs(kb_ref)))))
+        worst = float(np.maximum(worst, abs(k0 - g["kkk0"][n]) / g["kkk0"][n]))
     assert worst <= RTOL, worst
 
 
@@ -222,10 +217,10 @@ def test_weights_g_matches_reference_series(fk, p, suf):
         kb, k0 = oracle.weights_g(p, alpha, time, n)
         ref = _weights_of(g, n)
         if n > 1:
-            worst = max(worst, float(np.max(np.abs(kb[1:] - ref[1:]) / np.abs(ref[1:]))))
-        worst = max(worst, abs(k0 - g["kkk0"][n]) / g["kkk0"][n])
+            worst = float(np.maximum(worst, float(np.max(np.abs(kb[1:] - ref[1:]) / np.abs(ref[1:])))))
+        worst = float(np.maximum(worst, abs(k0 - g["kkk0"][n]) / g["kkk0"][n]))
         if p == 0.5:
-            worst = max(worst, abs(kb[0] - ref[0]) / ref[0])
+            worst = float(np.maximum(worst, abs(kb[0] - ref[0]) / ref[0]))
     assert worst <= 3e-13, worst
 
 
@@ -238,7 +233,7 @@ def test_weights_g_matches_exact_values(fk, p, suf):
     for n in range(rows.shape[0]):
         kb, k0 = oracle.weights_g(p, alpha, time, n)
         got = np.append(kb, k0)
-        worst = max(worst, float(np.max(np.abs(got - rows[n, :n + 1]) / rows[n, :n + 1])))
+        worst = float(np.maximum(worst, float(np.max(np.abs(got - rows[n, :n + 1]) / rows[n, :n + 1]))))
     assert worst <= 2e-15, worst
 
 
@@ -352,7 +347,7 @@ def test_richards_lod_replays_reference_run(kform):
         S = oracle.lod_step_richards(dims, U, hist, n, kb if n else np.zeros(1), g["tau"], g["Da"], g["kkk0"][n],
                                      g["sZ"], g["sdL"], g["dLx"], g["dLy"], kform, g["k_sat"], g["E"][n], g["Rp"][n],
                                      want_S=True)
-        worst = max(worst, float(np.max(np.abs(U - g["U"][n])) / np.max(np.abs(g["U"][n]))))
+        worst = float(np.maximum(worst, float(np.max(np.abs(U - g["U"][n])) / np.max(np.abs(g["U"][n])))))
         if n > 0:                                   # the history sums on the K-pass nodes
             sl = (slice(1, dims[2] + 1), slice(1, dims[1]), slice(1, dims[0]))
             assert np.allclose(S[sl], g["S"][n][sl], rtol=1e-13, atol=1e-13 * np.max(np.abs(g["S"][n][sl])))

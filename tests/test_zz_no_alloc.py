@@ -13,13 +13,10 @@ import ctypes as C
 
 import numpy as np
 import pytest
+from conftest import relmax
 
 pytestmark = pytest.mark.gpu
 RTOL = 1e-12
-
-
-def relmax(a, b):
-    return float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
 
 
 def test_noalloc_sum_equals_allocating_entry_point_twice():
