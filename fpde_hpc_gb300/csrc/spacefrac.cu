@@ -282,22 +282,58 @@ __device__ __forceinline__ void cta_dot2(const double *a0, const double *b0, boo
     __syncthreads();
 }
 
-// Row i of the product with fused multiply-adds (the reference's terms in its order).
-__device__ __forceinline__ double sf_row_fast(const SfVec &s, int n, int sd, bool has_iw, bool has_rs,
-                                              const double *xv, int i)
+// The Toeplitz sums of one lane's rows a = k+1 and b = n-1-k as chains of n-2 fused multiply-adds
+// for every lane of the warp (kw: the largest k among the warp's lanes). Row a has k lower terms
+// and row b n-2-k; the lane runs row a's and then the first kw-k of row b's (kw steps), then row
+// b's other n-2-kw (the same count on every lane), so no lane idles in a longer loop of its
+// partner. Two-sided: the upper terms (row b has k, row a n-2-k) follow in the same way with the
+// rows swapped, each chain continuing from its row's lower sum. Every term is the reference's
+// bt[j] Tm[|i-j|+1] (negated above the diagonal); only the order of the additions differs.
+__device__ __forceinline__ void sf_pair_fast(const double *__restrict__ bt, const double *__restrict__ Tm, int n,
+                                             int sd, int k, int kw, double &va, double &vb)
+{
+    const int a = k + 1, b = n - 1 - k;
+    const double *pb = bt + 1, *pt = Tm + a;
+    double v = 0.0, w = 0.0;
+    for (int t = 0; t < kw; ++t) {
+        if (t == k) { w = v; v = 0.0; pb = bt + 1; pt = Tm + b; }
+        v = fma(*pb, *pt, v);
+        ++pb; --pt;
+    }
+    if (k == kw) { w = v; v = 0.0; pb = bt + 1; pt = Tm + b; }
+    for (int t = kw; t < n - 2; ++t) {
+        v = fma(*pb, *pt, v);
+        ++pb; --pt;
+    }
+    // w: row a's lower sum, v: row b's
+    if (sd) {
+        pb = bt + b + 1; pt = Tm + 2;
+        for (int t = 0; t < kw; ++t) {
+            if (t == k) { const double y = v; v = w; w = y; pb = bt + a + 1; pt = Tm + 2; }
+            v = fma(-*pb, *pt, v);
+            ++pb; ++pt;
+        }
+        if (k == kw) { const double y = v; v = w; w = y; pb = bt + a + 1; pt = Tm + 2; }
+        for (int t = kw; t < n - 2; ++t) {
+            v = fma(-*pb, *pt, v);
+            ++pb; ++pt;
+        }
+        va = v; vb = w;   // row a's chain ends the upper pass, row b's was set aside at the swap
+    } else {
+        va = w; vb = v;
+    }
+}
+
+// Row i's value from its Toeplitz sum v: the tridiagonal terms plus v (over rs, times iw).
+__device__ __forceinline__ double sf_row_finish(const SfVec &s, bool has_iw, bool has_rs, const double *xv, int i,
+                                                double v)
 {
     const double r = fma(s.m2[i], xv[i + 1], fma(s.m1[i], xv[i], s.m0[i] * xv[i - 1]));
-    double v = 0.0;
-    for (int j = 1; j < i; ++j) v = fma(s.bt[j], s.Tm[i - j + 1], v);
-    if (sd)
-        for (int j = i + 1; j < n; ++j) v = fma(-s.bt[j], s.Tm[j - i + 1], v);
     if (has_rs) v = v / s.rs[i];
     return has_iw ? fma(v, s.iw[i], r) : r + v;
 }
 
-// rv = the product with fused multiply-adds; a thread takes the rows k+1 and n-1-k. (A walker that
-// evens out the lanes' loop lengths, as the 3D product does, measured slower here: its index
-// updates cost more than the divergent loop bounds.)
+// rv = the product with fused multiply-adds; a thread takes the rows k+1 and n-1-k (sf_pair_fast).
 __device__ void sf_apply_fast(const SfVec &s, int n, int sd, bool has_iw, bool has_rs, const double *xv, double *rv)
 {
     const int T = blockDim.x, tid = threadIdx.x;
@@ -309,9 +345,12 @@ __device__ void sf_apply_fast(const SfVec &s, int n, int sd, bool has_iw, bool h
     }
     const int pairs = n / 2;
     for (int k = tid; k < pairs; k += T) {
+        const int kw = min(k - (tid & 31) + 31, pairs - 1);   // the warp's largest k (T is a multiple of 32)
         const int a = k + 1, b = n - 1 - k;
-        rv[a] = sf_row_fast(s, n, sd, has_iw, has_rs, xv, a);
-        if (b != a) rv[b] = sf_row_fast(s, n, sd, has_iw, has_rs, xv, b);
+        double va, vb;
+        sf_pair_fast(s.bt, s.Tm, n, sd, k, kw, va, vb);
+        rv[a] = sf_row_finish(s, has_iw, has_rs, xv, a, va);
+        if (b != a) rv[b] = sf_row_finish(s, has_iw, has_rs, xv, b, vb);
     }
     __syncthreads();
 }
