@@ -43,25 +43,59 @@ __device__ __forceinline__ SfVec sf_carve(double *sm, int m)
     return v;
 }
 
-// Row i (1..n-1) of vmul_T: the tridiagonal part, then the Toeplitz sum in the reference's order.
-__device__ __forceinline__ double sf_row(const SfVec &s, int n, int sd, bool has_iw, bool has_rs, const double *xv,
-                                         int i)
+// The Toeplitz sums of one lane's rows a = k+1 and b = n-1-k as chains of n-2 terms for every lane
+// of the warp (kw: the largest k among the warp's lanes). Row a has k lower terms and row b n-2-k;
+// the lane runs row a's and then the first kw-k of row b's (kw steps), then row b's other n-2-kw
+// (the same count on every lane), so no lane idles in a longer loop of its partner. Two-sided: the
+// upper terms (row b has k, row a n-2-k) follow in the same way with the rows swapped, each chain
+// continuing from its row's lower sum. Each row's sum is its own chain over its terms in the
+// reference's order (j rising, lower then upper): EXACT adds the rounded products in turn
+// (da/ds of dm, bit for bit the reference's row sums); the fast form fuses each term (fma).
+template <bool EXACT>
+__device__ __forceinline__ void sf_pair(const double *__restrict__ bt, const double *__restrict__ Tm, int n, int sd,
+                                        int k, int kw, double &va, double &vb)
+{
+    const int a = k + 1, b = n - 1 - k;
+    const double *pb = bt + 1, *pt = Tm + a;
+    double v = 0.0, w = 0.0;
+    for (int t = 0; t < kw; ++t) {
+        if (t == k) { w = v; v = 0.0; pb = bt + 1; pt = Tm + b; }
+        v = EXACT ? da(v, dm(*pb, *pt)) : fma(*pb, *pt, v);
+        ++pb; --pt;
+    }
+    if (k == kw) { w = v; v = 0.0; pb = bt + 1; pt = Tm + b; }
+    for (int t = kw; t < n - 2; ++t) {
+        v = EXACT ? da(v, dm(*pb, *pt)) : fma(*pb, *pt, v);
+        ++pb; --pt;
+    }
+    // w: row a's lower sum, v: row b's
+    if (sd) {
+        pb = bt + b + 1; pt = Tm + 2;
+        for (int t = 0; t < kw; ++t) {
+            if (t == k) { const double y = v; v = w; w = y; pb = bt + a + 1; pt = Tm + 2; }
+            v = EXACT ? ds(v, dm(*pb, *pt)) : fma(-*pb, *pt, v);
+            ++pb; ++pt;
+        }
+        if (k == kw) { const double y = v; v = w; w = y; pb = bt + a + 1; pt = Tm + 2; }
+        for (int t = kw; t < n - 2; ++t) {
+            v = EXACT ? ds(v, dm(*pb, *pt)) : fma(-*pb, *pt, v);
+            ++pb; ++pt;
+        }
+        va = v; vb = w;   // row a's chain ends the upper pass, row b's was set aside at the swap
+    } else {
+        va = w; vb = v;
+    }
+}
+
+// Row i (1..n-1) of vmul_T from its Toeplitz sum v (sf_pair<true>): the tridiagonal part, then v,
+// in the reference's order of operations.
+__device__ __forceinline__ double sf_row_exact(const SfVec &s, bool has_iw, bool has_rs, const double *xv, int i,
+                                               double v)
 {
     const double r = da(da(dm(s.m0[i], xv[i - 1]), dm(s.m1[i], xv[i])), dm(s.m2[i], xv[i + 1]));
-    double v = 0.0;
-    for (int j = 1; j < i; ++j) v = da(v, dm(s.bt[j], s.Tm[i - j + 1]));
-    if (sd)
-        for (int j = i + 1; j < n; ++j) v = ds(v, dm(s.bt[j], s.Tm[j - i + 1]));
     if (has_rs) v = __ddiv_rn(v, s.rs[i]);
     return da(r, has_iw ? dm(v, s.iw[i]) : v);
 }
-
-// rv = vmul_T(xv) on the line's operands (:6662-6686). All threads; ends with a barrier.
-// Row i's one-sided sum has i-1 terms, so a thread takes the pair of rows k+1 and n-1-k: every
-// thread then runs n-2 terms and a warp issues no lanes idle on a shorter row. When side is given,
-// the CTA's last thread also forms *side_out = the sequential sum of the m products in side (one of
-// the reference's dot products), overlapping it with the rows; the second-to-last thread forms
-// the two boundary rows.
 __device__ void sf_apply(const SfVec &s, int n, int sd, bool has_iw, bool has_rs, const double *xv, double *rv,
                          const double *side = nullptr, double *side_out = nullptr)
 {
@@ -80,9 +114,12 @@ __device__ void sf_apply(const SfVec &s, int n, int sd, bool has_iw, bool has_rs
     }
     const int pairs = n / 2;
     for (int k = tid; k < pairs; k += T) {
+        const int kw = min(k - (tid & 31) + 31, pairs - 1);   // the warp's largest k (T is a multiple of 32)
         const int a = k + 1, b = n - 1 - k;
-        rv[a] = sf_row(s, n, sd, has_iw, has_rs, xv, a);
-        if (b != a) rv[b] = sf_row(s, n, sd, has_iw, has_rs, xv, b);
+        double va, vb;
+        sf_pair<true>(s.bt, s.Tm, n, sd, k, kw, va, vb);
+        rv[a] = sf_row_exact(s, has_iw, has_rs, xv, a, va);
+        if (b != a) rv[b] = sf_row_exact(s, has_iw, has_rs, xv, b, vb);
     }
     __syncthreads();
 }
@@ -282,48 +319,6 @@ __device__ __forceinline__ void cta_dot2(const double *a0, const double *b0, boo
     __syncthreads();
 }
 
-// The Toeplitz sums of one lane's rows a = k+1 and b = n-1-k as chains of n-2 fused multiply-adds
-// for every lane of the warp (kw: the largest k among the warp's lanes). Row a has k lower terms
-// and row b n-2-k; the lane runs row a's and then the first kw-k of row b's (kw steps), then row
-// b's other n-2-kw (the same count on every lane), so no lane idles in a longer loop of its
-// partner. Two-sided: the upper terms (row b has k, row a n-2-k) follow in the same way with the
-// rows swapped, each chain continuing from its row's lower sum. Every term is the reference's
-// bt[j] Tm[|i-j|+1] (negated above the diagonal); only the order of the additions differs.
-__device__ __forceinline__ void sf_pair_fast(const double *__restrict__ bt, const double *__restrict__ Tm, int n,
-                                             int sd, int k, int kw, double &va, double &vb)
-{
-    const int a = k + 1, b = n - 1 - k;
-    const double *pb = bt + 1, *pt = Tm + a;
-    double v = 0.0, w = 0.0;
-    for (int t = 0; t < kw; ++t) {
-        if (t == k) { w = v; v = 0.0; pb = bt + 1; pt = Tm + b; }
-        v = fma(*pb, *pt, v);
-        ++pb; --pt;
-    }
-    if (k == kw) { w = v; v = 0.0; pb = bt + 1; pt = Tm + b; }
-    for (int t = kw; t < n - 2; ++t) {
-        v = fma(*pb, *pt, v);
-        ++pb; --pt;
-    }
-    // w: row a's lower sum, v: row b's
-    if (sd) {
-        pb = bt + b + 1; pt = Tm + 2;
-        for (int t = 0; t < kw; ++t) {
-            if (t == k) { const double y = v; v = w; w = y; pb = bt + a + 1; pt = Tm + 2; }
-            v = fma(-*pb, *pt, v);
-            ++pb; ++pt;
-        }
-        if (k == kw) { const double y = v; v = w; w = y; pb = bt + a + 1; pt = Tm + 2; }
-        for (int t = kw; t < n - 2; ++t) {
-            v = fma(-*pb, *pt, v);
-            ++pb; ++pt;
-        }
-        va = v; vb = w;   // row a's chain ends the upper pass, row b's was set aside at the swap
-    } else {
-        va = w; vb = v;
-    }
-}
-
 // Row i's value from its Toeplitz sum v: the tridiagonal terms plus v (over rs, times iw).
 __device__ __forceinline__ double sf_row_finish(const SfVec &s, bool has_iw, bool has_rs, const double *xv, int i,
                                                 double v)
@@ -333,7 +328,7 @@ __device__ __forceinline__ double sf_row_finish(const SfVec &s, bool has_iw, boo
     return has_iw ? fma(v, s.iw[i], r) : r + v;
 }
 
-// rv = the product with fused multiply-adds; a thread takes the rows k+1 and n-1-k (sf_pair_fast).
+// rv = the product with fused multiply-adds; a thread takes the rows k+1 and n-1-k (sf_pair).
 __device__ void sf_apply_fast(const SfVec &s, int n, int sd, bool has_iw, bool has_rs, const double *xv, double *rv)
 {
     const int T = blockDim.x, tid = threadIdx.x;
@@ -348,7 +343,7 @@ __device__ void sf_apply_fast(const SfVec &s, int n, int sd, bool has_iw, bool h
         const int kw = min(k - (tid & 31) + 31, pairs - 1);   // the warp's largest k (T is a multiple of 32)
         const int a = k + 1, b = n - 1 - k;
         double va, vb;
-        sf_pair_fast(s.bt, s.Tm, n, sd, k, kw, va, vb);
+        sf_pair<false>(s.bt, s.Tm, n, sd, k, kw, va, vb);
         rv[a] = sf_row_finish(s, has_iw, has_rs, xv, a, va);
         if (b != a) rv[b] = sf_row_finish(s, has_iw, has_rs, xv, b, vb);
     }
