@@ -188,14 +188,17 @@ def _synthetic(dims, gam, seed):
     return coefA, coefB, coefR, mc, iw, Tm, rp, u0
 
 
-@pytest.mark.parametrize("exact", [False, True])
-@pytest.mark.parametrize("sd", [0, 1])
-def test_lod_larger_grid_vs_oracle(ctx, sd, exact):
-    """20 x 16 x 40 cells, 12 steps, both solved to a tight threshold: the GPU against the oracle.
-    The two sum the history in different orders (last bits); the bar is ten times the oracle's own
-    response to a 1e-15 change of the source (measured here: a few 1e-12)."""
+@pytest.mark.parametrize("dims,sd,exact", [((20, 16, 40), 0, False), ((20, 16, 40), 0, True),
+                                           ((20, 16, 40), 1, False), ((20, 16, 40), 1, True),
+                                           ((100, 6, 67), 0, False), ((100, 6, 67), 1, False)])
+def test_lod_larger_grid_vs_oracle(ctx, dims, sd, exact):
+    """20 x 16 x 40 and 100 x 6 x 67 cells, 12 steps, solved to a tight threshold: the GPU against
+    the oracle. Lines of 100 and 67 intervals put their row pairs on two warps of the CTA, the
+    second one partly filled (50 and 33 pairs). The two sum the history in different orders (last
+    bits); the bar is ten times the oracle's own response to a 1e-15 change of the source
+    (measured: 2e-9 to 5e-9 on the smaller grid, 2e-7 on the larger)."""
     import fpde_hpc_gb300 as fp
-    dims, alpha, tau, steps, thr, mx = (20, 16, 40), 0.75, 1e-3, 12, 1e-24, 300
+    alpha, tau, steps, thr, mx = 0.75, 1e-3, 12, 1e-24, 300
     coefA, coefB, coefR, mc, iw, Tm, rp, u0 = _synthetic(dims, 0.7, 3 + sd)
     Da = 1.0 / fp.gamma(1.0 - alpha)
     sf = dict(space_der=sd, tol=thr, max_iter=mx, Tm=list(Tm), mc=list(mc), iw=list(iw), exact=1 if exact else 0)
