@@ -96,6 +96,12 @@ __device__ __forceinline__ double sf_row_exact(const SfVec &s, bool has_iw, bool
     if (has_rs) v = __ddiv_rn(v, s.rs[i]);
     return da(r, has_iw ? dm(v, s.iw[i]) : v);
 }
+
+// rv = vmul_T(xv) on the line's operands (:6662-6686). All threads; ends with a barrier. A thread
+// takes the pair of rows k+1 and n-1-k as one chain of n-2 terms (sf_pair). When side is given, the
+// CTA's last thread also forms *side_out = the sequential sum of the m products in side (one of the
+// reference's dot products), overlapping it with the rows; the second-to-last thread forms the two
+// boundary rows.
 __device__ void sf_apply(const SfVec &s, int n, int sd, bool has_iw, bool has_rs, const double *xv, double *rv,
                          const double *side = nullptr, double *side_out = nullptr)
 {
