@@ -310,14 +310,25 @@ __device__ __forceinline__ double cta_dot(const double *a, const double *b, int 
     __syncthreads();
     return t;
 }
-// Two dot products on two warps; neg0: the first is -(a0.b0) (beta's "beta -= q*r").
+// Two dot products on one warp; neg0: the first is -(a0.b0) (beta's "beta -= q*r"). Each lane sums
+// both products' terms; one exchange then leaves lanes 0-15 with the first product's pair sums and
+// lanes 16-31 with the second's, and four levels finish each (five warp-wide FP64 adds for the two,
+// where two shuffle trees take ten).
 __device__ __forceinline__ void cta_dot2(const double *a0, const double *b0, bool neg0, const double *a1,
                                          const double *b1, int m, double *red, double *o0, double *o1)
 {
-    const int warp = threadIdx.x >> 5;
-    if (warp < 2) {
-        const double t = warp == 0 ? warp_dot(a0, b0, m, neg0) : warp_dot(a1, b1, m, false);
-        if ((threadIdx.x & 31) == 0) red[warp] = t;
+    if (threadIdx.x < 32) {
+        const int lane = threadIdx.x;
+        double t0 = 0.0, t1 = 0.0;
+        for (int i = lane; i < m; i += 32) {
+            t0 = fma(neg0 ? -a0[i] : a0[i], b0[i], t0);
+            t1 = fma(a1[i], b1[i], t1);
+        }
+        const bool up = lane >= 16;
+        double t = (up ? t1 : t0) + __shfl_xor_sync(0xffffffffu, up ? t0 : t1, 16);
+#pragma unroll
+        for (int o = 8; o >= 1; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+        if ((lane & 15) == 0) red[lane >> 4] = t;
     }
     __syncthreads();
     *o0 = red[0];
