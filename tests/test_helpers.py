@@ -9,7 +9,7 @@ from conftest import relmax
 def test_relmax_values():
     b = np.array([1.0, -2.0, 4.0])
     assert relmax(b, b) == 0.0
-    assert relmax(b + np.array([0.0, 0.0, 1e-12]), b) == 1e-12 / 4.0
+    assert abs(relmax(b + np.array([0.0, 0.0, 1e-12]), b) - 1e-12 / 4.0) <= 1e-16
     assert relmax(np.zeros(3), np.zeros(3)) == 0.0
 
 
