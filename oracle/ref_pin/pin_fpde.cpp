@@ -384,10 +384,11 @@ static void run_kat(const char *path, int kc, double alpha, double tau, int step
     printf("wrote %s (column K %d, %d steps, analytic squared error %.6g)\n", path, kc, steps, err);
 }
 
-/* The reference's 3D known answer of gpu_test.sh's error_tests (mode 3, NB M K 2 with BS 10: 20 x 20 x
+/* A 3D known answer with gpu_test.sh's error_tests parameters at NB M K 2 (mode 3, BS 10: 20 x 20 x
  * 20 cells, aa 0.8, bb 1.0, analytic problem 2, Dirichlet ends, FK 3 with FP 0.8: the generalized
  * kernel g(t) = t^0.8, EPS2 1e-7 with the default EPS 1e-5, Tau 0.0025, Tm 0.1: 40 steps, impl 0,
- * sum_alg 0): its run prints the squared error 0.157085 against the exact solution. Records as
+ * sum_alg 0; the script itself runs them at NB M K 4): the reference prints the squared error
+ * 0.0472441 against the exact solution. Records as
  * run_kat, plus the weight rows of every step (its series weights at EPS 1e-5: only its own rows
  * reproduce the run). */
 static void run_kat3d(const char *path, int bs, int nb, double alpha, double tau, int steps)

@@ -9,9 +9,9 @@ from conftest import golden_path
 
 
 def load(name="fpde_column_kat"):
-    """The column KAT (fpde_column_kat) or the 3D one (fpde_lod3d_kat: gpu_test.sh's error_tests at
-    20 x 20 x 20, g(t) = t^0.8, 40 steps; its run prints 0.0472441, and it carries the reference's
-    weight rows of every step in `rows`)."""
+    """The column KAT (fpde_column_kat) or the 3D one (fpde_lod3d_kat: gpu_test.sh's error_tests
+    parameters at 20 x 20 x 20, g(t) = t^0.8, 40 steps; its run prints 0.0472441, and it carries the
+    reference's weight rows of every step in `rows`)."""
     g = fgv.load(golden_path(name))
     dims = (int(g["sN"]), int(g["M"]), int(g["K"]))
     sN, M, K = dims

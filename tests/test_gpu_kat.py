@@ -59,9 +59,9 @@ def test_known_answer_split(ctx, case):
 
 
 def test_reference_known_answer_3d_generalized_kernel(ctx):
-    """gpu_test.sh's error_tests at 20 x 20 x 20 with g(t) = t^0.8 (the reference prints 0.0472441):
-    the 3D LOD's variable-step time loop with the reference's weight rows reproduces its final grid
-    to 1e-12 and that error."""
+    """gpu_test.sh's error_tests parameters at 20 x 20 x 20 with g(t) = t^0.8 (the reference prints
+    0.0472441): the 3D LOD's variable-step time loop with the reference's weight rows reproduces its
+    final grid to 1e-12 and that error."""
     import fpde_hpc_gb300 as fp
     c = kat_case.load("fpde_lod3d_kat")
     g = c["g"]

@@ -446,9 +446,10 @@ def test_reference_known_answer_column_k1000():
 
 
 def test_reference_known_answer_3d_generalized_kernel():
-    """gpu_test.sh's error_tests run at 20 x 20 x 20 (analytic problem 2, alpha 0.8, g(t) = t^0.8, 40
-    steps): the reference prints the squared error 0.0472441. The oracle, from the rebuilt inputs and
-    the reference's own weight rows (its series at EPS 1e-5), reproduces the final grid and that error."""
+    """gpu_test.sh's error_tests parameters at 20 x 20 x 20 (analytic problem 2, alpha 0.8,
+    g(t) = t^0.8, 40 steps): the reference prints the squared error 0.0472441. The oracle, from the
+    rebuilt inputs and the reference's own weight rows (its series at EPS 1e-5), reproduces the final
+    grid and that error."""
     import kat_case
     c = kat_case.load("fpde_lod3d_kat")
     g = c["g"]
