@@ -816,6 +816,14 @@ int main(int argc, char **argv)
         run_kat3d(q, 10, 2, 0.8, 0.0025, 40);
         return 0;
     }
+    if (argc >= 3 && strcmp(argv[1], "kat40") == 0) {
+        /* gpu_test.sh's error_tests as the script runs them (NB M K 4: 40 x 40 x 40 cells); the
+         * reference prints 0.403897. Several MB: written for a test's temporary folder, not kept. */
+        char q[4096];
+        snprintf(q, sizeof q, "%s/fpde_lod3d_kat40.fgv", argv[2]);
+        run_kat3d(q, 10, 4, 0.8, 0.0025, 40);
+        return 0;
+    }
     if (argc >= 3 && strcmp(argv[1], "lod_vartau") == 0) {
         /* the 3D LOD (6 x 4 x 8 cells, analytic problem 2, alpha 0.8) with variable steps, for the
          * device time loop with per-step weight rows: g(t) = t (func_in_kernel 0) and the

@@ -8,11 +8,12 @@ import fgv
 from conftest import golden_path
 
 
-def load(name="fpde_column_kat"):
+def load(name="fpde_column_kat", path=None):
     """The column KAT (fpde_column_kat) or the 3D one (fpde_lod3d_kat: gpu_test.sh's error_tests
     parameters at 20 x 20 x 20, g(t) = t^0.8, 40 steps; its run prints 0.0472441, and it carries the
-    reference's weight rows of every step in `rows`)."""
-    g = fgv.load(golden_path(name))
+    reference's weight rows of every step in `rows`). path: a fixture file written elsewhere (the
+    harness's 40 x 40 x 40 run)."""
+    g = fgv.load(path or golden_path(name))
     dims = (int(g["sN"]), int(g["M"]), int(g["K"]))
     sN, M, K = dims
     steps = g["p2"].size

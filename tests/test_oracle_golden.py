@@ -6,12 +6,15 @@ tests/golden/make_golden.py). Tolerances: 1e-12 relative wherever the oracle is 
 the reference's own weights (identical arithmetic up to operation order), and 1e-12 for
 the closed-form weights against the reference's series at EPS 1e-15.
 """
+import os
+import subprocess
+
 import numpy as np
 import pytest
 
 import fgv
 import oracle
-from conftest import golden_path
+from conftest import ROOT, golden_path
 from conftest import relmax as _relmax
 
 RTOL = 1e-12
@@ -464,3 +467,31 @@ def test_reference_known_answer_3d_generalized_kernel():
     err = kat_case.analytic_sq_err(U, c)
     assert abs(err - float(g["analytic_sq_err"])) <= 1e-8 * float(g["analytic_sq_err"])
     assert f"{err:.6g}" == "0.0472441"
+
+
+PIN_FPDE = os.path.join(ROOT, "oracle", "_ref", "pin_fpde")
+
+
+@pytest.mark.skipif(not os.access(PIN_FPDE, os.X_OK),
+                    reason="the reference harness is built only where the reference sources are")
+def test_reference_known_answer_3d_error_tests_40(tmp_path):
+    """gpu_test.sh's error_tests as the script runs them (NB M K 4: 40 x 40 x 40 cells, otherwise
+    as the 20 x 20 x 20 case): the reference prints the squared error 0.403897. The harness writes the
+    run's inputs and its weight rows (8 MB, so not kept as a fixture) into a temporary folder; the
+    oracle replays them, reproduces the final grid and prints the same error."""
+    import kat_case
+    subprocess.run([PIN_FPDE, "kat40", str(tmp_path)], cwd=tmp_path, check=True, timeout=300)
+    c = kat_case.load(path=str(tmp_path / "fpde_lod3d_kat40.fgv"))
+    g = c["g"]
+    assert c["dims"] == (40, 40, 40)
+    U = g["U0"].copy()
+    taus = g["tau_steps"]
+    hist = np.zeros((c["steps"],) + U.shape)
+    for n in range(c["steps"]):
+        kb = c["rows"][n, :n]
+        oracle.lod_step_dirichlet(c["dims"], U, hist, n, kb if n else np.zeros(1), taus, float(g["Da"]),
+                                  float(c["rows"][n, n]), *c["coefs"], c["src"][n], c["bc"][n])
+    assert _relmax(U, g["U_final"]) <= 1e-12
+    err = kat_case.analytic_sq_err(U, c)
+    assert abs(err - float(g["analytic_sq_err"])) <= 1e-8 * float(g["analytic_sq_err"])
+    assert f"{err:.6g}" == "0.403897"
