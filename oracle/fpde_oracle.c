@@ -397,11 +397,13 @@ int fo_lod_step_dirichlet(int sN, int M, int K, double *U, double *hist, int n,
                        S_out);
 }
 
-int fo_lod_step(int sN, int M, int K, double *U, double *hist, int n,
-                const double *kb, const double *tau, double Da, double kkk0,
-                const double *coefA, const double *coefB, const double *coefRlap,
-                const double *rp, const double *bc, const int *lkind, const int *rkind, const double *dLN,
-                double *S_out)
+/* fo_lod_step's body; S_in (may be NULL) replaces the L1 history sum with given sums on the
+ * K-pass nodes (the sum_alg 2 series, formed by the caller). */
+static int lod_step_impl(int sN, int M, int K, double *U, double *hist, int n,
+                         const double *kb, const double *tau, double Da, double kkk0,
+                         const double *coefA, const double *coefB, const double *coefRlap,
+                         const double *rp, const double *bc, const int *lkind, const int *rkind, const double *dLN,
+                         const double *S_in, double *S_out)
 {
     const double lam = Da * (kkk0 / tau[n]);      /* Om1 :4191 */
     const double lamR = Da * kkk0 / tau[n];       /* R :3120 */
@@ -415,7 +417,14 @@ int fo_lod_step(int sN, int M, int K, double *U, double *hist, int n,
      * runs from t = n-1 down to 0 in the reference's order, s = 0 then s += kb[t]*D/tau[t]; the
      * loops visit t outside the nodes so that each row is read contiguously (same per-node order
      * and rounding), k-planes in parallel */
-    if (n > 0) {
+    if (S_in) {
+        for (int k = 1; k <= K; k++)
+            for (int j = 1; j < M; j++)
+                for (int i = 1; i < sN; i++) {
+                    const int64_t id = i * sx + j * sy + k * sz;
+                    S[id] = S_in[id];
+                }
+    } else if (n > 0) {
 #pragma omp parallel for schedule(static)
         for (int k = 1; k <= K; k++)
             for (int t = n - 1; t >= 0; t--) {
@@ -473,6 +482,26 @@ int fo_lod_step(int sN, int M, int K, double *U, double *hist, int n,
     if (S_out) memcpy(S_out, S, sizeof(double) * (size_t)G);
     free(Uold); free(S);
     return 0;
+}
+
+int fo_lod_step(int sN, int M, int K, double *U, double *hist, int n,
+                const double *kb, const double *tau, double Da, double kkk0,
+                const double *coefA, const double *coefB, const double *coefRlap,
+                const double *rp, const double *bc, const int *lkind, const int *rkind, const double *dLN,
+                double *S_out)
+{
+    return lod_step_impl(sN, M, K, U, hist, n, kb, tau, Da, kkk0, coefA, coefB, coefRlap, rp, bc, lkind, rkind,
+                         dLN, NULL, S_out);
+}
+
+int fo_lod_step_dirichlet_sum(int sN, int M, int K, double *U, double *hist, int n, const double *tau, double Da,
+                              double kkk0, const double *coefA, const double *coefB, const double *coefRlap,
+                              const double *rp, const double *bc, const double *S_in)
+{
+    const int kinds[3] = {0, 0, 0};
+    const double dLN[3] = {0.0, 0.0, 0.0};
+    return lod_step_impl(sN, M, K, U, hist, n, NULL, tau, Da, kkk0, coefA, coefB, coefRlap, rp, bc, kinds, kinds,
+                         dLN, S_in, NULL);
 }
 
 /* ------------------------------------------------- Richards (solution-dependent coefficients) */

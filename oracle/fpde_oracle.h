@@ -140,6 +140,13 @@ int fo_lod_step(int sN, int M, int K, double *U, double *hist, int n,
                 const double *rp, const double *bc, const int *lkind, const int *rkind, const double *dLN,
                 double *S_out);
 
+/* The Dirichlet step with given history sums S_in (grid; read on the K-pass nodes) in place of
+ * the L1 sum: the reference's sum_alg 2 runs, whose series sums the caller forms (fo_sum_series).
+ * The new increment grid is still written as hist row n. */
+int fo_lod_step_dirichlet_sum(int sN, int M, int K, double *U, double *hist, int n, const double *tau, double Da,
+                              double kkk0, const double *coefA, const double *coefB, const double *coefRlap,
+                              const double *rp, const double *bc, const double *S_in);
+
 /* ---- Richards problem: solution-dependent coefficients ---- */
 
 /* The reference's closures at suctions P[0..n-1] (metres): water content (wetness, cv_form 4),

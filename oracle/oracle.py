@@ -54,6 +54,9 @@ def load():
     lib.fo_lod_step.argtypes = [i32, i32, i32, _dp, _dp, i32, _dp, _dp, d, d, _dp, _dp, _dp, vp, _dp,
                                 _ip, _ip, _dp, vp]
     lib.fo_lod_step.restype = i32
+    lib.fo_lod_step_dirichlet_sum.argtypes = [i32, i32, i32, _dp, _dp, i32, _dp, d, d, _dp, _dp, _dp, _dp, _dp,
+                                              _dp]
+    lib.fo_lod_step_dirichlet_sum.restype = i32
     lib.fo_richards_closures.argtypes = [i32, _dp, i32, d, vp, vp, vp]
     lib.fo_lod_step_richards.argtypes = [i32, i32, i32, _dp, _dp, i32, _dp, _dp, d, d, _dp, _dp, _dp, _dp, i32, d,
                                          d, vp, vp]
@@ -219,6 +222,18 @@ def lod_step_dirichlet(dims, U, hist, n, kb, tau, Da, kkk0, coefA, coefB, coefRl
                               coefA.reshape(-1), coefB.reshape(-1), coefRlap.reshape(-1),
                               rp.reshape(-1), bc.reshape(-1), _ptr(S))
     return S
+
+
+
+def lod_step_dirichlet_sum(dims, U, hist, n, tau, Da, kkk0, coefA, coefB, coefRlap, rp, bc, S):
+    """The Dirichlet step with the history sums S (grid) given: the reference's sum_alg 2 runs."""
+    lib = load()
+    sN, M, K = dims
+    lib.fo_lod_step_dirichlet_sum(sN, M, K, U.reshape(-1), hist.reshape(-1), n,
+                                  np.ascontiguousarray(tau, dtype=np.float64), Da, kkk0,
+                                  coefA.reshape(-1), coefB.reshape(-1), coefRlap.reshape(-1),
+                                  rp.reshape(-1), bc.reshape(-1),
+                                  np.ascontiguousarray(S, dtype=np.float64).reshape(-1))
 
 
 def lod_step(dims, U, hist, n, kb, tau, Da, kkk0, coefA, coefB, coefRlap, rp, bc, lkind=(0, 0, 0),

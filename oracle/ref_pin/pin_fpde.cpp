@@ -391,11 +391,12 @@ static void run_kat(const char *path, int kc, double alpha, double tau, int step
  * 0.0472441 against the exact solution. Records as
  * run_kat, plus the weight rows of every step (its series weights at EPS 1e-5: only its own rows
  * reproduce the run). */
-static void run_kat3d(const char *path, int bs, int nb, double alpha, double tau, int steps)
+static void run_kat3d(const char *path, int bs, int nb, double alpha, double tau, int steps, int alg = 0)
 {
     set_dims(bs, nb, nb, nb);
     varT = 0; varZ = 0; varXY = 0;
-    implicit = 0; implicit3d = 0; rp_split_3d = 0; sum_alg = 0;
+    implicit = 0; implicit3d = 0; rp_split_3d = 0; sum_alg = alg;
+    if (alg == 2) sum_param = 16;
     func_in_kernel = 3; func_power = 0.8;
     global_eps = 1e-5; global_eps2 = 1e-7;
     FILE *lg = fopen("/dev/null", "w");
@@ -406,9 +407,16 @@ static void run_kat3d(const char *path, int bs, int nb, double alpha, double tau
     w.scalar("alpha", alpha); w.scalar("Da", s->Da); w.scalar("tau", tau); w.scalar("func_power", func_power);
     std::vector<uint64_t> gdims = {(uint64_t)(K + 2), (uint64_t)(_M + 2), (uint64_t)(sN + 2)};
     w.put("U0", gdims, s->b_U);
-    std::vector<double> p2, vt, kkk0, tauv, kb_all, kb_off, rp0, bc0g, S1(G, 0.0);
+    std::vector<double> p2, vt, kkk0, tauv, kb_all, kb_off, rp0, bc0g, S1(G, 0.0), row2, gt, gtj;
+    const int P = 16;
     for (int n = 0; n < steps; n++) {
         s->calc_step(tau);
+        if (alg == 2) {       /* the series inputs of this step, as run_sumalg */
+            const std::vector<double> &r = s->row2_precalc[s->time_i1][0];
+            for (int j = 0; j < P; j++) row2.push_back(j < (int)r.size() ? r[j] : 0.0);
+            gt.push_back(s->g(s->Time[s->tstep]));
+            gtj.push_back(s->g(s->Time[s->tstep + 1]));
+        }
         kb_off.push_back((double)kb_all.size());
         kb_all.insert(kb_all.end(), s->kb_3_cache.begin(), s->kb_3_cache.end());
         kkk0.push_back(s->kkk0);
@@ -447,10 +455,17 @@ static void run_kat3d(const char *path, int bs, int nb, double alpha, double tau
     w.put("U_final", gdims, s->b_U);
     w.put("exact_final", gdims, exact.data());
     w.scalar("analytic_sq_err", err);
+    w.scalar("sum_alg", alg);
+    if (alg == 2) {
+        w.scalar("sum_param", P);
+        w.put("row2", {(uint64_t)steps, (uint64_t)P}, row2.data());
+        w.put("gt", gt); w.put("gtj", gtj);
+    }
     delete s;
     fclose(lg);
     func_in_kernel = 0; func_power = 0.6;
     global_eps = 1e-15; global_eps2 = 1e-15;
+    sum_alg = 0; sum_param = 1e-5;
     printf("wrote %s (%d x %d x %d, FK 3 FP 0.8, %d steps, analytic squared error %.6g)\n", path, sN, _M, K, steps,
            err);
 }
@@ -822,6 +837,14 @@ int main(int argc, char **argv)
         char q[4096];
         snprintf(q, sizeof q, "%s/fpde_lod3d_kat40.fgv", argv[2]);
         run_kat3d(q, 10, 4, 0.8, 0.0025, 40);
+        return 0;
+    }
+    if (argc >= 3 && strcmp(argv[1], "kat_alg2") == 0) {
+        /* the 20 x 20 x 20 known answer with the 16-term series history (sum_alg 2 sum_param 16);
+         * the reference prints 0.0733568 */
+        char q[4096];
+        snprintf(q, sizeof q, "%s/fpde_lod3d_kat_alg2.fgv", argv[2]);
+        run_kat3d(q, 10, 2, 0.8, 0.0025, 40, 2);
         return 0;
     }
     if (argc >= 3 && strcmp(argv[1], "lod_vartau") == 0) {

@@ -6,11 +6,13 @@ gzips their output here. Needs the reference checkout: REF_DIR on the command li
 $FPDE_REFERENCE_DIR, else a directory named "reference" beside the repository; the fixtures
 themselves are committed so tests never need it.
 
-    python tests/golden/make_golden.py [REF_DIR] [--only gamma|richards|richards_ct|spacefrac|spacefrac3d|lod_vartau|kat|frdo_kat]
+    python tests/golden/make_golden.py [REF_DIR] [--only gamma|richards|richards_ct|spacefrac|spacefrac3d|lod_vartau|kat|kat_alg2|frdo_kat]
 
-The richards, richards_ct, spacefrac, spacefrac3d, lod_vartau and kat (the column and the 3D known answers)
-scenarios, and frdo_kat (fr_do's runs at its defaults), run only with --only
-(each sets its own solver mode).
+The richards, richards_ct, spacefrac, spacefrac3d, lod_vartau, kat (the column and the 3D known
+answers) and kat_alg2 (the 3D known answer with the series history) scenarios, and frdo_kat
+(fr_do's runs at its defaults), run only with --only (each sets its own solver mode). The
+harness's kat40 scenario (the 40 x 40 x 40 known answer, 8 MB) is written by its test into a
+temporary folder instead.
 
 The 40-digit weights fixture (fpde_weights_g_exact.fgv.gz) is computed from the time grids of
 the fpde_weights_fk* fixtures written here: rerun make_weights_exact.py after this script.

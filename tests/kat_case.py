@@ -30,7 +30,8 @@ def load(name="fpde_column_kat", path=None):
     bc = np.where(mask[None], V[None] + g["vt"][:, None, None, None], 0.0)
     coefs = [np.stack([g[f"{k}_pass{p}"] for p in range(3)]) for k in ("coefA", "coefB", "coefRlap")]
     c = dict(g=g, dims=dims, steps=steps, src=src, bc=bc, coefs=coefs, interior=interior)
-    if "kb_off" in g:                       # the reference's own weight rows (row n: kb_3_cache, kkk0)
+    if "kb_off" in g and int(g.get("sum_alg", 0)) != 2:   # the reference's weight rows (row n: kb_3_cache, kkk0);
+                                                          # its series mode keeps none
         kbo = g["kb_off"].astype(np.int64)
         rows = np.zeros((steps, steps + 1))
         for n in range(steps):

@@ -469,6 +469,34 @@ def test_reference_known_answer_3d_generalized_kernel():
     assert f"{err:.6g}" == "0.0472441"
 
 
+def test_reference_known_answer_3d_series_history():
+    """The 20 x 20 x 20 known answer with the 16-term series history (sum_alg 2 sum_param 16,
+    otherwise as above): the reference prints 0.0733568. The oracle carries the moments from its own
+    grids step by step (fo_sum_series with the reference's recorded row2_precalc rows and g(t) at
+    each step's ends), steps the LOD with those sums, reproduces the final grid and that error."""
+    import kat_case
+    c = kat_case.load("fpde_lod3d_kat_alg2")
+    g = c["g"]
+    assert int(g["sum_alg"]) == 2 and int(g["sum_param"]) == 16
+    U = g["U0"].copy()
+    taus = g["tau_steps"]
+    hist = np.zeros((c["steps"],) + U.shape)
+    H = np.zeros((U.size, int(g["sum_param"])))
+    grids = [U.copy()]
+    for n in range(c["steps"]):
+        S = np.zeros(U.size)
+        if n:
+            S = oracle.sum_series(grids[n - 1].reshape(-1), grids[n].reshape(-1), H, g["row2"][n], g["gt"][n],
+                                  g["gtj"][n], float(g["alpha"]), taus[n])
+        oracle.lod_step_dirichlet_sum(c["dims"], U, hist, n, taus, float(g["Da"]), float(g["kkk0"][n]), *c["coefs"],
+                                      c["src"][n], c["bc"][n], S)
+        grids.append(U.copy())
+    assert _relmax(U, g["U_final"]) <= 1e-12
+    err = kat_case.analytic_sq_err(U, c)
+    assert abs(err - float(g["analytic_sq_err"])) <= 1e-8 * float(g["analytic_sq_err"])
+    assert f"{err:.6g}" == "0.0733568"
+
+
 PIN_FPDE = os.path.join(ROOT, "oracle", "_ref", "pin_fpde")
 
 
