@@ -832,11 +832,14 @@ int main(int argc, char **argv)
         return 0;
     }
     if (argc >= 3 && strcmp(argv[1], "kat40") == 0) {
-        /* gpu_test.sh's error_tests as the script runs them (NB M K 4: 40 x 40 x 40 cells); the
-         * reference prints 0.403897. Several MB: written for a test's temporary folder, not kept. */
+        /* gpu_test.sh's error_tests as the script runs them (NB M K 4: 40 x 40 x 40 cells), with
+         * sum_alg 0 and with sum_alg 2 sum_param 16; the reference prints 0.403897 and 0.600943.
+         * Several MB each: written for a test's temporary folder, not kept. */
         char q[4096];
         snprintf(q, sizeof q, "%s/fpde_lod3d_kat40.fgv", argv[2]);
         run_kat3d(q, 10, 4, 0.8, 0.0025, 40);
+        snprintf(q, sizeof q, "%s/fpde_lod3d_kat40_alg2.fgv", argv[2]);
+        run_kat3d(q, 10, 4, 0.8, 0.0025, 40, 2);
         return 0;
     }
     if (argc >= 3 && strcmp(argv[1], "kat_alg2") == 0) {

@@ -456,70 +456,80 @@ def test_reference_known_answer_3d_generalized_kernel():
     import kat_case
     c = kat_case.load("fpde_lod3d_kat")
     g = c["g"]
-    U = g["U0"].copy()
-    taus = g["tau_steps"]
-    hist = np.zeros((c["steps"],) + U.shape)
-    for n in range(c["steps"]):
-        kb = c["rows"][n, :n]
-        oracle.lod_step_dirichlet(c["dims"], U, hist, n, kb if n else np.zeros(1), taus, float(g["Da"]),
-                                  float(c["rows"][n, n]), *c["coefs"], c["src"][n], c["bc"][n])
+    U = _replay_kat3d(c)
     assert _relmax(U, g["U_final"]) <= 1e-12
     err = kat_case.analytic_sq_err(U, c)
     assert abs(err - float(g["analytic_sq_err"])) <= 1e-8 * float(g["analytic_sq_err"])
     assert f"{err:.6g}" == "0.0472441"
 
 
+def _replay_kat3d(c):
+    """Step the oracle's LOD through a recorded 3D known-answer run: from the reference's weight
+    rows (sum_alg 0), or (sum_alg 2) with the series sums formed from the oracle's own grids
+    (fo_sum_series with the recorded row2_precalc rows and g(t) at each step's ends; the moments are
+    carried from zero). Returns the final grid."""
+    g = c["g"]
+    U = g["U0"].copy()
+    taus = g["tau_steps"]
+    hist = np.zeros((c["steps"],) + U.shape)
+    series = int(g.get("sum_alg", 0)) == 2
+    H = np.zeros((U.size, int(g["sum_param"]))) if series else None
+    grids = [U.copy()]
+    for n in range(c["steps"]):
+        if series:
+            S = np.zeros(U.size)
+            if n:
+                S = oracle.sum_series(grids[n - 1].reshape(-1), grids[n].reshape(-1), H, g["row2"][n], g["gt"][n],
+                                      g["gtj"][n], float(g["alpha"]), taus[n])
+            oracle.lod_step_dirichlet_sum(c["dims"], U, hist, n, taus, float(g["Da"]), float(g["kkk0"][n]),
+                                          *c["coefs"], c["src"][n], c["bc"][n], S)
+        else:
+            kb = c["rows"][n, :n]
+            oracle.lod_step_dirichlet(c["dims"], U, hist, n, kb if n else np.zeros(1), taus, float(g["Da"]),
+                                      float(c["rows"][n, n]), *c["coefs"], c["src"][n], c["bc"][n])
+        grids.append(U.copy())
+    return U
+
+
 def test_reference_known_answer_3d_series_history():
     """The 20 x 20 x 20 known answer with the 16-term series history (sum_alg 2 sum_param 16,
-    otherwise as above): the reference prints 0.0733568. The oracle carries the moments from its own
-    grids step by step (fo_sum_series with the reference's recorded row2_precalc rows and g(t) at
-    each step's ends), steps the LOD with those sums, reproduces the final grid and that error."""
+    otherwise as above): the reference prints 0.0733568. The oracle, with the series sums formed from
+    its own grids, reproduces the final grid and that error."""
     import kat_case
     c = kat_case.load("fpde_lod3d_kat_alg2")
     g = c["g"]
     assert int(g["sum_alg"]) == 2 and int(g["sum_param"]) == 16
-    U = g["U0"].copy()
-    taus = g["tau_steps"]
-    hist = np.zeros((c["steps"],) + U.shape)
-    H = np.zeros((U.size, int(g["sum_param"])))
-    grids = [U.copy()]
-    for n in range(c["steps"]):
-        S = np.zeros(U.size)
-        if n:
-            S = oracle.sum_series(grids[n - 1].reshape(-1), grids[n].reshape(-1), H, g["row2"][n], g["gt"][n],
-                                  g["gtj"][n], float(g["alpha"]), taus[n])
-        oracle.lod_step_dirichlet_sum(c["dims"], U, hist, n, taus, float(g["Da"]), float(g["kkk0"][n]), *c["coefs"],
-                                      c["src"][n], c["bc"][n], S)
-        grids.append(U.copy())
+    U = _replay_kat3d(c)
     assert _relmax(U, g["U_final"]) <= 1e-12
     err = kat_case.analytic_sq_err(U, c)
     assert abs(err - float(g["analytic_sq_err"])) <= 1e-8 * float(g["analytic_sq_err"])
     assert f"{err:.6g}" == "0.0733568"
 
-
 PIN_FPDE = os.path.join(ROOT, "oracle", "_ref", "pin_fpde")
+
+
+@pytest.fixture(scope="module")
+def kat40_dir(tmp_path_factory):
+    d = tmp_path_factory.mktemp("kat40")
+    subprocess.run([PIN_FPDE, "kat40", str(d)], cwd=d, check=True, timeout=300)
+    return d
 
 
 @pytest.mark.skipif(not os.access(PIN_FPDE, os.X_OK),
                     reason="the reference harness is built only where the reference sources are")
-def test_reference_known_answer_3d_error_tests_40(tmp_path):
+@pytest.mark.parametrize("name,printed", [("fpde_lod3d_kat40", "0.403897"), ("fpde_lod3d_kat40_alg2", "0.600943")])
+def test_reference_known_answer_3d_error_tests_40(kat40_dir, name, printed):
     """gpu_test.sh's error_tests as the script runs them (NB M K 4: 40 x 40 x 40 cells, otherwise
-    as the 20 x 20 x 20 case): the reference prints the squared error 0.403897. The harness writes the
-    run's inputs and its weight rows (8 MB, so not kept as a fixture) into a temporary folder; the
-    oracle replays them, reproduces the final grid and prints the same error."""
+    as the 20 x 20 x 20 case), with sum_alg 0 and with the 16-term series: the reference prints
+    0.403897 and 0.600943. The harness writes the runs' inputs (8 MB each, so not kept as fixtures)
+    into a temporary folder; the oracle replays them, reproduces the final grids and prints the same
+    errors."""
     import kat_case
-    subprocess.run([PIN_FPDE, "kat40", str(tmp_path)], cwd=tmp_path, check=True, timeout=300)
-    c = kat_case.load(path=str(tmp_path / "fpde_lod3d_kat40.fgv"))
+    c = kat_case.load(path=str(kat40_dir / (name + ".fgv")))
     g = c["g"]
     assert c["dims"] == (40, 40, 40)
-    U = g["U0"].copy()
-    taus = g["tau_steps"]
-    hist = np.zeros((c["steps"],) + U.shape)
-    for n in range(c["steps"]):
-        kb = c["rows"][n, :n]
-        oracle.lod_step_dirichlet(c["dims"], U, hist, n, kb if n else np.zeros(1), taus, float(g["Da"]),
-                                  float(c["rows"][n, n]), *c["coefs"], c["src"][n], c["bc"][n])
+    U = _replay_kat3d(c)
     assert _relmax(U, g["U_final"]) <= 1e-12
     err = kat_case.analytic_sq_err(U, c)
     assert abs(err - float(g["analytic_sq_err"])) <= 1e-8 * float(g["analytic_sq_err"])
-    assert f"{err:.6g}" == "0.403897"
+    assert f"{err:.6g}" == printed
