@@ -391,12 +391,13 @@ static void run_kat(const char *path, int kc, double alpha, double tau, int step
  * 0.0472441 against the exact solution. Records as
  * run_kat, plus the weight rows of every step (its series weights at EPS 1e-5: only its own rows
  * reproduce the run). */
-static void run_kat3d(const char *path, int bs, int nb, double alpha, double tau, int steps, int alg = 0)
+static void run_kat3d(const char *path, int bs, int nb, double alpha, double tau, int steps, int alg = 0,
+                      int moments = 16)
 {
     set_dims(bs, nb, nb, nb);
     varT = 0; varZ = 0; varXY = 0;
     implicit = 0; implicit3d = 0; rp_split_3d = 0; sum_alg = alg;
-    if (alg == 2) sum_param = 16;
+    if (alg == 2) sum_param = moments;
     func_in_kernel = 3; func_power = 0.8;
     global_eps = 1e-5; global_eps2 = 1e-7;
     FILE *lg = fopen("/dev/null", "w");
@@ -408,7 +409,7 @@ static void run_kat3d(const char *path, int bs, int nb, double alpha, double tau
     std::vector<uint64_t> gdims = {(uint64_t)(K + 2), (uint64_t)(_M + 2), (uint64_t)(sN + 2)};
     w.put("U0", gdims, s->b_U);
     std::vector<double> p2, vt, kkk0, tauv, kb_all, kb_off, rp0, bc0g, S1(G, 0.0), row2, gt, gtj;
-    const int P = 16;
+    const int P = moments;
     for (int n = 0; n < steps; n++) {
         s->calc_step(tau);
         if (alg == 2) {       /* the series inputs of this step, as run_sumalg */
@@ -833,13 +834,18 @@ int main(int argc, char **argv)
     }
     if (argc >= 3 && strcmp(argv[1], "kat40") == 0) {
         /* gpu_test.sh's error_tests as the script runs them (NB M K 4: 40 x 40 x 40 cells), with
-         * sum_alg 0 and with sum_alg 2 sum_param 16; the reference prints 0.403897 and 0.600943.
+         * sum_alg 0 and with sum_alg 2 sum_param 16, and its bs_tests (sum_alg 2 with sum_param 32,
+         * 48, 64); the reference prints 0.403897, 0.600943, 0.474818, 0.437075 and 0.421276.
          * Several MB each: written for a test's temporary folder, not kept. */
         char q[4096];
         snprintf(q, sizeof q, "%s/fpde_lod3d_kat40.fgv", argv[2]);
         run_kat3d(q, 10, 4, 0.8, 0.0025, 40);
         snprintf(q, sizeof q, "%s/fpde_lod3d_kat40_alg2.fgv", argv[2]);
         run_kat3d(q, 10, 4, 0.8, 0.0025, 40, 2);
+        for (int P = 32; P <= 64; P += 16) {
+            snprintf(q, sizeof q, "%s/fpde_lod3d_kat40_alg2_p%d.fgv", argv[2], P);
+            run_kat3d(q, 10, 4, 0.8, 0.0025, 40, 2, P);
+        }
         return 0;
     }
     if (argc >= 3 && strcmp(argv[1], "kat_alg2") == 0) {

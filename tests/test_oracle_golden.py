@@ -517,11 +517,15 @@ def kat40_dir(tmp_path_factory):
 
 @pytest.mark.skipif(not os.access(PIN_FPDE, os.X_OK),
                     reason="the reference harness is built only where the reference sources are")
-@pytest.mark.parametrize("name,printed", [("fpde_lod3d_kat40", "0.403897"), ("fpde_lod3d_kat40_alg2", "0.600943")])
+@pytest.mark.parametrize("name,printed", [("fpde_lod3d_kat40", "0.403897"), ("fpde_lod3d_kat40_alg2", "0.600943"),
+                                          ("fpde_lod3d_kat40_alg2_p32", "0.474818"),
+                                          ("fpde_lod3d_kat40_alg2_p48", "0.437075"),
+                                          ("fpde_lod3d_kat40_alg2_p64", "0.421276")])
 def test_reference_known_answer_3d_error_tests_40(kat40_dir, name, printed):
     """gpu_test.sh's error_tests as the script runs them (NB M K 4: 40 x 40 x 40 cells, otherwise
-    as the 20 x 20 x 20 case), with sum_alg 0 and with the 16-term series: the reference prints
-    0.403897 and 0.600943. The harness writes the runs' inputs (8 MB each, so not kept as fixtures)
+    as the 20 x 20 x 20 case), with sum_alg 0 and with the 16-term series, and its bs_tests (the
+    series with 32, 48 and 64 terms): the reference prints 0.403897, 0.600943, 0.474818, 0.437075 and
+    0.421276. The harness writes the runs' inputs (8 MB each, so not kept as fixtures)
     into a temporary folder; the oracle replays them, reproduces the final grids and prints the same
     errors."""
     import kat_case
